@@ -1,0 +1,365 @@
+#!/usr/bin/env python
+"""Throughput of the MGLET RK time step on GB300 (cell-updates/s).
+
+Workload (default): 4096 grids of 24^3 cells with two ghost layers
+(16 x 16 x 16 tiling of a periodic box of side 2*pi, 56.6 M cells), the 3-D
+Taylor-Green field plus seeded uniform noise of amplitude 1e-2 on u, v, w
+(splitmix64, seed 42), nu = 1/1600, Williamson RK3, dt = 5e-4, hyperplane
+SIP with ninner = 5, nouter = 9, epcorr = 1e-10.  One step = one time step
+= three RK stages, each with its full pressure solve.  Inputs and the
+working set (>10 GB) are far larger than L2, so no flush is needed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form plain|mixed]
+  python bench.py --impl reference   # the CPU restatement on the host cores
+
+Prints one JSON line (rank 0).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "mglet-base_gb300"))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s per RK step: mixed/batched vs plain FP64, 1 GB300; % HBM roofline"
+UNIT = "cell-updates/s"
+
+# Algorithmic bytes per interior cell and launch of the kernel families,
+# FP64 plain form (8 B per value; one read or write of each operand).
+PLAIN_BYTES = {
+    "tstle4": 8 * (5 + 3),          # read u,v,w,p,g; write uo,vo,wo
+    "rkstep": 8 * 4,                # read p,dp,rhs; write p,dp (per component) / 1.25 ~ 4+1
+    "laplacephi": 8 * 4,            # read phi, ap, bp; write res
+    "sipiter1": 8 * 7,              # read rhs, res, lw, ls, lb, lpr; write res
+    "sipiter2": 8 * 7,              # read res, ue, un, ut, phi; write res, phi
+    "divcal": 8 * 4,                # read u, v, w; write rhs
+    "rescal_maxabs": 8 * 3,         # read rhs, res; write rhs
+    "accumulate": 8 * 4,            # read dp, hilf; write dp, hilf (whole slab)
+    "mgpcorr": 8 * 9,               # read dp,u,v,w,p; write u,v,w,p
+}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--form", choices=["plain", "mixed"], default="plain")
+    ap.add_argument("--tiles", type=int, nargs=3, default=[16, 16, 16])
+    ap.add_argument("--n", type=int, default=24)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-kernels", action="store_true", default=True)
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def make_case(args):
+    from mglet_gb300 import cases
+    nx, ny, nz = args.tiles
+    return cases.periodic_box(nx, ny, nz, n=args.n)
+
+
+def init_fields(case):
+    from mglet_gb300 import cases
+    u, v, w, p = cases.taylor_green(case)
+    u, v, w = cases.add_noise(case, (u, v, w), amplitude=1e-2, seed=42)
+    return u, v, w, p
+
+
+def flow_params(form):
+    from mglet_gb300 import abi
+    return abi.make_flow_params(gmol=1.0 / 1600, rho=1.0, epcorr=1e-10, nouter=9, ninner=5,
+                                nouter_min=0,
+                                form=abi.FORM_MIXED if form == "mixed" else abi.FORM_PLAIN)
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return out
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for q, nm in enumerate(names):
+                if r[5 + q].lower() == "active":
+                    reasons.add(nm)
+        out["sm_mhz"] = sm[len(sm) // 2] if sm else None
+        out["sm_max_mhz"] = max(mx) if mx else None
+        out["reasons"] = sorted(reasons)
+        out["samples"] = len(rows)
+        return out
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_sample(threads=None, tiles=(4, 4, 4), steps=2, warmup=1):
+    """The CPU restatement on a bounded sample of the same workload: a
+    periodic 4x4x4 tiling of 24^3 grids (0.88 M cells), Williamson RK3."""
+    from oracle import binding
+    from mglet_gb300 import cases
+    binding.build()
+    if threads:
+        binding.set_threads(threads)
+    nthreads = binding.max_threads()
+    case = cases.periodic_box(*tiles, n=24)
+    o = binding.Oracle(case, flow_params("plain"))
+    for nm, a in zip("UVWP", init_fields(case)):
+        o.set(nm, a)
+    o.connect(0, 2, "U", "V", "W", "P", corners=True)
+    rk = binding.rk_scheme("williamson")
+    it = 0
+    for _ in range(warmup):
+        it += 1
+        for irk in range(1, 4):
+            o.timeintegrate_flow(it, it, 0.0, 5e-4, irk, rk)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        it += 1
+        for irk in range(1, 4):
+            o.timeintegrate_flow(it, it, 0.0, 5e-4, irk, rk)
+    dt = time.perf_counter() - t0
+    value = case.ncells * steps / dt
+    return value, nthreads, (f"{tiles[0]}x{tiles[1]}x{tiles[2]} periodic tiling of 24^3 grids "
+                             f"({case.ncells} cells), {steps} steps after {warmup} warm-up, "
+                             f"{dt:.1f} s")
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return 0
+    t_all = []
+    value = None
+    for s in range(args.warmup + args.steps):
+        v, nthreads, sample = cpu_sample(steps=1, warmup=0 if s else 1)
+        if s >= args.warmup:
+            t_all.append(v)
+    value = sum(t_all) / len(t_all)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: Taylor-Green + splitmix64 noise (seed 42)",
+        "config": {"workload": "periodic 4096 x 24^3 grids (16x16x16), TG+noise, RK3 dt=5e-4, "
+                               "SIP ninner=5 nouter=9 epcorr=1e-10; each step a bounded sample",
+                   "sample_tiling": "4x4x4"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, rank, world, local):
+    import numpy as np
+    import torch
+    from mglet_gb300 import gpu
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    case = make_case(args)
+    prm = flow_params(args.form)
+    s = gpu.Solver(case, prm, device=local)
+    fields = init_fields(case)
+    for nm, a in zip("UVWP", fields):
+        s.set(nm, a)
+    s.connect(0, 2, "U", "V", "W", "P", corners=True)
+    rk = gpu.rk_scheme("williamson")
+    dt = 5e-4
+    stream = torch.cuda.ExternalStream(s.stream, device=local)
+
+    def step(it):
+        st = None
+        for irk in range(1, 4):
+            st = s.timeintegrate_flow(it, it, 0.0, dt, irk, rk)
+        return st
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    it = 0
+    for _ in range(args.warmup):
+        it += 1
+        step(it)
+    s.synchronize()
+    clocks = Clocks(local)
+    if args.profile_kernels:
+        s.profile(True)
+    barrier()
+    torch.cuda.synchronize()
+    l0 = s.launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    clocks.start()
+    ipcs = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        it += 1
+        st = step(it)
+        ipcs.append(st.ipc)
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1)
+    launches = s.launches - l0
+    if dist is not None:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    kern = {}
+    if args.profile_kernels:
+        for name in s.profile_names():
+            tot, n = s.profile_get(name)
+            kern[name] = (tot, n)
+        s.profile(False)
+    value = case.ncells * args.steps * world / (ms / 1e3)
+
+    # roofline of the dominant kernel family
+    peak, peak_kind = measured_peaks()
+    roof = None
+    if kern:
+        top = max(kern, key=lambda k: kern[k][0])
+        tot, n = kern[top]
+        per_cell = PLAIN_BYTES.get(top)
+        if per_cell and n:
+            bytes_per_launch = per_cell * case.ncells
+            achieved = bytes_per_launch / (tot / n / 1e3) / 1e9
+            roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
+                    "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
+                    "traffic": None, "share": tot / ms,
+                    "algorithmic_bytes_per_launch": bytes_per_launch,
+                    "avg_launch_ms": tot / n}
+
+    # end to end through the public API with host buffers
+    e2e = None
+    if not args.no_e2e:
+        n = case.idim3d
+        host = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(4)]
+        for h, a in zip(host, fields):
+            h.copy_(torch.from_numpy(a))
+        ksteps = max(1, min(args.steps, 3))
+        s.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(ksteps):
+            it += 1
+            for nm, h in zip("UVWP", host):
+                s.set_ptr(nm, h.data_ptr(), n)
+            step(it)
+            for nm, h in zip("UVWP", host):
+                s.get_ptr(nm, h.data_ptr(), n)
+        s.synchronize()
+        te = time.perf_counter() - t0
+        e2e = {"value": case.ncells * ksteps * world / te, "unit": UNIT,
+               "h2d_bytes_per_step": 4 * n * 8, "d2h_bytes_per_step": 4 * n * 8,
+               "steps": ksteps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            v, nth, sample = cpu_sample()
+            cpu = {"value": v, "unit": UNIT, "cores": nth, "kind": "port", "sample": sample}
+        except Exception as ex:   # the baseline never blocks the GPU line
+            cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port",
+                   "sample": f"failed: {ex}"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.form == "plain" else "f64+f32",
+            "data": "synthetic: Taylor-Green + splitmix64 noise (seed 42)",
+            "config": {"workload": f"periodic {case.ngrid} x {args.n}^3 grids "
+                                   f"({args.tiles[0]}x{args.tiles[1]}x{args.tiles[2]}), "
+                                   "TG+noise, RK3 dt=5e-4, SIP ninner=5 nouter=9 epcorr=1e-10",
+                       "form": args.form, "cells": case.ncells,
+                       "l2": "working set > L2 (no flush needed)",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                       "ipc_per_stage_last": ipcs[-1] if ipcs else None},
+            "clocks": clk,
+            "e2e": e2e,
+            "gpu_launches": launches,
+            "roofline": roof,
+            "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        return run_reference(args, rank)
+    return run_ours(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

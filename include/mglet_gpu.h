@@ -1,0 +1,232 @@
+/*
+ * mglet_gpu.h -- C ABI of the GB300 implementation of MGLET-base's
+ * Runge-Kutta stage (momentum fluxes, RK update, pressure-Poisson solve with
+ * divergence and projection, intra-level halo copies).
+ *
+ * Conventions (mirroring the reference's own C interop, e.g.
+ * src/core/exprtk_wrapper.h:18-24, src/core/jsoncpp_wrapper.h:11-30):
+ *   - every entry point returns an int status: 0 = ok, > 0 = error
+ *     (MGLET_ERR_*); the Fortran side turns a nonzero status into
+ *     errr(__FILE__, __LINE__) exactly as it does for its other C helpers;
+ *   - scalars by value, arrays as plain pointers plus element counts;
+ *   - the library never takes ownership of caller memory.
+ *
+ * Storage contract (src/core/pointers_mod.F90:23-75, field_t%arr):
+ *   a 3-D field is one flat array over all grids, grid g (1-based, in grid
+ *   order) starting at element ip3(g) = sum of kk*jj*ii of grids 1..g-1;
+ *   inside a grid the layout is Fortran column-major (k fastest), with two
+ *   ghost layers on each side (interior k = 3..kk-2 etc.).  1-D spacing
+ *   arrays are concatenated per grid the same way (ip1x/ip1y/ip1z).
+ *   Real type is FP64 (the reference's -DMGLET_REAL64=ON build).
+ */
+#ifndef MGLET_GPU_H
+#define MGLET_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MGLET_GPU_ABI_VERSION 1
+
+/* Status codes */
+enum {
+    MGLET_OK = 0,
+    MGLET_ERR_ARG = 1,          /* invalid argument / inconsistent description */
+    MGLET_ERR_UNSUPPORTED = 2,  /* feature of the reference not built (e.g. PAR faces) */
+    MGLET_ERR_CUDA = 3,         /* CUDA runtime error; see mglet_gpu_last_error() */
+    MGLET_ERR_NAME = 4,         /* unknown field name */
+    MGLET_ERR_SIZE = 5,         /* element count does not match the field */
+    MGLET_ERR_EXPLODED = 6,     /* NaN/Inf detected (itinfo "exploded") */
+    MGLET_ERR_NOMEM = 7         /* device allocation failed */
+};
+
+/* Boundary-condition type codes of itypboconds(1, iface, igrid),
+ * src/core/grids_mod.F90:252-289 (setcobone). */
+enum {
+    MGLET_BC_FIX = 2,
+    MGLET_BC_OP1 = 3,
+    MGLET_BC_NOS = 5,
+    MGLET_BC_SLI = 6,
+    MGLET_BC_CON = 7,
+    MGLET_BC_PAR = 8,
+    MGLET_BC_CO1 = 19
+};
+
+/* Pressure solver types, src/flow/pressuresolver_mod.F90:17-21,96-107. */
+enum {
+    MGLET_PSOLVER_SIP = 0,      /* hyperplane SIP (default "sip") */
+    MGLET_PSOLVER_SOR = 1,      /* SIP on minlevel, red-black SOR above ("sor") */
+    MGLET_PSOLVER_CLASSIC = 2   /* lexicographic SIP ("classic") */
+};
+
+/* Execution forms of the stage. */
+enum {
+    /* FP64 throughout, reference operation order, no FMA contraction:
+     * the parity form (relative L2 <= 1e-12 against the FP64 oracle). */
+    MGLET_FORM_PLAIN = 0,
+    /* Batched mixed precision: FP64 velocity/pressure, divergence,
+     * projection, outer defect-correction residual and reductions; FP32
+     * inner SIP sweeps; stage captured in one CUDA graph with a
+     * device-side convergence flag. */
+    MGLET_FORM_MIXED = 1
+};
+
+/* Grid hierarchy description: what grids.h5 (GRIDINFO + BC tables,
+ * src/core/gridio_mod.F90:12-46) and the spacing arrays of
+ * src/core/corefields_mod.F90:98-151 hold for a single-rank run. */
+typedef struct mglet_grid_desc {
+    int32_t ngrid;
+    const int32_t* mgdims;    /* [ngrid][3]: kk, jj, ii (incl. ghosts)   */
+    const int32_t* level;     /* [ngrid]                                   */
+    const int32_t* bctype;    /* [ngrid][6]: faces F,B,R,L,Bo,T (1..6)     */
+    const int32_t* nbrgrid;   /* [ngrid][26]: neighbour grid ids (1-based,
+                                 0 = none), NBRGRID of grids.h5          */
+    const int32_t* gradpflag; /* [ngrid] or NULL (= all 1)                 */
+    /* concatenated 1-D arrays; x/dx/ddx have sum(ii) entries etc. */
+    const double* x;   const double* y;   const double* z;
+    const double* dx;  const double* dy;  const double* dz;
+    const double* ddx; const double* ddy; const double* ddz;
+} mglet_grid_desc;
+
+/* Flow and pressure-solver parameters (src/flow/flowcore_mod.F90:30-148,
+ * src/flow/pressuresolver_mod.F90:47-145). */
+typedef struct mglet_flow_params {
+    double gmol;
+    double rho;
+    double gradp[3];
+    int32_t psolver;      /* MGLET_PSOLVER_* */
+    int32_t ninner;
+    int32_t nouter;
+    int32_t nouter_min;
+    double epcorr;
+    double omega;         /* SOR relaxation factor */
+    int32_t form;         /* MGLET_FORM_* */
+    int32_t reserved;
+} mglet_flow_params;
+
+/* Low-storage (2N) Runge-Kutta scheme, rk_2n_t of
+ * src/core/rungekutta_mod.F90:29-44. */
+typedef struct mglet_rk_scheme {
+    int32_t nrk;
+    int32_t reserved;
+    double cflmax;
+    double a[6];
+    double b[6];
+    double c[6];
+} mglet_rk_scheme;
+
+/* Per-stage statistics (the reference samples ipc into itinfo,
+ * src/flow/pressuresolver_mod.F90:306-308). */
+typedef struct mglet_stage_stats {
+    int32_t ipc;          /* inner iterations performed (nouter_done*ninner) */
+    int32_t nouter_done;  /* outer defect-correction iterations performed   */
+    double maxrhs;        /* last max|rhs| (level scaled), before /prefak   */
+    double prefak;        /* rho/dt of the solve                            */
+} mglet_stage_stats;
+
+/* itinfo diagnostics (src/flow/timeintegration_mod.F90:145-252,306-452). */
+typedef struct mglet_itinfo {
+    double cflmax;
+    double divmax;
+    double energy;        /* enerfg: volume-weighted mean 0.5|u|^2 */
+    int32_t exploded;     /* 1 if any of the above is NaN/Inf       */
+    int32_t reserved;
+} mglet_itinfo;
+
+typedef struct mglet_ctx mglet_ctx;
+
+/* ---- Runge-Kutta coefficients (host only) -------------------------------
+ * Replaces rk_2n_t%init (src/core/rungekutta_mod.F90:49-67): name is one of
+ * "williamson", "berland", "carpenter", "bernardini". */
+int mglet_rk_init(const char* name, mglet_rk_scheme* out);
+/* Replaces rk_2n_t%get_coeffs (src/core/rungekutta_mod.F90:240-256). */
+int mglet_rk_get_coeffs(const mglet_rk_scheme* rk, int32_t irk, double* frhs,
+                        double* fu, double* dtrk, double* dtrki);
+
+/* ---- Context lifetime ---------------------------------------------------
+ * Replaces the device-side part of init_core/init_ib/init_flow:
+ * init_connect_core (src/core/connect/connect_core_mod.F90:167-370),
+ * giteig (src/ib/noib_mod.F90:81-250), init_pressuresolver
+ * (src/flow/pressuresolver_mod.F90:47-145: SIP hyperplane/classic LU,
+ * SOR_RAP).  Allocates every device field (U,V,W,P,G,DU,DV,DW, BP, SDIV,
+ * the pooled scratch UO..RES and the solver coefficients); G is set to
+ * gmol and BP to 1 as the reference does for ib type "noib". */
+int mglet_gpu_create(const mglet_grid_desc* desc, const mglet_flow_params* prm,
+                     int32_t device, mglet_ctx** out);
+int mglet_gpu_destroy(mglet_ctx* ctx);
+
+/* Number of elements of a 3-D field (idim3d, pointers_mod.F90:11). */
+int64_t mglet_gpu_idim3d(const mglet_ctx* ctx);
+
+/* ---- Host <-> device field transfer --------------------------------------
+ * Equivalent of map_arr_to_device / map_arr_from_device
+ * (src/core/fieldhelper_mod.F90:97-143).  name is a field name of the
+ * reference (U, V, W, P, G, DU, DV, DW, BP, SDIV, UO, VO, WO, DP, HILF,
+ * RHS, RES, GSAP, SIPLW, SIPLS, SIPLB, SIPLPR, SIPUE, SIPUN, SIPUT); n must
+ * equal idim3d.  Host memory may be pageable or pinned. */
+int mglet_gpu_set_field(mglet_ctx* ctx, const char* name, const double* host, int64_t n);
+int mglet_gpu_get_field(mglet_ctx* ctx, const char* name, double* host, int64_t n);
+
+/* ---- The RK stage ---------------------------------------------------------
+ * Replaces timeintegrate_flow (src/flow/timeintegration_mod.F90:22-142) for
+ * ib type "noib": tstle4 -> rkstep(u,v,w) -> connect(1, normal, forward=1)
+ * -> mgpoisl.  stats may be NULL. */
+int mglet_gpu_timeintegrate_flow(mglet_ctx* ctx, int32_t itstep, int32_t ittot,
+                                 double timeph, double dt, int32_t irk,
+                                 const mglet_rk_scheme* rk, mglet_stage_stats* stats);
+
+/* ---- Module-level drop-ins ------------------------------------------------
+ * tstle4(uo,vo,wo,u,v,w,u,v,w,p,g) (src/flow/tstle4_mod.F90:13-120):
+ * writes the device fields UO, VO, WO. */
+int mglet_gpu_tstle4(mglet_ctx* ctx);
+/* rkstep(p, dp, rhsp, frhs, dtfu) over the whole flat arrays
+ * (src/core/rungekutta_mod.F90:315-333); arguments are field names. */
+int mglet_gpu_rkstep(mglet_ctx* ctx, const char* p, const char* dp, const char* rhsp,
+                     double frhs, double dtfu);
+/* connect(ilevel, layers, v1..s3, corners, normal, forward)
+ * (src/core/connect/connect2_mod.F90:75-139); ilevel <= 0 means all levels;
+ * unused field slots are NULL. */
+int mglet_gpu_connect(mglet_ctx* ctx, int32_t ilevel, int32_t layers,
+                      const char* v1, const char* v2, const char* v3,
+                      const char* s1, const char* s2, const char* s3,
+                      int32_t corners, int32_t normal, int32_t forward);
+/* ib%divcal(div, u, v, w, fak) for noib (src/ib/noib_mod.F90:253-354). */
+int mglet_gpu_divcal(mglet_ctx* ctx, const char* div, double fak);
+/* laplacephi(res, phi) over all grids (src/flow/laplacephi_mod.F90:14-70). */
+int mglet_gpu_laplacephi(mglet_ctx* ctx, const char* res, const char* phi);
+/* mgpoisl(u, v, w, p, dt, ittot, irk) (src/flow/pressuresolver_mod.F90:160-357):
+ * divergence, outer defect-correction loop, projection (mgpcorr) and the
+ * closing connect(2 layers, corners). */
+int mglet_gpu_mgpoisl(mglet_ctx* ctx, double dt, int32_t ittot, int32_t irk,
+                      mglet_stage_stats* stats);
+/* compcflmax / compdivmax / enerfg of itinfo_flow
+ * (src/flow/timeintegration_mod.F90:202-240); out->exploded mirrors the NaN
+ * check of itinfo_print (src/flow/itinfo_mod.F90:296-320). */
+int mglet_gpu_itinfo(mglet_ctx* ctx, double dt, mglet_itinfo* out);
+
+/* ---- Misc ----------------------------------------------------------------- */
+int mglet_gpu_synchronize(mglet_ctx* ctx);
+/* The cudaStream_t all of this context's work is issued on (for callers that
+ * time or order their own work against it). */
+void* mglet_gpu_stream(const mglet_ctx* ctx);
+/* Per-kernel device timing: while enabled, every launch is bracketed by CUDA
+ * events on the context's stream.  mglet_gpu_profile_get returns the
+ * accumulated milliseconds and launch count of one kernel family (name as
+ * listed by mglet_gpu_profile_names, comma separated) and resets it. */
+int mglet_gpu_profile(mglet_ctx* ctx, int32_t enable);
+int mglet_gpu_profile_get(mglet_ctx* ctx, const char* kernel, double* total_ms, int64_t* launches);
+int mglet_gpu_profile_names(mglet_ctx* ctx, char* buf, int64_t buflen);
+/* Number of kernels this context has launched so far (graph launches count
+ * the kernels inside the graph). */
+int64_t mglet_gpu_kernel_launches(const mglet_ctx* ctx);
+/* Message of the last error in this thread ("" if none). */
+const char* mglet_gpu_last_error(void);
+int32_t mglet_gpu_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MGLET_GPU_H */

@@ -1,0 +1,158 @@
+// internal.h -- shared declarations of the GB300 stage library.
+//
+// Device data layout: every 3-D field is one flat FP64 (or FP32 for the
+// mixed-form inner solver) array over all grids, grid g starting at ip3(g),
+// Fortran order (k fastest) inside a grid -- the reference's field_t%arr
+// layout (src/core/pointers_mod.F90:23-75), so host<->device copies are
+// single memcpys.  Each 24^3 grid slab (28^3 points incl. ghosts) is
+// 175,616 bytes, a multiple of 256, so every grid starts 256-byte aligned.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/mglet_gpu.h"
+
+namespace mg {
+
+// Per-grid record visible to kernels.
+struct DevGrid {
+    int kk, jj, ii;
+    int level;
+    int bc[6];          // faces 1..6 -> bc[0..5]
+    int gradpflag;
+    int cls;            // index of the SIP index table of this grid's dims
+    long long ip3;      // 0-based element offset of the 3-D slab
+    int ipx, ipy, ipz;  // 0-based offsets into the concatenated 1-D arrays
+};
+
+// One box copy of connect_self_single (connect2_mod.F90:947-995): the
+// destination box starts at dst (flat element offset), the source box at
+// src; extents nk*nj*ni with per-grid strides.
+struct BoxCopy {
+    long long dst, src;
+    int nk, nj, ni;
+    int dkk, djj;       // destination grid kk, kk*jj would overflow int? (no: <= 2^31)
+    int skk, sjj;
+    int slot;           // which field slot (0..5: v1 v2 v3 s1 s2 s3)
+    int npts;
+};
+
+struct ConnectPlan {
+    BoxCopy* d_tasks = nullptr;
+    int ntasks = 0;
+    long long npts = 0;
+};
+
+// Hyperplane traversal table of one grid shape (sip_hyperplane_mod.F90:269-334):
+// plane start offsets mip[m] (0-based, m = 9..n3dmax+1) and the 0-based
+// local linear index of every interior point in plane order.
+struct HpTable {
+    int kk, jj, ii;
+    int n3dmin, n3dmax;
+    int* d_mip = nullptr;   // [kk+jj+ii+2]
+    int* d_idx = nullptr;   // [(kk-4)(jj-4)(ii-4)]
+    int maxplane = 0;
+    int npts = 0;
+};
+
+struct ProfEntry {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    double total_ms = 0.0;
+    long long launches = 0;
+};
+
+struct Ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int ngrid = 0;
+    int minlevel = 0, maxlevel = 0;
+    long long idim3d = 0;
+    int idimx = 0, idimy = 0, idimz = 0;
+    bool uniform = true;      // all grids share kk, jj, ii
+    mglet_flow_params prm{};
+    std::vector<DevGrid> grids;            // host copy
+    std::vector<std::vector<int>> nbr;     // [ngrid][27] 1-based neighbour ids
+    std::vector<int> levelgrids_count;
+    DevGrid* d_grids = nullptr;
+    std::map<std::string, double*> f3;     // 3-D FP64 fields
+    std::map<std::string, double*> f1;     // 1-D FP64 spacing / coefficient arrays
+    std::vector<HpTable> hp;               // one per distinct grid shape
+    std::vector<int> d_cls_host;
+    // connection table rows (recvgrid, sendgrid, recvface, sendface), 1-based
+    std::vector<int> conns;
+    std::map<std::string, ConnectPlan> plans;
+    // reductions
+    double* d_gridred = nullptr;   // [4*ngrid]
+    double* d_scalar = nullptr;    // [8]
+    double* h_scalar = nullptr;    // pinned [8]
+    long long launches = 0;
+    bool prof = false;
+    std::map<std::string, ProfEntry> profd;
+
+    double* F(const char* n) { return f3.at(n); }
+    double* L(const char* n) { return f1.at(n); }
+};
+
+// ---- error reporting -------------------------------------------------------
+void set_error(const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define MG_CUDA(call)                                            \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return ::mg::cuda_fail(e_, #call); \
+    } while (0)
+
+#define MG_LAUNCHED(ctx)                                              \
+    do {                                                              \
+        (ctx)->launches++;                                            \
+        cudaError_t e_ = cudaGetLastError();                          \
+        if (e_ != cudaSuccess) return ::mg::cuda_fail(e_, "launch");  \
+    } while (0)
+
+// Brackets the kernels launched in its scope with CUDA events on the
+// context's stream while profiling is enabled.
+struct ProfScope {
+    Ctx* c;
+    ProfEntry* e = nullptr;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(Ctx* ctx, const char* name) : c(ctx) {
+        if (!c->prof) return;
+        e = &c->profd[name];
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, c->stream);
+    }
+    ~ProfScope() {
+        if (!e) return;
+        cudaEventRecord(b, c->stream);
+        e->pending.emplace_back(a, b);
+    }
+};
+
+// ---- kernels: FP64 parity form (plain_*.cu, compiled with -fmad=false) ---
+int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, const double* v,
+                  const double* w, const double* p, const double* g);
+int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu);
+int launch_divcal(Ctx* c, double* div, const double* u, const double* v, const double* w,
+                  double fak);
+int launch_laplacephi(Ctx* c, int ilevel, double* res, const double* phi);
+int launch_sip_lu_hp(Ctx* c);
+int launch_sip_lu_classic(Ctx* c);
+int launch_sipiter1(Ctx* c, int ilevel, const double* rhs, double* res);
+int launch_sipiter2(Ctx* c, int ilevel, double* phi, double* res);
+int launch_sor(Ctx* c, int ilevel, double* dp, const double* rhs);
+int launch_giteig(Ctx* c);
+int launch_rescal_maxabs(Ctx* c, double* rhs, const double* res);
+int launch_accumulate(Ctx* c, double* dp, double* hilf);
+int launch_mgpcorr(Ctx* c, double* u, double* v, double* w, double* p, const double* dp,
+                   double rfak);
+int launch_itinfo(Ctx* c, double dt);
+int launch_connect(Ctx* c, const ConnectPlan& plan, double* const fields[6]);
+
+}  // namespace mg

@@ -1,0 +1,20 @@
+// mixed.h -- batched mixed-precision form of the stage (MGLET_FORM_MIXED).
+#pragma once
+
+#include "internal.h"
+
+namespace mg {
+
+int mixed_init(Ctx* c);
+void mixed_release(Ctx* c);
+void mixed_field_changed(Ctx* c, const char* name);
+int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st);
+int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st);
+
+// shared with api.cu
+int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,
+            double* s2, double* s3, bool corners, bool normal, int forward);
+int rk_coeffs(const mglet_rk_scheme* rk, int irk, double* frhs, double* fu, double* dtrk,
+              double* dtrki);
+
+}  // namespace mg

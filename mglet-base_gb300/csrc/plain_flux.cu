@@ -1,0 +1,287 @@
+// plain_flux.cu -- FP64 parity form of the momentum right-hand side and the
+// low-storage RK update.  Compiled with -fmad=false: every multiply and add
+// is rounded separately, in the operation order of the reference, so the
+// results agree with a plain FP64 build of the Fortran bit for bit.
+//
+//   tstle4_kon   src/flow/tstle4_mod.F90:139-265
+//   tstle4_diff  src/flow/tstle4_mod.F90:268-458 (no LES: qc = st*0)
+//   tstle4_gradp src/flow/tstle4_mod.F90:461-529
+//   rkstep       src/core/rungekutta_mod.F90:315-333
+//
+// GB300 note: FP64 issues at a small fraction of the FP32 rate on this part,
+// so this kernel is FP64-compute bound (~430 flop per cell, incl. divides);
+// it is the reference-order baseline, the mixed form is the fast path.
+#include "internal.h"
+
+namespace mg {
+namespace {
+
+struct GridPtrs {
+    int kk, jj, ii;
+    const double *dx, *dy, *dz, *ddx, *ddy, *ddz, *rdx, *rdy, *rdz, *rddx, *rddy, *rddz;
+};
+
+struct Spacing {
+    const double *dx, *dy, *dz, *ddx, *ddy, *ddz, *rdx, *rdy, *rdz, *rddx, *rddy, *rddz;
+};
+
+#define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
+#define A(a, k, j, i) a[IX(k, j, i)]
+
+__device__ __forceinline__ double dmax(double a, double b) { return a < b ? b : a; }
+// harmonic face mean of tstle4_diff: g*g'/MAX(g+g', gmol)
+__device__ __forceinline__ double hm(double a, double b, double gmol) {
+    return a * b / dmax(a + b, gmol);
+}
+
+// One output point of tstle4 for the U component (kon + diff + gradp).
+__device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
+                           const double* w, const double* p, const double* gg, const GridPtrs& s,
+                           double gmol, double rho, double gpx) {
+    const double *dx = s.dx, *dy = s.dy, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
+    const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
+                 *rddz = s.rddz;
+    const double *ut = u, *vt = v, *wt = w;
+    double uo;
+    {
+        double ax = ddy[j] * ddz[k], ay = dx[i] * ddz[k], az = dx[i] * ddy[j];
+        double fe = ax * (A(ut, k, j, i) + (A(ut, k, j, i + 1) - A(ut, k, j, i)) * 0.5 * dx[i] / ddx[i + 1]);
+        double fw = ax * (A(ut, k, j, i - 1) + (A(ut, k, j, i) - A(ut, k, j, i - 1)) * 0.5 * dx[i - 1] / ddx[i]);
+        double fn = ay * (A(vt, k, j, i) + A(vt, k, j, i + 1)) * 0.5;
+        double fs = ay * (A(vt, k, j - 1, i) + A(vt, k, j - 1, i + 1)) * 0.5;
+        double ft = az * (A(wt, k, j, i) + A(wt, k, j, i + 1)) * 0.5;
+        double fb = az * (A(wt, k - 1, j, i) + A(wt, k - 1, j, i + 1)) * 0.5;
+        double qe = 0.5 * fe * (A(u, k, j, i) + A(u, k, j, i + 1));
+        double qw = 0.5 * fw * (A(u, k, j, i - 1) + A(u, k, j, i));
+        double qn = 0.5 * fn * (A(u, k, j, i) + A(u, k, j + 1, i));
+        double qs = 0.5 * fs * (A(u, k, j - 1, i) + A(u, k, j, i));
+        double qt = 0.5 * ft * (A(u, k, j, i) + A(u, k + 1, j, i));
+        double qb = 0.5 * fb * (A(u, k - 1, j, i) + A(u, k, j, i));
+        uo = -(qe - qw + qn - qs + qt - qb) * rdx[i] * rddy[j] * rddz[k];
+    }
+    {
+        double ax = ddy[j] * ddz[k], ay = dx[i] * ddz[k], az = dx[i] * ddy[j];
+        double ge = A(gg, k, j, i + 1);
+        double gw = A(gg, k, j, i);
+        double gn = hm(A(gg, k, j, i), A(gg, k, j + 1, i), gmol) + hm(A(gg, k, j, i + 1), A(gg, k, j + 1, i + 1), gmol);
+        double gs = hm(A(gg, k, j - 1, i), A(gg, k, j, i), gmol) + hm(A(gg, k, j - 1, i + 1), A(gg, k, j, i + 1), gmol);
+        double gt = hm(A(gg, k, j, i), A(gg, k + 1, j, i), gmol) + hm(A(gg, k, j, i + 1), A(gg, k + 1, j, i + 1), gmol);
+        double gb = hm(A(gg, k - 1, j, i), A(gg, k, j, i), gmol) + hm(A(gg, k - 1, j, i + 1), A(gg, k, j, i + 1), gmol);
+        double qe = -ge * ax * rddx[i + 1] * (A(u, k, j, i + 1) - A(u, k, j, i));
+        double qw = -gw * ax * rddx[i] * (A(u, k, j, i) - A(u, k, j, i - 1));
+        double qn = -gn * ay * rdy[j] * (A(u, k, j + 1, i) - A(u, k, j, i));
+        double qs = -gs * ay * rdy[j - 1] * (A(u, k, j, i) - A(u, k, j - 1, i));
+        double qt = -gt * az * rdz[k] * (A(u, k + 1, j, i) - A(u, k, j, i));
+        double qb = -gb * az * rdz[k - 1] * (A(u, k, j, i) - A(u, k - 1, j, i));
+        double st = ((ge * (A(u, k, j, i + 1) - A(u, k, j, i)) * rddx[i + 1]) -
+                     (gw * (A(u, k, j, i) - A(u, k, j, i - 1)) * rddx[i])) * ax +
+                    ((gn * (A(v, k, j, i + 1) - A(v, k, j, i))) -
+                     (gs * (A(v, k, j - 1, i + 1) - A(v, k, j - 1, i)))) * ddz[k] +
+                    ((gt * (A(w, k, j, i + 1) - A(w, k, j, i))) -
+                     (gb * (A(w, k - 1, j, i + 1) - A(w, k - 1, j, i)))) * ddy[j];
+        double qc = st * 0.0;   // iles = 0 (lesmodel "none")
+        double fak = 1.0 / rho * rddy[j] * rdx[i] * rddz[k];
+        uo = uo - fak * (qe - qw + qn - qs + qt - qb - qc);
+    }
+    uo = uo - 1.0 / (rho * dx[i]) * (A(p, k, j, i + 1) - A(p, k, j, i) + gpx * dx[i]);
+    return uo;
+}
+
+__device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
+                           const double* w, const double* p, const double* gg, const GridPtrs& s,
+                           double gmol, double rho, double gpy) {
+    const double *dy = s.dy, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
+    const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
+                 *rddz = s.rddz;
+    const double *ut = u, *vt = v, *wt = w;
+    double vo;
+    {
+        double ax = dy[j] * ddz[k], ay = ddx[i] * ddz[k], az = ddx[i] * dy[j];
+        double fe = ax * (A(ut, k, j, i) + A(ut, k, j + 1, i)) * 0.5;
+        double fw = ax * (A(ut, k, j, i - 1) + A(ut, k, j + 1, i - 1)) * 0.5;
+        double fn = ay * (A(vt, k, j, i) + (A(vt, k, j + 1, i) - A(vt, k, j, i)) * 0.5 * dy[j] / ddy[j + 1]);
+        double fs = ay * (A(vt, k, j - 1, i) + (A(vt, k, j, i) - A(vt, k, j - 1, i)) * 0.5 * dy[j - 1] / ddy[j]);
+        double ft = az * (A(wt, k, j, i) + A(wt, k, j + 1, i)) * 0.5;
+        double fb = az * (A(wt, k - 1, j, i) + A(wt, k - 1, j + 1, i)) * 0.5;
+        double qe = 0.5 * fe * (A(v, k, j, i) + A(v, k, j, i + 1));
+        double qw = 0.5 * fw * (A(v, k, j, i - 1) + A(v, k, j, i));
+        double qn = 0.5 * fn * (A(v, k, j, i) + A(v, k, j + 1, i));
+        double qs = 0.5 * fs * (A(v, k, j - 1, i) + A(v, k, j, i));
+        double qt = 0.5 * ft * (A(v, k, j, i) + A(v, k + 1, j, i));
+        double qb = 0.5 * fb * (A(v, k - 1, j, i) + A(v, k, j, i));
+        vo = -(qe - qw + qn - qs + qt - qb) * rddx[i] * rdy[j] * rddz[k];
+    }
+    {
+        double ax = dy[j] * ddz[k], ay = ddx[i] * ddz[k], az = ddx[i] * dy[j];
+        double ge = hm(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hm(A(gg, k, j + 1, i), A(gg, k, j + 1, i + 1), gmol);
+        double gw = hm(A(gg, k, j, i - 1), A(gg, k, j, i), gmol) + hm(A(gg, k, j + 1, i - 1), A(gg, k, j + 1, i), gmol);
+        double gn = A(gg, k, j + 1, i);
+        double gs = A(gg, k, j, i);
+        double gt = hm(A(gg, k, j, i), A(gg, k + 1, j, i), gmol) + hm(A(gg, k, j + 1, i), A(gg, k + 1, j + 1, i), gmol);
+        double gb = hm(A(gg, k - 1, j, i), A(gg, k, j, i), gmol) + hm(A(gg, k - 1, j + 1, i), A(gg, k, j + 1, i), gmol);
+        double qe = -ge * ax * rdx[i] * (A(v, k, j, i + 1) - A(v, k, j, i));
+        double qw = -gw * ax * rdx[i - 1] * (A(v, k, j, i) - A(v, k, j, i - 1));
+        double qn = -gn * ay * rddy[j + 1] * (A(v, k, j + 1, i) - A(v, k, j, i));
+        double qs = -gs * ay * rddy[j] * (A(v, k, j, i) - A(v, k, j - 1, i));
+        double qt = -gt * az * rdz[k] * (A(v, k + 1, j, i) - A(v, k, j, i));
+        double qb = -gb * az * rdz[k - 1] * (A(v, k, j, i) - A(v, k - 1, j, i));
+        double st = ((ge * (A(u, k, j + 1, i) - A(u, k, j, i))) -
+                     (gw * (A(u, k, j + 1, i - 1) - A(u, k, j, i - 1)))) * ddz[k] +
+                    ((gn * (A(v, k, j + 1, i) - A(v, k, j, i)) * rddy[j + 1]) -
+                     (gs * (A(v, k, j, i) - A(v, k, j - 1, i)) * rddy[j])) * ay +
+                    ((gt * (A(w, k, j + 1, i) - A(w, k, j, i))) -
+                     (gb * (A(w, k - 1, j + 1, i) - A(w, k - 1, j, i)))) * ddx[i];
+        double qc = st * 0.0;
+        double fak = 1.0 / rho * rddx[i] * rdy[j] * rddz[k];
+        vo = vo - fak * (qe - qw + qn - qs + qt - qb - qc);
+    }
+    vo = vo - 1.0 / (rho * dy[j]) * (A(p, k, j + 1, i) - A(p, k, j, i) + gpy * dy[j]);
+    return vo;
+}
+
+__device__ double wo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
+                           const double* w, const double* p, const double* gg, const GridPtrs& s,
+                           double gmol, double rho, double gpz) {
+    const double *dz = s.dz, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
+    const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
+                 *rddz = s.rddz;
+    const double *ut = u, *vt = v, *wt = w;
+    double wo;
+    {
+        double ax = ddy[j] * dz[k], ay = ddx[i] * dz[k], az = ddx[i] * ddy[j];
+        double fe = ax * (A(ut, k, j, i) + A(ut, k + 1, j, i)) * 0.5;
+        double fw = ax * (A(ut, k, j, i - 1) + A(ut, k + 1, j, i - 1)) * 0.5;
+        double fn = ay * (A(vt, k, j, i) + A(vt, k + 1, j, i)) * 0.5;
+        double fs = ay * (A(vt, k, j - 1, i) + A(vt, k + 1, j - 1, i)) * 0.5;
+        double ft = az * (A(wt, k, j, i) + (A(wt, k + 1, j, i) - A(wt, k, j, i)) * 0.5 * dz[k] / ddz[k + 1]);
+        double fb = az * (A(wt, k - 1, j, i) + (A(wt, k, j, i) - A(wt, k - 1, j, i)) * 0.5 * dz[k - 1] / ddz[k]);
+        double qe = 0.5 * fe * (A(w, k, j, i) + A(w, k, j, i + 1));
+        double qw = 0.5 * fw * (A(w, k, j, i - 1) + A(w, k, j, i));
+        double qn = 0.5 * fn * (A(w, k, j, i) + A(w, k, j + 1, i));
+        double qs = 0.5 * fs * (A(w, k, j - 1, i) + A(w, k, j, i));
+        double qt = 0.5 * ft * (A(w, k, j, i) + A(w, k + 1, j, i));
+        double qb = 0.5 * fb * (A(w, k - 1, j, i) + A(w, k, j, i));
+        wo = -(qe - qw + qn - qs + qt - qb) * rddx[i] * rddy[j] * rdz[k];
+    }
+    {
+        double ax = ddy[j] * dz[k], ay = ddx[i] * dz[k], az = ddx[i] * ddy[j];
+        double ge = hm(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j, i + 1), gmol);
+        double gw = hm(A(gg, k, j, i - 1), A(gg, k, j, i), gmol) + hm(A(gg, k + 1, j, i - 1), A(gg, k + 1, j, i), gmol);
+        double gn = hm(A(gg, k, j, i), A(gg, k, j + 1, i), gmol) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j + 1, i), gmol);
+        double gs = hm(A(gg, k, j - 1, i), A(gg, k, j, i), gmol) + hm(A(gg, k + 1, j - 1, i), A(gg, k + 1, j, i), gmol);
+        double gt = A(gg, k + 1, j, i);
+        double gb = A(gg, k, j, i);
+        double qe = -ge * ax * rdx[i] * (A(w, k, j, i + 1) - A(w, k, j, i));
+        double qw = -gw * ax * rdx[i - 1] * (A(w, k, j, i) - A(w, k, j, i - 1));
+        double qn = -gn * ay * rdy[j] * (A(w, k, j + 1, i) - A(w, k, j, i));
+        double qs = -gs * ay * rdy[j - 1] * (A(w, k, j, i) - A(w, k, j - 1, i));
+        double qt = -gt * az * rddz[k + 1] * (A(w, k + 1, j, i) - A(w, k, j, i));
+        double qb = -gb * az * rddz[k] * (A(w, k, j, i) - A(w, k - 1, j, i));
+        double st = ((ge * (A(u, k + 1, j, i) - A(u, k, j, i))) -
+                     (gw * (A(u, k + 1, j, i - 1) - A(u, k, j, i - 1)))) * ddy[j] +
+                    ((gn * (A(v, k + 1, j, i) - A(v, k, j, i))) -
+                     (gs * (A(v, k + 1, j - 1, i) - A(v, k, j - 1, i)))) * ddx[i] +
+                    ((gt * (A(w, k + 1, j, i) - A(w, k, j, i)) * rddz[k + 1]) -
+                     (gb * (A(w, k, j, i) - A(w, k - 1, j, i)) * rddz[k])) * az;
+        double qc = st * 0.0;
+        double fak = 1.0 / rho * rddx[i] * rddy[j] * rdz[k];
+        wo = wo - fak * (qe - qw + qn - qs + qt - qb - qc);
+    }
+    wo = wo - 1.0 / (rho * dz[k]) * (A(p, k + 1, j, i) - A(p, k, j, i) + gpz * dz[k]);
+    return wo;
+}
+
+// tstle4 over the full box of every grid: points outside the reference's
+// loop ranges get 0, as tstle4 zeroes uo, vo, wo before its loops.
+__global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grids, Spacing sp,
+                                                double* __restrict__ uo, double* __restrict__ vo,
+                                                double* __restrict__ wo, const double* __restrict__ U,
+                                                const double* __restrict__ V, const double* __restrict__ W,
+                                                const double* __restrict__ P, const double* __restrict__ Gf,
+                                                double gmol, double rho, double gx, double gy, double gz) {
+    const DevGrid G = grids[blockIdx.y];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int npts = kk * jj * ii;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npts) return;
+    const int k = t % kk + 1;
+    const int j = (t / kk) % jj + 1;
+    const int i = t / (kk * jj) + 1;
+    GridPtrs s;
+    s.kk = kk; s.jj = jj; s.ii = ii;
+    s.dx = sp.dx + G.ipx - 1; s.dy = sp.dy + G.ipy - 1; s.dz = sp.dz + G.ipz - 1;
+    s.ddx = sp.ddx + G.ipx - 1; s.ddy = sp.ddy + G.ipy - 1; s.ddz = sp.ddz + G.ipz - 1;
+    s.rdx = sp.rdx + G.ipx - 1; s.rdy = sp.rdy + G.ipy - 1; s.rdz = sp.rdz + G.ipz - 1;
+    s.rddx = sp.rddx + G.ipx - 1; s.rddy = sp.rddy + G.ipy - 1; s.rddz = sp.rddz + G.ipz - 1;
+    const long long o = G.ip3;
+    const double *u = U + o, *v = V + o, *w = W + o, *p = P + o, *g = Gf + o;
+    const int nfro = G.bc[0], nbac = G.bc[1], nrgt = G.bc[2], nlft = G.bc[3], nbot = G.bc[4],
+              ntop = G.bc[5];
+    const int nbu = (nbac == 7 || nbac == 3) ? 1 : 0;
+    const int nlv = (nlft == 7 || nlft == 3) ? 1 : 0;
+    const int ntw = (ntop == 7 || ntop == 3) ? 1 : 0;
+    const int nfu = nfro == 3 ? 1 : 0, nrv = nrgt == 3 ? 1 : 0, nbw = nbot == 3 ? 1 : 0;
+    const double gfl = (double)G.gradpflag;
+    const bool jin = j >= 3 && j <= jj - 2, kin = k >= 3 && k <= kk - 2, iin = i >= 3 && i <= ii - 2;
+    double ru = 0.0, rv = 0.0, rw = 0.0;
+    if (i >= 3 - nfu && i <= ii - 3 + nbu && jin && kin)
+        ru = uo_point(k, j, i, kk, jj, u, v, w, p, g, s, gmol, rho, gx * gfl);
+    if (iin && j >= 3 - nrv && j <= jj - 3 + nlv && kin)
+        rv = vo_point(k, j, i, kk, jj, u, v, w, p, g, s, gmol, rho, gy * gfl);
+    if (iin && jin && k >= 3 - nbw && k <= kk - 3 + ntw)
+        rw = wo_point(k, j, i, kk, jj, u, v, w, p, g, s, gmol, rho, gz * gfl);
+    uo[o + t] = ru;
+    vo[o + t] = rv;
+    wo[o + t] = rw;
+}
+
+// rkstep: dp = frhs*dp + rhs; p = p + dtfu*dp over the whole flat array.
+__global__ void k_rkstep(double* __restrict__ p, double* __restrict__ dp,
+                         const double* __restrict__ rhs, double frhs, double dtfu, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (; t < n; t += stride) {
+        double d = frhs * dp[t] + rhs[t];
+        dp[t] = d;
+        p[t] = p[t] + dtfu * d;
+    }
+}
+
+}  // namespace
+
+static Spacing spacing(Ctx* c) {
+    Spacing s;
+    s.dx = c->L("DX"); s.dy = c->L("DY"); s.dz = c->L("DZ");
+    s.ddx = c->L("DDX"); s.ddy = c->L("DDY"); s.ddz = c->L("DDZ");
+    s.rdx = c->L("RDX"); s.rdy = c->L("RDY"); s.rdz = c->L("RDZ");
+    s.rddx = c->L("RDDX"); s.rddy = c->L("RDDY"); s.rddz = c->L("RDDZ");
+    return s;
+}
+
+static int max_points(Ctx* c) {
+    int m = 0;
+    for (const DevGrid& g : c->grids) m = std::max(m, g.kk * g.jj * g.ii);
+    return m;
+}
+
+int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, const double* v,
+                  const double* w, const double* p, const double* g) {
+    ProfScope ps_(c, "tstle4");
+    dim3 grid((max_points(c) + 255) / 256, c->ngrid);
+    k_tstle4<<<grid, 256, 0, c->stream>>>(c->d_grids, spacing(c), uo, vo, wo, u, v, w, p, g,
+                                          c->prm.gmol, c->prm.rho, c->prm.gradp[0],
+                                          c->prm.gradp[1], c->prm.gradp[2]);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu) {
+    ProfScope ps_(c, "rkstep");
+    long long n = c->idim3d;
+    int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+    k_rkstep<<<blocks, 256, 0, c->stream>>>(p, dp, rhs, frhs, dtfu, n);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+}  // namespace mg

@@ -1,0 +1,244 @@
+"""Host-side case generation: grid tables, spacing arrays, initial fields.
+
+This plays the role of the reference's grid preprocessor (grids.h5 with
+GRIDINFO, NBRGRID and the BC tables, src/core/gridio_mod.F90:12-46) for the
+uniform periodic tilings the hot path is measured on, and of init_uvwp
+(src/flow/flow_mod.F90:123-172) for the closed-form initial fields.
+
+Conventions: faces 1..6 = front(-x), back(+x), right(-y), left(+y),
+bottom(-z), top(+z); neighbour slots 7..26 follow facelist of
+src/core/connect/connect_core_mod.F90:38-64.  Field arrays are flat FP64,
+grid after grid, each grid Fortran-ordered (k fastest) with two ghost
+layers (src/core/pointers_mod.F90:23-75).
+"""
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .abi import BC_CON, GridDesc
+
+# Elementary directions of the 26 neighbour slots (facelist of
+# connect_core_mod.F90:38-64): each slot is a combination of faces.
+_FACE_DIR = {1: (-1, 0, 0), 2: (1, 0, 0), 3: (0, -1, 0), 4: (0, 1, 0), 5: (0, 0, -1), 6: (0, 0, 1)}
+FACELIST = [
+    (1,), (2,), (3,), (4,), (5,), (6,),
+    (1, 3), (1, 4), (1, 5), (1, 6), (2, 3), (2, 4), (2, 5), (2, 6), (3, 5), (3, 6), (4, 5), (4, 6),
+    (1, 3, 5), (1, 3, 6), (1, 4, 5), (1, 4, 6), (2, 3, 5), (2, 3, 6), (2, 4, 5), (2, 4, 6),
+]
+
+
+def slot_offset(slot):
+    """(di, dj, dk) of neighbour slot 1..26."""
+    d = [0, 0, 0]
+    for f in FACELIST[slot - 1]:
+        for q in range(3):
+            d[q] += _FACE_DIR[f][q]
+    return tuple(d)
+
+
+@dataclass
+class Case:
+    """A single-level grid hierarchy plus its flat-array geometry."""
+    ngrid: int
+    kk: int
+    jj: int
+    ii: int
+    mgdims: np.ndarray        # int32 [ngrid, 3] (kk, jj, ii)
+    level: np.ndarray         # int32 [ngrid]
+    bctype: np.ndarray        # int32 [ngrid, 6]
+    nbrgrid: np.ndarray       # int32 [ngrid, 26]
+    gridpos: np.ndarray       # int32 [ngrid, 3] (gx, gy, gz)
+    x: np.ndarray
+    y: np.ndarray
+    z: np.ndarray
+    dx: np.ndarray
+    dy: np.ndarray
+    dz: np.ndarray
+    ddx: np.ndarray
+    ddy: np.ndarray
+    ddz: np.ndarray
+    _keep: list = field(default_factory=list, repr=False)
+
+    @property
+    def idim3d(self):
+        return self.ngrid * self.kk * self.jj * self.ii
+
+    @property
+    def ncells(self):
+        """Interior cells (the TPC denominator of timeloop_mod.F90:149)."""
+        return self.ngrid * (self.kk - 4) * (self.jj - 4) * (self.ii - 4)
+
+    def desc(self):
+        """A GridDesc whose pointers stay valid as long as this Case lives."""
+        d = GridDesc()
+        d.ngrid = self.ngrid
+        arrs = {}
+        for name in ("mgdims", "level", "bctype", "nbrgrid"):
+            a = np.ascontiguousarray(getattr(self, name), dtype=np.int32)
+            arrs[name] = a
+            setattr(d, name, a.ctypes.data_as(C.POINTER(C.c_int32)))
+        d.gradpflag = C.POINTER(C.c_int32)()
+        for name in ("x", "y", "z", "dx", "dy", "dz", "ddx", "ddy", "ddz"):
+            a = np.ascontiguousarray(getattr(self, name), dtype=np.float64)
+            arrs[name] = a
+            setattr(d, name, a.ctypes.data_as(C.POINTER(C.c_double)))
+        self._keep.append(arrs)
+        return d
+
+    # -- field helpers ------------------------------------------------------
+    def zeros(self):
+        return np.zeros(self.idim3d, dtype=np.float64)
+
+    def view(self, flat):
+        """[ngrid, ii, jj, kk] view of a flat field (C order of the Fortran slab)."""
+        return flat.reshape(self.ngrid, self.ii, self.jj, self.kk)
+
+    def interior(self, flat):
+        v = self.view(flat)
+        return v[:, 2:self.ii - 2, 2:self.jj - 2, 2:self.kk - 2]
+
+    def coords(self):
+        """Per-grid 1-D coordinate arrays as [ngrid, n] views."""
+        return (self.x.reshape(self.ngrid, self.ii), self.y.reshape(self.ngrid, self.jj),
+                self.z.reshape(self.ngrid, self.kk))
+
+
+def periodic_box(nx, ny, nz, n=24, length=(2 * np.pi, 2 * np.pi, 2 * np.pi), nk=None, nj=None):
+    """nx*ny*nz grids of n^3 interior cells tiling a periodic box.
+
+    Every face is CON (code 7) and every one of the 26 neighbour slots
+    points at the periodic image grid, as a grids.h5 for a fully periodic
+    one-level domain holds.  Grid ids run x fastest.
+    """
+    ni = n
+    nj = n if nj is None else nj
+    nk = n if nk is None else nk
+    ii, jj, kk = ni + 4, nj + 4, nk + 4
+    ngrid = nx * ny * nz
+    gx, gy, gz = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    gx = gx.transpose(2, 1, 0).ravel()
+    gy = gy.transpose(2, 1, 0).ravel()
+    gz = gz.transpose(2, 1, 0).ravel()
+    gid = lambda a, b, c: 1 + (a % nx) + nx * ((b % ny) + ny * (c % nz))
+    nbr = np.zeros((ngrid, 26), dtype=np.int32)
+    for s in range(1, 27):
+        di, dj, dk = slot_offset(s)
+        nbr[:, s - 1] = gid(gx + di, gy + dj, gz + dk)
+    hx, hy, hz = length[0] / (nx * ni), length[1] / (ny * nj), length[2] / (nz * nk)
+
+    def axis(g0, h, npts):
+        # cell i (1-based) spans [g0 + (i-3) h, g0 + (i-2) h]; x(i) its centre
+        i = np.arange(1, npts + 1, dtype=np.float64)
+        return g0[:, None] + (i[None, :] - 2.5) * h
+
+    x = axis(gx * ni * hx, hx, ii).ravel()
+    y = axis(gy * nj * hy, hy, jj).ravel()
+    z = axis(gz * nk * hz, hz, kk).ravel()
+    return Case(
+        ngrid=ngrid, kk=kk, jj=jj, ii=ii,
+        mgdims=np.tile(np.array([kk, jj, ii], dtype=np.int32), (ngrid, 1)),
+        level=np.ones(ngrid, dtype=np.int32),
+        bctype=np.full((ngrid, 6), BC_CON, dtype=np.int32),
+        nbrgrid=nbr,
+        gridpos=np.stack([gx, gy, gz], axis=1).astype(np.int32),
+        x=x, y=y, z=z,
+        dx=np.full(ngrid * ii, hx), dy=np.full(ngrid * jj, hy), dz=np.full(ngrid * kk, hz),
+        ddx=np.full(ngrid * ii, hx), ddy=np.full(ngrid * jj, hy), ddz=np.full(ngrid * kk, hz),
+    )
+
+
+def _stag(case):
+    xg, yg, zg = case.coords()
+    hx = case.dx.reshape(case.ngrid, case.ii)
+    hy = case.dy.reshape(case.ngrid, case.jj)
+    hz = case.dz.reshape(case.ngrid, case.kk)
+    # calc_stag, corefields_mod.F90:176-192
+    return xg, yg, zg, xg + 0.5 * hx, yg + 0.5 * hy, zg + 0.5 * hz
+
+
+def _eval(case, fn, xa, ya, za):
+    out = np.empty((case.ngrid, case.ii, case.jj, case.kk))
+    for g in range(case.ngrid):
+        X = xa[g][:, None, None]
+        Y = ya[g][None, :, None]
+        Z = za[g][None, None, :]
+        out[g] = fn(X, Y, Z)
+    return out.ravel()
+
+
+def taylor_green(case):
+    """3-D Taylor-Green vortex at the staggered positions (init_uvw_expr,
+    src/flow/flow_mod.F90:201-248): u at (xstag, y, z), v at (x, ystag, z),
+    w at (x, y, zstag), p at the cell centre."""
+    xg, yg, zg, xs, ys, zs = _stag(case)
+    u = _eval(case, lambda X, Y, Z: np.sin(X) * np.cos(Y) * np.cos(Z), xs, yg, zg)
+    v = _eval(case, lambda X, Y, Z: -np.cos(X) * np.sin(Y) * np.cos(Z), xg, ys, zg)
+    w = np.zeros(case.idim3d)
+    p = _eval(case, lambda X, Y, Z: (np.cos(2 * X) + np.cos(2 * Y)) * (np.cos(2 * Z) + 2.0) / 16.0,
+              xg, yg, zg)
+    return u, v, w, p
+
+
+def splitmix64_uniform(n, seed, lo, hi):
+    """n uniform doubles in [lo, hi) from a splitmix64 counter stream."""
+    with np.errstate(over="ignore"):
+        s = (np.uint64(seed) + np.arange(1, n + 1, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15))
+        z = s
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    u01 = (z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)
+    return lo + (hi - lo) * u01
+
+
+def add_noise(case, fields, amplitude=1e-2, seed=42):
+    """Seeded uniform noise in [-a, a] on the interior of each field."""
+    out = []
+    for q, f in enumerate(fields):
+        f = f.copy()
+        it = case.interior(f)
+        it += splitmix64_uniform(it.size, seed + 7919 * q, -amplitude, amplitude).reshape(it.shape)
+        out.append(f)
+    return out
+
+
+def divergence_free_modes(case, nmodes=24, kpeak=4.0, urms=1.0, seed=1234):
+    """Solenoidal random field: a sum of Fourier modes with |k| drawn from a
+    Gaussian shell around kpeak, each amplitude orthogonal to its wave
+    vector (continuous divergence exactly zero), scaled to rms urms."""
+    rng = np.random.default_rng(seed)
+    Lx = case.dx[0] * (case.ii - 4) * (case.gridpos[:, 0].max() + 1)
+    Ly = case.dy[0] * (case.jj - 4) * (case.gridpos[:, 1].max() + 1)
+    Lz = case.dz[0] * (case.kk - 4) * (case.gridpos[:, 2].max() + 1)
+    modes = []
+    while len(modes) < nmodes:
+        kmag = rng.normal(kpeak, 1.0)
+        if kmag < 1.0:
+            continue
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        n = np.round(d * kmag * np.array([Lx, Ly, Lz]) / (2 * np.pi))
+        if not n.any():
+            continue
+        k = 2 * np.pi * n / np.array([Lx, Ly, Lz])
+        a = np.cross(k, rng.normal(size=3))
+        a /= np.linalg.norm(a)
+        modes.append((k, a, rng.uniform(0, 2 * np.pi)))
+    xg, yg, zg, xs, ys, zs = _stag(case)
+
+    def comp(c, xa, ya, za):
+        def fn(X, Y, Z):
+            s = 0.0
+            for k, a, ph in modes:
+                s = s + a[c] * np.cos(k[0] * X + k[1] * Y + k[2] * Z + ph)
+            return s
+        return _eval(case, fn, xa, ya, za)
+
+    u = comp(0, xs, yg, zg)
+    v = comp(1, xg, ys, zg)
+    w = comp(2, xg, yg, zs)
+    rms = np.sqrt((np.mean(case.interior(u) ** 2) + np.mean(case.interior(v) ** 2)
+                   + np.mean(case.interior(w) ** 2)) / 3.0)
+    s = urms / rms
+    return u * s, v * s, w * s

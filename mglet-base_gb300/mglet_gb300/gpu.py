@@ -1,0 +1,200 @@
+"""ctypes binding of libmglet_gpu.so, shaped like the reference's modules.
+
+`Solver` wraps one mglet_ctx and exposes the calls timeloop_mod makes
+(timeintegrate_flow, itinfo) plus the module-level procedures
+(tstle4, rkstep, connect, divcal, laplacephi, mgpoisl).  There is no CPU
+fallback: if the CUDA library is missing or no GPU is present, every
+constructor raises.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .build import LIB
+
+_lib = None
+
+# Every symbol declared in include/mglet_gpu.h.
+EXPORTS = [
+    "mglet_rk_init", "mglet_rk_get_coeffs", "mglet_gpu_create", "mglet_gpu_destroy",
+    "mglet_gpu_idim3d", "mglet_gpu_set_field", "mglet_gpu_get_field",
+    "mglet_gpu_timeintegrate_flow", "mglet_gpu_tstle4", "mglet_gpu_rkstep", "mglet_gpu_connect",
+    "mglet_gpu_divcal", "mglet_gpu_laplacephi", "mglet_gpu_mgpoisl", "mglet_gpu_itinfo",
+    "mglet_gpu_synchronize", "mglet_gpu_kernel_launches", "mglet_gpu_last_error",
+    "mglet_gpu_abi_version", "mglet_gpu_stream", "mglet_gpu_profile", "mglet_gpu_profile_get",
+    "mglet_gpu_profile_names",
+]
+
+
+class MgletError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"mglet_gpu status {code}: {msg}")
+        self.code = code
+
+
+def load(path=None):
+    """Load the CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} not built: run __graft_entry__.build() "
+                           "(the GPU path has no CPU fallback)")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    cp = C.c_char_p
+    L.mglet_gpu_last_error.restype = C.c_char_p
+    L.mglet_gpu_abi_version.restype = C.c_int32
+    L.mglet_gpu_idim3d.restype = C.c_int64
+    L.mglet_gpu_idim3d.argtypes = [vp]
+    L.mglet_gpu_kernel_launches.restype = C.c_int64
+    L.mglet_gpu_kernel_launches.argtypes = [vp]
+    L.mglet_rk_init.argtypes = [cp, vp]
+    L.mglet_rk_get_coeffs.argtypes = [vp, C.c_int32] + [C.POINTER(C.c_double)] * 4
+    L.mglet_gpu_create.argtypes = [vp, vp, C.c_int32, C.POINTER(vp)]
+    L.mglet_gpu_destroy.argtypes = [vp]
+    L.mglet_gpu_set_field.argtypes = [vp, cp, vp, C.c_int64]
+    L.mglet_gpu_get_field.argtypes = [vp, cp, vp, C.c_int64]
+    L.mglet_gpu_timeintegrate_flow.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, C.c_double,
+                                               C.c_int32, vp, vp]
+    L.mglet_gpu_tstle4.argtypes = [vp]
+    L.mglet_gpu_rkstep.argtypes = [vp, cp, cp, cp, C.c_double, C.c_double]
+    L.mglet_gpu_connect.argtypes = [vp, C.c_int32, C.c_int32] + [cp] * 6 + [C.c_int32] * 3
+    L.mglet_gpu_divcal.argtypes = [vp, cp, C.c_double]
+    L.mglet_gpu_laplacephi.argtypes = [vp, cp, cp]
+    L.mglet_gpu_mgpoisl.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, vp]
+    L.mglet_gpu_itinfo.argtypes = [vp, C.c_double, vp]
+    L.mglet_gpu_synchronize.argtypes = [vp]
+    L.mglet_gpu_stream.restype = vp
+    L.mglet_gpu_stream.argtypes = [vp]
+    L.mglet_gpu_profile.argtypes = [vp, C.c_int32]
+    L.mglet_gpu_profile_get.argtypes = [vp, cp, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
+    L.mglet_gpu_profile_names.argtypes = [vp, cp, C.c_int64]
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise MgletError(rc, load().mglet_gpu_last_error().decode())
+
+
+def rk_scheme(name="williamson"):
+    rk = abi.RKScheme()
+    _check(load().mglet_rk_init(name.encode(), C.byref(rk)))
+    return rk
+
+
+def rk_coeffs(rk, irk):
+    v = [C.c_double() for _ in range(4)]
+    _check(load().mglet_rk_get_coeffs(C.byref(rk), irk, *[C.byref(x) for x in v]))
+    return tuple(x.value for x in v)
+
+
+def _b(s):
+    return None if s is None else s.encode()
+
+
+class Solver:
+    """One GPU context holding a case's fields and solver state."""
+
+    def __init__(self, case, params, device=0):
+        L = load()
+        self.case = case
+        self._desc = case.desc()
+        self.params = params
+        h = C.c_void_p()
+        _check(L.mglet_gpu_create(C.byref(self._desc), C.byref(params), device, C.byref(h)))
+        self.h = h
+        self.n = L.mglet_gpu_idim3d(h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().mglet_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        _check(load().mglet_gpu_set_field(self.h, name.encode(), a.ctypes.data, a.size))
+
+    def get(self, name, n=None, out=None):
+        n = self.n if n is None else n
+        a = np.empty(n, dtype=np.float64) if out is None else out
+        _check(load().mglet_gpu_get_field(self.h, name.encode(), a.ctypes.data, n))
+        return a
+
+    def set_ptr(self, name, ptr, n):
+        _check(load().mglet_gpu_set_field(self.h, name.encode(), ptr, n))
+
+    def get_ptr(self, name, ptr, n):
+        _check(load().mglet_gpu_get_field(self.h, name.encode(), ptr, n))
+
+    def timeintegrate_flow(self, itstep, ittot, timeph, dt, irk, rk):
+        st = abi.StageStats()
+        _check(load().mglet_gpu_timeintegrate_flow(self.h, itstep, ittot, timeph, dt, irk,
+                                                   C.byref(rk), C.byref(st)))
+        return st
+
+    def tstle4(self):
+        _check(load().mglet_gpu_tstle4(self.h))
+
+    def rkstep(self, p, dp, rhs, frhs, dtfu):
+        _check(load().mglet_gpu_rkstep(self.h, p.encode(), dp.encode(), rhs.encode(), frhs, dtfu))
+
+    def connect(self, ilevel=0, layers=1, v1=None, v2=None, v3=None, s1=None, s2=None, s3=None,
+                corners=False, normal=False, forward=0):
+        _check(load().mglet_gpu_connect(self.h, ilevel, layers, _b(v1), _b(v2), _b(v3), _b(s1),
+                                        _b(s2), _b(s3), int(corners), int(normal), int(forward)))
+
+    def divcal(self, div, fak):
+        _check(load().mglet_gpu_divcal(self.h, div.encode(), fak))
+
+    def laplacephi(self, res, phi):
+        _check(load().mglet_gpu_laplacephi(self.h, res.encode(), phi.encode()))
+
+    def mgpoisl(self, dt, ittot=1, irk=1):
+        st = abi.StageStats()
+        _check(load().mglet_gpu_mgpoisl(self.h, dt, ittot, irk, C.byref(st)))
+        return st
+
+    def itinfo(self, dt):
+        out = abi.ItInfo()
+        rc = load().mglet_gpu_itinfo(self.h, dt, C.byref(out))
+        if rc not in (0, abi.MGLET_ERR_EXPLODED):
+            _check(rc)
+        return out
+
+    def synchronize(self):
+        _check(load().mglet_gpu_synchronize(self.h))
+
+    @property
+    def stream(self):
+        """cudaStream_t (as an int) the context issues its work on."""
+        return load().mglet_gpu_stream(self.h)
+
+    def profile(self, enable=True):
+        _check(load().mglet_gpu_profile(self.h, int(enable)))
+
+    def profile_names(self):
+        buf = C.create_string_buffer(4096)
+        _check(load().mglet_gpu_profile_names(self.h, buf, 4096))
+        return [x for x in buf.value.decode().split(",") if x]
+
+    def profile_get(self, kernel):
+        ms = C.c_double()
+        n = C.c_int64()
+        _check(load().mglet_gpu_profile_get(self.h, kernel.encode(), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    @property
+    def launches(self):
+        return load().mglet_gpu_kernel_launches(self.h)

@@ -1,0 +1,182 @@
+"""ctypes binding of the CPU oracle (oracle/_build/liboracle.so).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg, never by the product path.  The oracle's
+parity status against the reference is stated in mglet_oracle.cpp's header.
+"""
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+
+
+def build(quiet=True):
+    """Compile the oracle with its Makefile (g++, -ffp-contract=off)."""
+    r = subprocess.run(["make", "-C", HERE], capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + r.stdout + r.stderr)
+    if not quiet:
+        print(r.stdout)
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = C.CDLL(LIB)
+        vp = C.c_void_p
+        _lib.oracle_last_error.restype = C.c_char_p
+        _lib.oracle_idim3d.restype = C.c_int64
+        _lib.oracle_idim3d.argtypes = [vp]
+        _lib.oracle_create.argtypes = [vp, vp, C.POINTER(vp)]
+        for fn in ("oracle_tstle4", "oracle_destroy"):
+            getattr(_lib, fn).argtypes = [vp]
+        _lib.oracle_set_field.argtypes = [vp, C.c_char_p, vp, C.c_int64]
+        _lib.oracle_get_field.argtypes = [vp, C.c_char_p, vp, C.c_int64]
+        _lib.oracle_get_sip_index.argtypes = [vp, vp, vp, C.c_int64]
+        _lib.oracle_get_conns.argtypes = [vp, vp, C.c_int64, C.POINTER(C.c_int64)]
+        _lib.oracle_rkstep.argtypes = [vp, C.c_char_p, C.c_char_p, C.c_char_p, C.c_double,
+                                       C.c_double]
+        _lib.oracle_connect.argtypes = [vp, C.c_int, C.c_int] + [C.c_char_p] * 6 + [
+            C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]
+        _lib.oracle_divcal.argtypes = [vp, C.c_char_p, C.c_double]
+        _lib.oracle_laplacephi.argtypes = [vp, C.c_char_p, C.c_char_p]
+        _lib.oracle_mgpoisl.argtypes = [vp, C.c_double, C.c_int, C.c_int, vp]
+        _lib.oracle_timeintegrate_flow.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double,
+                                                   C.c_int, vp, vp]
+        _lib.oracle_itinfo.argtypes = [vp, C.c_double, vp]
+        _lib.oracle_rk_init.argtypes = [C.c_char_p, vp]
+        _lib.oracle_rk_get_coeffs.argtypes = [vp, C.c_int] + [C.POINTER(C.c_double)] * 4
+        _lib.oracle_set_threads.argtypes = [C.c_int]
+        _lib.oracle_max_threads.restype = C.c_int
+    return _lib
+
+
+def _b(s):
+    return None if s is None else s.encode()
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _check(rc):
+    if rc != 0:
+        raise OracleError(f"oracle status {rc}: {lib().oracle_last_error().decode()}")
+
+
+def rk_scheme(name):
+    from mglet_gb300.abi import RKScheme
+    rk = RKScheme()
+    _check(lib().oracle_rk_init(name.encode(), C.byref(rk)))
+    return rk
+
+
+def rk_coeffs(rk, irk):
+    vals = [C.c_double() for _ in range(4)]
+    _check(lib().oracle_rk_get_coeffs(C.byref(rk), irk, *[C.byref(v) for v in vals]))
+    return tuple(v.value for v in vals)
+
+
+def set_threads(n):
+    lib().oracle_set_threads(int(n))
+
+
+def max_threads():
+    return lib().oracle_max_threads()
+
+
+class Oracle:
+    """One oracle context: the FP64 CPU restatement of the stage."""
+
+    def __init__(self, case, params):
+        from mglet_gb300.abi import GridDesc  # noqa: F401  (struct layout)
+        self.case = case
+        self._desc = case.desc()
+        self._params = params
+        h = C.c_void_p()
+        _check(lib().oracle_create(C.byref(self._desc), C.byref(params), C.byref(h)))
+        self.h = h
+        self.n = lib().oracle_idim3d(h)
+
+    def close(self):
+        if self.h:
+            lib().oracle_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set(self, name, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        _check(lib().oracle_set_field(self.h, name.encode(), a.ctypes.data, a.size))
+
+    def get(self, name, n=None):
+        n = self.n if n is None else n
+        a = np.empty(n, dtype=np.float64)
+        _check(lib().oracle_get_field(self.h, name.encode(), a.ctypes.data, n))
+        return a
+
+    def sip_index(self):
+        mip = np.empty(self.n, dtype=np.int64)
+        idx = np.empty(self.n, dtype=np.int64)
+        _check(lib().oracle_get_sip_index(self.h, mip.ctypes.data, idx.ctypes.data, self.n))
+        return mip, idx
+
+    def conns(self):
+        nrows = C.c_int64()
+        _check(lib().oracle_get_conns(self.h, None, 0, C.byref(nrows)))
+        rows = np.zeros((nrows.value, 4), dtype=np.int32)
+        _check(lib().oracle_get_conns(self.h, rows.ctypes.data, nrows.value, C.byref(nrows)))
+        return rows
+
+    def tstle4(self):
+        _check(lib().oracle_tstle4(self.h))
+
+    def rkstep(self, p, dp, rhs, frhs, dtfu):
+        _check(lib().oracle_rkstep(self.h, p.encode(), dp.encode(), rhs.encode(), frhs, dtfu))
+
+    def connect(self, ilevel=0, layers=1, v1=None, v2=None, v3=None, s1=None, s2=None, s3=None,
+                corners=False, normal=False, forward=0):
+        n = C.c_int64()
+        _check(lib().oracle_connect(self.h, ilevel, layers, _b(v1), _b(v2), _b(v3), _b(s1),
+                                    _b(s2), _b(s3), int(corners), int(normal), int(forward),
+                                    C.byref(n)))
+        return n.value
+
+    def divcal(self, div, fak):
+        _check(lib().oracle_divcal(self.h, div.encode(), fak))
+
+    def laplacephi(self, res, phi):
+        _check(lib().oracle_laplacephi(self.h, res.encode(), phi.encode()))
+
+    def mgpoisl(self, dt, ittot=1, irk=1):
+        from mglet_gb300.abi import StageStats
+        st = StageStats()
+        _check(lib().oracle_mgpoisl(self.h, dt, ittot, irk, C.byref(st)))
+        return st
+
+    def timeintegrate_flow(self, itstep, ittot, timeph, dt, irk, rk):
+        from mglet_gb300.abi import StageStats
+        st = StageStats()
+        _check(lib().oracle_timeintegrate_flow(self.h, itstep, ittot, timeph, dt, irk,
+                                               C.byref(rk), C.byref(st)))
+        return st
+
+    def itinfo(self, dt):
+        from mglet_gb300.abi import ItInfo
+        out = ItInfo()
+        _check(lib().oracle_itinfo(self.h, dt, C.byref(out)))
+        return out

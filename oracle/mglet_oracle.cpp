@@ -1,0 +1,1463 @@
+// mglet_oracle.cpp -- CPU restatement of MGLET-base's Runge-Kutta stage.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the checker for the GPU library:
+// only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load
+// it.  The product path never links, loads or calls it.
+//
+// What it restates (FP64 build of the reference, -DMGLET_REAL64=ON), loop by
+// loop and in the reference's operation order, compiled with
+// -ffp-contract=off so no FMA contraction changes the rounding:
+//   src/flow/timeintegration_mod.F90:22-142   timeintegrate_flow (noib)
+//   src/core/rungekutta_mod.F90:70-333        RK coefficients, rkstep
+//   src/flow/tstle4_mod.F90:13-529            tstle4 kon / diff / gradp
+//   src/ib/noib_mod.F90:81-354                giteig, divcal
+//   src/flow/sip_hyperplane_mod.F90:22-569    hyperplane SIP init/LU/iter
+//   src/flow/sip_classic_mod.F90:17-198       classic SIP
+//   src/flow/sor_mod.F90:18-203               red-black SOR
+//   src/flow/laplacephi_mod.F90:134-165       laplacephi
+//   src/flow/pressuresolver_mod.F90:160-908   mgpoisl, mgpoisit, sip,
+//                                             maxabscal, rescal, mgpcorr,
+//                                             accumulate_pcorr
+//   src/core/connect/connect_core_mod.F90     connection table, box extents
+//   src/core/connect/connect2_mod.F90:839-998 connect_self
+//   src/flow/timeintegration_mod.F90:306-452  compcflmax, compdivmax, enerfg
+//
+// Parity status: the reference is Fortran and cannot be compiled here (no
+// Fortran compiler, MPI or HDF5), and its own tests hold no golden field
+// vectors.  This restatement is therefore pinned only by known-answer
+// checks (analytic Taylor-Green decay, discrete Fourier eigenvalues of the
+// Poisson operator, kinetic-energy conservation of the skew-symmetric
+// convection, SIP hyperplane self-checks, connect message sizes, RK order):
+// "parity unpinned" against reference outputs.
+//
+// Single-rank, single- or multi-grid, one level, ib type "noib", CON/CO1
+// faces; other boundary types are rejected with MGLET_ERR_UNSUPPORTED.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#include "../include/mglet_gpu.h"
+
+namespace {
+
+// Fortran default-kind (REAL32) literals widened to REAL64, as a REAL64 build
+// of the reference evaluates them (sip_hyperplane_mod.F90:123,202).
+const double kAlfa = (double)0.92f;
+const double kTiny = (double)1.0e-20f;
+
+struct Grid {
+    int kk, jj, ii;
+    int level;
+    int bc[7];        // 1..6
+    int nbr[27];      // 1..26
+    int gradpflag;
+    int64_t ip3;      // 0-based element offset of the 3-D slab
+    int64_t ipx, ipy, ipz;
+};
+
+struct Conn {         // one row of sendconns (single rank: send == recv)
+    int recvgrid, sendgrid, recvface, sendface;
+};
+
+// facelist(4, 26), facenbr(26), rescue_dir(7, 26), rescue_nbr(7, 26) of
+// src/core/connect/connect_core_mod.F90:38-159.
+const int facelist[27][4] = {
+    {0, 0, 0, 0},
+    {1, 1, 0, 0}, {1, 2, 0, 0}, {1, 3, 0, 0}, {1, 4, 0, 0}, {1, 5, 0, 0}, {1, 6, 0, 0},
+    {2, 1, 3, 0}, {2, 1, 4, 0}, {2, 1, 5, 0}, {2, 1, 6, 0}, {2, 2, 3, 0}, {2, 2, 4, 0},
+    {2, 2, 5, 0}, {2, 2, 6, 0}, {2, 3, 5, 0}, {2, 3, 6, 0}, {2, 4, 5, 0}, {2, 4, 6, 0},
+    {3, 1, 3, 5}, {3, 1, 3, 6}, {3, 1, 4, 5}, {3, 1, 4, 6}, {3, 2, 3, 5}, {3, 2, 3, 6},
+    {3, 2, 4, 5}, {3, 2, 4, 6}};
+const int facenbr[27] = {0, 2, 1, 4, 3, 6, 5, 12, 11, 14, 13, 8, 7, 10, 9,
+                         18, 17, 16, 15, 26, 25, 24, 23, 22, 21, 20, 19};
+const int rescue_dir[27][7] = {
+    {0, 0, 0, 0, 0, 0, 0},
+    {1, 0, 0, 0, 0, 0, 0}, {2, 0, 0, 0, 0, 0, 0}, {3, 0, 0, 0, 0, 0, 0},
+    {4, 0, 0, 0, 0, 0, 0}, {5, 0, 0, 0, 0, 0, 0}, {6, 0, 0, 0, 0, 0, 0},
+    {7, 1, 3, 0, 0, 0, 0}, {8, 4, 1, 0, 0, 0, 0}, {9, 1, 5, 0, 0, 0, 0},
+    {10, 6, 1, 0, 0, 0, 0}, {11, 2, 3, 0, 0, 0, 0}, {12, 2, 4, 0, 0, 0, 0},
+    {13, 2, 5, 0, 0, 0, 0}, {14, 2, 6, 0, 0, 0, 0}, {15, 3, 5, 0, 0, 0, 0},
+    {16, 6, 3, 0, 0, 0, 0}, {17, 4, 5, 0, 0, 0, 0}, {18, 4, 6, 0, 0, 0, 0},
+    {19, 7, 9, 15, 1, 3, 5}, {20, 7, 10, 16, 1, 3, 6}, {21, 8, 9, 17, 1, 4, 5},
+    {22, 8, 10, 18, 1, 4, 6}, {23, 11, 13, 15, 2, 3, 5}, {24, 11, 14, 16, 2, 3, 6},
+    {25, 12, 13, 17, 2, 4, 5}, {26, 12, 14, 18, 2, 4, 6}};
+const int rescue_nbr[27][7] = {
+    {0, 0, 0, 0, 0, 0, 0},
+    {2, 0, 0, 0, 0, 0, 0}, {1, 0, 0, 0, 0, 0, 0}, {4, 0, 0, 0, 0, 0, 0},
+    {3, 0, 0, 0, 0, 0, 0}, {6, 0, 0, 0, 0, 0, 0}, {5, 0, 0, 0, 0, 0, 0},
+    {12, 11, 8, 0, 0, 0, 0}, {11, 7, 12, 0, 0, 0, 0}, {14, 13, 10, 0, 0, 0, 0},
+    {13, 9, 14, 0, 0, 0, 0}, {8, 7, 12, 0, 0, 0, 0}, {7, 8, 11, 0, 0, 0, 0},
+    {10, 9, 14, 0, 0, 0, 0}, {9, 10, 13, 0, 0, 0, 0}, {18, 17, 16, 0, 0, 0, 0},
+    {17, 15, 18, 0, 0, 0, 0}, {16, 15, 18, 0, 0, 0, 0}, {15, 16, 17, 0, 0, 0, 0},
+    {26, 25, 24, 22, 23, 21, 20}, {25, 26, 23, 21, 24, 22, 19},
+    {24, 23, 26, 20, 25, 19, 22}, {23, 24, 25, 19, 26, 20, 21},
+    {22, 21, 20, 26, 19, 25, 24}, {21, 22, 19, 25, 20, 26, 23},
+    {20, 19, 22, 24, 21, 23, 26}, {19, 20, 21, 23, 22, 24, 25}};
+
+inline bool is_con(int t) { return t == MGLET_BC_CON || t == MGLET_BC_CO1; }
+
+struct Ctx {
+    std::vector<Grid> g;   // 1-based (g[0] unused)
+    int ngrid = 0;
+    int minlevel = 0, maxlevel = 0;
+    int64_t idim3d = 0, idimx = 0, idimy = 0, idimz = 0;
+    mglet_flow_params prm{};
+    int ilesmodel = 0;
+    std::map<std::string, std::vector<double>> f3;   // 3-D fields
+    std::map<std::string, std::vector<double>> f1;   // 1-D fields
+    std::vector<int64_t> mip, idxsip;                // SIP_MIP_HP, SIP_IDX_HP
+    std::vector<Conn> conns;
+
+    double* F(const char* n) { return f3.at(n).data(); }
+    double* L(const char* n) { return f1.at(n).data(); }
+};
+
+std::string g_err;
+
+int fail(int code, const std::string& msg) {
+    g_err = msg;
+    return code;
+}
+
+// ---------------------------------------------------------------------------
+// Index helpers: Fortran 1-based (k, j, i) into a grid slab of (kk, jj, ii).
+#define IX(k, j, i) ((int64_t)((i) - 1) * kk * jj + (int64_t)((j) - 1) * kk + ((k) - 1))
+
+// ---------------------------------------------------------------------------
+// connect_core_mod.F90:373-433 get_nbrs
+void get_nbrs(const Ctx& c, int iface, const int* neighbours, int& nbrgrid, int& nbrface) {
+    nbrgrid = 0;
+    nbrface = 0;
+    for (int i = 0; i < 7; ++i) {
+        int dir = rescue_dir[iface][i];
+        if (dir == 0) break;
+        if (neighbours[dir] > 0) {
+            nbrgrid = neighbours[dir];
+            nbrface = rescue_nbr[iface][i];
+            if (nbrface > 18) {
+                int t1 = c.g[nbrgrid].bc[facelist[nbrface][1]];
+                int t2 = c.g[nbrgrid].bc[facelist[nbrface][2]];
+                int t3 = c.g[nbrgrid].bc[facelist[nbrface][3]];
+                if (!is_con(t1) && !is_con(t2) && !is_con(t3)) {
+                    nbrgrid = 0;
+                    nbrface = 0;
+                    continue;
+                }
+            }
+            break;
+        }
+    }
+}
+
+// connect_core_mod.F90:167-370 init_connect_core (single rank: the
+// Alltoallv leaves sendconns identical to recvconns)
+void init_connect_core(Ctx& c) {
+    c.conns.clear();
+    for (int igrid = 1; igrid <= c.ngrid; ++igrid) {
+        const Grid& G = c.g[igrid];
+        for (int iface = 1; iface <= 6; ++iface) {
+            if (is_con(G.bc[iface])) {
+                int ng, nf;
+                get_nbrs(c, iface, G.nbr, ng, nf);
+                if (ng == 0) continue;
+                c.conns.push_back({igrid, ng, iface, nf});
+            }
+        }
+        for (int iface = 7; iface <= 18; ++iface) {
+            int t1 = G.bc[facelist[iface][1]], t2 = G.bc[facelist[iface][2]];
+            if (is_con(t1) || is_con(t2)) {
+                int ng, nf;
+                get_nbrs(c, iface, G.nbr, ng, nf);
+                if (ng == 0) continue;
+                c.conns.push_back({igrid, ng, iface, nf});
+            }
+        }
+        for (int iface = 19; iface <= 26; ++iface) {
+            int t1 = G.bc[facelist[iface][1]], t2 = G.bc[facelist[iface][2]],
+                t3 = G.bc[facelist[iface][3]];
+            if (is_con(t1) || is_con(t2) || is_con(t3)) {
+                int ng, nf;
+                get_nbrs(c, iface, G.nbr, ng, nf);
+                if (ng == 0) continue;
+                c.conns.push_back({igrid, ng, iface, nf});
+            }
+        }
+    }
+}
+
+// connect_core_mod.F90:488-572 start_and_stop_face
+void start_and_stop_face(const Grid& G, int iface, int& is, int& ie, int& js, int& je,
+                         int& ks, int& ke, int nplane, bool nghost) {
+    switch (iface) {
+        case 1: is = 3 - nplane; ie = 2; break;
+        case 2: is = G.ii - 1; ie = G.ii - (2 - nplane); break;
+        case 3: js = 3 - nplane; je = 2; break;
+        case 4: js = G.jj - 1; je = G.jj - (2 - nplane); break;
+        case 5: ks = 3 - nplane; ke = 2; break;
+        case 6: ks = G.kk - 1; ke = G.kk - (2 - nplane); break;
+    }
+    if (nghost) {   // flag /= 'Y' and nghost present
+        switch (iface) {
+            case 1: is += nplane; ie += nplane; break;
+            case 2: is -= nplane; ie -= nplane; break;
+            case 3: js += nplane; je += nplane; break;
+            case 4: js -= nplane; je -= nplane; break;
+            case 5: ks += nplane; ke += nplane; break;
+            case 6: ks -= nplane; ke -= nplane; break;
+        }
+    }
+}
+
+// connect_core_mod.F90:454-485 start_and_stop
+void start_and_stop(const Grid& G, int iface, int& is, int& ie, int& js, int& je, int& ks,
+                    int& ke, int nplane, bool nghost) {
+    is = 3; ie = G.ii - 2;
+    js = 3; je = G.jj - 2;
+    ks = 3; ke = G.kk - 2;
+    for (int i = 1; i <= facelist[iface][0]; ++i)
+        start_and_stop_face(G, facelist[iface][i], is, ie, js, je, ks, ke, nplane, nghost);
+}
+
+// connect_core_mod.F90:575-602 corr_start_stop
+void corr_start_stop(const Grid& G, int fsend, int frecv, int& is, int& ie, int& js, int& je,
+                     int& ks, int& ke, int nplane) {
+    if (frecv <= 6) return;
+    for (int i = 1; i <= facelist[fsend][0]; ++i)
+        for (int j = 1; j <= facelist[frecv][0]; ++j)
+            if (facelist[fsend][i] == facelist[frecv][j])
+                start_and_stop_face(G, facelist[fsend][i], is, ie, js, je, ks, ke, nplane, false);
+}
+
+// connect_core_mod.F90:640-682 decide (geometry flag never set on this path)
+bool decide(const Ctx& c, const Conn& cn, bool vertices, int fwd, int minl, int maxl) {
+    bool ex = true;
+    int lvl = c.g[cn.recvgrid].level;
+    if (lvl > maxl || lvl < minl) ex = false;
+    if (!vertices && cn.recvface > 6) ex = false;
+    if (fwd == 1 && (cn.recvface == 2 || cn.recvface == 4 || cn.recvface == 6)) ex = false;
+    else if (fwd == -1 && (cn.recvface == 1 || cn.recvface == 3 || cn.recvface == 5)) ex = false;
+    return ex;
+}
+
+// connect2_mod.F90:947-995 connect_self_single
+int64_t connect_self_single(Ctx& c, double* arr, int sg, int dg, int is, int js, int ks,
+                            int isd, int ied, int jsd, int jed, int ksd, int ked) {
+    const Grid& S = c.g[sg];
+    const Grid& D = c.g[dg];
+    int koff = ks - ksd, joff = js - jsd, ioff = is - isd;
+    double* src = arr + S.ip3;
+    double* dst = arr + D.ip3;
+    int64_t n = 0;
+    for (int i = isd; i <= ied; ++i)
+        for (int j = jsd; j <= jed; ++j)
+            for (int k = ksd; k <= ked; ++k) {
+                int64_t di = (int64_t)(i - 1) * D.kk * D.jj + (int64_t)(j - 1) * D.kk + (k - 1);
+                int64_t si = (int64_t)(i + ioff - 1) * S.kk * S.jj +
+                             (int64_t)(j + joff - 1) * S.kk + (k + koff - 1);
+                dst[di] = src[si];
+                ++n;
+            }
+    return n;
+}
+
+// connect2_mod.F90:75-139,208-402,481-520,839-944: connect / conn1 for one
+// rank (all connections are self connections).  Returns copied points.
+int64_t connect(Ctx& c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,
+                double* s2, double* s3, bool corners, bool normal, int forward) {
+    int nplane = layers;
+    int minl = c.minlevel, maxl = c.maxlevel;
+    if (ilevel > 0) { minl = ilevel; maxl = ilevel; }
+    int fwd = forward > 0 ? 1 : (forward < 0 ? -1 : 0);
+    bool sn = normal;
+    int64_t ncopied = 0;
+    for (const Conn& cn : c.conns) {
+        if (!decide(c, cn, corners, fwd, minl, maxl)) continue;
+        const Grid& S = c.g[cn.sendgrid];
+        const Grid& D = c.g[cn.recvgrid];
+        int is, ie, js, je, ks, ke;
+        start_and_stop(S, facenbr[cn.recvface], is, ie, js, je, ks, ke, nplane, true);
+        corr_start_stop(S, cn.sendface, cn.recvface, is, ie, js, je, ks, ke, nplane);
+        int isd, ied, jsd, jed, ksd, ked;
+        start_and_stop(D, cn.recvface, isd, ied, jsd, jed, ksd, ked, nplane, false);
+        int64_t ssz = (int64_t)(ie - is + 1) * (je - js + 1) * (ke - ks + 1);
+        int64_t dsz = (int64_t)(ied - isd + 1) * (jed - jsd + 1) * (ked - ksd + 1);
+        if (ssz != dsz) { g_err = "connect: source/destination size mismatch"; return -1; }
+        int rf = cn.recvface;
+        bool exU = (sn && rf < 3) || !sn;
+        bool exV = (sn && (rf > 2 && rf < 5)) || !sn;
+        bool exW = (sn && rf > 4) || !sn;
+        double* flds[6] = {exU ? v1 : nullptr, exV ? v2 : nullptr, exW ? v3 : nullptr, s1, s2, s3};
+        for (double* a : flds)
+            if (a)
+                ncopied += connect_self_single(c, a, cn.sendgrid, cn.recvgrid, is, js, ks, isd,
+                                               ied, jsd, jed, ksd, ked);
+    }
+    return ncopied;
+}
+
+// ---------------------------------------------------------------------------
+// noib_mod.F90:81-250 giteig
+void giteig(Ctx& c) {
+    double* aw = c.L("GSAW"); double* ae = c.L("GSAE");
+    double* as = c.L("GSAS"); double* an = c.L("GSAN");
+    double* ab = c.L("GSAB"); double* at = c.L("GSAT");
+    double* AP = c.F("GSAP"); double* BP = c.F("BP");
+    const double* DX = c.L("DX"); const double* DY = c.L("DY"); const double* DZ = c.L("DZ");
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const double* dx = DX + G.ipx - 1;   // dx[i], i 1-based
+        const double* dy = DY + G.ipy - 1;
+        const double* dz = DZ + G.ipz - 1;
+        double* AW = aw + G.ipx - 1; double* AE = ae + G.ipx - 1;
+        double* AS = as + G.ipy - 1; double* AN = an + G.ipy - 1;
+        double* AB = ab + G.ipz - 1; double* AT = at + G.ipz - 1;
+        double* ap = AP + G.ip3;
+        const double* bp = BP + G.ip3;
+        for (int i = 3; i <= ii - 2; ++i) {
+            AE[i] = 2.0 / ((dx[i - 1] + dx[i]) * dx[i]);
+            AW[i] = 2.0 / ((dx[i - 1] + dx[i]) * dx[i - 1]);
+        }
+        for (int j = 3; j <= jj - 2; ++j) {
+            AN[j] = 2.0 / ((dy[j - 1] + dy[j]) * dy[j]);
+            AS[j] = 2.0 / ((dy[j - 1] + dy[j]) * dy[j - 1]);
+        }
+        for (int k = 3; k <= kk - 2; ++k) {
+            AT[k] = 2.0 / ((dz[k - 1] + dz[k]) * dz[k]);
+            AB[k] = 2.0 / ((dz[k - 1] + dz[k]) * dz[k - 1]);
+        }
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k)
+                    ap[IX(k, j, i)] = -2.0 / (dx[i - 1] * dx[i]) - 2.0 / (dy[j - 1] * dy[j]) -
+                                      2.0 / (dz[k - 1] * dz[k]);
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k)
+                    ap[IX(k, j, i)] = ap[IX(k, j, i)] +
+                                      AW[i] * (1.0 - bp[IX(k, j, i - 1)] * bp[IX(k, j, i)]) +
+                                      AE[i] * (1.0 - bp[IX(k, j, i)] * bp[IX(k, j, i + 1)]) +
+                                      AS[j] * (1.0 - bp[IX(k, j - 1, i)] * bp[IX(k, j, i)]) +
+                                      AN[j] * (1.0 - bp[IX(k, j, i)] * bp[IX(k, j + 1, i)]) +
+                                      AB[k] * (1.0 - bp[IX(k - 1, j, i)] * bp[IX(k, j, i)]) +
+                                      AT[k] * (1.0 - bp[IX(k, j, i)] * bp[IX(k + 1, j, i)]);
+        auto wall_lo = [](int t) { return t == 2 || t == 5 || t == 6 || t == 19; };
+        auto wall_hi = [](int t) { return t == 2 || t == 5 || t == 6; };
+        if (wall_lo(G.bc[1])) {
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k)
+                    ap[IX(k, j, 3)] = ap[IX(k, j, 3)] + AW[3] * (bp[IX(k, j, 2)] * bp[IX(k, j, 3)]);
+            AW[3] = 0.0;
+        }
+        if (wall_hi(G.bc[2])) {
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k)
+                    ap[IX(k, j, ii - 2)] = ap[IX(k, j, ii - 2)] +
+                                           AE[ii - 2] * (bp[IX(k, j, ii - 2)] * bp[IX(k, j, ii - 1)]);
+            AE[ii - 2] = 0.0;
+        }
+        if (wall_lo(G.bc[3])) {
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int k = 3; k <= kk - 2; ++k)
+                    ap[IX(k, 3, i)] = ap[IX(k, 3, i)] + AS[3] * (bp[IX(k, 2, i)] * bp[IX(k, 3, i)]);
+            AS[3] = 0.0;
+        }
+        if (wall_hi(G.bc[4])) {
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int k = 3; k <= kk - 2; ++k)
+                    ap[IX(k, jj - 2, i)] = ap[IX(k, jj - 2, i)] +
+                                           AN[jj - 2] * (bp[IX(k, jj - 2, i)] * bp[IX(k, jj - 1, i)]);
+            AN[jj - 2] = 0.0;
+        }
+        if (wall_lo(G.bc[5])) {
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    ap[IX(3, j, i)] = ap[IX(3, j, i)] + AB[3] * (bp[IX(2, j, i)] * bp[IX(3, j, i)]);
+            AB[3] = 0.0;
+        }
+        if (wall_hi(G.bc[6])) {
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    ap[IX(kk - 2, j, i)] = ap[IX(kk - 2, j, i)] +
+                                           AT[kk - 2] * (bp[IX(kk - 2, j, i)] * bp[IX(kk - 1, j, i)]);
+            AT[kk - 2] = 0.0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// sip_hyperplane_mod.F90:269-334,339-393,398-447: index lists, sort, check.
+// mip and idx use the reference's 1-based values, stored in the grid's slab.
+int sip_hyperplane_init_grid(int kk, int jj, int ii, int64_t* mip, int64_t* idx) {
+    // mip(1..ii+jj+kk) -> mip[m-1]; idxsip(1..) -> idx[n-1]
+    const int n3dmin = 9, n3dmax = (ii - 2) + (jj - 2) + (kk - 2);
+    for (int m = 1; m <= ii + jj + kk; ++m) mip[m - 1] = 0;
+    for (int64_t n = 0; n < (int64_t)ii * jj * kk; ++n) idx[n] = -1;
+    for (int m = n3dmin; m <= n3dmax; ++m) {
+        int64_t ic1 = 0;
+        int64_t lm = mip[m - 1];
+        int nkmin = std::max(m - (ii - 2) - (jj - 2), 3);
+        int nkmax = std::min(m - 2 * 3, kk - 2);
+        for (int k = nkmin; k <= nkmax; ++k) {
+            int nimin = std::max(m - (jj - 2) - k, 3);
+            int nimax = std::min(m - k - 1 * 3, ii - 2);
+            for (int i = nimin; i <= nimax; ++i) {
+                int j = m - k - i;
+                if (i < 3 || i > ii - 2 || j < 3 || j > jj - 2 || k < 3 || k > kk - 2)
+                    return fail(MGLET_ERR_ARG, "hyperplane_init_grid: index out of bounds");
+                ++ic1;
+                idx[lm + ic1 - 1] = (int64_t)k + (int64_t)(j - 1) * kk + (int64_t)(i - 1) * kk * jj;
+            }
+        }
+        mip[m] = mip[m - 1] + ic1;   // mip(m+1)
+    }
+    // selection sort within each plane (any ascending sort gives the same list)
+    for (int m = n3dmin; m <= n3dmax; ++m) {
+        int64_t s = mip[m - 1], e = mip[m];
+        std::vector<int64_t> v(idx + s, idx + e);
+        std::sort(v.begin(), v.end());
+        for (size_t q = 1; q < v.size(); ++q)
+            if (v[q] <= v[q - 1]) return fail(MGLET_ERR_ARG, "sort: sorting failed");
+        std::copy(v.begin(), v.end(), idx + s);
+    }
+    // check
+    std::vector<int> test((size_t)kk * jj * ii, 0);
+    for (int m = n3dmin; m <= n3dmax; ++m) {
+        for (int64_t ip = mip[m - 1]; ip < mip[m]; ++ip) {
+            int64_t id = idx[ip];
+            int64_t r = id - 1;
+            int k = (int)(r % kk) + 1;
+            int j = (int)((r / kk) % jj) + 1;
+            int i = (int)(r / ((int64_t)kk * jj)) + 1;
+            test[IX(k, j, i)] += 1;
+            if (k + j + i != m) return fail(MGLET_ERR_ARG, "hyperplane_check_grid: index error");
+        }
+    }
+    int64_t sum = 0;
+    for (int i = 1; i <= ii; ++i)
+        for (int j = 1; j <= jj; ++j)
+            for (int k = 1; k <= kk; ++k) {
+                int t = test[IX(k, j, i)];
+                if (t > 1) return fail(MGLET_ERR_ARG, "hyperplane_check_grid: duplicated");
+                if (i >= 3 && i <= ii - 2 && j >= 3 && j <= jj - 2 && k >= 3 && k <= kk - 2 && t < 1)
+                    return fail(MGLET_ERR_ARG, "hyperplane_check_grid: missing");
+                sum += t;
+            }
+    if (sum != (int64_t)(kk - 4) * (jj - 4) * (ii - 4))
+        return fail(MGLET_ERR_ARG, "hyperplane_check_grid: summation failed");
+    return 0;
+}
+
+// sip_hyperplane_mod.F90:106-257 sip_hyperplane_lu
+void sip_hyperplane_lu(int kk, int jj, int ii, double* lw, double* ls, double* lb, double* lpr,
+                       double* ue, double* un, double* ut, const double* aw, const double* ae,
+                       const double* as, const double* an, const double* ab, const double* at,
+                       const double* ap, const double* bp, const int64_t* mip,
+                       const int64_t* idxsip) {
+    // aw..at are 1-based views (aw[i]); ap, bp are grid slabs.
+    const int64_t n = (int64_t)kk * jj * ii;
+    std::vector<double> lw_t(n + 1, 0.0), ls_t(n + 1, 0.0), lb_t(n + 1, 0.0), lpr_t(n + 1, 0.0),
+        ue_t(n + 1, 0.0), un_t(n + 1, 0.0), ut_t(n + 1, 0.0);
+    auto BP = [&](int k, int j, int i) { return bp[IX(k, j, i)]; };
+    auto bu = [&](int k, int j, int i) { return BP(k, j, i) * BP(k, j, i + 1); };
+    auto bv = [&](int k, int j, int i) { return BP(k, j, i) * BP(k, j + 1, i); };
+    auto bw = [&](int k, int j, int i) { return BP(k, j, i) * BP(k + 1, j, i); };
+    const int n3dmin = 9, n3dmax = (ii - 2) + (jj - 2) + (kk - 2);
+    for (int m = n3dmin; m <= n3dmax; ++m) {
+        int64_t lm = mip[m - 1];
+        int64_t lp = mip[m] - lm;
+        for (int64_t ip = 1; ip <= lp; ++ip) {
+            int64_t iacc = lm + ip;
+            int64_t id = idxsip[iacc - 1];
+            int64_t km = id - 1, jm = id - kk, im = id - (int64_t)kk * jj;
+            int64_t r = id - 1;
+            int k = (int)(r % kk) + 1;
+            int j = (int)((r / kk) % jj) + 1;
+            int i = (int)(r / ((int64_t)kk * jj)) + 1;
+            lw_t[id] = aw[i] * bu(k, j, i - 1) / (1.0 + kAlfa * (un_t[im] + ut_t[im]));
+            ls_t[id] = as[j] * bv(k, j - 1, i) / (1.0 + kAlfa * (ue_t[jm] + ut_t[jm]));
+            lb_t[id] = ab[k] * bw(k - 1, j, i) / (1.0 + kAlfa * (un_t[km] + ue_t[km]));
+            double p1 = kAlfa * (lb_t[id] * ue_t[km] + ls_t[id] * ue_t[jm]);
+            double p2 = kAlfa * (lb_t[id] * un_t[km] + lw_t[id] * un_t[im]);
+            double p3 = kAlfa * (lw_t[id] * ut_t[im] + ls_t[id] * ut_t[jm]);
+            lpr_t[id] = 1.0 / (ap[IX(k, j, i)] + p1 + p2 + p3 - lb_t[id] * ut_t[km] -
+                               lw_t[id] * ue_t[im] - ls_t[id] * un_t[jm] + kTiny);
+            ue_t[id] = (ae[i] * bu(k, j, i) - p1) * lpr_t[id];
+            un_t[id] = (an[j] * bv(k, j, i) - p2) * lpr_t[id];
+            ut_t[id] = (at[k] * bw(k, j, i) - p3) * lpr_t[id];
+            lw_t[id] = lw_t[id] * lpr_t[id];
+            ls_t[id] = ls_t[id] * lpr_t[id];
+            lb_t[id] = lb_t[id] * lpr_t[id];
+            lw[iacc - 1] = lw_t[id];
+            ls[iacc - 1] = ls_t[id];
+            lb[iacc - 1] = lb_t[id];
+            lpr[iacc - 1] = lpr_t[id];
+            ue[iacc - 1] = ue_t[id];
+            un[iacc - 1] = un_t[id];
+            ut[iacc - 1] = ut_t[id];
+        }
+    }
+}
+
+// sip_classic_mod.F90:17-127 sip_classic_init (one grid)
+void sip_classic_lu(int kk, int jj, int ii, double* lw, double* ls, double* lb, double* lpr,
+                    double* ue, double* un, double* ut, const double* aw, const double* ae,
+                    const double* as, const double* an, const double* ab, const double* at,
+                    const double* ap, const double* bp) {
+    auto BP = [&](int k, int j, int i) { return bp[IX(k, j, i)]; };
+    auto bu = [&](int k, int j, int i) { return BP(k, j, i) * BP(k, j, i + 1); };
+    auto bv = [&](int k, int j, int i) { return BP(k, j, i) * BP(k, j + 1, i); };
+    auto bw = [&](int k, int j, int i) { return BP(k, j, i) * BP(k + 1, j, i); };
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                int64_t c = IX(k, j, i);
+                int64_t cim = IX(k, j, i - 1), cjm = IX(k, j - 1, i), ckm = IX(k - 1, j, i);
+                lw[c] = aw[i] * bu(k, j, i - 1) / (1.0 + kAlfa * (un[cim] + ut[cim]));
+                ls[c] = as[j] * bv(k, j - 1, i) / (1.0 + kAlfa * (ue[cjm] + ut[cjm]));
+                lb[c] = ab[k] * bw(k - 1, j, i) / (1.0 + kAlfa * (un[ckm] + ue[ckm]));
+                double p1 = kAlfa * (lb[c] * ue[ckm] + ls[c] * ue[cjm]);
+                double p2 = kAlfa * (lb[c] * un[ckm] + lw[c] * un[cim]);
+                double p3 = kAlfa * (lw[c] * ut[cim] + ls[c] * ut[cjm]);
+                lpr[c] = 1.0 / (ap[c] + p1 + p2 + p3 - lb[c] * ut[ckm] - lw[c] * ue[cim] -
+                                ls[c] * un[cjm] + kTiny);
+                ue[c] = (ae[i] * bu(k, j, i) - p1) * lpr[c];
+                un[c] = (an[j] * bv(k, j, i) - p2) * lpr[c];
+                ut[c] = (at[k] * bw(k, j, i) - p3) * lpr[c];
+            }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j) {
+            for (int k = 3; k <= kk - 2; ++k) lw[IX(k, j, i)] = lw[IX(k, j, i)] * lpr[IX(k, j, i)];
+            for (int k = 3; k <= kk - 2; ++k) ls[IX(k, j, i)] = ls[IX(k, j, i)] * lpr[IX(k, j, i)];
+            for (int k = 3; k <= kk - 2; ++k) lb[IX(k, j, i)] = lb[IX(k, j, i)] * lpr[IX(k, j, i)];
+        }
+}
+
+// pressuresolver_mod.F90:47-145 init_pressuresolver (SIP coefficient part)
+int init_pressuresolver(Ctx& c) {
+    for (const char* n : {"SIPLW", "SIPLS", "SIPLB", "SIPUE", "SIPUN", "SIPUT", "SIPLPR"})
+        c.f3[n].assign(c.idim3d, 0.0);
+    c.mip.assign(c.idim3d, 0);
+    c.idxsip.assign(c.idim3d, -1);
+    double* aw = c.L("GSAW"); double* ae = c.L("GSAE"); double* as = c.L("GSAS");
+    double* an = c.L("GSAN"); double* ab = c.L("GSAB"); double* at = c.L("GSAT");
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        int64_t o = G.ip3;
+        if (c.prm.psolver == MGLET_PSOLVER_CLASSIC) {
+            sip_classic_lu(G.kk, G.jj, G.ii, c.F("SIPLW") + o, c.F("SIPLS") + o, c.F("SIPLB") + o,
+                           c.F("SIPLPR") + o, c.F("SIPUE") + o, c.F("SIPUN") + o,
+                           c.F("SIPUT") + o, aw + G.ipx - 1, ae + G.ipx - 1, as + G.ipy - 1,
+                           an + G.ipy - 1, ab + G.ipz - 1, at + G.ipz - 1, c.F("GSAP") + o,
+                           c.F("BP") + o);
+        } else {
+            int rc = sip_hyperplane_init_grid(G.kk, G.jj, G.ii, c.mip.data() + o,
+                                              c.idxsip.data() + o);
+            if (rc) return rc;
+            sip_hyperplane_lu(G.kk, G.jj, G.ii, c.F("SIPLW") + o, c.F("SIPLS") + o,
+                              c.F("SIPLB") + o, c.F("SIPLPR") + o, c.F("SIPUE") + o,
+                              c.F("SIPUN") + o, c.F("SIPUT") + o, aw + G.ipx - 1, ae + G.ipx - 1,
+                              as + G.ipy - 1, an + G.ipy - 1, ab + G.ipz - 1, at + G.ipz - 1,
+                              c.F("GSAP") + o, c.F("BP") + o, c.mip.data() + o,
+                              c.idxsip.data() + o);
+        }
+    }
+    if (c.prm.psolver == MGLET_PSOLVER_SOR) {
+        // sor_mod.F90:18-49 (divide0, simdfunctions_mod.F90:56-80)
+        c.f3["SOR_RAP"].assign(c.idim3d, 0.0);
+        for (int g = 1; g <= c.ngrid; ++g) {
+            const Grid& G = c.g[g];
+            const int kk = G.kk, jj = G.jj, ii = G.ii;
+            double* rap = c.F("SOR_RAP") + G.ip3;
+            const double* ap = c.F("GSAP") + G.ip3;
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    for (int k = 3; k <= kk - 2; ++k) {
+                        double a = ap[IX(k, j, i)];
+                        rap[IX(k, j, i)] = a == 0.0 ? 0.0 : 1.0 / a;
+                    }
+        }
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// laplacephi_mod.F90:134-165 laplacephi_grid
+void laplacephi_grid(Ctx& c, int g, double* RES, const double* PHI) {
+    const Grid& G = c.g[g];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    double* res = RES + G.ip3;
+    const double* phi = PHI + G.ip3;
+    const double* ap = c.F("GSAP") + G.ip3;
+    const double* bp = c.F("BP") + G.ip3;
+    const double* aw = c.L("GSAW") + G.ipx - 1; const double* ae = c.L("GSAE") + G.ipx - 1;
+    const double* as = c.L("GSAS") + G.ipy - 1; const double* an = c.L("GSAN") + G.ipy - 1;
+    const double* ab = c.L("GSAB") + G.ipz - 1; const double* at = c.L("GSAT") + G.ipz - 1;
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k)
+                res[IX(k, j, i)] =
+                    -aw[i] * phi[IX(k, j, i - 1)] * bp[IX(k, j, i - 1)] * bp[IX(k, j, i)] -
+                    ae[i] * phi[IX(k, j, i + 1)] * bp[IX(k, j, i)] * bp[IX(k, j, i + 1)] -
+                    as[j] * phi[IX(k, j - 1, i)] * bp[IX(k, j - 1, i)] * bp[IX(k, j, i)] -
+                    an[j] * phi[IX(k, j + 1, i)] * bp[IX(k, j, i)] * bp[IX(k, j + 1, i)] -
+                    ab[k] * phi[IX(k - 1, j, i)] * bp[IX(k - 1, j, i)] * bp[IX(k, j, i)] -
+                    at[k] * phi[IX(k + 1, j, i)] * bp[IX(k, j, i)] * bp[IX(k + 1, j, i)] -
+                    ap[IX(k, j, i)] * phi[IX(k, j, i)];
+}
+
+void laplacephi_level(Ctx& c, int ilevel, double* res, const double* phi) {
+#pragma omp parallel for schedule(dynamic)
+    for (int g = 1; g <= c.ngrid; ++g)
+        if (ilevel <= 0 || c.g[g].level == ilevel) laplacephi_grid(c, g, res, phi);
+}
+
+// sip_hyperplane_mod.F90:450-505 sipiter1
+void sipiter1_hp(int kk, int jj, int ii, const double* rhs, double* res, const double* lw,
+                 const double* ls, const double* lb, const double* lpr, const int64_t* mip,
+                 const int64_t* idxsip) {
+    const int n3dmin = 9, n3dmax = (ii - 2) + (jj - 2) + (kk - 2);
+    for (int m = n3dmin; m <= n3dmax; ++m) {
+        int64_t lm = mip[m - 1], lp = mip[m] - lm;
+        for (int64_t ip = 1; ip <= lp; ++ip) {
+            int64_t iacc = lm + ip - 1;            // 0-based
+            int64_t id = idxsip[iacc] - 1;         // 0-based
+            int64_t km = id - 1, jm = id - kk, im = id - (int64_t)kk * jj;
+            res[id] = (rhs[id] + res[id]) * lpr[iacc];
+            res[id] = res[id] - lb[iacc] * res[km] - ls[iacc] * res[jm] - lw[iacc] * res[im];
+        }
+    }
+}
+
+// sip_hyperplane_mod.F90:508-569 sipiter2
+void sipiter2_hp(int kk, int jj, int ii, double* phi, double* res, const double* ue,
+                 const double* un, const double* ut, const int64_t* mip, const int64_t* idxsip) {
+    const int n3dmin = 9, n3dmax = (ii - 2) + (jj - 2) + (kk - 2);
+    for (int m = n3dmax; m >= n3dmin; --m) {
+        int64_t lm = mip[m - 1], lp = mip[m] - lm;
+        for (int64_t ip = 1; ip <= lp; ++ip) {
+            int64_t iacc = lm + ip - 1;
+            int64_t id = idxsip[iacc] - 1;
+            int64_t kp = id + 1, jp = id + kk, ipp = id + (int64_t)kk * jj;
+            res[id] = res[id] - ut[iacc] * res[kp] - un[iacc] * res[jp] - ue[iacc] * res[ipp];
+        }
+    }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) phi[IX(k, j, i)] = phi[IX(k, j, i)] + res[IX(k, j, i)];
+}
+
+// sip_classic_mod.F90:143-166 sipiter1
+void sipiter1_cl(int kk, int jj, int ii, const double* rhs, double* res, const double* lw,
+                 const double* ls, const double* lb, const double* lpr) {
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j) {
+            for (int k = 3; k <= kk - 2; ++k) {
+                int64_t c = IX(k, j, i);
+                res[c] = (rhs[c] + res[c]) * lpr[c];
+                res[c] = res[c] - lw[c] * res[IX(k, j, i - 1)] - ls[c] * res[IX(k, j - 1, i)];
+            }
+            for (int k = 3; k <= kk - 2; ++k) {
+                int64_t c = IX(k, j, i);
+                res[c] = res[c] - lb[c] * res[IX(k - 1, j, i)];
+            }
+        }
+}
+
+// sip_classic_mod.F90:169-198 sipiter2
+void sipiter2_cl(int kk, int jj, int ii, double* phi, double* res, const double* ue,
+                 const double* un, const double* ut) {
+    for (int i = ii - 2; i >= 3; --i)
+        for (int j = jj - 2; j >= 3; --j) {
+            for (int k = 3; k <= kk - 2; ++k) {
+                int64_t c = IX(k, j, i);
+                res[c] = res[c] - un[c] * res[IX(k, j + 1, i)] - ue[c] * res[IX(k, j, i + 1)];
+            }
+            for (int k = kk - 2; k >= 3; --k) {
+                int64_t c = IX(k, j, i);
+                res[c] = res[c] - ut[c] * res[IX(k + 1, j, i)];
+            }
+        }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) phi[IX(k, j, i)] = phi[IX(k, j, i)] + res[IX(k, j, i)];
+}
+
+// sor_mod.F90:102-203 relax (no bp: ib type noib passes no BP)
+void relax(Ctx& c, int g, double* DP, const double* RHS) {
+    const Grid& G = c.g[g];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    double* dp = DP + G.ip3;
+    const double* rhs = RHS + G.ip3;
+    const double* rap = c.F("SOR_RAP") + G.ip3;
+    const double* aw = c.L("GSAW") + G.ipx - 1; const double* ae = c.L("GSAE") + G.ipx - 1;
+    const double* as = c.L("GSAS") + G.ipy - 1; const double* an = c.L("GSAN") + G.ipy - 1;
+    const double* ab = c.L("GSAB") + G.ipz - 1; const double* at = c.L("GSAT") + G.ipz - 1;
+    const double omg = c.prm.omega;
+    for (int rb = 0; rb <= 1; ++rb)
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j) {
+                int ks, ke;
+                if ((i + j) % 2 == rb) { ks = 4; ke = kk - 2; }
+                else { ks = 3; ke = kk - 3; }
+                for (int k = ks; k <= ke; k += 2) {
+                    double res = (aw[i] * dp[IX(k, j, i - 1)] + ae[i] * dp[IX(k, j, i + 1)] +
+                                  as[j] * dp[IX(k, j - 1, i)] + an[j] * dp[IX(k, j + 1, i)] +
+                                  ab[k] * dp[IX(k - 1, j, i)] + at[k] * dp[IX(k + 1, j, i)] -
+                                  rhs[IX(k, j, i)]) * rap[IX(k, j, i)];
+                    dp[IX(k, j, i)] = (1.0 - omg) * dp[IX(k, j, i)] - omg * res;
+                }
+            }
+}
+
+// pressuresolver_mod.F90:423-465 sip
+void sip(Ctx& c, int ilevel, int iloop, double* dp, double* res, const double* rhs) {
+    laplacephi_level(c, ilevel, res, dp);
+    const bool classic = c.prm.psolver == MGLET_PSOLVER_CLASSIC;
+#pragma omp parallel for schedule(dynamic)
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel) continue;
+        int64_t o = G.ip3;
+        if (classic)
+            sipiter1_cl(G.kk, G.jj, G.ii, rhs + o, res + o, c.F("SIPLW") + o, c.F("SIPLS") + o,
+                        c.F("SIPLB") + o, c.F("SIPLPR") + o);
+        else
+            sipiter1_hp(G.kk, G.jj, G.ii, rhs + o, res + o, c.F("SIPLW") + o, c.F("SIPLS") + o,
+                        c.F("SIPLB") + o, c.F("SIPLPR") + o, c.mip.data() + o,
+                        c.idxsip.data() + o);
+    }
+    if (iloop < c.prm.ninner)
+        connect(c, ilevel, 1, nullptr, nullptr, nullptr, res, nullptr, nullptr, false, false, 0);
+    else
+        connect(c, ilevel, 1, nullptr, nullptr, nullptr, res, nullptr, nullptr, false, false, -1);
+#pragma omp parallel for schedule(dynamic)
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel) continue;
+        int64_t o = G.ip3;
+        if (classic)
+            sipiter2_cl(G.kk, G.jj, G.ii, dp + o, res + o, c.F("SIPUE") + o, c.F("SIPUN") + o,
+                        c.F("SIPUT") + o);
+        else
+            sipiter2_hp(G.kk, G.jj, G.ii, dp + o, res + o, c.F("SIPUE") + o, c.F("SIPUN") + o,
+                        c.F("SIPUT") + o, c.mip.data() + o, c.idxsip.data() + o);
+    }
+}
+
+// pressuresolver_mod.F90:361-420 mgpoisit (bound_pressure: no PAR faces)
+void mgpoisit(Ctx& c, int ilevel, double* dp, const double* rhs, double* res) {
+    for (int iloop = 1; iloop <= c.prm.ninner; ++iloop) {
+        if (c.prm.psolver == MGLET_PSOLVER_SOR && ilevel > c.minlevel) {
+#pragma omp parallel for schedule(dynamic)
+            for (int g = 1; g <= c.ngrid; ++g)
+                if (c.g[g].level == ilevel) relax(c, g, dp, rhs);
+        } else {
+            sip(c, ilevel, iloop, dp, res, rhs);
+        }
+        connect(c, ilevel, 1, nullptr, nullptr, nullptr, dp, nullptr, nullptr, false, false, 0);
+    }
+}
+
+// pressuresolver_mod.F90:623-689 maxabscal
+double maxabscal(Ctx& c, const double* PHI) {
+    std::vector<double> mg(c.ngrid + 1, 0.0);
+#pragma omp parallel for schedule(dynamic)
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const double* phi = PHI + G.ip3;
+        double m = 0.0;
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k) m = std::max(std::fabs(phi[IX(k, j, i)]), m);
+        mg[g] = m;
+    }
+    double maxabs = 0.0;
+    for (int g = 1; g <= c.ngrid; ++g)
+        maxabs = std::max(std::fabs(mg[g] * std::ldexp(1.0, c.maxlevel - c.g[g].level)), maxabs);
+    return maxabs;
+}
+
+// pressuresolver_mod.F90:787-879 mgpcorr_grid (bp absent for noib)
+void mgpcorr(Ctx& c, double* U, double* V, double* W, double* P, const double* DP, double rfak) {
+#pragma omp parallel for schedule(dynamic)
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        double* u = U + G.ip3; double* v = V + G.ip3; double* w = W + G.ip3;
+        double* p = P + G.ip3;
+        const double* dp = DP + G.ip3;
+        const double* rdx = c.L("RDX") + G.ipx - 1;
+        const double* rdy = c.L("RDY") + G.ipy - 1;
+        const double* rdz = c.L("RDZ") + G.ipz - 1;
+        for (int i = 2; i <= ii - 1; ++i)
+            for (int j = 2; j <= jj - 1; ++j)
+                for (int k = 2; k <= kk - 1; ++k) p[IX(k, j, i)] = p[IX(k, j, i)] + dp[IX(k, j, i)];
+        for (int i = 2; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k)
+                    u[IX(k, j, i)] = u[IX(k, j, i)] +
+                                     (dp[IX(k, j, i)] - dp[IX(k, j, i + 1)]) * rdx[i] * rfak;
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 2; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k)
+                    v[IX(k, j, i)] = v[IX(k, j, i)] +
+                                     (dp[IX(k, j, i)] - dp[IX(k, j + 1, i)]) * rdy[j] * rfak;
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 2; k <= kk - 2; ++k)
+                    w[IX(k, j, i)] = w[IX(k, j, i)] +
+                                     (dp[IX(k, j, i)] - dp[IX(k + 1, j, i)]) * rdz[k] * rfak;
+    }
+}
+
+// noib_mod.F90:253-354 divcal (noib: no bp, no sdiv)
+void divcal(Ctx& c, double* DIV, const double* U, const double* V, const double* W, double fak) {
+#pragma omp parallel for schedule(dynamic)
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        double* div = DIV + G.ip3;
+        const double* u = U + G.ip3; const double* v = V + G.ip3; const double* w = W + G.ip3;
+        const double* rddx = c.L("RDDX") + G.ipx - 1;
+        const double* rddy = c.L("RDDY") + G.ipy - 1;
+        const double* rddz = c.L("RDDZ") + G.ipz - 1;
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k)
+                    div[IX(k, j, i)] = fak * ((u[IX(k, j, i)] - u[IX(k, j, i - 1)]) * rddx[i] +
+                                              (v[IX(k, j, i)] - v[IX(k, j - 1, i)]) * rddy[j] +
+                                              (w[IX(k, j, i)] - w[IX(k - 1, j, i)]) * rddz[k]);
+    }
+}
+
+// pressuresolver_mod.F90:160-357 mgpoisl (single level, noib)
+void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
+    double* U = c.F("U"); double* V = c.F("V"); double* W = c.F("W"); double* P = c.F("P");
+    for (const char* n : {"DP", "HILF", "RHS", "RES"}) c.f3[n].assign(c.idim3d, 0.0);
+    double* dp = c.F("DP"); double* hilf = c.F("HILF");
+    double* rhs = c.F("RHS"); double* res = c.F("RES");
+    const double prefak = c.prm.rho / dt;
+    divcal(c, rhs, U, V, W, prefak);
+    int ipc = 0, ipcount_done = 0;
+    double maxrhs = 0.0;
+    for (int ipcount = 1; ipcount <= c.prm.nouter; ++ipcount) {
+        for (int ilevel = c.minlevel; ilevel <= c.maxlevel; ++ilevel)
+            mgpoisit(c, ilevel, hilf, rhs, res);
+        connect(c, 0, 1, nullptr, nullptr, nullptr, hilf, nullptr, nullptr, false, false, 0);
+        laplacephi_level(c, 0, res, hilf);
+        // rescal: rhs += res on the interior
+#pragma omp parallel for schedule(dynamic)
+        for (int g = 1; g <= c.ngrid; ++g) {
+            const Grid& G = c.g[g];
+            const int kk = G.kk, jj = G.jj, ii = G.ii;
+            double* r = rhs + G.ip3; const double* s = res + G.ip3;
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    for (int k = 3; k <= kk - 2; ++k) r[IX(k, j, i)] = r[IX(k, j, i)] + s[IX(k, j, i)];
+        }
+        maxrhs = maxabscal(c, rhs);
+        // accumulate_pcorr over the whole flat array, then hilf = 0
+        for (int64_t n = 0; n < c.idim3d; ++n) dp[n] = dp[n] + hilf[n];
+        std::fill(c.f3["HILF"].begin(), c.f3["HILF"].end(), 0.0);
+        ipc += c.prm.ninner;
+        ipcount_done = ipcount;
+        if (ipcount >= c.prm.nouter_min && maxrhs / prefak < c.prm.epcorr) break;
+    }
+    mgpcorr(c, U, V, W, P, dp, dt / c.prm.rho);
+    connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0);
+    if (st) {
+        st->ipc = ipc;
+        st->nouter_done = ipcount_done;
+        st->maxrhs = maxrhs;
+        st->prefak = prefak;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// tstle4_mod.F90:139-265 tstle4_kon, :268-458 tstle4_diff, :461-529 tstle4_gradp
+void tstle4_grid(Ctx& c, int g) {
+    const Grid& G = c.g[g];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int64_t o = G.ip3;
+    double* uo = c.F("UO") + o; double* vo = c.F("VO") + o; double* wo = c.F("WO") + o;
+    const double* u = c.F("U") + o; const double* v = c.F("V") + o; const double* w = c.F("W") + o;
+    const double* ut = u; const double* vt = v; const double* wt = w;   // noib
+    const double* p = c.F("P") + o; const double* gg = c.F("G") + o;
+    const double* dx = c.L("DX") + G.ipx - 1; const double* dy = c.L("DY") + G.ipy - 1;
+    const double* dz = c.L("DZ") + G.ipz - 1;
+    const double* ddx = c.L("DDX") + G.ipx - 1; const double* ddy = c.L("DDY") + G.ipy - 1;
+    const double* ddz = c.L("DDZ") + G.ipz - 1;
+    const double* rdx = c.L("RDX") + G.ipx - 1; const double* rdy = c.L("RDY") + G.ipy - 1;
+    const double* rdz = c.L("RDZ") + G.ipz - 1;
+    const double* rddx = c.L("RDDX") + G.ipx - 1; const double* rddy = c.L("RDDY") + G.ipy - 1;
+    const double* rddz = c.L("RDDZ") + G.ipz - 1;
+    const int nfro = G.bc[1], nbac = G.bc[2], nrgt = G.bc[3], nlft = G.bc[4], nbot = G.bc[5],
+              ntop = G.bc[6];
+    int nfu = 0, nbu = 0, nrv = 0, nlv = 0, nbw = 0, ntw = 0;
+    if (nbac == 7) nbu = 1;
+    if (nlft == 7) nlv = 1;
+    if (ntop == 7) ntw = 1;
+    if (nfro == 3) nfu = 1;
+    if (nbac == 3) nbu = 1;
+    if (nrgt == 3) nrv = 1;
+    if (nlft == 3) nlv = 1;
+    if (nbot == 3) nbw = 1;
+    if (ntop == 3) ntw = 1;
+    const double gmol = c.prm.gmol, rho = c.prm.rho;
+    const double iles = c.ilesmodel == 0 ? 0.0 : 1.0;
+#define A(a, k, j, i) a[IX(k, j, i)]
+    // ---- kon
+    for (int i = 3 - nfu; i <= ii - 3 + nbu; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                double ax = ddy[j] * ddz[k], ay = dx[i] * ddz[k], az = dx[i] * ddy[j];
+                double fe = ax * (A(ut, k, j, i) + (A(ut, k, j, i + 1) - A(ut, k, j, i)) * 0.5 * dx[i] / ddx[i + 1]);
+                double fw = ax * (A(ut, k, j, i - 1) + (A(ut, k, j, i) - A(ut, k, j, i - 1)) * 0.5 * dx[i - 1] / ddx[i]);
+                double fn = ay * (A(vt, k, j, i) + A(vt, k, j, i + 1)) * 0.5;
+                double fs = ay * (A(vt, k, j - 1, i) + A(vt, k, j - 1, i + 1)) * 0.5;
+                double ft = az * (A(wt, k, j, i) + A(wt, k, j, i + 1)) * 0.5;
+                double fb = az * (A(wt, k - 1, j, i) + A(wt, k - 1, j, i + 1)) * 0.5;
+                double qe = 0.5 * fe * (A(u, k, j, i) + A(u, k, j, i + 1));
+                double qw = 0.5 * fw * (A(u, k, j, i - 1) + A(u, k, j, i));
+                double qn = 0.5 * fn * (A(u, k, j, i) + A(u, k, j + 1, i));
+                double qs = 0.5 * fs * (A(u, k, j - 1, i) + A(u, k, j, i));
+                double qt = 0.5 * ft * (A(u, k, j, i) + A(u, k + 1, j, i));
+                double qb = 0.5 * fb * (A(u, k - 1, j, i) + A(u, k, j, i));
+                A(uo, k, j, i) = -(qe - qw + qn - qs + qt - qb) * rdx[i] * rddy[j] * rddz[k];
+            }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3 - nrv; j <= jj - 3 + nlv; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                double ax = dy[j] * ddz[k], ay = ddx[i] * ddz[k], az = ddx[i] * dy[j];
+                double fe = ax * (A(ut, k, j, i) + A(ut, k, j + 1, i)) * 0.5;
+                double fw = ax * (A(ut, k, j, i - 1) + A(ut, k, j + 1, i - 1)) * 0.5;
+                double fn = ay * (A(vt, k, j, i) + (A(vt, k, j + 1, i) - A(vt, k, j, i)) * 0.5 * dy[j] / ddy[j + 1]);
+                double fs = ay * (A(vt, k, j - 1, i) + (A(vt, k, j, i) - A(vt, k, j - 1, i)) * 0.5 * dy[j - 1] / ddy[j]);
+                double ft = az * (A(wt, k, j, i) + A(wt, k, j + 1, i)) * 0.5;
+                double fb = az * (A(wt, k - 1, j, i) + A(wt, k - 1, j + 1, i)) * 0.5;
+                double qe = 0.5 * fe * (A(v, k, j, i) + A(v, k, j, i + 1));
+                double qw = 0.5 * fw * (A(v, k, j, i - 1) + A(v, k, j, i));
+                double qn = 0.5 * fn * (A(v, k, j, i) + A(v, k, j + 1, i));
+                double qs = 0.5 * fs * (A(v, k, j - 1, i) + A(v, k, j, i));
+                double qt = 0.5 * ft * (A(v, k, j, i) + A(v, k + 1, j, i));
+                double qb = 0.5 * fb * (A(v, k - 1, j, i) + A(v, k, j, i));
+                A(vo, k, j, i) = -(qe - qw + qn - qs + qt - qb) * rddx[i] * rdy[j] * rddz[k];
+            }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k) {
+                double ax = ddy[j] * dz[k], ay = ddx[i] * dz[k], az = ddx[i] * ddy[j];
+                double fe = ax * (A(ut, k, j, i) + A(ut, k + 1, j, i)) * 0.5;
+                double fw = ax * (A(ut, k, j, i - 1) + A(ut, k + 1, j, i - 1)) * 0.5;
+                double fn = ay * (A(vt, k, j, i) + A(vt, k + 1, j, i)) * 0.5;
+                double fs = ay * (A(vt, k, j - 1, i) + A(vt, k + 1, j - 1, i)) * 0.5;
+                double ft = az * (A(wt, k, j, i) + (A(wt, k + 1, j, i) - A(wt, k, j, i)) * 0.5 * dz[k] / ddz[k + 1]);
+                double fb = az * (A(wt, k - 1, j, i) + (A(wt, k, j, i) - A(wt, k - 1, j, i)) * 0.5 * dz[k - 1] / ddz[k]);
+                double qe = 0.5 * fe * (A(w, k, j, i) + A(w, k, j, i + 1));
+                double qw = 0.5 * fw * (A(w, k, j, i - 1) + A(w, k, j, i));
+                double qn = 0.5 * fn * (A(w, k, j, i) + A(w, k, j + 1, i));
+                double qs = 0.5 * fs * (A(w, k, j - 1, i) + A(w, k, j, i));
+                double qt = 0.5 * ft * (A(w, k, j, i) + A(w, k + 1, j, i));
+                double qb = 0.5 * fb * (A(w, k - 1, j, i) + A(w, k, j, i));
+                A(wo, k, j, i) = -(qe - qw + qn - qs + qt - qb) * rddx[i] * rddy[j] * rdz[k];
+            }
+    // ---- diff (swcle3d acts on NOS faces only; NOS is rejected at create)
+    auto hm = [&](double a, double b) { return a * b / std::max(a + b, gmol); };
+    for (int i = 3 - nfu; i <= ii - 3 + nbu; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                double ax = ddy[j] * ddz[k], ay = dx[i] * ddz[k], az = dx[i] * ddy[j];
+                double ge = A(gg, k, j, i + 1);
+                double gw = A(gg, k, j, i);
+                double gn = hm(A(gg, k, j, i), A(gg, k, j + 1, i)) + hm(A(gg, k, j, i + 1), A(gg, k, j + 1, i + 1));
+                double gs = hm(A(gg, k, j - 1, i), A(gg, k, j, i)) + hm(A(gg, k, j - 1, i + 1), A(gg, k, j, i + 1));
+                double gt = hm(A(gg, k, j, i), A(gg, k + 1, j, i)) + hm(A(gg, k, j, i + 1), A(gg, k + 1, j, i + 1));
+                double gb = hm(A(gg, k - 1, j, i), A(gg, k, j, i)) + hm(A(gg, k - 1, j, i + 1), A(gg, k, j, i + 1));
+                double qe = -ge * ax * rddx[i + 1] * (A(u, k, j, i + 1) - A(u, k, j, i));
+                double qw = -gw * ax * rddx[i] * (A(u, k, j, i) - A(u, k, j, i - 1));
+                double qn = -gn * ay * rdy[j] * (A(u, k, j + 1, i) - A(u, k, j, i));
+                double qs = -gs * ay * rdy[j - 1] * (A(u, k, j, i) - A(u, k, j - 1, i));
+                double qt = -gt * az * rdz[k] * (A(u, k + 1, j, i) - A(u, k, j, i));
+                double qb = -gb * az * rdz[k - 1] * (A(u, k, j, i) - A(u, k - 1, j, i));
+                double st = ((ge * (A(u, k, j, i + 1) - A(u, k, j, i)) * rddx[i + 1]) -
+                             (gw * (A(u, k, j, i) - A(u, k, j, i - 1)) * rddx[i])) * ax +
+                            ((gn * (A(v, k, j, i + 1) - A(v, k, j, i))) -
+                             (gs * (A(v, k, j - 1, i + 1) - A(v, k, j - 1, i)))) * ddz[k] +
+                            ((gt * (A(w, k, j, i + 1) - A(w, k, j, i))) -
+                             (gb * (A(w, k - 1, j, i + 1) - A(w, k - 1, j, i)))) * ddy[j];
+                double qc = st * iles;
+                double fak = 1.0 / rho * rddy[j] * rdx[i] * rddz[k];
+                A(uo, k, j, i) = A(uo, k, j, i) - fak * (qe - qw + qn - qs + qt - qb - qc);
+            }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3 - nrv; j <= jj - 3 + nlv; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                double ax = dy[j] * ddz[k], ay = ddx[i] * ddz[k], az = ddx[i] * dy[j];
+                double ge = hm(A(gg, k, j, i), A(gg, k, j, i + 1)) + hm(A(gg, k, j + 1, i), A(gg, k, j + 1, i + 1));
+                double gw = hm(A(gg, k, j, i - 1), A(gg, k, j, i)) + hm(A(gg, k, j + 1, i - 1), A(gg, k, j + 1, i));
+                double gn = A(gg, k, j + 1, i);
+                double gs = A(gg, k, j, i);
+                double gt = hm(A(gg, k, j, i), A(gg, k + 1, j, i)) + hm(A(gg, k, j + 1, i), A(gg, k + 1, j + 1, i));
+                double gb = hm(A(gg, k - 1, j, i), A(gg, k, j, i)) + hm(A(gg, k - 1, j + 1, i), A(gg, k, j + 1, i));
+                double qe = -ge * ax * rdx[i] * (A(v, k, j, i + 1) - A(v, k, j, i));
+                double qw = -gw * ax * rdx[i - 1] * (A(v, k, j, i) - A(v, k, j, i - 1));
+                double qn = -gn * ay * rddy[j + 1] * (A(v, k, j + 1, i) - A(v, k, j, i));
+                double qs = -gs * ay * rddy[j] * (A(v, k, j, i) - A(v, k, j - 1, i));
+                double qt = -gt * az * rdz[k] * (A(v, k + 1, j, i) - A(v, k, j, i));
+                double qb = -gb * az * rdz[k - 1] * (A(v, k, j, i) - A(v, k - 1, j, i));
+                double st = ((ge * (A(u, k, j + 1, i) - A(u, k, j, i))) -
+                             (gw * (A(u, k, j + 1, i - 1) - A(u, k, j, i - 1)))) * ddz[k] +
+                            ((gn * (A(v, k, j + 1, i) - A(v, k, j, i)) * rddy[j + 1]) -
+                             (gs * (A(v, k, j, i) - A(v, k, j - 1, i)) * rddy[j])) * ay +
+                            ((gt * (A(w, k, j + 1, i) - A(w, k, j, i))) -
+                             (gb * (A(w, k - 1, j + 1, i) - A(w, k - 1, j, i)))) * ddx[i];
+                double qc = st * iles;
+                double fak = 1.0 / rho * rddx[i] * rdy[j] * rddz[k];
+                A(vo, k, j, i) = A(vo, k, j, i) - fak * (qe - qw + qn - qs + qt - qb - qc);
+            }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k) {
+                double ax = ddy[j] * dz[k], ay = ddx[i] * dz[k], az = ddx[i] * ddy[j];
+                double ge = hm(A(gg, k, j, i), A(gg, k, j, i + 1)) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j, i + 1));
+                double gw = hm(A(gg, k, j, i - 1), A(gg, k, j, i)) + hm(A(gg, k + 1, j, i - 1), A(gg, k + 1, j, i));
+                double gn = hm(A(gg, k, j, i), A(gg, k, j + 1, i)) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j + 1, i));
+                double gs = hm(A(gg, k, j - 1, i), A(gg, k, j, i)) + hm(A(gg, k + 1, j - 1, i), A(gg, k + 1, j, i));
+                double gt = A(gg, k + 1, j, i);
+                double gb = A(gg, k, j, i);
+                double qe = -ge * ax * rdx[i] * (A(w, k, j, i + 1) - A(w, k, j, i));
+                double qw = -gw * ax * rdx[i - 1] * (A(w, k, j, i) - A(w, k, j, i - 1));
+                double qn = -gn * ay * rdy[j] * (A(w, k, j + 1, i) - A(w, k, j, i));
+                double qs = -gs * ay * rdy[j - 1] * (A(w, k, j, i) - A(w, k, j - 1, i));
+                double qt = -gt * az * rddz[k + 1] * (A(w, k + 1, j, i) - A(w, k, j, i));
+                double qb = -gb * az * rddz[k] * (A(w, k, j, i) - A(w, k - 1, j, i));
+                double st = ((ge * (A(u, k + 1, j, i) - A(u, k, j, i))) -
+                             (gw * (A(u, k + 1, j, i - 1) - A(u, k, j, i - 1)))) * ddy[j] +
+                            ((gn * (A(v, k + 1, j, i) - A(v, k, j, i))) -
+                             (gs * (A(v, k + 1, j - 1, i) - A(v, k, j - 1, i)))) * ddx[i] +
+                            ((gt * (A(w, k + 1, j, i) - A(w, k, j, i)) * rddz[k + 1]) -
+                             (gb * (A(w, k, j, i) - A(w, k - 1, j, i)) * rddz[k])) * az;
+                double qc = st * iles;
+                double fak = 1.0 / rho * rddx[i] * rddy[j] * rdz[k];
+                A(wo, k, j, i) = A(wo, k, j, i) - fak * (qe - qw + qn - qs + qt - qb - qc);
+            }
+    // ---- gradp
+    const double gpx = c.prm.gradp[0] * G.gradpflag, gpy = c.prm.gradp[1] * G.gradpflag,
+                 gpz = c.prm.gradp[2] * G.gradpflag;
+    for (int i = 3 - nfu; i <= ii - 3 + nbu; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k)
+                A(uo, k, j, i) = A(uo, k, j, i) - 1.0 / (rho * dx[i]) * (A(p, k, j, i + 1) - A(p, k, j, i) + gpx * dx[i]);
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3 - nrv; j <= jj - 3 + nlv; ++j)
+            for (int k = 3; k <= kk - 2; ++k)
+                A(vo, k, j, i) = A(vo, k, j, i) - 1.0 / (rho * dy[j]) * (A(p, k, j + 1, i) - A(p, k, j, i) + gpy * dy[j]);
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k)
+                A(wo, k, j, i) = A(wo, k, j, i) - 1.0 / (rho * dz[k]) * (A(p, k + 1, j, i) - A(p, k, j, i) + gpz * dz[k]);
+#undef A
+}
+
+void tstle4(Ctx& c) {
+    for (const char* n : {"UO", "VO", "WO"}) c.f3[n].assign(c.idim3d, 0.0);
+#pragma omp parallel for schedule(dynamic)
+    for (int g = 1; g <= c.ngrid; ++g) tstle4_grid(c, g);
+}
+
+// rungekutta_mod.F90:315-333 rkstep
+void rkstep(double* p, double* dp, const double* rhsp, int64_t n, double frhs, double dtfu) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < n; ++i) {
+        dp[i] = frhs * dp[i] + rhsp[i];
+        p[i] = p[i] + dtfu * dp[i];
+    }
+}
+
+// rungekutta_mod.F90:70-95,98-237 (init_*), :288-309 comp_c
+int rk_init(const char* name, mglet_rk_scheme* rk) {
+    std::memset(rk, 0, sizeof(*rk));
+    std::string n(name ? name : "");
+    for (auto& ch : n) ch = (char)std::tolower((unsigned char)ch);
+    auto comp_c = [&]() {
+        for (int q = 0; q < 6; ++q) rk->c[q] = 0.0;
+        for (int i = 1; i <= rk->nrk; ++i)
+            for (int j = 1; j <= i - 1; ++j) {
+                double fak = 1.0;
+                for (int k = 2; k <= j; ++k) fak = rk->a[k - 1] * fak + 1.0;
+                rk->c[i - 1] = rk->c[i - 1] + rk->b[j - 1] * fak;
+            }
+    };
+    if (n == "williamson") {
+        rk->nrk = 3;
+        rk->cflmax = (1.0 - 2.220446049250313e-16) * std::sqrt(3.0);
+        double c[3] = {0.0, 1.0 / 3.0, 3.0 / 4.0}, a[3] = {0.0, -5.0 / 9.0, -153.0 / 128.0},
+               b[3] = {1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0};
+        for (int q = 0; q < 3; ++q) { rk->a[q] = a[q]; rk->b[q] = b[q]; rk->c[q] = c[q]; }
+    } else if (n == "berland") {
+        rk->nrk = 6;
+        rk->cflmax = (double)(3.80f - 0.01f);
+        double a[6] = {0.0, -0.737101392796, -1.634740794341, -0.744739003780, -1.469897351522, -2.813971388035};
+        double b[6] = {0.032918605146, 0.823256998200, 0.381530948900, 0.200092213184, 1.718581042715, 0.27};
+        for (int q = 0; q < 6; ++q) { rk->a[q] = a[q]; rk->b[q] = b[q]; }
+        comp_c();
+    } else if (n == "carpenter") {
+        rk->nrk = 5;
+        rk->cflmax = (double)(3.34f - 0.01f);
+        double a[5] = {0.0, -567301805773.0 / 1357537059087.0, -2404267990393.0 / 2016746695238.0,
+                       -3550918686646.0 / 2091501179385.0, -1275806237668.0 / 842570457699.0};
+        double b[5] = {1432997174477.0 / 9575080441755.0, 5161836677717.0 / 13612068292357.0,
+                       1720146321549.0 / 2090206949498.0, 3134564353537.0 / 4481467310338.0,
+                       2277821191437.0 / 14882151754819.0};
+        for (int q = 0; q < 5; ++q) { rk->a[q] = a[q]; rk->b[q] = b[q]; }
+        comp_c();
+    } else if (n == "bernardini") {
+        rk->nrk = 5;
+        rk->cflmax = (double)(3.47f - 0.01f);
+        const double eps = -3.88856487394645e-7;
+        double a[5] = {0.0, -1.0, -1.55798 + eps, -1.0, -0.45031 + eps};
+        double b[5] = {0.2, 0.83204 + eps, 0.6, 0.35394 + eps, 0.2};
+        for (int q = 0; q < 5; ++q) { rk->a[q] = a[q]; rk->b[q] = b[q]; }
+        comp_c();
+    } else {
+        return fail(MGLET_ERR_ARG, "rk_init: invalid scheme " + n);
+    }
+    return 0;
+}
+
+// timeintegration_mod.F90:306-452 compcflmax, compdivmax, enerfg
+void itinfo(Ctx& c, double dt, mglet_itinfo* out) {
+    std::vector<double> cfl(c.ngrid + 1), dmx(c.ngrid + 1), es(c.ngrid + 1), vs(c.ngrid + 1);
+#pragma omp parallel for schedule(dynamic)
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const double* u = c.F("U") + G.ip3; const double* v = c.F("V") + G.ip3;
+        const double* w = c.F("W") + G.ip3; const double* bp = c.F("BP") + G.ip3;
+        const double* sdiv = c.F("SDIV") + G.ip3;
+        const double* dx = c.L("DX") + G.ipx - 1; const double* dy = c.L("DY") + G.ipy - 1;
+        const double* dz = c.L("DZ") + G.ipz - 1;
+        const double* ddx = c.L("DDX") + G.ipx - 1; const double* ddy = c.L("DDY") + G.ipy - 1;
+        const double* ddz = c.L("DDZ") + G.ipz - 1;
+        const double* rddx = c.L("RDDX") + G.ipx - 1; const double* rddy = c.L("RDDY") + G.ipy - 1;
+        const double* rddz = c.L("RDDZ") + G.ipz - 1;
+#define A(a, k, j, i) a[IX(k, j, i)]
+        double cmax = 0.0;
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k) {
+                    double cflu = std::fabs(2.0 * A(u, k, j, i - 1) + (A(u, k, j, i) - A(u, k, j, i - 1)) * dx[i - 1] / ddx[i]) / ddx[i] +
+                                  std::fabs(2.0 * A(u, k, j, i) + (A(u, k, j, i + 1) - A(u, k, j, i)) * dx[i] / ddx[i + 1]) / ddx[i] +
+                                  std::fabs(A(v, k, j, i) + A(v, k, j, i + 1)) / ddy[j] +
+                                  std::fabs(A(v, k, j - 1, i) + A(v, k, j - 1, i + 1)) / ddy[j] +
+                                  std::fabs(A(w, k, j, i) + A(w, k, j, i + 1)) / ddz[k] +
+                                  std::fabs(A(w, k - 1, j, i) + A(w, k - 1, j, i + 1)) / ddz[k];
+                    cflu = cflu * A(bp, k, j, i) * A(bp, k, j, i + 1);
+                    double cflv = std::fabs(A(u, k, j, i) + A(u, k, j + 1, i)) / ddx[i] +
+                                  std::fabs(A(u, k, j, i - 1) + A(u, k, j + 1, i - 1)) / ddx[i] +
+                                  std::fabs(2.0 * A(v, k, j - 1, i) + (A(v, k, j, i) - A(v, k, j - 1, i)) * dy[j - 1] / ddy[j]) / ddy[j] +
+                                  std::fabs(2.0 * A(v, k, j, i) + (A(v, k, j + 1, i) - A(v, k, j, i)) * dy[j] / ddy[j + 1]) / ddy[j] +
+                                  std::fabs(A(w, k, j, i) + A(w, k, j + 1, i)) / ddz[k] +
+                                  std::fabs(A(w, k - 1, j, i) + A(w, k - 1, j + 1, i)) / ddz[k];
+                    cflv = cflv * A(bp, k, j, i) * A(bp, k, j + 1, i);
+                    double cflw = std::fabs(A(u, k, j, i) + A(u, k + 1, j, i)) / ddx[i] +
+                                  std::fabs(A(u, k, j, i - 1) + A(u, k + 1, j, i - 1)) / ddx[i] +
+                                  std::fabs(A(v, k, j, i) + A(v, k + 1, j, i)) / ddy[j] +
+                                  std::fabs(A(v, k, j - 1, i) + A(v, k + 1, j - 1, i)) / ddy[j] +
+                                  std::fabs(2.0 * A(w, k - 1, j, i) + (A(w, k, j, i) - A(w, k - 1, j, i)) * dz[k - 1] / ddz[k]) / ddz[k] +
+                                  std::fabs(2.0 * A(w, k, j, i) + (A(w, k + 1, j, i) - A(w, k, j, i)) * dz[k] / ddz[k + 1]) / ddz[k];
+                    cflw = cflw * A(bp, k, j, i) * A(bp, k + 1, j, i);
+                    double m = std::max(cflu, std::max(cflv, cflw));
+                    if (m > cmax) cmax = m;
+                }
+        cfl[g] = cmax * 0.25 * dt;
+        double dm = 0.0;
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k) {
+                    double div = A(sdiv, k, j, i) + (A(u, k, j, i) - A(u, k, j, i - 1)) * rddx[i] +
+                                 (A(v, k, j, i) - A(v, k, j - 1, i)) * rddy[j] +
+                                 (A(w, k, j, i) - A(w, k - 1, j, i)) * rddz[k];
+                    div = A(bp, k, j, i) * div;
+                    if (std::fabs(div) > dm) dm = std::fabs(div);
+                }
+        dmx[g] = dm;
+        double esum = 0.0, vsum = 0.0;
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k) {
+                    double up = A(u, k, j, i - 1) + (A(u, k, j, i) - A(u, k, j, i - 1)) * 0.5 * dx[i - 1] / ddx[i];
+                    double vp = A(v, k, j - 1, i) + (A(v, k, j, i) - A(v, k, j - 1, i)) * 0.5 * dy[j - 1] / ddy[j];
+                    double wp = A(w, k - 1, j, i) + (A(w, k, j, i) - A(w, k - 1, j, i)) * 0.5 * dz[k - 1] / ddz[k];
+                    double vol = ddx[i] * ddy[j] * ddz[k];
+                    esum = esum + vol * 0.5 * (up * up + vp * vp + wp * wp);
+                    vsum = vsum + vol;
+                }
+        es[g] = esum / vsum;
+        vs[g] = vsum;
+#undef A
+    }
+    // itinfo_mod.F90:204-226: maxima over grids; energy as the running
+    // volume-weighted mean of the per-grid means, in grid order.
+    double cm = 0.0, dm = 0.0, esum = 0.0, vol = 0.0;
+    bool nan = false;
+    for (int g = 1; g <= c.ngrid; ++g) {
+        cm = std::max(cm, cfl[g]);
+        dm = std::max(dm, dmx[g]);
+        if (vol + vs[g] > 0.0) esum = (esum * vol + es[g] * vs[g]) / (vol + vs[g]);
+        else esum = 0.0;
+        vol = vol + vs[g];
+        if (!std::isfinite(cfl[g]) || !std::isfinite(dmx[g]) || !std::isfinite(es[g])) nan = true;
+    }
+    out->cflmax = cm;
+    out->divmax = dm;
+    out->energy = esum;
+    out->exploded = nan ? 1 : 0;
+}
+
+bool check_supported(const Ctx& c) {
+    for (int g = 1; g <= c.ngrid; ++g)
+        for (int f = 1; f <= 6; ++f)
+            if (!is_con(c.g[g].bc[f])) return false;
+    return true;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI (mirrors include/mglet_gpu.h with an oracle_ prefix)
+struct oracle_ctx : Ctx {};
+
+extern "C" {
+
+const char* oracle_last_error(void) { return g_err.c_str(); }
+
+void oracle_set_threads(int n) {
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+int oracle_max_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+int oracle_rk_init(const char* name, mglet_rk_scheme* out) { return rk_init(name, out); }
+
+int oracle_rk_get_coeffs(const mglet_rk_scheme* rk, int irk, double* frhs, double* fu,
+                         double* dtrk, double* dtrki) {
+    if (irk > rk->nrk || irk < 0) return fail(MGLET_ERR_ARG, "get_coeffs: irk out of range");
+    *frhs = rk->a[irk - 1];
+    *fu = rk->b[irk - 1];
+    *dtrk = irk < rk->nrk ? rk->c[irk] : 1.0;
+    *dtrki = *dtrk - rk->c[irk - 1];
+    return 0;
+}
+
+int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle_ctx** out) {
+    if (!d || !prm || !out || d->ngrid <= 0) return fail(MGLET_ERR_ARG, "create: bad arguments");
+    oracle_ctx* c = new oracle_ctx();
+    c->ngrid = d->ngrid;
+    c->prm = *prm;
+    c->g.resize(d->ngrid + 1);
+    int64_t o3 = 0, ox = 1, oy = 1, oz = 1;
+    c->minlevel = 1 << 30;
+    c->maxlevel = -1;
+    for (int g = 1; g <= d->ngrid; ++g) {
+        Grid& G = c->g[g];
+        G.kk = d->mgdims[3 * (g - 1) + 0];
+        G.jj = d->mgdims[3 * (g - 1) + 1];
+        G.ii = d->mgdims[3 * (g - 1) + 2];
+        G.level = d->level[g - 1];
+        for (int f = 1; f <= 6; ++f) G.bc[f] = d->bctype[6 * (g - 1) + f - 1];
+        for (int f = 1; f <= 26; ++f) G.nbr[f] = d->nbrgrid[26 * (g - 1) + f - 1];
+        G.gradpflag = d->gradpflag ? d->gradpflag[g - 1] : 1;
+        G.ip3 = o3; G.ipx = ox; G.ipy = oy; G.ipz = oz;
+        o3 += (int64_t)G.kk * G.jj * G.ii;
+        ox += G.ii; oy += G.jj; oz += G.kk;
+        c->minlevel = std::min(c->minlevel, G.level);
+        c->maxlevel = std::max(c->maxlevel, G.level);
+    }
+    if (c->minlevel != c->maxlevel) {
+        delete c;
+        return fail(MGLET_ERR_UNSUPPORTED, "oracle: only one grid level is restated");
+    }
+    if (!check_supported(*c)) {
+        delete c;
+        return fail(MGLET_ERR_UNSUPPORTED, "oracle: only CON/CO1 faces are restated");
+    }
+    c->idim3d = o3; c->idimx = ox - 1; c->idimy = oy - 1; c->idimz = oz - 1;
+    for (const char* n : {"U", "V", "W", "P", "G", "DU", "DV", "DW", "BP", "SDIV", "UO", "VO",
+                          "WO", "DP", "HILF", "RHS", "RES", "GSAP"})
+        c->f3[n].assign(o3, 0.0);
+    std::fill(c->f3["G"].begin(), c->f3["G"].end(), prm->gmol);   // lesmodel_mod.F90:70
+    std::fill(c->f3["BP"].begin(), c->f3["BP"].end(), 1.0);       // noib_mod.F90:45-47
+    auto set1 = [&](const char* n, const double* src, int64_t len) {
+        c->f1[n].assign(src, src + len);
+    };
+    set1("X", d->x, c->idimx); set1("Y", d->y, c->idimy); set1("Z", d->z, c->idimz);
+    set1("DX", d->dx, c->idimx); set1("DY", d->dy, c->idimy); set1("DZ", d->dz, c->idimz);
+    set1("DDX", d->ddx, c->idimx); set1("DDY", d->ddy, c->idimy); set1("DDZ", d->ddz, c->idimz);
+    // corefields_mod.F90:139-173 calc_reciprocal with divide0
+    auto recip = [&](const char* r, const char* s) {
+        const std::vector<double>& a = c->f1[s];
+        std::vector<double>& b = c->f1[r];
+        b.resize(a.size());
+        for (size_t q = 0; q < a.size(); ++q) b[q] = a[q] == 0.0 ? 0.0 : 1.0 / a[q];
+    };
+    recip("RDDX", "DDX"); recip("RDDY", "DDY"); recip("RDDZ", "DDZ");
+    recip("RDX", "DX"); recip("RDY", "DY"); recip("RDZ", "DZ");
+    for (const char* n : {"GSAW", "GSAE"}) c->f1[n].assign(c->idimx, 0.0);
+    for (const char* n : {"GSAS", "GSAN"}) c->f1[n].assign(c->idimy, 0.0);
+    for (const char* n : {"GSAB", "GSAT"}) c->f1[n].assign(c->idimz, 0.0);
+    init_connect_core(*c);
+    giteig(*c);
+    int rc = init_pressuresolver(*c);
+    if (rc) {
+        delete c;
+        return rc;
+    }
+    *out = c;
+    return 0;
+}
+
+int oracle_destroy(oracle_ctx* c) {
+    delete c;
+    return 0;
+}
+
+int64_t oracle_idim3d(const oracle_ctx* c) { return c->idim3d; }
+
+int oracle_set_field(oracle_ctx* c, const char* name, const double* host, int64_t n) {
+    auto it = c->f3.find(name);
+    if (it == c->f3.end()) return fail(MGLET_ERR_NAME, std::string("unknown field ") + name);
+    if (n != c->idim3d) return fail(MGLET_ERR_SIZE, "size mismatch");
+    std::copy(host, host + n, it->second.begin());
+    return 0;
+}
+
+int oracle_get_field(oracle_ctx* c, const char* name, double* host, int64_t n) {
+    auto it = c->f3.find(name);
+    if (it == c->f3.end()) {
+        auto i1 = c->f1.find(name);
+        if (i1 == c->f1.end()) return fail(MGLET_ERR_NAME, std::string("unknown field ") + name);
+        if (n != (int64_t)i1->second.size()) return fail(MGLET_ERR_SIZE, "size mismatch");
+        std::copy(i1->second.begin(), i1->second.end(), host);
+        return 0;
+    }
+    if (n != c->idim3d) return fail(MGLET_ERR_SIZE, "size mismatch");
+    std::copy(it->second.begin(), it->second.end(), host);
+    return 0;
+}
+
+// SIP_MIP_HP / SIP_IDX_HP (1-based values as the reference stores them)
+int oracle_get_sip_index(oracle_ctx* c, int64_t* mip, int64_t* idx, int64_t n) {
+    if (n != c->idim3d) return fail(MGLET_ERR_SIZE, "size mismatch");
+    std::copy(c->mip.begin(), c->mip.end(), mip);
+    std::copy(c->idxsip.begin(), c->idxsip.end(), idx);
+    return 0;
+}
+
+// Number of connections (rows of sendconns) and their content.
+int oracle_get_conns(oracle_ctx* c, int32_t* rows, int64_t maxrows, int64_t* nrows) {
+    *nrows = (int64_t)c->conns.size();
+    for (int64_t q = 0; q < *nrows && q < maxrows; ++q) {
+        rows[4 * q + 0] = c->conns[q].recvgrid;
+        rows[4 * q + 1] = c->conns[q].sendgrid;
+        rows[4 * q + 2] = c->conns[q].recvface;
+        rows[4 * q + 3] = c->conns[q].sendface;
+    }
+    return 0;
+}
+
+int oracle_tstle4(oracle_ctx* c) {
+    tstle4(*c);
+    return 0;
+}
+
+int oracle_rkstep(oracle_ctx* c, const char* p, const char* dp, const char* rhsp, double frhs,
+                  double dtfu) {
+    if (!c->f3.count(p) || !c->f3.count(dp) || !c->f3.count(rhsp))
+        return fail(MGLET_ERR_NAME, "rkstep: unknown field");
+    rkstep(c->F(p), c->F(dp), c->F(rhsp), c->idim3d, frhs, dtfu);
+    return 0;
+}
+
+// Returns the number of copied points in *ncopied (the message-length check
+// of connect2_mod.F90:879-885 is applied per connection).
+int oracle_connect(oracle_ctx* c, int ilevel, int layers, const char* v1, const char* v2,
+                   const char* v3, const char* s1, const char* s2, const char* s3, int corners,
+                   int normal, int forward, int64_t* ncopied) {
+    auto get = [&](const char* n) -> double* { return n ? c->F(n) : nullptr; };
+    if (layers < 1 || layers > 2) return fail(MGLET_ERR_ARG, "connect: layers must be 1 or 2");
+    if ((forward != 0 || normal) && corners) return fail(MGLET_ERR_ARG, "connect: bad flags");
+    int64_t n;
+    try {
+        n = connect(*c, ilevel, layers, get(v1), get(v2), get(v3), get(s1), get(s2), get(s3),
+                    corners != 0, normal != 0, forward);
+    } catch (...) {
+        return fail(MGLET_ERR_NAME, "connect: unknown field");
+    }
+    if (n < 0) return MGLET_ERR_ARG;
+    if (ncopied) *ncopied = n;
+    return 0;
+}
+
+int oracle_divcal(oracle_ctx* c, const char* div, double fak) {
+    divcal(*c, c->F(div), c->F("U"), c->F("V"), c->F("W"), fak);
+    return 0;
+}
+
+int oracle_laplacephi(oracle_ctx* c, const char* res, const char* phi) {
+    laplacephi_level(*c, 0, c->F(res), c->F(phi));
+    return 0;
+}
+
+int oracle_mgpoisl(oracle_ctx* c, double dt, int ittot, int irk, mglet_stage_stats* st) {
+    (void)ittot; (void)irk;
+    mgpoisl(*c, dt, st);
+    return 0;
+}
+
+// timeintegration_mod.F90:22-142 (noib, no LES, no Boussinesq/Coriolis)
+int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timeph, double dt,
+                              int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st) {
+    (void)itstep; (void)timeph;
+    double frhs, fu, dtrk, dtrki;
+    int rc = oracle_rk_get_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki);
+    if (rc) return rc;
+    tstle4(*c);
+    rkstep(c->F("U"), c->F("DU"), c->F("UO"), c->idim3d, frhs, dt * fu);
+    rkstep(c->F("V"), c->F("DV"), c->F("VO"), c->idim3d, frhs, dt * fu);
+    rkstep(c->F("W"), c->F("DW"), c->F("WO"), c->idim3d, frhs, dt * fu);
+    for (int l = c->minlevel; l <= c->maxlevel; ++l)
+        connect(*c, l, 1, c->F("U"), c->F("V"), c->F("W"), nullptr, nullptr, nullptr, false, true, 1);
+    mgpoisl(*c, dtrk * dt, st);
+    (void)ittot;
+    return 0;
+}
+
+int oracle_itinfo(oracle_ctx* c, double dt, mglet_itinfo* out) {
+    itinfo(*c, dt, out);
+    return 0;
+}
+
+}  // extern "C"
