@@ -299,6 +299,19 @@ int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, 
     return launch_connect(c, it->second, f);
 }
 
+int get_plan(Ctx* c, int ilevel, int layers, int slots, bool corners, bool normal, int fwd,
+             const ConnectPlan** out) {
+    const std::string key = plan_key(ilevel, layers, slots, corners, normal, fwd);
+    auto it = c->plans.find(key);
+    if (it == c->plans.end()) {
+        ConnectPlan p;
+        if (int rc = build_plan(c, ilevel, layers, slots, corners, normal, fwd, p)) return rc;
+        it = c->plans.emplace(key, p).first;
+    }
+    *out = &it->second;
+    return 0;
+}
+
 long long connect_points(Ctx* c, int ilevel, int layers, int slots, bool corners, bool normal,
                          int fwd) {
     const std::string key = plan_key(ilevel, layers, slots, corners, normal, fwd);
@@ -676,6 +689,7 @@ int mglet_gpu_get_field(mglet_ctx* c, const char* name, double* host, int64_t n)
     }
     if (n != len) return fail(MGLET_ERR_SIZE, "get_field: element count mismatch");
     cudaSetDevice(c->device);
+    if (c->prm.form == MGLET_FORM_MIXED) mixed_field_sync_out(c, name);
     MG_CUDA(cudaMemcpyAsync(host, p, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     MG_CUDA(cudaStreamSynchronize(c->stream));
     return 0;

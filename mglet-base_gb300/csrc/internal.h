@@ -66,7 +66,10 @@ struct ProfEntry {
     long long launches = 0;
 };
 
+struct MixedState;   // mixed.cu
+
 struct Ctx {
+    MixedState* mx = nullptr;
     int device = 0;
     cudaStream_t stream = nullptr;
     int ngrid = 0;
@@ -154,5 +157,10 @@ int launch_mgpcorr(Ctx* c, double* u, double* v, double* w, double* p, const dou
                    double rfak);
 int launch_itinfo(Ctx* c, double dt);
 int launch_connect(Ctx* c, const ConnectPlan& plan, double* const fields[6]);
+// FP32 copy of the same task list; returns early when *skip != 0 (device
+// flag of the mixed form's converged outer loop), skip may be null.
+int launch_connect32(Ctx* c, const ConnectPlan& plan, float* const fields[6], const int* skip);
+int get_plan(Ctx* c, int ilevel, int layers, int slots, bool corners, bool normal, int fwd,
+             const ConnectPlan** out);
 
 }  // namespace mg

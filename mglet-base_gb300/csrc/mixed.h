@@ -8,6 +8,7 @@ namespace mg {
 int mixed_init(Ctx* c);
 void mixed_release(Ctx* c);
 void mixed_field_changed(Ctx* c, const char* name);
+void mixed_field_sync_out(Ctx* c, const char* name);
 int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st);
 int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st);
 

@@ -1,0 +1,331 @@
+// mixed_flux.cu -- momentum right-hand side and RK update of the mixed form.
+//
+// Same discretisation as tstle4 (src/flow/tstle4_mod.F90:139-529: skew-
+// symmetric convection with interpolated mass fluxes, viscous fluxes with
+// the harmonic face viscosity, pressure gradient) followed by rkstep
+// (src/core/rungekutta_mod.F90:315-333), fused into one pass per grid, with
+// the arithmetic reorganised for GB300:
+//
+//  * u, v, w, p stay FP64 in HBM.  Each value is split once, with integer
+//    operations only, into an FP32 pair (hi, lo) with x = hi + lo to about
+//    2^-48 relative.  Every stencil difference is then formed in FP32 as
+//    (hi_a - hi_b) + (lo_a - lo_b): the hi difference of neighbouring values
+//    is exact, so the differences carry ~FP32 relative accuracy *of the
+//    difference*, and the convective term is written around the centre value
+//    (c * div(mass flux) + 1/2 sum f * delta) so that nothing cancels in FP32.
+//    The FP64 units of this part issue ~2 instructions/clk/SM; this form
+//    needs only the 3 FP64 adds of the RK update per cell.
+//  * the 2N-storage register DU is kept in FP32 (it only ever carries
+//    dt * rhs); u = u + dtfu * du is the one FP64 operation per component.
+//  * the grid is swept plane by plane in i with 3-plane windows of (hi, lo)
+//    in shared memory; every thread owns one (k, j) column and keeps the raw
+//    FP64 value of its own points for the update, so u is updated exactly.
+//
+// Requires a uniform viscosity field (G = gmol, no LES model) and CON faces;
+// the diffusive harmonic means then collapse to one host-computed constant.
+#include <algorithm>
+
+#include "internal.h"
+
+namespace mg {
+namespace {
+
+// x (FP64, normal or zero, |x| < 2^127) -> (hi, lo) FP32 with
+// hi = x truncated to 24 significant bits, lo = rest (29 bits) rounded to 24.
+__device__ __forceinline__ float2 split64(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned int sign = (unsigned int)(b >> 32) & 0x80000000u;
+    const int e = (int)((b >> 52) & 0x7FF);
+    const unsigned long long m = b & 0x000FFFFFFFFFFFFFULL;
+    const int fe = e - 1023 + 127;
+    if (e == 0 || fe <= 0) return make_float2(__uint_as_float(sign), __uint_as_float(sign));
+    const float hi = __uint_as_float(sign | ((unsigned int)fe << 23) | (unsigned int)(m >> 29));
+    const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFu);            // 29 bits
+    const int le = fe - 52 + 23;                                           // exponent of rem's lsb (float bias)
+    float lo = 0.f;
+    if (rem != 0 && le > 0) {
+        const float scale = __uint_as_float((unsigned int)le << 23);      // 2^(fe-127-29)
+        lo = __uint2float_rn(rem) * scale;
+        lo = __uint_as_float(__float_as_uint(lo) | sign);
+    }
+    return make_float2(hi, lo);
+}
+
+__device__ __forceinline__ float dif(float2 a, float2 b) { return (a.x - b.x) + (a.y - b.y); }
+__device__ __forceinline__ float val(float2 a) { return a.x + a.y; }
+
+struct FluxArgs {
+    const DevGrid* grids;
+    const double *U0, *V0, *W0, *P0;   // read
+    double *U, *V, *W;                 // written (interior)
+    float *DU, *DV, *DW;               // FP32 RK registers
+    // FP32 spacing tables per axis, concatenated like the FP64 arrays:
+    // [0] d, [1] dd, [2] rd, [3] rdd, [4] d(i)/dd(i+1), [5] d(i-1)/dd(i)
+    const float *sx, *sy, *sz;
+    long long nx, ny, nz;     // stride between the 6 tables of an axis
+    float g, gh;                       // uniform face viscosities (ge=gw, gn.. harmonic sum)
+    float rrho;
+    float gpx, gpy, gpz;
+    double frhs, dtfu;
+};
+
+// One CTA per grid, one thread per interior (k, j), marching i.
+__global__ void __launch_bounds__(576, 1) k_mx_flux(FluxArgs a) {
+    extern __shared__ float2 sm[];
+    const DevGrid G = a.grids[blockIdx.x];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int pk = kk - 2, pj = jj - 2, plane = pk * pj;     // plane of k = 2..kk-1, j = 2..jj-1
+    float2* su = sm;                  // [3][plane]
+    float2* sv = su + 3 * plane;
+    float2* sw = sv + 3 * plane;
+    float2* sp = sw + 3 * plane;      // [2][plane]
+    const long long o = G.ip3;
+    const int kj = kk * jj;
+    const int nk = kk - 4, nj = jj - 4;
+    const int t = threadIdx.x;
+    const bool on = t < nk * nj;
+    const int k = on ? t % nk + 3 : 3, j = on ? t / nk + 3 : 3;
+    const int nring = plane - nk * nj;
+    // plane-local index of (k, j): (k-2) + (j-2)*pk
+    auto pl = [pk](int kq, int jq) { return (kq - 2) + (jq - 2) * pk; };
+    // ring point r (0..nring-1) -> (k, j) on the border of the 2..kk-1 x 2..jj-1 plane
+    auto ring = [&](int r, int& kq, int& jq) {
+        if (r < pk) { kq = 2 + r; jq = 2; return; }
+        r -= pk;
+        if (r < pk) { kq = 2 + r; jq = jj - 1; return; }
+        r -= pk;
+        jq = 3 + r / 2;
+        kq = (r & 1) ? kk - 1 : 2;
+    };
+    const double *U0 = a.U0 + o, *V0 = a.V0 + o, *W0 = a.W0 + o, *P0 = a.P0 + o;
+    // 1-based views of the FP32 spacing tables of this grid
+    const float* X = a.sx + G.ipx - 1;
+    const float* Y = a.sy + G.ipy - 1;
+    const float* Z = a.sz + G.ipz - 1;
+    const long long nx = a.nx, ny = a.ny, nz = a.nz;
+#define DX(i) X[(i)]
+#define DDX(i) X[nx + (i)]
+#define RDX(i) X[2 * nx + (i)]
+#define RDDX(i) X[3 * nx + (i)]
+#define RX1(i) X[4 * nx + (i)]
+#define RX0(i) X[5 * nx + (i)]
+    // j- and k-dependent factors are fixed per thread
+    const float dy_j = Y[j], ddy_j = Y[ny + j], rdy_j = Y[2 * ny + j], rdy_jm = Y[2 * ny + j - 1];
+    const float rddy_j = Y[3 * ny + j], rddy_jp = Y[3 * ny + j + 1];
+    const float ry1 = Y[4 * ny + j], ry0 = Y[5 * ny + j];
+    const float dz_k = Z[k], ddz_k = Z[nz + k], rdz_k = Z[2 * nz + k], rdz_km = Z[2 * nz + k - 1];
+    const float rddz_k = Z[3 * nz + k], rddz_kp = Z[3 * nz + k + 1];
+    const float rz1 = Z[4 * nz + k], rz0 = Z[5 * nz + k];
+
+    // own raw FP64 values of planes i (cur) and i+1, i+2 (pipeline)
+    double ucur = 0, vcur = 0, wcur = 0, unx = 0, vnx = 0, wnx = 0;
+
+    auto load_plane = [&](int i, int slot3, int slot2, bool with_p, double& uo_, double& vo_,
+                          double& wo_) {
+        // interior point of this thread
+        if (on) {
+            const long long c = (long long)(i - 1) * kj + (long long)(j - 1) * kk + (k - 1);
+            const double u = U0[c], v = V0[c], w = W0[c];
+            uo_ = u; vo_ = v; wo_ = w;
+            const int q = pl(k, j);
+            su[slot3 * plane + q] = split64(u);
+            sv[slot3 * plane + q] = split64(v);
+            sw[slot3 * plane + q] = split64(w);
+            if (with_p) sp[slot2 * plane + q] = split64(P0[c]);
+        }
+        for (int r = t; r < nring; r += blockDim.x) {
+            int kq, jq;
+            ring(r, kq, jq);
+            const long long c = (long long)(i - 1) * kj + (long long)(jq - 1) * kk + (kq - 1);
+            const int q = pl(kq, jq);
+            su[slot3 * plane + q] = split64(U0[c]);
+            sv[slot3 * plane + q] = split64(V0[c]);
+            sw[slot3 * plane + q] = split64(W0[c]);
+            if (with_p) sp[slot2 * plane + q] = split64(P0[c]);
+        }
+    };
+
+    double dummy0, dummy1, dummy2;
+    load_plane(2, 2 % 3, 0, false, dummy0, dummy1, dummy2);
+    load_plane(3, 3 % 3, 3 % 2, true, ucur, vcur, wcur);
+    load_plane(4, 4 % 3, 4 % 2, true, unx, vnx, wnx);
+    __syncthreads();
+
+    const float g = a.g, gh = a.gh;
+    const int q = pl(k, j);
+    for (int i = 3; i <= ii - 2; ++i) {
+        const int sm1 = (i - 1) % 3, s0 = i % 3, sp1 = (i + 1) % 3;
+        const int p0 = i % 2, p1 = (i + 1) % 2;
+        float uo = 0.f, vo = 0.f, wo = 0.f;
+        if (on) {
+            const float2* u_m = su + sm1 * plane;
+            const float2* u_0 = su + s0 * plane;
+            const float2* u_p = su + sp1 * plane;
+            const float2* v_m = sv + sm1 * plane;
+            const float2* v_0 = sv + s0 * plane;
+            const float2* v_p = sv + sp1 * plane;
+            const float2* w_m = sw + sm1 * plane;
+            const float2* w_0 = sw + s0 * plane;
+            const float2* w_p = sw + sp1 * plane;
+            const float2* p_0 = sp + p0 * plane;
+            const float2* p_p = sp + p1 * plane;
+            const int qs = q - pk, qn = q + pk, qb = q - 1, qt = q + 1;   // j-1, j+1, k-1, k+1
+            const float fdx_i = DX(i), fddx = DDX(i), rdx_i = RDX(i), rdx_im = RDX(i - 1);
+            const float rddx_i = RDDX(i), rddx_ip = RDDX(i + 1), rx1 = RX1(i), rx0 = RX0(i);
+            const float fdy_j = dy_j, fddy = ddy_j, fdz_k = dz_k, fddz = ddz_k;
+            // ---------------- U at (k, j, i+1/2)
+            {
+                const float2 c = u_0[q];
+                const float cf = val(c);
+                const float dE = dif(u_p[q], c), dW = dif(u_m[q], c);
+                const float dN = dif(u_0[qn], c), dS = dif(u_0[qs], c);
+                const float dT = dif(u_0[qt], c), dB = dif(u_0[qb], c);
+                const float ax = fddy * fddz, ay = fdx_i * fddz, az = fdx_i * fddy;
+                const float fe = ax * (cf + 0.5f * dE * rx1);
+                const float fw = ax * (val(u_m[q]) - 0.5f * dW * rx0);
+                const float fn = 0.5f * ay * (val(v_0[q]) + val(v_p[q]));
+                const float fs = 0.5f * ay * (val(v_0[qs]) + val(v_p[qs]));
+                const float ft = 0.5f * az * (val(w_0[q]) + val(w_p[q]));
+                const float fb = 0.5f * az * (val(w_0[qb]) + val(w_p[qb]));
+                const float divf = ax * (-dW + 0.5f * dE * rx1 + 0.5f * dW * rx0) +
+                                   0.5f * ay * (dif(v_0[q], v_0[qs]) + dif(v_p[q], v_p[qs])) +
+                                   0.5f * az * (dif(w_0[q], w_0[qb]) + dif(w_p[q], w_p[qb]));
+                const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
+                                                      ft * dT - fb * dB);
+                const float vol = rdx_i * rddy_j * rddz_k;
+                const float conv = -sig * vol;
+                const float qd = -g * ax * (rddx_ip * dE + rddx_i * dW) -
+                                 gh * ay * (rdy_j * dN + rdy_jm * dS) -
+                                 gh * az * (rdz_k * dT + rdz_km * dB);
+                const float fak = a.rrho * vol;
+                const float gp = (dif(p_p[q], p_0[q]) + a.gpx * fdx_i) * (a.rrho / fdx_i);
+                uo = conv - fak * qd - gp;
+            }
+            // ---------------- V at (k, j+1/2, i)
+            {
+                const float2 c = v_0[q];
+                const float cf = val(c);
+                const float dE = dif(v_p[q], c), dW = dif(v_m[q], c);
+                const float dN = dif(v_0[qn], c), dS = dif(v_0[qs], c);
+                const float dT = dif(v_0[qt], c), dB = dif(v_0[qb], c);
+                const float ax = fdy_j * fddz, ay = fddx * fddz, az = fddx * fdy_j;
+                const float fe = 0.5f * ax * (val(u_0[q]) + val(u_0[qn]));
+                const float fw = 0.5f * ax * (val(u_m[q]) + val(u_m[qn]));
+                const float fn = ay * (cf + 0.5f * dN * ry1);
+                const float fs = ay * (val(v_0[qs]) - 0.5f * dS * ry0);
+                const float ft = 0.5f * az * (val(w_0[q]) + val(w_0[qn]));
+                const float fb = 0.5f * az * (val(w_0[qb]) + val(w_0[qb + pk]));
+                const float divf = 0.5f * ax * (dif(u_0[q], u_m[q]) + dif(u_0[qn], u_m[qn])) +
+                                   ay * (-dS + 0.5f * dN * ry1 + 0.5f * dS * ry0) +
+                                   0.5f * az * (dif(w_0[q], w_0[qb]) + dif(w_0[qn], w_0[qb + pk]));
+                const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
+                                                      ft * dT - fb * dB);
+                const float vol = rddx_i * rdy_j * rddz_k;
+                const float conv = -sig * vol;
+                const float qd = -gh * ax * (rdx_i * dE + rdx_im * dW) -
+                                 g * ay * (rddy_jp * dN + rddy_j * dS) -
+                                 gh * az * (rdz_k * dT + rdz_km * dB);
+                const float fak = a.rrho * vol;
+                const float gp = (dif(p_0[qn], p_0[q]) + a.gpy * fdy_j) * (a.rrho / fdy_j);
+                vo = conv - fak * qd - gp;
+            }
+            // ---------------- W at (k+1/2, j, i)
+            {
+                const float2 c = w_0[q];
+                const float cf = val(c);
+                const float dE = dif(w_p[q], c), dW = dif(w_m[q], c);
+                const float dN = dif(w_0[qn], c), dS = dif(w_0[qs], c);
+                const float dT = dif(w_0[qt], c), dB = dif(w_0[qb], c);
+                const float ax = fddy * fdz_k, ay = fddx * fdz_k, az = fddx * fddy;
+                const float fe = 0.5f * ax * (val(u_0[q]) + val(u_0[qt]));
+                const float fw = 0.5f * ax * (val(u_m[q]) + val(u_m[qt]));
+                const float fn = 0.5f * ay * (val(v_0[q]) + val(v_0[qt]));
+                const float fs = 0.5f * ay * (val(v_0[qs]) + val(v_0[qs + 1]));
+                const float ft = az * (cf + 0.5f * dT * rz1);
+                const float fb = az * (val(w_0[qb]) - 0.5f * dB * rz0);
+                const float divf = 0.5f * ax * (dif(u_0[q], u_m[q]) + dif(u_0[qt], u_m[qt])) +
+                                   0.5f * ay * (dif(v_0[q], v_0[qs]) + dif(v_0[qt], v_0[qs + 1])) +
+                                   az * (-dB + 0.5f * dT * rz1 + 0.5f * dB * rz0);
+                const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
+                                                      ft * dT - fb * dB);
+                const float vol = rddx_i * rddy_j * rdz_k;
+                const float conv = -sig * vol;
+                const float qd = -gh * ax * (rdx_i * dE + rdx_im * dW) -
+                                 gh * ay * (rdy_j * dN + rdy_jm * dS) -
+                                 g * az * (rddz_kp * dT + rddz_k * dB);
+                const float fak = a.rrho * vol;
+                const float gp = (dif(p_0[qt], p_0[q]) + a.gpz * fdz_k) * (a.rrho / fdz_k);
+                wo = conv - fak * qd - gp;
+            }
+        }
+        // issue the global loads of plane i+2 before the RK update and the barrier
+        double unx2 = 0, vnx2 = 0, wnx2 = 0;
+        __syncthreads();   // every thread is done with slot (i-1)%3 and p slot i%2
+        if (i + 2 <= ii - 1) load_plane(i + 2, (i + 2) % 3, (i + 2) % 2, true, unx2, vnx2, wnx2);
+        if (on) {
+            const long long c = o + (long long)(i - 1) * kj + (long long)(j - 1) * kk + (k - 1);
+            const float du = (float)a.frhs * a.DU[c] + uo;
+            const float dv = (float)a.frhs * a.DV[c] + vo;
+            const float dw = (float)a.frhs * a.DW[c] + wo;
+            a.DU[c] = du; a.DV[c] = dv; a.DW[c] = dw;
+            const float fdt = (float)a.dtfu;
+            a.U[c] = ucur + (double)(fdt * du);
+            a.V[c] = vcur + (double)(fdt * dv);
+            a.W[c] = wcur + (double)(fdt * dw);
+        }
+        ucur = unx; vcur = vnx; wcur = wnx;
+        unx = unx2; vnx = vnx2; wnx = wnx2;
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+static size_t flux_smem(const DevGrid& G0) {
+    return (size_t)11 * (G0.kk - 2) * (G0.jj - 2) * sizeof(float2);
+}
+
+// Checks the launch limits of the flux kernel for this grid shape and opts
+// in to the dynamic shared memory it needs.
+int mx_flux_prepare(Ctx* c) {
+    const DevGrid& G0 = c->grids[0];
+    if ((G0.kk - 4) * (G0.jj - 4) > 576) {
+        set_error("mixed form: the flux kernel takes at most 576 (k, j) columns per grid");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    const size_t smem = flux_smem(G0);
+    if (smem > 200 * 1024) {
+        set_error("mixed form: grid planes too large for the flux kernel's shared memory");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    MG_CUDA(cudaFuncSetAttribute(k_mx_flux, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return 0;
+}
+
+int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
+                   const float* sz, double frhs, double dtfu) {
+    ProfScope ps_(c, "mx_flux");
+    const DevGrid& G0 = c->grids[0];
+    const size_t smem = flux_smem(G0);
+    const int threads = ((G0.kk - 4) * (G0.jj - 4) + 31) / 32 * 32;
+    FluxArgs a;
+    a.grids = c->d_grids;
+    a.U0 = c->F("U"); a.V0 = c->F("V"); a.W0 = c->F("W"); a.P0 = c->F("P");
+    a.U = c->F("U"); a.V = c->F("V"); a.W = c->F("W");
+    a.DU = du; a.DV = dv; a.DW = dw;
+    a.sx = sx; a.sy = sy; a.sz = sz;
+    a.nx = c->idimx; a.ny = c->idimy; a.nz = c->idimz;
+    const double gm = c->prm.gmol;
+    const double h0 = gm * gm / std::max(gm + gm, gm);
+    a.g = (float)gm;
+    a.gh = (float)(h0 + h0);
+    a.rrho = (float)(1.0 / c->prm.rho);
+    a.gpx = (float)c->prm.gradp[0]; a.gpy = (float)c->prm.gradp[1]; a.gpz = (float)c->prm.gradp[2];
+    a.frhs = frhs;
+    a.dtfu = dtfu;
+    k_mx_flux<<<c->ngrid, threads, smem, c->stream>>>(a);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+}  // namespace mg

@@ -34,6 +34,23 @@ __global__ void k_connect(const BoxCopy* __restrict__ tasks, FieldSlots fs) {
     }
 }
 
+struct FieldSlots32 {
+    float* f[6];
+};
+
+__global__ void k_connect32(const BoxCopy* __restrict__ tasks, FieldSlots32 fs,
+                            const int* __restrict__ skip) {
+    if (skip && *skip) return;
+    const BoxCopy t = tasks[blockIdx.x];
+    float* a = fs.f[t.slot];
+    const int nkj = t.nk * t.nj;
+    for (int q = threadIdx.x; q < t.npts; q += blockDim.x) {
+        const int k = q % t.nk, j = (q / t.nk) % t.nj, i = q / nkj;
+        a[t.dst + (long long)i * t.djj + (long long)j * t.dkk + k] =
+            a[t.src + (long long)i * t.sjj + (long long)j * t.skk + k];
+    }
+}
+
 // Per-grid partial diagnostics: red[4g+0] = cflmax*0.25*dt, [4g+1] = divmax,
 // [4g+2] = esum, [4g+3] = vsum.
 __global__ void __launch_bounds__(256) k_itinfo(const DevGrid* __restrict__ grids,
@@ -129,6 +146,16 @@ int launch_connect(Ctx* c, const ConnectPlan& plan, double* const fields[6]) {
     FieldSlots fs;
     for (int q = 0; q < 6; ++q) fs.f[q] = fields[q];
     k_connect<<<plan.ntasks, 128, 0, c->stream>>>(plan.d_tasks, fs);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int launch_connect32(Ctx* c, const ConnectPlan& plan, float* const fields[6], const int* skip) {
+    ProfScope ps_(c, "connect32");
+    if (plan.ntasks == 0) return 0;
+    FieldSlots32 fs;
+    for (int q = 0; q < 6; ++q) fs.f[q] = fields[q];
+    k_connect32<<<plan.ntasks, 128, 0, c->stream>>>(plan.d_tasks, fs, skip);
     MG_LAUNCHED(c);
     return 0;
 }

@@ -1,0 +1,173 @@
+! mglet_gpu_mod.F90 -- ISO_C_BINDING interface to libmglet_gpu.so
+! (include/mglet_gpu.h) for the reference's Fortran callers.
+!
+! The module keeps the call shapes of the reference's hot-path modules so
+! that timeloop_mod (src/timeloop_mod.F90:229-317) can call
+!     CALL gpu_timeintegrate_flow(itstep, ittot, timeph, dt, irk, rkscheme)
+! in place of timeintegrate_flow (src/flow/timeintegration_mod.F90:22).
+! Field arrays are passed as the flat field_t%arr (src/core/field_t), so a
+! host<->device copy is one memcpy of idim3d reals (REAL64 build).
+! Every nonzero status goes to errr(__FILE__, __LINE__), as for the other C
+! helpers of the reference (src/core/err_mod.F90:57-100).
+MODULE mglet_gpu_mod
+    USE, INTRINSIC :: ISO_C_BINDING
+    USE err_mod, ONLY: errr
+    IMPLICIT NONE(type, external)
+    PRIVATE
+
+    TYPE, BIND(C) :: mglet_grid_desc
+        INTEGER(c_int32_t) :: ngrid
+        TYPE(c_ptr) :: mgdims, level, bctype, nbrgrid, gradpflag
+        TYPE(c_ptr) :: x, y, z, dx, dy, dz, ddx, ddy, ddz
+    END TYPE mglet_grid_desc
+
+    TYPE, BIND(C) :: mglet_flow_params
+        REAL(c_double) :: gmol, rho, gradp(3)
+        INTEGER(c_int32_t) :: psolver, ninner, nouter, nouter_min
+        REAL(c_double) :: epcorr, omega
+        INTEGER(c_int32_t) :: form, reserved
+    END TYPE mglet_flow_params
+
+    TYPE, BIND(C) :: mglet_rk_scheme
+        INTEGER(c_int32_t) :: nrk, reserved
+        REAL(c_double) :: cflmax, a(6), b(6), c(6)
+    END TYPE mglet_rk_scheme
+
+    TYPE, BIND(C) :: mglet_stage_stats
+        INTEGER(c_int32_t) :: ipc, nouter_done
+        REAL(c_double) :: maxrhs, prefak
+    END TYPE mglet_stage_stats
+
+    TYPE, BIND(C) :: mglet_itinfo
+        REAL(c_double) :: cflmax, divmax, energy
+        INTEGER(c_int32_t) :: exploded, reserved
+    END TYPE mglet_itinfo
+
+    INTERFACE
+        INTEGER(c_int) FUNCTION mglet_rk_init(name, rk) BIND(C, name="mglet_rk_init")
+            IMPORT :: c_int, c_char, mglet_rk_scheme
+            CHARACTER(kind=c_char), INTENT(in) :: name(*)
+            TYPE(mglet_rk_scheme), INTENT(out) :: rk
+        END FUNCTION mglet_rk_init
+
+        INTEGER(c_int) FUNCTION mglet_gpu_create(desc, prm, device, ctx) &
+                BIND(C, name="mglet_gpu_create")
+            IMPORT :: c_int, c_int32_t, c_ptr, mglet_grid_desc, mglet_flow_params
+            TYPE(mglet_grid_desc), INTENT(in) :: desc
+            TYPE(mglet_flow_params), INTENT(in) :: prm
+            INTEGER(c_int32_t), VALUE :: device
+            TYPE(c_ptr), INTENT(out) :: ctx
+        END FUNCTION mglet_gpu_create
+
+        INTEGER(c_int) FUNCTION mglet_gpu_destroy(ctx) BIND(C, name="mglet_gpu_destroy")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+        END FUNCTION mglet_gpu_destroy
+
+        INTEGER(c_int) FUNCTION mglet_gpu_set_field(ctx, name, host, n) &
+                BIND(C, name="mglet_gpu_set_field")
+            IMPORT :: c_int, c_ptr, c_char, c_double, c_int64_t
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(in) :: name(*)
+            REAL(c_double), INTENT(in) :: host(*)
+            INTEGER(c_int64_t), VALUE :: n
+        END FUNCTION mglet_gpu_set_field
+
+        INTEGER(c_int) FUNCTION mglet_gpu_get_field(ctx, name, host, n) &
+                BIND(C, name="mglet_gpu_get_field")
+            IMPORT :: c_int, c_ptr, c_char, c_double, c_int64_t
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(in) :: name(*)
+            REAL(c_double), INTENT(inout) :: host(*)
+            INTEGER(c_int64_t), VALUE :: n
+        END FUNCTION mglet_gpu_get_field
+
+        INTEGER(c_int) FUNCTION mglet_gpu_timeintegrate_flow(ctx, itstep, ittot, timeph, dt, &
+                irk, rk, stats) BIND(C, name="mglet_gpu_timeintegrate_flow")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double, mglet_rk_scheme, mglet_stage_stats
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: itstep, ittot, irk
+            REAL(c_double), VALUE :: timeph, dt
+            TYPE(mglet_rk_scheme), INTENT(in) :: rk
+            TYPE(mglet_stage_stats), INTENT(out) :: stats
+        END FUNCTION mglet_gpu_timeintegrate_flow
+
+        INTEGER(c_int) FUNCTION mglet_gpu_connect(ctx, ilevel, layers, v1, v2, v3, s1, s2, s3, &
+                corners, normal, forward) BIND(C, name="mglet_gpu_connect")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: ilevel, layers, corners, normal, forward
+            TYPE(c_ptr), VALUE :: v1, v2, v3, s1, s2, s3    ! C strings or C_NULL_PTR
+        END FUNCTION mglet_gpu_connect
+
+        INTEGER(c_int) FUNCTION mglet_gpu_itinfo(ctx, dt, out) BIND(C, name="mglet_gpu_itinfo")
+            IMPORT :: c_int, c_ptr, c_double, mglet_itinfo
+            TYPE(c_ptr), VALUE :: ctx
+            REAL(c_double), VALUE :: dt
+            TYPE(mglet_itinfo), INTENT(out) :: out
+        END FUNCTION mglet_gpu_itinfo
+    END INTERFACE
+
+    TYPE(c_ptr), SAVE :: gctx = C_NULL_PTR
+    TYPE(mglet_rk_scheme), SAVE :: grk
+
+    PUBLIC :: mglet_grid_desc, mglet_flow_params, mglet_rk_scheme, mglet_stage_stats, &
+        mglet_itinfo, gpu_init, gpu_finish, gpu_upload, gpu_download, &
+        gpu_timeintegrate_flow, gpu_itinfo
+
+CONTAINS
+    ! Called once after init_flow: builds the device state from the same
+    ! tables grids.h5 provides (one rank, one level, noib).
+    SUBROUTINE gpu_init(desc, prm, rkname)
+        TYPE(mglet_grid_desc), INTENT(in) :: desc
+        TYPE(mglet_flow_params), INTENT(in) :: prm
+        CHARACTER(len=*), INTENT(in) :: rkname
+        IF (mglet_gpu_create(desc, prm, 0_c_int32_t, gctx) /= 0) CALL errr(__FILE__, __LINE__)
+        IF (mglet_rk_init(TRIM(rkname)//C_NULL_CHAR, grk) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_init
+
+    SUBROUTINE gpu_finish()
+        IF (mglet_gpu_destroy(gctx) /= 0) CALL errr(__FILE__, __LINE__)
+        gctx = C_NULL_PTR
+    END SUBROUTINE gpu_finish
+
+    ! map_arr_to_device equivalent for one field_t%arr
+    SUBROUTINE gpu_upload(name, arr)
+        CHARACTER(len=*), INTENT(in) :: name
+        REAL(c_double), INTENT(in) :: arr(:)
+        IF (mglet_gpu_set_field(gctx, TRIM(name)//C_NULL_CHAR, arr, &
+            INT(SIZE(arr), c_int64_t)) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_upload
+
+    SUBROUTINE gpu_download(name, arr)
+        CHARACTER(len=*), INTENT(in) :: name
+        REAL(c_double), INTENT(inout) :: arr(:)
+        IF (mglet_gpu_get_field(gctx, TRIM(name)//C_NULL_CHAR, arr, &
+            INT(SIZE(arr), c_int64_t)) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_download
+
+    ! Drop-in for timeintegrate_flow (src/flow/timeintegration_mod.F90:22)
+    SUBROUTINE gpu_timeintegrate_flow(itstep, ittot, timeph, dt, irk, ipc)
+        INTEGER, INTENT(in) :: itstep, ittot, irk
+        REAL(c_double), INTENT(in) :: timeph, dt
+        INTEGER, INTENT(out) :: ipc
+        TYPE(mglet_stage_stats) :: st
+        IF (mglet_gpu_timeintegrate_flow(gctx, INT(itstep, c_int32_t), INT(ittot, c_int32_t), &
+            timeph, dt, INT(irk, c_int32_t), grk, st) /= 0) CALL errr(__FILE__, __LINE__)
+        ipc = st%ipc
+    END SUBROUTINE gpu_timeintegrate_flow
+
+    SUBROUTINE gpu_itinfo(dt, cflmax, divmax, energy, exploded)
+        REAL(c_double), INTENT(in) :: dt
+        REAL(c_double), INTENT(out) :: cflmax, divmax, energy
+        INTEGER, INTENT(inout) :: exploded
+        TYPE(mglet_itinfo) :: info
+        INTEGER(c_int) :: rc
+        rc = mglet_gpu_itinfo(gctx, dt, info)
+        IF (rc /= 0 .AND. rc /= 6) CALL errr(__FILE__, __LINE__)
+        cflmax = info%cflmax
+        divmax = info%divmax
+        energy = info%energy
+        IF (info%exploded /= 0) exploded = 1
+    END SUBROUTINE gpu_itinfo
+END MODULE mglet_gpu_mod

@@ -19,7 +19,8 @@ LIB = os.path.join(OUT, "libmglet_gpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 BASE = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
-SOURCES = ["api.cu", "plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "mixed.cu"]
+SOURCES = ["api.cu", "plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "mixed.cu",
+           "mixed_flux.cu"]
 
 
 def nvcc():

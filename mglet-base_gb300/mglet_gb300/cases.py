@@ -242,3 +242,32 @@ def divergence_free_modes(case, nmodes=24, kpeak=4.0, urms=1.0, seed=1234):
                    + np.mean(case.interior(w) ** 2)) / 3.0)
     s = urms / rms
     return u * s, v * s, w * s
+
+
+def stretch(case, seed=11, amount=0.3):
+    """Replace the uniform spacing of a case by a smooth random stretching
+    (per grid and axis): cell widths ddx vary by +-amount, cell centres x
+    follow from them and dx(i) = x(i+1) - x(i), as a grid generator writes
+    them.  Used to exercise non-uniform coefficients; the geometry is no
+    longer periodic, which the parity tests do not need."""
+    rng = np.random.default_rng(seed)
+
+    def axis(n, ngrid):
+        X, D, DD = [], [], []
+        for _ in range(ngrid):
+            w = 1.0 + amount * np.sin(np.linspace(0, 3, n) + rng.uniform(0, 6)) * rng.uniform(0.5, 1)
+            w = w * (2 * np.pi / 24)
+            edges = np.concatenate([[0.0], np.cumsum(w)])
+            x = 0.5 * (edges[:-1] + edges[1:])
+            dx = np.empty(n)
+            dx[:-1] = x[1:] - x[:-1]
+            dx[-1] = w[-1]
+            X.append(x)
+            D.append(dx)
+            DD.append(w)
+        return np.concatenate(X), np.concatenate(D), np.concatenate(DD)
+
+    case.x, case.dx, case.ddx = axis(case.ii, case.ngrid)
+    case.y, case.dy, case.ddy = axis(case.jj, case.ngrid)
+    case.z, case.dz, case.ddz = axis(case.kk, case.ngrid)
+    return case

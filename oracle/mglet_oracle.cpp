@@ -62,7 +62,7 @@ struct Grid {
     int nbr[27];      // 1..26
     int gradpflag;
     int64_t ip3;      // 0-based element offset of the 3-D slab
-    int64_t ipx, ipy, ipz;
+    int64_t ipx, ipy, ipz;   // 0-based; view pointers use base + ipx - 1 for 1-based i
 };
 
 struct Conn {         // one row of sendconns (single rank: send == recv)
@@ -1278,7 +1278,7 @@ int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle
     c->ngrid = d->ngrid;
     c->prm = *prm;
     c->g.resize(d->ngrid + 1);
-    int64_t o3 = 0, ox = 1, oy = 1, oz = 1;
+    int64_t o3 = 0, ox = 0, oy = 0, oz = 0;   // ipx/ipy/ipz 0-based
     c->minlevel = 1 << 30;
     c->maxlevel = -1;
     for (int g = 1; g <= d->ngrid; ++g) {
@@ -1304,7 +1304,7 @@ int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle
         delete c;
         return fail(MGLET_ERR_UNSUPPORTED, "oracle: only CON/CO1 faces are restated");
     }
-    c->idim3d = o3; c->idimx = ox - 1; c->idimy = oy - 1; c->idimz = oz - 1;
+    c->idim3d = o3; c->idimx = ox; c->idimy = oy; c->idimz = oz;
     for (const char* n : {"U", "V", "W", "P", "G", "DU", "DV", "DW", "BP", "SDIV", "UO", "VO",
                           "WO", "DP", "HILF", "RHS", "RES", "GSAP"})
         c->f3[n].assign(o3, 0.0);

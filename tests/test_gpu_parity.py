@@ -45,6 +45,7 @@ CASES = {
     "tiles8": lambda: cases.periodic_box(2, 2, 2, n=8),
     "tiles24": lambda: cases.periodic_box(3, 2, 2, n=24),
     "aniso": lambda: cases.periodic_box(2, 1, 3, n=10, nj=12, nk=6),
+    "stretched": lambda: cases.stretch(cases.periodic_box(2, 2, 1, n=10, nj=9, nk=8)),
 }
 
 
@@ -89,7 +90,7 @@ def test_connect(gpu_lib, oracle_lib, layers, corners, normal, forward):
         assert np.array_equal(g.get(nm), o.get(nm)), nm
 
 
-@pytest.mark.parametrize("name", ["tg32", "tiles8", "aniso"])
+@pytest.mark.parametrize("name", ["tg32", "tiles8", "aniso", "stretched"])
 def test_tstle4_rkstep(gpu_lib, oracle_lib, name):
     case = CASES[name]()
     g, o = _pair(gpu_lib, oracle_lib, case, _prm(gradp=(0.3, -0.2, 0.1)), noise=1e-2)
@@ -105,7 +106,7 @@ def test_tstle4_rkstep(gpu_lib, oracle_lib, name):
     assert np.array_equal(g.get("DU"), o.get("DU"))
 
 
-@pytest.mark.parametrize("name", ["tg32", "tiles8", "aniso"])
+@pytest.mark.parametrize("name", ["tg32", "tiles8", "aniso", "stretched"])
 def test_divcal_laplacephi(gpu_lib, oracle_lib, name):
     case = CASES[name]()
     g, o = _pair(gpu_lib, oracle_lib, case, _prm(), noise=1e-2)
@@ -132,7 +133,8 @@ def test_mgpoisl(gpu_lib, oracle_lib, name, psolver):
         assert rel_l2(a, b) <= RTOL, nm
 
 
-@pytest.mark.parametrize("name,steps", [("tg32", 3), ("tiles8", 3), ("tiles24", 2), ("aniso", 2)])
+@pytest.mark.parametrize("name,steps", [("tg32", 3), ("tiles8", 3), ("tiles24", 2), ("aniso", 2),
+                                        ("stretched", 2)])
 def test_stage_parity(gpu_lib, oracle_lib, name, steps):
     case = CASES[name]()
     prm = _prm(nouter_min=9)      # fixed iteration counts: parity independent of epcorr
@@ -153,7 +155,8 @@ def test_stage_parity(gpu_lib, oracle_lib, name, steps):
     ig, io = g.itinfo(dt), o.itinfo(dt)
     assert abs(ig.cflmax - io.cflmax) <= 1e-14 * io.cflmax
     assert abs(ig.divmax - io.divmax) <= 1e-12 * max(io.divmax, 1e-300)
-    assert abs(ig.energy - io.energy) <= 1e-13 * io.energy
+    # enerfg sums in parallel on the GPU (different summation order)
+    assert abs(ig.energy - io.energy) <= 1e-11 * io.energy
 
 
 def test_taylor_green_32_hundred_steps(gpu_lib, oracle_lib):

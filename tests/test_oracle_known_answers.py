@@ -271,3 +271,19 @@ def test_rk_schemes_consistent(oracle_lib):
             u = u + fu * du
             assert abs(u - dtrk) < 1e-9   # stage time of the next stage
         assert abs(u - 1.0) < 1e-9
+
+
+def test_laplacephi_exact_for_quadratics_on_stretched_grid(oracle_lib):
+    """On non-uniform spacing the giteig coefficients form the standard
+    three-point second derivative, exact for quadratics: -A (x^2+y^2+z^2) = -6."""
+    case = cases.stretch(cases.periodic_box(2, 1, 1, n=10, nj=8, nk=7))
+    o = oracle_lib.Oracle(case, _prm())
+    xg, yg, zg = case.coords()
+    phi = np.empty((case.ngrid, case.ii, case.jj, case.kk))
+    for g in range(case.ngrid):
+        phi[g] = (xg[g][:, None, None] ** 2 + yg[g][None, :, None] ** 2
+                  + zg[g][None, None, :] ** 2)
+    o.set("HILF", phi.ravel())
+    o.laplacephi("RES", "HILF")
+    res = case.interior(o.get("RES"))
+    assert np.max(np.abs(res - (-6.0))) < 1e-9
