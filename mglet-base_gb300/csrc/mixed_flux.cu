@@ -41,10 +41,11 @@ __device__ __forceinline__ float2 split64(double x) {
     if (e == 0 || fe <= 0) return make_float2(__uint_as_float(sign), __uint_as_float(sign));
     const float hi = __uint_as_float(sign | ((unsigned int)fe << 23) | (unsigned int)(m >> 29));
     const unsigned int rem = (unsigned int)(m & 0x1FFFFFFFu);            // 29 bits
-    const int le = fe - 52 + 23;                                           // exponent of rem's lsb (float bias)
+    // weight of rem's lsb: 2^(e-1023-52), i.e. biased float exponent fe-52
+    const int le = fe - 52;
     float lo = 0.f;
     if (rem != 0 && le > 0) {
-        const float scale = __uint_as_float((unsigned int)le << 23);      // 2^(fe-127-29)
+        const float scale = __uint_as_float((unsigned int)le << 23);
         lo = __uint2float_rn(rem) * scale;
         lo = __uint_as_float(__float_as_uint(lo) | sign);
     }
