@@ -206,6 +206,33 @@ int mglet_gpu_mgpoisl(mglet_ctx* ctx, double dt, int32_t ittot, int32_t irk,
  * check of itinfo_print (src/flow/itinfo_mod.F90:296-320). */
 int mglet_gpu_itinfo(mglet_ctx* ctx, double dt, mglet_itinfo* out);
 
+/* ---- Allocation-free diagnostic ---------------------------------------------
+ * No counterpart in the reference: an addition for callers that must not let
+ * this library allocate device memory -- builds whose fields already live on
+ * the GPU under another runtime (an OpenMP-offload build maps field_t%arr
+ * itself and passes device addresses via use_device_ptr), and per-step
+ * diagnostics inside the time loop, where cudaMalloc/cudaFree would
+ * synchronise the device.
+ *
+ * max |div u| over the interior of ngrid grids of identical dimensions
+ * (kk, jj, ii) in field_t layout, ib type noib -- the divmax of
+ * mglet_gpu_itinfo.  u, v, w, the concatenated rddx/rddy/rddz arrays
+ * (ngrid*ii, ngrid*jj, ngrid*kk values) and the one-double result divmax
+ * are DEVICE pointers; work is queued on stream (a cudaStream_t, NULL for
+ * the default stream) and the call returns without synchronising.
+ * It allocates nothing: its scratch, one double per grid, is a static
+ * __device__ array of MGLET_NOALLOC_MAX_GRIDS doubles (512 KiB) held by every
+ * GPU that loads the library.  ngrid > MGLET_NOALLOC_MAX_GRIDS returns
+ * MGLET_ERR_SIZE.  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress) with that device current; make that first
+ * call before any stream capture.  All calls share the one array, so calls
+ * that overlap on the GPU (different streams, no ordering) race. */
+#define MGLET_NOALLOC_MAX_GRIDS 65536
+int mglet_gpu_divmax_noalloc(const double* u, const double* v, const double* w, int32_t ngrid,
+                             int32_t kk, int32_t jj, int32_t ii, const double* rddx,
+                             const double* rddy, const double* rddz, double* divmax,
+                             void* stream);
+
 /* ---- Misc ----------------------------------------------------------------- */
 int mglet_gpu_synchronize(mglet_ctx* ctx);
 /* The cudaStream_t all of this context's work is issued on (for callers that

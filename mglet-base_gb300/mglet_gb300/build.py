@@ -20,7 +20,9 @@ LIB = os.path.join(OUT, "libmglet_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 BASE = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 SOURCES = ["api.cu", "plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "mixed.cu",
-           "mixed_flux.cu"]
+           "mixed_flux.cu", "noalloc.cu"]
+# translation units whose FP64 arithmetic must not be contracted into FMAs
+NO_FMA = {"plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "noalloc.cu"}
 
 
 def nvcc():
@@ -32,7 +34,7 @@ def nvcc():
 
 def _flags(src):
     f = list(BASE) + ARCH
-    if src.startswith("plain_"):
+    if src in NO_FMA:
         f.append("-fmad=false")
     return f
 

@@ -24,7 +24,7 @@ EXPORTS = [
     "mglet_gpu_divcal", "mglet_gpu_laplacephi", "mglet_gpu_mgpoisl", "mglet_gpu_itinfo",
     "mglet_gpu_synchronize", "mglet_gpu_kernel_launches", "mglet_gpu_last_error",
     "mglet_gpu_abi_version", "mglet_gpu_stream", "mglet_gpu_profile", "mglet_gpu_profile_get",
-    "mglet_gpu_profile_names",
+    "mglet_gpu_profile_names", "mglet_gpu_divmax_noalloc",
 ]
 
 
@@ -73,6 +73,8 @@ def load(path=None):
     L.mglet_gpu_profile.argtypes = [vp, C.c_int32]
     L.mglet_gpu_profile_get.argtypes = [vp, cp, C.POINTER(C.c_double), C.POINTER(C.c_int64)]
     L.mglet_gpu_profile_names.argtypes = [vp, cp, C.c_int64]
+    L.mglet_gpu_divmax_noalloc.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, C.c_int32,
+                                           C.c_int32, vp, vp, vp, vp, vp]
     _lib = L
     return L
 
