@@ -1,32 +1,24 @@
 // mixed.cu -- the batched mixed-precision form of the RK stage.
 //
-// Same algorithm and data flow as the reference's mgpoisl
-// (src/flow/pressuresolver_mod.F90:160-357): an FP64 defect-correction outer
+// Same algorithm and data flow as the reference's timeintegrate_flow +
+// mgpoisl (src/flow/timeintegration_mod.F90:22-142,
+// src/flow/pressuresolver_mod.F90:160-357): an FP64 defect-correction outer
 // loop (laplacephi + rescal + maxabscal + accumulate_pcorr) around ninner SIP
-// iterations per level (mgpoisit/sip, :361-465) with the lagged halo
-// exchanges conn(res) and conn(dp) between them.  What changes:
+// iterations with the lagged halo exchanges of the reference.  What changes:
 //
-//  * the inner iterations run in FP32: hilf, res and an FP32 copy of the
-//    outer residual rhs, and FP32 SIP/Poisson coefficients.  The FP64 outer
-//    loop measures the true residual of the accumulated correction, so the
-//    converged pressure is an FP64 solution (the reference's own loop
-//    structure, only the inner precision drops);
-//  * grids with identical spacing, boundary types and BP share one
-//    coefficient set ("coefficient class"); on a uniform periodic tiling all
-//    4096 grids read the same 0.7 MB of FP32 coefficients from L2 instead
-//    of 7 x 719 MB of FP64 fields from HBM;
-//  * the SIP sweeps use a column wavefront: one CTA per grid, one thread per
-//    (j, i) column.  At step t the thread works on k = t - (i-3) - (j-3) + 3,
-//    so all active threads lie on the hyperplane i+j+k = t+9 -- the
-//    reference's wavefront (sip_hyperplane_mod.F90:450-569).  res(k-1)
-//    stays in a register, res(j-1) and res(i-1) come from a double-buffered
-//    shared-memory plane written one step earlier;
+//  * momentum RHS and RK update: one fused FP32 kernel over FP64 velocity
+//    storage (mixed_flux.cu);
+//  * inner SIP iterations in FP32, hyperplane layout, halos pulled from
+//    per-grid face buffers (mixed_sip.cu); the FP64 outer loop measures the
+//    true residual of the accumulated correction, so the converged pressure
+//    is an FP64 solution;
+//  * grids with identical spacing and boundary types share one coefficient
+//    set ("coefficient class"); on a uniform periodic tiling all grids read
+//    the same ~0.4 MB of FP32 SIP factors, which stay in L2;
 //  * convergence is decided on the device: the outer-loop kernels check a
 //    device flag and return at once after convergence, so a whole stage is
-//    one CUDA graph with no host round trip (the reference's MPI_Allreduce
-//    + host test per outer iteration).
-//
-// Compiled with FMA contraction on (the parity form lives in plain_*.cu).
+//    one CUDA graph with no host round trip (the reference's
+//    MPI_Allreduce + host test per outer iteration).
 #include <algorithm>
 #include <array>
 #include <cstring>
@@ -34,6 +26,7 @@
 #include <vector>
 
 #include "mixed.h"
+#include "mixed_sip.h"
 
 namespace mg {
 
@@ -45,14 +38,13 @@ struct MixedState {
     int nclass = 0;
     std::vector<int> gcls;          // coefficient class of each grid
     int* d_gcls = nullptr;
-    long long cls_stride = 0;       // points per class slab (kk*jj*ii of the shape)
-    // FP32 class coefficients, natural layout per class slab
+    // FP32 class coefficients, plane order [nclass][npts]
     float *lw = nullptr, *ls = nullptr, *lb = nullptr, *lpr = nullptr;
     float *ue = nullptr, *un = nullptr, *ut = nullptr, *ap32 = nullptr;
     double* ap64 = nullptr;
-    // FP32 inner-solver fields (natural layout with ghosts, like field_t%arr)
-    float *h32 = nullptr, *r32 = nullptr, *rhs32 = nullptr;
-    // FP32 2N-storage registers DU, DV, DW of the RK scheme
+    SipState sip;
+    const int* d_idx = nullptr;     // plane position -> natural local index (hp table)
+    // FP32 2N-storage registers DU, DV, DW of the RK scheme (natural layout)
     float *du32 = nullptr, *dv32 = nullptr, *dw32 = nullptr;
     // FP32 spacing tables per axis: d, dd, rd, rdd, d(i)/dd(i+1), d(i-1)/dd(i)
     float *sx = nullptr, *sy = nullptr, *sz = nullptr;
@@ -60,9 +52,8 @@ struct MixedState {
     // device control block: [0] converged flag, [1] outer iterations done
     int* d_ctl = nullptr;
     double* d_maxrhs = nullptr;
-    int* h_ctl = nullptr;           // pinned mirror
+    int* h_ctl = nullptr;           // pinned mirrors
     double* h_maxrhs = nullptr;
-    int maxcols = 0;
     // graph cache: (irk, dt, frhs, fu, dtrk bit patterns) -> executable graph
     // of the whole stage, and the number of kernels inside it
     using GraphKey = std::array<unsigned long long, 5>;
@@ -72,14 +63,10 @@ struct MixedState {
 
 namespace {
 
-#define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
-
-// ---------------------------------------------------------------------------
-// Coefficient classes: copy the representative grid's FP64 SIP coefficients
-// (hyperplane order for "sip", natural order for "classic") to FP32 natural
-// layout, and its GSAP to the FP32/FP64 class slabs.
+// FP32 (and FP64 ap) class coefficients in plane order from the
+// representative grid of each class.
 __global__ void k_extract(const DevGrid* __restrict__ grids, const int* __restrict__ reps,
-                          const int* const* __restrict__ idxs, int planeorder, long long stride,
+                          const int* __restrict__ idx, int planeorder, int npts,
                           const double* __restrict__ lw, const double* __restrict__ ls,
                           const double* __restrict__ lb, const double* __restrict__ lpr,
                           const double* __restrict__ ue, const double* __restrict__ un,
@@ -88,143 +75,16 @@ __global__ void k_extract(const DevGrid* __restrict__ grids, const int* __restri
                           float* out, float* oap, double* oap64) {
     const int cls = blockIdx.y;
     const DevGrid G = grids[reps[cls]];
-    const int kk = G.kk, jj = G.jj, ii = G.ii;
-    const int npts = (kk - 4) * (jj - 4) * (ii - 4);
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= npts) return;
-    const int id = idxs[G.cls][q];                // natural local index of plane entry q
+    const int id = idx[q];
     const long long src = G.ip3 + (planeorder ? q : id);
-    const long long dst = cls * stride + id;
+    const long long dst = (long long)cls * npts + q;
     olw[dst] = (float)lw[src]; ols[dst] = (float)ls[src]; olb[dst] = (float)lb[src];
     olpr[dst] = (float)lpr[src]; oue[dst] = (float)ue[src]; oun[dst] = (float)un[src];
     out[dst] = (float)ut[src];
     oap[dst] = (float)ap[G.ip3 + id];
     oap64[dst] = ap[G.ip3 + id];
-}
-
-struct Coef1 {
-    const double *aw, *ae, *as, *an, *ab, *at;
-};
-
-// ---------------------------------------------------------------------------
-// mixed divcal: FP64 divergence (noib_mod.F90:304-354) into rhs, plus its
-// FP32 copy for the inner iterations.
-__global__ void k_mx_divcal(const DevGrid* __restrict__ grids, double* __restrict__ RHS,
-                            float* __restrict__ RHS32, const double* __restrict__ U,
-                            const double* __restrict__ V, const double* __restrict__ W,
-                            const double* __restrict__ RDDX, const double* __restrict__ RDDY,
-                            const double* __restrict__ RDDZ, double fak) {
-    const DevGrid G = grids[blockIdx.y];
-    const int kk = G.kk, jj = G.jj, ii = G.ii;
-    const int ni = ii - 4, nj = jj - 4, nk = kk - 4;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ni * nj * nk) return;
-    const int k = t % nk + 3, j = (t / nk) % nj + 3, i = t / (nk * nj) + 3;
-    const long long o = G.ip3;
-    const long long c = IX(k, j, i);
-    const double *u = U + o, *v = V + o, *w = W + o;
-    const double d = fak * ((u[c] - u[IX(k, j, i - 1)]) * RDDX[G.ipx + i - 1] +
-                            (v[c] - v[IX(k, j - 1, i)]) * RDDY[G.ipy + j - 1] +
-                            (w[c] - w[IX(k - 1, j, i)]) * RDDZ[G.ipz + k - 1]);
-    RHS[o + c] = d;
-    RHS32[o + c] = (float)d;
-}
-
-// ---------------------------------------------------------------------------
-// Forward sweep: res = -A hilf (laplacephi_grid, bp = 1) then
-// res = (rhs + res) lpr - lb res(k-1) - ls res(j-1) - lw res(i-1), on the
-// column wavefront.  Ghost values of hilf and res come from conn.
-template <int MAXC>
-__global__ void __launch_bounds__(1024) k_mx_fwd(const DevGrid* __restrict__ grids,
-                                                 const int* __restrict__ gcls, long long cstride,
-                                                 const float* __restrict__ H,
-                                                 const float* __restrict__ RHS, float* R,
-                                                 const float* __restrict__ LW, const float* __restrict__ LS,
-                                                 const float* __restrict__ LB, const float* __restrict__ LPR,
-                                                 const float* __restrict__ AP, Coef1 cf,
-                                                 const int* __restrict__ conv) {
-    if (*conv) return;
-    __shared__ float xb[2][MAXC];
-    const DevGrid G = grids[blockIdx.x];
-    const int kk = G.kk, jj = G.jj, ii = G.ii;
-    const int ni = ii - 4, nj = jj - 4, nk = kk - 4;
-    const int col = threadIdx.x;
-    const bool on = col < ni * nj;
-    const int jo = on ? col % nj : 0, io = on ? col / nj : 0;   // 0-based column
-    const int j = jo + 3, i = io + 3;
-    const long long o = G.ip3;
-    const long long co = (long long)gcls[blockIdx.x] * cstride;
-    const float *h = H + o, *rhs = RHS + o;
-    float* res = R + o;
-    const float *lw = LW + co, *ls = LS + co, *lb = LB + co, *lpr = LPR + co, *ap = AP + co;
-    const float aw = (float)cf.aw[G.ipx + i - 1], ae = (float)cf.ae[G.ipx + i - 1];
-    const float as = (float)cf.as[G.ipy + j - 1], an = (float)cf.an[G.ipy + j - 1];
-    const int kj = kk * jj;
-    float rprev = 0.f;
-    const int nsteps = ni + nj + nk - 2;
-    for (int t = 0; t < nsteps; ++t) {
-        const int kx = t - io - jo;
-        if (on && kx >= 0 && kx < nk) {
-            const int k = kx + 3;
-            const long long c = IX(k, j, i);
-            const float ab = (float)cf.ab[G.ipz + k - 1], at = (float)cf.at[G.ipz + k - 1];
-            float lap = -aw * h[c - kj] - ae * h[c + kj] - as * h[c - kk] - an * h[c + kk] -
-                        ab * h[c - 1] - at * h[c + 1] - ap[c] * h[c];
-            const float rkm = (k == 3) ? res[c - 1] : rprev;
-            const float rjm = (j == 3) ? res[c - kk] : xb[(t + 1) & 1][col - 1];
-            const float rim = (i == 3) ? res[c - kj] : xb[(t + 1) & 1][col - nj];
-            float r = (rhs[c] + lap) * lpr[c];
-            r = r - lb[c] * rkm - ls[c] * rjm - lw[c] * rim;
-            res[c] = r;
-            xb[t & 1][col] = r;
-            rprev = r;
-        }
-        __syncthreads();
-    }
-}
-
-// Backward sweep: res = res - ut res(k+1) - un res(j+1) - ue res(i+1) in
-// reverse wavefront order, then hilf += res.
-template <int MAXC>
-__global__ void __launch_bounds__(1024) k_mx_bwd(const DevGrid* __restrict__ grids,
-                                                 const int* __restrict__ gcls, long long cstride,
-                                                 float* H, const float* __restrict__ R,
-                                                 const float* __restrict__ UE, const float* __restrict__ UN,
-                                                 const float* __restrict__ UT,
-                                                 const int* __restrict__ conv) {
-    if (*conv) return;
-    __shared__ float xb[2][MAXC];
-    const DevGrid G = grids[blockIdx.x];
-    const int kk = G.kk, jj = G.jj, ii = G.ii;
-    const int ni = ii - 4, nj = jj - 4, nk = kk - 4;
-    const int col = threadIdx.x;
-    const bool on = col < ni * nj;
-    const int jo = on ? col % nj : 0, io = on ? col / nj : 0;
-    const int j = jo + 3, i = io + 3;
-    const int jr = nj - 1 - jo, ir = ni - 1 - io;   // distance from the high faces
-    const long long o = G.ip3;
-    const long long co = (long long)gcls[blockIdx.x] * cstride;
-    float* h = H + o;
-    const float* res = R + o;
-    const float *ue = UE + co, *un = UN + co, *ut = UT + co;
-    const int kj = kk * jj;
-    float rprev = 0.f;
-    const int nsteps = ni + nj + nk - 2;
-    for (int t = 0; t < nsteps; ++t) {
-        const int kr = t - ir - jr;
-        if (on && kr >= 0 && kr < nk) {
-            const int k = kk - 2 - kr;
-            const long long c = IX(k, j, i);
-            const float rkp = (k == kk - 2) ? res[c + 1] : rprev;
-            const float rjp = (j == jj - 2) ? res[c + kk] : xb[(t + 1) & 1][col + 1];
-            const float rip = (i == ii - 2) ? res[c + kj] : xb[(t + 1) & 1][col + nj];
-            float r = res[c] - ut[c] * rkp - un[c] * rjp - ue[c] * rip;
-            h[c] = h[c] + r;
-            xb[t & 1][col] = r;
-            rprev = r;
-        }
-        __syncthreads();
-    }
 }
 
 __device__ __forceinline__ double block_max_d(double v, double* sh) {
@@ -238,50 +98,6 @@ __device__ __forceinline__ double block_max_d(double v, double* sh) {
     }
     __syncthreads();
     return v;
-}
-
-// Outer step in FP64: res = -A hilf (laplacephi), rhs += res (rescal),
-// max|rhs| per grid (maxabscal_grid), dp += hilf (accumulate_pcorr),
-// rhs32 = rhs, hilf = 0.
-__global__ void __launch_bounds__(512) k_mx_outer(const DevGrid* __restrict__ grids,
-                                                  const int* __restrict__ gcls, long long cstride,
-                                                  float* H, double* __restrict__ RHS,
-                                                  float* __restrict__ RHS32, double* __restrict__ DP,
-                                                  const double* __restrict__ AP64, Coef1 cf,
-                                                  double* __restrict__ gridmax,
-                                                  const int* __restrict__ conv) {
-    if (*conv) return;
-    __shared__ double sh[32];
-    const DevGrid G = grids[blockIdx.x];
-    const int kk = G.kk, jj = G.jj, ii = G.ii;
-    const int ni = ii - 4, nj = jj - 4, nk = kk - 4;
-    const long long o = G.ip3;
-    const long long co = (long long)gcls[blockIdx.x] * cstride;
-    float* h = H + o;
-    const double* ap = AP64 + co;
-    const int kj = kk * jj;
-    double m = 0.0;
-    for (int t = threadIdx.x; t < ni * nj * nk; t += blockDim.x) {
-        const int k = t % nk + 3, j = (t / nk) % nj + 3, i = t / (nk * nj) + 3;
-        const long long c = IX(k, j, i);
-        const double hc = h[c];
-        const double lap = -cf.aw[G.ipx + i - 1] * (double)h[c - kj] -
-                           cf.ae[G.ipx + i - 1] * (double)h[c + kj] -
-                           cf.as[G.ipy + j - 1] * (double)h[c - kk] -
-                           cf.an[G.ipy + j - 1] * (double)h[c + kk] -
-                           cf.ab[G.ipz + k - 1] * (double)h[c - 1] -
-                           cf.at[G.ipz + k - 1] * (double)h[c + 1] - ap[c] * hc;
-        const double r = RHS[o + c] + lap;
-        RHS[o + c] = r;
-        RHS32[o + c] = (float)r;
-        DP[o + c] = DP[o + c] + hc;
-        m = fmax(fabs(r), m);
-    }
-    m = block_max_d(m, sh);
-    if (threadIdx.x == 0) gridmax[blockIdx.x] = m;
-    // all reads of this grid's hilf (interior and ghosts) are done
-    const int npt = kk * jj * ii;
-    for (int t = threadIdx.x; t < npt; t += blockDim.x) h[t] = 0.f;
 }
 
 // maxabscal over grids + the outer-loop stopping test of mgpoisl
@@ -302,6 +118,8 @@ __global__ void k_mx_conv(const DevGrid* __restrict__ grids, int ngrid, int maxl
         if (done >= nouter_min && m / prefak < epcorr) ctl[0] = 1;
     }
 }
+
+#define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
 
 // mgpcorr on the interior only (the ghost layers it also touches in the
 // reference are overwritten by the closing connect), FP64.
@@ -325,88 +143,61 @@ __global__ void k_mx_mgpcorr(const DevGrid* __restrict__ grids, double* U, doubl
     W[o + c] = W[o + c] + (d - dp[c + 1]) * RDZ[G.ipz + k - 1] * rfak;
 }
 
-int interior_max(const Ctx* c) {
-    int m = 0;
-    for (const DevGrid& g : c->grids) m = std::max(m, (g.kk - 4) * (g.jj - 4) * (g.ii - 4));
-    return m;
+__global__ void k_cvt_64_32(float* d, const double* s, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) d[t] = (float)s[t];
 }
 
-Coef1 coef1(Ctx* c) {
-    return Coef1{c->L("GSAW"), c->L("GSAE"), c->L("GSAS"), c->L("GSAN"), c->L("GSAB"), c->L("GSAT")};
+__global__ void k_cvt_32_64(double* d, const float* s, long long n) {
+    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < n) d[t] = (double)s[t];
 }
 
+SipCoef coefs(const MixedState* m) {
+    return SipCoef{m->lw, m->ls, m->lb, m->lpr, m->ue, m->un, m->ut, m->ap32};
+}
+
+// The reference's inner-iteration halo semantics mapped onto the rotating
+// res face buffers: iteration G (1-based within one mgpoisl) writes slot G%3;
+// its forward sweep reads low ghosts written by the last iteration whose
+// conn(res) exchanged all faces (inner index < ninner), or zeros.
 int enqueue_mgpoisl(Ctx* c, double dt) {
     MixedState* m = c->mx;
+    SipState& s = m->sip;
     const double prefak = c->prm.rho / dt;
-    double* U = c->F("U"); double* V = c->F("V"); double* W = c->F("W"); double* P = c->F("P");
-    double* dp = c->F("DP"); double* rhs = c->F("RHS");
-    const size_t b8 = (size_t)c->idim3d * sizeof(double), b4 = (size_t)c->idim3d * sizeof(float);
-    MG_CUDA(cudaMemsetAsync(dp, 0, b8, c->stream));
-    MG_CUDA(cudaMemsetAsync(rhs, 0, b8, c->stream));
-    MG_CUDA(cudaMemsetAsync(m->h32, 0, b4, c->stream));
-    MG_CUDA(cudaMemsetAsync(m->r32, 0, b4, c->stream));
+    double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P"), *dp = c->F("DP");
+    MG_CUDA(cudaMemsetAsync(s.dp64, 0, (size_t)c->ngrid * s.npts * sizeof(double), c->stream));
     MG_CUDA(cudaMemsetAsync(m->d_ctl, 0, 2 * sizeof(int), c->stream));
-    {
-        ProfScope ps_(c, "mx_divcal");
-        dim3 grid((interior_max(c) + 255) / 256, c->ngrid);
-        k_mx_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, rhs, m->rhs32, U, V, W, c->L("RDDX"),
-                                                 c->L("RDDY"), c->L("RDDZ"), prefak);
-        MG_LAUNCHED(c);
-    }
-    const ConnectPlan *p_all, *p_hi;
-    if (int rc = get_plan(c, 0, 1, 1 << 3, false, false, 0, &p_all)) return rc;
-    if (int rc = get_plan(c, 0, 1, 1 << 3, false, false, -1, &p_hi)) return rc;
-    float* slot_r[6] = {nullptr, nullptr, nullptr, m->r32, nullptr, nullptr};
-    float* slot_h[6] = {nullptr, nullptr, nullptr, m->h32, nullptr, nullptr};
+    if (int rc = sip_divcal(c, s, m->d_idx, prefak)) return rc;
     const int* conv = m->d_ctl;
-    const Coef1 cf = coef1(c);
-    const int threads = ((m->maxcols + 31) / 32) * 32;
+    const SipCoef cf = coefs(m);
+    const int ninner = c->prm.ninner;
+    int gi = 0, lastfull = 0;
     for (int ipcount = 1; ipcount <= c->prm.nouter; ++ipcount) {
-        for (int iloop = 1; iloop <= c->prm.ninner; ++iloop) {
-            {
-                ProfScope ps_(c, "mx_sip_fwd");
-                if (m->maxcols <= 576)
-                    k_mx_fwd<576><<<c->ngrid, threads, 0, c->stream>>>(
-                        c->d_grids, m->d_gcls, m->cls_stride, m->h32, m->rhs32, m->r32, m->lw, m->ls,
-                        m->lb, m->lpr, m->ap32, cf, conv);
-                else
-                    k_mx_fwd<1024><<<c->ngrid, threads, 0, c->stream>>>(
-                        c->d_grids, m->d_gcls, m->cls_stride, m->h32, m->rhs32, m->r32, m->lw, m->ls,
-                        m->lb, m->lpr, m->ap32, cf, conv);
-                MG_LAUNCHED(c);
-            }
-            if (int rc = launch_connect32(c, iloop < c->prm.ninner ? *p_all : *p_hi, slot_r, conv))
-                return rc;
-            {
-                ProfScope ps_(c, "mx_sip_bwd");
-                if (m->maxcols <= 576)
-                    k_mx_bwd<576><<<c->ngrid, threads, 0, c->stream>>>(
-                        c->d_grids, m->d_gcls, m->cls_stride, m->h32, m->r32, m->ue, m->un, m->ut, conv);
-                else
-                    k_mx_bwd<1024><<<c->ngrid, threads, 0, c->stream>>>(
-                        c->d_grids, m->d_gcls, m->cls_stride, m->h32, m->r32, m->ue, m->un, m->ut, conv);
-                MG_LAUNCHED(c);
-            }
-            if (int rc = launch_connect32(c, *p_all, slot_h, conv)) return rc;
+        for (int iloop = 1; iloop <= ninner; ++iloop) {
+            ++gi;
+            const bool hz = iloop == 1;
+            const int rlow = lastfull > 0 ? lastfull % 3 : -1;
+            if (int rc = sip_forward(c, s, cf, m->d_gcls, conv, rlow, gi % 3, hz)) return rc;
+            if (int rc = sip_backward(c, s, cf, m->d_gcls, conv, gi % 3, hz)) return rc;
+            if (iloop < ninner) lastfull = gi;
         }
+        if (int rc = sip_outer(c, s, m->d_idx, m->ap64, m->d_gcls, conv)) return rc;
         {
-            ProfScope ps_(c, "mx_outer");
-            k_mx_outer<<<c->ngrid, 512, 0, c->stream>>>(c->d_grids, m->d_gcls, m->cls_stride, m->h32,
-                                                        rhs, m->rhs32, dp, m->ap64, cf, c->d_gridred,
-                                                        conv);
-            MG_LAUNCHED(c);
+            ProfScope ps_(c, "mx_conv");
             k_mx_conv<<<1, 1024, 0, c->stream>>>(c->d_grids, c->ngrid, c->maxlevel, c->d_gridred,
                                                  m->d_ctl, m->d_maxrhs, prefak, c->prm.epcorr,
                                                  c->prm.nouter_min);
             MG_LAUNCHED(c);
         }
     }
+    if (int rc = sip_scatter_dp(c, s, m->d_idx)) return rc;
     // dp ghosts (the reference accumulates the connected hilf ghosts into dp)
     if (int rc = connect(c, 0, 1, nullptr, nullptr, nullptr, dp, nullptr, nullptr, false, false, 0))
         return rc;
     {
         ProfScope ps_(c, "mx_mgpcorr");
-        dim3 grid((interior_max(c) + 255) / 256, c->ngrid);
+        dim3 grid((s.npts + 255) / 256, c->ngrid);
         k_mx_mgpcorr<<<grid, 256, 0, c->stream>>>(c->d_grids, U, V, W, P, dp, c->L("RDX"),
                                                   c->L("RDY"), c->L("RDZ"), dt / c->prm.rho);
         MG_LAUNCHED(c);
@@ -421,17 +212,16 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
 int enqueue_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) {
     double frhs, fu, dtrk, dtrki;
     if (int rc = rk_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki)) return rc;
-    double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P"), *G = c->F("G");
-    double *UO = c->F("UO"), *VO = c->F("VO"), *WO = c->F("WO");
     MixedState* m = c->mx;
-    (void)P; (void)G; (void)UO; (void)VO; (void)WO;
     if (!m->g_uniform) {
         set_error("mixed form: needs a uniform viscosity field G = gmol (no LES model)");
         return MGLET_ERR_UNSUPPORTED;
     }
     if (int rc = launch_mx_flux(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, frhs, dt * fu))
         return rc;
-    if (int rc = connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
+    if (int rc = connect(c, 0, 1, c->F("U"), c->F("V"), c->F("W"), nullptr, nullptr, nullptr, false,
+                         true, 1))
+        return rc;
     return enqueue_mgpoisl(c, dtrk * dt);
 }
 
@@ -443,6 +233,15 @@ void fill_stats(Ctx* c, double dt, mglet_stage_stats* st) {
     st->prefak = c->prm.rho / dt;
 }
 
+float* du_buffer(Ctx* c, const char* name) {
+    MixedState* m = c->mx;
+    if (!m) return nullptr;
+    if (!std::strcmp(name, "DU")) return m->du32;
+    if (!std::strcmp(name, "DV")) return m->dv32;
+    if (!std::strcmp(name, "DW")) return m->dw32;
+    return nullptr;
+}
+
 }  // namespace
 
 int mixed_init(Ctx* c) {
@@ -450,11 +249,23 @@ int mixed_init(Ctx* c) {
         set_error("mixed form: one grid level only");
         return MGLET_ERR_UNSUPPORTED;
     }
+    if (!c->uniform) {
+        set_error("mixed form: all grids must have the same dimensions");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    if (c->prm.ninner < 1) {
+        set_error("mixed form: ninner must be at least 1");
+        return MGLET_ERR_UNSUPPORTED;
+    }
     MixedState* m = new MixedState();
     c->mx = m;
+    if (int rc = sip_init(c, m->sip)) return rc;
+    if (int rc = mx_flux_prepare(c)) return rc;
+    const int npts = m->sip.npts;
+    m->d_idx = c->hp[0].d_idx;
     // coefficient classes: same dims, BC types and spacing arrays
-    std::vector<std::vector<double>> sp(9);
-    const char* names[9] = {"DX", "DY", "DZ", "DDX", "DDY", "DDZ", "X", "Y", "Z"};
+    std::vector<std::vector<double>> sp(6);
+    const char* names[6] = {"DX", "DY", "DZ", "DDX", "DDY", "DDZ"};
     const long long lens[3] = {c->idimx, c->idimy, c->idimz};
     for (int q = 0; q < 6; ++q) {
         sp[q].resize(lens[q % 3]);
@@ -478,23 +289,13 @@ int mixed_init(Ctx* c) {
             reps.push_back(g);
         }
         m->gcls[g] = it->second;
-        m->maxcols = std::max(m->maxcols, (G.ii - 4) * (G.jj - 4));
     }
-    if (m->maxcols > 1024) {
-        set_error("mixed form: more than 1024 (j, i) columns per grid");
-        return MGLET_ERR_UNSUPPORTED;
-    }
-    if (!c->uniform) {
-        set_error("mixed form: all grids must have the same dimensions");
-        return MGLET_ERR_UNSUPPORTED;
-    }
-    if (int rc = mx_flux_prepare(c)) return rc;
-    // FP32 spacing tables
+    m->nclass = (int)reps.size();
+    // FP32 spacing tables for the flux kernel
     {
-        const long long n3[3] = {c->idimx, c->idimy, c->idimz};
         float** dst[3] = {&m->sx, &m->sy, &m->sz};
         for (int ax = 0; ax < 3; ++ax) {
-            const long long n = n3[ax];
+            const long long n = lens[ax];
             const std::vector<double>& d = sp[ax];
             const std::vector<double>& dd = sp[ax + 3];
             std::vector<float> tb(6 * n, 0.f);
@@ -516,54 +317,39 @@ int mixed_init(Ctx* c) {
             MG_CUDA(cudaMemcpy(*dst[ax], tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice));
         }
     }
-    m->nclass = (int)reps.size();
-    long long stride = 0;
-    for (const DevGrid& G : c->grids) stride = std::max(stride, (long long)G.kk * G.jj * G.ii);
-    m->cls_stride = stride;
-    const size_t ncoef = (size_t)m->nclass * stride;
-    for (float** p : {&m->lw, &m->ls, &m->lb, &m->lpr, &m->ue, &m->un, &m->ut, &m->ap32}) {
+    const size_t ncoef = (size_t)m->nclass * npts;
+    for (float** p : {&m->lw, &m->ls, &m->lb, &m->lpr, &m->ue, &m->un, &m->ut, &m->ap32})
         MG_CUDA(cudaMalloc(p, ncoef * sizeof(float)));
-        MG_CUDA(cudaMemset(*p, 0, ncoef * sizeof(float)));
-    }
     MG_CUDA(cudaMalloc(&m->ap64, ncoef * sizeof(double)));
-    MG_CUDA(cudaMemset(m->ap64, 0, ncoef * sizeof(double)));
-    for (float** p : {&m->h32, &m->r32, &m->rhs32, &m->du32, &m->dv32, &m->dw32}) {
+    for (float** p : {&m->du32, &m->dv32, &m->dw32}) {
         MG_CUDA(cudaMalloc(p, (size_t)c->idim3d * sizeof(float)));
         MG_CUDA(cudaMemset(*p, 0, (size_t)c->idim3d * sizeof(float)));
     }
     MG_CUDA(cudaMalloc(&m->d_gcls, c->ngrid * sizeof(int)));
     MG_CUDA(cudaMemcpy(m->d_gcls, m->gcls.data(), c->ngrid * sizeof(int), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMalloc(&m->d_ctl, 4 * sizeof(int)));
+    MG_CUDA(cudaMemset(m->d_ctl, 0, 4 * sizeof(int)));
     MG_CUDA(cudaMalloc(&m->d_maxrhs, sizeof(double)));
     MG_CUDA(cudaMallocHost(&m->h_ctl, 4 * sizeof(int)));
     MG_CUDA(cudaMallocHost(&m->h_maxrhs, sizeof(double)));
     // every connect variant the stage issues, built before any graph capture
     const ConnectPlan* pl;
     if (int rc = get_plan(c, 0, 1, 1 << 3, false, false, 0, &pl)) return rc;
-    if (int rc = get_plan(c, 0, 1, 1 << 3, false, false, -1, &pl)) return rc;
     if (int rc = get_plan(c, 0, 1, 7, false, true, 1, &pl)) return rc;
     if (int rc = get_plan(c, 0, 2, 15, true, false, 0, &pl)) return rc;
-    for (int l = c->minlevel; l <= c->maxlevel; ++l)
-        if (int rc = get_plan(c, l, 1, 7, false, true, 1, &pl)) return rc;
-    // extract class coefficients from the representative grids
+    // class coefficients from the representative grids
     int* d_reps = nullptr;
     MG_CUDA(cudaMalloc(&d_reps, reps.size() * sizeof(int)));
     MG_CUDA(cudaMemcpy(d_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
-    std::vector<const int*> hi;
-    for (const HpTable& t : c->hp) hi.push_back(t.d_idx);
-    const int** d_idxs = nullptr;
-    MG_CUDA(cudaMalloc(&d_idxs, hi.size() * sizeof(int*)));
-    MG_CUDA(cudaMemcpy(d_idxs, hi.data(), hi.size() * sizeof(int*), cudaMemcpyHostToDevice));
-    dim3 grid((interior_max(c) + 255) / 256, m->nclass);
+    dim3 grid((npts + 255) / 256, m->nclass);
     k_extract<<<grid, 256, 0, c->stream>>>(
-        c->d_grids, d_reps, d_idxs, c->prm.psolver == MGLET_PSOLVER_CLASSIC ? 0 : 1, stride,
+        c->d_grids, d_reps, m->d_idx, c->prm.psolver == MGLET_PSOLVER_CLASSIC ? 0 : 1, npts,
         c->F("SIPLW"), c->F("SIPLS"), c->F("SIPLB"), c->F("SIPLPR"), c->F("SIPUE"), c->F("SIPUN"),
         c->F("SIPUT"), c->F("GSAP"), m->lw, m->ls, m->lb, m->lpr, m->ue, m->un, m->ut, m->ap32,
         m->ap64);
     c->launches++;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     cudaFree(d_reps);
-    cudaFree((void*)d_idxs);
     if (e != cudaSuccess) return cuda_fail(e, "mixed_init");
     return 0;
 }
@@ -572,34 +358,16 @@ void mixed_release(Ctx* c) {
     MixedState* m = c->mx;
     if (!m) return;
     for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+    sip_release(m->sip);
     for (void* p : {(void*)m->lw, (void*)m->ls, (void*)m->lb, (void*)m->lpr, (void*)m->ue,
-                    (void*)m->un, (void*)m->ut, (void*)m->ap32, (void*)m->ap64, (void*)m->h32,
-                    (void*)m->r32, (void*)m->rhs32, (void*)m->d_gcls, (void*)m->d_ctl,
-                    (void*)m->d_maxrhs, (void*)m->du32, (void*)m->dv32, (void*)m->dw32,
-                    (void*)m->sx, (void*)m->sy, (void*)m->sz})
+                    (void*)m->un, (void*)m->ut, (void*)m->ap32, (void*)m->ap64, (void*)m->d_gcls,
+                    (void*)m->d_ctl, (void*)m->d_maxrhs, (void*)m->du32, (void*)m->dv32,
+                    (void*)m->dw32, (void*)m->sx, (void*)m->sy, (void*)m->sz})
         cudaFree(p);
     if (m->h_ctl) cudaFreeHost(m->h_ctl);
     if (m->h_maxrhs) cudaFreeHost(m->h_maxrhs);
     delete m;
     c->mx = nullptr;
-}
-
-__global__ void k_cvt_64_32(float* d, const double* s, long long n) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) d[t] = (float)s[t];
-}
-__global__ void k_cvt_32_64(double* d, const float* s, long long n) {
-    long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < n) d[t] = (double)s[t];
-}
-
-static float* du_buffer(Ctx* c, const char* name) {
-    MixedState* m = c->mx;
-    if (!m) return nullptr;
-    if (!std::strcmp(name, "DU")) return m->du32;
-    if (!std::strcmp(name, "DV")) return m->dv32;
-    if (!std::strcmp(name, "DW")) return m->dw32;
-    return nullptr;
 }
 
 // A field was uploaded: the FP32 RK registers follow DU/DV/DW, and a
@@ -617,9 +385,8 @@ void mixed_field_changed(Ctx* c, const char* name) {
 
 // Before a download: DU/DV/DW live in FP32 in this form.
 void mixed_field_sync_out(Ctx* c, const char* name) {
-    if (float* f = du_buffer(c, name)) {
+    if (float* f = du_buffer(c, name))
         k_cvt_32_64<<<(unsigned)((c->idim3d + 255) / 256), 256, 0, c->stream>>>(c->F(name), f, c->idim3d);
-    }
 }
 
 int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st) {

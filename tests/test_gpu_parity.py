@@ -182,11 +182,11 @@ def test_exploded_flag(gpu_lib):
     case = CASES["tiles8"]()
     g = gpu_lib.Solver(case, _prm())
     u, v, w, p = cases.taylor_green(case)
-    u[case.idim3d // 2 + 3] = np.nan
+    case.interior(u)[3, 2, 1, 4] = np.nan      # an interior cell of grid 4
     for nm, a in zip("UVWP", (u, v, w, p)):
         g.set(nm, a)
     info = g.itinfo(1e-3)
     assert info.exploded == 1
-    u[case.idim3d // 2 + 3] = 0.0
+    case.interior(u)[3, 2, 1, 4] = 0.0
     g.set("U", u)
     assert g.itinfo(1e-3).exploded == 0
