@@ -9,7 +9,14 @@ SIP with ninner = 5, nouter = 9, epcorr = 1e-10.  One step = one time step
 = three RK stages, each with its full pressure solve.  Inputs and the
 working set (>10 GB) are far larger than L2, so no flush is needed.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form plain|mixed]
+The headline is the batched mixed-precision form (FP32 flux stencils and SIP
+sweeps under the FP64 defect-correction outer loop, one CUDA graph per RK
+stage); the plain FP64 form, bit-identical to the CPU restatement, is timed
+in the same run and reported beside it.  The timed region runs unprofiled;
+per-kernel times for the roofline come from a second, profiled pass of the
+same number of steps (per-launch CUDA events on the solver's stream).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|plain]
   python bench.py --impl reference   # the CPU restatement on the host cores
 
 Prints one JSON line (rank 0).
@@ -29,8 +36,8 @@ sys.path.insert(0, ROOT)
 METRIC = "cell-updates/s per RK step: mixed/batched vs plain FP64, 1 GB300; % HBM roofline"
 UNIT = "cell-updates/s"
 
-# Algorithmic bytes per interior cell and launch of the kernel families,
-# FP64 plain form (8 B per value; one read or write of each operand).
+# Algorithmic bytes per interior cell and launch of the kernel families:
+# every operand read once and every result written once (FP64 8 B, FP32 4 B).
 PLAIN_BYTES = {
     "tstle4": 8 * (5 + 3),          # read u,v,w,p,g; write uo,vo,wo
     "rkstep": 8 * 4,                # read p,dp,rhs; write p,dp (per component) / 1.25 ~ 4+1
@@ -42,6 +49,33 @@ PLAIN_BYTES = {
     "accumulate": 8 * 4,            # read dp, hilf; write dp, hilf (whole slab)
     "mgpcorr": 8 * 9,               # read dp,u,v,w,p; write u,v,w,p
 }
+MIXED_BYTES = {
+    "mx_flux": 8 * 4 + 4 * 6 + 8 * 3,   # read u,v,w,p (f64), du,dv,dw (f32); write du,dv,dw, u,v,w
+    "mx_outer": 4 + 8 * 3 + 4,          # read hilf (f32), rhs, dp; write rhs, rhs32, dp
+    "mx_divcal": 8 * 3 + 8 + 4,         # read u,v,w; write rhs (f64) and rhs32
+    "mx_mgpcorr": 8 + 8 * 4 * 2,        # read dp, u,v,w,p; write u,v,w,p
+    "mx_scatter": 8 + 8,                # read dp (plane order); write DP
+}
+
+
+def kernel_bytes(name, case, ninner):
+    """Algorithmic bytes of one launch of a kernel family on this case.
+    The SIP sweeps (FP32, plane order) read rhs and hilf and write res
+    (forward), read res and hilf and write hilf (backward), except that the
+    first inner iteration of an outer iteration starts from hilf = 0 and reads
+    no hilf; both also move their face buffers (six written, three or six
+    read per grid).  Class coefficients, shared by all grids of a class and
+    served from L2, are not counted."""
+    cells = case.ncells
+    nk, nj, ni = case.kk - 4, case.jj - 4, case.ii - 4
+    face = case.ngrid * 4 * ((max(nj * nk, ni * nk, ni * nj) + 3) // 4 * 4)
+    hz = 1.0 / ninner
+    if name == "mx_sip_fwd":
+        return cells * (12 - 4 * hz) + face * (6 + 3 + 6 * (1 - hz))
+    if name == "mx_sip_bwd":
+        return cells * (12 - 4 * hz) + face * (6 + 3)
+    per = MIXED_BYTES.get(name, PLAIN_BYTES.get(name))
+    return per * cells if per else None
 
 
 def parse():
@@ -50,12 +84,15 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--form", choices=["plain", "mixed"], default="plain")
+    ap.add_argument("--form", choices=["plain", "mixed"], default="mixed")
     ap.add_argument("--tiles", type=int, nargs=3, default=[16, 16, 16])
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile-kernels", action="store_true", default=True)
+    ap.add_argument("--no-plain", action="store_true",
+                    help="skip the plain FP64 form timed beside the mixed headline")
+    ap.add_argument("--no-profile", action="store_true",
+                    help="skip the profiled pass (per-kernel times, roofline)")
     return ap.parse_args()
 
 
@@ -77,6 +114,9 @@ def init_fields(case):
     u, v, w, p = cases.taylor_green(case)
     u, v, w = cases.add_noise(case, (u, v, w), amplitude=1e-2, seed=42)
     return u, v, w, p
+
+
+DT = 5e-4
 
 
 def flow_params(form):
@@ -207,45 +247,37 @@ def run_reference(args, rank):
     return 0
 
 
-def run_ours(args, rank, world, local):
-    import numpy as np
+def time_form(args, form, case, fields, local, dist, profile=True):
+    """K unprofiled steps on the device (CUDA events on the solver's stream),
+    then, if asked, K profiled steps for the per-kernel times.  Returns the
+    solver (still open), the step time and the kernel table."""
     import torch
     from mglet_gb300 import gpu
 
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    case = make_case(args)
-    prm = flow_params(args.form)
+    prm = flow_params(form)
     s = gpu.Solver(case, prm, device=local)
-    fields = init_fields(case)
     for nm, a in zip("UVWP", fields):
         s.set(nm, a)
     s.connect(0, 2, "U", "V", "W", "P", corners=True)
     rk = gpu.rk_scheme("williamson")
-    dt = 5e-4
     stream = torch.cuda.ExternalStream(s.stream, device=local)
+    state = {"it": 0}
 
-    def step(it):
+    def step():
+        state["it"] += 1
         st = None
         for irk in range(1, 4):
-            st = s.timeintegrate_flow(it, it, 0.0, dt, irk, rk)
+            st = s.timeintegrate_flow(state["it"], state["it"], 0.0, DT, irk, rk)
         return st
 
     def barrier():
         if dist is not None:
             dist.barrier()
 
-    it = 0
     for _ in range(args.warmup):
-        it += 1
-        step(it)
+        step()
     s.synchronize()
     clocks = Clocks(local)
-    if args.profile_kernels:
-        s.profile(True)
     barrier()
     torch.cuda.synchronize()
     l0 = s.launches
@@ -255,9 +287,7 @@ def run_ours(args, rank, world, local):
     ipcs = []
     e0.record(stream)
     for _ in range(args.steps):
-        it += 1
-        st = step(it)
-        ipcs.append(st.ipc)
+        ipcs.append(step().ipc)
     e1.record(stream)
     e1.synchronize()
     clk = clocks.stop()
@@ -269,31 +299,61 @@ def run_ours(args, rank, world, local):
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    kern = {}
-    if args.profile_kernels:
+    kern, prof_ms = {}, None
+    if profile:
+        s.profile(True)
+        p0 = torch.cuda.Event(enable_timing=True)
+        p1 = torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        for _ in range(args.steps):
+            step()
+        p1.record(stream)
+        p1.synchronize()
+        prof_ms = p0.elapsed_time(p1)
         for name in s.profile_names():
             tot, n = s.profile_get(name)
             kern[name] = (tot, n)
         s.profile(False)
-    value = case.ncells * args.steps * world / (ms / 1e3)
+    return {"solver": s, "ms": ms, "launches": launches, "clocks": clk, "ipcs": ipcs,
+            "kern": kern, "prof_ms": prof_ms, "step": step, "prm": prm}
 
-    # roofline of the dominant kernel family
+
+def roofline(kern, case, ninner, prof_ms):
+    """Roofline object of the dominant kernel family of the profiled pass."""
+    if not kern:
+        return None
     peak, peak_kind = measured_peaks()
-    roof = None
-    if kern:
-        top = max(kern, key=lambda k: kern[k][0])
-        tot, n = kern[top]
-        per_cell = PLAIN_BYTES.get(top)
-        if per_cell and n:
-            bytes_per_launch = per_cell * case.ncells
-            achieved = bytes_per_launch / (tot / n / 1e3) / 1e9
-            roof = {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak,
-                    "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_kind,
-                    "traffic": None, "share": tot / ms,
-                    "algorithmic_bytes_per_launch": bytes_per_launch,
-                    "avg_launch_ms": tot / n}
+    top = max(kern, key=lambda k: kern[k][0])
+    tot, n = kern[top]
+    b = kernel_bytes(top, case, ninner)
+    if not b or not n:
+        return None
+    achieved = b / (tot / n / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "share": tot / prof_ms if prof_ms else None,
+            "algorithmic_bytes_per_launch": b, "avg_launch_ms": tot / n}
 
-    # end to end through the public API with host buffers
+
+def run_ours(args, rank, world, local):
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    case = make_case(args)
+    fields = init_fields(case)
+    prof = not args.no_profile
+    r = time_form(args, args.form, case, fields, local, dist, profile=prof)
+    s = r["solver"]
+    ms = r["ms"]
+    value = case.ncells * args.steps * world / (ms / 1e3)
+    roof = roofline(r["kern"], case, r["prm"].ninner, r["prof_ms"])
+
+    # end to end through the public API with host buffers: every step uploads
+    # u, v, w, p from pinned host memory and downloads them again
     e2e = None
     if not args.no_e2e:
         n = case.idim3d
@@ -304,10 +364,9 @@ def run_ours(args, rank, world, local):
         s.synchronize()
         t0 = time.perf_counter()
         for _ in range(ksteps):
-            it += 1
             for nm, h in zip("UVWP", host):
                 s.set_ptr(nm, h.data_ptr(), n)
-            step(it)
+            r["step"]()
             for nm, h in zip("UVWP", host):
                 s.get_ptr(nm, h.data_ptr(), n)
         s.synchronize()
@@ -315,6 +374,19 @@ def run_ours(args, rank, world, local):
         e2e = {"value": case.ncells * ksteps * world / te, "unit": UNIT,
                "h2d_bytes_per_step": 4 * n * 8, "d2h_bytes_per_step": 4 * n * 8,
                "steps": ksteps}
+    s.close()
+
+    plain = None
+    if args.form == "mixed" and not args.no_plain:
+        q = time_form(args, "plain", case, fields, local, dist, profile=prof)
+        q["solver"].close()
+        pv = case.ncells * args.steps * world / (q["ms"] / 1e3)
+        plain = {"value": pv, "unit": UNIT, "ms_per_step": q["ms"] / args.steps,
+                 "gpu_launches": q["launches"], "clocks": q["clocks"],
+                 "roofline": roofline(q["kern"], case, q["prm"].ninner, q["prof_ms"]),
+                 "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]}
+                                for k, v in q["kern"].items()},
+                 "mixed_over_plain": value / pv}
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -326,6 +398,7 @@ def run_ours(args, rank, world, local):
                    "sample": f"failed: {ex}"}
 
     if rank == 0:
+        ipcs = r["ipcs"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
@@ -336,18 +409,20 @@ def run_ours(args, rank, world, local):
                                    f"({args.tiles[0]}x{args.tiles[1]}x{args.tiles[2]}), "
                                    "TG+noise, RK3 dt=5e-4, SIP ninner=5 nouter=9 epcorr=1e-10",
                        "form": args.form, "cells": case.ncells,
+                       "step": "one time step = 3 RK stages with their pressure solves",
                        "l2": "working set > L2 (no flush needed)",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                       "ipc_per_stage_last": ipcs[-1] if ipcs else None},
-            "clocks": clk,
+                       "ipc_per_stage_last": ipcs[-1] if ipcs else None,
+                       "kernel_times": "separate profiled pass of the same step count"},
+            "clocks": r["clocks"],
             "e2e": e2e,
-            "gpu_launches": launches,
+            "gpu_launches": r["launches"],
             "roofline": roof,
-            "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
+            "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in r["kern"].items()},
+            "plain_fp64": plain,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)
-    s.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0

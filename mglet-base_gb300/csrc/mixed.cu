@@ -38,9 +38,9 @@ struct MixedState {
     int nclass = 0;
     std::vector<int> gcls;          // coefficient class of each grid
     int* d_gcls = nullptr;
-    // FP32 class coefficients, plane order [nclass][npts]
-    float *lw = nullptr, *ls = nullptr, *lb = nullptr, *lpr = nullptr;
-    float *ue = nullptr, *un = nullptr, *ut = nullptr, *ap32 = nullptr;
+    // class coefficients in padded plane order: FP32 blocks [lw|ls|lb|lpr|ap]
+    // and [ue|un|ut], FP64 ap
+    float *cf = nullptr, *cb = nullptr;
     double* ap64 = nullptr;
     SipState sip;
     const int* d_idx = nullptr;     // plane position -> natural local index (hp table)
@@ -62,30 +62,6 @@ struct MixedState {
 };
 
 namespace {
-
-// FP32 (and FP64 ap) class coefficients in plane order from the
-// representative grid of each class.
-__global__ void k_extract(const DevGrid* __restrict__ grids, const int* __restrict__ reps,
-                          const int* __restrict__ idx, int planeorder, int npts,
-                          const double* __restrict__ lw, const double* __restrict__ ls,
-                          const double* __restrict__ lb, const double* __restrict__ lpr,
-                          const double* __restrict__ ue, const double* __restrict__ un,
-                          const double* __restrict__ ut, const double* __restrict__ ap,
-                          float* olw, float* ols, float* olb, float* olpr, float* oue, float* oun,
-                          float* out, float* oap, double* oap64) {
-    const int cls = blockIdx.y;
-    const DevGrid G = grids[reps[cls]];
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= npts) return;
-    const int id = idx[q];
-    const long long src = G.ip3 + (planeorder ? q : id);
-    const long long dst = (long long)cls * npts + q;
-    olw[dst] = (float)lw[src]; ols[dst] = (float)ls[src]; olb[dst] = (float)lb[src];
-    olpr[dst] = (float)lpr[src]; oue[dst] = (float)ue[src]; oun[dst] = (float)un[src];
-    out[dst] = (float)ut[src];
-    oap[dst] = (float)ap[G.ip3 + id];
-    oap64[dst] = ap[G.ip3 + id];
-}
 
 __device__ __forceinline__ double block_max_d(double v, double* sh) {
     for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -153,10 +129,6 @@ __global__ void k_cvt_32_64(double* d, const float* s, long long n) {
     if (t < n) d[t] = (double)s[t];
 }
 
-SipCoef coefs(const MixedState* m) {
-    return SipCoef{m->lw, m->ls, m->lb, m->lpr, m->ue, m->un, m->ut, m->ap32};
-}
-
 // The reference's inner-iteration halo semantics mapped onto the rotating
 // res face buffers: iteration G (1-based within one mgpoisl) writes slot G%3;
 // its forward sweep reads low ghosts written by the last iteration whose
@@ -166,11 +138,10 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
     SipState& s = m->sip;
     const double prefak = c->prm.rho / dt;
     double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P"), *dp = c->F("DP");
-    MG_CUDA(cudaMemsetAsync(s.dp64, 0, (size_t)c->ngrid * s.npts * sizeof(double), c->stream));
-    MG_CUDA(cudaMemsetAsync(m->d_ctl, 0, 2 * sizeof(int), c->stream));
-    if (int rc = sip_divcal(c, s, m->d_idx, prefak)) return rc;
-    const int* conv = m->d_ctl;
-    const SipCoef cf = coefs(m);
+    MG_CUDA(cudaMemsetAsync(s.dp64, 0, (size_t)c->ngrid * s.npp * sizeof(double), c->stream));
+    MG_CUDA(cudaMemsetAsync(m->d_ctl, 0, 3 * sizeof(int), c->stream));
+    if (int rc = sip_divcal(c, s, prefak)) return rc;
+    int* ctl = m->d_ctl;
     const int ninner = c->prm.ninner;
     int gi = 0, lastfull = 0;
     for (int ipcount = 1; ipcount <= c->prm.nouter; ++ipcount) {
@@ -178,11 +149,11 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
             ++gi;
             const bool hz = iloop == 1;
             const int rlow = lastfull > 0 ? lastfull % 3 : -1;
-            if (int rc = sip_forward(c, s, cf, m->d_gcls, conv, rlow, gi % 3, hz)) return rc;
-            if (int rc = sip_backward(c, s, cf, m->d_gcls, conv, gi % 3, hz)) return rc;
+            if (int rc = sip_forward(c, s, m->cf, m->d_gcls, ctl, rlow, gi % 3, hz)) return rc;
+            if (int rc = sip_backward(c, s, m->cb, m->d_gcls, ctl, gi % 3, hz)) return rc;
             if (iloop < ninner) lastfull = gi;
         }
-        if (int rc = sip_outer(c, s, m->d_idx, m->ap64, m->d_gcls, conv)) return rc;
+        if (int rc = sip_outer(c, s, m->ap64, m->d_gcls, ctl)) return rc;
         {
             ProfScope ps_(c, "mx_conv");
             k_mx_conv<<<1, 1024, 0, c->stream>>>(c->d_grids, c->ngrid, c->maxlevel, c->d_gridred,
@@ -191,7 +162,7 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
             MG_LAUNCHED(c);
         }
     }
-    if (int rc = sip_scatter_dp(c, s, m->d_idx)) return rc;
+    if (int rc = sip_scatter_dp(c, s)) return rc;
     // dp ghosts (the reference accumulates the connected hilf ghosts into dp)
     if (int rc = connect(c, 0, 1, nullptr, nullptr, nullptr, dp, nullptr, nullptr, false, false, 0))
         return rc;
@@ -203,7 +174,7 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
         MG_LAUNCHED(c);
     }
     if (int rc = connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
-    MG_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    MG_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     MG_CUDA(cudaMemcpyAsync(m->h_maxrhs, m->d_maxrhs, sizeof(double), cudaMemcpyDeviceToHost,
                             c->stream));
     return 0;
@@ -223,6 +194,17 @@ int enqueue_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) {
                          true, 1))
         return rc;
     return enqueue_mgpoisl(c, dtrk * dt);
+}
+
+// 0, or MGLET_ERR_CUDA when a wavefront kernel gave up waiting for its
+// bulk copies (the device error flag of the control block).
+int check_device_flag(Ctx* c) {
+    MixedState* m = c->mx;
+    if (m->h_ctl[2] != 0) {
+        set_error("mixed form: a wavefront kernel timed out waiting for its TMA copies");
+        return MGLET_ERR_CUDA;
+    }
+    return 0;
 }
 
 void fill_stats(Ctx* c, double dt, mglet_stage_stats* st) {
@@ -261,7 +243,6 @@ int mixed_init(Ctx* c) {
     c->mx = m;
     if (int rc = sip_init(c, m->sip)) return rc;
     if (int rc = mx_flux_prepare(c)) return rc;
-    const int npts = m->sip.npts;
     m->d_idx = c->hp[0].d_idx;
     // coefficient classes: same dims, BC types and spacing arrays
     std::vector<std::vector<double>> sp(6);
@@ -317,10 +298,6 @@ int mixed_init(Ctx* c) {
             MG_CUDA(cudaMemcpy(*dst[ax], tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice));
         }
     }
-    const size_t ncoef = (size_t)m->nclass * npts;
-    for (float** p : {&m->lw, &m->ls, &m->lb, &m->lpr, &m->ue, &m->un, &m->ut, &m->ap32})
-        MG_CUDA(cudaMalloc(p, ncoef * sizeof(float)));
-    MG_CUDA(cudaMalloc(&m->ap64, ncoef * sizeof(double)));
     for (float** p : {&m->du32, &m->dv32, &m->dw32}) {
         MG_CUDA(cudaMalloc(p, (size_t)c->idim3d * sizeof(float)));
         MG_CUDA(cudaMemset(*p, 0, (size_t)c->idim3d * sizeof(float)));
@@ -341,14 +318,13 @@ int mixed_init(Ctx* c) {
     int* d_reps = nullptr;
     MG_CUDA(cudaMalloc(&d_reps, reps.size() * sizeof(int)));
     MG_CUDA(cudaMemcpy(d_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
-    dim3 grid((npts + 255) / 256, m->nclass);
-    k_extract<<<grid, 256, 0, c->stream>>>(
-        c->d_grids, d_reps, m->d_idx, c->prm.psolver == MGLET_PSOLVER_CLASSIC ? 0 : 1, npts,
-        c->F("SIPLW"), c->F("SIPLS"), c->F("SIPLB"), c->F("SIPLPR"), c->F("SIPUE"), c->F("SIPUN"),
-        c->F("SIPUT"), c->F("GSAP"), m->lw, m->ls, m->lb, m->lpr, m->ue, m->un, m->ut, m->ap32,
-        m->ap64);
-    c->launches++;
+    int rc = sip_extract(c, m->sip, m->nclass, d_reps, m->d_idx,
+                         c->prm.psolver != MGLET_PSOLVER_CLASSIC, &m->cf, &m->cb, &m->ap64);
     cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (rc) {
+        cudaFree(d_reps);
+        return rc;
+    }
     cudaFree(d_reps);
     if (e != cudaSuccess) return cuda_fail(e, "mixed_init");
     return 0;
@@ -359,8 +335,7 @@ void mixed_release(Ctx* c) {
     if (!m) return;
     for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
     sip_release(m->sip);
-    for (void* p : {(void*)m->lw, (void*)m->ls, (void*)m->lb, (void*)m->lpr, (void*)m->ue,
-                    (void*)m->un, (void*)m->ut, (void*)m->ap32, (void*)m->ap64, (void*)m->d_gcls,
+    for (void* p : {(void*)m->cf, (void*)m->cb, (void*)m->ap64, (void*)m->d_gcls,
                     (void*)m->d_ctl, (void*)m->d_maxrhs, (void*)m->du32, (void*)m->dv32,
                     (void*)m->dw32, (void*)m->sx, (void*)m->sy, (void*)m->sz})
         cudaFree(p);
@@ -393,7 +368,7 @@ int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st) {
     if (int rc = enqueue_mgpoisl(c, dt)) return rc;
     MG_CUDA(cudaStreamSynchronize(c->stream));
     fill_stats(c, dt, st);
-    return 0;
+    return check_device_flag(c);
 }
 
 // One stage: captured once per (irk, dt) into a CUDA graph and replayed; with
@@ -433,6 +408,7 @@ int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_sta
     if (st) {
         MG_CUDA(cudaStreamSynchronize(c->stream));
         fill_stats(c, dtrk * dt, st);
+        return check_device_flag(c);
     }
     return 0;
 }

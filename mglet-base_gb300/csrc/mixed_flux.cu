@@ -68,34 +68,41 @@ struct FluxArgs {
     float rrho;
     float gpx, gpy, gpz;
     double frhs, dtfu;
+    int nslab;                         // j-slabs (CTAs) per grid
 };
 
-// One CTA per grid, one thread per interior (k, j), marching i.
+// One CTA per j-slab of a grid, one thread per interior (k, j) of the slab,
+// marching i.
 __global__ void __launch_bounds__(576, 1) k_mx_flux(FluxArgs a) {
     extern __shared__ float2 sm[];
-    const DevGrid G = a.grids[blockIdx.x];
+    const DevGrid G = a.grids[blockIdx.x / a.nslab];
+    const int slab = blockIdx.x % a.nslab;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
-    const int pk = kk - 2, pj = jj - 2, plane = pk * pj;     // plane of k = 2..kk-1, j = 2..jj-1
+    const int js = (jj - 4 + a.nslab - 1) / a.nslab;
+    const int j0 = 3 + slab * js;                     // first interior j of the slab
+    const int nj = min(js, jj - 1 - j0);              // interior j of the slab: j0 .. j0+nj-1
+    // plane window: k = 2..kk-1, j = j0-1..j0+nj
+    const int pk = kk - 2, pj = nj + 2, plane = pk * pj;
     float2* su = sm;                  // [3][plane]
     float2* sv = su + 3 * plane;
     float2* sw = sv + 3 * plane;
     float2* sp = sw + 3 * plane;      // [2][plane]
     const long long o = G.ip3;
     const int kj = kk * jj;
-    const int nk = kk - 4, nj = jj - 4;
+    const int nk = kk - 4;
     const int t = threadIdx.x;
     const bool on = t < nk * nj;
-    const int k = on ? t % nk + 3 : 3, j = on ? t / nk + 3 : 3;
+    const int k = on ? t % nk + 3 : 3, j = on ? t / nk + j0 : j0;
     const int nring = plane - nk * nj;
-    // plane-local index of (k, j): (k-2) + (j-2)*pk
-    auto pl = [pk](int kq, int jq) { return (kq - 2) + (jq - 2) * pk; };
-    // ring point r (0..nring-1) -> (k, j) on the border of the 2..kk-1 x 2..jj-1 plane
+    // window-local index of (k, j): (k-2) + (j-j0+1)*pk
+    auto pl = [pk, j0](int kq, int jq) { return (kq - 2) + (jq - j0 + 1) * pk; };
+    // ring point r (0..nring-1) -> (k, j) on the border of the window
     auto ring = [&](int r, int& kq, int& jq) {
-        if (r < pk) { kq = 2 + r; jq = 2; return; }
+        if (r < pk) { kq = 2 + r; jq = j0 - 1; return; }
         r -= pk;
-        if (r < pk) { kq = 2 + r; jq = jj - 1; return; }
+        if (r < pk) { kq = 2 + r; jq = j0 + nj; return; }
         r -= pk;
-        jq = 3 + r / 2;
+        jq = j0 + r / 2;
         kq = (r & 1) ? kk - 1 : 2;
     };
     const double *U0 = a.U0 + o, *V0 = a.V0 + o, *W0 = a.W0 + o, *P0 = a.P0 + o;
@@ -282,16 +289,26 @@ __global__ void __launch_bounds__(576, 1) k_mx_flux(FluxArgs a) {
 
 }  // namespace
 
+// j-slabs per grid: the fewest for which a slab has at most 576 (k, j) columns
+static int flux_slabs(const DevGrid& G0) {
+    const int nk = G0.kk - 4, nj = G0.jj - 4;
+    for (int s = 1; s <= nj; ++s)
+        if (nk * ((nj + s - 1) / s) <= 576) return s;
+    return 0;
+}
+
 static size_t flux_smem(const DevGrid& G0) {
-    return (size_t)11 * (G0.kk - 2) * (G0.jj - 2) * sizeof(float2);
+    const int nslab = flux_slabs(G0);
+    const int js = (G0.jj - 4 + nslab - 1) / nslab;
+    return (size_t)11 * (G0.kk - 2) * (js + 2) * sizeof(float2);
 }
 
 // Checks the launch limits of the flux kernel for this grid shape and opts
 // in to the dynamic shared memory it needs.
 int mx_flux_prepare(Ctx* c) {
     const DevGrid& G0 = c->grids[0];
-    if ((G0.kk - 4) * (G0.jj - 4) > 576) {
-        set_error("mixed form: the flux kernel takes at most 576 (k, j) columns per grid");
+    if (G0.kk - 4 > 576) {
+        set_error("mixed form: the flux kernel takes at most 576 cells in k per grid");
         return MGLET_ERR_UNSUPPORTED;
     }
     const size_t smem = flux_smem(G0);
@@ -308,8 +325,11 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
     ProfScope ps_(c, "mx_flux");
     const DevGrid& G0 = c->grids[0];
     const size_t smem = flux_smem(G0);
-    const int threads = ((G0.kk - 4) * (G0.jj - 4) + 31) / 32 * 32;
+    const int nslab = flux_slabs(G0);
+    const int js = (G0.jj - 4 + nslab - 1) / nslab;
+    const int threads = ((G0.kk - 4) * js + 31) / 32 * 32;
     FluxArgs a;
+    a.nslab = nslab;
     a.grids = c->d_grids;
     a.U0 = c->F("U"); a.V0 = c->F("V"); a.W0 = c->F("W"); a.P0 = c->F("P");
     a.U = c->F("U"); a.V = c->F("V"); a.W = c->F("W");
@@ -324,7 +344,7 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
     a.gpx = (float)c->prm.gradp[0]; a.gpy = (float)c->prm.gradp[1]; a.gpz = (float)c->prm.gradp[2];
     a.frhs = frhs;
     a.dtfu = dtfu;
-    k_mx_flux<<<c->ngrid, threads, smem, c->stream>>>(a);
+    k_mx_flux<<<c->ngrid * nslab, threads, smem, c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }

@@ -1,16 +1,20 @@
-// mixed_sip.cu -- inner SIP iterations of the mixed form in hyperplane layout.
+// mixed_sip.cu -- inner SIP iterations of the mixed form: hyperplane layout,
+// TMA-fed wavefronts, pulled halos.
 //
 // The reference stores its SIP factors in hyperplane ("iacc") order so that
 // each wavefront step reads a contiguous run (sip_hyperplane_mod.F90:106-257,
-// 450-569).  The mixed form carries that idea through the whole inner
-// solve: hilf, res and the FP32 copy of the outer residual live in plane
-// order too, so at every wavefront step the active threads of a warp touch
-// consecutive addresses.  Halos are pulled instead of copied: each sweep
-// writes the six boundary planes of its result into a per-grid face buffer,
-// and the next sweep of a neighbour reads its ghost values straight from
-// there (no conn kernels).  The lagged-coupling semantics of conn(res) and
-// conn(dp) in sip/mgpoisit (pressuresolver_mod.F90:400-465) are kept
-// exactly:
+// 450-569).  Here hilf, res and the FP32 outer residual use that order too,
+// with every plane padded to a 16-byte boundary, so each wavefront step's
+// operands are a handful of contiguous, aligned segments.  One thread per CTA
+// streams them into a shared-memory ring with cp.async.bulk (TMA), four
+// planes ahead of the wavefront, completion tracked by one mbarrier per ring
+// slot; the wavefront itself then only touches shared memory.
+//
+// Halos are pulled instead of copied: each sweep writes the six boundary
+// planes of its result into a per-grid face buffer, and the next sweep of a
+// neighbour reads its ghost values from there (no conn kernels).  The
+// lagged-coupling semantics of conn(res) and conn(dp) in sip/mgpoisit
+// (pressuresolver_mod.F90:400-465) are kept exactly:
 //   * the forward sweep of inner iteration G reads its low res ghosts from
 //     the forward results of the last iteration whose conn(res) was a full
 //     exchange (the last inner iteration only exchanges the high faces,
@@ -23,9 +27,12 @@
 //
 // Column wavefront: one CTA per grid, one thread per (j, i) column; at step
 // t the thread is at k = t - (i-3) - (j-3) + 3, on hyperplane i+j+k = t+9.
-// res(k-1) and hilf(k-1..k+1) of the own column stay in registers;
-// res(j-1), res(i-1) and hilf of the four lateral columns come through
-// double-buffered shared memory.
+// res(k-1) stays in a register; res(j-1) and res(i-1) come through a
+// double-buffered shared-memory plane written one step earlier.
+//
+// Every mbarrier wait is bounded: after kWaitLimit polls the kernel records
+// an error in the control block, stops computing, and still waits (bounded)
+// for the copies it has in flight before it exits.
 #include <algorithm>
 #include <vector>
 
@@ -35,116 +42,224 @@
 namespace mg {
 namespace {
 
-struct SipShape {
-    int kk, jj, ii, ni, nj, nk, npts, fs;
-    const int* tpos;   // [(ni+nj+nk-2)+2][ni]: pos(m0, io, jo) = tpos[m0*ni + io] + jo
+constexpr int kFwdSlots = 6;   // planes t-1 .. t+4
+constexpr int kBwdSlots = 5;   // planes t .. t+4 (reverse order)
+constexpr int kLook = 4;       // records issued ahead of the wavefront
+constexpr int kMaxCols = 1024; // one thread per (j, i) column
+// A wait gives up after this many SM clock cycles (about one second); a
+// healthy wait lasts microseconds.
+constexpr long long kWaitCycles = 2000000000LL;
+
+struct Shape {
+    int kk, jj, ii, ni, nj, nk, nm, npp, fs, maxlp;
+    const int* tpos;   // [nm][ni]: padded position of (io, jo) in plane m0 is tpos[m0*ni+io] + jo
+    const int* pst;    // [nm+1] padded plane starts
 };
 
-// face-buffer index of a boundary point on slot f (0: x-low, 1: x-high,
-// 2: y-low, 3: y-high, 4: z-low, 5: z-high), 0-based (ko, jo, io)
-__device__ __forceinline__ int fidx_x(const SipShape& s, int ko, int jo) { return ko + jo * s.nk; }
-__device__ __forceinline__ int fidx_y(const SipShape& s, int ko, int io) { return ko + io * s.nk; }
-__device__ __forceinline__ int fidx_z(const SipShape& s, int jo, int io) { return jo + io * s.nj; }
+__device__ __forceinline__ int fidx_x(const Shape& s, int ko, int jo) { return ko + jo * s.nk; }
+__device__ __forceinline__ int fidx_y(const Shape& s, int ko, int io) { return ko + io * s.nk; }
+__device__ __forceinline__ int fidx_z(const Shape& s, int jo, int io) { return jo + io * s.nj; }
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void bar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void bar_expect(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes,
+                                          unsigned long long* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Bounded wait for the phase with the given parity; false on timeout.
+__device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parity) {
+    const unsigned a = smem_u32(bar);
+    const long long t0 = clock64();
+    while (true) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(a), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kWaitCycles) return false;
+    }
+}
+
+__device__ __forceinline__ void proxy_fence() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
 
 struct FwdArgs {
-    SipShape s;
+    Shape s;
     const int* fnbr;            // [ngrid][6] neighbour grid (0-based) across faces 1..6
     const int* gcls;
-    const float *H, *RHS;       // plane order [ngrid][npts]
-    float* R;                   // plane order, forward results
+    const float* H;             // padded plane order [ngrid][npp]
+    const float* RHS;
+    float* R;
     const float* HOUT;          // [ngrid][6][fs]
-    const float* RLOW;          // res face buffers to read low ghosts from (or null = 0)
+    const float* RLOW;          // res face buffers with the low ghosts (null: zeros)
     float* RW;                  // res face buffers to write
-    const float *LW, *LS, *LB, *LPR, *AP;   // class coefficients, plane order
+    const float* CF;            // class blocks: per plane [lw|ls|lb|lpr|ap] x Lp
     const float *AW, *AE, *AS, *AN, *AB, *AT;   // FP32 1-D coefficients (concatenated)
     const DevGrid* grids;
-    const int* conv;
-    int hzero;                  // first inner iteration: hilf == 0
+    int* ctl;                   // [0] converged (skip), [2] error flag
+    int hzero;
 };
 
-__global__ void __launch_bounds__(576) k_sip_fwd(FwdArgs a) {
-    if (*a.conv) return;
-    const SipShape s = a.s;
-    const int nj = s.nj, ni = s.ni, nk = s.nk, npts = s.npts, fs = s.fs;
-    __shared__ float xr[2][576];
-    __shared__ float xkm[2][576], xkp[2][576];
+// Shared memory of the forward sweep (dynamic): kFwdSlots records of
+// (coefficient block 5*maxlp | rhs maxlp | hilf maxlp), the plane tables,
+// the res exchange planes and the slot barriers.
+__global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    const Shape s = a.s;
+    const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm, mlp = s.maxlp;
+    const int rec = 7 * mlp;   // floats per record
+    float* ring = reinterpret_cast<float*>(smraw);
+    int* stpos = reinterpret_cast<int*>(ring + kFwdSlots * rec);
+    int* spst = stpos + nm * ni;
+    const int xs = blockDim.x;
+    float* xr = reinterpret_cast<float*>(spst + nm + 1);            // [2][xs]
+    float* gh = reinterpret_cast<float*>(((size_t)(xr + 2 * xs) + 15) & ~(size_t)15);   // [6][fs]
+    float* gr = gh + 6 * fs;                                         // [3][fs]
+    float* sab = gr + 3 * fs;                                        // [kk]
+    float* sat = sab + s.kk;                                         // [kk]
+    unsigned long long* bars =
+        reinterpret_cast<unsigned long long*>(((size_t)(sat + s.kk) + 15) & ~(size_t)15);
+    unsigned long long* gbar = bars + kFwdSlots;                     // ghost faces
     const int g = blockIdx.x;
+    const int tid = threadIdx.x;
     const DevGrid G = a.grids[g];
-    const int col = threadIdx.x;
+    const long long base = (long long)g * s.npp;
+    const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
+    const bool hz = a.hzero != 0;
+    __shared__ int sbad;
+    for (int q = tid; q < nm * ni; q += blockDim.x) stpos[q] = s.tpos[q];
+    for (int q = tid; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
+    for (int q = tid; q < s.kk; q += blockDim.x) {
+        sab[q] = a.AB[G.ipz + q];      // sab[k-1] = ab(k)
+        sat[q] = a.AT[G.ipz + q];
+    }
+    if (!a.RLOW)
+        for (int q = tid; q < 3 * fs; q += blockDim.x) gr[q] = 0.f;
+    if (tid == 0) {
+        sbad = 0;
+        for (int q = 0; q <= kFwdSlots; ++q) bar_init(&bars[q], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int* fn = a.fnbr + 6 * g;
+    // ghost faces: hilf of the six neighbours' facing planes (unless hilf is
+    // zero) and res of the three low neighbours (unless there is none yet)
+    if (tid == 0) {
+        const unsigned fb = (unsigned)fs * 4u;
+        bar_expect(gbar, (hz ? 0u : 6u * fb) + (a.RLOW ? 3u * fb : 0u));
+        if (!hz) {
+            const int src_slot[6] = {1, 0, 3, 2, 5, 4};   // -x nbr's x-high plane, ...
+            for (int f = 0; f < 6; ++f)
+                bulk_load(gh + f * fs, a.HOUT + ((long long)fn[f] * 6 + src_slot[f]) * fs, fb, gbar);
+        }
+        if (a.RLOW) {
+            bulk_load(gr + 0 * fs, a.RLOW + ((long long)fn[0] * 6 + 1) * fs, fb, gbar);
+            bulk_load(gr + 1 * fs, a.RLOW + ((long long)fn[2] * 6 + 3) * fs, fb, gbar);
+            bulk_load(gr + 2 * fs, a.RLOW + ((long long)fn[4] * 6 + 5) * fs, fb, gbar);
+        }
+    }
+    int issued = -1;   // last record issued (thread 0)
+    // producer: record r = {coefficients, rhs, hilf} of plane r into slot r % kFwdSlots
+    auto issue = [&](int r) {
+        if (r >= nm) return;
+        issued = r;
+        const int sl = r % kFwdSlots;
+        const int p0 = spst[r], lp = spst[r + 1] - p0;
+        float* d = ring + sl * rec;
+        const unsigned b5 = 5u * lp * 4u, b1 = (unsigned)lp * 4u;
+        bar_expect(&bars[sl], b5 + b1 + (hz ? 0u : b1));
+        bulk_load(d, CF + 5LL * p0, b5, &bars[sl]);
+        bulk_load(d + 5 * mlp, a.RHS + base + p0, b1, &bars[sl]);
+        if (!hz) bulk_load(d + 6 * mlp, a.H + base + p0, b1, &bars[sl]);
+    };
+    if (tid == 0)
+        for (int r = 0; r <= kLook; ++r) issue(r);
+
+    const int col = tid;
     const bool on = col < ni * nj;
     const int jo = on ? col % nj : 0, io = on ? col / nj : 0;
-    const long long base = (long long)g * npts;
-    const long long cb = (long long)a.gcls[g] * npts;
-    const float *H = a.H + base, *RHS = a.RHS + base;
-    float* R = a.R + base;
-    const float *lw = a.LW + cb, *ls = a.LS + cb, *lb = a.LB + cb, *lpr = a.LPR + cb, *ap = a.AP + cb;
-    const int* fn = a.fnbr + 6 * g;
-    // ghost sources: hilf and res of the neighbours' facing boundary planes
-    const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;   // -x nbr, its x-high plane
-    const float* hxp = a.HOUT + ((long long)fn[1] * 6 + 0) * fs;
-    const float* hym = a.HOUT + ((long long)fn[2] * 6 + 3) * fs;
-    const float* hyp = a.HOUT + ((long long)fn[3] * 6 + 2) * fs;
-    const float* hzm = a.HOUT + ((long long)fn[4] * 6 + 5) * fs;
-    const float* hzp = a.HOUT + ((long long)fn[5] * 6 + 4) * fs;
-    const float* rxm = a.RLOW ? a.RLOW + ((long long)fn[0] * 6 + 1) * fs : nullptr;
-    const float* rym = a.RLOW ? a.RLOW + ((long long)fn[2] * 6 + 3) * fs : nullptr;
-    const float* rzm = a.RLOW ? a.RLOW + ((long long)fn[4] * 6 + 5) * fs : nullptr;
+    const float *hxm = gh, *hxp = gh + fs, *hym = gh + 2 * fs, *hyp = gh + 3 * fs,
+                *hzm = gh + 4 * fs, *hzp = gh + 5 * fs;
+    const float *rxm = gr, *rym = gr + fs, *rzm = gr + 2 * fs;
     float* rw = a.RW + (long long)g * 6 * fs;
+    float* R = a.R + base;
     const int i = io + 3, j = jo + 3;
     const float aw = a.AW[G.ipx + i - 1], ae = a.AE[G.ipx + i - 1];
     const float as = a.AS[G.ipy + j - 1], an = a.AN[G.ipy + j - 1];
-    const float* ab = a.AB + G.ipz - 1;   // 1-based k
-    const float* at = a.AT + G.ipz - 1;
-    const bool hz = a.hzero != 0;
-    // own-column hilf window at virtual k: hm = h(k-1), hc = h(k), hp = h(k+1)
-    auto hval = [&](int kv) -> float {     // h(kv, j, i) for kv in 2..kk-1 (ghosts from z nbrs)
-        if (hz || !on) return 0.f;
-        if (kv <= 2) return hzm[fidx_z(s, jo, io)];
-        if (kv >= nk + 3) return hzp[fidx_z(s, jo, io)];
-        const int ko = kv - 3;
-        return H[s.tpos[(io + jo + ko) * ni + io] + jo];
-    };
-    const int nsteps = ni + nj + nk - 2;
-    // own-column window at the virtual k of step 0 (k0 = 3 - io - jo); values
-    // for virtual k outside 2..kk-1 are never read by an active neighbour
-    const int k0 = 3 - io - jo;
-    int kv = k0;
-    auto hwin = [&](int kq) { return (on && kq >= 2 && kq <= nk + 3) ? hval(kq) : 0.f; };
-    float hm = hwin(kv - 1), hc = hwin(kv), hp = hwin(kv + 1);
+    const float* ab = sab - 1;   // 1-based k
+    const float* at = sat - 1;
+    bool bad = false;
+    if (!bar_wait(gbar, 0)) {
+        bad = true;
+        atomicOr(&sbad, 1);
+    }
+    int done = -1;     // every record <= done has landed (as seen by this thread)
     float rprev = 0.f;
-    for (int t = 0; t < nsteps; ++t) {
-        kv = k0 + t;
-        const int buf = t & 1;
-        if (on) {
-            xkm[buf][col] = hm;
-            xkp[buf][col] = hp;
-        }
-        __syncthreads();
-        const bool act = on && kv >= 3 && kv <= nk + 2;
-        float r = 0.f;
-        if (act) {
-            const int ko = kv - 3;
-            const int m0 = io + jo + ko;
-            const int pc = s.tpos[m0 * ni + io] + jo;
-            // lateral hilf: own neighbours in the row / column, ghosts from face buffers
-            float hjm, hjp, him, hip;
-            if (hz) {
-                hjm = hjp = him = hip = 0.f;
-            } else {
-                hjm = jo > 0 ? xkm[buf][col - 1] : hym[fidx_y(s, ko, io)];
-                hjp = jo < nj - 1 ? xkp[buf][col + 1] : hyp[fidx_y(s, ko, io)];
-                him = io > 0 ? xkm[buf][col - nj] : hxm[fidx_x(s, ko, jo)];
-                hip = io < ni - 1 ? xkp[buf][col + nj] : hxp[fidx_x(s, ko, jo)];
+    for (int t = 0; t < nm; ++t) {
+        // planes t and t+1 resident (t-1 was waited for one step earlier)
+        if (!bad && !*(volatile int*)&sbad) {
+            for (int r = done + 1; r <= t + 1 && r < nm; ++r) {
+                if (!bar_wait(&bars[r % kFwdSlots], (r / kFwdSlots) & 1)) {
+                    bad = true;
+                    atomicOr(&sbad, 1);
+                    break;
+                }
+                done = r;
             }
-            const float lap = -aw * him - ae * hip - as * hjm - an * hjp - ab[kv] * hm -
-                              at[kv] * hp - ap[pc] * hc;
-            const float rkm = ko > 0 ? rprev : (rzm ? rzm[fidx_z(s, jo, io)] : 0.f);
-            const float rjm = jo > 0 ? xr[buf ^ 1][col - 1] : (rym ? rym[fidx_y(s, ko, io)] : 0.f);
-            const float rim = io > 0 ? xr[buf ^ 1][col - nj] : (rxm ? rxm[fidx_x(s, ko, jo)] : 0.f);
-            r = (RHS[pc] + lap) * lpr[pc];
-            r = r - lb[pc] * rkm - ls[pc] * rjm - lw[pc] * rim;
-            R[pc] = r;
-            // boundary planes for the neighbours
+        }
+        const int buf = t & 1;
+        const int ko = t - io - jo;
+        if (on && !bad && ko >= 0 && ko < nk) {
+            const int k = ko + 3;
+            const float* c0 = ring + (t % kFwdSlots) * rec;
+            const float* hcur = c0 + 6 * mlp;
+            const float* hm1 = ring + ((t + kFwdSlots - 1) % kFwdSlots) * rec + 6 * mlp;
+            const float* hp1 = ring + ((t + 1) % kFwdSlots) * rec + 6 * mlp;
+            const int p0 = spst[t];
+            const int lp = spst[t + 1] - p0;
+            const int q = stpos[t * ni + io] + jo - p0;             // rank in plane t
+            const int pm = t > 0 ? spst[t - 1] : 0, pp = t + 1 < nm ? spst[t + 1] : 0;
+            float lap = 0.f;
+            if (!hz) {
+                const float hc = hcur[q];
+                const float hkm = ko > 0 ? hm1[stpos[(t - 1) * ni + io] + jo - pm] : hzm[fidx_z(s, jo, io)];
+                const float hkp = ko < nk - 1 ? hp1[stpos[(t + 1) * ni + io] + jo - pp] : hzp[fidx_z(s, jo, io)];
+                const float hjm = jo > 0 ? hm1[stpos[(t - 1) * ni + io] + jo - 1 - pm] : hym[fidx_y(s, ko, io)];
+                const float hjp = jo < nj - 1 ? hp1[stpos[(t + 1) * ni + io] + jo + 1 - pp] : hyp[fidx_y(s, ko, io)];
+                const float him = io > 0 ? hm1[stpos[(t - 1) * ni + io - 1] + jo - pm] : hxm[fidx_x(s, ko, jo)];
+                const float hip = io < ni - 1 ? hp1[stpos[(t + 1) * ni + io + 1] + jo - pp] : hxp[fidx_x(s, ko, jo)];
+                lap = -aw * him - ae * hip - as * hjm - an * hjp - ab[k] * hkm - at[k] * hkp -
+                      c0[4 * lp + q] * hc;
+            }
+            const float rkm = ko > 0 ? rprev : rzm[fidx_z(s, jo, io)];
+            const float rjm = jo > 0 ? xr[(buf ^ 1) * xs + col - 1] : rym[fidx_y(s, ko, io)];
+            const float rim = io > 0 ? xr[(buf ^ 1) * xs + col - nj] : rxm[fidx_x(s, ko, jo)];
+            // block layout: [lw | ls | lb | lpr | ap] with stride lp
+            float r = (c0[5 * mlp + q] + lap) * c0[3 * lp + q];
+            r = r - c0[2 * lp + q] * rkm - c0[lp + q] * rjm - c0[q] * rim;
+            R[p0 + q] = r;
             if (io == 0) rw[0 * fs + fidx_x(s, ko, jo)] = r;
             if (io == ni - 1) rw[1 * fs + fidx_x(s, ko, jo)] = r;
             if (jo == 0) rw[2 * fs + fidx_y(s, ko, io)] = r;
@@ -152,63 +267,135 @@ __global__ void __launch_bounds__(576) k_sip_fwd(FwdArgs a) {
             if (ko == 0) rw[4 * fs + fidx_z(s, jo, io)] = r;
             if (ko == nk - 1) rw[5 * fs + fidx_z(s, jo, io)] = r;
             rprev = r;
-            xr[buf][col] = r;
+            xr[buf * xs + col] = r;
         }
-        // slide the own-column hilf window to virtual k + 1
-        hm = hc;
-        hc = hp;
-        const int kn = kv + 2;
-        hp = hwin(kn);
+        __syncthreads();
+        // slot of plane t-1 is free now; refill it with plane t+kLook+1
+        if (tid == 0 && !sbad) {
+            proxy_fence();
+            issue(t + kLook + 1);
+        }
+    }
+    __syncthreads();
+    if (tid == 0 && sbad) {
+        // error path: let every copy still in flight land before the CTA exits
+        bar_wait(gbar, 0);
+        for (int r = done + 1; r <= issued; ++r)
+            if (!bar_wait(&bars[r % kFwdSlots], (r / kFwdSlots) & 1)) break;
+        atomicExch(&a.ctl[2], 1);
     }
 }
 
 struct BwdArgs {
-    SipShape s;
+    Shape s;
     const int* fnbr;
     const int* gcls;
-    float* H;                   // plane order, updated: h += res
-    float* HOUT;                // [ngrid][6][fs], written
-    const float* R;             // forward results, plane order
+    float* H;                   // padded plane order, updated: h += res
+    float* HOUT;
+    const float* R;             // forward results
     const float* RHI;           // res face buffers of this iteration (high ghosts)
-    const float *UE, *UN, *UT;
-    const int* conv;
-    int hzero;                  // first inner iteration: old hilf == 0
+    const float* CB;            // class blocks: per plane [ue|un|ut] x Lp
+    int* ctl;
+    int hzero;
 };
 
-__global__ void __launch_bounds__(576) k_sip_bwd(BwdArgs a) {
-    if (*a.conv) return;
-    const SipShape s = a.s;
-    const int nj = s.nj, ni = s.ni, nk = s.nk, npts = s.npts, fs = s.fs;
-    __shared__ float xr[2][576];
+__global__ void __launch_bounds__(kMaxCols) k_sip_bwd(BwdArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(128) unsigned char smraw[];
+    const Shape s = a.s;
+    const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm, mlp = s.maxlp;
+    const int rec = 5 * mlp;
+    float* ring = reinterpret_cast<float*>(smraw);
+    int* stpos = reinterpret_cast<int*>(ring + kBwdSlots * rec);
+    int* spst = stpos + nm * ni;
+    const int xs = blockDim.x;
+    float* xr = reinterpret_cast<float*>(spst + nm + 1);            // [2][xs]
+    float* gr = reinterpret_cast<float*>(((size_t)(xr + 2 * xs) + 15) & ~(size_t)15);   // [3][fs]
+    unsigned long long* bars =
+        reinterpret_cast<unsigned long long*>(((size_t)(gr + 3 * fs) + 15) & ~(size_t)15);
+    unsigned long long* gbar = bars + kBwdSlots;
     const int g = blockIdx.x;
-    const int col = threadIdx.x;
+    const int tid = threadIdx.x;
+    const long long base = (long long)g * s.npp;
+    const float* CB = a.CB + (long long)a.gcls[g] * 3 * s.npp;
+    const bool hz = a.hzero != 0;
+    __shared__ int sbad;
+    for (int q = tid; q < nm * ni; q += blockDim.x) stpos[q] = s.tpos[q];
+    for (int q = tid; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
+    if (tid == 0) {
+        sbad = 0;
+        for (int q = 0; q <= kBwdSlots; ++q) bar_init(&bars[q], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const int* fn = a.fnbr + 6 * g;
+    if (tid == 0) {   // high res ghosts: the +x, +y, +z neighbours' low planes
+        const unsigned fb = (unsigned)fs * 4u;
+        bar_expect(gbar, 3u * fb);
+        bulk_load(gr + 0 * fs, a.RHI + ((long long)fn[1] * 6 + 0) * fs, fb, gbar);
+        bulk_load(gr + 1 * fs, a.RHI + ((long long)fn[3] * 6 + 2) * fs, fb, gbar);
+        bulk_load(gr + 2 * fs, a.RHI + ((long long)fn[5] * 6 + 4) * fs, fb, gbar);
+    }
+    int issued = -1;
+    // record r (step r) = plane nm-1-r
+    auto issue = [&](int r) {
+        if (r >= nm) return;
+        issued = r;
+        const int m = nm - 1 - r;
+        const int sl = r % kBwdSlots;
+        const int p0 = spst[m], lp = spst[m + 1] - p0;
+        float* d = ring + sl * rec;
+        const unsigned b3 = 3u * lp * 4u, b1 = (unsigned)lp * 4u;
+        bar_expect(&bars[sl], b3 + b1 + (hz ? 0u : b1));
+        bulk_load(d, CB + 3LL * p0, b3, &bars[sl]);
+        bulk_load(d + 3 * mlp, a.R + base + p0, b1, &bars[sl]);
+        if (!hz) bulk_load(d + 4 * mlp, a.H + base + p0, b1, &bars[sl]);
+    };
+    if (tid == 0)
+        for (int r = 0; r < kLook; ++r) issue(r);
+    const int col = tid;
     const bool on = col < ni * nj;
     const int jo = on ? col % nj : 0, io = on ? col / nj : 0;
     const int jr = nj - 1 - jo, ir = ni - 1 - io;
-    const long long base = (long long)g * npts;
-    const long long cb = (long long)a.gcls[g] * npts;
-    float* H = a.H + base;
-    const float* R = a.R + base;
-    const float *ue = a.UE + cb, *un = a.UN + cb, *ut = a.UT + cb;
-    const int* fn = a.fnbr + 6 * g;
-    const float* rxp = a.RHI + ((long long)fn[1] * 6 + 0) * fs;   // +x nbr, its x-low plane
-    const float* ryp = a.RHI + ((long long)fn[3] * 6 + 2) * fs;
-    const float* rzp = a.RHI + ((long long)fn[5] * 6 + 4) * fs;
+    const float *rxp = gr, *ryp = gr + fs, *rzp = gr + 2 * fs;
     float* hw = a.HOUT + (long long)g * 6 * fs;
-    const int nsteps = ni + nj + nk - 2;
+    float* H = a.H + base;
+    bool bad = false;
+    if (!bar_wait(gbar, 0)) {
+        bad = true;
+        atomicOr(&sbad, 1);
+    }
+    int done = -1;
     float rprev = 0.f;
-    for (int t = 0; t < nsteps; ++t) {
-        const int kr = t - ir - jr;
+    for (int t = 0; t < nm; ++t) {
+        if (tid == 0 && !sbad) {
+            proxy_fence();
+            issue(t + kLook);   // slot of step t-1, released by the barrier below last step
+        }
+        if (!bad && !*(volatile int*)&sbad) {
+            if (bar_wait(&bars[t % kBwdSlots], (t / kBwdSlots) & 1)) {
+                done = t;
+            } else {
+                bad = true;
+                atomicOr(&sbad, 1);
+            }
+        }
         const int buf = t & 1;
-        if (on && kr >= 0 && kr < nk) {
+        const int kr = t - ir - jr;
+        if (on && !bad && kr >= 0 && kr < nk) {
             const int ko = nk - 1 - kr;
-            const int pc = s.tpos[(io + jo + ko) * ni + io] + jo;
+            const int m = nm - 1 - t;
+            const int p0 = spst[m];
+            const int lp = spst[m + 1] - p0;
+            const int q = stpos[m * ni + io] + jo - p0;
+            const float* c0 = ring + (t % kBwdSlots) * rec;
             const float rkp = kr > 0 ? rprev : rzp[fidx_z(s, jo, io)];
-            const float rjp = jo < nj - 1 ? xr[buf ^ 1][col + 1] : ryp[fidx_y(s, ko, io)];
-            const float rip = io < ni - 1 ? xr[buf ^ 1][col + nj] : rxp[fidx_x(s, ko, jo)];
-            const float r = R[pc] - ut[pc] * rkp - un[pc] * rjp - ue[pc] * rip;
-            const float h = (a.hzero ? 0.f : H[pc]) + r;
-            H[pc] = h;
+            const float rjp = jo < nj - 1 ? xr[(buf ^ 1) * xs + col + 1] : ryp[fidx_y(s, ko, io)];
+            const float rip = io < ni - 1 ? xr[(buf ^ 1) * xs + col + nj] : rxp[fidx_x(s, ko, jo)];
+            // block layout: [ue | un | ut] with stride lp
+            const float r = c0[3 * mlp + q] - c0[2 * lp + q] * rkp - c0[lp + q] * rjp - c0[q] * rip;
+            const float h = (hz ? 0.f : c0[4 * mlp + q]) + r;
+            H[p0 + q] = h;
             if (io == 0) hw[0 * fs + fidx_x(s, ko, jo)] = h;
             if (io == ni - 1) hw[1 * fs + fidx_x(s, ko, jo)] = h;
             if (jo == 0) hw[2 * fs + fidx_y(s, ko, io)] = h;
@@ -216,9 +403,15 @@ __global__ void __launch_bounds__(576) k_sip_bwd(BwdArgs a) {
             if (ko == 0) hw[4 * fs + fidx_z(s, jo, io)] = h;
             if (ko == nk - 1) hw[5 * fs + fidx_z(s, jo, io)] = h;
             rprev = r;
-            xr[buf][col] = r;
+            xr[buf * xs + col] = r;
         }
         __syncthreads();
+    }
+    if (tid == 0 && sbad) {
+        bar_wait(gbar, 0);
+        for (int r = done + 1; r <= issued; ++r)
+            if (!bar_wait(&bars[r % kBwdSlots], (r / kBwdSlots) & 1)) break;
+        atomicExch(&a.ctl[2], 1);
     }
 }
 
@@ -236,32 +429,32 @@ __device__ __forceinline__ double block_max2(double v, double* sh) {
 }
 
 struct OuterArgs {
-    SipShape s;
+    Shape s;
     const int* fnbr;
     const int* gcls;
-    const int* idx;             // plane position -> natural local index
+    const int* idxp;            // padded position -> natural local index, -1 for padding
     const float* H;
     const float* HOUT;
-    double* RHS64;              // plane order
+    double* RHS64;
     float* RHS32;
-    double* DP64;               // plane order
-    const double* AP64;         // class, plane order
+    double* DP64;
+    const double* AP64;         // class, padded plane order
     const double *AW, *AE, *AS, *AN, *AB, *AT;
     const DevGrid* grids;
     double* gridmax;
-    const int* conv;
+    const int* ctl;
 };
 
 // Outer step in FP64 (laplacephi + rescal + maxabscal_grid + accumulate_pcorr).
 __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
-    if (*a.conv) return;
+    if (a.ctl[0]) return;
     __shared__ double sh[32];
-    const SipShape s = a.s;
+    const Shape s = a.s;
     const int kk = s.kk, jj = s.jj, nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs;
     const int g = blockIdx.x;
     const DevGrid G = a.grids[g];
-    const long long base = (long long)g * s.npts;
-    const long long cb = (long long)a.gcls[g] * s.npts;
+    const long long base = (long long)g * s.npp;
+    const long long cb = (long long)a.gcls[g] * s.npp;
     const float* H = a.H + base;
     const int* fn = a.fnbr + 6 * g;
     const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;
@@ -272,8 +465,9 @@ __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
     const float* hzp = a.HOUT + ((long long)fn[5] * 6 + 4) * fs;
     auto pos = [&](int ko, int jo, int io) { return s.tpos[(io + jo + ko) * ni + io] + jo; };
     double mx = 0.0;
-    for (int q = threadIdx.x; q < s.npts; q += blockDim.x) {
-        const int id = a.idx[q];
+    for (int q = threadIdx.x; q < s.npp; q += blockDim.x) {
+        const int id = a.idxp[q];
+        if (id < 0) continue;
         const int k = id % kk + 1, j = (id / kk) % jj + 1, i = id / (kk * jj) + 1;
         const int ko = k - 3, jo = j - 3, io = i - 3;
         const double hc = H[q];
@@ -298,34 +492,104 @@ __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
 }
 
 // divcal into the plane-ordered FP64/FP32 residual (noib_mod.F90:304-354)
-__global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npts, const int* __restrict__ idx,
+__global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const int* __restrict__ idxp,
                              double* __restrict__ RHS64, float* __restrict__ RHS32,
                              const double* __restrict__ U, const double* __restrict__ V,
                              const double* __restrict__ W, const double* __restrict__ RDDX,
                              const double* __restrict__ RDDY, const double* __restrict__ RDDZ,
                              double fak) {
     const int g = blockIdx.y;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= npp) return;
+    const long long o = (long long)g * npp + q;
+    const int id = idxp[q];
+    if (id < 0) {       // padding stays zero for the bulk copies
+        RHS64[o] = 0.0;
+        RHS32[o] = 0.f;
+        return;
+    }
     const DevGrid G = grids[g];
     const int kk = G.kk, jj = G.jj;
-    const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= npts) return;
-    const int id = idx[q];
     const int k = id % kk + 1, j = (id / kk) % jj + 1, i = id / (kk * jj) + 1;
     const double *u = U + G.ip3, *v = V + G.ip3, *w = W + G.ip3;
     const double d = fak * ((u[id] - u[id - kk * jj]) * RDDX[G.ipx + i - 1] +
                             (v[id] - v[id - kk]) * RDDY[G.ipy + j - 1] +
                             (w[id] - w[id - 1]) * RDDZ[G.ipz + k - 1]);
-    RHS64[(long long)g * npts + q] = d;
-    RHS32[(long long)g * npts + q] = (float)d;
+    RHS64[o] = d;
+    RHS32[o] = (float)d;
 }
 
 // dp (plane order) -> DP field (natural layout, interior)
-__global__ void k_sip_scatter(const DevGrid* __restrict__ grids, int npts, const int* __restrict__ idx,
+__global__ void k_sip_scatter(const DevGrid* __restrict__ grids, int npp, const int* __restrict__ idxp,
                               const double* __restrict__ DP64, double* __restrict__ DP) {
     const int g = blockIdx.y;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= npts) return;
-    DP[grids[g].ip3 + idx[q]] = DP64[(long long)g * npts + q];
+    if (q >= npp) return;
+    const int id = idxp[q];
+    if (id >= 0) DP[grids[g].ip3 + id] = DP64[(long long)g * npp + q];
+}
+
+// class coefficients (FP64 fields of a representative grid, plane order of
+// the reference's hyperplane solver or natural order of the classic one)
+// -> padded FP32 blocks [lw|ls|lb|lpr|ap], [ue|un|ut] and padded FP64 ap
+__global__ void k_sip_extract(const DevGrid* __restrict__ grids, const int* __restrict__ reps,
+                              const int* __restrict__ qmap, const int* __restrict__ idx,
+                              const int* __restrict__ pst, int nm, int npp, int planeorder,
+                              const double* __restrict__ lw, const double* __restrict__ ls,
+                              const double* __restrict__ lb, const double* __restrict__ lpr,
+                              const double* __restrict__ ue, const double* __restrict__ un,
+                              const double* __restrict__ ut, const double* __restrict__ ap,
+                              float* CF, float* CB, double* AP64) {
+    const int cls = blockIdx.y;
+    const int qp = blockIdx.x * blockDim.x + threadIdx.x;
+    if (qp >= npp) return;
+    // plane of padded position qp
+    int m = 0;
+    while (m + 1 <= nm && pst[m + 1] <= qp) ++m;
+    const int p0 = pst[m], lp = pst[m + 1] - p0, rnk = qp - p0;
+    float* cf = CF + (long long)cls * 5 * npp + 5LL * p0;
+    float* cb = CB + (long long)cls * 3 * npp + 3LL * p0;
+    double* ap64 = AP64 + (long long)cls * npp;
+    const int q = qmap[qp];   // unpadded plane position, -1 for padding
+    if (q < 0) {
+        for (int f = 0; f < 5; ++f) cf[f * lp + rnk] = 0.f;
+        for (int f = 0; f < 3; ++f) cb[f * lp + rnk] = 0.f;
+        ap64[qp] = 0.0;
+        return;
+    }
+    const DevGrid G = grids[reps[cls]];
+    const int id = idx[q];
+    const long long src = G.ip3 + (planeorder ? q : id);
+    cf[0 * lp + rnk] = (float)lw[src];
+    cf[1 * lp + rnk] = (float)ls[src];
+    cf[2 * lp + rnk] = (float)lb[src];
+    cf[3 * lp + rnk] = (float)lpr[src];
+    cf[4 * lp + rnk] = (float)ap[G.ip3 + id];
+    cb[0 * lp + rnk] = (float)ue[src];
+    cb[1 * lp + rnk] = (float)un[src];
+    cb[2 * lp + rnk] = (float)ut[src];
+    ap64[qp] = ap[G.ip3 + id];
+}
+
+Shape shape(const SipState& st) {
+    Shape s;
+    s.kk = st.kk; s.jj = st.jj; s.ii = st.ii; s.ni = st.ni; s.nj = st.nj; s.nk = st.nk;
+    s.nm = st.nm; s.npp = st.npp; s.fs = st.fs; s.maxlp = st.maxlp;
+    s.tpos = st.d_tpos; s.pst = st.d_pst;
+    return s;
+}
+
+int sweep_threads(const SipState& st) { return (st.ni * st.nj + 31) / 32 * 32; }
+
+size_t fwd_smem(const SipState& st) {
+    return (size_t)kFwdSlots * 7 * st.maxlp * 4 + (size_t)(st.nm * st.ni + st.nm + 1) * 4 +
+           (size_t)2 * sweep_threads(st) * 4 + 16 + (size_t)9 * st.fs * 4 + (size_t)2 * st.kk * 4 + 16 +
+           (kFwdSlots + 1) * 8;
+}
+
+size_t bwd_smem(const SipState& st) {
+    return (size_t)kBwdSlots * 5 * st.maxlp * 4 + (size_t)(st.nm * st.ni + st.nm + 1) * 4 +
+           (size_t)2 * sweep_threads(st) * 4 + 16 + (size_t)3 * st.fs * 4 + 16 + (kBwdSlots + 1) * 8;
 }
 
 }  // namespace
@@ -335,28 +599,56 @@ int sip_init(Ctx* c, SipState& st) {
     st.kk = G0.kk; st.jj = G0.jj; st.ii = G0.ii;
     st.nk = G0.kk - 4; st.nj = G0.jj - 4; st.ni = G0.ii - 4;
     st.npts = st.ni * st.nj * st.nk;
-    st.fs = std::max(st.nj * st.nk, std::max(st.ni * st.nk, st.ni * st.nj));
-    if (st.ni * st.nj > 576) {
-        set_error("mixed form: at most 576 (j, i) columns per grid");
+    // face buffers are copied whole with cp.async.bulk: a multiple of 16 bytes
+    st.fs = (std::max(st.nj * st.nk, std::max(st.ni * st.nk, st.ni * st.nj)) + 3) & ~3;
+    st.nm = st.ni + st.nj + st.nk - 2;
+    if (st.ni * st.nj > kMaxCols) {
+        set_error("mixed form: at most 1024 (j, i) columns per grid");
         return MGLET_ERR_UNSUPPORTED;
     }
-    // plane positions: pos(m0, io, jo) = tpos[m0*ni + io] + jo
-    const int nm = st.ni + st.nj + st.nk - 2;
-    std::vector<int> tpos((size_t)(nm + 1) * st.ni, 0);
-    int p = 0;
-    for (int m0 = 0; m0 < nm; ++m0)
+    // padded plane starts, position table, padded -> natural index map
+    std::vector<int> pst(st.nm + 1, 0), tpos((size_t)st.nm * st.ni, 0);
+    std::vector<int> plen(st.nm, 0);
+    for (int m0 = 0; m0 < st.nm; ++m0) {
+        int cnt = 0;
+        for (int io = 0; io < st.ni; ++io) {
+            const int jlo = std::max(0, m0 - io - (st.nk - 1));
+            const int jhi = std::min(st.nj - 1, m0 - io);
+            if (jhi >= jlo) cnt += jhi - jlo + 1;
+        }
+        plen[m0] = cnt;
+        pst[m0 + 1] = pst[m0] + ((cnt + 3) & ~3);
+        st.maxlp = std::max(st.maxlp, (cnt + 3) & ~3);
+    }
+    st.npp = pst[st.nm];
+    std::vector<int> idxp(st.npp, -1), qmap(st.npp, -1);
+    int q = 0;   // unpadded position (the reference's iacc - 1)
+    for (int m0 = 0; m0 < st.nm; ++m0) {
+        int p = pst[m0];
         for (int io = 0; io < st.ni; ++io) {
             const int jlo = std::max(0, m0 - io - (st.nk - 1));
             const int jhi = std::min(st.nj - 1, m0 - io);
             tpos[(size_t)m0 * st.ni + io] = p - jlo;
-            if (jhi >= jlo) p += jhi - jlo + 1;
+            for (int jo = jlo; jo <= jhi; ++jo, ++p, ++q) {
+                const int ko = m0 - io - jo;
+                idxp[p] = (ko + 2) + (jo + 2) * st.kk + (io + 2) * st.kk * st.jj;
+                qmap[p] = q;
+            }
         }
-    if (p != st.npts) {
-        set_error("mixed form: hyperplane position table does not cover the grid");
+    }
+    if (q != st.npts) {
+        set_error("mixed form: hyperplane tables do not cover the grid");
         return MGLET_ERR_ARG;
     }
-    MG_CUDA(cudaMalloc(&st.d_tpos, tpos.size() * sizeof(int)));
-    MG_CUDA(cudaMemcpy(st.d_tpos, tpos.data(), tpos.size() * sizeof(int), cudaMemcpyHostToDevice));
+    auto up = [](int** d, const std::vector<int>& h) -> int {
+        MG_CUDA(cudaMalloc(d, h.size() * sizeof(int)));
+        MG_CUDA(cudaMemcpy(*d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+        return 0;
+    };
+    if (int rc = up(&st.d_tpos, tpos)) return rc;
+    if (int rc = up(&st.d_pst, pst)) return rc;
+    if (int rc = up(&st.d_idxp, idxp)) return rc;
+    if (int rc = up(&st.d_qmap, qmap)) return rc;
     // face neighbours from the connection table (regular periodic tiling)
     std::vector<int> fn((size_t)6 * c->ngrid, -1);
     for (size_t r = 0; r < c->conns.size(); r += 4) {
@@ -374,16 +666,15 @@ int sip_init(Ctx* c, SipState& st) {
             set_error("mixed form: every face needs a CON neighbour");
             return MGLET_ERR_UNSUPPORTED;
         }
-    MG_CUDA(cudaMalloc(&st.d_fnbr, fn.size() * sizeof(int)));
-    MG_CUDA(cudaMemcpy(st.d_fnbr, fn.data(), fn.size() * sizeof(int), cudaMemcpyHostToDevice));
-    const size_t n = (size_t)c->ngrid * st.npts;
-    for (float** q : {&st.h32, &st.r32, &st.rhs32}) {
-        MG_CUDA(cudaMalloc(q, n * sizeof(float)));
-        MG_CUDA(cudaMemset(*q, 0, n * sizeof(float)));
+    if (int rc = up(&st.d_fnbr, fn)) return rc;
+    const size_t n = (size_t)c->ngrid * st.npp;
+    for (float** p : {&st.h32, &st.r32, &st.rhs32}) {
+        MG_CUDA(cudaMalloc(p, n * sizeof(float)));
+        MG_CUDA(cudaMemset(*p, 0, n * sizeof(float)));
     }
-    for (double** q : {&st.rhs64, &st.dp64}) {
-        MG_CUDA(cudaMalloc(q, n * sizeof(double)));
-        MG_CUDA(cudaMemset(*q, 0, n * sizeof(double)));
+    for (double** p : {&st.rhs64, &st.dp64}) {
+        MG_CUDA(cudaMalloc(p, n * sizeof(double)));
+        MG_CUDA(cudaMemset(*p, 0, n * sizeof(double)));
     }
     const size_t nf = (size_t)c->ngrid * 6 * st.fs;
     MG_CUDA(cudaMalloc(&st.hout, nf * sizeof(float)));
@@ -395,44 +686,59 @@ int sip_init(Ctx* c, SipState& st) {
     // FP32 copies of the 1-D Poisson coefficients
     const char* n1[6] = {"GSAW", "GSAE", "GSAS", "GSAN", "GSAB", "GSAT"};
     const long long len[6] = {c->idimx, c->idimx, c->idimy, c->idimy, c->idimz, c->idimz};
-    for (int q = 0; q < 6; ++q) {
-        std::vector<double> h(len[q]);
-        MG_CUDA(cudaMemcpy(h.data(), c->L(n1[q]), len[q] * sizeof(double), cudaMemcpyDeviceToHost));
+    for (int qq = 0; qq < 6; ++qq) {
+        std::vector<double> h(len[qq]);
+        MG_CUDA(cudaMemcpy(h.data(), c->L(n1[qq]), len[qq] * sizeof(double), cudaMemcpyDeviceToHost));
         std::vector<float> f(h.begin(), h.end());
-        MG_CUDA(cudaMalloc(&st.a1[q], len[q] * sizeof(float)));
-        MG_CUDA(cudaMemcpy(st.a1[q], f.data(), len[q] * sizeof(float), cudaMemcpyHostToDevice));
+        MG_CUDA(cudaMalloc(&st.a1[qq], len[qq] * sizeof(float)));
+        MG_CUDA(cudaMemcpy(st.a1[qq], f.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
     }
+    const size_t smf = fwd_smem(st), smb = bwd_smem(st);
+    if (smf > 200 * 1024 || smb > 200 * 1024) {
+        set_error("mixed form: hyperplane ring buffers exceed shared memory");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    MG_CUDA(cudaFuncSetAttribute(k_sip_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
+    MG_CUDA(cudaFuncSetAttribute(k_sip_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+    return 0;
+}
+
+int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* d_idx,
+                bool planeorder, float** cf, float** cb, double** ap64) {
+    const size_t n = (size_t)nclass * st.npp;
+    MG_CUDA(cudaMalloc(cf, 5 * n * sizeof(float)));
+    MG_CUDA(cudaMalloc(cb, 3 * n * sizeof(float)));
+    MG_CUDA(cudaMalloc(ap64, n * sizeof(double)));
+    dim3 grid((st.npp + 255) / 256, nclass);
+    k_sip_extract<<<grid, 256, 0, c->stream>>>(
+        c->d_grids, d_reps, st.d_qmap, d_idx, st.d_pst, st.nm, st.npp, planeorder ? 1 : 0,
+        c->F("SIPLW"), c->F("SIPLS"), c->F("SIPLB"), c->F("SIPLPR"), c->F("SIPUE"), c->F("SIPUN"),
+        c->F("SIPUT"), c->F("GSAP"), *cf, *cb, *ap64);
+    MG_LAUNCHED(c);
     return 0;
 }
 
 void sip_release(SipState& st) {
-    for (void* p : {(void*)st.d_tpos, (void*)st.d_fnbr, (void*)st.h32, (void*)st.r32,
-                    (void*)st.rhs32, (void*)st.rhs64, (void*)st.dp64, (void*)st.hout,
-                    (void*)st.rout[0], (void*)st.rout[1], (void*)st.rout[2], (void*)st.a1[0],
-                    (void*)st.a1[1], (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4],
-                    (void*)st.a1[5]})
+    for (void* p : {(void*)st.d_tpos, (void*)st.d_pst, (void*)st.d_idxp, (void*)st.d_qmap,
+                    (void*)st.d_fnbr, (void*)st.h32, (void*)st.r32, (void*)st.rhs32,
+                    (void*)st.rhs64, (void*)st.dp64, (void*)st.hout, (void*)st.rout[0],
+                    (void*)st.rout[1], (void*)st.rout[2], (void*)st.a1[0], (void*)st.a1[1],
+                    (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5]})
         cudaFree(p);
 }
 
-static SipShape shape(const SipState& st) {
-    SipShape s;
-    s.kk = st.kk; s.jj = st.jj; s.ii = st.ii; s.ni = st.ni; s.nj = st.nj; s.nk = st.nk;
-    s.npts = st.npts; s.fs = st.fs; s.tpos = st.d_tpos;
-    return s;
-}
-
-int sip_divcal(Ctx* c, SipState& st, const int* idx, double fak) {
+int sip_divcal(Ctx* c, SipState& st, double fak) {
     ProfScope ps_(c, "mx_divcal");
-    dim3 grid((st.npts + 255) / 256, c->ngrid);
-    k_sip_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npts, idx, st.rhs64, st.rhs32,
+    dim3 grid((st.npp + 255) / 256, c->ngrid);
+    k_sip_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.rhs64, st.rhs32,
                                               c->F("U"), c->F("V"), c->F("W"), c->L("RDDX"),
                                               c->L("RDDY"), c->L("RDDZ"), fak);
     MG_LAUNCHED(c);
     return 0;
 }
 
-int sip_forward(Ctx* c, SipState& st, const SipCoef& cf, const int* gcls, const int* conv,
-                int rlow, int rwrite, bool hzero) {
+int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
+                int rwrite, bool hzero) {
     ProfScope ps_(c, "mx_sip_fwd");
     FwdArgs a;
     a.s = shape(st);
@@ -441,56 +747,55 @@ int sip_forward(Ctx* c, SipState& st, const SipCoef& cf, const int* gcls, const 
     a.HOUT = st.hout;
     a.RLOW = rlow >= 0 ? st.rout[rlow] : nullptr;
     a.RW = st.rout[rwrite];
-    a.LW = cf.lw; a.LS = cf.ls; a.LB = cf.lb; a.LPR = cf.lpr; a.AP = cf.ap;
+    a.CF = cf;
     a.AW = st.a1[0]; a.AE = st.a1[1]; a.AS = st.a1[2]; a.AN = st.a1[3]; a.AB = st.a1[4];
     a.AT = st.a1[5];
     a.grids = c->d_grids;
-    a.conv = conv;
+    a.ctl = ctl;
     a.hzero = hzero ? 1 : 0;
-    const int threads = (st.ni * st.nj + 31) / 32 * 32;
-    k_sip_fwd<<<c->ngrid, threads, 0, c->stream>>>(a);
+    const int threads = sweep_threads(st);
+    k_sip_fwd<<<c->ngrid, threads, fwd_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }
 
-int sip_backward(Ctx* c, SipState& st, const SipCoef& cf, const int* gcls, const int* conv,
-                 int rhi, bool hzero) {
+int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ctl, int rhi,
+                 bool hzero) {
     ProfScope ps_(c, "mx_sip_bwd");
     BwdArgs a;
     a.s = shape(st);
     a.fnbr = st.d_fnbr; a.gcls = gcls;
     a.H = st.h32; a.HOUT = st.hout; a.R = st.r32; a.RHI = st.rout[rhi];
-    a.UE = cf.ue; a.UN = cf.un; a.UT = cf.ut;
-    a.conv = conv;
+    a.CB = cb;
+    a.ctl = ctl;
     a.hzero = hzero ? 1 : 0;
-    const int threads = (st.ni * st.nj + 31) / 32 * 32;
-    k_sip_bwd<<<c->ngrid, threads, 0, c->stream>>>(a);
+    const int threads = sweep_threads(st);
+    k_sip_bwd<<<c->ngrid, threads, bwd_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }
 
-int sip_outer(Ctx* c, SipState& st, const int* idx, const double* ap64, const int* gcls,
-              const int* conv) {
+int sip_outer(Ctx* c, SipState& st, const double* ap64, const int* gcls, const int* ctl) {
     ProfScope ps_(c, "mx_outer");
     OuterArgs a;
     a.s = shape(st);
-    a.fnbr = st.d_fnbr; a.gcls = gcls; a.idx = idx;
+    a.fnbr = st.d_fnbr; a.gcls = gcls; a.idxp = st.d_idxp;
     a.H = st.h32; a.HOUT = st.hout;
     a.RHS64 = st.rhs64; a.RHS32 = st.rhs32; a.DP64 = st.dp64; a.AP64 = ap64;
     a.AW = c->L("GSAW"); a.AE = c->L("GSAE"); a.AS = c->L("GSAS"); a.AN = c->L("GSAN");
     a.AB = c->L("GSAB"); a.AT = c->L("GSAT");
     a.grids = c->d_grids;
     a.gridmax = c->d_gridred;
-    a.conv = conv;
+    a.ctl = ctl;
     k_sip_outer<<<c->ngrid, 512, 0, c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }
 
-int sip_scatter_dp(Ctx* c, SipState& st, const int* idx) {
+int sip_scatter_dp(Ctx* c, SipState& st) {
     ProfScope ps_(c, "mx_scatter");
-    dim3 grid((st.npts + 255) / 256, c->ngrid);
-    k_sip_scatter<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npts, idx, st.dp64, c->F("DP"));
+    dim3 grid((st.npp + 255) / 256, c->ngrid);
+    k_sip_scatter<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.dp64, c->F("DP"));
     MG_LAUNCHED(c);
     return 0;
 }

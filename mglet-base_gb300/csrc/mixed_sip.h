@@ -5,30 +5,35 @@
 
 namespace mg {
 
-struct SipCoef {   // FP32 class coefficients, plane order [nclass][npts]
-    const float *lw, *ls, *lb, *lpr, *ue, *un, *ut, *ap;
-};
-
 struct SipState {
     int kk = 0, jj = 0, ii = 0, ni = 0, nj = 0, nk = 0, npts = 0, fs = 0;
-    int* d_tpos = nullptr;      // plane position table
+    int nm = 0;                 // hyperplanes per grid
+    int npp = 0;                // points per grid with every plane padded to 4 floats
+    int maxlp = 0;              // longest padded plane
+    int* d_tpos = nullptr;      // [nm][ni] padded plane positions
+    int* d_pst = nullptr;       // [nm+1] padded plane starts
+    int* d_idxp = nullptr;      // [npp] natural local index, -1 for padding
+    int* d_qmap = nullptr;      // [npp] unpadded plane position (iacc-1), -1 for padding
     int* d_fnbr = nullptr;      // [ngrid][6] face neighbours (0-based)
-    float *h32 = nullptr, *r32 = nullptr, *rhs32 = nullptr;   // plane order
-    double *rhs64 = nullptr, *dp64 = nullptr;                 // plane order
+    float *h32 = nullptr, *r32 = nullptr, *rhs32 = nullptr;   // [ngrid][npp]
+    double *rhs64 = nullptr, *dp64 = nullptr;                 // [ngrid][npp]
     float* hout = nullptr;      // [ngrid][6][fs] hilf boundary planes
     float* rout[3] = {nullptr, nullptr, nullptr};   // rotating res boundary planes
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
 };
 
 int sip_init(Ctx* c, SipState& st);
+// Class coefficients: FP32 blocks [lw|ls|lb|lpr|ap] and [ue|un|ut] per padded
+// plane, FP64 ap, from the representative grid of each class.
+int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* d_idx,
+                bool planeorder, float** cf, float** cb, double** ap64);
 void sip_release(SipState& st);
-int sip_divcal(Ctx* c, SipState& st, const int* idx, double fak);
-int sip_forward(Ctx* c, SipState& st, const SipCoef& cf, const int* gcls, const int* conv,
-                int rlow, int rwrite, bool hzero);
-int sip_backward(Ctx* c, SipState& st, const SipCoef& cf, const int* gcls, const int* conv,
-                 int rhi, bool hzero);
-int sip_outer(Ctx* c, SipState& st, const int* idx, const double* ap64, const int* gcls,
-              const int* conv);
-int sip_scatter_dp(Ctx* c, SipState& st, const int* idx);
+int sip_divcal(Ctx* c, SipState& st, double fak);
+int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
+                int rwrite, bool hzero);
+int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ctl, int rhi,
+                 bool hzero);
+int sip_outer(Ctx* c, SipState& st, const double* ap64, const int* gcls, const int* ctl);
+int sip_scatter_dp(Ctx* c, SipState& st);
 
 }  // namespace mg
