@@ -41,7 +41,7 @@ struct MixedState {
     // class coefficients in padded plane order: FP32 blocks [lw|ls|lb|lpr|ap]
     // and [ue|un|ut], FP64 ap
     float *cf = nullptr, *cb = nullptr;
-    double* ap64 = nullptr;
+    float* apx = nullptr;      // class ap as two floats (outer step)
     SipState sip;
     const int* d_idx = nullptr;     // plane position -> natural local index (hp table)
     // FP32 2N-storage registers DU, DV, DW of the RK scheme (natural layout)
@@ -153,7 +153,7 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
             if (int rc = sip_backward(c, s, m->cb, m->d_gcls, ctl, gi % 3, hz)) return rc;
             if (iloop < ninner) lastfull = gi;
         }
-        if (int rc = sip_outer(c, s, m->ap64, m->d_gcls, ctl)) return rc;
+        if (int rc = sip_outer(c, s, m->apx, m->d_gcls, ctl)) return rc;
         {
             ProfScope ps_(c, "mx_conv");
             k_mx_conv<<<1, 1024, 0, c->stream>>>(c->d_grids, c->ngrid, c->maxlevel, c->d_gridred,
@@ -319,7 +319,7 @@ int mixed_init(Ctx* c) {
     MG_CUDA(cudaMalloc(&d_reps, reps.size() * sizeof(int)));
     MG_CUDA(cudaMemcpy(d_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
     int rc = sip_extract(c, m->sip, m->nclass, d_reps, m->d_idx,
-                         c->prm.psolver != MGLET_PSOLVER_CLASSIC, &m->cf, &m->cb, &m->ap64);
+                         c->prm.psolver != MGLET_PSOLVER_CLASSIC, &m->cf, &m->cb, &m->apx);
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (rc) {
         cudaFree(d_reps);
@@ -335,7 +335,7 @@ void mixed_release(Ctx* c) {
     if (!m) return;
     for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
     sip_release(m->sip);
-    for (void* p : {(void*)m->cf, (void*)m->cb, (void*)m->ap64, (void*)m->d_gcls,
+    for (void* p : {(void*)m->cf, (void*)m->cb, (void*)m->apx, (void*)m->d_gcls,
                     (void*)m->d_ctl, (void*)m->d_maxrhs, (void*)m->du32, (void*)m->dv32,
                     (void*)m->dw32, (void*)m->sx, (void*)m->sy, (void*)m->sz})
         cudaFree(p);

@@ -25,14 +25,19 @@
 //     the first inner iteration of an outer iteration starts from hilf = 0.
 // res face buffers rotate over three slots, which is enough for those reads.
 //
-// Column wavefront: one CTA per grid, one thread per (j, i) column; at step
-// t the thread is at k = t - (i-3) - (j-3) + 3, on hyperplane i+j+k = t+9.
-// res(k-1) stays in a register; res(j-1) and res(i-1) come through a
-// double-buffered shared-memory plane written one step earlier.
+// Point wavefront: one CTA per grid, one thread per point of the current
+// hyperplane i+j+k = t+9 (planes are at most 1024 points long).  Each plane
+// record carries a point table (io | jo << 10 | ko << 20) so a thread finds its
+// (i, j, k) without searching; the neighbours on planes t-1 and t+1 are
+// found through a per-plane row-offset table.  Only ceil(Lp/32) warps do
+// work in a step, instead of every warp holding a few columns on the band.
+// res of the previous plane comes from a double-buffered shared-memory plane.
 //
-// Every mbarrier wait is bounded: after kWaitLimit polls the kernel records
-// an error in the control block, stops computing, and still waits (bounded)
-// for the copies it has in flight before it exits.
+// Every mbarrier wait is bounded: after kWaitCycles SM clocks the kernel
+// records an error in the control block, stops computing, and still waits
+// (bounded) for the copies it has in flight before it exits.  Only thread 0
+// waits on the ring; the step's closing __syncthreads hands the landed data
+// and the error flag to the other threads.
 #include <algorithm>
 #include <vector>
 
@@ -45,7 +50,7 @@ namespace {
 constexpr int kFwdSlots = 6;   // planes t-1 .. t+4
 constexpr int kBwdSlots = 5;   // planes t .. t+4 (reverse order)
 constexpr int kLook = 4;       // records issued ahead of the wavefront
-constexpr int kMaxCols = 1024; // one thread per (j, i) column
+constexpr int kMaxCols = 1024; // one thread per hyperplane point
 // A wait gives up after this many SM clock cycles (about one second); a
 // healthy wait lasts microseconds.
 constexpr long long kWaitCycles = 2000000000LL;
@@ -54,6 +59,8 @@ struct Shape {
     int kk, jj, ii, ni, nj, nk, nm, npp, fs, maxlp;
     const int* tpos;   // [nm][ni]: padded position of (io, jo) in plane m0 is tpos[m0*ni+io] + jo
     const int* pst;    // [nm+1] padded plane starts
+    const short* rowoff;   // [nm][ni]: tpos - pst, the rank of (io, jo = 0) in its plane
+    const int* pq;     // [npp] point of each padded position: io | jo << 10 | ko << 20, -1 = padding
 };
 
 __device__ __forceinline__ int fidx_x(const Shape& s, int ko, int jo) { return ko + jo * s.nk; }
@@ -121,52 +128,125 @@ struct FwdArgs {
     int hzero;
 };
 
-// Shared memory of the forward sweep (dynamic): kFwdSlots records of
-// (coefficient block 5*maxlp | rhs maxlp | hilf maxlp), the plane tables,
-// the res exchange planes and the slot barriers.
+// Shared-memory carve-up common to both sweeps (byte offsets): the ring of
+// plane records, the plane starts, the row-offset table, the two res planes
+// of the recurrence, then the kernel's own tail (ghost faces, barriers).
+struct SweepLayout {
+    size_t pst, rowoff, xr, tail;
+};
+
+__host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+__host__ __device__ inline SweepLayout sweep_layout(int nm, int ni, int mlp, int slots, int rec) {
+    SweepLayout l;
+    l.pst = (size_t)slots * rec * 4;
+    l.rowoff = l.pst + (size_t)(nm + 1) * 4;
+    l.xr = align16(l.rowoff + (size_t)nm * ni * 2);
+    l.tail = l.xr + (size_t)2 * mlp * 4;
+    return l;
+}
+
+struct SweepSmem {
+    float* ring;
+    int* pst;                   // [nm+1] padded plane starts
+    short* rowoff;              // [nm][ni] rank of (io, jo = 0) in plane m
+    float* xr;                  // [2][maxlp]
+    float* tail;                // 16-byte aligned
+};
+
+__device__ __forceinline__ SweepSmem carve(unsigned char* raw, const Shape& s, int slots, int rec) {
+    const SweepLayout l = sweep_layout(s.nm, s.ni, s.maxlp, slots, rec);
+    SweepSmem m;
+    m.ring = reinterpret_cast<float*>(raw);
+    m.pst = reinterpret_cast<int*>(raw + l.pst);
+    m.rowoff = reinterpret_cast<short*>(raw + l.rowoff);
+    m.xr = reinterpret_cast<float*>(raw + l.xr);
+    m.tail = reinterpret_cast<float*>(raw + l.tail);
+    return m;
+}
+
+// Forward sweep, one thread per point of the current hyperplane.  A record
+// (one ring slot) holds plane r's coefficient block [lw|ls|lb|lpr|ap] (stride
+// Lp), its rhs, its hilf and its point table (io | jo << 10 | ko << 20,
+// -1 = padding).
+// Step t needs planes t-1, t and t+1; thread 0 refills the slot of plane t-2
+// with plane t+4 at the start of step t and waits for plane t+2 before the
+// step's closing barrier, so every other thread only meets __syncthreads.
 __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
     if (a.ctl[0]) return;
     extern __shared__ __align__(128) unsigned char smraw[];
     const Shape s = a.s;
     const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm, mlp = s.maxlp;
-    const int rec = 7 * mlp;   // floats per record
-    float* ring = reinterpret_cast<float*>(smraw);
-    int* stpos = reinterpret_cast<int*>(ring + kFwdSlots * rec);
-    int* spst = stpos + nm * ni;
-    const int xs = blockDim.x;
-    float* xr = reinterpret_cast<float*>(spst + nm + 1);            // [2][xs]
-    float* gh = reinterpret_cast<float*>(((size_t)(xr + 2 * xs) + 15) & ~(size_t)15);   // [6][fs]
-    float* gr = gh + 6 * fs;                                         // [3][fs]
-    float* sab = gr + 3 * fs;                                        // [kk]
-    float* sat = sab + s.kk;                                         // [kk]
+    const int rec = 8 * mlp;
+    const SweepSmem m = carve(smraw, s, kFwdSlots, rec);
+    float* gh = m.tail;                  // [6][fs] hilf ghosts
+    float* gr = gh + 6 * fs;             // [3][fs] low res ghosts
+    float* saw = gr + 3 * fs;            // [ii] each
+    float* sae = saw + s.ii;
+    float* sas = sae + s.ii;             // [jj] each
+    float* san = sas + s.jj;
+    float* sab = san + s.jj;             // [kk] each
+    float* sat = sab + s.kk;
     unsigned long long* bars =
         reinterpret_cast<unsigned long long*>(((size_t)(sat + s.kk) + 15) & ~(size_t)15);
-    unsigned long long* gbar = bars + kFwdSlots;                     // ghost faces
+    unsigned long long* gbar = bars + kFwdSlots;
     const int g = blockIdx.x;
     const int tid = threadIdx.x;
     const DevGrid G = a.grids[g];
     const long long base = (long long)g * s.npp;
     const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
     const bool hz = a.hzero != 0;
-    __shared__ int sbad;
-    for (int q = tid; q < nm * ni; q += blockDim.x) stpos[q] = s.tpos[q];
-    for (int q = tid; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
+    // error flag of step t in sflag[t & 1], written by thread 0 before the
+    // step's closing barrier and read by everyone after it; two slots so that
+    // thread 0 running ahead never overwrites a flag still being read
+    __shared__ int sflag[2];
+    for (int q = tid; q < nm * ni; q += blockDim.x) m.rowoff[q] = s.rowoff[q];
+    for (int q = tid; q <= nm; q += blockDim.x) m.pst[q] = s.pst[q];
+    for (int q = tid; q < s.ii; q += blockDim.x) {
+        saw[q] = a.AW[G.ipx + q];        // saw[i-1] = aw(i)
+        sae[q] = a.AE[G.ipx + q];
+    }
+    for (int q = tid; q < s.jj; q += blockDim.x) {
+        sas[q] = a.AS[G.ipy + q];
+        san[q] = a.AN[G.ipy + q];
+    }
     for (int q = tid; q < s.kk; q += blockDim.x) {
-        sab[q] = a.AB[G.ipz + q];      // sab[k-1] = ab(k)
+        sab[q] = a.AB[G.ipz + q];
         sat[q] = a.AT[G.ipz + q];
     }
     if (!a.RLOW)
         for (int q = tid; q < 3 * fs; q += blockDim.x) gr[q] = 0.f;
     if (tid == 0) {
-        sbad = 0;
+        sflag[0] = sflag[1] = 0;
         for (int q = 0; q <= kFwdSlots; ++q) bar_init(&bars[q], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
+    int issued = -1, waited = -1;   // thread 0's bookkeeping of the ring
+    int bad = 0;
+    auto issue = [&](int r) {
+        if (r >= nm) return;
+        issued = r;
+        const int sl = r % kFwdSlots;
+        const int p0 = m.pst[r], lp = m.pst[r + 1] - p0;
+        float* d = m.ring + sl * rec;
+        const unsigned b5 = 5u * lp * 4u, b1 = (unsigned)lp * 4u;
+        bar_expect(&bars[sl], b5 + 2u * b1 + (hz ? 0u : b1));
+        bulk_load(d, CF + 5LL * p0, b5, &bars[sl]);
+        bulk_load(d + 5 * mlp, a.RHS + base + p0, b1, &bars[sl]);
+        if (!hz) bulk_load(d + 6 * mlp, a.H + base + p0, b1, &bars[sl]);
+        bulk_load(d + 7 * mlp, s.pq + p0, b1, &bars[sl]);
+    };
+    auto wait_rec = [&](int r) -> bool {
+        if (r >= nm || r <= waited) return true;
+        if (!bar_wait(&bars[r % kFwdSlots], (r / kFwdSlots) & 1)) return false;
+        waited = r;
+        return true;
+    };
     const int* fn = a.fnbr + 6 * g;
-    // ghost faces: hilf of the six neighbours' facing planes (unless hilf is
-    // zero) and res of the three low neighbours (unless there is none yet)
+    __syncthreads();
     if (tid == 0) {
+        // ghost faces: hilf of the six neighbours' facing planes (unless hilf
+        // is zero) and res of the three low neighbours (unless none yet)
         const unsigned fb = (unsigned)fs * 4u;
         bar_expect(gbar, (hz ? 0u : 6u * fb) + (a.RLOW ? 3u * fb : 0u));
         if (!hz) {
@@ -179,108 +259,72 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
             bulk_load(gr + 1 * fs, a.RLOW + ((long long)fn[2] * 6 + 3) * fs, fb, gbar);
             bulk_load(gr + 2 * fs, a.RLOW + ((long long)fn[4] * 6 + 5) * fs, fb, gbar);
         }
-    }
-    int issued = -1;   // last record issued (thread 0)
-    // producer: record r = {coefficients, rhs, hilf} of plane r into slot r % kFwdSlots
-    auto issue = [&](int r) {
-        if (r >= nm) return;
-        issued = r;
-        const int sl = r % kFwdSlots;
-        const int p0 = spst[r], lp = spst[r + 1] - p0;
-        float* d = ring + sl * rec;
-        const unsigned b5 = 5u * lp * 4u, b1 = (unsigned)lp * 4u;
-        bar_expect(&bars[sl], b5 + b1 + (hz ? 0u : b1));
-        bulk_load(d, CF + 5LL * p0, b5, &bars[sl]);
-        bulk_load(d + 5 * mlp, a.RHS + base + p0, b1, &bars[sl]);
-        if (!hz) bulk_load(d + 6 * mlp, a.H + base + p0, b1, &bars[sl]);
-    };
-    if (tid == 0)
         for (int r = 0; r <= kLook; ++r) issue(r);
-
-    const int col = tid;
-    const bool on = col < ni * nj;
-    const int jo = on ? col % nj : 0, io = on ? col / nj : 0;
+        if (!bar_wait(gbar, 0) || !wait_rec(0) || !wait_rec(1)) bad = sflag[1] = 1;
+    }
+    __syncthreads();
     const float *hxm = gh, *hxp = gh + fs, *hym = gh + 2 * fs, *hyp = gh + 3 * fs,
                 *hzm = gh + 4 * fs, *hzp = gh + 5 * fs;
     const float *rxm = gr, *rym = gr + fs, *rzm = gr + 2 * fs;
     float* rw = a.RW + (long long)g * 6 * fs;
     float* R = a.R + base;
-    const int i = io + 3, j = jo + 3;
-    const float aw = a.AW[G.ipx + i - 1], ae = a.AE[G.ipx + i - 1];
-    const float as = a.AS[G.ipy + j - 1], an = a.AN[G.ipy + j - 1];
-    const float* ab = sab - 1;   // 1-based k
-    const float* at = sat - 1;
-    bool bad = false;
-    if (!bar_wait(gbar, 0)) {
-        bad = true;
-        atomicOr(&sbad, 1);
-    }
-    int done = -1;     // every record <= done has landed (as seen by this thread)
-    float rprev = 0.f;
+    const short* ro = m.rowoff;
     for (int t = 0; t < nm; ++t) {
-        // planes t and t+1 resident (t-1 was waited for one step earlier)
-        if (!bad && !*(volatile int*)&sbad) {
-            for (int r = done + 1; r <= t + 1 && r < nm; ++r) {
-                if (!bar_wait(&bars[r % kFwdSlots], (r / kFwdSlots) & 1)) {
-                    bad = true;
-                    atomicOr(&sbad, 1);
-                    break;
-                }
-                done = r;
-            }
+        if (sflag[(t + 1) & 1]) break;   // step t-1's flag, read after its barrier: uniform
+        if (tid == 0 && t >= 1) {
+            proxy_fence();
+            issue(t + kLook);   // slot of plane t-2, released by the last barrier
         }
-        const int buf = t & 1;
-        const int ko = t - io - jo;
-        if (on && !bad && ko >= 0 && ko < nk) {
-            const int k = ko + 3;
-            const float* c0 = ring + (t % kFwdSlots) * rec;
-            const float* hcur = c0 + 6 * mlp;
-            const float* hm1 = ring + ((t + kFwdSlots - 1) % kFwdSlots) * rec + 6 * mlp;
-            const float* hp1 = ring + ((t + 1) % kFwdSlots) * rec + 6 * mlp;
-            const int p0 = spst[t];
-            const int lp = spst[t + 1] - p0;
-            const int q = stpos[t * ni + io] + jo - p0;             // rank in plane t
-            const int pm = t > 0 ? spst[t - 1] : 0, pp = t + 1 < nm ? spst[t + 1] : 0;
+        const int p0 = m.pst[t], lp = m.pst[t + 1] - p0;
+        const float* c0 = m.ring + (t % kFwdSlots) * rec;
+        const int pq = tid < lp ? reinterpret_cast<const int*>(c0 + 7 * mlp)[tid] : -1;
+        if (pq >= 0) {
+            const int io = pq & 1023, jo = (pq >> 10) & 1023, ko = t - io - jo;
+            const int i = io + 3, j = jo + 3, k = ko + 3;
+            // rank of (io, jo, ko-1) in plane t-1; (io, jo-1, ko) is the one before it
+            const int rm = (ko > 0 || jo > 0) ? ro[(t - 1) * ni + io] + jo : 0;
+            const int rim = io > 0 ? ro[(t - 1) * ni + io - 1] + jo : 0;
             float lap = 0.f;
             if (!hz) {
-                const float hc = hcur[q];
-                const float hkm = ko > 0 ? hm1[stpos[(t - 1) * ni + io] + jo - pm] : hzm[fidx_z(s, jo, io)];
-                const float hkp = ko < nk - 1 ? hp1[stpos[(t + 1) * ni + io] + jo - pp] : hzp[fidx_z(s, jo, io)];
-                const float hjm = jo > 0 ? hm1[stpos[(t - 1) * ni + io] + jo - 1 - pm] : hym[fidx_y(s, ko, io)];
-                const float hjp = jo < nj - 1 ? hp1[stpos[(t + 1) * ni + io] + jo + 1 - pp] : hyp[fidx_y(s, ko, io)];
-                const float him = io > 0 ? hm1[stpos[(t - 1) * ni + io - 1] + jo - pm] : hxm[fidx_x(s, ko, jo)];
-                const float hip = io < ni - 1 ? hp1[stpos[(t + 1) * ni + io + 1] + jo - pp] : hxp[fidx_x(s, ko, jo)];
-                lap = -aw * him - ae * hip - as * hjm - an * hjp - ab[k] * hkm - at[k] * hkp -
-                      c0[4 * lp + q] * hc;
+                const float* hcur = c0 + 6 * mlp;
+                const float* hm1 = m.ring + ((t + kFwdSlots - 1) % kFwdSlots) * rec + 6 * mlp;
+                const float* hp1 = m.ring + ((t + 1) % kFwdSlots) * rec + 6 * mlp;
+                // rank of (io, jo, ko+1) in plane t+1; (io, jo+1, ko) is the one after it
+                const int rp = (ko < nk - 1 || jo < nj - 1) ? ro[(t + 1) * ni + io] + jo : 0;
+                const int rip = io < ni - 1 ? ro[(t + 1) * ni + io + 1] + jo : 0;
+                const float hc = hcur[tid];
+                const float hkm = ko > 0 ? hm1[rm] : hzm[fidx_z(s, jo, io)];
+                const float hkp = ko < nk - 1 ? hp1[rp] : hzp[fidx_z(s, jo, io)];
+                const float hjm = jo > 0 ? hm1[rm - 1] : hym[fidx_y(s, ko, io)];
+                const float hjp = jo < nj - 1 ? hp1[rp + 1] : hyp[fidx_y(s, ko, io)];
+                const float him = io > 0 ? hm1[rim] : hxm[fidx_x(s, ko, jo)];
+                const float hip = io < ni - 1 ? hp1[rip] : hxp[fidx_x(s, ko, jo)];
+                lap = -saw[i - 1] * him - sae[i - 1] * hip - sas[j - 1] * hjm - san[j - 1] * hjp -
+                      sab[k - 1] * hkm - sat[k - 1] * hkp - c0[4 * lp + tid] * hc;
             }
-            const float rkm = ko > 0 ? rprev : rzm[fidx_z(s, jo, io)];
-            const float rjm = jo > 0 ? xr[(buf ^ 1) * xs + col - 1] : rym[fidx_y(s, ko, io)];
-            const float rim = io > 0 ? xr[(buf ^ 1) * xs + col - nj] : rxm[fidx_x(s, ko, jo)];
+            const float* xp = m.xr + ((t + 1) & 1) * mlp;   // res of plane t-1
+            const float rkm = ko > 0 ? xp[rm] : rzm[fidx_z(s, jo, io)];
+            const float rjm = jo > 0 ? xp[rm - 1] : rym[fidx_y(s, ko, io)];
+            const float rimv = io > 0 ? xp[rim] : rxm[fidx_x(s, ko, jo)];
             // block layout: [lw | ls | lb | lpr | ap] with stride lp
-            float r = (c0[5 * mlp + q] + lap) * c0[3 * lp + q];
-            r = r - c0[2 * lp + q] * rkm - c0[lp + q] * rjm - c0[q] * rim;
-            R[p0 + q] = r;
+            float r = (c0[5 * mlp + tid] + lap) * c0[3 * lp + tid];
+            r = r - c0[2 * lp + tid] * rkm - c0[lp + tid] * rjm - c0[tid] * rimv;
+            R[p0 + tid] = r;
             if (io == 0) rw[0 * fs + fidx_x(s, ko, jo)] = r;
             if (io == ni - 1) rw[1 * fs + fidx_x(s, ko, jo)] = r;
             if (jo == 0) rw[2 * fs + fidx_y(s, ko, io)] = r;
             if (jo == nj - 1) rw[3 * fs + fidx_y(s, ko, io)] = r;
             if (ko == 0) rw[4 * fs + fidx_z(s, jo, io)] = r;
             if (ko == nk - 1) rw[5 * fs + fidx_z(s, jo, io)] = r;
-            rprev = r;
-            xr[buf * xs + col] = r;
+            m.xr[(t & 1) * mlp + tid] = r;
         }
+        if (tid == 0 && !wait_rec(t + 2)) bad = sflag[t & 1] = 1;
         __syncthreads();
-        // slot of plane t-1 is free now; refill it with plane t+kLook+1
-        if (tid == 0 && !sbad) {
-            proxy_fence();
-            issue(t + kLook + 1);
-        }
     }
-    __syncthreads();
-    if (tid == 0 && sbad) {
+    if (tid == 0 && bad) {
         // error path: let every copy still in flight land before the CTA exits
         bar_wait(gbar, 0);
-        for (int r = done + 1; r <= issued; ++r)
+        for (int r = waited + 1; r <= issued; ++r)
             if (!bar_wait(&bars[r % kFwdSlots], (r / kFwdSlots) & 1)) break;
         atomicExch(&a.ctl[2], 1);
     }
@@ -299,18 +343,18 @@ struct BwdArgs {
     int hzero;
 };
 
+// Backward sweep, one thread per point of the current hyperplane, planes in
+// reverse order.  A record holds [ue|un|ut] (stride Lp), the forward res, the
+// old hilf and the point table of one plane; step t (plane nm-1-t) needs only
+// its own record, so thread 0 refills the slot of step t-1 with step t+4.
 __global__ void __launch_bounds__(kMaxCols) k_sip_bwd(BwdArgs a) {
     if (a.ctl[0]) return;
     extern __shared__ __align__(128) unsigned char smraw[];
     const Shape s = a.s;
     const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm, mlp = s.maxlp;
-    const int rec = 5 * mlp;
-    float* ring = reinterpret_cast<float*>(smraw);
-    int* stpos = reinterpret_cast<int*>(ring + kBwdSlots * rec);
-    int* spst = stpos + nm * ni;
-    const int xs = blockDim.x;
-    float* xr = reinterpret_cast<float*>(spst + nm + 1);            // [2][xs]
-    float* gr = reinterpret_cast<float*>(((size_t)(xr + 2 * xs) + 15) & ~(size_t)15);   // [3][fs]
+    const int rec = 6 * mlp;
+    const SweepSmem m = carve(smraw, s, kBwdSlots, rec);
+    float* gr = m.tail;                  // [3][fs] high res ghosts
     unsigned long long* bars =
         reinterpret_cast<unsigned long long*>(((size_t)(gr + 3 * fs) + 15) & ~(size_t)15);
     unsigned long long* gbar = bars + kBwdSlots;
@@ -319,97 +363,94 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_bwd(BwdArgs a) {
     const long long base = (long long)g * s.npp;
     const float* CB = a.CB + (long long)a.gcls[g] * 3 * s.npp;
     const bool hz = a.hzero != 0;
-    __shared__ int sbad;
-    for (int q = tid; q < nm * ni; q += blockDim.x) stpos[q] = s.tpos[q];
-    for (int q = tid; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
+    // error flag of step t in sflag[t & 1], written by thread 0 before the
+    // step's closing barrier and read by everyone after it; two slots so that
+    // thread 0 running ahead never overwrites a flag still being read
+    __shared__ int sflag[2];
+    for (int q = tid; q < nm * ni; q += blockDim.x) m.rowoff[q] = s.rowoff[q];
+    for (int q = tid; q <= nm; q += blockDim.x) m.pst[q] = s.pst[q];
     if (tid == 0) {
-        sbad = 0;
+        sflag[0] = sflag[1] = 0;
         for (int q = 0; q <= kBwdSlots; ++q) bar_init(&bars[q], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
+    int issued = -1, waited = -1;
+    int bad = 0;
+    // record r (step r) = plane nm-1-r
+    auto issue = [&](int r) {
+        if (r >= nm) return;
+        issued = r;
+        const int pl = nm - 1 - r;
+        const int sl = r % kBwdSlots;
+        const int p0 = m.pst[pl], lp = m.pst[pl + 1] - p0;
+        float* d = m.ring + sl * rec;
+        const unsigned b3 = 3u * lp * 4u, b1 = (unsigned)lp * 4u;
+        bar_expect(&bars[sl], b3 + 2u * b1 + (hz ? 0u : b1));
+        bulk_load(d, CB + 3LL * p0, b3, &bars[sl]);
+        bulk_load(d + 3 * mlp, a.R + base + p0, b1, &bars[sl]);
+        if (!hz) bulk_load(d + 4 * mlp, a.H + base + p0, b1, &bars[sl]);
+        bulk_load(d + 5 * mlp, s.pq + p0, b1, &bars[sl]);
+    };
+    auto wait_rec = [&](int r) -> bool {
+        if (r >= nm || r <= waited) return true;
+        if (!bar_wait(&bars[r % kBwdSlots], (r / kBwdSlots) & 1)) return false;
+        waited = r;
+        return true;
+    };
     const int* fn = a.fnbr + 6 * g;
+    __syncthreads();
     if (tid == 0) {   // high res ghosts: the +x, +y, +z neighbours' low planes
         const unsigned fb = (unsigned)fs * 4u;
         bar_expect(gbar, 3u * fb);
         bulk_load(gr + 0 * fs, a.RHI + ((long long)fn[1] * 6 + 0) * fs, fb, gbar);
         bulk_load(gr + 1 * fs, a.RHI + ((long long)fn[3] * 6 + 2) * fs, fb, gbar);
         bulk_load(gr + 2 * fs, a.RHI + ((long long)fn[5] * 6 + 4) * fs, fb, gbar);
+        for (int r = 0; r < kBwdSlots; ++r) issue(r);
+        if (!bar_wait(gbar, 0) || !wait_rec(0)) bad = sflag[1] = 1;
     }
-    int issued = -1;
-    // record r (step r) = plane nm-1-r
-    auto issue = [&](int r) {
-        if (r >= nm) return;
-        issued = r;
-        const int m = nm - 1 - r;
-        const int sl = r % kBwdSlots;
-        const int p0 = spst[m], lp = spst[m + 1] - p0;
-        float* d = ring + sl * rec;
-        const unsigned b3 = 3u * lp * 4u, b1 = (unsigned)lp * 4u;
-        bar_expect(&bars[sl], b3 + b1 + (hz ? 0u : b1));
-        bulk_load(d, CB + 3LL * p0, b3, &bars[sl]);
-        bulk_load(d + 3 * mlp, a.R + base + p0, b1, &bars[sl]);
-        if (!hz) bulk_load(d + 4 * mlp, a.H + base + p0, b1, &bars[sl]);
-    };
-    if (tid == 0)
-        for (int r = 0; r < kLook; ++r) issue(r);
-    const int col = tid;
-    const bool on = col < ni * nj;
-    const int jo = on ? col % nj : 0, io = on ? col / nj : 0;
-    const int jr = nj - 1 - jo, ir = ni - 1 - io;
+    __syncthreads();
     const float *rxp = gr, *ryp = gr + fs, *rzp = gr + 2 * fs;
     float* hw = a.HOUT + (long long)g * 6 * fs;
     float* H = a.H + base;
-    bool bad = false;
-    if (!bar_wait(gbar, 0)) {
-        bad = true;
-        atomicOr(&sbad, 1);
-    }
-    int done = -1;
-    float rprev = 0.f;
+    const short* ro = m.rowoff;
     for (int t = 0; t < nm; ++t) {
-        if (tid == 0 && !sbad) {
+        if (sflag[(t + 1) & 1]) break;
+        if (tid == 0 && t >= 1) {
             proxy_fence();
-            issue(t + kLook);   // slot of step t-1, released by the barrier below last step
+            issue(t + kBwdSlots - 1);   // slot of step t-1, released by the last barrier
         }
-        if (!bad && !*(volatile int*)&sbad) {
-            if (bar_wait(&bars[t % kBwdSlots], (t / kBwdSlots) & 1)) {
-                done = t;
-            } else {
-                bad = true;
-                atomicOr(&sbad, 1);
-            }
-        }
-        const int buf = t & 1;
-        const int kr = t - ir - jr;
-        if (on && !bad && kr >= 0 && kr < nk) {
-            const int ko = nk - 1 - kr;
-            const int m = nm - 1 - t;
-            const int p0 = spst[m];
-            const int lp = spst[m + 1] - p0;
-            const int q = stpos[m * ni + io] + jo - p0;
-            const float* c0 = ring + (t % kBwdSlots) * rec;
-            const float rkp = kr > 0 ? rprev : rzp[fidx_z(s, jo, io)];
-            const float rjp = jo < nj - 1 ? xr[(buf ^ 1) * xs + col + 1] : ryp[fidx_y(s, ko, io)];
-            const float rip = io < ni - 1 ? xr[(buf ^ 1) * xs + col + nj] : rxp[fidx_x(s, ko, jo)];
+        const int pl = nm - 1 - t;
+        const int p0 = m.pst[pl], lp = m.pst[pl + 1] - p0;
+        const float* c0 = m.ring + (t % kBwdSlots) * rec;
+        const int pq = tid < lp ? reinterpret_cast<const int*>(c0 + 5 * mlp)[tid] : -1;
+        if (pq >= 0) {
+            const int io = pq & 1023, jo = (pq >> 10) & 1023, ko = pl - io - jo;
+            // rank of (io, jo, ko+1) in plane pl+1; (io, jo+1, ko) is the one after it
+            const int rp = (ko < nk - 1 || jo < nj - 1) ? ro[(pl + 1) * ni + io] + jo : 0;
+            const int rip = io < ni - 1 ? ro[(pl + 1) * ni + io + 1] + jo : 0;
+            const float* xp = m.xr + ((t + 1) & 1) * mlp;   // res of plane pl+1
+            const float rkp = ko < nk - 1 ? xp[rp] : rzp[fidx_z(s, jo, io)];
+            const float rjp = jo < nj - 1 ? xp[rp + 1] : ryp[fidx_y(s, ko, io)];
+            const float ripv = io < ni - 1 ? xp[rip] : rxp[fidx_x(s, ko, jo)];
             // block layout: [ue | un | ut] with stride lp
-            const float r = c0[3 * mlp + q] - c0[2 * lp + q] * rkp - c0[lp + q] * rjp - c0[q] * rip;
-            const float h = (hz ? 0.f : c0[4 * mlp + q]) + r;
-            H[p0 + q] = h;
+            const float r = c0[3 * mlp + tid] - c0[2 * lp + tid] * rkp - c0[lp + tid] * rjp -
+                            c0[tid] * ripv;
+            const float h = (hz ? 0.f : c0[4 * mlp + tid]) + r;
+            H[p0 + tid] = h;
             if (io == 0) hw[0 * fs + fidx_x(s, ko, jo)] = h;
             if (io == ni - 1) hw[1 * fs + fidx_x(s, ko, jo)] = h;
             if (jo == 0) hw[2 * fs + fidx_y(s, ko, io)] = h;
             if (jo == nj - 1) hw[3 * fs + fidx_y(s, ko, io)] = h;
             if (ko == 0) hw[4 * fs + fidx_z(s, jo, io)] = h;
             if (ko == nk - 1) hw[5 * fs + fidx_z(s, jo, io)] = h;
-            rprev = r;
-            xr[buf * xs + col] = r;
+            m.xr[(t & 1) * mlp + tid] = r;
         }
+        if (tid == 0 && !wait_rec(t + 1)) bad = sflag[t & 1] = 1;
         __syncthreads();
     }
-    if (tid == 0 && sbad) {
+    if (tid == 0 && bad) {
         bar_wait(gbar, 0);
-        for (int r = done + 1; r <= issued; ++r)
+        for (int r = waited + 1; r <= issued; ++r)
             if (!bar_wait(&bars[r % kBwdSlots], (r / kBwdSlots) & 1)) break;
         atomicExch(&a.ctl[2], 1);
     }
@@ -432,29 +473,57 @@ struct OuterArgs {
     Shape s;
     const int* fnbr;
     const int* gcls;
-    const int* idxp;            // padded position -> natural local index, -1 for padding
     const float* H;
     const float* HOUT;
     double* RHS64;
     float* RHS32;
     double* DP64;
-    const double* AP64;         // class, padded plane order
-    const double *AW, *AE, *AS, *AN, *AB, *AT;
+    const float* APX;           // class ap split in two floats: [ncls][hi npp | lo npp]
+    const float* A1[6];         // 1-D coefficients aw, ae, as, an, ab, at: FP32 rounding
+    const float* A1L[6];        //   and the FP32 rounding of the remainder
     const DevGrid* grids;
     double* gridmax;
     const int* ctl;
 };
 
-// Outer step in FP64 (laplacephi + rescal + maxabscal_grid + accumulate_pcorr).
+// a + b = s + e exactly (Knuth's TwoSum, no order of magnitudes assumed)
+__device__ __forceinline__ void two_sum(float a, float b, float& s, float& e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// (sum, comp) += (ch + cl) * h in float-float: ch*h splits exactly into its
+// rounding and an FMA remainder; cl*h is 2^-24 smaller and rounds once.
+__device__ __forceinline__ void ff_acc(float ch, float cl, float h, float& sum, float& comp) {
+    const float p = __fmul_rn(ch, h);
+    const float e = fmaf(ch, h, -p);
+    float t;
+    two_sum(sum, p, sum, t);
+    comp += t + fmaf(cl, h, e);
+}
+
+// Outer step (laplacephi + rescal + maxabscal_grid + accumulate_pcorr):
+// rhs <- rhs - A hilf, dp <- dp + hilf, per-grid max|rhs|.  A hilf is formed
+// in float-float arithmetic (about 48 significant bits; hilf itself is FP32)
+// and subtracted from the FP64 residual, so only the residual and dp updates
+// use the FP64 pipe.  One CTA per grid walks its points in plane order.
 __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
     if (a.ctl[0]) return;
     __shared__ double sh[32];
+    extern __shared__ __align__(16) unsigned char osm[];
     const Shape s = a.s;
-    const int kk = s.kk, jj = s.jj, nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs;
+    const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm;
+    int* spst = reinterpret_cast<int*>(osm);
+    short* ro = reinterpret_cast<short*>(spst + nm + 1);
+    for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
+    for (int q = threadIdx.x; q < nm * ni; q += blockDim.x) ro[q] = s.rowoff[q];
+    __syncthreads();
     const int g = blockIdx.x;
     const DevGrid G = a.grids[g];
     const long long base = (long long)g * s.npp;
-    const long long cb = (long long)a.gcls[g] * s.npp;
+    const float* APH = a.APX + (long long)a.gcls[g] * 2 * s.npp;
+    const float* APL = APH + s.npp;
     const float* H = a.H + base;
     const int* fn = a.fnbr + 6 * g;
     const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;
@@ -463,31 +532,45 @@ __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
     const float* hyp = a.HOUT + ((long long)fn[3] * 6 + 2) * fs;
     const float* hzm = a.HOUT + ((long long)fn[4] * 6 + 5) * fs;
     const float* hzp = a.HOUT + ((long long)fn[5] * 6 + 4) * fs;
-    auto pos = [&](int ko, int jo, int io) { return s.tpos[(io + jo + ko) * ni + io] + jo; };
-    double mx = 0.0;
+    // 1-D coefficients indexed by io, jo, ko (interior index 3 is io = 0)
+    const float *awh = a.A1[0] + G.ipx + 2, *awl = a.A1L[0] + G.ipx + 2;
+    const float *aeh = a.A1[1] + G.ipx + 2, *ael = a.A1L[1] + G.ipx + 2;
+    const float *ash = a.A1[2] + G.ipy + 2, *asl = a.A1L[2] + G.ipy + 2;
+    const float *anh = a.A1[3] + G.ipy + 2, *anl = a.A1L[3] + G.ipy + 2;
+    const float *abh = a.A1[4] + G.ipz + 2, *abl = a.A1L[4] + G.ipz + 2;
+    const float *ath = a.A1[5] + G.ipz + 2, *atl = a.A1L[5] + G.ipz + 2;
+    long long mxb = 0;   // max |r| as the bit pattern of a non-negative double
     for (int q = threadIdx.x; q < s.npp; q += blockDim.x) {
-        const int id = a.idxp[q];
-        if (id < 0) continue;
-        const int k = id % kk + 1, j = (id / kk) % jj + 1, i = id / (kk * jj) + 1;
-        const int ko = k - 3, jo = j - 3, io = i - 3;
-        const double hc = H[q];
-        const double him = io > 0 ? H[pos(ko, jo, io - 1)] : hxm[fidx_x(s, ko, jo)];
-        const double hip = io < ni - 1 ? H[pos(ko, jo, io + 1)] : hxp[fidx_x(s, ko, jo)];
-        const double hjm = jo > 0 ? H[pos(ko, jo - 1, io)] : hym[fidx_y(s, ko, io)];
-        const double hjp = jo < nj - 1 ? H[pos(ko, jo + 1, io)] : hyp[fidx_y(s, ko, io)];
-        const double hkm = ko > 0 ? H[pos(ko - 1, jo, io)] : hzm[fidx_z(s, jo, io)];
-        const double hkp = ko < nk - 1 ? H[pos(ko + 1, jo, io)] : hzp[fidx_z(s, jo, io)];
-        const double lap = -a.AW[G.ipx + i - 1] * him - a.AE[G.ipx + i - 1] * hip -
-                           a.AS[G.ipy + j - 1] * hjm - a.AN[G.ipy + j - 1] * hjp -
-                           a.AB[G.ipz + k - 1] * hkm - a.AT[G.ipz + k - 1] * hkp -
-                           a.AP64[cb + q] * hc;
-        const double r = a.RHS64[base + q] + lap;
+        const int v = s.pq[q];
+        if (v < 0) continue;
+        const int io = v & 1023, jo = (v >> 10) & 1023, ko = v >> 20;
+        const int t = io + jo + ko;
+        // positions of (io, jo, ko-1) on plane t-1 and (io, jo, ko+1) on plane
+        // t+1; the j neighbours sit next to them, the i neighbours one row over
+        const int bm = (ko > 0 || jo > 0) ? spst[t - 1] + ro[(t - 1) * ni + io] + jo : 0;
+        const int bp = (ko < nk - 1 || jo < nj - 1) ? spst[t + 1] + ro[(t + 1) * ni + io] + jo : 0;
+        const float hc = H[q];
+        const float him = io > 0 ? H[spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo] : hxm[fidx_x(s, ko, jo)];
+        const float hip = io < ni - 1 ? H[spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo] : hxp[fidx_x(s, ko, jo)];
+        const float hjm = jo > 0 ? H[bm - 1] : hym[fidx_y(s, ko, io)];
+        const float hjp = jo < nj - 1 ? H[bp + 1] : hyp[fidx_y(s, ko, io)];
+        const float hkm = ko > 0 ? H[bm] : hzm[fidx_z(s, jo, io)];
+        const float hkp = ko < nk - 1 ? H[bp] : hzp[fidx_z(s, jo, io)];
+        float sum = 0.f, comp = 0.f;
+        ff_acc(awh[io], awl[io], him, sum, comp);
+        ff_acc(aeh[io], ael[io], hip, sum, comp);
+        ff_acc(ash[jo], asl[jo], hjm, sum, comp);
+        ff_acc(anh[jo], anl[jo], hjp, sum, comp);
+        ff_acc(abh[ko], abl[ko], hkm, sum, comp);
+        ff_acc(ath[ko], atl[ko], hkp, sum, comp);
+        ff_acc(APH[q], APL[q], hc, sum, comp);
+        const double r = (a.RHS64[base + q] - (double)sum) - (double)comp;
         a.RHS64[base + q] = r;
         a.RHS32[base + q] = (float)r;
-        a.DP64[base + q] = a.DP64[base + q] + hc;
-        mx = fmax(fabs(r), mx);
+        a.DP64[base + q] = a.DP64[base + q] + (double)hc;
+        mxb = max(mxb, __double_as_longlong(r) & 0x7fffffffffffffffLL);
     }
-    mx = block_max2(mx, sh);
+    const double mx = block_max2(__longlong_as_double(mxb), sh);
     if (threadIdx.x == 0) a.gridmax[g] = mx;
 }
 
@@ -531,7 +614,8 @@ __global__ void k_sip_scatter(const DevGrid* __restrict__ grids, int npp, const 
 
 // class coefficients (FP64 fields of a representative grid, plane order of
 // the reference's hyperplane solver or natural order of the classic one)
-// -> padded FP32 blocks [lw|ls|lb|lpr|ap], [ue|un|ut] and padded FP64 ap
+// -> padded FP32 blocks [lw|ls|lb|lpr|ap], [ue|un|ut] and ap split in two
+// floats (rounding, rounding of the remainder) for the outer step
 __global__ void k_sip_extract(const DevGrid* __restrict__ grids, const int* __restrict__ reps,
                               const int* __restrict__ qmap, const int* __restrict__ idx,
                               const int* __restrict__ pst, int nm, int npp, int planeorder,
@@ -539,7 +623,7 @@ __global__ void k_sip_extract(const DevGrid* __restrict__ grids, const int* __re
                               const double* __restrict__ lb, const double* __restrict__ lpr,
                               const double* __restrict__ ue, const double* __restrict__ un,
                               const double* __restrict__ ut, const double* __restrict__ ap,
-                              float* CF, float* CB, double* AP64) {
+                              float* CF, float* CB, float* APX) {
     const int cls = blockIdx.y;
     const int qp = blockIdx.x * blockDim.x + threadIdx.x;
     if (qp >= npp) return;
@@ -549,12 +633,12 @@ __global__ void k_sip_extract(const DevGrid* __restrict__ grids, const int* __re
     const int p0 = pst[m], lp = pst[m + 1] - p0, rnk = qp - p0;
     float* cf = CF + (long long)cls * 5 * npp + 5LL * p0;
     float* cb = CB + (long long)cls * 3 * npp + 3LL * p0;
-    double* ap64 = AP64 + (long long)cls * npp;
+    float* aph = APX + (long long)cls * 2 * npp;
     const int q = qmap[qp];   // unpadded plane position, -1 for padding
     if (q < 0) {
         for (int f = 0; f < 5; ++f) cf[f * lp + rnk] = 0.f;
         for (int f = 0; f < 3; ++f) cb[f * lp + rnk] = 0.f;
-        ap64[qp] = 0.0;
+        aph[qp] = aph[npp + qp] = 0.f;
         return;
     }
     const DevGrid G = grids[reps[cls]];
@@ -568,28 +652,32 @@ __global__ void k_sip_extract(const DevGrid* __restrict__ grids, const int* __re
     cb[0 * lp + rnk] = (float)ue[src];
     cb[1 * lp + rnk] = (float)un[src];
     cb[2 * lp + rnk] = (float)ut[src];
-    ap64[qp] = ap[G.ip3 + id];
+    const double apv = ap[G.ip3 + id];
+    aph[qp] = (float)apv;
+    aph[npp + qp] = (float)(apv - (double)(float)apv);
 }
 
 Shape shape(const SipState& st) {
     Shape s;
     s.kk = st.kk; s.jj = st.jj; s.ii = st.ii; s.ni = st.ni; s.nj = st.nj; s.nk = st.nk;
     s.nm = st.nm; s.npp = st.npp; s.fs = st.fs; s.maxlp = st.maxlp;
-    s.tpos = st.d_tpos; s.pst = st.d_pst;
+    s.tpos = st.d_tpos; s.pst = st.d_pst; s.rowoff = st.d_rowoff; s.pq = st.d_pq;
     return s;
 }
 
-int sweep_threads(const SipState& st) { return (st.ni * st.nj + 31) / 32 * 32; }
+int sweep_threads(const SipState& st) { return (st.maxlp + 31) / 32 * 32; }
 
 size_t fwd_smem(const SipState& st) {
-    return (size_t)kFwdSlots * 7 * st.maxlp * 4 + (size_t)(st.nm * st.ni + st.nm + 1) * 4 +
-           (size_t)2 * sweep_threads(st) * 4 + 16 + (size_t)9 * st.fs * 4 + (size_t)2 * st.kk * 4 + 16 +
-           (kFwdSlots + 1) * 8;
+    const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kFwdSlots, 8 * st.maxlp);
+    const size_t tail = (size_t)9 * st.fs * 4 + (size_t)2 * (st.ii + st.jj + st.kk) * 4;
+    return align16(l.tail + tail) + (kFwdSlots + 1) * 8;
 }
 
+size_t outer_smem(const SipState& st) { return (size_t)(st.nm + 1) * 4 + (size_t)st.nm * st.ni * 2; }
+
 size_t bwd_smem(const SipState& st) {
-    return (size_t)kBwdSlots * 5 * st.maxlp * 4 + (size_t)(st.nm * st.ni + st.nm + 1) * 4 +
-           (size_t)2 * sweep_threads(st) * 4 + 16 + (size_t)3 * st.fs * 4 + 16 + (kBwdSlots + 1) * 8;
+    const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kBwdSlots, 6 * st.maxlp);
+    return align16(l.tail + (size_t)3 * st.fs * 4) + (kBwdSlots + 1) * 8;
 }
 
 }  // namespace
@@ -602,8 +690,8 @@ int sip_init(Ctx* c, SipState& st) {
     // face buffers are copied whole with cp.async.bulk: a multiple of 16 bytes
     st.fs = (std::max(st.nj * st.nk, std::max(st.ni * st.nk, st.ni * st.nj)) + 3) & ~3;
     st.nm = st.ni + st.nj + st.nk - 2;
-    if (st.ni * st.nj > kMaxCols) {
-        set_error("mixed form: at most 1024 (j, i) columns per grid");
+    if (st.ni > 1023 || st.nj > 1023 || st.nk > 1023) {
+        set_error("mixed form: grid too large for the hyperplane point table");
         return MGLET_ERR_UNSUPPORTED;
     }
     // padded plane starts, position table, padded -> natural index map
@@ -621,7 +709,12 @@ int sip_init(Ctx* c, SipState& st) {
         st.maxlp = std::max(st.maxlp, (cnt + 3) & ~3);
     }
     st.npp = pst[st.nm];
-    std::vector<int> idxp(st.npp, -1), qmap(st.npp, -1);
+    if (st.maxlp > kMaxCols) {
+        set_error("mixed form: at most 1024 points per hyperplane");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    std::vector<int> idxp(st.npp, -1), qmap(st.npp, -1), pq(st.npp, -1);
+    std::vector<short> rowoff((size_t)st.nm * st.ni, 0);
     int q = 0;   // unpadded position (the reference's iacc - 1)
     for (int m0 = 0; m0 < st.nm; ++m0) {
         int p = pst[m0];
@@ -629,10 +722,12 @@ int sip_init(Ctx* c, SipState& st) {
             const int jlo = std::max(0, m0 - io - (st.nk - 1));
             const int jhi = std::min(st.nj - 1, m0 - io);
             tpos[(size_t)m0 * st.ni + io] = p - jlo;
+            rowoff[(size_t)m0 * st.ni + io] = (short)(p - jlo - pst[m0]);
             for (int jo = jlo; jo <= jhi; ++jo, ++p, ++q) {
                 const int ko = m0 - io - jo;
                 idxp[p] = (ko + 2) + (jo + 2) * st.kk + (io + 2) * st.kk * st.jj;
                 qmap[p] = q;
+                pq[p] = io | (jo << 10) | (ko << 20);
             }
         }
     }
@@ -649,6 +744,10 @@ int sip_init(Ctx* c, SipState& st) {
     if (int rc = up(&st.d_pst, pst)) return rc;
     if (int rc = up(&st.d_idxp, idxp)) return rc;
     if (int rc = up(&st.d_qmap, qmap)) return rc;
+    if (int rc = up(&st.d_pq, pq)) return rc;
+    MG_CUDA(cudaMalloc(&st.d_rowoff, rowoff.size() * sizeof(short)));
+    MG_CUDA(cudaMemcpy(st.d_rowoff, rowoff.data(), rowoff.size() * sizeof(short),
+                       cudaMemcpyHostToDevice));
     // face neighbours from the connection table (regular periodic tiling)
     std::vector<int> fn((size_t)6 * c->ngrid, -1);
     for (size_t r = 0; r < c->conns.size(); r += 4) {
@@ -689,9 +788,12 @@ int sip_init(Ctx* c, SipState& st) {
     for (int qq = 0; qq < 6; ++qq) {
         std::vector<double> h(len[qq]);
         MG_CUDA(cudaMemcpy(h.data(), c->L(n1[qq]), len[qq] * sizeof(double), cudaMemcpyDeviceToHost));
-        std::vector<float> f(h.begin(), h.end());
+        std::vector<float> f(h.begin(), h.end()), fl(h.size());
+        for (size_t e = 0; e < h.size(); ++e) fl[e] = (float)(h[e] - (double)f[e]);
         MG_CUDA(cudaMalloc(&st.a1[qq], len[qq] * sizeof(float)));
         MG_CUDA(cudaMemcpy(st.a1[qq], f.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
+        MG_CUDA(cudaMalloc(&st.a1lo[qq], len[qq] * sizeof(float)));
+        MG_CUDA(cudaMemcpy(st.a1lo[qq], fl.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
     }
     const size_t smf = fwd_smem(st), smb = bwd_smem(st);
     if (smf > 200 * 1024 || smb > 200 * 1024) {
@@ -704,26 +806,29 @@ int sip_init(Ctx* c, SipState& st) {
 }
 
 int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* d_idx,
-                bool planeorder, float** cf, float** cb, double** ap64) {
+                bool planeorder, float** cf, float** cb, float** apx) {
     const size_t n = (size_t)nclass * st.npp;
     MG_CUDA(cudaMalloc(cf, 5 * n * sizeof(float)));
     MG_CUDA(cudaMalloc(cb, 3 * n * sizeof(float)));
-    MG_CUDA(cudaMalloc(ap64, n * sizeof(double)));
+    MG_CUDA(cudaMalloc(apx, 2 * n * sizeof(float)));
     dim3 grid((st.npp + 255) / 256, nclass);
     k_sip_extract<<<grid, 256, 0, c->stream>>>(
         c->d_grids, d_reps, st.d_qmap, d_idx, st.d_pst, st.nm, st.npp, planeorder ? 1 : 0,
         c->F("SIPLW"), c->F("SIPLS"), c->F("SIPLB"), c->F("SIPLPR"), c->F("SIPUE"), c->F("SIPUN"),
-        c->F("SIPUT"), c->F("GSAP"), *cf, *cb, *ap64);
+        c->F("SIPUT"), c->F("GSAP"), *cf, *cb, *apx);
     MG_LAUNCHED(c);
     return 0;
 }
 
 void sip_release(SipState& st) {
     for (void* p : {(void*)st.d_tpos, (void*)st.d_pst, (void*)st.d_idxp, (void*)st.d_qmap,
+                    (void*)st.d_pq, (void*)st.d_rowoff,
                     (void*)st.d_fnbr, (void*)st.h32, (void*)st.r32, (void*)st.rhs32,
                     (void*)st.rhs64, (void*)st.dp64, (void*)st.hout, (void*)st.rout[0],
                     (void*)st.rout[1], (void*)st.rout[2], (void*)st.a1[0], (void*)st.a1[1],
-                    (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5]})
+                    (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
+                    (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
+                    (void*)st.a1lo[4], (void*)st.a1lo[5]})
         cudaFree(p);
 }
 
@@ -775,19 +880,21 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
     return 0;
 }
 
-int sip_outer(Ctx* c, SipState& st, const double* ap64, const int* gcls, const int* ctl) {
+int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl) {
     ProfScope ps_(c, "mx_outer");
     OuterArgs a;
     a.s = shape(st);
-    a.fnbr = st.d_fnbr; a.gcls = gcls; a.idxp = st.d_idxp;
+    a.fnbr = st.d_fnbr; a.gcls = gcls;
     a.H = st.h32; a.HOUT = st.hout;
-    a.RHS64 = st.rhs64; a.RHS32 = st.rhs32; a.DP64 = st.dp64; a.AP64 = ap64;
-    a.AW = c->L("GSAW"); a.AE = c->L("GSAE"); a.AS = c->L("GSAS"); a.AN = c->L("GSAN");
-    a.AB = c->L("GSAB"); a.AT = c->L("GSAT");
+    a.RHS64 = st.rhs64; a.RHS32 = st.rhs32; a.DP64 = st.dp64; a.APX = apx;
+    for (int q = 0; q < 6; ++q) {
+        a.A1[q] = st.a1[q];
+        a.A1L[q] = st.a1lo[q];
+    }
     a.grids = c->d_grids;
     a.gridmax = c->d_gridred;
     a.ctl = ctl;
-    k_sip_outer<<<c->ngrid, 512, 0, c->stream>>>(a);
+    k_sip_outer<<<c->ngrid, 512, outer_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }

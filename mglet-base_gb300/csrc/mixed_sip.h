@@ -14,26 +14,30 @@ struct SipState {
     int* d_pst = nullptr;       // [nm+1] padded plane starts
     int* d_idxp = nullptr;      // [npp] natural local index, -1 for padding
     int* d_qmap = nullptr;      // [npp] unpadded plane position (iacc-1), -1 for padding
+    int* d_pq = nullptr;        // [npp] io | jo << 16 of each padded position, -1 for padding
+    short* d_rowoff = nullptr;  // [nm][ni] rank of (io, jo = 0) in plane m
     int* d_fnbr = nullptr;      // [ngrid][6] face neighbours (0-based)
     float *h32 = nullptr, *r32 = nullptr, *rhs32 = nullptr;   // [ngrid][npp]
     double *rhs64 = nullptr, *dp64 = nullptr;                 // [ngrid][npp]
     float* hout = nullptr;      // [ngrid][6][fs] hilf boundary planes
     float* rout[3] = {nullptr, nullptr, nullptr};   // rotating res boundary planes
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
+    float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
 
 int sip_init(Ctx* c, SipState& st);
 // Class coefficients: FP32 blocks [lw|ls|lb|lpr|ap] and [ue|un|ut] per padded
-// plane, FP64 ap, from the representative grid of each class.
+// plane, and ap split in two floats [hi npp | lo npp], from the representative
+// grid of each class.
 int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* d_idx,
-                bool planeorder, float** cf, float** cb, double** ap64);
+                bool planeorder, float** cf, float** cb, float** apx);
 void sip_release(SipState& st);
 int sip_divcal(Ctx* c, SipState& st, double fak);
 int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
                 int rwrite, bool hzero);
 int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ctl, int rhi,
                  bool hzero);
-int sip_outer(Ctx* c, SipState& st, const double* ap64, const int* gcls, const int* ctl);
+int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl);
 int sip_scatter_dp(Ctx* c, SipState& st);
 
 }  // namespace mg
