@@ -195,7 +195,7 @@ int build_plan(Ctx* c, int ilevel, int layers, int slots, bool corners, bool nor
     plan.npts = npts;
     if (!tasks.empty()) {
         MG_CUDA(cudaMalloc(&plan.d_tasks, tasks.size() * sizeof(BoxCopy)));
-        MG_CUDA(cudaMemcpy(plan.d_tasks, tasks.data(), tasks.size() * sizeof(BoxCopy),
+        MG_CUDA(copy_on(c->stream, plan.d_tasks, tasks.data(), tasks.size() * sizeof(BoxCopy),
                            cudaMemcpyHostToDevice));
     }
     return 0;
@@ -203,7 +203,7 @@ int build_plan(Ctx* c, int ilevel, int layers, int slots, bool corners, bool nor
 
 // Hyperplane traversal table for one grid shape: the same index lists as
 // sip_hyperplane_init_grid + sip_hyperplane_sort, 0-based.
-int build_hp_table(int kk, int jj, int ii, HpTable& t) {
+int build_hp_table(cudaStream_t stream, int kk, int jj, int ii, HpTable& t) {
     t.kk = kk; t.jj = jj; t.ii = ii;
     t.n3dmin = 9;
     t.n3dmax = (ii - 2) + (jj - 2) + (kk - 2);
@@ -226,8 +226,8 @@ int build_hp_table(int kk, int jj, int ii, HpTable& t) {
         return fail(MGLET_ERR_ARG, "hyperplane table does not cover the interior");
     MG_CUDA(cudaMalloc(&t.d_mip, mip.size() * sizeof(int)));
     MG_CUDA(cudaMalloc(&t.d_idx, idx.size() * sizeof(int)));
-    MG_CUDA(cudaMemcpy(t.d_mip, mip.data(), mip.size() * sizeof(int), cudaMemcpyHostToDevice));
-    MG_CUDA(cudaMemcpy(t.d_idx, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice));
+    MG_CUDA(copy_on(stream, t.d_mip, mip.data(), mip.size() * sizeof(int), cudaMemcpyHostToDevice));
+    MG_CUDA(copy_on(stream, t.d_idx, idx.data(), idx.size() * sizeof(int), cudaMemcpyHostToDevice));
     return 0;
 }
 
@@ -254,8 +254,8 @@ int alloc3(Ctx* c, const char* name) {
 int alloc1(Ctx* c, const char* name, long long n, const double* host) {
     double* p = nullptr;
     MG_CUDA(cudaMalloc(&p, (size_t)n * sizeof(double)));
-    if (host) MG_CUDA(cudaMemcpy(p, host, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
-    else MG_CUDA(cudaMemset(p, 0, (size_t)n * sizeof(double)));
+    if (host) MG_CUDA(copy_on(c->stream, p, host, (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+    else MG_CUDA(zero_on(c->stream, p, (size_t)n * sizeof(double)));
     c->f1[name] = p;
     return 0;
 }
@@ -578,11 +578,11 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     c->uniform = shapes.size() == 1;
     c->idim3d = o3; c->idimx = ox; c->idimy = oy; c->idimz = oz;
     MG_CUDA(cudaMalloc(&c->d_grids, c->ngrid * sizeof(DevGrid)));
-    MG_CUDA(cudaMemcpy(c->d_grids, c->grids.data(), c->ngrid * sizeof(DevGrid),
+    MG_CUDA(copy_on(c->stream, c->d_grids, c->grids.data(), c->ngrid * sizeof(DevGrid),
                        cudaMemcpyHostToDevice));
     for (long long key : shapes) {
         HpTable t;
-        if (int rc = build_hp_table((int)(key >> 40), (int)((key >> 20) & 0xFFFFF),
+        if (int rc = build_hp_table(c->stream, (int)(key >> 40), (int)((key >> 20) & 0xFFFFF),
                                     (int)(key & 0xFFFFF), t))
             return bail(rc);
         c->hp.push_back(t);

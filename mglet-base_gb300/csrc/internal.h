@@ -111,6 +111,17 @@ int cuda_fail(cudaError_t e, const char* what);
         if (e_ != cudaSuccess) return ::mg::cuda_fail(e_, #call); \
     } while (0)
 
+// Host <-> device copies and fills ordered on a stream.  The context's stream
+// is non-blocking, so the legacy-stream cudaMemcpy / cudaMemset are not
+// ordered with its kernels; copies also wait for completion, so the host
+// buffer may be released right after.
+inline cudaError_t copy_on(cudaStream_t s, void* dst, const void* src, size_t n,
+                           cudaMemcpyKind kind) {
+    cudaError_t e = cudaMemcpyAsync(dst, src, n, kind, s);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(s);
+}
+inline cudaError_t zero_on(cudaStream_t s, void* p, size_t n) { return cudaMemsetAsync(p, 0, n, s); }
+
 #define MG_LAUNCHED(ctx)                                              \
     do {                                                              \
         (ctx)->launches++;                                            \

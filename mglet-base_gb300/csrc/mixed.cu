@@ -250,7 +250,7 @@ int mixed_init(Ctx* c) {
     const long long lens[3] = {c->idimx, c->idimy, c->idimz};
     for (int q = 0; q < 6; ++q) {
         sp[q].resize(lens[q % 3]);
-        MG_CUDA(cudaMemcpy(sp[q].data(), c->L(names[q]), lens[q % 3] * sizeof(double),
+        MG_CUDA(copy_on(c->stream, sp[q].data(), c->L(names[q]), lens[q % 3] * sizeof(double),
                            cudaMemcpyDeviceToHost));
     }
     std::vector<int> reps;
@@ -295,17 +295,17 @@ int mixed_init(Ctx* c) {
                 }
             }
             MG_CUDA(cudaMalloc(dst[ax], tb.size() * sizeof(float)));
-            MG_CUDA(cudaMemcpy(*dst[ax], tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice));
+            MG_CUDA(copy_on(c->stream, *dst[ax], tb.data(), tb.size() * sizeof(float), cudaMemcpyHostToDevice));
         }
     }
     for (float** p : {&m->du32, &m->dv32, &m->dw32}) {
         MG_CUDA(cudaMalloc(p, (size_t)c->idim3d * sizeof(float)));
-        MG_CUDA(cudaMemset(*p, 0, (size_t)c->idim3d * sizeof(float)));
+        MG_CUDA(zero_on(c->stream, *p, (size_t)c->idim3d * sizeof(float)));
     }
     MG_CUDA(cudaMalloc(&m->d_gcls, c->ngrid * sizeof(int)));
-    MG_CUDA(cudaMemcpy(m->d_gcls, m->gcls.data(), c->ngrid * sizeof(int), cudaMemcpyHostToDevice));
+    MG_CUDA(copy_on(c->stream, m->d_gcls, m->gcls.data(), c->ngrid * sizeof(int), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMalloc(&m->d_ctl, 4 * sizeof(int)));
-    MG_CUDA(cudaMemset(m->d_ctl, 0, 4 * sizeof(int)));
+    MG_CUDA(zero_on(c->stream, m->d_ctl, 4 * sizeof(int)));
     MG_CUDA(cudaMalloc(&m->d_maxrhs, sizeof(double)));
     MG_CUDA(cudaMallocHost(&m->h_ctl, 4 * sizeof(int)));
     MG_CUDA(cudaMallocHost(&m->h_maxrhs, sizeof(double)));
@@ -317,7 +317,7 @@ int mixed_init(Ctx* c) {
     // class coefficients from the representative grids
     int* d_reps = nullptr;
     MG_CUDA(cudaMalloc(&d_reps, reps.size() * sizeof(int)));
-    MG_CUDA(cudaMemcpy(d_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
+    MG_CUDA(copy_on(c->stream, d_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
     int rc = sip_extract(c, m->sip, m->nclass, d_reps, m->d_idx,
                          c->prm.psolver != MGLET_PSOLVER_CLASSIC, &m->cf, &m->cb, &m->apx);
     cudaError_t e = cudaStreamSynchronize(c->stream);

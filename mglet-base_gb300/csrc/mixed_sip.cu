@@ -735,9 +735,9 @@ int sip_init(Ctx* c, SipState& st) {
         set_error("mixed form: hyperplane tables do not cover the grid");
         return MGLET_ERR_ARG;
     }
-    auto up = [](int** d, const std::vector<int>& h) -> int {
+    auto up = [c](int** d, const std::vector<int>& h) -> int {
         MG_CUDA(cudaMalloc(d, h.size() * sizeof(int)));
-        MG_CUDA(cudaMemcpy(*d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+        MG_CUDA(copy_on(c->stream, *d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
         return 0;
     };
     if (int rc = up(&st.d_tpos, tpos)) return rc;
@@ -746,7 +746,7 @@ int sip_init(Ctx* c, SipState& st) {
     if (int rc = up(&st.d_qmap, qmap)) return rc;
     if (int rc = up(&st.d_pq, pq)) return rc;
     MG_CUDA(cudaMalloc(&st.d_rowoff, rowoff.size() * sizeof(short)));
-    MG_CUDA(cudaMemcpy(st.d_rowoff, rowoff.data(), rowoff.size() * sizeof(short),
+    MG_CUDA(copy_on(c->stream, st.d_rowoff, rowoff.data(), rowoff.size() * sizeof(short),
                        cudaMemcpyHostToDevice));
     // face neighbours from the connection table (regular periodic tiling)
     std::vector<int> fn((size_t)6 * c->ngrid, -1);
@@ -769,31 +769,31 @@ int sip_init(Ctx* c, SipState& st) {
     const size_t n = (size_t)c->ngrid * st.npp;
     for (float** p : {&st.h32, &st.r32, &st.rhs32}) {
         MG_CUDA(cudaMalloc(p, n * sizeof(float)));
-        MG_CUDA(cudaMemset(*p, 0, n * sizeof(float)));
+        MG_CUDA(zero_on(c->stream, *p, n * sizeof(float)));
     }
     for (double** p : {&st.rhs64, &st.dp64}) {
         MG_CUDA(cudaMalloc(p, n * sizeof(double)));
-        MG_CUDA(cudaMemset(*p, 0, n * sizeof(double)));
+        MG_CUDA(zero_on(c->stream, *p, n * sizeof(double)));
     }
     const size_t nf = (size_t)c->ngrid * 6 * st.fs;
     MG_CUDA(cudaMalloc(&st.hout, nf * sizeof(float)));
-    MG_CUDA(cudaMemset(st.hout, 0, nf * sizeof(float)));
+    MG_CUDA(zero_on(c->stream, st.hout, nf * sizeof(float)));
     for (int b = 0; b < 3; ++b) {
         MG_CUDA(cudaMalloc(&st.rout[b], nf * sizeof(float)));
-        MG_CUDA(cudaMemset(st.rout[b], 0, nf * sizeof(float)));
+        MG_CUDA(zero_on(c->stream, st.rout[b], nf * sizeof(float)));
     }
     // FP32 copies of the 1-D Poisson coefficients
     const char* n1[6] = {"GSAW", "GSAE", "GSAS", "GSAN", "GSAB", "GSAT"};
     const long long len[6] = {c->idimx, c->idimx, c->idimy, c->idimy, c->idimz, c->idimz};
     for (int qq = 0; qq < 6; ++qq) {
         std::vector<double> h(len[qq]);
-        MG_CUDA(cudaMemcpy(h.data(), c->L(n1[qq]), len[qq] * sizeof(double), cudaMemcpyDeviceToHost));
+        MG_CUDA(copy_on(c->stream, h.data(), c->L(n1[qq]), len[qq] * sizeof(double), cudaMemcpyDeviceToHost));
         std::vector<float> f(h.begin(), h.end()), fl(h.size());
         for (size_t e = 0; e < h.size(); ++e) fl[e] = (float)(h[e] - (double)f[e]);
         MG_CUDA(cudaMalloc(&st.a1[qq], len[qq] * sizeof(float)));
-        MG_CUDA(cudaMemcpy(st.a1[qq], f.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
+        MG_CUDA(copy_on(c->stream, st.a1[qq], f.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
         MG_CUDA(cudaMalloc(&st.a1lo[qq], len[qq] * sizeof(float)));
-        MG_CUDA(cudaMemcpy(st.a1lo[qq], fl.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
+        MG_CUDA(copy_on(c->stream, st.a1lo[qq], fl.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
     }
     const size_t smf = fwd_smem(st), smb = bwd_smem(st);
     if (smf > 200 * 1024 || smb > 200 * 1024) {

@@ -474,8 +474,8 @@ int table_ptrs(Ctx* c, TablePtrs& out) {
     TablePtrs tp;
     MG_CUDA(cudaMalloc(&tp.mips, hm.size() * sizeof(int*)));
     MG_CUDA(cudaMalloc(&tp.idxs, hi.size() * sizeof(int*)));
-    MG_CUDA(cudaMemcpy(tp.mips, hm.data(), hm.size() * sizeof(int*), cudaMemcpyHostToDevice));
-    MG_CUDA(cudaMemcpy(tp.idxs, hi.data(), hi.size() * sizeof(int*), cudaMemcpyHostToDevice));
+    MG_CUDA(copy_on(c->stream, tp.mips, hm.data(), hm.size() * sizeof(int*), cudaMemcpyHostToDevice));
+    MG_CUDA(copy_on(c->stream, tp.idxs, hi.data(), hi.size() * sizeof(int*), cudaMemcpyHostToDevice));
     g_tables[c] = tp;
     out = tp;
     return 0;
