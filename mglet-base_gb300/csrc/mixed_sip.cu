@@ -47,9 +47,11 @@
 namespace mg {
 namespace {
 
-constexpr int kFwdSlots = 6;   // planes t-1 .. t+4
-constexpr int kBwdSlots = 5;   // planes t .. t+4 (reverse order)
-constexpr int kLook = 4;       // records issued ahead of the wavefront
+// Ring depths (plane records).  Shallow rings keep a CTA's shared memory
+// small enough for four CTAs per SM, which hides more latency than deeper
+// prefetch does (measured on 24^3 grids: 4/4 beats 6/5 and 8/7).
+constexpr int kFwdSlots = 4;   // steps t .. t+3
+constexpr int kBwdSlots = 4;   // steps t .. t+3 (planes in reverse order)
 constexpr int kMaxCols = 1024; // one thread per hyperplane point
 // A wait gives up after this many SM clock cycles (about one second); a
 // healthy wait lasts microseconds.
@@ -115,17 +117,11 @@ struct FwdArgs {
     Shape s;
     const int* fnbr;            // [ngrid][6] neighbour grid (0-based) across faces 1..6
     const int* gcls;
-    const float* H;             // padded plane order [ngrid][npp]
-    const float* RHS;
-    float* R;
-    const float* HOUT;          // [ngrid][6][fs]
+    float* R;                   // in: (rhs + lap) * lpr from k_sip_pre; out: res
     const float* RLOW;          // res face buffers with the low ghosts (null: zeros)
     float* RW;                  // res face buffers to write
     const float* CF;            // class blocks: per plane [lw|ls|lb|lpr|ap] x Lp
-    const float *AW, *AE, *AS, *AN, *AB, *AT;   // FP32 1-D coefficients (concatenated)
-    const DevGrid* grids;
     int* ctl;                   // [0] converged (skip), [2] error flag
-    int hzero;
 };
 
 // Shared-memory carve-up common to both sweeps (byte offsets): the ring of
@@ -165,55 +161,115 @@ __device__ __forceinline__ SweepSmem carve(unsigned char* raw, const Shape& s, i
     return m;
 }
 
-// Forward sweep, one thread per point of the current hyperplane.  A record
-// (one ring slot) holds plane r's coefficient block [lw|ls|lb|lpr|ap] (stride
-// Lp), its rhs, its hilf and its point table (io | jo << 10 | ko << 20,
-// -1 = padding).
-// Step t needs planes t-1, t and t+1; thread 0 refills the slot of plane t-2
-// with plane t+4 at the start of step t and waits for plane t+2 before the
-// step's closing barrier, so every other thread only meets __syncthreads.
+struct PreArgs {
+    Shape s;
+    const int* fnbr;
+    const int* gcls;
+    const float* H;             // hilf, padded plane order
+    const float* HOUT;          // hilf face buffers
+    const float* RHS;
+    float* PRE;                 // (rhs + lap) * lpr
+    const float* CF;
+    const float *AW, *AE, *AS, *AN, *AB, *AT;   // FP32 1-D coefficients (concatenated)
+    const DevGrid* grids;
+    const int* ctl;
+    int hzero;
+};
+
+// The part of sipiter1 that does not depend on the recurrence: laplacephi of
+// hilf added to rhs and scaled by lpr (sip_hyperplane_mod.F90:491 with the
+// res laplacephi left in it, laplacephi_mod.F90:153-160).  Every point is
+// independent, so this is a plain streaming pass; the forward sweep then
+// carries only the three-term recurrence.  hilf ghosts come from the face
+// buffers the neighbours' backward sweeps wrote.  One CTA per grid.
+__global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(16) unsigned char psm[];
+    const Shape s = a.s;
+    const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm;
+    int* spst = reinterpret_cast<int*>(psm);
+    short* ro = reinterpret_cast<short*>(spst + nm + 1);
+    for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
+    for (int q = threadIdx.x; q < nm * ni; q += blockDim.x) ro[q] = s.rowoff[q];
+    __syncthreads();
+    const int g = blockIdx.x;
+    const DevGrid G = a.grids[g];
+    const long long base = (long long)g * s.npp;
+    const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
+    const float* H = a.H + base;
+    const bool hz = a.hzero != 0;
+    const int* fn = a.fnbr + 6 * g;
+    const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;   // -x nbr, its x-high plane
+    const float* hxp = a.HOUT + ((long long)fn[1] * 6 + 0) * fs;
+    const float* hym = a.HOUT + ((long long)fn[2] * 6 + 3) * fs;
+    const float* hyp = a.HOUT + ((long long)fn[3] * 6 + 2) * fs;
+    const float* hzm = a.HOUT + ((long long)fn[4] * 6 + 5) * fs;
+    const float* hzp = a.HOUT + ((long long)fn[5] * 6 + 4) * fs;
+    // 1-D coefficients indexed by io, jo, ko (interior index 3 is io = 0)
+    const float *aw = a.AW + G.ipx + 2, *ae = a.AE + G.ipx + 2;
+    const float *as = a.AS + G.ipy + 2, *an = a.AN + G.ipy + 2;
+    const float *ab = a.AB + G.ipz + 2, *at = a.AT + G.ipz + 2;
+    for (int q = threadIdx.x; q < s.npp; q += blockDim.x) {
+        const int v = s.pq[q];
+        if (v < 0) {               // padding stays zero for the bulk copies
+            a.PRE[base + q] = 0.f;
+            continue;
+        }
+        const int io = v & 1023, jo = (v >> 10) & 1023, ko = v >> 20;
+        const int t = io + jo + ko;
+        const int p0 = spst[t], lp = spst[t + 1] - p0, rk = q - p0;
+        const float* cf = CF + 5LL * p0;   // [lw | ls | lb | lpr | ap] with stride lp
+        float lap = 0.f;
+        if (!hz) {
+            // positions of (io, jo, ko-1) on plane t-1 and (io, jo, ko+1) on
+            // plane t+1; the j neighbours sit next to them, the i neighbours
+            // one row over
+            const int bm = (ko > 0 || jo > 0) ? spst[t - 1] + ro[(t - 1) * ni + io] + jo : 0;
+            const int bp = (ko < nk - 1 || jo < nj - 1) ? spst[t + 1] + ro[(t + 1) * ni + io] + jo : 0;
+            const float hc = H[q];
+            const float him = io > 0 ? H[spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo] : hxm[fidx_x(s, ko, jo)];
+            const float hip = io < ni - 1 ? H[spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo] : hxp[fidx_x(s, ko, jo)];
+            const float hjm = jo > 0 ? H[bm - 1] : hym[fidx_y(s, ko, io)];
+            const float hjp = jo < nj - 1 ? H[bp + 1] : hyp[fidx_y(s, ko, io)];
+            const float hkm = ko > 0 ? H[bm] : hzm[fidx_z(s, jo, io)];
+            const float hkp = ko < nk - 1 ? H[bp] : hzp[fidx_z(s, jo, io)];
+            lap = -aw[io] * him - ae[io] * hip - as[jo] * hjm - an[jo] * hjp - ab[ko] * hkm -
+                  at[ko] * hkp - cf[4 * lp + rk] * hc;
+        }
+        a.PRE[base + q] = (a.RHS[base + q] + lap) * cf[3 * lp + rk];
+    }
+}
+
+// Forward sweep, one thread per point of the current hyperplane: the
+// three-term recurrence res -= lb res(k-1) + ls res(j-1) + lw res(i-1)
+// (sip_hyperplane_mod.F90:491-495) on top of k_sip_pre's (rhs + lap) * lpr.
+// A record (one ring slot) holds plane r's [lw|ls|lb] (stride Lp, the head of
+// the class block), its point table (io | jo << 10 | ko << 20, -1 = padding)
+// and its pre-recurrence values.  Step t needs only record t and the res of
+// plane t-1 (shared memory); thread 0 refills the slot of step t-1 with step
+// t+S-1 at the start of step t and waits for step t+1 before the step's
+// closing barrier, so every other thread only meets __syncthreads.
 __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
     if (a.ctl[0]) return;
     extern __shared__ __align__(128) unsigned char smraw[];
     const Shape s = a.s;
     const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm, mlp = s.maxlp;
-    const int rec = 8 * mlp;
+    const int rec = 5 * mlp;
     const SweepSmem m = carve(smraw, s, kFwdSlots, rec);
-    float* gh = m.tail;                  // [6][fs] hilf ghosts
-    float* gr = gh + 6 * fs;             // [3][fs] low res ghosts
-    float* saw = gr + 3 * fs;            // [ii] each
-    float* sae = saw + s.ii;
-    float* sas = sae + s.ii;             // [jj] each
-    float* san = sas + s.jj;
-    float* sab = san + s.jj;             // [kk] each
-    float* sat = sab + s.kk;
+    float* gr = m.tail;                  // [3][fs] low res ghosts
     unsigned long long* bars =
-        reinterpret_cast<unsigned long long*>(((size_t)(sat + s.kk) + 15) & ~(size_t)15);
+        reinterpret_cast<unsigned long long*>(((size_t)(gr + 3 * fs) + 15) & ~(size_t)15);
     unsigned long long* gbar = bars + kFwdSlots;
     const int g = blockIdx.x;
     const int tid = threadIdx.x;
-    const DevGrid G = a.grids[g];
     const long long base = (long long)g * s.npp;
     const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
-    const bool hz = a.hzero != 0;
     // error flag of step t in sflag[t & 1], written by thread 0 before the
     // step's closing barrier and read by everyone after it; two slots so that
     // thread 0 running ahead never overwrites a flag still being read
     __shared__ int sflag[2];
     for (int q = tid; q < nm * ni; q += blockDim.x) m.rowoff[q] = s.rowoff[q];
     for (int q = tid; q <= nm; q += blockDim.x) m.pst[q] = s.pst[q];
-    for (int q = tid; q < s.ii; q += blockDim.x) {
-        saw[q] = a.AW[G.ipx + q];        // saw[i-1] = aw(i)
-        sae[q] = a.AE[G.ipx + q];
-    }
-    for (int q = tid; q < s.jj; q += blockDim.x) {
-        sas[q] = a.AS[G.ipy + q];
-        san[q] = a.AN[G.ipy + q];
-    }
-    for (int q = tid; q < s.kk; q += blockDim.x) {
-        sab[q] = a.AB[G.ipz + q];
-        sat[q] = a.AT[G.ipz + q];
-    }
     if (!a.RLOW)
         for (int q = tid; q < 3 * fs; q += blockDim.x) gr[q] = 0.f;
     if (tid == 0) {
@@ -223,18 +279,18 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
     }
     int issued = -1, waited = -1;   // thread 0's bookkeeping of the ring
     int bad = 0;
+    float* R = a.R + base;
     auto issue = [&](int r) {
         if (r >= nm) return;
         issued = r;
         const int sl = r % kFwdSlots;
         const int p0 = m.pst[r], lp = m.pst[r + 1] - p0;
         float* d = m.ring + sl * rec;
-        const unsigned b5 = 5u * lp * 4u, b1 = (unsigned)lp * 4u;
-        bar_expect(&bars[sl], b5 + 2u * b1 + (hz ? 0u : b1));
-        bulk_load(d, CF + 5LL * p0, b5, &bars[sl]);
-        bulk_load(d + 5 * mlp, a.RHS + base + p0, b1, &bars[sl]);
-        if (!hz) bulk_load(d + 6 * mlp, a.H + base + p0, b1, &bars[sl]);
-        bulk_load(d + 7 * mlp, s.pq + p0, b1, &bars[sl]);
+        const unsigned b3 = 3u * lp * 4u, b1 = (unsigned)lp * 4u;
+        bar_expect(&bars[sl], b3 + 2u * b1);
+        bulk_load(d, CF + 5LL * p0, b3, &bars[sl]);
+        bulk_load(d + 3 * mlp, s.pq + p0, b1, &bars[sl]);
+        bulk_load(d + 4 * mlp, R + p0, b1, &bars[sl]);
     };
     auto wait_rec = [&](int r) -> bool {
         if (r >= nm || r <= waited) return true;
@@ -245,69 +301,41 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
     const int* fn = a.fnbr + 6 * g;
     __syncthreads();
     if (tid == 0) {
-        // ghost faces: hilf of the six neighbours' facing planes (unless hilf
-        // is zero) and res of the three low neighbours (unless none yet)
+        // low res ghosts: the three low neighbours' facing planes (unless none yet)
         const unsigned fb = (unsigned)fs * 4u;
-        bar_expect(gbar, (hz ? 0u : 6u * fb) + (a.RLOW ? 3u * fb : 0u));
-        if (!hz) {
-            const int src_slot[6] = {1, 0, 3, 2, 5, 4};   // -x nbr's x-high plane, ...
-            for (int f = 0; f < 6; ++f)
-                bulk_load(gh + f * fs, a.HOUT + ((long long)fn[f] * 6 + src_slot[f]) * fs, fb, gbar);
-        }
+        bar_expect(gbar, a.RLOW ? 3u * fb : 0u);
         if (a.RLOW) {
             bulk_load(gr + 0 * fs, a.RLOW + ((long long)fn[0] * 6 + 1) * fs, fb, gbar);
             bulk_load(gr + 1 * fs, a.RLOW + ((long long)fn[2] * 6 + 3) * fs, fb, gbar);
             bulk_load(gr + 2 * fs, a.RLOW + ((long long)fn[4] * 6 + 5) * fs, fb, gbar);
         }
-        for (int r = 0; r <= kLook; ++r) issue(r);
-        if (!bar_wait(gbar, 0) || !wait_rec(0) || !wait_rec(1)) bad = sflag[1] = 1;
+        for (int r = 0; r < kFwdSlots; ++r) issue(r);
+        if (!bar_wait(gbar, 0) || !wait_rec(0)) bad = sflag[1] = 1;
     }
     __syncthreads();
-    const float *hxm = gh, *hxp = gh + fs, *hym = gh + 2 * fs, *hyp = gh + 3 * fs,
-                *hzm = gh + 4 * fs, *hzp = gh + 5 * fs;
     const float *rxm = gr, *rym = gr + fs, *rzm = gr + 2 * fs;
     float* rw = a.RW + (long long)g * 6 * fs;
-    float* R = a.R + base;
     const short* ro = m.rowoff;
     for (int t = 0; t < nm; ++t) {
         if (sflag[(t + 1) & 1]) break;   // step t-1's flag, read after its barrier: uniform
         if (tid == 0 && t >= 1) {
             proxy_fence();
-            issue(t + kLook);   // slot of plane t-2, released by the last barrier
+            issue(t + kFwdSlots - 1);   // slot of step t-1, released by the last barrier
         }
         const int p0 = m.pst[t], lp = m.pst[t + 1] - p0;
         const float* c0 = m.ring + (t % kFwdSlots) * rec;
-        const int pq = tid < lp ? reinterpret_cast<const int*>(c0 + 7 * mlp)[tid] : -1;
+        const int pq = tid < lp ? reinterpret_cast<const int*>(c0 + 3 * mlp)[tid] : -1;
         if (pq >= 0) {
             const int io = pq & 1023, jo = (pq >> 10) & 1023, ko = t - io - jo;
-            const int i = io + 3, j = jo + 3, k = ko + 3;
             // rank of (io, jo, ko-1) in plane t-1; (io, jo-1, ko) is the one before it
             const int rm = (ko > 0 || jo > 0) ? ro[(t - 1) * ni + io] + jo : 0;
             const int rim = io > 0 ? ro[(t - 1) * ni + io - 1] + jo : 0;
-            float lap = 0.f;
-            if (!hz) {
-                const float* hcur = c0 + 6 * mlp;
-                const float* hm1 = m.ring + ((t + kFwdSlots - 1) % kFwdSlots) * rec + 6 * mlp;
-                const float* hp1 = m.ring + ((t + 1) % kFwdSlots) * rec + 6 * mlp;
-                // rank of (io, jo, ko+1) in plane t+1; (io, jo+1, ko) is the one after it
-                const int rp = (ko < nk - 1 || jo < nj - 1) ? ro[(t + 1) * ni + io] + jo : 0;
-                const int rip = io < ni - 1 ? ro[(t + 1) * ni + io + 1] + jo : 0;
-                const float hc = hcur[tid];
-                const float hkm = ko > 0 ? hm1[rm] : hzm[fidx_z(s, jo, io)];
-                const float hkp = ko < nk - 1 ? hp1[rp] : hzp[fidx_z(s, jo, io)];
-                const float hjm = jo > 0 ? hm1[rm - 1] : hym[fidx_y(s, ko, io)];
-                const float hjp = jo < nj - 1 ? hp1[rp + 1] : hyp[fidx_y(s, ko, io)];
-                const float him = io > 0 ? hm1[rim] : hxm[fidx_x(s, ko, jo)];
-                const float hip = io < ni - 1 ? hp1[rip] : hxp[fidx_x(s, ko, jo)];
-                lap = -saw[i - 1] * him - sae[i - 1] * hip - sas[j - 1] * hjm - san[j - 1] * hjp -
-                      sab[k - 1] * hkm - sat[k - 1] * hkp - c0[4 * lp + tid] * hc;
-            }
             const float* xp = m.xr + ((t + 1) & 1) * mlp;   // res of plane t-1
             const float rkm = ko > 0 ? xp[rm] : rzm[fidx_z(s, jo, io)];
             const float rjm = jo > 0 ? xp[rm - 1] : rym[fidx_y(s, ko, io)];
             const float rimv = io > 0 ? xp[rim] : rxm[fidx_x(s, ko, jo)];
-            // block layout: [lw | ls | lb | lpr | ap] with stride lp
-            float r = (c0[5 * mlp + tid] + lap) * c0[3 * lp + tid];
+            // block layout: [lw | ls | lb] with stride lp
+            float r = c0[4 * mlp + tid];
             r = r - c0[2 * lp + tid] * rkm - c0[lp + tid] * rjm - c0[tid] * rimv;
             R[p0 + tid] = r;
             if (io == 0) rw[0 * fs + fidx_x(s, ko, jo)] = r;
@@ -318,7 +346,7 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
             if (ko == nk - 1) rw[5 * fs + fidx_z(s, jo, io)] = r;
             m.xr[(t & 1) * mlp + tid] = r;
         }
-        if (tid == 0 && !wait_rec(t + 2)) bad = sflag[t & 1] = 1;
+        if (tid == 0 && !wait_rec(t + 1)) bad = sflag[t & 1] = 1;
         __syncthreads();
     }
     if (tid == 0 && bad) {
@@ -668,9 +696,8 @@ Shape shape(const SipState& st) {
 int sweep_threads(const SipState& st) { return (st.maxlp + 31) / 32 * 32; }
 
 size_t fwd_smem(const SipState& st) {
-    const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kFwdSlots, 8 * st.maxlp);
-    const size_t tail = (size_t)9 * st.fs * 4 + (size_t)2 * (st.ii + st.jj + st.kk) * 4;
-    return align16(l.tail + tail) + (kFwdSlots + 1) * 8;
+    const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kFwdSlots, 5 * st.maxlp);
+    return align16(l.tail + (size_t)3 * st.fs * 4) + (kFwdSlots + 1) * 8;
 }
 
 size_t outer_smem(const SipState& st) { return (size_t)(st.nm + 1) * 4 + (size_t)st.nm * st.ni * 2; }
@@ -844,20 +871,30 @@ int sip_divcal(Ctx* c, SipState& st, double fak) {
 
 int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
                 int rwrite, bool hzero) {
+    {
+        ProfScope ps_(c, "mx_sip_pre");
+        PreArgs p;
+        p.s = shape(st);
+        p.fnbr = st.d_fnbr; p.gcls = gcls;
+        p.H = st.h32; p.HOUT = st.hout; p.RHS = st.rhs32; p.PRE = st.r32;
+        p.CF = cf;
+        p.AW = st.a1[0]; p.AE = st.a1[1]; p.AS = st.a1[2]; p.AN = st.a1[3]; p.AB = st.a1[4];
+        p.AT = st.a1[5];
+        p.grids = c->d_grids;
+        p.ctl = ctl;
+        p.hzero = hzero ? 1 : 0;
+        k_sip_pre<<<c->ngrid, 512, outer_smem(st), c->stream>>>(p);
+        MG_LAUNCHED(c);
+    }
     ProfScope ps_(c, "mx_sip_fwd");
     FwdArgs a;
     a.s = shape(st);
     a.fnbr = st.d_fnbr; a.gcls = gcls;
-    a.H = st.h32; a.RHS = st.rhs32; a.R = st.r32;
-    a.HOUT = st.hout;
+    a.R = st.r32;
     a.RLOW = rlow >= 0 ? st.rout[rlow] : nullptr;
     a.RW = st.rout[rwrite];
     a.CF = cf;
-    a.AW = st.a1[0]; a.AE = st.a1[1]; a.AS = st.a1[2]; a.AN = st.a1[3]; a.AB = st.a1[4];
-    a.AT = st.a1[5];
-    a.grids = c->d_grids;
     a.ctl = ctl;
-    a.hzero = hzero ? 1 : 0;
     const int threads = sweep_threads(st);
     k_sip_fwd<<<c->ngrid, threads, fwd_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
