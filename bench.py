@@ -51,29 +51,35 @@ PLAIN_BYTES = {
 }
 MIXED_BYTES = {
     "mx_flux": 8 * 4 + 4 * 6 + 8 * 3,   # read u,v,w,p (f64), du,dv,dw (f32); write du,dv,dw, u,v,w
-    "mx_outer": 4 + 8 * 3 + 4,          # read hilf (f32), rhs, dp; write rhs, rhs32, dp
-    "mx_divcal": 8 * 3 + 8 + 4,         # read u,v,w; write rhs (f64) and rhs32
+    "mx_divcal": 8 * 3 + 4 * 2,         # read u,v,w; write rhs (float-float)
     "mx_mgpcorr": 8 + 8 * 4 * 2,        # read dp, u,v,w,p; write u,v,w,p
-    "mx_scatter": 8 + 8,                # read dp (plane order); write DP
+    "mx_scatter": 4 * 2 + 8,            # read dp (float-float, plane order); write DP
 }
 
 
 def kernel_bytes(name, case, ninner):
     """Algorithmic bytes of one launch of a kernel family on this case.
-    The SIP sweeps (FP32, plane order) read rhs and hilf and write res
-    (forward), read res and hilf and write hilf (backward), except that the
-    first inner iteration of an outer iteration starts from hilf = 0 and reads
-    no hilf; both also move their face buffers (six written, three or six
-    read per grid).  Class coefficients, shared by all grids of a class and
-    served from L2, are not counted."""
+    FP32 plane-order SIP kernels: the pre-pass reads hilf and rhs and writes
+    (rhs + laplacian) x lpr; the forward recurrence reads that and writes res
+    over it; the backward sweep reads res and hilf and writes hilf; the outer
+    step reads hilf and the float-float residual and correction and writes
+    both back.  The first inner iteration of an outer iteration starts from
+    hilf = 0 and reads no hilf.  Face buffers: six written, three read per
+    grid and sweep, six hilf faces read by the pre-pass and the outer step.
+    Class coefficients, shared by all grids of a class and served from L2,
+    are not counted."""
     cells = case.ncells
     nk, nj, ni = case.kk - 4, case.jj - 4, case.ii - 4
     face = case.ngrid * 4 * ((max(nj * nk, ni * nk, ni * nj) + 3) // 4 * 4)
     hz = 1.0 / ninner
+    if name == "mx_sip_pre":
+        return cells * (12 - 4 * hz) + face * 6 * (1 - hz)
     if name == "mx_sip_fwd":
-        return cells * (12 - 4 * hz) + face * (6 + 3 + 6 * (1 - hz))
+        return cells * 8 + face * (6 + 3)
     if name == "mx_sip_bwd":
         return cells * (12 - 4 * hz) + face * (6 + 3)
+    if name == "mx_outer":
+        return cells * (4 + 4 * 4 + 4 * 4) + face * 6
     per = MIXED_BYTES.get(name, PLAIN_BYTES.get(name))
     return per * cells if per else None
 
@@ -189,9 +195,10 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def cpu_sample(threads=None, tiles=(4, 4, 4), steps=2, warmup=1):
+def cpu_sample(threads=None, tiles=(8, 8, 8), steps=4, warmup=1):
     """The CPU restatement on a bounded sample of the same workload: a
-    periodic 4x4x4 tiling of 24^3 grids (0.88 M cells), Williamson RK3."""
+    periodic 8x8x8 tiling of 24^3 grids (7.1 M cells), Williamson RK3,
+    about ten seconds of host work."""
     from oracle import binding
     from mglet_gb300 import cases
     binding.build()
@@ -238,7 +245,7 @@ def run_reference(args, rank):
         "data": "synthetic: Taylor-Green + splitmix64 noise (seed 42)",
         "config": {"workload": "periodic 4096 x 24^3 grids (16x16x16), TG+noise, RK3 dt=5e-4, "
                                "SIP ninner=5 nouter=9 epcorr=1e-10; each step a bounded sample",
-                   "sample_tiling": "4x4x4"},
+                   "sample_tiling": "8x8x8"},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},

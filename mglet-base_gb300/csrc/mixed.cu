@@ -138,7 +138,8 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
     SipState& s = m->sip;
     const double prefak = c->prm.rho / dt;
     double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P"), *dp = c->F("DP");
-    MG_CUDA(cudaMemsetAsync(s.dp64, 0, (size_t)c->ngrid * s.npp * sizeof(double), c->stream));
+    MG_CUDA(cudaMemsetAsync(s.dph, 0, (size_t)c->ngrid * s.npp * sizeof(float), c->stream));
+    MG_CUDA(cudaMemsetAsync(s.dpl, 0, (size_t)c->ngrid * s.npp * sizeof(float), c->stream));
     MG_CUDA(cudaMemsetAsync(m->d_ctl, 0, 3 * sizeof(int), c->stream));
     if (int rc = sip_divcal(c, s, prefak)) return rc;
     int* ctl = m->d_ctl;

@@ -113,6 +113,28 @@ __device__ __forceinline__ void proxy_fence() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
+// Thread 0: copy a grid's whole plane-ordered array (n floats, n a multiple
+// of 4) into shared memory with bulk copies of at most 32 KB completing on
+// bar, and wait for it (bounded; a second bounded wait lets copies still in
+// flight land before the caller gives up).
+__device__ __forceinline__ bool stage_grid(float* dst, const float* src, int n,
+                                           unsigned long long* bar) {
+    bar_expect(bar, (unsigned)n * 4u);
+    for (int o = 0; o < n; o += 8192) {
+        const int len = n - o < 8192 ? n - o : 8192;
+        bulk_load(dst + o, src + o, (unsigned)len * 4u, bar);
+    }
+    if (bar_wait(bar, 0)) return true;
+    bar_wait(bar, 0);
+    return false;
+}
+
+// Shared memory of the streaming stencil kernels: plane starts, row offsets,
+// then the grid's hilf and its barrier.
+__host__ __device__ inline size_t stencil_tables_bytes(int nm, int ni) {
+    return ((size_t)(nm + 1) * 4 + (size_t)nm * ni * 2 + 15) & ~(size_t)15;
+}
+
 struct FwdArgs {
     Shape s;
     const int* fnbr;            // [ngrid][6] neighbour grid (0-based) across faces 1..6
@@ -172,7 +194,7 @@ struct PreArgs {
     const float* CF;
     const float *AW, *AE, *AS, *AN, *AB, *AT;   // FP32 1-D coefficients (concatenated)
     const DevGrid* grids;
-    const int* ctl;
+    int* ctl;
     int hzero;
 };
 
@@ -193,11 +215,11 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     for (int q = threadIdx.x; q < nm * ni; q += blockDim.x) ro[q] = s.rowoff[q];
     __syncthreads();
     const int g = blockIdx.x;
-    const DevGrid G = a.grids[g];
     const long long base = (long long)g * s.npp;
-    const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
-    const float* H = a.H + base;
     const bool hz = a.hzero != 0;
+    const float* H = a.H + base;   // neighbours gathered through L1
+    const DevGrid G = a.grids[g];
+    const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
     const int* fn = a.fnbr + 6 * g;
     const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;   // -x nbr, its x-high plane
     const float* hxp = a.HOUT + ((long long)fn[1] * 6 + 0) * fs;
@@ -503,15 +525,17 @@ struct OuterArgs {
     const int* gcls;
     const float* H;
     const float* HOUT;
-    double* RHS64;
-    float* RHS32;
-    double* DP64;
+    float* RHS;                 // rhs = RHS + RHSL in float-float; RHS alone is the sweeps' FP32 rhs
+    float* RHSL;
+    float* DPH;                 // dp = DPH + DPL in float-float
+    float* DPL;
     const float* APX;           // class ap split in two floats: [ncls][hi npp | lo npp]
     const float* A1[6];         // 1-D coefficients aw, ae, as, an, ab, at: FP32 rounding
     const float* A1L[6];        //   and the FP32 rounding of the remainder
     const DevGrid* grids;
     double* gridmax;
     const int* ctl;
+    int* ctl_err;               // ctl[2]
 };
 
 // a + b = s + e exactly (Knuth's TwoSum, no order of magnitudes assumed)
@@ -532,10 +556,11 @@ __device__ __forceinline__ void ff_acc(float ch, float cl, float h, float& sum, 
 }
 
 // Outer step (laplacephi + rescal + maxabscal_grid + accumulate_pcorr):
-// rhs <- rhs - A hilf, dp <- dp + hilf, per-grid max|rhs|.  A hilf is formed
-// in float-float arithmetic (about 48 significant bits; hilf itself is FP32)
-// and subtracted from the FP64 residual, so only the residual and dp updates
-// use the FP64 pipe.  One CTA per grid walks its points in plane order.
+// rhs <- rhs - A hilf, dp <- dp + hilf, per-grid max|rhs|.  The residual and
+// the accumulated correction are float-float pairs (about 48 significant
+// bits; hilf itself is FP32) and A hilf is formed in float-float arithmetic,
+// so the step runs on the FP32 pipe only: GB300 issues FP64 at a small
+// fraction of its FP32 rate.  One CTA per grid walks its points in plane order.
 __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
     if (a.ctl[0]) return;
     __shared__ double sh[32];
@@ -544,15 +569,27 @@ __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
     const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm;
     int* spst = reinterpret_cast<int*>(osm);
     short* ro = reinterpret_cast<short*>(spst + nm + 1);
+    float* H = reinterpret_cast<float*>(osm + stencil_tables_bytes(nm, ni));   // the grid's hilf
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(H + s.npp);
+    __shared__ int sok;
+    const int g = blockIdx.x;
+    const long long base = (long long)g * s.npp;
     for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
     for (int q = threadIdx.x; q < nm * ni; q += blockDim.x) ro[q] = s.rowoff[q];
+    if (threadIdx.x == 0) {
+        bar_init(bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
     __syncthreads();
-    const int g = blockIdx.x;
+    if (threadIdx.x == 0) sok = stage_grid(H, a.H + base, s.npp, bar);
+    __syncthreads();
+    if (!sok) {
+        if (threadIdx.x == 0) atomicExch(a.ctl_err, 1);
+        return;
+    }
     const DevGrid G = a.grids[g];
-    const long long base = (long long)g * s.npp;
     const float* APH = a.APX + (long long)a.gcls[g] * 2 * s.npp;
     const float* APL = APH + s.npp;
-    const float* H = a.H + base;
     const int* fn = a.fnbr + 6 * g;
     const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;
     const float* hxp = a.HOUT + ((long long)fn[1] * 6 + 0) * fs;
@@ -567,7 +604,7 @@ __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
     const float *anh = a.A1[3] + G.ipy + 2, *anl = a.A1L[3] + G.ipy + 2;
     const float *abh = a.A1[4] + G.ipz + 2, *abl = a.A1L[4] + G.ipz + 2;
     const float *ath = a.A1[5] + G.ipz + 2, *atl = a.A1L[5] + G.ipz + 2;
-    long long mxb = 0;   // max |r| as the bit pattern of a non-negative double
+    float mx = 0.f;      // max |rhs| (its leading float)
     for (int q = threadIdx.x; q < s.npp; q += blockDim.x) {
         const int v = s.pq[q];
         if (v < 0) continue;
@@ -592,19 +629,31 @@ __global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
         ff_acc(abh[ko], abl[ko], hkm, sum, comp);
         ff_acc(ath[ko], atl[ko], hkp, sum, comp);
         ff_acc(APH[q], APL[q], hc, sum, comp);
-        const double r = (a.RHS64[base + q] - (double)sum) - (double)comp;
-        a.RHS64[base + q] = r;
-        a.RHS32[base + q] = (float)r;
-        a.DP64[base + q] = a.DP64[base + q] + (double)hc;
-        mxb = max(mxb, __double_as_longlong(r) & 0x7fffffffffffffffLL);
+        // (rh + rl) - (sum + comp)
+        float rh, e;
+        two_sum(a.RHS[base + q], -sum, rh, e);
+        e = e + (a.RHSL[base + q] - comp);
+        float rl;
+        two_sum(rh, e, rh, rl);
+        a.RHS[base + q] = rh;
+        a.RHSL[base + q] = rl;
+        // (dh + dl) + hc
+        float dh, de;
+        two_sum(a.DPH[base + q], hc, dh, de);
+        de = de + a.DPL[base + q];
+        float dl;
+        two_sum(dh, de, dh, dl);
+        a.DPH[base + q] = dh;
+        a.DPL[base + q] = dl;
+        mx = fmaxf(mx, fabsf(rh));
     }
-    const double mx = block_max2(__longlong_as_double(mxb), sh);
-    if (threadIdx.x == 0) a.gridmax[g] = mx;
+    const double mxd = block_max2((double)mx, sh);
+    if (threadIdx.x == 0) a.gridmax[g] = mxd;
 }
 
 // divcal into the plane-ordered FP64/FP32 residual (noib_mod.F90:304-354)
 __global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const int* __restrict__ idxp,
-                             double* __restrict__ RHS64, float* __restrict__ RHS32,
+                             float* __restrict__ RHS, float* __restrict__ RHSL,
                              const double* __restrict__ U, const double* __restrict__ V,
                              const double* __restrict__ W, const double* __restrict__ RDDX,
                              const double* __restrict__ RDDY, const double* __restrict__ RDDZ,
@@ -615,8 +664,8 @@ __global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const i
     const long long o = (long long)g * npp + q;
     const int id = idxp[q];
     if (id < 0) {       // padding stays zero for the bulk copies
-        RHS64[o] = 0.0;
-        RHS32[o] = 0.f;
+        RHS[o] = 0.f;
+        RHSL[o] = 0.f;
         return;
     }
     const DevGrid G = grids[g];
@@ -626,18 +675,21 @@ __global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const i
     const double d = fak * ((u[id] - u[id - kk * jj]) * RDDX[G.ipx + i - 1] +
                             (v[id] - v[id - kk]) * RDDY[G.ipy + j - 1] +
                             (w[id] - w[id - 1]) * RDDZ[G.ipz + k - 1]);
-    RHS64[o] = d;
-    RHS32[o] = (float)d;
+    const float dh = (float)d;   // float-float: leading float and the rounding of the rest
+    RHS[o] = dh;
+    RHSL[o] = (float)(d - (double)dh);
 }
 
-// dp (plane order) -> DP field (natural layout, interior)
+// dp (plane order, float-float) -> DP field (natural layout, interior, FP64)
 __global__ void k_sip_scatter(const DevGrid* __restrict__ grids, int npp, const int* __restrict__ idxp,
-                              const double* __restrict__ DP64, double* __restrict__ DP) {
+                              const float* __restrict__ DPH, const float* __restrict__ DPL,
+                              double* __restrict__ DP) {
     const int g = blockIdx.y;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= npp) return;
     const int id = idxp[q];
-    if (id >= 0) DP[grids[g].ip3 + id] = DP64[(long long)g * npp + q];
+    const long long o = (long long)g * npp + q;
+    if (id >= 0) DP[grids[g].ip3 + id] = (double)DPH[o] + (double)DPL[o];
 }
 
 // class coefficients (FP64 fields of a representative grid, plane order of
@@ -700,7 +752,9 @@ size_t fwd_smem(const SipState& st) {
     return align16(l.tail + (size_t)3 * st.fs * 4) + (kFwdSlots + 1) * 8;
 }
 
-size_t outer_smem(const SipState& st) { return (size_t)(st.nm + 1) * 4 + (size_t)st.nm * st.ni * 2; }
+size_t stencil_smem(const SipState& st) {
+    return stencil_tables_bytes(st.nm, st.ni) + (size_t)st.npp * 4 + 8;
+}
 
 size_t bwd_smem(const SipState& st) {
     const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kBwdSlots, 6 * st.maxlp);
@@ -798,9 +852,9 @@ int sip_init(Ctx* c, SipState& st) {
         MG_CUDA(cudaMalloc(p, n * sizeof(float)));
         MG_CUDA(zero_on(c->stream, *p, n * sizeof(float)));
     }
-    for (double** p : {&st.rhs64, &st.dp64}) {
-        MG_CUDA(cudaMalloc(p, n * sizeof(double)));
-        MG_CUDA(zero_on(c->stream, *p, n * sizeof(double)));
+    for (float** p : {&st.rhsl, &st.dph, &st.dpl}) {
+        MG_CUDA(cudaMalloc(p, n * sizeof(float)));
+        MG_CUDA(zero_on(c->stream, *p, n * sizeof(float)));
     }
     const size_t nf = (size_t)c->ngrid * 6 * st.fs;
     MG_CUDA(cudaMalloc(&st.hout, nf * sizeof(float)));
@@ -829,6 +883,12 @@ int sip_init(Ctx* c, SipState& st) {
     }
     MG_CUDA(cudaFuncSetAttribute(k_sip_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
     MG_CUDA(cudaFuncSetAttribute(k_sip_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
+    const size_t sms = stencil_smem(st);
+    if (sms > 227 * 1024) {
+        set_error("mixed form: a grid's hilf does not fit in shared memory");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    MG_CUDA(cudaFuncSetAttribute(k_sip_outer, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sms));
     return 0;
 }
 
@@ -851,7 +911,7 @@ void sip_release(SipState& st) {
     for (void* p : {(void*)st.d_tpos, (void*)st.d_pst, (void*)st.d_idxp, (void*)st.d_qmap,
                     (void*)st.d_pq, (void*)st.d_rowoff,
                     (void*)st.d_fnbr, (void*)st.h32, (void*)st.r32, (void*)st.rhs32,
-                    (void*)st.rhs64, (void*)st.dp64, (void*)st.hout, (void*)st.rout[0],
+                    (void*)st.rhsl, (void*)st.dph, (void*)st.dpl, (void*)st.hout, (void*)st.rout[0],
                     (void*)st.rout[1], (void*)st.rout[2], (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
@@ -862,7 +922,7 @@ void sip_release(SipState& st) {
 int sip_divcal(Ctx* c, SipState& st, double fak) {
     ProfScope ps_(c, "mx_divcal");
     dim3 grid((st.npp + 255) / 256, c->ngrid);
-    k_sip_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.rhs64, st.rhs32,
+    k_sip_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.rhs32, st.rhsl,
                                               c->F("U"), c->F("V"), c->F("W"), c->L("RDDX"),
                                               c->L("RDDY"), c->L("RDDZ"), fak);
     MG_LAUNCHED(c);
@@ -883,7 +943,7 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
         p.grids = c->d_grids;
         p.ctl = ctl;
         p.hzero = hzero ? 1 : 0;
-        k_sip_pre<<<c->ngrid, 512, outer_smem(st), c->stream>>>(p);
+        k_sip_pre<<<c->ngrid, 512, stencil_tables_bytes(st.nm, st.ni), c->stream>>>(p);
         MG_LAUNCHED(c);
     }
     ProfScope ps_(c, "mx_sip_fwd");
@@ -923,7 +983,7 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     a.s = shape(st);
     a.fnbr = st.d_fnbr; a.gcls = gcls;
     a.H = st.h32; a.HOUT = st.hout;
-    a.RHS64 = st.rhs64; a.RHS32 = st.rhs32; a.DP64 = st.dp64; a.APX = apx;
+    a.RHS = st.rhs32; a.RHSL = st.rhsl; a.DPH = st.dph; a.DPL = st.dpl; a.APX = apx;
     for (int q = 0; q < 6; ++q) {
         a.A1[q] = st.a1[q];
         a.A1L[q] = st.a1lo[q];
@@ -931,7 +991,8 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     a.grids = c->d_grids;
     a.gridmax = c->d_gridred;
     a.ctl = ctl;
-    k_sip_outer<<<c->ngrid, 512, outer_smem(st), c->stream>>>(a);
+    a.ctl_err = const_cast<int*>(ctl) + 2;
+    k_sip_outer<<<c->ngrid, 512, stencil_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }
@@ -939,7 +1000,8 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
 int sip_scatter_dp(Ctx* c, SipState& st) {
     ProfScope ps_(c, "mx_scatter");
     dim3 grid((st.npp + 255) / 256, c->ngrid);
-    k_sip_scatter<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.dp64, c->F("DP"));
+    k_sip_scatter<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.dph, st.dpl,
+                                               c->F("DP"));
     MG_LAUNCHED(c);
     return 0;
 }

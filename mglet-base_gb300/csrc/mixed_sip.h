@@ -17,8 +17,10 @@ struct SipState {
     int* d_pq = nullptr;        // [npp] io | jo << 16 of each padded position, -1 for padding
     short* d_rowoff = nullptr;  // [nm][ni] rank of (io, jo = 0) in plane m
     int* d_fnbr = nullptr;      // [ngrid][6] face neighbours (0-based)
-    float *h32 = nullptr, *r32 = nullptr, *rhs32 = nullptr;   // [ngrid][npp]
-    double *rhs64 = nullptr, *dp64 = nullptr;                 // [ngrid][npp]
+    float *h32 = nullptr, *r32 = nullptr;                     // [ngrid][npp]
+    // outer residual and accumulated correction as float-float pairs; the
+    // leading float of the residual is the sweeps' FP32 rhs
+    float *rhs32 = nullptr, *rhsl = nullptr, *dph = nullptr, *dpl = nullptr;
     float* hout = nullptr;      // [ngrid][6][fs] hilf boundary planes
     float* rout[3] = {nullptr, nullptr, nullptr};   // rotating res boundary planes
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
