@@ -201,6 +201,23 @@ int mglet_gpu_laplacephi(mglet_ctx* ctx, const char* res, const char* phi);
  * closing connect(2 layers, corners). */
 int mglet_gpu_mgpoisl(mglet_ctx* ctx, double dt, int32_t ittot, int32_t irk,
                       mglet_stage_stats* stats);
+/* bound_flow%bound(ilevel, u, v, w, p) (src/core/bound_mod.F90:36-76 over
+ * src/flow/bound_flow_mod.F90:23-730): FIX, OP1, NOS and SLI faces of every
+ * grid, faces 1..6 in order, on the device fields U, V, W, P; ilevel <= 0
+ * means all levels.  CON/CO1 faces are left to connect. */
+int mglet_gpu_bound_flow(mglet_ctx* ctx, int32_t ilevel);
+/* Boundary buffer of U, V or W on face iface (1..6) of grid igrid (1-based),
+ * the plane field_t%get_buffer(buf, igrid, iface) returns
+ * (src/core/field_t/realfield_mod.F90:430-503): (kk,jj) for faces 1-2,
+ * (kk,ii) for 3-4, (jj,ii) for 5-6, first index fastest; n its size.  FIX
+ * faces take their prescribed velocities from it (setboundarybuffers fills
+ * it in the reference), OP1 faces their inflow tangential velocities. */
+int mglet_gpu_set_buffer(mglet_ctx* ctx, const char* name, int32_t igrid, int32_t iface,
+                         const double* host, int64_t n);
+/* The real parameter of an OP1 face, the far-field pressure pinf
+ * (get_bcprms with nreal = 1, src/flow/bound_flow_mod.F90:226-236); faces
+ * without one use pinf = 0. */
+int mglet_gpu_set_bc_real(mglet_ctx* ctx, int32_t igrid, int32_t iface, double value);
 /* compcflmax / compdivmax / enerfg of itinfo_flow
  * (src/flow/timeintegration_mod.F90:202-240); out->exploded mirrors the NaN
  * check of itinfo_print (src/flow/itinfo_mod.F90:296-320). */

@@ -379,6 +379,8 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
         maxrhs = c->h_scalar[0];
     }
     if (int rc = launch_mgpcorr(c, U, V, W, P, dp, dt / c->prm.rho)) return rc;
+    // pressuresolver_mod.F90:341-348: bound, then the corner connect
+    if (int rc = launch_bound_flow(c, U, V, W, P)) return rc;
     if (int rc = connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
     if (st) {
         st->ipc = ipc;
@@ -414,8 +416,11 @@ static int stage_plain(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk,
     if (int rc = launch_rkstep(c, U, c->F("DU"), UO, frhs, dt * fu)) return rc;
     if (int rc = launch_rkstep(c, V, c->F("DV"), VO, frhs, dt * fu)) return rc;
     if (int rc = launch_rkstep(c, W, c->F("DW"), WO, frhs, dt * fu)) return rc;
-    for (int l = c->minlevel; l <= c->maxlevel; ++l)
+    // timeintegration_mod.F90:116-121: connect (normal, forward), bound
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
         if (int rc = connect(c, l, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
+        if (int rc = launch_bound_flow(c, U, V, W, P)) return rc;
+    }
     return mgpoisl(c, dtrk * dt, st);
 }
 
@@ -553,9 +558,11 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
         G.level = d->level[g];
         for (int f = 0; f < 6; ++f) {
             G.bc[f] = d->bctype[6 * g + f];
-            if (!coupled(G.bc[f]))
+            const int t = G.bc[f];
+            if (!(coupled(t) || t == MGLET_BC_FIX || t == MGLET_BC_OP1 || t == MGLET_BC_NOS ||
+                  t == MGLET_BC_SLI))
                 return bail(fail(MGLET_ERR_UNSUPPORTED,
-                                 "create: only CON/CO1 faces are supported on the GPU path"));
+                                 "create: faces must be CON, CO1, FIX, OP1, NOS or SLI"));
         }
         for (int s = 1; s <= 26; ++s) {
             const int nb = d->nbrgrid[26 * g + s - 1];
@@ -618,6 +625,7 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     if (int rc = fill(c, c->F("G"), prm->gmol)) return bail(rc);
     if (int rc = fill(c, c->F("BP"), 1.0)) return bail(rc);
     build_connection_table(c);
+    if (int rc = bound_init(c)) return bail(rc);
     if (int rc = launch_giteig(c)) return bail(rc);
     MG_CUDA(cudaStreamSynchronize(c->stream));
     int rc = prm->psolver == MGLET_PSOLVER_CLASSIC ? launch_sip_lu_classic(c) : launch_sip_lu_hp(c);
@@ -651,6 +659,9 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     for (auto& kv : c->plans) cudaFree(kv.second.d_tasks);
     for (HpTable& t : c->hp) { cudaFree(t.d_mip); cudaFree(t.d_idx); }
     cudaFree(c->d_grids);
+    for (double* b : c->d_buf) cudaFree(b);
+    cudaFree(c->d_bface);
+    for (int* b : c->d_bgrids) cudaFree(b);
     cudaFree(c->d_gridred);
     cudaFree(c->d_scalar);
     if (c->h_scalar) cudaFreeHost(c->h_scalar);
@@ -758,6 +769,42 @@ int mglet_gpu_mgpoisl(mglet_ctx* c, double dt, int32_t ittot, int32_t irk, mglet
     cudaSetDevice(c->device);
     mglet_stage_stats tmp;
     return mgpoisl(c, dt, st ? st : &tmp);
+}
+
+int mglet_gpu_bound_flow(mglet_ctx* c, int32_t ilevel) {
+    (void)ilevel;   // one level
+    if (!c) return fail(MGLET_ERR_ARG, "bound_flow: null context");
+    cudaSetDevice(c->device);
+    return launch_bound_flow(c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
+}
+
+int mglet_gpu_set_buffer(mglet_ctx* c, const char* name, int32_t igrid, int32_t iface,
+                         const double* host, int64_t n) {
+    if (!c || !name || !host || igrid < 1 || igrid > c->ngrid || iface < 1 || iface > 6)
+        return fail(MGLET_ERR_ARG, "set_buffer: bad arguments");
+    const DevGrid& G = c->grids[igrid - 1];
+    const long long sz[3] = {(long long)G.kk * G.jj, (long long)G.kk * G.ii, (long long)G.jj * G.ii};
+    if (n != sz[(iface - 1) / 2]) return fail(MGLET_ERR_SIZE, "set_buffer: wrong plane size");
+    int q = -1;
+    if (!std::strcmp(name, "U")) q = 0;
+    else if (!std::strcmp(name, "V")) q = 1;
+    else if (!std::strcmp(name, "W")) q = 2;
+    if (q < 0) return fail(MGLET_ERR_NAME, "set_buffer: buffers exist for U, V, W");
+    cudaSetDevice(c->device);
+    MG_CUDA(copy_on(c->stream, c->d_buf[q] + c->bface[6 * (igrid - 1) + iface - 1].off, host,
+                    (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int mglet_gpu_set_bc_real(mglet_ctx* c, int32_t igrid, int32_t iface, double value) {
+    if (!c || igrid < 1 || igrid > c->ngrid || iface < 1 || iface > 6)
+        return fail(MGLET_ERR_ARG, "set_bc_real: bad arguments");
+    BFace& b = c->bface[6 * (igrid - 1) + iface - 1];
+    b.pinf = value;
+    cudaSetDevice(c->device);
+    MG_CUDA(copy_on(c->stream, c->d_bface + 6 * (igrid - 1) + iface - 1, &b, sizeof(BFace),
+                    cudaMemcpyHostToDevice));
+    return 0;
 }
 
 int mglet_gpu_itinfo(mglet_ctx* c, double dt, mglet_itinfo* out) {

@@ -30,6 +30,12 @@ struct DevGrid {
     int ipx, ipy, ipz;  // 0-based offsets into the concatenated 1-D arrays
 };
 
+// Boundary data of one face of one grid.
+struct BFace {
+    long long off;      // offset of the face plane in the buffer arrays
+    double pinf;        // OP1 far-field pressure (0 unless set)
+};
+
 // One box copy of connect_self_single (connect2_mod.F90:947-995): the
 // destination box starts at dst (flat element offset), the source box at
 // src; extents nk*nj*ni with per-grid strides.
@@ -93,6 +99,16 @@ struct Ctx {
     double* d_gridred = nullptr;   // [4*ngrid]
     double* d_scalar = nullptr;    // [8]
     double* h_scalar = nullptr;    // pinned [8]
+    // boundary buffers of U, V, W (field_t%get_buffer): one plane per grid and
+    // face, (kk,jj) / (kk,ii) / (jj,ii) column-major, at bface[6*g+f].off;
+    // bface also holds the OP1 far-field pressure of the face
+    double* d_buf[3] = {nullptr, nullptr, nullptr};
+    std::vector<BFace> bface;
+    BFace* d_bface = nullptr;
+    long long nbuf = 0;
+    // grids (0-based) with a FIX/OP1/NOS/SLI face, per face
+    std::vector<int> bgrids[6];
+    int* d_bgrids[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     long long launches = 0;
     bool prof = false;
     std::map<std::string, ProfEntry> profd;
@@ -167,6 +183,10 @@ int launch_accumulate(Ctx* c, double* dp, double* hilf);
 int launch_mgpcorr(Ctx* c, double* u, double* v, double* w, double* p, const double* dp,
                    double rfak);
 int launch_itinfo(Ctx* c, double dt);
+// bound_flow%bound on U, V, W and (unless null) P: faces 1..6 in order
+int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p);
+// boundary buffers and face table (create)
+int bound_init(Ctx* c);
 int launch_connect(Ctx* c, const ConnectPlan& plan, double* const fields[6]);
 // FP32 copy of the same task list; returns early when *skip != 0 (device
 // flag of the mixed form's converged outer loop), skip may be null.

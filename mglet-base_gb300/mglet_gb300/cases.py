@@ -104,13 +104,19 @@ class Case:
                 self.z.reshape(self.ngrid, self.kk))
 
 
-def periodic_box(nx, ny, nz, n=24, length=(2 * np.pi, 2 * np.pi, 2 * np.pi), nk=None, nj=None):
-    """nx*ny*nz grids of n^3 interior cells tiling a periodic box.
+def periodic_box(nx, ny, nz, n=24, length=(2 * np.pi, 2 * np.pi, 2 * np.pi), nk=None, nj=None,
+                 walls=None):
+    """nx*ny*nz grids of n^3 interior cells tiling a box, periodic unless
+    told otherwise.
 
     Every face is CON (code 7) and every one of the 26 neighbour slots
     points at the periodic image grid, as a grids.h5 for a fully periodic
-    one-level domain holds.  Grid ids run x fastest.
+    one-level domain holds.  `walls` maps box faces 1..6 to a boundary
+    code (FIX, OP1, NOS, SLI): the grids on that side of the box get it on
+    that face, and a direction with a boundary face is not periodic, so
+    neighbour slots that would cross it are 0.  Grid ids run x fastest.
     """
+    walls = dict(walls or {})
     ni = n
     nj = n if nj is None else nj
     nk = n if nk is None else nk
@@ -121,10 +127,20 @@ def periodic_box(nx, ny, nz, n=24, length=(2 * np.pi, 2 * np.pi, 2 * np.pi), nk=
     gy = gy.transpose(2, 1, 0).ravel()
     gz = gz.transpose(2, 1, 0).ravel()
     gid = lambda a, b, c: 1 + (a % nx) + nx * ((b % ny) + ny * (c % nz))
+    periodic = [not (2 * d + 1 in walls or 2 * d + 2 in walls) for d in range(3)]
     nbr = np.zeros((ngrid, 26), dtype=np.int32)
     for s in range(1, 27):
         di, dj, dk = slot_offset(s)
-        nbr[:, s - 1] = gid(gx + di, gy + dj, gz + dk)
+        ok = np.ones(ngrid, dtype=bool)
+        for d, (g, dd, nn) in enumerate(((gx, di, nx), (gy, dj, ny), (gz, dk, nz))):
+            if not periodic[d]:
+                ok &= (g + dd >= 0) & (g + dd < nn)
+        nbr[:, s - 1] = np.where(ok, gid(gx + di, gy + dj, gz + dk), 0)
+    bctype = np.full((ngrid, 6), BC_CON, dtype=np.int32)
+    for f, code in walls.items():
+        d, hi = (f - 1) // 2, (f - 1) % 2
+        g, nn = ((gx, nx), (gy, ny), (gz, nz))[d]
+        bctype[g == (nn - 1 if hi else 0), f - 1] = code
     hx, hy, hz = length[0] / (nx * ni), length[1] / (ny * nj), length[2] / (nz * nk)
 
     def axis(g0, h, npts):
@@ -139,7 +155,7 @@ def periodic_box(nx, ny, nz, n=24, length=(2 * np.pi, 2 * np.pi, 2 * np.pi), nk=
         ngrid=ngrid, kk=kk, jj=jj, ii=ii,
         mgdims=np.tile(np.array([kk, jj, ii], dtype=np.int32), (ngrid, 1)),
         level=np.ones(ngrid, dtype=np.int32),
-        bctype=np.full((ngrid, 6), BC_CON, dtype=np.int32),
+        bctype=bctype,
         nbrgrid=nbr,
         gridpos=np.stack([gx, gy, gz], axis=1).astype(np.int32),
         x=x, y=y, z=z,

@@ -24,7 +24,8 @@ EXPORTS = [
     "mglet_gpu_divcal", "mglet_gpu_laplacephi", "mglet_gpu_mgpoisl", "mglet_gpu_itinfo",
     "mglet_gpu_synchronize", "mglet_gpu_kernel_launches", "mglet_gpu_last_error",
     "mglet_gpu_abi_version", "mglet_gpu_stream", "mglet_gpu_profile", "mglet_gpu_profile_get",
-    "mglet_gpu_profile_names", "mglet_gpu_divmax_noalloc",
+    "mglet_gpu_profile_names", "mglet_gpu_divmax_noalloc", "mglet_gpu_bound_flow",
+    "mglet_gpu_set_buffer", "mglet_gpu_set_bc_real",
 ]
 
 
@@ -67,6 +68,9 @@ def load(path=None):
     L.mglet_gpu_laplacephi.argtypes = [vp, cp, cp]
     L.mglet_gpu_mgpoisl.argtypes = [vp, C.c_double, C.c_int32, C.c_int32, vp]
     L.mglet_gpu_itinfo.argtypes = [vp, C.c_double, vp]
+    L.mglet_gpu_bound_flow.argtypes = [vp, C.c_int32]
+    L.mglet_gpu_set_buffer.argtypes = [vp, cp, C.c_int32, C.c_int32, vp, C.c_int64]
+    L.mglet_gpu_set_bc_real.argtypes = [vp, C.c_int32, C.c_int32, C.c_double]
     L.mglet_gpu_synchronize.argtypes = [vp]
     L.mglet_gpu_stream.restype = vp
     L.mglet_gpu_stream.argtypes = [vp]
@@ -167,6 +171,19 @@ class Solver:
         st = abi.StageStats()
         _check(load().mglet_gpu_mgpoisl(self.h, dt, ittot, irk, C.byref(st)))
         return st
+
+    def bound_flow(self, ilevel=0):
+        _check(load().mglet_gpu_bound_flow(self.h, ilevel))
+
+    def set_buffer(self, name, igrid, iface, plane):
+        """Boundary buffer of U, V or W on face iface of grid igrid (1-based):
+        a (kk,jj), (kk,ii) or (jj,ii) plane, first index fastest."""
+        a = np.ascontiguousarray(plane, dtype=np.float64).ravel(order="F")
+        _check(load().mglet_gpu_set_buffer(self.h, name.encode(), igrid, iface,
+                                           a.ctypes.data_as(C.c_void_p), a.size))
+
+    def set_bc_real(self, igrid, iface, value):
+        _check(load().mglet_gpu_set_bc_real(self.h, igrid, iface, value))
 
     def itinfo(self, dt):
         out = abi.ItInfo()

@@ -54,6 +54,9 @@ def lib():
         _lib.oracle_timeintegrate_flow.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double,
                                                    C.c_int, vp, vp]
         _lib.oracle_itinfo.argtypes = [vp, C.c_double, vp]
+        _lib.oracle_set_buffer.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, vp, C.c_int64]
+        _lib.oracle_set_bc_real.argtypes = [vp, C.c_int, C.c_int, C.c_double]
+        _lib.oracle_bound_flow.argtypes = [vp, C.c_int]
         _lib.oracle_rk_init.argtypes = [C.c_char_p, vp]
         _lib.oracle_rk_get_coeffs.argtypes = [vp, C.c_int] + [C.POINTER(C.c_double)] * 4
         _lib.oracle_set_threads.argtypes = [C.c_int]
@@ -174,6 +177,20 @@ class Oracle:
         _check(lib().oracle_timeintegrate_flow(self.h, itstep, ittot, timeph, dt, irk,
                                                C.byref(rk), C.byref(st)))
         return st
+
+    def set_buffer(self, name, igrid, iface, plane):
+        """Boundary buffer of U, V or W on face iface (1..6) of grid igrid
+        (1-based): a (kk,jj), (kk,ii) or (jj,ii) plane, first index fastest."""
+        a = np.ascontiguousarray(plane, dtype=np.float64).ravel(order="F")
+        _check(lib().oracle_set_buffer(self.h, _b(name), igrid, iface,
+                                       a.ctypes.data_as(C.c_void_p), a.size))
+
+    def set_bc_real(self, igrid, iface, value):
+        """The real parameter of an OP1 face (the far-field pressure)."""
+        _check(lib().oracle_set_bc_real(self.h, igrid, iface, value))
+
+    def bound_flow(self, ilevel=0):
+        _check(lib().oracle_bound_flow(self.h, ilevel))
 
     def itinfo(self, dt):
         from mglet_gb300.abi import ItInfo

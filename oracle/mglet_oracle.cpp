@@ -117,6 +117,12 @@ struct Ctx {
     std::map<std::string, std::vector<double>> f1;   // 1-D fields
     std::vector<int64_t> mip, idxsip;                // SIP_MIP_HP, SIP_IDX_HP
     std::vector<Conn> conns;
+    // boundary buffers of U, V, W (field_t%get_buffer): per grid and face a
+    // (kk,jj), (kk,ii) or (jj,ii) plane, column-major; bufoff[6*(g-1)+f-1]
+    std::vector<double> bufU, bufV, bufW;
+    std::vector<int64_t> bufoff;
+    std::vector<double> pinf;    // OP1 real parameter per grid and face (nreal = 1)
+    std::vector<int> npinf;      // 0: no parameter (pinf = 0), 1: pinf given
 
     double* F(const char* n) { return f3.at(n).data(); }
     double* L(const char* n) { return f1.at(n).data(); }
@@ -843,6 +849,8 @@ void divcal(Ctx& c, double* DIV, const double* U, const double* V, const double*
 }
 
 // pressuresolver_mod.F90:160-357 mgpoisl (single level, noib)
+void bound_flow(Ctx& c, double* U, double* V, double* W, double* P);
+
 void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
     double* U = c.F("U"); double* V = c.F("V"); double* W = c.F("W"); double* P = c.F("P");
     for (const char* n : {"DP", "HILF", "RHS", "RES"}) c.f3[n].assign(c.idim3d, 0.0);
@@ -876,6 +884,8 @@ void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
         if (ipcount >= c.prm.nouter_min && maxrhs / prefak < c.prm.epcorr) break;
     }
     mgpcorr(c, U, V, W, P, dp, dt / c.prm.rho);
+    // pressuresolver_mod.F90:341-348: bound, then the corner connect
+    bound_flow(c, U, V, W, P);
     connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0);
     if (st) {
         st->ipc = ipc;
@@ -883,6 +893,138 @@ void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
         st->maxrhs = maxrhs;
         st->prefak = prefak;
     }
+}
+
+// ---------------------------------------------------------------------------
+// bound_flow_mod.F90 bfront (:23-256), bright (:259-494), bbottom (:497-730)
+// for FIX, OP1, NOS and SLI, dispatched grid by grid and face 1..6 as
+// bound_t%bound does (src/core/bound_mod.F90:36-76).  Face-local layout: the
+// face-normal index n (i, j or k), the two tangential indices a < b in the
+// reference's loop order (k, j for x faces; k, i for y faces; j, i for z).
+double fsign(double a, double b) { return std::copysign(std::fabs(a), b); }
+
+void bound_face(Ctx& c, int g, int iface, double* U, double* V, double* W, double* P) {
+    const Grid& G = c.g[g];
+    const int typ = G.bc[iface];
+    if (!(typ == MGLET_BC_FIX || typ == MGLET_BC_OP1 || typ == MGLET_BC_NOS || typ == MGLET_BC_SLI))
+        return;
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    double* u = U + G.ip3; double* v = V + G.ip3; double* w = W + G.ip3;
+    double* p = P ? P + G.ip3 : nullptr;
+    const int64_t bo = c.bufoff[6 * (g - 1) + iface - 1];
+    const double* ub = c.bufU.data() + bo; const double* vb = c.bufV.data() + bo;
+    const double* wb = c.bufW.data() + bo;
+    const double pin = c.npinf[6 * (g - 1) + iface - 1] ? c.pinf[6 * (g - 1) + iface - 1] : 0.0;
+    const double rho = c.prm.rho;
+    const int axis = (iface - 1) / 2;          // 0: x (bfront), 1: y (bright), 2: z (bbottom)
+    const bool lo = (iface % 2) == 1;
+    const int nn = axis == 0 ? ii : (axis == 1 ? jj : kk);
+    const int n2 = lo ? 2 : nn - 1, n3 = lo ? 3 : nn - 2;
+    const int st1 = lo ? 1 : nn - 1, st2 = lo ? 2 : nn - 2;
+    const double dir = lo ? -1.0 : 1.0;
+    // tangential extents of the face: a runs fastest
+    const int na = axis == 2 ? jj : kk, nb = axis == 0 ? jj : ii;
+    // index of (a, b, n) in the grid; a, b tangential, n normal
+    auto at = [&](int a, int b, int n) -> int64_t {
+        if (axis == 0) return IX(a, b, n);        // (k, j, i)
+        if (axis == 1) return IX(a, n, b);        // (k, j, i) with j normal
+        return IX(n, a, b);                       // k normal
+    };
+    auto bi = [&](int a, int b) -> int64_t { return (int64_t)(a - 1) + (int64_t)(b - 1) * na; };
+    // the normal component and the two tangential ones, in the reference's order
+    double* vn = axis == 0 ? u : (axis == 1 ? v : w);
+    const double* bn = axis == 0 ? ub : (axis == 1 ? vb : wb);
+    // tangential components t1, t2: x faces (v, w), y faces (u, w), z faces
+    // (u, v); t1 is staggered along b and t2 along a, so the OP1 flag of t1
+    // averages the normal velocity over (a, b), (a, b+1) and that of t2 over
+    // (a, b), (a+1, b)
+    double* t1 = axis == 0 ? v : u;
+    double* t2 = axis == 2 ? v : w;
+    const double* b1 = axis == 0 ? vb : ub;
+    const double* b2 = axis == 2 ? vb : wb;
+    if (typ == MGLET_BC_FIX) {
+        for (int b = 1; b <= nb; ++b)
+            for (int a = 1; a <= na; ++a) {
+                if (axis == 0) {
+                    vn[at(a, b, st2)] = bn[bi(a, b)];
+                    t1[at(a, b, n2)] = 2.0 * b1[bi(a, b)] - t1[at(a, b, n3)];
+                    t2[at(a, b, n2)] = 2.0 * b2[bi(a, b)] - t2[at(a, b, n3)];
+                } else if (axis == 1) {
+                    t1[at(a, b, n2)] = 2.0 * b1[bi(a, b)] - t1[at(a, b, n3)];
+                    vn[at(a, b, st2)] = bn[bi(a, b)];
+                    t2[at(a, b, n2)] = 2.0 * b2[bi(a, b)] - t2[at(a, b, n3)];
+                } else {
+                    t1[at(a, b, n2)] = 2.0 * b1[bi(a, b)] - t1[at(a, b, n3)];
+                    t2[at(a, b, n2)] = 2.0 * b2[bi(a, b)] - t2[at(a, b, n3)];
+                    vn[at(a, b, st2)] = bn[bi(a, b)];
+                }
+            }
+    } else if (typ == MGLET_BC_OP1) {
+        for (int b = 1; b <= nb - 1; ++b)
+            for (int a = 1; a <= na - 1; ++a) {
+                // 1 for outflow (zero gradient), 0 for inflow (prescribed)
+                double f1 = fsign(1.0, dir * (vn[at(a, b, st2)] + vn[at(a, b + 1, st2)]));
+                double f2 = fsign(1.0, dir * (vn[at(a, b, st2)] + vn[at(a + 1, b, st2)]));
+                f1 = 0.5 * (f1 + 1.0);
+                f2 = 0.5 * (f2 + 1.0);
+                const double n1v = f1 * t1[at(a, b, n3)] +
+                                   (1.0 - f1) * (2.0 * b1[bi(a, b)] - t1[at(a, b, n3)]);
+                const double n2v = f2 * t2[at(a, b, n3)] +
+                                   (1.0 - f2) * (2.0 * b2[bi(a, b)] - t2[at(a, b, n3)]);
+                if (axis == 0) {
+                    vn[at(a, b, st1)] = vn[at(a, b, st2)];
+                    t1[at(a, b, n2)] = n1v;
+                    t2[at(a, b, n2)] = n2v;
+                } else if (axis == 1) {
+                    t1[at(a, b, n2)] = n1v;
+                    vn[at(a, b, st1)] = vn[at(a, b, st2)];
+                    t2[at(a, b, n2)] = n2v;
+                } else {
+                    t1[at(a, b, n2)] = n1v;
+                    t2[at(a, b, n2)] = n2v;
+                    vn[at(a, b, st1)] = vn[at(a, b, st2)];
+                }
+            }
+    } else if (typ == MGLET_BC_NOS) {
+        for (int b = 1; b <= nb; ++b)
+            for (int a = 1; a <= na; ++a) {
+                vn[at(a, b, st2)] = 0.0;
+                t1[at(a, b, n2)] = 0.0;
+                t2[at(a, b, n2)] = 0.0;
+            }
+    } else {   // SLI
+        for (int b = 1; b <= nb; ++b)
+            for (int a = 1; a <= na; ++a) {
+                vn[at(a, b, st2)] = 0.0;
+                t1[at(a, b, n2)] = t1[at(a, b, n3)];
+                t2[at(a, b, n2)] = t2[at(a, b, n3)];
+            }
+    }
+    if (!p) return;
+    if (typ == MGLET_BC_OP1) {
+        for (int b = 2; b <= nb; ++b)
+            for (int a = 2; a <= na; ++a) {
+                // the two tangential components interpolated to the cell centre
+                const double c1 = 0.25 * (t1[at(a, b - 1, n2)] + t1[at(a, b, n2)] +
+                                          t1[at(a, b - 1, n3)] + t1[at(a, b, n3)]);
+                const double c2 = 0.25 * (t2[at(a - 1, b, n2)] + t2[at(a, b, n2)] +
+                                          t2[at(a - 1, b, n3)] + t2[at(a, b, n3)]);
+                const double un = vn[at(a, b, st2)];
+                double umagsqr;
+                if (axis == 0) umagsqr = un * un + c1 * c1 + c2 * c2;
+                else if (axis == 1) umagsqr = c1 * c1 + un * un + c2 * c2;
+                else umagsqr = c1 * c1 + c2 * c2 + un * un;
+                p[at(a, b, n2)] = pin + std::min(0.0, 0.5 * rho * fsign(umagsqr, dir * un));
+            }
+    } else {
+        for (int b = 1; b <= nb; ++b)
+            for (int a = 1; a <= na; ++a) p[at(a, b, n2)] = p[at(a, b, n3)];
+    }
+}
+
+void bound_flow(Ctx& c, double* U, double* V, double* W, double* P) {
+    for (int g = 1; g <= c.ngrid; ++g)
+        for (int f = 1; f <= 6; ++f) bound_face(c, g, f, U, V, W, P);
 }
 
 // ---------------------------------------------------------------------------
@@ -1229,8 +1371,12 @@ void itinfo(Ctx& c, double dt, mglet_itinfo* out) {
 
 bool check_supported(const Ctx& c) {
     for (int g = 1; g <= c.ngrid; ++g)
-        for (int f = 1; f <= 6; ++f)
-            if (!is_con(c.g[g].bc[f])) return false;
+        for (int f = 1; f <= 6; ++f) {
+            const int t = c.g[g].bc[f];
+            if (!(is_con(t) || t == MGLET_BC_FIX || t == MGLET_BC_OP1 || t == MGLET_BC_NOS ||
+                  t == MGLET_BC_SLI))
+                return false;
+        }
     return true;
 }
 
@@ -1302,7 +1448,8 @@ int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle
     }
     if (!check_supported(*c)) {
         delete c;
-        return fail(MGLET_ERR_UNSUPPORTED, "oracle: only CON/CO1 faces are restated");
+        return fail(MGLET_ERR_UNSUPPORTED,
+                    "oracle: only CON, CO1, FIX, OP1, NOS and SLI faces are restated");
     }
     c->idim3d = o3; c->idimx = ox; c->idimy = oy; c->idimz = oz;
     for (const char* n : {"U", "V", "W", "P", "G", "DU", "DV", "DW", "BP", "SDIV", "UO", "VO",
@@ -1328,6 +1475,20 @@ int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle
     for (const char* n : {"GSAW", "GSAE"}) c->f1[n].assign(c->idimx, 0.0);
     for (const char* n : {"GSAS", "GSAN"}) c->f1[n].assign(c->idimy, 0.0);
     for (const char* n : {"GSAB", "GSAT"}) c->f1[n].assign(c->idimz, 0.0);
+    // boundary buffers (zero until set) and OP1 parameters
+    c->bufoff.assign(6 * (size_t)d->ngrid, 0);
+    int64_t nb = 0;
+    for (int g = 1; g <= d->ngrid; ++g) {
+        const Grid& G = c->g[g];
+        const int64_t sz[3] = {(int64_t)G.kk * G.jj, (int64_t)G.kk * G.ii, (int64_t)G.jj * G.ii};
+        for (int f = 1; f <= 6; ++f) {
+            c->bufoff[6 * (g - 1) + f - 1] = nb;
+            nb += sz[(f - 1) / 2];
+        }
+    }
+    c->bufU.assign(nb, 0.0); c->bufV.assign(nb, 0.0); c->bufW.assign(nb, 0.0);
+    c->pinf.assign(6 * (size_t)d->ngrid, 0.0);
+    c->npinf.assign(6 * (size_t)d->ngrid, 0);
     init_connect_core(*c);
     giteig(*c);
     int rc = init_pressuresolver(*c);
@@ -1448,10 +1609,43 @@ int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timep
     rkstep(c->F("U"), c->F("DU"), c->F("UO"), c->idim3d, frhs, dt * fu);
     rkstep(c->F("V"), c->F("DV"), c->F("VO"), c->idim3d, frhs, dt * fu);
     rkstep(c->F("W"), c->F("DW"), c->F("WO"), c->idim3d, frhs, dt * fu);
-    for (int l = c->minlevel; l <= c->maxlevel; ++l)
+    // timeintegration_mod.F90:116-121: connect (normal, forward), bound
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
         connect(*c, l, 1, c->F("U"), c->F("V"), c->F("W"), nullptr, nullptr, nullptr, false, true, 1);
+        bound_flow(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
+    }
     mgpoisl(*c, dtrk * dt, st);
     (void)ittot;
+    return 0;
+}
+
+int oracle_set_buffer(oracle_ctx* c, const char* name, int igrid, int iface, const double* data,
+                      int64_t n) {
+    if (!c || !name || !data || igrid < 1 || igrid > c->ngrid || iface < 1 || iface > 6)
+        return fail(MGLET_ERR_ARG, "set_buffer: bad arguments");
+    const Grid& G = c->g[igrid];
+    const int64_t sz[3] = {(int64_t)G.kk * G.jj, (int64_t)G.kk * G.ii, (int64_t)G.jj * G.ii};
+    if (n != sz[(iface - 1) / 2]) return fail(MGLET_ERR_SIZE, "set_buffer: wrong plane size");
+    std::vector<double>* b = nullptr;
+    if (!std::strcmp(name, "U")) b = &c->bufU;
+    else if (!std::strcmp(name, "V")) b = &c->bufV;
+    else if (!std::strcmp(name, "W")) b = &c->bufW;
+    else return fail(MGLET_ERR_NAME, "set_buffer: buffers exist for U, V, W");
+    std::copy(data, data + n, b->begin() + c->bufoff[6 * (igrid - 1) + iface - 1]);
+    return 0;
+}
+
+int oracle_set_bc_real(oracle_ctx* c, int igrid, int iface, double value) {
+    if (!c || igrid < 1 || igrid > c->ngrid || iface < 1 || iface > 6)
+        return fail(MGLET_ERR_ARG, "set_bc_real: bad arguments");
+    c->pinf[6 * (igrid - 1) + iface - 1] = value;
+    c->npinf[6 * (igrid - 1) + iface - 1] = 1;
+    return 0;
+}
+
+int oracle_bound_flow(oracle_ctx* c, int ilevel) {
+    (void)ilevel;
+    bound_flow(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
     return 0;
 }
 

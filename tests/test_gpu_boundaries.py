@@ -1,0 +1,84 @@
+"""FIX / OP1 / NOS / SLI faces on the GPU (plain FP64 form) against the
+oracle: bound_flow alone and whole stages, bit for bit."""
+import numpy as np
+import pytest
+
+from mglet_gb300 import abi, cases
+from test_oracle_boundaries import face_plane_shape, random_bc_case
+
+pytestmark = pytest.mark.gpu
+
+WALLS = [
+    {1: abi.BC_FIX, 2: abi.BC_OP1},
+    {3: abi.BC_OP1, 4: abi.BC_FIX, 5: abi.BC_NOS, 6: abi.BC_SLI},
+    {1: abi.BC_SLI, 2: abi.BC_NOS, 5: abi.BC_OP1, 6: abi.BC_OP1},
+    {5: abi.BC_FIX, 6: abi.BC_FIX, 3: abi.BC_NOS, 4: abi.BC_SLI},
+]
+
+
+def _prm(form=abi.FORM_PLAIN, **kw):
+    base = dict(gmol=1e-2, epcorr=1e-12, nouter=6, ninner=5, nouter_min=6, form=form)
+    base.update(kw)
+    return abi.make_flow_params(**base)
+
+
+def _load(solvers, case, fields, bufs, pinf):
+    for s in solvers:
+        for nm, a in fields.items():
+            s.set(nm, a)
+        for (nm, g, f), b in bufs.items():
+            s.set_buffer(nm, g + 1, f, b)
+        for (g, f), val in pinf.items():
+            s.set_bc_real(g + 1, f, val)
+
+
+@pytest.mark.parametrize("walls", WALLS)
+def test_bound_flow_bit_exact(gpu_lib, oracle_lib, walls):
+    case, fields, bufs = random_bc_case(walls, seed=len(walls) * 11 + 3)
+    pinf = {(g, f): 0.1 * (g + f) for (nm, g, f) in bufs if case.bctype[g, f - 1] == abi.BC_OP1}
+    gs, o = gpu_lib.Solver(case, _prm()), oracle_lib.Oracle(case, _prm())
+    _load((gs, o), case, fields, bufs, pinf)
+    gs.bound_flow()
+    o.bound_flow()
+    for nm in "UVWP":
+        assert np.array_equal(gs.get(nm), o.get(nm)), nm
+
+
+@pytest.mark.parametrize("walls", WALLS)
+def test_wall_stages_bit_exact(gpu_lib, oracle_lib, walls):
+    """Two time steps (six stages) with the pressure solve, bound_flow before
+    it and after the projection, on a 2x2x1 tiling."""
+    case = cases.periodic_box(2, 2, 1, n=8, length=(2.0, 2.0, 1.0), walls=walls)
+    u, v, w, p = cases.taylor_green(case)
+    u, v, w = cases.add_noise(case, (u + 0.5, v, w), amplitude=1e-2, seed=9)
+    fields = dict(zip("UVWP", (u, v, w, p)))
+    rng = np.random.default_rng(17)
+    bufs, pinf = {}, {}
+    for g in range(case.ngrid):
+        for f in range(1, 7):
+            t = case.bctype[g, f - 1]
+            if t == abi.BC_FIX:
+                bufs[("U", g, f)] = 0.5 + 0.01 * rng.standard_normal(face_plane_shape(case, f))
+            if t == abi.BC_OP1:
+                pinf[(g, f)] = 0.05
+    gs, o = gpu_lib.Solver(case, _prm()), oracle_lib.Oracle(case, _prm())
+    _load((gs, o), case, fields, bufs, pinf)
+    for s in (gs, o):
+        s.connect(0, 2, "U", "V", "W", "P", corners=True)
+    rkg, rko = gpu_lib.rk_scheme("williamson"), oracle_lib.rk_scheme("williamson")
+    for it in range(1, 3):
+        for irk in range(1, 4):
+            sg = gs.timeintegrate_flow(it, it, 0.0, 2e-3, irk, rkg)
+            so = o.timeintegrate_flow(it, it, 0.0, 2e-3, irk, rko)
+            assert sg.ipc == so.ipc and sg.maxrhs == so.maxrhs
+    for nm in "UVWP":
+        assert np.array_equal(gs.get(nm), o.get(nm)), nm
+
+
+def test_mixed_form_refuses_walls(gpu_lib):
+    """The batched mixed form pulls every halo from a face neighbour, so a
+    hierarchy with wall faces is refused loudly, not run approximately."""
+    case = cases.periodic_box(2, 1, 1, n=8, walls={1: abi.BC_FIX, 2: abi.BC_OP1})
+    with pytest.raises(gpu_lib.MgletError) as e:
+        gpu_lib.Solver(case, _prm(abi.FORM_MIXED))
+    assert e.value.code == abi.MGLET_ERR_UNSUPPORTED
