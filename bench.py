@@ -18,6 +18,10 @@ same number of steps (per-launch CUDA events on the solver's stream).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|plain]
   python bench.py --impl reference   # the CPU restatement on the host cores
+  python bench.py --precision [--tiles 8 8 8] [--steps 200]
+      # mixed form against the plain FP64 form (bit-identical to the CPU
+      # restatement) from a solenoidal random field: relative L2 error of
+      # u, v, w, p every 50 steps
 
 Prints one JSON line (rank 0).
 """
@@ -99,6 +103,8 @@ def parse():
                     help="skip the plain FP64 form timed beside the mixed headline")
     ap.add_argument("--no-profile", action="store_true",
                     help="skip the profiled pass (per-kernel times, roofline)")
+    ap.add_argument("--precision", action="store_true",
+                    help="error of the mixed form against the plain FP64 form")
     return ap.parse_args()
 
 
@@ -435,9 +441,85 @@ def run_ours(args, rank, world, local):
     return 0
 
 
+def run_precision(args, rank, local):
+    """Precision of the mixed form: 24^3 grids tiling a periodic box of side
+    2 pi, a seeded solenoidal random field (Gaussian shell around k = 4, rms
+    velocity 1) projected once by the FP64 pressure solve, nu = 1e-3,
+    Williamson RK3 at dt = 2e-4, pressure solved to max|rhs|/prefak < 1e-10
+    (up to 40 outer iterations).  The plain FP64 form, bit-identical to the
+    CPU restatement, is the reference; the error is the relative L2 norm over
+    the interior (pressure with its mean removed)."""
+    import numpy as np
+    import torch
+    from mglet_gb300 import abi, cases, gpu
+
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    case = cases.periodic_box(*args.tiles, n=args.n)
+    u, v, w = cases.divergence_free_modes(case, nmodes=48, kpeak=4.0, urms=1.0, seed=4242)
+    p = np.zeros_like(u)
+
+    def prm(form):
+        return abi.make_flow_params(gmol=1e-3, rho=1.0, epcorr=1e-10, nouter=40, ninner=5,
+                                    nouter_min=0, form=form)
+    ref = gpu.Solver(case, prm(abi.FORM_PLAIN), device=local)
+    for nm, a in zip("UVWP", (u, v, w, p)):
+        ref.set(nm, a)
+    ref.connect(0, 2, "U", "V", "W", "P", corners=True)
+    ref.mgpoisl(1.0)   # discrete projection of the initial field
+    ref.set("P", p)
+    init = [ref.get(nm) for nm in "UVWP"]
+    div0 = ref.itinfo(2e-4).divmax
+    mix = gpu.Solver(case, prm(abi.FORM_MIXED), device=local)
+    for nm, a in zip("UVWP", init):
+        mix.set(nm, a)
+    mix.connect(0, 2, "U", "V", "W", "P", corners=True)
+    rk = gpu.rk_scheme("williamson")
+
+    def rel(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    rows = []
+    ipc = {"mixed": 0, "plain": 0}
+    t0 = time.perf_counter()
+    for it in range(1, args.steps + 1):
+        for irk in range(1, 4):
+            ipc["plain"] += ref.timeintegrate_flow(it, it, 0.0, 2e-4, irk, rk).ipc
+            ipc["mixed"] += mix.timeintegrate_flow(it, it, 0.0, 2e-4, irk, rk).ipc
+        if it % 50 == 0 or it == args.steps:
+            fr = {nm: case.interior(ref.get(nm)) for nm in "UVWP"}
+            fm = {nm: case.interior(mix.get(nm)) for nm in "UVWP"}
+            row = {"step": it}
+            for nm in "UVW":
+                row[nm.lower()] = rel(fm[nm], fr[nm])
+            row["p"] = rel(fm["P"] - fm["P"].mean(), fr["P"] - fr["P"].mean())
+            num = sum(np.sum((fm[nm] - fr[nm]) ** 2) for nm in "UVW")
+            den = sum(np.sum(fr[nm] ** 2) for nm in "UVW")
+            row["velocity"] = float(np.sqrt(num / den))
+            row["divmax_mixed"] = mix.itinfo(2e-4).divmax
+            row["divmax_plain"] = ref.itinfo(2e-4).divmax
+            rows.append(row)
+    line = {"precision": "mixed vs plain FP64", "workload":
+            f"periodic {case.ngrid} x {args.n}^3 grids, solenoidal random field (k ~ 4, rms 1), "
+            "nu=1e-3, RK3 dt=2e-4, epcorr=1e-10 (nouter<=40)",
+            "steps": args.steps, "initial_divmax": div0, "errors": rows,
+            "pressure_iterations": ipc, "seconds": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+    mix.close()
+    ref.close()
+    return 0
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.precision:
+        if args.steps == 5:
+            args.steps = 200
+        if args.tiles == [16, 16, 16]:
+            args.tiles = [8, 8, 8]
+        return run_precision(args, rank, local)
     if args.impl == "reference":
         return run_reference(args, rank)
     return run_ours(args, rank, world, local)
