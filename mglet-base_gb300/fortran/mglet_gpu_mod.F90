@@ -100,6 +100,30 @@ MODULE mglet_gpu_mod
             TYPE(c_ptr), VALUE :: v1, v2, v3, s1, s2, s3    ! C strings or C_NULL_PTR
         END FUNCTION mglet_gpu_connect
 
+        INTEGER(c_int) FUNCTION mglet_gpu_bound_flow(ctx, ilevel) BIND(C, name="mglet_gpu_bound_flow")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: ilevel
+        END FUNCTION mglet_gpu_bound_flow
+
+        INTEGER(c_int) FUNCTION mglet_gpu_set_buffer(ctx, name, igrid, iface, host, n) &
+                BIND(C, name="mglet_gpu_set_buffer")
+            IMPORT :: c_int, c_int32_t, c_int64_t, c_ptr, c_char, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(in) :: name(*)
+            INTEGER(c_int32_t), VALUE :: igrid, iface
+            REAL(c_double), INTENT(in) :: host(*)
+            INTEGER(c_int64_t), VALUE :: n
+        END FUNCTION mglet_gpu_set_buffer
+
+        INTEGER(c_int) FUNCTION mglet_gpu_set_bc_real(ctx, igrid, iface, value) &
+                BIND(C, name="mglet_gpu_set_bc_real")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: igrid, iface
+            REAL(c_double), VALUE :: value
+        END FUNCTION mglet_gpu_set_bc_real
+
         INTEGER(c_int) FUNCTION mglet_gpu_itinfo(ctx, dt, out) BIND(C, name="mglet_gpu_itinfo")
             IMPORT :: c_int, c_ptr, c_double, mglet_itinfo
             TYPE(c_ptr), VALUE :: ctx
@@ -113,7 +137,7 @@ MODULE mglet_gpu_mod
 
     PUBLIC :: mglet_grid_desc, mglet_flow_params, mglet_rk_scheme, mglet_stage_stats, &
         mglet_itinfo, gpu_init, gpu_finish, gpu_upload, gpu_download, &
-        gpu_timeintegrate_flow, gpu_itinfo
+        gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -145,6 +169,26 @@ CONTAINS
         IF (mglet_gpu_get_field(gctx, TRIM(name)//C_NULL_CHAR, arr, &
             INT(SIZE(arr), c_int64_t)) /= 0) CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_download
+
+    ! One boundary buffer plane (field_t%get_buffer(buf, igrid, iface)), for
+    ! FIX inflow values and OP1 inflow tangential velocities; call after
+    ! setboundarybuffers has filled the host copy.
+    SUBROUTINE gpu_upload_buffer(name, igrid, iface, buf)
+        CHARACTER(len=*), INTENT(in) :: name
+        INTEGER, INTENT(in) :: igrid, iface
+        REAL(c_double), INTENT(in) :: buf(:, :)
+        IF (mglet_gpu_set_buffer(gctx, TRIM(name)//C_NULL_CHAR, INT(igrid, c_int32_t), &
+            INT(iface, c_int32_t), buf, INT(SIZE(buf), c_int64_t)) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_upload_buffer
+
+    ! OP1 far-field pressure of one face (get_bcprms with nreal = 1)
+    SUBROUTINE gpu_set_pinf(igrid, iface, pinf)
+        INTEGER, INTENT(in) :: igrid, iface
+        REAL(c_double), INTENT(in) :: pinf
+        IF (mglet_gpu_set_bc_real(gctx, INT(igrid, c_int32_t), INT(iface, c_int32_t), pinf) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_set_pinf
 
     ! Drop-in for timeintegrate_flow (src/flow/timeintegration_mod.F90:22)
     SUBROUTINE gpu_timeintegrate_flow(itstep, ittot, timeph, dt, irk, ipc)
