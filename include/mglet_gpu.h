@@ -218,6 +218,30 @@ int mglet_gpu_set_buffer(mglet_ctx* ctx, const char* name, int32_t igrid, int32_
  * (get_bcprms with nreal = 1, src/flow/bound_flow_mod.F90:226-236); faces
  * without one use pinf = 0. */
 int mglet_gpu_set_bc_real(mglet_ctx* ctx, int32_t igrid, int32_t iface, double value);
+/* ---- Ghost-cell immersed boundary (ib%type = "GHOSTCELL") -------------------
+ * Stencil lists of grid igrid (1-based) in the formats of
+ * gc_flowstencils_mod.F90:37-100 (what the reference reads from
+ * ib_stencils.h5 and create_flowstencils builds): comp 1..3 for u, v, w with
+ * xpoli = [intcell, n, stcell x n] per ghost cell (1-based positions in the
+ * grid's flat array), xpolr and xpolrvel = [coeff x n, const] per ghost cell
+ * (nxrv == nxr); comp 4 for the flux correction with xpoli = [foundnr,
+ * intcell] and xpolr = [ax1, ax2, ay1, ay2, az1, az2, acoeff] per cell. */
+int mglet_gpu_set_stencils(mglet_ctx* ctx, int32_t igrid, int32_t comp, int32_t ncells,
+                           const int64_t* xpoli, int64_t nxi, const double* xpolr, int64_t nxr,
+                           const double* xpolrvel, int64_t nxrv);
+/* Switch the context to the ghost-cell IB after BP (mglet_gpu_set_field)
+ * and every grid's lists are set: Poisson coefficients and SIP factors are
+ * rebuilt with the blocked cells (giteig, src/ib/noib_mod.F90:81-250), the
+ * lists go to the device and SDIV is built (setsdivfield,
+ * gc_flowstencils_mod.F90:1488-1535).  Plain form only. */
+int mglet_gpu_set_ghostcell(mglet_ctx* ctx);
+/* setibvalues(u, v, w), getibvalues(u, v, w) and setpointvalues(pwu, pwv,
+ * pww, u, v, w, comp_new) (gc_flowstencils_mod.F90:1323-1453), maskbp(u, v,
+ * w, p) (src/flow/timeintegration_mod.F90:255-303) on the device fields. */
+int mglet_gpu_setibvalues(mglet_ctx* ctx);
+int mglet_gpu_getibvalues(mglet_ctx* ctx);
+int mglet_gpu_setpointvalues(mglet_ctx* ctx, int32_t comp_new);
+int mglet_gpu_maskbp(mglet_ctx* ctx);
 /* compcflmax / compdivmax / enerfg of itinfo_flow
  * (src/flow/timeintegration_mod.F90:202-240); out->exploded mirrors the NaN
  * check of itinfo_print (src/flow/itinfo_mod.F90:296-320). */

@@ -277,6 +277,8 @@ std::string plan_key(int ilevel, int layers, int slots, bool corners, bool norma
 
 }  // namespace
 
+int alloc_field3(Ctx* c, const char* name) { return alloc3(c, name); }
+
 int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,
             double* s2, double* s3, bool corners, bool normal, int forward) {
     if (layers < 1 || layers > 2) return fail(MGLET_ERR_ARG, "connect: layers must be 1 or 2");
@@ -412,16 +414,28 @@ static int stage_plain(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk,
     if (int rc = rk_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki)) return rc;
     double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P"), *G = c->F("G");
     double *UO = c->F("UO"), *VO = c->F("VO"), *WO = c->F("WO");
-    if (int rc = launch_tstle4(c, UO, VO, WO, U, V, W, P, G)) return rc;
+    const bool gc = c->ibtype == 1;
+    // timeintegration_mod.F90:96-99: the ghost-cell fluxes of the step
+    if (irk == 1 && gc)
+        if (int rc = gc_setibvalues(c, U, V, W)) return rc;
+    if (int rc = launch_tstle4(c, UO, VO, WO, gc ? c->F("PWU") : U, gc ? c->F("PWV") : V,
+                               gc ? c->F("PWW") : W, U, V, W, P, G))
+        return rc;
     if (int rc = launch_rkstep(c, U, c->F("DU"), UO, frhs, dt * fu)) return rc;
     if (int rc = launch_rkstep(c, V, c->F("DV"), VO, frhs, dt * fu)) return rc;
     if (int rc = launch_rkstep(c, W, c->F("DW"), WO, frhs, dt * fu)) return rc;
+    if (gc) {   // timeintegration_mod.F90:110-116: maskbp, getibvalues
+        if (int rc = launch_maskbp(c, U, V, W, P)) return rc;
+        if (int rc = launch_gc_mode(c, 'R', U, V, W)) return rc;
+    }
     // timeintegration_mod.F90:116-121: connect (normal, forward), bound
     for (int l = c->minlevel; l <= c->maxlevel; ++l) {
         if (int rc = connect(c, l, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
         if (int rc = launch_bound_flow(c, U, V, W, P)) return rc;
     }
-    return mgpoisl(c, dtrk * dt, st);
+    if (int rc = mgpoisl(c, dtrk * dt, st)) return rc;
+    if (gc) return gc_setpointvalues(c, irk == rk->nrk);   // :131-134
+    return 0;
 }
 
 int timeintegrate(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st) {
@@ -661,6 +675,10 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     cudaFree(c->d_grids);
     for (double* b : c->d_buf) cudaFree(b);
     cudaFree(c->d_bface);
+    for (void* p : {(void*)c->gcd.seg, (void*)c->gcd.xpoli, (void*)c->gcd.xpolr,
+                    (void*)c->gcd.xpolrvel, (void*)c->gcd.oldsol, (void*)c->gcd.oldsolvel,
+                    (void*)c->gcd.poldsol, (void*)c->gcd.poldsolvel})
+        cudaFree(p);
     for (int* b : c->d_bgrids) cudaFree(b);
     cudaFree(c->d_gridred);
     cudaFree(c->d_scalar);
@@ -719,7 +737,9 @@ int mglet_gpu_timeintegrate_flow(mglet_ctx* c, int32_t itstep, int32_t ittot, do
 int mglet_gpu_tstle4(mglet_ctx* c) {
     if (!c) return fail(MGLET_ERR_ARG, "tstle4: null context");
     cudaSetDevice(c->device);
-    return launch_tstle4(c, c->F("UO"), c->F("VO"), c->F("WO"), c->F("U"), c->F("V"), c->F("W"),
+    const bool gc = c->ibtype == 1;
+    return launch_tstle4(c, c->F("UO"), c->F("VO"), c->F("WO"), c->F(gc ? "PWU" : "U"),
+                         c->F(gc ? "PWV" : "V"), c->F(gc ? "PWW" : "W"), c->F("U"), c->F("V"), c->F("W"),
                          c->F("P"), c->F("G"));
 }
 
@@ -805,6 +825,94 @@ int mglet_gpu_set_bc_real(mglet_ctx* c, int32_t igrid, int32_t iface, double val
     MG_CUDA(copy_on(c->stream, c->d_bface + 6 * (igrid - 1) + iface - 1, &b, sizeof(BFace),
                     cudaMemcpyHostToDevice));
     return 0;
+}
+
+int mglet_gpu_set_stencils(mglet_ctx* c, int32_t igrid, int32_t comp, int32_t ncells,
+                           const int64_t* xpoli, int64_t nxi, const double* xpolr, int64_t nxr,
+                           const double* xpolrvel, int64_t nxrv) {
+    if (!c || igrid < 1 || igrid > c->ngrid || comp < 1 || comp > 4 || ncells < 0 || nxi < 0 ||
+        nxr < 0 || (nxi > 0 && !xpoli) || (nxr > 0 && !xpolr))
+        return fail(MGLET_ERR_ARG, "set_stencils: bad arguments");
+    if (c->gch.empty()) c->gch.resize(c->ngrid);
+    GcHostList& L = c->gch[igrid - 1];
+    const int q = comp - 1;
+    const DevGrid& G = c->grids[igrid - 1];
+    const long long npts = (long long)G.kk * G.jj * G.ii;
+    if (comp == 4) {
+        if (nxi != 2LL * ncells || nxr != 7LL * ncells)
+            return fail(MGLET_ERR_SIZE, "set_stencils: flux list sizes");
+        for (long long e = 1; e < nxi; e += 2)
+            if (xpoli[e] < 1 + (long long)G.kk * G.jj || xpoli[e] > npts)
+                return fail(MGLET_ERR_ARG, "set_stencils: flux cell outside the grid");
+    } else {
+        if (nxrv != nxr || (nxrv > 0 && !xpolrvel))
+            return fail(MGLET_ERR_SIZE, "set_stencils: xpolrvel must match xpolr");
+        // walk the list once: every position inside the grid, sizes consistent
+        long long pi = 0, pr = 0;
+        for (int cell = 0; cell < ncells; ++cell) {
+            if (pi + 2 > nxi) return fail(MGLET_ERR_SIZE, "set_stencils: xpoli too short");
+            const long long ic = xpoli[pi++], n = xpoli[pi++];
+            if (ic < 1 || ic > npts || n < 0 || pi + n > nxi || pr + n + 1 > nxr)
+                return fail(MGLET_ERR_ARG, "set_stencils: inconsistent list");
+            for (long long e = 0; e < n; ++e)
+                if (xpoli[pi + e] < 1 || xpoli[pi + e] > npts)
+                    return fail(MGLET_ERR_ARG, "set_stencils: stencil cell outside the grid");
+            pi += n;
+            pr += n + 1;
+        }
+        if (pi != nxi || pr != nxr) return fail(MGLET_ERR_SIZE, "set_stencils: list lengths");
+        L.xv[q].assign(xpolrvel, xpolrvel + nxrv);
+    }
+    L.n[q] = ncells;
+    L.xi[q].assign(xpoli, xpoli + nxi);
+    L.xr[q].assign(xpolr, xpolr + nxr);
+    return 0;
+}
+
+int mglet_gpu_set_ghostcell(mglet_ctx* c) {
+    if (!c) return fail(MGLET_ERR_ARG, "set_ghostcell: null context");
+    if (c->prm.form != MGLET_FORM_PLAIN)
+        return fail(MGLET_ERR_UNSUPPORTED, "set_ghostcell: the ghost-cell IB runs in the plain form");
+    cudaSetDevice(c->device);
+    if (c->gch.empty()) c->gch.resize(c->ngrid);
+    c->ibtype = 1;
+    if (int rc = launch_giteig(c)) return rc;
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    int rc = c->prm.psolver == MGLET_PSOLVER_CLASSIC ? launch_sip_lu_classic(c) : launch_sip_lu_hp(c);
+    if (rc) return rc;
+    if (c->prm.psolver == MGLET_PSOLVER_SOR)
+        return fail(MGLET_ERR_UNSUPPORTED, "set_ghostcell: SOR with blocked cells");
+    if ((rc = gc_upload(c))) return rc;
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+static int gc_ready(Ctx* c) {
+    if (!c) return fail(MGLET_ERR_ARG, "ghost-cell call: null context");
+    if (c->ibtype != 1) return fail(MGLET_ERR_ARG, "ghost-cell call before set_ghostcell");
+    cudaSetDevice(c->device);
+    return 0;
+}
+
+int mglet_gpu_setibvalues(mglet_ctx* c) {
+    if (int rc = gc_ready(c)) return rc;
+    return gc_setibvalues(c, c->F("U"), c->F("V"), c->F("W"));
+}
+
+int mglet_gpu_getibvalues(mglet_ctx* c) {
+    if (int rc = gc_ready(c)) return rc;
+    return launch_gc_mode(c, 'R', c->F("U"), c->F("V"), c->F("W"));
+}
+
+int mglet_gpu_setpointvalues(mglet_ctx* c, int32_t comp_new) {
+    if (int rc = gc_ready(c)) return rc;
+    return gc_setpointvalues(c, comp_new != 0);
+}
+
+int mglet_gpu_maskbp(mglet_ctx* c) {
+    if (!c) return fail(MGLET_ERR_ARG, "maskbp: null context");
+    cudaSetDevice(c->device);
+    return launch_maskbp(c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
 }
 
 int mglet_gpu_itinfo(mglet_ctx* c, double dt, mglet_itinfo* out) {

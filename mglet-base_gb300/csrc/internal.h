@@ -36,6 +36,28 @@ struct BFace {
     double pinf;        // OP1 far-field pressure (0 unless set)
 };
 
+// Ghost-cell lists of one grid as the caller set them
+struct GcHostList {
+    int n[4] = {0, 0, 0, 0};
+    std::vector<long long> xi[4];
+    std::vector<double> xr[4], xv[3];
+};
+
+// Device copies: per grid and component the offsets of its lists in the
+// concatenated arrays (components 0..2: xpoli / xpolr / xpolrvel / save
+// buffers; 3: flux-correction lists)
+struct GcSeg {
+    long long xi, xr, sv;   // offsets into xpoli, xpolr (= xpolrvel), save buffers
+    int n;
+};
+struct GcDev {
+    GcSeg* seg = nullptr;           // [ngrid][4]
+    long long* xpoli = nullptr;
+    double *xpolr = nullptr, *xpolrvel = nullptr;
+    double *oldsol = nullptr, *oldsolvel = nullptr;
+    long long *poldsol = nullptr, *poldsolvel = nullptr;
+};
+
 // One box copy of connect_self_single (connect2_mod.F90:947-995): the
 // destination box starts at dst (flat element offset), the source box at
 // src; extents nk*nj*ni with per-grid strides.
@@ -109,6 +131,11 @@ struct Ctx {
     // grids (0-based) with a FIX/OP1/NOS/SLI face, per face
     std::vector<int> bgrids[6];
     int* d_bgrids[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    // ghost-cell IB: 0 NONE, 1 GHOSTCELL; host lists per grid (1..3 u, v, w;
+    // 4 flux correction) until gc_upload, then their device copies
+    int ibtype = 0;
+    std::vector<GcHostList> gch;
+    GcDev gcd;
     long long launches = 0;
     bool prof = false;
     std::map<std::string, ProfEntry> profd;
@@ -166,8 +193,11 @@ struct ProfScope {
 };
 
 // ---- kernels: FP64 parity form (plain_*.cu, compiled with -fmad=false) ---
+// u, v, w: the transported velocities (point values PWU.. with the ghost-cell
+// IB), ut, vt, wt: the transporting ones (tstle4_mod.F90:13, 139)
 int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, const double* v,
-                  const double* w, const double* p, const double* g);
+                  const double* w, const double* ut, const double* vt, const double* wt,
+                  const double* p, const double* g);
 int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu);
 int launch_divcal(Ctx* c, double* div, const double* u, const double* v, const double* w,
                   double fak);
@@ -187,6 +217,14 @@ int launch_itinfo(Ctx* c, double dt);
 int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p);
 // boundary buffers and face table (create)
 int bound_init(Ctx* c);
+// 3-D FP64 field of idim3d points, zeroed (api.cu)
+int alloc_field3(Ctx* c, const char* name);
+// ghost-cell IB (plain_gc.cu)
+int gc_upload(Ctx* c);                       // lists to the device, PWU/PWV/PWW, SDIV
+int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w);   // F C S R X Y Z
+int launch_maskbp(Ctx* c, double* u, double* v, double* w, double* p);
+int gc_setibvalues(Ctx* c, double* u, double* v, double* w);
+int gc_setpointvalues(Ctx* c, bool comp_new);
 int launch_connect(Ctx* c, const ConnectPlan& plan, double* const fields[6]);
 // FP32 copy of the same task list; returns early when *skip != 0 (device
 // flag of the mixed form's converged outer loop), skip may be null.

@@ -36,12 +36,12 @@ __device__ __forceinline__ double hm(double a, double b, double gmol) {
 
 // One output point of tstle4 for the U component (kon + diff + gradp).
 __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
-                           const double* w, const double* p, const double* gg, const GridPtrs& s,
+                           const double* w, const double* ut, const double* vt, const double* wt,
+                           const double* p, const double* gg, const GridPtrs& s,
                            double gmol, double rho, double gpx) {
     const double *dx = s.dx, *dy = s.dy, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
                  *rddz = s.rddz;
-    const double *ut = u, *vt = v, *wt = w;
     double uo;
     {
         double ax = ddy[j] * ddz[k], ay = dx[i] * ddz[k], az = dx[i] * ddy[j];
@@ -88,12 +88,12 @@ __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u,
 }
 
 __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
-                           const double* w, const double* p, const double* gg, const GridPtrs& s,
+                           const double* w, const double* ut, const double* vt, const double* wt,
+                           const double* p, const double* gg, const GridPtrs& s,
                            double gmol, double rho, double gpy) {
     const double *dy = s.dy, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
                  *rddz = s.rddz;
-    const double *ut = u, *vt = v, *wt = w;
     double vo;
     {
         double ax = dy[j] * ddz[k], ay = ddx[i] * ddz[k], az = ddx[i] * dy[j];
@@ -140,12 +140,12 @@ __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u,
 }
 
 __device__ double wo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
-                           const double* w, const double* p, const double* gg, const GridPtrs& s,
+                           const double* w, const double* ut, const double* vt, const double* wt,
+                           const double* p, const double* gg, const GridPtrs& s,
                            double gmol, double rho, double gpz) {
     const double *dz = s.dz, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
                  *rddz = s.rddz;
-    const double *ut = u, *vt = v, *wt = w;
     double wo;
     {
         double ax = ddy[j] * dz[k], ay = ddx[i] * dz[k], az = ddx[i] * ddy[j];
@@ -197,6 +197,8 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
                                                 double* __restrict__ uo, double* __restrict__ vo,
                                                 double* __restrict__ wo, const double* __restrict__ U,
                                                 const double* __restrict__ V, const double* __restrict__ W,
+                                                const double* __restrict__ UT, const double* __restrict__ VT,
+                                                const double* __restrict__ WT,
                                                 const double* __restrict__ P, const double* __restrict__ Gf,
                                                 double gmol, double rho, double gx, double gy, double gz) {
     const DevGrid G = grids[blockIdx.y];
@@ -215,6 +217,7 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
     s.rddx = sp.rddx + G.ipx - 1; s.rddy = sp.rddy + G.ipy - 1; s.rddz = sp.rddz + G.ipz - 1;
     const long long o = G.ip3;
     const double *u = U + o, *v = V + o, *w = W + o, *p = P + o, *g = Gf + o;
+    const double *ut = UT + o, *vt = VT + o, *wt = WT + o;
     const int nfro = G.bc[0], nbac = G.bc[1], nrgt = G.bc[2], nlft = G.bc[3], nbot = G.bc[4],
               ntop = G.bc[5];
     const int nbu = (nbac == 7 || nbac == 3) ? 1 : 0;
@@ -225,11 +228,11 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
     const bool jin = j >= 3 && j <= jj - 2, kin = k >= 3 && k <= kk - 2, iin = i >= 3 && i <= ii - 2;
     double ru = 0.0, rv = 0.0, rw = 0.0;
     if (i >= 3 - nfu && i <= ii - 3 + nbu && jin && kin)
-        ru = uo_point(k, j, i, kk, jj, u, v, w, p, g, s, gmol, rho, gx * gfl);
+        ru = uo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, gmol, rho, gx * gfl);
     if (iin && j >= 3 - nrv && j <= jj - 3 + nlv && kin)
-        rv = vo_point(k, j, i, kk, jj, u, v, w, p, g, s, gmol, rho, gy * gfl);
+        rv = vo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, gmol, rho, gy * gfl);
     if (iin && jin && k >= 3 - nbw && k <= kk - 3 + ntw)
-        rw = wo_point(k, j, i, kk, jj, u, v, w, p, g, s, gmol, rho, gz * gfl);
+        rw = wo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, gmol, rho, gz * gfl);
     uo[o + t] = ru;
     vo[o + t] = rv;
     wo[o + t] = rw;
@@ -265,10 +268,11 @@ static int max_points(Ctx* c) {
 }
 
 int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, const double* v,
-                  const double* w, const double* p, const double* g) {
+                  const double* w, const double* ut, const double* vt, const double* wt,
+                  const double* p, const double* g) {
     ProfScope ps_(c, "tstle4");
     dim3 grid((max_points(c) + 255) / 256, c->ngrid);
-    k_tstle4<<<grid, 256, 0, c->stream>>>(c->d_grids, spacing(c), uo, vo, wo, u, v, w, p, g,
+    k_tstle4<<<grid, 256, 0, c->stream>>>(c->d_grids, spacing(c), uo, vo, wo, u, v, w, ut, vt, wt, p, g,
                                           c->prm.gmol, c->prm.rho, c->prm.gradp[0],
                                           c->prm.gradp[1], c->prm.gradp[2]);
     MG_LAUNCHED(c);

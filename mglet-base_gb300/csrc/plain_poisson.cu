@@ -343,7 +343,8 @@ __global__ void k_sor(const DevGrid* __restrict__ grids, int rb, double* DP,
 __global__ void k_divcal(const DevGrid* __restrict__ grids, double* DIV, const double* __restrict__ U,
                          const double* __restrict__ V, const double* __restrict__ W,
                          const double* __restrict__ RDDX, const double* __restrict__ RDDY,
-                         const double* __restrict__ RDDZ, double fak) {
+                         const double* __restrict__ RDDZ, double fak,
+                         const double* __restrict__ SDIV, const double* __restrict__ BP) {
     const DevGrid G = grids[blockIdx.y];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int ni = ii - 4, nj = jj - 4, nk = kk - 4;
@@ -353,9 +354,14 @@ __global__ void k_divcal(const DevGrid* __restrict__ grids, double* DIV, const d
     const long long o = G.ip3;
     const double *u = U + o, *v = V + o, *w = W + o;
     const double rddx = RDDX[G.ipx + i - 1], rddy = RDDY[G.ipy + j - 1], rddz = RDDZ[G.ipz + k - 1];
-    DIV[o + IX(k, j, i)] = fak * ((u[IX(k, j, i)] - u[IX(k, j, i - 1)]) * rddx +
-                                  (v[IX(k, j, i)] - v[IX(k, j - 1, i)]) * rddy +
-                                  (w[IX(k, j, i)] - w[IX(k - 1, j, i)]) * rddz);
+    double d = fak * ((u[IX(k, j, i)] - u[IX(k, j, i - 1)]) * rddx +
+                      (v[IX(k, j, i)] - v[IX(k, j - 1, i)]) * rddy +
+                      (w[IX(k, j, i)] - w[IX(k - 1, j, i)]) * rddz);
+    if (SDIV) {   // ghost-cell IB: gc_mod.F90:278-347 passes sdiv and bp (noib_mod.F90:328-353)
+        d = d + fak * SDIV[o + IX(k, j, i)];
+        d = BP[o + IX(k, j, i)] * d;   // the ghost layers of div stay 0 = bp * 0
+    }
+    DIV[o + IX(k, j, i)] = d;
 }
 
 __global__ void k_laplacephi(const DevGrid* __restrict__ grids, int ilevel, double* RES,
@@ -428,7 +434,7 @@ __global__ void k_accumulate(double* __restrict__ dp, double* __restrict__ hilf,
 __global__ void k_mgpcorr(const DevGrid* __restrict__ grids, double* U, double* V, double* W,
                           double* P, const double* __restrict__ DP, const double* __restrict__ RDX,
                           const double* __restrict__ RDY, const double* __restrict__ RDZ,
-                          double rfak) {
+                          double rfak, const double* __restrict__ BPF) {
     const DevGrid G = grids[blockIdx.y];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -437,6 +443,22 @@ __global__ void k_mgpcorr(const DevGrid* __restrict__ grids, double* U, double* 
     const long long o = G.ip3;
     const double* dp = DP + o;
     const long long c = IX(k, j, i);
+    if (BPF) {   // pressuresolver_mod.F90:808-844, the bp form (ghost-cell IB)
+        const double* bp = BPF + o;
+        if (i >= 2 && i <= ii - 1 && j >= 2 && j <= jj - 1 && k >= 2 && k <= kk - 1)
+            P[o + c] = P[o + c] + dp[c] * bp[c];
+        if (i >= 2 && i <= ii - 2 && j >= 3 && j <= jj - 2 && k >= 3 && k <= kk - 2)
+            U[o + c] = U[o + c] + (dp[c] - dp[IX(k, j, i + 1)]) * bp[c] * bp[IX(k, j, i + 1)] *
+                                      RDX[G.ipx + i - 1] * rfak;
+        if (i >= 3 && i <= ii - 2 && j >= 2 && j <= jj - 2 && k >= 3 && k <= kk - 2)
+            V[o + c] = V[o + c] + (dp[c] - dp[IX(k, j + 1, i)]) * bp[c] * bp[IX(k, j + 1, i)] *
+                                      RDY[G.ipy + j - 1] * rfak;
+        if (i >= 3 && i <= ii - 2 && j >= 3 && j <= jj - 2 && k >= 2 && k <= kk - 2)
+            W[o + c] = W[o + c] + (dp[c] - dp[IX(k + 1, j, i)]) * bp[c] * bp[IX(k + 1, j, i)] *
+                                      RDZ[G.ipz + k - 1] * rfak;
+        return;
+    }
+    // with bp = 1 (noib) the products by bp are exact, so they are left out
     if (i >= 2 && i <= ii - 1 && j >= 2 && j <= jj - 1 && k >= 2 && k <= kk - 1)
         P[o + c] = P[o + c] + dp[c];
     if (i >= 2 && i <= ii - 2 && j >= 3 && j <= jj - 2 && k >= 3 && k <= kk - 2)
@@ -591,8 +613,10 @@ int launch_divcal(Ctx* c, double* div, const double* u, const double* v, const d
                   double fak) {
     ProfScope ps_(c, "divcal");
     dim3 grid((interior_points_max(c) + 255) / 256, c->ngrid);
+    const bool gc = c->ibtype == 1;
     k_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, div, u, v, w, c->L("RDDX"), c->L("RDDY"),
-                                          c->L("RDDZ"), fak);
+                                          c->L("RDDZ"), fak, gc ? c->F("SDIV") : nullptr,
+                                          gc ? c->F("BP") : nullptr);
     MG_LAUNCHED(c);
     return 0;
 }
@@ -631,7 +655,8 @@ int launch_mgpcorr(Ctx* c, double* u, double* v, double* w, double* p, const dou
     ProfScope ps_(c, "mgpcorr");
     dim3 grid((box_points_max(c) + 255) / 256, c->ngrid);
     k_mgpcorr<<<grid, 256, 0, c->stream>>>(c->d_grids, u, v, w, p, dp, c->L("RDX"), c->L("RDY"),
-                                           c->L("RDZ"), rfak);
+                                           c->L("RDZ"), rfak,
+                                           c->ibtype == 1 ? c->F("BP") : nullptr);
     MG_LAUNCHED(c);
     return 0;
 }

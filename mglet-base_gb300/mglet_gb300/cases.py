@@ -287,3 +287,66 @@ def stretch(case, seed=11, amount=0.3):
     case.y, case.dy, case.ddy = axis(case.jj, case.ngrid)
     case.z, case.dz, case.ddz = axis(case.kk, case.ngrid)
     return case
+
+
+def block_body(case, lo, hi, nstc=3, seed=7):
+    """A blocked box of cells in every grid of a case and ghost-cell lists
+    around it, in the formats the reference reads from ib_stencils.h5
+    (gc_flowstencils_mod.F90:37-100).  lo/hi are the 1-based (i, j, k) of the
+    first and last blocked cell; they must stay two cells inside the
+    interior.  The stencils are synthetic (random nearby fluid points with
+    random weights): they exercise the runtime, not a geometry.
+
+    Returns (bp, lists) with lists[g] = {1: (ncells, xpoli, xpolr,
+    xpolrvel), 2: ..., 3: ..., 4: (ncells, fxpoli, fxpolr)}."""
+    rng = np.random.default_rng(seed)
+    kk, jj, ii = case.kk, case.jj, case.ii
+    bp1 = np.ones((ii, jj, kk))
+    bp1[lo[0] - 1:hi[0], lo[1] - 1:hi[1], lo[2] - 1:hi[2]] = 0.0
+    bp = np.tile(bp1.ravel(), case.ngrid)
+    flat = lambda i, j, k: (k - 1) + (j - 1) * kk + (i - 1) * kk * jj + 1   # 1-based
+    shift = {1: (1, 0, 0), 2: (0, 1, 0), 3: (0, 0, 1)}
+    lists = []
+    for g in range(case.ngrid):
+        gl = {}
+        for comp in (1, 2, 3):
+            di, dj, dk = shift[comp]
+            xi, xr, xv, n = [], [], [], 0
+            for i in range(3, ii - 1):
+                for j in range(3, jj - 1):
+                    for k in range(3, kk - 1):
+                        open_ = bp1[i - 1, j - 1, k - 1] * bp1[i - 1 + di, j - 1 + dj, k - 1 + dk]
+                        if open_ != 0.0:
+                            continue
+                        near = [(i + a, j + b, k + cc) for a in (-1, 0, 1) for b in (-1, 0, 1)
+                                for cc in (-1, 0, 1)
+                                if bp1[i + a - 1, j + b - 1, k + cc - 1] *
+                                bp1[i + a - 1 + di, j + b - 1 + dj, k + cc - 1 + dk] != 0.0]
+                        if not near:
+                            continue
+                        pick = rng.choice(len(near), size=min(nstc, len(near)), replace=False)
+                        xi += [flat(i, j, k), len(pick)] + [flat(*near[q]) for q in pick]
+                        w = rng.uniform(0.1, 1.0, len(pick))
+                        xr += list(-w / w.sum()) + [rng.uniform(-1e-3, 1e-3)]
+                        w2 = rng.uniform(0.1, 1.0, len(pick))
+                        xv += list(-w2 / w2.sum()) + [0.0]
+                        n += 1
+            gl[comp] = (n, np.array(xi, dtype=np.int64), np.array(xr), np.array(xv))
+        fi, fr, n = [], [], 0
+        for i in range(3, ii - 1):
+            for j in range(3, jj - 1):
+                for k in range(3, kk - 1):
+                    if bp1[i - 1, j - 1, k - 1] == 0.0:
+                        continue
+                    cut = any(bp1[i - 1 + a, j - 1 + b, k - 1 + cc] == 0.0
+                              for a, b, cc in ((1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0),
+                                               (0, 0, 1), (0, 0, -1)))
+                    if not cut:
+                        continue
+                    fi += [n + 1, flat(i, j, k)]
+                    fr += list(rng.uniform(0.2, 1.0, 6) * case.dx[0] * case.dx[0]) + \
+                        [rng.uniform(-1e-4, 1e-4)]
+                    n += 1
+        gl[4] = (n, np.array(fi, dtype=np.int64), np.array(fr))
+        lists.append(gl)
+    return bp, lists

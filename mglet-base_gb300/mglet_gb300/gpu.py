@@ -25,7 +25,9 @@ EXPORTS = [
     "mglet_gpu_synchronize", "mglet_gpu_kernel_launches", "mglet_gpu_last_error",
     "mglet_gpu_abi_version", "mglet_gpu_stream", "mglet_gpu_profile", "mglet_gpu_profile_get",
     "mglet_gpu_profile_names", "mglet_gpu_divmax_noalloc", "mglet_gpu_bound_flow",
-    "mglet_gpu_set_buffer", "mglet_gpu_set_bc_real",
+    "mglet_gpu_set_buffer", "mglet_gpu_set_bc_real", "mglet_gpu_set_stencils",
+    "mglet_gpu_set_ghostcell", "mglet_gpu_setibvalues", "mglet_gpu_getibvalues",
+    "mglet_gpu_setpointvalues", "mglet_gpu_maskbp",
 ]
 
 
@@ -71,6 +73,12 @@ def load(path=None):
     L.mglet_gpu_bound_flow.argtypes = [vp, C.c_int32]
     L.mglet_gpu_set_buffer.argtypes = [vp, cp, C.c_int32, C.c_int32, vp, C.c_int64]
     L.mglet_gpu_set_bc_real.argtypes = [vp, C.c_int32, C.c_int32, C.c_double]
+    L.mglet_gpu_set_stencils.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int64, vp,
+                                         C.c_int64, vp, C.c_int64]
+    for fn in ("mglet_gpu_set_ghostcell", "mglet_gpu_setibvalues", "mglet_gpu_getibvalues",
+               "mglet_gpu_maskbp"):
+        getattr(L, fn).argtypes = [vp]
+    L.mglet_gpu_setpointvalues.argtypes = [vp, C.c_int32]
     L.mglet_gpu_synchronize.argtypes = [vp]
     L.mglet_gpu_stream.restype = vp
     L.mglet_gpu_stream.argtypes = [vp]
@@ -184,6 +192,27 @@ class Solver:
 
     def set_bc_real(self, igrid, iface, value):
         _check(load().mglet_gpu_set_bc_real(self.h, igrid, iface, value))
+
+    def set_stencils(self, igrid, comp, ncells, xpoli, xpolr, xpolrvel=None):
+        xi = np.ascontiguousarray(xpoli, dtype=np.int64)
+        xr = np.ascontiguousarray(xpolr, dtype=np.float64)
+        xv = np.ascontiguousarray(xpolrvel if xpolrvel is not None else [], dtype=np.float64)
+        _check(load().mglet_gpu_set_stencils(self.h, igrid, comp, ncells,
+                                             xi.ctypes.data_as(C.c_void_p), xi.size,
+                                             xr.ctypes.data_as(C.c_void_p), xr.size,
+                                             xv.ctypes.data_as(C.c_void_p), xv.size))
+
+    def set_ghostcell(self):
+        _check(load().mglet_gpu_set_ghostcell(self.h))
+
+    def setpointvalues(self, comp_new=True):
+        _check(load().mglet_gpu_setpointvalues(self.h, 1 if comp_new else 0))
+
+    def gc_mode(self, mode):
+        """'I' setibvalues, 'R' getibvalues, 'M' maskbp (the oracle's names)."""
+        fn = {"I": "mglet_gpu_setibvalues", "R": "mglet_gpu_getibvalues",
+              "M": "mglet_gpu_maskbp"}[mode]
+        _check(getattr(load(), fn)(self.h))
 
     def itinfo(self, dt):
         out = abi.ItInfo()

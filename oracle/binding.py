@@ -57,6 +57,11 @@ def lib():
         _lib.oracle_set_buffer.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, vp, C.c_int64]
         _lib.oracle_set_bc_real.argtypes = [vp, C.c_int, C.c_int, C.c_double]
         _lib.oracle_bound_flow.argtypes = [vp, C.c_int]
+        _lib.oracle_set_stencils.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, C.c_int64, vp,
+                                             C.c_int64, vp, C.c_int64]
+        _lib.oracle_set_ghostcell.argtypes = [vp]
+        _lib.oracle_setpointvalues.argtypes = [vp, C.c_int]
+        _lib.oracle_gc_mode.argtypes = [vp, C.c_char_p]
         _lib.oracle_rk_init.argtypes = [C.c_char_p, vp]
         _lib.oracle_rk_get_coeffs.argtypes = [vp, C.c_int] + [C.POINTER(C.c_double)] * 4
         _lib.oracle_set_threads.argtypes = [C.c_int]
@@ -191,6 +196,30 @@ class Oracle:
 
     def bound_flow(self, ilevel=0):
         _check(lib().oracle_bound_flow(self.h, ilevel))
+
+    def set_stencils(self, igrid, comp, ncells, xpoli, xpolr, xpolrvel=None):
+        """Ghost-cell lists of grid igrid (1-based): comp 1..3 (u, v, w) with
+        xpoli [intcell, n, stcell x n], xpolr / xpolrvel [coeff x n, const];
+        comp 4 the flux correction, xpoli [foundnr, intcell], xpolr
+        [ax1, ax2, ay1, ay2, az1, az2, acoeff] per cell."""
+        xi = np.ascontiguousarray(xpoli, dtype=np.int64)
+        xr = np.ascontiguousarray(xpolr, dtype=np.float64)
+        xv = np.ascontiguousarray(xpolrvel if xpolrvel is not None else [], dtype=np.float64)
+        _check(lib().oracle_set_stencils(self.h, igrid, comp, ncells, xi.ctypes.data_as(C.c_void_p),
+                                         xi.size, xr.ctypes.data_as(C.c_void_p), xr.size,
+                                         xv.ctypes.data_as(C.c_void_p), xv.size))
+
+    def set_ghostcell(self):
+        _check(lib().oracle_set_ghostcell(self.h))
+
+    def setpointvalues(self, comp_new=True):
+        _check(lib().oracle_setpointvalues(self.h, 1 if comp_new else 0))
+
+    def gc_mode(self, mode):
+        """One ghost-cell operation on U, V, W: 'F', 'C', 'S', 'R', 'X', 'Y',
+        'Z' (setibvalues_level / setpointvalues_all), 'I' (setibvalues), 'M'
+        (maskbp, also P)."""
+        _check(lib().oracle_gc_mode(self.h, _b(mode)))
 
     def itinfo(self, dt):
         from mglet_gb300.abi import ItInfo

@@ -37,7 +37,9 @@
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <array>
 #include <cstring>
+#include <limits>
 #include <map>
 #include <string>
 #include <vector>
@@ -106,6 +108,26 @@ const int rescue_nbr[27][7] = {
 
 inline bool is_con(int t) { return t == MGLET_BC_CON || t == MGLET_BC_CO1; }
 
+// Ghost-cell stencil lists of one velocity component of one grid
+// (gc_flowstencils_mod.F90:37-100): per ghost cell xpoli holds
+// [intcell, n, stcell x n] (1-based positions in the grid's flat array) and
+// xpolr / xpolrvel [coeff x n, const]; oldsol / poldsol are the save buffers
+// of the 'S'/'R' and 'Z'/'Y' modes.
+struct GcList {
+    std::vector<int64_t> xpoli;
+    std::vector<double> xpolr, xpolrvel;
+    int ncells = 0;
+    std::vector<double> oldsol, oldsolvel;
+    std::vector<int64_t> poldsol, poldsolvel;
+};
+// Flux-correction list of one grid: per cell [foundnr, intcell] and
+// [ax1, ax2, ay1, ay2, az1, az2, acoeff].
+struct GcFlux {
+    std::vector<int64_t> fxpoli;
+    std::vector<double> fxpolr;
+    int ncells = 0;
+};
+
 struct Ctx {
     std::vector<Grid> g;   // 1-based (g[0] unused)
     int ngrid = 0;
@@ -123,6 +145,9 @@ struct Ctx {
     std::vector<int64_t> bufoff;
     std::vector<double> pinf;    // OP1 real parameter per grid and face (nreal = 1)
     std::vector<int> npinf;      // 0: no parameter (pinf = 0), 1: pinf given
+    int ibtype = 0;              // 0: NONE (noib), 1: GHOSTCELL
+    std::vector<std::array<GcList, 3>> gcl;   // [grid][component], 1-based grids
+    std::vector<GcFlux> gcf;
 
     double* F(const char* n) { return f3.at(n).data(); }
     double* L(const char* n) { return f1.at(n).data(); }
@@ -795,7 +820,8 @@ double maxabscal(Ctx& c, const double* PHI) {
     return maxabs;
 }
 
-// pressuresolver_mod.F90:787-879 mgpcorr_grid (bp absent for noib)
+// pressuresolver_mod.F90:787-879 mgpcorr_grid with bp (mgpoisl always passes
+// BP, line 333; for the noib BP = 1 the products are exact)
 void mgpcorr(Ctx& c, double* U, double* V, double* W, double* P, const double* DP, double rfak) {
 #pragma omp parallel for schedule(dynamic)
     for (int g = 1; g <= c.ngrid; ++g) {
@@ -807,24 +833,29 @@ void mgpcorr(Ctx& c, double* U, double* V, double* W, double* P, const double* D
         const double* rdx = c.L("RDX") + G.ipx - 1;
         const double* rdy = c.L("RDY") + G.ipy - 1;
         const double* rdz = c.L("RDZ") + G.ipz - 1;
+        const double* bp = c.F("BP") + G.ip3;
         for (int i = 2; i <= ii - 1; ++i)
             for (int j = 2; j <= jj - 1; ++j)
-                for (int k = 2; k <= kk - 1; ++k) p[IX(k, j, i)] = p[IX(k, j, i)] + dp[IX(k, j, i)];
+                for (int k = 2; k <= kk - 1; ++k)
+                    p[IX(k, j, i)] = p[IX(k, j, i)] + dp[IX(k, j, i)] * bp[IX(k, j, i)];
         for (int i = 2; i <= ii - 2; ++i)
             for (int j = 3; j <= jj - 2; ++j)
                 for (int k = 3; k <= kk - 2; ++k)
-                    u[IX(k, j, i)] = u[IX(k, j, i)] +
-                                     (dp[IX(k, j, i)] - dp[IX(k, j, i + 1)]) * rdx[i] * rfak;
+                    u[IX(k, j, i)] = u[IX(k, j, i)] + (dp[IX(k, j, i)] - dp[IX(k, j, i + 1)]) *
+                                                          bp[IX(k, j, i)] * bp[IX(k, j, i + 1)] *
+                                                          rdx[i] * rfak;
         for (int i = 3; i <= ii - 2; ++i)
             for (int j = 2; j <= jj - 2; ++j)
                 for (int k = 3; k <= kk - 2; ++k)
-                    v[IX(k, j, i)] = v[IX(k, j, i)] +
-                                     (dp[IX(k, j, i)] - dp[IX(k, j + 1, i)]) * rdy[j] * rfak;
+                    v[IX(k, j, i)] = v[IX(k, j, i)] + (dp[IX(k, j, i)] - dp[IX(k, j + 1, i)]) *
+                                                          bp[IX(k, j, i)] * bp[IX(k, j + 1, i)] *
+                                                          rdy[j] * rfak;
         for (int i = 3; i <= ii - 2; ++i)
             for (int j = 3; j <= jj - 2; ++j)
                 for (int k = 2; k <= kk - 2; ++k)
-                    w[IX(k, j, i)] = w[IX(k, j, i)] +
-                                     (dp[IX(k, j, i)] - dp[IX(k + 1, j, i)]) * rdz[k] * rfak;
+                    w[IX(k, j, i)] = w[IX(k, j, i)] + (dp[IX(k, j, i)] - dp[IX(k + 1, j, i)]) *
+                                                          bp[IX(k, j, i)] * bp[IX(k + 1, j, i)] *
+                                                          rdz[k] * rfak;
     }
 }
 
@@ -845,6 +876,16 @@ void divcal(Ctx& c, double* DIV, const double* U, const double* V, const double*
                     div[IX(k, j, i)] = fak * ((u[IX(k, j, i)] - u[IX(k, j, i - 1)]) * rddx[i] +
                                               (v[IX(k, j, i)] - v[IX(k, j - 1, i)]) * rddy[j] +
                                               (w[IX(k, j, i)] - w[IX(k - 1, j, i)]) * rddz[k]);
+        if (c.ibtype == 1) {
+            // gc_mod.F90:278-347 passes sdiv and bp to divcal_grid (noib_mod.F90:328-353)
+            const double* sdiv = c.F("SDIV") + G.ip3;
+            const double* bp = c.F("BP") + G.ip3;
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    for (int k = 3; k <= kk - 2; ++k)
+                        div[IX(k, j, i)] = div[IX(k, j, i)] + fak * sdiv[IX(k, j, i)];
+            for (int64_t q = 0; q < (int64_t)kk * jj * ii; ++q) div[q] = bp[q] * div[q];
+        }
     }
 }
 
@@ -1028,14 +1069,203 @@ void bound_flow(Ctx& c, double* U, double* V, double* W, double* P) {
 }
 
 // ---------------------------------------------------------------------------
+// Ghost-cell IB runtime (gc_flowstencils_mod.F90:922-1604, timeintegration_mod
+// :255-303).  The lists are walked cell after cell, as the reference does: a
+// ghost value may feed a later stencil of the same list.
+void wmxpolsol(double* var, const GcList& L, const std::vector<double>& xr) {
+    size_t pi = 0, pr = 0;
+    for (int cell = 0; cell < L.ncells; ++cell) {
+        const int64_t intcell = L.xpoli[pi++];
+        const int64_t n = L.xpoli[pi++];
+        double flux = 0.0;
+        for (int64_t q = 0; q < n; ++q) {
+            const int64_t st = L.xpoli[pi++];
+            flux = flux + var[st - 1] * xr[pr++];
+        }
+        flux = flux + xr[pr++];
+        var[intcell - 1] = flux;
+    }
+}
+
+void wmxpolsolrlx(double* var, int ncells, const std::vector<double>& oldsol,
+                  const std::vector<int64_t>& poldsol) {
+    for (int q = 0; q < ncells; ++q) var[poldsol[q] - 1] = oldsol[q];
+}
+
+void wmxpolsolsav(const double* var, const GcList& L, std::vector<double>& oldsol,
+                  std::vector<int64_t>& poldsol) {
+    oldsol.resize(L.ncells);
+    poldsol.resize(L.ncells);
+    size_t pi = 0;
+    for (int q = 0; q < L.ncells; ++q) {
+        const int64_t idx = L.xpoli[pi++];
+        const int64_t n = L.xpoli[pi++];
+        pi += (size_t)n;
+        poldsol[q] = idx;
+        oldsol[q] = var[idx - 1];
+    }
+}
+
+// gc_flowstencils_mod.F90:1113-1183 wmxpolsolcorr: spread the divergence of a
+// cut cell over its open face areas
+int wmxpolsolcorr(const Grid& G, double* u, double* v, double* w, const double* ddx,
+                  const double* ddy, const double* ddz, const GcFlux& F) {
+    const int kk = G.kk, jj = G.jj;
+    const int64_t ishift = (int64_t)jj * kk, jshift = kk, kshift = 1;
+    size_t pi = 0, pr = 0;
+    for (int cell = 0; cell < F.ncells; ++cell) {
+        pi++;   // foundnr
+        const int64_t intcell = F.fxpoli[pi++];
+        const double ax1 = F.fxpolr[pr++], ax2 = F.fxpolr[pr++], ay1 = F.fxpolr[pr++];
+        const double ay2 = F.fxpolr[pr++], az1 = F.fxpolr[pr++], az2 = F.fxpolr[pr++];
+        const double acoeffstc = F.fxpolr[pr++];
+        const int64_t c0 = intcell - 1;
+        const int k = (int)(c0 % kk) + 1, j = (int)((c0 / kk) % jj) + 1, i = (int)(c0 / ((int64_t)kk * jj)) + 1;
+        double div = ddy[j] * ddz[k] * (u[c0] - u[c0 - ishift]) +
+                     ddx[i] * ddz[k] * (v[c0] - v[c0 - jshift]) +
+                     ddx[i] * ddy[j] * (w[c0] - w[c0 - kshift]) + acoeffstc;
+        const double sarea = ax1 + ax2 + ay1 + ay2 + az1 + az2;
+        if (sarea < std::numeric_limits<double>::min())
+            return fail(MGLET_ERR_ARG, "wmxpolsolcorr: cut cell without open area");
+        div = div / sarea;
+        u[c0] = u[c0] - ax1 * div / (ddy[j] * ddz[k]);
+        u[c0 - ishift] = u[c0 - ishift] + ax2 * div / (ddy[j] * ddz[k]);
+        v[c0] = v[c0] - ay1 * div / (ddx[i] * ddz[k]);
+        v[c0 - jshift] = v[c0 - jshift] + ay2 * div / (ddx[i] * ddz[k]);
+        w[c0] = w[c0] - az1 * div / (ddx[i] * ddy[j]);
+        w[c0 - kshift] = w[c0 - kshift] + az2 * div / (ddx[i] * ddy[j]);
+    }
+    return 0;
+}
+
+// setibvalues_level (:1456-1485) modes F, R, S, C and wmxpolquadvel modes X,
+// Y, Z (setpointvalues_all, :1370-1390)
+int gc_level(Ctx& c, char mode, double* U, double* V, double* W) {
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        double* f[3] = {U + G.ip3, V + G.ip3, W + G.ip3};
+        if (mode == 'C') {
+            if (int rc = wmxpolsolcorr(G, f[0], f[1], f[2], c.L("DDX") + G.ipx - 1,
+                                       c.L("DDY") + G.ipy - 1, c.L("DDZ") + G.ipz - 1, c.gcf[g]))
+                return rc;
+            continue;
+        }
+        for (int cmp = 0; cmp < 3; ++cmp) {
+            GcList& L = c.gcl[g][cmp];
+            switch (mode) {
+            case 'F': wmxpolsol(f[cmp], L, L.xpolr); break;
+            case 'X': wmxpolsol(f[cmp], L, L.xpolrvel); break;
+            case 'R': wmxpolsolrlx(f[cmp], L.ncells, L.oldsol, L.poldsol); break;
+            case 'Y': wmxpolsolrlx(f[cmp], L.ncells, L.oldsolvel, L.poldsolvel); break;
+            case 'S': wmxpolsolsav(f[cmp], L, L.oldsol, L.poldsol); break;
+            case 'Z': wmxpolsolsav(f[cmp], L, L.oldsolvel, L.poldsolvel); break;
+            default: return fail(MGLET_ERR_ARG, "gc: unknown mode");
+            }
+        }
+    }
+    return 0;
+}
+
+// setibvalues (:1393-1438), one level
+int setibvalues(Ctx& c, double* U, double* V, double* W) {
+    bound_flow(c, U, V, W, nullptr);
+    connect(c, 0, 2, U, V, W, nullptr, nullptr, nullptr, false, false, 0);
+    if (int rc = gc_level(c, 'F', U, V, W)) return rc;
+    bound_flow(c, U, V, W, nullptr);
+    connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, true, false, 0);
+    if (int rc = gc_level(c, 'C', U, V, W)) return rc;
+    bound_flow(c, U, V, W, nullptr);
+    connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, true, false, 0);
+    bound_flow(c, U, V, W, nullptr);
+    connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, true, false, 0);
+    if (int rc = gc_level(c, 'C', U, V, W)) return rc;
+    bound_flow(c, U, V, W, nullptr);
+    connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, true, false, 0);
+    return gc_level(c, 'S', U, V, W);
+}
+
+// setpointvalues (:1323-1367): point values = velocities with the ghost
+// cells extrapolated ('X', new) or restored ('Y'), connected and bounded
+int setpointvalues(Ctx& c, bool comp_new) {
+    c.f3["PWU"] = c.f3["U"];
+    c.f3["PWV"] = c.f3["V"];
+    c.f3["PWW"] = c.f3["W"];
+    double *pu = c.F("PWU"), *pv = c.F("PWV"), *pw = c.F("PWW");
+    if (int rc = gc_level(c, comp_new ? 'X' : 'Y', pu, pv, pw)) return rc;
+    connect(c, 0, 1, pu, pv, pw, nullptr, nullptr, nullptr, false, false, 0);
+    bound_flow(c, pu, pv, pw, nullptr);
+    if (comp_new) return gc_level(c, 'Z', pu, pv, pw);
+    return 0;
+}
+
+// timeintegration_mod.F90:277-303 maskbp_grid
+void maskbp(Ctx& c, double* U, double* V, double* W, double* P) {
+    const double* BP = c.F("BP");
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        double* u = U + G.ip3; double* v = V + G.ip3; double* w = W + G.ip3; double* p = P + G.ip3;
+        const double* bp = BP + G.ip3;
+        for (int i = 1; i <= ii - 1; ++i)
+            for (int j = 1; j <= jj - 1; ++j) {
+                for (int k = 1; k <= kk - 1; ++k)
+                    u[IX(k, j, i)] = u[IX(k, j, i)] * bp[IX(k, j, i)] * bp[IX(k, j, i + 1)];
+                for (int k = 1; k <= kk - 1; ++k)
+                    v[IX(k, j, i)] = v[IX(k, j, i)] * bp[IX(k, j, i)] * bp[IX(k, j + 1, i)];
+                for (int k = 1; k <= kk - 1; ++k)
+                    w[IX(k, j, i)] = w[IX(k, j, i)] * bp[IX(k, j, i)] * bp[IX(k + 1, j, i)];
+                for (int k = 1; k <= kk - 1; ++k) p[IX(k, j, i)] = p[IX(k, j, i)] * bp[IX(k, j, i)];
+            }
+    }
+}
+
+// setsdivfield (:1488-1572): the flux-correction constants as a source
+// field, connected, and written back so that both sides of a connected face
+// correct alike
+void setsdivfield(Ctx& c) {
+    double* S = c.F("SDIV");
+    std::fill(c.f3["SDIV"].begin(), c.f3["SDIV"].end(), 0.0);
+    auto walk = [&](bool put) {
+        for (int g = 1; g <= c.ngrid; ++g) {
+            const Grid& G = c.g[g];
+            const int kk = G.kk, jj = G.jj;
+            const double* ddx = c.L("DDX") + G.ipx - 1;
+            const double* ddy = c.L("DDY") + G.ipy - 1;
+            const double* ddz = c.L("DDZ") + G.ipz - 1;
+            GcFlux& F = c.gcf[g];
+            size_t pi = 0, pr = 0;
+            for (int cell = 0; cell < F.ncells; ++cell) {
+                pi++;
+                const int64_t c0 = F.fxpoli[pi++] - 1;
+                pr += 6;
+                const int k = (int)(c0 % kk) + 1, j = (int)((c0 / kk) % jj) + 1;
+                const int i = (int)(c0 / ((int64_t)kk * jj)) + 1;
+                if (put) S[G.ip3 + c0] = F.fxpolr[pr] / (ddx[i] * ddy[j] * ddz[k]);
+                else F.fxpolr[pr] = S[G.ip3 + c0] * ddx[i] * ddy[j] * ddz[k];
+                pr++;
+            }
+        }
+    };
+    walk(true);
+    connect(c, 0, 2, nullptr, nullptr, nullptr, S, nullptr, nullptr, true, false, 0);
+    walk(false);
+}
+
+// ---------------------------------------------------------------------------
 // tstle4_mod.F90:139-265 tstle4_kon, :268-458 tstle4_diff, :461-529 tstle4_gradp
 void tstle4_grid(Ctx& c, int g) {
     const Grid& G = c.g[g];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int64_t o = G.ip3;
     double* uo = c.F("UO") + o; double* vo = c.F("VO") + o; double* wo = c.F("WO") + o;
-    const double* u = c.F("U") + o; const double* v = c.F("V") + o; const double* w = c.F("W") + o;
-    const double* ut = u; const double* vt = v; const double* wt = w;   // noib
+    // tstle4(uo, vo, wo, pwu, pwv, pww, u, v, w, p, g) (timeintegration_mod.F90:101):
+    // the transported velocities are the point values PWU.. for the
+    // ghost-cell IB and U.. otherwise; the transporting ones are always U..
+    const bool gc = c.ibtype == 1;
+    const double* u = c.F(gc ? "PWU" : "U") + o;
+    const double* v = c.F(gc ? "PWV" : "V") + o;
+    const double* w = c.F(gc ? "PWW" : "W") + o;
+    const double* ut = c.F("U") + o; const double* vt = c.F("V") + o; const double* wt = c.F("W") + o;
     const double* p = c.F("P") + o; const double* gg = c.F("G") + o;
     const double* dx = c.L("DX") + G.ipx - 1; const double* dy = c.L("DY") + G.ipy - 1;
     const double* dz = c.L("DZ") + G.ipz - 1;
@@ -1453,8 +1683,10 @@ int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle
     }
     c->idim3d = o3; c->idimx = ox; c->idimy = oy; c->idimz = oz;
     for (const char* n : {"U", "V", "W", "P", "G", "DU", "DV", "DW", "BP", "SDIV", "UO", "VO",
-                          "WO", "DP", "HILF", "RHS", "RES", "GSAP"})
+                          "WO", "DP", "HILF", "RHS", "RES", "GSAP", "PWU", "PWV", "PWW"})
         c->f3[n].assign(o3, 0.0);
+    c->gcl.resize(d->ngrid + 1);
+    c->gcf.resize(d->ngrid + 1);
     std::fill(c->f3["G"].begin(), c->f3["G"].end(), prm->gmol);   // lesmodel_mod.F90:70
     std::fill(c->f3["BP"].begin(), c->f3["BP"].end(), 1.0);       // noib_mod.F90:45-47
     auto set1 = [&](const char* n, const double* src, int64_t len) {
@@ -1605,10 +1837,18 @@ int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timep
     double frhs, fu, dtrk, dtrki;
     int rc = oracle_rk_get_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki);
     if (rc) return rc;
+    const bool gc = c->ibtype == 1;
+    // timeintegration_mod.F90:96-99: the ghost-cell fluxes of the step
+    if (irk == 1 && gc)
+        if (int rc2 = setibvalues(*c, c->F("U"), c->F("V"), c->F("W"))) return rc2;
     tstle4(*c);
     rkstep(c->F("U"), c->F("DU"), c->F("UO"), c->idim3d, frhs, dt * fu);
     rkstep(c->F("V"), c->F("DV"), c->F("VO"), c->idim3d, frhs, dt * fu);
     rkstep(c->F("W"), c->F("DW"), c->F("WO"), c->idim3d, frhs, dt * fu);
+    if (gc) {   // :110-116
+        maskbp(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
+        if (int rc2 = gc_level(*c, 'R', c->F("U"), c->F("V"), c->F("W"))) return rc2;
+    }
     // timeintegration_mod.F90:116-121: connect (normal, forward), bound
     for (int l = c->minlevel; l <= c->maxlevel; ++l) {
         connect(*c, l, 1, c->F("U"), c->F("V"), c->F("W"), nullptr, nullptr, nullptr, false, true, 1);
@@ -1616,6 +1856,7 @@ int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timep
     }
     mgpoisl(*c, dtrk * dt, st);
     (void)ittot;
+    if (gc) return setpointvalues(*c, irk == rk->nrk);   // :131-134
     return 0;
 }
 
@@ -1641,6 +1882,54 @@ int oracle_set_bc_real(oracle_ctx* c, int igrid, int iface, double value) {
     c->pinf[6 * (igrid - 1) + iface - 1] = value;
     c->npinf[6 * (igrid - 1) + iface - 1] = 1;
     return 0;
+}
+
+int oracle_set_stencils(oracle_ctx* c, int igrid, int comp, int ncells, const int64_t* xpoli,
+                        int64_t nxi, const double* xpolr, int64_t nxr, const double* xpolrvel,
+                        int64_t nxrv) {
+    if (!c || igrid < 1 || igrid > c->ngrid || comp < 1 || comp > 4 || ncells < 0 ||
+        (ncells > 0 && (!xpoli || !xpolr)))
+        return fail(MGLET_ERR_ARG, "set_stencils: bad arguments");
+    if (comp == 4) {
+        GcFlux& F = c->gcf[igrid];
+        if (nxi != 2LL * ncells || nxr != 7LL * ncells)
+            return fail(MGLET_ERR_SIZE, "set_stencils: flux list sizes");
+        F.fxpoli.assign(xpoli, xpoli + nxi);
+        F.fxpolr.assign(xpolr, xpolr + nxr);
+        F.ncells = ncells;
+        return 0;
+    }
+    GcList& L = c->gcl[igrid][comp - 1];
+    if (nxrv != nxr || (nxrv > 0 && !xpolrvel)) return fail(MGLET_ERR_SIZE, "set_stencils: xpolrvel");
+    L.xpoli.assign(xpoli, xpoli + nxi);
+    L.xpolr.assign(xpolr, xpolr + nxr);
+    L.xpolrvel.assign(xpolrvel, xpolrvel + nxrv);
+    L.ncells = ncells;
+    return 0;
+}
+
+int oracle_set_ghostcell(oracle_ctx* c) {
+    if (!c) return fail(MGLET_ERR_ARG, "set_ghostcell: null context");
+    c->ibtype = 1;
+    giteig(*c);                       // Poisson coefficients with the blocked cells
+    if (int rc = init_pressuresolver(*c)) return rc;
+    setsdivfield(*c);
+    return 0;
+}
+
+int oracle_setpointvalues(oracle_ctx* c, int comp_new) {
+    if (!c || c->ibtype != 1) return fail(MGLET_ERR_ARG, "setpointvalues: not a ghost-cell case");
+    return setpointvalues(*c, comp_new != 0);
+}
+
+int oracle_gc_mode(oracle_ctx* c, const char* mode) {
+    if (!c || !mode) return fail(MGLET_ERR_ARG, "gc_mode: bad arguments");
+    if (mode[0] == 'M') {
+        maskbp(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
+        return 0;
+    }
+    if (mode[0] == 'I') return setibvalues(*c, c->F("U"), c->F("V"), c->F("W"));
+    return gc_level(*c, mode[0], c->F("U"), c->F("V"), c->F("W"));
 }
 
 int oracle_bound_flow(oracle_ctx* c, int ilevel) {
