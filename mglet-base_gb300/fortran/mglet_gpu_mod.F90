@@ -124,6 +124,28 @@ MODULE mglet_gpu_mod
             REAL(c_double), VALUE :: value
         END FUNCTION mglet_gpu_set_bc_real
 
+        INTEGER(c_int) FUNCTION mglet_gpu_set_stencils(ctx, igrid, comp, ncells, xpoli, nxi, &
+                xpolr, nxr, xpolrvel, nxrv) BIND(C, name="mglet_gpu_set_stencils")
+            IMPORT :: c_int, c_int32_t, c_int64_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: igrid, comp, ncells
+            INTEGER(c_int64_t), INTENT(in) :: xpoli(*)
+            INTEGER(c_int64_t), VALUE :: nxi, nxr, nxrv
+            REAL(c_double), INTENT(in) :: xpolr(*), xpolrvel(*)
+        END FUNCTION mglet_gpu_set_stencils
+
+        INTEGER(c_int) FUNCTION mglet_gpu_set_ghostcell(ctx) BIND(C, name="mglet_gpu_set_ghostcell")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+        END FUNCTION mglet_gpu_set_ghostcell
+
+        INTEGER(c_int) FUNCTION mglet_gpu_setpointvalues(ctx, comp_new) &
+                BIND(C, name="mglet_gpu_setpointvalues")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: comp_new
+        END FUNCTION mglet_gpu_setpointvalues
+
         INTEGER(c_int) FUNCTION mglet_gpu_itinfo(ctx, dt, out) BIND(C, name="mglet_gpu_itinfo")
             IMPORT :: c_int, c_ptr, c_double, mglet_itinfo
             TYPE(c_ptr), VALUE :: ctx
@@ -137,7 +159,8 @@ MODULE mglet_gpu_mod
 
     PUBLIC :: mglet_grid_desc, mglet_flow_params, mglet_rk_scheme, mglet_stage_stats, &
         mglet_itinfo, gpu_init, gpu_finish, gpu_upload, gpu_download, &
-        gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf
+        gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf, &
+        gpu_upload_stencils, gpu_start_ghostcell
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -189,6 +212,27 @@ CONTAINS
         IF (mglet_gpu_set_bc_real(gctx, INT(igrid, c_int32_t), INT(iface, c_int32_t), pinf) /= 0) &
             CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_set_pinf
+
+    ! Ghost-cell lists of one grid and component (the uxpoli/uxpolr/uxpolrvel,
+    ! .., fxpoli/fxpolr arrays of gc_flowstencils_mod after
+    ! create_flowstencils); comp 4 is the flux correction (xpolrvel unused).
+    SUBROUTINE gpu_upload_stencils(igrid, comp, ncells, xpoli, xpolr, xpolrvel)
+        INTEGER, INTENT(in) :: igrid, comp, ncells
+        INTEGER(c_int64_t), INTENT(in) :: xpoli(:)
+        REAL(c_double), INTENT(in) :: xpolr(:), xpolrvel(:)
+        IF (mglet_gpu_set_stencils(gctx, INT(igrid, c_int32_t), INT(comp, c_int32_t), &
+            INT(ncells, c_int32_t), xpoli, INT(SIZE(xpoli), c_int64_t), xpolr, &
+            INT(SIZE(xpolr), c_int64_t), xpolrvel, INT(SIZE(xpolrvel), c_int64_t)) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_upload_stencils
+
+    ! After BP and all lists are uploaded: rebuild the Poisson coefficients,
+    ! build SDIV, and initialise the point values (setpointvalues with new
+    ! extrapolation, as the reference's flow initialisation does).
+    SUBROUTINE gpu_start_ghostcell()
+        IF (mglet_gpu_set_ghostcell(gctx) /= 0) CALL errr(__FILE__, __LINE__)
+        IF (mglet_gpu_setpointvalues(gctx, 1_c_int32_t) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_start_ghostcell
 
     ! Drop-in for timeintegrate_flow (src/flow/timeintegration_mod.F90:22)
     SUBROUTINE gpu_timeintegrate_flow(itstep, ittot, timeph, dt, irk, ipc)
