@@ -61,6 +61,19 @@ MIXED_BYTES = {
 }
 
 
+# DRAM bytes per interior cell and launch measured by ncu (dram__bytes over one
+# launch on 1024 grids of 24^3, profiles/mixed_kernels_1024x24c.md), scaled to
+# the bench case by the number of cells; on 1024 grids part of the working set
+# stays in L2, so these are lower bounds for the full-size launch.
+NCU_TRAFFIC_PER_CELL = {
+    "mx_sip_fwd": 79.4e6 / (1024 * 13824),
+    "mx_sip_bwd": 144.4e6 / (1024 * 13824),
+    "mx_sip_pre": 161.3e6 / (1024 * 13824),
+    "mx_outer": 469.9e6 / (1024 * 13824),
+    "mx_flux": 1383.5e6 / (1024 * 13824),
+}
+
+
 def kernel_bytes(name, case, ninner):
     """Algorithmic bytes of one launch of a kernel family on this case.
     FP32 plane-order SIP kernels: the pre-pass reads hilf and rhs and writes
@@ -342,8 +355,12 @@ def roofline(kern, case, ninner, prof_ms):
     if not b or not n:
         return None
     achieved = b / (tot / n / 1e3) / 1e9
+    tpc = NCU_TRAFFIC_PER_CELL.get(top) if case.n_interior == 24 else None
+    traffic = tpc * case.ncells if tpc else None
     return {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+            "traffic_source": ("ncu dram__bytes of one launch on 1024 x 24^3 grids, scaled by "
+                               "cells" if traffic else None),
             "share": tot / prof_ms if prof_ms else None,
             "algorithmic_bytes_per_launch": b, "avg_launch_ms": tot / n}
 

@@ -217,9 +217,11 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     const int g = blockIdx.x;
     const long long base = (long long)g * s.npp;
     const bool hz = a.hzero != 0;
-    const float* H = a.H + base;   // neighbours gathered through L1
+    const float* __restrict__ H = a.H + base;   // neighbours gathered through L1
+    const float* __restrict__ RHS = a.RHS + base;
+    float* __restrict__ PRE = a.PRE + base;
     const DevGrid G = a.grids[g];
-    const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
+    const float* __restrict__ CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
     const int* fn = a.fnbr + 6 * g;
     const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;   // -x nbr, its x-high plane
     const float* hxp = a.HOUT + ((long long)fn[1] * 6 + 0) * fs;
@@ -231,12 +233,10 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     const float *aw = a.AW + G.ipx + 2, *ae = a.AE + G.ipx + 2;
     const float *as = a.AS + G.ipy + 2, *an = a.AN + G.ipy + 2;
     const float *ab = a.AB + G.ipz + 2, *at = a.AT + G.ipz + 2;
-    for (int q = threadIdx.x; q < s.npp; q += blockDim.x) {
-        const int v = s.pq[q];
-        if (v < 0) {               // padding stays zero for the bulk copies
-            a.PRE[base + q] = 0.f;
-            continue;
-        }
+    // one point: (rhs + lap) * lpr, 0 for padding
+    auto point = [&](int q) -> float {
+        const int v = __ldg(s.pq + q);
+        if (v < 0) return 0.f;     // padding stays zero for the bulk copies
         const int io = v & 1023, jo = (v >> 10) & 1023, ko = v >> 20;
         const int t = io + jo + ko;
         const int p0 = spst[t], lp = spst[t + 1] - p0, rk = q - p0;
@@ -248,18 +248,31 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
             // one row over
             const int bm = (ko > 0 || jo > 0) ? spst[t - 1] + ro[(t - 1) * ni + io] + jo : 0;
             const int bp = (ko < nk - 1 || jo < nj - 1) ? spst[t + 1] + ro[(t + 1) * ni + io] + jo : 0;
-            const float hc = H[q];
-            const float him = io > 0 ? H[spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo] : hxm[fidx_x(s, ko, jo)];
-            const float hip = io < ni - 1 ? H[spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo] : hxp[fidx_x(s, ko, jo)];
-            const float hjm = jo > 0 ? H[bm - 1] : hym[fidx_y(s, ko, io)];
-            const float hjp = jo < nj - 1 ? H[bp + 1] : hyp[fidx_y(s, ko, io)];
-            const float hkm = ko > 0 ? H[bm] : hzm[fidx_z(s, jo, io)];
-            const float hkp = ko < nk - 1 ? H[bp] : hzp[fidx_z(s, jo, io)];
-            lap = -aw[io] * him - ae[io] * hip - as[jo] * hjm - an[jo] * hjp - ab[ko] * hkm -
-                  at[ko] * hkp - cf[4 * lp + rk] * hc;
+            const float hc = __ldg(H + q);
+            const float him = io > 0 ? __ldg(H + spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo)
+                                     : __ldg(hxm + fidx_x(s, ko, jo));
+            const float hip = io < ni - 1 ? __ldg(H + spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo)
+                                          : __ldg(hxp + fidx_x(s, ko, jo));
+            const float hjm = jo > 0 ? __ldg(H + bm - 1) : __ldg(hym + fidx_y(s, ko, io));
+            const float hjp = jo < nj - 1 ? __ldg(H + bp + 1) : __ldg(hyp + fidx_y(s, ko, io));
+            const float hkm = ko > 0 ? __ldg(H + bm) : __ldg(hzm + fidx_z(s, jo, io));
+            const float hkp = ko < nk - 1 ? __ldg(H + bp) : __ldg(hzp + fidx_z(s, jo, io));
+            lap = -__ldg(aw + io) * him - __ldg(ae + io) * hip - __ldg(as + jo) * hjm -
+                  __ldg(an + jo) * hjp - __ldg(ab + ko) * hkm - __ldg(at + ko) * hkp -
+                  __ldg(cf + 4 * lp + rk) * hc;
         }
-        a.PRE[base + q] = (a.RHS[base + q] + lap) * cf[3 * lp + rk];
+        return (__ldg(RHS + q) + lap) * __ldg(cf + 3 * lp + rk);
+    };
+    // two independent points per iteration so their gathers overlap
+    const int stride = blockDim.x;
+    int q = threadIdx.x;
+    for (; q + stride < s.npp; q += 2 * stride) {
+        const float r0 = point(q);
+        const float r1 = point(q + stride);
+        PRE[q] = r0;
+        PRE[q + stride] = r1;
     }
+    if (q < s.npp) PRE[q] = point(q);
 }
 
 // Forward sweep, one thread per point of the current hyperplane: the

@@ -65,6 +65,11 @@ class Case:
         return self.ngrid * self.kk * self.jj * self.ii
 
     @property
+    def n_interior(self):
+        """Interior cells per grid along i (the grids of a case share it)."""
+        return self.ii - 4
+
+    @property
     def ncells(self):
         """Interior cells (the TPC denominator of timeloop_mod.F90:149)."""
         return self.ngrid * (self.kk - 4) * (self.jj - 4) * (self.ii - 4)
