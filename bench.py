@@ -273,6 +273,18 @@ def run_reference(args, rank):
     return 0
 
 
+def reduce_max(value, dist):
+    """The largest value over all ranks (the step time every rank reports is
+    the slowest rank's); the identity without a process group."""
+    if dist is None:
+        return value
+    import torch
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def time_form(args, form, case, fields, local, dist, profile=True):
     """K unprofiled steps on the device (CUDA events on the solver's stream),
     then, if asked, K profiled steps for the per-kernel times.  Returns the
@@ -321,10 +333,7 @@ def time_form(args, form, case, fields, local, dist, profile=True):
     barrier()
     ms = e0.elapsed_time(e1)
     launches = s.launches - l0
-    if dist is not None:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = reduce_max(ms, dist)
     kern, prof_ms = {}, None
     if profile:
         s.profile(True)
