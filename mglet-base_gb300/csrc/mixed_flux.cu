@@ -73,7 +73,7 @@ struct FluxArgs {
 
 // One CTA per j-slab of a grid, one thread per interior (k, j) of the slab,
 // marching i.
-__global__ void __launch_bounds__(576, 1) k_mx_flux(FluxArgs a) {
+__global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     extern __shared__ float2 sm[];
     const DevGrid G = a.grids[blockIdx.x / a.nslab];
     const int slab = blockIdx.x % a.nslab;

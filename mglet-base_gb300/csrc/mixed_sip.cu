@@ -574,7 +574,7 @@ __device__ __forceinline__ void ff_acc(float ch, float cl, float h, float& sum, 
 // bits; hilf itself is FP32) and A hilf is formed in float-float arithmetic,
 // so the step runs on the FP32 pipe only: GB300 issues FP64 at a small
 // fraction of its FP32 rate.  One CTA per grid walks its points in plane order.
-__global__ void __launch_bounds__(512) k_sip_outer(OuterArgs a) {
+__global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
     if (a.ctl[0]) return;
     __shared__ double sh[32];
     extern __shared__ __align__(16) unsigned char osm[];
