@@ -63,6 +63,7 @@ struct Shape {
     const int* pst;    // [nm+1] padded plane starts
     const short* rowoff;   // [nm][ni]: tpos - pst, the rank of (io, jo = 0) in its plane
     const int* pq;     // [npp] point of each padded position: io | jo << 10 | ko << 20, -1 = padding
+    const int* facepos;   // [6][fs] padded position of the boundary point of each face index, -1 = none
 };
 
 __device__ __forceinline__ int fidx_x(const Shape& s, int ko, int jo) { return ko + jo * s.nk; }
@@ -115,18 +116,33 @@ __device__ __forceinline__ void proxy_fence() {
 
 // Thread 0: copy a grid's whole plane-ordered array (n floats, n a multiple
 // of 4) into shared memory with bulk copies of at most 32 KB completing on
-// bar, and wait for it (bounded; a second bounded wait lets copies still in
-// flight land before the caller gives up).
-__device__ __forceinline__ bool stage_grid(float* dst, const float* src, int n,
-                                           unsigned long long* bar) {
+// bar; stage_wait waits for it (bounded; a second bounded wait lets copies
+// still in flight land before the caller gives up).
+__device__ __forceinline__ void stage_issue(float* dst, const float* src, int n,
+                                            unsigned long long* bar) {
     bar_expect(bar, (unsigned)n * 4u);
     for (int o = 0; o < n; o += 8192) {
         const int len = n - o < 8192 ? n - o : 8192;
         bulk_load(dst + o, src + o, (unsigned)len * 4u, bar);
     }
+}
+__device__ __forceinline__ bool stage_wait(unsigned long long* bar) {
     if (bar_wait(bar, 0)) return true;
     bar_wait(bar, 0);
     return false;
+}
+
+// All threads: the hilf ghosts of grid g into gh[6][fs] -- ghost face f is
+// the facing boundary plane of the neighbour across face f (its face f ^ 1),
+// gathered from that neighbour's plane-ordered hilf at the facepos positions.
+__device__ __forceinline__ void gather_hilf_ghosts(float* gh, const Shape& s, const float* H,
+                                                   const int* fn) {
+    const int fs = s.fs;
+    for (int q = threadIdx.x; q < 6 * fs; q += blockDim.x) {
+        const int f = q / fs, fi = q - f * fs;
+        const int pos = __ldg(s.facepos + (f ^ 1) * fs + fi);
+        gh[q] = pos >= 0 ? __ldg(H + (long long)fn[f] * s.npp + pos) : 0.f;
+    }
 }
 
 // Shared memory of the streaming stencil kernels: plane starts, row offsets,
@@ -140,8 +156,7 @@ struct FwdArgs {
     const int* fnbr;            // [ngrid][6] neighbour grid (0-based) across faces 1..6
     const int* gcls;
     float* R;                   // in: (rhs + lap) * lpr from k_sip_pre; out: res
-    const float* RLOW;          // res face buffers with the low ghosts (null: zeros)
-    float* RW;                  // res face buffers to write
+    const float* RLOW;          // res of the iteration the low ghosts come from (null: zeros)
     const float* CF;            // class blocks: per plane [lw|ls|lb|lpr|ap] x Lp
     int* ctl;                   // [0] converged (skip), [2] error flag
 };
@@ -187,8 +202,7 @@ struct PreArgs {
     Shape s;
     const int* fnbr;
     const int* gcls;
-    const float* H;             // hilf, padded plane order
-    const float* HOUT;          // hilf face buffers
+    const float* H;             // hilf, padded plane order (all grids)
     const float* RHS;
     float* PRE;                 // (rhs + lap) * lpr
     const float* CF;
@@ -202,8 +216,8 @@ struct PreArgs {
 // hilf added to rhs and scaled by lpr (sip_hyperplane_mod.F90:491 with the
 // res laplacephi left in it, laplacephi_mod.F90:153-160).  Every point is
 // independent, so this is a plain streaming pass; the forward sweep then
-// carries only the three-term recurrence.  hilf ghosts come from the face
-// buffers the neighbours' backward sweeps wrote.  One CTA per grid.
+// carries only the three-term recurrence.  hilf ghosts are gathered from the
+// neighbours' hilf into shared memory first.  One CTA per grid.
 __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     if (a.ctl[0]) return;
     extern __shared__ __align__(16) unsigned char psm[];
@@ -211,24 +225,20 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm;
     int* spst = reinterpret_cast<int*>(psm);
     short* ro = reinterpret_cast<short*>(spst + nm + 1);
+    float* gh = reinterpret_cast<float*>(psm + stencil_tables_bytes(nm, ni));   // [6][fs]
+    const int g = blockIdx.x;
+    const bool hz = a.hzero != 0;
+    const int* fn = a.fnbr + 6 * g;
     for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
     for (int q = threadIdx.x; q < nm * ni; q += blockDim.x) ro[q] = s.rowoff[q];
+    if (!hz) gather_hilf_ghosts(gh, s, a.H, fn);
     __syncthreads();
-    const int g = blockIdx.x;
     const long long base = (long long)g * s.npp;
-    const bool hz = a.hzero != 0;
-    const float* __restrict__ H = a.H + base;   // neighbours gathered through L1
+    const float* __restrict__ H = a.H + base;
     const float* __restrict__ RHS = a.RHS + base;
     float* __restrict__ PRE = a.PRE + base;
     const DevGrid G = a.grids[g];
     const float* __restrict__ CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
-    const int* fn = a.fnbr + 6 * g;
-    const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;   // -x nbr, its x-high plane
-    const float* hxp = a.HOUT + ((long long)fn[1] * 6 + 0) * fs;
-    const float* hym = a.HOUT + ((long long)fn[2] * 6 + 3) * fs;
-    const float* hyp = a.HOUT + ((long long)fn[3] * 6 + 2) * fs;
-    const float* hzm = a.HOUT + ((long long)fn[4] * 6 + 5) * fs;
-    const float* hzp = a.HOUT + ((long long)fn[5] * 6 + 4) * fs;
     // 1-D coefficients indexed by io, jo, ko (interior index 3 is io = 0)
     const float *aw = a.AW + G.ipx + 2, *ae = a.AE + G.ipx + 2;
     const float *as = a.AS + G.ipy + 2, *an = a.AN + G.ipy + 2;
@@ -250,13 +260,13 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
             const int bp = (ko < nk - 1 || jo < nj - 1) ? spst[t + 1] + ro[(t + 1) * ni + io] + jo : 0;
             const float hc = __ldg(H + q);
             const float him = io > 0 ? __ldg(H + spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo)
-                                     : __ldg(hxm + fidx_x(s, ko, jo));
+                                     : gh[0 * fs + fidx_x(s, ko, jo)];
             const float hip = io < ni - 1 ? __ldg(H + spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo)
-                                          : __ldg(hxp + fidx_x(s, ko, jo));
-            const float hjm = jo > 0 ? __ldg(H + bm - 1) : __ldg(hym + fidx_y(s, ko, io));
-            const float hjp = jo < nj - 1 ? __ldg(H + bp + 1) : __ldg(hyp + fidx_y(s, ko, io));
-            const float hkm = ko > 0 ? __ldg(H + bm) : __ldg(hzm + fidx_z(s, jo, io));
-            const float hkp = ko < nk - 1 ? __ldg(H + bp) : __ldg(hzp + fidx_z(s, jo, io));
+                                          : gh[1 * fs + fidx_x(s, ko, jo)];
+            const float hjm = jo > 0 ? __ldg(H + bm - 1) : gh[2 * fs + fidx_y(s, ko, io)];
+            const float hjp = jo < nj - 1 ? __ldg(H + bp + 1) : gh[3 * fs + fidx_y(s, ko, io)];
+            const float hkm = ko > 0 ? __ldg(H + bm) : gh[4 * fs + fidx_z(s, jo, io)];
+            const float hkp = ko < nk - 1 ? __ldg(H + bp) : gh[5 * fs + fidx_z(s, jo, io)];
             lap = -__ldg(aw + io) * him - __ldg(ae + io) * hip - __ldg(as + jo) * hjm -
                   __ldg(an + jo) * hjp - __ldg(ab + ko) * hkm - __ldg(at + ko) * hkp -
                   __ldg(cf + 4 * lp + rk) * hc;
@@ -294,22 +304,28 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
     float* gr = m.tail;                  // [3][fs] low res ghosts
     unsigned long long* bars =
         reinterpret_cast<unsigned long long*>(((size_t)(gr + 3 * fs) + 15) & ~(size_t)15);
-    unsigned long long* gbar = bars + kFwdSlots;
     const int g = blockIdx.x;
     const int tid = threadIdx.x;
     const long long base = (long long)g * s.npp;
     const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
+    const int* fn = a.fnbr + 6 * g;
     // error flag of step t in sflag[t & 1], written by thread 0 before the
     // step's closing barrier and read by everyone after it; two slots so that
     // thread 0 running ahead never overwrites a flag still being read
     __shared__ int sflag[2];
     for (int q = tid; q < nm * ni; q += blockDim.x) m.rowoff[q] = s.rowoff[q];
     for (int q = tid; q <= nm; q += blockDim.x) m.pst[q] = s.pst[q];
-    if (!a.RLOW)
-        for (int q = tid; q < 3 * fs; q += blockDim.x) gr[q] = 0.f;
+    // low res ghosts: the facing boundary planes of the -x, -y, -z neighbours
+    // (their high faces 2, 4, 6), gathered from the res of the iteration whose
+    // conn(res) was the last full exchange; zero before there is one
+    for (int q = tid; q < 3 * fs; q += blockDim.x) {
+        const int d = q / fs, fi = q - d * fs;
+        const int pos = s.facepos[(2 * d + 1) * fs + fi];
+        gr[q] = (a.RLOW && pos >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f;
+    }
     if (tid == 0) {
         sflag[0] = sflag[1] = 0;
-        for (int q = 0; q <= kFwdSlots; ++q) bar_init(&bars[q], 1);
+        for (int q = 0; q < kFwdSlots; ++q) bar_init(&bars[q], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     int issued = -1, waited = -1;   // thread 0's bookkeeping of the ring
@@ -333,23 +349,13 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
         waited = r;
         return true;
     };
-    const int* fn = a.fnbr + 6 * g;
     __syncthreads();
     if (tid == 0) {
-        // low res ghosts: the three low neighbours' facing planes (unless none yet)
-        const unsigned fb = (unsigned)fs * 4u;
-        bar_expect(gbar, a.RLOW ? 3u * fb : 0u);
-        if (a.RLOW) {
-            bulk_load(gr + 0 * fs, a.RLOW + ((long long)fn[0] * 6 + 1) * fs, fb, gbar);
-            bulk_load(gr + 1 * fs, a.RLOW + ((long long)fn[2] * 6 + 3) * fs, fb, gbar);
-            bulk_load(gr + 2 * fs, a.RLOW + ((long long)fn[4] * 6 + 5) * fs, fb, gbar);
-        }
         for (int r = 0; r < kFwdSlots; ++r) issue(r);
-        if (!bar_wait(gbar, 0) || !wait_rec(0)) bad = sflag[1] = 1;
+        if (!wait_rec(0)) bad = sflag[1] = 1;
     }
     __syncthreads();
     const float *rxm = gr, *rym = gr + fs, *rzm = gr + 2 * fs;
-    float* rw = a.RW + (long long)g * 6 * fs;
     const short* ro = m.rowoff;
     for (int t = 0; t < nm; ++t) {
         if (sflag[(t + 1) & 1]) break;   // step t-1's flag, read after its barrier: uniform
@@ -373,12 +379,6 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
             float r = c0[4 * mlp + tid];
             r = r - c0[2 * lp + tid] * rkm - c0[lp + tid] * rjm - c0[tid] * rimv;
             R[p0 + tid] = r;
-            if (io == 0) rw[0 * fs + fidx_x(s, ko, jo)] = r;
-            if (io == ni - 1) rw[1 * fs + fidx_x(s, ko, jo)] = r;
-            if (jo == 0) rw[2 * fs + fidx_y(s, ko, io)] = r;
-            if (jo == nj - 1) rw[3 * fs + fidx_y(s, ko, io)] = r;
-            if (ko == 0) rw[4 * fs + fidx_z(s, jo, io)] = r;
-            if (ko == nk - 1) rw[5 * fs + fidx_z(s, jo, io)] = r;
             m.xr[(t & 1) * mlp + tid] = r;
         }
         if (tid == 0 && !wait_rec(t + 1)) bad = sflag[t & 1] = 1;
@@ -386,7 +386,6 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
     }
     if (tid == 0 && bad) {
         // error path: let every copy still in flight land before the CTA exits
-        bar_wait(gbar, 0);
         for (int r = waited + 1; r <= issued; ++r)
             if (!bar_wait(&bars[r % kFwdSlots], (r / kFwdSlots) & 1)) break;
         atomicExch(&a.ctl[2], 1);
@@ -398,9 +397,7 @@ struct BwdArgs {
     const int* fnbr;
     const int* gcls;
     float* H;                   // padded plane order, updated: h += res
-    float* HOUT;
-    const float* R;             // forward results
-    const float* RHI;           // res face buffers of this iteration (high ghosts)
+    const float* R;             // forward results of this iteration (also the high ghosts)
     const float* CB;            // class blocks: per plane [ue|un|ut] x Lp
     int* ctl;
     int hzero;
@@ -420,7 +417,6 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_bwd(BwdArgs a) {
     float* gr = m.tail;                  // [3][fs] high res ghosts
     unsigned long long* bars =
         reinterpret_cast<unsigned long long*>(((size_t)(gr + 3 * fs) + 15) & ~(size_t)15);
-    unsigned long long* gbar = bars + kBwdSlots;
     const int g = blockIdx.x;
     const int tid = threadIdx.x;
     const long long base = (long long)g * s.npp;
@@ -432,9 +428,17 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_bwd(BwdArgs a) {
     __shared__ int sflag[2];
     for (int q = tid; q < nm * ni; q += blockDim.x) m.rowoff[q] = s.rowoff[q];
     for (int q = tid; q <= nm; q += blockDim.x) m.pst[q] = s.pst[q];
+    const int* fn = a.fnbr + 6 * g;
+    // high res ghosts: the facing boundary planes of the +x, +y, +z
+    // neighbours (their low faces 1, 3, 5) from this iteration's forward sweep
+    for (int q = tid; q < 3 * fs; q += blockDim.x) {
+        const int d = q / fs, fi = q - d * fs;
+        const int pos = s.facepos[(2 * d) * fs + fi];
+        gr[q] = pos >= 0 ? a.R[(long long)fn[2 * d + 1] * s.npp + pos] : 0.f;
+    }
     if (tid == 0) {
         sflag[0] = sflag[1] = 0;
-        for (int q = 0; q <= kBwdSlots; ++q) bar_init(&bars[q], 1);
+        for (int q = 0; q < kBwdSlots; ++q) bar_init(&bars[q], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     int issued = -1, waited = -1;
@@ -460,20 +464,13 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_bwd(BwdArgs a) {
         waited = r;
         return true;
     };
-    const int* fn = a.fnbr + 6 * g;
     __syncthreads();
-    if (tid == 0) {   // high res ghosts: the +x, +y, +z neighbours' low planes
-        const unsigned fb = (unsigned)fs * 4u;
-        bar_expect(gbar, 3u * fb);
-        bulk_load(gr + 0 * fs, a.RHI + ((long long)fn[1] * 6 + 0) * fs, fb, gbar);
-        bulk_load(gr + 1 * fs, a.RHI + ((long long)fn[3] * 6 + 2) * fs, fb, gbar);
-        bulk_load(gr + 2 * fs, a.RHI + ((long long)fn[5] * 6 + 4) * fs, fb, gbar);
+    if (tid == 0) {
         for (int r = 0; r < kBwdSlots; ++r) issue(r);
-        if (!bar_wait(gbar, 0) || !wait_rec(0)) bad = sflag[1] = 1;
+        if (!wait_rec(0)) bad = sflag[1] = 1;
     }
     __syncthreads();
     const float *rxp = gr, *ryp = gr + fs, *rzp = gr + 2 * fs;
-    float* hw = a.HOUT + (long long)g * 6 * fs;
     float* H = a.H + base;
     const short* ro = m.rowoff;
     for (int t = 0; t < nm; ++t) {
@@ -500,19 +497,12 @@ __global__ void __launch_bounds__(kMaxCols) k_sip_bwd(BwdArgs a) {
                             c0[tid] * ripv;
             const float h = (hz ? 0.f : c0[4 * mlp + tid]) + r;
             H[p0 + tid] = h;
-            if (io == 0) hw[0 * fs + fidx_x(s, ko, jo)] = h;
-            if (io == ni - 1) hw[1 * fs + fidx_x(s, ko, jo)] = h;
-            if (jo == 0) hw[2 * fs + fidx_y(s, ko, io)] = h;
-            if (jo == nj - 1) hw[3 * fs + fidx_y(s, ko, io)] = h;
-            if (ko == 0) hw[4 * fs + fidx_z(s, jo, io)] = h;
-            if (ko == nk - 1) hw[5 * fs + fidx_z(s, jo, io)] = h;
             m.xr[(t & 1) * mlp + tid] = r;
         }
         if (tid == 0 && !wait_rec(t + 1)) bad = sflag[t & 1] = 1;
         __syncthreads();
     }
     if (tid == 0 && bad) {
-        bar_wait(gbar, 0);
         for (int r = waited + 1; r <= issued; ++r)
             if (!bar_wait(&bars[r % kBwdSlots], (r / kBwdSlots) & 1)) break;
         atomicExch(&a.ctl[2], 1);
@@ -537,7 +527,6 @@ struct OuterArgs {
     const int* fnbr;
     const int* gcls;
     const float* H;
-    const float* HOUT;
     float* RHS;                 // rhs = RHS + RHSL in float-float; RHS alone is the sweeps' FP32 rhs
     float* RHSL;
     float* DPH;                 // dp = DPH + DPL in float-float
@@ -583,18 +572,21 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
     int* spst = reinterpret_cast<int*>(osm);
     short* ro = reinterpret_cast<short*>(spst + nm + 1);
     float* H = reinterpret_cast<float*>(osm + stencil_tables_bytes(nm, ni));   // the grid's hilf
-    unsigned long long* bar = reinterpret_cast<unsigned long long*>(H + s.npp);
+    float* gh = H + s.npp;                                                     // [6][fs] its ghosts
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(gh + 6 * fs);
     __shared__ int sok;
     const int g = blockIdx.x;
     const long long base = (long long)g * s.npp;
+    const int* fn = a.fnbr + 6 * g;
     for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
     for (int q = threadIdx.x; q < nm * ni; q += blockDim.x) ro[q] = s.rowoff[q];
     if (threadIdx.x == 0) {
         bar_init(bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        stage_issue(H, a.H + base, s.npp, bar);
     }
-    __syncthreads();
-    if (threadIdx.x == 0) sok = stage_grid(H, a.H + base, s.npp, bar);
+    gather_hilf_ghosts(gh, s, a.H, fn);   // while the bulk copy is in flight
+    if (threadIdx.x == 0) sok = stage_wait(bar);
     __syncthreads();
     if (!sok) {
         if (threadIdx.x == 0) atomicExch(a.ctl_err, 1);
@@ -603,13 +595,6 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
     const DevGrid G = a.grids[g];
     const float* APH = a.APX + (long long)a.gcls[g] * 2 * s.npp;
     const float* APL = APH + s.npp;
-    const int* fn = a.fnbr + 6 * g;
-    const float* hxm = a.HOUT + ((long long)fn[0] * 6 + 1) * fs;
-    const float* hxp = a.HOUT + ((long long)fn[1] * 6 + 0) * fs;
-    const float* hym = a.HOUT + ((long long)fn[2] * 6 + 3) * fs;
-    const float* hyp = a.HOUT + ((long long)fn[3] * 6 + 2) * fs;
-    const float* hzm = a.HOUT + ((long long)fn[4] * 6 + 5) * fs;
-    const float* hzp = a.HOUT + ((long long)fn[5] * 6 + 4) * fs;
     // 1-D coefficients indexed by io, jo, ko (interior index 3 is io = 0)
     const float *awh = a.A1[0] + G.ipx + 2, *awl = a.A1L[0] + G.ipx + 2;
     const float *aeh = a.A1[1] + G.ipx + 2, *ael = a.A1L[1] + G.ipx + 2;
@@ -628,12 +613,12 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
         const int bm = (ko > 0 || jo > 0) ? spst[t - 1] + ro[(t - 1) * ni + io] + jo : 0;
         const int bp = (ko < nk - 1 || jo < nj - 1) ? spst[t + 1] + ro[(t + 1) * ni + io] + jo : 0;
         const float hc = H[q];
-        const float him = io > 0 ? H[spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo] : hxm[fidx_x(s, ko, jo)];
-        const float hip = io < ni - 1 ? H[spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo] : hxp[fidx_x(s, ko, jo)];
-        const float hjm = jo > 0 ? H[bm - 1] : hym[fidx_y(s, ko, io)];
-        const float hjp = jo < nj - 1 ? H[bp + 1] : hyp[fidx_y(s, ko, io)];
-        const float hkm = ko > 0 ? H[bm] : hzm[fidx_z(s, jo, io)];
-        const float hkp = ko < nk - 1 ? H[bp] : hzp[fidx_z(s, jo, io)];
+        const float him = io > 0 ? H[spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo] : gh[0 * fs + fidx_x(s, ko, jo)];
+        const float hip = io < ni - 1 ? H[spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo] : gh[1 * fs + fidx_x(s, ko, jo)];
+        const float hjm = jo > 0 ? H[bm - 1] : gh[2 * fs + fidx_y(s, ko, io)];
+        const float hjp = jo < nj - 1 ? H[bp + 1] : gh[3 * fs + fidx_y(s, ko, io)];
+        const float hkm = ko > 0 ? H[bm] : gh[4 * fs + fidx_z(s, jo, io)];
+        const float hkp = ko < nk - 1 ? H[bp] : gh[5 * fs + fidx_z(s, jo, io)];
         float sum = 0.f, comp = 0.f;
         ff_acc(awh[io], awl[io], him, sum, comp);
         ff_acc(aeh[io], ael[io], hip, sum, comp);
@@ -755,6 +740,7 @@ Shape shape(const SipState& st) {
     s.kk = st.kk; s.jj = st.jj; s.ii = st.ii; s.ni = st.ni; s.nj = st.nj; s.nk = st.nk;
     s.nm = st.nm; s.npp = st.npp; s.fs = st.fs; s.maxlp = st.maxlp;
     s.tpos = st.d_tpos; s.pst = st.d_pst; s.rowoff = st.d_rowoff; s.pq = st.d_pq;
+    s.facepos = st.d_facepos;
     return s;
 }
 
@@ -762,16 +748,20 @@ int sweep_threads(const SipState& st) { return (st.maxlp + 31) / 32 * 32; }
 
 size_t fwd_smem(const SipState& st) {
     const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kFwdSlots, 5 * st.maxlp);
-    return align16(l.tail + (size_t)3 * st.fs * 4) + (kFwdSlots + 1) * 8;
+    return align16(l.tail + (size_t)3 * st.fs * 4) + kFwdSlots * 8;
 }
 
 size_t stencil_smem(const SipState& st) {
-    return stencil_tables_bytes(st.nm, st.ni) + (size_t)st.npp * 4 + 8;
+    return stencil_tables_bytes(st.nm, st.ni) + (size_t)st.npp * 4 + (size_t)6 * st.fs * 4 + 8;
+}
+
+size_t pre_smem(const SipState& st) {
+    return stencil_tables_bytes(st.nm, st.ni) + (size_t)6 * st.fs * 4;
 }
 
 size_t bwd_smem(const SipState& st) {
     const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kBwdSlots, 6 * st.maxlp);
-    return align16(l.tail + (size_t)3 * st.fs * 4) + (kBwdSlots + 1) * 8;
+    return align16(l.tail + (size_t)3 * st.fs * 4) + kBwdSlots * 8;
 }
 
 }  // namespace
@@ -829,6 +819,26 @@ int sip_init(Ctx* c, SipState& st) {
         set_error("mixed form: hyperplane tables do not cover the grid");
         return MGLET_ERR_ARG;
     }
+    // padded position of the boundary point behind every face index: faces
+    // 1/2 (io = 0 / ni-1) indexed by ko + jo nk, 3/4 (jo = 0 / nj-1) by
+    // ko + io nk, 5/6 (ko = 0 / nk-1) by jo + io nj; -1 past the face
+    std::vector<int> facepos((size_t)6 * st.fs, -1);
+    auto posof = [&](int io, int jo, int ko) { return tpos[(size_t)(io + jo + ko) * st.ni + io] + jo; };
+    for (int jo = 0; jo < st.nj; ++jo)
+        for (int ko = 0; ko < st.nk; ++ko) {
+            facepos[0 * st.fs + ko + jo * st.nk] = posof(0, jo, ko);
+            facepos[1 * st.fs + ko + jo * st.nk] = posof(st.ni - 1, jo, ko);
+        }
+    for (int io = 0; io < st.ni; ++io)
+        for (int ko = 0; ko < st.nk; ++ko) {
+            facepos[2 * st.fs + ko + io * st.nk] = posof(io, 0, ko);
+            facepos[3 * st.fs + ko + io * st.nk] = posof(io, st.nj - 1, ko);
+        }
+    for (int io = 0; io < st.ni; ++io)
+        for (int jo = 0; jo < st.nj; ++jo) {
+            facepos[4 * st.fs + jo + io * st.nj] = posof(io, jo, 0);
+            facepos[5 * st.fs + jo + io * st.nj] = posof(io, jo, st.nk - 1);
+        }
     auto up = [c](int** d, const std::vector<int>& h) -> int {
         MG_CUDA(cudaMalloc(d, h.size() * sizeof(int)));
         MG_CUDA(copy_on(c->stream, *d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -839,6 +849,7 @@ int sip_init(Ctx* c, SipState& st) {
     if (int rc = up(&st.d_idxp, idxp)) return rc;
     if (int rc = up(&st.d_qmap, qmap)) return rc;
     if (int rc = up(&st.d_pq, pq)) return rc;
+    if (int rc = up(&st.d_facepos, facepos)) return rc;
     MG_CUDA(cudaMalloc(&st.d_rowoff, rowoff.size() * sizeof(short)));
     MG_CUDA(copy_on(c->stream, st.d_rowoff, rowoff.data(), rowoff.size() * sizeof(short),
                        cudaMemcpyHostToDevice));
@@ -861,20 +872,13 @@ int sip_init(Ctx* c, SipState& st) {
         }
     if (int rc = up(&st.d_fnbr, fn)) return rc;
     const size_t n = (size_t)c->ngrid * st.npp;
-    for (float** p : {&st.h32, &st.r32, &st.rhs32}) {
+    for (float** p : {&st.h32, &st.rs[0], &st.rs[1], &st.rs[2], &st.rhs32}) {
         MG_CUDA(cudaMalloc(p, n * sizeof(float)));
         MG_CUDA(zero_on(c->stream, *p, n * sizeof(float)));
     }
     for (float** p : {&st.rhsl, &st.dph, &st.dpl}) {
         MG_CUDA(cudaMalloc(p, n * sizeof(float)));
         MG_CUDA(zero_on(c->stream, *p, n * sizeof(float)));
-    }
-    const size_t nf = (size_t)c->ngrid * 6 * st.fs;
-    MG_CUDA(cudaMalloc(&st.hout, nf * sizeof(float)));
-    MG_CUDA(zero_on(c->stream, st.hout, nf * sizeof(float)));
-    for (int b = 0; b < 3; ++b) {
-        MG_CUDA(cudaMalloc(&st.rout[b], nf * sizeof(float)));
-        MG_CUDA(zero_on(c->stream, st.rout[b], nf * sizeof(float)));
     }
     // FP32 copies of the 1-D Poisson coefficients
     const char* n1[6] = {"GSAW", "GSAE", "GSAS", "GSAN", "GSAB", "GSAT"};
@@ -923,9 +927,9 @@ int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* 
 void sip_release(SipState& st) {
     for (void* p : {(void*)st.d_tpos, (void*)st.d_pst, (void*)st.d_idxp, (void*)st.d_qmap,
                     (void*)st.d_pq, (void*)st.d_rowoff,
-                    (void*)st.d_fnbr, (void*)st.h32, (void*)st.r32, (void*)st.rhs32,
-                    (void*)st.rhsl, (void*)st.dph, (void*)st.dpl, (void*)st.hout, (void*)st.rout[0],
-                    (void*)st.rout[1], (void*)st.rout[2], (void*)st.a1[0], (void*)st.a1[1],
+                    (void*)st.d_fnbr, (void*)st.h32, (void*)st.rs[0], (void*)st.rs[1],
+                    (void*)st.rs[2], (void*)st.rhs32, (void*)st.rhsl, (void*)st.dph, (void*)st.dpl,
+                    (void*)st.d_facepos, (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
                     (void*)st.a1lo[4], (void*)st.a1lo[5]})
@@ -949,23 +953,22 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
         PreArgs p;
         p.s = shape(st);
         p.fnbr = st.d_fnbr; p.gcls = gcls;
-        p.H = st.h32; p.HOUT = st.hout; p.RHS = st.rhs32; p.PRE = st.r32;
+        p.H = st.h32; p.RHS = st.rhs32; p.PRE = st.rs[rwrite];
         p.CF = cf;
         p.AW = st.a1[0]; p.AE = st.a1[1]; p.AS = st.a1[2]; p.AN = st.a1[3]; p.AB = st.a1[4];
         p.AT = st.a1[5];
         p.grids = c->d_grids;
         p.ctl = ctl;
         p.hzero = hzero ? 1 : 0;
-        k_sip_pre<<<c->ngrid, 512, stencil_tables_bytes(st.nm, st.ni), c->stream>>>(p);
+        k_sip_pre<<<c->ngrid, 512, pre_smem(st), c->stream>>>(p);
         MG_LAUNCHED(c);
     }
     ProfScope ps_(c, "mx_sip_fwd");
     FwdArgs a;
     a.s = shape(st);
     a.fnbr = st.d_fnbr; a.gcls = gcls;
-    a.R = st.r32;
-    a.RLOW = rlow >= 0 ? st.rout[rlow] : nullptr;
-    a.RW = st.rout[rwrite];
+    a.R = st.rs[rwrite];
+    a.RLOW = rlow >= 0 ? st.rs[rlow] : nullptr;
     a.CF = cf;
     a.ctl = ctl;
     const int threads = sweep_threads(st);
@@ -980,7 +983,7 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
     BwdArgs a;
     a.s = shape(st);
     a.fnbr = st.d_fnbr; a.gcls = gcls;
-    a.H = st.h32; a.HOUT = st.hout; a.R = st.r32; a.RHI = st.rout[rhi];
+    a.H = st.h32; a.R = st.rs[rhi];
     a.CB = cb;
     a.ctl = ctl;
     a.hzero = hzero ? 1 : 0;
@@ -995,7 +998,7 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     OuterArgs a;
     a.s = shape(st);
     a.fnbr = st.d_fnbr; a.gcls = gcls;
-    a.H = st.h32; a.HOUT = st.hout;
+    a.H = st.h32;
     a.RHS = st.rhs32; a.RHSL = st.rhsl; a.DPH = st.dph; a.DPL = st.dpl; a.APX = apx;
     for (int q = 0; q < 6; ++q) {
         a.A1[q] = st.a1[q];

@@ -17,12 +17,16 @@ struct SipState {
     int* d_pq = nullptr;        // [npp] io | jo << 16 of each padded position, -1 for padding
     short* d_rowoff = nullptr;  // [nm][ni] rank of (io, jo = 0) in plane m
     int* d_fnbr = nullptr;      // [ngrid][6] face neighbours (0-based)
-    float *h32 = nullptr, *r32 = nullptr;                     // [ngrid][npp]
+    float* h32 = nullptr;                                     // [ngrid][npp]
+    // res in three rotating slots (inner iteration G writes G % 3): the
+    // forward sweep reads its low ghosts from the neighbours' res of the last
+    // fully exchanged iteration, the backward sweep its high ghosts from this
+    // iteration's
+    float* rs[3] = {nullptr, nullptr, nullptr};
     // outer residual and accumulated correction as float-float pairs; the
     // leading float of the residual is the sweeps' FP32 rhs
     float *rhs32 = nullptr, *rhsl = nullptr, *dph = nullptr, *dpl = nullptr;
-    float* hout = nullptr;      // [ngrid][6][fs] hilf boundary planes
-    float* rout[3] = {nullptr, nullptr, nullptr};   // rotating res boundary planes
+    int* d_facepos = nullptr;   // [6][fs] padded position of each face point
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
