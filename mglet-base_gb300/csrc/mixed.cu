@@ -9,7 +9,7 @@
 //  * momentum RHS and RK update: one fused FP32 kernel over FP64 velocity
 //    storage (mixed_flux.cu);
 //  * inner SIP iterations in FP32, hyperplane layout, halos pulled from
-//    per-grid face buffers (mixed_sip.cu); the FP64 outer loop measures the
+//    the neighbours' plane-ordered arrays (mixed_sip.cu); the FP64 outer loop measures the
 //    true residual of the accumulated correction, so the converged pressure
 //    is an FP64 solution;
 //  * grids with identical spacing and boundary types share one coefficient
@@ -130,7 +130,7 @@ __global__ void k_cvt_32_64(double* d, const float* s, long long n) {
 }
 
 // The reference's inner-iteration halo semantics mapped onto the rotating
-// res face buffers: iteration G (1-based within one mgpoisl) writes slot G%3;
+// res slots: iteration G (1-based within one mgpoisl) writes slot G%3;
 // its forward sweep reads low ghosts written by the last iteration whose
 // conn(res) exchanged all faces (inner index < ninner), or zeros.
 int enqueue_mgpoisl(Ctx* c, double dt) {

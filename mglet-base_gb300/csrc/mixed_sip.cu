@@ -1,20 +1,27 @@
 // mixed_sip.cu -- inner SIP iterations of the mixed form: hyperplane layout,
-// TMA-fed wavefronts, pulled halos.
+// register-pipelined wavefronts, pulled halos.
 //
 // The reference stores its SIP factors in hyperplane ("iacc") order so that
 // each wavefront step reads a contiguous run (sip_hyperplane_mod.F90:106-257,
 // 450-569).  Here hilf, res and the FP32 outer residual use that order too,
-// with every plane padded to a 16-byte boundary, so each wavefront step's
-// operands are a handful of contiguous, aligned segments.  One thread per CTA
-// streams them into a shared-memory ring with cp.async.bulk (TMA), four
-// planes ahead of the wavefront, completion tracked by one mbarrier per ring
-// slot; the wavefront itself then only touches shared memory.
+// with every plane padded to a 16-byte boundary.
 //
-// Halos are pulled instead of copied: each sweep writes the six boundary
-// planes of its result into a per-grid face buffer, and the next sweep of a
-// neighbour reads its ghost values from there (no conn kernels).  The
-// lagged-coupling semantics of conn(res) and conn(dp) in sip/mgpoisit
-// (pressuresolver_mod.F90:400-465) are kept exactly:
+// Wavefronts: one CTA per grid walks the i+j+k hyperplanes; a thread owns
+// two ranks of every plane.  Each point's three recurrence neighbours are
+// precomputed (shape only) as positions in one shared-memory array -- the
+// res planes of the previous and current step followed by the ghost faces --
+// so a step is three shared loads, three FMAs, two stores and one
+// __syncthreads.  Every thread loads its points' record for the next step
+// (positions, class coefficients, its res) into registers while it works on
+// the current one: plain coalesced loads, the class coefficients and the
+// tables shared by all grids and served from L2.  Small CTAs (at most 256
+// threads, 32 registers) let eight or more grids share an SM, which is what
+// hides the per-step latency.
+//
+// Halos are pulled instead of copied: a kernel reads its ghost values from
+// the neighbours' plane-ordered arrays through a face position table (no
+// conn kernels).  The lagged-coupling semantics of conn(res) and conn(dp) in
+// sip/mgpoisit (pressuresolver_mod.F90:400-465) are kept exactly:
 //   * the forward sweep of inner iteration G reads its low res ghosts from
 //     the forward results of the last iteration whose conn(res) was a full
 //     exchange (the last inner iteration only exchanges the high faces,
@@ -23,21 +30,13 @@
 //     forward results;
 //   * hilf ghosts are the neighbours' hilf after their last backward sweep;
 //     the first inner iteration of an outer iteration starts from hilf = 0.
-// res face buffers rotate over three slots, which is enough for those reads.
+// res rotates over three slots, which is enough for those reads.
 //
-// Point wavefront: one CTA per grid, one thread per point of the current
-// hyperplane i+j+k = t+9 (planes are at most 1024 points long).  Each plane
-// record carries a point table (io | jo << 10 | ko << 20) so a thread finds its
-// (i, j, k) without searching; the neighbours on planes t-1 and t+1 are
-// found through a per-plane row-offset table.  Only ceil(Lp/32) warps do
-// work in a step, instead of every warp holding a few columns on the band.
-// res of the previous plane comes from a double-buffered shared-memory plane.
-//
-// Every mbarrier wait is bounded: after kWaitCycles SM clocks the kernel
-// records an error in the control block, stops computing, and still waits
-// (bounded) for the copies it has in flight before it exits.  Only thread 0
-// waits on the ring; the step's closing __syncthreads hands the landed data
-// and the error flag to the other threads.
+// The outer step stages its grid's hilf in shared memory with cp.async.bulk;
+// that mbarrier wait is bounded: after kWaitCycles SM clocks the kernel
+// records an error in the control block and, after a second bounded wait for
+// the copies in flight, exits.
+
 #include <algorithm>
 #include <vector>
 
@@ -47,12 +46,7 @@
 namespace mg {
 namespace {
 
-// Ring depths (plane records).  Shallow rings keep a CTA's shared memory
-// small enough for four CTAs per SM, which hides more latency than deeper
-// prefetch does (measured on 24^3 grids: 4/4 beats 6/5 and 8/7).
-constexpr int kFwdSlots = 4;   // steps t .. t+3
-constexpr int kBwdSlots = 4;   // steps t .. t+3 (planes in reverse order)
-constexpr int kMaxCols = 1024; // one thread per hyperplane point
+constexpr int kMaxCols = 1024; // longest hyperplane (points)
 // A wait gives up after this many SM clock cycles (about one second); a
 // healthy wait lasts microseconds.
 constexpr long long kWaitCycles = 2000000000LL;
@@ -64,6 +58,11 @@ struct Shape {
     const short* rowoff;   // [nm][ni]: tpos - pst, the rank of (io, jo = 0) in its plane
     const int* pq;     // [npp] point of each padded position: io | jo << 10 | ko << 20, -1 = padding
     const int* facepos;   // [6][fs] padded position of the boundary point of each face index, -1 = none
+    // [npp][2] per padded position: the positions of the point's three
+    // recurrence neighbours in the sweep's shared array (k | j << 16, i;
+    // i = -1 for padding), forward and backward
+    const int* dscf;
+    const int* dscb;
 };
 
 __device__ __forceinline__ int fidx_x(const Shape& s, int ko, int jo) { return ko + jo * s.nk; }
@@ -108,10 +107,6 @@ __device__ __forceinline__ bool bar_wait(unsigned long long* bar, unsigned parit
         if (done) return true;
         if (clock64() - t0 > kWaitCycles) return false;
     }
-}
-
-__device__ __forceinline__ void proxy_fence() {
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
 // Thread 0: copy a grid's whole plane-ordered array (n floats, n a multiple
@@ -161,42 +156,7 @@ struct FwdArgs {
     int* ctl;                   // [0] converged (skip), [2] error flag
 };
 
-// Shared-memory carve-up common to both sweeps (byte offsets): the ring of
-// plane records, the plane starts, the row-offset table, the two res planes
-// of the recurrence, then the kernel's own tail (ghost faces, barriers).
-struct SweepLayout {
-    size_t pst, rowoff, xr, tail;
-};
-
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
-
-__host__ __device__ inline SweepLayout sweep_layout(int nm, int ni, int mlp, int slots, int rec) {
-    SweepLayout l;
-    l.pst = (size_t)slots * rec * 4;
-    l.rowoff = l.pst + (size_t)(nm + 1) * 4;
-    l.xr = align16(l.rowoff + (size_t)nm * ni * 2);
-    l.tail = l.xr + (size_t)2 * mlp * 4;
-    return l;
-}
-
-struct SweepSmem {
-    float* ring;
-    int* pst;                   // [nm+1] padded plane starts
-    short* rowoff;              // [nm][ni] rank of (io, jo = 0) in plane m
-    float* xr;                  // [2][maxlp]
-    float* tail;                // 16-byte aligned
-};
-
-__device__ __forceinline__ SweepSmem carve(unsigned char* raw, const Shape& s, int slots, int rec) {
-    const SweepLayout l = sweep_layout(s.nm, s.ni, s.maxlp, slots, rec);
-    SweepSmem m;
-    m.ring = reinterpret_cast<float*>(raw);
-    m.pst = reinterpret_cast<int*>(raw + l.pst);
-    m.rowoff = reinterpret_cast<short*>(raw + l.rowoff);
-    m.xr = reinterpret_cast<float*>(raw + l.xr);
-    m.tail = reinterpret_cast<float*>(raw + l.tail);
-    return m;
-}
 
 struct PreArgs {
     Shape s;
@@ -285,113 +245,6 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     if (q < s.npp) PRE[q] = point(q);
 }
 
-// Forward sweep, one thread per point of the current hyperplane: the
-// three-term recurrence res -= lb res(k-1) + ls res(j-1) + lw res(i-1)
-// (sip_hyperplane_mod.F90:491-495) on top of k_sip_pre's (rhs + lap) * lpr.
-// A record (one ring slot) holds plane r's [lw|ls|lb] (stride Lp, the head of
-// the class block), its point table (io | jo << 10 | ko << 20, -1 = padding)
-// and its pre-recurrence values.  Step t needs only record t and the res of
-// plane t-1 (shared memory); thread 0 refills the slot of step t-1 with step
-// t+S-1 at the start of step t and waits for step t+1 before the step's
-// closing barrier, so every other thread only meets __syncthreads.
-__global__ void __launch_bounds__(kMaxCols) k_sip_fwd(FwdArgs a) {
-    if (a.ctl[0]) return;
-    extern __shared__ __align__(128) unsigned char smraw[];
-    const Shape s = a.s;
-    const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm, mlp = s.maxlp;
-    const int rec = 5 * mlp;
-    const SweepSmem m = carve(smraw, s, kFwdSlots, rec);
-    float* gr = m.tail;                  // [3][fs] low res ghosts
-    unsigned long long* bars =
-        reinterpret_cast<unsigned long long*>(((size_t)(gr + 3 * fs) + 15) & ~(size_t)15);
-    const int g = blockIdx.x;
-    const int tid = threadIdx.x;
-    const long long base = (long long)g * s.npp;
-    const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
-    const int* fn = a.fnbr + 6 * g;
-    // error flag of step t in sflag[t & 1], written by thread 0 before the
-    // step's closing barrier and read by everyone after it; two slots so that
-    // thread 0 running ahead never overwrites a flag still being read
-    __shared__ int sflag[2];
-    for (int q = tid; q < nm * ni; q += blockDim.x) m.rowoff[q] = s.rowoff[q];
-    for (int q = tid; q <= nm; q += blockDim.x) m.pst[q] = s.pst[q];
-    // low res ghosts: the facing boundary planes of the -x, -y, -z neighbours
-    // (their high faces 2, 4, 6), gathered from the res of the iteration whose
-    // conn(res) was the last full exchange; zero before there is one
-    for (int q = tid; q < 3 * fs; q += blockDim.x) {
-        const int d = q / fs, fi = q - d * fs;
-        const int pos = s.facepos[(2 * d + 1) * fs + fi];
-        gr[q] = (a.RLOW && pos >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f;
-    }
-    if (tid == 0) {
-        sflag[0] = sflag[1] = 0;
-        for (int q = 0; q < kFwdSlots; ++q) bar_init(&bars[q], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    int issued = -1, waited = -1;   // thread 0's bookkeeping of the ring
-    int bad = 0;
-    float* R = a.R + base;
-    auto issue = [&](int r) {
-        if (r >= nm) return;
-        issued = r;
-        const int sl = r % kFwdSlots;
-        const int p0 = m.pst[r], lp = m.pst[r + 1] - p0;
-        float* d = m.ring + sl * rec;
-        const unsigned b3 = 3u * lp * 4u, b1 = (unsigned)lp * 4u;
-        bar_expect(&bars[sl], b3 + 2u * b1);
-        bulk_load(d, CF + 5LL * p0, b3, &bars[sl]);
-        bulk_load(d + 3 * mlp, s.pq + p0, b1, &bars[sl]);
-        bulk_load(d + 4 * mlp, R + p0, b1, &bars[sl]);
-    };
-    auto wait_rec = [&](int r) -> bool {
-        if (r >= nm || r <= waited) return true;
-        if (!bar_wait(&bars[r % kFwdSlots], (r / kFwdSlots) & 1)) return false;
-        waited = r;
-        return true;
-    };
-    __syncthreads();
-    if (tid == 0) {
-        for (int r = 0; r < kFwdSlots; ++r) issue(r);
-        if (!wait_rec(0)) bad = sflag[1] = 1;
-    }
-    __syncthreads();
-    const float *rxm = gr, *rym = gr + fs, *rzm = gr + 2 * fs;
-    const short* ro = m.rowoff;
-    for (int t = 0; t < nm; ++t) {
-        if (sflag[(t + 1) & 1]) break;   // step t-1's flag, read after its barrier: uniform
-        if (tid == 0 && t >= 1) {
-            proxy_fence();
-            issue(t + kFwdSlots - 1);   // slot of step t-1, released by the last barrier
-        }
-        const int p0 = m.pst[t], lp = m.pst[t + 1] - p0;
-        const float* c0 = m.ring + (t % kFwdSlots) * rec;
-        const int pq = tid < lp ? reinterpret_cast<const int*>(c0 + 3 * mlp)[tid] : -1;
-        if (pq >= 0) {
-            const int io = pq & 1023, jo = (pq >> 10) & 1023, ko = t - io - jo;
-            // rank of (io, jo, ko-1) in plane t-1; (io, jo-1, ko) is the one before it
-            const int rm = (ko > 0 || jo > 0) ? ro[(t - 1) * ni + io] + jo : 0;
-            const int rim = io > 0 ? ro[(t - 1) * ni + io - 1] + jo : 0;
-            const float* xp = m.xr + ((t + 1) & 1) * mlp;   // res of plane t-1
-            const float rkm = ko > 0 ? xp[rm] : rzm[fidx_z(s, jo, io)];
-            const float rjm = jo > 0 ? xp[rm - 1] : rym[fidx_y(s, ko, io)];
-            const float rimv = io > 0 ? xp[rim] : rxm[fidx_x(s, ko, jo)];
-            // block layout: [lw | ls | lb] with stride lp
-            float r = c0[4 * mlp + tid];
-            r = r - c0[2 * lp + tid] * rkm - c0[lp + tid] * rjm - c0[tid] * rimv;
-            R[p0 + tid] = r;
-            m.xr[(t & 1) * mlp + tid] = r;
-        }
-        if (tid == 0 && !wait_rec(t + 1)) bad = sflag[t & 1] = 1;
-        __syncthreads();
-    }
-    if (tid == 0 && bad) {
-        // error path: let every copy still in flight land before the CTA exits
-        for (int r = waited + 1; r <= issued; ++r)
-            if (!bar_wait(&bars[r % kFwdSlots], (r / kFwdSlots) & 1)) break;
-        atomicExch(&a.ctl[2], 1);
-    }
-}
-
 struct BwdArgs {
     Shape s;
     const int* fnbr;
@@ -403,109 +256,179 @@ struct BwdArgs {
     int hzero;
 };
 
-// Backward sweep, one thread per point of the current hyperplane, planes in
-// reverse order.  A record holds [ue|un|ut] (stride Lp), the forward res, the
-// old hilf and the point table of one plane; step t (plane nm-1-t) needs only
-// its own record, so thread 0 refills the slot of step t-1 with step t+4.
-__global__ void __launch_bounds__(kMaxCols) k_sip_bwd(BwdArgs a) {
+// Sweeps.  Shared memory holds the plane starts and nb = [res plane buffer 0
+// (mlp) | buffer 1 (mlp) | ghost faces x, y, z (fs each)]; step t writes
+// buffer t & 1 and reads the previous plane from buffer (t+1) & 1.  Every
+// thread loads its points' records kAhead steps ahead into registers.
+
+__host__ __device__ inline size_t rp_nb_offset(int nm) { return align16((size_t)(nm + 1) * 4); }
+
+struct FRec {
+    int2 dn;
+    float lw, ls, lb, pre;
+};
+
+// Forward sweep: the three-term recurrence res -= lb res(k-1) + ls res(j-1)
+// + lw res(i-1) (sip_hyperplane_mod.F90:491-495) on top of k_sip_pre's
+// (rhs + lap) * lpr, planes in order.  Thread tid owns plane ranks
+// tid + i * blockDim.x, i < kPts.
+template <int kThreads, int kMinBlocks, int kAhead, int kPts>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd(FwdArgs a) {
     if (a.ctl[0]) return;
-    extern __shared__ __align__(128) unsigned char smraw[];
+    extern __shared__ __align__(16) unsigned char rsm[];
     const Shape s = a.s;
-    const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm, mlp = s.maxlp;
-    const int rec = 6 * mlp;
-    const SweepSmem m = carve(smraw, s, kBwdSlots, rec);
-    float* gr = m.tail;                  // [3][fs] high res ghosts
-    unsigned long long* bars =
-        reinterpret_cast<unsigned long long*>(((size_t)(gr + 3 * fs) + 15) & ~(size_t)15);
+    const int fs = s.fs, nm = s.nm, mlp = s.maxlp;
+    int* pst = reinterpret_cast<int*>(rsm);
+    float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // [2][mlp] res planes
+    float* gr = nb + 2 * mlp;                                         // [3][fs] low res ghosts
     const int g = blockIdx.x;
-    const int tid = threadIdx.x;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const long long base = (long long)g * s.npp;
+    const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
+    const int2* D = reinterpret_cast<const int2*>(s.dscf);
+    const int* fn = a.fnbr + 6 * g;
+    float* R = a.R + base;
+    for (int q = tid; q <= nm; q += nt) pst[q] = s.pst[q];
+    // low res ghosts: the facing boundary planes of the -x, -y, -z neighbours
+    // (their high faces 2, 4, 6), gathered from the res of the iteration whose
+    // conn(res) was the last full exchange; zero before there is one
+    for (int q = tid; q < 3 * fs; q += nt) {
+        const int d = q / fs, fi = q - d * fs;
+        const int pos = s.facepos[(2 * d + 1) * fs + fi];
+        gr[q] = (a.RLOW && pos >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f;
+    }
+    __syncthreads();
+    auto fetch = [&](int t, FRec* r) {
+        const int p0 = t < nm ? pst[t] : 0, lp = t < nm ? pst[t + 1] - p0 : 0;
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) {
+            const int k = tid + i * nt;
+            r[i].dn = make_int2(0, -1);
+            r[i].lw = r[i].ls = r[i].lb = r[i].pre = 0.f;
+            if (k < lp) {
+                r[i].dn = __ldg(D + p0 + k);
+                const float* cf = CF + 5LL * p0 + k;   // [lw | ls | lb | ...] with stride lp
+                r[i].lw = __ldg(cf);
+                r[i].ls = __ldg(cf + lp);
+                r[i].lb = __ldg(cf + 2 * lp);
+                r[i].pre = __ldcg(R + p0 + k);
+            }
+        }
+    };
+    FRec q[kAhead][kPts];
+#pragma unroll
+    for (int j = 0; j < kAhead; ++j) fetch(j, q[j]);
+    for (int t = 0; t < nm; ++t) {
+        FRec c[kPts];
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) c[i] = q[0][i];
+#pragma unroll
+        for (int j = 0; j + 1 < kAhead; ++j)
+#pragma unroll
+            for (int i = 0; i < kPts; ++i) q[j][i] = q[j + 1][i];
+        fetch(t + kAhead, q[kAhead - 1]);
+        const int p0 = pst[t];
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) {
+            if (c[i].dn.y >= 0) {
+                const int k = tid + i * nt;
+                const float rkm = nb[c[i].dn.x & 0xffff];
+                const float rjm = nb[(unsigned)c[i].dn.x >> 16];
+                const float rim = nb[c[i].dn.y];
+                float r = c[i].pre;
+                r = r - c[i].lb * rkm - c[i].ls * rjm - c[i].lw * rim;
+                R[p0 + k] = r;
+                nb[(t & 1) * mlp + k] = r;
+            }
+        }
+        __syncthreads();
+    }
+}
+
+struct BRec {
+    int2 dn;
+    float ue, un, ut, res;
+};
+
+// Backward sweep: res -= ut res(k+1) + un res(j+1) + ue res(i+1), hilf +=
+// res (sip_hyperplane_mod.F90:546-547, 559-567), planes in reverse order.
+template <int kThreads, int kMinBlocks, int kAhead, int kPts>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd(BwdArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(16) unsigned char rsm[];
+    const Shape s = a.s;
+    const int fs = s.fs, nm = s.nm, mlp = s.maxlp;
+    int* pst = reinterpret_cast<int*>(rsm);
+    float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // [2][mlp] res planes
+    float* gr = nb + 2 * mlp;                                         // [3][fs] high res ghosts
+    const int g = blockIdx.x;
+    const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float* CB = a.CB + (long long)a.gcls[g] * 3 * s.npp;
-    const bool hz = a.hzero != 0;
-    // error flag of step t in sflag[t & 1], written by thread 0 before the
-    // step's closing barrier and read by everyone after it; two slots so that
-    // thread 0 running ahead never overwrites a flag still being read
-    __shared__ int sflag[2];
-    for (int q = tid; q < nm * ni; q += blockDim.x) m.rowoff[q] = s.rowoff[q];
-    for (int q = tid; q <= nm; q += blockDim.x) m.pst[q] = s.pst[q];
+    const int2* D = reinterpret_cast<const int2*>(s.dscb);
     const int* fn = a.fnbr + 6 * g;
+    const bool hz = a.hzero != 0;
+    const float* R = a.R + base;
+    float* H = a.H + base;
+    for (int q = tid; q <= nm; q += nt) pst[q] = s.pst[q];
     // high res ghosts: the facing boundary planes of the +x, +y, +z
     // neighbours (their low faces 1, 3, 5) from this iteration's forward sweep
-    for (int q = tid; q < 3 * fs; q += blockDim.x) {
+    for (int q = tid; q < 3 * fs; q += nt) {
         const int d = q / fs, fi = q - d * fs;
         const int pos = s.facepos[(2 * d) * fs + fi];
         gr[q] = pos >= 0 ? a.R[(long long)fn[2 * d + 1] * s.npp + pos] : 0.f;
     }
-    if (tid == 0) {
-        sflag[0] = sflag[1] = 0;
-        for (int q = 0; q < kBwdSlots; ++q) bar_init(&bars[q], 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    int issued = -1, waited = -1;
-    int bad = 0;
-    // record r (step r) = plane nm-1-r
-    auto issue = [&](int r) {
-        if (r >= nm) return;
-        issued = r;
-        const int pl = nm - 1 - r;
-        const int sl = r % kBwdSlots;
-        const int p0 = m.pst[pl], lp = m.pst[pl + 1] - p0;
-        float* d = m.ring + sl * rec;
-        const unsigned b3 = 3u * lp * 4u, b1 = (unsigned)lp * 4u;
-        bar_expect(&bars[sl], b3 + 2u * b1 + (hz ? 0u : b1));
-        bulk_load(d, CB + 3LL * p0, b3, &bars[sl]);
-        bulk_load(d + 3 * mlp, a.R + base + p0, b1, &bars[sl]);
-        if (!hz) bulk_load(d + 4 * mlp, a.H + base + p0, b1, &bars[sl]);
-        bulk_load(d + 5 * mlp, s.pq + p0, b1, &bars[sl]);
-    };
-    auto wait_rec = [&](int r) -> bool {
-        if (r >= nm || r <= waited) return true;
-        if (!bar_wait(&bars[r % kBwdSlots], (r / kBwdSlots) & 1)) return false;
-        waited = r;
-        return true;
-    };
     __syncthreads();
-    if (tid == 0) {
-        for (int r = 0; r < kBwdSlots; ++r) issue(r);
-        if (!wait_rec(0)) bad = sflag[1] = 1;
-    }
-    __syncthreads();
-    const float *rxp = gr, *ryp = gr + fs, *rzp = gr + 2 * fs;
-    float* H = a.H + base;
-    const short* ro = m.rowoff;
-    for (int t = 0; t < nm; ++t) {
-        if (sflag[(t + 1) & 1]) break;
-        if (tid == 0 && t >= 1) {
-            proxy_fence();
-            issue(t + kBwdSlots - 1);   // slot of step t-1, released by the last barrier
-        }
+    // step t is plane nm-1-t
+    auto fetch = [&](int t, BRec* r) {
         const int pl = nm - 1 - t;
-        const int p0 = m.pst[pl], lp = m.pst[pl + 1] - p0;
-        const float* c0 = m.ring + (t % kBwdSlots) * rec;
-        const int pq = tid < lp ? reinterpret_cast<const int*>(c0 + 5 * mlp)[tid] : -1;
-        if (pq >= 0) {
-            const int io = pq & 1023, jo = (pq >> 10) & 1023, ko = pl - io - jo;
-            // rank of (io, jo, ko+1) in plane pl+1; (io, jo+1, ko) is the one after it
-            const int rp = (ko < nk - 1 || jo < nj - 1) ? ro[(pl + 1) * ni + io] + jo : 0;
-            const int rip = io < ni - 1 ? ro[(pl + 1) * ni + io + 1] + jo : 0;
-            const float* xp = m.xr + ((t + 1) & 1) * mlp;   // res of plane pl+1
-            const float rkp = ko < nk - 1 ? xp[rp] : rzp[fidx_z(s, jo, io)];
-            const float rjp = jo < nj - 1 ? xp[rp + 1] : ryp[fidx_y(s, ko, io)];
-            const float ripv = io < ni - 1 ? xp[rip] : rxp[fidx_x(s, ko, jo)];
-            // block layout: [ue | un | ut] with stride lp
-            const float r = c0[3 * mlp + tid] - c0[2 * lp + tid] * rkp - c0[lp + tid] * rjp -
-                            c0[tid] * ripv;
-            const float h = (hz ? 0.f : c0[4 * mlp + tid]) + r;
-            H[p0 + tid] = h;
-            m.xr[(t & 1) * mlp + tid] = r;
+        const int p0 = t < nm ? pst[pl] : 0, lp = t < nm ? pst[pl + 1] - p0 : 0;
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) {
+            const int k = tid + i * nt;
+            r[i].dn = make_int2(0, -1);
+            r[i].ue = r[i].un = r[i].ut = r[i].res = 0.f;
+            if (k < lp) {
+                r[i].dn = __ldg(D + p0 + k);
+                const float* cb = CB + 3LL * p0 + k;   // [ue | un | ut] with stride lp
+                r[i].ue = __ldg(cb);
+                r[i].un = __ldg(cb + lp);
+                r[i].ut = __ldg(cb + 2 * lp);
+                r[i].res = __ldg(R + p0 + k);
+            }
         }
-        if (tid == 0 && !wait_rec(t + 1)) bad = sflag[t & 1] = 1;
+    };
+    BRec q[kAhead][kPts];
+#pragma unroll
+    for (int j = 0; j < kAhead; ++j) fetch(j, q[j]);
+    for (int t = 0; t < nm; ++t) {
+        BRec c[kPts];
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) c[i] = q[0][i];
+#pragma unroll
+        for (int j = 0; j + 1 < kAhead; ++j)
+#pragma unroll
+            for (int i = 0; i < kPts; ++i) q[j][i] = q[j + 1][i];
+        fetch(t + kAhead, q[kAhead - 1]);
+        const int p0 = pst[nm - 1 - t];
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) {
+            if (c[i].dn.y >= 0) {
+                const int k = tid + i * nt;
+                const float rkp = nb[c[i].dn.x & 0xffff];
+                const float rjp = nb[(unsigned)c[i].dn.x >> 16];
+                const float rip = nb[c[i].dn.y];
+                const float r = c[i].res - c[i].ut * rkp - c[i].un * rjp - c[i].ue * rip;
+                // hilf += res: one writer per element, so the reduction
+                // (round to nearest) is the plain sum without a load
+                if (hz)
+                    H[p0 + k] = r;
+                else
+                    atomicAdd(H + p0 + k, r);
+                nb[(t & 1) * mlp + k] = r;
+            }
+        }
         __syncthreads();
-    }
-    if (tid == 0 && bad) {
-        for (int r = waited + 1; r <= issued; ++r)
-            if (!bar_wait(&bars[r % kBwdSlots], (r / kBwdSlots) & 1)) break;
-        atomicExch(&a.ctl[2], 1);
     }
 }
 
@@ -741,27 +664,24 @@ Shape shape(const SipState& st) {
     s.nm = st.nm; s.npp = st.npp; s.fs = st.fs; s.maxlp = st.maxlp;
     s.tpos = st.d_tpos; s.pst = st.d_pst; s.rowoff = st.d_rowoff; s.pq = st.d_pq;
     s.facepos = st.d_facepos;
+    s.dscf = st.d_dscf;
+    s.dscb = st.d_dscb;
     return s;
 }
 
-int sweep_threads(const SipState& st) { return (st.maxlp + 31) / 32 * 32; }
-
-size_t fwd_smem(const SipState& st) {
-    const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kFwdSlots, 5 * st.maxlp);
-    return align16(l.tail + (size_t)3 * st.fs * 4) + kFwdSlots * 8;
-}
+// two plane ranks per thread; at most 512 threads (planes of <= 1024 points)
+int sweep_threads(const SipState& st) { return (st.maxlp + 63) / 64 * 32; }
 
 size_t stencil_smem(const SipState& st) {
     return stencil_tables_bytes(st.nm, st.ni) + (size_t)st.npp * 4 + (size_t)6 * st.fs * 4 + 8;
 }
 
-size_t pre_smem(const SipState& st) {
-    return stencil_tables_bytes(st.nm, st.ni) + (size_t)6 * st.fs * 4;
+size_t sweep_smem(const SipState& st) {
+    return rp_nb_offset(st.nm) + ((size_t)2 * st.maxlp + 3 * st.fs) * 4;
 }
 
-size_t bwd_smem(const SipState& st) {
-    const SweepLayout l = sweep_layout(st.nm, st.ni, st.maxlp, kBwdSlots, 6 * st.maxlp);
-    return align16(l.tail + (size_t)3 * st.fs * 4) + kBwdSlots * 8;
+size_t pre_smem(const SipState& st) {
+    return stencil_tables_bytes(st.nm, st.ni) + (size_t)6 * st.fs * 4;
 }
 
 }  // namespace
@@ -771,7 +691,7 @@ int sip_init(Ctx* c, SipState& st) {
     st.kk = G0.kk; st.jj = G0.jj; st.ii = G0.ii;
     st.nk = G0.kk - 4; st.nj = G0.jj - 4; st.ni = G0.ii - 4;
     st.npts = st.ni * st.nj * st.nk;
-    // face buffers are copied whole with cp.async.bulk: a multiple of 16 bytes
+    // length of a ghost face array (the largest face, padded to 4 floats)
     st.fs = (std::max(st.nj * st.nk, std::max(st.ni * st.nk, st.ni * st.nj)) + 3) & ~3;
     st.nm = st.ni + st.nj + st.nk - 2;
     if (st.ni > 1023 || st.nj > 1023 || st.nk > 1023) {
@@ -839,6 +759,41 @@ int sip_init(Ctx* c, SipState& st) {
             facepos[4 * st.fs + jo + io * st.nj] = posof(io, jo, 0);
             facepos[5 * st.fs + jo + io * st.nj] = posof(io, jo, st.nk - 1);
         }
+    // neighbour positions of the sweeps in their shared array nb = [res plane
+    // buffer 0 (mlp) | buffer 1 (mlp) | ghost faces x, y, z (fs each)]: step t
+    // writes buffer t & 1 and reads the previous plane from buffer (t+1) & 1;
+    // the forward sweep's step t is plane t, the backward sweep's plane nm-1-t
+    if (2 * st.maxlp + 3 * st.fs > 65535) {
+        set_error("mixed form: sweep neighbour table exceeds 16-bit positions");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    std::vector<int> dscf((size_t)2 * st.npp, 0), dscb((size_t)2 * st.npp, 0);
+    {
+        auto rank = [&](int io, int jo, int ko) {
+            const int t = io + jo + ko;
+            return tpos[(size_t)t * st.ni + io] + jo - pst[t];
+        };
+        const int gx = 2 * st.maxlp, gy = gx + st.fs, gz = gy + st.fs;
+        for (int p = 0; p < st.npp; ++p) {
+            if (pq[p] < 0) {
+                dscf[2 * p + 1] = dscb[2 * p + 1] = -1;
+                continue;
+            }
+            const int io = pq[p] & 1023, jo = (pq[p] >> 10) & 1023, ko = pq[p] >> 20;
+            const int m0 = io + jo + ko;
+            const int bf = ((m0 + 1) & 1) * st.maxlp, bb = ((st.nm - m0) & 1) * st.maxlp;
+            const int fk = ko > 0 ? bf + rank(io, jo, ko - 1) : gz + jo + io * st.nj;
+            const int fj = jo > 0 ? bf + rank(io, jo - 1, ko) : gy + ko + io * st.nk;
+            const int fi = io > 0 ? bf + rank(io - 1, jo, ko) : gx + ko + jo * st.nk;
+            const int bk = ko < st.nk - 1 ? bb + rank(io, jo, ko + 1) : gz + jo + io * st.nj;
+            const int bj = jo < st.nj - 1 ? bb + rank(io, jo + 1, ko) : gy + ko + io * st.nk;
+            const int bi = io < st.ni - 1 ? bb + rank(io + 1, jo, ko) : gx + ko + jo * st.nk;
+            dscf[2 * p] = fk | (fj << 16);
+            dscf[2 * p + 1] = fi;
+            dscb[2 * p] = bk | (bj << 16);
+            dscb[2 * p + 1] = bi;
+        }
+    }
     auto up = [c](int** d, const std::vector<int>& h) -> int {
         MG_CUDA(cudaMalloc(d, h.size() * sizeof(int)));
         MG_CUDA(copy_on(c->stream, *d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -850,6 +805,8 @@ int sip_init(Ctx* c, SipState& st) {
     if (int rc = up(&st.d_qmap, qmap)) return rc;
     if (int rc = up(&st.d_pq, pq)) return rc;
     if (int rc = up(&st.d_facepos, facepos)) return rc;
+    if (int rc = up(&st.d_dscf, dscf)) return rc;
+    if (int rc = up(&st.d_dscb, dscb)) return rc;
     MG_CUDA(cudaMalloc(&st.d_rowoff, rowoff.size() * sizeof(short)));
     MG_CUDA(copy_on(c->stream, st.d_rowoff, rowoff.data(), rowoff.size() * sizeof(short),
                        cudaMemcpyHostToDevice));
@@ -893,13 +850,10 @@ int sip_init(Ctx* c, SipState& st) {
         MG_CUDA(cudaMalloc(&st.a1lo[qq], len[qq] * sizeof(float)));
         MG_CUDA(copy_on(c->stream, st.a1lo[qq], fl.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
     }
-    const size_t smf = fwd_smem(st), smb = bwd_smem(st);
-    if (smf > 200 * 1024 || smb > 200 * 1024) {
-        set_error("mixed form: hyperplane ring buffers exceed shared memory");
+    if (sweep_smem(st) > 48 * 1024) {
+        set_error("mixed form: sweep shared memory above 48 KB");
         return MGLET_ERR_UNSUPPORTED;
     }
-    MG_CUDA(cudaFuncSetAttribute(k_sip_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smf));
-    MG_CUDA(cudaFuncSetAttribute(k_sip_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smb));
     const size_t sms = stencil_smem(st);
     if (sms > 227 * 1024) {
         set_error("mixed form: a grid's hilf does not fit in shared memory");
@@ -929,7 +883,7 @@ void sip_release(SipState& st) {
                     (void*)st.d_pq, (void*)st.d_rowoff,
                     (void*)st.d_fnbr, (void*)st.h32, (void*)st.rs[0], (void*)st.rs[1],
                     (void*)st.rs[2], (void*)st.rhs32, (void*)st.rhsl, (void*)st.dph, (void*)st.dpl,
-                    (void*)st.d_facepos, (void*)st.a1[0], (void*)st.a1[1],
+                    (void*)st.d_facepos, (void*)st.d_dscf, (void*)st.d_dscb, (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
                     (void*)st.a1lo[4], (void*)st.a1lo[5]})
@@ -971,8 +925,14 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
     a.RLOW = rlow >= 0 ? st.rs[rlow] : nullptr;
     a.CF = cf;
     a.ctl = ctl;
+    // 256-thread CTAs at 32 registers: eight grids per SM (measured on 24^3
+    // grids against one rank per thread at four CTAs per SM and deeper
+    // register prefetch, both slower)
     const int threads = sweep_threads(st);
-    k_sip_fwd<<<c->ngrid, threads, fwd_smem(st), c->stream>>>(a);
+    if (threads <= 256)
+        k_sip_fwd<256, 8, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
+    else
+        k_sip_fwd<512, 4, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }
@@ -987,8 +947,14 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
     a.CB = cb;
     a.ctl = ctl;
     a.hzero = hzero ? 1 : 0;
+    // 256-thread CTAs at 32 registers: eight grids per SM (measured on 24^3
+    // grids against one rank per thread at four CTAs per SM and deeper
+    // register prefetch, both slower)
     const int threads = sweep_threads(st);
-    k_sip_bwd<<<c->ngrid, threads, bwd_smem(st), c->stream>>>(a);
+    if (threads <= 256)
+        k_sip_bwd<256, 8, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
+    else
+        k_sip_bwd<512, 4, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }

@@ -14,7 +14,7 @@ struct SipState {
     int* d_pst = nullptr;       // [nm+1] padded plane starts
     int* d_idxp = nullptr;      // [npp] natural local index, -1 for padding
     int* d_qmap = nullptr;      // [npp] unpadded plane position (iacc-1), -1 for padding
-    int* d_pq = nullptr;        // [npp] io | jo << 16 of each padded position, -1 for padding
+    int* d_pq = nullptr;        // [npp] io | jo << 10 | ko << 20 of each padded position, -1 for padding
     short* d_rowoff = nullptr;  // [nm][ni] rank of (io, jo = 0) in plane m
     int* d_fnbr = nullptr;      // [ngrid][6] face neighbours (0-based)
     float* h32 = nullptr;                                     // [ngrid][npp]
@@ -27,6 +27,8 @@ struct SipState {
     // leading float of the residual is the sweeps' FP32 rhs
     float *rhs32 = nullptr, *rhsl = nullptr, *dph = nullptr, *dpl = nullptr;
     int* d_facepos = nullptr;   // [6][fs] padded position of each face point
+    int* d_dscf = nullptr;      // [npp][2] forward / backward sweep neighbour positions
+    int* d_dscb = nullptr;
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
