@@ -153,6 +153,7 @@ struct FwdArgs {
     float* R;                   // in: (rhs + lap) * lpr from k_sip_pre; out: res
     const float* RLOW;          // res of the iteration the low ghosts come from (null: zeros)
     const float* CF;            // class blocks: per plane [lw|ls|lb|lpr|ap] x Lp
+    const float4* SW;           // packed records {position word, lw, ls, lb} (packed form)
     int* ctl;                   // [0] converged (skip), [2] error flag
 };
 
@@ -252,6 +253,7 @@ struct BwdArgs {
     float* H;                   // padded plane order, updated: h += res
     const float* R;             // forward results of this iteration (also the high ghosts)
     const float* CB;            // class blocks: per plane [ue|un|ut] x Lp
+    const float4* SW;           // packed records {position word, ue, un, ut} (packed form)
     int* ctl;
     int hzero;
 };
@@ -430,6 +432,198 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd(BwdArgs a) {
         }
         __syncthreads();
     }
+}
+
+// Packed sweeps, for shapes with maxlp + fs <= 1024 and maxlp + 2 fs <= 2048
+// (24^3 grids: 432 + 576).  Shared memory holds two regions [y ghosts (fs) |
+// res plane (mlp) | z ghosts (fs) | x ghosts (fs)] -- the ghost faces copied
+// into both -- and step t writes the plane of region t & 1 and reads the
+// previous plane from region (t+1) & 1.  A point's three neighbours then fit
+// one word relative to the region: j | k << 10 | i << 20 (j from the region
+// start, k and i from its plane; -1 for padding), and a point's record
+// {word, three coefficients} is one 16-byte load, its res / pre value a
+// second.  The step loop is unrolled by two so the two record sets alternate
+// without copies.
+__host__ __device__ inline size_t packed_region(int mlp, int fs) { return (size_t)mlp + 3 * (size_t)fs; }
+
+// the ghost value of face direction d (0 x, 1 y, 2 z), face index fi, into
+// both regions
+__device__ __forceinline__ void put_ghost(float* nb, int rs, int mlp, int fs, int d, int fi, float v) {
+    const int off = d == 1 ? fi : (d == 2 ? fs + mlp + fi : 2 * fs + mlp + fi);
+    nb[off] = v;
+    nb[rs + off] = v;
+}
+
+struct PRec {
+    float4 w;    // position word (bits), three coefficients
+    float v;     // pre (forward) / res (backward)
+};
+
+template <int kThreads, int kMinBlocks, int kPts>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd_packed(FwdArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(16) unsigned char rsm[];
+    const Shape s = a.s;
+    const int fs = s.fs, nm = s.nm, mlp = s.maxlp;
+    const int rs = (int)packed_region(mlp, fs);
+    int* pst = reinterpret_cast<int*>(rsm);
+    float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // two regions
+    const int g = blockIdx.x;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const long long base = (long long)g * s.npp;
+    const float4* SW = a.SW + (long long)a.gcls[g] * s.npp;
+    const int* fn = a.fnbr + 6 * g;
+    float* R = a.R + base;
+    for (int q = tid; q <= nm; q += nt) pst[q] = s.pst[q];
+    // low res ghosts: the facing boundary planes of the -x, -y, -z neighbours
+    // (their high faces 2, 4, 6), gathered from the res of the iteration whose
+    // conn(res) was the last full exchange; zero before there is one
+    for (int q = tid; q < 3 * fs; q += nt) {
+        const int d = q / fs, fi = q - d * fs;
+        const int pos = s.facepos[(2 * d + 1) * fs + fi];
+        put_ghost(nb, rs, mlp, fs, d, fi,
+                  (a.RLOW && pos >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f);
+    }
+    __syncthreads();
+    auto fetch = [&](int t, PRec* r) {
+        const int p0 = t < nm ? pst[t] : 0, lp = t < nm ? pst[t + 1] - p0 : 0;
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) {
+            const int k = tid + i * nt;
+            if (k < lp) {
+                r[i].w = __ldg(SW + p0 + k);
+                r[i].v = __ldcg(R + p0 + k);
+            } else {
+                r[i].w.x = __int_as_float(-1);
+            }
+        }
+    };
+    auto step = [&](int t, const PRec* c) {
+        const int p0 = pst[t];
+        const float* pv = nb + ((t + 1) & 1) * rs;   // region of plane t-1
+        float* cur = nb + (t & 1) * rs + fs;         // plane t
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) {
+            const int w = __float_as_int(c[i].w.x);
+            if (w >= 0) {
+                const int k = tid + i * nt;
+                const float rjm = pv[w & 1023];
+                const float rkm = pv[fs + ((w >> 10) & 1023)];
+                const float rim = pv[fs + (w >> 20)];
+                // record: {word, lw, ls, lb}
+                float r = c[i].v;
+                r = r - c[i].w.w * rkm - c[i].w.z * rjm - c[i].w.y * rim;
+                R[p0 + k] = r;
+                cur[k] = r;
+            }
+        }
+    };
+    PRec qa[kPts], qb[kPts];
+    fetch(0, qa);
+    for (int t = 0; t < nm; t += 2) {
+        fetch(t + 1, qb);
+        step(t, qa);
+        __syncthreads();
+        if (t + 1 >= nm) break;
+        fetch(t + 2, qa);
+        step(t + 1, qb);
+        __syncthreads();
+    }
+}
+
+template <int kThreads, int kMinBlocks, int kPts>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(16) unsigned char rsm[];
+    const Shape s = a.s;
+    const int fs = s.fs, nm = s.nm, mlp = s.maxlp;
+    const int rs = (int)packed_region(mlp, fs);
+    int* pst = reinterpret_cast<int*>(rsm);
+    float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // two regions
+    const int g = blockIdx.x;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const long long base = (long long)g * s.npp;
+    const float4* SW = a.SW + (long long)a.gcls[g] * s.npp;
+    const int* fn = a.fnbr + 6 * g;
+    const bool hz = a.hzero != 0;
+    const float* R = a.R + base;
+    float* H = a.H + base;
+    for (int q = tid; q <= nm; q += nt) pst[q] = s.pst[q];
+    // high res ghosts: the facing boundary planes of the +x, +y, +z
+    // neighbours (their low faces 1, 3, 5) from this iteration's forward sweep
+    for (int q = tid; q < 3 * fs; q += nt) {
+        const int d = q / fs, fi = q - d * fs;
+        const int pos = s.facepos[(2 * d) * fs + fi];
+        put_ghost(nb, rs, mlp, fs, d, fi, pos >= 0 ? a.R[(long long)fn[2 * d + 1] * s.npp + pos] : 0.f);
+    }
+    __syncthreads();
+    // step t is plane nm-1-t
+    auto fetch = [&](int t, PRec* r) {
+        const int pl = nm - 1 - t;
+        const int p0 = t < nm ? pst[pl] : 0, lp = t < nm ? pst[pl + 1] - p0 : 0;
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) {
+            const int k = tid + i * nt;
+            if (k < lp) {
+                r[i].w = __ldg(SW + p0 + k);
+                r[i].v = __ldg(R + p0 + k);
+            } else {
+                r[i].w.x = __int_as_float(-1);
+            }
+        }
+    };
+    auto step = [&](int t, const PRec* c) {
+        const int p0 = pst[nm - 1 - t];
+        const float* pv = nb + ((t + 1) & 1) * rs;   // region of plane pl+1
+        float* cur = nb + (t & 1) * rs + fs;
+#pragma unroll
+        for (int i = 0; i < kPts; ++i) {
+            const int w = __float_as_int(c[i].w.x);
+            if (w >= 0) {
+                const int k = tid + i * nt;
+                const float rjp = pv[w & 1023];
+                const float rkp = pv[fs + ((w >> 10) & 1023)];
+                const float rip = pv[fs + (w >> 20)];
+                // record: {word, ue, un, ut}
+                const float r = c[i].v - c[i].w.w * rkp - c[i].w.z * rjp - c[i].w.y * rip;
+                // hilf += res: one writer per element, so the reduction
+                // (round to nearest) is the plain sum without a load
+                if (hz)
+                    H[p0 + k] = r;
+                else
+                    atomicAdd(H + p0 + k, r);
+                cur[k] = r;
+            }
+        }
+    };
+    PRec qa[kPts], qb[kPts];
+    fetch(0, qa);
+    for (int t = 0; t < nm; t += 2) {
+        fetch(t + 1, qb);
+        step(t, qa);
+        __syncthreads();
+        if (t + 1 >= nm) break;
+        fetch(t + 2, qa);
+        step(t + 1, qb);
+        __syncthreads();
+    }
+}
+
+// packed records of a class: {position word, the three coefficients of the
+// class block of the sweep} per padded position
+__global__ void k_sip_records(const int* __restrict__ pst, int nm, int npp, const int* __restrict__ wf,
+                              const int* __restrict__ wb, const float* __restrict__ CF,
+                              const float* __restrict__ CB, float4* SWF, float4* SWB) {
+    const int cls = blockIdx.y;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npp) return;
+    int m = 0;
+    while (m + 1 <= nm && pst[m + 1] <= p) ++m;
+    const int p0 = pst[m], lp = pst[m + 1] - p0, rk = p - p0;
+    const float* cf = CF + (long long)cls * 5 * npp + 5LL * p0 + rk;
+    const float* cb = CB + (long long)cls * 3 * npp + 3LL * p0 + rk;
+    SWF[(long long)cls * npp + p] = make_float4(__int_as_float(wf[p]), cf[0], cf[lp], cf[2 * lp]);
+    SWB[(long long)cls * npp + p] = make_float4(__int_as_float(wb[p]), cb[0], cb[lp], cb[2 * lp]);
 }
 
 __device__ __forceinline__ double block_max2(double v, double* sh) {
@@ -676,6 +870,10 @@ size_t stencil_smem(const SipState& st) {
     return stencil_tables_bytes(st.nm, st.ni) + (size_t)st.npp * 4 + (size_t)6 * st.fs * 4 + 8;
 }
 
+size_t packed_smem(const SipState& st) {
+    return rp_nb_offset(st.nm) + 2 * packed_region(st.maxlp, st.fs) * 4;
+}
+
 size_t sweep_smem(const SipState& st) {
     return rp_nb_offset(st.nm) + ((size_t)2 * st.maxlp + 3 * st.fs) * 4;
 }
@@ -794,6 +992,30 @@ int sip_init(Ctx* c, SipState& st) {
             dscb[2 * p + 1] = bi;
         }
     }
+    // packed position words (see k_sip_fwd_packed) when the shape allows them
+    st.packed = st.maxlp + st.fs <= 1024 && st.maxlp + 2 * st.fs <= 2048;
+    std::vector<int> wf, wb;
+    if (st.packed) {
+        wf.assign(st.npp, -1);
+        wb.assign(st.npp, -1);
+        auto rank = [&](int io, int jo, int ko) {
+            const int t = io + jo + ko;
+            return tpos[(size_t)t * st.ni + io] + jo - pst[t];
+        };
+        const int pz = st.maxlp, px = st.maxlp + st.fs;   // ghost offsets from the plane
+        for (int p = 0; p < st.npp; ++p) {
+            if (pq[p] < 0) continue;
+            const int io = pq[p] & 1023, jo = (pq[p] >> 10) & 1023, ko = pq[p] >> 20;
+            const int fj = jo > 0 ? st.fs + rank(io, jo - 1, ko) : ko + io * st.nk;
+            const int fk = ko > 0 ? rank(io, jo, ko - 1) : pz + jo + io * st.nj;
+            const int fi = io > 0 ? rank(io - 1, jo, ko) : px + ko + jo * st.nk;
+            const int bj = jo < st.nj - 1 ? st.fs + rank(io, jo + 1, ko) : ko + io * st.nk;
+            const int bk = ko < st.nk - 1 ? rank(io, jo, ko + 1) : pz + jo + io * st.nj;
+            const int bi = io < st.ni - 1 ? rank(io + 1, jo, ko) : px + ko + jo * st.nk;
+            wf[p] = fj | (fk << 10) | (fi << 20);
+            wb[p] = bj | (bk << 10) | (bi << 20);
+        }
+    }
     auto up = [c](int** d, const std::vector<int>& h) -> int {
         MG_CUDA(cudaMalloc(d, h.size() * sizeof(int)));
         MG_CUDA(copy_on(c->stream, *d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -807,6 +1029,10 @@ int sip_init(Ctx* c, SipState& st) {
     if (int rc = up(&st.d_facepos, facepos)) return rc;
     if (int rc = up(&st.d_dscf, dscf)) return rc;
     if (int rc = up(&st.d_dscb, dscb)) return rc;
+    if (st.packed) {
+        if (int rc = up(&st.d_wf, wf)) return rc;
+        if (int rc = up(&st.d_wb, wb)) return rc;
+    }
     MG_CUDA(cudaMalloc(&st.d_rowoff, rowoff.size() * sizeof(short)));
     MG_CUDA(copy_on(c->stream, st.d_rowoff, rowoff.data(), rowoff.size() * sizeof(short),
                        cudaMemcpyHostToDevice));
@@ -850,7 +1076,7 @@ int sip_init(Ctx* c, SipState& st) {
         MG_CUDA(cudaMalloc(&st.a1lo[qq], len[qq] * sizeof(float)));
         MG_CUDA(copy_on(c->stream, st.a1lo[qq], fl.data(), len[qq] * sizeof(float), cudaMemcpyHostToDevice));
     }
-    if (sweep_smem(st) > 48 * 1024) {
+    if (sweep_smem(st) > 48 * 1024 || (st.packed && packed_smem(st) > 48 * 1024)) {
         set_error("mixed form: sweep shared memory above 48 KB");
         return MGLET_ERR_UNSUPPORTED;
     }
@@ -875,6 +1101,13 @@ int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* 
         c->F("SIPLW"), c->F("SIPLS"), c->F("SIPLB"), c->F("SIPLPR"), c->F("SIPUE"), c->F("SIPUN"),
         c->F("SIPUT"), c->F("GSAP"), *cf, *cb, *apx);
     MG_LAUNCHED(c);
+    if (st.packed) {
+        MG_CUDA(cudaMalloc(&st.swf, n * sizeof(float4)));
+        MG_CUDA(cudaMalloc(&st.swb, n * sizeof(float4)));
+        k_sip_records<<<grid, 256, 0, c->stream>>>(st.d_pst, st.nm, st.npp, st.d_wf, st.d_wb, *cf, *cb,
+                                                   st.swf, st.swb);
+        MG_LAUNCHED(c);
+    }
     return 0;
 }
 
@@ -883,7 +1116,8 @@ void sip_release(SipState& st) {
                     (void*)st.d_pq, (void*)st.d_rowoff,
                     (void*)st.d_fnbr, (void*)st.h32, (void*)st.rs[0], (void*)st.rs[1],
                     (void*)st.rs[2], (void*)st.rhs32, (void*)st.rhsl, (void*)st.dph, (void*)st.dpl,
-                    (void*)st.d_facepos, (void*)st.d_dscf, (void*)st.d_dscb, (void*)st.a1[0], (void*)st.a1[1],
+                    (void*)st.d_facepos, (void*)st.d_dscf, (void*)st.d_dscb,
+                    (void*)st.d_wf, (void*)st.d_wb, (void*)st.swf, (void*)st.swb, (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
                     (void*)st.a1lo[4], (void*)st.a1lo[5]})
@@ -929,7 +1163,12 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
     // grids against one rank per thread at four CTAs per SM and deeper
     // register prefetch, both slower)
     const int threads = sweep_threads(st);
-    if (threads <= 256)
+    a.SW = st.swf;
+    if (st.packed && threads <= 256)
+        k_sip_fwd_packed<256, 8, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
+    else if (st.packed)
+        k_sip_fwd_packed<512, 4, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
+    else if (threads <= 256)
         k_sip_fwd<256, 8, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
     else
         k_sip_fwd<512, 4, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
@@ -951,7 +1190,12 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
     // grids against one rank per thread at four CTAs per SM and deeper
     // register prefetch, both slower)
     const int threads = sweep_threads(st);
-    if (threads <= 256)
+    a.SW = st.swb;
+    if (st.packed && threads <= 256)
+        k_sip_bwd_packed<256, 8, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
+    else if (st.packed)
+        k_sip_bwd_packed<512, 4, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
+    else if (threads <= 256)
         k_sip_bwd<256, 8, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
     else
         k_sip_bwd<512, 4, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);

@@ -29,6 +29,13 @@ struct SipState {
     int* d_facepos = nullptr;   // [6][fs] padded position of each face point
     int* d_dscf = nullptr;      // [npp][2] forward / backward sweep neighbour positions
     int* d_dscb = nullptr;
+    // packed sweeps (shapes whose neighbour positions fit one word): the
+    // words, and per class the records {word, three coefficients}
+    bool packed = false;
+    int* d_wf = nullptr;
+    int* d_wb = nullptr;
+    float4* swf = nullptr;      // [ncls][npp]
+    float4* swb = nullptr;
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
