@@ -38,6 +38,7 @@
 // the copies in flight, exits.
 
 #include <algorithm>
+#include <map>
 #include <vector>
 
 #include "internal.h"
@@ -155,6 +156,7 @@ struct FwdArgs {
     const float* CF;            // class blocks: per plane [lw|ls|lb|lpr|ap] x Lp
     const float4* SW;           // packed records {position word, lw, ls, lb} (packed form)
     int* ctl;                   // [0] converged (skip), [2] error flag
+    int rev;                    // walk the grids in reverse block order
 };
 
 __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~(size_t)15; }
@@ -169,8 +171,10 @@ struct PreArgs {
     const float* CF;
     const float *AW, *AE, *AS, *AN, *AB, *AT;   // FP32 1-D coefficients (concatenated)
     const DevGrid* grids;
+    const float4* PR;           // packed pre-pass records (packed form)
     int* ctl;
     int hzero;
+    int rev;                    // walk the grids in reverse block order
 };
 
 // The part of sipiter1 that does not depend on the recurrence: laplacephi of
@@ -187,7 +191,7 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     int* spst = reinterpret_cast<int*>(psm);
     short* ro = reinterpret_cast<short*>(spst + nm + 1);
     float* gh = reinterpret_cast<float*>(psm + stencil_tables_bytes(nm, ni));   // [6][fs]
-    const int g = blockIdx.x;
+    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
     const bool hz = a.hzero != 0;
     const int* fn = a.fnbr + 6 * g;
     for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
@@ -246,6 +250,99 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     if (q < s.npp) PRE[q] = point(q);
 }
 
+// Packed pre-pass, for shapes with npp + 6 fs < 32768: per class three
+// 16-byte records per padded position, {the six neighbour codes as 16-bit
+// pairs (i-1 | i+1, j-1 | j+1, k-1 | k+1), lpr}, {aw, ae, as, an},
+// {ab, at, ap, 0}; a code below npp is a position in the grid's hilf, above
+// it a ghost in shared memory (npp + face * fs + face index).  Padding has
+// a negative first word and gets 0.  The two streams that come from DRAM --
+// the point's own hilf and rhs -- are loaded kAhead iterations ahead into
+// registers, so that each thread keeps several points' DRAM loads in flight
+// (the kernel is bound by DRAM latency, not by its instructions).
+template <int kAhead, int kMinBlocks>
+__global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(16) float gh[];   // [6][fs]
+    const Shape s = a.s;
+    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const bool hz = a.hzero != 0;
+    const int npp = s.npp;
+    if (!hz) gather_hilf_ghosts(gh, s, a.H, a.fnbr + 6 * g);
+    __syncthreads();
+    const long long base = (long long)g * npp;
+    const float* __restrict__ H = a.H + base;
+    const float* __restrict__ RHS = a.RHS + base;
+    float* __restrict__ PRE = a.PRE + base;
+    const float4* __restrict__ P1 = a.PR + (long long)a.gcls[g] * 3 * npp;
+    const float* ghb = gh - npp;
+    const int nt = blockDim.x;
+    float hq[kAhead], rq[kAhead];
+#pragma unroll
+    for (int j = 0; j < kAhead; ++j) {
+        const int q = threadIdx.x + j * nt;
+        hq[j] = (!hz && q < npp) ? __ldcs(H + q) : 0.f;
+        rq[j] = q < npp ? __ldcs(RHS + q) : 0.f;
+    }
+    for (int q = threadIdx.x; q < npp; q += nt) {
+        const float hc = hq[0], rh = rq[0];
+#pragma unroll
+        for (int j = 0; j + 1 < kAhead; ++j) {
+            hq[j] = hq[j + 1];
+            rq[j] = rq[j + 1];
+        }
+        const int qn = q + kAhead * nt;
+        hq[kAhead - 1] = (!hz && qn < npp) ? __ldcs(H + qn) : 0.f;
+        rq[kAhead - 1] = qn < npp ? __ldcs(RHS + qn) : 0.f;
+        const float4 r1 = __ldg(P1 + q);
+        const int w0 = __float_as_int(r1.x);
+        float v = 0.f;
+        if (w0 >= 0) {
+            float lap = 0.f;
+            if (!hz) {
+                const float4 r2 = __ldg(P1 + npp + q), r3 = __ldg(P1 + 2 * npp + q);
+                const int w1 = __float_as_int(r1.y), w2 = __float_as_int(r1.z);
+                auto nbv = [&](int code) -> float { return code < npp ? __ldg(H + code) : ghb[code]; };
+                lap = -r2.x * nbv(w0 & 0xffff) - r2.y * nbv(w0 >> 16) - r2.z * nbv(w1 & 0xffff) -
+                      r2.w * nbv(w1 >> 16) - r3.x * nbv(w2 & 0xffff) - r3.y * nbv(w2 >> 16) - r3.z * hc;
+            }
+            v = (rh + lap) * r1.w;
+        }
+        PRE[q] = v;
+    }
+}
+
+// class pre-pass records (see k_sip_pre_pf) from the shape's codes, the
+// class blocks and the representative grid's FP32 1-D coefficients
+__global__ void k_sip_pre_records(const DevGrid* __restrict__ grids, const int* __restrict__ reps,
+                                  const int* __restrict__ pst, int nm, int npp,
+                                  const int* __restrict__ pq, const int* __restrict__ code,
+                                  const float* __restrict__ CF, const float* __restrict__ AW,
+                                  const float* __restrict__ AE, const float* __restrict__ AS,
+                                  const float* __restrict__ AN, const float* __restrict__ AB,
+                                  const float* __restrict__ AT, float4* PR) {
+    const int cls = blockIdx.y;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= npp) return;
+    float4* P1 = PR + (long long)cls * 3 * npp;
+    const int v = pq[p];
+    if (v < 0) {
+        P1[p] = make_float4(__int_as_float(-1), 0.f, 0.f, 0.f);
+        P1[npp + p] = P1[2 * npp + p] = make_float4(0.f, 0.f, 0.f, 0.f);
+        return;
+    }
+    int m = 0;
+    while (m + 1 <= nm && pst[m + 1] <= p) ++m;
+    const int p0 = pst[m], lp = pst[m + 1] - p0, rk = p - p0;
+    const float* cf = CF + (long long)cls * 5 * npp + 5LL * p0 + rk;   // [lw|ls|lb|lpr|ap]
+    const DevGrid G = grids[reps[cls]];
+    const int io = v & 1023, jo = (v >> 10) & 1023, ko = v >> 20;
+    const int ix = G.ipx + 2 + io, iy = G.ipy + 2 + jo, iz = G.ipz + 2 + ko;
+    P1[p] = make_float4(__int_as_float(code[3 * p]), __int_as_float(code[3 * p + 1]),
+                        __int_as_float(code[3 * p + 2]), cf[3 * lp]);
+    P1[npp + p] = make_float4(AW[ix], AE[ix], AS[iy], AN[iy]);
+    P1[2 * npp + p] = make_float4(AB[iz], AT[iz], cf[4 * lp], 0.f);
+}
+
 struct BwdArgs {
     Shape s;
     const int* fnbr;
@@ -256,6 +353,7 @@ struct BwdArgs {
     const float4* SW;           // packed records {position word, ue, un, ut} (packed form)
     int* ctl;
     int hzero;
+    int rev;                    // walk the grids in reverse block order
 };
 
 // Sweeps.  Shared memory holds the plane starts and nb = [res plane buffer 0
@@ -283,7 +381,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd(FwdArgs a) {
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // [2][mlp] res planes
     float* gr = nb + 2 * mlp;                                         // [3][fs] low res ghosts
-    const int g = blockIdx.x;
+    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
@@ -363,7 +461,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd(BwdArgs a) {
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // [2][mlp] res planes
     float* gr = nb + 2 * mlp;                                         // [3][fs] high res ghosts
-    const int g = blockIdx.x;
+    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float* CB = a.CB + (long long)a.gcls[g] * 3 * s.npp;
@@ -468,7 +566,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd_packed(FwdArgs
     const int rs = (int)packed_region(mlp, fs);
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // two regions
-    const int g = blockIdx.x;
+    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float4* SW = a.SW + (long long)a.gcls[g] * s.npp;
@@ -540,7 +638,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs
     const int rs = (int)packed_region(mlp, fs);
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // two regions
-    const int g = blockIdx.x;
+    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float4* SW = a.SW + (long long)a.gcls[g] * s.npp;
@@ -655,6 +753,7 @@ struct OuterArgs {
     double* gridmax;
     const int* ctl;
     int* ctl_err;               // ctl[2]
+    int rev;                    // walk the grids in reverse block order
 };
 
 // a + b = s + e exactly (Knuth's TwoSum, no order of magnitudes assumed)
@@ -692,7 +791,7 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
     float* gh = H + s.npp;                                                     // [6][fs] its ghosts
     unsigned long long* bar = reinterpret_cast<unsigned long long*>(gh + 6 * fs);
     __shared__ int sok;
-    const int g = blockIdx.x;
+    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
     const long long base = (long long)g * s.npp;
     const int* fn = a.fnbr + 6 * g;
     for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
@@ -863,6 +962,15 @@ Shape shape(const SipState& st) {
     return s;
 }
 
+// Grid order of the next per-grid kernel: consecutive kernels walk the grids
+// in opposite directions, so each starts on the grids whose data the
+// previous one touched last and that are still in L2.
+int next_order(SipState& st) {
+    const int r = st.order;
+    st.order ^= 1;
+    return r;
+}
+
 // two plane ranks per thread; at most 512 threads (planes of <= 1024 points)
 int sweep_threads(const SipState& st) { return (st.maxlp + 63) / 64 * 32; }
 
@@ -1016,6 +1124,27 @@ int sip_init(Ctx* c, SipState& st) {
             wb[p] = bj | (bk << 10) | (bi << 20);
         }
     }
+    // packed pre-pass codes (see k_sip_pre_pf)
+    st.prepk = st.npp + 6 * st.fs < 32768;
+    std::vector<int> pcode;
+    if (st.prepk) {
+        pcode.assign((size_t)3 * st.npp, -1);
+        auto pos = [&](int io, int jo, int ko) { return tpos[(size_t)(io + jo + ko) * st.ni + io] + jo; };
+        const int gb = st.npp;
+        for (int p = 0; p < st.npp; ++p) {
+            if (pq[p] < 0) continue;
+            const int io = pq[p] & 1023, jo = (pq[p] >> 10) & 1023, ko = pq[p] >> 20;
+            const int im = io > 0 ? pos(io - 1, jo, ko) : gb + 0 * st.fs + ko + jo * st.nk;
+            const int ip = io < st.ni - 1 ? pos(io + 1, jo, ko) : gb + 1 * st.fs + ko + jo * st.nk;
+            const int jm = jo > 0 ? pos(io, jo - 1, ko) : gb + 2 * st.fs + ko + io * st.nk;
+            const int jp = jo < st.nj - 1 ? pos(io, jo + 1, ko) : gb + 3 * st.fs + ko + io * st.nk;
+            const int km = ko > 0 ? pos(io, jo, ko - 1) : gb + 4 * st.fs + jo + io * st.nj;
+            const int kp = ko < st.nk - 1 ? pos(io, jo, ko + 1) : gb + 5 * st.fs + jo + io * st.nj;
+            pcode[3 * (size_t)p] = im | (ip << 16);
+            pcode[3 * (size_t)p + 1] = jm | (jp << 16);
+            pcode[3 * (size_t)p + 2] = km | (kp << 16);
+        }
+    }
     auto up = [c](int** d, const std::vector<int>& h) -> int {
         MG_CUDA(cudaMalloc(d, h.size() * sizeof(int)));
         MG_CUDA(copy_on(c->stream, *d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
@@ -1033,6 +1162,8 @@ int sip_init(Ctx* c, SipState& st) {
         if (int rc = up(&st.d_wf, wf)) return rc;
         if (int rc = up(&st.d_wb, wb)) return rc;
     }
+    if (st.prepk)
+        if (int rc = up(&st.d_pcode, pcode)) return rc;
     MG_CUDA(cudaMalloc(&st.d_rowoff, rowoff.size() * sizeof(short)));
     MG_CUDA(copy_on(c->stream, st.d_rowoff, rowoff.data(), rowoff.size() * sizeof(short),
                        cudaMemcpyHostToDevice));
@@ -1108,6 +1239,13 @@ int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* 
                                                    st.swf, st.swb);
         MG_LAUNCHED(c);
     }
+    if (st.prepk) {
+        MG_CUDA(cudaMalloc(&st.spr, 3 * n * sizeof(float4)));
+        k_sip_pre_records<<<grid, 256, 0, c->stream>>>(
+            c->d_grids, d_reps, st.d_pst, st.nm, st.npp, st.d_pq, st.d_pcode, *cf, st.a1[0], st.a1[1],
+            st.a1[2], st.a1[3], st.a1[4], st.a1[5], st.spr);
+        MG_LAUNCHED(c);
+    }
     return 0;
 }
 
@@ -1117,7 +1255,8 @@ void sip_release(SipState& st) {
                     (void*)st.d_fnbr, (void*)st.h32, (void*)st.rs[0], (void*)st.rs[1],
                     (void*)st.rs[2], (void*)st.rhs32, (void*)st.rhsl, (void*)st.dph, (void*)st.dpl,
                     (void*)st.d_facepos, (void*)st.d_dscf, (void*)st.d_dscb,
-                    (void*)st.d_wf, (void*)st.d_wb, (void*)st.swf, (void*)st.swb, (void*)st.a1[0], (void*)st.a1[1],
+                    (void*)st.d_wf, (void*)st.d_wb, (void*)st.swf, (void*)st.swb,
+                    (void*)st.d_pcode, (void*)st.spr, (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
                     (void*)st.a1lo[4], (void*)st.a1lo[5]})
@@ -1148,7 +1287,14 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
         p.grids = c->d_grids;
         p.ctl = ctl;
         p.hzero = hzero ? 1 : 0;
-        k_sip_pre<<<c->ngrid, 512, pre_smem(st), c->stream>>>(p);
+        p.PR = st.spr;
+        p.rev = next_order(st);
+        // two points' DRAM loads ahead at three CTAs per SM (measured on 24^3
+        // grids against one or three points ahead at four or two CTAs)
+        if (st.prepk)
+            k_sip_pre_pf<2, 3><<<c->ngrid, 512, (size_t)6 * st.fs * 4, c->stream>>>(p);
+        else
+            k_sip_pre<<<c->ngrid, 512, pre_smem(st), c->stream>>>(p);
         MG_LAUNCHED(c);
     }
     ProfScope ps_(c, "mx_sip_fwd");
@@ -1164,6 +1310,7 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
     // register prefetch, both slower)
     const int threads = sweep_threads(st);
     a.SW = st.swf;
+    a.rev = next_order(st);
     if (st.packed && threads <= 256)
         k_sip_fwd_packed<256, 8, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
     else if (st.packed)
@@ -1191,6 +1338,7 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
     // register prefetch, both slower)
     const int threads = sweep_threads(st);
     a.SW = st.swb;
+    a.rev = next_order(st);
     if (st.packed && threads <= 256)
         k_sip_bwd_packed<256, 8, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
     else if (st.packed)
@@ -1218,6 +1366,7 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     a.gridmax = c->d_gridred;
     a.ctl = ctl;
     a.ctl_err = const_cast<int*>(ctl) + 2;
+    a.rev = next_order(st);
     k_sip_outer<<<c->ngrid, 512, stencil_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;

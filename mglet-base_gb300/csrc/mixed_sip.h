@@ -36,6 +36,12 @@ struct SipState {
     int* d_wb = nullptr;
     float4* swf = nullptr;      // [ncls][npp]
     float4* swb = nullptr;
+    // packed pre-pass (npp + 6 fs < 32768): neighbour codes [npp][3] and per
+    // class the records [ncls][3][npp]
+    bool prepk = false;
+    int* d_pcode = nullptr;
+    float4* spr = nullptr;
+    int order = 0;              // direction of the next per-grid kernel (next_order)
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
