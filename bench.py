@@ -66,11 +66,11 @@ MIXED_BYTES = {
 # the bench case by the number of cells; on 1024 grids part of the working set
 # stays in L2, so these are lower bounds for the full-size launch.
 NCU_TRAFFIC_PER_CELL = {
-    "mx_sip_fwd": 79.4e6 / (1024 * 13824),
-    "mx_sip_bwd": 144.4e6 / (1024 * 13824),
-    "mx_sip_pre": 161.3e6 / (1024 * 13824),
-    "mx_outer": 469.9e6 / (1024 * 13824),
-    "mx_flux": 1383.5e6 / (1024 * 13824),
+    "mx_sip_fwd": 94.6e6 / (1024 * 13824),
+    "mx_sip_bwd": 127.6e6 / (1024 * 13824),
+    "mx_sip_pre": 140.7e6 / (1024 * 13824),
+    "mx_outer": 476.1e6 / (1024 * 13824),
+    "mx_flux": 1540.8e6 / (1024 * 13824),
 }
 
 
@@ -81,8 +81,9 @@ def kernel_bytes(name, case, ninner):
     over it; the backward sweep reads res and hilf and writes hilf; the outer
     step reads hilf and the float-float residual and correction and writes
     both back.  The first inner iteration of an outer iteration starts from
-    hilf = 0 and reads no hilf.  Face buffers: six written, three read per
-    grid and sweep, six hilf faces read by the pre-pass and the outer step.
+    hilf = 0 and reads no hilf.  Ghost faces: three res faces read per grid
+    and sweep, six hilf faces read by the pre-pass and the outer step, all
+    gathered from the neighbours' arrays.
     Class coefficients, shared by all grids of a class and served from L2,
     are not counted."""
     cells = case.ncells
@@ -92,9 +93,9 @@ def kernel_bytes(name, case, ninner):
     if name == "mx_sip_pre":
         return cells * (12 - 4 * hz) + face * 6 * (1 - hz)
     if name == "mx_sip_fwd":
-        return cells * 8 + face * (6 + 3)
+        return cells * 8 + face * 3
     if name == "mx_sip_bwd":
-        return cells * (12 - 4 * hz) + face * (6 + 3)
+        return cells * (12 - 4 * hz) + face * 3
     if name == "mx_outer":
         return cells * (4 + 4 * 4 + 4 * 4) + face * 6
     per = MIXED_BYTES.get(name, PLAIN_BYTES.get(name))

@@ -202,7 +202,7 @@ int enqueue_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) {
 int check_device_flag(Ctx* c) {
     MixedState* m = c->mx;
     if (m->h_ctl[2] != 0) {
-        set_error("mixed form: a wavefront kernel timed out waiting for its TMA copies");
+        set_error("mixed form: the outer step timed out waiting for its bulk copies");
         return MGLET_ERR_CUDA;
     }
     return 0;
