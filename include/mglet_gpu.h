@@ -202,11 +202,12 @@ int mglet_gpu_laplacephi(mglet_ctx* ctx, const char* res, const char* phi);
 int mglet_gpu_mgpoisl(mglet_ctx* ctx, double dt, int32_t ittot, int32_t irk,
                       mglet_stage_stats* stats);
 /* bound_flow%bound(ilevel, u, v, w, p) (src/core/bound_mod.F90:36-76 over
- * src/flow/bound_flow_mod.F90:23-730): FIX, OP1, NOS and SLI faces of every
- * grid, faces 1..6 in order, on the device fields U, V, W, P; ilevel <= 0
- * means all levels.  CON/CO1 faces are left to connect. */
+ * src/flow/bound_flow_mod.F90:23-730): FIX, OP1, NOS, SLI and PAR faces of the
+ * grids of level ilevel (<= 0: every level), faces 1..6 in order, on the
+ * device fields U, V, W, P.  CON/CO1 faces are left to connect; PAR faces
+ * take their values from the U, V, W buffers that mglet_gpu_parent fills. */
 int mglet_gpu_bound_flow(mglet_ctx* ctx, int32_t ilevel);
-/* Boundary buffer of U, V or W on face iface (1..6) of grid igrid (1-based),
+/* Boundary buffer of a field on face iface (1..6) of grid igrid (1-based),
  * the plane field_t%get_buffer(buf, igrid, iface) returns
  * (src/core/field_t/realfield_mod.F90:430-503): (kk,jj) for faces 1-2,
  * (kk,ii) for 3-4, (jj,ii) for 5-6, first index fastest; n its size.  FIX
@@ -218,6 +219,52 @@ int mglet_gpu_set_buffer(mglet_ctx* ctx, const char* name, int32_t igrid, int32_
  * (get_bcprms with nreal = 1, src/flow/bound_flow_mod.F90:226-236); faces
  * without one use pinf = 0. */
 int mglet_gpu_set_bc_real(mglet_ctx* ctx, int32_t igrid, int32_t iface, double value);
+/* Reads a boundary buffer back (same plane layout as mglet_gpu_set_buffer). */
+int mglet_gpu_get_buffer(mglet_ctx* ctx, const char* name, int32_t igrid, int32_t iface,
+                         double* host, int64_t n);
+
+/* ---- Grid hierarchies (more than one level, PAR faces) -------------------
+ * A context may hold several levels with PAR (code 8) faces; these
+ * module-level drop-ins then run on it, level by level as the reference
+ * calls them.  mglet_gpu_timeintegrate_flow and mglet_gpu_mgpoisl refuse
+ * such contexts (MGLET_ERR_UNSUPPORTED): the multi-level schedule of the
+ * stage and tstle4_par are not part of this library.
+ *
+ * gridinfo%iparent and i/j/kposition (src/core/grids_mod.F90:768-781):
+ * iparent[g] the 1-based parent of grid g+1 (0 = none, one level coarser),
+ * position[3g..3g+2] = iposition, jposition, kposition, the parent's
+ * 1-based cell index where the fine grid starts.  Required before parent,
+ * ftoc and ctof. */
+int mglet_gpu_set_hierarchy(mglet_ctx* ctx, const int32_t* iparent, const int32_t* position);
+/* parent(ilevel, v1, v2, v3, s1, s2, s3, normal) (src/ib/parent/parent_mod.F90:16,
+ * parent1_mod.F90:24-584): for every PAR face of the grids of level ilevel the
+ * parent's boundary slab, prolonged onto the fine face (piecewise constant;
+ * along a staggered direction the first fine point averages two coarse
+ * ones), into the field's boundary buffer.  v1..v3 (all or none) are the
+ * velocity components staggered along x, y, z; with normal only the
+ * face-normal one; s1..s3 scalars; NULL for absent. */
+int mglet_gpu_parent(mglet_ctx* ctx, int32_t ilevel, const char* v1, const char* v2,
+                     const char* v3, const char* s1, const char* s2, const char* s3,
+                     int32_t normal);
+/* ftoc(ilevel, ff, fc, flag) (src/ib/ftoc_mod.F90:39-60,581-626 with the no-IB
+ * restriction src/ib/noib_restrict_mod.F90:126-298): the grids of level
+ * ilevel restricted into their parents -- face-area means for U, V, W,
+ * volume means for P, R, S, T.  ff and fc may be the same field. */
+int mglet_gpu_ftoc(mglet_ctx* ctx, int32_t ilevel, const char* ff, const char* fc, char flag);
+/* ftoc(ilevel, v1, v2, v3, s1, s2, s3) (src/ib/ftoc_mod.F90:64-85): flags U, V,
+ * W for v1..v3 and P for the scalars, each field into itself. */
+int mglet_gpu_ftoc_multiple(mglet_ctx* ctx, int32_t ilevel, const char* v1, const char* v2,
+                            const char* v3, const char* s1, const char* s2, const char* s3);
+/* ctof(ilevel, ff, fc) (src/ib/ctof/ctof_mod.F90:16-56, ctof1_mod.F90:167-331):
+ * every point of the grids of level ilevel, ghosts included, takes the
+ * value of the parent cell it lies in; nothing on the coarsest level. */
+int mglet_gpu_ctof(mglet_ctx* ctx, int32_t ilevel, const char* ff, const char* fc);
+/* bound_pressure(ilevel, dp, bp) (src/flow/bound_pressure_mod.F90:106-609):
+ * the ghost plane of dp on every PAR face of the grids of level ilevel from
+ * the field's boundary buffer (mglet_gpu_parent with s1 = dp) corrected by
+ * the fine mean next to the face; with_bp selects the BP-weighted form
+ * (the reference passes bp for the ghost-cell IB only). */
+int mglet_gpu_bound_pressure(mglet_ctx* ctx, int32_t ilevel, const char* dp, int32_t with_bp);
 /* ---- Ghost-cell immersed boundary (ib%type = "GHOSTCELL") -------------------
  * Stencil lists of grid igrid (1-based) in the formats of
  * gc_flowstencils_mod.F90:37-100 (what the reference reads from

@@ -393,7 +393,20 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
     return 0;
 }
 
+// The stage driver and the pressure solve are built for one grid level
+// without PAR faces (the multi-level schedule of mgpoisl and tstle4_par are
+// not part of this library); hierarchies use the level operators.
+int single_level_stage(Ctx* c) {
+    if (c->minlevel != c->maxlevel)
+        return fail(MGLET_ERR_UNSUPPORTED, "the multi-level stage is not built; use the level operators");
+    for (int f = 0; f < 6; ++f)
+        if (!c->pgrids[f].empty())
+            return fail(MGLET_ERR_UNSUPPORTED, "PAR faces need the multi-level stage, which is not built");
+    return 0;
+}
+
 int mgpoisl(Ctx* c, double dt, mglet_stage_stats* st) {
+    if (int rc = single_level_stage(c)) return rc;
     if (c->prm.form == MGLET_FORM_MIXED) return mixed_mgpoisl(c, dt, st);
     return mgpoisl_plain(c, dt, st);
 }
@@ -439,6 +452,7 @@ static int stage_plain(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk,
 }
 
 int timeintegrate(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st) {
+    if (int rc = single_level_stage(c)) return rc;
     if (c->prm.form == MGLET_FORM_MIXED) return mixed_stage(c, dt, irk, rk, st);
     return stage_plain(c, dt, irk, rk, st);
 }
@@ -574,9 +588,9 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
             G.bc[f] = d->bctype[6 * g + f];
             const int t = G.bc[f];
             if (!(coupled(t) || t == MGLET_BC_FIX || t == MGLET_BC_OP1 || t == MGLET_BC_NOS ||
-                  t == MGLET_BC_SLI))
+                  t == MGLET_BC_SLI || t == MGLET_BC_PAR))
                 return bail(fail(MGLET_ERR_UNSUPPORTED,
-                                 "create: faces must be CON, CO1, FIX, OP1, NOS or SLI"));
+                                 "create: faces must be CON, CO1, FIX, OP1, NOS, SLI or PAR"));
         }
         for (int s = 1; s <= 26; ++s) {
             const int nb = d->nbrgrid[26 * g + s - 1];
@@ -594,8 +608,11 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
         G.cls = (int)(it - shapes.begin());
         if (it == shapes.end()) shapes.push_back(key);
     }
-    if (c->minlevel != c->maxlevel)
-        return bail(fail(MGLET_ERR_UNSUPPORTED, "create: multi-level hierarchies are not supported"));
+    // hierarchies: the level operators (parent, ftoc, ctof, bound_pressure,
+    // bound_flow on PAR faces) and every per-level module procedure work;
+    // the stage driver and mgpoisl refuse them (single_level_stage)
+    if (c->minlevel != c->maxlevel && prm->form == MGLET_FORM_MIXED)
+        return bail(fail(MGLET_ERR_UNSUPPORTED, "create: the mixed form runs one grid level"));
     c->uniform = shapes.size() == 1;
     c->idim3d = o3; c->idimx = ox; c->idimy = oy; c->idimz = oz;
     MG_CUDA(cudaMalloc(&c->d_grids, c->ngrid * sizeof(DevGrid)));
@@ -640,6 +657,7 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     if (int rc = fill(c, c->F("BP"), 1.0)) return bail(rc);
     build_connection_table(c);
     if (int rc = bound_init(c)) return bail(rc);
+    if (int rc = level_init(c)) return bail(rc);
     if (int rc = launch_giteig(c)) return bail(rc);
     MG_CUDA(cudaStreamSynchronize(c->stream));
     int rc = prm->psolver == MGLET_PSOLVER_CLASSIC ? launch_sip_lu_classic(c) : launch_sip_lu_hp(c);
@@ -680,6 +698,10 @@ int mglet_gpu_destroy(mglet_ctx* c) {
                     (void*)c->gcd.poldsol, (void*)c->gcd.poldsolvel})
         cudaFree(p);
     for (int* b : c->d_bgrids) cudaFree(b);
+    for (int* b : c->d_pgrids) cudaFree(b);
+    for (auto& kv : c->d_children) cudaFree(kv.second);
+    for (auto& kv : c->fbuf) cudaFree(kv.second);
+    cudaFree(c->d_hier);
     cudaFree(c->d_gridred);
     cudaFree(c->d_scalar);
     if (c->h_scalar) cudaFreeHost(c->h_scalar);
@@ -792,10 +814,86 @@ int mglet_gpu_mgpoisl(mglet_ctx* c, double dt, int32_t ittot, int32_t irk, mglet
 }
 
 int mglet_gpu_bound_flow(mglet_ctx* c, int32_t ilevel) {
-    (void)ilevel;   // one level
     if (!c) return fail(MGLET_ERR_ARG, "bound_flow: null context");
     cudaSetDevice(c->device);
-    return launch_bound_flow(c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
+    return launch_bound_flow(c, c->F("U"), c->F("V"), c->F("W"), c->F("P"), ilevel);
+}
+
+int mglet_gpu_set_hierarchy(mglet_ctx* c, const int32_t* iparent, const int32_t* position) {
+    if (!c || !iparent || !position) return fail(MGLET_ERR_ARG, "set_hierarchy: null argument");
+    cudaSetDevice(c->device);
+    return set_hierarchy(c, iparent, position);
+}
+
+int mglet_gpu_parent(mglet_ctx* c, int32_t ilevel, const char* v1, const char* v2, const char* v3,
+                     const char* s1, const char* s2, const char* s3, int32_t normal) {
+    if (!c) return fail(MGLET_ERR_ARG, "parent: null context");
+    if ((v1 != nullptr) != (v2 != nullptr) || (v1 != nullptr) != (v3 != nullptr))
+        return fail(MGLET_ERR_ARG, "parent: give all three vector components or none");
+    const char* const v[3] = {v1, v2, v3};
+    const char* const s[3] = {s1, s2, s3};
+    for (const char* n : {v1, v2, v3, s1, s2, s3})
+        if (n && !field_ptr(c, n)) return fail(MGLET_ERR_NAME, std::string("parent: unknown field ") + n);
+    cudaSetDevice(c->device);
+    return launch_parent(c, ilevel, v, s, normal != 0);
+}
+
+int mglet_gpu_ftoc(mglet_ctx* c, int32_t ilevel, const char* ff, const char* fc, char flag) {
+    if (!c) return fail(MGLET_ERR_ARG, "ftoc: null context");
+    double *f = field_ptr(c, ff), *g = field_ptr(c, fc);
+    if (!f || !g) return fail(MGLET_ERR_NAME, "ftoc: unknown field");
+    if (!flag || !std::strchr("UVWPRST", flag))
+        return fail(MGLET_ERR_ARG, "ftoc: flag is one of U V W P R S T");
+    cudaSetDevice(c->device);
+    return launch_ftoc(c, ilevel, f, g, flag);
+}
+
+int mglet_gpu_ftoc_multiple(mglet_ctx* c, int32_t ilevel, const char* v1, const char* v2,
+                            const char* v3, const char* s1, const char* s2, const char* s3) {
+    if (!c) return fail(MGLET_ERR_ARG, "ftoc: null context");
+    const char* n[6] = {v1, v2, v3, s1, s2, s3};
+    const char fl[6] = {'U', 'V', 'W', 'P', 'P', 'P'};
+    for (int q = 0; q < 6; ++q)
+        if (n[q] && !field_ptr(c, n[q])) return fail(MGLET_ERR_NAME, "ftoc: unknown field");
+    cudaSetDevice(c->device);
+    for (int q = 0; q < 6; ++q)
+        if (n[q])
+            if (int rc = launch_ftoc(c, ilevel, field_ptr(c, n[q]), field_ptr(c, n[q]), fl[q])) return rc;
+    return 0;
+}
+
+int mglet_gpu_ctof(mglet_ctx* c, int32_t ilevel, const char* ff, const char* fc) {
+    if (!c) return fail(MGLET_ERR_ARG, "ctof: null context");
+    double *f = field_ptr(c, ff), *g = field_ptr(c, fc);
+    if (!f || !g) return fail(MGLET_ERR_NAME, "ctof: unknown field");
+    cudaSetDevice(c->device);
+    return launch_ctof(c, ilevel, f, g);
+}
+
+int mglet_gpu_bound_pressure(mglet_ctx* c, int32_t ilevel, const char* dp, int32_t with_bp) {
+    if (!c) return fail(MGLET_ERR_ARG, "bound_pressure: null context");
+    double* p = field_ptr(c, dp);
+    if (!p) return fail(MGLET_ERR_NAME, "bound_pressure: unknown field");
+    cudaSetDevice(c->device);
+    double* b = field_buffer(c, dp);
+    if (!b) return fail(MGLET_ERR_CUDA, "bound_pressure: buffer allocation");
+    return launch_bound_pressure(c, ilevel, p, b, with_bp != 0);
+}
+
+int mglet_gpu_get_buffer(mglet_ctx* c, const char* name, int32_t igrid, int32_t iface, double* host,
+                         int64_t n) {
+    if (!c || !name || !host || igrid < 1 || igrid > c->ngrid || iface < 1 || iface > 6)
+        return fail(MGLET_ERR_ARG, "get_buffer: bad arguments");
+    const DevGrid& G = c->grids[igrid - 1];
+    const long long sz[3] = {(long long)G.kk * G.jj, (long long)G.kk * G.ii, (long long)G.jj * G.ii};
+    if (n != sz[(iface - 1) / 2]) return fail(MGLET_ERR_SIZE, "get_buffer: wrong plane size");
+    if (!field_ptr(c, name)) return fail(MGLET_ERR_NAME, "get_buffer: unknown field");
+    cudaSetDevice(c->device);
+    double* b = field_buffer(c, name);
+    if (!b) return fail(MGLET_ERR_CUDA, "get_buffer: buffer allocation");
+    MG_CUDA(copy_on(c->stream, host, b + c->bface[6 * (igrid - 1) + iface - 1].off,
+                    (size_t)n * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
 }
 
 int mglet_gpu_set_buffer(mglet_ctx* c, const char* name, int32_t igrid, int32_t iface,
@@ -805,13 +903,11 @@ int mglet_gpu_set_buffer(mglet_ctx* c, const char* name, int32_t igrid, int32_t 
     const DevGrid& G = c->grids[igrid - 1];
     const long long sz[3] = {(long long)G.kk * G.jj, (long long)G.kk * G.ii, (long long)G.jj * G.ii};
     if (n != sz[(iface - 1) / 2]) return fail(MGLET_ERR_SIZE, "set_buffer: wrong plane size");
-    int q = -1;
-    if (!std::strcmp(name, "U")) q = 0;
-    else if (!std::strcmp(name, "V")) q = 1;
-    else if (!std::strcmp(name, "W")) q = 2;
-    if (q < 0) return fail(MGLET_ERR_NAME, "set_buffer: buffers exist for U, V, W");
+    if (!field_ptr(c, name)) return fail(MGLET_ERR_NAME, "set_buffer: unknown field");
     cudaSetDevice(c->device);
-    MG_CUDA(copy_on(c->stream, c->d_buf[q] + c->bface[6 * (igrid - 1) + iface - 1].off, host,
+    double* b = field_buffer(c, name);
+    if (!b) return fail(MGLET_ERR_CUDA, "set_buffer: buffer allocation");
+    MG_CUDA(copy_on(c->stream, b + c->bface[6 * (igrid - 1) + iface - 1].off, host,
                     (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
     return 0;
 }

@@ -136,6 +136,18 @@ struct Ctx {
     int ibtype = 0;
     std::vector<GcHostList> gch;
     GcDev gcd;
+    // grid hierarchy (gridinfo%iparent, i/j/kposition): per grid {parent
+    // 0-based or -1, iposition, jposition, kposition}; per level the grids
+    // with a parent (ftoc / ctof) and per level and face the grids with a
+    // PAR face there (parent, bound_flow, bound_pressure); boundary buffers
+    // of fields other than U, V, W, allocated on first use
+    std::vector<int4> hier;
+    int4* d_hier = nullptr;
+    std::map<int, std::vector<int>> children;
+    std::map<int, int*> d_children;
+    std::vector<int> pgrids[6];
+    int* d_pgrids[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    std::map<std::string, double*> fbuf;
     long long launches = 0;
     bool prof = false;
     std::map<std::string, ProfEntry> profd;
@@ -213,8 +225,18 @@ int launch_accumulate(Ctx* c, double* dp, double* hilf);
 int launch_mgpcorr(Ctx* c, double* u, double* v, double* w, double* p, const double* dp,
                    double rfak);
 int launch_itinfo(Ctx* c, double dt);
-// bound_flow%bound on U, V, W and (unless null) P: faces 1..6 in order
-int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p);
+// bound_flow%bound on U, V, W and (unless null) P: faces 1..6 in order, the
+// grids of ilevel (0: all levels)
+int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p, int ilevel = 0);
+// multi-level operators (plain_level.cu)
+int level_init(Ctx* c);                      // PAR face lists (create)
+int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos);
+double* field_buffer(Ctx* c, const std::string& name);   // boundary buffers of a field
+int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w);
+int launch_parent(Ctx* c, int ilevel, const char* const v[3], const char* const s[3], bool normal);
+int launch_ftoc(Ctx* c, int ilevel, const double* ff, double* fc, char flag);
+int launch_ctof(Ctx* c, int ilevel, double* ff, const double* fc);
+int launch_bound_pressure(Ctx* c, int ilevel, double* p, const double* buf, bool withbp);
 // boundary buffers and face table (create)
 int bound_init(Ctx* c);
 // 3-D FP64 field of idim3d points, zeroed (api.cu)

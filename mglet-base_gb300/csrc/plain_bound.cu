@@ -1,4 +1,5 @@
-// plain_bound.cu -- bound_flow for FIX, OP1, NOS and SLI faces, FP64.
+// plain_bound.cu -- bound_flow for FIX, OP1, NOS and SLI faces, FP64 (PAR
+// faces: plain_level.cu).
 //
 // bound_flow_mod.F90 bfront (:23-256), bright (:259-494) and bbottom
 // (:497-730), dispatched as bound_t%bound does (src/core/bound_mod.F90:36-76):
@@ -57,6 +58,7 @@ struct BoundArgs {
     const double *ub, *vb, *wb;
     double *u, *v, *w, *p;
     int iface;
+    int ilevel;                 // 0: all levels
     double rho;
 };
 
@@ -66,6 +68,7 @@ struct BoundArgs {
 __global__ void k_bound_vel(BoundArgs a) {
     const int g = a.list[blockIdx.y];
     const DevGrid G = a.grids[g];
+    if (a.ilevel && G.level != a.ilevel) return;
     const int typ = G.bc[a.iface - 1];
     const Face f = make_face(G, a.iface);
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -116,6 +119,7 @@ __global__ void k_bound_vel(BoundArgs a) {
 __global__ void k_bound_p(BoundArgs a) {
     const int g = a.list[blockIdx.y];
     const DevGrid G = a.grids[g];
+    if (a.ilevel && G.level != a.ilevel) return;
     const int typ = G.bc[a.iface - 1];
     const Face f = make_face(G, a.iface);
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -178,9 +182,12 @@ int bound_init(Ctx* c) {
     return 0;
 }
 
-int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p) {
+int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p, int ilevel) {
     ProfScope ps_(c, "bound_flow");
     for (int f = 0; f < 6; ++f) {
+        // PAR faces (plain_level.cu): no pressure, other grids than this
+        // face's FIX/OP1/NOS/SLI ones, so the order within a face is free
+        if (int rc = launch_bound_par(c, f + 1, ilevel, u, v, w)) return rc;
         if (c->bgrids[f].empty()) continue;
         int maxq = 0;
         for (int g : c->bgrids[f]) {
@@ -195,6 +202,7 @@ int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p) {
         a.ub = c->d_buf[0]; a.vb = c->d_buf[1]; a.wb = c->d_buf[2];
         a.u = u; a.v = v; a.w = w; a.p = p;
         a.iface = f + 1;
+        a.ilevel = ilevel;
         a.rho = c->prm.rho;
         const dim3 grid((maxq + 127) / 128, (unsigned)c->bgrids[f].size());
         k_bound_vel<<<grid, 128, 0, c->stream>>>(a);

@@ -1,0 +1,607 @@
+// plain_level.cu -- the inter-level operators of a grid hierarchy, FP64.
+//
+// parent (src/ib/parent/parent1_mod.F90 with parent_core_mod.F90): the PAR
+// face buffers of fine grids prolonged from their parents' boundary slabs;
+// the PAR branch of bound_flow (src/flow/bound_flow_mod.F90:139-256,
+// 377-494, 613-730); bound_pressure (src/flow/bound_pressure_mod.F90:106-609);
+// ftoc with the no-IB restriction (src/ib/ftoc_mod.F90:581-626,
+// src/ib/noib_restrict_mod.F90:126-298); ctof (src/ib/ctof/ctof1_mod.F90:
+// 167-331).  On one GPU the reference's MPI messages become direct reads of
+// the other grid's slab; every fine grid, face and point is independent,
+// except that the faces of one grid run in order 1..6 (bound_flow edges).
+// Compiled without FMA contraction: every value matches the CPU
+// restatement bit for bit.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace mg {
+namespace {
+
+// default-kind literal 0.1 of the PAR branches, as a REAL64 build widens it
+constexpr float kPoint1f = 0.1f;
+
+struct FaceIx {
+    int axis, kk, jj;
+    __device__ long long at(int a, int b, int n) const {
+        int k, j, i;
+        if (axis == 0) { k = a; j = b; i = n; }
+        else if (axis == 1) { k = a; j = n; i = b; }
+        else { k = n; j = a; i = b; }
+        return (long long)(i - 1) * kk * jj + (long long)(j - 1) * kk + (k - 1);
+    }
+};
+
+// ---- PAR branch of bound_flow -------------------------------------------
+struct ParArgs {
+    const DevGrid* grids;
+    const int* list;            // grids with a PAR face iface
+    const BFace* bface;
+    const double *ub, *vb, *wb, *bp;
+    const double *ddx, *ddy, *ddz;
+    double *u, *v, *w;
+    int iface, ilevel;
+};
+
+// One thread per tangential position (a, b): the tangential components, and
+// at odd a, b >= 3 also the 2x2 block of face-normal fine faces.  The two
+// loops of the reference touch disjoint elements, so they share a launch.
+__global__ void k_bound_par(ParArgs A) {
+    const int g = A.list[blockIdx.y];
+    const DevGrid G = A.grids[g];
+    if (A.ilevel && G.level != A.ilevel) return;
+    const int axis = (A.iface - 1) / 2;
+    const bool lo = (A.iface % 2) == 1;
+    const int nn = axis == 0 ? G.ii : (axis == 1 ? G.jj : G.kk);
+    const int n2 = lo ? 2 : nn - 1, n3 = lo ? 3 : nn - 2, n4 = lo ? 4 : nn - 3;
+    const int st2 = lo ? 2 : nn - 2;
+    const int na = axis == 2 ? G.jj : G.kk, nb = axis == 0 ? G.jj : G.ii;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= na * nb) return;
+    const int a = q % na + 1, b = q / na + 1;
+    const FaceIx F{axis, G.kk, G.jj};
+    const long long o = G.ip3;
+    double *u = A.u + o, *v = A.v + o, *w = A.w + o;
+    const double* bp = A.bp + o;
+    const long long bo = A.bface[6 * g + A.iface - 1].off;
+    const double *ub = A.ub + bo, *vb = A.vb + bo, *wb = A.wb + bo;
+    const double* da = (axis == 2 ? A.ddy + G.ipy : A.ddz + G.ipz) - 1;   // 1-based
+    const double* db = (axis == 0 ? A.ddy + G.ipy : A.ddx + G.ipx) - 1;
+    double* vn = axis == 0 ? u : (axis == 1 ? v : w);
+    const double* bn = axis == 0 ? ub : (axis == 1 ? vb : wb);
+    double* t1 = axis == 0 ? v : u;
+    double* t2 = axis == 2 ? v : w;
+    const double* b1 = axis == 0 ? vb : ub;
+    const double* b2 = axis == 2 ? vb : wb;
+    auto bi = [&](int x, int y) -> long long { return (long long)(x - 1) + (long long)(y - 1) * na; };
+    if (a >= 2 && a <= na - 1 && b >= 2 && b <= nb - 1) {
+        const double s1 = bp[F.at(a, b, n2)] * bp[F.at(a, b + 1, n2)];
+        const double s2 = bp[F.at(a, b, n2)] * bp[F.at(a + 1, b, n2)];
+        t1[F.at(a, b, n2)] = (b1[bi(a, b)] - 0.5 * (t1[F.at(a, b, n3)] - t1[F.at(a, b, n4)])) * s1 +
+                             (1.0 - s1) * t1[F.at(a, b, n2)];
+        // the y faces take this slope from the ghost plane (bright)
+        const double slope2 = axis == 1 ? (t2[F.at(a, b, n2)] - t2[F.at(a, b, n4)])
+                                        : (t2[F.at(a, b, n3)] - t2[F.at(a, b, n4)]);
+        t2[F.at(a, b, n2)] = (b2[bi(a, b)] - 0.5 * slope2) * s2 + (1.0 - s2) * t2[F.at(a, b, n2)];
+    }
+    if (a < 3 || a > na - 2 || b < 3 || b > nb - 2 || ((a - 3) & 1) || ((b - 3) & 1)) return;
+    const double sbn = bp[F.at(a, b, n2)];
+    const int fa[4] = {a, a, a + 1, a + 1}, fb[4] = {b, b + 1, b, b + 1};
+    double sb[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const int x = fa[k], y = fb[k];
+        if (sbn > 0.5)
+            sb[k] = bp[F.at(x, y, n2)] * bp[F.at(x, y, n3)];
+        else
+            sb[k] = fmin(bp[F.at(x, y, n3)] + bp[F.at(x, y, n2)] + bp[F.at(x, y, n4)] +
+                             bp[F.at(x, y - 1, n3)] + bp[F.at(x, y + 1, n3)] + bp[F.at(x - 1, y, n3)] +
+                             bp[F.at(x + 1, y, n3)],
+                         1.0);
+    }
+    // x faces multiply by the b spacing first, y and z faces by the a spacing
+    const double area = axis == 0 ? (db[b] + db[b + 1]) * (da[a] + da[a + 1])
+                                  : (da[a] + da[a + 1]) * (db[b] + db[b + 1]);
+    double fak;
+    if (axis == 0)
+        fak = 1.0 / area * (sb[0] * db[b] * da[a] + sb[1] * db[b + 1] * da[a] + sb[2] * db[b] * da[a + 1] +
+                            sb[3] * db[b + 1] * da[a + 1]);
+    else
+        fak = 1.0 / area * (sb[0] * da[a] * db[b] + sb[1] * da[a] * db[b + 1] + sb[2] * da[a + 1] * db[b] +
+                            sb[3] * da[a + 1] * db[b + 1]);
+    if (fak < (double)kPoint1f) fak = 1.0;
+    fak = 1.0 / fak;
+    double fv[4], f[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        fv[k] = vn[F.at(fa[k], fb[k], st2)];
+        const double x = fv[k] * (1.0 - sb[k]);
+        f[k] = axis == 0 ? x * db[fb[k]] * da[fa[k]] : x * da[fa[k]] * db[fb[k]];
+    }
+    const double fine = (f[0] + f[1] + f[2] + f[3]) / area;
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+        vn[F.at(fa[k], fb[k], st2)] =
+            (bn[bi(fa[k], fb[k])] - fine) * fak * sb[k] + (1.0 - sb[k]) * fv[k] * sbn;
+}
+
+// ---- parent: prolongation into PAR face buffers --------------------------
+struct ParentArgs {
+    const DevGrid* grids;
+    const int4* hier;
+    const int* list;            // grids of the level with a PAR face iface
+    const BFace* bface;
+    const double* fc[6];        // coarse fields of the slots
+    double* buf[6];             // their boundary buffers
+    int comp[6];                // 1..3 vector component (staggered along x/y/z), 0 scalar
+    int iface;
+};
+
+// One thread per element (j, i) of the fine face buffer (jj2d x ii2d):
+// prolong2 of prolong1 of the parent's slab, evaluated in place.
+__global__ void k_parent(ParentArgs A) {
+    const int g = A.list[blockIdx.y];
+    const int slot = blockIdx.z;
+    const DevGrid G = A.grids[g];
+    const int4 H = A.hier[g];
+    const DevGrid P = A.grids[H.x];
+    const int iface = A.iface, comp = A.comp[slot];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    int jj2d, ii2d, st1 = 0, st2 = 0;
+    if (iface <= 2) { ii2d = jj; jj2d = kk; }
+    else if (iface <= 4) { ii2d = ii; jj2d = kk; }
+    else { ii2d = ii; jj2d = jj; }
+    if (iface <= 2) { st2 = comp == 2; st1 = comp == 3; }
+    else if (iface <= 4) { st2 = comp == 1; st1 = comp == 3; }
+    else { st2 = comp == 1; st1 = comp == 2; }
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= jj2d * ii2d) return;
+    const int j = q % jj2d + 1, i = q / jj2d + 1;
+    // the parent slab (parent_core_mod.F90:190-255)
+    int icomp = 0;
+    if ((iface == 1 || iface == 2) && comp == 1) icomp = 1;
+    if ((iface == 3 || iface == 4) && comp == 2) icomp = 2;
+    if ((iface == 5 || iface == 6) && comp == 3) icomp = 3;
+    const int ipos = H.y, jpos = H.z, kpos = H.w;
+    int is = ipos - 2, js = jpos - 2, ks = kpos - 2;
+    if (iface == 1) is = ipos - 1;
+    else if (iface == 2) is = ipos + (ii - 4) / 2 - (icomp == 1 ? 1 : 0);
+    else if (iface == 3) js = jpos - 1;
+    else if (iface == 4) js = jpos + (jj - 4) / 2 - (icomp == 2 ? 1 : 0);
+    else if (iface == 5) ks = kpos - 1;
+    else ks = kpos + (kk - 4) / 2 - (icomp == 3 ? 1 : 0);
+    const double* fc = A.fc[slot] + P.ip3;
+    // in(jc, ic): slab element with first index jc, second ic (1-based)
+    auto in = [&](int jc, int ic) -> double {
+        int kc, jcc, icc;
+        if (iface <= 2) { kc = ks + jc - 1; jcc = js + ic - 1; icc = is; }
+        else if (iface <= 4) { kc = ks + jc - 1; jcc = js; icc = is + ic - 1; }
+        else { kc = ks; jcc = js + jc - 1; icc = is + ic - 1; }
+        return fc[(long long)(icc - 1) * P.kk * P.jj + (long long)(jcc - 1) * P.kk + (kc - 1)];
+    };
+    // prolong1 value tmp(j, ic)
+    auto tmp = [&](int ic) -> double {
+        if (j & 1) {
+            const int jc = 2 + (j - 1) / 2;
+            const double x = in(jc, ic);
+            return st1 ? 0.5 * (x + in(jc - 1, ic)) : x;
+        }
+        return in(2 + (j - 2) / 2, ic);
+    };
+    double out;
+    if (i & 1) {
+        const int ic = 2 + (i - 1) / 2;
+        const double x = tmp(ic);
+        out = st2 ? 0.5 * (x + tmp(ic - 1)) : x;
+    } else {
+        out = tmp(2 + (i - 2) / 2);
+    }
+    A.buf[slot][A.bface[6 * g + iface - 1].off + (long long)(j - 1) + (long long)(i - 1) * jj2d] = out;
+}
+
+// ---- bound_pressure -------------------------------------------------------
+struct BpArgs {
+    const DevGrid* grids;
+    const int* list;
+    const BFace* bface;
+    const double* buf;
+    const double* bp;           // null: the no-BP forms
+    const double *ddx, *ddy, *ddz, *dx, *dy, *dz;
+    double* p;
+    int iface, ilevel;
+};
+
+// One thread per 2x2 block of the face (bfront/bright/bbottom and _bp)
+__global__ void k_bound_pressure(BpArgs A) {
+    const int g = A.list[blockIdx.y];
+    const DevGrid G = A.grids[g];
+    if (G.level != A.ilevel) return;
+    const int axis = (A.iface - 1) / 2;
+    const bool lo = (A.iface % 2) == 1;
+    const int nn = axis == 0 ? G.ii : (axis == 1 ? G.jj : G.kk);
+    const int n2 = lo ? 2 : nn - 1, n3 = lo ? 3 : nn - 2, n4 = lo ? 4 : nn - 3;
+    const int st2 = lo ? 2 : nn - 2;
+    const int nmin = n3 < n4 ? n3 : n4;
+    const int na = axis == 2 ? G.jj : G.kk, nb = axis == 0 ? G.jj : G.ii;
+    const int nba = (na - 4) / 2, nbb = (nb - 4) / 2;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nba * nbb) return;
+    const int a = 3 + 2 * (q % nba), b = 3 + 2 * (q / nba);
+    const FaceIx F{axis, G.kk, G.jj};
+    const long long o = G.ip3;
+    double* p = A.p + o;
+    const double* bp = A.bp ? A.bp + o : nullptr;
+    const double* ddx = A.ddx + G.ipx - 1;
+    const double* ddy = A.ddy + G.ipy - 1;
+    const double* ddz = A.ddz + G.ipz - 1;
+    const double* dn = axis == 0 ? ddx : (axis == 1 ? ddy : ddz);
+    const double* dstag = axis == 0 ? A.dx + G.ipx - 1 : (axis == 1 ? A.dy + G.ipy - 1 : A.dz + G.ipz - 1);
+    const double* da = axis == 2 ? ddy : ddz;
+    const double* db = axis == 0 ? ddy : ddx;
+    const double pbv = A.buf[A.bface[6 * g + A.iface - 1].off + (long long)(a - 1) + (long long)(b - 1) * na];
+    int k, j, i;
+    if (axis == 0) { k = a; j = b; i = nmin; }
+    else if (axis == 1) { k = a; j = nmin; i = b; }
+    else { k = nmin; j = a; i = b; }
+    const int kk = G.kk, jj = G.jj;
+    auto ix = [&](int kx, int jx, int ix_) -> long long {
+        return (long long)(ix_ - 1) * kk * jj + (long long)(jx - 1) * kk + (kx - 1);
+    };
+    // pressureftocone_A / _B
+    double pc, bpc;
+    if (!bp) {
+        bpc = 1.0;
+        double sump = 0.0, sumvol = 0.0;
+        for (int l = 0; l <= 1; ++l)
+            for (int m = 0; m <= 1; ++m)
+                for (int n = 0; n <= 1; ++n) {
+                    const double vol = ddz[k + n] * ddy[j + m] * ddx[i + l];
+                    sump = sump + p[ix(k + n, j + m, i + l)] * vol;
+                    sumvol = sumvol + vol;
+                }
+        pc = sump / sumvol;
+    } else {
+        double sumbp = 0.0;
+        for (int l = 0; l <= 1; ++l)
+            for (int m = 0; m <= 1; ++m)
+                for (int n = 0; n <= 1; ++n) sumbp = sumbp + bp[ix(k + n, j + m, i + l)];
+        bpc = fmin(sumbp, 1.0);
+        if (bpc < 0.5) {
+            pc = 0.0;
+        } else {
+            double sump = 0.0, sumvol = 0.0;
+            for (int l = 0; l <= 1; ++l)
+                for (int m = 0; m <= 1; ++m)
+                    for (int n = 0; n <= 1; ++n) {
+                        const double vol = bp[ix(k + n, j + m, i + l)] * ddz[k + n] * ddy[j + m] * ddx[i + l];
+                        sump = sump + p[ix(k + n, j + m, i + l)] * vol;
+                        sumvol = sumvol + vol;
+                    }
+            pc = sump / sumvol;
+        }
+    }
+    double fak = 1.0;
+    if (bp) {
+        if (bpc < 0.5) pc = pbv;
+        const double s11 = bp[F.at(a, b, n2)] * bp[F.at(a, b, n3)];
+        const double s12 = bp[F.at(a, b + 1, n2)] * bp[F.at(a, b + 1, n3)];
+        const double s13 = bp[F.at(a + 1, b, n2)] * bp[F.at(a + 1, b, n3)];
+        const double s14 = bp[F.at(a + 1, b + 1, n2)] * bp[F.at(a + 1, b + 1, n3)];
+        fak = (s11 * db[b] * da[a] + s12 * db[b + 1] * da[a] + s13 * db[b] * da[a + 1] + s14 * db[b + 1] * da[a + 1]) /
+              ((db[b] + db[b + 1]) * (da[a] + da[a + 1]));
+        if (fak < (double)kPoint1f) fak = 1.0;
+        fak = 1.0 / fak;
+    }
+    // the block's four ghost values all read the interior plane, which
+    // this launch does not write
+    for (int l = 0; l <= 1; ++l)
+        for (int n = 0; n <= 1; ++n) {
+            const long long dst = F.at(a + n, b + l, n2), src = F.at(a + n, b + l, n3);
+            if (bp)
+                p[dst] = p[src] + fak * dstag[st2] / (dn[n3] + dn[n2]) * (pbv - pc);
+            else
+                p[dst] = p[src] + dstag[st2] / (dn[n3] + dn[n2]) * (pbv - pc);
+        }
+}
+
+// ---- ftoc (no-IB restriction) ---------------------------------------------
+struct FtocArgs {
+    const DevGrid* grids;
+    const int4* hier;
+    const int* list;            // fine grids of the level
+    const double* ff;
+    double* fc;
+    const double *ddx, *ddy, *ddz;
+    char flag;                  // U V W, or P for the scalar (volume) mean
+};
+
+__global__ void k_ftoc(FtocArgs A) {
+    const int g = A.list[blockIdx.y];
+    const DevGrid G = A.grids[g];
+    const int4 H = A.hier[g];
+    const DevGrid P = A.grids[H.x];
+    const char f = A.flag;
+    const int is = f == 'U' ? 2 : 3, js = f == 'V' ? 2 : 3, ks = f == 'W' ? 2 : 3;
+    const int ie = G.ii - is, je = G.jj - js, ke = G.kk - ks;
+    const int ni = (ie - is) / 2 + 1, nj = (je - js) / 2 + 1, nk = (ke - ks) / 2 + 1;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= ni * nj * nk) return;
+    const int k = ks + 2 * (q % nk), j = js + 2 * ((q / nk) % nj), i = is + 2 * (q / (nk * nj));
+    const int kk = G.kk, jj = G.jj;
+    const double* fv = A.ff + G.ip3;
+    const double* ddx = A.ddx + G.ipx - 1;
+    const double* ddy = A.ddy + G.ipy - 1;
+    const double* ddz = A.ddz + G.ipz - 1;
+    auto F = [&](int kx, int jx, int ix) -> double {
+        return fv[(long long)(ix - 1) * kk * jj + (long long)(jx - 1) * kk + (kx - 1)];
+    };
+    double val;
+    if (f == 'U') {
+        const double s = F(k, j, i) * ddy[j] * ddz[k] + F(k, j + 1, i) * ddy[j + 1] * ddz[k] +
+                         F(k + 1, j, i) * ddy[j] * ddz[k + 1] + F(k + 1, j + 1, i) * ddy[j + 1] * ddz[k + 1];
+        val = s / ((ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
+    } else if (f == 'V') {
+        const double s = F(k, j, i) * ddx[i] * ddz[k] + F(k, j, i + 1) * ddx[i + 1] * ddz[k] +
+                         F(k + 1, j, i) * ddx[i] * ddz[k + 1] + F(k + 1, j, i + 1) * ddx[i + 1] * ddz[k + 1];
+        val = s / ((ddx[i] + ddx[i + 1]) * (ddz[k] + ddz[k + 1]));
+    } else if (f == 'W') {
+        const double s = F(k, j, i) * ddx[i] * ddy[j] + F(k, j, i + 1) * ddx[i + 1] * ddy[j] +
+                         F(k, j + 1, i) * ddx[i] * ddy[j + 1] + F(k, j + 1, i + 1) * ddx[i + 1] * ddy[j + 1];
+        val = s / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]));
+    } else {
+        const double s = F(k, j, i) * ddz[k] * ddy[j] * ddx[i] + F(k, j, i + 1) * ddz[k] * ddy[j] * ddx[i + 1] +
+                         F(k, j + 1, i) * ddz[k] * ddy[j + 1] * ddx[i] +
+                         F(k, j + 1, i + 1) * ddz[k] * ddy[j + 1] * ddx[i + 1] +
+                         F(k + 1, j, i) * ddz[k + 1] * ddy[j] * ddx[i] +
+                         F(k + 1, j, i + 1) * ddz[k + 1] * ddy[j] * ddx[i + 1] +
+                         F(k + 1, j + 1, i) * ddz[k + 1] * ddy[j + 1] * ddx[i] +
+                         F(k + 1, j + 1, i + 1) * ddz[k + 1] * ddy[j + 1] * ddx[i + 1];
+        val = s / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
+    }
+    const int ic0 = f == 'U', jc0 = f == 'V', kc0 = f == 'W';
+    const int ic = H.y + (i - 3 + ic0) / 2 - ic0;
+    const int jc = H.z + (j - 3 + jc0) / 2 - jc0;
+    const int kc = H.w + (k - 3 + kc0) / 2 - kc0;
+    A.fc[P.ip3 + (long long)(ic - 1) * P.kk * P.jj + (long long)(jc - 1) * P.kk + (kc - 1)] = val;
+}
+
+// ---- ctof (injection) -----------------------------------------------------
+__global__ void k_ctof(const DevGrid* __restrict__ grids, const int4* __restrict__ hier,
+                       const int* __restrict__ list, double* ff, const double* __restrict__ fc) {
+    const int g = list[blockIdx.y];
+    const DevGrid G = grids[g];
+    const int4 H = hier[g];
+    const DevGrid P = grids[H.x];
+    const long long n = (long long)G.kk * G.jj * G.ii;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int k = (int)(q % G.kk) + 1, j = (int)((q / G.kk) % G.jj) + 1, i = (int)(q / ((long long)G.kk * G.jj)) + 1;
+    const int ic = H.y - 1 + (i - 1) / 2, jc = H.z - 1 + (j - 1) / 2, kc = H.w - 1 + (k - 1) / 2;
+    ff[G.ip3 + q] = fc[P.ip3 + (long long)(ic - 1) * P.kk * P.jj + (long long)(jc - 1) * P.kk + (kc - 1)];
+}
+
+int upload_list(Ctx* c, const std::vector<int>& h, int** d) {
+    if (*d) cudaFree(*d);
+    *d = nullptr;
+    if (h.empty()) return 0;
+    MG_CUDA(cudaMalloc(d, h.size() * sizeof(int)));
+    MG_CUDA(copy_on(c->stream, *d, h.data(), h.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return 0;
+}
+
+}  // namespace
+
+int level_init(Ctx* c) {
+    for (int f = 0; f < 6; ++f) {
+        c->pgrids[f].clear();
+        for (int g = 0; g < c->ngrid; ++g)
+            if (c->grids[g].bc[f] == MGLET_BC_PAR) c->pgrids[f].push_back(g);
+        if (int rc = upload_list(c, c->pgrids[f], &c->d_pgrids[f])) return rc;
+    }
+    c->hier.assign(c->ngrid, make_int4(-1, 0, 0, 0));
+    MG_CUDA(cudaMalloc(&c->d_hier, (size_t)c->ngrid * sizeof(int4)));
+    MG_CUDA(copy_on(c->stream, c->d_hier, c->hier.data(), c->hier.size() * sizeof(int4),
+                    cudaMemcpyHostToDevice));
+    return 0;
+}
+
+int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos) {
+    std::vector<int4> h(c->ngrid);
+    for (int g = 0; g < c->ngrid; ++g) {
+        const int par = iparent[g];
+        if (par < 0 || par > c->ngrid || par == g + 1)
+        {
+            set_error("set_hierarchy: bad parent");
+            return MGLET_ERR_ARG;
+        }
+        if (par && c->grids[par - 1].level != c->grids[g].level - 1)
+        {
+            set_error("set_hierarchy: parent not one level coarser");
+            return MGLET_ERR_ARG;
+        }
+        const int ip = pos[3 * g], jp = pos[3 * g + 1], kp = pos[3 * g + 2];
+        if (par) {
+            // the slabs parent, ftoc and ctof read and write stay inside the parent
+            const DevGrid& G = c->grids[g];
+            const DevGrid& P = c->grids[par - 1];
+            if (ip < 3 || jp < 3 || kp < 3 || ip + G.ii / 2 - 1 > P.ii || jp + G.jj / 2 - 1 > P.jj ||
+                kp + G.kk / 2 - 1 > P.kk || (G.ii | G.jj | G.kk) & 1)
+            {
+                set_error("set_hierarchy: fine grid outside its parent");
+                return MGLET_ERR_ARG;
+            }
+        }
+        h[g] = make_int4(par - 1, ip, jp, kp);
+    }
+    c->hier = h;
+    MG_CUDA(copy_on(c->stream, c->d_hier, c->hier.data(), c->hier.size() * sizeof(int4),
+                    cudaMemcpyHostToDevice));
+    for (auto& kv : c->d_children) cudaFree(kv.second);
+    c->d_children.clear();
+    c->children.clear();
+    for (int g = 0; g < c->ngrid; ++g)
+        if (c->hier[g].x >= 0) c->children[c->grids[g].level].push_back(g);
+    for (auto& kv : c->children) {
+        int* d = nullptr;
+        if (int rc = upload_list(c, kv.second, &d)) return rc;
+        c->d_children[kv.first] = d;
+    }
+    return 0;
+}
+
+double* field_buffer(Ctx* c, const std::string& name) {
+    if (name == "U") return c->d_buf[0];
+    if (name == "V") return c->d_buf[1];
+    if (name == "W") return c->d_buf[2];
+    auto it = c->fbuf.find(name);
+    if (it != c->fbuf.end()) return it->second;
+    double* b = nullptr;
+    if (cudaMalloc(&b, (size_t)c->nbuf * sizeof(double)) != cudaSuccess) return nullptr;
+    if (zero_on(c->stream, b, (size_t)c->nbuf * sizeof(double)) != cudaSuccess) {
+        cudaFree(b);
+        return nullptr;
+    }
+    c->fbuf[name] = b;
+    return b;
+}
+
+int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w) {
+    const int f = iface - 1;
+    if (c->pgrids[f].empty()) return 0;
+    int maxq = 0;
+    for (int g : c->pgrids[f]) {
+        const DevGrid& G = c->grids[g];
+        maxq = std::max(maxq, (f / 2 == 2 ? G.jj : G.kk) * (f / 2 == 0 ? G.jj : G.ii));
+    }
+    ParArgs A;
+    A.grids = c->d_grids;
+    A.list = c->d_pgrids[f];
+    A.bface = c->d_bface;
+    A.ub = c->d_buf[0]; A.vb = c->d_buf[1]; A.wb = c->d_buf[2];
+    A.bp = c->F("BP");
+    A.ddx = c->L("DDX"); A.ddy = c->L("DDY"); A.ddz = c->L("DDZ");
+    A.u = u; A.v = v; A.w = w;
+    A.iface = iface;
+    A.ilevel = ilevel;
+    k_bound_par<<<dim3((maxq + 127) / 128, (unsigned)c->pgrids[f].size()), 128, 0, c->stream>>>(A);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int launch_parent(Ctx* c, int ilevel, const char* const v[3], const char* const s[3], bool normal) {
+    ProfScope ps_(c, "parent");
+    for (int f = 0; f < 6; ++f) {
+        std::vector<int> list;
+        for (int g : c->pgrids[f])
+            if (c->grids[g].level == ilevel && c->hier[g].x >= 0) list.push_back(g);
+        if (list.empty()) continue;
+        ParentArgs A;
+        A.grids = c->d_grids;
+        A.hier = c->d_hier;
+        A.bface = c->d_bface;
+        A.iface = f + 1;
+        int nslot = 0;
+        const bool ex[3] = {!normal || f < 2, !normal || (f >= 2 && f < 4), !normal || f >= 4};
+        for (int q = 0; q < 3; ++q)
+            if (v[q] && ex[q]) {
+                A.fc[nslot] = c->F(v[q]);
+                A.buf[nslot] = field_buffer(c, v[q]);
+                if (!A.buf[nslot]) return cuda_fail(cudaErrorMemoryAllocation, "parent buffers");
+                A.comp[nslot++] = q + 1;
+            }
+        for (int q = 0; q < 3; ++q)
+            if (s[q]) {
+                A.fc[nslot] = c->F(s[q]);
+                A.buf[nslot] = field_buffer(c, s[q]);
+                if (!A.buf[nslot]) return cuda_fail(cudaErrorMemoryAllocation, "parent buffers");
+                A.comp[nslot++] = 0;
+            }
+        if (!nslot) continue;
+        int* d = nullptr;
+        if (int rc = upload_list(c, list, &d)) return rc;
+        A.list = d;
+        int maxq = 0;
+        for (int g : list) {
+            const DevGrid& G = c->grids[g];
+            maxq = std::max(maxq, (f / 2 == 2 ? G.jj : G.kk) * (f / 2 == 0 ? G.jj : G.ii));
+        }
+        k_parent<<<dim3((maxq + 127) / 128, (unsigned)list.size(), nslot), 128, 0, c->stream>>>(A);
+        cudaError_t e = cudaGetLastError();
+        c->launches++;
+        cudaStreamSynchronize(c->stream);
+        cudaFree(d);
+        if (e != cudaSuccess) return cuda_fail(e, "parent");
+    }
+    return 0;
+}
+
+int launch_ftoc(Ctx* c, int ilevel, const double* ff, double* fc, char flag) {
+    ProfScope ps_(c, "ftoc");
+    auto it = c->d_children.find(ilevel);
+    if (it == c->d_children.end()) return 0;
+    const std::vector<int>& list = c->children[ilevel];
+    FtocArgs A;
+    A.grids = c->d_grids;
+    A.hier = c->d_hier;
+    A.list = it->second;
+    A.ff = ff;
+    A.fc = fc;
+    A.ddx = c->L("DDX"); A.ddy = c->L("DDY"); A.ddz = c->L("DDZ");
+    A.flag = (flag == 'R' || flag == 'S' || flag == 'T') ? 'P' : flag;
+    int maxq = 0;
+    for (int g : list) {
+        const DevGrid& G = c->grids[g];
+        maxq = std::max(maxq, (G.ii / 2 - 1) * (G.jj / 2 - 1) * (G.kk / 2 - 1));
+    }
+    k_ftoc<<<dim3((maxq + 127) / 128, (unsigned)list.size()), 128, 0, c->stream>>>(A);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int launch_ctof(Ctx* c, int ilevel, double* ff, const double* fc) {
+    ProfScope ps_(c, "ctof");
+    if (ilevel == c->minlevel) return 0;
+    auto it = c->d_children.find(ilevel);
+    if (it == c->d_children.end()) return 0;
+    const std::vector<int>& list = c->children[ilevel];
+    long long maxq = 0;
+    for (int g : list) {
+        const DevGrid& G = c->grids[g];
+        maxq = std::max(maxq, (long long)G.kk * G.jj * G.ii);
+    }
+    k_ctof<<<dim3((unsigned)((maxq + 255) / 256), (unsigned)list.size()), 256, 0, c->stream>>>(
+        c->d_grids, c->d_hier, it->second, ff, fc);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int launch_bound_pressure(Ctx* c, int ilevel, double* p, const double* buf, bool withbp) {
+    ProfScope ps_(c, "bound_pressure");
+    for (int f = 0; f < 6; ++f) {
+        if (c->pgrids[f].empty()) continue;
+        int maxq = 0;
+        for (int g : c->pgrids[f]) {
+            const DevGrid& G = c->grids[g];
+            const int na = f / 2 == 2 ? G.jj : G.kk, nb = f / 2 == 0 ? G.jj : G.ii;
+            maxq = std::max(maxq, ((na - 4) / 2) * ((nb - 4) / 2));
+        }
+        BpArgs A;
+        A.grids = c->d_grids;
+        A.list = c->d_pgrids[f];
+        A.bface = c->d_bface;
+        A.buf = buf;
+        A.bp = withbp ? c->F("BP") : nullptr;
+        A.ddx = c->L("DDX"); A.ddy = c->L("DDY"); A.ddz = c->L("DDZ");
+        A.dx = c->L("DX"); A.dy = c->L("DY"); A.dz = c->L("DZ");
+        A.p = p;
+        A.iface = f + 1;
+        A.ilevel = ilevel;
+        k_bound_pressure<<<dim3((maxq + 127) / 128, (unsigned)c->pgrids[f].size()), 128, 0, c->stream>>>(A);
+        MG_LAUNCHED(c);
+    }
+    return 0;
+}
+
+}  // namespace mg

@@ -58,6 +58,10 @@ class Case:
     ddx: np.ndarray
     ddy: np.ndarray
     ddz: np.ndarray
+    # grid hierarchy: 1-based parent per grid (0 = none) and the parent cell
+    # (iposition, jposition, kposition) where a fine grid starts
+    iparent: np.ndarray = None
+    position: np.ndarray = None
     _keep: list = field(default_factory=list, repr=False)
 
     @property
@@ -166,6 +170,62 @@ def periodic_box(nx, ny, nz, n=24, length=(2 * np.pi, 2 * np.pi, 2 * np.pi), nk=
         x=x, y=y, z=z,
         dx=np.full(ngrid * ii, hx), dy=np.full(ngrid * jj, hy), dz=np.full(ngrid * kk, hz),
         ddx=np.full(ngrid * ii, hx), ddy=np.full(ngrid * jj, hy), ddz=np.full(ngrid * kk, hz),
+    )
+
+
+def refined_box(nx, ny, nz, n=8, refine=(1,), length=(2 * np.pi, 2 * np.pi, 2 * np.pi)):
+    """A two-level hierarchy: the periodic tiling of periodic_box (level 1)
+    with every coarse grid listed in `refine` (1-based, not adjacent to each
+    other) covered by 2x2x2 grids of n^3 cells at half its spacing (level 2).
+    A fine face towards a sibling is CON, every other fine face PAR (code 8)
+    with the coarse grid as parent, as a grids.h5 of a locally refined
+    domain holds (src/core/gridio_mod.F90:61-245).  n must be even."""
+    from .abi import BC_PAR
+    assert n % 2 == 0
+    c = periodic_box(nx, ny, nz, n=n, length=length)
+    nc = c.ngrid
+    ii = jj = kk = n + 4
+    nf = 8 * len(refine)
+    ngrid = nc + nf
+    hx, hy, hz = c.dx[0], c.dy[0], c.dz[0]
+    octs = [(ox, oy, oz) for oz in range(2) for oy in range(2) for ox in range(2)]
+    bct = np.full((nf, 6), BC_PAR, dtype=np.int32)
+    nbr = np.zeros((nf, 26), dtype=np.int32)
+    iparent = np.zeros(ngrid, dtype=np.int32)
+    position = np.zeros((ngrid, 3), dtype=np.int32)
+    xs, ys, zs = [c.x], [c.y], [c.z]
+    for r, gc in enumerate(refine):
+        gx, gy, gz = c.gridpos[gc - 1]
+        for q, (ox, oy, oz) in enumerate(octs):
+            g = nc + 8 * r + q             # 0-based id of the fine grid
+            iparent[g] = gc
+            position[g] = (3 + ox * (n // 2), 3 + oy * (n // 2), 3 + oz * (n // 2))
+            for s in range(1, 27):
+                di, dj, dk = slot_offset(s)
+                tx, ty, tz = ox + di, oy + dj, oz + dk
+                if 0 <= tx < 2 and 0 <= ty < 2 and 0 <= tz < 2:
+                    nbr[g - nc, s - 1] = nc + 8 * r + octs.index((tx, ty, tz)) + 1
+            for f in range(1, 7):
+                d, hi = (f - 1) // 2, (f - 1) % 2
+                o = (ox, oy, oz)[d]
+                if (hi and o == 0) or (not hi and o == 1):
+                    bct[g - nc, f - 1] = BC_CON
+            i = np.arange(1, ii + 1, dtype=np.float64)
+            xs.append(gx * n * hx + ox * n * hx / 2 + (i - 2.5) * hx / 2)
+            ys.append(gy * n * hy + oy * n * hy / 2 + (i - 2.5) * hy / 2)
+            zs.append(gz * n * hz + oz * n * hz / 2 + (i - 2.5) * hz / 2)
+    full = lambda a, h: np.concatenate([a, np.full(nf * ii, h / 2)])
+    return Case(
+        ngrid=ngrid, kk=kk, jj=jj, ii=ii,
+        mgdims=np.tile(np.array([kk, jj, ii], dtype=np.int32), (ngrid, 1)),
+        level=np.concatenate([np.ones(nc, dtype=np.int32), np.full(nf, 2, dtype=np.int32)]),
+        bctype=np.concatenate([c.bctype, bct]),
+        nbrgrid=np.concatenate([c.nbrgrid, nbr]),
+        gridpos=np.concatenate([c.gridpos, np.zeros((nf, 3), dtype=np.int32)]),
+        x=np.concatenate(xs), y=np.concatenate(ys), z=np.concatenate(zs),
+        dx=full(c.dx, hx), dy=full(c.dy, hy), dz=full(c.dz, hz),
+        ddx=full(c.ddx, hx), ddy=full(c.ddy, hy), ddz=full(c.ddz, hz),
+        iparent=iparent, position=position,
     )
 
 

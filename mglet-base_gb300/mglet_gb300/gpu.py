@@ -27,7 +27,9 @@ EXPORTS = [
     "mglet_gpu_profile_names", "mglet_gpu_divmax_noalloc", "mglet_gpu_bound_flow",
     "mglet_gpu_set_buffer", "mglet_gpu_set_bc_real", "mglet_gpu_set_stencils",
     "mglet_gpu_set_ghostcell", "mglet_gpu_setibvalues", "mglet_gpu_getibvalues",
-    "mglet_gpu_setpointvalues", "mglet_gpu_maskbp",
+    "mglet_gpu_setpointvalues", "mglet_gpu_maskbp", "mglet_gpu_get_buffer",
+    "mglet_gpu_set_hierarchy", "mglet_gpu_parent", "mglet_gpu_ftoc", "mglet_gpu_ftoc_multiple",
+    "mglet_gpu_ctof", "mglet_gpu_bound_pressure",
 ]
 
 
@@ -73,6 +75,13 @@ def load(path=None):
     L.mglet_gpu_bound_flow.argtypes = [vp, C.c_int32]
     L.mglet_gpu_set_buffer.argtypes = [vp, cp, C.c_int32, C.c_int32, vp, C.c_int64]
     L.mglet_gpu_set_bc_real.argtypes = [vp, C.c_int32, C.c_int32, C.c_double]
+    L.mglet_gpu_get_buffer.argtypes = [vp, cp, C.c_int32, C.c_int32, vp, C.c_int64]
+    L.mglet_gpu_set_hierarchy.argtypes = [vp, vp, vp]
+    L.mglet_gpu_parent.argtypes = [vp, C.c_int32] + [cp] * 6 + [C.c_int32]
+    L.mglet_gpu_ftoc.argtypes = [vp, C.c_int32, cp, cp, C.c_char]
+    L.mglet_gpu_ftoc_multiple.argtypes = [vp, C.c_int32] + [cp] * 6
+    L.mglet_gpu_ctof.argtypes = [vp, C.c_int32, cp, cp]
+    L.mglet_gpu_bound_pressure.argtypes = [vp, C.c_int32, cp, C.c_int32]
     L.mglet_gpu_set_stencils.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int64, vp,
                                          C.c_int64, vp, C.c_int64]
     for fn in ("mglet_gpu_set_ghostcell", "mglet_gpu_setibvalues", "mglet_gpu_getibvalues",
@@ -192,6 +201,41 @@ class Solver:
 
     def set_bc_real(self, igrid, iface, value):
         _check(load().mglet_gpu_set_bc_real(self.h, igrid, iface, value))
+
+    def get_buffer(self, name, igrid, iface, shape):
+        """The boundary buffer plane of a field, shape (first, second) index."""
+        a = np.zeros(int(np.prod(shape)), dtype=np.float64)
+        _check(load().mglet_gpu_get_buffer(self.h, name.encode(), igrid, iface,
+                                           a.ctypes.data_as(C.c_void_p), a.size))
+        return a.reshape(shape, order="F")
+
+    # -- grid hierarchies ---------------------------------------------------
+    def set_hierarchy(self, iparent, position):
+        ip = np.ascontiguousarray(iparent, dtype=np.int32)
+        ps = np.ascontiguousarray(position, dtype=np.int32)
+        _check(load().mglet_gpu_set_hierarchy(self.h, ip.ctypes.data_as(C.c_void_p),
+                                              ps.ctypes.data_as(C.c_void_p)))
+
+    def parent(self, ilevel, v=None, s=(), normal=False):
+        v = list(v) if v else [None] * 3
+        s = list(s) + [None] * (3 - len(s))
+        e = lambda n: None if n is None else n.encode()
+        _check(load().mglet_gpu_parent(self.h, ilevel, *[e(n) for n in v + s], int(normal)))
+
+    def ftoc(self, ilevel, ff, fc, flag):
+        _check(load().mglet_gpu_ftoc(self.h, ilevel, ff.encode(), fc.encode(), flag.encode()))
+
+    def ftoc_multiple(self, ilevel, v=None, s=()):
+        v = list(v) if v else [None] * 3
+        s = list(s) + [None] * (3 - len(s))
+        e = lambda n: None if n is None else n.encode()
+        _check(load().mglet_gpu_ftoc_multiple(self.h, ilevel, *[e(n) for n in v + s]))
+
+    def ctof(self, ilevel, ff, fc):
+        _check(load().mglet_gpu_ctof(self.h, ilevel, ff.encode(), fc.encode()))
+
+    def bound_pressure(self, ilevel, dp, with_bp=False):
+        _check(load().mglet_gpu_bound_pressure(self.h, ilevel, dp.encode(), int(with_bp)))
 
     def set_stencils(self, igrid, comp, ncells, xpoli, xpolr, xpolrvel=None):
         xi = np.ascontiguousarray(xpoli, dtype=np.int64)

@@ -57,6 +57,13 @@ def lib():
         _lib.oracle_set_buffer.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, vp, C.c_int64]
         _lib.oracle_set_bc_real.argtypes = [vp, C.c_int, C.c_int, C.c_double]
         _lib.oracle_bound_flow.argtypes = [vp, C.c_int]
+        _lib.oracle_get_buffer.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, vp, C.c_int64]
+        _lib.oracle_set_hierarchy.argtypes = [vp, vp, vp]
+        _lib.oracle_parent.argtypes = [vp, C.c_int] + [C.c_char_p] * 6 + [C.c_int]
+        _lib.oracle_ftoc.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p, C.c_char]
+        _lib.oracle_ftoc_multiple.argtypes = [vp, C.c_int] + [C.c_char_p] * 6
+        _lib.oracle_ctof.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p]
+        _lib.oracle_bound_pressure.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
         _lib.oracle_set_stencils.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, C.c_int64, vp,
                                              C.c_int64, vp, C.c_int64]
         _lib.oracle_set_ghostcell.argtypes = [vp]
@@ -196,6 +203,37 @@ class Oracle:
 
     def bound_flow(self, ilevel=0):
         _check(lib().oracle_bound_flow(self.h, ilevel))
+
+    def get_buffer(self, name, igrid, iface, shape):
+        a = np.zeros(int(np.prod(shape)), dtype=np.float64)
+        _check(lib().oracle_get_buffer(self.h, _b(name), igrid, iface,
+                                       a.ctypes.data_as(C.c_void_p), a.size))
+        return a.reshape(shape, order="F")
+
+    def set_hierarchy(self, iparent, position):
+        ip = np.ascontiguousarray(iparent, dtype=np.int32)
+        ps = np.ascontiguousarray(position, dtype=np.int32)
+        _check(lib().oracle_set_hierarchy(self.h, ip.ctypes.data_as(C.c_void_p),
+                                          ps.ctypes.data_as(C.c_void_p)))
+
+    def parent(self, ilevel, v=None, s=(), normal=False):
+        v = list(v) if v else [None] * 3
+        s = list(s) + [None] * (3 - len(s))
+        _check(lib().oracle_parent(self.h, ilevel, *[_b(n) for n in v + s], int(normal)))
+
+    def ftoc(self, ilevel, ff, fc, flag):
+        _check(lib().oracle_ftoc(self.h, ilevel, _b(ff), _b(fc), flag.encode()))
+
+    def ftoc_multiple(self, ilevel, v=None, s=()):
+        v = list(v) if v else [None] * 3
+        s = list(s) + [None] * (3 - len(s))
+        _check(lib().oracle_ftoc_multiple(self.h, ilevel, *[_b(n) for n in v + s]))
+
+    def ctof(self, ilevel, ff, fc):
+        _check(lib().oracle_ctof(self.h, ilevel, _b(ff), _b(fc)))
+
+    def bound_pressure(self, ilevel, dp, with_bp=False):
+        _check(lib().oracle_bound_pressure(self.h, ilevel, _b(dp), int(with_bp)))
 
     def set_stencils(self, igrid, comp, ncells, xpoli, xpolr, xpolrvel=None):
         """Ghost-cell lists of grid igrid (1-based): comp 1..3 (u, v, w) with

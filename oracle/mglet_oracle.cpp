@@ -41,6 +41,7 @@
 #include <cstring>
 #include <limits>
 #include <map>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -148,6 +149,13 @@ struct Ctx {
     int ibtype = 0;              // 0: NONE (noib), 1: GHOSTCELL
     std::vector<std::array<GcList, 3>> gcl;   // [grid][component], 1-based grids
     std::vector<GcFlux> gcf;
+    // grid hierarchy (gridinfo%iparent and i/j/kposition, grids_mod.F90):
+    // iparent[g] 1-based (0 = none), pos[g] = (iposition, jposition,
+    // kposition) of the fine grid in its parent; boundary buffers of fields
+    // other than U, V, W (parent fills them for P, DP, HILF, ...)
+    std::vector<int> iparent;
+    std::vector<std::array<int, 3>> pos;
+    std::map<std::string, std::vector<double>> bufx;
 
     double* F(const char* n) { return f3.at(n).data(); }
     double* L(const char* n) { return f1.at(n).data(); }
@@ -890,7 +898,7 @@ void divcal(Ctx& c, double* DIV, const double* U, const double* V, const double*
 }
 
 // pressuresolver_mod.F90:160-357 mgpoisl (single level, noib)
-void bound_flow(Ctx& c, double* U, double* V, double* W, double* P);
+void bound_flow(Ctx& c, double* U, double* V, double* W, double* P, int ilevel = 0);
 
 void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
     double* U = c.F("U"); double* V = c.F("V"); double* W = c.F("W"); double* P = c.F("P");
@@ -944,9 +952,15 @@ void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
 // reference's loop order (k, j for x faces; k, i for y faces; j, i for z).
 double fsign(double a, double b) { return std::copysign(std::fabs(a), b); }
 
+void bound_par(Ctx& c, int g, int iface, double* U, double* V, double* W);
+
 void bound_face(Ctx& c, int g, int iface, double* U, double* V, double* W, double* P) {
     const Grid& G = c.g[g];
     const int typ = G.bc[iface];
+    if (typ == MGLET_BC_PAR) {
+        bound_par(c, g, iface, U, V, W);
+        return;
+    }
     if (!(typ == MGLET_BC_FIX || typ == MGLET_BC_OP1 || typ == MGLET_BC_NOS || typ == MGLET_BC_SLI))
         return;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
@@ -1063,9 +1077,407 @@ void bound_face(Ctx& c, int g, int iface, double* U, double* V, double* W, doubl
     }
 }
 
-void bound_flow(Ctx& c, double* U, double* V, double* W, double* P) {
-    for (int g = 1; g <= c.ngrid; ++g)
+void bound_flow(Ctx& c, double* U, double* V, double* W, double* P, int ilevel) {
+    for (int g = 1; g <= c.ngrid; ++g) {
+        if (ilevel && c.g[g].level != ilevel) continue;
         for (int f = 1; f <= 6; ++f) bound_face(c, g, f, U, V, W, P);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Multi-level operators (no IB restriction operator; BP enters bound_flow and
+// the bp form of bound_pressure).
+
+const double kPoint1 = (double)0.1f;   // the default-kind literal 0.1 of the PAR branches
+
+std::vector<double>& buffer_of(Ctx& c, const std::string& n) {
+    if (n == "U") return c.bufU;
+    if (n == "V") return c.bufV;
+    if (n == "W") return c.bufW;
+    std::vector<double>& b = c.bufx[n];
+    if (b.empty()) b.assign(c.bufU.size(), 0.0);
+    return b;
+}
+
+// bound_flow_mod.F90:139-256 (bfront), :377-494 (bright), :613-730 (bbottom):
+// the PAR branch.  Tangential components from the buffer with the
+// interior's slope, the normal one as the buffer's coarse flux minus the
+// fine flux of blocked faces.  Written per orientation: the three routines
+// differ in operand order (x faces multiply by the b spacing first, y and z
+// faces by the a spacing first) and the y faces take the tangential w slope
+// from the ghost plane.
+void bound_par(Ctx& c, int g, int iface, double* U, double* V, double* W) {
+    const Grid& G = c.g[g];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    double* u = U + G.ip3; double* v = V + G.ip3; double* w = W + G.ip3;
+    const double* bp = c.F("BP") + G.ip3;
+    const int64_t bo = c.bufoff[6 * (g - 1) + iface - 1];
+    const double* ub = c.bufU.data() + bo; const double* vb = c.bufV.data() + bo;
+    const double* wb = c.bufW.data() + bo;
+    const double* ddx = c.L("DDX") + G.ipx - 1;   // 1-based
+    const double* ddy = c.L("DDY") + G.ipy - 1;
+    const double* ddz = c.L("DDZ") + G.ipz - 1;
+    const int axis = (iface - 1) / 2;
+    const bool lo = (iface % 2) == 1;
+    const int nn = axis == 0 ? ii : (axis == 1 ? jj : kk);
+    const int n2 = lo ? 2 : nn - 1, n3 = lo ? 3 : nn - 2, n4 = lo ? 4 : nn - 3;
+    const int st2 = lo ? 2 : nn - 2;
+    const int na = axis == 2 ? jj : kk, nb = axis == 0 ? jj : ii;
+    auto at = [&](int a, int b, int n) -> int64_t {
+        if (axis == 0) return IX(a, b, n);
+        if (axis == 1) return IX(a, n, b);
+        return IX(n, a, b);
+    };
+    auto bi = [&](int a, int b) -> int64_t { return (int64_t)(a - 1) + (int64_t)(b - 1) * na; };
+    const double* da = axis == 2 ? ddy : ddz;     // spacing along a
+    const double* db = axis == 0 ? ddy : ddx;     // spacing along b
+    double* vn = axis == 0 ? u : (axis == 1 ? v : w);
+    const double* bn = axis == 0 ? ub : (axis == 1 ? vb : wb);
+    double* t1 = axis == 0 ? v : u;               // staggered along b
+    double* t2 = axis == 2 ? v : w;               // staggered along a
+    const double* b1 = axis == 0 ? vb : ub;
+    const double* b2 = axis == 2 ? vb : wb;
+    // tangential components
+    for (int b = 2; b <= nb - 1; ++b)
+        for (int a = 2; a <= na - 1; ++a) {
+            const double s1 = bp[at(a, b, n2)] * bp[at(a, b + 1, n2)];
+            const double s2 = bp[at(a, b, n2)] * bp[at(a + 1, b, n2)];
+            t1[at(a, b, n2)] = (b1[bi(a, b)] - 0.5 * (t1[at(a, b, n3)] - t1[at(a, b, n4)])) * s1 +
+                               (1.0 - s1) * t1[at(a, b, n2)];
+            const double slope2 = axis == 1 ? (t2[at(a, b, n2)] - t2[at(a, b, n4)])
+                                            : (t2[at(a, b, n3)] - t2[at(a, b, n4)]);
+            t2[at(a, b, n2)] = (b2[bi(a, b)] - 0.5 * slope2) * s2 + (1.0 - s2) * t2[at(a, b, n2)];
+        }
+    // face-normal component, 2x2 fine faces per coarse face
+    auto prod = [&](double s, double x, double y) { return s * x * y; };
+    for (int b = 3; b <= nb - 2; b += 2)
+        for (int a = 3; a <= na - 2; a += 2) {
+            const double sbn = bp[at(a, b, n2)];
+            // the four fine faces (a, b), (a, b+1), (a+1, b), (a+1, b+1)
+            const int fa[4] = {a, a, a + 1, a + 1}, fb[4] = {b, b + 1, b, b + 1};
+            double sb[4];
+            for (int q = 0; q < 4; ++q) {
+                const int a1 = fa[q], b1q = fb[q];
+                if (sbn > 0.5)
+                    sb[q] = bp[at(a1, b1q, n2)] * bp[at(a1, b1q, n3)];
+                else
+                    sb[q] = std::min(bp[at(a1, b1q, n3)] + bp[at(a1, b1q, n2)] + bp[at(a1, b1q, n4)] +
+                                         bp[at(a1, b1q - 1, n3)] + bp[at(a1, b1q + 1, n3)] +
+                                         bp[at(a1 - 1, b1q, n3)] + bp[at(a1 + 1, b1q, n3)],
+                                     1.0);
+            }
+            double fak, fine;
+            const double area = axis == 0 ? (db[b] + db[b + 1]) * (da[a] + da[a + 1])
+                                          : (da[a] + da[a + 1]) * (db[b] + db[b + 1]);
+            if (axis == 0) {
+                fak = 1.0 / area * (prod(sb[0], db[b], da[a]) + prod(sb[1], db[b + 1], da[a]) +
+                                    prod(sb[2], db[b], da[a + 1]) + prod(sb[3], db[b + 1], da[a + 1]));
+            } else {
+                fak = 1.0 / area * (prod(sb[0], da[a], db[b]) + prod(sb[1], da[a], db[b + 1]) +
+                                    prod(sb[2], da[a + 1], db[b]) + prod(sb[3], da[a + 1], db[b + 1]));
+            }
+            if (fak < kPoint1) fak = 1.0;
+            fak = 1.0 / fak;
+            double f[4];
+            for (int q = 0; q < 4; ++q) {
+                const double x = vn[at(fa[q], fb[q], st2)] * (1.0 - sb[q]);
+                f[q] = axis == 0 ? x * db[fb[q]] * da[fa[q]] : x * da[fa[q]] * db[fb[q]];
+            }
+            fine = (f[0] + f[1] + f[2] + f[3]) / area;
+            for (int q = 0; q < 4; ++q) {
+                double& x = vn[at(fa[q], fb[q], st2)];
+                x = (bn[bi(fa[q], fb[q])] - fine) * fak * sb[q] + (1.0 - sb[q]) * x * sbn;
+            }
+        }
+}
+
+// parent_core_mod.F90:190-255 start_and_stop: the coarse slab (1-based,
+// inclusive) that the PAR face iface of fine grid igrid is prolonged from
+void par_slab(const Ctx& c, int igrid, int iface, int icomp, int r[6]) {
+    const Grid& G = c.g[igrid];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int ipos = c.pos[igrid][0], jpos = c.pos[igrid][1], kpos = c.pos[igrid][2];
+    int ks = kpos - 2, js = jpos - 2, is = ipos - 2;
+    int ke = ks + kk / 2 + 1, je = js + jj / 2 + 1, ie = is + ii / 2 + 1;
+    if (iface == 1) { is = ipos - 1; ie = ipos - 1; }
+    else if (iface == 2) { is = ipos + (ii - 4) / 2; if (icomp == 1) is -= 1; ie = is; }
+    else if (iface == 3) { js = jpos - 1; je = jpos - 1; }
+    else if (iface == 4) { js = jpos + (jj - 4) / 2; if (icomp == 2) js -= 1; je = js; }
+    else if (iface == 5) { ks = kpos - 1; ke = kpos - 1; }
+    else { ks = kpos + (kk - 4) / 2; if (icomp == 3) ks -= 1; ke = ks; }
+    r[0] = is; r[1] = ie; r[2] = js; r[3] = je; r[4] = ks; r[5] = ke;
+}
+
+// parent1_mod.F90 (pack_single :287-325, read_buffer :345-470, prolong1
+// :515-547, prolong2 :550-584): for every PAR face of the grids of ilevel,
+// the parent's boundary slab is prolonged piecewise constant (staggered
+// directions: the first fine point averages two coarse ones) into the fine
+// grid's boundary buffer of the field.  comp: 1/2/3 for the vector
+// components (staggered along x / y / z), 0 for scalars.
+void parent_field(Ctx& c, int igrid, int iface, const std::string& name, int comp) {
+    const Grid& G = c.g[igrid];
+    const Grid& P = c.g[c.iparent[igrid]];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    int icomp = 0;
+    if ((iface == 1 || iface == 2) && comp == 1) icomp = 1;
+    if ((iface == 3 || iface == 4) && comp == 2) icomp = 2;
+    if ((iface == 5 || iface == 6) && comp == 3) icomp = 3;
+    int r[6];
+    par_slab(c, igrid, iface, icomp, r);
+    const double* fc = c.F(name.c_str()) + P.ip3;
+    std::vector<double> in;
+    {
+        const int kk_ = P.kk, jj_ = P.jj;
+        for (int i = r[0]; i <= r[1]; ++i)
+            for (int j = r[2]; j <= r[3]; ++j)
+                for (int k = r[4]; k <= r[5]; ++k)
+                    in.push_back(fc[(int64_t)(i - 1) * kk_ * jj_ + (int64_t)(j - 1) * kk_ + (k - 1)]);
+    }
+    // idx2d (parent_core_mod.F90:154-183) and stag (:186-210)
+    const int kkc = kk / 2 + 2, jjc = jj / 2 + 2, iic = ii / 2 + 2;
+    int jj2d, ii2d, jjc2d, iic2d, st1 = 0, st2 = 0;
+    if (iface <= 2) { ii2d = jj; jj2d = kk; iic2d = jjc; jjc2d = kkc; }
+    else if (iface <= 4) { ii2d = ii; jj2d = kk; iic2d = iic; jjc2d = kkc; }
+    else { ii2d = ii; jj2d = jj; iic2d = iic; jjc2d = jjc; }
+    if (iface <= 2) { if (comp == 2) st2 = 1; if (comp == 3) st1 = 1; }
+    else if (iface <= 4) { if (comp == 1) st2 = 1; if (comp == 3) st1 = 1; }
+    else { if (comp == 1) st2 = 1; if (comp == 2) st1 = 1; }
+    if ((int)in.size() != jjc2d * iic2d) throw std::runtime_error("parent: slab size");
+    // prolong1: first direction
+    std::vector<double> tmp((size_t)jj2d * iic2d);
+    for (int ic = 1; ic <= iic2d; ++ic)
+        for (int j = 1; j <= jj2d; j += 2) {
+            const int jc = 2 + (j - 1) / 2;
+            const double x = in[(jc - 1) + (size_t)(ic - 1) * jjc2d];
+            tmp[(j - 1) + (size_t)(ic - 1) * jj2d] =
+                st1 ? 0.5 * (x + in[(jc - 2) + (size_t)(ic - 1) * jjc2d]) : x;
+            tmp[j + (size_t)(ic - 1) * jj2d] = x;
+        }
+    // prolong2: second direction, into the buffer
+    double* out = buffer_of(c, name).data() + c.bufoff[6 * (igrid - 1) + iface - 1];
+    for (int i = 1; i <= ii2d; i += 2) {
+        const int ic = 2 + (i - 1) / 2;
+        for (int j = 1; j <= jj2d; ++j) {
+            const double x = tmp[(j - 1) + (size_t)(ic - 1) * jj2d];
+            out[(j - 1) + (size_t)(i - 1) * jj2d] =
+                st2 ? 0.5 * (x + tmp[(j - 1) + (size_t)(ic - 2) * jj2d]) : x;
+            out[(j - 1) + (size_t)i * jj2d] = x;
+        }
+    }
+}
+
+// parent1_mod.F90:24-71 parent1: vector components (v1, v2, v3; with normal
+// only the face-normal one) and scalars, PAR faces of the grids of ilevel
+void parent(Ctx& c, int ilevel, const char* v[3], const char* sc[3], bool normal) {
+    for (int g = 1; g <= c.ngrid; ++g) {
+        if (c.g[g].level != ilevel || !c.iparent[g]) continue;
+        for (int f = 1; f <= 6; ++f) {
+            if (c.g[g].bc[f] != MGLET_BC_PAR) continue;
+            const bool ex[3] = {!normal || f < 3, !normal || (f > 2 && f < 5), !normal || f > 4};
+            for (int q = 0; q < 3; ++q)
+                if (v[q] && ex[q]) parent_field(c, g, f, v[q], q + 1);
+            for (int q = 0; q < 3; ++q)
+                if (sc[q]) parent_field(c, g, f, sc[q], 0);
+        }
+    }
+}
+
+// bound_pressure_mod.F90:534-609 pressureftocone_A / _B: volume- (and bp-)
+// weighted mean of the 2x2x2 fine cells starting at (k, j, i)
+void pressureftocone(const Grid& G, int k, int j, int i, const double* p, const double* bp,
+                     const double* ddx, const double* ddy, const double* ddz, double& pc,
+                     double& bpc) {
+    const int kk = G.kk, jj = G.jj;
+    if (!bp) {
+        bpc = 1.0;
+        double sump = 0.0, sumvol = 0.0;
+        for (int l = 0; l <= 1; ++l)
+            for (int m = 0; m <= 1; ++m)
+                for (int n = 0; n <= 1; ++n) {
+                    const double vol = ddz[k + n] * ddy[j + m] * ddx[i + l];
+                    sump = sump + p[IX(k + n, j + m, i + l)] * vol;
+                    sumvol = sumvol + vol;
+                }
+        pc = sump / sumvol;
+        return;
+    }
+    double sumbp = 0.0;
+    for (int l = 0; l <= 1; ++l)
+        for (int m = 0; m <= 1; ++m)
+            for (int n = 0; n <= 1; ++n) sumbp = sumbp + bp[IX(k + n, j + m, i + l)];
+    bpc = std::min(sumbp, 1.0);
+    if (bpc < 0.5) {
+        pc = 0.0;
+        return;
+    }
+    double sump = 0.0, sumvol = 0.0;
+    for (int l = 0; l <= 1; ++l)
+        for (int m = 0; m <= 1; ++m)
+            for (int n = 0; n <= 1; ++n) {
+                const double vol = bp[IX(k + n, j + m, i + l)] * ddz[k + n] * ddy[j + m] * ddx[i + l];
+                sump = sump + p[IX(k + n, j + m, i + l)] * vol;
+                sumvol = sumvol + vol;
+            }
+    pc = sump / sumvol;
+}
+
+// bound_pressure_mod.F90:106-533: PAR faces of the grids of ilevel; the
+// ghost plane of dp from the buffer (the parent's value) minus the fine
+// mean next to the face, per 2x2 block.  withbp: the _bp forms.
+void bound_pressure(Ctx& c, int ilevel, const std::string& name, bool withbp) {
+    const std::vector<double>& buf = buffer_of(c, name);
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel) continue;
+        for (int iface = 1; iface <= 6; ++iface) {
+            if (G.bc[iface] != MGLET_BC_PAR) continue;
+            const int kk = G.kk, jj = G.jj, ii = G.ii;
+            double* p = c.F(name.c_str()) + G.ip3;
+            const double* bp = withbp ? c.F("BP") + G.ip3 : nullptr;
+            const double* pb = buf.data() + c.bufoff[6 * (g - 1) + iface - 1];
+            const double* ddx = c.L("DDX") + G.ipx - 1;
+            const double* ddy = c.L("DDY") + G.ipy - 1;
+            const double* ddz = c.L("DDZ") + G.ipz - 1;
+            const int axis = (iface - 1) / 2;
+            const bool lo = (iface % 2) == 1;
+            const int nn = axis == 0 ? ii : (axis == 1 ? jj : kk);
+            const int n2 = lo ? 2 : nn - 1, n3 = lo ? 3 : nn - 2, n4 = lo ? 4 : nn - 3;
+            const int st2 = lo ? 2 : nn - 2;
+            const int nmin = std::min(n3, n4);
+            const int na = axis == 2 ? jj : kk, nb = axis == 0 ? jj : ii;
+            const double* dn = axis == 0 ? ddx : (axis == 1 ? ddy : ddz);
+            const double* dstag = axis == 0 ? c.L("DX") + G.ipx - 1
+                                            : (axis == 1 ? c.L("DY") + G.ipy - 1 : c.L("DZ") + G.ipz - 1);
+            const double* da = axis == 2 ? ddy : ddz;
+            const double* db = axis == 0 ? ddy : ddx;
+            auto at = [&](int a, int b, int n) -> int64_t {
+                if (axis == 0) return IX(a, b, n);
+                if (axis == 1) return IX(a, n, b);
+                return IX(n, a, b);
+            };
+            for (int b = 3; b <= nb - 2; b += 2)
+                for (int a = 3; a <= na - 2; a += 2) {
+                    // (k, j, i) of the 2x2x2 block at the face
+                    int k, j, i;
+                    if (axis == 0) { k = a; j = b; i = nmin; }
+                    else if (axis == 1) { k = a; j = nmin; i = b; }
+                    else { k = nmin; j = a; i = b; }
+                    double pcnew, bpc;
+                    pressureftocone(G, k, j, i, p, bp, ddx, ddy, ddz, pcnew, bpc);
+                    const double pbv = pb[(a - 1) + (int64_t)(b - 1) * na];
+                    double fak = 1.0;
+                    if (withbp) {
+                        if (bpc < 0.5) pcnew = pbv;
+                        const double s11 = bp[at(a, b, n2)] * bp[at(a, b, n3)];
+                        const double s12 = bp[at(a, b + 1, n2)] * bp[at(a, b + 1, n3)];
+                        const double s13 = bp[at(a + 1, b, n2)] * bp[at(a + 1, b, n3)];
+                        const double s14 = bp[at(a + 1, b + 1, n2)] * bp[at(a + 1, b + 1, n3)];
+                        fak = (s11 * db[b] * da[a] + s12 * db[b + 1] * da[a] + s13 * db[b] * da[a + 1] +
+                               s14 * db[b + 1] * da[a + 1]) /
+                              ((db[b] + db[b + 1]) * (da[a] + da[a + 1]));
+                        if (fak < kPoint1) fak = 1.0;
+                        fak = 1.0 / fak;
+                    }
+                    for (int l = 0; l <= 1; ++l)
+                        for (int n = 0; n <= 1; ++n) {
+                            // the two tangential offsets: b outer, a inner
+                            const int64_t dst = at(a + n, b + l, n2), src = at(a + n, b + l, n3);
+                            if (withbp)
+                                p[dst] = p[src] + fak * dstag[st2] / (dn[n3] + dn[n2]) * (pbv - pcnew);
+                            else
+                                p[dst] = p[src] + dstag[st2] / (dn[n3] + dn[n2]) * (pbv - pcnew);
+                        }
+                }
+        }
+    }
+}
+
+// noib_restrict_mod.F90:40-124 start_and_stop: the fine loop ranges, stride 2
+void restrict_range(const Grid& G, char flag, int r[6]) {
+    int is = 3, ie = 3, js = 3, je = 3, ks = 3, ke = 3;
+    if (flag == 'U') { is = 2; ie = 2; }
+    else if (flag == 'V') { js = 2; je = 2; }
+    else if (flag == 'W') { ks = 2; ke = 2; }
+    r[0] = is; r[1] = G.ii - ie; r[2] = js; r[3] = G.jj - je; r[4] = ks; r[5] = G.kk - ke;
+}
+
+// noib_restrict_mod.F90:126-298 restrict_u/v/w/s (area- or volume-weighted
+// fine means) and ftoc_mod.F90:581-626 restrict_recieve_open (the coarse
+// index of every fine block): fine grids of ilevel into their parents
+void ftoc_one(Ctx& c, int ilevel, const std::string& ff, const std::string& fc, char flag) {
+    const char f = (flag == 'P' || flag == 'R' || flag == 'S' || flag == 'T') ? 'P' : flag;
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel || !c.iparent[g]) continue;
+        const Grid& P = c.g[c.iparent[g]];
+        const int kk = G.kk, jj = G.jj;
+        const double* fv = c.F(ff.c_str()) + G.ip3;
+        double* cv = c.F(fc.c_str()) + P.ip3;
+        const double* ddx = c.L("DDX") + G.ipx - 1;
+        const double* ddy = c.L("DDY") + G.ipy - 1;
+        const double* ddz = c.L("DDZ") + G.ipz - 1;
+        int r[6];
+        restrict_range(G, f, r);
+        const int ic0 = f == 'U', jc0 = f == 'V', kc0 = f == 'W';
+        const int ipos = c.pos[g][0], jpos = c.pos[g][1], kpos = c.pos[g][2];
+        for (int i = r[0]; i <= r[1]; i += 2)
+            for (int j = r[2]; j <= r[3]; j += 2)
+                for (int k = r[4]; k <= r[5]; k += 2) {
+                    double val;
+                    if (f == 'U') {
+                        const double s = fv[IX(k, j, i)] * ddy[j] * ddz[k] + fv[IX(k, j + 1, i)] * ddy[j + 1] * ddz[k] +
+                                         fv[IX(k + 1, j, i)] * ddy[j] * ddz[k + 1] +
+                                         fv[IX(k + 1, j + 1, i)] * ddy[j + 1] * ddz[k + 1];
+                        val = s / ((ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
+                    } else if (f == 'V') {
+                        const double s = fv[IX(k, j, i)] * ddx[i] * ddz[k] + fv[IX(k, j, i + 1)] * ddx[i + 1] * ddz[k] +
+                                         fv[IX(k + 1, j, i)] * ddx[i] * ddz[k + 1] +
+                                         fv[IX(k + 1, j, i + 1)] * ddx[i + 1] * ddz[k + 1];
+                        val = s / ((ddx[i] + ddx[i + 1]) * (ddz[k] + ddz[k + 1]));
+                    } else if (f == 'W') {
+                        const double s = fv[IX(k, j, i)] * ddx[i] * ddy[j] + fv[IX(k, j, i + 1)] * ddx[i + 1] * ddy[j] +
+                                         fv[IX(k, j + 1, i)] * ddx[i] * ddy[j + 1] +
+                                         fv[IX(k, j + 1, i + 1)] * ddx[i + 1] * ddy[j + 1];
+                        val = s / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]));
+                    } else {
+                        const double s = fv[IX(k, j, i)] * ddz[k] * ddy[j] * ddx[i] +
+                                         fv[IX(k, j, i + 1)] * ddz[k] * ddy[j] * ddx[i + 1] +
+                                         fv[IX(k, j + 1, i)] * ddz[k] * ddy[j + 1] * ddx[i] +
+                                         fv[IX(k, j + 1, i + 1)] * ddz[k] * ddy[j + 1] * ddx[i + 1] +
+                                         fv[IX(k + 1, j, i)] * ddz[k + 1] * ddy[j] * ddx[i] +
+                                         fv[IX(k + 1, j, i + 1)] * ddz[k + 1] * ddy[j] * ddx[i + 1] +
+                                         fv[IX(k + 1, j + 1, i)] * ddz[k + 1] * ddy[j + 1] * ddx[i] +
+                                         fv[IX(k + 1, j + 1, i + 1)] * ddz[k + 1] * ddy[j + 1] * ddx[i + 1];
+                        val = s / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
+                    }
+                    const int ic = ipos + (i - 3 + ic0) / 2 - ic0;
+                    const int jc = jpos + (j - 3 + jc0) / 2 - jc0;
+                    const int kc = kpos + (k - 3 + kc0) / 2 - kc0;
+                    cv[(int64_t)(ic - 1) * P.kk * P.jj + (int64_t)(jc - 1) * P.kk + (kc - 1)] = val;
+                }
+    }
+}
+
+// ctof1_mod.F90:167-211 write_buffer + :308-331 unpack_single: every point
+// of the fine grids of ilevel (ghosts included) takes the value of the
+// parent cell it lies in
+void ctof(Ctx& c, int ilevel, const std::string& ff, const std::string& fc) {
+    if (ilevel == c.minlevel) return;
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel || !c.iparent[g]) continue;
+        const Grid& P = c.g[c.iparent[g]];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        double* fv = c.F(ff.c_str()) + G.ip3;
+        const double* cv = c.F(fc.c_str()) + P.ip3;
+        const int is = c.pos[g][0] - 1, js = c.pos[g][1] - 1, ks = c.pos[g][2] - 1;
+        for (int i = 1; i <= ii; ++i)
+            for (int j = 1; j <= jj; ++j)
+                for (int k = 1; k <= kk; ++k) {
+                    const int ic = is + (i - 1) / 2, jc = js + (j - 1) / 2, kc = ks + (k - 1) / 2;
+                    fv[IX(k, j, i)] = cv[(int64_t)(ic - 1) * P.kk * P.jj + (int64_t)(jc - 1) * P.kk + (kc - 1)];
+                }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1604,7 +2016,7 @@ bool check_supported(const Ctx& c) {
         for (int f = 1; f <= 6; ++f) {
             const int t = c.g[g].bc[f];
             if (!(is_con(t) || t == MGLET_BC_FIX || t == MGLET_BC_OP1 || t == MGLET_BC_NOS ||
-                  t == MGLET_BC_SLI))
+                  t == MGLET_BC_SLI || t == MGLET_BC_PAR))
                 return false;
         }
     return true;
@@ -1615,6 +2027,19 @@ bool check_supported(const Ctx& c) {
 // ===========================================================================
 // C ABI (mirrors include/mglet_gpu.h with an oracle_ prefix)
 struct oracle_ctx : Ctx {};
+
+namespace {
+// the restated stage and pressure solve are single-level: no PAR faces
+int single_level_stage(const Ctx& c) {
+    if (c.minlevel != c.maxlevel)
+        return fail(MGLET_ERR_UNSUPPORTED, "oracle: the multi-level stage is not restated");
+    for (int g = 1; g <= c.ngrid; ++g)
+        for (int f = 1; f <= 6; ++f)
+            if (c.g[g].bc[f] == MGLET_BC_PAR)
+                return fail(MGLET_ERR_UNSUPPORTED, "oracle: PAR faces need the multi-level stage");
+    return 0;
+}
+}  // namespace
 
 extern "C" {
 
@@ -1672,15 +2097,13 @@ int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle
         c->minlevel = std::min(c->minlevel, G.level);
         c->maxlevel = std::max(c->maxlevel, G.level);
     }
-    if (c->minlevel != c->maxlevel) {
-        delete c;
-        return fail(MGLET_ERR_UNSUPPORTED, "oracle: only one grid level is restated");
-    }
     if (!check_supported(*c)) {
         delete c;
         return fail(MGLET_ERR_UNSUPPORTED,
-                    "oracle: only CON, CO1, FIX, OP1, NOS and SLI faces are restated");
+                    "oracle: only CON, CO1, FIX, OP1, NOS, SLI and PAR faces are restated");
     }
+    c->iparent.assign(d->ngrid + 1, 0);
+    c->pos.assign(d->ngrid + 1, {0, 0, 0});
     c->idim3d = o3; c->idimx = ox; c->idimy = oy; c->idimz = oz;
     for (const char* n : {"U", "V", "W", "P", "G", "DU", "DV", "DW", "BP", "SDIV", "UO", "VO",
                           "WO", "DP", "HILF", "RHS", "RES", "GSAP", "PWU", "PWV", "PWW"})
@@ -1826,6 +2249,7 @@ int oracle_laplacephi(oracle_ctx* c, const char* res, const char* phi) {
 
 int oracle_mgpoisl(oracle_ctx* c, double dt, int ittot, int irk, mglet_stage_stats* st) {
     (void)ittot; (void)irk;
+    if (int rc = single_level_stage(*c)) return rc;
     mgpoisl(*c, dt, st);
     return 0;
 }
@@ -1834,6 +2258,7 @@ int oracle_mgpoisl(oracle_ctx* c, double dt, int ittot, int irk, mglet_stage_sta
 int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timeph, double dt,
                               int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st) {
     (void)itstep; (void)timeph;
+    if (int rc = single_level_stage(*c)) return rc;
     double frhs, fu, dtrk, dtrki;
     int rc = oracle_rk_get_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki);
     if (rc) return rc;
@@ -1867,12 +2292,9 @@ int oracle_set_buffer(oracle_ctx* c, const char* name, int igrid, int iface, con
     const Grid& G = c->g[igrid];
     const int64_t sz[3] = {(int64_t)G.kk * G.jj, (int64_t)G.kk * G.ii, (int64_t)G.jj * G.ii};
     if (n != sz[(iface - 1) / 2]) return fail(MGLET_ERR_SIZE, "set_buffer: wrong plane size");
-    std::vector<double>* b = nullptr;
-    if (!std::strcmp(name, "U")) b = &c->bufU;
-    else if (!std::strcmp(name, "V")) b = &c->bufV;
-    else if (!std::strcmp(name, "W")) b = &c->bufW;
-    else return fail(MGLET_ERR_NAME, "set_buffer: buffers exist for U, V, W");
-    std::copy(data, data + n, b->begin() + c->bufoff[6 * (igrid - 1) + iface - 1]);
+    if (!c->f3.count(name)) return fail(MGLET_ERR_NAME, "set_buffer: unknown field");
+    std::vector<double>& b = buffer_of(*c, name);
+    std::copy(data, data + n, b.begin() + c->bufoff[6 * (igrid - 1) + iface - 1]);
     return 0;
 }
 
@@ -1933,8 +2355,75 @@ int oracle_gc_mode(oracle_ctx* c, const char* mode) {
 }
 
 int oracle_bound_flow(oracle_ctx* c, int ilevel) {
-    (void)ilevel;
-    bound_flow(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
+    bound_flow(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"), ilevel);
+    return 0;
+}
+
+int oracle_set_hierarchy(oracle_ctx* c, const int32_t* iparent, const int32_t* pos) {
+    if (!c || !iparent || !pos) return fail(MGLET_ERR_ARG, "set_hierarchy: bad arguments");
+    for (int g = 1; g <= c->ngrid; ++g) {
+        const int par = iparent[g - 1];
+        if (par < 0 || par > c->ngrid || par == g) return fail(MGLET_ERR_ARG, "set_hierarchy: bad parent");
+        if (par && c->g[par].level != c->g[g].level - 1)
+            return fail(MGLET_ERR_ARG, "set_hierarchy: parent not one level coarser");
+        c->iparent[g] = par;
+        c->pos[g] = {pos[3 * (g - 1)], pos[3 * (g - 1) + 1], pos[3 * (g - 1) + 2]};
+    }
+    return 0;
+}
+
+int oracle_get_buffer(oracle_ctx* c, const char* name, int igrid, int iface, double* data, int64_t n) {
+    if (!c || !name || !data || igrid < 1 || igrid > c->ngrid || iface < 1 || iface > 6)
+        return fail(MGLET_ERR_ARG, "get_buffer: bad arguments");
+    const Grid& G = c->g[igrid];
+    const int64_t sz[3] = {(int64_t)G.kk * G.jj, (int64_t)G.kk * G.ii, (int64_t)G.jj * G.ii};
+    if (n != sz[(iface - 1) / 2]) return fail(MGLET_ERR_SIZE, "get_buffer: wrong plane size");
+    const std::string nm(name);
+    const std::vector<double>& b = buffer_of(*c, nm);
+    const int64_t o = c->bufoff[6 * (igrid - 1) + iface - 1];
+    std::copy(b.begin() + o, b.begin() + o + n, data);
+    return 0;
+}
+
+int oracle_parent(oracle_ctx* c, int ilevel, const char* v1, const char* v2, const char* v3,
+                  const char* s1, const char* s2, const char* s3, int normal) {
+    if ((v1 != nullptr) != (v2 != nullptr) || (v1 != nullptr) != (v3 != nullptr))
+        return fail(MGLET_ERR_ARG, "parent: give all three vector components or none");
+    const char* v[3] = {v1, v2, v3};
+    const char* sc[3] = {s1, s2, s3};
+    for (const char* n : {v1, v2, v3, s1, s2, s3})
+        if (n && !c->f3.count(n)) return fail(MGLET_ERR_NAME, "parent: unknown field");
+    parent(*c, ilevel, v, sc, normal != 0);
+    return 0;
+}
+
+int oracle_ftoc(oracle_ctx* c, int ilevel, const char* ff, const char* fc, char flag) {
+    if (!c->f3.count(ff) || !c->f3.count(fc)) return fail(MGLET_ERR_NAME, "ftoc: unknown field");
+    if (!std::strchr("UVWPRST", flag)) return fail(MGLET_ERR_ARG, "ftoc: flag is one of U V W P R S T");
+    ftoc_one(*c, ilevel, ff, fc, flag);
+    return 0;
+}
+
+int oracle_ftoc_multiple(oracle_ctx* c, int ilevel, const char* v1, const char* v2, const char* v3,
+                         const char* s1, const char* s2, const char* s3) {
+    const char* n[6] = {v1, v2, v3, s1, s2, s3};
+    const char fl[6] = {'U', 'V', 'W', 'P', 'P', 'P'};
+    for (int q = 0; q < 6; ++q)
+        if (n[q] && !c->f3.count(n[q])) return fail(MGLET_ERR_NAME, "ftoc: unknown field");
+    for (int q = 0; q < 6; ++q)
+        if (n[q]) ftoc_one(*c, ilevel, n[q], n[q], fl[q]);
+    return 0;
+}
+
+int oracle_ctof(oracle_ctx* c, int ilevel, const char* ff, const char* fc) {
+    if (!c->f3.count(ff) || !c->f3.count(fc)) return fail(MGLET_ERR_NAME, "ctof: unknown field");
+    ctof(*c, ilevel, ff, fc);
+    return 0;
+}
+
+int oracle_bound_pressure(oracle_ctx* c, int ilevel, const char* name, int withbp) {
+    if (!c->f3.count(name)) return fail(MGLET_ERR_NAME, "bound_pressure: unknown field");
+    bound_pressure(*c, ilevel, name, withbp != 0);
     return 0;
 }
 

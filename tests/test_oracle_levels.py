@@ -1,0 +1,520 @@
+"""Inter-level operators of a grid hierarchy in the CPU oracle (no GPU).
+
+parent, ftoc, ctof, bound_pressure and the PAR branch of bound_flow are
+pinned against loop-by-loop numpy transcriptions of the reference's loops
+(src/ib/parent/parent1_mod.F90, parent_core_mod.F90; src/ib/ftoc_mod.F90,
+noib_restrict_mod.F90; src/ib/ctof/ctof1_mod.F90;
+src/flow/bound_pressure_mod.F90; src/flow/bound_flow_mod.F90), written
+per orientation and independently of the oracle's face-generic C++, on a
+two-level hierarchy (cases.refined_box): 2x2x2 periodic coarse grids of 8^3
+cells, the first one covered by 2x2x2 fine grids with PAR faces outward.
+All comparisons are exact.
+"""
+import numpy as np
+import pytest
+
+from mglet_gb300 import abi, cases
+
+F32_01 = float(np.float32(0.1))   # the default-kind literal 0.1 widened
+
+
+def _prm():
+    return abi.make_flow_params(gmol=1e-2, epcorr=1e-12, nouter=4, ninner=2, nouter_min=0)
+
+
+@pytest.fixture(scope="module")
+def case():
+    return cases.refined_box(2, 2, 2, n=8, refine=(1,))
+
+
+def _oracle(case):
+    from oracle.binding import Oracle
+    o = Oracle(case, _prm())
+    o.set_hierarchy(case.iparent, case.position)
+    return o
+
+
+def _g3(case, flat, g):
+    n3 = case.kk * case.jj * case.ii
+    return flat[g * n3:(g + 1) * n3].reshape(case.ii, case.jj, case.kk)
+
+
+def _g1(arr, g, n):
+    return arr[g * n:(g + 1) * n]
+
+
+def _fine(case):
+    return [g for g in range(case.ngrid) if case.iparent[g] > 0]
+
+
+def test_ctof_is_injection(case):
+    rng = np.random.default_rng(1)
+    o = _oracle(case)
+    fc = rng.standard_normal(case.idim3d)
+    ff = rng.standard_normal(case.idim3d)
+    o.set("HILF", ff)
+    o.set("RES", fc)
+    o.ctof(2, "HILF", "RES")
+    got = o.get("HILF")
+    exp = ff.copy()
+    kk, jj, ii = case.kk, case.jj, case.ii
+    for g in _fine(case):
+        P = _g3(case, fc, case.iparent[g] - 1)
+        E = _g3(case, exp, g)
+        ista, jsta, ksta = case.position[g] - 1
+        for i in range(1, ii + 1):
+            for j in range(1, jj + 1):
+                for k in range(1, kk + 1):
+                    E[i - 1, j - 1, k - 1] = P[ista + (i - 1) // 2 - 1, jsta + (j - 1) // 2 - 1,
+                                               ksta + (k - 1) // 2 - 1]
+    assert np.array_equal(got, exp)
+
+
+def _restrict_ref(case, ff, fc, flag):
+    """restrict_u/v/w/s + restrict_recieve_open for every fine grid."""
+    kk, jj, ii = case.kk, case.jj, case.ii
+    out = fc.copy()
+    f = "P" if flag in "PRST" else flag
+    for g in _fine(case):
+        Fv = _g3(case, ff, g)
+        C3 = _g3(case, out, case.iparent[g] - 1)
+        ddx, ddy, ddz = (_g1(case.ddx, g, ii), _g1(case.ddy, g, jj), _g1(case.ddz, g, kk))
+        X = lambda i: ddx[i - 1]
+        Y = lambda j: ddy[j - 1]
+        Z = lambda k: ddz[k - 1]
+        A = lambda k, j, i: Fv[i - 1, j - 1, k - 1]
+        ist, jst, kst = (2 if f == "U" else 3), (2 if f == "V" else 3), (2 if f == "W" else 3)
+        ic0, jc0, kc0 = int(f == "U"), int(f == "V"), int(f == "W")
+        ipos, jpos, kpos = case.position[g]
+        for i in range(ist, ii - ist + 1, 2):
+            for j in range(jst, jj - jst + 1, 2):
+                for k in range(kst, kk - kst + 1, 2):
+                    if f == "U":
+                        s = (A(k, j, i) * Y(j) * Z(k) + A(k, j + 1, i) * Y(j + 1) * Z(k)
+                             + A(k + 1, j, i) * Y(j) * Z(k + 1) + A(k + 1, j + 1, i) * Y(j + 1) * Z(k + 1))
+                        a = (Y(j) + Y(j + 1)) * (Z(k) + Z(k + 1))
+                    elif f == "V":
+                        s = (A(k, j, i) * X(i) * Z(k) + A(k, j, i + 1) * X(i + 1) * Z(k)
+                             + A(k + 1, j, i) * X(i) * Z(k + 1) + A(k + 1, j, i + 1) * X(i + 1) * Z(k + 1))
+                        a = (X(i) + X(i + 1)) * (Z(k) + Z(k + 1))
+                    elif f == "W":
+                        s = (A(k, j, i) * X(i) * Y(j) + A(k, j, i + 1) * X(i + 1) * Y(j)
+                             + A(k, j + 1, i) * X(i) * Y(j + 1) + A(k, j + 1, i + 1) * X(i + 1) * Y(j + 1))
+                        a = (X(i) + X(i + 1)) * (Y(j) + Y(j + 1))
+                    else:
+                        s = (A(k, j, i) * Z(k) * Y(j) * X(i) + A(k, j, i + 1) * Z(k) * Y(j) * X(i + 1)
+                             + A(k, j + 1, i) * Z(k) * Y(j + 1) * X(i)
+                             + A(k, j + 1, i + 1) * Z(k) * Y(j + 1) * X(i + 1)
+                             + A(k + 1, j, i) * Z(k + 1) * Y(j) * X(i)
+                             + A(k + 1, j, i + 1) * Z(k + 1) * Y(j) * X(i + 1)
+                             + A(k + 1, j + 1, i) * Z(k + 1) * Y(j + 1) * X(i)
+                             + A(k + 1, j + 1, i + 1) * Z(k + 1) * Y(j + 1) * X(i + 1))
+                        a = (X(i) + X(i + 1)) * (Y(j) + Y(j + 1)) * (Z(k) + Z(k + 1))
+                    ic = ipos + (i - 3 + ic0) // 2 - ic0
+                    jc = jpos + (j - 3 + jc0) // 2 - jc0
+                    kc = kpos + (k - 3 + kc0) // 2 - kc0
+                    C3[ic - 1, jc - 1, kc - 1] = s / a
+    return out
+
+
+@pytest.mark.parametrize("flag", ["U", "V", "W", "P", "R"])
+def test_ftoc_restriction(case, flag):
+    rng = np.random.default_rng(2)
+    o = _oracle(case)
+    ff = rng.standard_normal(case.idim3d)
+    fc = rng.standard_normal(case.idim3d)
+    o.set("RHS", ff)
+    o.set("RES", fc)
+    o.ftoc(2, "RHS", "RES", flag)
+    assert np.array_equal(o.get("RES"), _restrict_ref(case, ff, fc, flag))
+
+
+def test_ftoc_of_a_constant_is_the_constant(case):
+    o = _oracle(case)
+    o.set("P", np.full(case.idim3d, 0.75))
+    o.ftoc_multiple(2, s=["P"])
+    assert np.allclose(o.get("P"), 0.75, rtol=0, atol=1e-15)
+
+
+def _buf_shape(case, iface):
+    return [(case.kk, case.jj), (case.kk, case.ii), (case.jj, case.ii)][(iface - 1) // 2]
+
+
+def _parent_ref(case, fc, g, iface, comp):
+    """pack_single of the parent slab, then prolong1 and prolong2."""
+    kk, jj, ii = case.kk, case.jj, case.ii
+    P = _g3(case, fc, case.iparent[g] - 1)
+    ipos, jpos, kpos = case.position[g]
+    icomp = {(1, 1): 1, (2, 1): 1, (3, 2): 2, (4, 2): 2, (5, 3): 3, (6, 3): 3}.get((iface, comp), 0)
+    ks, js, is_ = kpos - 2, jpos - 2, ipos - 2
+    ke, je, ie = ks + kk // 2 + 1, js + jj // 2 + 1, is_ + ii // 2 + 1
+    if iface == 1:
+        is_ = ie = ipos - 1
+    elif iface == 2:
+        is_ = ipos + (ii - 4) // 2 - (1 if icomp == 1 else 0)
+        ie = is_
+    elif iface == 3:
+        js = je = jpos - 1
+    elif iface == 4:
+        js = jpos + (jj - 4) // 2 - (1 if icomp == 2 else 0)
+        je = js
+    elif iface == 5:
+        ks = ke = kpos - 1
+    else:
+        ks = kpos + (kk - 4) // 2 - (1 if icomp == 3 else 0)
+        ke = ks
+    buf = [P[i - 1, j - 1, k - 1] for i in range(is_, ie + 1) for j in range(js, je + 1)
+           for k in range(ks, ke + 1)]
+    kkc, jjc, iic = kk // 2 + 2, jj // 2 + 2, ii // 2 + 2
+    if iface in (1, 2):
+        jj2d, ii2d, jjc2d, iic2d = kk, jj, kkc, jjc
+        ustag = (0, 0); vstag = (0, 1); wstag = (1, 0)
+    elif iface in (3, 4):
+        jj2d, ii2d, jjc2d, iic2d = kk, ii, kkc, iic
+        ustag = (0, 1); vstag = (0, 0); wstag = (1, 0)
+    else:
+        jj2d, ii2d, jjc2d, iic2d = jj, ii, jjc, iic
+        ustag = (0, 1); vstag = (1, 0); wstag = (0, 0)
+    st1, st2 = {1: ustag, 2: vstag, 3: wstag}.get(comp, (0, 0))
+    inp = np.array(buf).reshape(iic2d, jjc2d).T          # in(jjc, iic), Fortran order
+    tmp = np.zeros((jj2d, iic2d))
+    for ic in range(1, iic2d + 1):
+        for j in range(1, jj2d + 1, 2):
+            jc = 2 + (j - 1) // 2
+            tmp[j - 1, ic - 1] = (0.5 * (inp[jc - 1, ic - 1] + inp[jc - 2, ic - 1]) if st1
+                                  else inp[jc - 1, ic - 1])
+            tmp[j, ic - 1] = inp[jc - 1, ic - 1]
+    out = np.zeros((jj2d, ii2d))
+    for i in range(1, ii2d + 1, 2):
+        ic = 2 + (i - 1) // 2
+        for j in range(1, jj2d + 1):
+            out[j - 1, i - 1] = (0.5 * (tmp[j - 1, ic - 1] + tmp[j - 1, ic - 2]) if st2
+                                 else tmp[j - 1, ic - 1])
+            out[j - 1, i] = tmp[j - 1, ic - 1]
+    return out
+
+
+@pytest.mark.parametrize("normal", [False, True])
+def test_parent_prolongation(case, normal):
+    rng = np.random.default_rng(3)
+    o = _oracle(case)
+    f = {n: rng.standard_normal(case.idim3d) for n in ("U", "V", "W", "DP")}
+    for n, a in f.items():
+        o.set(n, a)
+    o.parent(2, v=("U", "V", "W"), s=("DP",), normal=normal)
+    checked = 0
+    for g in _fine(case):
+        for iface in range(1, 7):
+            if case.bctype[g, iface - 1] != abi.BC_PAR:
+                continue
+            for comp, name in ((1, "U"), (2, "V"), (3, "W"), (0, "DP")):
+                if normal and comp and comp != (iface + 1) // 2:
+                    continue
+                got = o.get_buffer(name, g + 1, iface, _buf_shape(case, iface))
+                assert np.array_equal(got, _parent_ref(case, f[name], g, iface, comp)), (g, iface, name)
+                checked += 1
+    assert checked > 0
+
+
+def _random_bp(case, seed):
+    rng = np.random.default_rng(seed)
+    bp = np.ones(case.idim3d)
+    bp[rng.random(case.idim3d) < 0.15] = 0.0
+    return bp
+
+
+def _bound_pressure_ref(case, p, bp, bufs, withbp):
+    """bfront/bright/bbottom (and the _bp forms) with pressureftocone_A/_B."""
+    kk, jj, ii = case.kk, case.jj, case.ii
+    out = p.copy()
+    for g in _fine(case):
+        Pp = _g3(case, out, g)
+        B = _g3(case, bp, g)
+        ddx, ddy, ddz = (_g1(case.ddx, g, ii), _g1(case.ddy, g, jj), _g1(case.ddz, g, kk))
+        dx, dy, dz = (_g1(case.dx, g, ii), _g1(case.dy, g, jj), _g1(case.dz, g, kk))
+        X = lambda i: ddx[i - 1]
+        Y = lambda j: ddy[j - 1]
+        Z = lambda k: ddz[k - 1]
+        pa = lambda k, j, i: Pp[i - 1, j - 1, k - 1]
+        ba = lambda k, j, i: B[i - 1, j - 1, k - 1]
+
+        def ftoc1(k, j, i):
+            if not withbp:
+                sp = sv = 0.0
+                for l in (0, 1):
+                    for m in (0, 1):
+                        for n in (0, 1):
+                            vol = Z(k + n) * Y(j + m) * X(i + l)
+                            sp = sp + pa(k + n, j + m, i + l) * vol
+                            sv = sv + vol
+                return sp / sv, 1.0
+            sb = 0.0
+            for l in (0, 1):
+                for m in (0, 1):
+                    for n in (0, 1):
+                        sb = sb + ba(k + n, j + m, i + l)
+            bpc = min(sb, 1.0)
+            if bpc < 0.5:
+                return 0.0, bpc
+            sp = sv = 0.0
+            for l in (0, 1):
+                for m in (0, 1):
+                    for n in (0, 1):
+                        vol = ba(k + n, j + m, i + l) * Z(k + n) * Y(j + m) * X(i + l)
+                        sp = sp + pa(k + n, j + m, i + l) * vol
+                        sv = sv + vol
+            return sp / sv, bpc
+
+        for iface in range(1, 7):
+            if case.bctype[g, iface - 1] != abi.BC_PAR:
+                continue
+            pb = bufs[(g, iface)]
+            lo = iface % 2 == 1
+            if iface in (1, 2):
+                i2, i3, i4, s2 = (2, 3, 4, 2) if lo else (ii - 1, ii - 2, ii - 3, ii - 2)
+                i = min(i3, i4)
+                for j in range(3, jj - 1, 2):
+                    for k in range(3, kk - 1, 2):
+                        pc, bpc = ftoc1(k, j, i)
+                        fak = 1.0
+                        if withbp:
+                            if bpc < 0.5:
+                                pc = pb[k - 1, j - 1]
+                            s11 = ba(k, j, i2) * ba(k, j, i3)
+                            s12 = ba(k, j + 1, i2) * ba(k, j + 1, i3)
+                            s13 = ba(k + 1, j, i2) * ba(k + 1, j, i3)
+                            s14 = ba(k + 1, j + 1, i2) * ba(k + 1, j + 1, i3)
+                            fak = ((s11 * Y(j) * Z(k) + s12 * Y(j + 1) * Z(k) + s13 * Y(j) * Z(k + 1)
+                                    + s14 * Y(j + 1) * Z(k + 1)) / ((Y(j) + Y(j + 1)) * (Z(k) + Z(k + 1))))
+                            fak = 1.0 / (1.0 if fak < F32_01 else fak)
+                        for m in (0, 1):
+                            for n in (0, 1):
+                                base = dx[s2 - 1] / (X(i3) + X(i2)) if not withbp else \
+                                    fak * dx[s2 - 1] / (X(i3) + X(i2))
+                                Pp[i2 - 1, j + m - 1, k + n - 1] = (pa(k + n, j + m, i3)
+                                                                    + base * (pb[k - 1, j - 1] - pc))
+            elif iface in (3, 4):
+                j2, j3, j4, s2 = (2, 3, 4, 2) if lo else (jj - 1, jj - 2, jj - 3, jj - 2)
+                j = min(j3, j4)
+                for i in range(3, ii - 1, 2):
+                    for k in range(3, kk - 1, 2):
+                        pc, bpc = ftoc1(k, j, i)
+                        fak = 1.0
+                        if withbp:
+                            if bpc < 0.5:
+                                pc = pb[k - 1, i - 1]
+                            s11 = ba(k, j2, i) * ba(k, j3, i)
+                            s12 = ba(k, j2, i + 1) * ba(k, j3, i + 1)
+                            s13 = ba(k + 1, j2, i) * ba(k + 1, j3, i)
+                            s14 = ba(k + 1, j2, i + 1) * ba(k + 1, j3, i + 1)
+                            fak = ((s11 * X(i) * Z(k) + s12 * X(i + 1) * Z(k) + s13 * X(i) * Z(k + 1)
+                                    + s14 * X(i + 1) * Z(k + 1)) / ((X(i) + X(i + 1)) * (Z(k) + Z(k + 1))))
+                            fak = 1.0 / (1.0 if fak < F32_01 else fak)
+                        for l in (0, 1):
+                            for n in (0, 1):
+                                base = dy[s2 - 1] / (Y(j3) + Y(j2)) if not withbp else \
+                                    fak * dy[s2 - 1] / (Y(j3) + Y(j2))
+                                Pp[i + l - 1, j2 - 1, k + n - 1] = (pa(k + n, j3, i + l)
+                                                                    + base * (pb[k - 1, i - 1] - pc))
+            else:
+                k2, k3, k4, s2 = (2, 3, 4, 2) if lo else (kk - 1, kk - 2, kk - 3, kk - 2)
+                k = min(k3, k4)
+                for i in range(3, ii - 1, 2):
+                    for j in range(3, jj - 1, 2):
+                        pc, bpc = ftoc1(k, j, i)
+                        fak = 1.0
+                        if withbp:
+                            if bpc < 0.5:
+                                pc = pb[j - 1, i - 1]
+                            s11 = ba(k2, j, i) * ba(k3, j, i)
+                            s12 = ba(k2, j, i + 1) * ba(k3, j, i + 1)
+                            s13 = ba(k2, j + 1, i) * ba(k3, j + 1, i)
+                            s14 = ba(k2, j + 1, i + 1) * ba(k3, j + 1, i + 1)
+                            fak = ((s11 * X(i) * Y(j) + s12 * X(i + 1) * Y(j) + s13 * X(i) * Y(j + 1)
+                                    + s14 * X(i + 1) * Y(j + 1)) / ((X(i) + X(i + 1)) * (Y(j) + Y(j + 1))))
+                            fak = 1.0 / (1.0 if fak < F32_01 else fak)
+                        for l in (0, 1):
+                            for m in (0, 1):
+                                base = dz[s2 - 1] / (Z(k3) + Z(k2)) if not withbp else \
+                                    fak * dz[s2 - 1] / (Z(k3) + Z(k2))
+                                Pp[i + l - 1, j + m - 1, k2 - 1] = (pa(k3, j + m, i + l)
+                                                                    + base * (pb[j - 1, i - 1] - pc))
+    return out
+
+
+@pytest.mark.parametrize("withbp", [False, True])
+def test_bound_pressure(case, withbp):
+    rng = np.random.default_rng(4)
+    o = _oracle(case)
+    p = rng.standard_normal(case.idim3d)
+    bp = _random_bp(case, 5)
+    o.set("DP", p)
+    o.set("BP", bp)
+    bufs = {}
+    for g in _fine(case):
+        for iface in range(1, 7):
+            if case.bctype[g, iface - 1] == abi.BC_PAR:
+                b = rng.standard_normal(_buf_shape(case, iface))
+                bufs[(g, iface)] = b
+                o.set_buffer("DP", g + 1, iface, b)
+    o.bound_pressure(2, "DP", with_bp=withbp)
+    assert np.array_equal(o.get("DP"), _bound_pressure_ref(case, p, bp, bufs, withbp))
+
+
+def _par_ref(case, u, v, w, bp, bufs):
+    """The PAR branch of bfront / bright / bbottom, faces 1..6 per grid."""
+    kk, jj, ii = case.kk, case.jj, case.ii
+    u, v, w = u.copy(), v.copy(), w.copy()
+    for g in _fine(case):
+        U, V, W, B = (_g3(case, a, g) for a in (u, v, w, bp))
+        ddx, ddy, ddz = (_g1(case.ddx, g, ii), _g1(case.ddy, g, jj), _g1(case.ddz, g, kk))
+        X = lambda i: ddx[i - 1]
+        Y = lambda j: ddy[j - 1]
+        Z = lambda k: ddz[k - 1]
+        a_ = lambda A, k, j, i: A[i - 1, j - 1, k - 1]
+
+        def s_(A, k, j, i, val):
+            A[i - 1, j - 1, k - 1] = val
+
+        def sum_seq(vals):
+            s = 0.0
+            for x in vals:
+                s = s + x
+            return s
+
+        for iface in range(1, 7):
+            if case.bctype[g, iface - 1] != abi.BC_PAR:
+                continue
+            ub, vb, wb = bufs[(g, iface)]
+            lo = iface % 2 == 1
+            if iface in (1, 2):
+                i2, i3, i4, s2 = (2, 3, 4, 2) if lo else (ii - 1, ii - 2, ii - 3, ii - 2)
+                for j in range(2, jj):
+                    for k in range(2, kk):
+                        sbv = a_(B, k, j, i2) * a_(B, k, j + 1, i2)
+                        sbw = a_(B, k, j, i2) * a_(B, k + 1, j, i2)
+                        s_(V, k, j, i2, (vb[k - 1, j - 1] - 0.5 * (a_(V, k, j, i3) - a_(V, k, j, i4))) * sbv
+                           + (1.0 - sbv) * a_(V, k, j, i2))
+                        s_(W, k, j, i2, (wb[k - 1, j - 1] - 0.5 * (a_(W, k, j, i3) - a_(W, k, j, i4))) * sbw
+                           + (1.0 - sbw) * a_(W, k, j, i2))
+                for j in range(3, jj - 1, 2):
+                    for k in range(3, kk - 1, 2):
+                        sbu = a_(B, k, j, i2)
+                        bb = lambda k_, j_, i_: a_(B, k_, j_, i_)
+                        if sbu > 0.5:
+                            sb = [bb(k, j, i2) * bb(k, j, i3), bb(k, j + 1, i2) * bb(k, j + 1, i3),
+                                  bb(k + 1, j, i2) * bb(k + 1, j, i3), bb(k + 1, j + 1, i2) * bb(k + 1, j + 1, i3)]
+                        else:
+                            sb = [min(sum_seq([bb(kq, jq, i3), bb(kq, jq, i2), bb(kq, jq, i4), bb(kq, jq - 1, i3),
+                                               bb(kq, jq + 1, i3), bb(kq - 1, jq, i3), bb(kq + 1, jq, i3)]), 1.0)
+                                  for kq, jq in ((k, j), (k, j + 1), (k + 1, j), (k + 1, j + 1))]
+                        fak = 1.0 / ((Y(j) + Y(j + 1)) * (Z(k) + Z(k + 1))) * (
+                            sb[0] * Y(j) * Z(k) + sb[1] * Y(j + 1) * Z(k) + sb[2] * Y(j) * Z(k + 1)
+                            + sb[3] * Y(j + 1) * Z(k + 1))
+                        fak = 1.0 / (1.0 if fak < F32_01 else fak)
+                        q4 = ((k, j), (k, j + 1), (k + 1, j), (k + 1, j + 1))
+                        old = [a_(U, kq, jq, s2) for kq, jq in q4]
+                        fine = (old[0] * (1.0 - sb[0]) * Y(j) * Z(k) + old[1] * (1.0 - sb[1]) * Y(j + 1) * Z(k)
+                                + old[2] * (1.0 - sb[2]) * Y(j) * Z(k + 1)
+                                + old[3] * (1.0 - sb[3]) * Y(j + 1) * Z(k + 1)) / (
+                            (Y(j) + Y(j + 1)) * (Z(k) + Z(k + 1)))
+                        for q, (kq, jq) in enumerate(q4):
+                            s_(U, kq, jq, s2, (ub[kq - 1, jq - 1] - fine) * fak * sb[q]
+                               + (1.0 - sb[q]) * old[q] * sbu)
+            elif iface in (3, 4):
+                j2, j3, j4, s2 = (2, 3, 4, 2) if lo else (jj - 1, jj - 2, jj - 3, jj - 2)
+                for i in range(2, ii):
+                    for k in range(2, kk):
+                        sbu = a_(B, k, j2, i) * a_(B, k, j2, i + 1)
+                        sbw = a_(B, k, j2, i) * a_(B, k + 1, j2, i)
+                        s_(U, k, j2, i, (ub[k - 1, i - 1] - 0.5 * (a_(U, k, j3, i) - a_(U, k, j4, i))) * sbu
+                           + (1.0 - sbu) * a_(U, k, j2, i))
+                        s_(W, k, j2, i, (wb[k - 1, i - 1] - 0.5 * (a_(W, k, j2, i) - a_(W, k, j4, i))) * sbw
+                           + (1.0 - sbw) * a_(W, k, j2, i))
+                for i in range(3, ii - 1, 2):
+                    for k in range(3, kk - 1, 2):
+                        sbv = a_(B, k, j2, i)
+                        bb = lambda k_, j_, i_: a_(B, k_, j_, i_)
+                        q4 = ((k, i), (k, i + 1), (k + 1, i), (k + 1, i + 1))
+                        if sbv > 0.5:
+                            sb = [bb(kq, j2, iq) * bb(kq, j3, iq) for kq, iq in q4]
+                        else:
+                            sb = [min(sum_seq([bb(kq, j3, iq), bb(kq, j2, iq), bb(kq, j4, iq), bb(kq, j3, iq - 1),
+                                               bb(kq, j3, iq + 1), bb(kq - 1, j3, iq), bb(kq + 1, j3, iq)]), 1.0)
+                                  for kq, iq in q4]
+                        fak = 1.0 / ((Z(k) + Z(k + 1)) * (X(i) + X(i + 1))) * (
+                            sb[0] * Z(k) * X(i) + sb[1] * Z(k) * X(i + 1) + sb[2] * Z(k + 1) * X(i)
+                            + sb[3] * Z(k + 1) * X(i + 1))
+                        fak = 1.0 / (1.0 if fak < F32_01 else fak)
+                        old = [a_(V, kq, s2, iq) for kq, iq in q4]
+                        fine = (old[0] * (1.0 - sb[0]) * Z(k) * X(i) + old[1] * (1.0 - sb[1]) * Z(k) * X(i + 1)
+                                + old[2] * (1.0 - sb[2]) * Z(k + 1) * X(i)
+                                + old[3] * (1.0 - sb[3]) * Z(k + 1) * X(i + 1)) / (
+                            (Z(k) + Z(k + 1)) * (X(i) + X(i + 1)))
+                        for q, (kq, iq) in enumerate(q4):
+                            s_(V, kq, s2, iq, (vb[kq - 1, iq - 1] - fine) * fak * sb[q]
+                               + old[q] * (1.0 - sb[q]) * sbv)
+            else:
+                k2, k3, k4, s2 = (2, 3, 4, 2) if lo else (kk - 1, kk - 2, kk - 3, kk - 2)
+                for i in range(2, ii):
+                    for j in range(2, jj):
+                        sbu = a_(B, k2, j, i) * a_(B, k2, j, i + 1)
+                        sbv = a_(B, k2, j, i) * a_(B, k2, j + 1, i)
+                        s_(U, k2, j, i, (ub[j - 1, i - 1] - 0.5 * (a_(U, k3, j, i) - a_(U, k4, j, i))) * sbu
+                           + (1.0 - sbu) * a_(U, k2, j, i))
+                        s_(V, k2, j, i, (vb[j - 1, i - 1] - 0.5 * (a_(V, k3, j, i) - a_(V, k4, j, i))) * sbv
+                           + (1.0 - sbv) * a_(V, k2, j, i))
+                for i in range(3, ii - 1, 2):
+                    for j in range(3, jj - 1, 2):
+                        sbw = a_(B, k2, j, i)
+                        bb = lambda k_, j_, i_: a_(B, k_, j_, i_)
+                        q4 = ((j, i), (j, i + 1), (j + 1, i), (j + 1, i + 1))
+                        if sbw > 0.5:
+                            sb = [bb(k2, jq, iq) * bb(k3, jq, iq) for jq, iq in q4]
+                        else:
+                            sb = [min(sum_seq([bb(k3, jq, iq), bb(k2, jq, iq), bb(k4, jq, iq), bb(k3, jq, iq - 1),
+                                               bb(k3, jq, iq + 1), bb(k3, jq - 1, iq), bb(k3, jq + 1, iq)]), 1.0)
+                                  for jq, iq in q4]
+                        fak = 1.0 / ((Y(j) + Y(j + 1)) * (X(i) + X(i + 1))) * (
+                            sb[0] * Y(j) * X(i) + sb[1] * Y(j) * X(i + 1) + sb[2] * Y(j + 1) * X(i)
+                            + sb[3] * Y(j + 1) * X(i + 1))
+                        fak = 1.0 / (1.0 if fak < F32_01 else fak)
+                        old = [a_(W, s2, jq, iq) for jq, iq in q4]
+                        fine = (old[0] * (1.0 - sb[0]) * Y(j) * X(i) + old[1] * (1.0 - sb[1]) * Y(j) * X(i + 1)
+                                + old[2] * (1.0 - sb[2]) * Y(j + 1) * X(i)
+                                + old[3] * (1.0 - sb[3]) * Y(j + 1) * X(i + 1)) / (
+                            (Y(j) + Y(j + 1)) * (X(i) + X(i + 1)))
+                        for q, (jq, iq) in enumerate(q4):
+                            s_(W, s2, jq, iq, (wb[jq - 1, iq - 1] - fine) * fak * sb[q]
+                               + old[q] * (1.0 - sb[q]) * sbw)
+    return u, v, w
+
+
+@pytest.mark.parametrize("bp_seed", [None, 6])
+def test_bound_flow_par(case, bp_seed):
+    rng = np.random.default_rng(7)
+    o = _oracle(case)
+    u, v, w = (rng.standard_normal(case.idim3d) for _ in range(3))
+    bp = np.ones(case.idim3d) if bp_seed is None else _random_bp(case, bp_seed)
+    for n, a in (("U", u), ("V", v), ("W", w), ("BP", bp)):
+        o.set(n, a)
+    bufs = {}
+    for g in _fine(case):
+        for iface in range(1, 7):
+            if case.bctype[g, iface - 1] == abi.BC_PAR:
+                b = tuple(rng.standard_normal(_buf_shape(case, iface)) for _ in range(3))
+                bufs[(g, iface)] = b
+                for n, x in zip(("U", "V", "W"), b):
+                    o.set_buffer(n, g + 1, iface, x)
+    o.bound_flow(2)
+    eu, ev, ew = _par_ref(case, u, v, w, bp, bufs)
+    assert np.array_equal(o.get("U"), eu)
+    assert np.array_equal(o.get("V"), ev)
+    assert np.array_equal(o.get("W"), ew)
+
+
+def test_stage_refuses_hierarchies(case):
+    from oracle.binding import OracleError
+    o = _oracle(case)
+    with pytest.raises(OracleError):
+        o.mgpoisl(1e-3)
