@@ -322,11 +322,16 @@ long long connect_points(Ctx* c, int ilevel, int layers, int slots, bool corners
 }
 
 // ---------------------------------------------------------------------------
-// mgpoisl, plain FP64 form (pressuresolver_mod.F90:160-357; single level,
-// noib: bound_pressure, ctof, parent and ftoc have no work).
+// mgpoisl, plain FP64 form (pressuresolver_mod.F90:160-357) over every level
+// of the hierarchy; on one level ftoc, ctof, parent and bound_pressure have
+// no work.  mgpoisit works on HILF, whose PAR buffers parent fills.
 static int mgpoisit_plain(Ctx* c, int ilevel, double* dp, double* rhs, double* res) {
     const int ninner = c->prm.ninner;
+    const bool withbp = c->ibtype == 1;
+    double* hbuf = field_buffer(c, "HILF");
+    if (!hbuf) return fail(MGLET_ERR_CUDA, "mgpoisl: buffer allocation");
     for (int iloop = 1; iloop <= ninner; ++iloop) {
+        if (int rc = launch_bound_pressure(c, ilevel, dp, hbuf, withbp)) return rc;
         if (c->prm.psolver == MGLET_PSOLVER_SOR && ilevel > c->minlevel) {
             if (int rc = launch_sor(c, ilevel, dp, rhs)) return rc;
         } else {
@@ -341,7 +346,7 @@ static int mgpoisit_plain(Ctx* c, int ilevel, double* dp, double* rhs, double* r
                              false, 0))
             return rc;
     }
-    return 0;
+    return launch_bound_pressure(c, ilevel, dp, hbuf, withbp);
 }
 
 static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
@@ -351,17 +356,33 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
     const size_t bytes = (size_t)c->idim3d * sizeof(double);
     for (double* a : {dp, hilf, rhs, res}) MG_CUDA(cudaMemsetAsync(a, 0, bytes, c->stream));
     const double prefak = c->prm.rho / dt;
+    const bool multi = c->minlevel != c->maxlevel;
+    const char* const none[3] = {nullptr, nullptr, nullptr};
+    const char* const shilf[3] = {"HILF", nullptr, nullptr};
     if (int rc = launch_divcal(c, rhs, U, V, W, prefak)) return rc;
+    for (int l = c->maxlevel; l >= c->minlevel; --l)
+        if (int rc = launch_ftoc(c, l, rhs, rhs, 'R')) return rc;
     int ipc = 0, done = 0;
     double maxrhs = 0.0;
     for (int ipcount = 1; ipcount <= c->prm.nouter; ++ipcount) {
-        for (int l = c->minlevel; l <= c->maxlevel; ++l)
+        for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+            if (int rc = launch_ctof(c, l, hilf, hilf)) return rc;
+            if (int rc = launch_parent(c, l, none, shilf, false)) return rc;
             if (int rc = mgpoisit_plain(c, l, hilf, rhs, res)) return rc;
+        }
+        for (int l = c->maxlevel; l >= c->minlevel; --l)
+            if (int rc = launch_ftoc(c, l, hilf, hilf, 'P')) return rc;
         if (int rc = connect(c, 0, 1, nullptr, nullptr, nullptr, hilf, nullptr, nullptr, false,
                              false, 0))
             return rc;
         if (int rc = launch_laplacephi(c, 0, res, hilf)) return rc;
         if (int rc = launch_rescal_maxabs(c, rhs, res)) return rc;
+        if (multi) {
+            // rhs restricted into the coarse grids, then its maximum again
+            for (int l = c->maxlevel; l >= c->minlevel + 1; --l)
+                if (int rc = launch_ftoc(c, l, rhs, rhs, 'R')) return rc;
+            if (int rc = launch_rescal_maxabs(c, rhs, nullptr)) return rc;
+        }
         if (int rc = launch_accumulate(c, dp, hilf)) return rc;
         ipc += c->prm.ninner;
         done = ipcount;
@@ -380,10 +401,29 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
         MG_CUDA(cudaStreamSynchronize(c->stream));
         maxrhs = c->h_scalar[0];
     }
+    const char* const sdp[3] = {"DP", nullptr, nullptr};
+    double* dbuf = field_buffer(c, "DP");
+    if (!dbuf) return fail(MGLET_ERR_CUDA, "mgpoisl: buffer allocation");
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+        if (int rc = launch_parent(c, l, none, sdp, false)) return rc;
+        if (int rc = launch_bound_pressure(c, l, dp, dbuf, c->ibtype == 1)) return rc;
+    }
     if (int rc = launch_mgpcorr(c, U, V, W, P, dp, dt / c->prm.rho)) return rc;
-    // pressuresolver_mod.F90:341-348: bound, then the corner connect
-    if (int rc = launch_bound_flow(c, U, V, W, P)) return rc;
-    if (int rc = connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
+    // pressuresolver_mod.F90:334-348: ftoc fine to coarse, then per level
+    // parent, bound and the corner connect
+    for (int l = c->maxlevel; l >= c->minlevel; --l) {
+        if (int rc = launch_ftoc(c, l, U, U, 'U')) return rc;
+        if (int rc = launch_ftoc(c, l, V, V, 'V')) return rc;
+        if (int rc = launch_ftoc(c, l, W, W, 'W')) return rc;
+        if (int rc = launch_ftoc(c, l, P, P, 'P')) return rc;
+    }
+    const char* const vuvw[3] = {"U", "V", "W"};
+    const char* const sp[3] = {"P", nullptr, nullptr};
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+        if (int rc = launch_parent(c, l, vuvw, sp, false)) return rc;
+        if (int rc = launch_bound_flow(c, U, V, W, P, l)) return rc;
+        if (int rc = connect(c, l, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
+    }
     if (st) {
         st->ipc = ipc;
         st->nouter_done = done;
@@ -393,9 +433,8 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
     return 0;
 }
 
-// The stage driver and the pressure solve are built for one grid level
-// without PAR faces (the multi-level schedule of mgpoisl and tstle4_par are
-// not part of this library); hierarchies use the level operators.
+// The stage driver is built for one grid level without PAR faces:
+// tstle4_par (the PAR face fluxes of tstle4) is not part of this library.
 int single_level_stage(Ctx* c) {
     if (c->minlevel != c->maxlevel)
         return fail(MGLET_ERR_UNSUPPORTED, "the multi-level stage is not built; use the level operators");
@@ -405,8 +444,19 @@ int single_level_stage(Ctx* c) {
     return 0;
 }
 
+// The pressure solve runs on hierarchies once the parents are known; the
+// ghost-cell restriction (gc_restrict_mod.F90) is not built.
+int hierarchy_ready(Ctx* c) {
+    for (int g = 0; g < c->ngrid; ++g)
+        if (c->grids[g].level != c->minlevel && c->hier[g].x < 0)
+            return fail(MGLET_ERR_ARG, "mgpoisl: a fine grid without parent (mglet_gpu_set_hierarchy)");
+    if (c->minlevel != c->maxlevel && c->ibtype == 1)
+        return fail(MGLET_ERR_UNSUPPORTED, "mgpoisl: the ghost-cell restriction is not built");
+    return 0;
+}
+
 int mgpoisl(Ctx* c, double dt, mglet_stage_stats* st) {
-    if (int rc = single_level_stage(c)) return rc;
+    if (int rc = hierarchy_ready(c)) return rc;
     if (c->prm.form == MGLET_FORM_MIXED) return mixed_mgpoisl(c, dt, st);
     return mgpoisl_plain(c, dt, st);
 }
@@ -699,6 +749,8 @@ int mglet_gpu_destroy(mglet_ctx* c) {
         cudaFree(p);
     for (int* b : c->d_bgrids) cudaFree(b);
     for (int* b : c->d_pgrids) cudaFree(b);
+    for (auto& m : c->d_plist)
+        for (auto& kv : m) cudaFree(kv.second);
     for (auto& kv : c->d_children) cudaFree(kv.second);
     for (auto& kv : c->fbuf) cudaFree(kv.second);
     cudaFree(c->d_hier);

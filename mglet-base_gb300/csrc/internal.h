@@ -147,6 +147,8 @@ struct Ctx {
     std::map<int, int*> d_children;
     std::vector<int> pgrids[6];
     int* d_pgrids[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    std::map<int, std::vector<int>> plist[6];   // per level: grids with a parent and PAR on the face
+    std::map<int, int*> d_plist[6];
     std::map<std::string, double*> fbuf;
     long long launches = 0;
     bool prof = false;

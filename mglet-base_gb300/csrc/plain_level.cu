@@ -448,6 +448,18 @@ int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos) {
         if (int rc = upload_list(c, kv.second, &d)) return rc;
         c->d_children[kv.first] = d;
     }
+    for (int f = 0; f < 6; ++f) {
+        for (auto& kv : c->d_plist[f]) cudaFree(kv.second);
+        c->d_plist[f].clear();
+        c->plist[f].clear();
+        for (int g : c->pgrids[f])
+            if (c->hier[g].x >= 0) c->plist[f][c->grids[g].level].push_back(g);
+        for (auto& kv : c->plist[f]) {
+            int* d = nullptr;
+            if (int rc = upload_list(c, kv.second, &d)) return rc;
+            c->d_plist[f][kv.first] = d;
+        }
+    }
     return 0;
 }
 
@@ -493,14 +505,14 @@ int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double
 int launch_parent(Ctx* c, int ilevel, const char* const v[3], const char* const s[3], bool normal) {
     ProfScope ps_(c, "parent");
     for (int f = 0; f < 6; ++f) {
-        std::vector<int> list;
-        for (int g : c->pgrids[f])
-            if (c->grids[g].level == ilevel && c->hier[g].x >= 0) list.push_back(g);
-        if (list.empty()) continue;
+        auto it = c->d_plist[f].find(ilevel);
+        if (it == c->d_plist[f].end()) continue;
+        const std::vector<int>& list = c->plist[f][ilevel];
         ParentArgs A;
         A.grids = c->d_grids;
         A.hier = c->d_hier;
         A.bface = c->d_bface;
+        A.list = it->second;
         A.iface = f + 1;
         int nslot = 0;
         const bool ex[3] = {!normal || f < 2, !normal || (f >= 2 && f < 4), !normal || f >= 4};
@@ -519,20 +531,13 @@ int launch_parent(Ctx* c, int ilevel, const char* const v[3], const char* const 
                 A.comp[nslot++] = 0;
             }
         if (!nslot) continue;
-        int* d = nullptr;
-        if (int rc = upload_list(c, list, &d)) return rc;
-        A.list = d;
         int maxq = 0;
         for (int g : list) {
             const DevGrid& G = c->grids[g];
             maxq = std::max(maxq, (f / 2 == 2 ? G.jj : G.kk) * (f / 2 == 0 ? G.jj : G.ii));
         }
         k_parent<<<dim3((maxq + 127) / 128, (unsigned)list.size(), nslot), 128, 0, c->stream>>>(A);
-        cudaError_t e = cudaGetLastError();
-        c->launches++;
-        cudaStreamSynchronize(c->stream);
-        cudaFree(d);
-        if (e != cudaSuccess) return cuda_fail(e, "parent");
+        MG_LAUNCHED(c);
     }
     return 0;
 }

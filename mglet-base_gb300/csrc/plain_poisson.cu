@@ -197,10 +197,12 @@ struct SipArgs {
     const int* const* mips; const int* const* idxs;
     const double* rhs; double* res; double* phi;
     const double *c0, *c1, *c2, *c3;   // lw ls lb lpr  |  ue un ut
+    int ilevel;                         // the grids of this level (<= 0: all)
 };
 
 __global__ void __launch_bounds__(512) k_sipiter1_hp(SipArgs a) {
     const DevGrid G = a.grids[blockIdx.x];
+    if (a.ilevel > 0 && G.level != a.ilevel) return;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int* mip = a.mips[G.cls];
     const int* idx = a.idxs[G.cls];
@@ -226,6 +228,7 @@ __global__ void __launch_bounds__(512) k_sipiter1_hp(SipArgs a) {
 // sipiter2 (hyperplane): backward substitution, then phi += res.
 __global__ void __launch_bounds__(512) k_sipiter2_hp(SipArgs a) {
     const DevGrid G = a.grids[blockIdx.x];
+    if (a.ilevel > 0 && G.level != a.ilevel) return;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int* mip = a.mips[G.cls];
     const int* idx = a.idxs[G.cls];
@@ -257,6 +260,7 @@ __global__ void __launch_bounds__(512) k_sipiter2_hp(SipArgs a) {
 // sipiter1 (classic): columns (j, i) on the diagonal i+j = d in parallel.
 __global__ void k_sipiter1_cl(SipArgs a) {
     const DevGrid G = a.grids[blockIdx.x];
+    if (a.ilevel > 0 && G.level != a.ilevel) return;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const long long o = G.ip3;
     const double* rhs = a.rhs + o;
@@ -284,6 +288,7 @@ __global__ void k_sipiter1_cl(SipArgs a) {
 // sipiter2 (classic)
 __global__ void k_sipiter2_cl(SipArgs a) {
     const DevGrid G = a.grids[blockIdx.x];
+    if (a.ilevel > 0 && G.level != a.ilevel) return;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const long long o = G.ip3;
     double* res = a.res + o;
@@ -317,8 +322,10 @@ __global__ void k_sor(const DevGrid* __restrict__ grids, int rb, double* DP,
                       const double* __restrict__ RHS, const double* __restrict__ RAP,
                       const double* __restrict__ AW, const double* __restrict__ AE,
                       const double* __restrict__ AS, const double* __restrict__ AN,
-                      const double* __restrict__ AB, const double* __restrict__ AT, double omg) {
+                      const double* __restrict__ AB, const double* __restrict__ AT, double omg,
+                      int ilevel) {
     const DevGrid G = grids[blockIdx.y];
+    if (ilevel > 0 && G.level != ilevel) return;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int ni = ii - 4, nj = jj - 4, nk = kk - 4;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -390,7 +397,8 @@ __global__ void k_laplacephi(const DevGrid* __restrict__ grids, int ilevel, doub
                            AP[o + IX(k, j, i)] * phi[IX(k, j, i)];
 }
 
-// rescal (rhs += res on the interior) fused with maxabscal_grid.
+// rescal (rhs += res on the interior) fused with maxabscal_grid; with RES
+// null only the maximum (after ftoc has restricted rhs into coarse grids).
 __global__ void __launch_bounds__(256) k_rescal_maxabs(const DevGrid* __restrict__ grids, double* RHS,
                                                        const double* __restrict__ RES,
                                                        double* __restrict__ gridmax) {
@@ -403,8 +411,11 @@ __global__ void __launch_bounds__(256) k_rescal_maxabs(const DevGrid* __restrict
     for (int t = threadIdx.x; t < ni * nj * nk; t += blockDim.x) {
         const int k = t % nk + 3, j = (t / nk) % nj + 3, i = t / (nk * nj) + 3;
         const long long c = o + IX(k, j, i);
-        const double r = RHS[c] + RES[c];
-        RHS[c] = r;
+        double r = RHS[c];
+        if (RES) {
+            r = r + RES[c];
+            RHS[c] = r;
+        }
         m = fmax(fabs(r), m);
     }
     m = block_max(m, sh);
@@ -564,13 +575,13 @@ int launch_sip_lu_classic(Ctx* c) {
 
 int launch_sipiter1(Ctx* c, int ilevel, const double* rhs, double* res) {
     ProfScope ps_(c, "sipiter1");
-    (void)ilevel;   // one level
     TablePtrs tp;
     if (int rc = table_ptrs(c, tp)) return rc;
     SipArgs a;
     a.grids = c->d_grids; a.mips = tp.mips; a.idxs = tp.idxs;
     a.rhs = rhs; a.res = res; a.phi = nullptr;
     a.c0 = c->F("SIPLW"); a.c1 = c->F("SIPLS"); a.c2 = c->F("SIPLB"); a.c3 = c->F("SIPLPR");
+    a.ilevel = ilevel;
     if (c->prm.psolver == MGLET_PSOLVER_CLASSIC)
         k_sipiter1_cl<<<c->ngrid, 32, 0, c->stream>>>(a);
     else
@@ -581,13 +592,13 @@ int launch_sipiter1(Ctx* c, int ilevel, const double* rhs, double* res) {
 
 int launch_sipiter2(Ctx* c, int ilevel, double* phi, double* res) {
     ProfScope ps_(c, "sipiter2");
-    (void)ilevel;
     TablePtrs tp;
     if (int rc = table_ptrs(c, tp)) return rc;
     SipArgs a;
     a.grids = c->d_grids; a.mips = tp.mips; a.idxs = tp.idxs;
     a.rhs = nullptr; a.res = res; a.phi = phi;
     a.c0 = c->F("SIPUE"); a.c1 = c->F("SIPUN"); a.c2 = c->F("SIPUT"); a.c3 = nullptr;
+    a.ilevel = ilevel;
     if (c->prm.psolver == MGLET_PSOLVER_CLASSIC)
         k_sipiter2_cl<<<c->ngrid, 32, 0, c->stream>>>(a);
     else
@@ -598,12 +609,11 @@ int launch_sipiter2(Ctx* c, int ilevel, double* phi, double* res) {
 
 int launch_sor(Ctx* c, int ilevel, double* dp, const double* rhs) {
     ProfScope ps_(c, "sor");
-    (void)ilevel;
     dim3 grid((interior_points_max(c) + 255) / 256, c->ngrid);
     for (int rb = 0; rb <= 1; ++rb) {
         k_sor<<<grid, 256, 0, c->stream>>>(c->d_grids, rb, dp, rhs, c->F("SOR_RAP"), c->L("GSAW"),
                                            c->L("GSAE"), c->L("GSAS"), c->L("GSAN"),
-                                           c->L("GSAB"), c->L("GSAT"), c->prm.omega);
+                                           c->L("GSAB"), c->L("GSAT"), c->prm.omega, ilevel);
         MG_LAUNCHED(c);
     }
     return 0;

@@ -794,9 +794,16 @@ void sip(Ctx& c, int ilevel, int iloop, double* dp, double* res, const double* r
     }
 }
 
-// pressuresolver_mod.F90:361-420 mgpoisit (bound_pressure: no PAR faces)
-void mgpoisit(Ctx& c, int ilevel, double* dp, const double* rhs, double* res) {
+void bound_pressure(Ctx& c, int ilevel, const std::string& name, bool withbp);
+void parent(Ctx& c, int ilevel, const char* v[3], const char* sc[3], bool normal);
+void ftoc_one(Ctx& c, int ilevel, const std::string& ff, const std::string& fc, char flag);
+void ctof(Ctx& c, int ilevel, const std::string& ff, const std::string& fc);
+
+// pressuresolver_mod.F90:361-420 mgpoisit on the field HILF (bound_pressure
+// acts on PAR faces only; withbp for the ghost-cell IB, which passes bp)
+void mgpoisit(Ctx& c, int ilevel, double* dp, const double* rhs, double* res, bool withbp) {
     for (int iloop = 1; iloop <= c.prm.ninner; ++iloop) {
+        bound_pressure(c, ilevel, "HILF", withbp);
         if (c.prm.psolver == MGLET_PSOLVER_SOR && ilevel > c.minlevel) {
 #pragma omp parallel for schedule(dynamic)
             for (int g = 1; g <= c.ngrid; ++g)
@@ -806,6 +813,7 @@ void mgpoisit(Ctx& c, int ilevel, double* dp, const double* rhs, double* res) {
         }
         connect(c, ilevel, 1, nullptr, nullptr, nullptr, dp, nullptr, nullptr, false, false, 0);
     }
+    bound_pressure(c, ilevel, "HILF", withbp);
 }
 
 // pressuresolver_mod.F90:623-689 maxabscal
@@ -897,7 +905,8 @@ void divcal(Ctx& c, double* DIV, const double* U, const double* V, const double*
     }
 }
 
-// pressuresolver_mod.F90:160-357 mgpoisl (single level, noib)
+// pressuresolver_mod.F90:160-357 mgpoisl over every level of the hierarchy
+// (one level: ftoc, ctof, parent and bound_pressure have no work)
 void bound_flow(Ctx& c, double* U, double* V, double* W, double* P, int ilevel = 0);
 
 void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
@@ -906,12 +915,20 @@ void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
     double* dp = c.F("DP"); double* hilf = c.F("HILF");
     double* rhs = c.F("RHS"); double* res = c.F("RES");
     const double prefak = c.prm.rho / dt;
+    const bool withbp = c.ibtype == 1;
+    const char* none[3] = {nullptr, nullptr, nullptr};
+    const char* shilf[3] = {"HILF", nullptr, nullptr};
     divcal(c, rhs, U, V, W, prefak);
+    for (int l = c.maxlevel; l >= c.minlevel; --l) ftoc_one(c, l, "RHS", "RHS", 'R');
     int ipc = 0, ipcount_done = 0;
     double maxrhs = 0.0;
     for (int ipcount = 1; ipcount <= c.prm.nouter; ++ipcount) {
-        for (int ilevel = c.minlevel; ilevel <= c.maxlevel; ++ilevel)
-            mgpoisit(c, ilevel, hilf, rhs, res);
+        for (int ilevel = c.minlevel; ilevel <= c.maxlevel; ++ilevel) {
+            ctof(c, ilevel, "HILF", "HILF");
+            parent(c, ilevel, none, shilf, false);
+            mgpoisit(c, ilevel, hilf, rhs, res, withbp);
+        }
+        for (int l = c.maxlevel; l >= c.minlevel; --l) ftoc_one(c, l, "HILF", "HILF", 'P');
         connect(c, 0, 1, nullptr, nullptr, nullptr, hilf, nullptr, nullptr, false, false, 0);
         laplacephi_level(c, 0, res, hilf);
         // rescal: rhs += res on the interior
@@ -924,6 +941,7 @@ void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
                 for (int j = 3; j <= jj - 2; ++j)
                     for (int k = 3; k <= kk - 2; ++k) r[IX(k, j, i)] = r[IX(k, j, i)] + s[IX(k, j, i)];
         }
+        for (int l = c.maxlevel; l >= c.minlevel + 1; --l) ftoc_one(c, l, "RHS", "RHS", 'R');
         maxrhs = maxabscal(c, rhs);
         // accumulate_pcorr over the whole flat array, then hilf = 0
         for (int64_t n = 0; n < c.idim3d; ++n) dp[n] = dp[n] + hilf[n];
@@ -932,10 +950,27 @@ void mgpoisl(Ctx& c, double dt, mglet_stage_stats* st) {
         ipcount_done = ipcount;
         if (ipcount >= c.prm.nouter_min && maxrhs / prefak < c.prm.epcorr) break;
     }
+    const char* sdp[3] = {"DP", nullptr, nullptr};
+    for (int l = c.minlevel; l <= c.maxlevel; ++l) {
+        parent(c, l, none, sdp, false);
+        bound_pressure(c, l, "DP", withbp);
+    }
     mgpcorr(c, U, V, W, P, dp, dt / c.prm.rho);
-    // pressuresolver_mod.F90:341-348: bound, then the corner connect
-    bound_flow(c, U, V, W, P);
-    connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0);
+    // pressuresolver_mod.F90:334-348: ftoc fine to coarse, then per level
+    // parent, bound and the corner connect
+    for (int l = c.maxlevel; l >= c.minlevel; --l) {
+        ftoc_one(c, l, "U", "U", 'U');
+        ftoc_one(c, l, "V", "V", 'V');
+        ftoc_one(c, l, "W", "W", 'W');
+        ftoc_one(c, l, "P", "P", 'P');
+    }
+    const char* vuvw[3] = {"U", "V", "W"};
+    const char* sp[3] = {"P", nullptr, nullptr};
+    for (int l = c.minlevel; l <= c.maxlevel; ++l) {
+        parent(c, l, vuvw, sp, false);
+        bound_flow(c, U, V, W, P, l);
+        connect(c, l, 2, U, V, W, P, nullptr, nullptr, true, false, 0);
+    }
     if (st) {
         st->ipc = ipc;
         st->nouter_done = ipcount_done;
@@ -2029,7 +2064,19 @@ bool check_supported(const Ctx& c) {
 struct oracle_ctx : Ctx {};
 
 namespace {
-// the restated stage and pressure solve are single-level: no PAR faces
+// the pressure solve runs on hierarchies once their parents are known; the
+// ghost-cell restriction (gc_restrict_mod.F90) is not restated
+int hierarchy_ready(const Ctx& c) {
+    for (int g = 1; g <= c.ngrid; ++g) {
+        if (c.g[g].level == c.minlevel) continue;
+        if (!c.iparent[g]) return fail(MGLET_ERR_ARG, "oracle: a fine grid without parent (set_hierarchy)");
+    }
+    if (c.minlevel != c.maxlevel && c.ibtype == 1)
+        return fail(MGLET_ERR_UNSUPPORTED, "oracle: the ghost-cell restriction is not restated");
+    return 0;
+}
+
+// the restated stage is single-level: no PAR faces (tstle4_par is not restated)
 int single_level_stage(const Ctx& c) {
     if (c.minlevel != c.maxlevel)
         return fail(MGLET_ERR_UNSUPPORTED, "oracle: the multi-level stage is not restated");
@@ -2249,7 +2296,7 @@ int oracle_laplacephi(oracle_ctx* c, const char* res, const char* phi) {
 
 int oracle_mgpoisl(oracle_ctx* c, double dt, int ittot, int irk, mglet_stage_stats* st) {
     (void)ittot; (void)irk;
-    if (int rc = single_level_stage(*c)) return rc;
+    if (int rc = hierarchy_ready(*c)) return rc;
     mgpoisl(*c, dt, st);
     return 0;
 }

@@ -6,7 +6,7 @@ import numpy as np
 import pytest
 
 from mglet_gb300 import abi, cases
-from test_oracle_levels import _buf_shape, _fine, _random_bp
+from test_oracle_levels import _buf_shape, _fine, _random_bp, prepare_levels
 
 pytestmark = pytest.mark.gpu
 
@@ -107,7 +107,31 @@ def test_bound_flow_par(gpu_lib, oracle_lib, h, blocked):
         assert np.array_equal(gs.get(n), o.get(n)), n
 
 
+@pytest.mark.parametrize("h", HIERARCHIES)
+@pytest.mark.parametrize("psolver", [abi.PSOLVER_SIP, abi.PSOLVER_SOR])
+def test_multilevel_mgpoisl_bit_exact(gpu_lib, oracle_lib, h, psolver):
+    """The pressure solve over both levels, six outer iterations fixed, after
+    the calls that precede it in the stage; every field bit for bit."""
+    case = cases.refined_box(h["nx"], h["ny"], h["nz"], n=h["n"], refine=h["refine"])
+    prm = abi.make_flow_params(gmol=1e-2, epcorr=1e-12, nouter=6, ninner=5, nouter_min=6,
+                               psolver=psolver)
+    gs, o = gpu_lib.Solver(case, prm), oracle_lib.Oracle(case, prm)
+    rng = np.random.default_rng(17)
+    _set((gs, o), {n: rng.standard_normal(case.idim3d) for n in "UVWP"})
+    for s in (gs, o):
+        s.set_hierarchy(case.iparent, case.position)
+        for lvl in (1, 2):
+            s.connect(lvl, 2, v1="U", v2="V", v3="W", s1="P", corners=True)
+        prepare_levels(s, case)
+    sg, so = gs.mgpoisl(2e-3), o.mgpoisl(2e-3)
+    assert (sg.ipc, sg.nouter_done) == (so.ipc, so.nouter_done) == (30, 6)
+    assert sg.maxrhs == so.maxrhs
+    for n in ("U", "V", "W", "P", "DP"):
+        assert np.array_equal(gs.get(n), o.get(n)), n
+
+
 def test_stage_refuses_hierarchies(gpu_lib, oracle_lib):
+    from oracle.binding import rk_scheme
     case, gs, o = _pair(gpu_lib, oracle_lib, HIERARCHIES[0])
     with pytest.raises(gpu_lib.MgletError):
-        gs.mgpoisl(1e-3)
+        gs.timeintegrate_flow(1, 1, 0.0, 1e-3, 1, rk_scheme("williamson"))
