@@ -146,6 +146,44 @@ MODULE mglet_gpu_mod
             INTEGER(c_int32_t), VALUE :: comp_new
         END FUNCTION mglet_gpu_setpointvalues
 
+        INTEGER(c_int) FUNCTION mglet_gpu_set_hierarchy(ctx, iparent, position) &
+                BIND(C, name="mglet_gpu_set_hierarchy")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), INTENT(in) :: iparent(*), position(*)
+        END FUNCTION mglet_gpu_set_hierarchy
+
+        INTEGER(c_int) FUNCTION mglet_gpu_parent(ctx, ilevel, v1, v2, v3, s1, s2, s3, normal) &
+                BIND(C, name="mglet_gpu_parent")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: ilevel, normal
+            TYPE(c_ptr), VALUE :: v1, v2, v3, s1, s2, s3    ! C strings or C_NULL_PTR
+        END FUNCTION mglet_gpu_parent
+
+        INTEGER(c_int) FUNCTION mglet_gpu_ftoc(ctx, ilevel, ff, fc, flag) BIND(C, name="mglet_gpu_ftoc")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_char
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: ilevel
+            CHARACTER(kind=c_char), INTENT(in) :: ff(*), fc(*)
+            CHARACTER(kind=c_char), VALUE :: flag
+        END FUNCTION mglet_gpu_ftoc
+
+        INTEGER(c_int) FUNCTION mglet_gpu_ctof(ctx, ilevel, ff, fc) BIND(C, name="mglet_gpu_ctof")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_char
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: ilevel
+            CHARACTER(kind=c_char), INTENT(in) :: ff(*), fc(*)
+        END FUNCTION mglet_gpu_ctof
+
+        INTEGER(c_int) FUNCTION mglet_gpu_bound_pressure(ctx, ilevel, dp, with_bp) &
+                BIND(C, name="mglet_gpu_bound_pressure")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_char
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: ilevel, with_bp
+            CHARACTER(kind=c_char), INTENT(in) :: dp(*)
+        END FUNCTION mglet_gpu_bound_pressure
+
         INTEGER(c_int) FUNCTION mglet_gpu_itinfo(ctx, dt, out) BIND(C, name="mglet_gpu_itinfo")
             IMPORT :: c_int, c_ptr, c_double, mglet_itinfo
             TYPE(c_ptr), VALUE :: ctx
@@ -160,7 +198,8 @@ MODULE mglet_gpu_mod
     PUBLIC :: mglet_grid_desc, mglet_flow_params, mglet_rk_scheme, mglet_stage_stats, &
         mglet_itinfo, gpu_init, gpu_finish, gpu_upload, gpu_download, &
         gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf, &
-        gpu_upload_stencils, gpu_start_ghostcell
+        gpu_upload_stencils, gpu_start_ghostcell, gpu_set_hierarchy, gpu_ftoc, gpu_ctof, &
+        gpu_bound_pressure
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -212,6 +251,42 @@ CONTAINS
         IF (mglet_gpu_set_bc_real(gctx, INT(igrid, c_int32_t), INT(iface, c_int32_t), pinf) /= 0) &
             CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_set_pinf
+
+    ! The grid hierarchy (gridinfo%iparent, i/j/kposition of every grid):
+    ! needed before gpu_parent, gpu_ftoc, gpu_ctof and a multi-level mgpoisl.
+    SUBROUTINE gpu_set_hierarchy(iparent, position)
+        INTEGER(c_int32_t), INTENT(in) :: iparent(:), position(:, :)   ! position(3, ngrid)
+        IF (mglet_gpu_set_hierarchy(gctx, iparent, position) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_set_hierarchy
+
+    ! Drop-in for ftoc(ilevel, ff, fc, flag) on the device copies
+    SUBROUTINE gpu_ftoc(ilevel, ff, fc, flag)
+        INTEGER, INTENT(in) :: ilevel
+        CHARACTER(len=*), INTENT(in) :: ff, fc
+        CHARACTER(len=1), INTENT(in) :: flag
+        IF (mglet_gpu_ftoc(gctx, INT(ilevel, c_int32_t), TRIM(ff)//C_NULL_CHAR, &
+            TRIM(fc)//C_NULL_CHAR, flag) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_ftoc
+
+    ! Drop-in for ctof(ilevel, ff, fc) on the device copies
+    SUBROUTINE gpu_ctof(ilevel, ff, fc)
+        INTEGER, INTENT(in) :: ilevel
+        CHARACTER(len=*), INTENT(in) :: ff, fc
+        IF (mglet_gpu_ctof(gctx, INT(ilevel, c_int32_t), TRIM(ff)//C_NULL_CHAR, &
+            TRIM(fc)//C_NULL_CHAR) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_ctof
+
+    ! Drop-in for bound_pressure(ilevel, dp[, bp]) on the device copies
+    SUBROUTINE gpu_bound_pressure(ilevel, dp, with_bp)
+        INTEGER, INTENT(in) :: ilevel
+        CHARACTER(len=*), INTENT(in) :: dp
+        LOGICAL, INTENT(in) :: with_bp
+        INTEGER(c_int32_t) :: wb
+        wb = 0
+        IF (with_bp) wb = 1
+        IF (mglet_gpu_bound_pressure(gctx, INT(ilevel, c_int32_t), TRIM(dp)//C_NULL_CHAR, wb) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_bound_pressure
 
     ! Ghost-cell lists of one grid and component (the uxpoli/uxpolr/uxpolrvel,
     ! .., fxpoli/fxpolr arrays of gc_flowstencils_mod after
