@@ -171,15 +171,17 @@ int mglet_gpu_get_field(mglet_ctx* ctx, const char* name, double* host, int64_t 
 
 /* ---- The RK stage ---------------------------------------------------------
  * Replaces timeintegrate_flow (src/flow/timeintegration_mod.F90:22-142) for
- * ib type "noib": tstle4 -> rkstep(u,v,w) -> connect(1, normal, forward=1)
- * -> mgpoisl.  stats may be NULL. */
+ * ib types "noib" and "ghostcell": tstle4 -> rkstep(u,v,w) -> per level
+ * connect(1, normal, forward=1), parent(u,v,w,p), bound_flow -> mgpoisl.
+ * stats may be NULL. */
 int mglet_gpu_timeintegrate_flow(mglet_ctx* ctx, int32_t itstep, int32_t ittot,
                                  double timeph, double dt, int32_t irk,
                                  const mglet_rk_scheme* rk, mglet_stage_stats* stats);
 
 /* ---- Module-level drop-ins ------------------------------------------------
  * tstle4(uo,vo,wo,u,v,w,u,v,w,p,g) (src/flow/tstle4_mod.F90:13-120):
- * writes the device fields UO, VO, WO. */
+ * kon, diff, gradp and, on grids with PAR faces, tstle4_par; writes the
+ * device fields UO, VO, WO. */
 int mglet_gpu_tstle4(mglet_ctx* ctx);
 /* rkstep(p, dp, rhsp, frhs, dtfu) over the whole flat arrays
  * (src/core/rungekutta_mod.F90:315-333); arguments are field names. */
@@ -224,11 +226,15 @@ int mglet_gpu_get_buffer(mglet_ctx* ctx, const char* name, int32_t igrid, int32_
                          double* host, int64_t n);
 
 /* ---- Grid hierarchies (more than one level, PAR faces) -------------------
- * A context may hold several levels with PAR (code 8) faces; these
- * module-level drop-ins then run on it, level by level as the reference
- * calls them.  mglet_gpu_timeintegrate_flow and mglet_gpu_mgpoisl refuse
- * such contexts (MGLET_ERR_UNSUPPORTED): the multi-level schedule of the
- * stage and tstle4_par are not part of this library.
+ * A context may hold several levels with PAR (code 8) faces (plain form
+ * only; the mixed form runs one level).  These module-level drop-ins then
+ * run on it, level by level as the reference calls them; mglet_gpu_tstle4
+ * adds tstle4_par on PAR faces (src/flow/tstle4_mod.F90:532-1753), and
+ * mglet_gpu_mgpoisl and mglet_gpu_timeintegrate_flow run the multi-level
+ * schedule (per level connect, parent and bound_flow before the pressure
+ * solve, timeintegration_mod.F90:117-122).  Both need the hierarchy set;
+ * ghost-cell contexts with more than one level are refused
+ * (MGLET_ERR_UNSUPPORTED): the ghost-cell restriction is not built.
  *
  * gridinfo%iparent and i/j/kposition (src/core/grids_mod.F90:768-781):
  * iparent[g] the 1-based parent of grid g+1 (0 = none, one level coarser),

@@ -433,17 +433,6 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
     return 0;
 }
 
-// The stage driver is built for one grid level without PAR faces:
-// tstle4_par (the PAR face fluxes of tstle4) is not part of this library.
-int single_level_stage(Ctx* c) {
-    if (c->minlevel != c->maxlevel)
-        return fail(MGLET_ERR_UNSUPPORTED, "the multi-level stage is not built; use the level operators");
-    for (int f = 0; f < 6; ++f)
-        if (!c->pgrids[f].empty())
-            return fail(MGLET_ERR_UNSUPPORTED, "PAR faces need the multi-level stage, which is not built");
-    return 0;
-}
-
 // The pressure solve runs on hierarchies once the parents are known; the
 // ghost-cell restriction (gc_restrict_mod.F90) is not built.
 int hierarchy_ready(Ctx* c) {
@@ -491,10 +480,15 @@ static int stage_plain(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk,
         if (int rc = launch_maskbp(c, U, V, W, P)) return rc;
         if (int rc = launch_gc_mode(c, 'R', U, V, W)) return rc;
     }
-    // timeintegration_mod.F90:116-121: connect (normal, forward), bound
+    // timeintegration_mod.F90:117-122: per level connect (normal, forward),
+    // parent (u, v, w, p into the PAR buffers) and bound_flow
+    static const char* const vn[3] = {"U", "V", "W"};
+    static const char* const sn[3] = {"P", nullptr, nullptr};
     for (int l = c->minlevel; l <= c->maxlevel; ++l) {
         if (int rc = connect(c, l, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
-        if (int rc = launch_bound_flow(c, U, V, W, P)) return rc;
+        if (c->minlevel != c->maxlevel)
+            if (int rc = launch_parent(c, l, vn, sn, false)) return rc;
+        if (int rc = launch_bound_flow(c, U, V, W, P, c->minlevel != c->maxlevel ? l : 0)) return rc;
     }
     if (int rc = mgpoisl(c, dtrk * dt, st)) return rc;
     if (gc) return gc_setpointvalues(c, irk == rk->nrk);   // :131-134
@@ -502,7 +496,7 @@ static int stage_plain(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk,
 }
 
 int timeintegrate(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st) {
-    if (int rc = single_level_stage(c)) return rc;
+    if (int rc = hierarchy_ready(c)) return rc;
     if (c->prm.form == MGLET_FORM_MIXED) return mixed_stage(c, dt, irk, rk, st);
     return stage_plain(c, dt, irk, rk, st);
 }
@@ -659,8 +653,8 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
         if (it == shapes.end()) shapes.push_back(key);
     }
     // hierarchies: the level operators (parent, ftoc, ctof, bound_pressure,
-    // bound_flow on PAR faces) and every per-level module procedure work;
-    // the stage driver and mgpoisl refuse them (single_level_stage)
+    // bound_flow on PAR faces), tstle4 with tstle4_par, mgpoisl and the
+    // stage run on them in the plain form
     if (c->minlevel != c->maxlevel && prm->form == MGLET_FORM_MIXED)
         return bail(fail(MGLET_ERR_UNSUPPORTED, "create: the mixed form runs one grid level"));
     c->uniform = shapes.size() == 1;
@@ -754,6 +748,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     for (auto& kv : c->d_children) cudaFree(kv.second);
     for (auto& kv : c->fbuf) cudaFree(kv.second);
     cudaFree(c->d_hier);
+    cudaFree(c->d_pargrids);
     cudaFree(c->d_gridred);
     cudaFree(c->d_scalar);
     if (c->h_scalar) cudaFreeHost(c->h_scalar);

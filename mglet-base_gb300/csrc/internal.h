@@ -147,6 +147,8 @@ struct Ctx {
     std::map<int, int*> d_children;
     std::vector<int> pgrids[6];
     int* d_pgrids[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    int* d_pargrids = nullptr;                  // grids with any PAR face (tstle4_par)
+    int npargrids = 0;
     std::map<int, std::vector<int>> plist[6];   // per level: grids with a parent and PAR on the face
     std::map<int, int*> d_plist[6];
     std::map<std::string, double*> fbuf;
@@ -235,6 +237,9 @@ int level_init(Ctx* c);                      // PAR face lists (create)
 int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos);
 double* field_buffer(Ctx* c, const std::string& name);   // boundary buffers of a field
 int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w);
+// tstle4_par on every grid with a PAR face, after kon, diff and gradp
+int launch_tstle4_par(Ctx* c, double* uo, double* vo, double* wo, const double* u, const double* v,
+                      const double* w, const double* ut, const double* vt, const double* wt);
 int launch_parent(Ctx* c, int ilevel, const char* const v[3], const char* const s[3], bool normal);
 int launch_ftoc(Ctx* c, int ilevel, const double* ff, double* fc, char flag);
 int launch_ctof(Ctx* c, int ilevel, double* ff, const double* fc);

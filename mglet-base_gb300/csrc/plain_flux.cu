@@ -276,7 +276,8 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
                                           c->prm.gmol, c->prm.rho, c->prm.gradp[0],
                                           c->prm.gradp[1], c->prm.gradp[2]);
     MG_LAUNCHED(c);
-    return 0;
+    // tstle4_mod.F90:114: tstle4_par after kon, diff and gradp (PAR faces)
+    return launch_tstle4_par(c, uo, vo, wo, u, v, w, ut, vt, wt);
 }
 
 int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu) {

@@ -382,6 +382,377 @@ __global__ void k_ctof(const DevGrid* __restrict__ grids, const int4* __restrict
     ff[G.ip3 + q] = fc[P.ip3 + (long long)(ic - 1) * P.kk * P.jj + (long long)(jc - 1) * P.kk + (kc - 1)];
 }
 
+
+// ---- tstle4_par (tstle4_mod.F90:532-1753) --------------------------------
+// One CTA per grid with a PAR face, the reference's blocks in its order
+// (upwind front, back, right, left, bottom, top; then the momentum-
+// conserving fluxes back, front, top, bottom, left, right), each block's
+// loop nests spread over the threads and closed by __syncthreads.  The
+// work arrays of one block are two planes in shared memory: S the standard
+// flux (the reference's wc*(..., i+-1) plane), N the flux of the coarse
+// velocities and its interpolation (the wc*(..., i) plane).
+struct ParFluxArgs {
+    const DevGrid* grids;
+    const int* list;
+    double *uo, *vo, *wo;
+    const double *u, *v, *w, *ut, *vt, *wt;
+    const double *dx, *dy, *dz, *ddx, *ddy, *ddz, *rdx, *rdy, *rdz, *rddx, *rddy, *rddz;
+};
+
+// a flattened loop over a in [alo, ahi] step sa (outer) and b in [blo, bhi]
+// step sb (inner), then the block barrier
+#define PAR_LOOP2(a, alo, ahi, sa, b, blo, bhi, sb, ...)                                       \
+    {                                                                                           \
+        const int na_ = (ahi) >= (alo) ? ((ahi) - (alo)) / (sa) + 1 : 0;                        \
+        const int nb_ = (bhi) >= (blo) ? ((bhi) - (blo)) / (sb) + 1 : 0;                        \
+        for (int q_ = threadIdx.x; q_ < na_ * nb_; q_ += blockDim.x) {                          \
+            const int a = (alo) + (q_ / nb_) * (sa);                                            \
+            const int b = (blo) + (q_ % nb_) * (sb);                                            \
+            __VA_ARGS__                                                                         \
+        }                                                                                       \
+        __syncthreads();                                                                        \
+    }
+
+__global__ void k_tstle4_par(ParFluxArgs A) {
+    extern __shared__ double psm2[];
+    const int g = A.list[blockIdx.x];
+    const DevGrid G = A.grids[g];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int nfro = G.bc[0], nbac = G.bc[1], nrgt = G.bc[2], nlft = G.bc[3], nbot = G.bc[4],
+              ntop = G.bc[5];
+    const long long o = G.ip3;
+    double *uo = A.uo + o, *vo = A.vo + o, *wo = A.wo + o;
+    const double *u = A.u + o, *v = A.v + o, *w = A.w + o;
+    const double *ut = A.ut + o, *vt = A.vt + o, *wt = A.wt + o;
+    const double *dx = A.dx + G.ipx - 1, *dy = A.dy + G.ipy - 1, *dz = A.dz + G.ipz - 1;
+    const double *ddx = A.ddx + G.ipx - 1, *ddy = A.ddy + G.ipy - 1, *ddz = A.ddz + G.ipz - 1;
+    const double *rdx = A.rdx + G.ipx - 1, *rdy = A.rdy + G.ipy - 1, *rdz = A.rdz + G.ipz - 1;
+    const double *rddx = A.rddx + G.ipx - 1, *rddy = A.rddy + G.ipy - 1, *rddz = A.rddz + G.ipz - 1;
+    const int pl = max(kk * jj, max(kk * ii, jj * ii));
+    double* S = psm2;
+    double* N = psm2 + pl;
+    const double wkon = 1.0;
+    auto X = [&](int k, int j, int i) -> long long {
+        return (long long)(i - 1) * kk * jj + (long long)(j - 1) * kk + (k - 1);
+    };
+#define F3(a, k, j, i) a[X(k, j, i)]
+    // planes: x faces (k, j), z faces (j, i), y faces (k, i)
+    auto PX = [&](int k, int j) { return (k - 1) + (j - 1) * kk; };
+    auto PZ = [&](int j, int i) { return (j - 1) + (i - 1) * jj; };
+    auto PY = [&](int k, int i) { return (k - 1) + (i - 1) * kk; };
+
+    // ---- upwind in the second-to-last layer
+    if (nfro == 8) {
+        const int i = 4;
+        PAR_LOOP2(j, 3, jj - 2, 1, k, 3, kk - 2, 1, {
+            const double dyj = dy[j], ddyj = ddy[j];
+            const double fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            const double fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            const double dzk = dz[k], rdzk = rdz[k], ddzk = ddz[k], rddzk = rddz[k];
+            const double avx = dyj * ddzk, awx = ddyj * dzk;
+            const double fvw = avx * (F3(ut, k, j, i - 1) + F3(ut, k, j + 1, i - 1)) * 0.5;
+            const double qv = 0.5 * (fvw - fabs(fvw)) *
+                              (0.5 * F3(v, k, j, i) - 1.5 * F3(v, k, j, i - 1) + F3(v, k, j, i - 2)) * 0.5 * 0.5;
+            F3(vo, k, j, i) = F3(vo, k, j, i) + fkdtv * rddzk * (-qv);
+            F3(vo, k, j, i - 1) = F3(vo, k, j, i - 1) + fkdtv * rddzk * (+qv);
+            const double fww = awx * (F3(ut, k, j, i - 1) + F3(ut, k + 1, j, i - 1)) * 0.5;
+            const double qw = 0.5 * (fww - fabs(fww)) *
+                              (0.5 * F3(w, k, j, i) - 1.5 * F3(w, k, j, i - 1) + F3(w, k, j, i - 2)) * 0.5 * 0.5;
+            F3(wo, k, j, i) = F3(wo, k, j, i) + fkdtw * rdzk * (-qw);
+            F3(wo, k, j, i - 1) = F3(wo, k, j, i - 1) + fkdtw * rdzk * (+qw);
+        })
+    }
+    if (nbac == 8) {
+        const int i = ii - 2;
+        PAR_LOOP2(j, 3, jj - 2, 1, k, 3, kk - 2, 1, {
+            const double dyj = dy[j], ddyj = ddy[j];
+            const double fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            const double fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            const double dzk = dz[k], rdzk = rdz[k], ddzk = ddz[k], rddzk = rddz[k];
+            const double avx = dyj * ddzk, awx = ddyj * dzk;
+            const double fvw = avx * (F3(ut, k, j, i - 1) + F3(ut, k, j + 1, i - 1)) * 0.5;
+            const double qv = 0.5 * (fvw + fabs(fvw)) *
+                              (0.5 * F3(v, k, j, i - 1) - 1.5 * F3(v, k, j, i) + F3(v, k, j, i + 1)) * 0.5 * 0.5;
+            F3(vo, k, j, i) = F3(vo, k, j, i) + fkdtv * rddzk * (-qv);
+            F3(vo, k, j, i - 1) = F3(vo, k, j, i - 1) + fkdtv * rddzk * (+qv);
+            const double fww = awx * (F3(ut, k, j, i - 1) + F3(ut, k + 1, j, i - 1)) * 0.5;
+            const double qw = 0.5 * (fww + fabs(fww)) *
+                              (0.5 * F3(w, k, j, i - 1) - 1.5 * F3(w, k, j, i) + F3(w, k, j, i + 1)) * 0.5 * 0.5;
+            F3(wo, k, j, i) = F3(wo, k, j, i) + fkdtw * rdzk * (-qw);
+            F3(wo, k, j, i - 1) = F3(wo, k, j, i - 1) + fkdtw * rdzk * (+qw);
+        })
+    }
+    if (nrgt == 8 || nlft == 8) {
+        for (int side = 0; side < 2; ++side) {
+            const bool lft = side == 1;
+            if ((lft ? nlft : nrgt) != 8) continue;
+            const int j = lft ? jj - 2 : 4;
+            PAR_LOOP2(i, 3, ii - 2, 1, k, 3, kk - 2, 1, {
+                const double dxi = dx[i], ddxi = ddx[i];
+                const double fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+                const double fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+                const double dzk = dz[k], rdzk = rdz[k], ddzk = ddz[k], rddzk = rddz[k];
+                const double auy = dxi * ddzk, awy = ddxi * dzk;
+                const double fus = auy * (F3(vt, k, j - 1, i) + F3(vt, k, j - 1, i + 1)) * 0.5;
+                const double qu = lft ? 0.5 * (fus + fabs(fus)) *
+                                            (0.5 * F3(u, k, j - 1, i) - 1.5 * F3(u, k, j, i) + F3(u, k, j + 1, i)) * 0.5 * 0.5
+                                      : 0.5 * (fus - fabs(fus)) *
+                                            (0.5 * F3(u, k, j, i) - 1.5 * F3(u, k, j - 1, i) + F3(u, k, j - 2, i)) * 0.5 * 0.5;
+                F3(uo, k, j, i) = F3(uo, k, j, i) + fkdtu * rddzk * (-qu);
+                F3(uo, k, j - 1, i) = F3(uo, k, j - 1, i) + fkdtu * rddzk * (+qu);
+                const double fws = awy * (F3(vt, k, j - 1, i) + F3(vt, k + 1, j - 1, i)) * 0.5;
+                const double qw = lft ? 0.5 * (fws + fabs(fws)) *
+                                            (0.5 * F3(w, k, j - 1, i) - 1.5 * F3(w, k, j, i) + F3(w, k, j + 1, i)) * 0.5 * 0.5
+                                      : 0.5 * (fws - fabs(fws)) *
+                                            (0.5 * F3(w, k, j, i) - 1.5 * F3(w, k, j - 1, i) + F3(w, k, j - 2, i)) * 0.5 * 0.5;
+                F3(wo, k, j, i) = F3(wo, k, j, i) + fkdtw * rdzk * (-qw);
+                F3(wo, k, j - 1, i) = F3(wo, k, j - 1, i) + fkdtw * rdzk * (+qw);
+            })
+        }
+    }
+    for (int side = 0; side < 2; ++side) {
+        const bool top = side == 1;
+        if ((top ? ntop : nbot) != 8) continue;
+        const int k = top ? kk - 2 : 4;
+        PAR_LOOP2(i, 3, ii - 2, 1, j, 3, jj - 2, 1, {
+            const double dxi = dx[i], ddxi = ddx[i];
+            const double fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+            const double fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            const double dyj = dy[j], ddyj = ddy[j];
+            const double auz = dxi * ddyj, avz = ddxi * dyj;
+            const double rddzk = rddz[k];
+            const double fub = auz * (F3(wt, k - 1, j, i) + F3(wt, k - 1, j, i + 1)) * 0.5;
+            const double qu = top ? 0.5 * (fub + fabs(fub)) *
+                                        (0.5 * F3(u, k - 1, j, i) - 1.5 * F3(u, k, j, i) + F3(u, k + 1, j, i)) * 0.5 * 0.5
+                                  : 0.5 * (fub - fabs(fub)) *
+                                        (0.5 * F3(u, k, j, i) - 1.5 * F3(u, k - 1, j, i) + F3(u, k - 2, j, i)) * 0.5 * 0.5;
+            F3(uo, k, j, i) = F3(uo, k, j, i) + fkdtu * rddzk * (-qu);
+            F3(uo, k - 1, j, i) = F3(uo, k - 1, j, i) + fkdtu * rddzk * (+qu);
+            const double fvb = avz * (F3(wt, k - 1, j, i) + F3(wt, k - 1, j + 1, i)) * 0.5;
+            const double qv = top ? 0.5 * (fvb + fabs(fvb)) *
+                                        (0.5 * F3(v, k - 1, j, i) - 1.5 * F3(v, k, j, i) + F3(v, k + 1, j, i)) * 0.5 * 0.5
+                                  : 0.5 * (fvb - fabs(fvb)) *
+                                        (0.5 * F3(v, k, j, i) - 1.5 * F3(v, k - 1, j, i) + F3(v, k - 2, j, i)) * 0.5 * 0.5;
+            F3(vo, k, j, i) = F3(vo, k, j, i) + fkdtv * rddzk * (-qv);
+            F3(vo, k - 1, j, i) = F3(vo, k - 1, j, i) + fkdtv * rddzk * (+qv);
+        })
+    }
+
+    // ---- BACK and FRONT (x faces): w cell, then v cell; e = +1 back
+    for (int side = 0; side < 2; ++side) {
+        const bool back = side == 0;
+        if ((back ? nbac : nfro) != 8) continue;
+        const int i = back ? ii - 2 : 3;
+        const int it = back ? i : i - 1;          // ut plane
+        const int iw = back ? i + 1 : i - 1;      // the other w/v plane of the flux
+        // w cell
+        PAR_LOOP2(j, 3, jj - 2, 1, k, 2, kk - 2, 1, {
+            const double awx = ddy[j] * dz[k];
+            const double f = awx * (F3(ut, k, j, it) + F3(ut, k + 1, j, it)) * 0.5;
+            S[PX(k, j)] = 0.5 * f * (F3(w, k, j, i) + F3(w, k, j, iw));
+        })
+        PAR_LOOP2(j, 3, jj - 2, 2, k, 2, kk - 2, 2, {
+            const double awx = ddy[j] * dz[k];
+            double f;
+            if (k == 2)
+                f = awx * (2 * F3(ut, k, j, it) + 2 * F3(ut, k, j + 1, it) + F3(ut, k + 1, j, it) +
+                           F3(ut, k + 1, j + 1, it) + F3(ut, k + 2, j, it) + F3(ut, k + 2, j + 1, it)) * 0.125;
+            else if (k == kk - 2)
+                f = awx * (F3(ut, k - 1, j, it) + F3(ut, k - 1, j + 1, it) + F3(ut, k, j, it) + F3(ut, k, j + 1, it) +
+                           2 * F3(ut, k + 1, j, it) + 2 * F3(ut, k + 1, j + 1, it)) * 0.125;
+            else
+                f = awx * (F3(ut, k - 1, j, it) + F3(ut, k - 1, j + 1, it) + F3(ut, k, j, it) + F3(ut, k, j + 1, it) +
+                           F3(ut, k + 1, j, it) + F3(ut, k + 1, j + 1, it) + F3(ut, k + 2, j, it) +
+                           F3(ut, k + 2, j + 1, it)) * 0.125;
+            N[PX(k, j)] = 0.5 * f * (F3(w, k, j, i) + F3(w, k, j, iw));
+            N[PX(k, j + 1)] = 0.5 * f * (F3(w, k, j + 1, i) + F3(w, k, j + 1, iw));
+        })
+        PAR_LOOP2(j, 3, jj - 2, 1, k, 2, kk - 4, 2, { N[PX(k + 1, j)] = 0.5 * (N[PX(k, j)] + N[PX(k + 2, j)]); })
+        PAR_LOOP2(j, 3, jj - 2, 1, k, 2, kk - 2, 1, {
+            const double fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            const double rdzk = rdz[k];
+            if (back)
+                F3(wo, k, j, i) = F3(wo, k, j, i) + fkdtw * rdzk * (-S[PX(k, j)] + N[PX(k, j)]);
+            else
+                F3(wo, k, j, i) = F3(wo, k, j, i) + fkdtw * rdzk * (S[PX(k, j)] - N[PX(k, j)]);
+        })
+        // v cell
+        PAR_LOOP2(j, 2, jj - 2, 1, k, 3, kk - 2, 1, {
+            const double avx = ddz[k] * dy[j];
+            const double f = avx * (F3(ut, k, j, it) + F3(ut, k, j + 1, it)) * 0.5;
+            S[PX(k, j)] = 0.5 * f * (F3(v, k, j, i) + F3(v, k, j, iw));
+        })
+        PAR_LOOP2(j, 2, jj - 2, 2, k, 3, kk - 2, 2, {
+            const double avx = ddz[k] * dy[j];
+            double f;
+            if (j == 2)
+                f = avx * (2 * F3(ut, k, j, it) + 2 * F3(ut, k + 1, j, it) + F3(ut, k, j + 1, it) +
+                           F3(ut, k + 1, j + 1, it) + F3(ut, k, j + 2, it) + F3(ut, k + 1, j + 2, it)) * 0.125;
+            else if (j == jj - 2)
+                f = avx * (F3(ut, k, j - 1, it) + F3(ut, k + 1, j - 1, it) + F3(ut, k, j, it) + F3(ut, k + 1, j, it) +
+                           2 * F3(ut, k, j + 1, it) + 2 * F3(ut, k + 1, j + 1, it)) * 0.125;
+            else
+                f = avx * (F3(ut, k, j - 1, it) + F3(ut, k + 1, j - 1, it) + F3(ut, k, j, it) + F3(ut, k + 1, j, it) +
+                           F3(ut, k, j + 1, it) + F3(ut, k + 1, j + 1, it) + F3(ut, k, j + 2, it) +
+                           F3(ut, k + 1, j + 2, it)) * 0.125;
+            N[PX(k, j)] = 0.5 * f * (F3(v, k, j, i) + F3(v, k, j, iw));
+            N[PX(k + 1, j)] = 0.5 * f * (F3(v, k + 1, j, i) + F3(v, k + 1, j, iw));
+        })
+        PAR_LOOP2(j, 2, jj - 4, 2, k, 3, kk - 2, 1, { N[PX(k, j + 1)] = 0.5 * (N[PX(k, j)] + N[PX(k, j + 2)]); })
+        PAR_LOOP2(j, 2, jj - 2, 1, k, 3, kk - 2, 1, {
+            const double fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            const double rddzk = rddz[k];
+            if (back)
+                F3(vo, k, j, i) = F3(vo, k, j, i) + fkdtv * rddzk * (N[PX(k, j)] - S[PX(k, j)]);
+            else
+                F3(vo, k, j, i) = F3(vo, k, j, i) + fkdtv * rddzk * (-N[PX(k, j)] + S[PX(k, j)]);
+        })
+    }
+
+    // ---- TOP and BOTTOM (z faces): u cell, then v cell
+    for (int side = 0; side < 2; ++side) {
+        const bool top = side == 0;
+        if ((top ? ntop : nbot) != 8) continue;
+        const int k = top ? kk - 2 : 3;
+        const int kw = top ? k : k - 1;
+        const int kn = top ? k + 1 : k - 1;
+        PAR_LOOP2(i, 2, ii - 2, 1, j, 3, jj - 2, 1, {
+            const double auz = dx[i] * ddy[j];
+            const double f = auz * (F3(wt, kw, j, i) + F3(wt, kw, j, i + 1)) * 0.5;
+            S[PZ(j, i)] = 0.5 * f * (F3(u, k, j, i) + F3(u, kn, j, i));
+        })
+        PAR_LOOP2(i, 2, ii - 2, 2, j, 3, jj - 2, 2, {
+            const double auz = dx[i] * ddy[j];
+            double f;
+            if (i == 2)
+                f = auz * (2 * F3(wt, kw, j, i) + 2 * F3(wt, kw, j + 1, i) + F3(wt, kw, j, i + 1) +
+                           F3(wt, kw, j + 1, i + 1) + F3(wt, kw, j, i + 2) + F3(wt, kw, j + 1, i + 2)) * 0.125;
+            else if (i == ii - 2)
+                f = auz * (F3(wt, kw, j, i - 1) + F3(wt, kw, j + 1, i - 1) + F3(wt, kw, j, i) + F3(wt, kw, j + 1, i) +
+                           2 * F3(wt, kw, j, i + 1) + 2 * F3(wt, kw, j + 1, i + 1)) * 0.125;
+            else
+                f = auz * (F3(wt, kw, j, i - 1) + F3(wt, kw, j + 1, i - 1) + F3(wt, kw, j, i) + F3(wt, kw, j + 1, i) +
+                           F3(wt, kw, j, i + 1) + F3(wt, kw, j + 1, i + 1) + F3(wt, kw, j, i + 2) +
+                           F3(wt, kw, j + 1, i + 2)) * 0.125;
+            N[PZ(j, i)] = 0.5 * f * (F3(u, k, j, i) + F3(u, kn, j, i));
+            N[PZ(j + 1, i)] = 0.5 * f * (F3(u, k, j + 1, i) + F3(u, kn, j + 1, i));
+        })
+        PAR_LOOP2(i, 2, ii - 4, 2, j, 3, jj - 2, 1, { N[PZ(j, i + 1)] = 0.5 * (N[PZ(j, i)] + N[PZ(j, i + 2)]); })
+        PAR_LOOP2(i, 2, ii - 2, 1, j, 3, jj - 2, 1, {
+            const double fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+            const double rddzk = rddz[k];
+            if (top)
+                F3(uo, k, j, i) = F3(uo, k, j, i) + fkdtu * rddzk * (N[PZ(j, i)] - S[PZ(j, i)]);
+            else
+                F3(uo, k, j, i) = F3(uo, k, j, i) + fkdtu * rddzk * (-N[PZ(j, i)] + S[PZ(j, i)]);
+        })
+        PAR_LOOP2(i, 3, ii - 2, 1, j, 2, jj - 2, 1, {
+            const double avz = ddx[i] * dy[j];
+            const double f = avz * (F3(wt, kw, j, i) + F3(wt, kw, j + 1, i)) * 0.5;
+            S[PZ(j, i)] = 0.5 * f * (F3(v, k, j, i) + F3(v, kn, j, i));
+        })
+        PAR_LOOP2(i, 3, ii - 2, 2, j, 2, jj - 2, 2, {
+            const double avz = ddx[i] * dy[j];
+            double f;
+            if (j == 2)
+                f = avz * (2 * F3(wt, kw, j, i) + 2 * F3(wt, kw, j, i + 1) + F3(wt, kw, j + 1, i) +
+                           F3(wt, kw, j + 1, i + 1) + F3(wt, kw, j + 2, i) + F3(wt, kw, j + 2, i + 1)) * 0.125;
+            else if (j == jj - 2)
+                f = avz * (F3(wt, kw, j - 1, i) + F3(wt, kw, j - 1, i + 1) + F3(wt, kw, j, i) + F3(wt, kw, j, i + 1) +
+                           2 * F3(wt, kw, j + 1, i) + 2 * F3(wt, kw, j + 1, i + 1)) * 0.125;
+            else
+                f = avz * (F3(wt, kw, j - 1, i) + F3(wt, kw, j - 1, i + 1) + F3(wt, kw, j, i) + F3(wt, kw, j, i + 1) +
+                           F3(wt, kw, j + 1, i) + F3(wt, kw, j + 1, i + 1) + F3(wt, kw, j + 2, i) +
+                           F3(wt, kw, j + 2, i + 1)) * 0.125;
+            N[PZ(j, i)] = 0.5 * f * (F3(v, k, j, i) + F3(v, kn, j, i));
+            N[PZ(j, i + 1)] = 0.5 * f * (F3(v, k, j, i + 1) + F3(v, kn, j, i + 1));
+        })
+        PAR_LOOP2(i, 3, ii - 2, 1, j, 2, jj - 4, 2, { N[PZ(j + 1, i)] = 0.5 * (N[PZ(j, i)] + N[PZ(j + 2, i)]); })
+        PAR_LOOP2(i, 3, ii - 2, 1, j, 2, jj - 2, 1, {
+            const double fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            const double rddzk = rddz[k];
+            if (top)
+                F3(vo, k, j, i) = F3(vo, k, j, i) + fkdtv * rddzk * (N[PZ(j, i)] - S[PZ(j, i)]);
+            else
+                F3(vo, k, j, i) = F3(vo, k, j, i) + fkdtv * rddzk * (-N[PZ(j, i)] + S[PZ(j, i)]);
+        })
+    }
+
+    // ---- LEFT and RIGHT (y faces): u cell, then w cell
+    for (int side = 0; side < 2; ++side) {
+        const bool left = side == 0;
+        if ((left ? nlft : nrgt) != 8) continue;
+        const int j = left ? jj - 2 : 3;
+        const int jv = left ? j : j - 1;
+        const int jn = left ? j + 1 : j - 1;
+        PAR_LOOP2(i, 2, ii - 2, 1, k, 3, kk - 2, 1, {
+            const double auy = dx[i] * ddz[k];
+            const double f = auy * (F3(vt, k, jv, i) + F3(vt, k, jv, i + 1)) * 0.5;
+            S[PY(k, i)] = 0.5 * f * (F3(u, k, j, i) + F3(u, k, jn, i));
+        })
+        PAR_LOOP2(i, 2, ii - 2, 2, k, 3, kk - 2, 2, {
+            const double auy = dx[i] * ddz[k];
+            double f;
+            if (i == 2)
+                f = auy * (2 * F3(vt, k, jv, i) + 2 * F3(vt, k + 1, jv, i) + F3(vt, k, jv, i + 1) +
+                           F3(vt, k + 1, jv, i + 1) + F3(vt, k, jv, i + 2) + F3(vt, k + 1, jv, i + 2)) * 0.125;
+            else if (i == ii - 2)
+                f = auy * (F3(vt, k, jv, i - 1) + F3(vt, k + 1, jv, i - 1) + F3(vt, k, jv, i) + F3(vt, k + 1, jv, i) +
+                           2 * F3(vt, k, jv, i + 1) + 2 * F3(vt, k + 1, jv, i + 1)) * 0.125;
+            else
+                f = auy * (F3(vt, k, jv, i - 1) + F3(vt, k + 1, jv, i - 1) + F3(vt, k, jv, i) + F3(vt, k + 1, jv, i) +
+                           F3(vt, k, jv, i + 1) + F3(vt, k + 1, jv, i + 1) + F3(vt, k, jv, i + 2) +
+                           F3(vt, k + 1, jv, i + 2)) * 0.125;
+            N[PY(k, i)] = 0.5 * f * (F3(u, k, j, i) + F3(u, k, jn, i));
+            N[PY(k + 1, i)] = 0.5 * f * (F3(u, k + 1, j, i) + F3(u, k + 1, jn, i));
+        })
+        PAR_LOOP2(i, 2, ii - 4, 2, k, 3, kk - 2, 1, { N[PY(k, i + 1)] = 0.5 * (N[PY(k, i)] + N[PY(k, i + 2)]); })
+        PAR_LOOP2(i, 2, ii - 2, 1, k, 3, kk - 2, 1, {
+            const double fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+            const double rddzk = rddz[k];
+            if (left)
+                F3(uo, k, j, i) = F3(uo, k, j, i) + fkdtu * rddzk * (N[PY(k, i)] - S[PY(k, i)]);
+            else
+                F3(uo, k, j, i) = F3(uo, k, j, i) + fkdtu * rddzk * (-N[PY(k, i)] + S[PY(k, i)]);
+        })
+        PAR_LOOP2(i, 3, ii - 2, 1, k, 2, kk - 2, 1, {
+            const double awy = ddx[i] * dz[k];
+            const double f = awy * (F3(vt, k, jv, i) + F3(vt, k + 1, jv, i)) * 0.5;
+            S[PY(k, i)] = 0.5 * f * (F3(w, k, j, i) + F3(w, k, jn, i));
+        })
+        // the reference runs the interior k loop with step 1; its odd k
+        // entries are overwritten by the interpolation below, so step 2 is
+        // the same result
+        PAR_LOOP2(i, 3, ii - 2, 2, k, 2, kk - 2, 2, {
+            const double awy = ddx[i] * dz[k];
+            double f;
+            if (k == 2)
+                f = awy * (2 * F3(vt, k, jv, i) + 2 * F3(vt, k, jv, i + 1) + F3(vt, k + 1, jv, i) +
+                           F3(vt, k + 1, jv, i + 1) + F3(vt, k + 2, jv, i) + F3(vt, k + 2, jv, i + 1)) * 0.125;
+            else if (k == kk - 2)
+                f = awy * (F3(vt, k - 1, jv, i) + F3(vt, k - 1, jv, i + 1) + F3(vt, k, jv, i) + F3(vt, k, jv, i + 1) +
+                           2 * F3(vt, k + 1, jv, i) + 2 * F3(vt, k + 1, jv, i + 1)) * 0.125;
+            else
+                f = awy * (F3(vt, k - 1, jv, i) + F3(vt, k - 1, jv, i + 1) + F3(vt, k, jv, i) + F3(vt, k, jv, i + 1) +
+                           F3(vt, k + 1, jv, i) + F3(vt, k + 1, jv, i + 1) + F3(vt, k + 2, jv, i) +
+                           F3(vt, k + 2, jv, i + 1)) * 0.125;
+            N[PY(k, i)] = 0.5 * f * (F3(w, k, j, i) + F3(w, k, jn, i));
+            N[PY(k, i + 1)] = 0.5 * f * (F3(w, k, j, i + 1) + F3(w, k, jn, i + 1));
+        })
+        PAR_LOOP2(i, 3, ii - 2, 1, k, 2, kk - 4, 2, { N[PY(k + 1, i)] = 0.5 * (N[PY(k, i)] + N[PY(k + 2, i)]); })
+        PAR_LOOP2(i, 3, ii - 2, 1, k, 2, kk - 2, 1, {
+            const double fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            const double rdzk = rdz[k];
+            if (left)
+                F3(wo, k, j, i) = F3(wo, k, j, i) + fkdtw * rdzk * (-S[PY(k, i)] + N[PY(k, i)]);
+            else
+                F3(wo, k, j, i) = F3(wo, k, j, i) + fkdtw * rdzk * (S[PY(k, i)] - N[PY(k, i)]);
+        })
+    }
+#undef F3
+}
+#undef PAR_LOOP2
+
 int upload_list(Ctx* c, const std::vector<int>& h, int** d) {
     if (*d) cudaFree(*d);
     *d = nullptr;
@@ -394,6 +765,15 @@ int upload_list(Ctx* c, const std::vector<int>& h, int** d) {
 }  // namespace
 
 int level_init(Ctx* c) {
+    std::vector<int> any;
+    for (int g = 0; g < c->ngrid; ++g)
+        for (int f = 0; f < 6; ++f)
+            if (c->grids[g].bc[f] == MGLET_BC_PAR) {
+                any.push_back(g);
+                break;
+            }
+    c->npargrids = (int)any.size();
+    if (int rc = upload_list(c, any, &c->d_pargrids)) return rc;
     for (int f = 0; f < 6; ++f) {
         c->pgrids[f].clear();
         for (int g = 0; g < c->ngrid; ++g)
@@ -477,6 +857,33 @@ double* field_buffer(Ctx* c, const std::string& name) {
     }
     c->fbuf[name] = b;
     return b;
+}
+
+int launch_tstle4_par(Ctx* c, double* uo, double* vo, double* wo, const double* u, const double* v,
+                      const double* w, const double* ut, const double* vt, const double* wt) {
+    if (!c->npargrids) return 0;
+    ProfScope ps_(c, "tstle4_par");
+    ParFluxArgs A;
+    A.grids = c->d_grids;
+    A.list = c->d_pargrids;
+    A.uo = uo; A.vo = vo; A.wo = wo;
+    A.u = u; A.v = v; A.w = w; A.ut = ut; A.vt = vt; A.wt = wt;
+    A.dx = c->L("DX"); A.dy = c->L("DY"); A.dz = c->L("DZ");
+    A.ddx = c->L("DDX"); A.ddy = c->L("DDY"); A.ddz = c->L("DDZ");
+    A.rdx = c->L("RDX"); A.rdy = c->L("RDY"); A.rdz = c->L("RDZ");
+    A.rddx = c->L("RDDX"); A.rddy = c->L("RDDY"); A.rddz = c->L("RDDZ");
+    int pl = 0;
+    for (const DevGrid& G : c->grids) pl = std::max(pl, std::max(G.kk * G.jj, std::max(G.kk * G.ii, G.jj * G.ii)));
+    const size_t smem = (size_t)2 * pl * sizeof(double);
+    if (smem > 227 * 1024) {
+        set_error("tstle4_par: a face plane of more than 14528 points does not fit in shared memory");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    if (smem > 48 * 1024)
+        MG_CUDA(cudaFuncSetAttribute(k_tstle4_par, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    k_tstle4_par<<<c->npargrids, 256, smem, c->stream>>>(A);
+    MG_LAUNCHED(c);
+    return 0;
 }
 
 int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w) {

@@ -253,7 +253,8 @@ CONTAINS
     END SUBROUTINE gpu_set_pinf
 
     ! The grid hierarchy (gridinfo%iparent, i/j/kposition of every grid):
-    ! needed before gpu_parent, gpu_ftoc, gpu_ctof and a multi-level mgpoisl.
+    ! needed before gpu_parent, gpu_ftoc, gpu_ctof, a multi-level mgpoisl and
+    ! a multi-level gpu_timeintegrate_flow.
     SUBROUTINE gpu_set_hierarchy(iparent, position)
         INTEGER(c_int32_t), INTENT(in) :: iparent(:), position(:, :)   ! position(3, ngrid)
         IF (mglet_gpu_set_hierarchy(gctx, iparent, position) /= 0) CALL errr(__FILE__, __LINE__)

@@ -1699,7 +1699,615 @@ void setsdivfield(Ctx& c) {
 }
 
 // ---------------------------------------------------------------------------
-// tstle4_mod.F90:139-265 tstle4_kon, :268-458 tstle4_diff, :461-529 tstle4_gradp
+
+// tstle4_mod.F90:532-1753 tstle4_par, a loop-by-loop transcription: on PAR
+// faces (code 8) the upwind correction of the second-to-last layer, then the
+// momentum-conserving convective fluxes of the coarse velocities,
+// redistributed onto the fine cells (back, front, top, bottom, left, right).
+// The work arrays start as NaN: a read of an entry the reference does not
+// write would reach the result.
+void tstle4_par(int kk, int jj, int ii, double* uo, double* vo, double* wo, const double* u,
+                const double* v, const double* w, const double* ut, const double* vt,
+                const double* wt, const double* dx, const double* dy, const double* dz,
+                const double* ddx, const double* ddy, const double* ddz, const double* rdx,
+                const double* rdy, const double* rdz, const double* rddx, const double* rddy,
+                const double* rddz, int nfro, int nbac, int nrgt, int nlft, int nbot, int ntop) {
+    if (nfro != 8 && nbac != 8 && nrgt != 8 && nlft != 8 && nbot != 8 && ntop != 8) return;
+    const double wkon = 1.0;
+    const int64_t n3 = (int64_t)kk * jj * ii;
+    const double nan = std::numeric_limits<double>::quiet_NaN();
+    std::vector<double> wcu_(n3, nan), wcv_(n3, nan), wcw_(n3, nan);
+    double* wcu = wcu_.data(); double* wcv = wcv_.data(); double* wcw = wcw_.data();
+#define A(a, k, j, i) a[IX(k, j, i)]
+    double fkdtu, fkdtv, fkdtw, dxi, ddxi, dyj, ddyj, dzk, ddzk, rdzk, rddzk;
+    double auy, auz, avx, avz, awx, awy;
+    // ---- upwind in the second-to-last layer
+    if (nfro == 8) {
+        const int i = 4;
+        for (int j = 3; j <= jj - 2; ++j) {
+            dyj = dy[j]; ddyj = ddy[j];
+            fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+            fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            for (int k = 3; k <= kk - 2; ++k) {
+                dzk = dz[k]; rdzk = rdz[k]; ddzk = ddz[k]; rddzk = rddz[k];
+                avx = dyj * ddzk;
+                awx = ddyj * dzk;
+                const double fvw = avx * (A(ut, k, j, i - 1) + A(ut, k, j + 1, i - 1)) * 0.5;
+                const double qv = 0.5 * (fvw - std::fabs(fvw)) *
+                                  (0.5 * A(v, k, j, i) - 1.5 * A(v, k, j, i - 1) + A(v, k, j, i - 2)) * 0.5 * 0.5;
+                A(vo, k, j, i) = A(vo, k, j, i) + fkdtv * rddzk * (-qv);
+                A(vo, k, j, i - 1) = A(vo, k, j, i - 1) + fkdtv * rddzk * (+qv);
+                const double fww = awx * (A(ut, k, j, i - 1) + A(ut, k + 1, j, i - 1)) * 0.5;
+                const double qw = 0.5 * (fww - std::fabs(fww)) *
+                                  (0.5 * A(w, k, j, i) - 1.5 * A(w, k, j, i - 1) + A(w, k, j, i - 2)) * 0.5 * 0.5;
+                A(wo, k, j, i) = A(wo, k, j, i) + fkdtw * rdzk * (-qw);
+                A(wo, k, j, i - 1) = A(wo, k, j, i - 1) + fkdtw * rdzk * (+qw);
+            }
+        }
+    }
+    if (nbac == 8) {
+        const int i = ii - 2;
+        for (int j = 3; j <= jj - 2; ++j) {
+            dyj = dy[j]; ddyj = ddy[j];
+            fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+            fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            for (int k = 3; k <= kk - 2; ++k) {
+                dzk = dz[k]; rdzk = rdz[k]; ddzk = ddz[k]; rddzk = rddz[k];
+                avx = dyj * ddzk;
+                awx = ddyj * dzk;
+                const double fvw = avx * (A(ut, k, j, i - 1) + A(ut, k, j + 1, i - 1)) * 0.5;
+                const double qv = 0.5 * (fvw + std::fabs(fvw)) *
+                                  (0.5 * A(v, k, j, i - 1) - 1.5 * A(v, k, j, i) + A(v, k, j, i + 1)) * 0.5 * 0.5;
+                A(vo, k, j, i) = A(vo, k, j, i) + fkdtv * rddzk * (-qv);
+                A(vo, k, j, i - 1) = A(vo, k, j, i - 1) + fkdtv * rddzk * (+qv);
+                const double fww = awx * (A(ut, k, j, i - 1) + A(ut, k + 1, j, i - 1)) * 0.5;
+                const double qw = 0.5 * (fww + std::fabs(fww)) *
+                                  (0.5 * A(w, k, j, i - 1) - 1.5 * A(w, k, j, i) + A(w, k, j, i + 1)) * 0.5 * 0.5;
+                A(wo, k, j, i) = A(wo, k, j, i) + fkdtw * rdzk * (-qw);
+                A(wo, k, j, i - 1) = A(wo, k, j, i - 1) + fkdtw * rdzk * (+qw);
+            }
+        }
+    }
+    if (nrgt == 8) {
+        for (int i = 3; i <= ii - 2; ++i) {
+            const int j = 4;
+            dxi = dx[i]; ddxi = ddx[i];
+            fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+            fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            for (int k = 3; k <= kk - 2; ++k) {
+                dzk = dz[k]; rdzk = rdz[k]; ddzk = ddz[k]; rddzk = rddz[k];
+                auy = dxi * ddzk;
+                awy = ddxi * dzk;
+                const double fus = auy * (A(vt, k, j - 1, i) + A(vt, k, j - 1, i + 1)) * 0.5;
+                const double qu = 0.5 * (fus - std::fabs(fus)) *
+                                  (0.5 * A(u, k, j, i) - 1.5 * A(u, k, j - 1, i) + A(u, k, j - 2, i)) * 0.5 * 0.5;
+                A(uo, k, j, i) = A(uo, k, j, i) + fkdtu * rddzk * (-qu);
+                A(uo, k, j - 1, i) = A(uo, k, j - 1, i) + fkdtu * rddzk * (+qu);
+                const double fws = awy * (A(vt, k, j - 1, i) + A(vt, k + 1, j - 1, i)) * 0.5;
+                const double qw = 0.5 * (fws - std::fabs(fws)) *
+                                  (0.5 * A(w, k, j, i) - 1.5 * A(w, k, j - 1, i) + A(w, k, j - 2, i)) * 0.5 * 0.5;
+                A(wo, k, j, i) = A(wo, k, j, i) + fkdtw * rdzk * (-qw);
+                A(wo, k, j - 1, i) = A(wo, k, j - 1, i) + fkdtw * rdzk * (+qw);
+            }
+        }
+    }
+    if (nlft == 8) {
+        for (int i = 3; i <= ii - 2; ++i) {
+            const int j = jj - 2;
+            dxi = dx[i]; ddxi = ddx[i];
+            fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+            fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            for (int k = 3; k <= kk - 2; ++k) {
+                dzk = dz[k]; rdzk = rdz[k]; ddzk = ddz[k]; rddzk = rddz[k];
+                auy = dxi * ddzk;
+                awy = ddxi * dzk;
+                const double fus = auy * (A(vt, k, j - 1, i) + A(vt, k, j - 1, i + 1)) * 0.5;
+                const double qu = 0.5 * (fus + std::fabs(fus)) *
+                                  (0.5 * A(u, k, j - 1, i) - 1.5 * A(u, k, j, i) + A(u, k, j + 1, i)) * 0.5 * 0.5;
+                A(uo, k, j, i) = A(uo, k, j, i) + fkdtu * rddzk * (-qu);
+                A(uo, k, j - 1, i) = A(uo, k, j - 1, i) + fkdtu * rddzk * (+qu);
+                const double fws = awy * (A(vt, k, j - 1, i) + A(vt, k + 1, j - 1, i)) * 0.5;
+                const double qw = 0.5 * (fws + std::fabs(fws)) *
+                                  (0.5 * A(w, k, j - 1, i) - 1.5 * A(w, k, j, i) + A(w, k, j + 1, i)) * 0.5 * 0.5;
+                A(wo, k, j, i) = A(wo, k, j, i) + fkdtw * rdzk * (-qw);
+                A(wo, k, j - 1, i) = A(wo, k, j - 1, i) + fkdtw * rdzk * (+qw);
+            }
+        }
+    }
+    if (nbot == 8) {
+        for (int i = 3; i <= ii - 2; ++i) {
+            dxi = dx[i]; ddxi = ddx[i];
+            for (int j = 3; j <= jj - 2; ++j) {
+                const int k = 4;
+                fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+                fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+                fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+                dyj = dy[j]; ddyj = ddy[j];
+                auz = dxi * ddyj;
+                avz = ddxi * dyj;
+                rdzk = rdz[k]; rddzk = rddz[k];
+                const double fub = auz * (A(wt, k - 1, j, i) + A(wt, k - 1, j, i + 1)) * 0.5;
+                const double qu = 0.5 * (fub - std::fabs(fub)) *
+                                  (0.5 * A(u, k, j, i) - 1.5 * A(u, k - 1, j, i) + A(u, k - 2, j, i)) * 0.5 * 0.5;
+                A(uo, k, j, i) = A(uo, k, j, i) + fkdtu * rddzk * (-qu);
+                A(uo, k - 1, j, i) = A(uo, k - 1, j, i) + fkdtu * rddzk * (+qu);
+                const double fvb = avz * (A(wt, k - 1, j, i) + A(wt, k - 1, j + 1, i)) * 0.5;
+                const double qv = 0.5 * (fvb - std::fabs(fvb)) *
+                                  (0.5 * A(v, k, j, i) - 1.5 * A(v, k - 1, j, i) + A(v, k - 2, j, i)) * 0.5 * 0.5;
+                A(vo, k, j, i) = A(vo, k, j, i) + fkdtv * rddzk * (-qv);
+                A(vo, k - 1, j, i) = A(vo, k - 1, j, i) + fkdtv * rddzk * (+qv);
+            }
+        }
+    }
+    if (ntop == 8) {
+        for (int i = 3; i <= ii - 2; ++i) {
+            dxi = dx[i]; ddxi = ddx[i];
+            for (int j = 3; j <= jj - 2; ++j) {
+                const int k = kk - 2;
+                fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+                fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+                fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+                dyj = dy[j]; ddyj = ddy[j];
+                auz = dxi * ddyj;
+                avz = ddxi * dyj;
+                rdzk = rdz[k]; rddzk = rddz[k];
+                const double fub = auz * (A(wt, k - 1, j, i) + A(wt, k - 1, j, i + 1)) * 0.5;
+                const double qu = 0.5 * (fub + std::fabs(fub)) *
+                                  (0.5 * A(u, k - 1, j, i) - 1.5 * A(u, k, j, i) + A(u, k + 1, j, i)) * 0.5 * 0.5;
+                A(uo, k, j, i) = A(uo, k, j, i) + fkdtu * rddzk * (-qu);
+                A(uo, k - 1, j, i) = A(uo, k - 1, j, i) + fkdtu * rddzk * (+qu);
+                const double fvb = avz * (A(wt, k - 1, j, i) + A(wt, k - 1, j + 1, i)) * 0.5;
+                const double qv = 0.5 * (fvb + std::fabs(fvb)) *
+                                  (0.5 * A(v, k - 1, j, i) - 1.5 * A(v, k, j, i) + A(v, k + 1, j, i)) * 0.5 * 0.5;
+                A(vo, k, j, i) = A(vo, k, j, i) + fkdtv * rddzk * (-qv);
+                A(vo, k - 1, j, i) = A(vo, k - 1, j, i) + fkdtv * rddzk * (+qv);
+            }
+        }
+    }
+    (void)fkdtu;
+    // ---- momentum-conserving fluxes: BACK
+    if (nbac == 8) {
+        int i = ii - 2;
+        // w cell: standard flux, then the flux of every coarse velocity
+        for (int j = 3; j <= jj - 2; ++j) {
+            ddyj = ddy[j];
+            for (int k = 2; k <= kk - 2; ++k) {
+                dzk = dz[k];
+                awx = ddyj * dzk;
+                const double fwe = awx * (A(ut, k, j, i) + A(ut, k + 1, j, i)) * 0.5;
+                A(wcw, k, j, i + 1) = 0.5 * fwe * (A(w, k, j, i) + A(w, k, j, i + 1));
+            }
+        }
+        for (int j = 3; j <= jj - 2; j += 2) {
+            ddyj = ddy[j];
+            int k = 2;
+            dzk = dz[k];
+            awx = ddyj * dzk;
+            double fwe = awx * (2 * A(ut, k, j, i) + 2 * A(ut, k, j + 1, i) + A(ut, k + 1, j, i) +
+                                A(ut, k + 1, j + 1, i) + A(ut, k + 2, j, i) + A(ut, k + 2, j + 1, i)) * 0.125;
+            A(wcw, k, j, i) = 0.5 * fwe * (A(w, k, j, i) + A(w, k, j, i + 1));
+            A(wcw, k, j + 1, i) = 0.5 * fwe * (A(w, k, j + 1, i) + A(w, k, j + 1, i + 1));
+            for (k = 4; k <= kk - 4; k += 2) {
+                dzk = dz[k];
+                awx = ddyj * dzk;
+                fwe = awx * (A(ut, k - 1, j, i) + A(ut, k - 1, j + 1, i) + A(ut, k, j, i) + A(ut, k, j + 1, i) +
+                             A(ut, k + 1, j, i) + A(ut, k + 1, j + 1, i) + A(ut, k + 2, j, i) +
+                             A(ut, k + 2, j + 1, i)) * 0.125;
+                A(wcw, k, j, i) = 0.5 * fwe * (A(w, k, j, i) + A(w, k, j, i + 1));
+                A(wcw, k, j + 1, i) = 0.5 * fwe * (A(w, k, j + 1, i) + A(w, k, j + 1, i + 1));
+            }
+            k = kk - 2;
+            dzk = dz[k];
+            awx = ddyj * dzk;
+            fwe = awx * (A(ut, k - 1, j, i) + A(ut, k - 1, j + 1, i) + A(ut, k, j, i) + A(ut, k, j + 1, i) +
+                         2 * A(ut, k + 1, j, i) + 2 * A(ut, k + 1, j + 1, i)) * 0.125;
+            A(wcw, k, j, i) = 0.5 * fwe * (A(w, k, j, i) + A(w, k, j, i + 1));
+            A(wcw, k, j + 1, i) = 0.5 * fwe * (A(w, k, j + 1, i) + A(w, k, j + 1, i + 1));
+        }
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 2; k <= kk - 4; k += 2)
+                A(wcw, k + 1, j, i) = 0.5 * (A(wcw, k, j, i) + A(wcw, k + 2, j, i));
+        for (int j = 3; j <= jj - 2; ++j) {
+            fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            for (int k = 2; k <= kk - 2; ++k) {
+                rdzk = rdz[k];
+                A(wo, k, j, i) = A(wo, k, j, i) + fkdtw * rdzk * (-A(wcw, k, j, i + 1) + A(wcw, k, j, i));
+            }
+        }
+        // v cell
+        for (int j = 2; j <= jj - 2; ++j) {
+            dyj = dy[j];
+            for (int k = 3; k <= kk - 2; ++k) {
+                ddzk = ddz[k];
+                avx = ddzk * dyj;
+                const double fve = avx * (A(ut, k, j, i) + A(ut, k, j + 1, i)) * 0.5;
+                A(wcv, k, j, i + 1) = 0.5 * fve * (A(v, k, j, i) + A(v, k, j, i + 1));
+            }
+        }
+        {
+            int j = 2;
+            dyj = dy[j];
+            for (int k = 3; k <= kk - 2; k += 2) {
+                ddzk = ddz[k];
+                avx = ddzk * dyj;
+                const double fve = avx * (2 * A(ut, k, j, i) + 2 * A(ut, k + 1, j, i) + A(ut, k, j + 1, i) +
+                                          A(ut, k + 1, j + 1, i) + A(ut, k, j + 2, i) + A(ut, k + 1, j + 2, i)) * 0.125;
+                A(wcv, k, j, i) = 0.5 * fve * (A(v, k, j, i) + A(v, k, j, i + 1));
+                A(wcv, k + 1, j, i) = 0.5 * fve * (A(v, k + 1, j, i) + A(v, k + 1, j, i + 1));
+            }
+            for (j = 4; j <= jj - 4; j += 2) {
+                dyj = dy[j];
+                for (int k = 3; k <= kk - 2; k += 2) {
+                    ddzk = ddz[k];
+                    avx = ddzk * dyj;
+                    const double fve = avx * (A(ut, k, j - 1, i) + A(ut, k + 1, j - 1, i) + A(ut, k, j, i) +
+                                              A(ut, k + 1, j, i) + A(ut, k, j + 1, i) + A(ut, k + 1, j + 1, i) +
+                                              A(ut, k, j + 2, i) + A(ut, k + 1, j + 2, i)) * 0.125;
+                    A(wcv, k, j, i) = 0.5 * fve * (A(v, k, j, i) + A(v, k, j, i + 1));
+                    A(wcv, k + 1, j, i) = 0.5 * fve * (A(v, k + 1, j, i) + A(v, k + 1, j, i + 1));
+                }
+            }
+            j = jj - 2;
+            dyj = dy[j];
+            for (int k = 3; k <= kk - 2; k += 2) {
+                ddzk = ddz[k];
+                avx = ddzk * dyj;
+                const double fve = avx * (A(ut, k, j - 1, i) + A(ut, k + 1, j - 1, i) + A(ut, k, j, i) +
+                                          A(ut, k + 1, j, i) + 2 * A(ut, k, j + 1, i) + 2 * A(ut, k + 1, j + 1, i)) * 0.125;
+                A(wcv, k, j, i) = 0.5 * fve * (A(v, k, j, i) + A(v, k, j, i + 1));
+                A(wcv, k + 1, j, i) = 0.5 * fve * (A(v, k + 1, j, i) + A(v, k + 1, j, i + 1));
+            }
+        }
+        for (int j = 2; j <= jj - 4; j += 2)
+            for (int k = 3; k <= kk - 2; ++k)
+                A(wcv, k, j + 1, i) = 0.5 * (A(wcv, k, j, i) + A(wcv, k, j + 2, i));
+        for (int j = 2; j <= jj - 2; ++j) {
+            fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            for (int k = 3; k <= kk - 2; ++k) {
+                rddzk = rddz[k];
+                A(vo, k, j, i) = A(vo, k, j, i) + fkdtv * rddzk * (A(wcv, k, j, i) - A(wcv, k, j, i + 1));
+            }
+        }
+    }
+    // ---- FRONT
+    if (nfro == 8) {
+        int i = 3;
+        for (int j = 3; j <= jj - 2; ++j) {
+            ddyj = ddy[j];
+            for (int k = 2; k <= kk - 2; ++k) {
+                dzk = dz[k];
+                awx = ddyj * dzk;
+                const double fww = awx * (A(ut, k, j, i - 1) + A(ut, k + 1, j, i - 1)) * 0.5;
+                A(wcw, k, j, i - 1) = 0.5 * fww * (A(w, k, j, i) + A(w, k, j, i - 1));
+            }
+        }
+        for (int j = 3; j <= jj - 2; j += 2) {
+            ddyj = ddy[j];
+            int k = 2;
+            dzk = dz[k];
+            awx = ddyj * dzk;
+            double fww = awx * (2 * A(ut, k, j, i - 1) + 2 * A(ut, k, j + 1, i - 1) + A(ut, k + 1, j, i - 1) +
+                                A(ut, k + 1, j + 1, i - 1) + A(ut, k + 2, j, i - 1) + A(ut, k + 2, j + 1, i - 1)) * 0.125;
+            A(wcw, k, j, i) = 0.5 * fww * (A(w, k, j, i) + A(w, k, j, i - 1));
+            A(wcw, k, j + 1, i) = 0.5 * fww * (A(w, k, j + 1, i) + A(w, k, j + 1, i - 1));
+            for (k = 4; k <= kk - 4; k += 2) {
+                dzk = dz[k];
+                awx = ddyj * dzk;
+                fww = awx * (A(ut, k - 1, j, i - 1) + A(ut, k - 1, j + 1, i - 1) + A(ut, k, j, i - 1) +
+                             A(ut, k, j + 1, i - 1) + A(ut, k + 1, j, i - 1) + A(ut, k + 1, j + 1, i - 1) +
+                             A(ut, k + 2, j, i - 1) + A(ut, k + 2, j + 1, i - 1)) * 0.125;
+                A(wcw, k, j, i) = 0.5 * fww * (A(w, k, j, i) + A(w, k, j, i - 1));
+                A(wcw, k, j + 1, i) = 0.5 * fww * (A(w, k, j + 1, i) + A(w, k, j + 1, i - 1));
+            }
+            k = kk - 2;
+            dzk = dz[k];
+            awx = ddyj * dzk;
+            fww = awx * (A(ut, k - 1, j, i - 1) + A(ut, k - 1, j + 1, i - 1) + A(ut, k, j, i - 1) +
+                         A(ut, k, j + 1, i - 1) + 2 * A(ut, k + 1, j, i - 1) + 2 * A(ut, k + 1, j + 1, i - 1)) * 0.125;
+            A(wcw, k, j, i) = 0.5 * fww * (A(w, k, j, i) + A(w, k, j, i - 1));
+            A(wcw, k, j + 1, i) = 0.5 * fww * (A(w, k, j + 1, i) + A(w, k, j + 1, i - 1));
+        }
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 2; k <= kk - 4; k += 2)
+                A(wcw, k + 1, j, i) = 0.5 * (A(wcw, k, j, i) + A(wcw, k + 2, j, i));
+        for (int j = 3; j <= jj - 2; ++j) {
+            fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            for (int k = 2; k <= kk - 2; ++k) {
+                rdzk = rdz[k];
+                A(wo, k, j, i) = A(wo, k, j, i) + fkdtw * rdzk * (A(wcw, k, j, i - 1) - A(wcw, k, j, i));
+            }
+        }
+        for (int j = 2; j <= jj - 2; ++j) {
+            dyj = dy[j];
+            for (int k = 3; k <= kk - 2; ++k) {
+                ddzk = ddz[k];
+                avx = ddzk * dyj;
+                const double fvw = avx * (A(ut, k, j, i - 1) + A(ut, k, j + 1, i - 1)) * 0.5;
+                A(wcv, k, j, i - 1) = 0.5 * fvw * (A(v, k, j, i) + A(v, k, j, i - 1));
+            }
+        }
+        {
+            int j = 2;
+            dyj = dy[j];
+            for (int k = 3; k <= kk - 2; k += 2) {
+                ddzk = ddz[k];
+                avx = ddzk * dyj;
+                const double fvw = avx * (2 * A(ut, k, j, i - 1) + 2 * A(ut, k + 1, j, i - 1) + A(ut, k, j + 1, i - 1) +
+                                          A(ut, k + 1, j + 1, i - 1) + A(ut, k, j + 2, i - 1) + A(ut, k + 1, j + 2, i - 1)) * 0.125;
+                A(wcv, k, j, i) = 0.5 * fvw * (A(v, k, j, i) + A(v, k, j, i - 1));
+                A(wcv, k + 1, j, i) = 0.5 * fvw * (A(v, k + 1, j, i) + A(v, k + 1, j, i - 1));
+            }
+            for (j = 4; j <= jj - 4; j += 2) {
+                dyj = dy[j];
+                for (int k = 3; k <= kk - 2; k += 2) {
+                    ddzk = ddz[k];
+                    avx = ddzk * dyj;
+                    const double fvw = avx * (A(ut, k, j - 1, i - 1) + A(ut, k + 1, j - 1, i - 1) + A(ut, k, j, i - 1) +
+                                              A(ut, k + 1, j, i - 1) + A(ut, k, j + 1, i - 1) + A(ut, k + 1, j + 1, i - 1) +
+                                              A(ut, k, j + 2, i - 1) + A(ut, k + 1, j + 2, i - 1)) * 0.125;
+                    A(wcv, k, j, i) = 0.5 * fvw * (A(v, k, j, i) + A(v, k, j, i - 1));
+                    A(wcv, k + 1, j, i) = 0.5 * fvw * (A(v, k + 1, j, i) + A(v, k + 1, j, i - 1));
+                }
+            }
+            j = jj - 2;
+            dyj = dy[j];
+            for (int k = 3; k <= kk - 2; k += 2) {
+                ddzk = ddz[k];
+                avx = ddzk * dyj;
+                const double fvw = avx * (A(ut, k, j - 1, i - 1) + A(ut, k + 1, j - 1, i - 1) + A(ut, k, j, i - 1) +
+                                          A(ut, k + 1, j, i - 1) + 2 * A(ut, k, j + 1, i - 1) + 2 * A(ut, k + 1, j + 1, i - 1)) * 0.125;
+                A(wcv, k, j, i) = 0.5 * fvw * (A(v, k, j, i) + A(v, k, j, i - 1));
+                A(wcv, k + 1, j, i) = 0.5 * fvw * (A(v, k + 1, j, i) + A(v, k + 1, j, i - 1));
+            }
+        }
+        for (int j = 2; j <= jj - 4; j += 2)
+            for (int k = 3; k <= kk - 2; ++k)
+                A(wcv, k, j + 1, i) = 0.5 * (A(wcv, k, j, i) + A(wcv, k, j + 2, i));
+        for (int j = 2; j <= jj - 2; ++j) {
+            fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+            for (int k = 3; k <= kk - 2; ++k) {
+                rddzk = rddz[k];
+                A(vo, k, j, i) = A(vo, k, j, i) + fkdtv * rddzk * (-A(wcv, k, j, i) + A(wcv, k, j, i - 1));
+            }
+        }
+    }
+    // ---- TOP and BOTTOM: u cell (pairs in j, distribution in i), v cell
+    // (pairs in i, distribution in j); kq the plane of the fine fluxes, kc
+    // that of the standard flux, ks the transporting layer, sgn the order of
+    // the two w-flux planes in the update
+    for (int side = 0; side < 2; ++side) {
+        const bool top = side == 0;
+        if ((top ? ntop : nbot) != 8) continue;
+        const int k = top ? kk - 2 : 3;
+        const int kw = top ? k : k - 1;          // wt plane
+        const int kn = top ? k + 1 : k - 1;      // the other u/v plane of the flux
+        const int kc = top ? k + 1 : k - 1;      // standard-flux plane of wcu / wcv
+        for (int i = 2; i <= ii - 2; ++i) {
+            dxi = dx[i];
+            for (int j = 3; j <= jj - 2; ++j) {
+                ddyj = ddy[j];
+                auz = dxi * ddyj;
+                const double f = auz * (A(wt, kw, j, i) + A(wt, kw, j, i + 1)) * 0.5;
+                A(wcu, kc, j, i) = 0.5 * f * (A(u, k, j, i) + A(u, kn, j, i));
+            }
+        }
+        {
+            int i = 2;
+            dxi = dx[i];
+            for (int j = 3; j <= jj - 2; j += 2) {
+                ddyj = ddy[j];
+                auz = dxi * ddyj;
+                const double f = auz * (2 * A(wt, kw, j, i) + 2 * A(wt, kw, j + 1, i) + A(wt, kw, j, i + 1) +
+                                        A(wt, kw, j + 1, i + 1) + A(wt, kw, j, i + 2) + A(wt, kw, j + 1, i + 2)) * 0.125;
+                A(wcu, k, j, i) = 0.5 * f * (A(u, k, j, i) + A(u, kn, j, i));
+                A(wcu, k, j + 1, i) = 0.5 * f * (A(u, k, j + 1, i) + A(u, kn, j + 1, i));
+            }
+            for (i = 4; i <= ii - 4; i += 2) {
+                dxi = dx[i];
+                for (int j = 3; j <= jj - 2; j += 2) {
+                    ddyj = ddy[j];
+                    auz = dxi * ddyj;
+                    const double f = auz * (A(wt, kw, j, i - 1) + A(wt, kw, j + 1, i - 1) + A(wt, kw, j, i) +
+                                            A(wt, kw, j + 1, i) + A(wt, kw, j, i + 1) + A(wt, kw, j + 1, i + 1) +
+                                            A(wt, kw, j, i + 2) + A(wt, kw, j + 1, i + 2)) * 0.125;
+                    A(wcu, k, j, i) = 0.5 * f * (A(u, k, j, i) + A(u, kn, j, i));
+                    A(wcu, k, j + 1, i) = 0.5 * f * (A(u, k, j + 1, i) + A(u, kn, j + 1, i));
+                }
+            }
+            i = ii - 2;
+            dxi = dx[i];
+            for (int j = 3; j <= jj - 2; j += 2) {
+                ddyj = ddy[j];
+                auz = dxi * ddyj;
+                const double f = auz * (A(wt, kw, j, i - 1) + A(wt, kw, j + 1, i - 1) + A(wt, kw, j, i) +
+                                        A(wt, kw, j + 1, i) + 2 * A(wt, kw, j, i + 1) + 2 * A(wt, kw, j + 1, i + 1)) * 0.125;
+                A(wcu, k, j, i) = 0.5 * f * (A(u, k, j, i) + A(u, kn, j, i));
+                A(wcu, k, j + 1, i) = 0.5 * f * (A(u, k, j + 1, i) + A(u, kn, j + 1, i));
+            }
+        }
+        for (int i = 2; i <= ii - 4; i += 2)
+            for (int j = 3; j <= jj - 2; ++j)
+                A(wcu, k, j, i + 1) = 0.5 * (A(wcu, k, j, i) + A(wcu, k, j, i + 2));
+        rddzk = rddz[k];
+        for (int i = 2; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j) {
+                fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+                if (top)
+                    A(uo, k, j, i) = A(uo, k, j, i) + fkdtu * rddzk * (A(wcu, k, j, i) - A(wcu, k + 1, j, i));
+                else
+                    A(uo, k, j, i) = A(uo, k, j, i) + fkdtu * rddzk * (-A(wcu, k, j, i) + A(wcu, k - 1, j, i));
+            }
+        for (int i = 3; i <= ii - 2; ++i) {
+            ddxi = ddx[i];
+            for (int j = 2; j <= jj - 2; ++j) {
+                dyj = dy[j];
+                avz = ddxi * dyj;
+                const double f = avz * (A(wt, kw, j, i) + A(wt, kw, j + 1, i)) * 0.5;
+                A(wcv, kc, j, i) = 0.5 * f * (A(v, k, j, i) + A(v, kn, j, i));
+            }
+        }
+        for (int i = 3; i <= ii - 2; i += 2) {
+            ddxi = ddx[i];
+            int j = 2;
+            dyj = dy[j];
+            avz = ddxi * dyj;
+            double f = avz * (2 * A(wt, kw, j, i) + 2 * A(wt, kw, j, i + 1) + A(wt, kw, j + 1, i) +
+                              A(wt, kw, j + 1, i + 1) + A(wt, kw, j + 2, i) + A(wt, kw, j + 2, i + 1)) * 0.125;
+            A(wcv, k, j, i) = 0.5 * f * (A(v, k, j, i) + A(v, kn, j, i));
+            A(wcv, k, j, i + 1) = 0.5 * f * (A(v, k, j, i + 1) + A(v, kn, j, i + 1));
+            for (j = 4; j <= jj - 4; j += 2) {
+                dyj = dy[j];
+                avz = ddxi * dyj;
+                f = avz * (A(wt, kw, j - 1, i) + A(wt, kw, j - 1, i + 1) + A(wt, kw, j, i) + A(wt, kw, j, i + 1) +
+                           A(wt, kw, j + 1, i) + A(wt, kw, j + 1, i + 1) + A(wt, kw, j + 2, i) +
+                           A(wt, kw, j + 2, i + 1)) * 0.125;
+                A(wcv, k, j, i) = 0.5 * f * (A(v, k, j, i) + A(v, kn, j, i));
+                A(wcv, k, j, i + 1) = 0.5 * f * (A(v, k, j, i + 1) + A(v, kn, j, i + 1));
+            }
+            j = jj - 2;
+            dyj = dy[j];
+            avz = ddxi * dyj;
+            f = avz * (A(wt, kw, j - 1, i) + A(wt, kw, j - 1, i + 1) + A(wt, kw, j, i) + A(wt, kw, j, i + 1) +
+                       2 * A(wt, kw, j + 1, i) + 2 * A(wt, kw, j + 1, i + 1)) * 0.125;
+            A(wcv, k, j, i) = 0.5 * f * (A(v, k, j, i) + A(v, kn, j, i));
+            A(wcv, k, j, i + 1) = 0.5 * f * (A(v, k, j, i + 1) + A(v, kn, j, i + 1));
+        }
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 2; j <= jj - 4; j += 2)
+                A(wcv, k, j + 1, i) = 0.5 * (A(wcv, k, j, i) + A(wcv, k, j + 2, i));
+        rddzk = rddz[k];
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 2; j <= jj - 2; ++j) {
+                fkdtv = -1.0 * rddx[i] * rdy[j] * wkon;
+                if (top)
+                    A(vo, k, j, i) = A(vo, k, j, i) + fkdtv * rddzk * (A(wcv, k, j, i) - A(wcv, k + 1, j, i));
+                else
+                    A(vo, k, j, i) = A(vo, k, j, i) + fkdtv * rddzk * (-A(wcv, k, j, i) + A(wcv, k - 1, j, i));
+            }
+    }
+    // ---- LEFT and RIGHT: u cell (pairs in k, distribution in i), w cell
+    // (pairs in i, distribution in k)
+    for (int side = 0; side < 2; ++side) {
+        const bool left = side == 0;
+        if ((left ? nlft : nrgt) != 8) continue;
+        const int j = left ? jj - 2 : 3;
+        const int jv = left ? j : j - 1;          // vt plane
+        const int jn = left ? j + 1 : j - 1;      // the other u/w plane of the flux
+        const int jc = left ? j + 1 : j - 1;      // standard-flux plane
+        for (int i = 2; i <= ii - 2; ++i) {
+            dxi = dx[i];
+            for (int k = 3; k <= kk - 2; ++k) {
+                ddzk = ddz[k];
+                auy = dxi * ddzk;
+                const double f = auy * (A(vt, k, jv, i) + A(vt, k, jv, i + 1)) * 0.5;
+                A(wcu, k, jc, i) = 0.5 * f * (A(u, k, j, i) + A(u, k, jn, i));
+            }
+        }
+        {
+            int i = 2;
+            dxi = dx[i];
+            for (int k = 3; k <= kk - 2; k += 2) {
+                ddzk = ddz[k];
+                auy = dxi * ddzk;
+                const double f = auy * (2 * A(vt, k, jv, i) + 2 * A(vt, k + 1, jv, i) + A(vt, k, jv, i + 1) +
+                                        A(vt, k + 1, jv, i + 1) + A(vt, k, jv, i + 2) + A(vt, k + 1, jv, i + 2)) * 0.125;
+                A(wcu, k, j, i) = 0.5 * f * (A(u, k, j, i) + A(u, k, jn, i));
+                A(wcu, k + 1, j, i) = 0.5 * f * (A(u, k + 1, j, i) + A(u, k + 1, jn, i));
+            }
+            for (i = 4; i <= ii - 4; i += 2) {
+                dxi = dx[i];
+                for (int k = 3; k <= kk - 2; k += 2) {
+                    ddzk = ddz[k];
+                    auy = dxi * ddzk;
+                    const double f = auy * (A(vt, k, jv, i - 1) + A(vt, k + 1, jv, i - 1) + A(vt, k, jv, i) +
+                                            A(vt, k + 1, jv, i) + A(vt, k, jv, i + 1) + A(vt, k + 1, jv, i + 1) +
+                                            A(vt, k, jv, i + 2) + A(vt, k + 1, jv, i + 2)) * 0.125;
+                    A(wcu, k, j, i) = 0.5 * f * (A(u, k, j, i) + A(u, k, jn, i));
+                    A(wcu, k + 1, j, i) = 0.5 * f * (A(u, k + 1, j, i) + A(u, k + 1, jn, i));
+                }
+            }
+            i = ii - 2;
+            dxi = dx[i];
+            for (int k = 3; k <= kk - 2; k += 2) {
+                ddzk = ddz[k];
+                auy = dxi * ddzk;
+                const double f = auy * (A(vt, k, jv, i - 1) + A(vt, k + 1, jv, i - 1) + A(vt, k, jv, i) +
+                                        A(vt, k + 1, jv, i) + 2 * A(vt, k, jv, i + 1) + 2 * A(vt, k + 1, jv, i + 1)) * 0.125;
+                A(wcu, k, j, i) = 0.5 * f * (A(u, k, j, i) + A(u, k, jn, i));
+                A(wcu, k + 1, j, i) = 0.5 * f * (A(u, k + 1, j, i) + A(u, k + 1, jn, i));
+            }
+        }
+        for (int i = 2; i <= ii - 4; i += 2)
+            for (int k = 3; k <= kk - 2; ++k)
+                A(wcu, k, j, i + 1) = 0.5 * (A(wcu, k, j, i) + A(wcu, k, j, i + 2));
+        for (int i = 2; i <= ii - 2; ++i) {
+            fkdtu = -1.0 * rddy[j] * rdx[i] * wkon;
+            for (int k = 3; k <= kk - 2; ++k) {
+                rddzk = rddz[k];
+                if (left)
+                    A(uo, k, j, i) = A(uo, k, j, i) + fkdtu * rddzk * (A(wcu, k, j, i) - A(wcu, k, j + 1, i));
+                else
+                    A(uo, k, j, i) = A(uo, k, j, i) + fkdtu * rddzk * (-A(wcu, k, j, i) + A(wcu, k, j - 1, i));
+            }
+        }
+        for (int i = 3; i <= ii - 2; ++i) {
+            ddxi = ddx[i];
+            for (int k = 2; k <= kk - 2; ++k) {
+                dzk = dz[k];
+                awy = ddxi * dzk;
+                const double f = awy * (A(vt, k, jv, i) + A(vt, k + 1, jv, i)) * 0.5;
+                A(wcw, k, jc, i) = 0.5 * f * (A(w, k, j, i) + A(w, k, jn, i));
+            }
+        }
+        for (int i = 3; i <= ii - 2; i += 2) {
+            ddxi = ddx[i];
+            int k = 2;
+            dzk = dz[k];
+            awy = ddxi * dzk;
+            double f = awy * (2 * A(vt, k, jv, i) + 2 * A(vt, k, jv, i + 1) + A(vt, k + 1, jv, i) +
+                              A(vt, k + 1, jv, i + 1) + A(vt, k + 2, jv, i) + A(vt, k + 2, jv, i + 1)) * 0.125;
+            A(wcw, k, j, i) = 0.5 * f * (A(w, k, j, i) + A(w, k, jn, i));
+            A(wcw, k, j, i + 1) = 0.5 * f * (A(w, k, j, i + 1) + A(w, k, jn, i + 1));
+            for (k = 4; k <= kk - 4; ++k) {   // every k, as the reference runs it
+                dzk = dz[k];
+                awy = ddxi * dzk;
+                f = awy * (A(vt, k - 1, jv, i) + A(vt, k - 1, jv, i + 1) + A(vt, k, jv, i) + A(vt, k, jv, i + 1) +
+                           A(vt, k + 1, jv, i) + A(vt, k + 1, jv, i + 1) + A(vt, k + 2, jv, i) +
+                           A(vt, k + 2, jv, i + 1)) * 0.125;
+                A(wcw, k, j, i) = 0.5 * f * (A(w, k, j, i) + A(w, k, jn, i));
+                A(wcw, k, j, i + 1) = 0.5 * f * (A(w, k, j, i + 1) + A(w, k, jn, i + 1));
+            }
+            k = kk - 2;
+            dzk = dz[k];
+            awy = ddxi * dzk;
+            f = awy * (A(vt, k - 1, jv, i) + A(vt, k - 1, jv, i + 1) + A(vt, k, jv, i) + A(vt, k, jv, i + 1) +
+                       2 * A(vt, k + 1, jv, i) + 2 * A(vt, k + 1, jv, i + 1)) * 0.125;
+            A(wcw, k, j, i) = 0.5 * f * (A(w, k, j, i) + A(w, k, jn, i));
+            A(wcw, k, j, i + 1) = 0.5 * f * (A(w, k, j, i + 1) + A(w, k, jn, i + 1));
+        }
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int k = 2; k <= kk - 4; k += 2)
+                A(wcw, k + 1, j, i) = 0.5 * (A(wcw, k, j, i) + A(wcw, k + 2, j, i));
+        for (int i = 3; i <= ii - 2; ++i) {
+            fkdtw = -1.0 * rddx[i] * rddy[j] * wkon;
+            for (int k = 2; k <= kk - 2; ++k) {
+                rdzk = rdz[k];
+                if (left)
+                    A(wo, k, j, i) = A(wo, k, j, i) + fkdtw * rdzk * (-A(wcw, k, j + 1, i) + A(wcw, k, j, i));
+                else
+                    A(wo, k, j, i) = A(wo, k, j, i) + fkdtw * rdzk * (A(wcw, k, j - 1, i) - A(wcw, k, j, i));
+            }
+        }
+    }
+#undef A
+}
+
+// tstle4_mod.F90:139-265 tstle4_kon, :268-458 tstle4_diff, :461-529 tstle4_gradp,
+// :532-1753 tstle4_par
 void tstle4_grid(Ctx& c, int g) {
     const Grid& G = c.g[g];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
@@ -1888,6 +2496,8 @@ void tstle4_grid(Ctx& c, int g) {
             for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k)
                 A(wo, k, j, i) = A(wo, k, j, i) - 1.0 / (rho * dz[k]) * (A(p, k + 1, j, i) - A(p, k, j, i) + gpz * dz[k]);
 #undef A
+    tstle4_par(kk, jj, ii, uo, vo, wo, u, v, w, ut, vt, wt, dx, dy, dz, ddx, ddy, ddz, rdx, rdy, rdz,
+               rddx, rddy, rddz, nfro, nbac, nrgt, nlft, nbot, ntop);
 }
 
 void tstle4(Ctx& c) {
@@ -2076,16 +2686,6 @@ int hierarchy_ready(const Ctx& c) {
     return 0;
 }
 
-// the restated stage is single-level: no PAR faces (tstle4_par is not restated)
-int single_level_stage(const Ctx& c) {
-    if (c.minlevel != c.maxlevel)
-        return fail(MGLET_ERR_UNSUPPORTED, "oracle: the multi-level stage is not restated");
-    for (int g = 1; g <= c.ngrid; ++g)
-        for (int f = 1; f <= 6; ++f)
-            if (c.g[g].bc[f] == MGLET_BC_PAR)
-                return fail(MGLET_ERR_UNSUPPORTED, "oracle: PAR faces need the multi-level stage");
-    return 0;
-}
 }  // namespace
 
 extern "C" {
@@ -2305,7 +2905,7 @@ int oracle_mgpoisl(oracle_ctx* c, double dt, int ittot, int irk, mglet_stage_sta
 int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timeph, double dt,
                               int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st) {
     (void)itstep; (void)timeph;
-    if (int rc = single_level_stage(*c)) return rc;
+    if (int rc = hierarchy_ready(*c)) return rc;
     double frhs, fu, dtrk, dtrki;
     int rc = oracle_rk_get_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki);
     if (rc) return rc;
@@ -2321,10 +2921,14 @@ int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timep
         maskbp(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
         if (int rc2 = gc_level(*c, 'R', c->F("U"), c->F("V"), c->F("W"))) return rc2;
     }
-    // timeintegration_mod.F90:116-121: connect (normal, forward), bound
+    // timeintegration_mod.F90:117-122: per level connect (normal, forward),
+    // parent (u, v, w, p into the PAR buffers) and bound_flow
+    const char* vn[3] = {"U", "V", "W"};
+    const char* sn[3] = {"P", nullptr, nullptr};
     for (int l = c->minlevel; l <= c->maxlevel; ++l) {
         connect(*c, l, 1, c->F("U"), c->F("V"), c->F("W"), nullptr, nullptr, nullptr, false, true, 1);
-        bound_flow(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
+        parent(*c, l, vn, sn, false);
+        bound_flow(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"), l);
     }
     mgpoisl(*c, dtrk * dt, st);
     (void)ittot;

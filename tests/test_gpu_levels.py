@@ -1,7 +1,8 @@
 """Inter-level operators on the GPU (plain FP64 form) against the oracle, bit
 for bit: parent, ftoc (every restriction kind), ctof, bound_pressure (with
-and without BP) and bound_flow on PAR faces (BP = 1 and with blocked
-cells), on the two-level hierarchies of cases.refined_box."""
+and without BP), bound_flow on PAR faces (BP = 1 and with blocked cells),
+tstle4 with tstle4_par, the multi-level pressure solve and the multi-level
+RK stage, on the two-level hierarchies of cases.refined_box."""
 import numpy as np
 import pytest
 
@@ -130,8 +131,48 @@ def test_multilevel_mgpoisl_bit_exact(gpu_lib, oracle_lib, h, psolver):
         assert np.array_equal(gs.get(n), o.get(n)), n
 
 
-def test_stage_refuses_hierarchies(gpu_lib, oracle_lib):
+@pytest.mark.parametrize("h", HIERARCHIES)
+def test_tstle4_par_bit_exact(gpu_lib, oracle_lib, h):
+    """tstle4 with tstle4_par on every grid with PAR faces."""
+    case, gs, o = _pair(gpu_lib, oracle_lib, h)
+    rng = np.random.default_rng(18)
+    _set((gs, o), {**{n: rng.standard_normal(case.idim3d) for n in "UVWP"},
+                   "G": 1e-2 * (1.0 + rng.random(case.idim3d))})
+    for s in (gs, o):
+        s.tstle4()
+    for n in ("UO", "VO", "WO"):
+        assert np.array_equal(gs.get(n), o.get(n)), n
+
+
+@pytest.mark.parametrize("h", HIERARCHIES)
+def test_multilevel_stage_bit_exact(gpu_lib, oracle_lib, h):
+    """Three RK stages of timeintegrate_flow on the hierarchy, six outer
+    iterations of the pressure solve fixed per stage; every field bit for
+    bit."""
     from oracle.binding import rk_scheme
-    case, gs, o = _pair(gpu_lib, oracle_lib, HIERARCHIES[0])
+    case = cases.refined_box(h["nx"], h["ny"], h["nz"], n=h["n"], refine=h["refine"])
+    prm = abi.make_flow_params(gmol=1e-2, epcorr=1e-12, nouter=6, ninner=5, nouter_min=6)
+    gs, o = gpu_lib.Solver(case, prm), oracle_lib.Oracle(case, prm)
+    rng = np.random.default_rng(19)
+    _set((gs, o), {**{n: rng.standard_normal(case.idim3d) for n in "UVW"},
+                   "G": np.full(case.idim3d, 1e-2)})
+    rk = rk_scheme("williamson")
+    for s in (gs, o):
+        s.set_hierarchy(case.iparent, case.position)
+        for lvl in (1, 2):
+            s.connect(lvl, 2, v1="U", v2="V", v3="W", s1="P", corners=True)
+        prepare_levels(s, case)
+    for irk in (1, 2, 3):
+        sg = gs.timeintegrate_flow(1, 1, 0.0, 1e-2, irk, rk)
+        so = o.timeintegrate_flow(1, 1, 0.0, 1e-2, irk, rk)
+        assert (sg.ipc, sg.nouter_done, sg.maxrhs) == (so.ipc, so.nouter_done, so.maxrhs)
+        for n in ("U", "V", "W", "P", "DU", "DV", "DW", "UO", "VO", "WO"):
+            assert np.array_equal(gs.get(n), o.get(n)), (irk, n)
+
+
+def test_mixed_form_refuses_hierarchies(gpu_lib):
+    case = cases.refined_box(2, 2, 2, n=8, refine=(1,))
+    prm = abi.make_flow_params(gmol=1e-2, epcorr=1e-12, nouter=4, ninner=2, nouter_min=0,
+                               form=abi.FORM_MIXED)
     with pytest.raises(gpu_lib.MgletError):
-        gs.timeintegrate_flow(1, 1, 0.0, 1e-3, 1, rk_scheme("williamson"))
+        gpu_lib.Solver(case, prm)

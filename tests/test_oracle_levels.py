@@ -557,8 +557,82 @@ def test_multilevel_projection_is_divergence_free(case, psolver):
     assert after.max() < 1e-9 * before.max()
 
 
-def test_stage_refuses_hierarchies(case):
-    from oracle.binding import OracleError, rk_scheme
+def test_tstle4_par_keeps_a_uniform_flow(case):
+    """A uniform flow stays a steady solution of tstle4 with PAR faces
+    (tstle4_mod.F90:532-1753): the upwind term's second difference
+    0.5*v - 1.5*v + v and the difference between the flux of the coarse
+    velocities and the standard flux are exactly zero, so UO, VO and WO are
+    zero on every grid."""
     o = _oracle(case)
-    with pytest.raises(OracleError):
-        o.timeintegrate_flow(1, 1, 0.0, 1e-3, 1, rk_scheme("williamson"))
+    for n, val in zip("UVWPG", (1.0, 2.0, -3.0, 0.5, 1e-2)):
+        o.set(n, np.full(case.idim3d, val))
+    o.tstle4()
+    for n in ("UO", "VO", "WO"):
+        assert not np.any(o.get(n)), n
+
+
+def _par_layers(case):
+    """Per grid, the cells tstle4_par may write: on a PAR face the last two
+    layers inside the grid (front i = 3, 4; back i = ii-3, ii-2; and the
+    same in j and k)."""
+    m = np.zeros((case.ngrid, case.ii, case.jj, case.kk), dtype=bool)
+    for g in range(case.ngrid):
+        bc = case.bctype[g]
+        if bc[0] == abi.BC_PAR: m[g, 2:4] = True
+        if bc[1] == abi.BC_PAR: m[g, -4:-2] = True
+        if bc[2] == abi.BC_PAR: m[g, :, 2:4] = True
+        if bc[3] == abi.BC_PAR: m[g, :, -4:-2] = True
+        if bc[4] == abi.BC_PAR: m[g, :, :, 2:4] = True
+        if bc[5] == abi.BC_PAR: m[g, :, :, -4:-2] = True
+    return m.ravel()
+
+
+def test_tstle4_par_acts_on_the_par_layers_only(case):
+    """tstle4 on the refined case against the same grids with their PAR
+    faces relabelled FIX: kon, diff and gradp treat both codes alike (only
+    CON is special there), so the two differ by tstle4_par alone, which
+    writes the two layers inside each PAR face and nothing else."""
+    import dataclasses
+    from oracle.binding import Oracle
+    fixc = dataclasses.replace(case, bctype=np.where(case.bctype == abi.BC_PAR, abi.BC_FIX,
+                                                     case.bctype).astype(np.int32))
+    o, f = _oracle(case), Oracle(fixc, _prm())
+    rng = np.random.default_rng(21)
+    for n in "UVWP":
+        a = rng.standard_normal(case.idim3d)
+        o.set(n, a)
+        f.set(n, a)
+    g = 1e-2 * (1.0 + rng.random(case.idim3d))
+    o.set("G", g)
+    f.set("G", g)
+    o.tstle4()
+    f.tstle4()
+    mask = _par_layers(case)
+    for n in ("UO", "VO", "WO"):
+        d = o.get(n) - f.get(n)
+        assert not np.any(d[~mask]), n
+        assert np.count_nonzero(d[mask]) > 0.5 * mask.sum() / 3, n
+
+
+def test_multilevel_stage_is_divergence_free(case):
+    """timeintegrate_flow on the two-level hierarchy (tstle4 with
+    tstle4_par, rkstep, per level connect / parent / bound_flow, mgpoisl):
+    after each of the three RK stages the velocity is divergence free on
+    every grid to the solver tolerance."""
+    from oracle.binding import Oracle, rk_scheme
+    prm = abi.make_flow_params(gmol=1e-2, epcorr=1e-11, nouter=200, ninner=5, nouter_min=0)
+    o = Oracle(case, prm)
+    o.set_hierarchy(case.iparent, case.position)
+    rng = np.random.default_rng(22)
+    for n in "UVW":
+        o.set(n, rng.standard_normal(case.idim3d))
+    o.set("G", np.full(case.idim3d, 1e-2))
+    for lvl in (1, 2):
+        o.connect(lvl, 2, v1="U", v2="V", v3="W", s1="P", corners=True)
+    prepare_levels(o, case)
+    o.mgpoisl(1.0)
+    rk = rk_scheme("williamson")
+    for irk in (1, 2, 3):
+        st = o.timeintegrate_flow(1, 1, 0.0, 1e-2, irk, rk)
+        assert st.maxrhs / st.prefak < 1e-11 and st.nouter_done < 200
+        assert _divmax(o, case).max() < 1e-9
