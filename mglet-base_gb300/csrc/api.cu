@@ -682,6 +682,14 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
         if (!h1[q]) return bail(fail(MGLET_ERR_ARG, "create: missing spacing array"));
         if (int rc = alloc1(c, n1[q], len1[q % 3], h1[q])) return bail(rc);
     }
+    // tauwin's dds**(-cwb) for every cell width (wernerwengle_mod.F90:81),
+    // taken once on the host
+    for (int q = 0; q < 3; ++q) {
+        std::vector<double> wv(h1[6 + q], h1[6 + q] + len1[q]);
+        for (double& x : wv) x = std::pow(x, -(1.0 / 7.0));
+        const char* wn[3] = {"WWX", "WWY", "WWZ"};
+        if (int rc = alloc1(c, wn[q], len1[q], wv.data())) return bail(rc);
+    }
     const char* rn[6] = {"RDX", "RDY", "RDZ", "RDDX", "RDDY", "RDDZ"};
     const char* sn[6] = {"DX", "DY", "DZ", "DDX", "DDY", "DDZ"};
     for (int q = 0; q < 6; ++q) {

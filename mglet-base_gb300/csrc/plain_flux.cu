@@ -19,10 +19,20 @@ namespace {
 struct GridPtrs {
     int kk, jj, ii;
     const double *dx, *dy, *dz, *ddx, *ddy, *ddz, *rdx, *rdy, *rdz, *rddx, *rddy, *rddz;
+    const double *wx, *wy, *wz;   // ddx**(-cwb), ddy**(-cwb), ddz**(-cwb)
 };
 
 struct Spacing {
     const double *dx, *dy, *dz, *ddx, *ddy, *ddz, *rdx, *rdy, *rdz, *rddx, *rddy, *rddz;
+    const double *wx, *wy, *wz;
+};
+
+// The Werner-Wengle constants (wernerwengle_mod.F90:13-28) and the face
+// codes of one grid, for swcle3d on NOS (code 5) faces.
+struct Wall {
+    double rho, gmol, cpo4, cpo5, cpo6, cpo8;
+    int bc[6];
+    bool any;
 };
 
 #define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
@@ -34,10 +44,57 @@ __device__ __forceinline__ double hm(double a, double b, double gmol) {
     return a * b / dmax(a + b, gmol);
 }
 
-// One output point of tstle4 for the U component (kon + diff + gradp).
+// tauwin (wernerwengle_mod.F90:64-87) over rho and dds, swcle3d_one
+// (tstle4_mod.F90:1832-1844); ddsb = dds**(-cwb) comes from the host.
+__device__ double swcle3d_one(const Wall& q, double dds, double ddsb, double u) {
+    const double vz = copysign(1.0, u);
+    const double uquern = fabs(u);
+    double tauwin;
+    if (uquern >= q.cpo6 / dds)
+        tauwin = vz * q.rho * pow(ddsb * (q.cpo4 * uquern + q.cpo5 / dds), q.cpo8);
+    else
+        tauwin = vz * 2.0 * q.gmol * uquern / dds;
+    return tauwin / q.rho / dds;
+}
+
+// swcle3d (tstle4_mod.F90:1756-1829) at one point, per component in the
+// reference's face order (front, back, right, left, bottom, top); each face
+// acts on the layer next to the wall over its rows 2..n-1.
+__device__ double wall_u(double x, int k, int j, int i, const GridPtrs& s, const Wall& q, double u) {
+    if (!q.any) return x;
+    const bool ik = i >= 2 && i <= s.ii - 1 && k >= 2 && k <= s.kk - 1;
+    const bool ij = i >= 2 && i <= s.ii - 1 && j >= 2 && j <= s.jj - 1;
+    if (q.bc[2] == 5 && j == 3 && ik) x = x - swcle3d_one(q, s.ddy[j], s.wy[j], u);
+    if (q.bc[3] == 5 && j == s.jj - 2 && ik) x = x - swcle3d_one(q, s.ddy[j], s.wy[j], u);
+    if (q.bc[4] == 5 && k == 3 && ij) x = x - swcle3d_one(q, s.ddz[k], s.wz[k], u);
+    if (q.bc[5] == 5 && k == s.kk - 2 && ij) x = x - swcle3d_one(q, s.ddz[k], s.wz[k], u);
+    return x;
+}
+__device__ double wall_v(double x, int k, int j, int i, const GridPtrs& s, const Wall& q, double v) {
+    if (!q.any) return x;
+    const bool jk = j >= 2 && j <= s.jj - 1 && k >= 2 && k <= s.kk - 1;
+    const bool ij = i >= 2 && i <= s.ii - 1 && j >= 2 && j <= s.jj - 1;
+    if (q.bc[0] == 5 && i == 3 && jk) x = x - swcle3d_one(q, s.ddx[i], s.wx[i], v);
+    if (q.bc[1] == 5 && i == s.ii - 2 && jk) x = x - swcle3d_one(q, s.ddx[i], s.wx[i], v);
+    if (q.bc[4] == 5 && k == 3 && ij) x = x - swcle3d_one(q, s.ddz[k], s.wz[k], v);
+    if (q.bc[5] == 5 && k == s.kk - 2 && ij) x = x - swcle3d_one(q, s.ddz[k], s.wz[k], v);
+    return x;
+}
+__device__ double wall_w(double x, int k, int j, int i, const GridPtrs& s, const Wall& q, double w) {
+    if (!q.any) return x;
+    const bool jk = j >= 2 && j <= s.jj - 1 && k >= 2 && k <= s.kk - 1;
+    const bool ik = i >= 2 && i <= s.ii - 1 && k >= 2 && k <= s.kk - 1;
+    if (q.bc[0] == 5 && i == 3 && jk) x = x - swcle3d_one(q, s.ddx[i], s.wx[i], w);
+    if (q.bc[1] == 5 && i == s.ii - 2 && jk) x = x - swcle3d_one(q, s.ddx[i], s.wx[i], w);
+    if (q.bc[2] == 5 && j == 3 && ik) x = x - swcle3d_one(q, s.ddy[j], s.wy[j], w);
+    if (q.bc[3] == 5 && j == s.jj - 2 && ik) x = x - swcle3d_one(q, s.ddy[j], s.wy[j], w);
+    return x;
+}
+
+// One output point of tstle4 for the U component (kon, swcle3d, diff, gradp).
 __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
                            const double* w, const double* ut, const double* vt, const double* wt,
-                           const double* p, const double* gg, const GridPtrs& s,
+                           const double* p, const double* gg, const GridPtrs& s, const Wall& wl,
                            double gmol, double rho, double gpx) {
     const double *dx = s.dx, *dy = s.dy, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
@@ -59,6 +116,7 @@ __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u,
         double qb = 0.5 * fb * (A(u, k - 1, j, i) + A(u, k, j, i));
         uo = -(qe - qw + qn - qs + qt - qb) * rdx[i] * rddy[j] * rddz[k];
     }
+    uo = wall_u(uo, k, j, i, s, wl, A(u, k, j, i));
     {
         double ax = ddy[j] * ddz[k], ay = dx[i] * ddz[k], az = dx[i] * ddy[j];
         double ge = A(gg, k, j, i + 1);
@@ -89,7 +147,7 @@ __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u,
 
 __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
                            const double* w, const double* ut, const double* vt, const double* wt,
-                           const double* p, const double* gg, const GridPtrs& s,
+                           const double* p, const double* gg, const GridPtrs& s, const Wall& wl,
                            double gmol, double rho, double gpy) {
     const double *dy = s.dy, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
@@ -111,6 +169,7 @@ __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u,
         double qb = 0.5 * fb * (A(v, k - 1, j, i) + A(v, k, j, i));
         vo = -(qe - qw + qn - qs + qt - qb) * rddx[i] * rdy[j] * rddz[k];
     }
+    vo = wall_v(vo, k, j, i, s, wl, A(v, k, j, i));
     {
         double ax = dy[j] * ddz[k], ay = ddx[i] * ddz[k], az = ddx[i] * dy[j];
         double ge = hm(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hm(A(gg, k, j + 1, i), A(gg, k, j + 1, i + 1), gmol);
@@ -141,7 +200,7 @@ __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u,
 
 __device__ double wo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
                            const double* w, const double* ut, const double* vt, const double* wt,
-                           const double* p, const double* gg, const GridPtrs& s,
+                           const double* p, const double* gg, const GridPtrs& s, const Wall& wl,
                            double gmol, double rho, double gpz) {
     const double *dz = s.dz, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
@@ -163,6 +222,7 @@ __device__ double wo_point(int k, int j, int i, int kk, int jj, const double* u,
         double qb = 0.5 * fb * (A(w, k - 1, j, i) + A(w, k, j, i));
         wo = -(qe - qw + qn - qs + qt - qb) * rddx[i] * rddy[j] * rdz[k];
     }
+    wo = wall_w(wo, k, j, i, s, wl, A(w, k, j, i));
     {
         double ax = ddy[j] * dz[k], ay = ddx[i] * dz[k], az = ddx[i] * ddy[j];
         double ge = hm(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j, i + 1), gmol);
@@ -200,7 +260,7 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
                                                 const double* __restrict__ UT, const double* __restrict__ VT,
                                                 const double* __restrict__ WT,
                                                 const double* __restrict__ P, const double* __restrict__ Gf,
-                                                double gmol, double rho, double gx, double gy, double gz) {
+                                                Wall wl, double gx, double gy, double gz) {
     const DevGrid G = grids[blockIdx.y];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int npts = kk * jj * ii;
@@ -215,6 +275,7 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
     s.ddx = sp.ddx + G.ipx - 1; s.ddy = sp.ddy + G.ipy - 1; s.ddz = sp.ddz + G.ipz - 1;
     s.rdx = sp.rdx + G.ipx - 1; s.rdy = sp.rdy + G.ipy - 1; s.rdz = sp.rdz + G.ipz - 1;
     s.rddx = sp.rddx + G.ipx - 1; s.rddy = sp.rddy + G.ipy - 1; s.rddz = sp.rddz + G.ipz - 1;
+    s.wx = sp.wx + G.ipx - 1; s.wy = sp.wy + G.ipy - 1; s.wz = sp.wz + G.ipz - 1;
     const long long o = G.ip3;
     const double *u = U + o, *v = V + o, *w = W + o, *p = P + o, *g = Gf + o;
     const double *ut = UT + o, *vt = VT + o, *wt = WT + o;
@@ -226,13 +287,23 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
     const int nfu = nfro == 3 ? 1 : 0, nrv = nrgt == 3 ? 1 : 0, nbw = nbot == 3 ? 1 : 0;
     const double gfl = (double)G.gradpflag;
     const bool jin = j >= 3 && j <= jj - 2, kin = k >= 3 && k <= kk - 2, iin = i >= 3 && i <= ii - 2;
-    double ru = 0.0, rv = 0.0, rw = 0.0;
+    for (int f = 0; f < 6; ++f) wl.bc[f] = G.bc[f];
+    wl.any = nfro == 5 || nbac == 5 || nrgt == 5 || nlft == 5 || nbot == 5 || ntop == 5;
+    const double gmol = wl.gmol, rho = wl.rho;
+    // outside the flux ranges uo, vo, wo are zero apart from swcle3d's rows
+    double ru, rv, rw;
     if (i >= 3 - nfu && i <= ii - 3 + nbu && jin && kin)
-        ru = uo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, gmol, rho, gx * gfl);
+        ru = uo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gx * gfl);
+    else
+        ru = wall_u(0.0, k, j, i, s, wl, u[t]);
     if (iin && j >= 3 - nrv && j <= jj - 3 + nlv && kin)
-        rv = vo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, gmol, rho, gy * gfl);
+        rv = vo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gy * gfl);
+    else
+        rv = wall_v(0.0, k, j, i, s, wl, v[t]);
     if (iin && jin && k >= 3 - nbw && k <= kk - 3 + ntw)
-        rw = wo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, gmol, rho, gz * gfl);
+        rw = wo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gz * gfl);
+    else
+        rw = wall_w(0.0, k, j, i, s, wl, w[t]);
     uo[o + t] = ru;
     vo[o + t] = rv;
     wo[o + t] = rw;
@@ -258,6 +329,7 @@ static Spacing spacing(Ctx* c) {
     s.ddx = c->L("DDX"); s.ddy = c->L("DDY"); s.ddz = c->L("DDZ");
     s.rdx = c->L("RDX"); s.rdy = c->L("RDY"); s.rdz = c->L("RDZ");
     s.rddx = c->L("RDDX"); s.rddy = c->L("RDDY"); s.rddz = c->L("RDDZ");
+    s.wx = c->L("WWX"); s.wy = c->L("WWY"); s.wz = c->L("WWZ");
     return s;
 }
 
@@ -272,9 +344,18 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
                   const double* p, const double* g) {
     ProfScope ps_(c, "tstle4");
     dim3 grid((max_points(c) + 255) / 256, c->ngrid);
+    // wernerwengle_mod.F90:13-28 init_wernerwengle
+    Wall wl = {};
+    const double gmol = c->prm.gmol, rho = c->prm.rho, cwa = 8.3, cwb = 1.0 / 7.0;
+    const double cpo1 = 1.0 - cwb, cpo2 = 1.0 + cwb;
+    wl.rho = rho;
+    wl.gmol = gmol;
+    wl.cpo4 = cpo2 / cwa * std::pow(gmol / rho, cwb);
+    wl.cpo5 = 0.5 * cpo1 * std::pow(cwa, cpo2 / cpo1) * std::pow(gmol / rho, cpo2);
+    wl.cpo6 = 0.5 * gmol / rho * std::pow(cwa, 2.0 / cpo1);
+    wl.cpo8 = 2.0 / cpo2;
     k_tstle4<<<grid, 256, 0, c->stream>>>(c->d_grids, spacing(c), uo, vo, wo, u, v, w, ut, vt, wt, p, g,
-                                          c->prm.gmol, c->prm.rho, c->prm.gradp[0],
-                                          c->prm.gradp[1], c->prm.gradp[2]);
+                                          wl, c->prm.gradp[0], c->prm.gradp[1], c->prm.gradp[2]);
     MG_LAUNCHED(c);
     // tstle4_mod.F90:114: tstle4_par after kon, diff and gradp (PAR faces)
     return launch_tstle4_par(c, uo, vo, wo, u, v, w, ut, vt, wt);

@@ -2308,6 +2308,80 @@ void tstle4_par(int kk, int jj, int ii, double* uo, double* vo, double* wo, cons
 
 // tstle4_mod.F90:139-265 tstle4_kon, :268-458 tstle4_diff, :461-529 tstle4_gradp,
 // :532-1753 tstle4_par
+// wernerwengle_mod.F90:13-28 init_wernerwengle: the constants of the
+// Werner-Wengle wall function for gmol and rho
+struct WernerWengle {
+    double rho, gmol, cwb, cpo4, cpo5, cpo6, cpo8;
+};
+
+WernerWengle werner_wengle(double gmol, double rho) {
+    WernerWengle q;
+    const double cwa = 8.3;
+    q.rho = rho;
+    q.gmol = gmol;
+    q.cwb = 1.0 / 7.0;
+    const double cpo1 = 1.0 - q.cwb;
+    const double cpo2 = 1.0 + q.cwb;
+    q.cpo4 = cpo2 / cwa * std::pow(gmol / rho, q.cwb);
+    q.cpo5 = 0.5 * cpo1 * std::pow(cwa, cpo2 / cpo1) * std::pow(gmol / rho, cpo2);
+    q.cpo6 = 0.5 * gmol / rho * std::pow(cwa, 2.0 / cpo1);
+    q.cpo8 = 2.0 / cpo2;
+    return q;
+}
+
+// wernerwengle_mod.F90:64-87 tauwin and tstle4_mod.F90:1832-1844
+// swcle3d_one: the wall shear over rho and the wall-normal width dds
+double swcle3d_one(const WernerWengle& q, double dds, double u) {
+    const double vz = std::copysign(1.0, u);
+    const double uquern = std::fabs(u);
+    double tauwin;
+    if (uquern >= q.cpo6 / dds) {
+        const double ddsb = std::pow(dds, -q.cwb);
+        tauwin = vz * q.rho * std::pow(ddsb * (q.cpo4 * uquern + q.cpo5 / dds), q.cpo8);
+    } else {
+        tauwin = vz * 2.0 * q.gmol * uquern / dds;
+    }
+    return tauwin / q.rho / dds;
+}
+
+// tstle4_mod.F90:1756-1829 swcle3d: on NOS (code 5) faces the wall shear of
+// the two tangential components is taken from uo, vo, wo in the layer next to
+// the wall, over the whole face including its ghost rows (2..n-1)
+void swcle3d(const WernerWengle& q, int kk, int jj, int ii, double* uo, double* vo, double* wo,
+             const double* u, const double* v, const double* w, const double* ddx,
+             const double* ddy, const double* ddz, int nfro, int nbac, int nrgt, int nlft, int nbot,
+             int ntop) {
+#define A(a, k, j, i) a[IX(k, j, i)]
+    for (int side = 0; side < 2; ++side) {       // FRONT, BACK
+        if ((side ? nbac : nfro) != 5) continue;
+        const int i = side ? ii - 2 : 3;
+        for (int j = 2; j <= jj - 1; ++j)
+            for (int k = 2; k <= kk - 1; ++k) {
+                A(vo, k, j, i) = A(vo, k, j, i) - swcle3d_one(q, ddx[i], A(v, k, j, i));
+                A(wo, k, j, i) = A(wo, k, j, i) - swcle3d_one(q, ddx[i], A(w, k, j, i));
+            }
+    }
+    for (int side = 0; side < 2; ++side) {       // RIGHT, LEFT
+        if ((side ? nlft : nrgt) != 5) continue;
+        const int j = side ? jj - 2 : 3;
+        for (int i = 2; i <= ii - 1; ++i)
+            for (int k = 2; k <= kk - 1; ++k) {
+                A(uo, k, j, i) = A(uo, k, j, i) - swcle3d_one(q, ddy[j], A(u, k, j, i));
+                A(wo, k, j, i) = A(wo, k, j, i) - swcle3d_one(q, ddy[j], A(w, k, j, i));
+            }
+    }
+    for (int side = 0; side < 2; ++side) {       // BOTTOM, TOP
+        if ((side ? ntop : nbot) != 5) continue;
+        const int k = side ? kk - 2 : 3;
+        for (int i = 2; i <= ii - 1; ++i)
+            for (int j = 2; j <= jj - 1; ++j) {
+                A(uo, k, j, i) = A(uo, k, j, i) - swcle3d_one(q, ddz[k], A(u, k, j, i));
+                A(vo, k, j, i) = A(vo, k, j, i) - swcle3d_one(q, ddz[k], A(v, k, j, i));
+            }
+    }
+#undef A
+}
+
 void tstle4_grid(Ctx& c, int g) {
     const Grid& G = c.g[g];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
@@ -2400,7 +2474,9 @@ void tstle4_grid(Ctx& c, int g) {
                 double qb = 0.5 * fb * (A(w, k - 1, j, i) + A(w, k, j, i));
                 A(wo, k, j, i) = -(qe - qw + qn - qs + qt - qb) * rddx[i] * rddy[j] * rdz[k];
             }
-    // ---- diff (swcle3d acts on NOS faces only; NOS is rejected at create)
+    // ---- diff: swcle3d (tstle4_mod.F90:315-316), then the viscous fluxes
+    swcle3d(werner_wengle(gmol, rho), kk, jj, ii, uo, vo, wo, u, v, w, ddx, ddy, ddz, nfro, nbac,
+            nrgt, nlft, nbot, ntop);
     auto hm = [&](double a, double b) { return a * b / std::max(a + b, gmol); };
     for (int i = 3 - nfu; i <= ii - 3 + nbu; ++i)
         for (int j = 3; j <= jj - 2; ++j)

@@ -1,5 +1,7 @@
 """FIX / OP1 / NOS / SLI faces on the GPU (plain FP64 form) against the
-oracle: bound_flow alone and whole stages, bit for bit."""
+oracle: bound_flow alone and whole stages, bit for bit; tstle4 with the
+Werner-Wengle wall function of NOS walls (bit for bit in its laminar branch,
+to CUDA's pow in the turbulent one)."""
 import numpy as np
 import pytest
 
@@ -73,6 +75,55 @@ def test_wall_stages_bit_exact(gpu_lib, oracle_lib, walls):
             assert sg.ipc == so.ipc and sg.maxrhs == so.maxrhs
     for nm in "UVWP":
         assert np.array_equal(gs.get(nm), o.get(nm)), nm
+
+
+@pytest.mark.parametrize("gmol,amplitude", [(1e-2, 0.3), (1e-3, 1.0), (1e-5, 1.0)])
+def test_wall_function_tstle4(gpu_lib, oracle_lib, gmol, amplitude):
+    """tstle4 with the Werner-Wengle wall function on six NOS walls.  In the
+    laminar sublayer (gmol 1e-2) the result is bit for bit the oracle's; the
+    turbulent branch raises a base to the power 2/(1+1/7) with CUDA's pow
+    (at most 2 ulp from the correctly rounded value) where the oracle uses
+    the C library's, so there each wall term agrees to a relative 1e-15 and
+    every other point bit for bit."""
+    from test_oracle_wallfunction import ww_constants, wall_case, wall_fields, wall_terms
+    case = wall_case()
+    prm = abi.make_flow_params(gmol=gmol, epcorr=1e-12, nouter=4, ninner=2, nouter_min=0)
+    fields = wall_fields(case, amplitude, 33, gmol)
+    gs, o = gpu_lib.Solver(case, prm), oracle_lib.Oracle(case, prm)
+    _load((gs, o), case, fields, {}, {})
+    gs.tstle4()
+    o.tstle4()
+    _, M, nturb, _ = wall_terms(case, ww_constants(gmol, 1.0), fields["U"], fields["V"], fields["W"])
+    for nm in ("UO", "VO", "WO"):
+        a, b = gs.get(nm), o.get(nm)
+        m = M[nm[0]]
+        assert np.array_equal(a[~m], b[~m]), nm
+        if nturb == 0:
+            assert np.array_equal(a, b), nm
+        else:
+            assert np.abs(a[m] - b[m]).max() <= 1e-14 * np.abs(b).max(), nm
+
+
+def test_turbulent_wall_stage(gpu_lib, oracle_lib):
+    """Three stages with NOS walls in the wall function's turbulent branch
+    (gmol 1e-5), the pressure solve's six outer iterations fixed: the fields
+    follow the oracle's to a relative 1e-12 (the pow difference above,
+    carried through the solve)."""
+    case = cases.periodic_box(2, 2, 1, n=8, length=(2.0, 2.0, 1.0), walls={5: abi.BC_NOS, 6: abi.BC_NOS})
+    u, v, w, p = cases.taylor_green(case)
+    fields = dict(zip("UVWP", (u + 0.5, v, w, p)))
+    prm = _prm(gmol=1e-5)
+    gs, o = gpu_lib.Solver(case, prm), oracle_lib.Oracle(case, prm)
+    _load((gs, o), case, fields, {}, {})
+    for s in (gs, o):
+        s.connect(0, 2, "U", "V", "W", "P", corners=True)
+    rkg, rko = gpu_lib.rk_scheme("williamson"), oracle_lib.rk_scheme("williamson")
+    for irk in range(1, 4):
+        gs.timeintegrate_flow(1, 1, 0.0, 2e-3, irk, rkg)
+        o.timeintegrate_flow(1, 1, 0.0, 2e-3, irk, rko)
+    for nm in "UVWP":
+        a, b = gs.get(nm), o.get(nm)
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), nm
 
 
 def test_mixed_form_refuses_walls(gpu_lib):
