@@ -232,9 +232,11 @@ int mglet_gpu_get_buffer(mglet_ctx* ctx, const char* name, int32_t igrid, int32_
  * adds tstle4_par on PAR faces (src/flow/tstle4_mod.F90:532-1753), and
  * mglet_gpu_mgpoisl and mglet_gpu_timeintegrate_flow run the multi-level
  * schedule (per level connect, parent and bound_flow before the pressure
- * solve, timeintegration_mod.F90:117-122).  Both need the hierarchy set;
- * ghost-cell contexts with more than one level are refused
- * (MGLET_ERR_UNSUPPORTED): the ghost-cell restriction is not built.
+ * solve, timeintegration_mod.F90:117-122).  Both need the hierarchy set.
+ * With the ghost-cell IB the multi-level schedule of setibvalues (level
+ * sweeps, ftoc and par_ftoc_norm between them), setpointvalues and
+ * setsdivfield runs too; call mglet_gpu_set_hierarchy before
+ * mglet_gpu_set_ghostcell.
  *
  * gridinfo%iparent and i/j/kposition (src/core/grids_mod.F90:768-781):
  * iparent[g] the 1-based parent of grid g+1 (0 = none, one level coarser),
@@ -255,12 +257,23 @@ int mglet_gpu_parent(mglet_ctx* ctx, int32_t ilevel, const char* v1, const char*
 /* ftoc(ilevel, ff, fc, flag) (src/ib/ftoc_mod.F90:39-60,581-626 with the no-IB
  * restriction src/ib/noib_restrict_mod.F90:126-298): the grids of level
  * ilevel restricted into their parents -- face-area means for U, V, W,
- * volume means for P, R, S, T.  ff and fc may be the same field. */
+ * volume means for P, R, S, T.  With the ghost-cell IB P and R take the
+ * BP-weighted forms of src/ib/gc_restrict_mod.F90:59-259 and T is refused
+ * (it weighs by the temperature blocking BT, which is not kept).  ff and fc
+ * may be the same field. */
 int mglet_gpu_ftoc(mglet_ctx* ctx, int32_t ilevel, const char* ff, const char* fc, char flag);
 /* ftoc(ilevel, v1, v2, v3, s1, s2, s3) (src/ib/ftoc_mod.F90:64-85): flags U, V,
  * W for v1..v3 and P for the scalars, each field into itself. */
 int mglet_gpu_ftoc_multiple(mglet_ctx* ctx, int32_t ilevel, const char* v1, const char* v2,
                             const char* v3, const char* s1, const char* s2, const char* s3);
+/* par_ftoc_norm(ilevel, v1, v2, v3, sum) (src/ib/par_ftoc_mod.F90:36-810):
+ * on every PAR face of the grids of level ilevel the face-normal component
+ * (v1 on x faces, v2 on y, v3 on z), the area mean of 2x2 fine faces (the
+ * plain sum when sum is nonzero), is written into the parent -- inside it,
+ * or onto its own face when the PAR lies on a coarse face, and then also
+ * onto the opposite face of the parent's neighbour across it. */
+int mglet_gpu_par_ftoc_norm(mglet_ctx* ctx, int32_t ilevel, const char* v1, const char* v2,
+                            const char* v3, int32_t sum);
 /* ctof(ilevel, ff, fc) (src/ib/ctof/ctof_mod.F90:16-56, ctof1_mod.F90:167-331):
  * every point of the grids of level ilevel, ghosts included, takes the
  * value of the parent cell it lies in; nothing on the coarsest level. */

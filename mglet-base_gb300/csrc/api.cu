@@ -433,14 +433,12 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
     return 0;
 }
 
-// The pressure solve runs on hierarchies once the parents are known; the
-// ghost-cell restriction (gc_restrict_mod.F90) is not built.
+// The pressure solve and the stage run on hierarchies once the parents are
+// known.
 int hierarchy_ready(Ctx* c) {
     for (int g = 0; g < c->ngrid; ++g)
         if (c->grids[g].level != c->minlevel && c->hier[g].x < 0)
-            return fail(MGLET_ERR_ARG, "mgpoisl: a fine grid without parent (mglet_gpu_set_hierarchy)");
-    if (c->minlevel != c->maxlevel && c->ibtype == 1)
-        return fail(MGLET_ERR_UNSUPPORTED, "mgpoisl: the ghost-cell restriction is not built");
+            return fail(MGLET_ERR_ARG, "a fine grid without parent (mglet_gpu_set_hierarchy first)");
     return 0;
 }
 
@@ -757,6 +755,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     for (auto& kv : c->fbuf) cudaFree(kv.second);
     cudaFree(c->d_hier);
     cudaFree(c->d_pargrids);
+    for (auto& kv : c->d_pftasks) cudaFree(kv.second);
     cudaFree(c->d_gridred);
     cudaFree(c->d_scalar);
     if (c->h_scalar) cudaFreeHost(c->h_scalar);
@@ -903,6 +902,15 @@ int mglet_gpu_ftoc(mglet_ctx* c, int32_t ilevel, const char* ff, const char* fc,
     return launch_ftoc(c, ilevel, f, g, flag);
 }
 
+int mglet_gpu_par_ftoc_norm(mglet_ctx* c, int32_t ilevel, const char* v1, const char* v2,
+                            const char* v3, int32_t sum) {
+    if (!c) return fail(MGLET_ERR_ARG, "par_ftoc_norm: null context");
+    double *u = field_ptr(c, v1), *v = field_ptr(c, v2), *w = field_ptr(c, v3);
+    if (!u || !v || !w) return fail(MGLET_ERR_NAME, "par_ftoc_norm: unknown field");
+    cudaSetDevice(c->device);
+    return launch_par_ftoc_norm(c, ilevel, u, v, w, sum != 0);
+}
+
 int mglet_gpu_ftoc_multiple(mglet_ctx* c, int32_t ilevel, const char* v1, const char* v2,
                             const char* v3, const char* s1, const char* s2, const char* s3) {
     if (!c) return fail(MGLET_ERR_ARG, "ftoc: null context");
@@ -1025,6 +1033,8 @@ int mglet_gpu_set_ghostcell(mglet_ctx* c) {
     if (c->prm.form != MGLET_FORM_PLAIN)
         return fail(MGLET_ERR_UNSUPPORTED, "set_ghostcell: the ghost-cell IB runs in the plain form");
     cudaSetDevice(c->device);
+    if (c->minlevel != c->maxlevel)   // setsdivfield restricts SDIV level by level
+        if (int rc = hierarchy_ready(c)) return rc;
     if (c->gch.empty()) c->gch.resize(c->ngrid);
     c->ibtype = 1;
     if (int rc = launch_giteig(c)) return rc;
@@ -1034,6 +1044,7 @@ int mglet_gpu_set_ghostcell(mglet_ctx* c) {
     if (c->prm.psolver == MGLET_PSOLVER_SOR)
         return fail(MGLET_ERR_UNSUPPORTED, "set_ghostcell: SOR with blocked cells");
     if ((rc = gc_upload(c))) return rc;
+    c->gc_saved[0] = c->gc_saved[1] = false;
     MG_CUDA(cudaStreamSynchronize(c->stream));
     return 0;
 }

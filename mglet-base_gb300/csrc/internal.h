@@ -61,6 +61,15 @@ struct GcDev {
 // One box copy of connect_self_single (connect2_mod.F90:947-995): the
 // destination box starts at dst (flat element offset), the source box at
 // src; extents nk*nj*ni with per-grid strides.
+// One message of par_ftoc_norm (par_ftoc_mod.F90:513-779): the PAR face
+// iface of fine grid gf into grid gc, whose plane of coarse faces starts at
+// (i0, j0, k0) and runs na x nb along the two in-plane directions.
+struct PfTask {
+    int gf, gc, iface;
+    int i0, j0, k0;
+    int na, nb;
+};
+
 struct BoxCopy {
     long long dst, src;
     int nk, nj, ni;
@@ -134,6 +143,9 @@ struct Ctx {
     // ghost-cell IB: 0 NONE, 1 GHOSTCELL; host lists per grid (1..3 u, v, w;
     // 4 flux correction) until gc_upload, then their device copies
     int ibtype = 0;
+    // the ghost-cell saves of setibvalues ('S') and setpointvalues ('Z')
+    // have run since the lists were set: their restores may follow
+    bool gc_saved[2] = {false, false};
     std::vector<GcHostList> gch;
     GcDev gcd;
     // grid hierarchy (gridinfo%iparent, i/j/kposition): per grid {parent
@@ -148,6 +160,8 @@ struct Ctx {
     std::vector<int> pgrids[6];
     int* d_pgrids[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     int* d_pargrids = nullptr;                  // grids with any PAR face (tstle4_par)
+    std::map<int, std::vector<PfTask>> pftasks; // per level: par_ftoc_norm messages
+    std::map<int, PfTask*> d_pftasks;
     int npargrids = 0;
     std::map<int, std::vector<int>> plist[6];   // per level: grids with a parent and PAR on the face
     std::map<int, int*> d_plist[6];
@@ -250,7 +264,10 @@ int bound_init(Ctx* c);
 int alloc_field3(Ctx* c, const char* name);
 // ghost-cell IB (plain_gc.cu)
 int gc_upload(Ctx* c);                       // lists to the device, PWU/PWV/PWW, SDIV
-int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w);   // F C S R X Y Z
+// F C S R X Y Z on the grids of ilevel (0: every grid)
+int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w, int ilevel = 0);
+// par_ftoc_norm (par_ftoc_mod.F90:36-64) of the grids of ilevel
+int launch_par_ftoc_norm(Ctx* c, int ilevel, double* u, double* v, double* w, bool sum);
 int launch_maskbp(Ctx* c, double* u, double* v, double* w, double* p);
 int gc_setibvalues(Ctx* c, double* u, double* v, double* w);
 int gc_setpointvalues(Ctx* c, bool comp_new);

@@ -18,10 +18,11 @@ namespace {
 
 // modes F / X: var(intcell) = sum var(stcell) coeff + const
 __global__ void k_gc_sol(const DevGrid* __restrict__ grids, GcDev d, double* U, double* V,
-                         double* W, int ngrid, int vel) {
+                         double* W, int ngrid, int vel, int ilevel) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * ngrid) return;
     const int g = t / 3, cmp = t % 3;
+    if (ilevel && grids[g].level != ilevel) return;
     const GcSeg s = d.seg[4 * g + cmp];
     double* var = (cmp == 0 ? U : (cmp == 1 ? V : W)) + grids[g].ip3;
     const long long* xi = d.xpoli + s.xi;
@@ -42,10 +43,11 @@ __global__ void k_gc_sol(const DevGrid* __restrict__ grids, GcDev d, double* U, 
 
 // modes S / Z (save) and R / Y (restore)
 __global__ void k_gc_savrst(const DevGrid* __restrict__ grids, GcDev d, double* U, double* V,
-                            double* W, int ngrid, int vel, int save) {
+                            double* W, int ngrid, int vel, int save, int ilevel) {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= 3 * ngrid) return;
     const int g = t / 3, cmp = t % 3;
+    if (ilevel && grids[g].level != ilevel) return;
     const GcSeg s = d.seg[4 * g + cmp];
     double* var = (cmp == 0 ? U : (cmp == 1 ? V : W)) + grids[g].ip3;
     double* old = (vel ? d.oldsolvel : d.oldsol) + s.sv;
@@ -68,10 +70,11 @@ __global__ void k_gc_savrst(const DevGrid* __restrict__ grids, GcDev d, double* 
 // mode C: wmxpolsolcorr, one thread per grid
 __global__ void k_gc_corr(const DevGrid* __restrict__ grids, GcDev d, double* U, double* V,
                           double* W, const double* __restrict__ DDX, const double* __restrict__ DDY,
-                          const double* __restrict__ DDZ, int ngrid, int* err) {
+                          const double* __restrict__ DDZ, int ngrid, int* err, int ilevel) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= ngrid) return;
     const DevGrid G = grids[g];
+    if (ilevel && G.level != ilevel) return;
     const GcSeg s = d.seg[4 * g + 3];
     double *u = U + G.ip3, *v = V + G.ip3, *w = W + G.ip3;
     const double *ddx = DDX + G.ipx - 1, *ddy = DDY + G.ipy - 1, *ddz = DDZ + G.ipz - 1;
@@ -208,6 +211,8 @@ int gc_upload(Ctx* c) {
     k_gc_sdiv<<<nb, 128, 0, c->stream>>>(c->d_grids, d, S, c->L("DDX"), c->L("DDY"), c->L("DDZ"),
                                          c->ngrid, 1);
     MG_LAUNCHED(c);
+    for (int l = c->maxlevel; l > c->minlevel; --l)
+        if (int rc = launch_ftoc(c, l, S, S, 'S')) return rc;
     if (int rc = connect(c, 0, 2, nullptr, nullptr, nullptr, S, nullptr, nullptr, true, false, 0))
         return rc;
     k_gc_sdiv<<<nb, 128, 0, c->stream>>>(c->d_grids, d, S, c->L("DDX"), c->L("DDY"), c->L("DDZ"),
@@ -216,7 +221,7 @@ int gc_upload(Ctx* c) {
     return 0;
 }
 
-int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w) {
+int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w, int ilevel) {
     ProfScope ps_(c, "gc");
     const GcDev& d = c->gcd;
     const int nt = 3 * c->ngrid;
@@ -224,20 +229,30 @@ int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w) {
     case 'F':
     case 'X':
         k_gc_sol<<<(nt + 127) / 128, 128, 0, c->stream>>>(c->d_grids, d, u, v, w, c->ngrid,
-                                                           mode == 'X');
+                                                           mode == 'X', ilevel);
         break;
     case 'S':
     case 'Z':
     case 'R':
-    case 'Y':
-        k_gc_savrst<<<(nt + 127) / 128, 128, 0, c->stream>>>(
-            c->d_grids, d, u, v, w, c->ngrid, mode == 'Z' || mode == 'Y', mode == 'S' || mode == 'Z');
+    case 'Y': {
+        // a restore reads positions only a save has written
+        const int vel = mode == 'Z' || mode == 'Y', save = mode == 'S' || mode == 'Z';
+        if (!save && !c->gc_saved[vel]) {
+            set_error(vel ? "gc: restore Y before any save Z (setpointvalues with comp_new first, "
+                            "as flow_mod.F90:83 does)"
+                          : "gc: restore R before any save S (setibvalues first, as flow_mod.F90:84 does)");
+            return MGLET_ERR_ARG;
+        }
+        k_gc_savrst<<<(nt + 127) / 128, 128, 0, c->stream>>>(c->d_grids, d, u, v, w, c->ngrid, vel, save,
+                                                              ilevel);
+        if (save) c->gc_saved[vel] = true;
         break;
+    }
     case 'C': {
         int* err = reinterpret_cast<int*>(c->d_scalar + 7);
         MG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
         k_gc_corr<<<(c->ngrid + 127) / 128, 128, 0, c->stream>>>(
-            c->d_grids, d, u, v, w, c->L("DDX"), c->L("DDY"), c->L("DDZ"), c->ngrid, err);
+            c->d_grids, d, u, v, w, c->L("DDX"), c->L("DDY"), c->L("DDZ"), c->ngrid, err, ilevel);
         MG_LAUNCHED(c);
         int herr = 0;
         MG_CUDA(copy_on(c->stream, &herr, err, sizeof(int), cudaMemcpyDeviceToHost));
@@ -265,25 +280,47 @@ int launch_maskbp(Ctx* c, double* u, double* v, double* w, double* p) {
     return 0;
 }
 
-// setibvalues (gc_flowstencils_mod.F90:1393-1438), one level
+// setibvalues (gc_flowstencils_mod.F90:1393-1438) of U, V, W: per level
+// (parent,) the extrapolation F and the flux correction C, each followed by
+// bound_flow and connect; fine to coarse (ftoc of U, V, W, par_ftoc_norm);
+// per level again (parent,) C and the save S
 int gc_setibvalues(Ctx* c, double* u, double* v, double* w) {
-    auto conn = [&](int layers, bool corners) {
-        return connect(c, 0, layers, u, v, w, nullptr, nullptr, nullptr, corners, false, 0);
+    static const char* const vn[3] = {"U", "V", "W"};
+    static const char* const none[3] = {nullptr, nullptr, nullptr};
+    const bool ml = c->minlevel != c->maxlevel;
+    auto bound = [&](int l) { return launch_bound_flow(c, u, v, w, nullptr, ml ? l : 0); };
+    auto conn = [&](int l, int layers, bool corners) {
+        return connect(c, ml ? l : 0, layers, u, v, w, nullptr, nullptr, nullptr, corners, false, 0);
     };
-    if (int rc = launch_bound_flow(c, u, v, w, nullptr)) return rc;
-    if (int rc = conn(2, false)) return rc;
-    if (int rc = launch_gc_mode(c, 'F', u, v, w)) return rc;
-    if (int rc = launch_bound_flow(c, u, v, w, nullptr)) return rc;
-    if (int rc = conn(1, true)) return rc;
-    if (int rc = launch_gc_mode(c, 'C', u, v, w)) return rc;
-    if (int rc = launch_bound_flow(c, u, v, w, nullptr)) return rc;
-    if (int rc = conn(1, true)) return rc;
-    if (int rc = launch_bound_flow(c, u, v, w, nullptr)) return rc;
-    if (int rc = conn(1, true)) return rc;
-    if (int rc = launch_gc_mode(c, 'C', u, v, w)) return rc;
-    if (int rc = launch_bound_flow(c, u, v, w, nullptr)) return rc;
-    if (int rc = conn(1, true)) return rc;
-    return launch_gc_mode(c, 'S', u, v, w);
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+        if (ml)
+            if (int rc = launch_parent(c, l, vn, none, false)) return rc;
+        if (int rc = bound(l)) return rc;
+        if (int rc = conn(l, 2, false)) return rc;
+        if (int rc = launch_gc_mode(c, 'F', u, v, w, l)) return rc;
+        if (int rc = bound(l)) return rc;
+        if (int rc = conn(l, 1, true)) return rc;
+        if (int rc = launch_gc_mode(c, 'C', u, v, w, l)) return rc;
+        if (int rc = bound(l)) return rc;
+        if (int rc = conn(l, 1, true)) return rc;
+    }
+    for (int l = c->maxlevel; l > c->minlevel; --l) {
+        if (int rc = launch_ftoc(c, l, u, u, 'U')) return rc;
+        if (int rc = launch_ftoc(c, l, v, v, 'V')) return rc;
+        if (int rc = launch_ftoc(c, l, w, w, 'W')) return rc;
+        if (int rc = launch_par_ftoc_norm(c, l, u, v, w, false)) return rc;
+    }
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+        if (ml)
+            if (int rc = launch_parent(c, l, vn, none, false)) return rc;
+        if (int rc = bound(l)) return rc;
+        if (int rc = conn(l, 1, true)) return rc;
+        if (int rc = launch_gc_mode(c, 'C', u, v, w, l)) return rc;
+        if (int rc = bound(l)) return rc;
+        if (int rc = conn(l, 1, true)) return rc;
+        if (int rc = launch_gc_mode(c, 'S', u, v, w, l)) return rc;
+    }
+    return 0;
 }
 
 // setpointvalues (:1323-1367)
@@ -294,8 +331,13 @@ int gc_setpointvalues(Ctx* c, bool comp_new) {
     MG_CUDA(cudaMemcpyAsync(pv, c->F("V"), n, cudaMemcpyDeviceToDevice, c->stream));
     MG_CUDA(cudaMemcpyAsync(pw, c->F("W"), n, cudaMemcpyDeviceToDevice, c->stream));
     if (int rc = launch_gc_mode(c, comp_new ? 'X' : 'Y', pu, pv, pw)) return rc;
-    if (int rc = connect(c, 0, 1, pu, pv, pw, nullptr, nullptr, nullptr, false, false, 0)) return rc;
-    if (int rc = launch_bound_flow(c, pu, pv, pw, nullptr)) return rc;
+    // pwu%buffers = u%buffers: bound_flow takes the U, V, W boundary buffers
+    const bool ml = c->minlevel != c->maxlevel;
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+        if (int rc = connect(c, ml ? l : 0, 1, pu, pv, pw, nullptr, nullptr, nullptr, false, false, 0))
+            return rc;
+        if (int rc = launch_bound_flow(c, pu, pv, pw, nullptr, ml ? l : 0)) return rc;
+    }
     if (comp_new) return launch_gc_mode(c, 'Z', pu, pv, pw);
     return 0;
 }

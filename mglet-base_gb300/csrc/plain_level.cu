@@ -314,7 +314,10 @@ struct FtocArgs {
     const double* ff;
     double* fc;
     const double *ddx, *ddy, *ddz;
-    char flag;                  // U V W, or P for the scalar (volume) mean
+    const double* bp;
+    // U V W, P for the scalar (volume) mean, G and H for the ghost-cell
+    // forms of P and R
+    char flag;
 };
 
 __global__ void k_ftoc(FtocArgs A) {
@@ -323,6 +326,7 @@ __global__ void k_ftoc(FtocArgs A) {
     const int4 H = A.hier[g];
     const DevGrid P = A.grids[H.x];
     const char f = A.flag;
+    const double* bp = A.bp + G.ip3;
     const int is = f == 'U' ? 2 : 3, js = f == 'V' ? 2 : 3, ks = f == 'W' ? 2 : 3;
     const int ie = G.ii - is, je = G.jj - js, ke = G.kk - ks;
     const int ni = (ie - is) / 2 + 1, nj = (je - js) / 2 + 1, nk = (ke - ks) / 2 + 1;
@@ -350,6 +354,32 @@ __global__ void k_ftoc(FtocArgs A) {
         const double s = F(k, j, i) * ddx[i] * ddy[j] + F(k, j, i + 1) * ddx[i + 1] * ddy[j] +
                          F(k, j + 1, i) * ddx[i] * ddy[j + 1] + F(k, j + 1, i + 1) * ddx[i + 1] * ddy[j + 1];
         val = s / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]));
+    } else if (f == 'G' || f == 'H') {
+        // gc_restrict_mod.F90:59-171 restrict_p (G) and :174-259 restrict_r (H)
+        const int cj[4] = {j, j, j + 1, j + 1}, ci[4] = {i, i + 1, i, i + 1};
+        auto B = [&](int kx, int jx, int ix) -> double {
+            return bp[(long long)(ix - 1) * kk * jj + (long long)(jx - 1) * kk + (kx - 1)];
+        };
+        double spv = 0.0, sv = 0.0;
+        bool first = true;
+        for (int l = 0; l < 2; ++l)
+            for (int m = 0; m < 4; ++m) {
+                const int kq = k + l;
+                double pv, vol = 0.0;
+                if (f == 'G') {
+                    vol = B(kq, cj[m], ci[m]) * ddz[kq] * ddy[cj[m]] * ddx[ci[m]];
+                    pv = F(kq, cj[m], ci[m]) * vol;
+                } else {
+                    pv = F(kq, cj[m], ci[m]) * B(kq, cj[m], ci[m]) * ddz[kq] * ddy[cj[m]] * ddx[ci[m]];
+                }
+                spv = first ? pv : spv + pv;
+                sv = first ? vol : sv + vol;
+                first = false;
+            }
+        if (f == 'G')
+            val = sv > 0.0 ? spv / sv : 0.0;
+        else
+            val = spv / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
     } else {
         const double s = F(k, j, i) * ddz[k] * ddy[j] * ddx[i] + F(k, j, i + 1) * ddz[k] * ddy[j] * ddx[i + 1] +
                          F(k, j + 1, i) * ddz[k] * ddy[j + 1] * ddx[i] +
@@ -753,6 +783,66 @@ __global__ void k_tstle4_par(ParFluxArgs A) {
 }
 #undef PAR_LOOP2
 
+// ---- par_ftoc_norm (par_ftoc_mod.F90:36-318) ------------------------------
+// One block per message, one thread per coarse face: the area mean (or the
+// sum) of the 2x2 fine faces of the PAR plane (pack_single), written where
+// unpack_single puts it.
+__global__ void k_par_ftoc(const DevGrid* __restrict__ grids, const PfTask* __restrict__ tasks,
+                           double* U, double* V, double* W, const double* __restrict__ DDX,
+                           const double* __restrict__ DDY, const double* __restrict__ DDZ, int sum) {
+    const PfTask T = tasks[blockIdx.y];
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= T.na * T.nb) return;
+    const int a = q / T.nb, b = q % T.nb;
+    const DevGrid G = grids[T.gf];
+    const DevGrid C = grids[T.gc];
+    const int d = (T.iface - 1) / 2;
+    double* field = d == 0 ? U : (d == 1 ? V : W);
+    const double* ff = field + G.ip3;
+    const double *ddx = DDX + G.ipx - 1, *ddy = DDY + G.ipy - 1, *ddz = DDZ + G.ipz - 1;
+    const int kk = G.kk, jj = G.jj;
+    auto F = [&](int k, int j, int i) -> double {
+        return ff[(long long)(i - 1) * kk * jj + (long long)(j - 1) * kk + (k - 1)];
+    };
+    const int lay = T.iface == 1 || T.iface == 3 || T.iface == 5
+                        ? 2
+                        : (d == 0 ? G.ii - 2 : (d == 1 ? G.jj - 2 : G.kk - 2));
+    double val;
+    int di, dj, dk;
+    if (d == 0) {
+        const int i = lay, j = 3 + 2 * a, k = 3 + 2 * b;
+        if (sum) {
+            val = F(k, j, i) + F(k, j + 1, i) + F(k + 1, j, i) + F(k + 1, j + 1, i);
+        } else {
+            const double sua = F(k, j, i) * ddy[j] * ddz[k] + F(k, j + 1, i) * ddy[j + 1] * ddz[k] +
+                               F(k + 1, j, i) * ddy[j] * ddz[k + 1] + F(k + 1, j + 1, i) * ddy[j + 1] * ddz[k + 1];
+            val = sua / ((ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
+        }
+        di = T.i0; dj = T.j0 + a; dk = T.k0 + b;
+    } else if (d == 1) {
+        const int i = 3 + 2 * a, j = lay, k = 3 + 2 * b;
+        if (sum) {
+            val = F(k, j, i) + F(k, j, i + 1) + F(k + 1, j, i) + F(k + 1, j, i + 1);
+        } else {
+            const double sua = F(k, j, i) * ddx[i] * ddz[k] + F(k, j, i + 1) * ddx[i + 1] * ddz[k] +
+                               F(k + 1, j, i) * ddx[i] * ddz[k + 1] + F(k + 1, j, i + 1) * ddx[i + 1] * ddz[k + 1];
+            val = sua / ((ddx[i] + ddx[i + 1]) * (ddz[k] + ddz[k + 1]));
+        }
+        di = T.i0 + a; dj = T.j0; dk = T.k0 + b;
+    } else {
+        const int i = 3 + 2 * a, j = 3 + 2 * b, k = lay;
+        if (sum) {
+            val = F(k, j, i) + F(k, j + 1, i) + F(k, j, i + 1) + F(k, j + 1, i + 1);
+        } else {
+            const double sua = F(k, j, i) * ddx[i] * ddy[j] + F(k, j + 1, i) * ddx[i] * ddy[j + 1] +
+                               F(k, j, i + 1) * ddx[i + 1] * ddy[j] + F(k, j + 1, i + 1) * ddx[i + 1] * ddy[j + 1];
+            val = sua / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]));
+        }
+        di = T.i0 + a; dj = T.j0 + b; dk = T.k0;
+    }
+    field[C.ip3 + (long long)(di - 1) * C.kk * C.jj + (long long)(dj - 1) * C.kk + (dk - 1)] = val;
+}
+
 int upload_list(Ctx* c, const std::vector<int>& h, int** d) {
     if (*d) cudaFree(*d);
     *d = nullptr;
@@ -828,6 +918,69 @@ int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos) {
         if (int rc = upload_list(c, kv.second, &d)) return rc;
         c->d_children[kv.first] = d;
     }
+    // par_ftoc_norm messages (init_par_ftoc, par_ftoc_mod.F90:513-690) and
+    // the coarse planes unpack_single (:366-469) writes them to
+    for (auto& kv : c->d_pftasks) cudaFree(kv.second);
+    c->d_pftasks.clear();
+    c->pftasks.clear();
+    for (int g = 0; g < c->ngrid; ++g) {
+        const int4 H = c->hier[g];
+        if (H.x < 0) continue;
+        const DevGrid& G = c->grids[g];
+        const DevGrid& P = c->grids[H.x];
+        for (int iface = 1; iface <= 6; ++iface) {
+            if (G.bc[iface - 1] != MGLET_BC_PAR) continue;
+            const int d = (iface - 1) / 2;
+            const bool odd = iface % 2 == 1;
+            const int pos = d == 0 ? H.y : (d == 1 ? H.z : H.w);
+            const int nf = d == 0 ? G.ii : (d == 1 ? G.jj : G.kk);
+            const int nc = d == 0 ? P.ii : (d == 1 ? P.jj : P.kk);
+            const bool one_connect = !(nf > nc);
+            int recv1 = iface;
+            if (pos == 3 && one_connect) {
+                if (!odd) recv1 = -1;
+            } else if (pos > 3) {
+                if (odd) recv1 = -1;
+            }
+            auto add = [&](int gc, int ifr) -> int {
+                const DevGrid& C = c->grids[gc];
+                int lo[3] = {H.y, H.z, H.w};
+                int hi[3] = {H.y + (G.ii - 4) / 2 - 1, H.z + (G.jj - 4) / 2 - 1, H.w + (G.kk - 4) / 2 - 1};
+                if (ifr < 0) {
+                    if (odd) lo[d] = hi[d] = lo[d] - 1;
+                    else lo[d] = hi[d];
+                } else {
+                    const int n = d == 0 ? C.ii : (d == 1 ? C.jj : C.kk);
+                    lo[d] = hi[d] = ifr % 2 == 1 ? 2 : n - 2;
+                }
+                const int dims[3] = {C.ii, C.jj, C.kk};
+                for (int q = 0; q < 3; ++q)
+                    if (lo[q] < 1 || hi[q] > dims[q]) {
+                        set_error("set_hierarchy: a par_ftoc_norm plane lies outside its coarse grid");
+                        return MGLET_ERR_ARG;
+                    }
+                PfTask t;
+                t.gf = g; t.gc = gc; t.iface = iface;
+                t.i0 = lo[0]; t.j0 = lo[1]; t.k0 = lo[2];
+                t.na = d == 0 ? (G.jj - 4) / 2 : (G.ii - 4) / 2;
+                t.nb = d == 2 ? (G.jj - 4) / 2 : (G.kk - 4) / 2;
+                c->pftasks[G.level].push_back(t);
+                return 0;
+            };
+            if (int rc = add(H.x, recv1)) return rc;
+            if (recv1 < 0) continue;
+            const int nb = c->nbr[H.x + 1][iface];
+            if (nb <= 0) continue;
+            if (int rc = add(nb - 1, odd ? iface + 1 : iface - 1)) return rc;
+        }
+    }
+    for (auto& kv : c->pftasks) {
+        PfTask* d = nullptr;
+        MG_CUDA(cudaMalloc(&d, kv.second.size() * sizeof(PfTask)));
+        MG_CUDA(copy_on(c->stream, d, kv.second.data(), kv.second.size() * sizeof(PfTask),
+                        cudaMemcpyHostToDevice));
+        c->d_pftasks[kv.first] = d;
+    }
     for (int f = 0; f < 6; ++f) {
         for (auto& kv : c->d_plist[f]) cudaFree(kv.second);
         c->d_plist[f].clear();
@@ -882,6 +1035,19 @@ int launch_tstle4_par(Ctx* c, double* uo, double* vo, double* wo, const double* 
     if (smem > 48 * 1024)
         MG_CUDA(cudaFuncSetAttribute(k_tstle4_par, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_tstle4_par<<<c->npargrids, 256, smem, c->stream>>>(A);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int launch_par_ftoc_norm(Ctx* c, int ilevel, double* u, double* v, double* w, bool sum) {
+    ProfScope ps_(c, "par_ftoc_norm");
+    auto it = c->d_pftasks.find(ilevel);
+    if (it == c->d_pftasks.end()) return 0;
+    const std::vector<PfTask>& ts = c->pftasks[ilevel];
+    int maxq = 0;
+    for (const PfTask& t : ts) maxq = std::max(maxq, t.na * t.nb);
+    k_par_ftoc<<<dim3((maxq + 127) / 128, (unsigned)ts.size()), 128, 0, c->stream>>>(
+        c->d_grids, it->second, u, v, w, c->L("DDX"), c->L("DDY"), c->L("DDZ"), sum ? 1 : 0);
     MG_LAUNCHED(c);
     return 0;
 }
@@ -961,7 +1127,14 @@ int launch_ftoc(Ctx* c, int ilevel, const double* ff, double* fc, char flag) {
     A.ff = ff;
     A.fc = fc;
     A.ddx = c->L("DDX"); A.ddy = c->L("DDY"); A.ddz = c->L("DDZ");
+    A.bp = c->F("BP");
     A.flag = (flag == 'R' || flag == 'S' || flag == 'T') ? 'P' : flag;
+    if (c->ibtype == 1 && flag == 'P') A.flag = 'G';       // gc_restrict_t
+    if (c->ibtype == 1 && flag == 'R') A.flag = 'H';
+    if (c->ibtype == 1 && flag == 'T') {
+        set_error("ftoc: the ghost-cell T restriction weighs by BT, which is not kept");
+        return MGLET_ERR_UNSUPPORTED;
+    }
     int maxq = 0;
     for (int g : list) {
         const DevGrid& G = c->grids[g];

@@ -139,6 +139,11 @@ MODULE mglet_gpu_mod
             TYPE(c_ptr), VALUE :: ctx
         END FUNCTION mglet_gpu_set_ghostcell
 
+        INTEGER(c_int) FUNCTION mglet_gpu_setibvalues(ctx) BIND(C, name="mglet_gpu_setibvalues")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+        END FUNCTION mglet_gpu_setibvalues
+
         INTEGER(c_int) FUNCTION mglet_gpu_setpointvalues(ctx, comp_new) &
                 BIND(C, name="mglet_gpu_setpointvalues")
             IMPORT :: c_int, c_int32_t, c_ptr
@@ -176,6 +181,14 @@ MODULE mglet_gpu_mod
             CHARACTER(kind=c_char), INTENT(in) :: ff(*), fc(*)
         END FUNCTION mglet_gpu_ctof
 
+        INTEGER(c_int) FUNCTION mglet_gpu_par_ftoc_norm(ctx, ilevel, v1, v2, v3, sum) &
+                BIND(C, name="mglet_gpu_par_ftoc_norm")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_char
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: ilevel, sum
+            CHARACTER(kind=c_char), INTENT(in) :: v1(*), v2(*), v3(*)
+        END FUNCTION mglet_gpu_par_ftoc_norm
+
         INTEGER(c_int) FUNCTION mglet_gpu_bound_pressure(ctx, ilevel, dp, with_bp) &
                 BIND(C, name="mglet_gpu_bound_pressure")
             IMPORT :: c_int, c_int32_t, c_ptr, c_char
@@ -199,7 +212,7 @@ MODULE mglet_gpu_mod
         mglet_itinfo, gpu_init, gpu_finish, gpu_upload, gpu_download, &
         gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf, &
         gpu_upload_stencils, gpu_start_ghostcell, gpu_set_hierarchy, gpu_ftoc, gpu_ctof, &
-        gpu_bound_pressure
+        gpu_bound_pressure, gpu_par_ftoc_norm
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -277,6 +290,20 @@ CONTAINS
             TRIM(fc)//C_NULL_CHAR) /= 0) CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_ctof
 
+    ! Drop-in for par_ftoc_norm(ilevel, v1, v2, v3[, sum]) on the device copies
+    SUBROUTINE gpu_par_ftoc_norm(ilevel, v1, v2, v3, sum)
+        INTEGER, INTENT(in) :: ilevel
+        CHARACTER(len=*), INTENT(in) :: v1, v2, v3
+        LOGICAL, OPTIONAL, INTENT(in) :: sum
+        INTEGER(c_int32_t) :: s
+        s = 0
+        IF (PRESENT(sum)) THEN
+            IF (sum) s = 1
+        END IF
+        IF (mglet_gpu_par_ftoc_norm(gctx, INT(ilevel, c_int32_t), TRIM(v1)//C_NULL_CHAR, &
+            TRIM(v2)//C_NULL_CHAR, TRIM(v3)//C_NULL_CHAR, s) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_par_ftoc_norm
+
     ! Drop-in for bound_pressure(ilevel, dp[, bp]) on the device copies
     SUBROUTINE gpu_bound_pressure(ilevel, dp, with_bp)
         INTEGER, INTENT(in) :: ilevel
@@ -305,9 +332,13 @@ CONTAINS
     ! After BP and all lists are uploaded: rebuild the Poisson coefficients,
     ! build SDIV, and initialise the point values (setpointvalues with new
     ! extrapolation, as the reference's flow initialisation does).
+    ! The end of init_flow (src/flow/flow_mod.F90:83-84): point values and
+    ! ghost values once before the first stage.  With grid hierarchies call
+    ! gpu_set_hierarchy first.
     SUBROUTINE gpu_start_ghostcell()
         IF (mglet_gpu_set_ghostcell(gctx) /= 0) CALL errr(__FILE__, __LINE__)
         IF (mglet_gpu_setpointvalues(gctx, 1_c_int32_t) /= 0) CALL errr(__FILE__, __LINE__)
+        IF (mglet_gpu_setibvalues(gctx) /= 0) CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_start_ghostcell
 
     ! Drop-in for timeintegrate_flow (src/flow/timeintegration_mod.F90:22)

@@ -173,22 +173,27 @@ def periodic_box(nx, ny, nz, n=24, length=(2 * np.pi, 2 * np.pi, 2 * np.pi), nk=
     )
 
 
-def refined_box(nx, ny, nz, n=8, refine=(1,), length=(2 * np.pi, 2 * np.pi, 2 * np.pi)):
+def refined_box(nx, ny, nz, n=8, refine=(1,), length=(2 * np.pi, 2 * np.pi, 2 * np.pi),
+                octants=None):
     """A two-level hierarchy: the periodic tiling of periodic_box (level 1)
     with every coarse grid listed in `refine` (1-based, not adjacent to each
-    other) covered by 2x2x2 grids of n^3 cells at half its spacing (level 2).
-    A fine face towards a sibling is CON, every other fine face PAR (code 8)
-    with the coarse grid as parent, as a grids.h5 of a locally refined
-    domain holds (src/core/gridio_mod.F90:61-245).  n must be even."""
+    other) covered by 2x2x2 grids of n^3 cells at half its spacing (level 2),
+    or by the subset `octants` of them ((ox, oy, oz) in {0, 1}^3).  A fine
+    face towards a sibling is CON, every other fine face PAR (code 8) with
+    the coarse grid as parent, as a grids.h5 of a locally refined domain
+    holds (src/core/gridio_mod.F90:61-245).  n must be even."""
     from .abi import BC_PAR
     assert n % 2 == 0
     c = periodic_box(nx, ny, nz, n=n, length=length)
     nc = c.ngrid
     ii = jj = kk = n + 4
-    nf = 8 * len(refine)
+    octs = [(ox, oy, oz) for oz in range(2) for oy in range(2) for ox in range(2)]
+    if octants is not None:
+        octs = [o for o in octs if tuple(o) in {tuple(x) for x in octants}]
+    no = len(octs)
+    nf = no * len(refine)
     ngrid = nc + nf
     hx, hy, hz = c.dx[0], c.dy[0], c.dz[0]
-    octs = [(ox, oy, oz) for oz in range(2) for oy in range(2) for ox in range(2)]
     bct = np.full((nf, 6), BC_PAR, dtype=np.int32)
     nbr = np.zeros((nf, 26), dtype=np.int32)
     iparent = np.zeros(ngrid, dtype=np.int32)
@@ -197,18 +202,19 @@ def refined_box(nx, ny, nz, n=8, refine=(1,), length=(2 * np.pi, 2 * np.pi, 2 * 
     for r, gc in enumerate(refine):
         gx, gy, gz = c.gridpos[gc - 1]
         for q, (ox, oy, oz) in enumerate(octs):
-            g = nc + 8 * r + q             # 0-based id of the fine grid
+            g = nc + no * r + q            # 0-based id of the fine grid
             iparent[g] = gc
             position[g] = (3 + ox * (n // 2), 3 + oy * (n // 2), 3 + oz * (n // 2))
             for s in range(1, 27):
                 di, dj, dk = slot_offset(s)
                 tx, ty, tz = ox + di, oy + dj, oz + dk
-                if 0 <= tx < 2 and 0 <= ty < 2 and 0 <= tz < 2:
-                    nbr[g - nc, s - 1] = nc + 8 * r + octs.index((tx, ty, tz)) + 1
+                if (tx, ty, tz) in octs:
+                    nbr[g - nc, s - 1] = nc + no * r + octs.index((tx, ty, tz)) + 1
             for f in range(1, 7):
                 d, hi = (f - 1) // 2, (f - 1) % 2
-                o = (ox, oy, oz)[d]
-                if (hi and o == 0) or (not hi and o == 1):
+                o = list((ox, oy, oz))
+                o[d] += 1 if hi else -1
+                if tuple(o) in octs:
                     bct[g - nc, f - 1] = BC_CON
             i = np.arange(1, ii + 1, dtype=np.float64)
             xs.append(gx * n * hx + ox * n * hx / 2 + (i - 2.5) * hx / 2)
@@ -354,13 +360,15 @@ def stretch(case, seed=11, amount=0.3):
     return case
 
 
-def block_body(case, lo, hi, nstc=3, seed=7):
+def block_body(case, lo, hi, nstc=3, seed=7, grids=None):
     """A blocked box of cells in every grid of a case and ghost-cell lists
     around it, in the formats the reference reads from ib_stencils.h5
     (gc_flowstencils_mod.F90:37-100).  lo/hi are the 1-based (i, j, k) of the
     first and last blocked cell; they must stay two cells inside the
-    interior.  The stencils are synthetic (random nearby fluid points with
-    random weights): they exercise the runtime, not a geometry.
+    interior.  `grids` (0-based ids) limits the body to those grids; the
+    others stay open with empty lists.  The stencils are synthetic (random
+    nearby fluid points with random weights): they exercise the runtime, not
+    a geometry.
 
     Returns (bp, lists) with lists[g] = {1: (ncells, xpoli, xpolr,
     xpolrvel), 2: ..., 3: ..., 4: (ncells, fxpoli, fxpolr)}."""
@@ -368,11 +376,16 @@ def block_body(case, lo, hi, nstc=3, seed=7):
     kk, jj, ii = case.kk, case.jj, case.ii
     bp1 = np.ones((ii, jj, kk))
     bp1[lo[0] - 1:hi[0], lo[1] - 1:hi[1], lo[2] - 1:hi[2]] = 0.0
-    bp = np.tile(bp1.ravel(), case.ngrid)
+    sel = set(range(case.ngrid)) if grids is None else set(grids)
+    bp = np.concatenate([bp1.ravel() if g in sel else np.ones(ii * jj * kk) for g in range(case.ngrid)])
     flat = lambda i, j, k: (k - 1) + (j - 1) * kk + (i - 1) * kk * jj + 1   # 1-based
     shift = {1: (1, 0, 0), 2: (0, 1, 0), 3: (0, 0, 1)}
     lists = []
+    empty = (0, np.zeros(0, dtype=np.int64), np.zeros(0), np.zeros(0))
     for g in range(case.ngrid):
+        if g not in sel:
+            lists.append({1: empty, 2: empty, 3: empty, 4: (0, np.zeros(0, dtype=np.int64), np.zeros(0))})
+            continue
         gl = {}
         for comp in (1, 2, 3):
             di, dj, dk = shift[comp]

@@ -29,7 +29,7 @@ EXPORTS = [
     "mglet_gpu_set_ghostcell", "mglet_gpu_setibvalues", "mglet_gpu_getibvalues",
     "mglet_gpu_setpointvalues", "mglet_gpu_maskbp", "mglet_gpu_get_buffer",
     "mglet_gpu_set_hierarchy", "mglet_gpu_parent", "mglet_gpu_ftoc", "mglet_gpu_ftoc_multiple",
-    "mglet_gpu_ctof", "mglet_gpu_bound_pressure",
+    "mglet_gpu_ctof", "mglet_gpu_bound_pressure", "mglet_gpu_par_ftoc_norm",
 ]
 
 
@@ -81,6 +81,7 @@ def load(path=None):
     L.mglet_gpu_ftoc.argtypes = [vp, C.c_int32, cp, cp, C.c_char]
     L.mglet_gpu_ftoc_multiple.argtypes = [vp, C.c_int32] + [cp] * 6
     L.mglet_gpu_ctof.argtypes = [vp, C.c_int32, cp, cp]
+    L.mglet_gpu_par_ftoc_norm.argtypes = [vp, C.c_int32, cp, cp, cp, C.c_int32]
     L.mglet_gpu_bound_pressure.argtypes = [vp, C.c_int32, cp, C.c_int32]
     L.mglet_gpu_set_stencils.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int64, vp,
                                          C.c_int64, vp, C.c_int64]
@@ -233,6 +234,10 @@ class Solver:
 
     def ctof(self, ilevel, ff, fc):
         _check(load().mglet_gpu_ctof(self.h, ilevel, ff.encode(), fc.encode()))
+
+    def par_ftoc_norm(self, ilevel, v1="U", v2="V", v3="W", sum=False):
+        _check(load().mglet_gpu_par_ftoc_norm(self.h, ilevel, v1.encode(), v2.encode(), v3.encode(),
+                                              int(sum)))
 
     def bound_pressure(self, ilevel, dp, with_bp=False):
         _check(load().mglet_gpu_bound_pressure(self.h, ilevel, dp.encode(), int(with_bp)))

@@ -62,6 +62,7 @@ def lib():
         _lib.oracle_parent.argtypes = [vp, C.c_int] + [C.c_char_p] * 6 + [C.c_int]
         _lib.oracle_ftoc.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p, C.c_char]
         _lib.oracle_ftoc_multiple.argtypes = [vp, C.c_int] + [C.c_char_p] * 6
+        _lib.oracle_par_ftoc_norm.argtypes = [vp, C.c_int] + [C.c_char_p] * 3 + [C.c_int]
         _lib.oracle_ctof.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p]
         _lib.oracle_bound_pressure.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
         _lib.oracle_set_stencils.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, C.c_int64, vp,
@@ -228,6 +229,9 @@ class Oracle:
         v = list(v) if v else [None] * 3
         s = list(s) + [None] * (3 - len(s))
         _check(lib().oracle_ftoc_multiple(self.h, ilevel, *[_b(n) for n in v + s]))
+
+    def par_ftoc_norm(self, ilevel, v1="U", v2="V", v3="W", sum=False):
+        _check(lib().oracle_par_ftoc_norm(self.h, ilevel, _b(v1), _b(v2), _b(v3), int(sum)))
 
     def ctof(self, ilevel, ff, fc):
         _check(lib().oracle_ctof(self.h, ilevel, _b(ff), _b(fc)))

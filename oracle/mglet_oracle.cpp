@@ -1439,13 +1439,18 @@ void restrict_range(const Grid& G, char flag, int r[6]) {
 // noib_restrict_mod.F90:126-298 restrict_u/v/w/s (area- or volume-weighted
 // fine means) and ftoc_mod.F90:581-626 restrict_recieve_open (the coarse
 // index of every fine block): fine grids of ilevel into their parents
+//
+// With the ghost-cell IB (gc_restrict_t, gc_restrict_mod.F90:8-17) P and R
+// take the BP-weighted forms; U, V, W and S stay the no-IB means.
 void ftoc_one(Ctx& c, int ilevel, const std::string& ff, const std::string& fc, char flag) {
     const char f = (flag == 'P' || flag == 'R' || flag == 'S' || flag == 'T') ? 'P' : flag;
+    const bool gcp = c.ibtype == 1 && flag == 'P', gcr = c.ibtype == 1 && flag == 'R';
     for (int g = 1; g <= c.ngrid; ++g) {
         const Grid& G = c.g[g];
         if (G.level != ilevel || !c.iparent[g]) continue;
         const Grid& P = c.g[c.iparent[g]];
         const int kk = G.kk, jj = G.jj;
+        const double* bp = c.F("BP") + G.ip3;
         const double* fv = c.F(ff.c_str()) + G.ip3;
         double* cv = c.F(fc.c_str()) + P.ip3;
         const double* ddx = c.L("DDX") + G.ipx - 1;
@@ -1474,6 +1479,32 @@ void ftoc_one(Ctx& c, int ilevel, const std::string& ff, const std::string& fc, 
                                          fv[IX(k, j + 1, i)] * ddx[i] * ddy[j + 1] +
                                          fv[IX(k, j + 1, i + 1)] * ddx[i + 1] * ddy[j + 1];
                         val = s / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]));
+                    } else if (gcp) {
+                        // gc_restrict_mod.F90:59-171 restrict_p: BP-weighted volume mean
+                        double vol[4][2], pv[4][2];
+                        const int cj[4] = {j, j, j + 1, j + 1}, ci[4] = {i, i + 1, i, i + 1};
+                        for (int m = 0; m < 4; ++m)
+                            for (int l = 0; l < 2; ++l) {
+                                vol[m][l] = bp[IX(k + l, cj[m], ci[m])] * ddz[k + l] * ddy[cj[m]] * ddx[ci[m]];
+                                pv[m][l] = fv[IX(k + l, cj[m], ci[m])] * vol[m][l];
+                            }
+                        const double sum_pv = pv[0][0] + pv[1][0] + pv[2][0] + pv[3][0] + pv[0][1] + pv[1][1] +
+                                              pv[2][1] + pv[3][1];
+                        const double sum_v = vol[0][0] + vol[1][0] + vol[2][0] + vol[3][0] + vol[0][1] +
+                                             vol[1][1] + vol[2][1] + vol[3][1];
+                        val = sum_v > 0.0 ? sum_pv / sum_v : 0.0;
+                    } else if (gcr) {
+                        // gc_restrict_mod.F90:174-259 restrict_r: BP-weighted sum over the full volume
+                        double pv[4][2];
+                        const int cj[4] = {j, j, j + 1, j + 1}, ci[4] = {i, i + 1, i, i + 1};
+                        for (int m = 0; m < 4; ++m)
+                            for (int l = 0; l < 2; ++l)
+                                pv[m][l] = fv[IX(k + l, cj[m], ci[m])] * bp[IX(k + l, cj[m], ci[m])] * ddz[k + l] *
+                                           ddy[cj[m]] * ddx[ci[m]];
+                        const double sum_pv = pv[0][0] + pv[1][0] + pv[2][0] + pv[3][0] + pv[0][1] + pv[1][1] +
+                                              pv[2][1] + pv[3][1];
+                        const double sum_v = (ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]);
+                        val = sum_pv / sum_v;
                     } else {
                         const double s = fv[IX(k, j, i)] * ddz[k] * ddy[j] * ddx[i] +
                                          fv[IX(k, j, i + 1)] * ddz[k] * ddy[j] * ddx[i + 1] +
@@ -1512,6 +1543,120 @@ void ctof(Ctx& c, int ilevel, const std::string& ff, const std::string& fc) {
                     const int ic = is + (i - 1) / 2, jc = js + (j - 1) / 2, kc = ks + (k - 1) / 2;
                     fv[IX(k, j, i)] = cv[(int64_t)(ic - 1) * P.kk * P.jj + (int64_t)(jc - 1) * P.kk + (kc - 1)];
                 }
+    }
+}
+
+// par_ftoc_mod.F90:36-64 par_ftoc_norm with init_par_ftoc :513-779: on every
+// PAR face of the grids of ilevel the face-normal velocity, as the area mean
+// of 2x2 fine faces (pack_single :226-318; the plain sum when sum is set),
+// goes to the parent -- inside it (front at ipos-1, back at the last covered
+// face) or onto its own boundary face when the PAR lies on a coarse face,
+// and in that case also onto the opposite face of the parent's neighbour
+// across that face (unpack_single :366-469).
+void par_ftoc_norm(Ctx& c, int ilevel, double* U, double* V, double* W, bool sum) {
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel || !c.iparent[g]) continue;
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const double* ddx = c.L("DDX") + G.ipx - 1;
+        const double* ddy = c.L("DDY") + G.ipy - 1;
+        const double* ddz = c.L("DDZ") + G.ipz - 1;
+        const int par = c.iparent[g];
+        const Grid& P = c.g[par];
+        const int ipos = c.pos[g][0], jpos = c.pos[g][1], kpos = c.pos[g][2];
+        for (int iface = 1; iface <= 6; ++iface) {
+            if (G.bc[iface] != MGLET_BC_PAR) continue;
+            double* field = iface <= 2 ? U : (iface <= 4 ? V : W);
+            const double* ff = field + G.ip3;
+            // start_and_stop (:760-810) of the fine face
+            int ks = 3, ke = kk - 2, js = 3, je = jj - 2, is = 3, ie = ii - 2;
+            switch (iface) {
+            case 1: is = ie = 2; break;
+            case 2: is = ie = ii - 2; break;
+            case 3: js = je = 2; break;
+            case 4: js = je = jj - 2; break;
+            case 5: ks = ke = 2; break;
+            case 6: ks = ke = kk - 2; break;
+            }
+            std::vector<double> buf;
+            auto F = [&](int k, int j, int i) { return ff[IX(k, j, i)]; };
+            if (iface <= 2) {
+                const int i = is;
+                for (int j = js; j <= je; j += 2)
+                    for (int k = ks; k <= ke; k += 2) {
+                        if (sum) { buf.push_back(F(k, j, i) + F(k, j + 1, i) + F(k + 1, j, i) + F(k + 1, j + 1, i)); continue; }
+                        const double sua = F(k, j, i) * ddy[j] * ddz[k] + F(k, j + 1, i) * ddy[j + 1] * ddz[k] +
+                                           F(k + 1, j, i) * ddy[j] * ddz[k + 1] + F(k + 1, j + 1, i) * ddy[j + 1] * ddz[k + 1];
+                        buf.push_back(sua / ((ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1])));
+                    }
+            } else if (iface <= 4) {
+                const int j = js;
+                for (int i = is; i <= ie; i += 2)
+                    for (int k = ks; k <= ke; k += 2) {
+                        if (sum) { buf.push_back(F(k, j, i) + F(k, j, i + 1) + F(k + 1, j, i) + F(k + 1, j, i + 1)); continue; }
+                        const double sua = F(k, j, i) * ddx[i] * ddz[k] + F(k, j, i + 1) * ddx[i + 1] * ddz[k] +
+                                           F(k + 1, j, i) * ddx[i] * ddz[k + 1] + F(k + 1, j, i + 1) * ddx[i + 1] * ddz[k + 1];
+                        buf.push_back(sua / ((ddx[i] + ddx[i + 1]) * (ddz[k] + ddz[k + 1])));
+                    }
+            } else {
+                const int k = ks;
+                for (int i = is; i <= ie; i += 2)
+                    for (int j = js; j <= je; j += 2) {
+                        if (sum) { buf.push_back(F(k, j, i) + F(k, j + 1, i) + F(k, j, i + 1) + F(k, j + 1, i + 1)); continue; }
+                        const double sua = F(k, j, i) * ddx[i] * ddy[j] + F(k, j + 1, i) * ddx[i] * ddy[j + 1] +
+                                           F(k, j, i + 1) * ddx[i + 1] * ddy[j] + F(k, j + 1, i + 1) * ddx[i + 1] * ddy[j + 1];
+                        buf.push_back(sua / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1])));
+                    }
+            }
+            // the destinations (init_par_ftoc :566-690)
+            const int pos = iface <= 2 ? ipos : (iface <= 4 ? jpos : kpos);
+            const int nf = iface <= 2 ? ii : (iface <= 4 ? jj : kk);
+            const int nc = iface <= 2 ? P.ii : (iface <= 4 ? P.jj : P.kk);
+            const bool one_connect = !(nf > nc);
+            const bool odd = iface % 2 == 1;
+            int recv1 = iface;
+            if (pos == 3 && one_connect) {
+                if (!odd) recv1 = -1;
+            } else if (pos > 3) {
+                if (odd) recv1 = -1;
+            }
+            auto unpack = [&](int gc, int ifr) {
+                const Grid& C = c.g[gc];
+                int ista = ipos, isto = ipos + (ii - 4) / 2 - 1;
+                int jsta = jpos, jsto = jpos + (jj - 4) / 2 - 1;
+                int ksta = kpos, ksto = kpos + (kk - 4) / 2 - 1;
+                if (ifr < 0) {
+                    switch (iface) {
+                    case 1: ista = isto = ipos - 1; break;
+                    case 2: ista = isto; break;
+                    case 3: jsta = jsto = jpos - 1; break;
+                    case 4: jsta = jsto; break;
+                    case 5: ksta = ksto = kpos - 1; break;
+                    case 6: ksta = ksto; break;
+                    }
+                } else {
+                    switch (ifr) {
+                    case 1: ista = isto = 2; break;
+                    case 2: ista = isto = C.ii - 2; break;
+                    case 3: jsta = jsto = 2; break;
+                    case 4: jsta = jsto = C.jj - 2; break;
+                    case 5: ksta = ksto = 2; break;
+                    case 6: ksta = ksto = C.kk - 2; break;
+                    }
+                }
+                double* fc = field + C.ip3;
+                size_t n = 0;
+                for (int i = ista; i <= isto; ++i)
+                    for (int j = jsta; j <= jsto; ++j)
+                        for (int k = ksta; k <= ksto; ++k)
+                            fc[(int64_t)(i - 1) * C.kk * C.jj + (int64_t)(j - 1) * C.kk + (k - 1)] = buf[n++];
+            };
+            unpack(par, recv1);
+            if (recv1 < 0) continue;
+            const int nbr = P.nbr[iface];
+            if (nbr <= 0) continue;
+            unpack(nbr, odd ? iface + 1 : iface - 1);
+        }
     }
 }
 
@@ -1587,9 +1732,11 @@ int wmxpolsolcorr(const Grid& G, double* u, double* v, double* w, const double* 
 
 // setibvalues_level (:1456-1485) modes F, R, S, C and wmxpolquadvel modes X,
 // Y, Z (setpointvalues_all, :1370-1390)
-int gc_level(Ctx& c, char mode, double* U, double* V, double* W) {
+// on the grids of ilevel (0: every grid)
+int gc_level(Ctx& c, char mode, double* U, double* V, double* W, int ilevel = 0) {
     for (int g = 1; g <= c.ngrid; ++g) {
         const Grid& G = c.g[g];
+        if (ilevel && G.level != ilevel) continue;
         double* f[3] = {U + G.ip3, V + G.ip3, W + G.ip3};
         if (mode == 'C') {
             if (int rc = wmxpolsolcorr(G, f[0], f[1], f[2], c.L("DDX") + G.ipx - 1,
@@ -1602,8 +1749,16 @@ int gc_level(Ctx& c, char mode, double* U, double* V, double* W) {
             switch (mode) {
             case 'F': wmxpolsol(f[cmp], L, L.xpolr); break;
             case 'X': wmxpolsol(f[cmp], L, L.xpolrvel); break;
-            case 'R': wmxpolsolrlx(f[cmp], L.ncells, L.oldsol, L.poldsol); break;
-            case 'Y': wmxpolsolrlx(f[cmp], L.ncells, L.oldsolvel, L.poldsolvel); break;
+            case 'R':
+                if (L.poldsol.size() < (size_t)L.ncells)
+                    return fail(MGLET_ERR_ARG, "gc: restore R before any save S (setibvalues first)");
+                wmxpolsolrlx(f[cmp], L.ncells, L.oldsol, L.poldsol);
+                break;
+            case 'Y':
+                if (L.poldsolvel.size() < (size_t)L.ncells)
+                    return fail(MGLET_ERR_ARG, "gc: restore Y before any save Z (setpointvalues first)");
+                wmxpolsolrlx(f[cmp], L.ncells, L.oldsolvel, L.poldsolvel);
+                break;
             case 'S': wmxpolsolsav(f[cmp], L, L.oldsol, L.poldsol); break;
             case 'Z': wmxpolsolsav(f[cmp], L, L.oldsolvel, L.poldsolvel); break;
             default: return fail(MGLET_ERR_ARG, "gc: unknown mode");
@@ -1613,22 +1768,44 @@ int gc_level(Ctx& c, char mode, double* U, double* V, double* W) {
     return 0;
 }
 
-// setibvalues (:1393-1438), one level
-int setibvalues(Ctx& c, double* U, double* V, double* W) {
-    bound_flow(c, U, V, W, nullptr);
-    connect(c, 0, 2, U, V, W, nullptr, nullptr, nullptr, false, false, 0);
-    if (int rc = gc_level(c, 'F', U, V, W)) return rc;
-    bound_flow(c, U, V, W, nullptr);
-    connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, true, false, 0);
-    if (int rc = gc_level(c, 'C', U, V, W)) return rc;
-    bound_flow(c, U, V, W, nullptr);
-    connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, true, false, 0);
-    bound_flow(c, U, V, W, nullptr);
-    connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, true, false, 0);
-    if (int rc = gc_level(c, 'C', U, V, W)) return rc;
-    bound_flow(c, U, V, W, nullptr);
-    connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, true, false, 0);
-    return gc_level(c, 'S', U, V, W);
+// setibvalues (:1393-1438) of the velocity fields U, V, W: per level
+// (parent,) extrapolation F and flux correction C, each followed by
+// bound_flow and connect; fine to coarse (ftoc, par_ftoc_norm); per level
+// again (parent,) C and the save S
+int setibvalues(Ctx& c) {
+    double *U = c.F("U"), *V = c.F("V"), *W = c.F("W");
+    const char* vn[3] = {"U", "V", "W"};
+    const char* none[3] = {nullptr, nullptr, nullptr};
+    const bool ml = c.minlevel != c.maxlevel;
+    auto bound = [&](int l) { bound_flow(c, U, V, W, nullptr, ml ? l : 0); };
+    auto conn = [&](int l, int layers, bool corners) {
+        connect(c, ml ? l : 0, layers, U, V, W, nullptr, nullptr, nullptr, corners, false, 0);
+    };
+    for (int l = c.minlevel; l <= c.maxlevel; ++l) {
+        if (ml) parent(c, l, vn, none, false);
+        bound(l);
+        conn(l, 2, false);
+        if (int rc = gc_level(c, 'F', U, V, W, l)) return rc;
+        bound(l);
+        conn(l, 1, true);
+        if (int rc = gc_level(c, 'C', U, V, W, l)) return rc;
+        bound(l);
+        conn(l, 1, true);
+    }
+    for (int l = c.maxlevel; l > c.minlevel; --l) {
+        for (int q = 0; q < 3; ++q) ftoc_one(c, l, vn[q], vn[q], "UVW"[q]);
+        par_ftoc_norm(c, l, U, V, W, false);
+    }
+    for (int l = c.minlevel; l <= c.maxlevel; ++l) {
+        if (ml) parent(c, l, vn, none, false);
+        bound(l);
+        conn(l, 1, true);
+        if (int rc = gc_level(c, 'C', U, V, W, l)) return rc;
+        bound(l);
+        conn(l, 1, true);
+        if (int rc = gc_level(c, 'S', U, V, W, l)) return rc;
+    }
+    return 0;
 }
 
 // setpointvalues (:1323-1367): point values = velocities with the ghost
@@ -1637,10 +1814,14 @@ int setpointvalues(Ctx& c, bool comp_new) {
     c.f3["PWU"] = c.f3["U"];
     c.f3["PWV"] = c.f3["V"];
     c.f3["PWW"] = c.f3["W"];
+    // pwu%buffers = u%buffers: bound_flow takes the U, V, W boundary buffers
     double *pu = c.F("PWU"), *pv = c.F("PWV"), *pw = c.F("PWW");
     if (int rc = gc_level(c, comp_new ? 'X' : 'Y', pu, pv, pw)) return rc;
-    connect(c, 0, 1, pu, pv, pw, nullptr, nullptr, nullptr, false, false, 0);
-    bound_flow(c, pu, pv, pw, nullptr);
+    const bool ml = c.minlevel != c.maxlevel;
+    for (int l = c.minlevel; l <= c.maxlevel; ++l) {
+        connect(c, ml ? l : 0, 1, pu, pv, pw, nullptr, nullptr, nullptr, false, false, 0);
+        bound_flow(c, pu, pv, pw, nullptr, ml ? l : 0);
+    }
     if (comp_new) return gc_level(c, 'Z', pu, pv, pw);
     return 0;
 }
@@ -1694,6 +1875,7 @@ void setsdivfield(Ctx& c) {
         }
     };
     walk(true);
+    for (int l = c.maxlevel; l > c.minlevel; --l) ftoc_one(c, l, "SDIV", "SDIV", 'S');
     connect(c, 0, 2, nullptr, nullptr, nullptr, S, nullptr, nullptr, true, false, 0);
     walk(false);
 }
@@ -2757,8 +2939,6 @@ int hierarchy_ready(const Ctx& c) {
         if (c.g[g].level == c.minlevel) continue;
         if (!c.iparent[g]) return fail(MGLET_ERR_ARG, "oracle: a fine grid without parent (set_hierarchy)");
     }
-    if (c.minlevel != c.maxlevel && c.ibtype == 1)
-        return fail(MGLET_ERR_UNSUPPORTED, "oracle: the ghost-cell restriction is not restated");
     return 0;
 }
 
@@ -2988,7 +3168,7 @@ int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timep
     const bool gc = c->ibtype == 1;
     // timeintegration_mod.F90:96-99: the ghost-cell fluxes of the step
     if (irk == 1 && gc)
-        if (int rc2 = setibvalues(*c, c->F("U"), c->F("V"), c->F("W"))) return rc2;
+        if (int rc2 = setibvalues(*c)) return rc2;
     tstle4(*c);
     rkstep(c->F("U"), c->F("DU"), c->F("UO"), c->idim3d, frhs, dt * fu);
     rkstep(c->F("V"), c->F("DV"), c->F("VO"), c->idim3d, frhs, dt * fu);
@@ -3054,11 +3234,14 @@ int oracle_set_stencils(oracle_ctx* c, int igrid, int comp, int ncells, const in
     L.xpolr.assign(xpolr, xpolr + nxr);
     L.xpolrvel.assign(xpolrvel, xpolrvel + nxrv);
     L.ncells = ncells;
+    L.oldsol.clear(); L.poldsol.clear(); L.oldsolvel.clear(); L.poldsolvel.clear();
     return 0;
 }
 
 int oracle_set_ghostcell(oracle_ctx* c) {
     if (!c) return fail(MGLET_ERR_ARG, "set_ghostcell: null context");
+    if (c->minlevel != c->maxlevel)   // setsdivfield restricts SDIV level by level
+        if (int rc = hierarchy_ready(*c)) return rc;
     c->ibtype = 1;
     giteig(*c);                       // Poisson coefficients with the blocked cells
     if (int rc = init_pressuresolver(*c)) return rc;
@@ -3077,7 +3260,7 @@ int oracle_gc_mode(oracle_ctx* c, const char* mode) {
         maskbp(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"));
         return 0;
     }
-    if (mode[0] == 'I') return setibvalues(*c, c->F("U"), c->F("V"), c->F("W"));
+    if (mode[0] == 'I') return setibvalues(*c);
     return gc_level(*c, mode[0], c->F("U"), c->F("V"), c->F("W"));
 }
 
@@ -3127,7 +3310,18 @@ int oracle_parent(oracle_ctx* c, int ilevel, const char* v1, const char* v2, con
 int oracle_ftoc(oracle_ctx* c, int ilevel, const char* ff, const char* fc, char flag) {
     if (!c->f3.count(ff) || !c->f3.count(fc)) return fail(MGLET_ERR_NAME, "ftoc: unknown field");
     if (!std::strchr("UVWPRST", flag)) return fail(MGLET_ERR_ARG, "ftoc: flag is one of U V W P R S T");
+    if (c->ibtype == 1 && flag == 'T')
+        return fail(MGLET_ERR_UNSUPPORTED, "ftoc: the ghost-cell T restriction weighs by BT, which is not kept");
     ftoc_one(*c, ilevel, ff, fc, flag);
+    return 0;
+}
+
+int oracle_par_ftoc_norm(oracle_ctx* c, int ilevel, const char* v1, const char* v2, const char* v3,
+                         int sum) {
+    if (!c || !v1 || !v2 || !v3) return fail(MGLET_ERR_ARG, "par_ftoc_norm: bad arguments");
+    for (const char* n : {v1, v2, v3})
+        if (!c->f3.count(n)) return fail(MGLET_ERR_NAME, "par_ftoc_norm: unknown field");
+    par_ftoc_norm(*c, ilevel, c->F(v1), c->F(v2), c->F(v3), sum != 0);
     return 0;
 }
 
