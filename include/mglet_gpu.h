@@ -284,6 +284,26 @@ int mglet_gpu_ctof(mglet_ctx* ctx, int32_t ilevel, const char* ff, const char* f
  * the fine mean next to the face; with_bp selects the BP-weighted form
  * (the reference passes bp for the ghost-cell IB only). */
 int mglet_gpu_bound_pressure(mglet_ctx* ctx, int32_t ilevel, const char* dp, int32_t with_bp);
+/* ---- Body force and the discrete adjoint (no counterpart in the reference) --
+ * A steady body force per unit mass, added to uo, vo, wo in tstle4 after
+ * gradp over the same points (plain form); n must equal idim3d. */
+int mglet_gpu_set_body_force(mglet_ctx* ctx, const double* fx, const double* fy, const double* fz,
+                             int64_t n);
+/* The adjoint of one RK stage of mglet_gpu_timeintegrate_flow (plain form,
+ * one level, no IB, every face CON, uniform spacing): the device fields U, V,
+ * W hold the stage's input velocity, LU, LV, LW, LP, LDU, LDV, LDW the
+ * adjoint of its output state; on return they hold the adjoint of its input
+ * state and GFX, GFY, GFZ have gained the stage's dJ/d(body force).  The
+ * pressure solve is transposed with the prm's SIP outer loop. */
+int mglet_gpu_adjoint_rk_stage(mglet_ctx* ctx, int32_t irk, double dt, const mglet_rk_scheme* rk);
+/* The gradient of the kinetic energy (the itinfo energy) after nsteps time
+ * steps with respect to the body force: a forward run from the current state
+ * keeping a checkpoint every ncheck steps, then each segment recomputed from
+ * its checkpoint and run backwards stage by stage.  energy receives J;
+ * GFX, GFY, GFZ dJ/df; LU, LV, LW, LP dJ/d of the initial state.  The
+ * context ends in the final forward state. */
+int mglet_gpu_energy_gradient(mglet_ctx* ctx, int32_t nsteps, int32_t ncheck, double dt,
+                              const mglet_rk_scheme* rk, double* energy);
 /* ---- Ghost-cell immersed boundary (ib%type = "GHOSTCELL") -------------------
  * Stencil lists of grid igrid (1-based) in the formats of
  * gc_flowstencils_mod.F90:37-100 (what the reference reads from

@@ -349,19 +349,30 @@ static int mgpoisit_plain(Ctx* c, int ilevel, double* dp, double* rhs, double* r
     return launch_bound_pressure(c, ilevel, dp, hbuf, withbp);
 }
 
-static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
-    double* U = c->F("U"); double* V = c->F("V"); double* W = c->F("W"); double* P = c->F("P");
+// The outer defect-correction loop of mgpoisl (pressuresolver_mod.F90:
+// 203-305) on RHS, accumulating DP; HILF, RES and DP start at zero (cleared
+// here when zero_work is set).  prefak scales the convergence test; 0 takes
+// max|RHS| (a relative test), and an all-zero RHS returns DP = 0.
+int solve_pressure_system(Ctx* c, double prefak, mglet_stage_stats* st, bool zero_work) {
     double* dp = c->F("DP"); double* hilf = c->F("HILF");
     double* rhs = c->F("RHS"); double* res = c->F("RES");
     const size_t bytes = (size_t)c->idim3d * sizeof(double);
-    for (double* a : {dp, hilf, rhs, res}) MG_CUDA(cudaMemsetAsync(a, 0, bytes, c->stream));
-    const double prefak = c->prm.rho / dt;
+    if (zero_work)
+        for (double* a : {dp, hilf, res}) MG_CUDA(cudaMemsetAsync(a, 0, bytes, c->stream));
+    if (prefak <= 0.0) {
+        if (int rc = launch_rescal_maxabs(c, rhs, nullptr)) return rc;
+        MG_CUDA(cudaMemcpyAsync(c->h_scalar, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost,
+                                c->stream));
+        MG_CUDA(cudaStreamSynchronize(c->stream));
+        prefak = c->h_scalar[0];
+        if (!(prefak > 0.0)) {
+            if (st) *st = mglet_stage_stats{0, 0, 0.0, 0.0};
+            return 0;
+        }
+    }
     const bool multi = c->minlevel != c->maxlevel;
     const char* const none[3] = {nullptr, nullptr, nullptr};
     const char* const shilf[3] = {"HILF", nullptr, nullptr};
-    if (int rc = launch_divcal(c, rhs, U, V, W, prefak)) return rc;
-    for (int l = c->maxlevel; l >= c->minlevel; --l)
-        if (int rc = launch_ftoc(c, l, rhs, rhs, 'R')) return rc;
     int ipc = 0, done = 0;
     double maxrhs = 0.0;
     for (int ipcount = 1; ipcount <= c->prm.nouter; ++ipcount) {
@@ -401,6 +412,27 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
         MG_CUDA(cudaStreamSynchronize(c->stream));
         maxrhs = c->h_scalar[0];
     }
+    if (st) {
+        st->ipc = ipc;
+        st->nouter_done = done;
+        st->maxrhs = maxrhs;
+        st->prefak = prefak;
+    }
+    return 0;
+}
+
+static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
+    double* U = c->F("U"); double* V = c->F("V"); double* W = c->F("W"); double* P = c->F("P");
+    double* dp = c->F("DP"); double* hilf = c->F("HILF");
+    double* rhs = c->F("RHS"); double* res = c->F("RES");
+    const size_t bytes = (size_t)c->idim3d * sizeof(double);
+    for (double* a : {dp, hilf, rhs, res}) MG_CUDA(cudaMemsetAsync(a, 0, bytes, c->stream));
+    const double prefak = c->prm.rho / dt;
+    const char* const none[3] = {nullptr, nullptr, nullptr};
+    if (int rc = launch_divcal(c, rhs, U, V, W, prefak)) return rc;
+    for (int l = c->maxlevel; l >= c->minlevel; --l)
+        if (int rc = launch_ftoc(c, l, rhs, rhs, 'R')) return rc;
+    if (int rc = solve_pressure_system(c, prefak, st, false)) return rc;
     const char* const sdp[3] = {"DP", nullptr, nullptr};
     double* dbuf = field_buffer(c, "DP");
     if (!dbuf) return fail(MGLET_ERR_CUDA, "mgpoisl: buffer allocation");
@@ -423,12 +455,6 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
         if (int rc = launch_parent(c, l, vuvw, sp, false)) return rc;
         if (int rc = launch_bound_flow(c, U, V, W, P, l)) return rc;
         if (int rc = connect(c, l, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
-    }
-    if (st) {
-        st->ipc = ipc;
-        st->nouter_done = done;
-        st->maxrhs = maxrhs;
-        st->prefak = prefak;
     }
     return 0;
 }
@@ -755,6 +781,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     for (auto& kv : c->fbuf) cudaFree(kv.second);
     cudaFree(c->d_hier);
     cudaFree(c->d_pargrids);
+    cudaFree(c->d_sptab);
     for (auto& kv : c->d_pftasks) cudaFree(kv.second);
     cudaFree(c->d_gridred);
     cudaFree(c->d_scalar);
@@ -900,6 +927,40 @@ int mglet_gpu_ftoc(mglet_ctx* c, int32_t ilevel, const char* ff, const char* fc,
         return fail(MGLET_ERR_ARG, "ftoc: flag is one of U V W P R S T");
     cudaSetDevice(c->device);
     return launch_ftoc(c, ilevel, f, g, flag);
+}
+
+int mglet_gpu_set_body_force(mglet_ctx* c, const double* fx, const double* fy, const double* fz,
+                             int64_t n) {
+    if (!c || !fx || !fy || !fz) return fail(MGLET_ERR_ARG, "set_body_force: null argument");
+    if (c->prm.form != MGLET_FORM_PLAIN)
+        return fail(MGLET_ERR_UNSUPPORTED, "set_body_force: the plain form only");
+    if (n != c->idim3d) return fail(MGLET_ERR_SIZE, "set_body_force: n must equal idim3d");
+    cudaSetDevice(c->device);
+    const char* nm[3] = {"FBX", "FBY", "FBZ"};
+    const double* h[3] = {fx, fy, fz};
+    for (int q = 0; q < 3; ++q) {
+        if (!c->f3.count(nm[q]))
+            if (int rc = alloc3(c, nm[q])) return rc;
+        MG_CUDA(copy_on(c->stream, c->F(nm[q]), h[q], (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    c->bodyforce = true;
+    return 0;
+}
+
+int mglet_gpu_adjoint_rk_stage(mglet_ctx* c, int32_t irk, double dt, const mglet_rk_scheme* rk) {
+    if (!c || !rk) return fail(MGLET_ERR_ARG, "adjoint_rk_stage: null argument");
+    cudaSetDevice(c->device);
+    if (int rc = adjoint_ready(c)) return rc;
+    if (int rc = adjoint_stage(c, dt, irk, rk)) return rc;
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int mglet_gpu_energy_gradient(mglet_ctx* c, int32_t nsteps, int32_t ncheck, double dt,
+                              const mglet_rk_scheme* rk, double* energy) {
+    if (!c) return fail(MGLET_ERR_ARG, "energy_gradient: null context");
+    cudaSetDevice(c->device);
+    return energy_gradient(c, nsteps, ncheck, dt, rk, energy);
 }
 
 int mglet_gpu_par_ftoc_norm(mglet_ctx* c, int32_t ilevel, const char* v1, const char* v2,

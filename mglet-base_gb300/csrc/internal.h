@@ -146,6 +146,8 @@ struct Ctx {
     // the ghost-cell saves of setibvalues ('S') and setpointvalues ('Z')
     // have run since the lists were set: their restores may follow
     bool gc_saved[2] = {false, false};
+    bool bodyforce = false;      // FBX, FBY, FBZ added in tstle4 (plain form)
+    void* d_sptab = nullptr;     // device table of the 12 spacing arrays (adjoint)
     std::vector<GcHostList> gch;
     GcDev gcd;
     // grid hierarchy (gridinfo%iparent, i/j/kposition): per grid {parent
@@ -264,6 +266,17 @@ int bound_init(Ctx* c);
 int alloc_field3(Ctx* c, const char* name);
 // ghost-cell IB (plain_gc.cu)
 int gc_upload(Ctx* c);                       // lists to the device, PWU/PWV/PWW, SDIV
+// the outer loop of mgpoisl on RHS into DP (api.cu)
+int solve_pressure_system(Ctx* c, double prefak, mglet_stage_stats* st, bool zero_work = true);
+int rk_coeffs(const mglet_rk_scheme* rk, int irk, double* frhs, double* fu, double* dtrk,
+              double* dtrki);
+int timeintegrate(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st);
+// the discrete adjoint (adjoint.cu)
+int adjoint_ready(Ctx* c);
+int adjoint_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk);
+int energy_gradient_init(Ctx* c, double* J);
+int adjoint_fold_initial(Ctx* c);
+int energy_gradient(Ctx* c, int nsteps, int ncheck, double dt, const mglet_rk_scheme* rk, double* J);
 // F C S R X Y Z on the grids of ilevel (0: every grid)
 int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w, int ilevel = 0);
 // par_ftoc_norm (par_ftoc_mod.F90:36-64) of the grids of ilevel

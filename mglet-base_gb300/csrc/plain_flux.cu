@@ -260,7 +260,9 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
                                                 const double* __restrict__ UT, const double* __restrict__ VT,
                                                 const double* __restrict__ WT,
                                                 const double* __restrict__ P, const double* __restrict__ Gf,
-                                                Wall wl, double gx, double gy, double gz) {
+                                                Wall wl, double gx, double gy, double gz,
+                                                const double* __restrict__ FX, const double* __restrict__ FY,
+                                                const double* __restrict__ FZ) {
     const DevGrid G = grids[blockIdx.y];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int npts = kk * jj * ii;
@@ -292,18 +294,25 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
     const double gmol = wl.gmol, rho = wl.rho;
     // outside the flux ranges uo, vo, wo are zero apart from swcle3d's rows
     double ru, rv, rw;
-    if (i >= 3 - nfu && i <= ii - 3 + nbu && jin && kin)
+    // the steady body force FX, FY, FZ (when set) follows gradp
+    if (i >= 3 - nfu && i <= ii - 3 + nbu && jin && kin) {
         ru = uo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gx * gfl);
-    else
+        if (FX) ru = ru + FX[o + t];
+    } else {
         ru = wall_u(0.0, k, j, i, s, wl, u[t]);
-    if (iin && j >= 3 - nrv && j <= jj - 3 + nlv && kin)
+    }
+    if (iin && j >= 3 - nrv && j <= jj - 3 + nlv && kin) {
         rv = vo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gy * gfl);
-    else
+        if (FY) rv = rv + FY[o + t];
+    } else {
         rv = wall_v(0.0, k, j, i, s, wl, v[t]);
-    if (iin && jin && k >= 3 - nbw && k <= kk - 3 + ntw)
+    }
+    if (iin && jin && k >= 3 - nbw && k <= kk - 3 + ntw) {
         rw = wo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gz * gfl);
-    else
+        if (FZ) rw = rw + FZ[o + t];
+    } else {
         rw = wall_w(0.0, k, j, i, s, wl, w[t]);
+    }
     uo[o + t] = ru;
     vo[o + t] = rv;
     wo[o + t] = rw;
@@ -355,7 +364,10 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
     wl.cpo6 = 0.5 * gmol / rho * std::pow(cwa, 2.0 / cpo1);
     wl.cpo8 = 2.0 / cpo2;
     k_tstle4<<<grid, 256, 0, c->stream>>>(c->d_grids, spacing(c), uo, vo, wo, u, v, w, ut, vt, wt, p, g,
-                                          wl, c->prm.gradp[0], c->prm.gradp[1], c->prm.gradp[2]);
+                                          wl, c->prm.gradp[0], c->prm.gradp[1], c->prm.gradp[2],
+                                          c->bodyforce ? c->F("FBX") : nullptr,
+                                          c->bodyforce ? c->F("FBY") : nullptr,
+                                          c->bodyforce ? c->F("FBZ") : nullptr);
     MG_LAUNCHED(c);
     // tstle4_mod.F90:114: tstle4_par after kon, diff and gradp (PAR faces)
     return launch_tstle4_par(c, uo, vo, wo, u, v, w, ut, vt, wt);

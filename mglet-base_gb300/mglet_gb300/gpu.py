@@ -30,6 +30,7 @@ EXPORTS = [
     "mglet_gpu_setpointvalues", "mglet_gpu_maskbp", "mglet_gpu_get_buffer",
     "mglet_gpu_set_hierarchy", "mglet_gpu_parent", "mglet_gpu_ftoc", "mglet_gpu_ftoc_multiple",
     "mglet_gpu_ctof", "mglet_gpu_bound_pressure", "mglet_gpu_par_ftoc_norm",
+    "mglet_gpu_set_body_force", "mglet_gpu_adjoint_rk_stage", "mglet_gpu_energy_gradient",
 ]
 
 
@@ -82,6 +83,10 @@ def load(path=None):
     L.mglet_gpu_ftoc_multiple.argtypes = [vp, C.c_int32] + [cp] * 6
     L.mglet_gpu_ctof.argtypes = [vp, C.c_int32, cp, cp]
     L.mglet_gpu_par_ftoc_norm.argtypes = [vp, C.c_int32, cp, cp, cp, C.c_int32]
+    L.mglet_gpu_set_body_force.argtypes = [vp, vp, vp, vp, C.c_int64]
+    L.mglet_gpu_adjoint_rk_stage.argtypes = [vp, C.c_int32, C.c_double, vp]
+    L.mglet_gpu_energy_gradient.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, vp,
+                                            C.POINTER(C.c_double)]
     L.mglet_gpu_bound_pressure.argtypes = [vp, C.c_int32, cp, C.c_int32]
     L.mglet_gpu_set_stencils.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp, C.c_int64, vp,
                                          C.c_int64, vp, C.c_int64]
@@ -234,6 +239,21 @@ class Solver:
 
     def ctof(self, ilevel, ff, fc):
         _check(load().mglet_gpu_ctof(self.h, ilevel, ff.encode(), fc.encode()))
+
+    def set_body_force(self, fx, fy, fz):
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (fx, fy, fz)]
+        _check(load().mglet_gpu_set_body_force(self.h, *[x.ctypes.data_as(C.c_void_p) for x in a],
+                                               a[0].size))
+
+    def adjoint_rk_stage(self, irk, dt, rk):
+        _check(load().mglet_gpu_adjoint_rk_stage(self.h, irk, dt, C.byref(rk)))
+
+    def energy_gradient(self, nsteps, ncheck, dt, rk):
+        """J (the itinfo kinetic energy after nsteps steps) and dJ/d(body
+        force) as three flat arrays."""
+        e = C.c_double(0.0)
+        _check(load().mglet_gpu_energy_gradient(self.h, nsteps, ncheck, dt, C.byref(rk), C.byref(e)))
+        return e.value, tuple(self.get(n) for n in ("GFX", "GFY", "GFZ"))
 
     def par_ftoc_norm(self, ilevel, v1="U", v2="V", v3="W", sum=False):
         _check(load().mglet_gpu_par_ftoc_norm(self.h, ilevel, v1.encode(), v2.encode(), v3.encode(),

@@ -62,6 +62,7 @@ def lib():
         _lib.oracle_parent.argtypes = [vp, C.c_int] + [C.c_char_p] * 6 + [C.c_int]
         _lib.oracle_ftoc.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p, C.c_char]
         _lib.oracle_ftoc_multiple.argtypes = [vp, C.c_int] + [C.c_char_p] * 6
+        _lib.oracle_set_body_force.argtypes = [vp, vp, vp, vp, C.c_int64]
         _lib.oracle_par_ftoc_norm.argtypes = [vp, C.c_int] + [C.c_char_p] * 3 + [C.c_int]
         _lib.oracle_ctof.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p]
         _lib.oracle_bound_pressure.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
@@ -229,6 +230,10 @@ class Oracle:
         v = list(v) if v else [None] * 3
         s = list(s) + [None] * (3 - len(s))
         _check(lib().oracle_ftoc_multiple(self.h, ilevel, *[_b(n) for n in v + s]))
+
+    def set_body_force(self, fx, fy, fz):
+        a = [np.ascontiguousarray(x, dtype=np.float64) for x in (fx, fy, fz)]
+        _check(lib().oracle_set_body_force(self.h, *[x.ctypes.data_as(C.c_void_p) for x in a], a[0].size))
 
     def par_ftoc_norm(self, ilevel, v1="U", v2="V", v3="W", sum=False):
         _check(lib().oracle_par_ftoc_norm(self.h, ilevel, _b(v1), _b(v2), _b(v3), int(sum)))

@@ -147,6 +147,7 @@ struct Ctx {
     std::vector<double> pinf;    // OP1 real parameter per grid and face (nreal = 1)
     std::vector<int> npinf;      // 0: no parameter (pinf = 0), 1: pinf given
     int ibtype = 0;              // 0: NONE (noib), 1: GHOSTCELL
+    bool bodyforce = false;      // FBX, FBY, FBZ added in tstle4
     std::vector<std::array<GcList, 3>> gcl;   // [grid][component], 1-based grids
     std::vector<GcFlux> gcf;
     // grid hierarchy (gridinfo%iparent and i/j/kposition, grids_mod.F90):
@@ -2753,6 +2754,20 @@ void tstle4_grid(Ctx& c, int g) {
         for (int j = 3; j <= jj - 2; ++j)
             for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k)
                 A(wo, k, j, i) = A(wo, k, j, i) - 1.0 / (rho * dz[k]) * (A(p, k + 1, j, i) - A(p, k, j, i) + gpz * dz[k]);
+    // the steady body force (a source term the reference does not have):
+    // added after gradp over the same ranges
+    if (c.bodyforce) {
+        const double* fx = c.F("FBX") + o; const double* fy = c.F("FBY") + o; const double* fz = c.F("FBZ") + o;
+        for (int i = 3 - nfu; i <= ii - 3 + nbu; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k) A(uo, k, j, i) = A(uo, k, j, i) + A(fx, k, j, i);
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3 - nrv; j <= jj - 3 + nlv; ++j)
+                for (int k = 3; k <= kk - 2; ++k) A(vo, k, j, i) = A(vo, k, j, i) + A(fy, k, j, i);
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k) A(wo, k, j, i) = A(wo, k, j, i) + A(fz, k, j, i);
+    }
 #undef A
     tstle4_par(kk, jj, ii, uo, vo, wo, u, v, w, ut, vt, wt, dx, dy, dz, ddx, ddy, ddz, rdx, rdy, rdz,
                rddx, rddy, rddz, nfro, nbac, nrgt, nlft, nbot, ntop);
@@ -3313,6 +3328,17 @@ int oracle_ftoc(oracle_ctx* c, int ilevel, const char* ff, const char* fc, char 
     if (c->ibtype == 1 && flag == 'T')
         return fail(MGLET_ERR_UNSUPPORTED, "ftoc: the ghost-cell T restriction weighs by BT, which is not kept");
     ftoc_one(*c, ilevel, ff, fc, flag);
+    return 0;
+}
+
+int oracle_set_body_force(oracle_ctx* c, const double* fx, const double* fy, const double* fz,
+                          int64_t n) {
+    if (!c || !fx || !fy || !fz) return fail(MGLET_ERR_ARG, "set_body_force: bad arguments");
+    if (n != c->idim3d) return fail(MGLET_ERR_SIZE, "set_body_force: n must equal idim3d");
+    c->f3["FBX"].assign(fx, fx + n);
+    c->f3["FBY"].assign(fy, fy + n);
+    c->f3["FBZ"].assign(fz, fz + n);
+    c->bodyforce = true;
     return 0;
 }
 
