@@ -728,12 +728,12 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     MG_CUDA(cudaMalloc(&c->d_gridred, (size_t)4 * c->ngrid * sizeof(double)));
     MG_CUDA(cudaMalloc(&c->d_scalar, 8 * sizeof(double)));
     MG_CUDA(cudaMallocHost(&c->h_scalar, 8 * sizeof(double)));
-    // lesmodel_mod.F90:70 (G = gmol), noib_mod.F90:45-52 (BP = 1, SDIV = 0)
-    if (int rc = fill(c, c->F("G"), prm->gmol)) return bail(rc);
+    // noib_mod.F90:45-52 (BP = 1, SDIV = 0)
     if (int rc = fill(c, c->F("BP"), 1.0)) return bail(rc);
     build_connection_table(c);
     if (int rc = bound_init(c)) return bail(rc);
     if (int rc = level_init(c)) return bail(rc);
+    if (int rc = init_viscosity(c)) return bail(rc);
     if (int rc = launch_giteig(c)) return bail(rc);
     MG_CUDA(cudaStreamSynchronize(c->stream));
     int rc = prm->psolver == MGLET_PSOLVER_CLASSIC ? launch_sip_lu_classic(c) : launch_sip_lu_hp(c);
@@ -803,6 +803,7 @@ int mglet_gpu_set_field(mglet_ctx* c, const char* name, const double* host, int6
     cudaSetDevice(c->device);
     MG_CUDA(cudaMemcpyAsync(p, host, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     MG_CUDA(cudaStreamSynchronize(c->stream));
+    if (std::strcmp(name, "G") == 0) c->g_user = true;
     if (c->prm.form == MGLET_FORM_MIXED) mixed_field_changed(c, name);
     return 0;
 }

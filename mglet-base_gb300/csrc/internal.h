@@ -147,6 +147,7 @@ struct Ctx {
     // have run since the lists were set: their restores may follow
     bool gc_saved[2] = {false, false};
     bool bodyforce = false;      // FBX, FBY, FBZ added in tstle4 (plain form)
+    bool g_user = false;         // G set by the caller: set_hierarchy keeps it
     void* d_sptab = nullptr;     // device table of the 12 spacing arrays (adjoint)
     std::vector<GcHostList> gch;
     GcDev gcd;
@@ -250,6 +251,7 @@ int launch_itinfo(Ctx* c, double dt);
 int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p, int ilevel = 0);
 // multi-level operators (plain_level.cu)
 int level_init(Ctx* c);                      // PAR face lists (create)
+int init_viscosity(Ctx* c);                  // G of init_lesmodel, model "none"
 int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos);
 double* field_buffer(Ctx* c, const std::string& name);   // boundary buffers of a field
 int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w);
@@ -285,6 +287,9 @@ int launch_maskbp(Ctx* c, double* u, double* v, double* w, double* p);
 int gc_setibvalues(Ctx* c, double* u, double* v, double* w);
 int gc_setpointvalues(Ctx* c, bool comp_new);
 int launch_connect(Ctx* c, const ConnectPlan& plan, double* const fields[6]);
+// connect(ilevel, layers, v1..s3, corners, normal, forward) (api.cu)
+int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,
+            double* s2, double* s3, bool corners, bool normal, int forward);
 // FP32 copy of the same task list; returns early when *skip != 0 (device
 // flag of the mixed form's converged outer loop), skip may be null.
 int launch_connect32(Ctx* c, const ConnectPlan& plan, float* const fields[6], const int* skip);

@@ -13,6 +13,7 @@
 // restatement bit for bit.
 #include <algorithm>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #include "internal.h"
@@ -783,6 +784,56 @@ __global__ void k_tstle4_par(ParFluxArgs A) {
 }
 #undef PAR_LOOP2
 
+// ---- the viscosity field G (lesmodel_mod.F90:63-80, 573-764) --------------
+// G = gmol inside every grid, 0 on its ghost layers
+__global__ void k_init_g(const DevGrid* __restrict__ grids, double* Gf, double gmol) {
+    const DevGrid G = grids[blockIdx.y];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= kk * jj * ii) return;
+    const int k = t % kk + 1, j = (t / kk) % jj + 1, i = t / (kk * jj) + 1;
+    const bool in = i >= 3 && i <= ii - 2 && j >= 3 && j <= jj - 2 && k >= 3 && k <= kk - 2;
+    Gf[G.ip3 + t] = in ? gmol : 0.0;
+}
+
+// bfront / bright / bbottom of G for face f (1..6) of the grids of ilevel
+__global__ void k_bound_g(const DevGrid* __restrict__ grids, const BFace* __restrict__ bface,
+                          int f, int ilevel, double* Gf, const double* __restrict__ BPF,
+                          const double* __restrict__ buf, double geps) {
+    const DevGrid G = grids[blockIdx.y];
+    if (G.level != ilevel) return;
+    const int t = G.bc[f - 1];
+    const bool wall = t == MGLET_BC_NOS || t == MGLET_BC_SLI;
+    const bool copy = t == MGLET_BC_FIX || t == MGLET_BC_OP1;
+    const bool par = t == MGLET_BC_PAR;
+    if (!wall && !copy && !par) return;
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int d = (f - 1) / 2;
+    const int na = d == 0 ? jj : ii, nq = d == 2 ? jj : kk;
+    const int q0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q0 >= na * nq) return;
+    const int a = q0 / nq + 1, q = q0 % nq + 1;
+    if (par && (a < 2 || a > na - 1 || q < 2 || q > nq - 1)) return;
+    const int n = d == 0 ? ii : (d == 1 ? jj : kk);
+    const int p2 = f % 2 == 1 ? 2 : n - 1, p3 = f % 2 == 1 ? 3 : n - 2;
+    auto at = [&](int p) -> long long {
+        if (d == 0) return (long long)(p - 1) * kk * jj + (long long)(a - 1) * kk + (q - 1);
+        if (d == 1) return (long long)(a - 1) * kk * jj + (long long)(p - 1) * kk + (q - 1);
+        return (long long)(a - 1) * kk * jj + (long long)(q - 1) * kk + (p - 1);
+    };
+    double* gv = Gf + G.ip3;
+    const long long x = at(p2);
+    if (wall) {
+        gv[x] = geps;
+    } else if (copy) {
+        gv[x] = gv[at(p3)];
+    } else {
+        const double sbp = BPF[G.ip3 + x];
+        const double* b = buf + bface[6 * blockIdx.y + f - 1].off;
+        gv[x] = b[(q - 1) + (long long)(a - 1) * nq] * sbp + (1.0 - sbp) * gv[x];
+    }
+}
+
 // ---- par_ftoc_norm (par_ftoc_mod.F90:36-318) ------------------------------
 // One block per message, one thread per coarse face: the area mean (or the
 // sum) of the 2x2 fine faces of the PAR plane (pack_single), written where
@@ -993,6 +1044,9 @@ int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos) {
             c->d_plist[f][kv.first] = d;
         }
     }
+    // the finer levels' G takes its PAR values now that the parents are known
+    if (!c->g_user)
+        if (int rc = init_viscosity(c)) return rc;
     return 0;
 }
 
@@ -1036,6 +1090,40 @@ int launch_tstle4_par(Ctx* c, double* uo, double* vo, double* wo, const double* 
         MG_CUDA(cudaFuncSetAttribute(k_tstle4_par, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     k_tstle4_par<<<c->npargrids, 256, smem, c->stream>>>(A);
     MG_LAUNCHED(c);
+    return 0;
+}
+
+// init_lesmodel for the model "none" (lesmodel_mod.F90:63-80): G = gmol
+// inside, 0 on the ghost layers (zero_ghostlayers), connected with corners;
+// on the finer levels the parent's values into the PAR buffers and the bound
+// of G.  The coarsest level's wall ghosts keep 0: no viscous flux crosses
+// those faces (NOS walls carry the wall function instead).
+int init_viscosity(Ctx* c) {
+    double* Gf = c->F("G");
+    int m = 0;
+    for (const DevGrid& g : c->grids) m = std::max(m, g.kk * g.jj * g.ii);
+    k_init_g<<<dim3((m + 255) / 256, c->ngrid), 256, 0, c->stream>>>(c->d_grids, Gf, c->prm.gmol);
+    MG_LAUNCHED(c);
+    if (int rc = connect(c, 0, 2, nullptr, nullptr, nullptr, Gf, nullptr, nullptr, true, false, 0))
+        return rc;
+    static const char* const none[3] = {nullptr, nullptr, nullptr};
+    static const char* const sg[3] = {"G", nullptr, nullptr};
+    double* buf = field_buffer(c, "G");
+    if (!buf) {
+        set_error("init_viscosity: buffer allocation");
+        return MGLET_ERR_CUDA;
+    }
+    int mp = 0;
+    for (const DevGrid& g : c->grids) mp = std::max(mp, std::max(g.jj * g.kk, std::max(g.ii * g.kk, g.ii * g.jj)));
+    const double geps = -std::numeric_limits<double>::epsilon() * c->prm.gmol;
+    for (int l = c->minlevel + 1; l <= c->maxlevel; ++l) {
+        if (int rc = launch_parent(c, l, none, sg, false)) return rc;
+        for (int f = 1; f <= 6; ++f) {
+            k_bound_g<<<dim3((mp + 127) / 128, c->ngrid), 128, 0, c->stream>>>(
+                c->d_grids, c->d_bface, f, l, Gf, c->F("BP"), buf, geps);
+            MG_LAUNCHED(c);
+        }
+    }
     return 0;
 }
 

@@ -290,6 +290,34 @@ def add_noise(case, fields, amplitude=1e-2, seed=42):
     return out
 
 
+def gaussian_force(case, rms=0.1, length=0.5, seed=2025):
+    """A steady body force drawn from a seeded Gaussian random field: white
+    noise on the global periodic cell lattice of the tiling, filtered in
+    Fourier space by exp(-(k length)^2 / 2) (correlation length `length`),
+    each component scaled to the given rms over the interior.  Returns
+    (fx, fy, fz) as flat fields; the ghost layers are 0 (tstle4 reads the
+    force on interior points only)."""
+    rng = np.random.default_rng(seed)
+    n = case.ii - 4
+    gp = case.gridpos
+    nx, ny, nz = (int(gp[:, q].max()) + 1 for q in range(3))
+    N = (nx * n, ny * n, nz * n)
+    h = (case.dx[0], case.dy[0], case.dz[0])
+    ks = [2 * np.pi * np.fft.fftfreq(N[q], d=h[q]) for q in range(3)]
+    k2 = ks[0][:, None, None] ** 2 + ks[1][None, :, None] ** 2 + ks[2][None, None, :] ** 2
+    filt = np.exp(-0.5 * k2 * length ** 2)
+    out = []
+    for _ in range(3):
+        g = np.real(np.fft.ifftn(np.fft.fftn(rng.standard_normal(N)) * filt))
+        g *= rms / np.sqrt(np.mean(g * g))
+        f = np.zeros((case.ngrid, case.ii, case.jj, case.kk))
+        for q in range(case.ngrid):
+            x0, y0, z0 = gp[q, 0] * n, gp[q, 1] * n, gp[q, 2] * n
+            f[q, 2:-2, 2:-2, 2:-2] = g[x0:x0 + n, y0:y0 + n, z0:z0 + n]
+        out.append(f.ravel())
+    return tuple(out)
+
+
 def divergence_free_modes(case, nmodes=24, kpeak=4.0, urms=1.0, seed=1234):
     """Solenoidal random field: a sum of Fourier modes with |k| drawn from a
     Gaussian shell around kpeak, each amplitude orthogonal to its wave

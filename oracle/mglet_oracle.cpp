@@ -148,6 +148,8 @@ struct Ctx {
     std::vector<int> npinf;      // 0: no parameter (pinf = 0), 1: pinf given
     int ibtype = 0;              // 0: NONE (noib), 1: GHOSTCELL
     bool bodyforce = false;      // FBX, FBY, FBZ added in tstle4
+    bool g_user = false;         // G set by the caller: set_hierarchy keeps it
+    double cm = 0.0;             // LES model constant
     std::vector<std::array<GcList, 3>> gcl;   // [grid][component], 1-based grids
     std::vector<GcFlux> gcf;
     // grid hierarchy (gridinfo%iparent and i/j/kposition, grids_mod.F90):
@@ -1661,6 +1663,269 @@ void par_ftoc_norm(Ctx& c, int ilevel, double* U, double* V, double* W, bool sum
     }
 }
 
+// lesmodel_mod.F90:573-764 bfront / bright / bbottom, the bound of the
+// viscosity G on the grids of ilevel, faces in the order of bound_mod.F90:
+// 36-76: NOS and SLI put -EPSILON*gmol into the first ghost plane, FIX and
+// OP1 copy the first interior plane there, PAR takes its buffer (rows
+// 2..n-1) where BP is open.
+void bound_g(Ctx& c, int ilevel) {
+    double* Gf = c.F("G");
+    const double* BP = c.F("BP");
+    const std::vector<double>& buf = buffer_of(c, "G");
+    const double geps = -std::numeric_limits<double>::epsilon() * c.prm.gmol;
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel) continue;
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        double* gv = Gf + G.ip3;
+        const double* bp = BP + G.ip3;
+        for (int f = 1; f <= 6; ++f) {
+            const int t = G.bc[f];
+            const bool wall = t == MGLET_BC_NOS || t == MGLET_BC_SLI;
+            const bool copy = t == MGLET_BC_FIX || t == MGLET_BC_OP1;
+            const bool par = t == MGLET_BC_PAR;
+            if (!wall && !copy && !par) continue;
+            const int d = (f - 1) / 2;
+            const int n = d == 0 ? ii : (d == 1 ? jj : kk);
+            const int p2 = f % 2 == 1 ? 2 : n - 1, p3 = f % 2 == 1 ? 3 : n - 2;
+            const double* b = buf.data() + c.bufoff[6 * (g - 1) + f - 1];
+            // the plane's two directions (a outer, q inner) and the flat index
+            const int na = d == 2 ? ii : (d == 1 ? ii : jj), nq = d == 2 ? jj : kk;
+            auto at = [&](int p, int a, int q) -> int64_t {
+                if (d == 0) return IX(q, a, p);
+                if (d == 1) return IX(q, p, a);
+                return IX(p, q, a);
+            };
+            const int lo = par ? 2 : 1, ahi = par ? na - 1 : na, qhi = par ? nq - 1 : nq;
+            for (int a = lo; a <= ahi; ++a)
+                for (int q = lo; q <= qhi; ++q) {
+                    const int64_t x = at(p2, a, q);
+                    if (wall) {
+                        gv[x] = geps;
+                    } else if (copy) {
+                        gv[x] = gv[at(p3, a, q)];
+                    } else {
+                        const double sbp = bp[x];
+                        gv[x] = b[(q - 1) + (int64_t)(a - 1) * nq] * sbp + (1.0 - sbp) * gv[x];
+                    }
+                }
+        }
+    }
+}
+
+// lesmodel_mod.F90:63-80 init_lesmodel for the model "none": G = gmol inside
+// every grid and 0 on its ghost layers (zero_ghostlayers, mgletmath_mod.F90:
+// 27-44), connected with corners; on the finer levels the PAR buffers from
+// the parent (parent, s1 = G) and the bound above.  The coarsest level's
+// wall faces keep G = 0 in their ghosts, so no viscous flux crosses them.
+void init_viscosity(Ctx& c) {
+    double* Gf = c.F("G");
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        double* gv = Gf + G.ip3;
+        for (int i = 1; i <= ii; ++i)
+            for (int j = 1; j <= jj; ++j)
+                for (int k = 1; k <= kk; ++k) {
+                    const bool in = i >= 3 && i <= ii - 2 && j >= 3 && j <= jj - 2 && k >= 3 && k <= kk - 2;
+                    gv[IX(k, j, i)] = in ? c.prm.gmol : 0.0;
+                }
+    }
+    connect(c, 0, 2, nullptr, nullptr, nullptr, Gf, nullptr, nullptr, true, false, 0);
+    const char* none[3] = {nullptr, nullptr, nullptr};
+    const char* sg[3] = {"G", nullptr, nullptr};
+    for (int l = c.minlevel + 1; l <= c.maxlevel; ++l) {
+        parent(c, l, none, sg, false);
+        bound_g(c, l);
+    }
+}
+
+// wernerwengle_mod.F90:13-28 init_wernerwengle: the constants of the
+// Werner-Wengle wall function for gmol and rho
+struct WernerWengle {
+    double rho, gmol, cwb, cpo4, cpo5, cpo6, cpo8;
+};
+
+WernerWengle werner_wengle(double gmol, double rho) {
+    WernerWengle q;
+    const double cwa = 8.3;
+    q.rho = rho;
+    q.gmol = gmol;
+    q.cwb = 1.0 / 7.0;
+    const double cpo1 = 1.0 - q.cwb;
+    const double cpo2 = 1.0 + q.cwb;
+    q.cpo4 = cpo2 / cwa * std::pow(gmol / rho, q.cwb);
+    q.cpo5 = 0.5 * cpo1 * std::pow(cwa, cpo2 / cpo1) * std::pow(gmol / rho, cpo2);
+    q.cpo6 = 0.5 * gmol / rho * std::pow(cwa, 2.0 / cpo1);
+    q.cpo8 = 2.0 / cpo2;
+    return q;
+}
+
+// ---- LES models (lesmodel_mod.F90:93-570) ---------------------------------
+
+// the default-kind literal of a model constant, widened: Cm = 0.1 is the
+// single-precision 0.1
+double les_default_cm(int model) {
+    return model == 1 ? (double)0.1f : (model == 2 ? 0.5 : (double)1.35f);
+}
+
+double sabs(double dudx, double dudy, double dudz, double dvdx, double dvdy, double dvdz,
+            double dwdx, double dwdy, double dwdz) {
+    // lesmodel_mod.F90:520-540
+    return std::sqrt(dudx * dudx + dvdy * dvdy + dwdz * dwdz + 0.5 * ((dvdx + dudy) * (dvdx + dudy)) +
+                     0.5 * ((dwdx + dudz) * (dwdx + dudz)) + 0.5 * ((dwdy + dvdz) * (dwdy + dvdz)));
+}
+
+// lesmodel_mod.F90:368-390 smagorinsky: Cm^2 sqrt(2) |S|
+double les_smagorinsky(double cm, const double* gr) {
+    return cm * cm * std::sqrt(2.0) * sabs(gr[0], gr[1], gr[2], gr[3], gr[4], gr[5], gr[6], gr[7], gr[8]);
+}
+
+// lesmodel_mod.F90:393-487 wale; x**5 as x^3 x^2, the expansion of an
+// integer power by repeated products
+double les_wale(double cm, double tol, const double* gr) {
+    const double dudx = gr[0], dudy = gr[1], dudz = gr[2], dvdx = gr[3], dvdy = gr[4], dvdz = gr[5];
+    const double dwdx = gr[6], dwdy = gr[7], dwdz = gr[8];
+    const double third = (double)(1.0f / 3.0f);   // (1.0/3.0) of default-kind literals
+    const double tr = dudx * dudx + dudy * dvdx + dudz * dwdx + dvdx * dudy + dvdy * dvdy + dvdz * dwdy +
+                      dwdx * dudz + dwdy * dvdz + dwdz * dwdz;
+    const double sd00 = 0.5 * (dudx * dudx + dudy * dvdx + dudz * dwdx + dudx * dudx + dudy * dvdx + dudz * dwdx) -
+                        third * tr;
+    const double sd01 = 0.5 * (dudx * dudy + dudy * dvdy + dudz * dwdy + dvdx * dudx + dvdy * dvdx + dvdz * dwdx);
+    const double sd02 = 0.5 * (dudx * dudz + dudy * dvdz + dudz * dwdz + dwdx * dudx + dwdy * dvdx + dwdz * dwdx);
+    const double sd11 = 0.5 * (dvdx * dudy + dvdy * dvdy + dvdz * dwdy + dvdx * dudy + dvdy * dvdy + dvdz * dwdy) -
+                        third * tr;
+    const double sd12 = 0.5 * (dvdx * dudz + dvdy * dvdz + dvdz * dwdz + dwdx * dudy + dwdy * dvdy + dwdz * dwdy);
+    const double sd22 = 0.5 * (dwdx * dudz + dwdy * dvdz + dwdz * dwdz + dwdx * dudz + dwdy * dvdz + dwdz * dwdz) -
+                        third * tr;
+    const double sdabs = std::sqrt(sd00 * sd00 + 2 * (sd01 * sd01) + 2 * (sd02 * sd02) + sd11 * sd11 +
+                                   2 * (sd12 * sd12) + sd22 * sd22);
+    const double sa = sabs(dudx, dudy, dudz, dvdx, dvdy, dvdz, dwdx, dwdy, dwdz);
+    const double root = std::sqrt(sdabs);
+    if (root < tol * sa) return 0.0;
+    const double x = root == 0.0 ? 0.0 : sa / root;
+    const double x2 = x * x, x3 = x2 * x;
+    return cm * cm * root / (x3 * x2 + 1.0);
+}
+
+// the Werner-Wengle gradient dds/2 from the wall (wernerwengle_mod.F90:36-61)
+double gradp2(const WernerWengle& q, double cpo11, double cpo12, double uquer, double dds) {
+    const double uquern = std::fabs(uquer);
+    const double vz = std::copysign(1.0, uquer);
+    const double rdds = 1.0 / dds;
+    if (uquern >= q.cpo6 * rdds) return rdds * (cpo12 * uquern + cpo11 * rdds) * vz;
+    return 2.0 * uquern / dds * vz;
+}
+
+// efvisc_gc (lesmodel_mod.F90:200-365) of one grid: G inside from the
+// velocity gradients, the filter width cbrt(cell volume) * BP, and the NOS
+// wall-model gradients
+void efvisc_grid(Ctx& c, int g) {
+    const Grid& G = c.g[g];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int64_t o = G.ip3;
+    const double* u = c.F("U") + o; const double* v = c.F("V") + o; const double* w = c.F("W") + o;
+    const double* bp = c.F("BP") + o;
+    double* gv = c.F("G") + o;
+    const double* dx = c.L("DX") + G.ipx - 1; const double* dy = c.L("DY") + G.ipy - 1;
+    const double* dz = c.L("DZ") + G.ipz - 1;
+    const double* ddx = c.L("DDX") + G.ipx - 1; const double* ddy = c.L("DDY") + G.ipy - 1;
+    const double* ddz = c.L("DDZ") + G.ipz - 1;
+    const double* rddx = c.L("RDDX") + G.ipx - 1; const double* rddy = c.L("RDDY") + G.ipy - 1;
+    const double* rddz = c.L("RDDZ") + G.ipz - 1;
+    const double gmol = c.prm.gmol, rho = c.prm.rho;
+    const WernerWengle q = werner_wengle(gmol, rho);
+    const double cwb = q.cwb, cpo1 = 1.0 - cwb, cpo2 = 1.0 + cwb;
+    const double cpo11 = 2.0 * q.cpo6 * cwb * cpo1 / std::pow(2.0, cwb);
+    const double cpo12 = cwb * cpo2 / std::pow(2.0, cwb - 1.0);
+    const double tol = 1.0 / std::pow(std::numeric_limits<double>::max(), 1.0 / 6.0);
+    const int nfro = G.bc[1], nbac = G.bc[2], nrgt = G.bc[3], nlft = G.bc[4], nbot = G.bc[5], ntop = G.bc[6];
+#define A(a, k, j, i) a[IX(k, j, i)]
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                double gr[9];
+                const double dxf = 0.25 * dx[i - 1] * rddx[i];
+                gr[0] = (A(u, k, j, i) - A(u, k, j, i - 1)) * rddx[i];
+                gr[1] = ((A(u, k, j + 1, i) - A(u, k, j - 1, i)) * dxf +
+                         (A(u, k, j + 1, i - 1) - A(u, k, j - 1, i - 1)) * (0.5 - dxf)) * rddy[j];
+                gr[2] = ((A(u, k + 1, j, i) - A(u, k - 1, j, i)) * dxf +
+                         (A(u, k + 1, j, i - 1) - A(u, k - 1, j, i - 1)) * (0.5 - dxf)) * rddz[k];
+                const double dyf = 0.25 * dy[j - 1] * rddy[j];
+                gr[3] = ((A(v, k, j, i + 1) - A(v, k, j, i - 1)) * dyf +
+                         (A(v, k, j - 1, i + 1) - A(v, k, j - 1, i - 1)) * (0.5 - dyf)) * rddx[i];
+                gr[4] = (A(v, k, j, i) - A(v, k, j - 1, i)) * rddy[j];
+                gr[5] = ((A(v, k + 1, j, i) - A(v, k - 1, j, i)) * dyf +
+                         (A(v, k + 1, j - 1, i) - A(v, k - 1, j - 1, i)) * (0.5 - dyf)) * rddz[k];
+                const double dzf = 0.25 * dz[k - 1] * rddz[k];
+                gr[6] = ((A(w, k, j, i + 1) - A(w, k, j, i - 1)) * dzf +
+                         (A(w, k - 1, j, i + 1) - A(w, k - 1, j, i - 1)) * (0.5 - dzf)) * rddx[i];
+                gr[7] = ((A(w, k, j + 1, i) - A(w, k, j - 1, i)) * dzf +
+                         (A(w, k - 1, j + 1, i) - A(w, k - 1, j - 1, i)) * (0.5 - dzf)) * rddy[j];
+                gr[8] = (A(w, k, j, i) - A(w, k - 1, j, i)) * rddz[k];
+                double delta = std::cbrt(ddx[i] * ddy[j] * ddz[k]);
+                delta = delta * A(bp, k, j, i);
+                // NOS corrections (:261-330), in the reference's order
+                const double dyf2 = 0.5 * dy[j - 1] * rddy[j], dzf2 = 0.5 * dz[k - 1] * rddz[k];
+                const double dxf2 = 0.5 * dx[i - 1] * rddx[i];
+                const double vm = dyf2 * A(v, k, j, i) + (1.0 - dyf2) * A(v, k, j - 1, i);
+                const double wm = dzf2 * A(w, k, j, i) + (1.0 - dzf2) * A(w, k - 1, j, i);
+                const double um = dxf2 * A(u, k, j, i) + (1.0 - dxf2) * A(u, k, j, i - 1);
+                if (nfro == 5 && i == 3) { gr[3] = gradp2(q, cpo11, cpo12, vm, ddx[i]); gr[6] = gradp2(q, cpo11, cpo12, wm, ddx[i]); }
+                if (nbac == 5 && i == ii - 2) { gr[3] = -gradp2(q, cpo11, cpo12, vm, ddx[i]); gr[6] = -gradp2(q, cpo11, cpo12, wm, ddx[i]); }
+                if (nrgt == 5 && j == 3) { gr[1] = gradp2(q, cpo11, cpo12, um, ddy[j]); gr[7] = gradp2(q, cpo11, cpo12, wm, ddy[j]); }
+                if (nlft == 5 && j == jj - 2) { gr[1] = -gradp2(q, cpo11, cpo12, um, ddy[j]); gr[7] = -gradp2(q, cpo11, cpo12, wm, ddy[j]); }
+                if (nbot == 5 && k == 3) { gr[2] = gradp2(q, cpo11, cpo12, um, ddz[k]); gr[5] = gradp2(q, cpo11, cpo12, vm, ddz[k]); }
+                if (ntop == 5 && k == kk - 2) { gr[2] = -gradp2(q, cpo11, cpo12, um, ddz[k]); gr[5] = -gradp2(q, cpo11, cpo12, vm, ddz[k]); }
+                const double dm = c.ilesmodel == 1 ? les_smagorinsky(c.cm, gr) : les_wale(c.cm, tol, gr);
+                A(gv, k, j, i) = rho * (delta * delta) * dm + gmol;
+            }
+#undef A
+}
+
+// setginbody (lesmodel_mod.F90:543-570): in blocked cells G is the mean of
+// the open neighbours, in place and in loop order
+void setginbody(Ctx& c, int g) {
+    const Grid& G = c.g[g];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    double* gv = c.F("G") + G.ip3;
+    const double* bp = c.F("BP") + G.ip3;
+#define A(a, k, j, i) a[IX(k, j, i)]
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                double nn = A(bp, k, j, i + 1) + A(bp, k, j, i - 1) + A(bp, k, j + 1, i) + A(bp, k, j - 1, i) +
+                            A(bp, k + 1, j, i) + A(bp, k - 1, j, i);
+                nn = std::max(nn, 1.0);
+                const double gbpn = (A(gv, k, j, i + 1) * A(bp, k, j, i + 1) + A(gv, k, j, i - 1) * A(bp, k, j, i - 1) +
+                                     A(gv, k, j + 1, i) * A(bp, k, j + 1, i) + A(gv, k, j - 1, i) * A(bp, k, j - 1, i) +
+                                     A(gv, k + 1, j, i) * A(bp, k + 1, j, i) + A(gv, k - 1, j, i) * A(bp, k - 1, j, i)) /
+                                    nn;
+                A(gv, k, j, i) = A(bp, k, j, i) * A(gv, k, j, i) + (1.0 - A(bp, k, j, i)) * gbpn;
+            }
+#undef A
+}
+
+// lesmodel / lesmodel_gc (lesmodel_mod.F90:93-197): efvisc level by level
+// (finest first), then per level parent, bound and connect of G, setginbody,
+// and the corner connect tstle4 needs
+void lesmodel(Ctx& c) {
+    if (c.ilesmodel == 0) return;
+    for (int l = c.maxlevel; l >= c.minlevel; --l)
+        for (int g = 1; g <= c.ngrid; ++g)
+            if (c.g[g].level == l) efvisc_grid(c, g);
+    double* Gf = c.F("G");
+    const char* none[3] = {nullptr, nullptr, nullptr};
+    const char* sg[3] = {"G", nullptr, nullptr};
+    for (int l = c.minlevel; l <= c.maxlevel; ++l) {
+        parent(c, l, none, sg, false);
+        bound_g(c, l);
+        connect(c, l, 1, nullptr, nullptr, nullptr, Gf, nullptr, nullptr, false, false, 0);
+    }
+    for (int g = 1; g <= c.ngrid; ++g) setginbody(c, g);
+    connect(c, 0, 1, nullptr, nullptr, nullptr, Gf, nullptr, nullptr, true, false, 0);
+}
+
 // ---------------------------------------------------------------------------
 // Ghost-cell IB runtime (gc_flowstencils_mod.F90:922-1604, timeintegration_mod
 // :255-303).  The lists are walked cell after cell, as the reference does: a
@@ -2491,27 +2756,6 @@ void tstle4_par(int kk, int jj, int ii, double* uo, double* vo, double* wo, cons
 
 // tstle4_mod.F90:139-265 tstle4_kon, :268-458 tstle4_diff, :461-529 tstle4_gradp,
 // :532-1753 tstle4_par
-// wernerwengle_mod.F90:13-28 init_wernerwengle: the constants of the
-// Werner-Wengle wall function for gmol and rho
-struct WernerWengle {
-    double rho, gmol, cwb, cpo4, cpo5, cpo6, cpo8;
-};
-
-WernerWengle werner_wengle(double gmol, double rho) {
-    WernerWengle q;
-    const double cwa = 8.3;
-    q.rho = rho;
-    q.gmol = gmol;
-    q.cwb = 1.0 / 7.0;
-    const double cpo1 = 1.0 - q.cwb;
-    const double cpo2 = 1.0 + q.cwb;
-    q.cpo4 = cpo2 / cwa * std::pow(gmol / rho, q.cwb);
-    q.cpo5 = 0.5 * cpo1 * std::pow(cwa, cpo2 / cpo1) * std::pow(gmol / rho, cpo2);
-    q.cpo6 = 0.5 * gmol / rho * std::pow(cwa, 2.0 / cpo1);
-    q.cpo8 = 2.0 / cpo2;
-    return q;
-}
-
 // wernerwengle_mod.F90:64-87 tauwin and tstle4_mod.F90:1832-1844
 // swcle3d_one: the wall shear over rho and the wall-normal width dds
 double swcle3d_one(const WernerWengle& q, double dds, double u) {
@@ -3028,7 +3272,6 @@ int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle
         c->f3[n].assign(o3, 0.0);
     c->gcl.resize(d->ngrid + 1);
     c->gcf.resize(d->ngrid + 1);
-    std::fill(c->f3["G"].begin(), c->f3["G"].end(), prm->gmol);   // lesmodel_mod.F90:70
     std::fill(c->f3["BP"].begin(), c->f3["BP"].end(), 1.0);       // noib_mod.F90:45-47
     auto set1 = [&](const char* n, const double* src, int64_t len) {
         c->f1[n].assign(src, src + len);
@@ -3063,6 +3306,7 @@ int oracle_create(const mglet_grid_desc* d, const mglet_flow_params* prm, oracle
     c->pinf.assign(6 * (size_t)d->ngrid, 0.0);
     c->npinf.assign(6 * (size_t)d->ngrid, 0);
     init_connect_core(*c);
+    init_viscosity(*c);
     giteig(*c);
     int rc = init_pressuresolver(*c);
     if (rc) {
@@ -3085,6 +3329,7 @@ int oracle_set_field(oracle_ctx* c, const char* name, const double* host, int64_
     if (it == c->f3.end()) return fail(MGLET_ERR_NAME, std::string("unknown field ") + name);
     if (n != c->idim3d) return fail(MGLET_ERR_SIZE, "size mismatch");
     std::copy(host, host + n, it->second.begin());
+    if (std::strcmp(name, "G") == 0) c->g_user = true;
     return 0;
 }
 
@@ -3294,6 +3539,8 @@ int oracle_set_hierarchy(oracle_ctx* c, const int32_t* iparent, const int32_t* p
         c->iparent[g] = par;
         c->pos[g] = {pos[3 * (g - 1)], pos[3 * (g - 1) + 1], pos[3 * (g - 1) + 2]};
     }
+    // the finer levels' G takes its PAR values now that the parents are known
+    if (!c->g_user) init_viscosity(*c);
     return 0;
 }
 

@@ -126,6 +126,13 @@ def test_turbulent_wall_stage(gpu_lib, oracle_lib):
         assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), nm
 
 
+@pytest.mark.parametrize("walls", WALLS)
+def test_viscosity_field_at_start(gpu_lib, oracle_lib, walls):
+    case = cases.periodic_box(2, 2, 1, n=8, length=(2.0, 2.0, 1.0), walls=walls)
+    gs, o = gpu_lib.Solver(case, _prm()), oracle_lib.Oracle(case, _prm())
+    assert np.array_equal(gs.get("G"), o.get("G"))
+
+
 def test_mixed_form_refuses_walls(gpu_lib):
     """The batched mixed form pulls every halo from a face neighbour, so a
     hierarchy with wall faces is refused loudly, not run approximately."""

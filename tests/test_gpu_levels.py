@@ -132,6 +132,13 @@ def test_multilevel_mgpoisl_bit_exact(gpu_lib, oracle_lib, h, psolver):
 
 
 @pytest.mark.parametrize("h", HIERARCHIES)
+def test_viscosity_on_par_faces(gpu_lib, oracle_lib, h):
+    """G after set_hierarchy: the parent's values on the PAR ghost planes."""
+    case, gs, o = _pair(gpu_lib, oracle_lib, h)
+    assert np.array_equal(gs.get("G"), o.get("G"))
+
+
+@pytest.mark.parametrize("h", HIERARCHIES)
 def test_tstle4_par_bit_exact(gpu_lib, oracle_lib, h):
     """tstle4 with tstle4_par on every grid with PAR faces."""
     case, gs, o = _pair(gpu_lib, oracle_lib, h)

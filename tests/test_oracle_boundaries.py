@@ -252,3 +252,25 @@ def test_op1_ghost_pressure(oracle_lib, udir, expect):
     P = o.get("P").reshape(case.ii, case.jj, case.kk)
     ghost = P[case.ii - 2, 1:, 1:]   # i2 = ii-1, j, k = 2..
     assert np.allclose(ghost, expect, rtol=0, atol=1e-15)
+
+
+@pytest.mark.parametrize("walls", [{5: abi.BC_NOS, 6: abi.BC_SLI}, {1: abi.BC_FIX, 2: abi.BC_OP1}, None])
+def test_viscosity_field_at_start(oracle_lib, walls):
+    """G as init_lesmodel leaves it for the model "none" (lesmodel_mod.F90:
+    63-80): gmol inside, 0 on the ghost layers, then connected with corners,
+    so the ghost layers of a CON face hold gmol and those of a boundary face
+    stay 0 on the coarsest level (no viscous flux through it; NOS walls carry
+    the wall function instead)."""
+    gmol = 0.02
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0), walls=walls)
+    o = oracle_lib.Oracle(case, _prm(gmol=gmol))
+    G = o.get("G").reshape(case.ngrid, case.ii, case.jj, case.kk)
+    assert np.all(G[:, 2:-2, 2:-2, 2:-2] == gmol)
+    for g in range(case.ngrid):
+        for f in range(1, 7):
+            d, hi = (f - 1) // 2, (f - 1) % 2
+            ghost = [slice(2, -2)] * 3
+            ghost[d] = slice(-2, None) if hi else slice(0, 2)
+            plane = G[g][tuple(ghost)]
+            want = gmol if case.bctype[g, f - 1] == abi.BC_CON else 0.0
+            assert np.all(plane == want), (g, f)

@@ -636,3 +636,27 @@ def test_multilevel_stage_is_divergence_free(case):
         st = o.timeintegrate_flow(1, 1, 0.0, 1e-2, irk, rk)
         assert st.maxrhs / st.prefak < 1e-11 and st.nouter_done < 200
         assert _divmax(o, case).max() < 1e-9
+
+
+def test_viscosity_on_par_faces(case):
+    """On the finer level G takes the parent's value in the first ghost plane
+    of a PAR face (parent, s1 = G, then the PAR branch of the bound of G,
+    lesmodel_mod.F90:573-764, rows 2..n-1), and the outer ghost plane keeps
+    the 0 of zero_ghostlayers."""
+    o = _oracle(case)
+    gmol = 1e-2
+    G = o.get("G").reshape(case.ngrid, case.ii, case.jj, case.kk)
+    checked = 0
+    for g in _fine(case):
+        for f in range(1, 7):
+            if case.bctype[g, f - 1] != abi.BC_PAR:
+                continue
+            d, hi = (f - 1) // 2, (f - 1) % 2
+            first = [slice(1, -1)] * 3
+            first[d] = -2 if hi else 1
+            outer = [slice(None)] * 3
+            outer[d] = -1 if hi else 0
+            assert np.all(G[g][tuple(first)] == gmol), (g, f)
+            assert np.all(G[g][tuple(outer)] == 0.0), (g, f)
+            checked += 1
+    assert checked > 0

@@ -140,3 +140,24 @@ def test_wall_stage_with_turbulent_wall_function_is_divergence_free(oracle_lib):
     res = st.maxrhs / st.prefak
     assert res < 1e-9
     assert o.itinfo(1e-2).divmax <= 1.01 * res + 1e-13
+
+
+def test_body_force_enters_tstle4(oracle_lib):
+    """The steady body force (a source term the reference does not have) is
+    added to uo, vo, wo over the flux ranges of tstle4, after gradp: on a
+    fluid at rest it is the whole of uo, vo, wo there, and nothing outside."""
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0))
+    o = oracle_lib.Oracle(case, abi.make_flow_params(gmol=1e-2, epcorr=1e-12, nouter=4, ninner=2))
+    rng = np.random.default_rng(12)
+    f = [rng.standard_normal(case.idim3d) for _ in range(3)]
+    for n in "UVWP":
+        o.set(n, case.zeros())
+    o.set_body_force(*f)
+    o.tstle4()
+    inner = np.zeros((case.ngrid, case.ii, case.jj, case.kk), dtype=bool)
+    inner[:, 2:-2, 2:-2, 2:-2] = True       # every face CON: 3..n-2 for every component
+    inner = inner.ravel()
+    for n, fv in zip(("UO", "VO", "WO"), f):
+        a = o.get(n)
+        assert np.array_equal(a[inner], fv[inner]), n
+        assert not np.any(a[~inner]), n
