@@ -284,6 +284,13 @@ int mglet_gpu_ctof(mglet_ctx* ctx, int32_t ilevel, const char* ff, const char* f
  * the fine mean next to the face; with_bp selects the BP-weighted form
  * (the reference passes bp for the ghost-cell IB only). */
 int mglet_gpu_bound_pressure(mglet_ctx* ctx, int32_t ilevel, const char* dp, int32_t with_bp);
+/* The LES model of the stage (lesmodel_mod.F90:34-84, plain form): 0 none,
+ * 1 smagorinsky, 2 wale (sigma is not built); cm < 0 takes the model's
+ * default constant.  Computes G of the current velocity at once, as
+ * init_lesmodel does; the stage then updates G after the pressure solve and
+ * tstle4_diff adds its LES cross term.  Model 0 restores G = gmol with the
+ * ghost layers of init_lesmodel. */
+int mglet_gpu_set_lesmodel(mglet_ctx* ctx, int32_t model, double cm);
 /* ---- Body force and the discrete adjoint (no counterpart in the reference) --
  * A steady body force per unit mass, added to uo, vo, wo in tstle4 after
  * gradp over the same points (plain form); n must equal idim3d. */

@@ -446,6 +446,8 @@ int adjoint_ready(Ctx* c) {
         return fail(MGLET_ERR_UNSUPPORTED, "adjoint: one grid level without immersed boundary");
     if (c->prm.psolver == MGLET_PSOLVER_SOR)
         return fail(MGLET_ERR_UNSUPPORTED, "adjoint: the SIP pressure solver");
+    if (c->ilesmodel != 0)
+        return fail(MGLET_ERR_UNSUPPORTED, "adjoint: constant viscosity (no LES model)");
     for (const DevGrid& G : c->grids)
         for (int f = 0; f < 6; ++f)
             if (G.bc[f] != MGLET_BC_CON)

@@ -515,6 +515,7 @@ static int stage_plain(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk,
         if (int rc = launch_bound_flow(c, U, V, W, P, c->minlevel != c->maxlevel ? l : 0)) return rc;
     }
     if (int rc = mgpoisl(c, dtrk * dt, st)) return rc;
+    if (int rc = lesmodel(c)) return rc;                  // :125
     if (gc) return gc_setpointvalues(c, irk == rk->nrk);   // :131-134
     return 0;
 }
@@ -945,6 +946,14 @@ int mglet_gpu_set_body_force(mglet_ctx* c, const double* fx, const double* fy, c
         MG_CUDA(copy_on(c->stream, c->F(nm[q]), h[q], (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
     }
     c->bodyforce = true;
+    return 0;
+}
+
+int mglet_gpu_set_lesmodel(mglet_ctx* c, int32_t model, double cm) {
+    if (!c) return fail(MGLET_ERR_ARG, "set_lesmodel: null context");
+    cudaSetDevice(c->device);
+    if (int rc = set_lesmodel(c, model, cm)) return rc;
+    MG_CUDA(cudaStreamSynchronize(c->stream));
     return 0;
 }
 

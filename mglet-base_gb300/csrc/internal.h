@@ -148,6 +148,8 @@ struct Ctx {
     bool gc_saved[2] = {false, false};
     bool bodyforce = false;      // FBX, FBY, FBZ added in tstle4 (plain form)
     bool g_user = false;         // G set by the caller: set_hierarchy keeps it
+    int ilesmodel = 0;           // 0 none, 1 smagorinsky, 2 wale
+    double cm = 0.0;             // the LES model constant
     void* d_sptab = nullptr;     // device table of the 12 spacing arrays (adjoint)
     std::vector<GcHostList> gch;
     GcDev gcd;
@@ -252,6 +254,9 @@ int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p, int il
 // multi-level operators (plain_level.cu)
 int level_init(Ctx* c);                      // PAR face lists (create)
 int init_viscosity(Ctx* c);                  // G of init_lesmodel, model "none"
+int launch_bound_g(Ctx* c, int ilevel);      // the bound of G (lesmodel_mod.F90:573-764)
+int lesmodel(Ctx* c);                        // G from the LES model (les.cu)
+int set_lesmodel(Ctx* c, int model, double cm);
 int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos);
 double* field_buffer(Ctx* c, const std::string& name);   // boundary buffers of a field
 int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w);

@@ -95,7 +95,7 @@ __device__ double wall_w(double x, int k, int j, int i, const GridPtrs& s, const
 __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
                            const double* w, const double* ut, const double* vt, const double* wt,
                            const double* p, const double* gg, const GridPtrs& s, const Wall& wl,
-                           double gmol, double rho, double gpx) {
+                           double gmol, double rho, double iles, double gpx) {
     const double *dx = s.dx, *dy = s.dy, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
                  *rddz = s.rddz;
@@ -137,7 +137,7 @@ __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u,
                      (gs * (A(v, k, j - 1, i + 1) - A(v, k, j - 1, i)))) * ddz[k] +
                     ((gt * (A(w, k, j, i + 1) - A(w, k, j, i))) -
                      (gb * (A(w, k - 1, j, i + 1) - A(w, k - 1, j, i)))) * ddy[j];
-        double qc = st * 0.0;   // iles = 0 (lesmodel "none")
+        double qc = st * iles;   // the LES cross term (iles = 0 without LES model)
         double fak = 1.0 / rho * rddy[j] * rdx[i] * rddz[k];
         uo = uo - fak * (qe - qw + qn - qs + qt - qb - qc);
     }
@@ -148,7 +148,7 @@ __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u,
 __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
                            const double* w, const double* ut, const double* vt, const double* wt,
                            const double* p, const double* gg, const GridPtrs& s, const Wall& wl,
-                           double gmol, double rho, double gpy) {
+                           double gmol, double rho, double iles, double gpy) {
     const double *dy = s.dy, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
                  *rddz = s.rddz;
@@ -190,7 +190,7 @@ __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u,
                      (gs * (A(v, k, j, i) - A(v, k, j - 1, i)) * rddy[j])) * ay +
                     ((gt * (A(w, k, j + 1, i) - A(w, k, j, i))) -
                      (gb * (A(w, k - 1, j + 1, i) - A(w, k - 1, j, i)))) * ddx[i];
-        double qc = st * 0.0;
+        double qc = st * iles;
         double fak = 1.0 / rho * rddx[i] * rdy[j] * rddz[k];
         vo = vo - fak * (qe - qw + qn - qs + qt - qb - qc);
     }
@@ -201,7 +201,7 @@ __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u,
 __device__ double wo_point(int k, int j, int i, int kk, int jj, const double* u, const double* v,
                            const double* w, const double* ut, const double* vt, const double* wt,
                            const double* p, const double* gg, const GridPtrs& s, const Wall& wl,
-                           double gmol, double rho, double gpz) {
+                           double gmol, double rho, double iles, double gpz) {
     const double *dz = s.dz, *ddx = s.ddx, *ddy = s.ddy, *ddz = s.ddz;
     const double *rdx = s.rdx, *rdy = s.rdy, *rdz = s.rdz, *rddx = s.rddx, *rddy = s.rddy,
                  *rddz = s.rddz;
@@ -243,7 +243,7 @@ __device__ double wo_point(int k, int j, int i, int kk, int jj, const double* u,
                      (gs * (A(v, k + 1, j - 1, i) - A(v, k, j - 1, i)))) * ddx[i] +
                     ((gt * (A(w, k + 1, j, i) - A(w, k, j, i)) * rddz[k + 1]) -
                      (gb * (A(w, k, j, i) - A(w, k - 1, j, i)) * rddz[k])) * az;
-        double qc = st * 0.0;
+        double qc = st * iles;
         double fak = 1.0 / rho * rddx[i] * rddy[j] * rdz[k];
         wo = wo - fak * (qe - qw + qn - qs + qt - qb - qc);
     }
@@ -260,7 +260,7 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
                                                 const double* __restrict__ UT, const double* __restrict__ VT,
                                                 const double* __restrict__ WT,
                                                 const double* __restrict__ P, const double* __restrict__ Gf,
-                                                Wall wl, double gx, double gy, double gz,
+                                                Wall wl, double iles, double gx, double gy, double gz,
                                                 const double* __restrict__ FX, const double* __restrict__ FY,
                                                 const double* __restrict__ FZ) {
     const DevGrid G = grids[blockIdx.y];
@@ -296,19 +296,19 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
     double ru, rv, rw;
     // the steady body force FX, FY, FZ (when set) follows gradp
     if (i >= 3 - nfu && i <= ii - 3 + nbu && jin && kin) {
-        ru = uo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gx * gfl);
+        ru = uo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, iles, gx * gfl);
         if (FX) ru = ru + FX[o + t];
     } else {
         ru = wall_u(0.0, k, j, i, s, wl, u[t]);
     }
     if (iin && j >= 3 - nrv && j <= jj - 3 + nlv && kin) {
-        rv = vo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gy * gfl);
+        rv = vo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, iles, gy * gfl);
         if (FY) rv = rv + FY[o + t];
     } else {
         rv = wall_v(0.0, k, j, i, s, wl, v[t]);
     }
     if (iin && jin && k >= 3 - nbw && k <= kk - 3 + ntw) {
-        rw = wo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, gz * gfl);
+        rw = wo_point(k, j, i, kk, jj, u, v, w, ut, vt, wt, p, g, s, wl, gmol, rho, iles, gz * gfl);
         if (FZ) rw = rw + FZ[o + t];
     } else {
         rw = wall_w(0.0, k, j, i, s, wl, w[t]);
@@ -364,7 +364,8 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
     wl.cpo6 = 0.5 * gmol / rho * std::pow(cwa, 2.0 / cpo1);
     wl.cpo8 = 2.0 / cpo2;
     k_tstle4<<<grid, 256, 0, c->stream>>>(c->d_grids, spacing(c), uo, vo, wo, u, v, w, ut, vt, wt, p, g,
-                                          wl, c->prm.gradp[0], c->prm.gradp[1], c->prm.gradp[2],
+                                          wl, c->ilesmodel ? 1.0 : 0.0, c->prm.gradp[0], c->prm.gradp[1],
+                                          c->prm.gradp[2],
                                           c->bodyforce ? c->F("FBX") : nullptr,
                                           c->bodyforce ? c->F("FBY") : nullptr,
                                           c->bodyforce ? c->F("FBZ") : nullptr);

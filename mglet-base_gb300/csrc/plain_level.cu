@@ -1108,21 +1108,28 @@ int init_viscosity(Ctx* c) {
         return rc;
     static const char* const none[3] = {nullptr, nullptr, nullptr};
     static const char* const sg[3] = {"G", nullptr, nullptr};
+    for (int l = c->minlevel + 1; l <= c->maxlevel; ++l) {
+        if (int rc = launch_parent(c, l, none, sg, false)) return rc;
+        if (int rc = launch_bound_g(c, l)) return rc;
+    }
+    return 0;
+}
+
+// the bound of G on the grids of ilevel, faces 1..6 one after the other
+// (bound_mod.F90:36-76)
+int launch_bound_g(Ctx* c, int ilevel) {
     double* buf = field_buffer(c, "G");
     if (!buf) {
-        set_error("init_viscosity: buffer allocation");
+        set_error("bound of G: buffer allocation");
         return MGLET_ERR_CUDA;
     }
     int mp = 0;
     for (const DevGrid& g : c->grids) mp = std::max(mp, std::max(g.jj * g.kk, std::max(g.ii * g.kk, g.ii * g.jj)));
     const double geps = -std::numeric_limits<double>::epsilon() * c->prm.gmol;
-    for (int l = c->minlevel + 1; l <= c->maxlevel; ++l) {
-        if (int rc = launch_parent(c, l, none, sg, false)) return rc;
-        for (int f = 1; f <= 6; ++f) {
-            k_bound_g<<<dim3((mp + 127) / 128, c->ngrid), 128, 0, c->stream>>>(
-                c->d_grids, c->d_bface, f, l, Gf, c->F("BP"), buf, geps);
-            MG_LAUNCHED(c);
-        }
+    for (int f = 1; f <= 6; ++f) {
+        k_bound_g<<<dim3((mp + 127) / 128, c->ngrid), 128, 0, c->stream>>>(
+            c->d_grids, c->d_bface, f, ilevel, c->F("G"), c->F("BP"), buf, geps);
+        MG_LAUNCHED(c);
     }
     return 0;
 }

@@ -181,6 +181,32 @@ MODULE mglet_gpu_mod
             CHARACTER(kind=c_char), INTENT(in) :: ff(*), fc(*)
         END FUNCTION mglet_gpu_ctof
 
+        INTEGER(c_int) FUNCTION mglet_gpu_set_lesmodel(ctx, model, cm) &
+                BIND(C, name="mglet_gpu_set_lesmodel")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: model
+            REAL(c_double), VALUE :: cm
+        END FUNCTION mglet_gpu_set_lesmodel
+
+        INTEGER(c_int) FUNCTION mglet_gpu_set_body_force(ctx, fx, fy, fz, n) &
+                BIND(C, name="mglet_gpu_set_body_force")
+            IMPORT :: c_int, c_int64_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            REAL(c_double), INTENT(in) :: fx(*), fy(*), fz(*)
+            INTEGER(c_int64_t), VALUE :: n
+        END FUNCTION mglet_gpu_set_body_force
+
+        INTEGER(c_int) FUNCTION mglet_gpu_energy_gradient(ctx, nsteps, ncheck, dt, rk, energy) &
+                BIND(C, name="mglet_gpu_energy_gradient")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double, mglet_rk_scheme
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: nsteps, ncheck
+            REAL(c_double), VALUE :: dt
+            TYPE(mglet_rk_scheme), INTENT(in) :: rk
+            REAL(c_double), INTENT(out) :: energy
+        END FUNCTION mglet_gpu_energy_gradient
+
         INTEGER(c_int) FUNCTION mglet_gpu_par_ftoc_norm(ctx, ilevel, v1, v2, v3, sum) &
                 BIND(C, name="mglet_gpu_par_ftoc_norm")
             IMPORT :: c_int, c_int32_t, c_ptr, c_char
@@ -212,7 +238,8 @@ MODULE mglet_gpu_mod
         mglet_itinfo, gpu_init, gpu_finish, gpu_upload, gpu_download, &
         gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf, &
         gpu_upload_stencils, gpu_start_ghostcell, gpu_set_hierarchy, gpu_ftoc, gpu_ctof, &
-        gpu_bound_pressure, gpu_par_ftoc_norm
+        gpu_bound_pressure, gpu_par_ftoc_norm, gpu_set_lesmodel, gpu_set_body_force, &
+        gpu_energy_gradient
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -289,6 +316,31 @@ CONTAINS
         IF (mglet_gpu_ctof(gctx, INT(ilevel, c_int32_t), TRIM(ff)//C_NULL_CHAR, &
             TRIM(fc)//C_NULL_CHAR) /= 0) CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_ctof
+
+    ! init_lesmodel (src/flow/lesmodel_mod.F90:34-84): model 0 none,
+    ! 1 smagorinsky, 2 wale; cm < 0 takes the model's default constant
+    SUBROUTINE gpu_set_lesmodel(model, cm)
+        INTEGER, INTENT(in) :: model
+        REAL(c_double), INTENT(in) :: cm
+        IF (mglet_gpu_set_lesmodel(gctx, INT(model, c_int32_t), cm) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_set_lesmodel
+
+    ! A steady body force per unit mass (flat fields of idim3d reals)
+    SUBROUTINE gpu_set_body_force(fx, fy, fz)
+        REAL(c_double), INTENT(in) :: fx(:), fy(:), fz(:)
+        IF (mglet_gpu_set_body_force(gctx, fx, fy, fz, INT(SIZE(fx), c_int64_t)) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_set_body_force
+
+    ! The kinetic energy after nsteps steps and its gradient with respect to
+    ! the body force (device fields GFX, GFY, GFZ; gpu_download them)
+    SUBROUTINE gpu_energy_gradient(nsteps, ncheck, dt, energy)
+        INTEGER, INTENT(in) :: nsteps, ncheck
+        REAL(c_double), INTENT(in) :: dt
+        REAL(c_double), INTENT(out) :: energy
+        IF (mglet_gpu_energy_gradient(gctx, INT(nsteps, c_int32_t), INT(ncheck, c_int32_t), dt, &
+            grk, energy) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_energy_gradient
 
     ! Drop-in for par_ftoc_norm(ilevel, v1, v2, v3[, sum]) on the device copies
     SUBROUTINE gpu_par_ftoc_norm(ilevel, v1, v2, v3, sum)

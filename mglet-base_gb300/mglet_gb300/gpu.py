@@ -31,6 +31,7 @@ EXPORTS = [
     "mglet_gpu_set_hierarchy", "mglet_gpu_parent", "mglet_gpu_ftoc", "mglet_gpu_ftoc_multiple",
     "mglet_gpu_ctof", "mglet_gpu_bound_pressure", "mglet_gpu_par_ftoc_norm",
     "mglet_gpu_set_body_force", "mglet_gpu_adjoint_rk_stage", "mglet_gpu_energy_gradient",
+    "mglet_gpu_set_lesmodel",
 ]
 
 
@@ -84,6 +85,7 @@ def load(path=None):
     L.mglet_gpu_ctof.argtypes = [vp, C.c_int32, cp, cp]
     L.mglet_gpu_par_ftoc_norm.argtypes = [vp, C.c_int32, cp, cp, cp, C.c_int32]
     L.mglet_gpu_set_body_force.argtypes = [vp, vp, vp, vp, C.c_int64]
+    L.mglet_gpu_set_lesmodel.argtypes = [vp, C.c_int32, C.c_double]
     L.mglet_gpu_adjoint_rk_stage.argtypes = [vp, C.c_int32, C.c_double, vp]
     L.mglet_gpu_energy_gradient.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, vp,
                                             C.POINTER(C.c_double)]
@@ -239,6 +241,10 @@ class Solver:
 
     def ctof(self, ilevel, ff, fc):
         _check(load().mglet_gpu_ctof(self.h, ilevel, ff.encode(), fc.encode()))
+
+    def set_lesmodel(self, model, cm=-1.0):
+        """0 none, 1 smagorinsky, 2 wale; cm < 0 takes the model's default."""
+        _check(load().mglet_gpu_set_lesmodel(self.h, model, cm))
 
     def set_body_force(self, fx, fy, fz):
         a = [np.ascontiguousarray(x, dtype=np.float64) for x in (fx, fy, fz)]

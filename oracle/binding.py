@@ -63,6 +63,7 @@ def lib():
         _lib.oracle_ftoc.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p, C.c_char]
         _lib.oracle_ftoc_multiple.argtypes = [vp, C.c_int] + [C.c_char_p] * 6
         _lib.oracle_set_body_force.argtypes = [vp, vp, vp, vp, C.c_int64]
+        _lib.oracle_set_lesmodel.argtypes = [vp, C.c_int, C.c_double]
         _lib.oracle_par_ftoc_norm.argtypes = [vp, C.c_int] + [C.c_char_p] * 3 + [C.c_int]
         _lib.oracle_ctof.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p]
         _lib.oracle_bound_pressure.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
@@ -230,6 +231,10 @@ class Oracle:
         v = list(v) if v else [None] * 3
         s = list(s) + [None] * (3 - len(s))
         _check(lib().oracle_ftoc_multiple(self.h, ilevel, *[_b(n) for n in v + s]))
+
+    def set_lesmodel(self, model, cm=-1.0):
+        """0 none, 1 smagorinsky, 2 wale; cm < 0 takes the model's default."""
+        _check(lib().oracle_set_lesmodel(self.h, model, cm))
 
     def set_body_force(self, fx, fy, fz):
         a = [np.ascontiguousarray(x, dtype=np.float64) for x in (fx, fy, fz)]

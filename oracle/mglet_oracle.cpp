@@ -3447,6 +3447,7 @@ int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timep
         bound_flow(*c, c->F("U"), c->F("V"), c->F("W"), c->F("P"), l);
     }
     mgpoisl(*c, dtrk * dt, st);
+    lesmodel(*c);                                             // :125
     (void)ittot;
     if (gc) return setpointvalues(*c, irk == rk->nrk);   // :131-134
     return 0;
@@ -3575,6 +3576,17 @@ int oracle_ftoc(oracle_ctx* c, int ilevel, const char* ff, const char* fc, char 
     if (c->ibtype == 1 && flag == 'T')
         return fail(MGLET_ERR_UNSUPPORTED, "ftoc: the ghost-cell T restriction weighs by BT, which is not kept");
     ftoc_one(*c, ilevel, ff, fc, flag);
+    return 0;
+}
+
+int oracle_set_lesmodel(oracle_ctx* c, int model, double cm) {
+    if (!c || (model != 0 && model != 1 && model != 2))
+        return fail(MGLET_ERR_ARG, "set_lesmodel: model 0 (none), 1 (smagorinsky) or 2 (wale)");
+    c->ilesmodel = model;
+    c->cm = cm < 0.0 ? les_default_cm(model) : cm;
+    // init_lesmodel (lesmodel_mod.F90:63-80): G of the current field
+    if (model == 0) init_viscosity(*c);
+    else lesmodel(*c);
     return 0;
 }
 

@@ -1,0 +1,143 @@
+"""LES models in the oracle (no GPU): the effective viscosity G of
+lesmodel_mod.F90 (efvisc_gc :200-365 with smagorinsky :368-390 and wale
+:393-487) pinned against a vectorised numpy transcription on a random
+periodic field; G of a uniform flow is gmol; a stage with either model runs
+the LES cross term of tstle4_diff and stays divergence free."""
+import math
+
+import numpy as np
+import pytest
+
+from mglet_gb300 import abi, cases
+
+
+def _prm(**kw):
+    base = dict(gmol=1e-3, epcorr=1e-12, nouter=40, ninner=5, nouter_min=0)
+    base.update(kw)
+    return abi.make_flow_params(**base)
+
+
+def _grads(case, u, v, w, g):
+    """The nine velocity gradients of efvisc_gc at the interior cells of grid g."""
+    kk, jj, ii = case.kk, case.jj, case.ii
+    U = u.reshape(case.ngrid, ii, jj, kk)[g]
+    V = v.reshape(case.ngrid, ii, jj, kk)[g]
+    W = w.reshape(case.ngrid, ii, jj, kk)[g]
+    dx = case.dx.reshape(case.ngrid, ii)[g]
+    dy = case.dy.reshape(case.ngrid, jj)[g]
+    dz = case.dz.reshape(case.ngrid, kk)[g]
+    rddx = 1.0 / case.ddx.reshape(case.ngrid, ii)[g]
+    rddy = 1.0 / case.ddy.reshape(case.ngrid, jj)[g]
+    rddz = 1.0 / case.ddz.reshape(case.ngrid, kk)[g]
+    I = slice(2, ii - 2)
+    J = slice(2, jj - 2)
+    K = slice(2, kk - 2)
+
+    def s(a, di, dj, dk):   # a at (i + di, j + dj, k + dk) over the interior
+        return a[2 + di:ii - 2 + di, 2 + dj:jj - 2 + dj, 2 + dk:kk - 2 + dk]
+
+    X = lambda a: a[I][:, None, None]
+    Y = lambda a: a[J][None, :, None]
+    Z = lambda a: a[K][None, None, :]
+    Xm = lambda a: a[1:ii - 3][:, None, None]
+    Ym = lambda a: a[1:jj - 3][None, :, None]
+    Zm = lambda a: a[1:kk - 3][None, None, :]
+    dxf = 0.25 * Xm(dx) * X(rddx)
+    dyf = 0.25 * Ym(dy) * Y(rddy)
+    dzf = 0.25 * Zm(dz) * Z(rddz)
+    gr = [
+        (s(U, 0, 0, 0) - s(U, -1, 0, 0)) * X(rddx),
+        ((s(U, 0, 1, 0) - s(U, 0, -1, 0)) * dxf + (s(U, -1, 1, 0) - s(U, -1, -1, 0)) * (0.5 - dxf)) * Y(rddy),
+        ((s(U, 0, 0, 1) - s(U, 0, 0, -1)) * dxf + (s(U, -1, 0, 1) - s(U, -1, 0, -1)) * (0.5 - dxf)) * Z(rddz),
+        ((s(V, 1, 0, 0) - s(V, -1, 0, 0)) * dyf + (s(V, 1, -1, 0) - s(V, -1, -1, 0)) * (0.5 - dyf)) * X(rddx),
+        (s(V, 0, 0, 0) - s(V, 0, -1, 0)) * Y(rddy),
+        ((s(V, 0, 0, 1) - s(V, 0, 0, -1)) * dyf + (s(V, 0, -1, 1) - s(V, 0, -1, -1)) * (0.5 - dyf)) * Z(rddz),
+        ((s(W, 1, 0, 0) - s(W, -1, 0, 0)) * dzf + (s(W, 1, 0, -1) - s(W, -1, 0, -1)) * (0.5 - dzf)) * X(rddx),
+        ((s(W, 0, 1, 0) - s(W, 0, -1, 0)) * dzf + (s(W, 0, 1, -1) - s(W, 0, -1, -1)) * (0.5 - dzf)) * Y(rddy),
+        (s(W, 0, 0, 0) - s(W, 0, 0, -1)) * Z(rddz),
+    ]
+    vol = X(case.ddx.reshape(case.ngrid, ii)[g]) * Y(case.ddy.reshape(case.ngrid, jj)[g]) * \
+        Z(case.ddz.reshape(case.ngrid, kk)[g])
+    # cube_root is the C library's cbrt (simdfunctions_mod.F90:165-180);
+    # math.cbrt calls it, numpy's cbrt is its own
+    return gr, np.vectorize(math.cbrt)(vol)
+
+
+def _sabs(gr):
+    a = gr
+    return np.sqrt(a[0] * a[0] + a[4] * a[4] + a[8] * a[8] + 0.5 * ((a[3] + a[1]) * (a[3] + a[1]))
+                   + 0.5 * ((a[6] + a[2]) * (a[6] + a[2])) + 0.5 * ((a[7] + a[5]) * (a[7] + a[5])))
+
+
+def _wale(cm, gr):
+    dudx, dudy, dudz, dvdx, dvdy, dvdz, dwdx, dwdy, dwdz = gr
+    third = float(np.float32(1.0) / np.float32(3.0))
+    tr = (dudx * dudx + dudy * dvdx + dudz * dwdx + dvdx * dudy + dvdy * dvdy + dvdz * dwdy
+          + dwdx * dudz + dwdy * dvdz + dwdz * dwdz)
+    s00 = 0.5 * (dudx * dudx + dudy * dvdx + dudz * dwdx + dudx * dudx + dudy * dvdx + dudz * dwdx) - third * tr
+    s01 = 0.5 * (dudx * dudy + dudy * dvdy + dudz * dwdy + dvdx * dudx + dvdy * dvdx + dvdz * dwdx)
+    s02 = 0.5 * (dudx * dudz + dudy * dvdz + dudz * dwdz + dwdx * dudx + dwdy * dvdx + dwdz * dwdx)
+    s11 = 0.5 * (dvdx * dudy + dvdy * dvdy + dvdz * dwdy + dvdx * dudy + dvdy * dvdy + dvdz * dwdy) - third * tr
+    s12 = 0.5 * (dvdx * dudz + dvdy * dvdz + dvdz * dwdz + dwdx * dudy + dwdy * dvdy + dwdz * dwdy)
+    s22 = 0.5 * (dwdx * dudz + dwdy * dvdz + dwdz * dwdz + dwdx * dudz + dwdy * dvdz + dwdz * dwdz) - third * tr
+    sd = np.sqrt(s00 * s00 + 2 * (s01 * s01) + 2 * (s02 * s02) + s11 * s11 + 2 * (s12 * s12) + s22 * s22)
+    sa = _sabs(gr)
+    root = np.sqrt(sd)
+    tol = 1.0 / np.finfo(np.float64).max ** (1.0 / 6.0)
+    x = np.where(root == 0.0, 0.0, sa / np.where(root == 0.0, 1.0, root))
+    x2 = x * x
+    out = cm * cm * root / (x2 * x * x2 + 1.0)
+    return np.where(root < tol * sa, 0.0, out)
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_effective_viscosity_matches_transcription(oracle_lib, model):
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0))
+    gmol, rho = 1e-3, 1.0
+    o = oracle_lib.Oracle(case, _prm(gmol=gmol))
+    rng = np.random.default_rng(31)
+    f = {n: rng.standard_normal(case.idim3d) for n in "UVW"}
+    for n, a in f.items():
+        o.set(n, a)
+    o.connect(0, 2, "U", "V", "W", corners=True)
+    u, v, w = (o.get(n) for n in "UVW")
+    o.set_lesmodel(model)
+    G = o.get("G").reshape(case.ngrid, case.ii, case.jj, case.kk)
+    cm = float(np.float32(0.1)) if model == 1 else 0.5
+    for g in range(case.ngrid):
+        gr, delta = _grads(case, u, v, w, g)
+        dm = cm * cm * np.sqrt(2.0) * _sabs(gr) if model == 1 else _wale(cm, gr)
+        ref = rho * (delta * delta) * dm + gmol
+        assert np.array_equal(G[g, 2:-2, 2:-2, 2:-2], ref), g
+    # periodic: every ghost of G is a connected copy
+    assert np.all(G > 0)
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_uniform_flow_has_molecular_viscosity(oracle_lib, model):
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0))
+    o = oracle_lib.Oracle(case, _prm(gmol=2e-3))
+    for n, val in zip("UVW", (1.0, -0.5, 0.25)):
+        o.set(n, np.full(case.idim3d, val))
+    o.set_lesmodel(model)
+    assert np.all(o.get("G") == 2e-3)
+
+
+@pytest.mark.parametrize("model", [1, 2])
+def test_les_stage_is_divergence_free(oracle_lib, model):
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0))
+    o = oracle_lib.Oracle(case, _prm(gmol=1e-4))
+    u, v, w, p = cases.taylor_green(case)
+    u, v, w = cases.add_noise(case, (u, v, w), amplitude=5e-2, seed=3)
+    for n, a in zip("UVWP", (u, v, w, p)):
+        o.set(n, a)
+    o.connect(0, 2, "U", "V", "W", "P", corners=True)
+    o.set_lesmodel(model)
+    g0 = o.get("G").copy()
+    rk = oracle_lib.rk_scheme("williamson")
+    for irk in (1, 2, 3):
+        st = o.timeintegrate_flow(1, 1, 0.0, 1e-2, irk, rk)
+        assert st.maxrhs / st.prefak < 1e-12
+    assert o.itinfo(1e-2).divmax < 1e-10
+    assert not np.array_equal(o.get("G"), g0)       # lesmodel ran after the pressure solve
+    assert np.all(o.get("G")[case.interior(np.arange(case.idim3d)).ravel()] >= 1e-4)
