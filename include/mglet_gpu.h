@@ -285,8 +285,8 @@ int mglet_gpu_ctof(mglet_ctx* ctx, int32_t ilevel, const char* ff, const char* f
  * (the reference passes bp for the ghost-cell IB only). */
 int mglet_gpu_bound_pressure(mglet_ctx* ctx, int32_t ilevel, const char* dp, int32_t with_bp);
 /* The LES model of the stage (lesmodel_mod.F90:34-84, plain form): 0 none,
- * 1 smagorinsky, 2 wale (sigma is not built); cm < 0 takes the model's
- * default constant.  Computes G of the current velocity at once, as
+ * 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default
+ * constant.  Computes G of the current velocity at once, as
  * init_lesmodel does; the stage then updates G after the pressure solve and
  * tstle4_diff adds its LES cross term.  Model 0 restores G = gmol with the
  * ghost layers of init_lesmodel. */

@@ -1,13 +1,14 @@
 // les.cu -- the LES models of lesmodel_mod.F90 (plain FP64 form): the
 // effective viscosity G = rho delta^2 D_m + gmol of efvisc_gc (:200-365)
-// with the Smagorinsky (:368-390) or WALE (:393-487) operator D_m, one
-// thread per interior cell; the filter width delta = cbrt(cell volume) is
+// with the Smagorinsky (:368-390), WALE (:393-487) or sigma (:490-517)
+// operator D_m, one thread per interior cell; the filter width delta = cbrt(cell volume) is
 // taken once on the host with the C library's cbrt, the routine the
 // reference calls (simdfunctions_mod.F90:165-180), and kept as the field
 // LESD.  After efvisc: per level parent, bound and connect of G, setginbody
 // (ghost-cell IB only; with BP = 1 it leaves G unchanged) and the corner
 // connect tstle4 reads (lesmodel_gc :108-197).  Built without FMA
-// contraction, so that G matches the CPU restatement bit for bit.
+// contraction, so that G of Smagorinsky and WALE matches the CPU
+// restatement bit for bit (sigma to the ulps of CUDA's pow, acos, cos).
 
 #include <algorithm>
 #include <cmath>
@@ -28,6 +29,7 @@ struct LesArgs {
     const double *dx, *dy, *dz, *ddx, *ddy, *ddz, *rddx, *rddy, *rddz;
     double gmol, rho, cm, tol;
     double cpo6, cpo11, cpo12;   // gradp2 (wernerwengle_mod.F90:36-61)
+    double pi;                   // 4 atan(1), taken on the host
     int model;
 };
 
@@ -58,6 +60,49 @@ __device__ double wale(double cm, double tol, const double* gr) {
     const double x = root == 0.0 ? 0.0 : sa / root;
     const double x2 = x * x, x3 = x2 * x;
     return cm * cm * root / (x3 * x2 + 1.0);
+}
+
+// sigma (lesmodel_mod.F90:490-517) with the tensor products of
+// tensormath_mod.F90 and the analytic eigenvalues of eig_b (:221-268); pow,
+// acos and cos are CUDA's, within a few ulp of the C library's the
+// reference calls
+__device__ double sigma(double cm, double pi, const double* gr) {
+    double g[3][3];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) g[c][r] = gr[3 * c + r];
+    double G[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double a = 0.0;
+            for (int k = 0; k < 3; ++k) a = a + g[k][i] * g[k][j];
+            G[i][j] = a;
+        }
+#define AT(r, c) G[(c) - 1][(r) - 1]
+    const double q11 = AT(1, 1) * AT(1, 1) + AT(2, 1) * AT(1, 2) + AT(3, 1) * AT(1, 3);
+    const double q22 = AT(1, 2) * AT(2, 1) + AT(2, 2) * AT(2, 2) + AT(3, 2) * AT(2, 3);
+    const double q33 = AT(1, 3) * AT(3, 1) + AT(2, 3) * AT(3, 2) + AT(3, 3) * AT(3, 3);
+    const double i1 = AT(1, 1) + AT(2, 2) + AT(3, 3);
+    const double i2 = 0.5 * (i1 * i1 - (q11 + q22 + q33));
+    const double i3 = AT(1, 1) * (AT(2, 2) * AT(3, 3) - AT(3, 2) * AT(2, 3)) -
+                      AT(2, 1) * (AT(1, 2) * AT(3, 3) - AT(3, 2) * AT(1, 3)) +
+                      AT(3, 1) * (AT(1, 2) * AT(2, 3) - AT(2, 2) * AT(1, 3));
+#undef AT
+    double a1 = i1 * i1 / 9.0 - i2 / 3.0;
+    const double a2 = i1 * i1 * i1 / 27.0 - (i1 * i2) / 6.0 + i3 / 2.0;
+    a1 = a1 < 0.0 ? 0.0 : a1;
+    const double den = pow(a1, 3.0 / 2.0);
+    double arg = den == 0.0 ? 0.0 : a2 / den;
+    arg = arg > 1.0 ? 1.0 : (arg < -1.0 ? -1.0 : arg);
+    const double a3 = (1.0 / 3.0) * acos(arg);
+    double e1 = i1 / 3.0 + 2.0 * sqrt(a1) * cos(a3);
+    double e2 = i1 / 3.0 - 2.0 * sqrt(a1) * cos(pi / 3.0 + a3);
+    double e3 = i1 / 3.0 - 2.0 * sqrt(a1) * cos(pi / 3.0 - a3);
+    e1 = e1 < 0.0 ? 0.0 : e1;
+    e2 = e2 < 0.0 ? 0.0 : e2;
+    e3 = e3 < 0.0 ? 0.0 : e3;
+    const double s1 = sqrt(e1), s2 = sqrt(e2), s3 = sqrt(e3);
+    const double num = s3 * (s1 - s2) * (s2 - s3), d1 = s1 * s1;
+    return cm * cm * (d1 == 0.0 ? 0.0 : num / d1);
 }
 
 __device__ __forceinline__ double gradp2(const LesArgs& A, double uquer, double dds) {
@@ -111,7 +156,8 @@ __global__ void k_efvisc(LesArgs A) {
         if (ntop == 5 && k == kk - 2) { gr[2] = -gradp2(A, um, ddz[k]); gr[5] = -gradp2(A, vm, ddz[k]); }
     }
 #undef F
-    const double dm = A.model == 1 ? A.cm * A.cm * sqrt(2.0) * sabs(gr) : wale(A.cm, A.tol, gr);
+    const double dm = A.model == 1 ? A.cm * A.cm * sqrt(2.0) * sabs(gr)
+                                   : (A.model == 2 ? wale(A.cm, A.tol, gr) : sigma(A.cm, A.pi, gr));
     A.g[o + IX(k, j, i)] = A.rho * (delta * delta) * dm + A.gmol;
 }
 
@@ -158,6 +204,7 @@ int lesmodel(Ctx* c) {
     A.cm = c->cm;
     A.model = c->ilesmodel;
     A.tol = 1.0 / std::pow(std::numeric_limits<double>::max(), 1.0 / 6.0);
+    A.pi = 4.0 * std::atan(1.0);
     // init_wernerwengle (wernerwengle_mod.F90:13-28)
     const double cwa = 8.3, cwb = 1.0 / 7.0, cpo1 = 1.0 - cwb, cpo2 = 1.0 + cwb;
     A.cpo6 = 0.5 * A.gmol / A.rho * std::pow(cwa, 2.0 / cpo1);
@@ -187,8 +234,8 @@ int lesmodel(Ctx* c) {
 // 0 none, 1 smagorinsky, 2 wale; cm < 0 takes the model's default (the
 // default-kind literals 0.1 and 0.5)
 int set_lesmodel(Ctx* c, int model, double cm) {
-    if (model != 0 && model != 1 && model != 2) {
-        set_error("set_lesmodel: model 0 (none), 1 (smagorinsky) or 2 (wale)");
+    if (model != 0 && model != 1 && model != 2 && model != 5) {
+        set_error("set_lesmodel: model 0 (none), 1 (smagorinsky), 2 (wale) or 5 (sigma)");
         return MGLET_ERR_ARG;
     }
     if (model != 0 && c->prm.form != MGLET_FORM_PLAIN) {
@@ -196,7 +243,7 @@ int set_lesmodel(Ctx* c, int model, double cm) {
         return MGLET_ERR_UNSUPPORTED;
     }
     c->ilesmodel = model;
-    c->cm = cm < 0.0 ? (model == 1 ? (double)0.1f : 0.5) : cm;
+    c->cm = cm < 0.0 ? (model == 1 ? (double)0.1f : (model == 2 ? 0.5 : (double)1.35f)) : cm;
     if (model == 0) return init_viscosity(c);
     if (!c->f3.count("LESD")) {
         if (int rc = alloc_field3(c, "LESD")) return rc;

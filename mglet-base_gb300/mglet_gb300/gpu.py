@@ -243,7 +243,7 @@ class Solver:
         _check(load().mglet_gpu_ctof(self.h, ilevel, ff.encode(), fc.encode()))
 
     def set_lesmodel(self, model, cm=-1.0):
-        """0 none, 1 smagorinsky, 2 wale; cm < 0 takes the model's default."""
+        """0 none, 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default."""
         _check(load().mglet_gpu_set_lesmodel(self.h, model, cm))
 
     def set_body_force(self, fx, fy, fz):

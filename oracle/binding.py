@@ -233,7 +233,7 @@ class Oracle:
         _check(lib().oracle_ftoc_multiple(self.h, ilevel, *[_b(n) for n in v + s]))
 
     def set_lesmodel(self, model, cm=-1.0):
-        """0 none, 1 smagorinsky, 2 wale; cm < 0 takes the model's default."""
+        """0 none, 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default."""
         _check(lib().oracle_set_lesmodel(self.h, model, cm))
 
     def set_body_force(self, fx, fy, fz):

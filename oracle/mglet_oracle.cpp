@@ -1808,6 +1808,49 @@ double les_wale(double cm, double tol, const double* gr) {
     return cm * cm * root / (x3 * x2 + 1.0);
 }
 
+// lesmodel_mod.F90:490-517 sigma with tensormath_mod.F90 (t, multiply, sqr,
+// trace, det) and eig_b :221-268 (the analytic eigenvalues of Hasan et al.):
+// the singular values of the velocity gradient; the C library's pow, acos
+// and cos as the reference calls them
+double les_sigma(double cm, const double* gr) {
+    double g[3][3];   // g[c][r] = gij%g(r+1, c+1): columns dudx..dudz, dvdx.., dwdx..
+    for (int cc = 0; cc < 3; ++cc)
+        for (int r = 0; r < 3; ++r) g[cc][r] = gr[3 * cc + r];
+    // G = gij^T gij: G(j,i) = sum_k gij(i,k) gij(j,k), from 0 in k order
+    double G[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            double a = 0.0;
+            for (int k = 0; k < 3; ++k) a = a + g[k][i] * g[k][j];
+            G[i][j] = a;   // G[i][j] = G%g(j+1, i+1)
+        }
+    auto at = [&](int r, int cc) { return G[cc - 1][r - 1]; };   // G%g(r, c)
+    double sq[3][3];
+    for (int i = 1; i <= 3; ++i)
+        for (int j = 1; j <= 3; ++j)
+            sq[i - 1][j - 1] = at(1, i) * at(j, 1) + at(2, i) * at(j, 2) + at(3, i) * at(j, 3);
+    const double i1 = at(1, 1) + at(2, 2) + at(3, 3);
+    const double i2 = 0.5 * (i1 * i1 - (sq[0][0] + sq[1][1] + sq[2][2]));
+    const double i3 = at(1, 1) * (at(2, 2) * at(3, 3) - at(3, 2) * at(2, 3)) -
+                      at(2, 1) * (at(1, 2) * at(3, 3) - at(3, 2) * at(1, 3)) +
+                      at(3, 1) * (at(1, 2) * at(2, 3) - at(2, 2) * at(1, 3));
+    double a1 = i1 * i1 / 9.0 - i2 / 3.0;
+    const double a2 = i1 * i1 * i1 / 27.0 - (i1 * i2) / 6.0 + i3 / 2.0;
+    a1 = std::max(a1, 0.0);
+    const double den = std::pow(a1, 3.0 / 2.0);
+    double arg = den == 0.0 ? 0.0 : a2 / den;
+    arg = std::max(std::min(arg, 1.0), -1.0);
+    const double a3 = (1.0 / 3.0) * std::acos(arg);
+    const double pi = 4.0 * std::atan(1.0);
+    double e1 = i1 / 3.0 + 2.0 * std::sqrt(a1) * std::cos(a3);
+    double e2 = i1 / 3.0 - 2.0 * std::sqrt(a1) * std::cos(pi / 3.0 + a3);
+    double e3 = i1 / 3.0 - 2.0 * std::sqrt(a1) * std::cos(pi / 3.0 - a3);
+    e1 = std::max(e1, 0.0); e2 = std::max(e2, 0.0); e3 = std::max(e3, 0.0);
+    const double s1 = std::sqrt(e1), s2 = std::sqrt(e2), s3 = std::sqrt(e3);
+    const double num = s3 * (s1 - s2) * (s2 - s3), d1 = s1 * s1;
+    return cm * cm * (d1 == 0.0 ? 0.0 : num / d1);
+}
+
 // the Werner-Wengle gradient dds/2 from the wall (wernerwengle_mod.F90:36-61)
 double gradp2(const WernerWengle& q, double cpo11, double cpo12, double uquer, double dds) {
     const double uquern = std::fabs(uquer);
@@ -1877,7 +1920,8 @@ void efvisc_grid(Ctx& c, int g) {
                 if (nlft == 5 && j == jj - 2) { gr[1] = -gradp2(q, cpo11, cpo12, um, ddy[j]); gr[7] = -gradp2(q, cpo11, cpo12, wm, ddy[j]); }
                 if (nbot == 5 && k == 3) { gr[2] = gradp2(q, cpo11, cpo12, um, ddz[k]); gr[5] = gradp2(q, cpo11, cpo12, vm, ddz[k]); }
                 if (ntop == 5 && k == kk - 2) { gr[2] = -gradp2(q, cpo11, cpo12, um, ddz[k]); gr[5] = -gradp2(q, cpo11, cpo12, vm, ddz[k]); }
-                const double dm = c.ilesmodel == 1 ? les_smagorinsky(c.cm, gr) : les_wale(c.cm, tol, gr);
+                const double dm = c.ilesmodel == 1 ? les_smagorinsky(c.cm, gr)
+                                   : (c.ilesmodel == 2 ? les_wale(c.cm, tol, gr) : les_sigma(c.cm, gr));
                 A(gv, k, j, i) = rho * (delta * delta) * dm + gmol;
             }
 #undef A
@@ -3580,8 +3624,8 @@ int oracle_ftoc(oracle_ctx* c, int ilevel, const char* ff, const char* fc, char 
 }
 
 int oracle_set_lesmodel(oracle_ctx* c, int model, double cm) {
-    if (!c || (model != 0 && model != 1 && model != 2))
-        return fail(MGLET_ERR_ARG, "set_lesmodel: model 0 (none), 1 (smagorinsky) or 2 (wale)");
+    if (!c || (model != 0 && model != 1 && model != 2 && model != 5))
+        return fail(MGLET_ERR_ARG, "set_lesmodel: model 0 (none), 1 (smagorinsky), 2 (wale) or 5 (sigma)");
     c->ilesmodel = model;
     c->cm = cm < 0.0 ? les_default_cm(model) : cm;
     // init_lesmodel (lesmodel_mod.F90:63-80): G of the current field
