@@ -291,6 +291,20 @@ int mglet_gpu_bound_pressure(mglet_ctx* ctx, int32_t ilevel, const char* dp, int
  * tstle4_diff adds its LES cross term.  Model 0 restores G = gmol with the
  * ghost layers of init_lesmodel. */
 int mglet_gpu_set_lesmodel(mglet_ctx* ctx, int32_t model, double cm);
+/* Passive scalars (src/scalar, plain form, no ghost-cell IB): nsca (0..9)
+ * scalars as the device fields T1..Tn with their RK increments DT1..DTn;
+ * prmol the molecular Prandtl numbers, kayscrawford the switch of the
+ * turbulent Prandtl number fit (scacore_mod.F90:232-262, else prturb),
+ * source (may be NULL) a constant source per scalar.  The scalar wall and
+ * in/outflow conditions (SWA, SIO) are not built: non-CON, non-PAR faces
+ * carry no scalar flux. */
+int mglet_gpu_set_scalars(mglet_ctx* ctx, int32_t nsca, const double* prmol,
+                          const int32_t* kayscrawford, const double* source, double prturb);
+/* timeintegrate_scalar (src/scalar/timeintegrate_scalar_mod.F90:17-108): one
+ * RK stage of every scalar on the current velocity; the reference calls it
+ * before timeintegrate_flow in each stage (timeloop_mod.F90:233-235). */
+int mglet_gpu_timeintegrate_scalar(mglet_ctx* ctx, double dt, int32_t irk,
+                                   const mglet_rk_scheme* rk);
 /* ---- Body force and the discrete adjoint (no counterpart in the reference) --
  * A steady body force per unit mass, added to uo, vo, wo in tstle4 after
  * gradp over the same points (plain form); n must equal idim3d. */

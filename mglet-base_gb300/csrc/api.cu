@@ -278,6 +278,7 @@ std::string plan_key(int ilevel, int layers, int slots, bool corners, bool norma
 }  // namespace
 
 int alloc_field3(Ctx* c, const char* name) { return alloc3(c, name); }
+int fill_field(Ctx* c, double* a, double v) { return fill(c, a, v); }
 
 int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,
             double* s2, double* s3, bool corners, bool normal, int forward) {
@@ -946,6 +947,24 @@ int mglet_gpu_set_body_force(mglet_ctx* c, const double* fx, const double* fy, c
         MG_CUDA(copy_on(c->stream, c->F(nm[q]), h[q], (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
     }
     c->bodyforce = true;
+    return 0;
+}
+
+int mglet_gpu_set_scalars(mglet_ctx* c, int32_t nsca, const double* prmol, const int32_t* kayscrawford,
+                          const double* source, double prturb) {
+    if (!c) return fail(MGLET_ERR_ARG, "set_scalars: null context");
+    cudaSetDevice(c->device);
+    if (int rc = set_scalars(c, nsca, prmol, kayscrawford, source, prturb)) return rc;
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int mglet_gpu_timeintegrate_scalar(mglet_ctx* c, double dt, int32_t irk, const mglet_rk_scheme* rk) {
+    if (!c || !rk) return fail(MGLET_ERR_ARG, "timeintegrate_scalar: null argument");
+    cudaSetDevice(c->device);
+    if (int rc = hierarchy_ready(c)) return rc;
+    if (int rc = timeintegrate_scalar(c, dt, irk, rk)) return rc;
+    MG_CUDA(cudaStreamSynchronize(c->stream));
     return 0;
 }
 

@@ -148,7 +148,16 @@ struct Ctx {
     bool gc_saved[2] = {false, false};
     bool bodyforce = false;      // FBX, FBY, FBZ added in tstle4 (plain form)
     bool g_user = false;         // G set by the caller: set_hierarchy keeps it
-    int ilesmodel = 0;           // 0 none, 1 smagorinsky, 2 wale
+    // passive scalars T1..Tn (scacore_mod.F90): molecular Prandtl number,
+    // Kays/Crawford switch, constant source
+    struct ScalarDef {
+        std::string name;
+        double prmol = 1.0, source = 0.0;
+        int kayscrawford = 0;
+    };
+    std::vector<ScalarDef> sca;
+    double prturb = 1.0;
+    int ilesmodel = 0;           // 0 none, 1 smagorinsky, 2 wale, 5 sigma
     double cm = 0.0;             // the LES model constant
     void* d_sptab = nullptr;     // device table of the 12 spacing arrays (adjoint)
     std::vector<GcHostList> gch;
@@ -257,6 +266,11 @@ int init_viscosity(Ctx* c);                  // G of init_lesmodel, model "none"
 int launch_bound_g(Ctx* c, int ilevel);      // the bound of G (lesmodel_mod.F90:573-764)
 int lesmodel(Ctx* c);                        // G from the LES model (les.cu)
 int set_lesmodel(Ctx* c, int model, double cm);
+int fill_field(Ctx* c, double* a, double v);   // a[0..idim3d) = v (api.cu)
+// scalar transport (scalar.cu)
+int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawford, const double* source,
+                double prturb);
+int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk);
 int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos);
 double* field_buffer(Ctx* c, const std::string& name);   // boundary buffers of a field
 int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w);

@@ -1,0 +1,247 @@
+// scalar.cu -- transport of passive scalars (src/scalar/
+// timeintegrate_scalar_mod.F90:17-545, plain FP64 form, no IB): per scalar
+// and RK stage the face fluxes of tstsca4 (central convection, diffusion
+// with the LES diffusivity and the turbulent Prandtl number of
+// scacore_mod.F90:232-262, upwind at PAR faces), the parent's fluxes on PAR
+// faces split by open area (bound_scalar_mod.F90:103-123 and twins), the
+// flux balance with a constant source, the RK update, the restriction of T
+// to the coarser levels and the corner connect.  One thread per point; the
+// thread of a point computes its three face fluxes, so the PAR correction
+// of a face follows its central flux as in the reference's loop order.
+// Built without FMA contraction (bit-exact with the CPU restatement; the
+// Kays/Crawford fit takes CUDA's exp).
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace mg {
+namespace {
+
+#define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
+
+struct ScaArgs {
+    const DevGrid* grids;
+    const double *t, *u, *v, *w, *g, *bt;
+    double *qtu, *qtv, *qtw;
+    const double *ddx, *ddy, *ddz, *rdx, *rdy, *rdz;
+    double gmol, rho, prmol, prturb;
+    int kayscrawford, les;
+};
+
+__device__ __forceinline__ double prt(const ScaArgs& A, double gtgmol) {
+    if (A.kayscrawford == 0) return A.prturb;
+    if (gtgmol > 0.0)
+        return (double)0.5882f + (double)0.228f * gtgmol -
+               (double)0.0441f * (gtgmol * gtgmol) * (1.0 - exp((double)(-5.165f) / gtgmol));
+    return A.prmol;
+}
+
+__device__ __forceinline__ double gsca(const ScaArgs& A, double g0, double g1) {
+    const double gscamol = A.gmol / A.rho / A.prmol;
+    if (!A.les) return gscamol;
+    const double gtgmolp = (g0 - A.gmol) / A.gmol, gtgmoln = (g1 - A.gmol) / A.gmol;
+    const double gs = gscamol + (g1 + g0 - 2.0 * A.gmol) / A.rho / (prt(A, gtgmoln) + prt(A, gtgmolp));
+    return gscamol < gs ? gs : gscamol;
+}
+
+__global__ void k_tstsca4(ScaArgs A) {
+    const DevGrid G = A.grids[blockIdx.y];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int tt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tt >= kk * jj * ii) return;
+    const int k = tt % kk + 1, j = (tt / kk) % jj + 1, i = tt / (kk * jj) + 1;
+    const long long o = G.ip3;
+    const double *t = A.t + o, *u = A.u + o, *v = A.v + o, *w = A.w + o, *g = A.g + o, *bt = A.bt + o;
+    const double *ddx = A.ddx + G.ipx - 1, *ddy = A.ddy + G.ipy - 1, *ddz = A.ddz + G.ipz - 1;
+    const double *rdx = A.rdx + G.ipx - 1, *rdy = A.rdy + G.ipy - 1, *rdz = A.rdz + G.ipz - 1;
+    const int nfro = G.bc[0], nbac = G.bc[1], nrgt = G.bc[2], nlft = G.bc[3], nbot = G.bc[4], ntop = G.bc[5];
+    const int nfu = nfro == 7, nbu = nbac == 7, nrv = nrgt == 7, nlv = nlft == 7, nbw = nbot == 7, ntw = ntop == 7;
+    const bool iin = i >= 3 && i <= ii - 2, jin = j >= 3 && j <= jj - 2, kin = k >= 3 && k <= kk - 2;
+    const long long c = IX(k, j, i);
+    double qu = 0.0, qv = 0.0, qw = 0.0;
+    if (i >= 3 - nfu && i <= ii - 3 + nbu && jin && kin) {
+        const double gs = gsca(A, g[c], g[IX(k, j, i + 1)]);
+        const double adv = (ddy[j] * ddz[k]) * u[c] * 0.5 * (t[c] + t[IX(k, j, i + 1)]);
+        const double area = bt[c] * bt[IX(k, j, i + 1)] * (ddy[j] * ddz[k]);
+        const double diff = -gs * rdx[i] * (t[IX(k, j, i + 1)] - t[c]) * area;
+        qu = adv + diff;
+        if (nfro == 8 && i == 3)
+            qu = qu + (ddy[j] * ddz[k]) * (u[c] - fabs(u[c])) * 0.5 * 0.5 * (-t[c] + t[IX(k, j, i + 1)]);
+        if (nbac == 8 && i == ii - 3)
+            qu = qu + (ddy[j] * ddz[k]) * (u[c] + fabs(u[c])) * 0.5 * 0.5 * (t[c] - t[IX(k, j, i + 1)]);
+    }
+    if (iin && j >= 3 - nrv && j <= jj - 3 + nlv && kin) {
+        const double gs = gsca(A, g[c], g[IX(k, j + 1, i)]);
+        const double adv = (ddx[i] * ddz[k]) * v[c] * 0.5 * (t[c] + t[IX(k, j + 1, i)]);
+        const double area = bt[c] * bt[IX(k, j + 1, i)] * (ddx[i] * ddz[k]);
+        const double diff = -gs * rdy[j] * (t[IX(k, j + 1, i)] - t[c]) * area;
+        qv = adv + diff;
+        if (nrgt == 8 && j == 3)
+            qv = qv + (ddx[i] * ddz[k]) * (v[c] - fabs(v[c])) * 0.5 * 0.5 * (-t[c] + t[IX(k, j + 1, i)]);
+        if (nlft == 8 && j == jj - 3)
+            qv = qv + (ddx[i] * ddz[k]) * (v[c] + fabs(v[c])) * 0.5 * 0.5 * (t[c] - t[IX(k, j + 1, i)]);
+    }
+    if (iin && jin && k >= 3 - nbw && k <= kk - 3 + ntw) {
+        const double gs = gsca(A, g[c], g[IX(k + 1, j, i)]);
+        const double adv = (ddx[i] * ddy[j]) * w[c] * 0.5 * (t[c] + t[IX(k + 1, j, i)]);
+        const double area = bt[c] * bt[IX(k + 1, j, i)] * (ddx[i] * ddy[j]);
+        const double diff = -gs * rdz[k] * (t[IX(k + 1, j, i)] - t[c]) * area;
+        qw = adv + diff;
+        if (nbot == 8 && k == 3)
+            qw = qw + (ddx[i] * ddy[j]) * (w[c] - fabs(w[c])) * 0.5 * 0.5 * (-t[c] + t[IX(k + 1, j, i)]);
+        if (ntop == 8 && k == kk - 3)
+            qw = qw + (ddx[i] * ddy[j]) * (w[c] + fabs(w[c])) * 0.5 * 0.5 * (t[c] - t[IX(k + 1, j, i)]);
+    }
+    A.qtu[o + c] = qu;
+    A.qtv[o + c] = qv;
+    A.qtw[o + c] = qw;
+}
+
+// the PAR flux of face f (1..6) of the grids of ilevel: one thread per 2x2
+// block of fine faces
+__global__ void k_scaflux_par(const DevGrid* __restrict__ grids, const BFace* __restrict__ bface, int f,
+                              int ilevel, double* Q, const double* __restrict__ buf, const double* __restrict__ BT) {
+    const DevGrid G = grids[blockIdx.y];
+    if (G.level != ilevel || G.bc[f - 1] != MGLET_BC_PAR) return;
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int d = (f - 1) / 2;
+    const int na = d == 0 ? jj : ii, nq = d == 2 ? jj : kk;
+    const int nba = (na - 4) / 2, nbq = (nq - 4) / 2;
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nba * nbq) return;
+    const int a = 3 + 2 * (b / nbq), q = 3 + 2 * (b % nbq);
+    const int n = d == 0 ? ii : (d == 1 ? jj : kk);
+    const int p3 = f % 2 == 1 ? 3 : n - 2, ps = f % 2 == 1 ? 2 : n - 2;
+    auto at = [&](int p, int aa, int qq) -> long long {
+        if (d == 0) return IX(qq, aa, p);
+        if (d == 1) return IX(qq, p, aa);
+        return IX(p, qq, aa);
+    };
+    const double* bt = BT + G.ip3;
+    double* qf = Q + G.ip3;
+    const double a1 = bt[at(p3, a, q)], a2 = bt[at(p3, a, q + 1)];
+    const double a3 = bt[at(p3, a + 1, q)], a4 = bt[at(p3, a + 1, q + 1)];
+    const double tot = a1 + a2 + a3 + a4;
+    const double qtot = buf[bface[6 * blockIdx.y + f - 1].off + (q - 1) + (long long)(a - 1) * nq];
+    qf[at(ps, a, q)] = (tot == 0.0 ? 0.0 : a1 / tot) * qtot;
+    qf[at(ps, a, q + 1)] = (tot == 0.0 ? 0.0 : a2 / tot) * qtot;
+    qf[at(ps, a + 1, q)] = (tot == 0.0 ? 0.0 : a3 / tot) * qtot;
+    qf[at(ps, a + 1, q + 1)] = (tot == 0.0 ? 0.0 : a4 / tot) * qtot;
+}
+
+// fluxbalance_grid (:520-545) and sourceterm_const (:590-607) over the box
+__global__ void k_fluxbalance(const DevGrid* __restrict__ grids, const double* __restrict__ QTU,
+                              const double* __restrict__ QTV, const double* __restrict__ QTW,
+                              double* __restrict__ QTT, const double* __restrict__ RDDX,
+                              const double* __restrict__ RDDY, const double* __restrict__ RDDZ,
+                              double source) {
+    const DevGrid G = grids[blockIdx.y];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int tt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tt >= kk * jj * ii) return;
+    const int k = tt % kk + 1, j = (tt / kk) % jj + 1, i = tt / (kk * jj) + 1;
+    const long long o = G.ip3;
+    double r = 0.0;
+    if (i >= 3 && i <= ii - 2 && j >= 3 && j <= jj - 2 && k >= 3 && k <= kk - 2) {
+        const double* qtu = QTU + o;
+        const double* qtv = QTV + o;
+        const double* qtw = QTW + o;
+        const double net = qtu[IX(k, j, i - 1)] - qtu[IX(k, j, i)] + qtv[IX(k, j - 1, i)] - qtv[IX(k, j, i)] +
+                           qtw[IX(k - 1, j, i)] - qtw[IX(k, j, i)];
+        r = RDDZ[G.ipz + k - 1] * RDDY[G.ipy + j - 1] * RDDX[G.ipx + i - 1] * net;
+        if (source != 0.0) r = r + source;
+    }
+    QTT[o + tt] = r;
+}
+
+#undef IX
+
+}  // namespace
+
+int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawford, const double* source,
+                double prturb) {
+    if (nsca < 0 || nsca > 9 || (nsca && (!prmol || !kayscrawford))) {
+        set_error("set_scalars: 0..9 scalars with prmol and kayscrawford");
+        return MGLET_ERR_ARG;
+    }
+    if (nsca && (c->prm.form != MGLET_FORM_PLAIN || c->ibtype == 1)) {
+        set_error("set_scalars: the plain form without the ghost-cell IB");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    c->sca.clear();
+    for (int l = 0; l < nsca; ++l) {
+        Ctx::ScalarDef sd;
+        sd.name = "T" + std::to_string(l + 1);
+        sd.prmol = prmol[l];
+        sd.kayscrawford = kayscrawford[l];
+        sd.source = source ? source[l] : 0.0;
+        for (const std::string& n : {sd.name, "D" + sd.name}) {
+            if (!c->f3.count(n))
+                if (int rc = alloc_field3(c, n.c_str())) return rc;
+            MG_CUDA(cudaMemsetAsync(c->F(n.c_str()), 0, (size_t)c->idim3d * sizeof(double), c->stream));
+        }
+        c->sca.push_back(sd);
+    }
+    c->prturb = prturb;
+    for (const char* n : {"QTU", "QTV", "QTW", "QTT", "BT"})
+        if (!c->f3.count(n))
+            if (int rc = alloc_field3(c, n)) return rc;
+    // blockbt: every cell open without the ghost-cell IB
+    return fill_field(c, c->F("BT"), 1.0);
+}
+
+int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) {
+    double frhs, fu, dtrk, dtrki;
+    if (int rc = rk_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki)) return rc;
+    ProfScope ps_(c, "scalar");
+    int m = 0;
+    for (const DevGrid& g : c->grids) m = std::max(m, g.kk * g.jj * g.ii);
+    const dim3 bg((m + 255) / 256, c->ngrid);
+    int mb = 0;
+    for (const DevGrid& g : c->grids)
+        mb = std::max(mb, std::max((g.jj - 4) * (g.kk - 4), std::max((g.ii - 4) * (g.kk - 4), (g.ii - 4) * (g.jj - 4))) / 4);
+    static const char* const qn[3] = {"QTU", "QTV", "QTW"};
+    static const char* const none[3] = {nullptr, nullptr, nullptr};
+    for (const Ctx::ScalarDef& sd : c->sca) {
+        double* T = c->F(sd.name.c_str());
+        double* DT = c->F(("D" + sd.name).c_str());
+        ScaArgs A;
+        A.grids = c->d_grids;
+        A.t = T; A.u = c->F("U"); A.v = c->F("V"); A.w = c->F("W"); A.g = c->F("G"); A.bt = c->F("BT");
+        A.qtu = c->F("QTU"); A.qtv = c->F("QTV"); A.qtw = c->F("QTW");
+        A.ddx = c->L("DDX"); A.ddy = c->L("DDY"); A.ddz = c->L("DDZ");
+        A.rdx = c->L("RDX"); A.rdy = c->L("RDY"); A.rdz = c->L("RDZ");
+        A.gmol = c->prm.gmol; A.rho = c->prm.rho; A.prmol = sd.prmol; A.prturb = c->prturb;
+        A.kayscrawford = sd.kayscrawford; A.les = c->ilesmodel != 0;
+        k_tstsca4<<<bg, 256, 0, c->stream>>>(A);
+        MG_LAUNCHED(c);
+        for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+            if (c->minlevel == c->maxlevel) break;
+            if (int rc = launch_parent(c, l, qn, none, false)) return rc;
+            for (int f = 1; f <= 6; ++f) {
+                double* Q = c->F(qn[(f - 1) / 2]);
+                const double* buf = field_buffer(c, qn[(f - 1) / 2]);
+                if (!buf) {
+                    set_error("timeintegrate_scalar: buffer allocation");
+                    return MGLET_ERR_CUDA;
+                }
+                k_scaflux_par<<<dim3((mb + 127) / 128, c->ngrid), 128, 0, c->stream>>>(
+                    c->d_grids, c->d_bface, f, l, Q, buf, c->F("BT"));
+                MG_LAUNCHED(c);
+            }
+        }
+        k_fluxbalance<<<bg, 256, 0, c->stream>>>(c->d_grids, c->F("QTU"), c->F("QTV"), c->F("QTW"), c->F("QTT"),
+                                                 c->L("RDDX"), c->L("RDDY"), c->L("RDDZ"), sd.source);
+        MG_LAUNCHED(c);
+        if (int rc = launch_rkstep(c, T, DT, c->F("QTT"), frhs, dt * fu)) return rc;
+        for (int l = c->maxlevel; l > c->minlevel; --l)
+            if (int rc = launch_ftoc(c, l, T, T, 'T')) return rc;
+        if (int rc = connect(c, 0, 2, nullptr, nullptr, nullptr, T, nullptr, nullptr, true, false, 0)) return rc;
+    }
+    return 0;
+}
+
+}  // namespace mg

@@ -181,6 +181,25 @@ MODULE mglet_gpu_mod
             CHARACTER(kind=c_char), INTENT(in) :: ff(*), fc(*)
         END FUNCTION mglet_gpu_ctof
 
+        INTEGER(c_int) FUNCTION mglet_gpu_set_scalars(ctx, nsca, prmol, kayscrawford, source, &
+                prturb) BIND(C, name="mglet_gpu_set_scalars")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: nsca
+            REAL(c_double), INTENT(in) :: prmol(*), source(*)
+            INTEGER(c_int32_t), INTENT(in) :: kayscrawford(*)
+            REAL(c_double), VALUE :: prturb
+        END FUNCTION mglet_gpu_set_scalars
+
+        INTEGER(c_int) FUNCTION mglet_gpu_timeintegrate_scalar(ctx, dt, irk, rk) &
+                BIND(C, name="mglet_gpu_timeintegrate_scalar")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double, mglet_rk_scheme
+            TYPE(c_ptr), VALUE :: ctx
+            REAL(c_double), VALUE :: dt
+            INTEGER(c_int32_t), VALUE :: irk
+            TYPE(mglet_rk_scheme), INTENT(in) :: rk
+        END FUNCTION mglet_gpu_timeintegrate_scalar
+
         INTEGER(c_int) FUNCTION mglet_gpu_set_lesmodel(ctx, model, cm) &
                 BIND(C, name="mglet_gpu_set_lesmodel")
             IMPORT :: c_int, c_int32_t, c_ptr, c_double
@@ -239,7 +258,7 @@ MODULE mglet_gpu_mod
         gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf, &
         gpu_upload_stencils, gpu_start_ghostcell, gpu_set_hierarchy, gpu_ftoc, gpu_ctof, &
         gpu_bound_pressure, gpu_par_ftoc_norm, gpu_set_lesmodel, gpu_set_body_force, &
-        gpu_energy_gradient
+        gpu_energy_gradient, gpu_set_scalars, gpu_timeintegrate_scalar
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -316,6 +335,22 @@ CONTAINS
         IF (mglet_gpu_ctof(gctx, INT(ilevel, c_int32_t), TRIM(ff)//C_NULL_CHAR, &
             TRIM(fc)//C_NULL_CHAR) /= 0) CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_ctof
+
+    ! The scalars of scacore_mod (device fields T1..Tn)
+    SUBROUTINE gpu_set_scalars(prmol, kayscrawford, source, prturb)
+        REAL(c_double), INTENT(in) :: prmol(:), source(:), prturb
+        INTEGER(c_int32_t), INTENT(in) :: kayscrawford(:)
+        IF (mglet_gpu_set_scalars(gctx, INT(SIZE(prmol), c_int32_t), prmol, kayscrawford, source, &
+            prturb) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_set_scalars
+
+    ! Drop-in for timeintegrate_scalar (src/scalar/timeintegrate_scalar_mod.F90:17)
+    SUBROUTINE gpu_timeintegrate_scalar(dt, irk)
+        REAL(c_double), INTENT(in) :: dt
+        INTEGER, INTENT(in) :: irk
+        IF (mglet_gpu_timeintegrate_scalar(gctx, dt, INT(irk, c_int32_t), grk) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_timeintegrate_scalar
 
     ! init_lesmodel (src/flow/lesmodel_mod.F90:34-84): model 0 none,
     ! 1 smagorinsky, 2 wale; cm < 0 takes the model's default constant

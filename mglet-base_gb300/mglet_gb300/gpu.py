@@ -31,7 +31,7 @@ EXPORTS = [
     "mglet_gpu_set_hierarchy", "mglet_gpu_parent", "mglet_gpu_ftoc", "mglet_gpu_ftoc_multiple",
     "mglet_gpu_ctof", "mglet_gpu_bound_pressure", "mglet_gpu_par_ftoc_norm",
     "mglet_gpu_set_body_force", "mglet_gpu_adjoint_rk_stage", "mglet_gpu_energy_gradient",
-    "mglet_gpu_set_lesmodel",
+    "mglet_gpu_set_lesmodel", "mglet_gpu_set_scalars", "mglet_gpu_timeintegrate_scalar",
 ]
 
 
@@ -86,6 +86,8 @@ def load(path=None):
     L.mglet_gpu_par_ftoc_norm.argtypes = [vp, C.c_int32, cp, cp, cp, C.c_int32]
     L.mglet_gpu_set_body_force.argtypes = [vp, vp, vp, vp, C.c_int64]
     L.mglet_gpu_set_lesmodel.argtypes = [vp, C.c_int32, C.c_double]
+    L.mglet_gpu_set_scalars.argtypes = [vp, C.c_int32, vp, vp, vp, C.c_double]
+    L.mglet_gpu_timeintegrate_scalar.argtypes = [vp, C.c_double, C.c_int32, vp]
     L.mglet_gpu_adjoint_rk_stage.argtypes = [vp, C.c_int32, C.c_double, vp]
     L.mglet_gpu_energy_gradient.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, vp,
                                             C.POINTER(C.c_double)]
@@ -241,6 +243,18 @@ class Solver:
 
     def ctof(self, ilevel, ff, fc):
         _check(load().mglet_gpu_ctof(self.h, ilevel, ff.encode(), fc.encode()))
+
+    def set_scalars(self, prmol, kayscrawford=None, source=None, prturb=1.0):
+        n = len(prmol)
+        pr = np.ascontiguousarray(prmol, dtype=np.float64)
+        kc = np.ascontiguousarray(kayscrawford if kayscrawford is not None else [0] * n, dtype=np.int32)
+        so = np.ascontiguousarray(source if source is not None else [0.0] * n, dtype=np.float64)
+        _check(load().mglet_gpu_set_scalars(self.h, n, pr.ctypes.data_as(C.c_void_p),
+                                            kc.ctypes.data_as(C.c_void_p), so.ctypes.data_as(C.c_void_p),
+                                            prturb))
+
+    def timeintegrate_scalar(self, dt, irk, rk):
+        _check(load().mglet_gpu_timeintegrate_scalar(self.h, dt, irk, C.byref(rk)))
 
     def set_lesmodel(self, model, cm=-1.0):
         """0 none, 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default."""

@@ -64,6 +64,8 @@ def lib():
         _lib.oracle_ftoc_multiple.argtypes = [vp, C.c_int] + [C.c_char_p] * 6
         _lib.oracle_set_body_force.argtypes = [vp, vp, vp, vp, C.c_int64]
         _lib.oracle_set_lesmodel.argtypes = [vp, C.c_int, C.c_double]
+        _lib.oracle_set_scalars.argtypes = [vp, C.c_int, vp, vp, vp, C.c_double]
+        _lib.oracle_timeintegrate_scalar.argtypes = [vp, C.c_double, C.c_int, vp]
         _lib.oracle_par_ftoc_norm.argtypes = [vp, C.c_int] + [C.c_char_p] * 3 + [C.c_int]
         _lib.oracle_ctof.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p]
         _lib.oracle_bound_pressure.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
@@ -231,6 +233,20 @@ class Oracle:
         v = list(v) if v else [None] * 3
         s = list(s) + [None] * (3 - len(s))
         _check(lib().oracle_ftoc_multiple(self.h, ilevel, *[_b(n) for n in v + s]))
+
+    def set_scalars(self, prmol, kayscrawford=None, source=None, prturb=1.0):
+        """Scalars T1..Tn with molecular Prandtl numbers prmol, the
+        Kays/Crawford switch and a constant source each."""
+        n = len(prmol)
+        pr = np.ascontiguousarray(prmol, dtype=np.float64)
+        kc = np.ascontiguousarray(kayscrawford if kayscrawford is not None else [0] * n, dtype=np.int32)
+        so = np.ascontiguousarray(source if source is not None else [0.0] * n, dtype=np.float64)
+        self._sca = (pr, kc, so)
+        _check(lib().oracle_set_scalars(self.h, n, pr.ctypes.data_as(C.c_void_p), kc.ctypes.data_as(C.c_void_p),
+                                        so.ctypes.data_as(C.c_void_p), prturb))
+
+    def timeintegrate_scalar(self, dt, irk, rk):
+        _check(lib().oracle_timeintegrate_scalar(self.h, dt, irk, C.byref(rk)))
 
     def set_lesmodel(self, model, cm=-1.0):
         """0 none, 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default."""

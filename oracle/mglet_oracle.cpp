@@ -149,6 +149,15 @@ struct Ctx {
     int ibtype = 0;              // 0: NONE (noib), 1: GHOSTCELL
     bool bodyforce = false;      // FBX, FBY, FBZ added in tstle4
     bool g_user = false;         // G set by the caller: set_hierarchy keeps it
+    // scalars (scacore_mod.F90): T<n> and DT<n>, their molecular Prandtl
+    // number, the Kays/Crawford switch and a constant source
+    struct ScalarDef {
+        std::string name;
+        double prmol = 1.0, source = 0.0;
+        int kayscrawford = 0;
+    };
+    std::vector<ScalarDef> sca;
+    double prturb = 1.0;
     double cm = 0.0;             // LES model constant
     std::vector<std::array<GcList, 3>> gcl;   // [grid][component], 1-based grids
     std::vector<GcFlux> gcf;
@@ -799,6 +808,7 @@ void sip(Ctx& c, int ilevel, int iloop, double* dp, double* res, const double* r
 
 void bound_pressure(Ctx& c, int ilevel, const std::string& name, bool withbp);
 void parent(Ctx& c, int ilevel, const char* v[3], const char* sc[3], bool normal);
+void rkstep(double* p, double* dp, const double* rhsp, int64_t n, double frhs, double dtfu);
 void ftoc_one(Ctx& c, int ilevel, const std::string& ff, const std::string& fc, char flag);
 void ctof(Ctx& c, int ilevel, const std::string& ff, const std::string& fc);
 
@@ -1968,6 +1978,208 @@ void lesmodel(Ctx& c) {
     }
     for (int g = 1; g <= c.ngrid; ++g) setginbody(c, g);
     connect(c, 0, 1, nullptr, nullptr, nullptr, Gf, nullptr, nullptr, true, false, 0);
+}
+
+// ---- scalar transport (src/scalar/timeintegrate_scalar_mod.F90) -----------
+
+// scacore_mod.F90:232-262 prt: the turbulent Prandtl number (default-kind
+// literals of the Kays/Crawford fit widened)
+double prt(const Ctx& c, const Ctx::ScalarDef& s, double gtgmol) {
+    if (s.kayscrawford == 0) return c.prturb;
+    if (gtgmol > 0.0)
+        return (double)0.5882f + (double)0.228f * gtgmol -
+               (double)0.0441f * (gtgmol * gtgmol) * (1.0 - std::exp((double)(-5.165f) / gtgmol));
+    return s.prmol;
+}
+
+// timeintegrate_scalar_mod.F90:229-476 tstsca4_grid: the face fluxes QTU,
+// QTV, QTW of scalar t (central convection, diffusion with the LES
+// diffusivity where a model runs, the upwind correction at PAR faces)
+void tstsca4_grid(Ctx& c, int g, const Ctx::ScalarDef& sd, const double* T) {
+    const Grid& G = c.g[g];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int64_t o = G.ip3;
+    double* qtu = c.F("QTU") + o; double* qtv = c.F("QTV") + o; double* qtw = c.F("QTW") + o;
+    const double* t = T + o;
+    const double* u = c.F("U") + o; const double* v = c.F("V") + o; const double* w = c.F("W") + o;
+    const double* gg = c.F("G") + o; const double* bt = c.F("BT") + o;
+    const double* ddx = c.L("DDX") + G.ipx - 1; const double* ddy = c.L("DDY") + G.ipy - 1;
+    const double* ddz = c.L("DDZ") + G.ipz - 1;
+    const double* rdx = c.L("RDX") + G.ipx - 1; const double* rdy = c.L("RDY") + G.ipy - 1;
+    const double* rdz = c.L("RDZ") + G.ipz - 1;
+    const double gmol = c.prm.gmol, rho = c.prm.rho;
+    const int nfro = G.bc[1], nbac = G.bc[2], nrgt = G.bc[3], nlft = G.bc[4], nbot = G.bc[5], ntop = G.bc[6];
+    const int nfu = nfro == 7, nbu = nbac == 7, nrv = nrgt == 7, nlv = nlft == 7, nbw = nbot == 7, ntw = ntop == 7;
+#define A(a, k, j, i) a[IX(k, j, i)]
+    for (int i = 1; i <= ii; ++i)
+        for (int j = 1; j <= jj; ++j)
+            for (int k = 1; k <= kk; ++k) A(qtu, k, j, i) = A(qtv, k, j, i) = A(qtw, k, j, i) = 0.0;
+    auto gsca = [&](double g0, double g1) {
+        const double gscamol = gmol / rho / sd.prmol;
+        if (c.ilesmodel == 0) return gscamol;
+        const double gtgmolp = (g0 - gmol) / gmol, gtgmoln = (g1 - gmol) / gmol;
+        const double gs = gscamol + (g1 + g0 - 2.0 * gmol) / rho / (prt(c, sd, gtgmoln) + prt(c, sd, gtgmolp));
+        return std::max(gscamol, gs);
+    };
+    for (int i = 3 - nfu; i <= ii - 3 + nbu; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                const double gs = gsca(A(gg, k, j, i), A(gg, k, j, i + 1));
+                const double adv = (ddy[j] * ddz[k]) * A(u, k, j, i) * 0.5 * (A(t, k, j, i) + A(t, k, j, i + 1));
+                const double area = A(bt, k, j, i) * A(bt, k, j, i + 1) * (ddy[j] * ddz[k]);
+                const double diff = -gs * rdx[i] * (A(t, k, j, i + 1) - A(t, k, j, i)) * area;
+                A(qtu, k, j, i) = adv + diff;
+            }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3 - nrv; j <= jj - 3 + nlv; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                const double gs = gsca(A(gg, k, j, i), A(gg, k, j + 1, i));
+                const double adv = (ddx[i] * ddz[k]) * A(v, k, j, i) * 0.5 * (A(t, k, j, i) + A(t, k, j + 1, i));
+                const double area = A(bt, k, j, i) * A(bt, k, j + 1, i) * (ddx[i] * ddz[k]);
+                const double diff = -gs * rdy[j] * (A(t, k, j + 1, i) - A(t, k, j, i)) * area;
+                A(qtv, k, j, i) = adv + diff;
+            }
+    for (int i = 3; i <= ii - 2; ++i)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k) {
+                const double gs = gsca(A(gg, k, j, i), A(gg, k + 1, j, i));
+                const double adv = (ddx[i] * ddy[j]) * A(w, k, j, i) * 0.5 * (A(t, k, j, i) + A(t, k + 1, j, i));
+                const double area = A(bt, k, j, i) * A(bt, k + 1, j, i) * (ddx[i] * ddy[j]);
+                const double diff = -gs * rdz[k] * (A(t, k + 1, j, i) - A(t, k, j, i)) * area;
+                A(qtw, k, j, i) = adv + diff;
+            }
+    // PAR faces: upwind in the layer next to the coarse grid
+    if (nfro == 8)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                const int i = 3;
+                A(qtu, k, j, i) = A(qtu, k, j, i) + (ddy[j] * ddz[k]) * (A(u, k, j, i) - std::fabs(A(u, k, j, i))) *
+                                                        0.5 * 0.5 * (-A(t, k, j, i) + A(t, k, j, i + 1));
+            }
+    if (nbac == 8)
+        for (int j = 3; j <= jj - 2; ++j)
+            for (int k = 3; k <= kk - 2; ++k) {
+                const int i = ii - 3;
+                A(qtu, k, j, i) = A(qtu, k, j, i) + (ddy[j] * ddz[k]) * (A(u, k, j, i) + std::fabs(A(u, k, j, i))) *
+                                                        0.5 * 0.5 * (A(t, k, j, i) - A(t, k, j, i + 1));
+            }
+    if (nrgt == 8)
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int k = 3; k <= kk - 2; ++k) {
+                const int j = 3;
+                A(qtv, k, j, i) = A(qtv, k, j, i) + (ddx[i] * ddz[k]) * (A(v, k, j, i) - std::fabs(A(v, k, j, i))) *
+                                                        0.5 * 0.5 * (-A(t, k, j, i) + A(t, k, j + 1, i));
+            }
+    if (nlft == 8)
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int k = 3; k <= kk - 2; ++k) {
+                const int j = jj - 3;
+                A(qtv, k, j, i) = A(qtv, k, j, i) + (ddx[i] * ddz[k]) * (A(v, k, j, i) + std::fabs(A(v, k, j, i))) *
+                                                        0.5 * 0.5 * (A(t, k, j, i) - A(t, k, j + 1, i));
+            }
+    if (nbot == 8)
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j) {
+                const int k = 3;
+                A(qtw, k, j, i) = A(qtw, k, j, i) + (ddx[i] * ddy[j]) * (A(w, k, j, i) - std::fabs(A(w, k, j, i))) *
+                                                        0.5 * 0.5 * (-A(t, k, j, i) + A(t, k + 1, j, i));
+            }
+    if (ntop == 8)
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j) {
+                const int k = kk - 3;
+                A(qtw, k, j, i) = A(qtw, k, j, i) + (ddx[i] * ddy[j]) * (A(w, k, j, i) + std::fabs(A(w, k, j, i))) *
+                                                        0.5 * 0.5 * (A(t, k, j, i) - A(t, k + 1, j, i));
+            }
+#undef A
+}
+
+// bound_scalar_mod.F90:103-123 (and the right / bottom twins): on a PAR
+// face the coarse flux of the buffer split over the four fine faces by
+// their open areas
+void bound_scaflux_par(Ctx& c, int ilevel) {
+    const double* BT = c.F("BT");
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel) continue;
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const double* bt = BT + G.ip3;
+        for (int f = 1; f <= 6; ++f) {
+            if (G.bc[f] != MGLET_BC_PAR) continue;
+            const int d = (f - 1) / 2;
+            const char* fn = d == 0 ? "QTU" : (d == 1 ? "QTV" : "QTW");
+            double* q = c.F(fn) + G.ip3;
+            const double* buf = buffer_of(c, fn).data() + c.bufoff[6 * (g - 1) + f - 1];
+            const int n = d == 0 ? ii : (d == 1 ? jj : kk);
+            const int p3 = f % 2 == 1 ? 3 : n - 2, ps = f % 2 == 1 ? 2 : n - 2;
+            const int na = d == 0 ? jj : ii, nq = d == 2 ? jj : kk;
+            auto at = [&](int p, int a, int qq) -> int64_t {
+                if (d == 0) return IX(qq, a, p);
+                if (d == 1) return IX(qq, p, a);
+                return IX(p, qq, a);
+            };
+            for (int a = 3; a <= na - 2; a += 2)
+                for (int qq = 3; qq <= nq - 2; qq += 2) {
+                    const double a1 = bt[at(p3, a, qq)], a2 = bt[at(p3, a, qq + 1)];
+                    const double a3 = bt[at(p3, a + 1, qq)], a4 = bt[at(p3, a + 1, qq + 1)];
+                    const double tot = a1 + a2 + a3 + a4;
+                    const double qtot = buf[(qq - 1) + (int64_t)(a - 1) * nq];
+                    auto d0 = [&](double x) { return tot == 0.0 ? 0.0 : x / tot; };
+                    q[at(ps, a, qq)] = d0(a1) * qtot;
+                    q[at(ps, a, qq + 1)] = d0(a2) * qtot;
+                    q[at(ps, a + 1, qq)] = d0(a3) * qtot;
+                    q[at(ps, a + 1, qq + 1)] = d0(a4) * qtot;
+                }
+        }
+    }
+}
+
+// timeintegrate_scalar (timeintegrate_scalar_mod.F90:17-108) for every
+// scalar: fluxes, PAR fluxes from the parent, flux balance, source, RK
+// update, restriction and the corner connect
+int timeintegrate_scalar(Ctx& c, double dt, int irk, const mglet_rk_scheme* rk) {
+    double frhs, fu, dtrk, dtrki;
+    if (irk > rk->nrk || irk < 1) return fail(MGLET_ERR_ARG, "timeintegrate_scalar: irk out of range");
+    frhs = rk->a[irk - 1];
+    fu = rk->b[irk - 1];
+    dtrk = irk < rk->nrk ? rk->c[irk] : 1.0;
+    dtrki = dtrk - rk->c[irk - 1];
+    (void)dtrki;
+    const char* qn[3] = {"QTU", "QTV", "QTW"};
+    const char* none[3] = {nullptr, nullptr, nullptr};
+    for (const Ctx::ScalarDef& sd : c.sca) {
+        double* T = c.F(sd.name.c_str());
+        double* DT = c.F(("D" + sd.name).c_str());
+        for (int g = 1; g <= c.ngrid; ++g) tstsca4_grid(c, g, sd, T);
+        for (int l = c.minlevel; l <= c.maxlevel; ++l) {
+            parent(c, l, qn, none, false);
+            bound_scaflux_par(c, l);
+        }
+        double* qtt = c.F("QTT");
+        std::fill(c.f3["QTT"].begin(), c.f3["QTT"].end(), 0.0);
+        for (int g = 1; g <= c.ngrid; ++g) {
+            const Grid& G = c.g[g];
+            const int kk = G.kk, jj = G.jj, ii = G.ii;
+            const int64_t o = G.ip3;
+            const double* qtu = c.F("QTU") + o; const double* qtv = c.F("QTV") + o;
+            const double* qtw = c.F("QTW") + o;
+            const double* rddx = c.L("RDDX") + G.ipx - 1; const double* rddy = c.L("RDDY") + G.ipy - 1;
+            const double* rddz = c.L("RDDZ") + G.ipz - 1;
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    for (int k = 3; k <= kk - 2; ++k) {
+                        const double net = qtu[IX(k, j, i - 1)] - qtu[IX(k, j, i)] + qtv[IX(k, j - 1, i)] -
+                                           qtv[IX(k, j, i)] + qtw[IX(k - 1, j, i)] - qtw[IX(k, j, i)];
+                        double q = rddz[k] * rddy[j] * rddx[i] * net;
+                        if (sd.source != 0.0) q = q + sd.source;   // sourceterm_const
+                        qtt[o + IX(k, j, i)] = q;
+                    }
+        }
+        rkstep(T, DT, qtt, c.idim3d, frhs, dt * fu);
+        for (int l = c.maxlevel; l > c.minlevel; --l) ftoc_one(c, l, sd.name, sd.name, 'T');
+        connect(c, 0, 2, nullptr, nullptr, nullptr, T, nullptr, nullptr, true, false, 0);
+    }
+    return 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -3632,6 +3844,35 @@ int oracle_set_lesmodel(oracle_ctx* c, int model, double cm) {
     if (model == 0) init_viscosity(*c);
     else lesmodel(*c);
     return 0;
+}
+
+int oracle_set_scalars(oracle_ctx* c, int nsca, const double* prmol, const int32_t* kayscrawford,
+                       const double* source, double prturb) {
+    if (!c || nsca < 0 || nsca > 9 || (nsca && (!prmol || !kayscrawford)))
+        return fail(MGLET_ERR_ARG, "set_scalars: 0..9 scalars with prmol and kayscrawford");
+    if (nsca && c->ibtype == 1)
+        return fail(MGLET_ERR_UNSUPPORTED, "set_scalars: the ghost-cell scalar stencils are not restated");
+    c->sca.clear();
+    for (int l = 0; l < nsca; ++l) {
+        Ctx::ScalarDef sd;
+        sd.name = "T" + std::to_string(l + 1);
+        sd.prmol = prmol[l];
+        sd.kayscrawford = kayscrawford[l];
+        sd.source = source ? source[l] : 0.0;
+        c->sca.push_back(sd);
+        c->f3[sd.name].assign(c->idim3d, 0.0);
+        c->f3["D" + sd.name].assign(c->idim3d, 0.0);
+    }
+    c->prturb = prturb;
+    for (const char* n : {"QTU", "QTV", "QTW", "QTT", "BT"}) c->f3[n].assign(c->idim3d, 0.0);
+    std::fill(c->f3["BT"].begin(), c->f3["BT"].end(), 1.0);   // blockbt: open everywhere (noib)
+    return 0;
+}
+
+int oracle_timeintegrate_scalar(oracle_ctx* c, double dt, int irk, const mglet_rk_scheme* rk) {
+    if (!c || !rk) return fail(MGLET_ERR_ARG, "timeintegrate_scalar: null argument");
+    if (int rc = hierarchy_ready(*c)) return rc;
+    return timeintegrate_scalar(*c, dt, irk, rk);
 }
 
 int oracle_set_body_force(oracle_ctx* c, const double* fx, const double* fy, const double* fz,

@@ -1,0 +1,76 @@
+"""Scalar transport on the GPU (plain FP64 form) against the oracle: RK
+stages of two scalars interleaved with the flow stages, bit for bit on one
+level and on a two-level hierarchy (PAR fluxes from the parent), and with
+an LES model (within 1e-12 where the Kays/Crawford fit takes CUDA's exp)."""
+import numpy as np
+import pytest
+
+from mglet_gb300 import abi, cases
+from test_oracle_levels import prepare_levels
+
+pytestmark = pytest.mark.gpu
+
+
+def _prm(**kw):
+    base = dict(gmol=1e-2, epcorr=1e-12, nouter=6, ninner=5, nouter_min=6)
+    base.update(kw)
+    return abi.make_flow_params(**base)
+
+
+def _run(gs, o, case, rk, les=0, kc=(0, 0), stages=3, levels=False):
+    rng = np.random.default_rng(12)
+    u, v, w, p = cases.taylor_green(case)
+    f = dict(zip("UVWP", (u + 0.2, v, w, p)))
+    t1 = 1.0 + 0.1 * rng.standard_normal(case.idim3d)
+    t2 = rng.standard_normal(case.idim3d)
+    for s in (gs, o):
+        if levels:
+            s.set_hierarchy(case.iparent, case.position)
+        for n, a in f.items():
+            s.set(n, a)
+        s.set_scalars([0.71, 2.0], kayscrawford=list(kc), source=[0.0, 0.05], prturb=0.9)
+        s.set("T1", t1)
+        s.set("T2", t2)
+        if levels:
+            for lvl in (1, 2):
+                s.connect(lvl, 2, v1="U", v2="V", v3="W", s1="P", s2="T1", s3="T2", corners=True)
+            prepare_levels(s, case)
+        else:
+            s.connect(0, 2, "U", "V", "W", "P", corners=True)
+            s.connect(0, 2, s1="T1", s2="T2", corners=True)
+        if les:
+            s.set_lesmodel(les)
+    for irk in range(1, stages + 1):
+        for s in (gs, o):
+            s.timeintegrate_scalar(5e-3, irk, rk)
+            s.timeintegrate_flow(1, 1, 0.0, 5e-3, irk, rk)
+
+
+def test_scalar_stages_bit_exact(gpu_lib, oracle_lib):
+    case = cases.periodic_box(2, 2, 1, n=8, length=(2.0, 2.0, 1.0))
+    gs, o = gpu_lib.Solver(case, _prm()), oracle_lib.Oracle(case, _prm())
+    _run(gs, o, case, oracle_lib.rk_scheme("williamson"))
+    for n in ("T1", "T2", "DT1", "DT2", "U", "P"):
+        assert np.array_equal(gs.get(n), o.get(n)), n
+
+
+def test_scalar_on_a_hierarchy_bit_exact(gpu_lib, oracle_lib):
+    case = cases.refined_box(2, 2, 2, n=8, refine=(1,))
+    gs, o = gpu_lib.Solver(case, _prm()), oracle_lib.Oracle(case, _prm())
+    _run(gs, o, case, oracle_lib.rk_scheme("williamson"), levels=True)
+    for n in ("T1", "T2", "U"):
+        assert np.array_equal(gs.get(n), o.get(n)), n
+
+
+@pytest.mark.parametrize("kc", [(0, 0), (1, 1)])
+def test_scalar_with_les(gpu_lib, oracle_lib, kc):
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0))
+    prm = _prm(gmol=1e-4)
+    gs, o = gpu_lib.Solver(case, prm), oracle_lib.Oracle(case, prm)
+    _run(gs, o, case, oracle_lib.rk_scheme("williamson"), les=1, kc=kc)
+    for n in ("T1", "T2"):
+        a, b = gs.get(n), o.get(n)
+        if kc == (0, 0):
+            assert np.array_equal(a, b), n
+        else:
+            assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), n
