@@ -305,6 +305,13 @@ int mglet_gpu_set_scalars(mglet_ctx* ctx, int32_t nsca, const double* prmol,
  * before timeintegrate_flow in each stage (timeloop_mod.F90:233-235). */
 int mglet_gpu_timeintegrate_scalar(mglet_ctx* ctx, double dt, int32_t irk,
                                    const mglet_rk_scheme* rk);
+/* The Boussinesq buoyancy term (boussinesqterm_mod.F90): -gravity beta T_old
+ * of scalar iscalar (1-based) added to uo, vo, wo after tstle4; T_old is
+ * the scalar before its latest mglet_gpu_timeintegrate_scalar. */
+int mglet_gpu_set_buoyancy(mglet_ctx* ctx, const double* gravity, double beta, int32_t iscalar);
+/* The Coriolis term (coriolisterm_mod.F90): -2 omega x u added to uo, vo, wo
+ * after tstle4 (and the buoyancy term). */
+int mglet_gpu_set_coriolis(mglet_ctx* ctx, const double* omega);
 /* ---- Body force and the discrete adjoint (no counterpart in the reference) --
  * A steady body force per unit mass, added to uo, vo, wo in tstle4 after
  * gradp over the same points (plain form); n must equal idim3d. */

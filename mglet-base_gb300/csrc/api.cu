@@ -498,6 +498,7 @@ static int stage_plain(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk,
     if (int rc = launch_tstle4(c, UO, VO, WO, gc ? c->F("PWU") : U, gc ? c->F("PWV") : V,
                                gc ? c->F("PWW") : W, U, V, W, P, G))
         return rc;
+    if (int rc = launch_momentum_sources(c)) return rc;     // :102-103 boussinesq, coriolis
     if (int rc = launch_rkstep(c, U, c->F("DU"), UO, frhs, dt * fu)) return rc;
     if (int rc = launch_rkstep(c, V, c->F("DV"), VO, frhs, dt * fu)) return rc;
     if (int rc = launch_rkstep(c, W, c->F("DW"), WO, frhs, dt * fu)) return rc;
@@ -965,6 +966,25 @@ int mglet_gpu_timeintegrate_scalar(mglet_ctx* c, double dt, int32_t irk, const m
     if (int rc = hierarchy_ready(c)) return rc;
     if (int rc = timeintegrate_scalar(c, dt, irk, rk)) return rc;
     MG_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int mglet_gpu_set_buoyancy(mglet_ctx* c, const double* gravity, double beta, int32_t iscalar) {
+    if (!c || !gravity || iscalar < 1 || iscalar > (int)c->sca.size())
+        return fail(MGLET_ERR_ARG, "set_buoyancy: gravity and a scalar 1..nsca");
+    if (c->prm.form != MGLET_FORM_PLAIN) return fail(MGLET_ERR_UNSUPPORTED, "set_buoyancy: the plain form only");
+    for (int q = 0; q < 3; ++q) c->gravity[q] = gravity[q];
+    c->beta = beta;
+    c->buoyancy_scalar = iscalar;
+    c->buoyancy = true;
+    return 0;
+}
+
+int mglet_gpu_set_coriolis(mglet_ctx* c, const double* omega) {
+    if (!c || !omega) return fail(MGLET_ERR_ARG, "set_coriolis: null argument");
+    if (c->prm.form != MGLET_FORM_PLAIN) return fail(MGLET_ERR_UNSUPPORTED, "set_coriolis: the plain form only");
+    for (int q = 0; q < 3; ++q) c->omega[q] = omega[q];
+    c->coriolis = true;
     return 0;
 }
 

@@ -157,6 +157,10 @@ struct Ctx {
     };
     std::vector<ScalarDef> sca;
     double prturb = 1.0;
+    // boussinesqterm_mod.F90 / coriolisterm_mod.F90 parameters
+    bool buoyancy = false, coriolis = false;
+    double gravity[3] = {0.0, 0.0, 0.0}, beta = 0.0, omega[3] = {0.0, 0.0, 0.0};
+    int buoyancy_scalar = 1;
     int ilesmodel = 0;           // 0 none, 1 smagorinsky, 2 wale, 5 sigma
     double cm = 0.0;             // the LES model constant
     void* d_sptab = nullptr;     // device table of the 12 spacing arrays (adjoint)
@@ -271,6 +275,8 @@ int fill_field(Ctx* c, double* a, double v);   // a[0..idim3d) = v (api.cu)
 int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawford, const double* source,
                 double prturb);
 int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk);
+// boussinesqterm and coriolisterm on UO, VO, WO after tstle4 (scalar.cu)
+int launch_momentum_sources(Ctx* c);
 int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos);
 double* field_buffer(Ctx* c, const std::string& name);   // boundary buffers of a field
 int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w);

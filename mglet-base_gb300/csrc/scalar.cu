@@ -157,9 +157,74 @@ __global__ void k_fluxbalance(const DevGrid* __restrict__ grids, const double* _
     QTT[o + tt] = r;
 }
 
+// boussinesqterm_grid (boussinesqterm_mod.F90:92-181) and coriolis_grid
+// (coriolisterm_mod.F90:100-189) at one point, over tstle4's ranges
+__global__ void k_momentum_sources(const DevGrid* __restrict__ grids, double* UO, double* VO, double* WO,
+                                   const double* __restrict__ U, const double* __restrict__ V,
+                                   const double* __restrict__ W, const double* __restrict__ TOLD, double gx,
+                                   double gy, double gz, double beta, int buoy, double o1, double o2, double o3,
+                                   int cori) {
+    const DevGrid G = grids[blockIdx.y];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int tt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (tt >= kk * jj * ii) return;
+    const int k = tt % kk + 1, j = (tt / kk) % jj + 1, i = tt / (kk * jj) + 1;
+    const long long o = G.ip3, c = IX(k, j, i);
+    const int nfro = G.bc[0], nbac = G.bc[1], nrgt = G.bc[2], nlft = G.bc[3], nbot = G.bc[4], ntop = G.bc[5];
+    const int nbu = (nbac == 7 || nbac == 3), nlv = (nlft == 7 || nlft == 3), ntw = (ntop == 7 || ntop == 3);
+    const int nfu = nfro == 3, nrv = nrgt == 3, nbw = nbot == 3;
+    const bool iin = i >= 3 && i <= ii - 2, jin = j >= 3 && j <= jj - 2, kin = k >= 3 && k <= kk - 2;
+    const double *u = U + o, *v = V + o, *w = W + o, *t = TOLD ? TOLD + o : nullptr;
+    if (i >= 3 - nfu && i <= ii - 3 + nbu && jin && kin) {
+        double x = UO[o + c];
+        if (buoy && fabs(gx) > 0.0) x = x + -gx * beta * (0.5 * (t[c] + t[IX(k, j, i + 1)]));
+        if (cori && fabs(o2) + fabs(o3) > 0.0) {
+            const double v2 = 0.25 * (v[IX(k, j - 1, i)] + v[IX(k, j - 1, i + 1)] + v[c] + v[IX(k, j, i + 1)]);
+            const double v3 = 0.25 * (w[IX(k - 1, j, i)] + w[IX(k - 1, j, i + 1)] + w[c] + w[IX(k, j, i + 1)]);
+            x = x + -2.0 * (o2 * v3 - o3 * v2);
+        }
+        UO[o + c] = x;
+    }
+    if (iin && j >= 3 - nrv && j <= jj - 3 + nlv && kin) {
+        double x = VO[o + c];
+        if (buoy && fabs(gy) > 0.0) x = x + -gy * beta * (0.5 * (t[c] + t[IX(k, j + 1, i)]));
+        if (cori && fabs(o1) + fabs(o3) > 0.0) {
+            const double v1 = 0.25 * (u[IX(k, j, i - 1)] + u[IX(k, j + 1, i - 1)] + u[c] + u[IX(k, j + 1, i)]);
+            const double v3 = 0.25 * (w[IX(k - 1, j, i)] + w[IX(k - 1, j + 1, i)] + w[c] + w[IX(k, j + 1, i)]);
+            x = x + -2.0 * (o3 * v1 - o1 * v3);
+        }
+        VO[o + c] = x;
+    }
+    if (iin && jin && k >= 3 - nbw && k <= kk - 3 + ntw) {
+        double x = WO[o + c];
+        if (buoy && fabs(gz) > 0.0) x = x + -gz * beta * (0.5 * (t[c] + t[IX(k + 1, j, i)]));
+        if (cori && fabs(o1) + fabs(o2) > 0.0) {
+            const double v1 = 0.25 * (u[IX(k, j, i - 1)] + u[IX(k + 1, j, i - 1)] + u[c] + u[IX(k + 1, j, i)]);
+            const double v2 = 0.25 * (v[IX(k, j - 1, i)] + v[IX(k + 1, j - 1, i)] + v[c] + v[IX(k + 1, j, i)]);
+            x = x + -2.0 * (o1 * v2 - o2 * v1);
+        }
+        WO[o + c] = x;
+    }
+}
+
 #undef IX
 
 }  // namespace
+
+int launch_momentum_sources(Ctx* c) {
+    if (!c->buoyancy && !c->coriolis) return 0;
+    ProfScope ps_(c, "momentum_sources");
+    int m = 0;
+    for (const DevGrid& g : c->grids) m = std::max(m, g.kk * g.jj * g.ii);
+    const double* told = nullptr;
+    if (c->buoyancy) told = c->F(("T" + std::to_string(c->buoyancy_scalar) + "_OLD").c_str());
+    k_momentum_sources<<<dim3((m + 255) / 256, c->ngrid), 256, 0, c->stream>>>(
+        c->d_grids, c->F("UO"), c->F("VO"), c->F("WO"), c->F("U"), c->F("V"), c->F("W"), told, c->gravity[0],
+        c->gravity[1], c->gravity[2], c->beta, c->buoyancy ? 1 : 0, c->omega[0], c->omega[1], c->omega[2],
+        c->coriolis ? 1 : 0);
+    MG_LAUNCHED(c);
+    return 0;
+}
 
 int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawford, const double* source,
                 double prturb) {
@@ -178,7 +243,7 @@ int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawfo
         sd.prmol = prmol[l];
         sd.kayscrawford = kayscrawford[l];
         sd.source = source ? source[l] : 0.0;
-        for (const std::string& n : {sd.name, "D" + sd.name}) {
+        for (const std::string& n : {sd.name, "D" + sd.name, sd.name + "_OLD"}) {
             if (!c->f3.count(n))
                 if (int rc = alloc_field3(c, n.c_str())) return rc;
             MG_CUDA(cudaMemsetAsync(c->F(n.c_str()), 0, (size_t)c->idim3d * sizeof(double), c->stream));
@@ -208,6 +273,9 @@ int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) 
     for (const Ctx::ScalarDef& sd : c->sca) {
         double* T = c->F(sd.name.c_str());
         double* DT = c->F(("D" + sd.name).c_str());
+        // T_OLD = T (timeintegrate_scalar_mod.F90:56-57), read by the Boussinesq term
+        MG_CUDA(cudaMemcpyAsync(c->F((sd.name + "_OLD").c_str()), T, (size_t)c->idim3d * sizeof(double),
+                                cudaMemcpyDeviceToDevice, c->stream));
         ScaArgs A;
         A.grids = c->d_grids;
         A.t = T; A.u = c->F("U"); A.v = c->F("V"); A.w = c->F("W"); A.g = c->F("G"); A.bt = c->F("BT");

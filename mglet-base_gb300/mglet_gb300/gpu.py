@@ -32,6 +32,7 @@ EXPORTS = [
     "mglet_gpu_ctof", "mglet_gpu_bound_pressure", "mglet_gpu_par_ftoc_norm",
     "mglet_gpu_set_body_force", "mglet_gpu_adjoint_rk_stage", "mglet_gpu_energy_gradient",
     "mglet_gpu_set_lesmodel", "mglet_gpu_set_scalars", "mglet_gpu_timeintegrate_scalar",
+    "mglet_gpu_set_buoyancy", "mglet_gpu_set_coriolis",
 ]
 
 
@@ -87,6 +88,8 @@ def load(path=None):
     L.mglet_gpu_set_body_force.argtypes = [vp, vp, vp, vp, C.c_int64]
     L.mglet_gpu_set_lesmodel.argtypes = [vp, C.c_int32, C.c_double]
     L.mglet_gpu_set_scalars.argtypes = [vp, C.c_int32, vp, vp, vp, C.c_double]
+    L.mglet_gpu_set_buoyancy.argtypes = [vp, vp, C.c_double, C.c_int32]
+    L.mglet_gpu_set_coriolis.argtypes = [vp, vp]
     L.mglet_gpu_timeintegrate_scalar.argtypes = [vp, C.c_double, C.c_int32, vp]
     L.mglet_gpu_adjoint_rk_stage.argtypes = [vp, C.c_int32, C.c_double, vp]
     L.mglet_gpu_energy_gradient.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, vp,
@@ -255,6 +258,14 @@ class Solver:
 
     def timeintegrate_scalar(self, dt, irk, rk):
         _check(load().mglet_gpu_timeintegrate_scalar(self.h, dt, irk, C.byref(rk)))
+
+    def set_buoyancy(self, gravity, beta, iscalar=1):
+        g = np.ascontiguousarray(gravity, dtype=np.float64)
+        _check(load().mglet_gpu_set_buoyancy(self.h, g.ctypes.data_as(C.c_void_p), beta, iscalar))
+
+    def set_coriolis(self, omega):
+        om = np.ascontiguousarray(omega, dtype=np.float64)
+        _check(load().mglet_gpu_set_coriolis(self.h, om.ctypes.data_as(C.c_void_p)))
 
     def set_lesmodel(self, model, cm=-1.0):
         """0 none, 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default."""

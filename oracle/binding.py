@@ -66,6 +66,8 @@ def lib():
         _lib.oracle_set_lesmodel.argtypes = [vp, C.c_int, C.c_double]
         _lib.oracle_set_scalars.argtypes = [vp, C.c_int, vp, vp, vp, C.c_double]
         _lib.oracle_timeintegrate_scalar.argtypes = [vp, C.c_double, C.c_int, vp]
+        _lib.oracle_set_buoyancy.argtypes = [vp, vp, C.c_double, C.c_int]
+        _lib.oracle_set_coriolis.argtypes = [vp, vp]
         _lib.oracle_par_ftoc_norm.argtypes = [vp, C.c_int] + [C.c_char_p] * 3 + [C.c_int]
         _lib.oracle_ctof.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p]
         _lib.oracle_bound_pressure.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
@@ -247,6 +249,16 @@ class Oracle:
 
     def timeintegrate_scalar(self, dt, irk, rk):
         _check(lib().oracle_timeintegrate_scalar(self.h, dt, irk, C.byref(rk)))
+
+    def set_buoyancy(self, gravity, beta, iscalar=1):
+        g = np.ascontiguousarray(gravity, dtype=np.float64)
+        self._g = g
+        _check(lib().oracle_set_buoyancy(self.h, g.ctypes.data_as(C.c_void_p), beta, iscalar))
+
+    def set_coriolis(self, omega):
+        om = np.ascontiguousarray(omega, dtype=np.float64)
+        self._om = om
+        _check(lib().oracle_set_coriolis(self.h, om.ctypes.data_as(C.c_void_p)))
 
     def set_lesmodel(self, model, cm=-1.0):
         """0 none, 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default."""

@@ -158,6 +158,10 @@ struct Ctx {
     };
     std::vector<ScalarDef> sca;
     double prturb = 1.0;
+    // boussinesqterm_mod.F90 / coriolisterm_mod.F90 parameters
+    bool buoyancy = false, coriolis = false;
+    double gravity[3] = {0.0, 0.0, 0.0}, beta = 0.0, omega[3] = {0.0, 0.0, 0.0};
+    int buoyancy_scalar = 1;
     double cm = 0.0;             // LES model constant
     std::vector<std::array<GcList, 3>> gcl;   // [grid][component], 1-based grids
     std::vector<GcFlux> gcf;
@@ -1980,6 +1984,84 @@ void lesmodel(Ctx& c) {
     connect(c, 0, 1, nullptr, nullptr, nullptr, Gf, nullptr, nullptr, true, false, 0);
 }
 
+// ---- momentum source terms after tstle4 (timeintegration_mod.F90:102-103) --
+
+// boussinesqterm_grid (boussinesqterm_mod.F90:92-181): -gravity beta T_old at
+// the velocity points, over tstle4's ranges, per component with gravity
+void boussinesqterm(Ctx& c) {
+    if (!c.buoyancy) return;
+    const std::string nm = "T" + std::to_string(c.buoyancy_scalar) + "_OLD";
+    const double* T = c.F(nm.c_str());
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const int64_t o = G.ip3;
+        double* uo = c.F("UO") + o; double* vo = c.F("VO") + o; double* wo = c.F("WO") + o;
+        const double* t = T + o;
+        const int nfro = G.bc[1], nbac = G.bc[2], nrgt = G.bc[3], nlft = G.bc[4], nbot = G.bc[5], ntop = G.bc[6];
+        const int nbu = (nbac == 7 || nbac == 3), nlv = (nlft == 7 || nlft == 3), ntw = (ntop == 7 || ntop == 3);
+        const int nfu = nfro == 3, nrv = nrgt == 3, nbw = nbot == 3;
+        if (std::fabs(c.gravity[0]) > 0.0)
+            for (int i = 3 - nfu; i <= ii - 3 + nbu; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    for (int k = 3; k <= kk - 2; ++k)
+                        uo[IX(k, j, i)] = uo[IX(k, j, i)] + -c.gravity[0] * c.beta * (0.5 * (t[IX(k, j, i)] + t[IX(k, j, i + 1)]));
+        if (std::fabs(c.gravity[1]) > 0.0)
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3 - nrv; j <= jj - 3 + nlv; ++j)
+                    for (int k = 3; k <= kk - 2; ++k)
+                        vo[IX(k, j, i)] = vo[IX(k, j, i)] + -c.gravity[1] * c.beta * (0.5 * (t[IX(k, j, i)] + t[IX(k, j + 1, i)]));
+        if (std::fabs(c.gravity[2]) > 0.0)
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k)
+                        wo[IX(k, j, i)] = wo[IX(k, j, i)] + -c.gravity[2] * c.beta * (0.5 * (t[IX(k, j, i)] + t[IX(k + 1, j, i)]));
+    }
+}
+
+// coriolis_grid (coriolisterm_mod.F90:100-189): -2 omega x u with the other
+// components averaged to the velocity point
+void coriolisterm(Ctx& c) {
+    if (!c.coriolis) return;
+    const double* om = c.omega;
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const int64_t o = G.ip3;
+        double* uo = c.F("UO") + o; double* vo = c.F("VO") + o; double* wo = c.F("WO") + o;
+        const double* u = c.F("U") + o; const double* v = c.F("V") + o; const double* w = c.F("W") + o;
+        const int nfro = G.bc[1], nbac = G.bc[2], nrgt = G.bc[3], nlft = G.bc[4], nbot = G.bc[5], ntop = G.bc[6];
+        const int nbu = (nbac == 7 || nbac == 3), nlv = (nlft == 7 || nlft == 3), ntw = (ntop == 7 || ntop == 3);
+        const int nfu = nfro == 3, nrv = nrgt == 3, nbw = nbot == 3;
+#define A(a, k, j, i) a[IX(k, j, i)]
+        if (std::fabs(om[1]) + std::fabs(om[2]) > 0.0)
+            for (int i = 3 - nfu; i <= ii - 3 + nbu; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    for (int k = 3; k <= kk - 2; ++k) {
+                        const double v2 = 0.25 * (A(v, k, j - 1, i) + A(v, k, j - 1, i + 1) + A(v, k, j, i) + A(v, k, j, i + 1));
+                        const double v3 = 0.25 * (A(w, k - 1, j, i) + A(w, k - 1, j, i + 1) + A(w, k, j, i) + A(w, k, j, i + 1));
+                        A(uo, k, j, i) = A(uo, k, j, i) + -2.0 * (om[1] * v3 - om[2] * v2);
+                    }
+        if (std::fabs(om[0]) + std::fabs(om[2]) > 0.0)
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3 - nrv; j <= jj - 3 + nlv; ++j)
+                    for (int k = 3; k <= kk - 2; ++k) {
+                        const double v1 = 0.25 * (A(u, k, j, i - 1) + A(u, k, j + 1, i - 1) + A(u, k, j, i) + A(u, k, j + 1, i));
+                        const double v3 = 0.25 * (A(w, k - 1, j, i) + A(w, k - 1, j + 1, i) + A(w, k, j, i) + A(w, k, j + 1, i));
+                        A(vo, k, j, i) = A(vo, k, j, i) + -2.0 * (om[2] * v1 - om[0] * v3);
+                    }
+        if (std::fabs(om[0]) + std::fabs(om[1]) > 0.0)
+            for (int i = 3; i <= ii - 2; ++i)
+                for (int j = 3; j <= jj - 2; ++j)
+                    for (int k = 3 - nbw; k <= kk - 3 + ntw; ++k) {
+                        const double v1 = 0.25 * (A(u, k, j, i - 1) + A(u, k + 1, j, i - 1) + A(u, k, j, i) + A(u, k + 1, j, i));
+                        const double v2 = 0.25 * (A(v, k, j - 1, i) + A(v, k + 1, j - 1, i) + A(v, k, j, i) + A(v, k + 1, j, i));
+                        A(wo, k, j, i) = A(wo, k, j, i) + -2.0 * (om[0] * v2 - om[1] * v1);
+                    }
+#undef A
+    }
+}
+
 // ---- scalar transport (src/scalar/timeintegrate_scalar_mod.F90) -----------
 
 // scacore_mod.F90:232-262 prt: the turbulent Prandtl number (default-kind
@@ -2150,6 +2232,9 @@ int timeintegrate_scalar(Ctx& c, double dt, int irk, const mglet_rk_scheme* rk) 
     for (const Ctx::ScalarDef& sd : c.sca) {
         double* T = c.F(sd.name.c_str());
         double* DT = c.F(("D" + sd.name).c_str());
+        c.f3[sd.name + "_OLD"] = c.f3[sd.name];   // :56-57, for the Boussinesq term
+        T = c.F(sd.name.c_str());
+        DT = c.F(("D" + sd.name).c_str());
         for (int g = 1; g <= c.ngrid; ++g) tstsca4_grid(c, g, sd, T);
         for (int l = c.minlevel; l <= c.maxlevel; ++l) {
             parent(c, l, qn, none, false);
@@ -3686,6 +3771,8 @@ int oracle_timeintegrate_flow(oracle_ctx* c, int itstep, int ittot, double timep
     if (irk == 1 && gc)
         if (int rc2 = setibvalues(*c)) return rc2;
     tstle4(*c);
+    boussinesqterm(*c);                                       // :102
+    coriolisterm(*c);                                         // :103
     rkstep(c->F("U"), c->F("DU"), c->F("UO"), c->idim3d, frhs, dt * fu);
     rkstep(c->F("V"), c->F("DV"), c->F("VO"), c->idim3d, frhs, dt * fu);
     rkstep(c->F("W"), c->F("DW"), c->F("WO"), c->idim3d, frhs, dt * fu);
@@ -3862,6 +3949,7 @@ int oracle_set_scalars(oracle_ctx* c, int nsca, const double* prmol, const int32
         c->sca.push_back(sd);
         c->f3[sd.name].assign(c->idim3d, 0.0);
         c->f3["D" + sd.name].assign(c->idim3d, 0.0);
+        c->f3[sd.name + "_OLD"].assign(c->idim3d, 0.0);
     }
     c->prturb = prturb;
     for (const char* n : {"QTU", "QTV", "QTW", "QTT", "BT"}) c->f3[n].assign(c->idim3d, 0.0);
@@ -3873,6 +3961,23 @@ int oracle_timeintegrate_scalar(oracle_ctx* c, double dt, int irk, const mglet_r
     if (!c || !rk) return fail(MGLET_ERR_ARG, "timeintegrate_scalar: null argument");
     if (int rc = hierarchy_ready(*c)) return rc;
     return timeintegrate_scalar(*c, dt, irk, rk);
+}
+
+int oracle_set_buoyancy(oracle_ctx* c, const double* gravity, double beta, int iscalar) {
+    if (!c || !gravity || iscalar < 1 || iscalar > (int)c->sca.size())
+        return fail(MGLET_ERR_ARG, "set_buoyancy: gravity and a scalar 1..nsca");
+    for (int q = 0; q < 3; ++q) c->gravity[q] = gravity[q];
+    c->beta = beta;
+    c->buoyancy_scalar = iscalar;
+    c->buoyancy = true;
+    return 0;
+}
+
+int oracle_set_coriolis(oracle_ctx* c, const double* omega) {
+    if (!c || !omega) return fail(MGLET_ERR_ARG, "set_coriolis: null argument");
+    for (int q = 0; q < 3; ++q) c->omega[q] = omega[q];
+    c->coriolis = true;
+    return 0;
 }
 
 int oracle_set_body_force(oracle_ctx* c, const double* fx, const double* fy, const double* fz,

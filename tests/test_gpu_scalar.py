@@ -74,3 +74,16 @@ def test_scalar_with_les(gpu_lib, oracle_lib, kc):
             assert np.array_equal(a, b), n
         else:
             assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), n
+
+
+def test_buoyancy_and_coriolis_bit_exact(gpu_lib, oracle_lib):
+    case = cases.periodic_box(2, 2, 1, n=8, length=(2.0, 2.0, 1.0))
+    gs, o = gpu_lib.Solver(case, _prm()), oracle_lib.Oracle(case, _prm())
+    for s in (gs, o):
+        s.set_scalars([0.71, 2.0])
+    for s in (gs, o):
+        s.set_buoyancy([0.3, -0.2, -9.81], 3e-3, iscalar=2)
+        s.set_coriolis([0.1, -0.2, 0.25])
+    _run(gs, o, case, oracle_lib.rk_scheme("williamson"))
+    for n in ("T1", "T2", "U", "V", "W", "P"):
+        assert np.array_equal(gs.get(n), o.get(n)), n

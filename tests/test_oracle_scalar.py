@@ -123,3 +123,37 @@ def test_diffusing_mode_decays_at_the_discrete_rate(oracle_lib):
     got = case.interior(o.get("T1"))
     want = case.interior(t.ravel()) * amp
     assert np.allclose(got, want, rtol=0, atol=1e-13)
+
+
+def test_buoyancy_of_a_uniform_scalar_accelerates_uniformly(oracle_lib):
+    """-gravity beta T of a uniform scalar is a uniform force, which the
+    pressure of a periodic box cannot take up: after one time step the fluid
+    moves against gravity at dt g beta T (RK3 integrates a constant force
+    exactly), and not across it (boussinesqterm_mod.F90)."""
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0))
+    o = oracle_lib.Oracle(case, _prm())
+    o.set_scalars([0.71])
+    o.set("T1", np.full(case.idim3d, 2.0))
+    o.set_buoyancy([0.0, 0.0, -9.81], 3e-3)
+    rk = oracle_lib.rk_scheme("williamson")
+    for irk in (1, 2, 3):
+        o.timeintegrate_scalar(1e-2, irk, rk)
+        o.timeintegrate_flow(1, 1, 0.0, 1e-2, irk, rk)
+    for n in "UV":
+        assert np.abs(case.interior(o.get(n))).max() < 1e-14, n
+    assert np.allclose(case.interior(o.get("W")), 1e-2 * 9.81 * 3e-3 * 2.0, rtol=1e-12, atol=0)
+
+
+def test_coriolis_turns_a_uniform_stream(oracle_lib):
+    """-2 omega x u of a uniform stream u0 along x with omega along z
+    accelerates v by -2 omega u0 (coriolisterm_mod.F90): after the first RK
+    stage v = dt b1 (-2 omega u0) everywhere inside."""
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0))
+    o = oracle_lib.Oracle(case, _prm())
+    o.set("U", np.full(case.idim3d, 1.5))
+    o.set_coriolis([0.0, 0.0, 0.25])
+    rk = oracle_lib.rk_scheme("williamson")
+    o.timeintegrate_flow(1, 1, 0.0, 1e-2, 1, rk)
+    want = 1e-2 * rk.b[0] * (-2.0 * 0.25 * 1.5)
+    assert np.allclose(case.interior(o.get("V")), want, rtol=1e-12, atol=0)
+    assert np.allclose(case.interior(o.get("U")), 1.5, rtol=0, atol=1e-14)
