@@ -295,11 +295,18 @@ int mglet_gpu_set_lesmodel(mglet_ctx* ctx, int32_t model, double cm);
  * scalars as the device fields T1..Tn with their RK increments DT1..DTn;
  * prmol the molecular Prandtl numbers, kayscrawford the switch of the
  * turbulent Prandtl number fit (scacore_mod.F90:232-262, else prturb),
- * source (may be NULL) a constant source per scalar.  The scalar wall and
- * in/outflow conditions (SWA, SIO) are not built: non-CON, non-PAR faces
- * carry no scalar flux. */
+ * source (may be NULL) a constant source per scalar.  A boundary face
+ * without a scalar condition (mglet_gpu_set_scalar_bc) carries no scalar
+ * flux. */
 int mglet_gpu_set_scalars(mglet_ctx* ctx, int32_t nsca, const double* prmol,
                           const int32_t* kayscrawford, const double* source, double prturb);
+/* A scalar boundary condition beside the flow condition of boundary face
+ * iface of grid igrid (bound_scalar_mod.F90:124-210 and twins): kind 1 SWA
+ * (wall), 2 SIO (inflow/outflow), 0 none; types[l] per scalar: 0 fixed
+ * value, 1 fixed flux, the value or flux taken from the scalar's boundary
+ * buffer (mglet_gpu_set_buffer with the scalar's name). */
+int mglet_gpu_set_scalar_bc(mglet_ctx* ctx, int32_t igrid, int32_t iface, int32_t kind,
+                            const int32_t* types);
 /* timeintegrate_scalar (src/scalar/timeintegrate_scalar_mod.F90:17-108): one
  * RK stage of every scalar on the current velocity; the reference calls it
  * before timeintegrate_flow in each stage (timeloop_mod.F90:233-235). */

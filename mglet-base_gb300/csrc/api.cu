@@ -785,6 +785,8 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     cudaFree(c->d_hier);
     cudaFree(c->d_pargrids);
     cudaFree(c->d_sptab);
+    cudaFree(c->d_scabc_kind);
+    cudaFree(c->d_scabc_type);
     for (auto& kv : c->d_pftasks) cudaFree(kv.second);
     cudaFree(c->d_gridred);
     cudaFree(c->d_scalar);
@@ -967,6 +969,12 @@ int mglet_gpu_timeintegrate_scalar(mglet_ctx* c, double dt, int32_t irk, const m
     if (int rc = timeintegrate_scalar(c, dt, irk, rk)) return rc;
     MG_CUDA(cudaStreamSynchronize(c->stream));
     return 0;
+}
+
+int mglet_gpu_set_scalar_bc(mglet_ctx* c, int32_t igrid, int32_t iface, int32_t kind, const int32_t* types) {
+    if (!c) return fail(MGLET_ERR_ARG, "set_scalar_bc: null context");
+    cudaSetDevice(c->device);
+    return set_scalar_bc(c, igrid, iface, kind, types);
 }
 
 int mglet_gpu_set_buoyancy(mglet_ctx* c, const double* gravity, double beta, int32_t iscalar) {

@@ -157,6 +157,10 @@ struct Ctx {
     };
     std::vector<ScalarDef> sca;
     double prturb = 1.0;
+    // scalar conditions beside a face's flow condition: kind 1 SWA (wall),
+    // 2 SIO (in/outflow); per scalar 0 fixed value, 1 fixed flux
+    std::vector<int> scabc_kind, scabc_type;
+    int *d_scabc_kind = nullptr, *d_scabc_type = nullptr;
     // boussinesqterm_mod.F90 / coriolisterm_mod.F90 parameters
     bool buoyancy = false, coriolis = false;
     double gravity[3] = {0.0, 0.0, 0.0}, beta = 0.0, omega[3] = {0.0, 0.0, 0.0};
@@ -277,6 +281,7 @@ int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawfo
 int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk);
 // boussinesqterm and coriolisterm on UO, VO, WO after tstle4 (scalar.cu)
 int launch_momentum_sources(Ctx* c);
+int set_scalar_bc(Ctx* c, int igrid, int iface, int kind, const int32_t* types);
 int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos);
 double* field_buffer(Ctx* c, const std::string& name);   // boundary buffers of a field
 int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w);

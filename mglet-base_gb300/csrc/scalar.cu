@@ -12,6 +12,7 @@
 // Kays/Crawford fit takes CUDA's exp).
 
 #include <algorithm>
+#include <cmath>
 #include <string>
 #include <vector>
 
@@ -130,6 +131,107 @@ __global__ void k_scaflux_par(const DevGrid* __restrict__ grids, const BFace* __
     qf[at(ps, a, q + 1)] = (tot == 0.0 ? 0.0 : a2 / tot) * qtot;
     qf[at(ps, a + 1, q)] = (tot == 0.0 ? 0.0 : a3 / tot) * qtot;
     qf[at(ps, a + 1, q + 1)] = (tot == 0.0 ? 0.0 : a4 / tot) * qtot;
+}
+
+struct WallArgs {
+    const DevGrid* grids;
+    const BFace* bface;
+    const int *kind, *type;      // [ngrid*6], [ngrid*6*9]
+    const double *t, *u, *v, *w, *tb;
+    double *qtu, *qtv, *qtw;
+    const double *dx, *dy, *dz, *ddx, *ddy, *ddz;
+    double gmol, rho, prmol;
+    // wernerwengle_mod.F90:13-28
+    double cwa, cwb, cpo4, cpo5, cpo6, cpo8;
+    int f, ilevel, l, les;
+};
+
+// wernerwengle_mod.F90:92-122 qwallfix (CUDA's pow)
+__device__ double qwallfix(const WallArgs& A, double tbound, double tfluid, double uquer, double dds) {
+    const double cpo1 = 1.0 - A.cwb, cpo2 = 1.0 + A.cwb;
+    const double uquern = fabs(uquer);
+    if (uquern >= A.cpo6 / dds) {
+        const double ddsb = pow(dds, -A.cwb);
+        const double tauwin = A.rho * pow(ddsb * (A.cpo4 * uquern + A.cpo5 / dds), A.cpo8);
+        const double sm = A.gmol / sqrt(tauwin * A.rho) * pow(A.cwa, 1.0 / (1.0 - A.cwb));
+        const double fsm = 1.0 / (dds * dds) *
+                           (0.5 * (sm * sm) * A.prmol + pow(sqrt(tauwin * A.rho) / A.gmol, -cpo1) * A.cwa / cpo2 *
+                                                            (pow(dds, cpo2) - pow(sm, cpo2)));
+        return A.gmol / A.rho * (tbound - tfluid) / dds / fsm;
+    }
+    return A.gmol / A.rho / A.prmol * (tbound - tfluid) * 2.0 / dds;
+}
+
+// bound_scalar_mod.F90:124-210 and twins: the SWA / SIO flux of face A.f
+// of scalar A.l on the grids of A.ilevel, one thread per plane point
+__global__ void k_scaflux_walls(WallArgs A) {
+    const DevGrid G = A.grids[blockIdx.y];
+    if (G.level != A.ilevel) return;
+    const int f = A.f;
+    const int kind = A.kind[6 * blockIdx.y + f - 1];
+    if (kind == 0) return;
+    const int type = A.type[(6 * blockIdx.y + f - 1) * 9 + A.l];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int d = (f - 1) / 2;
+    const double dir = f % 2 == 1 ? -1.0 : 1.0;
+    const int n = d == 0 ? ii : (d == 1 ? jj : kk);
+    const int p2 = f % 2 == 1 ? 2 : n - 2, p3 = f % 2 == 1 ? 3 : n - 2;
+    const int na = d == 0 ? jj : ii, nq = d == 2 ? jj : kk;
+    const int q0 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q0 >= na * nq) return;
+    const int a = q0 / nq + 1, qq = q0 % nq + 1;
+    const bool les_wall = kind == 1 && type == 0 && A.les;
+    if (les_wall && (a < 2 || qq < 2)) return;
+    const long long o = G.ip3;
+    const double *dd0 = A.ddx + G.ipx - 1, *dd1 = A.ddy + G.ipy - 1, *dd2 = A.ddz + G.ipz - 1;
+    const double* dxs = d == 0 ? A.dx + G.ipx - 1 : (d == 1 ? A.dy + G.ipy - 1 : A.dz + G.ipz - 1);
+    const double* A1 = d == 0 ? dd1 : dd0;
+    const double* A2 = d == 2 ? dd1 : dd2;
+    auto at = [&](int p) -> long long {
+        if (d == 0) return IX(qq, a, p);
+        if (d == 1) return IX(qq, p, a);
+        return IX(p, qq, a);
+    };
+    const double *t = A.t + o, *u = A.u + o, *v = A.v + o, *w = A.w + o;
+    const double tbv = A.tb[A.bface[6 * blockIdx.y + f - 1].off + (qq - 1) + (long long)(a - 1) * nq];
+    const double tin = t[at(p3)];
+    double r;
+    if (type == 1) {
+        const double area = A1[a] * A2[qq];
+        r = -dir * tbv * area;
+    } else if (kind == 1 && !A.les) {
+        const double gamma2dx = 2.0 * A.gmol / A.rho / A.prmol / dxs[p2];
+        const double diff = gamma2dx * (tbv - tin);
+        r = -dir * diff * A1[a] * A2[qq];
+    } else if (kind == 1) {
+        double s1, s2;
+        if (d == 0) {
+            const int k = qq, j = a, i = p3;
+            s1 = w[IX(k - 1, j, i)] + (w[IX(k, j, i)] - w[IX(k - 1, j, i)]) / dd2[k] * dd2[k - 1] * 0.5;
+            s2 = v[IX(k, j - 1, i)] + (v[IX(k, j, i)] - v[IX(k, j - 1, i)]) / dd1[j] * dd1[j - 1] * 0.5;
+        } else if (d == 1) {
+            const int k = qq, i = a, j = p3;
+            s1 = w[IX(k - 1, j, i)] + (w[IX(k, j, i)] - w[IX(k - 1, j, i)]) / dd2[k] * dd2[k - 1] * 0.5;
+            s2 = u[IX(k, j, i - 1)] + (u[IX(k, j, i)] - u[IX(k, j, i - 1)]) / dd0[i] * dd0[i - 1] * 0.5;
+        } else {
+            const int j = qq, i = a, k = p3;
+            s1 = u[IX(k, j, i - 1)] + (u[IX(k, j, i)] - u[IX(k, j, i - 1)]) / dd0[i] * dd0[i - 1] * 0.5;
+            s2 = v[IX(k, j - 1, i)] + (v[IX(k, j, i)] - v[IX(k, j - 1, i)]) / dd1[j] * dd1[j - 1] * 0.5;
+        }
+        const double uquer = sqrt(s1 * s1 + s2 * s2);
+        const double dds = d == 0 ? dd0[p3] : (d == 1 ? dd1[p3] : dd2[p3]);
+        r = -dir * qwallfix(A, tbv, tin, uquer, dds) * (A1[a] * A2[qq]);
+    } else {
+        const double gamma = A.gmol / A.rho / A.prmol;
+        const double* un = d == 0 ? u : (d == 1 ? v : w);
+        const double unv = un[at(p2)];
+        const double tout = -dir * unv >= 0.0 ? 2.0 * tbv - tin : tin;
+        const double adv = -dir * unv * 0.5 * (tout + tin);
+        const double diff = gamma * (tout - tin) / dxs[p2];
+        r = -dir * (adv + diff) * (A1[a] * A2[qq]);
+    }
+    double* qf = (d == 0 ? A.qtu : (d == 1 ? A.qtv : A.qtw)) + o;
+    qf[at(p2)] = r;
 }
 
 // fluxbalance_grid (:520-545) and sourceterm_const (:590-607) over the box
@@ -258,6 +360,38 @@ int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawfo
     return fill_field(c, c->F("BT"), 1.0);
 }
 
+int set_scalar_bc(Ctx* c, int igrid, int iface, int kind, const int32_t* types) {
+    if (igrid < 1 || igrid > c->ngrid || iface < 1 || iface > 6 || kind < 0 || kind > 2 || (kind && !types)) {
+        set_error("set_scalar_bc: bad arguments");
+        return MGLET_ERR_ARG;
+    }
+    const int t = c->grids[igrid - 1].bc[iface - 1];
+    if (kind && (t == MGLET_BC_CON || t == MGLET_BC_CO1 || t == MGLET_BC_PAR)) {
+        set_error("set_scalar_bc: SWA and SIO sit on boundary faces");
+        return MGLET_ERR_ARG;
+    }
+    if (c->scabc_kind.empty()) {
+        c->scabc_kind.assign(6 * (size_t)c->ngrid, 0);
+        c->scabc_type.assign(6 * (size_t)c->ngrid * 9, 0);
+        MG_CUDA(cudaMalloc(&c->d_scabc_kind, c->scabc_kind.size() * sizeof(int)));
+        MG_CUDA(cudaMalloc(&c->d_scabc_type, c->scabc_type.size() * sizeof(int)));
+    }
+    const size_t x = 6 * (size_t)(igrid - 1) + iface - 1;
+    c->scabc_kind[x] = kind;
+    for (size_t l = 0; l < c->sca.size() && kind; ++l) {
+        if (types[l] != 0 && types[l] != 1) {
+            set_error("set_scalar_bc: type 0 (value) or 1 (flux)");
+            return MGLET_ERR_ARG;
+        }
+        c->scabc_type[x * 9 + l] = types[l];
+    }
+    MG_CUDA(copy_on(c->stream, c->d_scabc_kind, c->scabc_kind.data(), c->scabc_kind.size() * sizeof(int),
+                    cudaMemcpyHostToDevice));
+    MG_CUDA(copy_on(c->stream, c->d_scabc_type, c->scabc_type.data(), c->scabc_type.size() * sizeof(int),
+                    cudaMemcpyHostToDevice));
+    return 0;
+}
+
 int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) {
     double frhs, fu, dtrk, dtrki;
     if (int rc = rk_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki)) return rc;
@@ -286,6 +420,38 @@ int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) 
         A.kayscrawford = sd.kayscrawford; A.les = c->ilesmodel != 0;
         k_tstsca4<<<bg, 256, 0, c->stream>>>(A);
         MG_LAUNCHED(c);
+        if (!c->scabc_kind.empty()) {
+            // SWA / SIO faces (bound_scalar_mod.F90:124-210), faces in order
+            WallArgs W;
+            W.grids = c->d_grids; W.bface = c->d_bface; W.kind = c->d_scabc_kind; W.type = c->d_scabc_type;
+            W.t = T; W.u = c->F("U"); W.v = c->F("V"); W.w = c->F("W");
+            W.tb = field_buffer(c, sd.name);
+            if (!W.tb) {
+                set_error("timeintegrate_scalar: buffer allocation");
+                return MGLET_ERR_CUDA;
+            }
+            W.qtu = c->F("QTU"); W.qtv = c->F("QTV"); W.qtw = c->F("QTW");
+            W.dx = c->L("DX"); W.dy = c->L("DY"); W.dz = c->L("DZ");
+            W.ddx = c->L("DDX"); W.ddy = c->L("DDY"); W.ddz = c->L("DDZ");
+            W.gmol = c->prm.gmol; W.rho = c->prm.rho; W.prmol = sd.prmol;
+            W.cwa = 8.3; W.cwb = 1.0 / 7.0;
+            const double cpo1 = 1.0 - W.cwb, cpo2 = 1.0 + W.cwb;
+            W.cpo4 = cpo2 / W.cwa * std::pow(W.gmol / W.rho, W.cwb);
+            W.cpo5 = 0.5 * cpo1 * std::pow(W.cwa, cpo2 / cpo1) * std::pow(W.gmol / W.rho, cpo2);
+            W.cpo6 = 0.5 * W.gmol / W.rho * std::pow(W.cwa, 2.0 / cpo1);
+            W.cpo8 = 2.0 / cpo2;
+            W.l = (int)(&sd - c->sca.data());
+            W.les = c->ilesmodel != 0;
+            int mp = 0;
+            for (const DevGrid& g : c->grids) mp = std::max(mp, std::max(g.jj * g.kk, std::max(g.ii * g.kk, g.ii * g.jj)));
+            for (int l = c->minlevel; l <= c->maxlevel; ++l)
+                for (int f = 1; f <= 6; ++f) {
+                    W.f = f;
+                    W.ilevel = l;
+                    k_scaflux_walls<<<dim3((mp + 127) / 128, c->ngrid), 128, 0, c->stream>>>(W);
+                    MG_LAUNCHED(c);
+                }
+        }
         for (int l = c->minlevel; l <= c->maxlevel; ++l) {
             if (c->minlevel == c->maxlevel) break;
             if (int rc = launch_parent(c, l, qn, none, false)) return rc;

@@ -200,6 +200,14 @@ MODULE mglet_gpu_mod
             TYPE(mglet_rk_scheme), INTENT(in) :: rk
         END FUNCTION mglet_gpu_timeintegrate_scalar
 
+        INTEGER(c_int) FUNCTION mglet_gpu_set_scalar_bc(ctx, igrid, iface, kind, types) &
+                BIND(C, name="mglet_gpu_set_scalar_bc")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: igrid, iface, kind
+            INTEGER(c_int32_t), INTENT(in) :: types(*)
+        END FUNCTION mglet_gpu_set_scalar_bc
+
         INTEGER(c_int) FUNCTION mglet_gpu_set_lesmodel(ctx, model, cm) &
                 BIND(C, name="mglet_gpu_set_lesmodel")
             IMPORT :: c_int, c_int32_t, c_ptr, c_double
@@ -258,7 +266,7 @@ MODULE mglet_gpu_mod
         gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf, &
         gpu_upload_stencils, gpu_start_ghostcell, gpu_set_hierarchy, gpu_ftoc, gpu_ctof, &
         gpu_bound_pressure, gpu_par_ftoc_norm, gpu_set_lesmodel, gpu_set_body_force, &
-        gpu_energy_gradient, gpu_set_scalars, gpu_timeintegrate_scalar
+        gpu_energy_gradient, gpu_set_scalars, gpu_timeintegrate_scalar, gpu_set_scalar_bc
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -343,6 +351,17 @@ CONTAINS
         IF (mglet_gpu_set_scalars(gctx, INT(SIZE(prmol), c_int32_t), prmol, kayscrawford, source, &
             prturb) /= 0) CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_set_scalars
+
+    ! The scalar condition of a boundary face, as get_bcprms hands
+    ! bound_scalar_mod.F90 its scbtype: kind 1 SWA, 2 SIO; scbtype(l) 0 value,
+    ! 1 flux; the value or flux goes in with gpu_upload_buffer under the
+    ! scalar's name
+    SUBROUTINE gpu_set_scalar_bc(igrid, iface, kind, scbtype)
+        INTEGER, INTENT(in) :: igrid, iface, kind
+        INTEGER(c_int32_t), INTENT(in) :: scbtype(:)
+        IF (mglet_gpu_set_scalar_bc(gctx, INT(igrid, c_int32_t), INT(iface, c_int32_t), &
+            INT(kind, c_int32_t), scbtype) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_set_scalar_bc
 
     ! Drop-in for timeintegrate_scalar (src/scalar/timeintegrate_scalar_mod.F90:17)
     SUBROUTINE gpu_timeintegrate_scalar(dt, irk)

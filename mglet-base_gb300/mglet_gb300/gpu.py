@@ -32,7 +32,7 @@ EXPORTS = [
     "mglet_gpu_ctof", "mglet_gpu_bound_pressure", "mglet_gpu_par_ftoc_norm",
     "mglet_gpu_set_body_force", "mglet_gpu_adjoint_rk_stage", "mglet_gpu_energy_gradient",
     "mglet_gpu_set_lesmodel", "mglet_gpu_set_scalars", "mglet_gpu_timeintegrate_scalar",
-    "mglet_gpu_set_buoyancy", "mglet_gpu_set_coriolis",
+    "mglet_gpu_set_buoyancy", "mglet_gpu_set_coriolis", "mglet_gpu_set_scalar_bc",
 ]
 
 
@@ -90,6 +90,7 @@ def load(path=None):
     L.mglet_gpu_set_scalars.argtypes = [vp, C.c_int32, vp, vp, vp, C.c_double]
     L.mglet_gpu_set_buoyancy.argtypes = [vp, vp, C.c_double, C.c_int32]
     L.mglet_gpu_set_coriolis.argtypes = [vp, vp]
+    L.mglet_gpu_set_scalar_bc.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp]
     L.mglet_gpu_timeintegrate_scalar.argtypes = [vp, C.c_double, C.c_int32, vp]
     L.mglet_gpu_adjoint_rk_stage.argtypes = [vp, C.c_int32, C.c_double, vp]
     L.mglet_gpu_energy_gradient.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, vp,
@@ -266,6 +267,10 @@ class Solver:
     def set_coriolis(self, omega):
         om = np.ascontiguousarray(omega, dtype=np.float64)
         _check(load().mglet_gpu_set_coriolis(self.h, om.ctypes.data_as(C.c_void_p)))
+
+    def set_scalar_bc(self, igrid, iface, kind, types=()):
+        ty = np.ascontiguousarray(list(types) + [0] * 9, dtype=np.int32)
+        _check(load().mglet_gpu_set_scalar_bc(self.h, igrid, iface, kind, ty.ctypes.data_as(C.c_void_p)))
 
     def set_lesmodel(self, model, cm=-1.0):
         """0 none, 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default."""

@@ -159,6 +159,9 @@ struct Ctx {
     std::vector<ScalarDef> sca;
     double prturb = 1.0;
     // boussinesqterm_mod.F90 / coriolisterm_mod.F90 parameters
+    // scalar boundary conditions beside a face's flow condition: kind 1 SWA
+    // (wall), 2 SIO (in/outflow), per scalar 0 fixed value, 1 fixed flux
+    std::vector<int> scabc_kind, scabc_type;
     bool buoyancy = false, coriolis = false;
     double gravity[3] = {0.0, 0.0, 0.0}, beta = 0.0, omega[3] = {0.0, 0.0, 0.0};
     int buoyancy_scalar = 1;
@@ -2216,6 +2219,107 @@ void bound_scaflux_par(Ctx& c, int ilevel) {
     }
 }
 
+// wernerwengle_mod.F90:92-122 qwallfix: the wall heat flux of the wall model
+double qwallfix(const Ctx& c, double tbound, double tfluid, double uquer, double dds, double prmol) {
+    const WernerWengle q = werner_wengle(c.prm.gmol, c.prm.rho);
+    const double gmol = c.prm.gmol, rho = c.prm.rho, cwa = 8.3, cwb = q.cwb;
+    const double cpo1 = 1.0 - cwb, cpo2 = 1.0 + cwb;
+    const double uquern = std::fabs(uquer);
+    if (uquern >= q.cpo6 / dds) {
+        const double ddsb = std::pow(dds, -cwb);
+        const double tauwin = rho * std::pow(ddsb * (q.cpo4 * uquern + q.cpo5 / dds), q.cpo8);
+        const double sm = gmol / std::sqrt(tauwin * rho) * std::pow(cwa, 1.0 / (1.0 - cwb));
+        const double fsm = 1.0 / (dds * dds) *
+                           (0.5 * (sm * sm) * prmol + std::pow(std::sqrt(tauwin * rho) / gmol, -cpo1) * cwa / cpo2 *
+                                                          (std::pow(dds, cpo2) - std::pow(sm, cpo2)));
+        return gmol / rho * (tbound - tfluid) / dds / fsm;
+    }
+    return gmol / rho / prmol * (tbound - tfluid) * 2.0 / dds;
+}
+
+// bound_scalar_mod.F90:124-210 (and the right / bottom twins): the SWA and
+// SIO conditions of scalar l on the grids of ilevel, from the scalar's
+// boundary buffer (a wall or inflow value, or a flux)
+void bound_scaflux_walls(Ctx& c, int ilevel, int l, const double* T) {
+    if (c.scabc_kind.empty()) return;
+    const Ctx::ScalarDef& sd = c.sca[l];
+    const std::vector<double>& tb = buffer_of(c, sd.name);
+    const double gmol = c.prm.gmol, rho = c.prm.rho;
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        if (G.level != ilevel) continue;
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const int64_t o = G.ip3;
+        const double* t = T + o;
+        const double* u = c.F("U") + o; const double* v = c.F("V") + o; const double* w = c.F("W") + o;
+        const double* dxs[3] = {c.L("DX") + G.ipx - 1, c.L("DY") + G.ipy - 1, c.L("DZ") + G.ipz - 1};
+        const double* dd[3] = {c.L("DDX") + G.ipx - 1, c.L("DDY") + G.ipy - 1, c.L("DDZ") + G.ipz - 1};
+        for (int f = 1; f <= 6; ++f) {
+            const int kind = c.scabc_kind[6 * (g - 1) + f - 1];
+            if (kind == 0) continue;
+            const int type = c.scabc_type[(6 * (g - 1) + f - 1) * 9 + l];
+            const int d = (f - 1) / 2;
+            const double dir = f % 2 == 1 ? -1.0 : 1.0;
+            const int n = d == 0 ? ii : (d == 1 ? jj : kk);
+            const int p2 = f % 2 == 1 ? 2 : n - 2, p3 = f % 2 == 1 ? 3 : n - 2;
+            const int na = d == 0 ? jj : ii, nq = d == 2 ? jj : kk;
+            const double* A1 = d == 0 ? dd[1] : dd[0];      // ddy (x faces) or ddx
+            const double* A2 = d == 2 ? dd[1] : dd[2];      // ddz, or ddy (z faces)
+            double* qf = c.F(d == 0 ? "QTU" : (d == 1 ? "QTV" : "QTW")) + o;
+            const double* un = d == 0 ? u : (d == 1 ? v : w);
+            const double* b = tb.data() + c.bufoff[6 * (g - 1) + f - 1];
+            auto at = [&](int p, int a, int qq) -> int64_t {
+                if (d == 0) return IX(qq, a, p);
+                if (d == 1) return IX(qq, p, a);
+                return IX(p, qq, a);
+            };
+            const bool les_wall = kind == 1 && type == 0 && c.ilesmodel != 0;
+            for (int a = les_wall ? 2 : 1; a <= na; ++a)
+                for (int qq = les_wall ? 2 : 1; qq <= nq; ++qq) {
+                    const double tbv = b[(qq - 1) + (int64_t)(a - 1) * nq];
+                    const double tin = t[at(p3, a, qq)];
+                    double r;
+                    if (type == 1) {
+                        const double area = A1[a] * A2[qq];
+                        r = -dir * tbv * area;
+                    } else if (kind == 1 && c.ilesmodel == 0) {
+                        const double gamma2dx = 2.0 * gmol / rho / sd.prmol / dxs[d][p2];
+                        const double diff = gamma2dx * (tbv - tin);
+                        r = -dir * diff * A1[a] * A2[qq];
+                    } else if (kind == 1) {
+                        // the two tangential velocities at the cell centre of the first layer
+                        double s1, s2;
+                        if (d == 0) {
+                            const int k = qq, j = a, i = p3;
+                            s1 = w[IX(k - 1, j, i)] + (w[IX(k, j, i)] - w[IX(k - 1, j, i)]) / dd[2][k] * dd[2][k - 1] * 0.5;
+                            s2 = v[IX(k, j - 1, i)] + (v[IX(k, j, i)] - v[IX(k, j - 1, i)]) / dd[1][j] * dd[1][j - 1] * 0.5;
+                        } else if (d == 1) {
+                            const int k = qq, i = a, j = p3;
+                            s1 = w[IX(k - 1, j, i)] + (w[IX(k, j, i)] - w[IX(k - 1, j, i)]) / dd[2][k] * dd[2][k - 1] * 0.5;
+                            s2 = u[IX(k, j, i - 1)] + (u[IX(k, j, i)] - u[IX(k, j, i - 1)]) / dd[0][i] * dd[0][i - 1] * 0.5;
+                        } else {
+                            const int j = qq, i = a, k = p3;
+                            s1 = u[IX(k, j, i - 1)] + (u[IX(k, j, i)] - u[IX(k, j, i - 1)]) / dd[0][i] * dd[0][i - 1] * 0.5;
+                            s2 = v[IX(k, j - 1, i)] + (v[IX(k, j, i)] - v[IX(k, j - 1, i)]) / dd[1][j] * dd[1][j - 1] * 0.5;
+                        }
+                        const double uquer = std::sqrt(s1 * s1 + s2 * s2);
+                        const double area = A1[a] * A2[qq];
+                        r = -dir * qwallfix(c, tbv, tin, uquer, dd[d][p3], sd.prmol) * area;
+                    } else {
+                        const double gamma = gmol / rho / sd.prmol;
+                        const double unv = un[at(p2, a, qq)];
+                        const double tout = -dir * unv >= 0.0 ? 2.0 * tbv - tin : tin;
+                        const double adv = -dir * unv * 0.5 * (tout + tin);
+                        const double diff = gamma * (tout - tin) / dxs[d][p2];
+                        const double area = A1[a] * A2[qq];
+                        r = -dir * (adv + diff) * area;
+                    }
+                    qf[at(p2, a, qq)] = r;
+                }
+        }
+    }
+}
+
 // timeintegrate_scalar (timeintegrate_scalar_mod.F90:17-108) for every
 // scalar: fluxes, PAR fluxes from the parent, flux balance, source, RK
 // update, restriction and the corner connect
@@ -2229,16 +2333,18 @@ int timeintegrate_scalar(Ctx& c, double dt, int irk, const mglet_rk_scheme* rk) 
     (void)dtrki;
     const char* qn[3] = {"QTU", "QTV", "QTW"};
     const char* none[3] = {nullptr, nullptr, nullptr};
-    for (const Ctx::ScalarDef& sd : c.sca) {
+    for (size_t l = 0; l < c.sca.size(); ++l) {
+        const Ctx::ScalarDef& sd = c.sca[l];
         double* T = c.F(sd.name.c_str());
         double* DT = c.F(("D" + sd.name).c_str());
         c.f3[sd.name + "_OLD"] = c.f3[sd.name];   // :56-57, for the Boussinesq term
         T = c.F(sd.name.c_str());
         DT = c.F(("D" + sd.name).c_str());
         for (int g = 1; g <= c.ngrid; ++g) tstsca4_grid(c, g, sd, T);
-        for (int l = c.minlevel; l <= c.maxlevel; ++l) {
-            parent(c, l, qn, none, false);
-            bound_scaflux_par(c, l);
+        for (int lv = c.minlevel; lv <= c.maxlevel; ++lv) {
+            parent(c, lv, qn, none, false);
+            bound_scaflux_par(c, lv);
+            bound_scaflux_walls(c, lv, (int)l, T);
         }
         double* qtt = c.F("QTT");
         std::fill(c.f3["QTT"].begin(), c.f3["QTT"].end(), 0.0);
@@ -3954,6 +4060,26 @@ int oracle_set_scalars(oracle_ctx* c, int nsca, const double* prmol, const int32
     c->prturb = prturb;
     for (const char* n : {"QTU", "QTV", "QTW", "QTT", "BT"}) c->f3[n].assign(c->idim3d, 0.0);
     std::fill(c->f3["BT"].begin(), c->f3["BT"].end(), 1.0);   // blockbt: open everywhere (noib)
+    return 0;
+}
+
+int oracle_set_scalar_bc(oracle_ctx* c, int igrid, int iface, int kind, const int32_t* types) {
+    if (!c || igrid < 1 || igrid > c->ngrid || iface < 1 || iface > 6 || kind < 0 || kind > 2 ||
+        (kind && !types))
+        return fail(MGLET_ERR_ARG, "set_scalar_bc: bad arguments");
+    const int t = c->g[igrid].bc[iface];
+    if (kind && (t == MGLET_BC_CON || t == MGLET_BC_CO1 || t == MGLET_BC_PAR))
+        return fail(MGLET_ERR_ARG, "set_scalar_bc: SWA and SIO sit on boundary faces");
+    if (c->scabc_kind.empty()) {
+        c->scabc_kind.assign(6 * (size_t)c->ngrid, 0);
+        c->scabc_type.assign(6 * (size_t)c->ngrid * 9, 0);
+    }
+    const size_t x = 6 * (size_t)(igrid - 1) + iface - 1;
+    c->scabc_kind[x] = kind;
+    for (size_t l = 0; l < c->sca.size() && kind; ++l) {
+        if (types[l] != 0 && types[l] != 1) return fail(MGLET_ERR_ARG, "set_scalar_bc: type 0 or 1");
+        c->scabc_type[x * 9 + l] = types[l];
+    }
     return 0;
 }
 
