@@ -360,6 +360,7 @@ int solve_pressure_system(Ctx* c, double prefak, mglet_stage_stats* st, bool zer
     const size_t bytes = (size_t)c->idim3d * sizeof(double);
     if (zero_work)
         for (double* a : {dp, hilf, res}) MG_CUDA(cudaMemsetAsync(a, 0, bytes, c->stream));
+    if (int rc = launch_bp_ones(c)) return rc;
     if (prefak <= 0.0) {
         if (int rc = launch_rescal_maxabs(c, rhs, nullptr)) return rc;
         MG_CUDA(cudaMemcpyAsync(c->h_scalar, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost,
@@ -729,6 +730,7 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     for (const char* n : {"GSAS", "GSAN"}) if (int rc = alloc1(c, n, oy, nullptr)) return bail(rc);
     for (const char* n : {"GSAB", "GSAT"}) if (int rc = alloc1(c, n, oz, nullptr)) return bail(rc);
     MG_CUDA(cudaMalloc(&c->d_gridred, (size_t)4 * c->ngrid * sizeof(double)));
+    MG_CUDA(cudaMalloc(&c->d_bpone, (size_t)c->ngrid * sizeof(int)));
     MG_CUDA(cudaMalloc(&c->d_scalar, 8 * sizeof(double)));
     MG_CUDA(cudaMallocHost(&c->h_scalar, 8 * sizeof(double)));
     // noib_mod.F90:45-52 (BP = 1, SDIV = 0)
@@ -789,6 +791,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     cudaFree(c->d_scabc_type);
     for (auto& kv : c->d_pftasks) cudaFree(kv.second);
     cudaFree(c->d_gridred);
+    cudaFree(c->d_bpone);
     cudaFree(c->d_scalar);
     if (c->h_scalar) cudaFreeHost(c->h_scalar);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -889,6 +892,7 @@ int mglet_gpu_laplacephi(mglet_ctx* c, const char* res, const char* phi) {
     double *r = field_ptr(c, res), *p = field_ptr(c, phi);
     if (!r || !p) return fail(MGLET_ERR_NAME, "laplacephi: unknown field");
     cudaSetDevice(c->device);
+    if (int rc = launch_bp_ones(c)) return rc;
     return launch_laplacephi(c, 0, r, p);
 }
 

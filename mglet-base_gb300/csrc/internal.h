@@ -128,6 +128,7 @@ struct Ctx {
     std::map<std::string, ConnectPlan> plans;
     // reductions
     double* d_gridred = nullptr;   // [4*ngrid]
+    int* d_bpone = nullptr;        // [ngrid] 1 where BP is 1.0 at every point laplacephi reads
     double* d_scalar = nullptr;    // [8]
     double* h_scalar = nullptr;    // pinned [8]
     // boundary buffers of U, V, W (field_t%get_buffer): one plane per grid and
@@ -253,6 +254,7 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
 int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu);
 int launch_divcal(Ctx* c, double* div, const double* u, const double* v, const double* w,
                   double fak);
+int launch_bp_ones(Ctx* c);
 int launch_laplacephi(Ctx* c, int ilevel, double* res, const double* phi);
 int launch_sip_lu_hp(Ctx* c);
 int launch_sip_lu_classic(Ctx* c);

@@ -371,12 +371,30 @@ __global__ void k_divcal(const DevGrid* __restrict__ grids, double* DIV, const d
     DIV[o + IX(k, j, i)] = d;
 }
 
+// Per grid: is BP exactly 1.0 on the box 2..n-1 in every direction (every
+// point laplacephi reads)?  Then each bp factor of laplacephi is a product
+// with 1.0, which rounds to the other operand, and the kernel may drop it
+// with the same bits (the no-IB grids: noib_mod.F90 leaves bp at 1).
+__global__ void k_bp_ones(const DevGrid* __restrict__ grids, const double* __restrict__ BP, int* ones) {
+    const DevGrid G = grids[blockIdx.x];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int nk = kk - 2, nj = jj - 2, ni = ii - 2;
+    const double* bp = BP + G.ip3;
+    int bad = 0;
+    for (int t = threadIdx.x; t < ni * nj * nk; t += blockDim.x) {
+        const int k = t % nk + 2, j = (t / nk) % nj + 2, i = t / (nk * nj) + 2;
+        bad |= !(bp[IX(k, j, i)] == 1.0);
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) ones[blockIdx.x] = !bad;
+}
+
 __global__ void k_laplacephi(const DevGrid* __restrict__ grids, int ilevel, double* RES,
                              const double* __restrict__ PHI, const double* __restrict__ AP,
                              const double* __restrict__ BP, const double* __restrict__ AW,
                              const double* __restrict__ AE, const double* __restrict__ AS,
                              const double* __restrict__ AN, const double* __restrict__ AB,
-                             const double* __restrict__ AT) {
+                             const double* __restrict__ AT, const int* __restrict__ bpone) {
     const DevGrid G = grids[blockIdx.y];
     if (ilevel > 0 && G.level != ilevel) return;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
@@ -388,6 +406,13 @@ __global__ void k_laplacephi(const DevGrid* __restrict__ grids, int ilevel, doub
     const double *phi = PHI + o, *bp = BP + o;
     const double aw = AW[G.ipx + i - 1], ae = AE[G.ipx + i - 1], as = AS[G.ipy + j - 1],
                  an = AN[G.ipy + j - 1], ab = AB[G.ipz + k - 1], at = AT[G.ipz + k - 1];
+    if (bpone[blockIdx.y]) {
+        RES[o + IX(k, j, i)] = -aw * phi[IX(k, j, i - 1)] - ae * phi[IX(k, j, i + 1)] -
+                               as * phi[IX(k, j - 1, i)] - an * phi[IX(k, j + 1, i)] -
+                               ab * phi[IX(k - 1, j, i)] - at * phi[IX(k + 1, j, i)] -
+                               AP[o + IX(k, j, i)] * phi[IX(k, j, i)];
+        return;
+    }
     RES[o + IX(k, j, i)] = -aw * phi[IX(k, j, i - 1)] * bp[IX(k, j, i - 1)] * bp[IX(k, j, i)] -
                            ae * phi[IX(k, j, i + 1)] * bp[IX(k, j, i)] * bp[IX(k, j, i + 1)] -
                            as * phi[IX(k, j - 1, i)] * bp[IX(k, j - 1, i)] * bp[IX(k, j, i)] -
@@ -631,12 +656,18 @@ int launch_divcal(Ctx* c, double* div, const double* u, const double* v, const d
     return 0;
 }
 
+int launch_bp_ones(Ctx* c) {
+    k_bp_ones<<<c->ngrid, 256, 0, c->stream>>>(c->d_grids, c->F("BP"), c->d_bpone);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
 int launch_laplacephi(Ctx* c, int ilevel, double* res, const double* phi) {
     ProfScope ps_(c, "laplacephi");
     dim3 grid((interior_points_max(c) + 255) / 256, c->ngrid);
     k_laplacephi<<<grid, 256, 0, c->stream>>>(c->d_grids, ilevel, res, phi, c->F("GSAP"), c->F("BP"),
                                               c->L("GSAW"), c->L("GSAE"), c->L("GSAS"),
-                                              c->L("GSAN"), c->L("GSAB"), c->L("GSAT"));
+                                              c->L("GSAN"), c->L("GSAB"), c->L("GSAT"), c->d_bpone);
     MG_LAUNCHED(c);
     return 0;
 }
