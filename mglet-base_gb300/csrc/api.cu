@@ -731,6 +731,7 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     for (const char* n : {"GSAB", "GSAT"}) if (int rc = alloc1(c, n, oz, nullptr)) return bail(rc);
     MG_CUDA(cudaMalloc(&c->d_gridred, (size_t)4 * c->ngrid * sizeof(double)));
     MG_CUDA(cudaMalloc(&c->d_bpone, (size_t)c->ngrid * sizeof(int)));
+    MG_CUDA(cudaMalloc(&c->d_guni, (size_t)2 * c->ngrid * sizeof(double)));
     MG_CUDA(cudaMalloc(&c->d_scalar, 8 * sizeof(double)));
     MG_CUDA(cudaMallocHost(&c->h_scalar, 8 * sizeof(double)));
     // noib_mod.F90:45-52 (BP = 1, SDIV = 0)
@@ -792,6 +793,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     for (auto& kv : c->d_pftasks) cudaFree(kv.second);
     cudaFree(c->d_gridred);
     cudaFree(c->d_bpone);
+    cudaFree(c->d_guni);
     cudaFree(c->d_scalar);
     if (c->h_scalar) cudaFreeHost(c->h_scalar);
     if (c->stream) cudaStreamDestroy(c->stream);

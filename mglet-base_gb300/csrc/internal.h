@@ -128,7 +128,8 @@ struct Ctx {
     std::map<std::string, ConnectPlan> plans;
     // reductions
     double* d_gridred = nullptr;   // [4*ngrid]
-    int* d_bpone = nullptr;        // [ngrid] 1 where BP is 1.0 at every point laplacephi reads
+    int* d_bpone = nullptr;
+    double* d_guni = nullptr;      // [2*ngrid] tstle4's uniform-G flag and face mean        // [ngrid] 1 where BP is 1.0 at every point laplacephi reads
     double* d_scalar = nullptr;    // [8]
     double* h_scalar = nullptr;    // pinned [8]
     // boundary buffers of U, V, W (field_t%get_buffer): one plane per grid and

@@ -33,6 +33,10 @@ struct Wall {
     double rho, gmol, cpo4, cpo5, cpo6, cpo8;
     int bc[6];
     bool any;
+    // G equal to one value g0 on every point tstle4_diff reads: each face
+    // mean pair hm(g0, g0) + hm(g0, g0) is the same number h2
+    bool guni;
+    double h2;
 };
 
 #define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
@@ -121,10 +125,10 @@ __device__ double uo_point(int k, int j, int i, int kk, int jj, const double* u,
         double ax = ddy[j] * ddz[k], ay = dx[i] * ddz[k], az = dx[i] * ddy[j];
         double ge = A(gg, k, j, i + 1);
         double gw = A(gg, k, j, i);
-        double gn = hm(A(gg, k, j, i), A(gg, k, j + 1, i), gmol) + hm(A(gg, k, j, i + 1), A(gg, k, j + 1, i + 1), gmol);
-        double gs = hm(A(gg, k, j - 1, i), A(gg, k, j, i), gmol) + hm(A(gg, k, j - 1, i + 1), A(gg, k, j, i + 1), gmol);
-        double gt = hm(A(gg, k, j, i), A(gg, k + 1, j, i), gmol) + hm(A(gg, k, j, i + 1), A(gg, k + 1, j, i + 1), gmol);
-        double gb = hm(A(gg, k - 1, j, i), A(gg, k, j, i), gmol) + hm(A(gg, k - 1, j, i + 1), A(gg, k, j, i + 1), gmol);
+        double gn = wl.guni ? wl.h2 : hm(A(gg, k, j, i), A(gg, k, j + 1, i), gmol) + hm(A(gg, k, j, i + 1), A(gg, k, j + 1, i + 1), gmol);
+        double gs = wl.guni ? wl.h2 : hm(A(gg, k, j - 1, i), A(gg, k, j, i), gmol) + hm(A(gg, k, j - 1, i + 1), A(gg, k, j, i + 1), gmol);
+        double gt = wl.guni ? wl.h2 : hm(A(gg, k, j, i), A(gg, k + 1, j, i), gmol) + hm(A(gg, k, j, i + 1), A(gg, k + 1, j, i + 1), gmol);
+        double gb = wl.guni ? wl.h2 : hm(A(gg, k - 1, j, i), A(gg, k, j, i), gmol) + hm(A(gg, k - 1, j, i + 1), A(gg, k, j, i + 1), gmol);
         double qe = -ge * ax * rddx[i + 1] * (A(u, k, j, i + 1) - A(u, k, j, i));
         double qw = -gw * ax * rddx[i] * (A(u, k, j, i) - A(u, k, j, i - 1));
         double qn = -gn * ay * rdy[j] * (A(u, k, j + 1, i) - A(u, k, j, i));
@@ -172,12 +176,12 @@ __device__ double vo_point(int k, int j, int i, int kk, int jj, const double* u,
     vo = wall_v(vo, k, j, i, s, wl, A(v, k, j, i));
     {
         double ax = dy[j] * ddz[k], ay = ddx[i] * ddz[k], az = ddx[i] * dy[j];
-        double ge = hm(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hm(A(gg, k, j + 1, i), A(gg, k, j + 1, i + 1), gmol);
-        double gw = hm(A(gg, k, j, i - 1), A(gg, k, j, i), gmol) + hm(A(gg, k, j + 1, i - 1), A(gg, k, j + 1, i), gmol);
+        double ge = wl.guni ? wl.h2 : hm(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hm(A(gg, k, j + 1, i), A(gg, k, j + 1, i + 1), gmol);
+        double gw = wl.guni ? wl.h2 : hm(A(gg, k, j, i - 1), A(gg, k, j, i), gmol) + hm(A(gg, k, j + 1, i - 1), A(gg, k, j + 1, i), gmol);
         double gn = A(gg, k, j + 1, i);
         double gs = A(gg, k, j, i);
-        double gt = hm(A(gg, k, j, i), A(gg, k + 1, j, i), gmol) + hm(A(gg, k, j + 1, i), A(gg, k + 1, j + 1, i), gmol);
-        double gb = hm(A(gg, k - 1, j, i), A(gg, k, j, i), gmol) + hm(A(gg, k - 1, j + 1, i), A(gg, k, j + 1, i), gmol);
+        double gt = wl.guni ? wl.h2 : hm(A(gg, k, j, i), A(gg, k + 1, j, i), gmol) + hm(A(gg, k, j + 1, i), A(gg, k + 1, j + 1, i), gmol);
+        double gb = wl.guni ? wl.h2 : hm(A(gg, k - 1, j, i), A(gg, k, j, i), gmol) + hm(A(gg, k - 1, j + 1, i), A(gg, k, j + 1, i), gmol);
         double qe = -ge * ax * rdx[i] * (A(v, k, j, i + 1) - A(v, k, j, i));
         double qw = -gw * ax * rdx[i - 1] * (A(v, k, j, i) - A(v, k, j, i - 1));
         double qn = -gn * ay * rddy[j + 1] * (A(v, k, j + 1, i) - A(v, k, j, i));
@@ -225,10 +229,10 @@ __device__ double wo_point(int k, int j, int i, int kk, int jj, const double* u,
     wo = wall_w(wo, k, j, i, s, wl, A(w, k, j, i));
     {
         double ax = ddy[j] * dz[k], ay = ddx[i] * dz[k], az = ddx[i] * ddy[j];
-        double ge = hm(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j, i + 1), gmol);
-        double gw = hm(A(gg, k, j, i - 1), A(gg, k, j, i), gmol) + hm(A(gg, k + 1, j, i - 1), A(gg, k + 1, j, i), gmol);
-        double gn = hm(A(gg, k, j, i), A(gg, k, j + 1, i), gmol) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j + 1, i), gmol);
-        double gs = hm(A(gg, k, j - 1, i), A(gg, k, j, i), gmol) + hm(A(gg, k + 1, j - 1, i), A(gg, k + 1, j, i), gmol);
+        double ge = wl.guni ? wl.h2 : hm(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j, i + 1), gmol);
+        double gw = wl.guni ? wl.h2 : hm(A(gg, k, j, i - 1), A(gg, k, j, i), gmol) + hm(A(gg, k + 1, j, i - 1), A(gg, k + 1, j, i), gmol);
+        double gn = wl.guni ? wl.h2 : hm(A(gg, k, j, i), A(gg, k, j + 1, i), gmol) + hm(A(gg, k + 1, j, i), A(gg, k + 1, j + 1, i), gmol);
+        double gs = wl.guni ? wl.h2 : hm(A(gg, k, j - 1, i), A(gg, k, j, i), gmol) + hm(A(gg, k + 1, j - 1, i), A(gg, k + 1, j, i), gmol);
         double gt = A(gg, k + 1, j, i);
         double gb = A(gg, k, j, i);
         double qe = -ge * ax * rdx[i] * (A(w, k, j, i + 1) - A(w, k, j, i));
@@ -262,7 +266,7 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
                                                 const double* __restrict__ P, const double* __restrict__ Gf,
                                                 Wall wl, double iles, double gx, double gy, double gz,
                                                 const double* __restrict__ FX, const double* __restrict__ FY,
-                                                const double* __restrict__ FZ) {
+                                                const double* __restrict__ FZ, const double* __restrict__ GU) {
     const DevGrid G = grids[blockIdx.y];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int npts = kk * jj * ii;
@@ -271,6 +275,10 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
     const int k = t % kk + 1;
     const int j = (t / kk) % jj + 1;
     const int i = t / (kk * jj) + 1;
+    if (GU) {
+        wl.guni = GU[2 * blockIdx.y] != 0.0;
+        wl.h2 = GU[2 * blockIdx.y + 1];
+    }
     GridPtrs s;
     s.kk = kk; s.jj = jj; s.ii = ii;
     s.dx = sp.dx + G.ipx - 1; s.dy = sp.dy + G.ipy - 1; s.dz = sp.dz + G.ipz - 1;
@@ -342,6 +350,30 @@ static Spacing spacing(Ctx* c) {
     return s;
 }
 
+// Per grid {1, h2} when G holds one value g0 on the box 2..n-1 in every
+// direction (all points of G that tstle4_diff reads), else {0, 0}; h2 is
+// hm(g0, g0) + hm(g0, g0) by the same operations, so the shortcut keeps the
+// bits.  Without an LES model G is gmol there on grids without walls.
+__global__ void k_g_uniform(const DevGrid* __restrict__ grids, const double* __restrict__ Gf, double gmol,
+                            double* __restrict__ out) {
+    const DevGrid G = grids[blockIdx.x];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int nk = kk - 2, nj = jj - 2, ni = ii - 2;
+    const double* g = Gf + G.ip3;
+    const double g0 = A(g, 2, 2, 2);
+    int bad = 0;
+    for (int t = threadIdx.x; t < ni * nj * nk; t += blockDim.x) {
+        const int k = t % nk + 2, j = (t / nk) % nj + 2, i = t / (nk * nj) + 2;
+        bad |= !(A(g, k, j, i) == g0);
+    }
+    bad = __syncthreads_or(bad);
+    if (threadIdx.x == 0) {
+        const double h = hm(g0, g0, gmol);
+        out[2 * blockIdx.x] = bad ? 0.0 : 1.0;
+        out[2 * blockIdx.x + 1] = bad ? 0.0 : h + h;
+    }
+}
+
 static int max_points(Ctx* c) {
     int m = 0;
     for (const DevGrid& g : c->grids) m = std::max(m, g.kk * g.jj * g.ii);
@@ -353,6 +385,8 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
                   const double* p, const double* g) {
     ProfScope ps_(c, "tstle4");
     dim3 grid((max_points(c) + 255) / 256, c->ngrid);
+    k_g_uniform<<<c->ngrid, 256, 0, c->stream>>>(c->d_grids, g, c->prm.gmol, c->d_guni);
+    MG_LAUNCHED(c);
     // wernerwengle_mod.F90:13-28 init_wernerwengle
     Wall wl = {};
     const double gmol = c->prm.gmol, rho = c->prm.rho, cwa = 8.3, cwb = 1.0 / 7.0;
@@ -368,7 +402,7 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
                                           c->prm.gradp[2],
                                           c->bodyforce ? c->F("FBX") : nullptr,
                                           c->bodyforce ? c->F("FBY") : nullptr,
-                                          c->bodyforce ? c->F("FBZ") : nullptr);
+                                          c->bodyforce ? c->F("FBZ") : nullptr, c->d_guni);
     MG_LAUNCHED(c);
     // tstle4_mod.F90:114: tstle4_par after kon, diff and gradp (PAR faces)
     return launch_tstle4_par(c, uo, vo, wo, u, v, w, ut, vt, wt);
