@@ -307,6 +307,13 @@ int mglet_gpu_set_scalars(mglet_ctx* ctx, int32_t nsca, const double* prmol,
  * buffer (mglet_gpu_set_buffer with the scalar's name). */
 int mglet_gpu_set_scalar_bc(mglet_ctx* ctx, int32_t igrid, int32_t iface, int32_t kind,
                             const int32_t* types);
+/* Appends a source to scalar isca (1-based), as an entry of sca%sources
+ * (timeintegrate_scalar_mod.F90:549-634): field NULL or "" adds value to
+ * the scalar's balance on every interior cell (sourceterm_const), else
+ * value times the named cell-centred field (sourceterm_field).  Sources
+ * apply in the order added, after a constant source from
+ * mglet_gpu_set_scalars; at most 8 per scalar. */
+int mglet_gpu_add_scalar_source(mglet_ctx* ctx, int32_t isca, const char* field, double value);
 /* timeintegrate_scalar (src/scalar/timeintegrate_scalar_mod.F90:17-108): one
  * RK stage of every scalar on the current velocity; the reference calls it
  * before timeintegrate_flow in each stage (timeloop_mod.F90:233-235). */

@@ -983,6 +983,11 @@ int mglet_gpu_set_scalar_bc(mglet_ctx* c, int32_t igrid, int32_t iface, int32_t 
     return set_scalar_bc(c, igrid, iface, kind, types);
 }
 
+int mglet_gpu_add_scalar_source(mglet_ctx* c, int32_t isca, const char* field, double value) {
+    if (!c) return fail(MGLET_ERR_ARG, "add_scalar_source: null context");
+    return add_scalar_source(c, isca, field, value);
+}
+
 int mglet_gpu_set_buoyancy(mglet_ctx* c, const double* gravity, double beta, int32_t iscalar) {
     if (!c || !gravity || iscalar < 1 || iscalar > (int)c->sca.size())
         return fail(MGLET_ERR_ARG, "set_buoyancy: gravity and a scalar 1..nsca");

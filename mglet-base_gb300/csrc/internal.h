@@ -154,8 +154,11 @@ struct Ctx {
     // Kays/Crawford switch, constant source
     struct ScalarDef {
         std::string name;
-        double prmol = 1.0, source = 0.0;
+        double prmol = 1.0;
         int kayscrawford = 0;
+        // sources in order: empty field name = constant (sourceterm_const),
+        // else value * field (sourceterm_field)
+        std::vector<std::pair<std::string, double>> sources;
     };
     std::vector<ScalarDef> sca;
     double prturb = 1.0;
@@ -285,6 +288,7 @@ int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk);
 // boussinesqterm and coriolisterm on UO, VO, WO after tstle4 (scalar.cu)
 int launch_momentum_sources(Ctx* c);
 int set_scalar_bc(Ctx* c, int igrid, int iface, int kind, const int32_t* types);
+int add_scalar_source(Ctx* c, int isca, const char* field, double value);
 int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos);
 double* field_buffer(Ctx* c, const std::string& name);   // boundary buffers of a field
 int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double* w);

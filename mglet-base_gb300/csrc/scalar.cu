@@ -234,12 +234,20 @@ __global__ void k_scaflux_walls(WallArgs A) {
     qf[at(p2)] = r;
 }
 
-// fluxbalance_grid (:520-545) and sourceterm_const (:590-607) over the box
+// the sources of one scalar in order (at most 8): field null = constant
+struct SrcList {
+    int n;
+    double val[8];
+    const double* field[8];
+};
+
+// fluxbalance_grid (:520-545) and sourceterm (:549-634: sourceterm_const,
+// sourceterm_field, the sources in order) over the box
 __global__ void k_fluxbalance(const DevGrid* __restrict__ grids, const double* __restrict__ QTU,
                               const double* __restrict__ QTV, const double* __restrict__ QTW,
                               double* __restrict__ QTT, const double* __restrict__ RDDX,
                               const double* __restrict__ RDDY, const double* __restrict__ RDDZ,
-                              double source) {
+                              SrcList src) {
     const DevGrid G = grids[blockIdx.y];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int tt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -254,7 +262,8 @@ __global__ void k_fluxbalance(const DevGrid* __restrict__ grids, const double* _
         const double net = qtu[IX(k, j, i - 1)] - qtu[IX(k, j, i)] + qtv[IX(k, j - 1, i)] - qtv[IX(k, j, i)] +
                            qtw[IX(k - 1, j, i)] - qtw[IX(k, j, i)];
         r = RDDZ[G.ipz + k - 1] * RDDY[G.ipy + j - 1] * RDDX[G.ipx + i - 1] * net;
-        if (source != 0.0) r = r + source;
+        for (int s = 0; s < src.n; ++s)
+            r = src.field[s] ? r + src.val[s] * src.field[s][o + tt] : r + src.val[s];
     }
     QTT[o + tt] = r;
 }
@@ -344,7 +353,7 @@ int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawfo
         sd.name = "T" + std::to_string(l + 1);
         sd.prmol = prmol[l];
         sd.kayscrawford = kayscrawford[l];
-        sd.source = source ? source[l] : 0.0;
+        if (source && source[l] != 0.0) sd.sources.push_back({"", source[l]});
         for (const std::string& n : {sd.name, "D" + sd.name, sd.name + "_OLD"}) {
             if (!c->f3.count(n))
                 if (int rc = alloc_field3(c, n.c_str())) return rc;
@@ -358,6 +367,24 @@ int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawfo
             if (int rc = alloc_field3(c, n)) return rc;
     // blockbt: every cell open without the ghost-cell IB
     return fill_field(c, c->F("BT"), 1.0);
+}
+
+int add_scalar_source(Ctx* c, int isca, const char* field, double value) {
+    if (isca < 1 || isca > (int)c->sca.size()) {
+        set_error("add_scalar_source: no such scalar");
+        return MGLET_ERR_ARG;
+    }
+    const std::string f = field ? field : "";
+    if (!f.empty() && !c->f3.count(f)) {
+        set_error("add_scalar_source: unknown field");
+        return MGLET_ERR_NAME;
+    }
+    if (c->sca[isca - 1].sources.size() >= 8) {
+        set_error("add_scalar_source: at most 8 sources");
+        return MGLET_ERR_ARG;
+    }
+    c->sca[isca - 1].sources.push_back({f, value});
+    return 0;
 }
 
 int set_scalar_bc(Ctx* c, int igrid, int iface, int kind, const int32_t* types) {
@@ -467,8 +494,14 @@ int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) 
                 MG_LAUNCHED(c);
             }
         }
+        SrcList src = {};
+        src.n = (int)sd.sources.size();
+        for (int s = 0; s < src.n; ++s) {
+            src.val[s] = sd.sources[s].second;
+            src.field[s] = sd.sources[s].first.empty() ? nullptr : c->F(sd.sources[s].first.c_str());
+        }
         k_fluxbalance<<<bg, 256, 0, c->stream>>>(c->d_grids, c->F("QTU"), c->F("QTV"), c->F("QTW"), c->F("QTT"),
-                                                 c->L("RDDX"), c->L("RDDY"), c->L("RDDZ"), sd.source);
+                                                 c->L("RDDX"), c->L("RDDY"), c->L("RDDZ"), src);
         MG_LAUNCHED(c);
         if (int rc = launch_rkstep(c, T, DT, c->F("QTT"), frhs, dt * fu)) return rc;
         for (int l = c->maxlevel; l > c->minlevel; --l)

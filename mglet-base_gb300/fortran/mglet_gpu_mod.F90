@@ -208,6 +208,15 @@ MODULE mglet_gpu_mod
             INTEGER(c_int32_t), INTENT(in) :: types(*)
         END FUNCTION mglet_gpu_set_scalar_bc
 
+        INTEGER(c_int) FUNCTION mglet_gpu_add_scalar_source(ctx, isca, field, value) &
+                BIND(C, name="mglet_gpu_add_scalar_source")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double, c_char
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: isca
+            CHARACTER(kind=c_char), INTENT(in) :: field(*)
+            REAL(c_double), VALUE :: value
+        END FUNCTION mglet_gpu_add_scalar_source
+
         INTEGER(c_int) FUNCTION mglet_gpu_set_lesmodel(ctx, model, cm) &
                 BIND(C, name="mglet_gpu_set_lesmodel")
             IMPORT :: c_int, c_int32_t, c_ptr, c_double
@@ -266,7 +275,8 @@ MODULE mglet_gpu_mod
         gpu_timeintegrate_flow, gpu_itinfo, gpu_upload_buffer, gpu_set_pinf, &
         gpu_upload_stencils, gpu_start_ghostcell, gpu_set_hierarchy, gpu_ftoc, gpu_ctof, &
         gpu_bound_pressure, gpu_par_ftoc_norm, gpu_set_lesmodel, gpu_set_body_force, &
-        gpu_energy_gradient, gpu_set_scalars, gpu_timeintegrate_scalar, gpu_set_scalar_bc
+        gpu_energy_gradient, gpu_set_scalars, gpu_timeintegrate_scalar, gpu_set_scalar_bc, &
+        gpu_add_scalar_source
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -362,6 +372,16 @@ CONTAINS
         IF (mglet_gpu_set_scalar_bc(gctx, INT(igrid, c_int32_t), INT(iface, c_int32_t), &
             INT(kind, c_int32_t), scbtype) /= 0) CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_set_scalar_bc
+
+    ! One entry of sca%sources (timeintegrate_scalar_mod.F90:549-634): an
+    ! empty field name is a constant source, else value * that field
+    SUBROUTINE gpu_add_scalar_source(isca, field, value)
+        INTEGER, INTENT(in) :: isca
+        CHARACTER(len=*), INTENT(in) :: field
+        REAL(c_double), INTENT(in) :: value
+        IF (mglet_gpu_add_scalar_source(gctx, INT(isca, c_int32_t), TRIM(field)//c_null_char, value) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_add_scalar_source
 
     ! Drop-in for timeintegrate_scalar (src/scalar/timeintegrate_scalar_mod.F90:17)
     SUBROUTINE gpu_timeintegrate_scalar(dt, irk)

@@ -33,6 +33,7 @@ EXPORTS = [
     "mglet_gpu_set_body_force", "mglet_gpu_adjoint_rk_stage", "mglet_gpu_energy_gradient",
     "mglet_gpu_set_lesmodel", "mglet_gpu_set_scalars", "mglet_gpu_timeintegrate_scalar",
     "mglet_gpu_set_buoyancy", "mglet_gpu_set_coriolis", "mglet_gpu_set_scalar_bc",
+    "mglet_gpu_add_scalar_source",
 ]
 
 
@@ -91,6 +92,7 @@ def load(path=None):
     L.mglet_gpu_set_buoyancy.argtypes = [vp, vp, C.c_double, C.c_int32]
     L.mglet_gpu_set_coriolis.argtypes = [vp, vp]
     L.mglet_gpu_set_scalar_bc.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, vp]
+    L.mglet_gpu_add_scalar_source.argtypes = [vp, C.c_int32, C.c_char_p, C.c_double]
     L.mglet_gpu_timeintegrate_scalar.argtypes = [vp, C.c_double, C.c_int32, vp]
     L.mglet_gpu_adjoint_rk_stage.argtypes = [vp, C.c_int32, C.c_double, vp]
     L.mglet_gpu_energy_gradient.argtypes = [vp, C.c_int32, C.c_int32, C.c_double, vp,
@@ -267,6 +269,9 @@ class Solver:
     def set_coriolis(self, omega):
         om = np.ascontiguousarray(omega, dtype=np.float64)
         _check(load().mglet_gpu_set_coriolis(self.h, om.ctypes.data_as(C.c_void_p)))
+
+    def add_scalar_source(self, isca, value, field=None):
+        _check(load().mglet_gpu_add_scalar_source(self.h, isca, field.encode() if field else None, value))
 
     def set_scalar_bc(self, igrid, iface, kind, types=()):
         ty = np.ascontiguousarray(list(types) + [0] * 9, dtype=np.int32)

@@ -69,6 +69,7 @@ def lib():
         _lib.oracle_set_buoyancy.argtypes = [vp, vp, C.c_double, C.c_int]
         _lib.oracle_set_coriolis.argtypes = [vp, vp]
         _lib.oracle_set_scalar_bc.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
+        _lib.oracle_add_scalar_source.argtypes = [vp, C.c_int, C.c_char_p, C.c_double]
         _lib.oracle_par_ftoc_norm.argtypes = [vp, C.c_int] + [C.c_char_p] * 3 + [C.c_int]
         _lib.oracle_ctof.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p]
         _lib.oracle_bound_pressure.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
@@ -255,6 +256,9 @@ class Oracle:
         g = np.ascontiguousarray(gravity, dtype=np.float64)
         self._g = g
         _check(lib().oracle_set_buoyancy(self.h, g.ctypes.data_as(C.c_void_p), beta, iscalar))
+
+    def add_scalar_source(self, isca, value, field=None):
+        _check(lib().oracle_add_scalar_source(self.h, isca, field.encode() if field else None, value))
 
     def set_scalar_bc(self, igrid, iface, kind, types=()):
         ty = np.ascontiguousarray(list(types) + [0] * 9, dtype=np.int32)

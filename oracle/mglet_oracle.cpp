@@ -153,8 +153,11 @@ struct Ctx {
     // number, the Kays/Crawford switch and a constant source
     struct ScalarDef {
         std::string name;
-        double prmol = 1.0, source = 0.0;
+        double prmol = 1.0;
         int kayscrawford = 0;
+        // the scalar's sources in order (sca%sources): an empty field name
+        // is sourceterm_const, else sourceterm_field of that field
+        std::vector<std::pair<std::string, double>> sources;
     };
     std::vector<ScalarDef> sca;
     double prturb = 1.0;
@@ -2348,6 +2351,8 @@ int timeintegrate_scalar(Ctx& c, double dt, int irk, const mglet_rk_scheme* rk) 
         }
         double* qtt = c.F("QTT");
         std::fill(c.f3["QTT"].begin(), c.f3["QTT"].end(), 0.0);
+        std::vector<const double*> srcf;
+        for (const auto& src : sd.sources) srcf.push_back(src.first.empty() ? nullptr : c.F(src.first.c_str()));
         for (int g = 1; g <= c.ngrid; ++g) {
             const Grid& G = c.g[g];
             const int kk = G.kk, jj = G.jj, ii = G.ii;
@@ -2362,7 +2367,10 @@ int timeintegrate_scalar(Ctx& c, double dt, int irk, const mglet_rk_scheme* rk) 
                         const double net = qtu[IX(k, j, i - 1)] - qtu[IX(k, j, i)] + qtv[IX(k, j - 1, i)] -
                                            qtv[IX(k, j, i)] + qtw[IX(k - 1, j, i)] - qtw[IX(k, j, i)];
                         double q = rddz[k] * rddy[j] * rddx[i] * net;
-                        if (sd.source != 0.0) q = q + sd.source;   // sourceterm_const
+                        // sourceterm (:549-634), the sources in order
+                        for (size_t s = 0; s < srcf.size(); ++s)
+                            q = srcf[s] ? q + sd.sources[s].second * srcf[s][o + IX(k, j, i)]
+                                        : q + sd.sources[s].second;
                         qtt[o + IX(k, j, i)] = q;
                     }
         }
@@ -4051,7 +4059,7 @@ int oracle_set_scalars(oracle_ctx* c, int nsca, const double* prmol, const int32
         sd.name = "T" + std::to_string(l + 1);
         sd.prmol = prmol[l];
         sd.kayscrawford = kayscrawford[l];
-        sd.source = source ? source[l] : 0.0;
+        if (source && source[l] != 0.0) sd.sources.push_back({"", source[l]});
         c->sca.push_back(sd);
         c->f3[sd.name].assign(c->idim3d, 0.0);
         c->f3["D" + sd.name].assign(c->idim3d, 0.0);
@@ -4060,6 +4068,16 @@ int oracle_set_scalars(oracle_ctx* c, int nsca, const double* prmol, const int32
     c->prturb = prturb;
     for (const char* n : {"QTU", "QTV", "QTW", "QTT", "BT"}) c->f3[n].assign(c->idim3d, 0.0);
     std::fill(c->f3["BT"].begin(), c->f3["BT"].end(), 1.0);   // blockbt: open everywhere (noib)
+    return 0;
+}
+
+int oracle_add_scalar_source(oracle_ctx* c, int isca, const char* field, double value) {
+    if (!c || isca < 1 || isca > (int)c->sca.size())
+        return fail(MGLET_ERR_ARG, "add_scalar_source: no such scalar");
+    const std::string f = field ? field : "";
+    if (!f.empty() && !c->f3.count(f)) return fail(MGLET_ERR_NAME, "add_scalar_source: unknown field");
+    if (c->sca[isca - 1].sources.size() >= 8) return fail(MGLET_ERR_ARG, "add_scalar_source: at most 8 sources");
+    c->sca[isca - 1].sources.push_back({f, value});
     return 0;
 }
 

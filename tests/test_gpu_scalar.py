@@ -144,3 +144,29 @@ def test_scalar_wall_model_with_les(gpu_lib, oracle_lib):
     for n in ("T1", "T2"):
         a, b = gs.get(n), o.get(n)
         assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), n
+
+
+def test_scalar_field_sources_bit_exact(gpu_lib, oracle_lib):
+    case = cases.periodic_box(2, 2, 1, n=8, length=(2.0, 2.0, 1.0))
+    gs, o = gpu_lib.Solver(case, _prm()), oracle_lib.Oracle(case, _prm())
+    rng = np.random.default_rng(17)
+    u, v, w, p = cases.taylor_green(case)
+    t1, t2 = rng.standard_normal(case.idim3d), rng.standard_normal(case.idim3d)
+    rk = oracle_lib.rk_scheme("williamson")
+    for s in (gs, o):
+        for n, a in zip("UVWP", (u, v, w, p)):
+            s.set(n, a)
+        s.connect(0, 2, "U", "V", "W", "P", corners=True)
+        s.set_scalars([0.71, 2.0], source=[0.05, 0.0])
+        s.set("T1", t1)
+        s.set("T2", t2)
+        s.connect(0, 2, s1="T1", s2="T2", corners=True)
+        s.add_scalar_source(1, -0.75, "T2")
+        s.add_scalar_source(1, 0.01)
+        s.add_scalar_source(2, 0.3, "P")
+    for irk in (1, 2, 3):
+        for s in (gs, o):
+            s.timeintegrate_scalar(5e-3, irk, rk)
+            s.timeintegrate_flow(1, 1, 0.0, 5e-3, irk, rk)
+    for n in ("T1", "T2", "DT1", "DT2"):
+        assert np.array_equal(gs.get(n), o.get(n)), n

@@ -157,3 +157,38 @@ def test_coriolis_turns_a_uniform_stream(oracle_lib):
     want = 1e-2 * rk.b[0] * (-2.0 * 0.25 * 1.5)
     assert np.allclose(case.interior(o.get("V")), want, rtol=1e-12, atol=0)
     assert np.allclose(case.interior(o.get("U")), 1.5, rtol=0, atol=1e-14)
+
+
+def test_sources_apply_in_order(oracle_lib):
+    """sourceterm (timeintegrate_scalar_mod.F90:549-634): a constant source
+    and value * field sources add to the balance in the order given; at rest
+    with a uniform scalar the first stage's DT is exactly that sum."""
+    case = cases.periodic_box(2, 1, 1, n=8, length=(2.0, 1.0, 1.0))
+    o = oracle_lib.Oracle(case, _prm())
+    o.set_scalars([0.7, 1.0], source=[0.25, 0.0])
+    rng = np.random.default_rng(9)
+    f = rng.standard_normal(case.idim3d)
+    o.set("T1", np.full(case.idim3d, 2.0))
+    o.set("T2", f)
+    o.add_scalar_source(1, -1.5, "T2")
+    o.add_scalar_source(1, 0.125)
+    rk = oracle_lib.rk_scheme("williamson")
+    o.timeintegrate_scalar(1e-2, 1, rk)
+    want = (0.0 + 0.25) + -1.5 * f
+    want = want + 0.125
+    assert np.array_equal(case.interior(o.get("DT1")), case.interior(want))
+    # a field of ones times c is the constant source c, bit for bit
+    a, b = (oracle_lib.Oracle(case, _prm()) for _ in range(2))
+    for s in (a, b):
+        s.set_scalars([0.7, 1.0])
+        s.set("T1", f)
+    a.add_scalar_source(1, 0.3)
+    b.set("T2", np.ones(case.idim3d))
+    b.add_scalar_source(1, 0.3, "T2")
+    for s in (a, b):
+        s.timeintegrate_scalar(1e-2, 1, rk)
+    assert np.array_equal(a.get("T1"), b.get("T1"))
+    with pytest.raises(RuntimeError):
+        o.add_scalar_source(3, 1.0)
+    with pytest.raises(RuntimeError):
+        o.add_scalar_source(1, 1.0, "NOPE")
