@@ -214,7 +214,8 @@ __global__ void __launch_bounds__(512) k_sipiter1_hp(SipArgs a) {
     const int n3dmax = (ii - 2) + (jj - 2) + (kk - 2);
     // (loading the next plane's values ahead of the barrier, as sipiter2
     // does, measured slower here: 2.2 against 1.44 ms on 4096 x 24^3 grids,
-    // at three and at four CTAs per SM)
+    // at three and at four CTAs per SM; so did CTAs of 256 or 1024 threads,
+    // 2.08 and 2.05 ms)
     for (int m = 9; m <= n3dmax; ++m) {
         const int lm = mip[m], lp = mip[m + 1] - lm;
         for (int ip = threadIdx.x; ip < lp; ip += blockDim.x) {
