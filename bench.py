@@ -45,7 +45,7 @@ UNIT = "cell-updates/s"
 PLAIN_BYTES = {
     "tstle4": 8 * (5 + 3),          # read u,v,w,p,g; write uo,vo,wo
     "rkstep": 8 * 4,                # read p,dp,rhs; write p,dp (per component) / 1.25 ~ 4+1
-    "laplacephi": 8 * 4,            # read phi, ap, bp; write res
+    "laplacephi": 8 * 3,            # read phi, ap; write res (bp is skipped where it is 1.0)
     "sipiter1": 8 * 7,              # read rhs, res, lw, ls, lb, lpr; write res
     "sipiter2": 8 * 7,              # read res, ue, un, ut, phi; write res, phi
     "divcal": 8 * 4,                # read u, v, w; write rhs
@@ -62,9 +62,9 @@ MIXED_BYTES = {
 
 
 # DRAM bytes per interior cell and launch measured by ncu (dram__bytes over one
-# launch on 1024 grids of 24^3, profiles/mixed_kernels_1024x24c.md), scaled to
-# the bench case by the number of cells; on 1024 grids part of the working set
-# stays in L2, so these are lower bounds for the full-size launch.
+# launch on 1024 grids of 24^3), scaled to the bench case by the number of
+# cells; on 1024 grids part of the working set stays in L2, so these are lower
+# bounds for the full-size launch.
 NCU_TRAFFIC_PER_CELL = {
     "mx_sip_fwd": 94.6e6 / (1024 * 13824),
     "mx_sip_bwd": 127.6e6 / (1024 * 13824),
@@ -72,6 +72,14 @@ NCU_TRAFFIC_PER_CELL = {
     "mx_outer": 476.1e6 / (1024 * 13824),
     "mx_flux": 1540.8e6 / (1024 * 13824),
 }
+
+
+# FP64 thread instructions (DADD, DMUL, DFMA and the conversions the FP64 pipe
+# issues) per interior cell and launch of the plain FP64 kernels, measured by
+# ncu (sm__inst_executed_pipe_fp64 x 32 over one launch on 1024 grids of 24^3,
+# parity build without FMA contraction); with the measured FP64 issue rate
+# they give each kernel's fraction of the second roof.
+FP64_INSTR_PER_CELL = {}
 
 
 def kernel_bytes(name, case, ninner):
@@ -380,6 +388,34 @@ def roofline(kern, case, ninner, prof_ms):
             "algorithmic_bytes_per_launch": b, "avg_launch_ms": tot / n}
 
 
+def kernel_roofs(kern, case, ninner, fp64=None):
+    """Per kernel family: average launch time, algorithmic bytes and flops
+    per launch, the fraction of the measured HBM bandwidth and, for the FP64
+    kernels with a known instruction count, the fraction of the measured FP64
+    issue rate; "bound" names the larger of the two."""
+    peak, _ = measured_peaks()
+    out = {}
+    for name, (tot, n) in kern.items():
+        if not n:
+            continue
+        ms = tot / n
+        row = {"avg_launch_ms": ms, "launches": n}
+        b = kernel_bytes(name, case, ninner)
+        if b:
+            row["bytes_per_launch"] = b
+            row["hbm_frac"] = b / (ms / 1e3) / 1e9 / peak
+        ipc = FP64_INSTR_PER_CELL.get(name)
+        if ipc and fp64:
+            rate = ipc * case.ncells / (ms / 1e3)
+            row["fp64_instr_per_cell"] = ipc
+            row["fp64_frac"] = rate / fp64["dfma"]
+        if "hbm_frac" in row or "fp64_frac" in row:
+            row["bound"] = ("fp64" if row.get("fp64_frac", 0) > row.get("hbm_frac", 0)
+                            else "hbm")
+        out[name] = row
+    return out
+
+
 def run_ours(args, rank, world, local):
     import torch
 
@@ -391,6 +427,8 @@ def run_ours(args, rank, world, local):
     case = make_case(args)
     fields = init_fields(case)
     prof = not args.no_profile
+    from mglet_gb300 import gpu
+    fp64 = gpu.fp64_roof(local)
     r = time_form(args, args.form, case, fields, local, dist, profile=prof)
     s = r["solver"]
     ms = r["ms"]
@@ -405,7 +443,7 @@ def run_ours(args, rank, world, local):
         host = [torch.empty(n, dtype=torch.float64, pin_memory=True) for _ in range(4)]
         for h, a in zip(host, fields):
             h.copy_(torch.from_numpy(a))
-        ksteps = max(1, min(args.steps, 3))
+        ksteps = args.steps
         s.synchronize()
         t0 = time.perf_counter()
         for _ in range(ksteps):
@@ -429,6 +467,7 @@ def run_ours(args, rank, world, local):
         plain = {"value": pv, "unit": UNIT, "ms_per_step": q["ms"] / args.steps,
                  "gpu_launches": q["launches"], "clocks": q["clocks"],
                  "roofline": roofline(q["kern"], case, q["prm"].ninner, q["prof_ms"]),
+                 "kernel_roofs": kernel_roofs(q["kern"], case, q["prm"].ninner, fp64),
                  "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]}
                                 for k, v in q["kern"].items()},
                  "mixed_over_plain": value / pv}
@@ -464,6 +503,10 @@ def run_ours(args, rank, world, local):
             "gpu_launches": r["launches"],
             "roofline": roof,
             "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in r["kern"].items()},
+            "kernel_roofs": kernel_roofs(r["kern"], case, r["prm"].ninner, fp64),
+            "fp64_roof": {"dfma_per_s": fp64["dfma"], "dadd_per_s": fp64["dadd"],
+                          "dmul_per_s": fp64["dmul"], "tflops_fma": 2 * fp64["dfma"] / 1e12,
+                          "how": "independent FP64 chains on every SM, CUDA events, best of 5"},
             "plain_fp64": plain,
             "cpu_baseline": cpu,
         }

@@ -395,12 +395,24 @@ int mglet_gpu_itinfo(mglet_ctx* ctx, double dt, mglet_itinfo* out);
  * MGLET_ERR_SIZE.  The first call on a device looks up the array's device
  * address (cudaGetSymbolAddress) with that device current; make that first
  * call before any stream capture.  All calls share the one array, so calls
- * that overlap on the GPU (different streams, no ordering) race. */
+ * that overlap on the GPU (different streams, no ordering) race.
+ * Unlike the reference's compdivmax (ABS(div) > divmax skips a NaN) and
+ * unlike mglet_gpu_itinfo (which reports MGLET_ERR_EXPLODED), a NaN in the
+ * interior divergence propagates: *divmax becomes NaN and the call still
+ * returns 0, so a caller detects an exploded field by testing the result
+ * for NaN. */
 #define MGLET_NOALLOC_MAX_GRIDS 65536
 int mglet_gpu_divmax_noalloc(const double* u, const double* v, const double* w, int32_t ngrid,
                              int32_t kk, int32_t jj, int32_t ii, const double* rddx,
                              const double* rddy, const double* rddz, double* divmax,
                              void* stream);
+
+/* ---- Device roofs (no counterpart in the reference) ------------------------
+ * The measured FP64 issue rate of device: out[0] DFMA, out[1] DADD, out[2]
+ * DMUL thread instructions per second over the whole GPU (one DFMA = two
+ * flops), each from independent dependent chains on every SM, timed with
+ * CUDA events (best of five).  The second roof of the FP64 parity form. */
+int mglet_gpu_fp64_roof(int32_t device, double* out);
 
 /* ---- Misc ----------------------------------------------------------------- */
 int mglet_gpu_synchronize(mglet_ctx* ctx);

@@ -20,7 +20,6 @@
 //    one CUDA graph with no host round trip (the reference's
 //    MPI_Allreduce + host test per outer iteration).
 #include <algorithm>
-#include <array>
 #include <cstring>
 #include <map>
 #include <vector>
@@ -31,7 +30,7 @@
 namespace mg {
 
 int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
-                   const float* sz, double frhs, double dtfu);
+                   const float* sz, const double* sprm);
 int mx_flux_prepare(Ctx* c);
 
 struct MixedState {
@@ -51,14 +50,17 @@ struct MixedState {
     bool g_uniform = true;
     // device control block: [0] converged flag, [1] outer iterations done
     int* d_ctl = nullptr;
+    // stage scalars read by the kernels from device memory, so that one
+    // captured graph serves every stage and every time step size:
+    // [0] frhs, [1] dt*fu, [2] prefak = rho/dt of the solve, [3] dt/rho
+    double* d_sprm = nullptr;
     double* d_maxrhs = nullptr;
     int* h_ctl = nullptr;           // pinned mirrors
     double* h_maxrhs = nullptr;
-    // graph cache: (irk, dt, frhs, fu, dtrk bit patterns) -> executable graph
-    // of the whole stage, and the number of kernels inside it
-    using GraphKey = std::array<unsigned long long, 5>;
-    std::map<GraphKey, cudaGraphExec_t> graphs;
-    std::map<GraphKey, long long> graph_launches;
+    // the whole stage captured once as a graph (its scalars come from
+    // d_sprm), and the number of kernels inside it
+    cudaGraphExec_t graph = nullptr;
+    long long graph_launches = 0;
 };
 
 namespace {
@@ -80,8 +82,9 @@ __device__ __forceinline__ double block_max_d(double v, double* sh) {
 // (pressuresolver_mod.F90:275,294-301), on the device.
 __global__ void k_mx_conv(const DevGrid* __restrict__ grids, int ngrid, int maxlevel,
                           const double* __restrict__ gridmax, int* ctl, double* maxrhs,
-                          double prefak, double epcorr, int nouter_min) {
+                          const double* __restrict__ sprm, double epcorr, int nouter_min) {
     if (ctl[0]) return;
+    const double prefak = sprm[2];
     __shared__ double sh[32];
     double m = 0.0;
     for (int g = threadIdx.x; g < ngrid; g += blockDim.x)
@@ -102,8 +105,9 @@ __global__ void k_mx_conv(const DevGrid* __restrict__ grids, int ngrid, int maxl
 __global__ void k_mx_mgpcorr(const DevGrid* __restrict__ grids, double* U, double* V, double* W,
                              double* P, const double* __restrict__ DP, const double* __restrict__ RDX,
                              const double* __restrict__ RDY, const double* __restrict__ RDZ,
-                             double rfak) {
+                             const double* __restrict__ sprm) {
     const DevGrid G = grids[blockIdx.y];
+    const double rfak = sprm[3];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int ni = ii - 4, nj = jj - 4, nk = kk - 4;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -119,6 +123,13 @@ __global__ void k_mx_mgpcorr(const DevGrid* __restrict__ grids, double* U, doubl
     W[o + c] = W[o + c] + (d - dp[c + 1]) * RDZ[G.ipz + k - 1] * rfak;
 }
 
+__global__ void k_mx_setprm(double* sprm, double frhs, double dtfu, double prefak, double rfak) {
+    sprm[0] = frhs;
+    sprm[1] = dtfu;
+    sprm[2] = prefak;
+    sprm[3] = rfak;
+}
+
 __global__ void k_cvt_64_32(float* d, const double* s, long long n) {
     long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < n) d[t] = (float)s[t];
@@ -132,16 +143,16 @@ __global__ void k_cvt_32_64(double* d, const float* s, long long n) {
 // The reference's inner-iteration halo semantics mapped onto the rotating
 // res slots: iteration G (1-based within one mgpoisl) writes slot G%3;
 // its forward sweep reads low ghosts written by the last iteration whose
-// conn(res) exchanged all faces (inner index < ninner), or zeros.
-int enqueue_mgpoisl(Ctx* c, double dt) {
+// conn(res) exchanged all faces (inner index < ninner), or zeros.  The
+// solve's prefak and dt/rho come from the stage scalars (d_sprm).
+int enqueue_mgpoisl(Ctx* c) {
     MixedState* m = c->mx;
     SipState& s = m->sip;
-    const double prefak = c->prm.rho / dt;
     double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P"), *dp = c->F("DP");
     MG_CUDA(cudaMemsetAsync(s.dph, 0, (size_t)c->ngrid * s.npp * sizeof(float), c->stream));
     MG_CUDA(cudaMemsetAsync(s.dpl, 0, (size_t)c->ngrid * s.npp * sizeof(float), c->stream));
     MG_CUDA(cudaMemsetAsync(m->d_ctl, 0, 3 * sizeof(int), c->stream));
-    if (int rc = sip_divcal(c, s, prefak)) return rc;
+    if (int rc = sip_divcal(c, s, m->d_sprm + 2)) return rc;
     int* ctl = m->d_ctl;
     const int ninner = c->prm.ninner;
     int gi = 0, lastfull = 0;
@@ -158,7 +169,7 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
         {
             ProfScope ps_(c, "mx_conv");
             k_mx_conv<<<1, 1024, 0, c->stream>>>(c->d_grids, c->ngrid, c->maxlevel, c->d_gridred,
-                                                 m->d_ctl, m->d_maxrhs, prefak, c->prm.epcorr,
+                                                 m->d_ctl, m->d_maxrhs, m->d_sprm, c->prm.epcorr,
                                                  c->prm.nouter_min);
             MG_LAUNCHED(c);
         }
@@ -171,7 +182,7 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
         ProfScope ps_(c, "mx_mgpcorr");
         dim3 grid((s.npts + 255) / 256, c->ngrid);
         k_mx_mgpcorr<<<grid, 256, 0, c->stream>>>(c->d_grids, U, V, W, P, dp, c->L("RDX"),
-                                                  c->L("RDY"), c->L("RDZ"), dt / c->prm.rho);
+                                                  c->L("RDY"), c->L("RDZ"), m->d_sprm);
         MG_LAUNCHED(c);
     }
     if (int rc = connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
@@ -181,20 +192,27 @@ int enqueue_mgpoisl(Ctx* c, double dt) {
     return 0;
 }
 
-int enqueue_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) {
-    double frhs, fu, dtrk, dtrki;
-    if (int rc = rk_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki)) return rc;
+// The stage's scalars into d_sprm (a one-thread kernel on the stream, so the
+// values are fixed at launch and need no host buffer that outlives the call).
+int set_stage_scalars(Ctx* c, double frhs, double dtfu, double dtsolve) {
+    k_mx_setprm<<<1, 1, 0, c->stream>>>(c->mx->d_sprm, frhs, dtfu, c->prm.rho / dtsolve,
+                                        dtsolve / c->prm.rho);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int enqueue_stage(Ctx* c) {
     MixedState* m = c->mx;
     if (!m->g_uniform) {
         set_error("mixed form: needs a uniform viscosity field G = gmol (no LES model)");
         return MGLET_ERR_UNSUPPORTED;
     }
-    if (int rc = launch_mx_flux(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, frhs, dt * fu))
+    if (int rc = launch_mx_flux(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, m->d_sprm))
         return rc;
     if (int rc = connect(c, 0, 1, c->F("U"), c->F("V"), c->F("W"), nullptr, nullptr, nullptr, false,
                          true, 1))
         return rc;
-    return enqueue_mgpoisl(c, dtrk * dt);
+    return enqueue_mgpoisl(c);
 }
 
 // 0, or MGLET_ERR_CUDA when a wavefront kernel gave up waiting for its
@@ -308,6 +326,8 @@ int mixed_init(Ctx* c) {
     MG_CUDA(cudaMalloc(&m->d_ctl, 4 * sizeof(int)));
     MG_CUDA(zero_on(c->stream, m->d_ctl, 4 * sizeof(int)));
     MG_CUDA(cudaMalloc(&m->d_maxrhs, sizeof(double)));
+    MG_CUDA(cudaMalloc(&m->d_sprm, 4 * sizeof(double)));
+    MG_CUDA(zero_on(c->stream, m->d_sprm, 4 * sizeof(double)));
     MG_CUDA(cudaMallocHost(&m->h_ctl, 4 * sizeof(int)));
     MG_CUDA(cudaMallocHost(&m->h_maxrhs, sizeof(double)));
     // every connect variant the stage issues, built before any graph capture
@@ -334,10 +354,10 @@ int mixed_init(Ctx* c) {
 void mixed_release(Ctx* c) {
     MixedState* m = c->mx;
     if (!m) return;
-    for (auto& kv : m->graphs) cudaGraphExecDestroy(kv.second);
+    if (m->graph) cudaGraphExecDestroy(m->graph);
     sip_release(m->sip);
     for (void* p : {(void*)m->cf, (void*)m->cb, (void*)m->apx, (void*)m->d_gcls,
-                    (void*)m->d_ctl, (void*)m->d_maxrhs, (void*)m->du32, (void*)m->dv32,
+                    (void*)m->d_ctl, (void*)m->d_maxrhs, (void*)m->d_sprm, (void*)m->du32, (void*)m->dv32,
                     (void*)m->dw32, (void*)m->sx, (void*)m->sy, (void*)m->sz})
         cudaFree(p);
     if (m->h_ctl) cudaFreeHost(m->h_ctl);
@@ -366,32 +386,35 @@ void mixed_field_sync_out(Ctx* c, const char* name) {
 }
 
 int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st) {
-    if (int rc = enqueue_mgpoisl(c, dt)) return rc;
+    // frhs and dt*fu are not read by the solve
+    if (int rc = set_stage_scalars(c, 0.0, 0.0, dt)) return rc;
+    if (int rc = enqueue_mgpoisl(c)) return rc;
     MG_CUDA(cudaStreamSynchronize(c->stream));
     fill_stats(c, dt, st);
     return check_device_flag(c);
 }
 
-// One stage: captured once per (irk, dt) into a CUDA graph and replayed; with
+// One stage: its scalars go to d_sprm, then the stage graph (captured on the
+// first call, the same for every stage and time step size) is replayed; with
 // per-kernel profiling enabled the stage is issued eagerly so that every
 // launch is bracketed by its events.
 int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st) {
     MixedState* m = c->mx;
     double frhs, fu, dtrk, dtrki;
     if (int rc = rk_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki)) return rc;
+    if (!m->g_uniform) {
+        set_error("mixed form: needs a uniform viscosity field G = gmol (no LES model)");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    if (int rc = set_stage_scalars(c, frhs, dt * fu, dtrk * dt)) return rc;
     if (c->prof) {
-        if (int rc = enqueue_stage(c, dt, irk, rk)) return rc;
+        if (int rc = enqueue_stage(c)) return rc;
     } else {
-        MixedState::GraphKey k;
-        const double vals[4] = {dt, frhs, fu, dtrk};
-        k[0] = (unsigned long long)irk;
-        for (int q = 0; q < 4; ++q) std::memcpy(&k[q + 1], &vals[q], sizeof(double));
-        auto it = m->graphs.find(k);
-        if (it == m->graphs.end()) {
+        if (!m->graph) {
             cudaGraph_t g;
             const long long l0 = c->launches;
             MG_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            int rc = enqueue_stage(c, dt, irk, rk);
+            int rc = enqueue_stage(c);
             cudaError_t e = cudaStreamEndCapture(c->stream, &g);
             if (rc) return rc;
             if (e != cudaSuccess) return cuda_fail(e, "graph capture");
@@ -399,12 +422,12 @@ int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_sta
             e = cudaGraphInstantiate(&ex, g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return cuda_fail(e, "graph instantiate");
-            it = m->graphs.emplace(k, ex).first;
-            m->graph_launches[k] = c->launches - l0;
+            m->graph = ex;
+            m->graph_launches = c->launches - l0;
             c->launches = l0;
         }
-        MG_CUDA(cudaGraphLaunch(it->second, c->stream));
-        c->launches += m->graph_launches[k];
+        MG_CUDA(cudaGraphLaunch(m->graph, c->stream));
+        c->launches += m->graph_launches;
     }
     if (st) {
         MG_CUDA(cudaStreamSynchronize(c->stream));

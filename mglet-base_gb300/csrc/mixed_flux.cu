@@ -67,7 +67,7 @@ struct FluxArgs {
     float g, gh;                       // uniform face viscosities (ge=gw, gn.. harmonic sum)
     float rrho;
     float gpx, gpy, gpz;
-    double frhs, dtfu;
+    const double* sprm;                // [0] frhs, [1] dt*fu (device)
     int nslab;                         // j-slabs (CTAs) per grid
 };
 
@@ -272,11 +272,12 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
         if (i + 2 <= ii - 1) load_plane(i + 2, (i + 2) % 3, (i + 2) % 2, true, unx2, vnx2, wnx2);
         if (on) {
             const long long c = o + (long long)(i - 1) * kj + (long long)(j - 1) * kk + (k - 1);
-            const float du = (float)a.frhs * a.DU[c] + uo;
-            const float dv = (float)a.frhs * a.DV[c] + vo;
-            const float dw = (float)a.frhs * a.DW[c] + wo;
+            const float frhs = (float)a.sprm[0];
+            const float du = frhs * a.DU[c] + uo;
+            const float dv = frhs * a.DV[c] + vo;
+            const float dw = frhs * a.DW[c] + wo;
             a.DU[c] = du; a.DV[c] = dv; a.DW[c] = dw;
-            const float fdt = (float)a.dtfu;
+            const float fdt = (float)a.sprm[1];
             a.U[c] = ucur + (double)(fdt * du);
             a.V[c] = vcur + (double)(fdt * dv);
             a.W[c] = wcur + (double)(fdt * dw);
@@ -321,7 +322,7 @@ int mx_flux_prepare(Ctx* c) {
 }
 
 int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
-                   const float* sz, double frhs, double dtfu) {
+                   const float* sz, const double* sprm) {
     ProfScope ps_(c, "mx_flux");
     const DevGrid& G0 = c->grids[0];
     const size_t smem = flux_smem(G0);
@@ -342,8 +343,7 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
     a.gh = (float)(h0 + h0);
     a.rrho = (float)(1.0 / c->prm.rho);
     a.gpx = (float)c->prm.gradp[0]; a.gpy = (float)c->prm.gradp[1]; a.gpz = (float)c->prm.gradp[2];
-    a.frhs = frhs;
-    a.dtfu = dtfu;
+    a.sprm = sprm;
     k_mx_flux<<<c->ngrid * nslab, threads, smem, c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;

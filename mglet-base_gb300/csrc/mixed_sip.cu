@@ -871,7 +871,7 @@ __global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const i
                              const double* __restrict__ U, const double* __restrict__ V,
                              const double* __restrict__ W, const double* __restrict__ RDDX,
                              const double* __restrict__ RDDY, const double* __restrict__ RDDZ,
-                             double fak) {
+                             const double* __restrict__ pfak) {
     const int g = blockIdx.y;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= npp) return;
@@ -886,6 +886,7 @@ __global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const i
     const int kk = G.kk, jj = G.jj;
     const int k = id % kk + 1, j = (id / kk) % jj + 1, i = id / (kk * jj) + 1;
     const double *u = U + G.ip3, *v = V + G.ip3, *w = W + G.ip3;
+    const double fak = *pfak;
     const double d = fak * ((u[id] - u[id - kk * jj]) * RDDX[G.ipx + i - 1] +
                             (v[id] - v[id - kk]) * RDDY[G.ipy + j - 1] +
                             (w[id] - w[id - 1]) * RDDZ[G.ipz + k - 1]);
@@ -1263,7 +1264,7 @@ void sip_release(SipState& st) {
         cudaFree(p);
 }
 
-int sip_divcal(Ctx* c, SipState& st, double fak) {
+int sip_divcal(Ctx* c, SipState& st, const double* fak) {
     ProfScope ps_(c, "mx_divcal");
     dim3 grid((st.npp + 255) / 256, c->ngrid);
     k_sip_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.rhs32, st.rhsl,

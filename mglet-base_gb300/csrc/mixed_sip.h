@@ -53,7 +53,8 @@ int sip_init(Ctx* c, SipState& st);
 int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* d_idx,
                 bool planeorder, float** cf, float** cb, float** apx);
 void sip_release(SipState& st);
-int sip_divcal(Ctx* c, SipState& st, double fak);
+// fak (the solve's prefak) is read from device memory
+int sip_divcal(Ctx* c, SipState& st, const double* fak);
 int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
                 int rwrite, bool hzero);
 int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ctl, int rhi,

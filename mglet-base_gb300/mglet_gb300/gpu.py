@@ -33,7 +33,7 @@ EXPORTS = [
     "mglet_gpu_set_body_force", "mglet_gpu_adjoint_rk_stage", "mglet_gpu_energy_gradient",
     "mglet_gpu_set_lesmodel", "mglet_gpu_set_scalars", "mglet_gpu_timeintegrate_scalar",
     "mglet_gpu_set_buoyancy", "mglet_gpu_set_coriolis", "mglet_gpu_set_scalar_bc",
-    "mglet_gpu_add_scalar_source",
+    "mglet_gpu_add_scalar_source", "mglet_gpu_fp64_roof",
 ]
 
 
@@ -112,8 +112,17 @@ def load(path=None):
     L.mglet_gpu_profile_names.argtypes = [vp, cp, C.c_int64]
     L.mglet_gpu_divmax_noalloc.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, C.c_int32,
                                            C.c_int32, vp, vp, vp, vp, vp]
+    L.mglet_gpu_fp64_roof.argtypes = [C.c_int32, C.POINTER(C.c_double)]
     _lib = L
     return L
+
+
+def fp64_roof(device=0):
+    """Measured FP64 issue rates of the device (thread instructions per
+    second): {"dfma": .., "dadd": .., "dmul": ..}."""
+    out = (C.c_double * 3)()
+    _check(load().mglet_gpu_fp64_roof(device, out))
+    return {"dfma": out[0], "dadd": out[1], "dmul": out[2]}
 
 
 def _check(rc):

@@ -103,6 +103,32 @@ def test_graph_replay_matches_eager(gpu_lib):
         assert np.array_equal(a, b)
 
 
+def test_graph_serves_changing_dt(gpu_lib):
+    """A time step size that changes every step (as targetcflmax does,
+    timeloop_mod.F90:105-121) replays the one captured stage graph: the
+    stage scalars come from device memory, so the result equals eager issue
+    bit for bit and every stage launches the same number of kernels."""
+    case = cases.periodic_box(2, 2, 1, n=24)
+    out, per_stage = [], []
+    dts = [5e-4, 4.3e-4, 6.1e-4, 5.7e-4]
+    for profile in (False, True):
+        g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=9))
+        _init(g, case)
+        g.profile(profile)
+        rk = gpu_lib.rk_scheme("williamson")
+        counts = []
+        for it, dt in enumerate(dts, start=1):
+            for irk in range(1, 4):
+                n0 = g.launches
+                g.timeintegrate_flow(it, it, 0.0, dt, irk, rk)
+                counts.append(g.launches - n0)
+        out.append([g.get(nm) for nm in "UVWP"])
+        per_stage.append(counts)
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
+    assert len(set(per_stage[0])) == 1, per_stage[0]
+
+
 def test_mixed_matches_plain_gpu(gpu_lib):
     """Mixed against the plain FP64 GPU form on the 4-grid 24^3 tiling."""
     case = cases.periodic_box(2, 2, 1, n=24)
