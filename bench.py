@@ -18,6 +18,7 @@ same number of steps (per-launch CUDA events on the solver's stream).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|plain]
   python bench.py --impl reference   # the CPU restatement on the host cores
+  python bench.py --sphere [--sphere-check]   # multi-level ghost-cell case
   python bench.py --precision [--tiles 8 8 8] [--steps 200]
       # mixed form against the plain FP64 form (bit-identical to the CPU
       # restatement) from a solenoidal random field: relative L2 error of
@@ -130,6 +131,12 @@ def parse():
     ap.add_argument("--adjoint", action="store_true",
                     help="dJ/df of the final kinetic energy by the discrete adjoint, timed, with a "
                          "finite-difference check")
+    ap.add_argument("--sphere", action="store_true",
+                    help="the multi-level ghost-cell case: a sphere in a channel, 16x8x8 level-1 "
+                         "grids of 24^3 and two refinement levels (plain FP64 form)")
+    ap.add_argument("--sphere-check", action="store_true",
+                    help="with --sphere: one RK stage of the full case on the GPU and on the CPU "
+                         "restatement, compared bit for bit")
     ap.add_argument("--fd-dirs", type=int, default=20,
                     help="random directions of the adjoint's finite-difference check")
     return ap.parse_args()
@@ -660,6 +667,107 @@ def run_adjoint(args, rank, local):
     return 0
 
 
+def run_sphere(args, rank, local):
+    """The sphere in a channel, 8D x 4D x 4D: level 1 = 16 x 8 x 8 grids of
+    24^3, levels 2 and 3 refined around the sphere (1024 + 704 + 2112
+    grids, 53.1 M cells), the ghost-cell IB built from the sphere's signed
+    distance, FIX inflow u = 1, OP1 outflow, periodic in y and z, Re_D = 300,
+    dt of CFL 0.5 on the finest level, Williamson RK3, SIP ninner = 5,
+    nouter = 9, epcorr = 1e-10; plain FP64 form (the mixed form runs one
+    level).  Steps timed with CUDA events on the solver's stream."""
+    import numpy as np
+    import torch
+    from mglet_gb300 import channel, gpu
+
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    sc = channel.SphereChannel()
+    case = sc.case
+    lists = sc.lists
+    t_setup = time.perf_counter() - t0
+    prm = sc.flow_params(epcorr=1e-10, nouter=9, ninner=5)
+    dt = sc.dt(0.5)
+    s = gpu.Solver(case, prm, device=local)
+    sc.setup(s)
+    rk = gpu.rk_scheme("williamson")
+    stream = torch.cuda.ExternalStream(s.stream, device=local)
+    state = {"it": 0}
+
+    def step():
+        state["it"] += 1
+        st = None
+        for irk in range(1, 4):
+            st = s.timeintegrate_flow(state["it"], state["it"], 0.0, dt, irk, rk)
+        return st
+
+    for _ in range(args.warmup):
+        step()
+    s.synchronize()
+    clocks = Clocks(local)
+    torch.cuda.synchronize()
+    l0 = s.launches
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks.start()
+    ipcs = []
+    e0.record(stream)
+    for _ in range(args.steps):
+        ipcs.append(step().ipc)
+    e1.record(stream)
+    e1.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    launches = s.launches - l0
+    info = s.itinfo(dt)
+    s.profile(True)
+    for _ in range(max(1, min(args.steps, 2))):
+        step()
+    s.synchronize()
+    kern = {name: s.profile_get(name) for name in s.profile_names()}
+    s.profile(False)
+    s.close()
+    value = case.ncells * args.steps / (ms / 1e3)
+    check = None
+    if args.sphere_check:
+        from oracle import binding
+        binding.build()
+        prm1 = sc.flow_params(epcorr=1e-10, nouter=9, ninner=5, nouter_min=9)
+        g1 = gpu.Solver(case, prm1, device=local)
+        o = binding.Oracle(case, prm1)
+        tc = time.perf_counter()
+        for x in (g1, o):
+            sc.setup(x)
+        sg = g1.timeintegrate_flow(1, 1, 0.0, dt, 1, rk)
+        so = o.timeintegrate_flow(1, 1, 0.0, dt, 1, binding.rk_scheme("williamson"))
+        eq = {n: bool(np.array_equal(g1.get(n), o.get(n))) for n in ("U", "V", "W", "P")}
+        check = {"stage": 1, "bit_exact": eq, "ipc": [sg.ipc, so.ipc],
+                 "maxrhs": [sg.maxrhs, so.maxrhs], "seconds": time.perf_counter() - tc}
+        g1.close()
+    levels = [int((case.level == lv).sum()) for lv in (1, 2, 3)]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: uniform inflow past a sphere given by its signed distance",
+        "config": {"workload": f"sphere channel 8D x 4D x 4D, {levels[0]}+{levels[1]}+{levels[2]} "
+                               f"grids of 24^3 on 3 levels ({case.ncells} cells), ghost-cell IB, "
+                               "FIX inflow, OP1 outflow, Re_D=300, CFL 0.5, RK3, SIP ninner=5 "
+                               "nouter=9 epcorr=1e-10",
+                   "form": "plain", "cells": case.ncells, "grids_per_level": levels,
+                   "ghost_cell_entries": int(sum(gl[1][0] + gl[2][0] + gl[3][0] for gl in lists)),
+                   "intersected_cells": int(sc.geo["icells"].sum()), "dt": dt,
+                   "setup_s": t_setup, "ipc_per_stage_last": ipcs[-1] if ipcs else None,
+                   "l2": "working set > L2 (no flush needed)"},
+        "clocks": clk, "gpu_launches": launches,
+        "itinfo": {"cflmax": info.cflmax, "divmax": info.divmax, "energy": info.energy},
+        "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
+        "oracle_check": check,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -669,6 +777,10 @@ def main():
         if args.tiles == [16, 16, 16]:
             args.tiles = [8, 8, 8]
         return run_adjoint(args, rank, local)
+    if args.sphere:
+        if args.tiles != [16, 16, 16]:
+            raise SystemExit("--sphere runs the full configuration only")
+        return run_sphere(args, rank, local)
     if args.precision:
         if args.steps == 5:
             args.steps = 200

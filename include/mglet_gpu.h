@@ -363,6 +363,38 @@ int mglet_gpu_set_stencils(mglet_ctx* ctx, int32_t igrid, int32_t comp, int32_t 
  * lists go to the device and SDIV is built (setsdivfield,
  * gc_flowstencils_mod.F90:1488-1535).  Plain form only. */
 int mglet_gpu_set_ghostcell(mglet_ctx* ctx);
+/* ---- Ghost-cell stencil construction (host only, no device needed) -------
+ * Replaces create_flowstencils (src/flow/gc_flowstencils_mod.F90:37-100):
+ * from the blocking of every grid it builds the lists mglet_gpu_set_stencils
+ * takes -- fluxcorrection (:199-553) for component 4 and fluxstencil /
+ * calcflux (:556-752,838-920) for u, v, w.  The geometry arrays are what the
+ * reference's blocking leaves in its fields (gc_blockbp_mod.F90:41-271):
+ * all idim3d-sized arrays in field_t layout, BP/BU/BV/BW 1 open, 0 blocked,
+ * AREAU/AREAV/AREAW the open area of the face at i+1/2 (j+1/2, k+1/2);
+ * BZELLTYP negative, -(n), at the n-th intersected cell of its grid (1-based),
+ * non-negative elsewhere; icells[g] the intersected cells of grid g+1; per
+ * intersected cell, grid after grid, nvecs = the plane a x + b y + c z = dpl
+ * of the body surface (unit normal pointing into the fluid) and ucell = the
+ * body velocity.  Spacing comes from desc (x, dx give xstag = x + dx/2). */
+typedef struct mglet_ib_geometry {
+    const double *bp, *bu, *bv, *bw;
+    const double *areau, *areav, *areaw;
+    const int32_t* bzelltyp;
+    const int32_t* icells;    /* [ngrid] */
+    const double* nvecs;      /* [sum icells][4]: a, b, c, dpl */
+    const double* ucell;      /* [sum icells][3] */
+} mglet_ib_geometry;
+typedef struct mglet_flowstencils mglet_flowstencils;
+int mglet_create_flowstencils(const mglet_grid_desc* desc, const mglet_ib_geometry* geo,
+                              mglet_flowstencils** out);
+/* Sizes of the lists of grid igrid (1-based), component comp (1..4): the
+ * entry count and the lengths of xpoli and of xpolr (= xpolrvel for 1..3). */
+int mglet_flowstencils_size(const mglet_flowstencils* s, int32_t igrid, int32_t comp,
+                            int32_t* ncells, int64_t* nxi, int64_t* nxr);
+/* Copies them out (xpolrvel NULL for component 4). */
+int mglet_flowstencils_copy(const mglet_flowstencils* s, int32_t igrid, int32_t comp,
+                            int64_t* xpoli, double* xpolr, double* xpolrvel);
+int mglet_flowstencils_free(mglet_flowstencils* s);
 /* setibvalues(u, v, w), getibvalues(u, v, w) and setpointvalues(pwu, pwv,
  * pww, u, v, w, comp_new) (gc_flowstencils_mod.F90:1323-1453), maskbp(u, v,
  * w, p) (src/flow/timeintegration_mod.F90:255-303) on the device fields. */
@@ -413,6 +445,18 @@ int mglet_gpu_divmax_noalloc(const double* u, const double* v, const double* w, 
  * flops), each from independent dependent chains on every SM, timed with
  * CUDA events (best of five).  The second roof of the FP64 parity form. */
 int mglet_gpu_fp64_roof(int32_t device, double* out);
+
+/* ---- Launch tuning of the mixed form (no counterpart in the reference) -----
+ * mglet_gpu_create times the launch variants of the mixed form's pre-pass
+ * (points loaded ahead, CTAs per SM, and the uniform-coefficient variant
+ * where every coefficient class allows it) on the case itself and keeps the
+ * fastest, cached per grid shape for the process; the environment variable
+ * MGLET_TUNE=0 keeps the defaults.  mglet_gpu_tuning describes the choice
+ * ("" for the plain form); mglet_gpu_force_variant overrides it (kernel
+ * "mx_sip_pre", variant 0..9, -1 = default).  All variants compute the same
+ * bits. */
+int mglet_gpu_tuning(mglet_ctx* ctx, char* buf, int64_t buflen);
+int mglet_gpu_force_variant(mglet_ctx* ctx, const char* kernel, int32_t variant);
 
 /* ---- Misc ----------------------------------------------------------------- */
 int mglet_gpu_synchronize(mglet_ctx* ctx);

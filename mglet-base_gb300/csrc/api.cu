@@ -1286,6 +1286,19 @@ int mglet_gpu_profile_names(mglet_ctx* c, char* buf, int64_t buflen) {
     return 0;
 }
 
+int mglet_gpu_tuning(mglet_ctx* c, char* buf, int64_t buflen) {
+    if (!c || !buf || buflen <= 0) return fail(MGLET_ERR_ARG, "tuning: bad buffer");
+    const std::string s = mixed_tuning(c);
+    if ((int64_t)s.size() + 1 > buflen) return fail(MGLET_ERR_SIZE, "tuning: buffer too small");
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+    return 0;
+}
+
+int mglet_gpu_force_variant(mglet_ctx* c, const char* kernel, int32_t variant) {
+    if (!c || !kernel) return fail(MGLET_ERR_ARG, "force_variant: null argument");
+    return mixed_force_variant(c, kernel, variant);
+}
+
 int mglet_gpu_synchronize(mglet_ctx* c) {
     if (!c) return fail(MGLET_ERR_ARG, "synchronize: null context");
     cudaSetDevice(c->device);

@@ -20,6 +20,9 @@
 //    one CUDA graph with no host round trip (the reference's
 //    MPI_Allreduce + host test per outer iteration).
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+#include <string>
 #include <cstring>
 #include <map>
 #include <vector>
@@ -348,6 +351,43 @@ int mixed_init(Ctx* c) {
     }
     cudaFree(d_reps);
     if (e != cudaSuccess) return cuda_fail(e, "mixed_init");
+    // launch shapes picked by measurement on this case (MGLET_TUNE=0 keeps
+    // the defaults)
+    const char* tune = std::getenv("MGLET_TUNE");
+    if (!(tune && tune[0] == '0')) {
+        if (int rc2 = sip_tune(c, m->sip, m->cf, m->d_gcls, m->d_ctl)) return rc2;
+        MG_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return 0;
+}
+
+// Text of the launch variants in use ("kernel: variant (ms per launch)").
+std::string mixed_tuning(Ctx* c) {
+    MixedState* m = c->mx;
+    if (!m) return "";
+    const SipState& s = m->sip;
+    char buf[256];
+    std::snprintf(buf, sizeof buf, "mx_sip_pre: %s%s (%.4f ms); uniform classes: %s",
+                  sip_pre_variant_name(s.pre_variant >= 0 ? s.pre_variant : 0),
+                  s.pre_variant >= 0 ? "" : " [default]", s.pre_ms, s.unicls ? "yes" : "no");
+    return buf;
+}
+
+int mixed_force_variant(Ctx* c, const char* kernel, int v) {
+    MixedState* m = c->mx;
+    if (!m || std::strcmp(kernel, "mx_sip_pre") != 0 || v < -1 || v >= sip_pre_variants()) {
+        set_error("force_variant: needs the mixed form, kernel mx_sip_pre and a valid variant");
+        return MGLET_ERR_ARG;
+    }
+    if (v >= 5 && !m->sip.unicls) {
+        set_error("force_variant: the uniform pre-pass needs classes with constant coefficients");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    m->sip.pre_variant = v;
+    if (m->graph) {          // the captured stage holds the old launch
+        cudaGraphExecDestroy(m->graph);
+        m->graph = nullptr;
+    }
     return 0;
 }
 

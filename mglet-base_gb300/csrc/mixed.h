@@ -1,6 +1,8 @@
 // mixed.h -- batched mixed-precision form of the stage (MGLET_FORM_MIXED).
 #pragma once
 
+#include <string>
+
 #include "internal.h"
 
 namespace mg {
@@ -11,6 +13,8 @@ void mixed_field_changed(Ctx* c, const char* name);
 void mixed_field_sync_out(Ctx* c, const char* name);
 int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_stage_stats* st);
 int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st);
+std::string mixed_tuning(Ctx* c);
+int mixed_force_variant(Ctx* c, const char* kernel, int v);
 
 // shared with api.cu
 int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,

@@ -38,6 +38,7 @@
 // the copies in flight, exits.
 
 #include <algorithm>
+#include <cstring>
 #include <map>
 #include <vector>
 
@@ -172,6 +173,7 @@ struct PreArgs {
     const float *AW, *AE, *AS, *AN, *AB, *AT;   // FP32 1-D coefficients (concatenated)
     const DevGrid* grids;
     const float4* PR;           // packed pre-pass records (packed form)
+    const float* UNI;           // [ncls][8] aw, ae, as, an, ab, at, ap of uniform classes
     int* ctl;
     int hzero;
     int rev;                    // walk the grids in reverse block order
@@ -259,7 +261,12 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
 // the point's own hilf and rhs -- are loaded kAhead iterations ahead into
 // registers, so that each thread keeps several points' DRAM loads in flight
 // (the kernel is bound by DRAM latency, not by its instructions).
-template <int kAhead, int kMinBlocks>
+//
+// kUni: every class has one value of each of the seven Laplacian
+// coefficients at all its points (a uniform tiling without walls), so only
+// the first record {codes, lpr} is read per point and the coefficients come
+// from UNI; the arithmetic is the same, so the result is bit-identical.
+template <int kAhead, int kMinBlocks, bool kUni>
 __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
     if (a.ctl[0]) return;
     extern __shared__ __align__(16) float gh[];   // [6][fs]
@@ -299,7 +306,15 @@ __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
         if (w0 >= 0) {
             float lap = 0.f;
             if (!hz) {
-                const float4 r2 = __ldg(P1 + npp + q), r3 = __ldg(P1 + 2 * npp + q);
+                float4 r2, r3;
+                if (kUni) {
+                    const float* u = a.UNI + 8 * a.gcls[g];
+                    r2 = make_float4(u[0], u[1], u[2], u[3]);
+                    r3 = make_float4(u[4], u[5], u[6], 0.f);
+                } else {
+                    r2 = __ldg(P1 + npp + q);
+                    r3 = __ldg(P1 + 2 * npp + q);
+                }
                 const int w1 = __float_as_int(r1.y), w2 = __float_as_int(r1.z);
                 auto nbv = [&](int code) -> float { return code < npp ? __ldg(H + code) : ghb[code]; };
                 lap = -r2.x * nbv(w0 & 0xffff) - r2.y * nbv(w0 >> 16) - r2.z * nbv(w1 & 0xffff) -
@@ -991,7 +1006,110 @@ size_t pre_smem(const SipState& st) {
     return stencil_tables_bytes(st.nm, st.ni) + (size_t)6 * st.fs * 4;
 }
 
+// Pre-pass launch variants: loads ahead, minimum CTAs per SM, uniform class.
+struct PreVariant {
+    int ahead, minblocks;
+    bool uni;
+    const char* name;
+};
+const PreVariant kPreVariants[] = {
+    {2, 3, false, "ahead=2 ctas=3"}, {1, 3, false, "ahead=1 ctas=3"},
+    {3, 3, false, "ahead=3 ctas=3"}, {2, 2, false, "ahead=2 ctas=2"},
+    {2, 4, false, "ahead=2 ctas=4"}, {2, 3, true, "ahead=2 ctas=3 uniform"},
+    {1, 3, true, "ahead=1 ctas=3 uniform"}, {3, 3, true, "ahead=3 ctas=3 uniform"},
+    {2, 2, true, "ahead=2 ctas=2 uniform"}, {2, 4, true, "ahead=2 ctas=4 uniform"},
+};
+constexpr int kNumPre = (int)(sizeof(kPreVariants) / sizeof(kPreVariants[0]));
+
+void launch_pre_variant(int v, int ngrid, size_t smem, cudaStream_t s, const PreArgs& p) {
+    switch (v) {
+        case 0: k_sip_pre_pf<2, 3, false><<<ngrid, 512, smem, s>>>(p); break;
+        case 1: k_sip_pre_pf<1, 3, false><<<ngrid, 512, smem, s>>>(p); break;
+        case 2: k_sip_pre_pf<3, 3, false><<<ngrid, 512, smem, s>>>(p); break;
+        case 3: k_sip_pre_pf<2, 2, false><<<ngrid, 512, smem, s>>>(p); break;
+        case 4: k_sip_pre_pf<2, 4, false><<<ngrid, 512, smem, s>>>(p); break;
+        case 5: k_sip_pre_pf<2, 3, true><<<ngrid, 512, smem, s>>>(p); break;
+        case 6: k_sip_pre_pf<1, 3, true><<<ngrid, 512, smem, s>>>(p); break;
+        case 7: k_sip_pre_pf<3, 3, true><<<ngrid, 512, smem, s>>>(p); break;
+        case 8: k_sip_pre_pf<2, 2, true><<<ngrid, 512, smem, s>>>(p); break;
+        default: k_sip_pre_pf<2, 4, true><<<ngrid, 512, smem, s>>>(p); break;
+    }
+}
+
+PreArgs pre_args(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rwrite,
+                 bool hzero) {
+    PreArgs p;
+    p.s = shape(st);
+    p.fnbr = st.d_fnbr; p.gcls = gcls;
+    p.H = st.h32; p.RHS = st.rhs32; p.PRE = st.rs[rwrite];
+    p.CF = cf;
+    p.AW = st.a1[0]; p.AE = st.a1[1]; p.AS = st.a1[2]; p.AN = st.a1[3]; p.AB = st.a1[4];
+    p.AT = st.a1[5];
+    p.grids = c->d_grids;
+    p.ctl = ctl;
+    p.hzero = hzero ? 1 : 0;
+    p.PR = st.spr;
+    p.UNI = st.uni;
+    p.rev = 0;
+    return p;
+}
+
 }  // namespace
+
+int sip_pre_variants() { return kNumPre; }
+const char* sip_pre_variant_name(int v) { return v >= 0 && v < kNumPre ? kPreVariants[v].name : ""; }
+
+int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl) {
+    if (!st.prepk) return 0;
+    // process-wide cache: shape, grid count and class layout -> variant
+    static std::map<std::vector<long long>, std::pair<int, double>> cache;
+    const std::vector<long long> key = {st.kk, st.jj, st.ii, c->ngrid, st.unicls ? 1 : 0};
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        st.pre_variant = it->second.first;
+        st.pre_ms = it->second.second;
+        return 0;
+    }
+    PreArgs p = pre_args(c, st, cf, gcls, ctl, 0, false);
+    const size_t smem = (size_t)6 * st.fs * 4;
+    cudaEvent_t e0, e1;
+    MG_CUDA(cudaEventCreate(&e0));
+    MG_CUDA(cudaEventCreate(&e1));
+    int best = 0;
+    double best_ms = 1e30;
+    for (int v = 0; v < kNumPre; ++v) {
+        if (kPreVariants[v].uni && !st.unicls) continue;
+        for (int w = 0; w < 2; ++w) launch_pre_variant(v, c->ngrid, smem, c->stream, p);
+        cudaEventRecord(e0, c->stream);
+        const int reps = 5;
+        for (int r = 0; r < reps; ++r) {
+            p.rev = r & 1;
+            launch_pre_variant(v, c->ngrid, smem, c->stream, p);
+        }
+        cudaEventRecord(e1, c->stream);
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return cuda_fail(e, "sip_tune");
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms / reps < best_ms) {
+            best_ms = ms / reps;
+            best = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    // the timing launches wrote res slot 0; leave the inner solver zeroed
+    MG_CUDA(cudaMemsetAsync(st.rs[0], 0, (size_t)c->ngrid * st.npp * sizeof(float), c->stream));
+    st.pre_variant = best;
+    st.pre_ms = best_ms;
+    cache[key] = {best, best_ms};
+    return 0;
+}
 
 int sip_init(Ctx* c, SipState& st) {
     const DevGrid& G0 = c->grids[0];
@@ -1246,6 +1364,35 @@ int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* 
             c->d_grids, d_reps, st.d_pst, st.nm, st.npp, st.d_pq, st.d_pcode, *cf, st.a1[0], st.a1[1],
             st.a1[2], st.a1[3], st.a1[4], st.a1[5], st.spr);
         MG_LAUNCHED(c);
+        // classes whose seven Laplacian coefficients are the same at every point
+        std::vector<float4> rec(3 * n);
+        MG_CUDA(copy_on(c->stream, rec.data(), st.spr, rec.size() * sizeof(float4),
+                        cudaMemcpyDeviceToHost));
+        std::vector<float> uni(8 * (size_t)nclass, 0.f);
+        bool all = true;
+        for (int cls = 0; cls < nclass && all; ++cls) {
+            const float4* P1 = rec.data() + (size_t)cls * 3 * st.npp;
+            bool first = true;
+            for (int q = 0; q < st.npp && all; ++q) {
+                int w0;
+                std::memcpy(&w0, &P1[q].x, sizeof(int));
+                if (w0 < 0) continue;
+                const float4 r2 = P1[st.npp + q], r3 = P1[2 * st.npp + q];
+                const float v[7] = {r2.x, r2.y, r2.z, r2.w, r3.x, r3.y, r3.z};
+                float* u = uni.data() + 8 * cls;
+                for (int t = 0; t < 7; ++t) {
+                    if (first) u[t] = v[t];
+                    else if (std::memcmp(&u[t], &v[t], sizeof(float)) != 0) all = false;
+                }
+                first = false;
+            }
+        }
+        st.unicls = all;
+        if (all) {
+            MG_CUDA(cudaMalloc(&st.uni, uni.size() * sizeof(float)));
+            MG_CUDA(copy_on(c->stream, st.uni, uni.data(), uni.size() * sizeof(float),
+                            cudaMemcpyHostToDevice));
+        }
     }
     return 0;
 }
@@ -1257,7 +1404,7 @@ void sip_release(SipState& st) {
                     (void*)st.rs[2], (void*)st.rhs32, (void*)st.rhsl, (void*)st.dph, (void*)st.dpl,
                     (void*)st.d_facepos, (void*)st.d_dscf, (void*)st.d_dscb,
                     (void*)st.d_wf, (void*)st.d_wb, (void*)st.swf, (void*)st.swb,
-                    (void*)st.d_pcode, (void*)st.spr, (void*)st.a1[0], (void*)st.a1[1],
+                    (void*)st.d_pcode, (void*)st.spr, (void*)st.uni, (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
                     (void*)st.a1lo[4], (void*)st.a1lo[5]})
@@ -1278,22 +1425,13 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
                 int rwrite, bool hzero) {
     {
         ProfScope ps_(c, "mx_sip_pre");
-        PreArgs p;
-        p.s = shape(st);
-        p.fnbr = st.d_fnbr; p.gcls = gcls;
-        p.H = st.h32; p.RHS = st.rhs32; p.PRE = st.rs[rwrite];
-        p.CF = cf;
-        p.AW = st.a1[0]; p.AE = st.a1[1]; p.AS = st.a1[2]; p.AN = st.a1[3]; p.AB = st.a1[4];
-        p.AT = st.a1[5];
-        p.grids = c->d_grids;
-        p.ctl = ctl;
-        p.hzero = hzero ? 1 : 0;
-        p.PR = st.spr;
+        PreArgs p = pre_args(c, st, cf, gcls, ctl, rwrite, hzero);
         p.rev = next_order(st);
-        // two points' DRAM loads ahead at three CTAs per SM (measured on 24^3
-        // grids against one or three points ahead at four or two CTAs)
+        // the tuner's choice (loads ahead, CTAs per SM, uniform coefficients);
+        // untuned: two points ahead at three CTAs per SM
         if (st.prepk)
-            k_sip_pre_pf<2, 3><<<c->ngrid, 512, (size_t)6 * st.fs * 4, c->stream>>>(p);
+            launch_pre_variant(st.pre_variant >= 0 ? st.pre_variant : 0, c->ngrid,
+                               (size_t)6 * st.fs * 4, c->stream, p);
         else
             k_sip_pre<<<c->ngrid, 512, pre_smem(st), c->stream>>>(p);
         MG_LAUNCHED(c);

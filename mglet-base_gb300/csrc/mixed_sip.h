@@ -42,6 +42,14 @@ struct SipState {
     int* d_pcode = nullptr;
     float4* spr = nullptr;
     int order = 0;              // direction of the next per-grid kernel (next_order)
+    // every class has constant Laplacian coefficients: [ncls][8] aw, ae, as,
+    // an, ab, at, ap for the uniform pre-pass
+    bool unicls = false;
+    float* uni = nullptr;
+    // launch variant of the pre-pass (index into the variant table), picked by
+    // the tuner or forced by the caller; -1 = default
+    int pre_variant = -1;
+    double pre_ms = 0.0;        // its measured time per launch (tuner)
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
@@ -61,5 +69,11 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
                  bool hzero);
 int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl);
 int sip_scatter_dp(Ctx* c, SipState& st);
+// Times every valid pre-pass variant on the current buffers and keeps the
+// fastest (cached per grid shape and class layout for the process).
+int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl);
+// The pre-pass variants: count, and a description of variant v.
+int sip_pre_variants();
+const char* sip_pre_variant_name(int v);
 
 }  // namespace mg

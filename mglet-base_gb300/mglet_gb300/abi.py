@@ -83,6 +83,11 @@ class ItInfo(C.Structure):
     ]
 
 
+class IbGeometry(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("bp", "bu", "bv", "bw", "areau", "areav", "areaw",
+                                          "bzelltyp", "icells", "nvecs", "ucell")]
+
+
 def make_flow_params(gmol, rho=1.0, gradp=(0.0, 0.0, 0.0), psolver=PSOLVER_SIP, ninner=5,
                      nouter=9, nouter_min=0, epcorr=1e-10, omega=1.1, form=FORM_PLAIN):
     p = FlowParams()

@@ -21,7 +21,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 BASE = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 SOURCES = ["api.cu", "plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "plain_bound.cu",
            "plain_gc.cu", "plain_level.cu", "mixed.cu", "mixed_flux.cu", "mixed_sip.cu", "noalloc.cu",
-           "adjoint.cu", "les.cu", "scalar.cu", "diag.cu"]
+           "adjoint.cu", "les.cu", "scalar.cu", "diag.cu", "gc_create.cu"]
 # translation units whose FP64 arithmetic must not be contracted into FMAs
 NO_FMA = {"plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "plain_bound.cu", "plain_gc.cu",
           "plain_level.cu", "noalloc.cu", "les.cu", "scalar.cu"}
@@ -34,10 +34,17 @@ def nvcc():
     return exe
 
 
+# translation units with host arithmetic that must not be contracted either
+# (the ghost-cell stencil construction)
+HOST_NO_FMA = {"gc_create.cu"}
+
+
 def _flags(src):
     f = list(BASE) + ARCH
     if src in NO_FMA:
         f.append("-fmad=false")
+    if src in HOST_NO_FMA:
+        f += ["-Xcompiler", "-ffp-contract=off"]
     return f
 
 

@@ -456,3 +456,127 @@ def block_body(case, lo, hi, nstc=3, seed=7, grids=None):
         gl[4] = (n, np.array(fi, dtype=np.int64), np.array(fr))
         lists.append(gl)
     return bp, lists
+
+
+def _box_ball_distance(lo, hi, c):
+    """Distance from point c to the axis-aligned box [lo, hi] (0 inside)."""
+    d = np.maximum(np.maximum(lo - c, c - hi), 0.0)
+    return float(np.sqrt(np.sum(d * d)))
+
+
+def body_refined(nx, ny, nz, n=24, length=(8.0, 4.0, 4.0), center=(2.0, 2.0, 2.0),
+                 refine_radii=(1.0, 0.7), walls=None):
+    """A hierarchy refined around a body: level 1 tiles the box with nx*ny*nz
+    grids of n^3 cells (periodic_box, with `walls` on box faces); level L+1
+    covers every level-L grid whose box comes within refine_radii[L-1] of
+    `center` by 2x2x2 grids at half its spacing, if all its 26 same-level
+    neighbours exist (proper nesting), as grids.h5 of a locally refined
+    domain holds (src/core/gridio_mod.F90:61-245).  A fine face with
+    a same-level grid across it is CON, a fine face on a box face with a
+    wall code gets that code, every other fine face is PAR (code 8) towards
+    the parent.  Grid ids run level by level, x fastest within a level."""
+    from .abi import BC_PAR
+    assert n % 2 == 0
+    walls = dict(walls or {})
+    c0 = periodic_box(nx, ny, nz, n=n, length=length, walls=walls)
+    c = np.asarray(center, dtype=np.float64)
+    L = np.asarray(length, dtype=np.float64)
+    periodic = [not (2 * d + 1 in walls or 2 * d + 2 in walls) for d in range(3)]
+    ii = jj = kk = n + 4
+    # per level: lattice positions (gx, gy, gz) in grids of that level
+    levels = [[tuple(p) for p in c0.gridpos]]
+    parents = [[None] * len(levels[0])]
+    ntile = [np.array([nx, ny, nz])]
+    for lv, r in enumerate(refine_radii):
+        size = L / ntile[lv]
+        kids, kpar = [], []
+        have = set(levels[lv])
+
+        def nested(p, nt=ntile[lv]):
+            # proper nesting: all 26 same-level neighbours exist (or lie
+            # across a wall), so no fine face looks two levels down
+            for s in range(1, 27):
+                t = [p[a] + slot_offset(s)[a] for a in range(3)]
+                for a in range(3):
+                    if periodic[a]:
+                        t[a] %= nt[a]
+                    elif not 0 <= t[a] < nt[a]:
+                        t = None
+                        break
+                if t is not None and tuple(t) not in have:
+                    return False
+            return True
+
+        for q, (gx, gy, gz) in enumerate(levels[lv]):
+            lo = np.array([gx, gy, gz]) * size
+            if _box_ball_distance(lo, lo + size, c) <= r and nested((gx, gy, gz)):
+                for oz in range(2):
+                    for oy in range(2):
+                        for ox in range(2):
+                            kids.append((2 * gx + ox, 2 * gy + oy, 2 * gz + oz))
+                            kpar.append((q, ox, oy, oz))
+        order = sorted(range(len(kids)), key=lambda t: (kids[t][2], kids[t][1], kids[t][0]))
+        levels.append([kids[t] for t in order])
+        parents.append([kpar[t] for t in order])
+        ntile.append(ntile[lv] * 2)
+    base = np.cumsum([0] + [len(lv) for lv in levels])
+    ngrid = int(base[-1])
+    nbr = np.zeros((ngrid, 26), dtype=np.int32)
+    bct = np.zeros((ngrid, 6), dtype=np.int32)
+    level = np.zeros(ngrid, dtype=np.int32)
+    iparent = np.zeros(ngrid, dtype=np.int32)
+    position = np.zeros((ngrid, 3), dtype=np.int32)
+    gridpos = np.zeros((ngrid, 3), dtype=np.int32)
+    xs, ys, zs, hs = [], [], [], []
+    for lv, grids in enumerate(levels):
+        index = {p: base[lv] + q for q, p in enumerate(grids)}
+        nt = ntile[lv]
+        size = L / nt
+        h = size / n
+        for q, p in enumerate(grids):
+            g = base[lv] + q
+            level[g] = lv + 1
+            gridpos[g] = p
+            if lv == 0:
+                nbr[g] = c0.nbrgrid[q]
+                bct[g] = c0.bctype[q]
+            else:
+                pq, ox, oy, oz = parents[lv][q]
+                iparent[g] = base[lv - 1] + pq + 1
+                position[g] = (3 + ox * (n // 2), 3 + oy * (n // 2), 3 + oz * (n // 2))
+
+                def find(d):
+                    t = [p[0] + d[0], p[1] + d[1], p[2] + d[2]]
+                    for a in range(3):
+                        if periodic[a]:
+                            t[a] %= nt[a]
+                        elif not 0 <= t[a] < nt[a]:
+                            return 0
+                    return index.get(tuple(t), -1) + 1
+
+                for s in range(1, 27):
+                    nbr[g, s - 1] = max(find(slot_offset(s)), 0)
+                for f in range(1, 7):
+                    d = (f - 1) // 2
+                    step = [0, 0, 0]
+                    step[d] = 1 if f % 2 == 0 else -1
+                    t = p[d] + step[d]
+                    if not periodic[d] and not 0 <= t < nt[d] and f in walls:
+                        bct[g, f - 1] = walls[f]
+                    else:
+                        bct[g, f - 1] = BC_CON if find(step) > 0 else BC_PAR
+            i = np.arange(1, ii + 1, dtype=np.float64)
+            xs.append(p[0] * size[0] + (i - 2.5) * h[0])
+            ys.append(p[1] * size[1] + (i - 2.5) * h[1])
+            zs.append(p[2] * size[2] + (i - 2.5) * h[2])
+            hs.append(h)
+    hs = np.array(hs)
+    return Case(
+        ngrid=ngrid, kk=kk, jj=jj, ii=ii,
+        mgdims=np.tile(np.array([kk, jj, ii], dtype=np.int32), (ngrid, 1)),
+        level=level, bctype=bct, nbrgrid=nbr, gridpos=gridpos,
+        x=np.concatenate(xs), y=np.concatenate(ys), z=np.concatenate(zs),
+        dx=np.repeat(hs[:, 0], ii), dy=np.repeat(hs[:, 1], jj), dz=np.repeat(hs[:, 2], kk),
+        ddx=np.repeat(hs[:, 0], ii), ddy=np.repeat(hs[:, 1], jj), ddz=np.repeat(hs[:, 2], kk),
+        iparent=iparent, position=position,
+    )

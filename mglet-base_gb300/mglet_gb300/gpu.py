@@ -33,7 +33,9 @@ EXPORTS = [
     "mglet_gpu_set_body_force", "mglet_gpu_adjoint_rk_stage", "mglet_gpu_energy_gradient",
     "mglet_gpu_set_lesmodel", "mglet_gpu_set_scalars", "mglet_gpu_timeintegrate_scalar",
     "mglet_gpu_set_buoyancy", "mglet_gpu_set_coriolis", "mglet_gpu_set_scalar_bc",
-    "mglet_gpu_add_scalar_source", "mglet_gpu_fp64_roof",
+    "mglet_gpu_add_scalar_source", "mglet_gpu_fp64_roof", "mglet_gpu_tuning",
+    "mglet_gpu_force_variant", "mglet_create_flowstencils", "mglet_flowstencils_size",
+    "mglet_flowstencils_copy", "mglet_flowstencils_free",
 ]
 
 
@@ -113,6 +115,13 @@ def load(path=None):
     L.mglet_gpu_divmax_noalloc.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, C.c_int32,
                                            C.c_int32, vp, vp, vp, vp, vp]
     L.mglet_gpu_fp64_roof.argtypes = [C.c_int32, C.POINTER(C.c_double)]
+    L.mglet_gpu_tuning.argtypes = [vp, cp, C.c_int64]
+    L.mglet_gpu_force_variant.argtypes = [vp, cp, C.c_int32]
+    L.mglet_create_flowstencils.argtypes = [vp, vp, C.POINTER(vp)]
+    L.mglet_flowstencils_size.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+                                          C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.mglet_flowstencils_copy.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp]
+    L.mglet_flowstencils_free.argtypes = [vp]
     _lib = L
     return L
 
@@ -362,6 +371,54 @@ class Solver:
         _check(load().mglet_gpu_profile_get(self.h, kernel.encode(), C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    def tuning(self):
+        buf = C.create_string_buffer(512)
+        _check(load().mglet_gpu_tuning(self.h, buf, len(buf)))
+        return buf.value.decode()
+
+    def force_variant(self, kernel, variant):
+        _check(load().mglet_gpu_force_variant(self.h, kernel.encode(), variant))
+
     @property
     def launches(self):
         return load().mglet_gpu_kernel_launches(self.h)
+
+
+def create_flowstencils(case, geo):
+    """The ghost-cell stencil lists of every grid from the blocking fields
+    (geometry.block): mglet_create_flowstencils, host code, no device needed.
+    Returns lists[g] = {1: (ncells, xpoli, xpolr, xpolrvel), 2: .., 3: ..,
+    4: (ncells, xpoli, xpolr)}, the layout mglet_gpu_set_stencils takes."""
+    L = load()
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    keep = {n: f64(geo[n]) for n in ("bp", "bu", "bv", "bw", "areau", "areav", "areaw")}
+    keep["bzelltyp"] = np.ascontiguousarray(geo["bzelltyp"], dtype=np.int32)
+    keep["icells"] = np.ascontiguousarray(geo["icells"], dtype=np.int32)
+    keep["nvecs"] = f64(geo["nvecs"]).reshape(-1)
+    keep["ucell"] = f64(geo["ucell"]).reshape(-1)
+    g = abi.IbGeometry()
+    for n, a in keep.items():
+        setattr(g, n, a.ctypes.data_as(C.c_void_p))
+    desc = case.desc()
+    h = C.c_void_p()
+    _check(L.mglet_create_flowstencils(C.byref(desc), C.byref(g), C.byref(h)))
+    out = []
+    try:
+        for ig in range(1, case.ngrid + 1):
+            gl = {}
+            for comp in (1, 2, 3, 4):
+                n = C.c_int32()
+                nxi, nxr = C.c_int64(), C.c_int64()
+                _check(L.mglet_flowstencils_size(h, ig, comp, C.byref(n), C.byref(nxi), C.byref(nxr)))
+                xi = np.zeros(nxi.value, dtype=np.int64)
+                xr = np.zeros(nxr.value)
+                xv = np.zeros(nxr.value) if comp < 4 else None
+                _check(L.mglet_flowstencils_copy(h, ig, comp, xi.ctypes.data_as(C.c_void_p),
+                                                 xr.ctypes.data_as(C.c_void_p),
+                                                 xv.ctypes.data_as(C.c_void_p) if xv is not None
+                                                 else None))
+                gl[comp] = (n.value, xi, xr, xv) if comp < 4 else (n.value, xi, xr)
+            out.append(gl)
+    finally:
+        L.mglet_flowstencils_free(h)
+    return out

@@ -171,3 +171,34 @@ def test_mixed_precision_solenoidal_field(gpu_lib):
     assert vel_err(case, mix.get, ref.get) <= 1e-8
     pm, pr = case.interior(mix.get("P")), case.interior(ref.get("P"))
     assert rel_l2(pm - pm.mean(), pr - pr.mean()) <= 1e-6
+
+
+def test_pre_pass_variants_agree(gpu_lib):
+    """Every launch variant of the pre-pass the tuner may pick (loads ahead,
+    CTAs per SM, uniform-coefficient records) gives the same bits."""
+    case = cases.periodic_box(2, 2, 1, n=24)
+    out = []
+    g0 = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=3))
+    assert "mx_sip_pre" in g0.tuning() and "uniform classes: yes" in g0.tuning()
+    g0.close()
+    for v in range(10):
+        g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=3))
+        g.force_variant("mx_sip_pre", v)
+        _init(g, case)
+        rk = gpu_lib.rk_scheme("williamson")
+        for irk in range(1, 4):
+            g.timeintegrate_flow(1, 1, 0.0, 5e-4, irk, rk)
+        out.append([g.get(nm) for nm in "UVWP"])
+        g.close()
+    for o in out[1:]:
+        for a, b in zip(out[0], o):
+            assert np.array_equal(a, b)
+
+
+def test_uniform_variant_refused_without_uniform_classes(gpu_lib):
+    case = cases.stretch(cases.periodic_box(2, 1, 1, n=8))
+    g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED))
+    assert "uniform classes: no" in g.tuning()
+    with pytest.raises(gpu_lib.MgletError):
+        g.force_variant("mx_sip_pre", 5)
+    g.force_variant("mx_sip_pre", 2)
