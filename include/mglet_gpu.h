@@ -446,6 +446,35 @@ int mglet_gpu_divmax_noalloc(const double* u, const double* v, const double* w, 
  * CUDA events (best of five).  The second roof of the FP64 parity form. */
 int mglet_gpu_fp64_roof(int32_t device, double* out);
 
+/* ---- Grid-partitioned runs (several ranks) ---------------------------------
+ * The reference distributes whole grids over MPI ranks (dist_grids,
+ * src/core/grids_mod.F90:344-394) and exchanges halos between ranks inside
+ * connect (send/recv of connect2_mod.F90:406-548) and the maximum residual
+ * with MPI_Allreduce (pressuresolver_mod.F90:295).  Here a rank's context
+ * holds the grids it owns plus read-only copies of the remote grids next to
+ * them ("halo grids", halo[g] = 1); before every connect the library packs
+ * the boxes of its owned grids that other ranks' copies need, hands them to
+ * the caller's exchange function, and unpacks what it receives into its own
+ * copies, so every owned grid sees the same neighbour values as in a
+ * single-rank run.  Maximum reductions (pressure residual, CFL, divergence)
+ * skip the copies and are completed across ranks through the same function;
+ * the kinetic energy is summed across ranks.  Plain form, one level.
+ *
+ * send/recv rows are [peer, grid (1-based, of this context), k0, k1, j0, j1,
+ * i0, i1] (inclusive 1-based boxes); for every peer both sides list the same
+ * boxes in the same order.  The exchange function gets host buffers:
+ * op 0 exchanges -- send sendbuf[q] (sendn[q] doubles) to peers[q] and
+ * receive recvbuf[q] (recvn[q] doubles) from it, for all q at once; op 1
+ * replaces sendbuf[0][0..sendn[0]) by its maximum over all ranks, op 2 by its
+ * sum.  It returns 0, or nonzero to fail the calling entry point
+ * (MGLET_ERR_CUDA is not used for it: MGLET_ERR_ARG with its message). */
+typedef int (*mglet_exchange_fn)(void* user, int32_t op, int32_t npeers, const int32_t* peers,
+                                 double* const* sendbuf, const int64_t* sendn,
+                                 double* const* recvbuf, const int64_t* recvn);
+int mglet_gpu_set_partition(mglet_ctx* ctx, const int32_t* halo, int32_t nsend,
+                            const int32_t* send, int32_t nrecv, const int32_t* recv,
+                            mglet_exchange_fn fn, void* user);
+
 /* ---- Launch tuning of the mixed form (no counterpart in the reference) -----
  * mglet_gpu_create times the launch variants of the mixed form's pre-pass
  * (points loaded ahead, CTAs per SM, and the uniform-coefficient variant

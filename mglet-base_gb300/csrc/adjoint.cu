@@ -442,6 +442,8 @@ int adj_connect(Ctx* c, int ilevel, int layers, int slots, bool corners, bool no
 int adjoint_ready(Ctx* c) {
     if (c->prm.form != MGLET_FORM_PLAIN)
         return fail(MGLET_ERR_UNSUPPORTED, "adjoint: the plain FP64 form only");
+    if (c->part)
+        return fail(MGLET_ERR_UNSUPPORTED, "adjoint: one rank (no grid partition)");
     if (c->minlevel != c->maxlevel || c->ibtype != 0)
         return fail(MGLET_ERR_UNSUPPORTED, "adjoint: one grid level without immersed boundary");
     if (c->prm.psolver == MGLET_PSOLVER_SOR)

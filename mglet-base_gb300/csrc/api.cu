@@ -299,6 +299,10 @@ int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, 
         if (int rc = build_plan(c, ilevel, layers, slots, corners, normal, fwd, p)) return rc;
         it = c->plans.emplace(key, p).first;
     }
+    // several ranks: the copies of remote grids first get their owners'
+    // current boxes (the receive half of connect2_mod.F90:406-548)
+    if (c->part)
+        if (int rc = part_exchange(c, f)) return rc;
     return launch_connect(c, it->second, f);
 }
 
@@ -366,6 +370,7 @@ int solve_pressure_system(Ctx* c, double prefak, mglet_stage_stats* st, bool zer
         MG_CUDA(cudaMemcpyAsync(c->h_scalar, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost,
                                 c->stream));
         MG_CUDA(cudaStreamSynchronize(c->stream));
+        if (int rc = part_allreduce(c, c->h_scalar, 1, 1)) return rc;
         prefak = c->h_scalar[0];
         if (!(prefak > 0.0)) {
             if (st) *st = mglet_stage_stats{0, 0, 0.0, 0.0};
@@ -403,6 +408,8 @@ int solve_pressure_system(Ctx* c, double prefak, mglet_stage_stats* st, bool zer
             MG_CUDA(cudaMemcpyAsync(c->h_scalar, c->d_scalar, sizeof(double),
                                     cudaMemcpyDeviceToHost, c->stream));
             MG_CUDA(cudaStreamSynchronize(c->stream));
+            // MPI_Allreduce(MAX) of pressuresolver_mod.F90:295
+            if (int rc = part_allreduce(c, c->h_scalar, 1, 1)) return rc;
             maxrhs = c->h_scalar[0];
             if (maxrhs / prefak < c->prm.epcorr) break;
         }
@@ -412,6 +419,7 @@ int solve_pressure_system(Ctx* c, double prefak, mglet_stage_stats* st, bool zer
         MG_CUDA(cudaMemcpyAsync(c->h_scalar, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost,
                                 c->stream));
         MG_CUDA(cudaStreamSynchronize(c->stream));
+        if (int rc = part_allreduce(c, c->h_scalar, 1, 1)) return rc;
         maxrhs = c->h_scalar[0];
     }
     if (st) {
@@ -670,6 +678,7 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
             c->nbr[g + 1][s] = nb;
         }
         G.gradpflag = d->gradpflag ? d->gradpflag[g] : 1;
+        G.halo = 0;
         G.ip3 = o3; G.ipx = ox; G.ipy = oy; G.ipz = oz;
         o3 += (long long)G.kk * G.jj * G.ii;
         ox += G.ii; oy += G.jj; oz += G.kk;
@@ -761,6 +770,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     if (!c) return 0;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    part_release(c);
     for (auto& kv : c->profd)
         for (auto& ev : kv.second.pending) {
             cudaEventDestroy(ev.first);
@@ -1217,6 +1227,7 @@ int mglet_gpu_itinfo(mglet_ctx* c, double dt, mglet_itinfo* out) {
     double cm = 0.0, dm = 0.0, es = 0.0, vol = 0.0;
     bool bad = false;
     for (int g = 0; g < c->ngrid; ++g) {
+        if (c->grids[g].halo) continue;   // another rank's grid
         const double gc = red[4 * g], gd = red[4 * g + 1];
         const double ge = red[4 * g + 2] / red[4 * g + 3], gv = red[4 * g + 3];
         cm = std::max(cm, gc);
@@ -1224,6 +1235,16 @@ int mglet_gpu_itinfo(mglet_ctx* c, double dt, mglet_itinfo* out) {
         es = (vol + gv > 0.0) ? (es * vol + ge * gv) / (vol + gv) : 0.0;
         vol = vol + gv;
         if (!std::isfinite(gc) || !std::isfinite(gd) || !std::isfinite(ge)) bad = true;
+    }
+    if (c->part) {
+        // the maxima and the volume-weighted energy over all ranks
+        double mx[3] = {cm, dm, bad ? 1.0 : 0.0}, sm[2] = {es * vol, vol};
+        if (int rc = part_allreduce(c, mx, 3, 1)) return rc;
+        if (int rc = part_allreduce(c, sm, 2, 2)) return rc;
+        cm = mx[0];
+        dm = mx[1];
+        bad = mx[2] != 0.0;
+        es = sm[1] > 0.0 ? sm[0] / sm[1] : 0.0;
     }
     out->cflmax = cm;
     out->divmax = dm;
@@ -1284,6 +1305,13 @@ int mglet_gpu_profile_names(mglet_ctx* c, char* buf, int64_t buflen) {
     if ((int64_t)s.size() + 1 > buflen) return fail(MGLET_ERR_SIZE, "profile_names: buffer too small");
     std::memcpy(buf, s.c_str(), s.size() + 1);
     return 0;
+}
+
+int mglet_gpu_set_partition(mglet_ctx* c, const int32_t* halo, int32_t nsend, const int32_t* send,
+                            int32_t nrecv, const int32_t* recv, mglet_exchange_fn fn, void* user) {
+    if (!c) return fail(MGLET_ERR_ARG, "set_partition: null context");
+    cudaSetDevice(c->device);
+    return set_partition(c, halo, nsend, send, nrecv, recv, fn, user);
 }
 
 int mglet_gpu_tuning(mglet_ctx* c, char* buf, int64_t buflen) {

@@ -28,6 +28,7 @@ struct DevGrid {
     int cls;            // index of the SIP index table of this grid's dims
     long long ip3;      // 0-based element offset of the 3-D slab
     int ipx, ipy, ipz;  // 0-based offsets into the concatenated 1-D arrays
+    int halo;           // 1: read-only copy of a grid another rank owns
 };
 
 // Boundary data of one face of one grid.
@@ -104,9 +105,11 @@ struct ProfEntry {
 };
 
 struct MixedState;   // mixed.cu
+struct Part;         // dist.cu
 
 struct Ctx {
     MixedState* mx = nullptr;
+    Part* part = nullptr;      // grid partition over ranks (null: one rank)
     int device = 0;
     cudaStream_t stream = nullptr;
     int ngrid = 0;
@@ -332,5 +335,12 @@ int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, 
 int launch_connect32(Ctx* c, const ConnectPlan& plan, float* const fields[6], const int* skip);
 int get_plan(Ctx* c, int ilevel, int layers, int slots, bool corners, bool normal, int fwd,
              const ConnectPlan** out);
+// grid-partitioned runs (dist.cu): halo copies refreshed before a connect,
+// reductions completed across ranks (op 1 max, 2 sum), release
+int part_exchange(Ctx* c, double* const fields[6]);
+int part_allreduce(Ctx* c, double* v, int n, int op);
+int set_partition(Ctx* c, const int32_t* halo, int nsend, const int32_t* send, int nrecv,
+                  const int32_t* recv, mglet_exchange_fn fn, void* user);
+void part_release(Ctx* c);
 
 }  // namespace mg

@@ -479,7 +479,8 @@ __global__ void k_maxabs_final(const DevGrid* __restrict__ grids, int ngrid, int
     __shared__ double sh[32];
     double m = 0.0;
     for (int g = threadIdx.x; g < ngrid; g += blockDim.x)
-        m = fmax(fabs(gridmax[g] * ldexp(1.0, maxlevel - grids[g].level)), m);
+        if (!grids[g].halo)   // a copy of another rank's grid
+            m = fmax(fabs(gridmax[g] * ldexp(1.0, maxlevel - grids[g].level)), m);
     m = block_max(m, sh);
     if (threadIdx.x == 0) out[0] = m;
 }

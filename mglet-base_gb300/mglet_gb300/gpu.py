@@ -35,7 +35,7 @@ EXPORTS = [
     "mglet_gpu_set_buoyancy", "mglet_gpu_set_coriolis", "mglet_gpu_set_scalar_bc",
     "mglet_gpu_add_scalar_source", "mglet_gpu_fp64_roof", "mglet_gpu_tuning",
     "mglet_gpu_force_variant", "mglet_create_flowstencils", "mglet_flowstencils_size",
-    "mglet_flowstencils_copy", "mglet_flowstencils_free",
+    "mglet_flowstencils_copy", "mglet_flowstencils_free", "mglet_gpu_set_partition",
 ]
 
 
@@ -122,6 +122,7 @@ def load(path=None):
                                           C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
     L.mglet_flowstencils_copy.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp]
     L.mglet_flowstencils_free.argtypes = [vp]
+    L.mglet_gpu_set_partition.argtypes = [vp, vp, C.c_int32, vp, C.c_int32, vp, vp, vp]
     _lib = L
     return L
 
@@ -370,6 +371,18 @@ class Solver:
         n = C.c_int64()
         _check(load().mglet_gpu_profile_get(self.h, kernel.encode(), C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def set_partition(self, part, exchange):
+        """A rank's share of a partitioned run (dist.Partition) with its
+        exchange function (dist.TorchExchange or any EXCHANGE_FN owner)."""
+        self._part = (part, exchange)
+        halo = np.ascontiguousarray(part.halo, dtype=np.int32)
+        send = np.ascontiguousarray(part.send, dtype=np.int32)
+        recv = np.ascontiguousarray(part.recv, dtype=np.int32)
+        self._part_arrays = (halo, send, recv)
+        fnp = C.cast(exchange.fn, C.c_void_p)
+        _check(load().mglet_gpu_set_partition(self.h, halo.ctypes.data, len(send), send.ctypes.data,
+                                              len(recv), recv.ctypes.data, fnp, None))
 
     def tuning(self):
         buf = C.create_string_buffer(512)

@@ -54,6 +54,7 @@ def lib():
         _lib.oracle_timeintegrate_flow.argtypes = [vp, C.c_int, C.c_int, C.c_double, C.c_double,
                                                    C.c_int, vp, vp]
         _lib.oracle_itinfo.argtypes = [vp, C.c_double, vp]
+        _lib.oracle_set_partition.argtypes = [vp, vp, C.c_int32, vp, C.c_int32, vp, vp, vp]
         _lib.oracle_set_buffer.argtypes = [vp, C.c_char_p, C.c_int, C.c_int, vp, C.c_int64]
         _lib.oracle_set_bc_real.argtypes = [vp, C.c_int, C.c_int, C.c_double]
         _lib.oracle_bound_flow.argtypes = [vp, C.c_int]
@@ -309,6 +310,17 @@ class Oracle:
         'Z' (setibvalues_level / setpointvalues_all), 'I' (setibvalues), 'M'
         (maskbp, also P)."""
         _check(lib().oracle_gc_mode(self.h, _b(mode)))
+
+    def set_partition(self, part, exchange):
+        """The same partition hooks as the library's mglet_gpu_set_partition."""
+        self._part = (part, exchange)
+        halo = np.ascontiguousarray(part.halo, dtype=np.int32)
+        send = np.ascontiguousarray(part.send, dtype=np.int32)
+        recv = np.ascontiguousarray(part.recv, dtype=np.int32)
+        self._part_arrays = (halo, send, recv)
+        fnp = C.cast(exchange.fn, C.c_void_p)
+        _check(lib().oracle_set_partition(self.h, halo.ctypes.data, len(send), send.ctypes.data,
+                                          len(recv), recv.ctypes.data, fnp, None))
 
     def itinfo(self, dt):
         from mglet_gb300.abi import ItInfo

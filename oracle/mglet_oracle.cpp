@@ -66,6 +66,7 @@ struct Grid {
     int gradpflag;
     int64_t ip3;      // 0-based element offset of the 3-D slab
     int64_t ipx, ipy, ipz;   // 0-based; view pointers use base + ipx - 1 for 1-based i
+    int halo = 0;     // 1: read-only copy of a grid another rank owns
 };
 
 struct Conn {         // one row of sendconns (single rank: send == recv)
@@ -178,6 +179,15 @@ struct Ctx {
     std::vector<int> iparent;
     std::vector<std::array<int, 3>> pos;
     std::map<std::string, std::vector<double>> bufx;
+
+    // grid partition over ranks (the receive half of connect and the
+    // MPI_Allreduce of the reference, caller-provided): per peer the boxes
+    // sent from owned grids and received into halo copies, [g, k0, k1, j0,
+    // j1, i0, i1] rows
+    mglet_exchange_fn xfn = nullptr;
+    void* xuser = nullptr;
+    std::vector<int> peers;
+    std::vector<std::vector<std::array<int, 7>>> xsend, xrecv;
 
     double* F(const char* n) { return f3.at(n).data(); }
     double* L(const char* n) { return f1.at(n).data(); }
@@ -333,8 +343,67 @@ int64_t connect_self_single(Ctx& c, double* arr, int sg, int dg, int is, int js,
 
 // connect2_mod.F90:75-139,208-402,481-520,839-944: connect / conn1 for one
 // rank (all connections are self connections).  Returns copied points.
+// Boxes of one peer, field after field, each box k fastest, then j, then i.
+void part_pack(Ctx& c, const std::vector<std::array<int, 7>>& boxes, double* const* flds, int nf,
+               std::vector<double>& buf, bool unpack) {
+    size_t o = 0;
+    for (int q = 0; q < nf; ++q)
+        for (const auto& b : boxes) {
+            const Grid& G = c.g[b[0]];
+            const int kk = G.kk, jj = G.jj;
+            double* a = flds[q] + G.ip3;
+            for (int i = b[5]; i <= b[6]; ++i)
+                for (int j = b[3]; j <= b[4]; ++j)
+                    for (int k = b[1]; k <= b[2]; ++k) {
+                        if (unpack) a[IX(k, j, i)] = buf[o++];
+                        else buf[o++] = a[IX(k, j, i)];
+                    }
+        }
+}
+
+// halo copies of the present fields refreshed from their owners
+int part_exchange(Ctx& c, double* v1, double* v2, double* v3, double* s1, double* s2, double* s3) {
+    if (!c.xfn) return 0;
+    double* all[6] = {v1, v2, v3, s1, s2, s3};
+    double* flds[6];
+    int nf = 0;
+    for (double* a : all)
+        if (a) flds[nf++] = a;
+    const int np = (int)c.peers.size();
+    std::vector<std::vector<double>> sb(np), rb(np);
+    std::vector<double*> sp(np), rp(np);
+    std::vector<int64_t> sn(np), rn(np);
+    for (int q = 0; q < np; ++q) {
+        size_t ns = 0, nr = 0;
+        for (const auto& b : c.xsend[q]) ns += (size_t)(b[2] - b[1] + 1) * (b[4] - b[3] + 1) * (b[6] - b[5] + 1);
+        for (const auto& b : c.xrecv[q]) nr += (size_t)(b[2] - b[1] + 1) * (b[4] - b[3] + 1) * (b[6] - b[5] + 1);
+        sb[q].resize(ns * nf);
+        rb[q].resize(nr * nf);
+        part_pack(c, c.xsend[q], flds, nf, sb[q], false);
+        sp[q] = sb[q].data();
+        rp[q] = rb[q].data();
+        sn[q] = (int64_t)sb[q].size();
+        rn[q] = (int64_t)rb[q].size();
+    }
+    if (np && c.xfn(c.xuser, 0, np, c.peers.data(), sp.data(), sn.data(), rp.data(), rn.data()))
+        return fail(MGLET_ERR_ARG, "partition: the exchange function failed");
+    for (int q = 0; q < np; ++q) part_pack(c, c.xrecv[q], flds, nf, rb[q], true);
+    return 0;
+}
+
+// v[0..n) <- its maximum (op 1) or sum (op 2) over all ranks
+int part_allreduce(Ctx& c, double* v, int n, int op) {
+    if (!c.xfn) return 0;
+    double* b[1] = {v};
+    int64_t cnt[1] = {n};
+    if (c.xfn(c.xuser, op, 0, nullptr, b, cnt, nullptr, nullptr))
+        return fail(MGLET_ERR_ARG, "partition: the reduction failed");
+    return 0;
+}
+
 int64_t connect(Ctx& c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,
                 double* s2, double* s3, bool corners, bool normal, int forward) {
+    if (part_exchange(c, v1, v2, v3, s1, s2, s3)) return -1;
     int nplane = layers;
     int minl = c.minlevel, maxl = c.maxlevel;
     if (ilevel > 0) { minl = ilevel; maxl = ilevel; }
@@ -855,7 +924,10 @@ double maxabscal(Ctx& c, const double* PHI) {
     }
     double maxabs = 0.0;
     for (int g = 1; g <= c.ngrid; ++g)
-        maxabs = std::max(std::fabs(mg[g] * std::ldexp(1.0, c.maxlevel - c.g[g].level)), maxabs);
+        if (!c.g[g].halo)   // a copy of another rank's grid
+            maxabs = std::max(std::fabs(mg[g] * std::ldexp(1.0, c.maxlevel - c.g[g].level)), maxabs);
+    // MPI_Allreduce(MAX) of pressuresolver_mod.F90:295 (a failure leaves NaN)
+    if (part_allreduce(c, &maxabs, 1, 1)) return std::numeric_limits<double>::quiet_NaN();
     return maxabs;
 }
 
@@ -3615,12 +3687,21 @@ void itinfo(Ctx& c, double dt, mglet_itinfo* out) {
     double cm = 0.0, dm = 0.0, esum = 0.0, vol = 0.0;
     bool nan = false;
     for (int g = 1; g <= c.ngrid; ++g) {
+        if (c.g[g].halo) continue;   // another rank's grid
         cm = std::max(cm, cfl[g]);
         dm = std::max(dm, dmx[g]);
         if (vol + vs[g] > 0.0) esum = (esum * vol + es[g] * vs[g]) / (vol + vs[g]);
         else esum = 0.0;
         vol = vol + vs[g];
         if (!std::isfinite(cfl[g]) || !std::isfinite(dmx[g]) || !std::isfinite(es[g])) nan = true;
+    }
+    if (c.xfn) {
+        double mx[3] = {cm, dm, nan ? 1.0 : 0.0}, sm[2] = {esum * vol, vol};
+        if (part_allreduce(c, mx, 3, 1) || part_allreduce(c, sm, 2, 2)) nan = true;
+        cm = mx[0];
+        dm = mx[1];
+        nan = nan || mx[2] != 0.0;
+        esum = sm[1] > 0.0 ? sm[0] / sm[1] : 0.0;
     }
     out->cflmax = cm;
     out->divmax = dm;
@@ -4164,6 +4245,32 @@ int oracle_ctof(oracle_ctx* c, int ilevel, const char* ff, const char* fc) {
 int oracle_bound_pressure(oracle_ctx* c, int ilevel, const char* name, int withbp) {
     if (!c->f3.count(name)) return fail(MGLET_ERR_NAME, "bound_pressure: unknown field");
     bound_pressure(*c, ilevel, name, withbp != 0);
+    return 0;
+}
+
+int oracle_set_partition(oracle_ctx* c, const int32_t* halo, int32_t nsend, const int32_t* send,
+                         int32_t nrecv, const int32_t* recv, mglet_exchange_fn fn, void* user) {
+    if (!halo || !fn || c->minlevel != c->maxlevel)
+        return fail(MGLET_ERR_ARG, "set_partition: one level, halo flags and a function");
+    for (int g = 1; g <= c->ngrid; ++g) c->g[g].halo = halo[g - 1] != 0;
+    c->xfn = fn;
+    c->xuser = user;
+    c->peers.clear();
+    for (int r = 0; r < nsend; ++r) c->peers.push_back(send[8 * r]);
+    for (int r = 0; r < nrecv; ++r) c->peers.push_back(recv[8 * r]);
+    std::sort(c->peers.begin(), c->peers.end());
+    c->peers.erase(std::unique(c->peers.begin(), c->peers.end()), c->peers.end());
+    c->xsend.assign(c->peers.size(), {});
+    c->xrecv.assign(c->peers.size(), {});
+    auto add = [&](const int32_t* rows, int n, std::vector<std::vector<std::array<int, 7>>>& out) {
+        for (int r = 0; r < n; ++r) {
+            const int32_t* w = rows + 8 * r;
+            const int q = (int)(std::lower_bound(c->peers.begin(), c->peers.end(), w[0]) - c->peers.begin());
+            out[q].push_back({w[1], w[2], w[3], w[4], w[5], w[6], w[7]});
+        }
+    };
+    add(send, nsend, c->xsend);
+    add(recv, nrecv, c->xrecv);
     return 0;
 }
 
