@@ -80,7 +80,12 @@ NCU_TRAFFIC_PER_CELL = {
 # ncu (sm__inst_executed_pipe_fp64 x 32 over one launch on 1024 grids of 24^3,
 # parity build without FMA contraction); with the measured FP64 issue rate
 # they give each kernel's fraction of the second roof.
-FP64_INSTR_PER_CELL = {}
+FP64_INSTR_PER_CELL = {
+    "tstle4": 232650752 * 32 / (1024 * 13824),      # 525.9 (uniform-G shortcut)
+    "laplacephi": 5750784 * 32 / (1024 * 13824),    # 13.0
+    "sipiter1": 3850240 * 32 / (1024 * 13824),      # 8.70
+    "sipiter2": 3330048 * 32 / (1024 * 13824),      # 7.53
+}
 
 
 def kernel_bytes(name, case, ninner):
@@ -128,6 +133,13 @@ def parse():
                     help="skip the profiled pass (per-kernel times, roofline)")
     ap.add_argument("--precision", action="store_true",
                     help="error of the mixed form against the plain FP64 form")
+    ap.add_argument("--precision-field", choices=["solenoidal", "taylor-green"],
+                    default="solenoidal",
+                    help="with --precision: the solenoidal random field (nu=1e-3, dt=2e-4) or "
+                         "Taylor-Green plus noise (nu=1/1600, dt=5e-4)")
+    ap.add_argument("--parity", action="store_true",
+                    help="one time step of the plain FP64 form and of the CPU restatement on the "
+                         "full tiling, compared bit for bit")
     ap.add_argument("--adjoint", action="store_true",
                     help="dJ/df of the final kinetic energy by the discrete adjoint, timed, with a "
                          "finite-difference check")
@@ -371,7 +383,7 @@ def time_form(args, form, case, fields, local, dist, profile=True):
             kern[name] = (tot, n)
         s.profile(False)
     return {"solver": s, "ms": ms, "launches": launches, "clocks": clk, "ipcs": ipcs,
-            "kern": kern, "prof_ms": prof_ms, "step": step, "prm": prm}
+            "kern": kern, "prof_ms": prof_ms, "step": step, "prm": prm, "tuning": s.tuning()}
 
 
 def roofline(kern, case, ninner, prof_ms):
@@ -508,6 +520,7 @@ def run_ours(args, rank, world, local):
             "clocks": r["clocks"],
             "e2e": e2e,
             "gpu_launches": r["launches"],
+            "tuning": r["tuning"],
             "roofline": roof,
             "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in r["kern"].items()},
             "kernel_roofs": kernel_roofs(r["kern"], case, r["prm"].ninner, fp64),
@@ -539,20 +552,27 @@ def run_precision(args, rank, local):
         return 0
     torch.cuda.set_device(local)
     case = cases.periodic_box(*args.tiles, n=args.n)
-    u, v, w = cases.divergence_free_modes(case, nmodes=48, kpeak=4.0, urms=1.0, seed=4242)
-    p = np.zeros_like(u)
+    tg = args.precision_field == "taylor-green"
+    if tg:
+        u, v, w, p = init_fields(case)
+        nu, dtp = 1.0 / 1600, DT
+    else:
+        u, v, w = cases.divergence_free_modes(case, nmodes=48, kpeak=4.0, urms=1.0, seed=4242)
+        p = np.zeros_like(u)
+        nu, dtp = 1e-3, 2e-4
 
     def prm(form):
-        return abi.make_flow_params(gmol=1e-3, rho=1.0, epcorr=1e-10, nouter=40, ninner=5,
+        return abi.make_flow_params(gmol=nu, rho=1.0, epcorr=1e-10, nouter=40, ninner=5,
                                     nouter_min=0, form=form)
     ref = gpu.Solver(case, prm(abi.FORM_PLAIN), device=local)
     for nm, a in zip("UVWP", (u, v, w, p)):
         ref.set(nm, a)
     ref.connect(0, 2, "U", "V", "W", "P", corners=True)
-    ref.mgpoisl(1.0)   # discrete projection of the initial field
-    ref.set("P", p)
+    if not tg:
+        ref.mgpoisl(1.0)   # discrete projection of the initial field
+        ref.set("P", p)
     init = [ref.get(nm) for nm in "UVWP"]
-    div0 = ref.itinfo(2e-4).divmax
+    div0 = ref.itinfo(dtp).divmax
     mix = gpu.Solver(case, prm(abi.FORM_MIXED), device=local)
     for nm, a in zip("UVWP", init):
         mix.set(nm, a)
@@ -567,8 +587,8 @@ def run_precision(args, rank, local):
     t0 = time.perf_counter()
     for it in range(1, args.steps + 1):
         for irk in range(1, 4):
-            ipc["plain"] += ref.timeintegrate_flow(it, it, 0.0, 2e-4, irk, rk).ipc
-            ipc["mixed"] += mix.timeintegrate_flow(it, it, 0.0, 2e-4, irk, rk).ipc
+            ipc["plain"] += ref.timeintegrate_flow(it, it, 0.0, dtp, irk, rk).ipc
+            ipc["mixed"] += mix.timeintegrate_flow(it, it, 0.0, dtp, irk, rk).ipc
         if it % 50 == 0 or it == args.steps:
             fr = {nm: case.interior(ref.get(nm)) for nm in "UVWP"}
             fm = {nm: case.interior(mix.get(nm)) for nm in "UVWP"}
@@ -579,17 +599,59 @@ def run_precision(args, rank, local):
             num = sum(np.sum((fm[nm] - fr[nm]) ** 2) for nm in "UVW")
             den = sum(np.sum(fr[nm] ** 2) for nm in "UVW")
             row["velocity"] = float(np.sqrt(num / den))
-            row["divmax_mixed"] = mix.itinfo(2e-4).divmax
-            row["divmax_plain"] = ref.itinfo(2e-4).divmax
+            row["divmax_mixed"] = mix.itinfo(dtp).divmax
+            row["divmax_plain"] = ref.itinfo(dtp).divmax
             rows.append(row)
+    field = ("Taylor-Green + splitmix64 noise 1e-2 (seed 42), nu=1/1600, RK3 dt=5e-4" if tg else
+             "solenoidal random field (k ~ 4, rms 1), nu=1e-3, RK3 dt=2e-4")
     line = {"precision": "mixed vs plain FP64", "workload":
-            f"periodic {case.ngrid} x {args.n}^3 grids, solenoidal random field (k ~ 4, rms 1), "
-            "nu=1e-3, RK3 dt=2e-4, epcorr=1e-10 (nouter<=40)",
+            f"periodic {case.ngrid} x {args.n}^3 grids, {field}, epcorr=1e-10 (nouter<=40)",
             "steps": args.steps, "initial_divmax": div0, "errors": rows,
             "pressure_iterations": ipc, "seconds": time.perf_counter() - t0}
     print(json.dumps(line), flush=True)
     mix.close()
     ref.close()
+    return 0
+
+
+def run_parity(args, rank, local):
+    """The plain FP64 form against the CPU restatement on the bench workload
+    itself (4096 grids of 24^3, Taylor-Green + noise, dt = 5e-4): one time
+    step (three stages) on each, every field compared bit for bit."""
+    import numpy as np
+    import torch
+    from mglet_gb300 import gpu
+    from oracle import binding
+
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    binding.build()
+    case = make_case(args)
+    fields = init_fields(case)
+    prm = flow_params("plain")
+    g = gpu.Solver(case, prm, device=local)
+    o = binding.Oracle(case, prm)
+    for s in (g, o):
+        for nm, a in zip("UVWP", fields):
+            s.set(nm, a)
+        s.connect(0, 2, "U", "V", "W", "P", corners=True)
+    rkg, rko = gpu.rk_scheme("williamson"), binding.rk_scheme("williamson")
+    t0 = time.perf_counter()
+    stats = []
+    for irk in range(1, 4):
+        sg = g.timeintegrate_flow(1, 1, 0.0, DT, irk, rkg)
+        so = o.timeintegrate_flow(1, 1, 0.0, DT, irk, rko)
+        stats.append({"ipc": [sg.ipc, so.ipc], "maxrhs": [sg.maxrhs, so.maxrhs]})
+    eq = {nm: bool(np.array_equal(g.get(nm), o.get(nm)))
+          for nm in ("U", "V", "W", "P", "DU", "DV", "DW")}
+    line = {"parity": "plain FP64 GPU form vs CPU restatement, one time step",
+            "workload": f"periodic {case.ngrid} x {args.n}^3 grids ({case.ncells} cells), "
+                        "Taylor-Green + noise, RK3 dt=5e-4, SIP ninner=5 nouter=9",
+            "bit_exact": eq, "stages": stats, "seconds": time.perf_counter() - t0,
+            "oracle_threads": binding.max_threads()}
+    print(json.dumps(line), flush=True)
+    g.close()
     return 0
 
 
@@ -777,6 +839,8 @@ def main():
         if args.tiles == [16, 16, 16]:
             args.tiles = [8, 8, 8]
         return run_adjoint(args, rank, local)
+    if args.parity:
+        return run_parity(args, rank, local)
     if args.sphere:
         if args.tiles != [16, 16, 16]:
             raise SystemExit("--sphere runs the full configuration only")

@@ -796,6 +796,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     for (auto& kv : c->d_children) cudaFree(kv.second);
     for (auto& kv : c->fbuf) cudaFree(kv.second);
     cudaFree(c->d_hier);
+    cudaFree(c->d_ftoc_skip);
     cudaFree(c->d_pargrids);
     cudaFree(c->d_sptab);
     cudaFree(c->d_scabc_kind);

@@ -185,6 +185,7 @@ struct Ctx {
     // of fields other than U, V, W, allocated on first use
     std::vector<int4> hier;
     int4* d_hier = nullptr;
+    int* d_ftoc_skip = nullptr;     // [ngrid] sibling faces a grid does not restrict
     std::map<int, std::vector<int>> children;
     std::map<int, int*> d_children;
     std::vector<int> pgrids[6];

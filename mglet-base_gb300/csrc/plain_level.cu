@@ -316,6 +316,9 @@ struct FtocArgs {
     double* fc;
     const double *ddx, *ddy, *ddz;
     const double* bp;
+    // per grid: the faces (bit 2a low, 2a+1 high along axis a) whose coarse
+    // faces a later sibling restricts too; the later grid's value stands
+    const int* skip;
     // U V W, P for the scalar (volume) mean, G and H for the ghost-cell
     // forms of P and R
     char flag;
@@ -334,6 +337,13 @@ __global__ void k_ftoc(FtocArgs A) {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= ni * nj * nk) return;
     const int k = ks + 2 * (q % nk), j = js + 2 * ((q / nk) % nj), i = is + 2 * (q / (nk * nj));
+    // a staggered face two siblings share is written once, by the later
+    // grid, as the reference's grid-ordered unpack leaves it
+    const int sk = A.skip[g];
+    if ((f == 'U' && ((i == is && (sk & 1)) || (i == ie && (sk & 2)))) ||
+        (f == 'V' && ((j == js && (sk & 4)) || (j == je && (sk & 8)))) ||
+        (f == 'W' && ((k == ks && (sk & 16)) || (k == ke && (sk & 32)))))
+        return;
     const int kk = G.kk, jj = G.jj;
     const double* fv = A.ff + G.ip3;
     const double* ddx = A.ddx + G.ipx - 1;
@@ -959,6 +969,33 @@ int set_hierarchy(Ctx* c, const int32_t* iparent, const int32_t* pos) {
     c->hier = h;
     MG_CUDA(copy_on(c->stream, c->d_hier, c->hier.data(), c->hier.size() * sizeof(int4),
                     cudaMemcpyHostToDevice));
+    // siblings side by side restrict onto the same coarse face of their
+    // parent (U, V, W): the earlier grid of each such pair skips that face
+    {
+        std::vector<int> skip(c->ngrid, 0);
+        std::map<int, std::vector<int>> kids;
+        for (int g = 0; g < c->ngrid; ++g)
+            if (h[g].x >= 0) kids[h[g].x].push_back(g);
+        for (auto& kv : kids)
+            for (int a : kv.second)
+                for (int b : kv.second) {
+                    if (a >= b) continue;
+                    const DevGrid& A = c->grids[a];
+                    const int pa[3] = {h[a].y, h[a].z, h[a].w}, pb[3] = {h[b].y, h[b].z, h[b].w};
+                    const int half[3] = {(A.ii - 4) / 2, (A.jj - 4) / 2, (A.kk - 4) / 2};
+                    for (int ax = 0; ax < 3; ++ax) {
+                        bool same = true;
+                        for (int o = 0; o < 3; ++o)
+                            if (o != ax && pa[o] != pb[o]) same = false;
+                        if (!same) continue;
+                        if (pb[ax] == pa[ax] + half[ax]) skip[a] |= 2 << (2 * ax);   // b above a
+                        if (pa[ax] == pb[ax] + half[ax]) skip[a] |= 1 << (2 * ax);   // b below a
+                    }
+                }
+        if (!c->d_ftoc_skip) MG_CUDA(cudaMalloc(&c->d_ftoc_skip, c->ngrid * sizeof(int)));
+        MG_CUDA(copy_on(c->stream, c->d_ftoc_skip, skip.data(), c->ngrid * sizeof(int),
+                        cudaMemcpyHostToDevice));
+    }
     for (auto& kv : c->d_children) cudaFree(kv.second);
     c->d_children.clear();
     c->children.clear();
@@ -1223,6 +1260,7 @@ int launch_ftoc(Ctx* c, int ilevel, const double* ff, double* fc, char flag) {
     A.fc = fc;
     A.ddx = c->L("DDX"); A.ddy = c->L("DDY"); A.ddz = c->L("DDZ");
     A.bp = c->F("BP");
+    A.skip = c->d_ftoc_skip;
     A.flag = (flag == 'R' || flag == 'S' || flag == 'T') ? 'P' : flag;
     if (c->ibtype == 1 && flag == 'P') A.flag = 'G';       // gc_restrict_t
     if (c->ibtype == 1 && flag == 'R') A.flag = 'H';

@@ -43,6 +43,13 @@ MODULE mglet_gpu_mod
         INTEGER(c_int32_t) :: exploded, reserved
     END TYPE mglet_itinfo
 
+    ! Blocking fields of the ghost-cell IB for create_flowstencils (pointers
+    ! to field_t%arr of BP, BU, BV, BW, AREAU, AREAV, AREAW, BZELLTYP, icells,
+    ! nvecs(4, ncells), ucell(3, ncells))
+    TYPE, BIND(C) :: mglet_ib_geometry
+        TYPE(c_ptr) :: bp, bu, bv, bw, areau, areav, areaw, bzelltyp, icells, nvecs, ucell
+    END TYPE mglet_ib_geometry
+
     INTERFACE
         INTEGER(c_int) FUNCTION mglet_rk_init(name, rk) BIND(C, name="mglet_rk_init")
             IMPORT :: c_int, c_char, mglet_rk_scheme
@@ -259,6 +266,102 @@ MODULE mglet_gpu_mod
             CHARACTER(kind=c_char), INTENT(in) :: dp(*)
         END FUNCTION mglet_gpu_bound_pressure
 
+        INTEGER(c_int) FUNCTION mglet_gpu_tstle4(ctx) BIND(C, name="mglet_gpu_tstle4")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+        END FUNCTION mglet_gpu_tstle4
+
+        INTEGER(c_int) FUNCTION mglet_gpu_rkstep(ctx, p, dp, rhsp, frhs, dtfu) &
+                BIND(C, name="mglet_gpu_rkstep")
+            IMPORT :: c_int, c_ptr, c_char, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(in) :: p(*), dp(*), rhsp(*)
+            REAL(c_double), VALUE :: frhs, dtfu
+        END FUNCTION mglet_gpu_rkstep
+
+        INTEGER(c_int) FUNCTION mglet_gpu_divcal(ctx, div, fak) BIND(C, name="mglet_gpu_divcal")
+            IMPORT :: c_int, c_ptr, c_char, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(in) :: div(*)
+            REAL(c_double), VALUE :: fak
+        END FUNCTION mglet_gpu_divcal
+
+        INTEGER(c_int) FUNCTION mglet_gpu_laplacephi(ctx, res, phi) &
+                BIND(C, name="mglet_gpu_laplacephi")
+            IMPORT :: c_int, c_ptr, c_char
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(in) :: res(*), phi(*)
+        END FUNCTION mglet_gpu_laplacephi
+
+        INTEGER(c_int) FUNCTION mglet_gpu_mgpoisl(ctx, dt, ittot, irk, stats) &
+                BIND(C, name="mglet_gpu_mgpoisl")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double, mglet_stage_stats
+            TYPE(c_ptr), VALUE :: ctx
+            REAL(c_double), VALUE :: dt
+            INTEGER(c_int32_t), VALUE :: ittot, irk
+            TYPE(mglet_stage_stats), INTENT(out) :: stats
+        END FUNCTION mglet_gpu_mgpoisl
+
+        INTEGER(c_int) FUNCTION mglet_gpu_maskbp(ctx) BIND(C, name="mglet_gpu_maskbp")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+        END FUNCTION mglet_gpu_maskbp
+
+        INTEGER(c_int) FUNCTION mglet_gpu_getibvalues(ctx) BIND(C, name="mglet_gpu_getibvalues")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+        END FUNCTION mglet_gpu_getibvalues
+
+        INTEGER(c_int) FUNCTION mglet_gpu_adjoint_rk_stage(ctx, irk, dt, rk) &
+                BIND(C, name="mglet_gpu_adjoint_rk_stage")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double, mglet_rk_scheme
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: irk
+            REAL(c_double), VALUE :: dt
+            TYPE(mglet_rk_scheme), INTENT(in) :: rk
+        END FUNCTION mglet_gpu_adjoint_rk_stage
+
+        INTEGER(c_int) FUNCTION mglet_create_flowstencils(desc, geo, out) &
+                BIND(C, name="mglet_create_flowstencils")
+            IMPORT :: c_int, c_ptr, mglet_grid_desc, mglet_ib_geometry
+            TYPE(mglet_grid_desc), INTENT(in) :: desc
+            TYPE(mglet_ib_geometry), INTENT(in) :: geo
+            TYPE(c_ptr), INTENT(out) :: out
+        END FUNCTION mglet_create_flowstencils
+
+        INTEGER(c_int) FUNCTION mglet_flowstencils_size(s, igrid, comp, ncells, nxi, nxr) &
+                BIND(C, name="mglet_flowstencils_size")
+            IMPORT :: c_int, c_int32_t, c_int64_t, c_ptr
+            TYPE(c_ptr), VALUE :: s
+            INTEGER(c_int32_t), VALUE :: igrid, comp
+            INTEGER(c_int32_t), INTENT(out) :: ncells
+            INTEGER(c_int64_t), INTENT(out) :: nxi, nxr
+        END FUNCTION mglet_flowstencils_size
+
+        INTEGER(c_int) FUNCTION mglet_flowstencils_copy(s, igrid, comp, xpoli, xpolr, xpolrvel) &
+                BIND(C, name="mglet_flowstencils_copy")
+            IMPORT :: c_int, c_int32_t, c_int64_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: s
+            INTEGER(c_int32_t), VALUE :: igrid, comp
+            INTEGER(c_int64_t), INTENT(out) :: xpoli(*)
+            REAL(c_double), INTENT(out) :: xpolr(*), xpolrvel(*)
+        END FUNCTION mglet_flowstencils_copy
+
+        INTEGER(c_int) FUNCTION mglet_flowstencils_free(s) BIND(C, name="mglet_flowstencils_free")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: s
+        END FUNCTION mglet_flowstencils_free
+
+        INTEGER(c_int) FUNCTION mglet_gpu_set_partition(ctx, halo, nsend, send, nrecv, recv, &
+                fn, user) BIND(C, name="mglet_gpu_set_partition")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_funptr
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), INTENT(in) :: halo(*), send(*), recv(*)
+            INTEGER(c_int32_t), VALUE :: nsend, nrecv
+            TYPE(c_funptr), VALUE :: fn
+            TYPE(c_ptr), VALUE :: user
+        END FUNCTION mglet_gpu_set_partition
+
         INTEGER(c_int) FUNCTION mglet_gpu_itinfo(ctx, dt, out) BIND(C, name="mglet_gpu_itinfo")
             IMPORT :: c_int, c_ptr, c_double, mglet_itinfo
             TYPE(c_ptr), VALUE :: ctx
@@ -276,7 +379,9 @@ MODULE mglet_gpu_mod
         gpu_upload_stencils, gpu_start_ghostcell, gpu_set_hierarchy, gpu_ftoc, gpu_ctof, &
         gpu_bound_pressure, gpu_par_ftoc_norm, gpu_set_lesmodel, gpu_set_body_force, &
         gpu_energy_gradient, gpu_set_scalars, gpu_timeintegrate_scalar, gpu_set_scalar_bc, &
-        gpu_add_scalar_source
+        gpu_add_scalar_source, gpu_tstle4, gpu_rkstep, gpu_divcal, gpu_laplacephi, gpu_mgpoisl, &
+        gpu_maskbp, gpu_getibvalues, gpu_adjoint_rk_stage, mglet_ib_geometry, &
+        gpu_create_flowstencils
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -477,6 +582,93 @@ CONTAINS
             timeph, dt, INT(irk, c_int32_t), grk, st) /= 0) CALL errr(__FILE__, __LINE__)
         ipc = st%ipc
     END SUBROUTINE gpu_timeintegrate_flow
+
+    ! Drop-in for tstle4(uo, vo, wo, u, v, w, u, v, w, p, g) on the device
+    ! fields (src/flow/tstle4_mod.F90:13)
+    SUBROUTINE gpu_tstle4()
+        IF (mglet_gpu_tstle4(gctx) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_tstle4
+
+    ! Drop-in for rkstep(p, dp, rhsp, frhs, dtfu) (src/core/rungekutta_mod.F90:315)
+    SUBROUTINE gpu_rkstep(p, dp, rhsp, frhs, dtfu)
+        CHARACTER(len=*), INTENT(in) :: p, dp, rhsp
+        REAL(c_double), INTENT(in) :: frhs, dtfu
+        IF (mglet_gpu_rkstep(gctx, TRIM(p)//C_NULL_CHAR, TRIM(dp)//C_NULL_CHAR, &
+            TRIM(rhsp)//C_NULL_CHAR, frhs, dtfu) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_rkstep
+
+    ! Drop-in for ib%divcal(div, u, v, w, fak) (src/ib/noib_mod.F90:253)
+    SUBROUTINE gpu_divcal(div, fak)
+        CHARACTER(len=*), INTENT(in) :: div
+        REAL(c_double), INTENT(in) :: fak
+        IF (mglet_gpu_divcal(gctx, TRIM(div)//C_NULL_CHAR, fak) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_divcal
+
+    ! Drop-in for laplacephi(res, phi) (src/flow/laplacephi_mod.F90:14)
+    SUBROUTINE gpu_laplacephi(res, phi)
+        CHARACTER(len=*), INTENT(in) :: res, phi
+        IF (mglet_gpu_laplacephi(gctx, TRIM(res)//C_NULL_CHAR, TRIM(phi)//C_NULL_CHAR) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_laplacephi
+
+    ! Drop-in for mgpoisl(u, v, w, p, dt, ittot, irk)
+    ! (src/flow/pressuresolver_mod.F90:160)
+    SUBROUTINE gpu_mgpoisl(dt, ittot, irk, ipc)
+        REAL(c_double), INTENT(in) :: dt
+        INTEGER, INTENT(in) :: ittot, irk
+        INTEGER, INTENT(out) :: ipc
+        TYPE(mglet_stage_stats) :: st
+        IF (mglet_gpu_mgpoisl(gctx, dt, INT(ittot, c_int32_t), INT(irk, c_int32_t), st) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+        ipc = st%ipc
+    END SUBROUTINE gpu_mgpoisl
+
+    ! Drop-ins for maskbp(u, v, w, p) and getibvalues(u, v, w)
+    ! (src/flow/timeintegration_mod.F90:255, gc_flowstencils_mod.F90:1393)
+    SUBROUTINE gpu_maskbp()
+        IF (mglet_gpu_maskbp(gctx) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_maskbp
+
+    SUBROUTINE gpu_getibvalues()
+        IF (mglet_gpu_getibvalues(gctx) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_getibvalues
+
+    ! The adjoint of one stage (device fields LU.., GFX..; no reference
+    ! counterpart)
+    SUBROUTINE gpu_adjoint_rk_stage(irk, dt)
+        INTEGER, INTENT(in) :: irk
+        REAL(c_double), INTENT(in) :: dt
+        IF (mglet_gpu_adjoint_rk_stage(gctx, INT(irk, c_int32_t), dt, grk) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_adjoint_rk_stage
+
+    ! Replaces create_flowstencils (gc_flowstencils_mod.F90:37): builds every
+    ! grid's lists from the blocking fields and uploads them; call
+    ! gpu_start_ghostcell afterwards.
+    SUBROUTINE gpu_create_flowstencils(desc, geo)
+        TYPE(mglet_grid_desc), INTENT(in) :: desc
+        TYPE(mglet_ib_geometry), INTENT(in) :: geo
+        TYPE(c_ptr) :: s
+        INTEGER :: ig, comp
+        INTEGER(c_int32_t) :: nc
+        INTEGER(c_int64_t) :: nxi, nxr
+        INTEGER(c_int64_t), ALLOCATABLE :: xi(:)
+        REAL(c_double), ALLOCATABLE :: xr(:), xv(:)
+        IF (mglet_create_flowstencils(desc, geo, s) /= 0) CALL errr(__FILE__, __LINE__)
+        DO ig = 1, desc%ngrid
+            DO comp = 1, 4
+                IF (mglet_flowstencils_size(s, INT(ig, c_int32_t), INT(comp, c_int32_t), nc, nxi, &
+                    nxr) /= 0) CALL errr(__FILE__, __LINE__)
+                ALLOCATE(xi(MAX(nxi, 1_c_int64_t)), xr(MAX(nxr, 1_c_int64_t)), &
+                    xv(MAX(nxr, 1_c_int64_t)))
+                IF (mglet_flowstencils_copy(s, INT(ig, c_int32_t), INT(comp, c_int32_t), xi, xr, &
+                    xv) /= 0) CALL errr(__FILE__, __LINE__)
+                CALL gpu_upload_stencils(ig, comp, INT(nc), xi(1:nxi), xr(1:nxr), xv(1:nxr))
+                DEALLOCATE(xi, xr, xv)
+            END DO
+        END DO
+        IF (mglet_flowstencils_free(s) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_create_flowstencils
 
     SUBROUTINE gpu_itinfo(dt, cflmax, divmax, energy, exploded)
         REAL(c_double), INTENT(in) :: dt
