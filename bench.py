@@ -281,29 +281,60 @@ def cpu_sample(threads=None, tiles=(8, 8, 8), steps=4, warmup=1):
 
 
 def run_reference(args, rank):
+    """The CPU restatement of the reference path on the host cores, on the
+    same workload as the GPU arm (the full tiling, Taylor-Green + noise,
+    Williamson RK3, dt = 5e-4, the same SIP settings).  A time step of the
+    full tiling takes about half a minute on 16 cores, so the arm times at
+    most REF_STEPS of the requested steps after one warm-up step and says so
+    in its sample; the value is cell-updates per second of those steps."""
     if rank != 0:
         return 0
-    t_all = []
-    value = None
-    for s in range(args.warmup + args.steps):
-        v, nthreads, sample = cpu_sample(steps=1, warmup=0 if s else 1)
-        if s >= args.warmup:
-            t_all.append(v)
-    value = sum(t_all) / len(t_all)
+    from oracle import binding
+    binding.build()
+    case = make_case(args)
+    o = binding.Oracle(case, flow_params("plain"))
+    for nm, a in zip("UVWP", init_fields(case)):
+        o.set(nm, a)
+    o.connect(0, 2, "U", "V", "W", "P", corners=True)
+    rk = binding.rk_scheme("williamson")
+    nthreads = binding.max_threads()
+    warm = min(args.warmup, 1)
+    steps = max(1, min(args.steps, REF_STEPS))
+    it = 0
+    for _ in range(warm):
+        it += 1
+        for irk in range(1, 4):
+            o.timeintegrate_flow(it, it, 0.0, DT, irk, rk)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        it += 1
+        for irk in range(1, 4):
+            o.timeintegrate_flow(it, it, 0.0, DT, irk, rk)
+    dt = time.perf_counter() - t0
+    value = case.ncells * steps / dt
+    sample = (f"{args.tiles[0]}x{args.tiles[1]}x{args.tiles[2]} periodic tiling of {args.n}^3 grids "
+              f"({case.ncells} cells, the GPU arm's workload), {steps} timed steps after {warm} "
+              f"warm-up, {dt:.1f} s on {nthreads} threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": None,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt / steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic: Taylor-Green + splitmix64 noise (seed 42)",
-        "config": {"workload": "periodic 4096 x 24^3 grids (16x16x16), TG+noise, RK3 dt=5e-4, "
-                               "SIP ninner=5 nouter=9 epcorr=1e-10; each step a bounded sample",
-                   "sample_tiling": "8x8x8"},
+        "config": {"workload": f"periodic {case.ngrid} x {args.n}^3 grids "
+                               f"({args.tiles[0]}x{args.tiles[1]}x{args.tiles[2]}), TG+noise, RK3 "
+                               "dt=5e-4, SIP ninner=5 nouter=9 epcorr=1e-10",
+                   "timed_steps": steps, "same_config": True},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+# time steps of the full tiling the reference arm times (about 30 s each on
+# 16 host cores)
+REF_STEPS = 3
 
 
 def reduce_max(value, dist):
@@ -496,6 +527,10 @@ def run_ours(args, rank, world, local):
         try:
             v, nth, sample = cpu_sample()
             cpu = {"value": v, "unit": UNIT, "cores": nth, "kind": "port", "sample": sample}
+            v1, _, sample1 = cpu_sample(threads=1, tiles=(2, 2, 2), steps=2)
+            cpu["single_thread"] = {"value": v1, "unit": UNIT, "cores": 1, "sample": sample1}
+            from oracle import binding
+            binding.set_threads(nth)
         except Exception as ex:   # the baseline never blocks the GPU line
             cpu = {"value": None, "unit": UNIT, "cores": None, "kind": "port",
                    "sample": f"failed: {ex}"}

@@ -33,8 +33,13 @@
 namespace mg {
 
 int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
-                   const float* sz, const double* sprm);
+                   const float* sz, const double* sprm, int* err);
 int mx_flux_prepare(Ctx* c);
+void mx_flux_release(Ctx* c);
+int mx_flux_tune(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
+                 const float* sz, const double* sprm, int* err);
+int mx_flux_force(Ctx* c, int v);
+std::string mx_flux_tuning(Ctx* c);
 
 struct MixedState {
     int nclass = 0;
@@ -210,7 +215,8 @@ int enqueue_stage(Ctx* c) {
         set_error("mixed form: needs a uniform viscosity field G = gmol (no LES model)");
         return MGLET_ERR_UNSUPPORTED;
     }
-    if (int rc = launch_mx_flux(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, m->d_sprm))
+    if (int rc = launch_mx_flux(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, m->d_sprm,
+                                m->d_ctl + 2))
         return rc;
     if (int rc = connect(c, 0, 1, c->F("U"), c->F("V"), c->F("W"), nullptr, nullptr, nullptr, false,
                          true, 1))
@@ -223,7 +229,7 @@ int enqueue_stage(Ctx* c) {
 int check_device_flag(Ctx* c) {
     MixedState* m = c->mx;
     if (m->h_ctl[2] != 0) {
-        set_error("mixed form: the outer step timed out waiting for its bulk copies");
+        set_error("mixed form: a kernel timed out waiting for its bulk copies");
         return MGLET_ERR_CUDA;
     }
     return 0;
@@ -356,6 +362,9 @@ int mixed_init(Ctx* c) {
     const char* tune = std::getenv("MGLET_TUNE");
     if (!(tune && tune[0] == '0')) {
         if (int rc2 = sip_tune(c, m->sip, m->cf, m->d_gcls, m->d_ctl)) return rc2;
+        if (int rc2 = mx_flux_tune(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, m->d_sprm,
+                                   m->d_ctl + 2))
+            return rc2;
         MG_CUDA(cudaStreamSynchronize(c->stream));
     }
     return 0;
@@ -367,14 +376,22 @@ std::string mixed_tuning(Ctx* c) {
     if (!m) return "";
     const SipState& s = m->sip;
     char buf[256];
-    std::snprintf(buf, sizeof buf, "mx_sip_pre: %s%s (%.4f ms); uniform classes: %s",
+    std::snprintf(buf, sizeof buf, "mx_sip_pre: %s%s (%.4f ms); uniform classes: %s; ",
                   sip_pre_variant_name(s.pre_variant >= 0 ? s.pre_variant : 0),
                   s.pre_variant >= 0 ? "" : " [default]", s.pre_ms, s.unicls ? "yes" : "no");
-    return buf;
+    return buf + mx_flux_tuning(c);
 }
 
 int mixed_force_variant(Ctx* c, const char* kernel, int v) {
     MixedState* m = c->mx;
+    if (m && std::strcmp(kernel, "mx_flux") == 0) {
+        if (int rc = mx_flux_force(c, v)) return rc;
+        if (m->graph) {
+            cudaGraphExecDestroy(m->graph);
+            m->graph = nullptr;
+        }
+        return 0;
+    }
     if (!m || std::strcmp(kernel, "mx_sip_pre") != 0 || v < -1 || v >= sip_pre_variants()) {
         set_error("force_variant: needs the mixed form, kernel mx_sip_pre and a valid variant");
         return MGLET_ERR_ARG;
@@ -395,6 +412,7 @@ void mixed_release(Ctx* c) {
     MixedState* m = c->mx;
     if (!m) return;
     if (m->graph) cudaGraphExecDestroy(m->graph);
+    mx_flux_release(c);
     sip_release(m->sip);
     for (void* p : {(void*)m->cf, (void*)m->cb, (void*)m->apx, (void*)m->d_gcls,
                     (void*)m->d_ctl, (void*)m->d_maxrhs, (void*)m->d_sprm, (void*)m->du32, (void*)m->dv32,

@@ -23,7 +23,13 @@
 //
 // Requires a uniform viscosity field (G = gmol, no LES model) and CON faces;
 // the diffusive harmonic means then collapse to one host-computed constant.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include <algorithm>
+#include <cstdio>
+#include <map>
+#include <string>
 
 #include "internal.h"
 
@@ -68,8 +74,149 @@ struct FluxArgs {
     float rrho;
     float gpx, gpy, gpz;
     const double* sprm;                // [0] frhs, [1] dt*fu (device)
+    int* err;                          // set when a bulk-copy wait gives up
     int nslab;                         // j-slabs (CTAs) per grid
 };
+
+// j- and k-dependent spacing factors of one thread's (k, j) column
+struct Col {
+    float dy_j, ddy_j, rdy_j, rdy_jm, rddy_j, rddy_jp, ry1, ry0;
+    float dz_k, ddz_k, rdz_k, rdz_km, rddz_k, rddz_kp, rz1, rz0;
+};
+
+__device__ __forceinline__ Col column(const float* Y, long long ny, int j, const float* Z,
+                                      long long nz, int k) {
+    Col c;
+    c.dy_j = Y[j]; c.ddy_j = Y[ny + j]; c.rdy_j = Y[2 * ny + j]; c.rdy_jm = Y[2 * ny + j - 1];
+    c.rddy_j = Y[3 * ny + j]; c.rddy_jp = Y[3 * ny + j + 1];
+    c.ry1 = Y[4 * ny + j]; c.ry0 = Y[5 * ny + j];
+    c.dz_k = Z[k]; c.ddz_k = Z[nz + k]; c.rdz_k = Z[2 * nz + k]; c.rdz_km = Z[2 * nz + k - 1];
+    c.rddz_k = Z[3 * nz + k]; c.rddz_kp = Z[3 * nz + k + 1];
+    c.rz1 = Z[4 * nz + k]; c.rz0 = Z[5 * nz + k];
+    return c;
+}
+
+#define DX(i) X[(i)]
+#define DDX(i) X[nx + (i)]
+#define RDX(i) X[2 * nx + (i)]
+#define RDDX(i) X[3 * nx + (i)]
+#define RX1(i) X[4 * nx + (i)]
+#define RX0(i) X[5 * nx + (i)]
+
+// uo, vo, wo of the thread's point (window position q) on plane i from the
+// three-plane windows of (hi, lo) pairs (u, v, w: slots (i-1)%3, i%3,
+// (i+1)%3; p: slots i%2, (i+1)%2)
+__device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, long long nx,
+                                           const Col& cl, const float2* su, const float2* sv,
+                                           const float2* sw, const float2* sp, int plane, int pk,
+                                           int q, int i, float& uo, float& vo, float& wo) {
+    const float g = a.g, gh = a.gh;
+    const float dy_j = cl.dy_j, ddy_j = cl.ddy_j, rdy_j = cl.rdy_j, rdy_jm = cl.rdy_jm;
+    const float rddy_j = cl.rddy_j, rddy_jp = cl.rddy_jp, ry1 = cl.ry1, ry0 = cl.ry0;
+    const float dz_k = cl.dz_k, ddz_k = cl.ddz_k, rdz_k = cl.rdz_k, rdz_km = cl.rdz_km;
+    const float rddz_k = cl.rddz_k, rddz_kp = cl.rddz_kp, rz1 = cl.rz1, rz0 = cl.rz0;
+    const int sm1 = (i - 1) % 3, s0 = i % 3, sp1 = (i + 1) % 3;
+    const int p0 = i % 2, p1 = (i + 1) % 2;
+        const float2* u_m = su + sm1 * plane;
+        const float2* u_0 = su + s0 * plane;
+        const float2* u_p = su + sp1 * plane;
+        const float2* v_m = sv + sm1 * plane;
+        const float2* v_0 = sv + s0 * plane;
+        const float2* v_p = sv + sp1 * plane;
+        const float2* w_m = sw + sm1 * plane;
+        const float2* w_0 = sw + s0 * plane;
+        const float2* w_p = sw + sp1 * plane;
+        const float2* p_0 = sp + p0 * plane;
+        const float2* p_p = sp + p1 * plane;
+        const int qs = q - pk, qn = q + pk, qb = q - 1, qt = q + 1;   // j-1, j+1, k-1, k+1
+        const float fdx_i = DX(i), fddx = DDX(i), rdx_i = RDX(i), rdx_im = RDX(i - 1);
+        const float rddx_i = RDDX(i), rddx_ip = RDDX(i + 1), rx1 = RX1(i), rx0 = RX0(i);
+        const float fdy_j = dy_j, fddy = ddy_j, fdz_k = dz_k, fddz = ddz_k;
+        // ---------------- U at (k, j, i+1/2)
+        {
+            const float2 c = u_0[q];
+            const float cf = val(c);
+            const float dE = dif(u_p[q], c), dW = dif(u_m[q], c);
+            const float dN = dif(u_0[qn], c), dS = dif(u_0[qs], c);
+            const float dT = dif(u_0[qt], c), dB = dif(u_0[qb], c);
+            const float ax = fddy * fddz, ay = fdx_i * fddz, az = fdx_i * fddy;
+            const float fe = ax * (cf + 0.5f * dE * rx1);
+            const float fw = ax * (val(u_m[q]) - 0.5f * dW * rx0);
+            const float fn = 0.5f * ay * (val(v_0[q]) + val(v_p[q]));
+            const float fs = 0.5f * ay * (val(v_0[qs]) + val(v_p[qs]));
+            const float ft = 0.5f * az * (val(w_0[q]) + val(w_p[q]));
+            const float fb = 0.5f * az * (val(w_0[qb]) + val(w_p[qb]));
+            const float divf = ax * (-dW + 0.5f * dE * rx1 + 0.5f * dW * rx0) +
+                               0.5f * ay * (dif(v_0[q], v_0[qs]) + dif(v_p[q], v_p[qs])) +
+                               0.5f * az * (dif(w_0[q], w_0[qb]) + dif(w_p[q], w_p[qb]));
+            const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
+                                                  ft * dT - fb * dB);
+            const float vol = rdx_i * rddy_j * rddz_k;
+            const float conv = -sig * vol;
+            const float qd = -g * ax * (rddx_ip * dE + rddx_i * dW) -
+                             gh * ay * (rdy_j * dN + rdy_jm * dS) -
+                             gh * az * (rdz_k * dT + rdz_km * dB);
+            const float fak = a.rrho * vol;
+            const float gp = (dif(p_p[q], p_0[q]) + a.gpx * fdx_i) * (a.rrho / fdx_i);
+            uo = conv - fak * qd - gp;
+        }
+        // ---------------- V at (k, j+1/2, i)
+        {
+            const float2 c = v_0[q];
+            const float cf = val(c);
+            const float dE = dif(v_p[q], c), dW = dif(v_m[q], c);
+            const float dN = dif(v_0[qn], c), dS = dif(v_0[qs], c);
+            const float dT = dif(v_0[qt], c), dB = dif(v_0[qb], c);
+            const float ax = fdy_j * fddz, ay = fddx * fddz, az = fddx * fdy_j;
+            const float fe = 0.5f * ax * (val(u_0[q]) + val(u_0[qn]));
+            const float fw = 0.5f * ax * (val(u_m[q]) + val(u_m[qn]));
+            const float fn = ay * (cf + 0.5f * dN * ry1);
+            const float fs = ay * (val(v_0[qs]) - 0.5f * dS * ry0);
+            const float ft = 0.5f * az * (val(w_0[q]) + val(w_0[qn]));
+            const float fb = 0.5f * az * (val(w_0[qb]) + val(w_0[qb + pk]));
+            const float divf = 0.5f * ax * (dif(u_0[q], u_m[q]) + dif(u_0[qn], u_m[qn])) +
+                               ay * (-dS + 0.5f * dN * ry1 + 0.5f * dS * ry0) +
+                               0.5f * az * (dif(w_0[q], w_0[qb]) + dif(w_0[qn], w_0[qb + pk]));
+            const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
+                                                  ft * dT - fb * dB);
+            const float vol = rddx_i * rdy_j * rddz_k;
+            const float conv = -sig * vol;
+            const float qd = -gh * ax * (rdx_i * dE + rdx_im * dW) -
+                             g * ay * (rddy_jp * dN + rddy_j * dS) -
+                             gh * az * (rdz_k * dT + rdz_km * dB);
+            const float fak = a.rrho * vol;
+            const float gp = (dif(p_0[qn], p_0[q]) + a.gpy * fdy_j) * (a.rrho / fdy_j);
+            vo = conv - fak * qd - gp;
+        }
+        // ---------------- W at (k+1/2, j, i)
+        {
+            const float2 c = w_0[q];
+            const float cf = val(c);
+            const float dE = dif(w_p[q], c), dW = dif(w_m[q], c);
+            const float dN = dif(w_0[qn], c), dS = dif(w_0[qs], c);
+            const float dT = dif(w_0[qt], c), dB = dif(w_0[qb], c);
+            const float ax = fddy * fdz_k, ay = fddx * fdz_k, az = fddx * fddy;
+            const float fe = 0.5f * ax * (val(u_0[q]) + val(u_0[qt]));
+            const float fw = 0.5f * ax * (val(u_m[q]) + val(u_m[qt]));
+            const float fn = 0.5f * ay * (val(v_0[q]) + val(v_0[qt]));
+            const float fs = 0.5f * ay * (val(v_0[qs]) + val(v_0[qs + 1]));
+            const float ft = az * (cf + 0.5f * dT * rz1);
+            const float fb = az * (val(w_0[qb]) - 0.5f * dB * rz0);
+            const float divf = 0.5f * ax * (dif(u_0[q], u_m[q]) + dif(u_0[qt], u_m[qt])) +
+                               0.5f * ay * (dif(v_0[q], v_0[qs]) + dif(v_0[qt], v_0[qs + 1])) +
+                               az * (-dB + 0.5f * dT * rz1 + 0.5f * dB * rz0);
+            const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
+                                                  ft * dT - fb * dB);
+            const float vol = rddx_i * rddy_j * rdz_k;
+            const float conv = -sig * vol;
+            const float qd = -gh * ax * (rdx_i * dE + rdx_im * dW) -
+                             gh * ay * (rdy_j * dN + rdy_jm * dS) -
+                             g * az * (rddz_kp * dT + rddz_k * dB);
+            const float fak = a.rrho * vol;
+            const float gp = (dif(p_0[qt], p_0[q]) + a.gpz * fdz_k) * (a.rrho / fdz_k);
+            wo = conv - fak * qd - gp;
+        }
+}
 
 // One CTA per j-slab of a grid, one thread per interior (k, j) of the slab,
 // marching i.
@@ -111,19 +258,8 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     const float* Y = a.sy + G.ipy - 1;
     const float* Z = a.sz + G.ipz - 1;
     const long long nx = a.nx, ny = a.ny, nz = a.nz;
-#define DX(i) X[(i)]
-#define DDX(i) X[nx + (i)]
-#define RDX(i) X[2 * nx + (i)]
-#define RDDX(i) X[3 * nx + (i)]
-#define RX1(i) X[4 * nx + (i)]
-#define RX0(i) X[5 * nx + (i)]
     // j- and k-dependent factors are fixed per thread
-    const float dy_j = Y[j], ddy_j = Y[ny + j], rdy_j = Y[2 * ny + j], rdy_jm = Y[2 * ny + j - 1];
-    const float rddy_j = Y[3 * ny + j], rddy_jp = Y[3 * ny + j + 1];
-    const float ry1 = Y[4 * ny + j], ry0 = Y[5 * ny + j];
-    const float dz_k = Z[k], ddz_k = Z[nz + k], rdz_k = Z[2 * nz + k], rdz_km = Z[2 * nz + k - 1];
-    const float rddz_k = Z[3 * nz + k], rddz_kp = Z[3 * nz + k + 1];
-    const float rz1 = Z[4 * nz + k], rz0 = Z[5 * nz + k];
+    const Col cl = column(Y, ny, j, Z, nz, k);
 
     // own raw FP64 values of planes i (cur) and i+1, i+2 (pipeline)
     double ucur = 0, vcur = 0, wcur = 0, unx = 0, vnx = 0, wnx = 0;
@@ -159,113 +295,10 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     load_plane(4, 4 % 3, 4 % 2, true, unx, vnx, wnx);
     __syncthreads();
 
-    const float g = a.g, gh = a.gh;
     const int q = pl(k, j);
     for (int i = 3; i <= ii - 2; ++i) {
-        const int sm1 = (i - 1) % 3, s0 = i % 3, sp1 = (i + 1) % 3;
-        const int p0 = i % 2, p1 = (i + 1) % 2;
         float uo = 0.f, vo = 0.f, wo = 0.f;
-        if (on) {
-            const float2* u_m = su + sm1 * plane;
-            const float2* u_0 = su + s0 * plane;
-            const float2* u_p = su + sp1 * plane;
-            const float2* v_m = sv + sm1 * plane;
-            const float2* v_0 = sv + s0 * plane;
-            const float2* v_p = sv + sp1 * plane;
-            const float2* w_m = sw + sm1 * plane;
-            const float2* w_0 = sw + s0 * plane;
-            const float2* w_p = sw + sp1 * plane;
-            const float2* p_0 = sp + p0 * plane;
-            const float2* p_p = sp + p1 * plane;
-            const int qs = q - pk, qn = q + pk, qb = q - 1, qt = q + 1;   // j-1, j+1, k-1, k+1
-            const float fdx_i = DX(i), fddx = DDX(i), rdx_i = RDX(i), rdx_im = RDX(i - 1);
-            const float rddx_i = RDDX(i), rddx_ip = RDDX(i + 1), rx1 = RX1(i), rx0 = RX0(i);
-            const float fdy_j = dy_j, fddy = ddy_j, fdz_k = dz_k, fddz = ddz_k;
-            // ---------------- U at (k, j, i+1/2)
-            {
-                const float2 c = u_0[q];
-                const float cf = val(c);
-                const float dE = dif(u_p[q], c), dW = dif(u_m[q], c);
-                const float dN = dif(u_0[qn], c), dS = dif(u_0[qs], c);
-                const float dT = dif(u_0[qt], c), dB = dif(u_0[qb], c);
-                const float ax = fddy * fddz, ay = fdx_i * fddz, az = fdx_i * fddy;
-                const float fe = ax * (cf + 0.5f * dE * rx1);
-                const float fw = ax * (val(u_m[q]) - 0.5f * dW * rx0);
-                const float fn = 0.5f * ay * (val(v_0[q]) + val(v_p[q]));
-                const float fs = 0.5f * ay * (val(v_0[qs]) + val(v_p[qs]));
-                const float ft = 0.5f * az * (val(w_0[q]) + val(w_p[q]));
-                const float fb = 0.5f * az * (val(w_0[qb]) + val(w_p[qb]));
-                const float divf = ax * (-dW + 0.5f * dE * rx1 + 0.5f * dW * rx0) +
-                                   0.5f * ay * (dif(v_0[q], v_0[qs]) + dif(v_p[q], v_p[qs])) +
-                                   0.5f * az * (dif(w_0[q], w_0[qb]) + dif(w_p[q], w_p[qb]));
-                const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
-                                                      ft * dT - fb * dB);
-                const float vol = rdx_i * rddy_j * rddz_k;
-                const float conv = -sig * vol;
-                const float qd = -g * ax * (rddx_ip * dE + rddx_i * dW) -
-                                 gh * ay * (rdy_j * dN + rdy_jm * dS) -
-                                 gh * az * (rdz_k * dT + rdz_km * dB);
-                const float fak = a.rrho * vol;
-                const float gp = (dif(p_p[q], p_0[q]) + a.gpx * fdx_i) * (a.rrho / fdx_i);
-                uo = conv - fak * qd - gp;
-            }
-            // ---------------- V at (k, j+1/2, i)
-            {
-                const float2 c = v_0[q];
-                const float cf = val(c);
-                const float dE = dif(v_p[q], c), dW = dif(v_m[q], c);
-                const float dN = dif(v_0[qn], c), dS = dif(v_0[qs], c);
-                const float dT = dif(v_0[qt], c), dB = dif(v_0[qb], c);
-                const float ax = fdy_j * fddz, ay = fddx * fddz, az = fddx * fdy_j;
-                const float fe = 0.5f * ax * (val(u_0[q]) + val(u_0[qn]));
-                const float fw = 0.5f * ax * (val(u_m[q]) + val(u_m[qn]));
-                const float fn = ay * (cf + 0.5f * dN * ry1);
-                const float fs = ay * (val(v_0[qs]) - 0.5f * dS * ry0);
-                const float ft = 0.5f * az * (val(w_0[q]) + val(w_0[qn]));
-                const float fb = 0.5f * az * (val(w_0[qb]) + val(w_0[qb + pk]));
-                const float divf = 0.5f * ax * (dif(u_0[q], u_m[q]) + dif(u_0[qn], u_m[qn])) +
-                                   ay * (-dS + 0.5f * dN * ry1 + 0.5f * dS * ry0) +
-                                   0.5f * az * (dif(w_0[q], w_0[qb]) + dif(w_0[qn], w_0[qb + pk]));
-                const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
-                                                      ft * dT - fb * dB);
-                const float vol = rddx_i * rdy_j * rddz_k;
-                const float conv = -sig * vol;
-                const float qd = -gh * ax * (rdx_i * dE + rdx_im * dW) -
-                                 g * ay * (rddy_jp * dN + rddy_j * dS) -
-                                 gh * az * (rdz_k * dT + rdz_km * dB);
-                const float fak = a.rrho * vol;
-                const float gp = (dif(p_0[qn], p_0[q]) + a.gpy * fdy_j) * (a.rrho / fdy_j);
-                vo = conv - fak * qd - gp;
-            }
-            // ---------------- W at (k+1/2, j, i)
-            {
-                const float2 c = w_0[q];
-                const float cf = val(c);
-                const float dE = dif(w_p[q], c), dW = dif(w_m[q], c);
-                const float dN = dif(w_0[qn], c), dS = dif(w_0[qs], c);
-                const float dT = dif(w_0[qt], c), dB = dif(w_0[qb], c);
-                const float ax = fddy * fdz_k, ay = fddx * fdz_k, az = fddx * fddy;
-                const float fe = 0.5f * ax * (val(u_0[q]) + val(u_0[qt]));
-                const float fw = 0.5f * ax * (val(u_m[q]) + val(u_m[qt]));
-                const float fn = 0.5f * ay * (val(v_0[q]) + val(v_0[qt]));
-                const float fs = 0.5f * ay * (val(v_0[qs]) + val(v_0[qs + 1]));
-                const float ft = az * (cf + 0.5f * dT * rz1);
-                const float fb = az * (val(w_0[qb]) - 0.5f * dB * rz0);
-                const float divf = 0.5f * ax * (dif(u_0[q], u_m[q]) + dif(u_0[qt], u_m[qt])) +
-                                   0.5f * ay * (dif(v_0[q], v_0[qs]) + dif(v_0[qt], v_0[qs + 1])) +
-                                   az * (-dB + 0.5f * dT * rz1 + 0.5f * dB * rz0);
-                const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
-                                                      ft * dT - fb * dB);
-                const float vol = rddx_i * rddy_j * rdz_k;
-                const float conv = -sig * vol;
-                const float qd = -gh * ax * (rdx_i * dE + rdx_im * dW) -
-                                 gh * ay * (rdy_j * dN + rdy_jm * dS) -
-                                 g * az * (rddz_kp * dT + rddz_k * dB);
-                const float fak = a.rrho * vol;
-                const float gp = (dif(p_0[qt], p_0[q]) + a.gpz * fdz_k) * (a.rrho / fdz_k);
-                wo = conv - fak * qd - gp;
-            }
-        }
+        if (on) flux_point(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, uo, vo, wo);
         // issue the global loads of plane i+2 before the RK update and the barrier
         double unx2 = 0, vnx2 = 0, wnx2 = 0;
         __syncthreads();   // every thread is done with slot (i-1)%3 and p slot i%2
@@ -288,6 +321,197 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     }
 }
 
+// ---- the same kernel with the planes staged by TMA -------------------------
+// A wait for a bulk copy gives up after this many SM clock cycles (about one
+// second); a healthy wait lasts microseconds.
+constexpr long long kFluxWait = 2000000000LL;
+
+__device__ __forceinline__ unsigned fsm_u32(const void* p) {
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void fbar_init(unsigned long long* b) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(fsm_u32(b)));
+}
+
+__device__ __forceinline__ void fbar_expect(unsigned long long* b, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(fsm_u32(b)), "r"(bytes)
+                 : "memory");
+}
+
+// bounded wait for the phase of the given parity; false on timeout
+__device__ __forceinline__ bool fbar_wait(unsigned long long* b, unsigned parity) {
+    const long long t0 = clock64();
+    while (true) {
+        unsigned done;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+            " selp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(fsm_u32(b)), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if (clock64() - t0 > kFluxWait) return false;
+    }
+}
+
+// one (kk x jj) plane of a field, tensor coordinates (0, 0, z)
+__device__ __forceinline__ void tma_plane(double* dst, const CUtensorMap* m, int z,
+                                          unsigned long long* b) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(fsm_u32(dst)),
+        "l"((unsigned long long)m), "r"(0), "r"(0), "r"(z), "r"(fsm_u32(b))
+        : "memory");
+}
+
+// One CTA per grid (grids whose k x j interior fits one CTA), marching i.
+// Thread 0 issues TMA tensor copies of whole planes of U, V, W and P (each
+// a contiguous kk x jj slab of the grid) into two staging slots, two planes
+// ahead, completing on one mbarrier per slot; after a plane arrives every
+// thread splits its points of it (its own column and the window border)
+// into the (hi, lo) windows, as the plain-load kernel does from global
+// memory.  Same windows, same arithmetic (flux_point), same bits.
+__global__ void __launch_bounds__(576, 2)
+    k_mx_flux_tma(FluxArgs a, const __grid_constant__ CUtensorMap mu,
+                  const __grid_constant__ CUtensorMap mv, const __grid_constant__ CUtensorMap mw,
+                  const __grid_constant__ CUtensorMap mp) {
+    extern __shared__ __align__(128) unsigned char fraw[];
+    unsigned char* fsm = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<unsigned long long>(fraw) + 127) & ~127ULL);
+    const int gid = blockIdx.x;
+    const DevGrid G = a.grids[gid];
+    const int kk = G.kk, jj = G.jj, ii = G.ii, kj = kk * jj;
+    const int nk = kk - 4, nj = jj - 4, j0 = 3;
+    const int pk = kk - 2, pj = nj + 2, plane = pk * pj;
+    double* stage = reinterpret_cast<double*>(fsm);                 // [2][4][kj]
+    float2* su = reinterpret_cast<float2*>(fsm + (size_t)8 * kj * 8);
+    float2* sv = su + 3 * plane;
+    float2* sw = sv + 3 * plane;
+    float2* sp = sw + 3 * plane;
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(sp + 2 * plane);
+    const int t = threadIdx.x;
+    const bool on = t < nk * nj;
+    const int k = on ? t % nk + 3 : 3, j = on ? t / nk + j0 : j0;
+    const int nring = plane - nk * nj;
+    auto pl = [pk, j0](int kq, int jq) { return (kq - 2) + (jq - j0 + 1) * pk; };
+    auto ring = [&](int r, int& kq, int& jq) {
+        if (r < pk) { kq = 2 + r; jq = j0 - 1; return; }
+        r -= pk;
+        if (r < pk) { kq = 2 + r; jq = j0 + nj; return; }
+        r -= pk;
+        jq = j0 + r / 2;
+        kq = (r & 1) ? kk - 1 : 2;
+    };
+    const long long o = G.ip3;
+    const float* X = a.sx + G.ipx - 1;
+    const float* Y = a.sy + G.ipy - 1;
+    const float* Z = a.sz + G.ipz - 1;
+    const long long nx = a.nx, ny = a.ny, nz = a.nz;
+    const Col cl = column(Y, ny, j, Z, nz, k);
+    const int zbase = gid * ii;        // plane i of this grid is tensor z = zbase + i - 1
+    const unsigned bytes = (unsigned)(4 * kj * 8);
+    int last[2] = {0, 0};               // thread 0: plane last issued per slot
+    if (t == 0) {
+        fbar_init(&bar[0]);
+        fbar_init(&bar[1]);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    auto issue = [&](int pln) {
+        const int s = pln & 1;
+        double* d = stage + (size_t)s * 4 * kj;
+        fbar_expect(&bar[s], bytes);
+        tma_plane(d, &mu, zbase + pln - 1, &bar[s]);
+        tma_plane(d + kj, &mv, zbase + pln - 1, &bar[s]);
+        tma_plane(d + 2 * kj, &mw, zbase + pln - 1, &bar[s]);
+        tma_plane(d + 3 * kj, &mp, zbase + pln - 1, &bar[s]);
+        last[s] = pln;
+    };
+    // every thread waits for plane pln (slot pln & 1, its (pln-2)/2-th use)
+    auto arrived = [&](int pln) -> bool {
+        const bool ok = fbar_wait(&bar[pln & 1], (unsigned)(((pln - 2) >> 1) & 1));
+        return __syncthreads_and(ok) != 0;
+    };
+    auto fail = [&]() {
+        if (t == 0) {
+            atomicExch(a.err, 1);
+            // let the copies still in flight land before the CTA leaves
+            for (int s = 0; s < 2; ++s)
+                if (last[s]) fbar_wait(&bar[s], (unsigned)(((last[s] - 2) >> 1) & 1));
+        }
+    };
+    auto convert = [&](int pln, int slot3, int slot2, double& uo_, double& vo_, double& wo_) {
+        const double* Su = stage + (size_t)(pln & 1) * 4 * kj;
+        const double *Sv = Su + kj, *Sw = Sv + kj, *Sp = Sw + kj;
+        if (on) {
+            const int c = (j - 1) * kk + (k - 1);
+            const double u = Su[c], v = Sv[c], w = Sw[c];
+            uo_ = u; vo_ = v; wo_ = w;
+            const int q = pl(k, j);
+            su[slot3 * plane + q] = split64(u);
+            sv[slot3 * plane + q] = split64(v);
+            sw[slot3 * plane + q] = split64(w);
+            if (slot2 >= 0) sp[slot2 * plane + q] = split64(Sp[c]);
+        }
+        for (int r = t; r < nring; r += blockDim.x) {
+            int kq, jq;
+            ring(r, kq, jq);
+            const int c = (jq - 1) * kk + (kq - 1);
+            const int q = pl(kq, jq);
+            su[slot3 * plane + q] = split64(Su[c]);
+            sv[slot3 * plane + q] = split64(Sv[c]);
+            sw[slot3 * plane + q] = split64(Sw[c]);
+            if (slot2 >= 0) sp[slot2 * plane + q] = split64(Sp[c]);
+        }
+    };
+    double ucur = 0, vcur = 0, wcur = 0, unx = 0, vnx = 0, wnx = 0, d0, d1, d2;
+    if (t == 0) {
+        issue(2);
+        issue(3);
+    }
+    if (!arrived(2)) { fail(); return; }
+    convert(2, 2 % 3, -1, d0, d1, d2);
+    __syncthreads();
+    if (t == 0) issue(4);
+    if (!arrived(3)) { fail(); return; }
+    convert(3, 3 % 3, 3 % 2, ucur, vcur, wcur);
+    __syncthreads();
+    if (t == 0 && 5 <= ii - 1) issue(5);
+    if (!arrived(4)) { fail(); return; }
+    convert(4, 4 % 3, 4 % 2, unx, vnx, wnx);
+    __syncthreads();
+    if (t == 0 && 6 <= ii - 1) issue(6);
+
+    const int q = pl(k, j);
+    for (int i = 3; i <= ii - 2; ++i) {
+        float uo = 0.f, vo = 0.f, wo = 0.f;
+        if (on) flux_point(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, uo, vo, wo);
+        double unx2 = 0, vnx2 = 0, wnx2 = 0;
+        __syncthreads();   // every thread is done with slot (i-1)%3 and p slot i%2
+        if (i + 2 <= ii - 1) {
+            if (!arrived(i + 2)) { fail(); return; }
+            convert(i + 2, (i + 2) % 3, (i + 2) % 2, unx2, vnx2, wnx2);
+        }
+        if (on) {
+            const long long c = o + (long long)(i - 1) * kj + (long long)(j - 1) * kk + (k - 1);
+            const float frhs = (float)a.sprm[0];
+            const float du = frhs * a.DU[c] + uo;
+            const float dv = frhs * a.DV[c] + vo;
+            const float dw = frhs * a.DW[c] + wo;
+            a.DU[c] = du; a.DV[c] = dv; a.DW[c] = dw;
+            const float fdt = (float)a.sprm[1];
+            a.U[c] = ucur + (double)(fdt * du);
+            a.V[c] = vcur + (double)(fdt * dv);
+            a.W[c] = wcur + (double)(fdt * dw);
+        }
+        ucur = unx; vcur = vnx; wcur = wnx;
+        unx = unx2; vnx = vnx2; wnx = wnx2;
+        __syncthreads();   // staging slot (i+2)&1 consumed
+        if (t == 0 && i + 4 <= ii - 1) issue(i + 4);
+    }
+}
+
 }  // namespace
 
 // j-slabs per grid: the fewest for which a slab has at most 576 (k, j) columns
@@ -304,8 +528,57 @@ static size_t flux_smem(const DevGrid& G0) {
     return (size_t)11 * (G0.kk - 2) * (js + 2) * sizeof(float2);
 }
 
+// Per context: the tensor maps of U, V, W, P for the TMA variant and the
+// variant in use (0 plane loads, 1 TMA staging, -1 untuned default).
+struct FluxState {
+    CUtensorMap map[4];
+    bool tma = false;
+    int variant = -1;
+    double ms[2] = {0.0, 0.0};
+};
+static std::map<const Ctx*, FluxState> g_flux;
+
+static size_t flux_tma_smem(const DevGrid& G0) {
+    const size_t kj = (size_t)G0.kk * G0.jj, plane = (size_t)(G0.kk - 2) * (G0.jj - 2);
+    return 128 + 8 * kj * sizeof(double) + 11 * plane * sizeof(float2) + 16;
+}
+
+// 3-D tensor map over one field: (k, j, i + ii * grid), boxes of one plane
+static int encode_plane_map(Ctx* c, const double* base, CUtensorMap* m) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    if (!encode) {
+        cudaDriverEntryPointQueryResult q;
+        void* fn = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !fn) {
+            set_error("mixed form: cuTensorMapEncodeTiled is not available");
+            return MGLET_ERR_CUDA;
+        }
+        encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+    const DevGrid& G0 = c->grids[0];
+    const cuuint64_t dims[3] = {(cuuint64_t)G0.kk, (cuuint64_t)G0.jj,
+                                (cuuint64_t)G0.ii * (cuuint64_t)c->ngrid};
+    const cuuint64_t strides[2] = {(cuuint64_t)G0.kk * sizeof(double),
+                                   (cuuint64_t)G0.kk * G0.jj * sizeof(double)};
+    const cuuint32_t box[3] = {(cuuint32_t)G0.kk, (cuuint32_t)G0.jj, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 3, const_cast<double*>(base), dims,
+                              strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) {
+        set_error("mixed form: cuTensorMapEncodeTiled failed");
+        return MGLET_ERR_CUDA;
+    }
+    return 0;
+}
+
 // Checks the launch limits of the flux kernel for this grid shape and opts
-// in to the dynamic shared memory it needs.
+// in to the dynamic shared memory it needs; where a grid's k x j interior
+// fits one CTA and its planes meet the TMA rules (16-byte rows, boxes of at
+// most 256 points per side), also builds the TMA variant's tensor maps.
 int mx_flux_prepare(Ctx* c) {
     const DevGrid& G0 = c->grids[0];
     if (G0.kk - 4 > 576) {
@@ -318,17 +591,41 @@ int mx_flux_prepare(Ctx* c) {
         return MGLET_ERR_UNSUPPORTED;
     }
     MG_CUDA(cudaFuncSetAttribute(k_mx_flux, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    FluxState& fs = g_flux[c];
+    fs = FluxState();
+    const size_t tsm = flux_tma_smem(G0);
+    if (flux_slabs(G0) == 1 && (G0.kk * sizeof(double)) % 16 == 0 && G0.kk <= 256 &&
+        G0.jj <= 256 && tsm <= 113 * 1024) {
+        const char* names[4] = {"U", "V", "W", "P"};
+        for (int f = 0; f < 4; ++f)
+            if (int rc = encode_plane_map(c, c->F(names[f]), &fs.map[f])) return rc;
+        MG_CUDA(cudaFuncSetAttribute(k_mx_flux_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tsm));
+        fs.tma = true;
+    }
     return 0;
 }
 
-int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
-                   const float* sz, const double* sprm) {
-    ProfScope ps_(c, "mx_flux");
+void mx_flux_release(Ctx* c) { g_flux.erase(c); }
+
+static int launch_variant(Ctx* c, int v, const FluxArgs& a, int threads) {
     const DevGrid& G0 = c->grids[0];
-    const size_t smem = flux_smem(G0);
+    FluxState& fs = g_flux[c];
+    if (v == 1 && fs.tma)
+        k_mx_flux_tma<<<c->ngrid, threads, flux_tma_smem(G0), c->stream>>>(a, fs.map[0], fs.map[1],
+                                                                           fs.map[2], fs.map[3]);
+    else
+        k_mx_flux<<<c->ngrid * a.nslab, threads, flux_smem(G0), c->stream>>>(a);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+static FluxArgs flux_args(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
+                          const float* sz, const double* sprm, int* err, int* threads) {
+    const DevGrid& G0 = c->grids[0];
     const int nslab = flux_slabs(G0);
     const int js = (G0.jj - 4 + nslab - 1) / nslab;
-    const int threads = ((G0.kk - 4) * js + 31) / 32 * 32;
+    *threads = ((G0.kk - 4) * js + 31) / 32 * 32;
     FluxArgs a;
     a.nslab = nslab;
     a.grids = c->d_grids;
@@ -344,9 +641,70 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
     a.rrho = (float)(1.0 / c->prm.rho);
     a.gpx = (float)c->prm.gradp[0]; a.gpy = (float)c->prm.gradp[1]; a.gpz = (float)c->prm.gradp[2];
     a.sprm = sprm;
-    k_mx_flux<<<c->ngrid * nslab, threads, smem, c->stream>>>(a);
-    MG_LAUNCHED(c);
+    a.err = err;
+    return a;
+}
+
+// Times both variants on the current fields and keeps the faster; the
+// fields are still zero when the context is created, so the timing
+// launches leave them unchanged (zero fluxes, zero increments).
+int mx_flux_tune(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
+                 const float* sz, const double* sprm, int* err) {
+    FluxState& fs = g_flux[c];
+    if (!fs.tma) return 0;
+    int threads;
+    const FluxArgs a = flux_args(c, du, dv, dw, sx, sy, sz, sprm, err, &threads);
+    cudaEvent_t e0, e1;
+    MG_CUDA(cudaEventCreate(&e0));
+    MG_CUDA(cudaEventCreate(&e1));
+    for (int v = 0; v < 2; ++v) {
+        if (int rc = launch_variant(c, v, a, threads)) return rc;
+        cudaEventRecord(e0, c->stream);
+        for (int r = 0; r < 3; ++r)
+            if (int rc = launch_variant(c, v, a, threads)) return rc;
+        cudaEventRecord(e1, c->stream);
+        MG_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        fs.ms[v] = ms / 3.0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    fs.variant = fs.ms[1] < fs.ms[0] ? 1 : 0;
     return 0;
+}
+
+int mx_flux_force(Ctx* c, int v) {
+    FluxState& fs = g_flux[c];
+    if (v < -1 || v > 1) {
+        set_error("force_variant: mx_flux variants are 0 (plane loads) and 1 (TMA staging)");
+        return MGLET_ERR_ARG;
+    }
+    if (v == 1 && !fs.tma) {
+        set_error("force_variant: the TMA flux variant needs grids that fit one CTA");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    fs.variant = v;
+    return 0;
+}
+
+std::string mx_flux_tuning(Ctx* c) {
+    const FluxState& fs = g_flux[c];
+    char b[160];
+    const int v = fs.variant < 0 ? 0 : fs.variant;
+    std::snprintf(b, sizeof b, "mx_flux: %s%s (plane loads %.4f ms, TMA %.4f ms)",
+                  v == 1 ? "TMA tensor staging" : "plane loads", fs.variant < 0 ? " [default]" : "",
+                  fs.ms[0], fs.ms[1]);
+    return b;
+}
+
+int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
+                   const float* sz, const double* sprm, int* err) {
+    ProfScope ps_(c, "mx_flux");
+    int threads;
+    const FluxArgs a = flux_args(c, du, dv, dw, sx, sy, sz, sprm, err, &threads);
+    const FluxState& fs = g_flux[c];
+    return launch_variant(c, fs.variant == 1 ? 1 : 0, a, threads);
 }
 
 }  // namespace mg

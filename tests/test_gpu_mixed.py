@@ -202,3 +202,25 @@ def test_uniform_variant_refused_without_uniform_classes(gpu_lib):
     with pytest.raises(gpu_lib.MgletError):
         g.force_variant("mx_sip_pre", 5)
     g.force_variant("mx_sip_pre", 2)
+
+
+@pytest.mark.parametrize("n", [24, 8])
+def test_flux_tma_variant_agrees(gpu_lib, n):
+    """The flux kernel with its planes staged by TMA tensor copies gives the
+    same bits as the plane-load kernel (same windows, same arithmetic)."""
+    case = cases.periodic_box(2, 2, 1, n=n)
+    out = []
+    for v in (0, 1):
+        g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=3))
+        assert "mx_flux" in g.tuning()
+        g.force_variant("mx_flux", v)
+        _init(g, case)
+        rk = gpu_lib.rk_scheme("williamson")
+        for it in (1, 2):
+            for irk in range(1, 4):
+                st = g.timeintegrate_flow(it, it, 0.0, 5e-4, irk, rk)
+                assert np.isfinite(st.maxrhs)
+        out.append([g.get(nm) for nm in ("U", "V", "W", "P", "DU", "DV", "DW")])
+        g.close()
+    for a, b in zip(*out):
+        assert np.array_equal(a, b)
