@@ -123,7 +123,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--form", choices=["plain", "mixed"], default="mixed")
-    ap.add_argument("--tiles", type=int, nargs=3, default=[16, 16, 16])
+    ap.add_argument("--tiles", type=int, nargs=3, default=None,
+                    help="level-1 tiling (default 16 16 16; 8 8 8 for --precision and --adjoint)")
     ap.add_argument("--n", type=int, default=24)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -871,21 +872,20 @@ def main():
     if args.adjoint:
         if args.steps == 5:
             args.steps = 50
-        if args.tiles == [16, 16, 16]:
-            args.tiles = [8, 8, 8]
+        args.tiles = args.tiles or [8, 8, 8]
         return run_adjoint(args, rank, local)
-    if args.parity:
-        return run_parity(args, rank, local)
-    if args.sphere:
-        if args.tiles != [16, 16, 16]:
-            raise SystemExit("--sphere runs the full configuration only")
-        return run_sphere(args, rank, local)
     if args.precision:
         if args.steps == 5:
             args.steps = 200
-        if args.tiles == [16, 16, 16]:
-            args.tiles = [8, 8, 8]
+        args.tiles = args.tiles or [8, 8, 8]
         return run_precision(args, rank, local)
+    if args.sphere:
+        if args.tiles:
+            raise SystemExit("--sphere runs the full configuration only")
+        return run_sphere(args, rank, local)
+    args.tiles = args.tiles or [16, 16, 16]
+    if args.parity:
+        return run_parity(args, rank, local)
     if args.impl == "reference":
         return run_reference(args, rank)
     return run_ours(args, rank, world, local)

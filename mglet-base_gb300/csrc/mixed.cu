@@ -375,15 +375,31 @@ std::string mixed_tuning(Ctx* c) {
     MixedState* m = c->mx;
     if (!m) return "";
     const SipState& s = m->sip;
-    char buf[256];
-    std::snprintf(buf, sizeof buf, "mx_sip_pre: %s%s (%.4f ms); uniform classes: %s; ",
+    char buf[512];
+    std::snprintf(buf, sizeof buf,
+                  "mx_sip_pre: %s%s (%.4f ms); uniform classes: %s; sweeps: %s%s (%.4f ms per "
+                  "pair); ",
                   sip_pre_variant_name(s.pre_variant >= 0 ? s.pre_variant : 0),
-                  s.pre_variant >= 0 ? "" : " [default]", s.pre_ms, s.unicls ? "yes" : "no");
+                  s.pre_variant >= 0 ? "" : " [default]", s.pre_ms, s.unicls ? "yes" : "no",
+                  sip_sweep_variant_name(s.sweep_variant >= 0 ? s.sweep_variant : 0),
+                  s.sweep_variant >= 0 ? "" : " [default]", s.sweep_ms);
     return buf + mx_flux_tuning(c);
 }
 
 int mixed_force_variant(Ctx* c, const char* kernel, int v) {
     MixedState* m = c->mx;
+    if (m && std::strcmp(kernel, "mx_sip_sweep") == 0) {
+        if (v < -1 || v >= sip_sweep_variants()) {
+            set_error("force_variant: mx_sip_sweep variants are 0..4 (-1 default)");
+            return MGLET_ERR_ARG;
+        }
+        m->sip.sweep_variant = v;
+        if (m->graph) {
+            cudaGraphExecDestroy(m->graph);
+            m->graph = nullptr;
+        }
+        return 0;
+    }
     if (m && std::strcmp(kernel, "mx_flux") == 0) {
         if (int rc = mx_flux_force(c, v)) return rc;
         if (m->graph) {

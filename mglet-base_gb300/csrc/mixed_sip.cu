@@ -1036,6 +1036,48 @@ void launch_pre_variant(int v, int ngrid, size_t smem, cudaStream_t s, const Pre
     }
 }
 
+// Packed-sweep launch variants: ranks of a plane per thread, the CTA size
+// bound and minimum CTAs per SM (registers follow from these two).
+struct SweepVariant {
+    int pts, threads, minblocks;
+    const char* name;
+};
+const SweepVariant kSweepVariants[] = {
+    {2, 256, 8, "2 ranks/thread, 8 CTAs/SM"}, {3, 192, 9, "3 ranks/thread, 9 CTAs/SM"},
+    {4, 128, 12, "4 ranks/thread, 12 CTAs/SM"}, {2, 256, 7, "2 ranks/thread, 7 CTAs/SM"},
+    {3, 192, 8, "3 ranks/thread, 8 CTAs/SM"},
+};
+constexpr int kNumSweep = (int)(sizeof(kSweepVariants) / sizeof(kSweepVariants[0]));
+
+int sweep_threads_for(const SipState& st, int v) {
+    const int p = kSweepVariants[v].pts;
+    return ((st.maxlp + p - 1) / p + 31) / 32 * 32;
+}
+
+bool sweep_fits(const SipState& st, int v) {
+    return st.packed && sweep_threads_for(st, v) <= kSweepVariants[v].threads;
+}
+
+void launch_fwd_variant(int v, int ngrid, int threads, size_t smem, cudaStream_t s, const FwdArgs& a) {
+    switch (v) {
+        case 1: k_sip_fwd_packed<192, 9, 3><<<ngrid, threads, smem, s>>>(a); break;
+        case 2: k_sip_fwd_packed<128, 12, 4><<<ngrid, threads, smem, s>>>(a); break;
+        case 3: k_sip_fwd_packed<256, 7, 2><<<ngrid, threads, smem, s>>>(a); break;
+        case 4: k_sip_fwd_packed<192, 8, 3><<<ngrid, threads, smem, s>>>(a); break;
+        default: k_sip_fwd_packed<256, 8, 2><<<ngrid, threads, smem, s>>>(a); break;
+    }
+}
+
+void launch_bwd_variant(int v, int ngrid, int threads, size_t smem, cudaStream_t s, const BwdArgs& a) {
+    switch (v) {
+        case 1: k_sip_bwd_packed<192, 9, 3><<<ngrid, threads, smem, s>>>(a); break;
+        case 2: k_sip_bwd_packed<128, 12, 4><<<ngrid, threads, smem, s>>>(a); break;
+        case 3: k_sip_bwd_packed<256, 7, 2><<<ngrid, threads, smem, s>>>(a); break;
+        case 4: k_sip_bwd_packed<192, 8, 3><<<ngrid, threads, smem, s>>>(a); break;
+        default: k_sip_bwd_packed<256, 8, 2><<<ngrid, threads, smem, s>>>(a); break;
+    }
+}
+
 PreArgs pre_args(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rwrite,
                  bool hzero) {
     PreArgs p;
@@ -1057,6 +1099,10 @@ PreArgs pre_args(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ct
 }  // namespace
 
 int sip_pre_variants() { return kNumPre; }
+int sip_sweep_variants() { return kNumSweep; }
+const char* sip_sweep_variant_name(int v) {
+    return v >= 0 && v < kNumSweep ? kSweepVariants[v].name : "";
+}
 const char* sip_pre_variant_name(int v) { return v >= 0 && v < kNumPre ? kPreVariants[v].name : ""; }
 
 int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl) {
@@ -1103,11 +1149,66 @@ int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl) {
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    // the timing launches wrote res slot 0; leave the inner solver zeroed
-    MG_CUDA(cudaMemsetAsync(st.rs[0], 0, (size_t)c->ngrid * st.npp * sizeof(float), c->stream));
     st.pre_variant = best;
     st.pre_ms = best_ms;
     cache[key] = {best, best_ms};
+    // the packed sweeps: a forward + backward pair per variant
+    if (st.packed) {
+        static std::map<std::vector<long long>, std::pair<int, double>> scache;
+        auto sit = scache.find(key);
+        if (sit != scache.end()) {
+            st.sweep_variant = sit->second.first;
+            st.sweep_ms = sit->second.second;
+        } else {
+            FwdArgs fa;
+            fa.s = shape(st); fa.fnbr = st.d_fnbr; fa.gcls = gcls; fa.R = st.rs[0];
+            fa.RLOW = st.rs[1]; fa.CF = cf; fa.ctl = ctl; fa.SW = st.swf; fa.rev = 0;
+            BwdArgs ba;
+            ba.s = shape(st); ba.fnbr = st.d_fnbr; ba.gcls = gcls; ba.H = st.h32; ba.R = st.rs[0];
+            ba.CB = nullptr; ba.ctl = ctl; ba.hzero = 0; ba.SW = st.swb; ba.rev = 0;
+            int sbest = 0;
+            double sms = 1e30;
+            cudaEvent_t a0, a1;
+            MG_CUDA(cudaEventCreate(&a0));
+            MG_CUDA(cudaEventCreate(&a1));
+            for (int v = 0; v < kNumSweep; ++v) {
+                if (!sweep_fits(st, v)) continue;
+                const int th = sweep_threads_for(st, v);
+                for (int r = 0; r < 2; ++r) {
+                    launch_fwd_variant(v, c->ngrid, th, packed_smem(st), c->stream, fa);
+                    launch_bwd_variant(v, c->ngrid, th, packed_smem(st), c->stream, ba);
+                }
+                cudaEventRecord(a0, c->stream);
+                for (int r = 0; r < 4; ++r) {
+                    launch_fwd_variant(v, c->ngrid, th, packed_smem(st), c->stream, fa);
+                    launch_bwd_variant(v, c->ngrid, th, packed_smem(st), c->stream, ba);
+                }
+                cudaEventRecord(a1, c->stream);
+                cudaError_t e = cudaEventSynchronize(a1);
+                if (e == cudaSuccess) e = cudaGetLastError();
+                if (e != cudaSuccess) {
+                    cudaEventDestroy(a0);
+                    cudaEventDestroy(a1);
+                    return cuda_fail(e, "sip_tune: sweeps");
+                }
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, a0, a1);
+                if (ms / 4 < sms) {
+                    sms = ms / 4;
+                    sbest = v;
+                }
+            }
+            cudaEventDestroy(a0);
+            cudaEventDestroy(a1);
+            st.sweep_variant = sbest;
+            st.sweep_ms = sms;
+            scache[key] = {sbest, sms};
+        }
+    }
+    // the timing launches wrote the inner solver's arrays; leave them zeroed
+    for (int r = 0; r < 3; ++r)
+        MG_CUDA(cudaMemsetAsync(st.rs[r], 0, (size_t)c->ngrid * st.npp * sizeof(float), c->stream));
+    MG_CUDA(cudaMemsetAsync(st.h32, 0, (size_t)c->ngrid * st.npp * sizeof(float), c->stream));
     return 0;
 }
 
@@ -1450,7 +1551,10 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
     const int threads = sweep_threads(st);
     a.SW = st.swf;
     a.rev = next_order(st);
-    if (st.packed && threads <= 256)
+    if (st.packed && st.sweep_variant > 0 && sweep_fits(st, st.sweep_variant))
+        launch_fwd_variant(st.sweep_variant, c->ngrid, sweep_threads_for(st, st.sweep_variant),
+                           packed_smem(st), c->stream, a);
+    else if (st.packed && threads <= 256)
         k_sip_fwd_packed<256, 8, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
     else if (st.packed)
         k_sip_fwd_packed<512, 4, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
@@ -1478,7 +1582,10 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
     const int threads = sweep_threads(st);
     a.SW = st.swb;
     a.rev = next_order(st);
-    if (st.packed && threads <= 256)
+    if (st.packed && st.sweep_variant > 0 && sweep_fits(st, st.sweep_variant))
+        launch_bwd_variant(st.sweep_variant, c->ngrid, sweep_threads_for(st, st.sweep_variant),
+                           packed_smem(st), c->stream, a);
+    else if (st.packed && threads <= 256)
         k_sip_bwd_packed<256, 8, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
     else if (st.packed)
         k_sip_bwd_packed<512, 4, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);

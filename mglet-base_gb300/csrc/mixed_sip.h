@@ -50,6 +50,10 @@ struct SipState {
     // the tuner or forced by the caller; -1 = default
     int pre_variant = -1;
     double pre_ms = 0.0;        // its measured time per launch (tuner)
+    // launch variant of the packed sweeps (points per thread, CTAs per SM),
+    // -1 = default; the tuner's time of one forward + backward pair
+    int sweep_variant = -1;
+    double sweep_ms = 0.0;
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
@@ -75,5 +79,7 @@ int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl);
 // The pre-pass variants: count, and a description of variant v.
 int sip_pre_variants();
 const char* sip_pre_variant_name(int v);
+int sip_sweep_variants();
+const char* sip_sweep_variant_name(int v);
 
 }  // namespace mg

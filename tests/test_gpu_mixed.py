@@ -224,3 +224,23 @@ def test_flux_tma_variant_agrees(gpu_lib, n):
         g.close()
     for a, b in zip(*out):
         assert np.array_equal(a, b)
+
+
+def test_sweep_variants_agree(gpu_lib):
+    """The packed forward and backward sweeps in every launch variant the
+    tuner may pick (ranks per thread, CTAs per SM) give the same bits."""
+    case = cases.periodic_box(2, 2, 1, n=24)
+    out = []
+    for v in range(5):
+        g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=3))
+        assert "sweeps:" in g.tuning()
+        g.force_variant("mx_sip_sweep", v)
+        _init(g, case)
+        rk = gpu_lib.rk_scheme("williamson")
+        for irk in range(1, 4):
+            g.timeintegrate_flow(1, 1, 0.0, 5e-4, irk, rk)
+        out.append([g.get(nm) for nm in "UVWP"])
+        g.close()
+    for o in out[1:]:
+        for a, b in zip(out[0], o):
+            assert np.array_equal(a, b)
