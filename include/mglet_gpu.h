@@ -486,6 +486,13 @@ int mglet_gpu_set_partition(mglet_ctx* ctx, const int32_t* halo, int32_t nsend,
  * bits. */
 int mglet_gpu_tuning(mglet_ctx* ctx, char* buf, int64_t buflen);
 int mglet_gpu_force_variant(mglet_ctx* ctx, const char* kernel, int32_t variant);
+/* Test switch for the failure path of the bounded waits: the next mixed
+ * stage's flux kernel (TMA variant) leaves one plane's bulk copy out, so
+ * its mbarrier wait gives up after about a second, the kernel raises the
+ * control block's error flag and that stage returns MGLET_ERR_CUDA ("timed
+ * out waiting for its bulk copies"); the context stays usable and the next
+ * stage runs normally.  No fault, trap or hang is involved. */
+int mglet_gpu_test_wait_timeout(mglet_ctx* ctx);
 
 /* ---- Misc ----------------------------------------------------------------- */
 int mglet_gpu_synchronize(mglet_ctx* ctx);

@@ -1323,6 +1323,11 @@ int mglet_gpu_tuning(mglet_ctx* c, char* buf, int64_t buflen) {
     return 0;
 }
 
+int mglet_gpu_test_wait_timeout(mglet_ctx* c) {
+    if (!c) return fail(MGLET_ERR_ARG, "test_wait_timeout: null context");
+    return mixed_test_wait_timeout(c);
+}
+
 int mglet_gpu_force_variant(mglet_ctx* c, const char* kernel, int32_t variant) {
     if (!c || !kernel) return fail(MGLET_ERR_ARG, "force_variant: null argument");
     return mixed_force_variant(c, kernel, variant);

@@ -15,6 +15,7 @@ int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_sta
 int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st);
 std::string mixed_tuning(Ctx* c);
 int mixed_force_variant(Ctx* c, const char* kernel, int v);
+int mixed_test_wait_timeout(Ctx* c);
 
 // shared with api.cu
 int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,

@@ -75,6 +75,7 @@ struct FluxArgs {
     float gpx, gpy, gpz;
     const double* sprm;                // [0] frhs, [1] dt*fu (device)
     int* err;                          // set when a bulk-copy wait gives up
+    int skip_plane;                    // test switch: this plane's copy is not issued (0: none)
     int nslab;                         // j-slabs (CTAs) per grid
 };
 
@@ -420,6 +421,10 @@ __global__ void __launch_bounds__(576, 2)
     __syncthreads();
     auto issue = [&](int pln) {
         const int s = pln & 1;
+        if (pln == a.skip_plane) {   // test switch: the wait for this plane runs out
+            last[s] = 0;
+            return;
+        }
         double* d = stage + (size_t)s * 4 * kj;
         fbar_expect(&bar[s], bytes);
         tma_plane(d, &mu, zbase + pln - 1, &bar[s]);
@@ -642,6 +647,7 @@ static FluxArgs flux_args(Ctx* c, float* du, float* dv, float* dw, const float* 
     a.gpx = (float)c->prm.gradp[0]; a.gpy = (float)c->prm.gradp[1]; a.gpz = (float)c->prm.gradp[2];
     a.sprm = sprm;
     a.err = err;
+    a.skip_plane = 0;
     return a;
 }
 
@@ -699,12 +705,18 @@ std::string mx_flux_tuning(Ctx* c) {
 }
 
 int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
-                   const float* sz, const double* sprm, int* err) {
+                   const float* sz, const double* sprm, int* err, bool skip) {
     ProfScope ps_(c, "mx_flux");
     int threads;
-    const FluxArgs a = flux_args(c, du, dv, dw, sx, sy, sz, sprm, err, &threads);
+    FluxArgs a = flux_args(c, du, dv, dw, sx, sy, sz, sprm, err, &threads);
     const FluxState& fs = g_flux[c];
+    if (skip && fs.tma) {
+        a.skip_plane = 4;
+        return launch_variant(c, 1, a, threads);
+    }
     return launch_variant(c, fs.variant == 1 ? 1 : 0, a, threads);
 }
+
+bool mx_flux_has_tma(Ctx* c) { return g_flux[c].tma; }
 
 }  // namespace mg

@@ -36,6 +36,7 @@ EXPORTS = [
     "mglet_gpu_add_scalar_source", "mglet_gpu_fp64_roof", "mglet_gpu_tuning",
     "mglet_gpu_force_variant", "mglet_create_flowstencils", "mglet_flowstencils_size",
     "mglet_flowstencils_copy", "mglet_flowstencils_free", "mglet_gpu_set_partition",
+    "mglet_gpu_test_wait_timeout",
 ]
 
 
@@ -117,6 +118,7 @@ def load(path=None):
     L.mglet_gpu_fp64_roof.argtypes = [C.c_int32, C.POINTER(C.c_double)]
     L.mglet_gpu_tuning.argtypes = [vp, cp, C.c_int64]
     L.mglet_gpu_force_variant.argtypes = [vp, cp, C.c_int32]
+    L.mglet_gpu_test_wait_timeout.argtypes = [vp]
     L.mglet_create_flowstencils.argtypes = [vp, vp, C.POINTER(vp)]
     L.mglet_flowstencils_size.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                           C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
@@ -388,6 +390,9 @@ class Solver:
         buf = C.create_string_buffer(512)
         _check(load().mglet_gpu_tuning(self.h, buf, len(buf)))
         return buf.value.decode()
+
+    def test_wait_timeout(self):
+        _check(load().mglet_gpu_test_wait_timeout(self.h))
 
     def force_variant(self, kernel, variant):
         _check(load().mglet_gpu_force_variant(self.h, kernel.encode(), variant))

@@ -244,3 +244,23 @@ def test_sweep_variants_agree(gpu_lib):
     for o in out[1:]:
         for a, b in zip(out[0], o):
             assert np.array_equal(a, b)
+
+
+def test_bounded_wait_runs_out_and_recovers(gpu_lib):
+    """Failure detection without a fault: with the test switch the TMA flux
+    kernel leaves one plane's copy out, its mbarrier wait gives up after
+    about a second, the stage returns MGLET_ERR_CUDA, and the next stage on
+    the same context runs normally."""
+    case = cases.periodic_box(1, 1, 1, n=24)
+    g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=3))
+    _init(g, case)
+    g.force_variant("mx_flux", 1)
+    rk = gpu_lib.rk_scheme("williamson")
+    g.test_wait_timeout()
+    with pytest.raises(gpu_lib.MgletError) as err:
+        g.timeintegrate_flow(1, 1, 0.0, 5e-4, 1, rk)
+    assert err.value.code == abi.MGLET_ERR_CUDA and "timed out" in str(err.value)
+    st = g.timeintegrate_flow(1, 1, 0.0, 5e-4, 1, rk)
+    assert np.isfinite(st.maxrhs)
+    assert np.all(np.isfinite(g.get("U")))
+    g.close()
