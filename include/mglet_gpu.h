@@ -376,6 +376,17 @@ int mglet_gpu_set_ghostcell(mglet_ctx* ctx);
  * intersected cell, grid after grid, nvecs = the plane a x + b y + c z = dpl
  * of the body surface (unit normal pointing into the fluid) and ucell = the
  * body velocity.  Spacing comes from desc (x, dx give xstag = x + dx/2). */
+/* Bodies given as triangles (the reference reads STL, readstl.cxx): a closed,
+ * outward-oriented mesh of ntri triangles (9 doubles each) prepared for
+ * signed-distance queries (host only): phi[q] of point q, negative inside,
+ * and, unless normal is NULL, the unit direction from the closest surface
+ * point to the point, pointing out of the body.  The distances feed the
+ * blocking from which mglet_create_flowstencils builds the lists. */
+int mglet_mesh_create(const double* tri, int64_t ntri, void** mesh);
+int mglet_mesh_distance(const void* mesh, const double* pts, int64_t npts, double* phi,
+                        double* normal);
+int mglet_mesh_free(void* mesh);
+
 typedef struct mglet_ib_geometry {
     const double *bp, *bu, *bv, *bw;
     const double *areau, *areav, *areaw;

@@ -248,3 +248,130 @@ def block(case, body, samples=8):
     out["nvecs"] = np.concatenate(nvecs) if nvecs else np.zeros((0, 4))
     out["ucell"] = np.concatenate(ucell) if ucell else np.zeros((0, 3))
     return out
+
+
+# ---------------------------------------------------------------------------
+# Bodies given as triangles (STL), the reference's geometry input
+# (src/core/readstl.cxx): the library turns the mesh into signed distances
+# (mglet_mesh_create / mglet_mesh_distance), and the blocking above runs on
+# them unchanged.
+
+def read_stl(path):
+    """Triangles (ntri, 3, 3) of an ASCII or binary STL file."""
+    raw = open(path, "rb").read()
+    if len(raw) >= 84:
+        n = int(np.frombuffer(raw[80:84], dtype="<u4")[0])
+        if len(raw) == 84 + 50 * n:
+            rec = np.dtype([("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")])
+            return np.frombuffer(raw[84:], dtype=rec, count=n)["v"].astype(np.float64)
+    verts = []
+    for line in raw.decode("ascii", errors="replace").splitlines():
+        parts = line.split()
+        if parts and parts[0] == "vertex":
+            verts.append([float(v) for v in parts[1:4]])
+    a = np.array(verts, dtype=np.float64)
+    if len(a) % 3:
+        raise ValueError(f"{path}: vertex count {len(a)} is not a multiple of three")
+    return a.reshape(-1, 3, 3)
+
+
+def write_stl(path, tris, binary=True):
+    """Writes triangles (ntri, 3, 3) as STL (facet normals from the vertex order)."""
+    tris = np.asarray(tris, dtype=np.float64)
+    nrm = np.cross(tris[:, 1] - tris[:, 0], tris[:, 2] - tris[:, 0])
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-300)
+    if binary:
+        rec = np.zeros(len(tris), dtype=[("n", "<f4", 3), ("v", "<f4", (3, 3)), ("a", "<u2")])
+        rec["n"] = nrm
+        rec["v"] = tris
+        with open(path, "wb") as f:
+            f.write(b"binary STL".ljust(80, b" "))
+            f.write(np.array([len(tris)], dtype="<u4").tobytes())
+            f.write(rec.tobytes())
+        return
+    with open(path, "w") as f:
+        f.write("solid body\n")
+        for t, n in zip(tris, nrm):
+            f.write(f" facet normal {n[0]:.17g} {n[1]:.17g} {n[2]:.17g}\n  outer loop\n")
+            for v in t:
+                f.write(f"   vertex {v[0]:.17g} {v[1]:.17g} {v[2]:.17g}\n")
+            f.write("  endloop\n endfacet\n")
+        f.write("endsolid body\n")
+
+
+def icosphere(center, radius, level=3):
+    """A closed, outward-oriented triangle mesh of a sphere: the icosahedron
+    subdivided `level` times, vertices pushed onto the sphere."""
+    t = (1.0 + 5.0 ** 0.5) / 2.0
+    v = [(-1, t, 0), (1, t, 0), (-1, -t, 0), (1, -t, 0), (0, -1, t), (0, 1, t), (0, -1, -t),
+         (0, 1, -t), (t, 0, -1), (t, 0, 1), (-t, 0, -1), (-t, 0, 1)]
+    f = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4),
+         (11, 10, 2), (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8),
+         (3, 8, 9), (4, 9, 5), (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    verts = [np.array(p, dtype=np.float64) / np.linalg.norm(p) for p in v]
+    for _ in range(level):
+        mid = {}
+
+        def m(a, b):
+            key = (min(a, b), max(a, b))
+            if key not in mid:
+                p = verts[a] + verts[b]
+                verts.append(p / np.linalg.norm(p))
+                mid[key] = len(verts) - 1
+            return mid[key]
+
+        f = [tri for (a, b, c) in f
+             for tri in ((a, m(a, b), m(c, a)), (b, m(b, c), m(a, b)), (c, m(c, a), m(b, c)),
+                         (m(a, b), m(b, c), m(c, a)))]
+    V = np.array(verts) * radius + np.asarray(center, dtype=np.float64)
+    return V[np.array(f)]
+
+
+class Mesh:
+    """A body given by a closed, outward-oriented triangle mesh, with the
+    interface of Sphere (phi, plane, box_cut, reach) for block()."""
+
+    def __init__(self, tris):
+        import ctypes as C
+        from . import gpu
+        self._lib = gpu.load()
+        self.tris = np.ascontiguousarray(np.asarray(tris, dtype=np.float64).reshape(-1, 9))
+        self._h = C.c_void_p()
+        gpu._check(self._lib.mglet_mesh_create(self.tris.ctypes.data, len(self.tris),
+                                                C.byref(self._h)))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.mglet_mesh_free(self._h)
+            self._h = None
+
+    def _query(self, X, Y, Z, want_normal):
+        from . import gpu
+        X, Y, Z = np.broadcast_arrays(X, Y, Z)
+        pts = np.ascontiguousarray(np.stack([X.ravel(), Y.ravel(), Z.ravel()], axis=1))
+        phi = np.empty(len(pts))
+        nrm = np.empty((len(pts), 3)) if want_normal else None
+        gpu._check(self._lib.mglet_mesh_distance(self._h, pts.ctypes.data, len(pts),
+                                                 phi.ctypes.data,
+                                                 nrm.ctypes.data if want_normal else None))
+        return phi.reshape(X.shape), (nrm.reshape(X.shape + (3,)) if want_normal else None)
+
+    def phi(self, X, Y, Z):
+        return self._query(X, Y, Z, False)[0]
+
+    def plane(self, X, Y, Z):
+        phi, n = self._query(X, Y, Z, True)
+        P = np.stack(np.broadcast_arrays(X, Y, Z), axis=-1)
+        q = P - phi[..., None] * n
+        return np.concatenate([n, np.sum(n * q, axis=-1, keepdims=True)], axis=-1)
+
+    def box_cut(self, lo, hi):
+        c = 0.5 * (lo + hi)
+        half = 0.5 * np.linalg.norm(hi - lo, axis=-1)
+        return np.abs(self.phi(c[..., 0], c[..., 1], c[..., 2])) <= half
+
+    def reach(self, lo, hi):
+        c = 0.5 * (lo + hi)
+        half = 0.5 * float(np.linalg.norm(hi - lo))
+        d = abs(float(self.phi(np.array([c[0]]), np.array([c[1]]), np.array([c[2]]))[0]))
+        return max(0.0, d - half)

@@ -36,7 +36,7 @@ EXPORTS = [
     "mglet_gpu_add_scalar_source", "mglet_gpu_fp64_roof", "mglet_gpu_tuning",
     "mglet_gpu_force_variant", "mglet_create_flowstencils", "mglet_flowstencils_size",
     "mglet_flowstencils_copy", "mglet_flowstencils_free", "mglet_gpu_set_partition",
-    "mglet_gpu_test_wait_timeout",
+    "mglet_gpu_test_wait_timeout", "mglet_mesh_create", "mglet_mesh_distance", "mglet_mesh_free",
 ]
 
 
@@ -119,6 +119,9 @@ def load(path=None):
     L.mglet_gpu_tuning.argtypes = [vp, cp, C.c_int64]
     L.mglet_gpu_force_variant.argtypes = [vp, cp, C.c_int32]
     L.mglet_gpu_test_wait_timeout.argtypes = [vp]
+    L.mglet_mesh_create.argtypes = [vp, C.c_int64, C.POINTER(vp)]
+    L.mglet_mesh_distance.argtypes = [vp, vp, C.c_int64, vp, vp]
+    L.mglet_mesh_free.argtypes = [vp]
     L.mglet_create_flowstencils.argtypes = [vp, vp, C.POINTER(vp)]
     L.mglet_flowstencils_size.argtypes = [vp, C.c_int32, C.c_int32, C.POINTER(C.c_int32),
                                           C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
