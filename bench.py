@@ -62,17 +62,18 @@ MIXED_BYTES = {
 }
 
 
-# DRAM bytes per interior cell and launch measured by ncu (dram__bytes over one
-# launch on 1024 grids of 24^3), scaled to the bench case by the number of
-# cells; on 1024 grids part of the working set stays in L2, so these are lower
-# bounds for the full-size launch.
-NCU_TRAFFIC_PER_CELL = {
-    "mx_sip_fwd": 94.6e6 / (1024 * 13824),
-    "mx_sip_bwd": 127.6e6 / (1024 * 13824),
-    "mx_sip_pre": 140.7e6 / (1024 * 13824),
-    "mx_outer": 476.1e6 / (1024 * 13824),
-    "mx_flux": 1540.8e6 / (1024 * 13824),
+# DRAM bytes per launch measured by ncu on the default workload itself (4096
+# grids of 24^3): dram__bytes_read.sum and dram__bytes_write.sum of single
+# launches in steady state, averaged over the five inner iterations of one
+# outer iteration (the first of them starts from hilf = 0); scaled by cells
+# for other tilings.
+NCU_DRAM_4096 = {
+    "mx_sip_pre": (472.8e6, 184.3e6),
+    "mx_sip_fwd": (373.2e6, 168.0e6),
+    "mx_sip_bwd": (509.5e6, 177.3e6),
+    "mx_outer": (1263.3e6, 848.9e6),
 }
+NCU_CELLS = 4096 * 13824
 
 
 # FP64 thread instructions (DADD, DMUL, DFMA and the conversions the FP64 pipe
@@ -429,12 +430,16 @@ def roofline(kern, case, ninner, prof_ms):
     if not b or not n:
         return None
     achieved = b / (tot / n / 1e3) / 1e9
-    tpc = NCU_TRAFFIC_PER_CELL.get(top) if case.n_interior == 24 else None
-    traffic = tpc * case.ncells if tpc else None
+    rw = NCU_DRAM_4096.get(top) if case.n_interior == 24 else None
+    scale = case.ncells / NCU_CELLS
+    traffic = (rw[0] + rw[1]) * scale if rw else None
     return {"bound": "hbm", "kernel": top, "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
-            "traffic_source": ("ncu dram__bytes of one launch on 1024 x 24^3 grids, scaled by "
-                               "cells" if traffic else None),
+            "traffic_read": rw[0] * scale if rw else None,
+            "traffic_write": rw[1] * scale if rw else None,
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum per launch on "
+                               "4096 x 24^3 grids, mean over one outer iteration's launches"
+                               + ("" if scale == 1.0 else ", scaled by cells") if rw else None),
             "share": tot / prof_ms if prof_ms else None,
             "algorithmic_bytes_per_launch": b, "avg_launch_ms": tot / n}
 
