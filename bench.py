@@ -151,6 +151,10 @@ def parse():
     ap.add_argument("--sphere-check", action="store_true",
                     help="with --sphere: one RK stage of the full case on the GPU and on the CPU "
                          "restatement, compared bit for bit")
+    ap.add_argument("--channel", action="store_true",
+                    help="the sphere channel's three-level hierarchy without the body (1024 + 704 "
+                         "+ 2112 grids of 24^3, FIX inflow, OP1 outflow): the mixed form timed "
+                         "against the plain FP64 form, and their difference after the timed steps")
     ap.add_argument("--fd-dirs", type=int, default=20,
                     help="random directions of the adjoint's finite-difference check")
     return ap.parse_args()
@@ -776,8 +780,9 @@ def run_sphere(args, rank, local):
     grids, 53.1 M cells), the ghost-cell IB built from the sphere's signed
     distance, FIX inflow u = 1, OP1 outflow, periodic in y and z, Re_D = 300,
     dt of CFL 0.5 on the finest level, Williamson RK3, SIP ninner = 5,
-    nouter = 9, epcorr = 1e-10; plain FP64 form (the mixed form runs one
-    level).  Steps timed with CUDA events on the solver's stream."""
+    nouter = 9, epcorr = 1e-10; plain FP64 form (the ghost-cell IB runs in
+    the plain form only).  Steps timed with CUDA events on the solver's
+    stream."""
     import numpy as np
     import torch
     from mglet_gb300 import channel, gpu
@@ -871,6 +876,109 @@ def run_sphere(args, rank, local):
     return 0
 
 
+def run_channel(args, rank, local):
+    """The sphere channel's hierarchy without the sphere: 16 x 8 x 8 level-1
+    grids of 24^3 refined twice around the quarter point (1024 + 704 + 2112
+    grids, 53.1 M cells), FIX inflow u = 1, OP1 outflow, periodic in y and z,
+    nu = 1/300, a Taylor-Green perturbation of 10 % on the mean flow, dt of
+    CFL 0.5 on the finest level, Williamson RK3, SIP ninner = 5, nouter = 9,
+    epcorr = 1e-10.  The mixed form and the plain FP64 form each run the
+    warm-up and the timed steps from the same start (CUDA events on each
+    solver's stream); the line reports the mixed form and, beside it, the
+    plain one and the relative L2 difference of the fields after the run."""
+    import numpy as np
+    import torch
+    from mglet_gb300 import abi, cases, gpu
+
+    if rank != 0:
+        return 0
+    torch.cuda.set_device(local)
+    case = cases.body_refined(16, 8, 8, n=24, length=(8.0, 4.0, 4.0), center=(2.0, 2.0, 2.0),
+                              refine_radii=(1.0, 1.0), walls={1: abi.BC_FIX, 2: abi.BC_OP1})
+    levels = [int((case.level == lv).sum()) for lv in (1, 2, 3)]
+    u, v, w, p = cases.taylor_green(case)
+    init = dict(zip("UVWP", (1.0 + 0.1 * u, 0.1 * v, 0.1 * w, 0.01 * p)))
+    one = np.ones(case.kk * case.jj)
+    dt = 0.5 * float(case.ddx.min())
+    rk = gpu.rk_scheme("williamson")
+    out = {}
+    fields = {}
+    for form in (abi.FORM_MIXED, abi.FORM_PLAIN):
+        prm = abi.make_flow_params(gmol=1.0 / 300.0, epcorr=1e-10, nouter=9, ninner=5, nouter_min=0,
+                                   form=form)
+        s = gpu.Solver(case, prm, device=local)
+        s.set_hierarchy(case.iparent, case.position)
+        for g in range(case.ngrid):
+            if case.bctype[g, 0] == abi.BC_FIX:
+                s.set_buffer("U", g + 1, 1, one)
+        for nm, a in init.items():
+            s.set(nm, a)
+        for lvl in (1, 2, 3):
+            s.connect(lvl, 2, v1="U", v2="V", v3="W", s1="P", corners=True)
+        for lvl in (3, 2):
+            s.ftoc_multiple(lvl, v=("U", "V", "W"), s=("P",))
+        for lvl in (1, 2, 3):
+            s.connect(lvl, 1, v1="U", v2="V", v3="W", normal=True, forward=1)
+            s.parent(lvl, v=("U", "V", "W"), s=("P",))
+            s.bound_flow(lvl)
+        stream = torch.cuda.ExternalStream(s.stream, device=local)
+        it = [0]
+
+        def step():
+            it[0] += 1
+            st = None
+            for irk in range(1, 4):
+                st = s.timeintegrate_flow(it[0], it[0], 0.0, dt, irk, rk)
+            return st
+
+        for _ in range(args.warmup):
+            step()
+        s.synchronize()
+        clocks = Clocks(local)
+        torch.cuda.synchronize()
+        l0 = s.launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clocks.start()
+        e0.record(stream)
+        last = None
+        for _ in range(args.steps):
+            last = step()
+        e1.record(stream)
+        e1.synchronize()
+        clk = clocks.stop()
+        ms = e0.elapsed_time(e1)
+        out[form] = {"value": case.ncells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                     "launches": s.launches - l0, "clocks": clk,
+                     "nouter_last": last.nouter_done if last else None,
+                     "tuning": s.tuning() if form == abi.FORM_MIXED else ""}
+        fields[form] = {nm: case.interior(s.get(nm)) for nm in "UVWP"}
+        s.close()
+    fm, fp = fields[abi.FORM_MIXED], fields[abi.FORM_PLAIN]
+    num = sum(np.sum((fm[n] - fp[n]) ** 2) for n in "UVW")
+    den = sum(np.sum(fp[n] ** 2) for n in "UVW")
+    pm, pp = fm["P"] - fm["P"].mean(), fp["P"] - fp["P"].mean()
+    mixed, plain = out[abi.FORM_MIXED], out[abi.FORM_PLAIN]
+    line = {
+        "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 fluxes/sweeps, f64 storage",
+        "data": "synthetic: uniform inflow with a Taylor-Green perturbation",
+        "config": {"workload": f"channel 8 x 4 x 4, {levels[0]}+{levels[1]}+{levels[2]} grids of 24^3 "
+                               f"on 3 levels ({case.ncells} cells), FIX inflow, OP1 outflow, nu=1/300, "
+                               "CFL 0.5, RK3, SIP ninner=5 nouter=9 epcorr=1e-10",
+                   "form": "mixed", "cells": case.ncells, "grids_per_level": levels, "dt": dt,
+                   "l2": "working set > L2 (no flush needed)"},
+        "clocks": mixed["clocks"], "gpu_launches": mixed["launches"],
+        "nouter_last": mixed["nouter_last"], "tuning": mixed["tuning"],
+        "plain_fp64": {k: plain[k] for k in ("value", "ms_per_step", "launches", "nouter_last")},
+        "mixed_vs_plain": {"steps": args.warmup + args.steps,
+                           "velocity_rel_l2": float(np.sqrt(num / den)),
+                           "pressure_rel_l2": float(np.linalg.norm(pm - pp) / np.linalg.norm(pp))},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     args = parse()
     rank, world, local = dist_env()
@@ -888,6 +996,8 @@ def main():
         if args.tiles:
             raise SystemExit("--sphere runs the full configuration only")
         return run_sphere(args, rank, local)
+    if args.channel:
+        return run_channel(args, rank, local)
     args.tiles = args.tiles or [16, 16, 16]
     if args.parity:
         return run_parity(args, rank, local)

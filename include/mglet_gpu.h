@@ -66,10 +66,13 @@ enum {
     /* FP64 throughout, reference operation order, no FMA contraction:
      * the parity form (relative L2 <= 1e-12 against the FP64 oracle). */
     MGLET_FORM_PLAIN = 0,
-    /* Batched mixed precision: FP64 velocity/pressure, divergence,
-     * projection, outer defect-correction residual and reductions; FP32
-     * inner SIP sweeps; stage captured in one CUDA graph with a
-     * device-side convergence flag. */
+    /* Batched mixed precision: FP64 velocity/pressure storage, FP64
+     * projection and reductions, float-float outer defect-correction
+     * residual, FP32 fluxes and inner SIP sweeps; stage captured in one
+     * CUDA graph with a device-side convergence flag.  Runs grids of equal
+     * dimensions with CON, CO1, FIX, NOS, SLI, PAR (hierarchies, SIP on
+     * every level) and OP1 faces (OP1 on the high faces 2, 4, 6); the
+     * ghost-cell IB and LES models stay with the plain form. */
     MGLET_FORM_MIXED = 1
 };
 
@@ -226,8 +229,9 @@ int mglet_gpu_get_buffer(mglet_ctx* ctx, const char* name, int32_t igrid, int32_
                          double* host, int64_t n);
 
 /* ---- Grid hierarchies (more than one level, PAR faces) -------------------
- * A context may hold several levels with PAR (code 8) faces (plain form
- * only; the mixed form runs one level).  These module-level drop-ins then
+ * A context may hold several levels with PAR (code 8) faces (both forms;
+ * the mixed form's inner solver is SIP on every level).  These module-level
+ * drop-ins then
  * run on it, level by level as the reference calls them; mglet_gpu_tstle4
  * adds tstle4_par on PAR faces (src/flow/tstle4_mod.F90:532-1753), and
  * mglet_gpu_mgpoisl and mglet_gpu_timeintegrate_flow run the multi-level
@@ -488,12 +492,13 @@ int mglet_gpu_set_partition(mglet_ctx* ctx, const int32_t* halo, int32_t nsend,
 
 /* ---- Launch tuning of the mixed form (no counterpart in the reference) -----
  * mglet_gpu_create times the launch variants of the mixed form's pre-pass
- * (points loaded ahead, CTAs per SM, and the uniform-coefficient variant
- * where every coefficient class allows it) on the case itself and keeps the
+ * (points loaded ahead, CTAs per SM, records loaded ahead, hilf through L1,
+ * and the uniform-coefficient variants where every coefficient class allows
+ * them) on the case itself and keeps the
  * fastest, cached per grid shape for the process; the environment variable
  * MGLET_TUNE=0 keeps the defaults.  mglet_gpu_tuning describes the choice
  * ("" for the plain form); mglet_gpu_force_variant overrides it (kernel
- * "mx_sip_pre", variant 0..9, -1 = default).  All variants compute the same
+ * "mx_sip_pre", variant 0..14, -1 = default).  All variants compute the same
  * bits. */
 int mglet_gpu_tuning(mglet_ctx* ctx, char* buf, int64_t buflen);
 int mglet_gpu_force_variant(mglet_ctx* ctx, const char* kernel, int32_t variant);

@@ -691,9 +691,11 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     }
     // hierarchies: the level operators (parent, ftoc, ctof, bound_pressure,
     // bound_flow on PAR faces), tstle4 with tstle4_par, mgpoisl and the
-    // stage run on them in the plain form
-    if (c->minlevel != c->maxlevel && prm->form == MGLET_FORM_MIXED)
-        return bail(fail(MGLET_ERR_UNSUPPORTED, "create: the mixed form runs one grid level"));
+    // stage run on them in both forms; the mixed form's inner solver is SIP
+    // on every level
+    if (c->minlevel != c->maxlevel && prm->form == MGLET_FORM_MIXED &&
+        prm->psolver == MGLET_PSOLVER_SOR)
+        return bail(fail(MGLET_ERR_UNSUPPORTED, "create: the mixed form runs SIP on every level"));
     c->uniform = shapes.size() == 1;
     c->idim3d = o3; c->idimx = ox; c->idimy = oy; c->idimz = oz;
     MG_CUDA(cudaMalloc(&c->d_grids, c->ngrid * sizeof(DevGrid)));

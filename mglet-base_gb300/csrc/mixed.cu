@@ -28,6 +28,7 @@
 #include <vector>
 
 #include "mixed.h"
+#include "mixed_level.h"
 #include "mixed_sip.h"
 
 namespace mg {
@@ -57,6 +58,8 @@ struct MixedState {
     // FP32 spacing tables per axis: d, dd, rd, rdd, d(i)/dd(i+1), d(i-1)/dd(i)
     float *sx = nullptr, *sy = nullptr, *sz = nullptr;
     bool g_uniform = true;
+    bool walls = false;             // some grid has a FIX, OP1, NOS or SLI face
+    LevelState lv;                  // hierarchies: per-level lists (set up at the first stage)
     // device control block: [0] converged flag, [1] outer iterations done
     int* d_ctl = nullptr;
     // stage scalars read by the kernels from device memory, so that one
@@ -112,8 +115,9 @@ __global__ void k_mx_conv(const DevGrid* __restrict__ grids, int ngrid, int maxl
 
 #define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
 
-// mgpcorr on the interior only (the ghost layers it also touches in the
-// reference are overwritten by the closing connect), FP64.
+// mgpcorr (pressuresolver_mod.F90:808-844, no-BP form) over the reference's
+// ranges -- the pressure on the box 2..n-1, each velocity on its faces
+// 2..n-2 along its own axis -- in FP64, with dt/rho from the stage scalars.
 __global__ void k_mx_mgpcorr(const DevGrid* __restrict__ grids, double* U, double* V, double* W,
                              double* P, const double* __restrict__ DP, const double* __restrict__ RDX,
                              const double* __restrict__ RDY, const double* __restrict__ RDZ,
@@ -121,18 +125,23 @@ __global__ void k_mx_mgpcorr(const DevGrid* __restrict__ grids, double* U, doubl
     const DevGrid G = grids[blockIdx.y];
     const double rfak = sprm[3];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
-    const int ni = ii - 4, nj = jj - 4, nk = kk - 4;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= ni * nj * nk) return;
-    const int k = t % nk + 3, j = (t / nk) % nj + 3, i = t / (nk * nj) + 3;
+    if (t >= kk * jj * ii) return;
+    const int k = t % kk + 1, j = (t / kk) % jj + 1, i = t / (kk * jj) + 1;
     const long long o = G.ip3;
     const double* dp = DP + o;
     const long long c = IX(k, j, i);
+    const bool pi = i >= 2 && i <= ii - 1, pj = j >= 2 && j <= jj - 1, pk = k >= 2 && k <= kk - 1;
+    const bool ci = i >= 3 && i <= ii - 2, cj = j >= 3 && j <= jj - 2, ck = k >= 3 && k <= kk - 2;
+    if (!(pi && pj && pk)) return;
     const double d = dp[c];
     P[o + c] = P[o + c] + d;
-    U[o + c] = U[o + c] + (d - dp[c + (long long)kk * jj]) * RDX[G.ipx + i - 1] * rfak;
-    V[o + c] = V[o + c] + (d - dp[c + kk]) * RDY[G.ipy + j - 1] * rfak;
-    W[o + c] = W[o + c] + (d - dp[c + 1]) * RDZ[G.ipz + k - 1] * rfak;
+    if (i <= ii - 2 && cj && ck)
+        U[o + c] = U[o + c] + (d - dp[c + (long long)kk * jj]) * RDX[G.ipx + i - 1] * rfak;
+    if (ci && j <= jj - 2 && ck)
+        V[o + c] = V[o + c] + (d - dp[c + kk]) * RDY[G.ipy + j - 1] * rfak;
+    if (ci && cj && k <= kk - 2)
+        W[o + c] = W[o + c] + (d - dp[c + 1]) * RDZ[G.ipz + k - 1] * rfak;
 }
 
 __global__ void k_mx_setprm(double* sprm, int* err, double frhs, double dtfu, double prefak,
@@ -162,6 +171,8 @@ __global__ void k_cvt_32_64(double* d, const float* s, long long n) {
 int enqueue_mgpoisl(Ctx* c) {
     MixedState* m = c->mx;
     SipState& s = m->sip;
+    const LevelState& lv = m->lv;
+    const bool multi = c->minlevel != c->maxlevel;
     double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P"), *dp = c->F("DP");
     MG_CUDA(cudaMemsetAsync(s.dph, 0, (size_t)c->ngrid * s.npp * sizeof(float), c->stream));
     MG_CUDA(cudaMemsetAsync(s.dpl, 0, (size_t)c->ngrid * s.npp * sizeof(float), c->stream));
@@ -170,18 +181,51 @@ int enqueue_mgpoisl(Ctx* c) {
     MG_CUDA(cudaMemsetAsync(m->d_ctl, 0, 2 * sizeof(int), c->stream));
     if (int rc = sip_divcal(c, s, m->d_sprm + 2)) return rc;
     int* ctl = m->d_ctl;
+    // pressuresolver_mod.F90:196-199: the divergence restricted into the
+    // coarse grids, finest level first
+    for (int l = c->maxlevel; l > c->minlevel; --l)
+        if (int rc = mx_ftoc(c, s, lv, l, true, ctl)) return rc;
     const int ninner = c->prm.ninner;
-    int gi = 0, lastfull = 0;
+    // per level: inner iterations run and the last one whose res exchange
+    // covered every face (the rotating res slots of each level's grids)
+    const int nl = c->maxlevel - c->minlevel + 1;
+    std::vector<int> gi(nl, 0), lastfull(nl, 0);
     for (int ipcount = 1; ipcount <= c->prm.nouter; ++ipcount) {
-        for (int iloop = 1; iloop <= ninner; ++iloop) {
-            ++gi;
-            const bool hz = iloop == 1;
-            const int rlow = lastfull > 0 ? lastfull % 3 : -1;
-            if (int rc = sip_forward(c, s, m->cf, m->d_gcls, ctl, rlow, gi % 3, hz)) return rc;
-            if (int rc = sip_backward(c, s, m->cb, m->d_gcls, ctl, gi % 3, hz)) return rc;
-            if (iloop < ninner) lastfull = gi;
+        // pressuresolver_mod.F90:218-302: level by level, coarse to fine
+        for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+            const int li = l - c->minlevel;
+            const int* glist = multi ? lv.d_grids[li] : nullptr;
+            const int nlist = multi ? (int)lv.grids[li].size() : c->ngrid;
+            if (!nlist) continue;
+            if (multi && l > c->minlevel)
+                if (int rc = mx_ctof(c, s, lv, l, ctl)) return rc;
+            for (int iloop = 1; iloop <= ninner; ++iloop) {
+                if (multi)
+                    if (int rc = mx_bound_pressure(c, s, lv, l, ctl)) return rc;
+                ++gi[li];
+                // hilf starts at zero on the coarsest level (accumulate_pcorr
+                // cleared it); the finer levels start from the ctof values
+                const bool hz = iloop == 1 && l == c->minlevel;
+                const int rlow = lastfull[li] > 0 ? lastfull[li] % 3 : -1;
+                if (int rc = sip_forward(c, s, m->cf, m->d_gcls, ctl, rlow, gi[li] % 3, hz, glist,
+                                         nlist))
+                    return rc;
+                if (int rc = sip_backward(c, s, m->cb, m->d_gcls, ctl, gi[li] % 3, hz, glist, nlist))
+                    return rc;
+                if (iloop < ninner) lastfull[li] = gi[li];
+            }
+            if (multi)
+                if (int rc = mx_bound_pressure(c, s, lv, l, ctl)) return rc;
         }
+        for (int l = c->maxlevel; l > c->minlevel; --l)
+            if (int rc = mx_ftoc(c, s, lv, l, false, ctl)) return rc;
         if (int rc = sip_outer(c, s, m->apx, m->d_gcls, ctl)) return rc;
+        if (multi) {
+            // the residual restricted into the coarse grids, then its maxima again
+            for (int l = c->maxlevel; l > c->minlevel; --l)
+                if (int rc = mx_ftoc(c, s, lv, l, true, ctl)) return rc;
+            if (int rc = mx_gridmax(c, s, ctl)) return rc;
+        }
         {
             ProfScope ps_(c, "mx_conv");
             k_mx_conv<<<1, 1024, 0, c->stream>>>(c->d_grids, c->ngrid, c->maxlevel, c->d_gridred,
@@ -194,14 +238,45 @@ int enqueue_mgpoisl(Ctx* c) {
     // dp ghosts (the reference accumulates the connected hilf ghosts into dp)
     if (int rc = connect(c, 0, 1, nullptr, nullptr, nullptr, dp, nullptr, nullptr, false, false, 0))
         return rc;
+    if (multi) {
+        // pressuresolver_mod.F90:319-323: parent and bound_pressure of dp
+        static const char* const none[3] = {nullptr, nullptr, nullptr};
+        static const char* const sdp[3] = {"DP", nullptr, nullptr};
+        double* dbuf = field_buffer(c, "DP");
+        for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+            if (int rc = launch_parent(c, l, none, sdp, false)) return rc;
+            if (int rc = launch_bound_pressure(c, l, dp, dbuf, false)) return rc;
+        }
+    }
     {
         ProfScope ps_(c, "mx_mgpcorr");
-        dim3 grid((s.npts + 255) / 256, c->ngrid);
+        dim3 grid((s.kk * s.jj * s.ii + 255) / 256, c->ngrid);
         k_mx_mgpcorr<<<grid, 256, 0, c->stream>>>(c->d_grids, U, V, W, P, dp, c->L("RDX"),
                                                   c->L("RDY"), c->L("RDZ"), m->d_sprm);
         MG_LAUNCHED(c);
     }
-    if (int rc = connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
+    if (multi) {
+        // pressuresolver_mod.F90:334-348: ftoc fine to coarse, then per level
+        // parent, bound_flow and the corner connect
+        for (int l = c->maxlevel; l >= c->minlevel; --l) {
+            if (int rc = launch_ftoc(c, l, U, U, 'U')) return rc;
+            if (int rc = launch_ftoc(c, l, V, V, 'V')) return rc;
+            if (int rc = launch_ftoc(c, l, W, W, 'W')) return rc;
+            if (int rc = launch_ftoc(c, l, P, P, 'P')) return rc;
+        }
+        static const char* const vuvw[3] = {"U", "V", "W"};
+        static const char* const sp[3] = {"P", nullptr, nullptr};
+        for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+            if (int rc = launch_parent(c, l, vuvw, sp, false)) return rc;
+            if (int rc = launch_bound_flow(c, U, V, W, P, l)) return rc;
+            if (int rc = connect(c, l, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
+        }
+    } else {
+        // pressuresolver_mod.F90:341-348: bound_flow, then the corner connect
+        if (m->walls)
+            if (int rc = launch_bound_flow(c, U, V, W, P, 0)) return rc;
+        if (int rc = connect(c, 0, 2, U, V, W, P, nullptr, nullptr, true, false, 0)) return rc;
+    }
     MG_CUDA(cudaMemcpyAsync(m->h_ctl, m->d_ctl, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     MG_CUDA(cudaMemcpyAsync(m->h_maxrhs, m->d_maxrhs, sizeof(double), cudaMemcpyDeviceToHost,
                             c->stream));
@@ -228,9 +303,26 @@ int enqueue_stage(Ctx* c) {
     if (int rc = launch_mx_flux(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, m->d_sprm,
                                 m->d_ctl + 2, skip))
         return rc;
-    if (int rc = connect(c, 0, 1, c->F("U"), c->F("V"), c->F("W"), nullptr, nullptr, nullptr, false,
-                         true, 1))
-        return rc;
+    double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P");
+    if (c->minlevel == c->maxlevel) {
+        if (int rc = connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
+        // timeintegration_mod.F90:117-122: bound_flow after the connect
+        if (m->walls)
+            if (int rc = launch_bound_flow(c, U, V, W, P, 0)) return rc;
+        return enqueue_mgpoisl(c);
+    }
+    // grids with a PAR face: tstle4_par (tstle4_mod.F90:114) on the fluxes
+    // the flux kernel left in UO, VO, WO, then their RK update
+    if (int rc = launch_tstle4_par(c, c->F("UO"), c->F("VO"), c->F("WO"), U, V, W, U, V, W)) return rc;
+    if (int rc = mx_rk_par(c, m->lv, m->du32, m->dv32, m->dw32, m->d_sprm)) return rc;
+    // timeintegration_mod.F90:117-122: per level connect, parent, bound_flow
+    static const char* const vn[3] = {"U", "V", "W"};
+    static const char* const sn[3] = {"P", nullptr, nullptr};
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+        if (int rc = connect(c, l, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
+        if (int rc = launch_parent(c, l, vn, sn, false)) return rc;
+        if (int rc = launch_bound_flow(c, U, V, W, P, l)) return rc;
+    }
     return enqueue_mgpoisl(c);
 }
 
@@ -265,10 +357,6 @@ float* du_buffer(Ctx* c, const char* name) {
 }  // namespace
 
 int mixed_init(Ctx* c) {
-    if (c->minlevel != c->maxlevel) {
-        set_error("mixed form: one grid level only");
-        return MGLET_ERR_UNSUPPORTED;
-    }
     if (!c->uniform) {
         set_error("mixed form: all grids must have the same dimensions");
         return MGLET_ERR_UNSUPPORTED;
@@ -277,8 +365,26 @@ int mixed_init(Ctx* c) {
         set_error("mixed form: ninner must be at least 1");
         return MGLET_ERR_UNSUPPORTED;
     }
+    bool walls = false;
+    for (const DevGrid& G : c->grids)
+        for (int f = 0; f < 6; ++f) {
+            const int t = G.bc[f];
+            // tstle4 extends the flux ranges of an outflow face on the low
+            // side over the ghost plane (nfu, nrv, nbw), which this form's
+            // interior sweep does not visit
+            if (t == MGLET_BC_OP1 && f % 2 == 0) {
+                set_error("mixed form: OP1 only on the high faces (2, 4, 6)");
+                return MGLET_ERR_UNSUPPORTED;
+            }
+            walls |= t == MGLET_BC_FIX || t == MGLET_BC_OP1 || t == MGLET_BC_NOS ||
+                     t == MGLET_BC_SLI;
+        }
     MixedState* m = new MixedState();
     c->mx = m;
+    m->walls = walls;
+    // the ghosts of DP that no exchange writes (faces without a neighbour)
+    // must read zero in mgpcorr, as in the reference
+    MG_CUDA(cudaMemsetAsync(c->F("DP"), 0, (size_t)c->idim3d * sizeof(double), c->stream));
     if (int rc = sip_init(c, m->sip)) return rc;
     if (int rc = mx_flux_prepare(c)) return rc;
     m->d_idx = c->hp[0].d_idx;
@@ -432,7 +538,7 @@ int mixed_force_variant(Ctx* c, const char* kernel, int v) {
         set_error("force_variant: needs the mixed form, kernel mx_sip_pre and a valid variant");
         return MGLET_ERR_ARG;
     }
-    if (v >= 5 && !m->sip.unicls) {
+    if (sip_pre_variant_uniform(v) && !m->sip.unicls) {
         set_error("force_variant: the uniform pre-pass needs classes with constant coefficients");
         return MGLET_ERR_UNSUPPORTED;
     }
@@ -449,6 +555,7 @@ void mixed_release(Ctx* c) {
     if (!m) return;
     if (m->graph) cudaGraphExecDestroy(m->graph);
     mx_flux_release(c);
+    mx_level_release(m->lv);
     sip_release(m->sip);
     for (void* p : {(void*)m->cf, (void*)m->cb, (void*)m->apx, (void*)m->d_gcls,
                     (void*)m->d_ctl, (void*)m->d_maxrhs, (void*)m->d_sprm, (void*)m->du32, (void*)m->dv32,
@@ -479,7 +586,16 @@ void mixed_field_sync_out(Ctx* c, const char* name) {
         k_cvt_32_64<<<(unsigned)((c->idim3d + 255) / 256), 256, 0, c->stream>>>(c->F(name), f, c->idim3d);
 }
 
+// Hierarchies: the per-level lists and buffers, once the parents are known
+// (before the first stage is captured).
+static int levels_ready(Ctx* c) {
+    MixedState* m = c->mx;
+    if (c->minlevel == c->maxlevel || m->lv.ready) return 0;
+    return mx_level_prepare(c, m->sip, m->lv);
+}
+
 int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st) {
+    if (int rc = levels_ready(c)) return rc;
     // frhs and dt*fu are not read by the solve
     if (int rc = set_stage_scalars(c, 0.0, 0.0, dt)) return rc;
     if (int rc = enqueue_mgpoisl(c)) return rc;
@@ -500,6 +616,7 @@ int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_sta
         set_error("mixed form: needs a uniform viscosity field G = gmol (no LES model)");
         return MGLET_ERR_UNSUPPORTED;
     }
+    if (int rc = levels_ready(c)) return rc;
     if (int rc = set_stage_scalars(c, frhs, dt * fu, dtrk * dt)) return rc;
     if (c->prof || m->skip_once) {
         if (int rc = enqueue_stage(c)) return rc;

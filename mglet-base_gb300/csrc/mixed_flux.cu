@@ -21,12 +21,19 @@
 //    in shared memory; every thread owns one (k, j) column and keeps the raw
 //    FP64 value of its own points for the update, so u is updated exactly.
 //
-// Requires a uniform viscosity field (G = gmol, no LES model) and CON faces;
-// the diffusive harmonic means then collapse to one host-computed constant.
+// Requires a viscosity field without an LES model (G = gmol inside every
+// grid): away from faces without a neighbour the diffusive harmonic means
+// collapse to one host-computed constant.  Grids with FIX, OP1, NOS, SLI or
+// PAR faces take a second instantiation that reads G on their outermost
+// interior layer, drops the wall-normal flux points tstle4 does not compute
+// and adds the Werner-Wengle wall shear of NOS faces; on grids with a PAR
+// face it writes the fluxes to UO, VO, WO instead, for tstle4_par and the
+// separate RK update.
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <map>
 #include <string>
@@ -74,6 +81,15 @@ struct FluxArgs {
     float rrho;
     float gpx, gpy, gpz;
     const double* sprm;                // [0] frhs, [1] dt*fu (device)
+    // grids with faces that have no neighbour (walls, inflow, outflow):
+    // the viscosity field read next to those faces, the FP64 cell widths
+    // and width**(-1/7) of the wall function, the Werner-Wengle constants
+    const double* G;
+    const double *ddx, *ddy, *ddz, *wwx, *wwy, *wwz;
+    // grids with a PAR face: their fluxes go to UO, VO, WO (tstle4_par and
+    // the RK update follow in separate kernels)
+    double *UO, *VO, *WO;
+    double wrho, wgmol, cpo4, cpo5, cpo6, cpo8;
     int* err;                          // set when a bulk-copy wait gives up
     int skip_plane;                    // test switch: this plane's copy is not issued (0: none)
     int nslab;                         // j-slabs (CTAs) per grid
@@ -97,6 +113,14 @@ __device__ __forceinline__ Col column(const float* Y, long long ny, int j, const
     return c;
 }
 
+// Face viscosities of one component (east, west, north, south, top, bottom)
+struct Visc {
+    float e, w, n, s, t, b;
+};
+struct Visc3 {
+    Visc u, v, w;
+};
+
 #define DX(i) X[(i)]
 #define DDX(i) X[nx + (i)]
 #define RDX(i) X[2 * nx + (i)]
@@ -107,10 +131,14 @@ __device__ __forceinline__ Col column(const float* Y, long long ny, int j, const
 // uo, vo, wo of the thread's point (window position q) on plane i from the
 // three-plane windows of (hi, lo) pairs (u, v, w: slots (i-1)%3, i%3,
 // (i+1)%3; p: slots i%2, (i+1)%2)
+// kW: the face viscosities come from vs (grids with boundary faces); else
+// every face has the uniform a.g / a.gh.  gfl is the grid's gradpflag.
+template <bool kW>
 __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, long long nx,
                                            const Col& cl, const float2* su, const float2* sv,
                                            const float2* sw, const float2* sp, int plane, int pk,
-                                           int q, int i, float& uo, float& vo, float& wo) {
+                                           int q, int i, float gfl, const Visc3& vs, float& uo,
+                                           float& vo, float& wo) {
     const float g = a.g, gh = a.gh;
     const float dy_j = cl.dy_j, ddy_j = cl.ddy_j, rdy_j = cl.rdy_j, rdy_jm = cl.rdy_jm;
     const float rddy_j = cl.rddy_j, rddy_jp = cl.rddy_jp, ry1 = cl.ry1, ry0 = cl.ry0;
@@ -154,11 +182,14 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                                                   ft * dT - fb * dB);
             const float vol = rdx_i * rddy_j * rddz_k;
             const float conv = -sig * vol;
-            const float qd = -g * ax * (rddx_ip * dE + rddx_i * dW) -
-                             gh * ay * (rdy_j * dN + rdy_jm * dS) -
-                             gh * az * (rdz_k * dT + rdz_km * dB);
+            const float qd = kW ? -ax * (vs.u.e * rddx_ip * dE + vs.u.w * rddx_i * dW) -
+                                      ay * (vs.u.n * rdy_j * dN + vs.u.s * rdy_jm * dS) -
+                                      az * (vs.u.t * rdz_k * dT + vs.u.b * rdz_km * dB)
+                                : -g * ax * (rddx_ip * dE + rddx_i * dW) -
+                                      gh * ay * (rdy_j * dN + rdy_jm * dS) -
+                                      gh * az * (rdz_k * dT + rdz_km * dB);
             const float fak = a.rrho * vol;
-            const float gp = (dif(p_p[q], p_0[q]) + a.gpx * fdx_i) * (a.rrho / fdx_i);
+            const float gp = (dif(p_p[q], p_0[q]) + a.gpx * gfl * fdx_i) * (a.rrho / fdx_i);
             uo = conv - fak * qd - gp;
         }
         // ---------------- V at (k, j+1/2, i)
@@ -182,11 +213,14 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                                                   ft * dT - fb * dB);
             const float vol = rddx_i * rdy_j * rddz_k;
             const float conv = -sig * vol;
-            const float qd = -gh * ax * (rdx_i * dE + rdx_im * dW) -
-                             g * ay * (rddy_jp * dN + rddy_j * dS) -
-                             gh * az * (rdz_k * dT + rdz_km * dB);
+            const float qd = kW ? -ax * (vs.v.e * rdx_i * dE + vs.v.w * rdx_im * dW) -
+                                      ay * (vs.v.n * rddy_jp * dN + vs.v.s * rddy_j * dS) -
+                                      az * (vs.v.t * rdz_k * dT + vs.v.b * rdz_km * dB)
+                                : -gh * ax * (rdx_i * dE + rdx_im * dW) -
+                                      g * ay * (rddy_jp * dN + rddy_j * dS) -
+                                      gh * az * (rdz_k * dT + rdz_km * dB);
             const float fak = a.rrho * vol;
-            const float gp = (dif(p_0[qn], p_0[q]) + a.gpy * fdy_j) * (a.rrho / fdy_j);
+            const float gp = (dif(p_0[qn], p_0[q]) + a.gpy * gfl * fdy_j) * (a.rrho / fdy_j);
             vo = conv - fak * qd - gp;
         }
         // ---------------- W at (k+1/2, j, i)
@@ -210,17 +244,134 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                                                   ft * dT - fb * dB);
             const float vol = rddx_i * rddy_j * rdz_k;
             const float conv = -sig * vol;
-            const float qd = -gh * ax * (rdx_i * dE + rdx_im * dW) -
-                             gh * ay * (rdy_j * dN + rdy_jm * dS) -
-                             g * az * (rddz_kp * dT + rddz_k * dB);
+            const float qd = kW ? -ax * (vs.w.e * rdx_i * dE + vs.w.w * rdx_im * dW) -
+                                      ay * (vs.w.n * rdy_j * dN + vs.w.s * rdy_jm * dS) -
+                                      az * (vs.w.t * rddz_kp * dT + vs.w.b * rddz_k * dB)
+                                : -gh * ax * (rdx_i * dE + rdx_im * dW) -
+                                      gh * ay * (rdy_j * dN + rdy_jm * dS) -
+                                      g * az * (rddz_kp * dT + rddz_k * dB);
             const float fak = a.rrho * vol;
-            const float gp = (dif(p_0[qt], p_0[q]) + a.gpz * fdz_k) * (a.rrho / fdz_k);
+            const float gp = (dif(p_0[qt], p_0[q]) + a.gpz * gfl * fdz_k) * (a.rrho / fdz_k);
             wo = conv - fak * qd - gp;
         }
 }
 
+// ---- grids with faces that have no neighbour --------------------------------
+// harmonic face mean of tstle4_diff: g*g'/MAX(g+g', gmol)
+__device__ __forceinline__ double fhm(double x, double y, double gmol) {
+    const double s = x + y;
+    return x * y / (s < gmol ? gmol : s);
+}
+
+__device__ __forceinline__ Visc3 visc_uniform(const FluxArgs& a) {
+    const float g = a.g, h = a.gh;
+    return Visc3{{g, g, h, h, h, h}, {h, h, g, g, h, h}, {h, h, h, h, g, g}};
+}
+
+// The face viscosities of tstle4_diff (src/flow/tstle4_mod.F90:268-458) at
+// the point (k, j, i) of one grid, from its viscosity field gg: next to a face
+// without a neighbour the ghost values of G enter the means (zero on the
+// walls of the coarsest level, so no viscous flux crosses them).
+__device__ Visc3 visc_field(const double* gg, int kk, int jj, int k, int j, int i, double gm) {
+    auto G = [&](int kq, int jq, int iq) {
+        return gg[(long long)(iq - 1) * kk * jj + (long long)(jq - 1) * kk + (kq - 1)];
+    };
+    Visc3 v;
+    v.u.e = (float)G(k, j, i + 1);
+    v.u.w = (float)G(k, j, i);
+    v.u.n = (float)(fhm(G(k, j, i), G(k, j + 1, i), gm) + fhm(G(k, j, i + 1), G(k, j + 1, i + 1), gm));
+    v.u.s = (float)(fhm(G(k, j - 1, i), G(k, j, i), gm) + fhm(G(k, j - 1, i + 1), G(k, j, i + 1), gm));
+    v.u.t = (float)(fhm(G(k, j, i), G(k + 1, j, i), gm) + fhm(G(k, j, i + 1), G(k + 1, j, i + 1), gm));
+    v.u.b = (float)(fhm(G(k - 1, j, i), G(k, j, i), gm) + fhm(G(k - 1, j, i + 1), G(k, j, i + 1), gm));
+    v.v.e = (float)(fhm(G(k, j, i), G(k, j, i + 1), gm) + fhm(G(k, j + 1, i), G(k, j + 1, i + 1), gm));
+    v.v.w = (float)(fhm(G(k, j, i - 1), G(k, j, i), gm) + fhm(G(k, j + 1, i - 1), G(k, j + 1, i), gm));
+    v.v.n = (float)G(k, j + 1, i);
+    v.v.s = (float)G(k, j, i);
+    v.v.t = (float)(fhm(G(k, j, i), G(k + 1, j, i), gm) + fhm(G(k, j + 1, i), G(k + 1, j + 1, i), gm));
+    v.v.b = (float)(fhm(G(k - 1, j, i), G(k, j, i), gm) + fhm(G(k - 1, j + 1, i), G(k, j + 1, i), gm));
+    v.w.e = (float)(fhm(G(k, j, i), G(k, j, i + 1), gm) + fhm(G(k + 1, j, i), G(k + 1, j, i + 1), gm));
+    v.w.w = (float)(fhm(G(k, j, i - 1), G(k, j, i), gm) + fhm(G(k + 1, j, i - 1), G(k + 1, j, i), gm));
+    v.w.n = (float)(fhm(G(k, j, i), G(k, j + 1, i), gm) + fhm(G(k + 1, j, i), G(k + 1, j + 1, i), gm));
+    v.w.s = (float)(fhm(G(k, j - 1, i), G(k, j, i), gm) + fhm(G(k + 1, j - 1, i), G(k + 1, j, i), gm));
+    v.w.t = (float)G(k + 1, j, i);
+    v.w.b = (float)G(k, j, i);
+    return v;
+}
+
+// Does the grid have a face without a neighbour (anything but CON)?
+__device__ __forceinline__ bool has_open_face(const DevGrid& G) {
+    bool w = false;
+    for (int f = 0; f < 6; ++f) w |= G.bc[f] != MGLET_BC_CON;
+    return w;
+}
+__device__ __forceinline__ bool has_par_face(const DevGrid& G) {
+    bool w = false;
+    for (int f = 0; f < 6; ++f) w |= G.bc[f] == MGLET_BC_PAR;
+    return w;
+}
+
+// The face viscosities of the point: from G on the outermost interior layer
+// of a grid with a face without a neighbour, else the uniform ones.
+__device__ __forceinline__ Visc3 visc_at(const FluxArgs& a, const DevGrid& G, bool wg, int k, int j,
+                                         int i) {
+    const bool shell = i == 3 || i == G.ii - 2 || j == 3 || j == G.jj - 2 || k == 3 || k == G.kk - 2;
+    if (wg && shell) return visc_field(a.G + G.ip3, G.kk, G.jj, k, j, i, a.wgmol);
+    return visc_uniform(a);
+}
+
+// tauwin (src/flow/wernerwengle_mod.F90:64-87) / dds as swcle3d applies it
+// (src/flow/tstle4_mod.F90:1832-1844); ddsb = dds**(-1/7); FP64.
+__device__ double wall_shear(const FluxArgs& a, double dds, double ddsb, double u) {
+    const double vz = copysign(1.0, u);
+    const double uq = fabs(u);
+    double tau;
+    if (uq >= a.cpo6 / dds)
+        tau = vz * a.wrho * pow(ddsb * (a.cpo4 * uq + a.cpo5 / dds), a.cpo8);
+    else
+        tau = vz * 2.0 * a.wgmol * uq / dds;
+    return tau / a.wrho / dds;
+}
+
+// What tstle4 does differently next to faces without a neighbour, for the
+// point (k, j, i) with own values u, v, w (src/flow/tstle4_mod.F90:13-120):
+// the velocity normal to a wall, inflow or CO1 face on its last interior
+// position is not a flux point (only CON and OP1 faces extend the ranges),
+// and on NOS faces swcle3d (tstle4_mod.F90:1756-1829) subtracts the
+// Werner-Wengle wall shear from the tangential components next to the wall.
+__device__ void boundary_terms(const FluxArgs& a, const DevGrid& G, int k, int j, int i, double u,
+                               double v, double w, float& uo, float& vo, float& wo) {
+    const int* bc = G.bc;
+    auto ext = [](int t) { return t == MGLET_BC_CON || t == MGLET_BC_OP1; };
+    if (i == G.ii - 2 && !ext(bc[1])) uo = 0.f;
+    if (j == G.jj - 2 && !ext(bc[3])) vo = 0.f;
+    if (k == G.kk - 2 && !ext(bc[5])) wo = 0.f;
+    const double *ddx = a.ddx + G.ipx - 1, *ddy = a.ddy + G.ipy - 1, *ddz = a.ddz + G.ipz - 1;
+    const double *wwx = a.wwx + G.ipx - 1, *wwy = a.wwy + G.ipy - 1, *wwz = a.wwz + G.ipz - 1;
+    const bool xl = bc[0] == MGLET_BC_NOS && i == 3, xh = bc[1] == MGLET_BC_NOS && i == G.ii - 2;
+    const bool yl = bc[2] == MGLET_BC_NOS && j == 3, yh = bc[3] == MGLET_BC_NOS && j == G.jj - 2;
+    const bool zl = bc[4] == MGLET_BC_NOS && k == 3, zh = bc[5] == MGLET_BC_NOS && k == G.kk - 2;
+    if (!(xl || xh || yl || yh || zl || zh)) return;
+    double su = 0.0, sv = 0.0, sw = 0.0;
+    if (xl || xh) {
+        sv += wall_shear(a, ddx[i], wwx[i], v);
+        sw += wall_shear(a, ddx[i], wwx[i], w);
+    }
+    if (yl || yh) {
+        su += wall_shear(a, ddy[j], wwy[j], u);
+        sw += wall_shear(a, ddy[j], wwy[j], w);
+    }
+    if (zl || zh) {
+        su += wall_shear(a, ddz[k], wwz[k], u);
+        sv += wall_shear(a, ddz[k], wwz[k], v);
+    }
+    uo -= (float)su;
+    vo -= (float)sv;
+    wo -= (float)sw;
+}
+
 // One CTA per j-slab of a grid, one thread per interior (k, j) of the slab,
 // marching i.
+template <bool kW>
 __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     extern __shared__ float2 sm[];
     const DevGrid G = a.grids[blockIdx.x / a.nslab];
@@ -297,24 +448,40 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     __syncthreads();
 
     const int q = pl(k, j);
+    const float gfl = (float)G.gradpflag;
+    const bool wg = kW && has_open_face(G);
+    const bool pgrid = kW && has_par_face(G);
     for (int i = 3; i <= ii - 2; ++i) {
         float uo = 0.f, vo = 0.f, wo = 0.f;
-        if (on) flux_point(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, uo, vo, wo);
+        if (on) {
+            if constexpr (kW) {
+                const Visc3 vs = visc_at(a, G, wg, k, j, i);
+                flux_point<true>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo, wo);
+                if (wg) boundary_terms(a, G, k, j, i, ucur, vcur, wcur, uo, vo, wo);
+            } else {
+                const Visc3 vs{};
+                flux_point<false>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo, wo);
+            }
+        }
         // issue the global loads of plane i+2 before the RK update and the barrier
         double unx2 = 0, vnx2 = 0, wnx2 = 0;
         __syncthreads();   // every thread is done with slot (i-1)%3 and p slot i%2
         if (i + 2 <= ii - 1) load_plane(i + 2, (i + 2) % 3, (i + 2) % 2, true, unx2, vnx2, wnx2);
         if (on) {
             const long long c = o + (long long)(i - 1) * kj + (long long)(j - 1) * kk + (k - 1);
-            const float frhs = (float)a.sprm[0];
-            const float du = frhs * a.DU[c] + uo;
-            const float dv = frhs * a.DV[c] + vo;
-            const float dw = frhs * a.DW[c] + wo;
-            a.DU[c] = du; a.DV[c] = dv; a.DW[c] = dw;
-            const float fdt = (float)a.sprm[1];
-            a.U[c] = ucur + (double)(fdt * du);
-            a.V[c] = vcur + (double)(fdt * dv);
-            a.W[c] = wcur + (double)(fdt * dw);
+            if (kW && pgrid) {
+                a.UO[c] = (double)uo; a.VO[c] = (double)vo; a.WO[c] = (double)wo;
+            } else {
+                const float frhs = (float)a.sprm[0];
+                const float du = frhs * a.DU[c] + uo;
+                const float dv = frhs * a.DV[c] + vo;
+                const float dw = frhs * a.DW[c] + wo;
+                a.DU[c] = du; a.DV[c] = dv; a.DW[c] = dw;
+                const float fdt = (float)a.sprm[1];
+                a.U[c] = ucur + (double)(fdt * du);
+                a.V[c] = vcur + (double)(fdt * dv);
+                a.W[c] = wcur + (double)(fdt * dw);
+            }
         }
         ucur = unx; vcur = vnx; wcur = wnx;
         unx = unx2; vnx = vnx2; wnx = wnx2;
@@ -373,6 +540,7 @@ __device__ __forceinline__ void tma_plane(double* dst, const CUtensorMap* m, int
 // thread splits its points of it (its own column and the window border)
 // into the (hi, lo) windows, as the plain-load kernel does from global
 // memory.  Same windows, same arithmetic (flux_point), same bits.
+template <bool kW>
 __global__ void __launch_bounds__(576, 2)
     k_mx_flux_tma(FluxArgs a, const __grid_constant__ CUtensorMap mu,
                   const __grid_constant__ CUtensorMap mv, const __grid_constant__ CUtensorMap mw,
@@ -489,9 +657,21 @@ __global__ void __launch_bounds__(576, 2)
     if (t == 0 && 6 <= ii - 1) issue(6);
 
     const int q = pl(k, j);
+    const float gfl = (float)G.gradpflag;
+    const bool wg = kW && has_open_face(G);
+    const bool pgrid = kW && has_par_face(G);
     for (int i = 3; i <= ii - 2; ++i) {
         float uo = 0.f, vo = 0.f, wo = 0.f;
-        if (on) flux_point(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, uo, vo, wo);
+        if (on) {
+            if constexpr (kW) {
+                const Visc3 vs = visc_at(a, G, wg, k, j, i);
+                flux_point<true>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo, wo);
+                if (wg) boundary_terms(a, G, k, j, i, ucur, vcur, wcur, uo, vo, wo);
+            } else {
+                const Visc3 vs{};
+                flux_point<false>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo, wo);
+            }
+        }
         double unx2 = 0, vnx2 = 0, wnx2 = 0;
         __syncthreads();   // every thread is done with slot (i-1)%3 and p slot i%2
         if (i + 2 <= ii - 1) {
@@ -500,15 +680,19 @@ __global__ void __launch_bounds__(576, 2)
         }
         if (on) {
             const long long c = o + (long long)(i - 1) * kj + (long long)(j - 1) * kk + (k - 1);
-            const float frhs = (float)a.sprm[0];
-            const float du = frhs * a.DU[c] + uo;
-            const float dv = frhs * a.DV[c] + vo;
-            const float dw = frhs * a.DW[c] + wo;
-            a.DU[c] = du; a.DV[c] = dv; a.DW[c] = dw;
-            const float fdt = (float)a.sprm[1];
-            a.U[c] = ucur + (double)(fdt * du);
-            a.V[c] = vcur + (double)(fdt * dv);
-            a.W[c] = wcur + (double)(fdt * dw);
+            if (kW && pgrid) {
+                a.UO[c] = (double)uo; a.VO[c] = (double)vo; a.WO[c] = (double)wo;
+            } else {
+                const float frhs = (float)a.sprm[0];
+                const float du = frhs * a.DU[c] + uo;
+                const float dv = frhs * a.DV[c] + vo;
+                const float dw = frhs * a.DW[c] + wo;
+                a.DU[c] = du; a.DV[c] = dv; a.DW[c] = dw;
+                const float fdt = (float)a.sprm[1];
+                a.U[c] = ucur + (double)(fdt * du);
+                a.V[c] = vcur + (double)(fdt * dv);
+                a.W[c] = wcur + (double)(fdt * dw);
+            }
         }
         ucur = unx; vcur = vnx; wcur = wnx;
         unx = unx2; vnx = vnx2; wnx = wnx2;
@@ -538,6 +722,7 @@ static size_t flux_smem(const DevGrid& G0) {
 struct FluxState {
     CUtensorMap map[4];
     bool tma = false;
+    bool walls = false;     // some grid has a face that is not CON: the boundary path
     int variant = -1;
     double ms[2] = {0.0, 0.0};
 };
@@ -595,16 +780,21 @@ int mx_flux_prepare(Ctx* c) {
         set_error("mixed form: grid planes too large for the flux kernel's shared memory");
         return MGLET_ERR_UNSUPPORTED;
     }
-    MG_CUDA(cudaFuncSetAttribute(k_mx_flux, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MG_CUDA(cudaFuncSetAttribute(k_mx_flux<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    MG_CUDA(cudaFuncSetAttribute(k_mx_flux<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     FluxState& fs = g_flux[c];
     fs = FluxState();
+    for (const DevGrid& g : c->grids)
+        for (int f = 0; f < 6; ++f) fs.walls |= g.bc[f] != MGLET_BC_CON;
     const size_t tsm = flux_tma_smem(G0);
     if (flux_slabs(G0) == 1 && (G0.kk * sizeof(double)) % 16 == 0 && G0.kk <= 256 &&
         G0.jj <= 256 && tsm <= 113 * 1024) {
         const char* names[4] = {"U", "V", "W", "P"};
         for (int f = 0; f < 4; ++f)
             if (int rc = encode_plane_map(c, c->F(names[f]), &fs.map[f])) return rc;
-        MG_CUDA(cudaFuncSetAttribute(k_mx_flux_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        MG_CUDA(cudaFuncSetAttribute(k_mx_flux_tma<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)tsm));
+        MG_CUDA(cudaFuncSetAttribute(k_mx_flux_tma<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)tsm));
         fs.tma = true;
     }
@@ -616,11 +806,20 @@ void mx_flux_release(Ctx* c) { g_flux.erase(c); }
 static int launch_variant(Ctx* c, int v, const FluxArgs& a, int threads) {
     const DevGrid& G0 = c->grids[0];
     FluxState& fs = g_flux[c];
-    if (v == 1 && fs.tma)
-        k_mx_flux_tma<<<c->ngrid, threads, flux_tma_smem(G0), c->stream>>>(a, fs.map[0], fs.map[1],
-                                                                           fs.map[2], fs.map[3]);
-    else
-        k_mx_flux<<<c->ngrid * a.nslab, threads, flux_smem(G0), c->stream>>>(a);
+    const size_t tsm = flux_tma_smem(G0), psm = flux_smem(G0);
+    const unsigned nb = (unsigned)(c->ngrid * a.nslab);
+    if (v == 1 && fs.tma) {
+        if (fs.walls)
+            k_mx_flux_tma<true><<<c->ngrid, threads, tsm, c->stream>>>(a, fs.map[0], fs.map[1],
+                                                                      fs.map[2], fs.map[3]);
+        else
+            k_mx_flux_tma<false><<<c->ngrid, threads, tsm, c->stream>>>(a, fs.map[0], fs.map[1],
+                                                                       fs.map[2], fs.map[3]);
+    } else if (fs.walls) {
+        k_mx_flux<true><<<nb, threads, psm, c->stream>>>(a);
+    } else {
+        k_mx_flux<false><<<nb, threads, psm, c->stream>>>(a);
+    }
     MG_LAUNCHED(c);
     return 0;
 }
@@ -648,6 +847,20 @@ static FluxArgs flux_args(Ctx* c, float* du, float* dv, float* dw, const float* 
     a.sprm = sprm;
     a.err = err;
     a.skip_plane = 0;
+    // boundary path: G, FP64 widths and the Werner-Wengle constants
+    // (wernerwengle_mod.F90:13-28 init_wernerwengle)
+    a.G = c->F("G");
+    a.UO = c->F("UO"); a.VO = c->F("VO"); a.WO = c->F("WO");
+    a.ddx = c->L("DDX"); a.ddy = c->L("DDY"); a.ddz = c->L("DDZ");
+    a.wwx = c->L("WWX"); a.wwy = c->L("WWY"); a.wwz = c->L("WWZ");
+    const double rho = c->prm.rho, cwa = 8.3, cwb = 1.0 / 7.0;
+    const double cpo1 = 1.0 - cwb, cpo2 = 1.0 + cwb;
+    a.wrho = rho;
+    a.wgmol = gm;
+    a.cpo4 = cpo2 / cwa * std::pow(gm / rho, cwb);
+    a.cpo5 = 0.5 * cpo1 * std::pow(cwa, cpo2 / cpo1) * std::pow(gm / rho, cpo2);
+    a.cpo6 = 0.5 * gm / rho * std::pow(cwa, 2.0 / cpo1);
+    a.cpo8 = 2.0 / cpo2;
     return a;
 }
 

@@ -131,15 +131,32 @@ __device__ __forceinline__ bool stage_wait(unsigned long long* bar) {
 
 // All threads: the hilf ghosts of grid g into gh[6][fs] -- ghost face f is
 // the facing boundary plane of the neighbour across face f (its face f ^ 1),
-// gathered from that neighbour's plane-ordered hilf at the facepos positions.
+// gathered from that neighbour's plane-ordered hilf at the facepos positions;
+// across a face without a neighbour (fn < 0) the grid's own ghost plane in
+// pg ([6][fs], what bound_pressure set on a PAR face) or zero (no pg: walls,
+// inflow and outflow faces).
 __device__ __forceinline__ void gather_hilf_ghosts(float* gh, const Shape& s, const float* H,
-                                                   const int* fn) {
+                                                   const int* fn, const float* pg) {
     const int fs = s.fs;
     for (int q = threadIdx.x; q < 6 * fs; q += blockDim.x) {
         const int f = q / fs, fi = q - f * fs;
         const int pos = __ldg(s.facepos + (f ^ 1) * fs + fi);
-        gh[q] = pos >= 0 ? __ldg(H + (long long)fn[f] * s.npp + pos) : 0.f;
+        const int nb = fn[f];
+        float v = 0.f;
+        if (nb >= 0) {
+            if (pos >= 0) v = __ldg(H + (long long)nb * s.npp + pos);
+        } else if (pg) {
+            v = pg[q];
+        }
+        gh[q] = v;
     }
+}
+
+// The grid a CTA works on: its block index (walked in reverse when rev is
+// set) or, for the launches of one grid level, that entry of the level's list.
+__device__ __forceinline__ int cta_grid(const int* glist, int rev) {
+    const int b = rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    return glist ? glist[b] : b;
 }
 
 // Shared memory of the streaming stencil kernels: plane starts, row offsets,
@@ -150,6 +167,7 @@ __host__ __device__ inline size_t stencil_tables_bytes(int nm, int ni) {
 
 struct FwdArgs {
     Shape s;
+    const int* glist;           // the grids of this launch (null: all)
     const int* fnbr;            // [ngrid][6] neighbour grid (0-based) across faces 1..6
     const int* gcls;
     float* R;                   // in: (rhs + lap) * lpr from k_sip_pre; out: res
@@ -164,6 +182,8 @@ __host__ __device__ inline size_t align16(size_t v) { return (v + 15) & ~(size_t
 
 struct PreArgs {
     Shape s;
+    const int* glist;           // the grids of this launch (null: all)
+    const float* PG;            // [ngrid][6][fs] PAR ghost planes of hilf (null: none)
     const int* fnbr;
     const int* gcls;
     const float* H;             // hilf, padded plane order (all grids)
@@ -193,12 +213,12 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
     int* spst = reinterpret_cast<int*>(psm);
     short* ro = reinterpret_cast<short*>(spst + nm + 1);
     float* gh = reinterpret_cast<float*>(psm + stencil_tables_bytes(nm, ni));   // [6][fs]
-    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int g = cta_grid(a.glist, a.rev);
     const bool hz = a.hzero != 0;
     const int* fn = a.fnbr + 6 * g;
     for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
     for (int q = threadIdx.x; q < nm * ni; q += blockDim.x) ro[q] = s.rowoff[q];
-    if (!hz) gather_hilf_ghosts(gh, s, a.H, fn);
+    if (!hz) gather_hilf_ghosts(gh, s, a.H, fn, a.PG ? a.PG + (long long)g * 6 * fs : nullptr);
     __syncthreads();
     const long long base = (long long)g * s.npp;
     const float* __restrict__ H = a.H + base;
@@ -271,10 +291,11 @@ __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
     if (a.ctl[0]) return;
     extern __shared__ __align__(16) float gh[];   // [6][fs]
     const Shape s = a.s;
-    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int g = cta_grid(a.glist, a.rev);
     const bool hz = a.hzero != 0;
     const int npp = s.npp;
-    if (!hz) gather_hilf_ghosts(gh, s, a.H, a.fnbr + 6 * g);
+    if (!hz)
+        gather_hilf_ghosts(gh, s, a.H, a.fnbr + 6 * g, a.PG ? a.PG + (long long)g * 6 * s.fs : nullptr);
     __syncthreads();
     const long long base = (long long)g * npp;
     const float* __restrict__ H = a.H + base;
@@ -326,6 +347,81 @@ __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
     }
 }
 
+// The pre-pass with the first record {codes, lpr} loaded kAhead points ahead
+// as well, so that a point's neighbour gathers wait only for their own loads;
+// kL1: the hilf stream is loaded through L1 (the neighbours on the next plane
+// are then L1 hits) instead of with the streaming hint.  Same arithmetic as
+// k_sip_pre_pf, same bits.
+template <int kAhead, int kMinBlocks, bool kUni, bool kL1>
+__global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pr(PreArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(16) float gh[];   // [6][fs]
+    const Shape s = a.s;
+    const int g = cta_grid(a.glist, a.rev);
+    const bool hz = a.hzero != 0;
+    const int npp = s.npp;
+    if (!hz)
+        gather_hilf_ghosts(gh, s, a.H, a.fnbr + 6 * g, a.PG ? a.PG + (long long)g * 6 * s.fs : nullptr);
+    __syncthreads();
+    const long long base = (long long)g * npp;
+    const float* __restrict__ H = a.H + base;
+    const float* __restrict__ RHS = a.RHS + base;
+    float* __restrict__ PRE = a.PRE + base;
+    const float4* __restrict__ P1 = a.PR + (long long)a.gcls[g] * 3 * npp;
+    const float* ghb = gh - npp;
+    const int nt = blockDim.x;
+    float hq[kAhead], rq[kAhead];
+    float4 pq[kAhead];
+    auto ld_h = [&](int q) -> float { return kL1 ? __ldg(H + q) : __ldcs(H + q); };
+#pragma unroll
+    for (int j = 0; j < kAhead; ++j) {
+        const int q = threadIdx.x + j * nt;
+        hq[j] = (!hz && q < npp) ? ld_h(q) : 0.f;
+        rq[j] = q < npp ? __ldcs(RHS + q) : 0.f;
+        pq[j] = q < npp ? __ldg(P1 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f, u4 = 0.f, u5 = 0.f, u6 = 0.f;
+    if (kUni) {
+        const float* u = a.UNI + 8 * a.gcls[g];
+        u0 = u[0]; u1 = u[1]; u2 = u[2]; u3 = u[3]; u4 = u[4]; u5 = u[5]; u6 = u[6];
+    }
+    for (int q = threadIdx.x; q < npp; q += nt) {
+        const float hc = hq[0], rh = rq[0];
+        const float4 r1 = pq[0];
+#pragma unroll
+        for (int j = 0; j + 1 < kAhead; ++j) {
+            hq[j] = hq[j + 1];
+            rq[j] = rq[j + 1];
+            pq[j] = pq[j + 1];
+        }
+        const int qn = q + kAhead * nt;
+        hq[kAhead - 1] = (!hz && qn < npp) ? ld_h(qn) : 0.f;
+        rq[kAhead - 1] = qn < npp ? __ldcs(RHS + qn) : 0.f;
+        pq[kAhead - 1] = qn < npp ? __ldg(P1 + qn) : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int w0 = __float_as_int(r1.x);
+        float v = 0.f;
+        if (w0 >= 0) {
+            float lap = 0.f;
+            if (!hz) {
+                float4 r2, r3;
+                if (kUni) {
+                    r2 = make_float4(u0, u1, u2, u3);
+                    r3 = make_float4(u4, u5, u6, 0.f);
+                } else {
+                    r2 = __ldg(P1 + npp + q);
+                    r3 = __ldg(P1 + 2 * npp + q);
+                }
+                const int w1 = __float_as_int(r1.y), w2 = __float_as_int(r1.z);
+                auto nbv = [&](int code) -> float { return code < npp ? __ldg(H + code) : ghb[code]; };
+                lap = -r2.x * nbv(w0 & 0xffff) - r2.y * nbv(w0 >> 16) - r2.z * nbv(w1 & 0xffff) -
+                      r2.w * nbv(w1 >> 16) - r3.x * nbv(w2 & 0xffff) - r3.y * nbv(w2 >> 16) - r3.z * hc;
+            }
+            v = (rh + lap) * r1.w;
+        }
+        PRE[q] = v;
+    }
+}
+
 // class pre-pass records (see k_sip_pre_pf) from the shape's codes, the
 // class blocks and the representative grid's FP32 1-D coefficients
 __global__ void k_sip_pre_records(const DevGrid* __restrict__ grids, const int* __restrict__ reps,
@@ -360,6 +456,7 @@ __global__ void k_sip_pre_records(const DevGrid* __restrict__ grids, const int* 
 
 struct BwdArgs {
     Shape s;
+    const int* glist;           // the grids of this launch (null: all)
     const int* fnbr;
     const int* gcls;
     float* H;                   // padded plane order, updated: h += res
@@ -396,7 +493,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd(FwdArgs a) {
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // [2][mlp] res planes
     float* gr = nb + 2 * mlp;                                         // [3][fs] low res ghosts
-    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int g = cta_grid(a.glist, a.rev);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float* CF = a.CF + (long long)a.gcls[g] * 5 * s.npp;
@@ -410,7 +507,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd(FwdArgs a) {
     for (int q = tid; q < 3 * fs; q += nt) {
         const int d = q / fs, fi = q - d * fs;
         const int pos = s.facepos[(2 * d + 1) * fs + fi];
-        gr[q] = (a.RLOW && pos >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f;
+        gr[q] = (a.RLOW && pos >= 0 && fn[2 * d] >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f;
     }
     __syncthreads();
     auto fetch = [&](int t, FRec* r) {
@@ -476,7 +573,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd(BwdArgs a) {
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // [2][mlp] res planes
     float* gr = nb + 2 * mlp;                                         // [3][fs] high res ghosts
-    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int g = cta_grid(a.glist, a.rev);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float* CB = a.CB + (long long)a.gcls[g] * 3 * s.npp;
@@ -491,7 +588,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd(BwdArgs a) {
     for (int q = tid; q < 3 * fs; q += nt) {
         const int d = q / fs, fi = q - d * fs;
         const int pos = s.facepos[(2 * d) * fs + fi];
-        gr[q] = pos >= 0 ? a.R[(long long)fn[2 * d + 1] * s.npp + pos] : 0.f;
+        gr[q] = (pos >= 0 && fn[2 * d + 1] >= 0) ? a.R[(long long)fn[2 * d + 1] * s.npp + pos] : 0.f;
     }
     __syncthreads();
     // step t is plane nm-1-t
@@ -581,7 +678,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd_packed(FwdArgs
     const int rs = (int)packed_region(mlp, fs);
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // two regions
-    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int g = cta_grid(a.glist, a.rev);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float4* SW = a.SW + (long long)a.gcls[g] * s.npp;
@@ -595,7 +692,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd_packed(FwdArgs
         const int d = q / fs, fi = q - d * fs;
         const int pos = s.facepos[(2 * d + 1) * fs + fi];
         put_ghost(nb, rs, mlp, fs, d, fi,
-                  (a.RLOW && pos >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f);
+                  (a.RLOW && pos >= 0 && fn[2 * d] >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f);
     }
     __syncthreads();
     auto fetch = [&](int t, PRec* r) {
@@ -653,7 +750,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs
     const int rs = (int)packed_region(mlp, fs);
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // two regions
-    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    const int g = cta_grid(a.glist, a.rev);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float4* SW = a.SW + (long long)a.gcls[g] * s.npp;
@@ -667,7 +764,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs
     for (int q = tid; q < 3 * fs; q += nt) {
         const int d = q / fs, fi = q - d * fs;
         const int pos = s.facepos[(2 * d) * fs + fi];
-        put_ghost(nb, rs, mlp, fs, d, fi, pos >= 0 ? a.R[(long long)fn[2 * d + 1] * s.npp + pos] : 0.f);
+        put_ghost(nb, rs, mlp, fs, d, fi,
+                  (pos >= 0 && fn[2 * d + 1] >= 0) ? a.R[(long long)fn[2 * d + 1] * s.npp + pos] : 0.f);
     }
     __syncthreads();
     // step t is plane nm-1-t
@@ -754,6 +852,7 @@ __device__ __forceinline__ double block_max2(double v, double* sh) {
 
 struct OuterArgs {
     Shape s;
+    const float* PG;            // [ngrid][6][fs] PAR ghost planes of hilf (null: none)
     const int* fnbr;
     const int* gcls;
     const float* H;
@@ -816,7 +915,8 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         stage_issue(H, a.H + base, s.npp, bar);
     }
-    gather_hilf_ghosts(gh, s, a.H, fn);   // while the bulk copy is in flight
+    // while the bulk copy is in flight
+    gather_hilf_ghosts(gh, s, a.H, fn, a.PG ? a.PG + (long long)g * 6 * fs : nullptr);
     if (threadIdx.x == 0) sok = stage_wait(bar);
     __syncthreads();
     if (!sok) {
@@ -1018,6 +1118,11 @@ const PreVariant kPreVariants[] = {
     {2, 4, false, "ahead=2 ctas=4"}, {2, 3, true, "ahead=2 ctas=3 uniform"},
     {1, 3, true, "ahead=1 ctas=3 uniform"}, {3, 3, true, "ahead=3 ctas=3 uniform"},
     {2, 2, true, "ahead=2 ctas=2 uniform"}, {2, 4, true, "ahead=2 ctas=4 uniform"},
+    {2, 3, true, "records ahead=2 ctas=3 uniform"},
+    {2, 3, true, "records ahead=2 ctas=3 uniform, hilf via L1"},
+    {3, 3, true, "records ahead=3 ctas=3 uniform, hilf via L1"},
+    {2, 4, true, "records ahead=2 ctas=4 uniform, hilf via L1"},
+    {2, 3, false, "records ahead=2 ctas=3, hilf via L1"},
 };
 constexpr int kNumPre = (int)(sizeof(kPreVariants) / sizeof(kPreVariants[0]));
 
@@ -1032,7 +1137,12 @@ void launch_pre_variant(int v, int ngrid, size_t smem, cudaStream_t s, const Pre
         case 6: k_sip_pre_pf<1, 3, true><<<ngrid, 512, smem, s>>>(p); break;
         case 7: k_sip_pre_pf<3, 3, true><<<ngrid, 512, smem, s>>>(p); break;
         case 8: k_sip_pre_pf<2, 2, true><<<ngrid, 512, smem, s>>>(p); break;
-        default: k_sip_pre_pf<2, 4, true><<<ngrid, 512, smem, s>>>(p); break;
+        case 9: k_sip_pre_pf<2, 4, true><<<ngrid, 512, smem, s>>>(p); break;
+        case 10: k_sip_pre_pr<2, 3, true, false><<<ngrid, 512, smem, s>>>(p); break;
+        case 11: k_sip_pre_pr<2, 3, true, true><<<ngrid, 512, smem, s>>>(p); break;
+        case 12: k_sip_pre_pr<3, 3, true, true><<<ngrid, 512, smem, s>>>(p); break;
+        case 13: k_sip_pre_pr<2, 4, true, true><<<ngrid, 512, smem, s>>>(p); break;
+        default: k_sip_pre_pr<2, 3, false, true><<<ngrid, 512, smem, s>>>(p); break;
     }
 }
 
@@ -1082,6 +1192,8 @@ PreArgs pre_args(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ct
                  bool hzero) {
     PreArgs p;
     p.s = shape(st);
+    p.glist = nullptr;
+    p.PG = st.pg;
     p.fnbr = st.d_fnbr; p.gcls = gcls;
     p.H = st.h32; p.RHS = st.rhs32; p.PRE = st.rs[rwrite];
     p.CF = cf;
@@ -1104,6 +1216,7 @@ const char* sip_sweep_variant_name(int v) {
     return v >= 0 && v < kNumSweep ? kSweepVariants[v].name : "";
 }
 const char* sip_pre_variant_name(int v) { return v >= 0 && v < kNumPre ? kPreVariants[v].name : ""; }
+bool sip_pre_variant_uniform(int v) { return v >= 0 && v < kNumPre && kPreVariants[v].uni; }
 
 int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl) {
     if (!st.prepk) return 0;
@@ -1399,11 +1512,9 @@ int sip_init(Ctx* c, SipState& st) {
         }
         fn[(size_t)6 * (rg - 1) + rf - 1] = sg - 1;
     }
-    for (int v : fn)
-        if (v < 0) {
-            set_error("mixed form: every face needs a CON neighbour");
-            return MGLET_ERR_UNSUPPORTED;
-        }
+    // a face without a neighbour (a wall, an inflow or an outflow face) keeps
+    // -1: its hilf and res ghosts read as zero, as the reference's ghost
+    // layers that no exchange writes stay zero through mgpoisl
     if (int rc = up(&st.d_fnbr, fn)) return rc;
     const size_t n = (size_t)c->ngrid * st.npp;
     for (float** p : {&st.h32, &st.rs[0], &st.rs[1], &st.rs[2], &st.rhs32}) {
@@ -1508,7 +1619,7 @@ void sip_release(SipState& st) {
                     (void*)st.d_pcode, (void*)st.spr, (void*)st.uni, (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
-                    (void*)st.a1lo[4], (void*)st.a1lo[5]})
+                    (void*)st.a1lo[4], (void*)st.a1lo[5], (void*)st.pg})
         cudaFree(p);
 }
 
@@ -1523,23 +1634,26 @@ int sip_divcal(Ctx* c, SipState& st, const double* fak) {
 }
 
 int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
-                int rwrite, bool hzero) {
+                int rwrite, bool hzero, const int* glist, int nlist) {
+    const int ng = glist ? nlist : c->ngrid;
     {
         ProfScope ps_(c, "mx_sip_pre");
         PreArgs p = pre_args(c, st, cf, gcls, ctl, rwrite, hzero);
+        p.glist = glist;
         p.rev = next_order(st);
         // the tuner's choice (loads ahead, CTAs per SM, uniform coefficients);
         // untuned: two points ahead at three CTAs per SM
         if (st.prepk)
-            launch_pre_variant(st.pre_variant >= 0 ? st.pre_variant : 0, c->ngrid,
+            launch_pre_variant(st.pre_variant >= 0 ? st.pre_variant : 0, ng,
                                (size_t)6 * st.fs * 4, c->stream, p);
         else
-            k_sip_pre<<<c->ngrid, 512, pre_smem(st), c->stream>>>(p);
+            k_sip_pre<<<ng, 512, pre_smem(st), c->stream>>>(p);
         MG_LAUNCHED(c);
     }
     ProfScope ps_(c, "mx_sip_fwd");
     FwdArgs a;
     a.s = shape(st);
+    a.glist = glist;
     a.fnbr = st.d_fnbr; a.gcls = gcls;
     a.R = st.rs[rwrite];
     a.RLOW = rlow >= 0 ? st.rs[rlow] : nullptr;
@@ -1552,25 +1666,27 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
     a.SW = st.swf;
     a.rev = next_order(st);
     if (st.packed && st.sweep_variant > 0 && sweep_fits(st, st.sweep_variant))
-        launch_fwd_variant(st.sweep_variant, c->ngrid, sweep_threads_for(st, st.sweep_variant),
+        launch_fwd_variant(st.sweep_variant, ng, sweep_threads_for(st, st.sweep_variant),
                            packed_smem(st), c->stream, a);
     else if (st.packed && threads <= 256)
-        k_sip_fwd_packed<256, 8, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
+        k_sip_fwd_packed<256, 8, 2><<<ng, threads, packed_smem(st), c->stream>>>(a);
     else if (st.packed)
-        k_sip_fwd_packed<512, 4, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
+        k_sip_fwd_packed<512, 4, 2><<<ng, threads, packed_smem(st), c->stream>>>(a);
     else if (threads <= 256)
-        k_sip_fwd<256, 8, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
+        k_sip_fwd<256, 8, 1, 2><<<ng, threads, sweep_smem(st), c->stream>>>(a);
     else
-        k_sip_fwd<512, 4, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
+        k_sip_fwd<512, 4, 1, 2><<<ng, threads, sweep_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }
 
 int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ctl, int rhi,
-                 bool hzero) {
+                 bool hzero, const int* glist, int nlist) {
     ProfScope ps_(c, "mx_sip_bwd");
+    const int ng = glist ? nlist : c->ngrid;
     BwdArgs a;
     a.s = shape(st);
+    a.glist = glist;
     a.fnbr = st.d_fnbr; a.gcls = gcls;
     a.H = st.h32; a.R = st.rs[rhi];
     a.CB = cb;
@@ -1583,16 +1699,16 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
     a.SW = st.swb;
     a.rev = next_order(st);
     if (st.packed && st.sweep_variant > 0 && sweep_fits(st, st.sweep_variant))
-        launch_bwd_variant(st.sweep_variant, c->ngrid, sweep_threads_for(st, st.sweep_variant),
+        launch_bwd_variant(st.sweep_variant, ng, sweep_threads_for(st, st.sweep_variant),
                            packed_smem(st), c->stream, a);
     else if (st.packed && threads <= 256)
-        k_sip_bwd_packed<256, 8, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
+        k_sip_bwd_packed<256, 8, 2><<<ng, threads, packed_smem(st), c->stream>>>(a);
     else if (st.packed)
-        k_sip_bwd_packed<512, 4, 2><<<c->ngrid, threads, packed_smem(st), c->stream>>>(a);
+        k_sip_bwd_packed<512, 4, 2><<<ng, threads, packed_smem(st), c->stream>>>(a);
     else if (threads <= 256)
-        k_sip_bwd<256, 8, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
+        k_sip_bwd<256, 8, 1, 2><<<ng, threads, sweep_smem(st), c->stream>>>(a);
     else
-        k_sip_bwd<512, 4, 1, 2><<<c->ngrid, threads, sweep_smem(st), c->stream>>>(a);
+        k_sip_bwd<512, 4, 1, 2><<<ng, threads, sweep_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;
 }
@@ -1601,6 +1717,7 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     ProfScope ps_(c, "mx_outer");
     OuterArgs a;
     a.s = shape(st);
+    a.PG = st.pg;
     a.fnbr = st.d_fnbr; a.gcls = gcls;
     a.H = st.h32;
     a.RHS = st.rhs32; a.RHSL = st.rhsl; a.DPH = st.dph; a.DPL = st.dpl; a.APX = apx;

@@ -54,6 +54,9 @@ struct SipState {
     // -1 = default; the tuner's time of one forward + backward pair
     int sweep_variant = -1;
     double sweep_ms = 0.0;
+    // hierarchies: the hilf ghost planes of PAR faces [ngrid][6][fs], set by
+    // the mixed bound_pressure before every inner iteration of a level
+    float* pg = nullptr;
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
@@ -67,10 +70,11 @@ int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* 
 void sip_release(SipState& st);
 // fak (the solve's prefak) is read from device memory
 int sip_divcal(Ctx* c, SipState& st, const double* fak);
+// glist / nlist: the grids of one level (null: every grid)
 int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
-                int rwrite, bool hzero);
+                int rwrite, bool hzero, const int* glist = nullptr, int nlist = 0);
 int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ctl, int rhi,
-                 bool hzero);
+                 bool hzero, const int* glist = nullptr, int nlist = 0);
 int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl);
 int sip_scatter_dp(Ctx* c, SipState& st);
 // Times every valid pre-pass variant on the current buffers and keeps the
@@ -79,6 +83,7 @@ int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl);
 // The pre-pass variants: count, and a description of variant v.
 int sip_pre_variants();
 const char* sip_pre_variant_name(int v);
+bool sip_pre_variant_uniform(int v);
 int sip_sweep_variants();
 const char* sip_sweep_variant_name(int v);
 

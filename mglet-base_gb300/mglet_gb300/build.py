@@ -21,7 +21,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 BASE = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 SOURCES = ["api.cu", "plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "plain_bound.cu",
            "plain_gc.cu", "plain_level.cu", "mixed.cu", "mixed_flux.cu", "mixed_sip.cu", "noalloc.cu",
-           "adjoint.cu", "les.cu", "scalar.cu", "diag.cu", "gc_create.cu", "dist.cu", "mesh_sdf.cu"]
+           "adjoint.cu", "les.cu", "scalar.cu", "diag.cu", "gc_create.cu", "dist.cu", "mesh_sdf.cu",
+           "mixed_level.cu"]
 # translation units whose FP64 arithmetic must not be contracted into FMAs
 NO_FMA = {"plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "plain_bound.cu", "plain_gc.cu",
           "plain_level.cu", "noalloc.cu", "les.cu", "scalar.cu"}

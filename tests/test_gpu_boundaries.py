@@ -1,7 +1,8 @@
-"""FIX / OP1 / NOS / SLI faces on the GPU (plain FP64 form) against the
-oracle: bound_flow alone and whole stages, bit for bit; tstle4 with the
+"""FIX / OP1 / NOS / SLI faces on the GPU against the oracle: in the plain
+FP64 form bound_flow alone and whole stages bit for bit, tstle4 with the
 Werner-Wengle wall function of NOS walls (bit for bit in its laminar branch,
-to CUDA's pow in the turbulent one)."""
+to CUDA's pow in the turbulent one); in the batched mixed form whole stages
+within stated tolerances."""
 import numpy as np
 import pytest
 
@@ -133,10 +134,69 @@ def test_viscosity_field_at_start(gpu_lib, oracle_lib, walls):
     assert np.array_equal(gs.get("G"), o.get("G"))
 
 
-def test_mixed_form_refuses_walls(gpu_lib):
-    """The batched mixed form pulls every halo from a face neighbour, so a
-    hierarchy with wall faces is refused loudly, not run approximately."""
-    case = cases.periodic_box(2, 1, 1, n=8, walls={1: abi.BC_FIX, 2: abi.BC_OP1})
+MIXED_WALLS = [
+    {1: abi.BC_FIX, 2: abi.BC_OP1},
+    {5: abi.BC_FIX, 6: abi.BC_FIX, 3: abi.BC_NOS, 4: abi.BC_SLI},
+    {1: abi.BC_SLI, 2: abi.BC_NOS, 5: abi.BC_NOS, 6: abi.BC_OP1},
+    {3: abi.BC_NOS, 4: abi.BC_NOS},
+]
+
+
+@pytest.mark.parametrize("walls", MIXED_WALLS)
+def test_mixed_form_with_walls(gpu_lib, oracle_lib, walls):
+    """The batched mixed form on grids with FIX, OP1, NOS and SLI faces
+    against the FP64 oracle: two RK3 steps with the outer loop run to
+    convergence (epcorr 1e-11, at most 40 outer iterations) on both sides.
+    The velocity vector agrees to relative L2 <= 1e-7, the pressure (mean
+    removed) to 1e-5: FP32 fluxes and SIP sweeps under the float-float
+    outer loop.  With gmol = 1e-3 and u = 0.5 + Taylor-Green the NOS walls'
+    wall function runs in both of its branches."""
+    case = cases.periodic_box(2, 2, 1, n=8, length=(2.0, 2.0, 1.0), walls=walls)
+    u, v, w, p = cases.taylor_green(case)
+    u, v, w = cases.add_noise(case, (u + 0.5, v, w), amplitude=1e-2, seed=9)
+    fields = dict(zip("UVWP", (u, v, w, p)))
+    rng = np.random.default_rng(17)
+    bufs, pinf = {}, {}
+    for g in range(case.ngrid):
+        for f in range(1, 7):
+            t = case.bctype[g, f - 1]
+            if t == abi.BC_FIX:
+                bufs[("U", g, f)] = 0.5 + 0.01 * rng.standard_normal(face_plane_shape(case, f))
+            if t == abi.BC_OP1:
+                pinf[(g, f)] = 0.05
+    kw = dict(gmol=1e-3, epcorr=1e-11, nouter=40, nouter_min=0)
+    gs = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, **kw))
+    o = oracle_lib.Oracle(case, _prm(**kw))
+    _load((gs, o), case, fields, bufs, pinf)
+    for s in (gs, o):
+        s.connect(0, 2, "U", "V", "W", "P", corners=True)
+        s.bound_flow()
+    rkg, rko = gpu_lib.rk_scheme("williamson"), oracle_lib.rk_scheme("williamson")
+    for it in range(1, 3):
+        for irk in range(1, 4):
+            sg = gs.timeintegrate_flow(it, it, 0.0, 2e-3, irk, rkg)
+            so = o.timeintegrate_flow(it, it, 0.0, 2e-3, irk, rko)
+            assert np.isfinite(sg.maxrhs)
+            assert sg.maxrhs / sg.prefak < 1e-11 or sg.nouter_done == 40
+    num = sum(np.sum((case.interior(gs.get(n)) - case.interior(o.get(n))) ** 2) for n in "UVW")
+    den = sum(np.sum(case.interior(o.get(n)) ** 2) for n in "UVW")
+    ev = float(np.sqrt(num / den))
+    pg, po = case.interior(gs.get("P")), case.interior(o.get("P"))
+    pg, po = pg - pg.mean(), po - po.mean()
+    ep = float(np.linalg.norm(pg - po) / np.linalg.norm(po))
+    print(f"walls {walls}: velocity {ev:.3e}, pressure {ep:.3e}")
+    assert ev <= 1e-7, ev
+    assert ep <= 1e-5, ep
+    ig, io = gs.itinfo(2e-3), o.itinfo(2e-3)
+    assert abs(ig.cflmax - io.cflmax) <= 1e-6 * io.cflmax
+    gs.close()
+
+
+def test_mixed_form_refuses_low_outflow(gpu_lib):
+    """tstle4 extends the flux range of an outflow face on a low side (1, 3,
+    5) over the ghost plane, which the mixed form's interior sweep does not
+    visit: such a case is refused loudly, not run approximately."""
+    case = cases.periodic_box(2, 1, 1, n=8, walls={1: abi.BC_OP1, 2: abi.BC_FIX})
     with pytest.raises(gpu_lib.MgletError) as e:
         gpu_lib.Solver(case, _prm(abi.FORM_MIXED))
     assert e.value.code == abi.MGLET_ERR_UNSUPPORTED

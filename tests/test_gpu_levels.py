@@ -177,9 +177,12 @@ def test_multilevel_stage_bit_exact(gpu_lib, oracle_lib, h):
             assert np.array_equal(gs.get(n), o.get(n)), (irk, n)
 
 
-def test_mixed_form_refuses_hierarchies(gpu_lib):
+def test_mixed_form_refuses_sor_on_hierarchies(gpu_lib):
+    """The mixed form's inner solver is SIP on every level: SOR on the finer
+    levels (pressuresolver_mod.F90's psolver choice) is refused loudly."""
     case = cases.refined_box(2, 2, 2, n=8, refine=(1,))
     prm = abi.make_flow_params(gmol=1e-2, epcorr=1e-12, nouter=4, ninner=2, nouter_min=0,
-                               form=abi.FORM_MIXED)
-    with pytest.raises(gpu_lib.MgletError):
+                               form=abi.FORM_MIXED, psolver=abi.PSOLVER_SOR)
+    with pytest.raises(gpu_lib.MgletError) as e:
         gpu_lib.Solver(case, prm)
+    assert e.value.code == abi.MGLET_ERR_UNSUPPORTED
