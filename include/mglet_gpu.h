@@ -492,13 +492,12 @@ int mglet_gpu_set_partition(mglet_ctx* ctx, const int32_t* halo, int32_t nsend,
 
 /* ---- Launch tuning of the mixed form (no counterpart in the reference) -----
  * mglet_gpu_create times the launch variants of the mixed form's pre-pass
- * (points loaded ahead, CTAs per SM, records loaded ahead, hilf through L1,
- * and the uniform-coefficient variants where every coefficient class allows
- * them) on the case itself and keeps the
+ * (points loaded ahead, CTAs per SM, and the uniform-coefficient variant
+ * where every coefficient class allows it) on the case itself and keeps the
  * fastest, cached per grid shape for the process; the environment variable
  * MGLET_TUNE=0 keeps the defaults.  mglet_gpu_tuning describes the choice
  * ("" for the plain form); mglet_gpu_force_variant overrides it (kernel
- * "mx_sip_pre", variant 0..14, -1 = default).  All variants compute the same
+ * "mx_sip_pre", variant 0..9, -1 = default).  All variants compute the same
  * bits. */
 int mglet_gpu_tuning(mglet_ctx* ctx, char* buf, int64_t buflen);
 int mglet_gpu_force_variant(mglet_ctx* ctx, const char* kernel, int32_t variant);

@@ -192,7 +192,7 @@ __global__ void k_setginbody(const DevGrid* __restrict__ grids, double* Gf, cons
 int lesmodel(Ctx* c) {
     if (c->ilesmodel == 0) return 0;
     ProfScope ps_(c, "lesmodel");
-    LesArgs A;
+    LesArgs A{};
     A.grids = c->d_grids;
     A.u = c->F("U"); A.v = c->F("V"); A.w = c->F("W"); A.bp = c->F("BP"); A.delta = c->F("LESD");
     A.g = c->F("G");

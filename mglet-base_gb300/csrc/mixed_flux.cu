@@ -830,7 +830,7 @@ static FluxArgs flux_args(Ctx* c, float* du, float* dv, float* dw, const float* 
     const int nslab = flux_slabs(G0);
     const int js = (G0.jj - 4 + nslab - 1) / nslab;
     *threads = ((G0.kk - 4) * js + 31) / 32 * 32;
-    FluxArgs a;
+    FluxArgs a{};
     a.nslab = nslab;
     a.grids = c->d_grids;
     a.U0 = c->F("U"); a.V0 = c->F("V"); a.W0 = c->F("W"); a.P0 = c->F("P");

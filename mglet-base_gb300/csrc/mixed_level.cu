@@ -343,7 +343,7 @@ int mx_bound_pressure(Ctx* c, SipState& st, const LevelState& lv, int ilevel, co
     const int l = ilevel - c->minlevel;
     if (lv.pars[l].empty()) return 0;
     ProfScope ps_(c, "mx_bound_pressure");
-    BpArgs A;
+    BpArgs A{};
     A.grids = c->d_grids;
     A.hier = c->d_hier;
     A.list = lv.d_pars[l];

@@ -347,81 +347,6 @@ __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
     }
 }
 
-// The pre-pass with the first record {codes, lpr} loaded kAhead points ahead
-// as well, so that a point's neighbour gathers wait only for their own loads;
-// kL1: the hilf stream is loaded through L1 (the neighbours on the next plane
-// are then L1 hits) instead of with the streaming hint.  Same arithmetic as
-// k_sip_pre_pf, same bits.
-template <int kAhead, int kMinBlocks, bool kUni, bool kL1>
-__global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pr(PreArgs a) {
-    if (a.ctl[0]) return;
-    extern __shared__ __align__(16) float gh[];   // [6][fs]
-    const Shape s = a.s;
-    const int g = cta_grid(a.glist, a.rev);
-    const bool hz = a.hzero != 0;
-    const int npp = s.npp;
-    if (!hz)
-        gather_hilf_ghosts(gh, s, a.H, a.fnbr + 6 * g, a.PG ? a.PG + (long long)g * 6 * s.fs : nullptr);
-    __syncthreads();
-    const long long base = (long long)g * npp;
-    const float* __restrict__ H = a.H + base;
-    const float* __restrict__ RHS = a.RHS + base;
-    float* __restrict__ PRE = a.PRE + base;
-    const float4* __restrict__ P1 = a.PR + (long long)a.gcls[g] * 3 * npp;
-    const float* ghb = gh - npp;
-    const int nt = blockDim.x;
-    float hq[kAhead], rq[kAhead];
-    float4 pq[kAhead];
-    auto ld_h = [&](int q) -> float { return kL1 ? __ldg(H + q) : __ldcs(H + q); };
-#pragma unroll
-    for (int j = 0; j < kAhead; ++j) {
-        const int q = threadIdx.x + j * nt;
-        hq[j] = (!hz && q < npp) ? ld_h(q) : 0.f;
-        rq[j] = q < npp ? __ldcs(RHS + q) : 0.f;
-        pq[j] = q < npp ? __ldg(P1 + q) : make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    float u0 = 0.f, u1 = 0.f, u2 = 0.f, u3 = 0.f, u4 = 0.f, u5 = 0.f, u6 = 0.f;
-    if (kUni) {
-        const float* u = a.UNI + 8 * a.gcls[g];
-        u0 = u[0]; u1 = u[1]; u2 = u[2]; u3 = u[3]; u4 = u[4]; u5 = u[5]; u6 = u[6];
-    }
-    for (int q = threadIdx.x; q < npp; q += nt) {
-        const float hc = hq[0], rh = rq[0];
-        const float4 r1 = pq[0];
-#pragma unroll
-        for (int j = 0; j + 1 < kAhead; ++j) {
-            hq[j] = hq[j + 1];
-            rq[j] = rq[j + 1];
-            pq[j] = pq[j + 1];
-        }
-        const int qn = q + kAhead * nt;
-        hq[kAhead - 1] = (!hz && qn < npp) ? ld_h(qn) : 0.f;
-        rq[kAhead - 1] = qn < npp ? __ldcs(RHS + qn) : 0.f;
-        pq[kAhead - 1] = qn < npp ? __ldg(P1 + qn) : make_float4(0.f, 0.f, 0.f, 0.f);
-        const int w0 = __float_as_int(r1.x);
-        float v = 0.f;
-        if (w0 >= 0) {
-            float lap = 0.f;
-            if (!hz) {
-                float4 r2, r3;
-                if (kUni) {
-                    r2 = make_float4(u0, u1, u2, u3);
-                    r3 = make_float4(u4, u5, u6, 0.f);
-                } else {
-                    r2 = __ldg(P1 + npp + q);
-                    r3 = __ldg(P1 + 2 * npp + q);
-                }
-                const int w1 = __float_as_int(r1.y), w2 = __float_as_int(r1.z);
-                auto nbv = [&](int code) -> float { return code < npp ? __ldg(H + code) : ghb[code]; };
-                lap = -r2.x * nbv(w0 & 0xffff) - r2.y * nbv(w0 >> 16) - r2.z * nbv(w1 & 0xffff) -
-                      r2.w * nbv(w1 >> 16) - r3.x * nbv(w2 & 0xffff) - r3.y * nbv(w2 >> 16) - r3.z * hc;
-            }
-            v = (rh + lap) * r1.w;
-        }
-        PRE[q] = v;
-    }
-}
-
 // class pre-pass records (see k_sip_pre_pf) from the shape's codes, the
 // class blocks and the representative grid's FP32 1-D coefficients
 __global__ void k_sip_pre_records(const DevGrid* __restrict__ grids, const int* __restrict__ reps,
@@ -1118,11 +1043,6 @@ const PreVariant kPreVariants[] = {
     {2, 4, false, "ahead=2 ctas=4"}, {2, 3, true, "ahead=2 ctas=3 uniform"},
     {1, 3, true, "ahead=1 ctas=3 uniform"}, {3, 3, true, "ahead=3 ctas=3 uniform"},
     {2, 2, true, "ahead=2 ctas=2 uniform"}, {2, 4, true, "ahead=2 ctas=4 uniform"},
-    {2, 3, true, "records ahead=2 ctas=3 uniform"},
-    {2, 3, true, "records ahead=2 ctas=3 uniform, hilf via L1"},
-    {3, 3, true, "records ahead=3 ctas=3 uniform, hilf via L1"},
-    {2, 4, true, "records ahead=2 ctas=4 uniform, hilf via L1"},
-    {2, 3, false, "records ahead=2 ctas=3, hilf via L1"},
 };
 constexpr int kNumPre = (int)(sizeof(kPreVariants) / sizeof(kPreVariants[0]));
 
@@ -1137,12 +1057,7 @@ void launch_pre_variant(int v, int ngrid, size_t smem, cudaStream_t s, const Pre
         case 6: k_sip_pre_pf<1, 3, true><<<ngrid, 512, smem, s>>>(p); break;
         case 7: k_sip_pre_pf<3, 3, true><<<ngrid, 512, smem, s>>>(p); break;
         case 8: k_sip_pre_pf<2, 2, true><<<ngrid, 512, smem, s>>>(p); break;
-        case 9: k_sip_pre_pf<2, 4, true><<<ngrid, 512, smem, s>>>(p); break;
-        case 10: k_sip_pre_pr<2, 3, true, false><<<ngrid, 512, smem, s>>>(p); break;
-        case 11: k_sip_pre_pr<2, 3, true, true><<<ngrid, 512, smem, s>>>(p); break;
-        case 12: k_sip_pre_pr<3, 3, true, true><<<ngrid, 512, smem, s>>>(p); break;
-        case 13: k_sip_pre_pr<2, 4, true, true><<<ngrid, 512, smem, s>>>(p); break;
-        default: k_sip_pre_pr<2, 3, false, true><<<ngrid, 512, smem, s>>>(p); break;
+        default: k_sip_pre_pf<2, 4, true><<<ngrid, 512, smem, s>>>(p); break;
     }
 }
 
@@ -1190,7 +1105,7 @@ void launch_bwd_variant(int v, int ngrid, int threads, size_t smem, cudaStream_t
 
 PreArgs pre_args(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rwrite,
                  bool hzero) {
-    PreArgs p;
+    PreArgs p{};
     p.s = shape(st);
     p.glist = nullptr;
     p.PG = st.pg;
@@ -1273,10 +1188,10 @@ int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl) {
             st.sweep_variant = sit->second.first;
             st.sweep_ms = sit->second.second;
         } else {
-            FwdArgs fa;
+            FwdArgs fa{};
             fa.s = shape(st); fa.fnbr = st.d_fnbr; fa.gcls = gcls; fa.R = st.rs[0];
             fa.RLOW = st.rs[1]; fa.CF = cf; fa.ctl = ctl; fa.SW = st.swf; fa.rev = 0;
-            BwdArgs ba;
+            BwdArgs ba{};
             ba.s = shape(st); ba.fnbr = st.d_fnbr; ba.gcls = gcls; ba.H = st.h32; ba.R = st.rs[0];
             ba.CB = nullptr; ba.ctl = ctl; ba.hzero = 0; ba.SW = st.swb; ba.rev = 0;
             int sbest = 0;
@@ -1651,7 +1566,7 @@ int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl
         MG_LAUNCHED(c);
     }
     ProfScope ps_(c, "mx_sip_fwd");
-    FwdArgs a;
+    FwdArgs a{};
     a.s = shape(st);
     a.glist = glist;
     a.fnbr = st.d_fnbr; a.gcls = gcls;
@@ -1684,7 +1599,7 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
                  bool hzero, const int* glist, int nlist) {
     ProfScope ps_(c, "mx_sip_bwd");
     const int ng = glist ? nlist : c->ngrid;
-    BwdArgs a;
+    BwdArgs a{};
     a.s = shape(st);
     a.glist = glist;
     a.fnbr = st.d_fnbr; a.gcls = gcls;
@@ -1715,7 +1630,7 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
 
 int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl) {
     ProfScope ps_(c, "mx_outer");
-    OuterArgs a;
+    OuterArgs a{};
     a.s = shape(st);
     a.PG = st.pg;
     a.fnbr = st.d_fnbr; a.gcls = gcls;

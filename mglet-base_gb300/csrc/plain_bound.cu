@@ -195,7 +195,7 @@ int launch_bound_flow(Ctx* c, double* u, double* v, double* w, double* p, int il
             const int na = f / 2 == 2 ? G.jj : G.kk, nb = f / 2 == 0 ? G.jj : G.ii;
             maxq = std::max(maxq, na * nb);
         }
-        BoundArgs a;
+        BoundArgs a{};
         a.grids = c->d_grids;
         a.list = c->d_bgrids[f];
         a.bface = c->d_bface;

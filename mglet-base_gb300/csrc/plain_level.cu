@@ -1107,7 +1107,7 @@ int launch_tstle4_par(Ctx* c, double* uo, double* vo, double* wo, const double* 
                       const double* w, const double* ut, const double* vt, const double* wt) {
     if (!c->npargrids) return 0;
     ProfScope ps_(c, "tstle4_par");
-    ParFluxArgs A;
+    ParFluxArgs A{};
     A.grids = c->d_grids;
     A.list = c->d_pargrids;
     A.uo = uo; A.vo = vo; A.wo = wo;
@@ -1192,7 +1192,7 @@ int launch_bound_par(Ctx* c, int iface, int ilevel, double* u, double* v, double
         const DevGrid& G = c->grids[g];
         maxq = std::max(maxq, (f / 2 == 2 ? G.jj : G.kk) * (f / 2 == 0 ? G.jj : G.ii));
     }
-    ParArgs A;
+    ParArgs A{};
     A.grids = c->d_grids;
     A.list = c->d_pgrids[f];
     A.bface = c->d_bface;
@@ -1213,7 +1213,7 @@ int launch_parent(Ctx* c, int ilevel, const char* const v[3], const char* const 
         auto it = c->d_plist[f].find(ilevel);
         if (it == c->d_plist[f].end()) continue;
         const std::vector<int>& list = c->plist[f][ilevel];
-        ParentArgs A;
+        ParentArgs A{};
         A.grids = c->d_grids;
         A.hier = c->d_hier;
         A.bface = c->d_bface;
@@ -1252,7 +1252,7 @@ int launch_ftoc(Ctx* c, int ilevel, const double* ff, double* fc, char flag) {
     auto it = c->d_children.find(ilevel);
     if (it == c->d_children.end()) return 0;
     const std::vector<int>& list = c->children[ilevel];
-    FtocArgs A;
+    FtocArgs A{};
     A.grids = c->d_grids;
     A.hier = c->d_hier;
     A.list = it->second;
@@ -1305,7 +1305,7 @@ int launch_bound_pressure(Ctx* c, int ilevel, double* p, const double* buf, bool
             const int na = f / 2 == 2 ? G.jj : G.kk, nb = f / 2 == 0 ? G.jj : G.ii;
             maxq = std::max(maxq, ((na - 4) / 2) * ((nb - 4) / 2));
         }
-        BpArgs A;
+        BpArgs A{};
         A.grids = c->d_grids;
         A.list = c->d_pgrids[f];
         A.bface = c->d_bface;

@@ -593,7 +593,7 @@ static int launch_lu(Ctx* c, int planeorder) {
     const int chunk = std::max(1, std::min(c->ngrid, 512));
     double* tmp = nullptr;
     MG_CUDA(cudaMalloc(&tmp, (size_t)chunk * 7 * npt * sizeof(double)));
-    LuArgs a;
+    LuArgs a{};
     a.grids = c->d_grids;
     a.mips = tp.mips; a.idxs = tp.idxs;
     a.mip = nullptr; a.idx = nullptr;
@@ -629,7 +629,7 @@ int launch_sipiter1(Ctx* c, int ilevel, const double* rhs, double* res) {
     ProfScope ps_(c, "sipiter1");
     TablePtrs tp;
     if (int rc = table_ptrs(c, tp)) return rc;
-    SipArgs a;
+    SipArgs a{};
     a.grids = c->d_grids; a.mips = tp.mips; a.idxs = tp.idxs;
     a.rhs = rhs; a.res = res; a.phi = nullptr;
     a.c0 = c->F("SIPLW"); a.c1 = c->F("SIPLS"); a.c2 = c->F("SIPLB"); a.c3 = c->F("SIPLPR");
@@ -646,7 +646,7 @@ int launch_sipiter2(Ctx* c, int ilevel, double* phi, double* res) {
     ProfScope ps_(c, "sipiter2");
     TablePtrs tp;
     if (int rc = table_ptrs(c, tp)) return rc;
-    SipArgs a;
+    SipArgs a{};
     a.grids = c->d_grids; a.mips = tp.mips; a.idxs = tp.idxs;
     a.rhs = nullptr; a.res = res; a.phi = phi;
     a.c0 = c->F("SIPUE"); a.c1 = c->F("SIPUN"); a.c2 = c->F("SIPUT"); a.c3 = nullptr;

@@ -437,7 +437,7 @@ int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) 
         // T_OLD = T (timeintegrate_scalar_mod.F90:56-57), read by the Boussinesq term
         MG_CUDA(cudaMemcpyAsync(c->F((sd.name + "_OLD").c_str()), T, (size_t)c->idim3d * sizeof(double),
                                 cudaMemcpyDeviceToDevice, c->stream));
-        ScaArgs A;
+        ScaArgs A{};
         A.grids = c->d_grids;
         A.t = T; A.u = c->F("U"); A.v = c->F("V"); A.w = c->F("W"); A.g = c->F("G"); A.bt = c->F("BT");
         A.qtu = c->F("QTU"); A.qtv = c->F("QTV"); A.qtw = c->F("QTW");
@@ -449,7 +449,7 @@ int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) 
         MG_LAUNCHED(c);
         if (!c->scabc_kind.empty()) {
             // SWA / SIO faces (bound_scalar_mod.F90:124-210), faces in order
-            WallArgs W;
+            WallArgs W{};
             W.grids = c->d_grids; W.bface = c->d_bface; W.kind = c->d_scabc_kind; W.type = c->d_scabc_type;
             W.t = T; W.u = c->F("U"); W.v = c->F("V"); W.w = c->F("W");
             W.tb = field_buffer(c, sd.name);

