@@ -147,7 +147,7 @@ def parse():
                          "finite-difference check")
     ap.add_argument("--sphere", action="store_true",
                     help="the multi-level ghost-cell case: a sphere in a channel, 16x8x8 level-1 "
-                         "grids of 24^3 and two refinement levels (plain FP64 form)")
+                         "grids of 24^3 and two refinement levels, both forms")
     ap.add_argument("--sphere-check", action="store_true",
                     help="with --sphere: one RK stage of the full case on the GPU and on the CPU "
                          "restatement, compared bit for bit")
@@ -780,12 +780,14 @@ def run_sphere(args, rank, local):
     grids, 53.1 M cells), the ghost-cell IB built from the sphere's signed
     distance, FIX inflow u = 1, OP1 outflow, periodic in y and z, Re_D = 300,
     dt of CFL 0.5 on the finest level, Williamson RK3, SIP ninner = 5,
-    nouter = 9, epcorr = 1e-10; plain FP64 form (the ghost-cell IB runs in
-    the plain form only).  Steps timed with CUDA events on the solver's
-    stream."""
+    nouter = 9, epcorr = 1e-10.  The mixed form and the plain FP64 form each
+    run the warm-up and the timed steps from the same start (CUDA events on
+    each solver's stream); the line reports the form --form names (mixed by
+    default) with the other beside it and the relative L2 difference of the
+    fields after the run."""
     import numpy as np
     import torch
-    from mglet_gb300 import channel, gpu
+    from mglet_gb300 import abi, channel, gpu
 
     if rank != 0:
         return 0
@@ -795,47 +797,52 @@ def run_sphere(args, rank, local):
     case = sc.case
     lists = sc.lists
     t_setup = time.perf_counter() - t0
-    prm = sc.flow_params(epcorr=1e-10, nouter=9, ninner=5)
     dt = sc.dt(0.5)
-    s = gpu.Solver(case, prm, device=local)
-    sc.setup(s)
     rk = gpu.rk_scheme("williamson")
-    stream = torch.cuda.ExternalStream(s.stream, device=local)
-    state = {"it": 0}
+    res, fields = {}, {}
+    for form in ("mixed", "plain"):
+        prm = sc.flow_params(abi.FORM_MIXED if form == "mixed" else abi.FORM_PLAIN, epcorr=1e-10,
+                             nouter=9, ninner=5)
+        s = gpu.Solver(case, prm, device=local)
+        sc.setup(s)
+        stream = torch.cuda.ExternalStream(s.stream, device=local)
+        state = {"it": 0}
 
-    def step():
-        state["it"] += 1
-        st = None
-        for irk in range(1, 4):
-            st = s.timeintegrate_flow(state["it"], state["it"], 0.0, dt, irk, rk)
-        return st
+        def step():
+            state["it"] += 1
+            st = None
+            for irk in range(1, 4):
+                st = s.timeintegrate_flow(state["it"], state["it"], 0.0, dt, irk, rk)
+            return st
 
-    for _ in range(args.warmup):
-        step()
-    s.synchronize()
-    clocks = Clocks(local)
-    torch.cuda.synchronize()
-    l0 = s.launches
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clocks.start()
-    ipcs = []
-    e0.record(stream)
-    for _ in range(args.steps):
-        ipcs.append(step().ipc)
-    e1.record(stream)
-    e1.synchronize()
-    clk = clocks.stop()
-    ms = e0.elapsed_time(e1)
-    launches = s.launches - l0
-    info = s.itinfo(dt)
-    s.profile(True)
-    for _ in range(max(1, min(args.steps, 2))):
-        step()
-    s.synchronize()
-    kern = {name: s.profile_get(name) for name in s.profile_names()}
-    s.profile(False)
-    s.close()
-    value = case.ncells * args.steps / (ms / 1e3)
+        for _ in range(args.warmup):
+            step()
+        s.synchronize()
+        clocks = Clocks(local)
+        torch.cuda.synchronize()
+        l0 = s.launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        clocks.start()
+        ipcs = []
+        e0.record(stream)
+        for _ in range(args.steps):
+            ipcs.append(step().ipc)
+        e1.record(stream)
+        e1.synchronize()
+        clk = clocks.stop()
+        ms = e0.elapsed_time(e1)
+        info = s.itinfo(dt)
+        res[form] = {"value": case.ncells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                     "launches": s.launches - l0, "clocks": clk,
+                     "ipc_per_stage_last": ipcs[-1] if ipcs else None,
+                     "itinfo": {"cflmax": info.cflmax, "divmax": info.divmax, "energy": info.energy},
+                     "tuning": s.tuning() if form == "mixed" else ""}
+        fields[form] = {nm: case.interior(s.get(nm)) for nm in "UVWP"}
+        s.close()
+    fm, fp = fields["mixed"], fields["plain"]
+    num = sum(np.sum((fm[n] - fp[n]) ** 2) for n in "UVW")
+    den = sum(np.sum(fp[n] ** 2) for n in "UVW")
+    pm, pp = fm["P"] - fm["P"].mean(), fp["P"] - fp["P"].mean()
     check = None
     if args.sphere_check:
         from oracle import binding
@@ -849,27 +856,34 @@ def run_sphere(args, rank, local):
         sg = g1.timeintegrate_flow(1, 1, 0.0, dt, 1, rk)
         so = o.timeintegrate_flow(1, 1, 0.0, dt, 1, binding.rk_scheme("williamson"))
         eq = {n: bool(np.array_equal(g1.get(n), o.get(n))) for n in ("U", "V", "W", "P")}
-        check = {"stage": 1, "bit_exact": eq, "ipc": [sg.ipc, so.ipc],
+        check = {"form": "plain", "stage": 1, "bit_exact": eq, "ipc": [sg.ipc, so.ipc],
                  "maxrhs": [sg.maxrhs, so.maxrhs], "seconds": time.perf_counter() - tc}
         g1.close()
     levels = [int((case.level == lv).sum()) for lv in (1, 2, 3)]
+    form = "plain" if args.form == "plain" else "mixed"
+    other = "mixed" if form == "plain" else "plain"
+    main, side = res[form], res[other]
     line = {
-        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "metric": METRIC, "value": main["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if form == "plain" else "f32 fluxes/sweeps, f64 storage",
         "data": "synthetic: uniform inflow past a sphere given by its signed distance",
         "config": {"workload": f"sphere channel 8D x 4D x 4D, {levels[0]}+{levels[1]}+{levels[2]} "
                                f"grids of 24^3 on 3 levels ({case.ncells} cells), ghost-cell IB, "
                                "FIX inflow, OP1 outflow, Re_D=300, CFL 0.5, RK3, SIP ninner=5 "
                                "nouter=9 epcorr=1e-10",
-                   "form": "plain", "cells": case.ncells, "grids_per_level": levels,
+                   "form": form, "cells": case.ncells, "grids_per_level": levels,
                    "ghost_cell_entries": int(sum(gl[1][0] + gl[2][0] + gl[3][0] for gl in lists)),
                    "intersected_cells": int(sc.geo["icells"].sum()), "dt": dt,
-                   "setup_s": t_setup, "ipc_per_stage_last": ipcs[-1] if ipcs else None,
+                   "setup_s": t_setup, "ipc_per_stage_last": main["ipc_per_stage_last"],
                    "l2": "working set > L2 (no flush needed)"},
-        "clocks": clk, "gpu_launches": launches,
-        "itinfo": {"cflmax": info.cflmax, "divmax": info.divmax, "energy": info.energy},
-        "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in kern.items()},
+        "clocks": main["clocks"], "gpu_launches": main["launches"], "itinfo": main["itinfo"],
+        "tuning": res["mixed"]["tuning"],
+        other + "_form": {k: side[k] for k in ("value", "ms_per_step", "launches", "itinfo")},
+        "mixed_vs_plain": {"steps": args.warmup + args.steps,
+                           "velocity_rel_l2": float(np.sqrt(num / den)),
+                           "pressure_rel_l2": float(np.linalg.norm(pm - pp) / np.linalg.norm(pp))},
         "oracle_check": check,
     }
     print(json.dumps(line), flush=True)

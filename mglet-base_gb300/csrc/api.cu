@@ -1172,8 +1172,6 @@ int mglet_gpu_set_stencils(mglet_ctx* c, int32_t igrid, int32_t comp, int32_t nc
 
 int mglet_gpu_set_ghostcell(mglet_ctx* c) {
     if (!c) return fail(MGLET_ERR_ARG, "set_ghostcell: null context");
-    if (c->prm.form != MGLET_FORM_PLAIN)
-        return fail(MGLET_ERR_UNSUPPORTED, "set_ghostcell: the ghost-cell IB runs in the plain form");
     cudaSetDevice(c->device);
     if (c->minlevel != c->maxlevel)   // setsdivfield restricts SDIV level by level
         if (int rc = hierarchy_ready(c)) return rc;
@@ -1188,6 +1186,7 @@ int mglet_gpu_set_ghostcell(mglet_ctx* c) {
     if ((rc = gc_upload(c))) return rc;
     c->gc_saved[0] = c->gc_saved[1] = false;
     MG_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->prm.form == MGLET_FORM_MIXED) return mixed_ghostcell(c);
     return 0;
 }
 

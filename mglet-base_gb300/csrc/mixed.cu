@@ -36,6 +36,7 @@ namespace mg {
 int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
                    const float* sz, const double* sprm, int* err, bool skip);
 bool mx_flux_has_tma(Ctx* c);
+void mx_flux_set_skip(Ctx* c, const unsigned char* d_skip);
 int mx_flux_prepare(Ctx* c);
 void mx_flux_release(Ctx* c);
 int mx_flux_tune(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
@@ -115,13 +116,14 @@ __global__ void k_mx_conv(const DevGrid* __restrict__ grids, int ngrid, int maxl
 
 #define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
 
-// mgpcorr (pressuresolver_mod.F90:808-844, no-BP form) over the reference's
-// ranges -- the pressure on the box 2..n-1, each velocity on its faces
-// 2..n-2 along its own axis -- in FP64, with dt/rho from the stage scalars.
+// mgpcorr (pressuresolver_mod.F90:808-844; BPF non-null: the bp form of the
+// ghost-cell IB) over the reference's ranges -- the pressure on the box
+// 2..n-1, each velocity on its faces 2..n-2 along its own axis -- in FP64,
+// with dt/rho from the stage scalars.
 __global__ void k_mx_mgpcorr(const DevGrid* __restrict__ grids, double* U, double* V, double* W,
                              double* P, const double* __restrict__ DP, const double* __restrict__ RDX,
                              const double* __restrict__ RDY, const double* __restrict__ RDZ,
-                             const double* __restrict__ sprm) {
+                             const double* __restrict__ sprm, const double* __restrict__ BPF) {
     const DevGrid G = grids[blockIdx.y];
     const double rfak = sprm[3];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
@@ -135,6 +137,18 @@ __global__ void k_mx_mgpcorr(const DevGrid* __restrict__ grids, double* U, doubl
     const bool ci = i >= 3 && i <= ii - 2, cj = j >= 3 && j <= jj - 2, ck = k >= 3 && k <= kk - 2;
     if (!(pi && pj && pk)) return;
     const double d = dp[c];
+    if (BPF) {
+        const double* bp = BPF + o;
+        P[o + c] = P[o + c] + d * bp[c];
+        if (i <= ii - 2 && cj && ck)
+            U[o + c] = U[o + c] + (d - dp[c + (long long)kk * jj]) * bp[c] * bp[c + (long long)kk * jj] *
+                                      RDX[G.ipx + i - 1] * rfak;
+        if (ci && j <= jj - 2 && ck)
+            V[o + c] = V[o + c] + (d - dp[c + kk]) * bp[c] * bp[c + kk] * RDY[G.ipy + j - 1] * rfak;
+        if (ci && cj && k <= kk - 2)
+            W[o + c] = W[o + c] + (d - dp[c + 1]) * bp[c] * bp[c + 1] * RDZ[G.ipz + k - 1] * rfak;
+        return;
+    }
     P[o + c] = P[o + c] + d;
     if (i <= ii - 2 && cj && ck)
         U[o + c] = U[o + c] + (d - dp[c + (long long)kk * jj]) * RDX[G.ipx + i - 1] * rfak;
@@ -245,14 +259,15 @@ int enqueue_mgpoisl(Ctx* c) {
         double* dbuf = field_buffer(c, "DP");
         for (int l = c->minlevel; l <= c->maxlevel; ++l) {
             if (int rc = launch_parent(c, l, none, sdp, false)) return rc;
-            if (int rc = launch_bound_pressure(c, l, dp, dbuf, false)) return rc;
+            if (int rc = launch_bound_pressure(c, l, dp, dbuf, c->ibtype == 1)) return rc;
         }
     }
     {
         ProfScope ps_(c, "mx_mgpcorr");
         dim3 grid((s.kk * s.jj * s.ii + 255) / 256, c->ngrid);
         k_mx_mgpcorr<<<grid, 256, 0, c->stream>>>(c->d_grids, U, V, W, P, dp, c->L("RDX"),
-                                                  c->L("RDY"), c->L("RDZ"), m->d_sprm);
+                                                  c->L("RDY"), c->L("RDZ"), m->d_sprm,
+                                                  c->ibtype == 1 ? c->F("BP") : nullptr);
         MG_LAUNCHED(c);
     }
     if (multi) {
@@ -304,6 +319,28 @@ int enqueue_stage(Ctx* c) {
                                 m->d_ctl + 2, skip))
         return rc;
     double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P");
+    const bool gc = c->ibtype == 1;
+    if (gc) {
+        // grids next to the immersed boundary: tstle4 of the transported
+        // point values PWU, PWV, PWW by the transporting U, V, W
+        // (timeintegration_mod.F90:100-101), in FP64
+        const LevelState& lv = m->lv;
+        if (int rc = launch_tstle4_grids(c, lv.d_ib, (int)lv.ib.size(), c->F("UO"), c->F("VO"), c->F("WO"),
+                                         c->F("PWU"), c->F("PWV"), c->F("PWW"), U, V, W, P, c->F("G")))
+            return rc;
+    }
+    if (c->minlevel != c->maxlevel)
+        // grids with a PAR face: tstle4_par (tstle4_mod.F90:114) on the fluxes
+        // left in UO, VO, WO
+        if (int rc = launch_tstle4_par(c, c->F("UO"), c->F("VO"), c->F("WO"), gc ? c->F("PWU") : U,
+                                       gc ? c->F("PWV") : V, gc ? c->F("PWW") : W, U, V, W))
+            return rc;
+    // the RK update of the grids whose fluxes came from UO, VO, WO
+    if (int rc = mx_rk_par(c, m->lv, m->du32, m->dv32, m->dw32, m->d_sprm)) return rc;
+    if (gc) {   // timeintegration_mod.F90:110-116: maskbp, getibvalues
+        if (int rc = launch_maskbp(c, U, V, W, P)) return rc;
+        if (int rc = launch_gc_mode(c, 'R', U, V, W)) return rc;
+    }
     if (c->minlevel == c->maxlevel) {
         if (int rc = connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
         // timeintegration_mod.F90:117-122: bound_flow after the connect
@@ -311,10 +348,6 @@ int enqueue_stage(Ctx* c) {
             if (int rc = launch_bound_flow(c, U, V, W, P, 0)) return rc;
         return enqueue_mgpoisl(c);
     }
-    // grids with a PAR face: tstle4_par (tstle4_mod.F90:114) on the fluxes
-    // the flux kernel left in UO, VO, WO, then their RK update
-    if (int rc = launch_tstle4_par(c, c->F("UO"), c->F("VO"), c->F("WO"), U, V, W, U, V, W)) return rc;
-    if (int rc = mx_rk_par(c, m->lv, m->du32, m->dv32, m->dw32, m->d_sprm)) return rc;
     // timeintegration_mod.F90:117-122: per level connect, parent, bound_flow
     static const char* const vn[3] = {"U", "V", "W"};
     static const char* const sn[3] = {"P", nullptr, nullptr};
@@ -355,6 +388,56 @@ float* du_buffer(Ctx* c, const char* name) {
 }
 
 }  // namespace
+
+// Coefficient classes: grids with the same dimensions, boundary types and
+// spacing arrays share one set of SIP factors; a grid flagged in own (BP not
+// 1 everywhere: ghost-cell IB) keeps a class of its own.  sp: the spacing
+// arrays DX, DY, DZ, DDX, DDY, DDZ.
+static void class_keys(Ctx* c, const std::vector<std::vector<double>>& sp,
+                       const std::vector<unsigned char>& own, std::vector<int>& gcls,
+                       std::vector<int>& reps) {
+    gcls.assign(c->ngrid, -1);
+    reps.clear();
+    std::map<std::vector<double>, int> seen;
+    for (int g = 0; g < c->ngrid; ++g) {
+        const DevGrid& G = c->grids[g];
+        std::vector<double> key = {(double)G.kk, (double)G.jj, (double)G.ii};
+        for (int f = 0; f < 6; ++f) key.push_back(G.bc[f]);
+        const int off[3] = {G.ipx, G.ipy, G.ipz};
+        const int len[3] = {G.ii, G.jj, G.kk};
+        for (int q = 0; q < 6; ++q)
+            key.insert(key.end(), sp[q].begin() + off[q % 3], sp[q].begin() + off[q % 3] + len[q % 3]);
+        if (!own.empty() && own[g]) key.push_back(-1.0 - g);
+        auto it = seen.find(key);
+        if (it == seen.end()) {
+            it = seen.emplace(key, (int)reps.size()).first;
+            reps.push_back(g);
+        }
+        gcls[g] = it->second;
+    }
+}
+
+// The class map to the device and the class coefficients (SIP factors,
+// Laplacian records) from the representative grids; replaces earlier ones.
+static int extract_classes(Ctx* c, const std::vector<int>& reps) {
+    MixedState* m = c->mx;
+    m->nclass = (int)reps.size();
+    MG_CUDA(copy_on(c->stream, m->d_gcls, m->gcls.data(), c->ngrid * sizeof(int), cudaMemcpyHostToDevice));
+    for (float** p : {&m->cf, &m->cb, &m->apx}) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    int* d_reps = nullptr;
+    MG_CUDA(cudaMalloc(&d_reps, reps.size() * sizeof(int)));
+    MG_CUDA(copy_on(c->stream, d_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
+    int rc = sip_extract(c, m->sip, m->nclass, d_reps, m->d_idx,
+                         c->prm.psolver != MGLET_PSOLVER_CLASSIC, &m->cf, &m->cb, &m->apx);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_reps);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "mixed classes");
+    return 0;
+}
 
 int mixed_init(Ctx* c) {
     if (!c->uniform) {
@@ -398,23 +481,7 @@ int mixed_init(Ctx* c) {
                            cudaMemcpyDeviceToHost));
     }
     std::vector<int> reps;
-    m->gcls.assign(c->ngrid, -1);
-    std::map<std::vector<double>, int> seen;
-    for (int g = 0; g < c->ngrid; ++g) {
-        const DevGrid& G = c->grids[g];
-        std::vector<double> key = {(double)G.kk, (double)G.jj, (double)G.ii};
-        for (int f = 0; f < 6; ++f) key.push_back(G.bc[f]);
-        const int off[3] = {G.ipx, G.ipy, G.ipz};
-        const int len[3] = {G.ii, G.jj, G.kk};
-        for (int q = 0; q < 6; ++q)
-            key.insert(key.end(), sp[q].begin() + off[q % 3], sp[q].begin() + off[q % 3] + len[q % 3]);
-        auto it = seen.find(key);
-        if (it == seen.end()) {
-            it = seen.emplace(key, (int)reps.size()).first;
-            reps.push_back(g);
-        }
-        m->gcls[g] = it->second;
-    }
+    class_keys(c, sp, {}, m->gcls, reps);
     m->nclass = (int)reps.size();
     // FP32 spacing tables for the flux kernel
     {
@@ -447,7 +514,6 @@ int mixed_init(Ctx* c) {
         MG_CUDA(zero_on(c->stream, *p, (size_t)c->idim3d * sizeof(float)));
     }
     MG_CUDA(cudaMalloc(&m->d_gcls, c->ngrid * sizeof(int)));
-    MG_CUDA(copy_on(c->stream, m->d_gcls, m->gcls.data(), c->ngrid * sizeof(int), cudaMemcpyHostToDevice));
     MG_CUDA(cudaMalloc(&m->d_ctl, 4 * sizeof(int)));
     MG_CUDA(zero_on(c->stream, m->d_ctl, 4 * sizeof(int)));
     MG_CUDA(cudaMalloc(&m->d_maxrhs, sizeof(double)));
@@ -461,18 +527,7 @@ int mixed_init(Ctx* c) {
     if (int rc = get_plan(c, 0, 1, 7, false, true, 1, &pl)) return rc;
     if (int rc = get_plan(c, 0, 2, 15, true, false, 0, &pl)) return rc;
     // class coefficients from the representative grids
-    int* d_reps = nullptr;
-    MG_CUDA(cudaMalloc(&d_reps, reps.size() * sizeof(int)));
-    MG_CUDA(copy_on(c->stream, d_reps, reps.data(), reps.size() * sizeof(int), cudaMemcpyHostToDevice));
-    int rc = sip_extract(c, m->sip, m->nclass, d_reps, m->d_idx,
-                         c->prm.psolver != MGLET_PSOLVER_CLASSIC, &m->cf, &m->cb, &m->apx);
-    cudaError_t e = cudaStreamSynchronize(c->stream);
-    if (rc) {
-        cudaFree(d_reps);
-        return rc;
-    }
-    cudaFree(d_reps);
-    if (e != cudaSuccess) return cuda_fail(e, "mixed_init");
+    if (int rc = extract_classes(c, reps)) return rc;
     // launch shapes picked by measurement on this case (MGLET_TUNE=0 keeps
     // the defaults)
     const char* tune = std::getenv("MGLET_TUNE");
@@ -586,12 +641,79 @@ void mixed_field_sync_out(Ctx* c, const char* name) {
         k_cvt_32_64<<<(unsigned)((c->idim3d + 255) / 256), 256, 0, c->stream>>>(c->F(name), f, c->idim3d);
 }
 
-// Hierarchies: the per-level lists and buffers, once the parents are known
-// (before the first stage is captured).
+// Hierarchies and the ghost-cell IB: the per-level lists and buffers, once
+// the parents are known (before the first stage is captured).
 static int levels_ready(Ctx* c) {
     MixedState* m = c->mx;
-    if (c->minlevel == c->maxlevel || m->lv.ready) return 0;
+    if ((c->minlevel == c->maxlevel && c->ibtype != 1) || m->lv.ready) return 0;
     return mx_level_prepare(c, m->sip, m->lv);
+}
+
+// The ghost-cell IB in the mixed form, after mglet_gpu_set_ghostcell's plain
+// set-up (SIP coefficients with BP, the lists on the device, SDIV):
+//  * BP must be 0 or 1 (the couplings laplacephi's bp products close become
+//    per-point masks); grids where it is not 1 everywhere get classes of their
+//    own, whose Laplacian records carry the masks;
+//  * grids with ghost-cell lists and their neighbours on the same level
+//    (whose ghost layers hold the lists' point values) take the FP64 tstle4
+//    of PWU, PWV, PWW by U, V, W and the separate RK update.
+int mixed_ghostcell(Ctx* c) {
+    MixedState* m = c->mx;
+    SipState& st = m->sip;
+    if (!st.prepk) {
+        set_error("mixed form: the ghost-cell IB needs the packed pre-pass (smaller grids)");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    std::vector<double> bp((size_t)c->idim3d);
+    MG_CUDA(copy_on(c->stream, bp.data(), c->F("BP"), bp.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<unsigned char> own(c->ngrid, 0), ib(c->ngrid, 0);
+    for (int g = 0; g < c->ngrid; ++g) {
+        const DevGrid& G = c->grids[g];
+        const long long n = (long long)G.kk * G.jj * G.ii;
+        for (long long t = 0; t < n; ++t) {
+            const double v = bp[G.ip3 + t];
+            if (v != 0.0 && v != 1.0) {
+                set_error("mixed form: the ghost-cell IB needs BP of 0 or 1");
+                return MGLET_ERR_UNSUPPORTED;
+            }
+            if (v != 1.0) own[g] = 1;
+        }
+        const GcHostList& L = c->gch[g];
+        if (L.n[0] + L.n[1] + L.n[2] + L.n[3] > 0) {
+            ib[g] = 1;
+            for (int sl = 1; sl <= 26; ++sl) {
+                const int nb = c->nbr[g + 1][sl];
+                if (nb > 0) ib[nb - 1] = 1;
+            }
+        }
+    }
+    // classes with the BP masks
+    if (int rc = sip_bpmask(c, st)) return rc;
+    std::vector<std::vector<double>> sp(6);
+    const char* names[6] = {"DX", "DY", "DZ", "DDX", "DDY", "DDZ"};
+    const long long lens[3] = {c->idimx, c->idimy, c->idimz};
+    for (int q = 0; q < 6; ++q) {
+        sp[q].resize(lens[q % 3]);
+        MG_CUDA(copy_on(c->stream, sp[q].data(), c->L(names[q]), lens[q % 3] * sizeof(double),
+                        cudaMemcpyDeviceToHost));
+    }
+    std::vector<int> reps;
+    class_keys(c, sp, own, m->gcls, reps);
+    if (int rc = extract_classes(c, reps)) return rc;
+    // a uniform-coefficient pre-pass no longer applies: the same launch shape
+    // with per-point records
+    if (!st.unicls && sip_pre_variant_uniform(st.pre_variant)) st.pre_variant -= 5;
+    // the grids next to the body
+    mx_level_release(m->lv);
+    m->lv.ibflag = ib;
+    if (int rc = mx_level_prepare(c, st, m->lv)) return rc;
+    mx_flux_set_skip(c, m->lv.d_skip);
+    if (m->graph) {
+        cudaGraphExecDestroy(m->graph);
+        m->graph = nullptr;
+    }
+    MG_CUDA(cudaStreamSynchronize(c->stream));
+    return 0;
 }
 
 int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st) {
@@ -617,6 +739,11 @@ int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_sta
         return MGLET_ERR_UNSUPPORTED;
     }
     if (int rc = levels_ready(c)) return rc;
+    const bool gc = c->ibtype == 1;
+    // timeintegration_mod.F90:96-99: the ghost-cell values of the step, issued
+    // before the stage graph (the flux correction reads a device flag back)
+    if (gc && irk == 1)
+        if (int rc = gc_setibvalues(c, c->F("U"), c->F("V"), c->F("W"))) return rc;
     if (int rc = set_stage_scalars(c, frhs, dt * fu, dtrk * dt)) return rc;
     if (c->prof || m->skip_once) {
         if (int rc = enqueue_stage(c)) return rc;
@@ -640,6 +767,9 @@ int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_sta
         MG_CUDA(cudaGraphLaunch(m->graph, c->stream));
         c->launches += m->graph_launches;
     }
+    // timeintegration_mod.F90:131-134: setpointvalues after the solve
+    if (gc)
+        if (int rc = gc_setpointvalues(c, irk == rk->nrk)) return rc;
     if (st) {
         MG_CUDA(cudaStreamSynchronize(c->stream));
         fill_stats(c, dtrk * dt, st);

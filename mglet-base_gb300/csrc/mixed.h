@@ -16,6 +16,8 @@ int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st);
 std::string mixed_tuning(Ctx* c);
 int mixed_force_variant(Ctx* c, const char* kernel, int v);
 int mixed_test_wait_timeout(Ctx* c);
+// the ghost-cell IB (after mglet_gpu_set_ghostcell's plain set-up)
+int mixed_ghostcell(Ctx* c);
 
 // shared with api.cu
 int connect(Ctx* c, int ilevel, int layers, double* v1, double* v2, double* v3, double* s1,

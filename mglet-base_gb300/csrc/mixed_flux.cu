@@ -90,6 +90,9 @@ struct FluxArgs {
     // the RK update follow in separate kernels)
     double *UO, *VO, *WO;
     double wrho, wgmol, cpo4, cpo5, cpo6, cpo8;
+    // per grid: 1 where another kernel computes the fluxes (grids next to an
+    // immersed boundary, whose transported velocities are PWU, PWV, PWW)
+    const unsigned char* skip;
     int* err;                          // set when a bulk-copy wait gives up
     int skip_plane;                    // test switch: this plane's copy is not issued (0: none)
     int nslab;                         // j-slabs (CTAs) per grid
@@ -374,6 +377,7 @@ __device__ void boundary_terms(const FluxArgs& a, const DevGrid& G, int k, int j
 template <bool kW>
 __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     extern __shared__ float2 sm[];
+    if (kW && a.skip && a.skip[blockIdx.x / a.nslab]) return;
     const DevGrid G = a.grids[blockIdx.x / a.nslab];
     const int slab = blockIdx.x % a.nslab;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
@@ -549,6 +553,7 @@ __global__ void __launch_bounds__(576, 2)
     unsigned char* fsm = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<unsigned long long>(fraw) + 127) & ~127ULL);
     const int gid = blockIdx.x;
+    if (kW && a.skip && a.skip[gid]) return;
     const DevGrid G = a.grids[gid];
     const int kk = G.kk, jj = G.jj, ii = G.ii, kj = kk * jj;
     const int nk = kk - 4, nj = jj - 4, j0 = 3;
@@ -723,6 +728,7 @@ struct FluxState {
     CUtensorMap map[4];
     bool tma = false;
     bool walls = false;     // some grid has a face that is not CON: the boundary path
+    const unsigned char* d_skip = nullptr;   // grids whose fluxes another kernel computes
     int variant = -1;
     double ms[2] = {0.0, 0.0};
 };
@@ -851,6 +857,7 @@ static FluxArgs flux_args(Ctx* c, float* du, float* dv, float* dw, const float* 
     // (wernerwengle_mod.F90:13-28 init_wernerwengle)
     a.G = c->F("G");
     a.UO = c->F("UO"); a.VO = c->F("VO"); a.WO = c->F("WO");
+    a.skip = g_flux[c].d_skip;
     a.ddx = c->L("DDX"); a.ddy = c->L("DDY"); a.ddz = c->L("DDZ");
     a.wwx = c->L("WWX"); a.wwy = c->L("WWY"); a.wwz = c->L("WWZ");
     const double rho = c->prm.rho, cwa = 8.3, cwb = 1.0 / 7.0;
@@ -931,5 +938,14 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
 }
 
 bool mx_flux_has_tma(Ctx* c) { return g_flux[c].tma; }
+
+// Grids (device flags, 1 = skip) whose fluxes the caller computes with
+// another kernel; the boundary instantiation, which honours the flags, is
+// used from then on.
+void mx_flux_set_skip(Ctx* c, const unsigned char* d_skip) {
+    FluxState& fs = g_flux[c];
+    fs.d_skip = d_skip;
+    if (d_skip) fs.walls = true;
+}
 
 }  // namespace mg

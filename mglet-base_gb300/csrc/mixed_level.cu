@@ -67,6 +67,7 @@ struct BpArgs {
     const float* H;
     float* PG;                  // [ngrid][6][fs]
     const double *dx, *dy, *dz, *ddx, *ddy, *ddz;
+    const double* BP;           // ghost-cell IB: the BP field (null: the no-BP form)
     const int* ctl;
 };
 
@@ -133,20 +134,48 @@ __global__ void k_mx_bound_pressure(BpArgs A) {
         else { k = n; j = aa; i = bb; }
         return Hg[m.pos(i - 3, j - 3, k - 3)];
     };
-    // pressureftocone: volume mean of the 2x2x2 interior block next to the face
+    // pressureftocone_A / _B: the (BP-weighted) volume mean of the 2x2x2
+    // interior block next to the face
     int k0, j0, i0;
     if (axis == 0) { k0 = a; j0 = b; i0 = nmin; }
     else if (axis == 1) { k0 = a; j0 = nmin; i0 = b; }
     else { k0 = nmin; j0 = a; i0 = b; }
-    double sump = 0.0, sumvol = 0.0;
-    for (int l = 0; l <= 1; ++l)
-        for (int mm = 0; mm <= 1; ++mm)
-            for (int n = 0; n <= 1; ++n) {
-                const double vol = ddz[k0 + n] * ddy[j0 + mm] * ddx[i0 + l];
-                sump = sump + (double)Hg[m.pos(i0 + l - 3, j0 + mm - 3, k0 + n - 3)] * vol;
-                sumvol = sumvol + vol;
-            }
-    const double pc = sump / sumvol;
+    const double* bp = A.BP ? A.BP + G.ip3 : nullptr;
+    const int kk = G.kk, jj = G.jj;
+    auto bix = [&](int kx, int jx, int ix) -> long long {
+        return (long long)(ix - 1) * kk * jj + (long long)(jx - 1) * kk + (kx - 1);
+    };
+    double pc, bpc = 1.0;
+    if (!bp) {
+        double sump = 0.0, sumvol = 0.0;
+        for (int l = 0; l <= 1; ++l)
+            for (int mm = 0; mm <= 1; ++mm)
+                for (int n = 0; n <= 1; ++n) {
+                    const double vol = ddz[k0 + n] * ddy[j0 + mm] * ddx[i0 + l];
+                    sump = sump + (double)Hg[m.pos(i0 + l - 3, j0 + mm - 3, k0 + n - 3)] * vol;
+                    sumvol = sumvol + vol;
+                }
+        pc = sump / sumvol;
+    } else {
+        double sumbp = 0.0;
+        for (int l = 0; l <= 1; ++l)
+            for (int mm = 0; mm <= 1; ++mm)
+                for (int n = 0; n <= 1; ++n) sumbp = sumbp + bp[bix(k0 + n, j0 + mm, i0 + l)];
+        bpc = fmin(sumbp, 1.0);
+        pc = 0.0;
+        if (bpc >= 0.5) {
+            double sump = 0.0, sumvol = 0.0;
+            for (int l = 0; l <= 1; ++l)
+                for (int mm = 0; mm <= 1; ++mm)
+                    for (int n = 0; n <= 1; ++n) {
+                        const double vol = bp[bix(k0 + n, j0 + mm, i0 + l)] * ddz[k0 + n] * ddy[j0 + mm] *
+                                           ddx[i0 + l];
+                        sump = sump + (double)Hg[m.pos(i0 + l - 3, j0 + mm - 3, k0 + n - 3)] * vol;
+                        sumvol = sumvol + vol;
+                    }
+            pc = sump / sumvol;
+        }
+    }
     // the parent's slab cell of this block (parent_core_mod.F90:190-255 for a
     // scalar: both block corners odd, so the slab value itself)
     const int4 h = A.hier[g];
@@ -164,7 +193,28 @@ __global__ void k_mx_bound_pressure(BpArgs A) {
     else if (axis == 1) { kc = ks + jc - 1; jcc = js; icc = is + ic - 1; }
     else { kc = ks; jcc = js + jc - 1; icc = is + ic - 1; }
     const double pbv = (double)coarse_hilf(A, p, icc - 3, jcc - 3, kc - 3);
-    const double fac = dstag[st2] / (dn[n3] + dn[n2]);
+    double fak = 1.0;
+    if (bp) {
+        // bound_pressure's open-area factor of the block's four face pairs
+        const double* da = axis == 2 ? ddy : ddz;
+        const double* db = axis == 0 ? ddy : ddx;
+        auto fp = [&](int aa, int bb, int n) -> long long {
+            if (axis == 0) return bix(aa, bb, n);
+            if (axis == 1) return bix(aa, n, bb);
+            return bix(n, aa, bb);
+        };
+        if (bpc < 0.5) pc = pbv;
+        const double s11 = bp[fp(a, b, n2)] * bp[fp(a, b, n3)];
+        const double s12 = bp[fp(a, b + 1, n2)] * bp[fp(a, b + 1, n3)];
+        const double s13 = bp[fp(a + 1, b, n2)] * bp[fp(a + 1, b, n3)];
+        const double s14 = bp[fp(a + 1, b + 1, n2)] * bp[fp(a + 1, b + 1, n3)];
+        fak = (s11 * db[b] * da[a] + s12 * db[b + 1] * da[a] + s13 * db[b] * da[a + 1] +
+               s14 * db[b + 1] * da[a + 1]) /
+              ((db[b] + db[b + 1]) * (da[a] + da[a + 1]));
+        if (fak < (double)0.1f) fak = 1.0;
+        fak = 1.0 / fak;
+    }
+    const double fac = fak * dstag[st2] / (dn[n3] + dn[n2]);
     float* pg = A.PG + ((long long)g * 6 + f) * m.fs;
     for (int l = 0; l <= 1; ++l)
         for (int n = 0; n <= 1; ++n) {
@@ -180,10 +230,14 @@ __global__ void k_mx_bound_pressure(BpArgs A) {
 // ftoc of a cell-centred field from the fine grids of one level into their
 // parents: the volume mean of each 2x2x2 block (noib_restrict 'P', also the
 // 'R' of the residual).  LO null: FP32 H; else the float-float pair (H, LO).
+// With BP (ghost-cell IB) the forms of gc_restrict_mod.F90: restrict_p, the
+// mean over the open cells (hilf), and restrict_r, the BP-weighted sum over
+// the block volume (the residual).
 __global__ void k_mx_ftoc(const DevGrid* __restrict__ grids, const int4* __restrict__ hier,
                           const int* __restrict__ list, PlaneMap m, float* H, float* LO,
                           const double* __restrict__ DDX, const double* __restrict__ DDY,
-                          const double* __restrict__ DDZ, const int* ctl) {
+                          const double* __restrict__ DDZ, const double* __restrict__ BP,
+                          const int* ctl) {
     if (ctl[0]) return;
     const int g = list[blockIdx.y];
     const DevGrid G = grids[g];
@@ -199,14 +253,36 @@ __global__ void k_mx_ftoc(const DevGrid* __restrict__ grids, const int4* __restr
         const long long o = base + m.pos(ix - 3, jx - 3, kx - 3);
         return LO ? (double)H[o] + (double)LO[o] : (double)H[o];
     };
-    const double s = F(k, j, i) * ddz[k] * ddy[j] * ddx[i] + F(k, j, i + 1) * ddz[k] * ddy[j] * ddx[i + 1] +
-                     F(k, j + 1, i) * ddz[k] * ddy[j + 1] * ddx[i] +
-                     F(k, j + 1, i + 1) * ddz[k] * ddy[j + 1] * ddx[i + 1] +
-                     F(k + 1, j, i) * ddz[k + 1] * ddy[j] * ddx[i] +
-                     F(k + 1, j, i + 1) * ddz[k + 1] * ddy[j] * ddx[i + 1] +
-                     F(k + 1, j + 1, i) * ddz[k + 1] * ddy[j + 1] * ddx[i] +
-                     F(k + 1, j + 1, i + 1) * ddz[k + 1] * ddy[j + 1] * ddx[i + 1];
-    const double val = s / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
+    double val;
+    if (!BP) {
+        const double s = F(k, j, i) * ddz[k] * ddy[j] * ddx[i] + F(k, j, i + 1) * ddz[k] * ddy[j] * ddx[i + 1] +
+                         F(k, j + 1, i) * ddz[k] * ddy[j + 1] * ddx[i] +
+                         F(k, j + 1, i + 1) * ddz[k] * ddy[j + 1] * ddx[i + 1] +
+                         F(k + 1, j, i) * ddz[k + 1] * ddy[j] * ddx[i] +
+                         F(k + 1, j, i + 1) * ddz[k + 1] * ddy[j] * ddx[i + 1] +
+                         F(k + 1, j + 1, i) * ddz[k + 1] * ddy[j + 1] * ddx[i] +
+                         F(k + 1, j + 1, i + 1) * ddz[k + 1] * ddy[j + 1] * ddx[i + 1];
+        val = s / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
+    } else {
+        const int kk = G.kk, jj = G.jj;
+        const double* bp = BP + G.ip3;
+        auto B = [&](int kx, int jx, int ix) -> double {
+            return bp[(long long)(ix - 1) * kk * jj + (long long)(jx - 1) * kk + (kx - 1)];
+        };
+        const int cj[4] = {j, j, j + 1, j + 1}, ci[4] = {i, i + 1, i, i + 1};
+        double spv = 0.0, sv = 0.0;
+        for (int l = 0; l < 2; ++l)
+            for (int q4 = 0; q4 < 4; ++q4) {
+                const int kq = k + l;
+                const double vol = B(kq, cj[q4], ci[q4]) * ddz[kq] * ddy[cj[q4]] * ddx[ci[q4]];
+                spv = spv + F(kq, cj[q4], ci[q4]) * vol;
+                sv = sv + vol;
+            }
+        if (LO)   // restrict_r
+            val = spv / ((ddx[i] + ddx[i + 1]) * (ddy[j] + ddy[j + 1]) * (ddz[k] + ddz[k + 1]));
+        else      // restrict_p
+            val = sv > 0.0 ? spv / sv : 0.0;
+    }
     const int4 h = hier[g];
     const int ioc = h.y + (i - 3) / 2 - 3, joc = h.z + (j - 3) / 2 - 3, koc = h.w + (k - 3) / 2 - 3;
     if (ioc < 0 || ioc >= m.ni || joc < 0 || joc >= m.nj || koc < 0 || koc >= m.nk) return;
@@ -286,16 +362,18 @@ int mx_level_prepare(Ctx* c, SipState& st, LevelState& lv) {
         lv.grids[l].push_back(g);
         bool par = false;
         for (int f = 0; f < 6; ++f) par |= G.bc[f] == MGLET_BC_PAR;
+        const bool ib = !lv.ibflag.empty() && lv.ibflag[g];
         if (par) {
             lv.pars[l].push_back(g);
-            lv.parall.push_back(g);
             anypar = true;
-            if (c->hier[g].x < 0) {
+            if (c->hier.empty() || c->hier[g].x < 0) {
                 set_error("mixed form: a grid with a PAR face has no parent");
                 return MGLET_ERR_ARG;
             }
         }
-        if (l > 0 && c->hier[g].x < 0) {
+        if (par || ib) lv.parall.push_back(g);
+        if (ib) lv.ib.push_back(g);
+        if (l > 0 && (c->hier.empty() || c->hier[g].x < 0)) {
             set_error("mixed form: a fine grid without parent (mglet_gpu_set_hierarchy first)");
             return MGLET_ERR_ARG;
         }
@@ -305,6 +383,11 @@ int mx_level_prepare(Ctx* c, SipState& st, LevelState& lv) {
         if (int rc = upload(c, lv.pars[l], &lv.d_pars[l])) return rc;
     }
     if (int rc = upload(c, lv.parall, &lv.d_parall)) return rc;
+    if (int rc = upload(c, lv.ib, &lv.d_ib)) return rc;
+    if (!lv.ib.empty()) {
+        MG_CUDA(cudaMalloc(&lv.d_skip, (size_t)c->ngrid));
+        MG_CUDA(copy_on(c->stream, lv.d_skip, lv.ibflag.data(), (size_t)c->ngrid, cudaMemcpyHostToDevice));
+    }
     if (anypar && !st.pg) {
         const size_t n = (size_t)c->ngrid * 6 * st.fs * sizeof(float);
         MG_CUDA(cudaMalloc(&st.pg, n));
@@ -314,9 +397,15 @@ int mx_level_prepare(Ctx* c, SipState& st, LevelState& lv) {
     // the grids with PAR faces, tstle4_par adds, k_mx_rk_par clears them
     for (const char* nm : {"UO", "VO", "WO"})
         MG_CUDA(zero_on(c->stream, c->F(nm), (size_t)c->idim3d * sizeof(double)));
-    // the level operators' boundary buffers, allocated before any capture
+    // the level operators' boundary buffers and the per-level connect
+    // plans of the stage, built before any capture
     for (const char* nm : {"U", "V", "W", "P", "DP"})
         if (!field_buffer(c, nm)) return cuda_fail(cudaErrorMemoryAllocation, "mixed level buffers");
+    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+        const ConnectPlan* pl;
+        if (int rc = get_plan(c, l, 1, 7, false, true, 1, &pl)) return rc;
+        if (int rc = get_plan(c, l, 2, 15, true, false, 0, &pl)) return rc;
+    }
     lv.ready = true;
     return 0;
 }
@@ -325,6 +414,8 @@ void mx_level_release(LevelState& lv) {
     for (int* p : lv.d_grids) cudaFree(p);
     for (int* p : lv.d_pars) cudaFree(p);
     cudaFree(lv.d_parall);
+    cudaFree(lv.d_ib);
+    cudaFree(lv.d_skip);
     lv = LevelState();
 }
 
@@ -354,6 +445,7 @@ int mx_bound_pressure(Ctx* c, SipState& st, const LevelState& lv, int ilevel, co
     A.PG = st.pg;
     A.dx = c->L("DX"); A.dy = c->L("DY"); A.dz = c->L("DZ");
     A.ddx = c->L("DDX"); A.ddy = c->L("DDY"); A.ddz = c->L("DDZ");
+    A.BP = c->ibtype == 1 ? c->F("BP") : nullptr;
     A.ctl = ctl;
     const int nbmax = std::max(st.nk * st.nj, std::max(st.nk * st.ni, st.nj * st.ni)) / 4;
     const dim3 grid((nbmax + 127) / 128, (unsigned)lv.pars[l].size(), 6);
@@ -370,7 +462,8 @@ int mx_ftoc(Ctx* c, SipState& st, const LevelState& lv, int ilevel, bool rhs, co
     const dim3 grid((nq + 127) / 128, (unsigned)lv.grids[l].size());
     k_mx_ftoc<<<grid, 128, 0, c->stream>>>(c->d_grids, c->d_hier, lv.d_grids[l], plane_map(st),
                                            rhs ? st.rhs32 : st.h32, rhs ? st.rhsl : nullptr,
-                                           c->L("DDX"), c->L("DDY"), c->L("DDZ"), ctl);
+                                           c->L("DDX"), c->L("DDY"), c->L("DDZ"),
+                                           c->ibtype == 1 ? c->F("BP") : nullptr, ctl);
     MG_LAUNCHED(c);
     return 0;
 }

@@ -8,13 +8,21 @@
 namespace mg {
 
 // Per level (index ilevel - minlevel): its grids and those with a PAR face,
-// host and device lists; every grid with a PAR face.
+// host and device lists; every grid whose fluxes and RK update run apart
+// from the fused flux kernel (a PAR face, or next to an immersed boundary);
+// the grids next to an immersed boundary (ibflag, set before the set-up:
+// their transported velocities PWU, PWV, PWW differ from U, V, W) as a list
+// and as per-grid skip flags of the flux kernel.
 struct LevelState {
     bool ready = false;
     std::vector<std::vector<int>> grids, pars;
     std::vector<int*> d_grids, d_pars;
     std::vector<int> parall;
     int* d_parall = nullptr;
+    std::vector<unsigned char> ibflag;
+    std::vector<int> ib;
+    int* d_ib = nullptr;
+    unsigned char* d_skip = nullptr;
 };
 
 // Lists, the PAR ghost planes of hilf and the level operators' buffers; once,

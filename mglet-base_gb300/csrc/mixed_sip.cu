@@ -355,7 +355,8 @@ __global__ void k_sip_pre_records(const DevGrid* __restrict__ grids, const int* 
                                   const float* __restrict__ CF, const float* __restrict__ AW,
                                   const float* __restrict__ AE, const float* __restrict__ AS,
                                   const float* __restrict__ AN, const float* __restrict__ AB,
-                                  const float* __restrict__ AT, float4* PR) {
+                                  const float* __restrict__ AT, const unsigned char* __restrict__ BM,
+                                  float4* PR) {
     const int cls = blockIdx.y;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= npp) return;
@@ -375,8 +376,11 @@ __global__ void k_sip_pre_records(const DevGrid* __restrict__ grids, const int* 
     const int ix = G.ipx + 2 + io, iy = G.ipy + 2 + jo, iz = G.ipz + 2 + ko;
     P1[p] = make_float4(__int_as_float(code[3 * p]), __int_as_float(code[3 * p + 1]),
                         __int_as_float(code[3 * p + 2]), cf[3 * lp]);
-    P1[npp + p] = make_float4(AW[ix], AE[ix], AS[iy], AN[iy]);
-    P1[2 * npp + p] = make_float4(AB[iz], AT[iz], cf[4 * lp], 0.f);
+    // ghost-cell IB: the couplings BP closes (laplacephi's bp products)
+    const unsigned mk = BM ? BM[(long long)reps[cls] * npp + p] : 0x3Fu;
+    auto on = [mk](int b, float x) { return (mk >> b) & 1u ? x : 0.f; };
+    P1[npp + p] = make_float4(on(0, AW[ix]), on(1, AE[ix]), on(2, AS[iy]), on(3, AN[iy]));
+    P1[2 * npp + p] = make_float4(on(4, AB[iz]), on(5, AT[iz]), cf[4 * lp], 0.f);
 }
 
 struct BwdArgs {
@@ -778,6 +782,7 @@ __device__ __forceinline__ double block_max2(double v, double* sh) {
 struct OuterArgs {
     Shape s;
     const float* PG;            // [ngrid][6][fs] PAR ghost planes of hilf (null: none)
+    const unsigned char* BM;    // [ngrid][npp] open couplings (ghost-cell IB; null: all)
     const int* fnbr;
     const int* gcls;
     const float* H;
@@ -869,12 +874,21 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
         const int bm = (ko > 0 || jo > 0) ? spst[t - 1] + ro[(t - 1) * ni + io] + jo : 0;
         const int bp = (ko < nk - 1 || jo < nj - 1) ? spst[t + 1] + ro[(t + 1) * ni + io] + jo : 0;
         const float hc = H[q];
-        const float him = io > 0 ? H[spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo] : gh[0 * fs + fidx_x(s, ko, jo)];
-        const float hip = io < ni - 1 ? H[spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo] : gh[1 * fs + fidx_x(s, ko, jo)];
-        const float hjm = jo > 0 ? H[bm - 1] : gh[2 * fs + fidx_y(s, ko, io)];
-        const float hjp = jo < nj - 1 ? H[bp + 1] : gh[3 * fs + fidx_y(s, ko, io)];
-        const float hkm = ko > 0 ? H[bm] : gh[4 * fs + fidx_z(s, jo, io)];
-        const float hkp = ko < nk - 1 ? H[bp] : gh[5 * fs + fidx_z(s, jo, io)];
+        float him = io > 0 ? H[spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo] : gh[0 * fs + fidx_x(s, ko, jo)];
+        float hip = io < ni - 1 ? H[spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo] : gh[1 * fs + fidx_x(s, ko, jo)];
+        float hjm = jo > 0 ? H[bm - 1] : gh[2 * fs + fidx_y(s, ko, io)];
+        float hjp = jo < nj - 1 ? H[bp + 1] : gh[3 * fs + fidx_y(s, ko, io)];
+        float hkm = ko > 0 ? H[bm] : gh[4 * fs + fidx_z(s, jo, io)];
+        float hkp = ko < nk - 1 ? H[bp] : gh[5 * fs + fidx_z(s, jo, io)];
+        if (a.BM) {   // couplings BP closes contribute nothing (laplacephi's bp products)
+            const unsigned mk = a.BM[base + q];
+            him = mk & 1u ? him : 0.f;
+            hip = mk & 2u ? hip : 0.f;
+            hjm = mk & 4u ? hjm : 0.f;
+            hjp = mk & 8u ? hjp : 0.f;
+            hkm = mk & 16u ? hkm : 0.f;
+            hkp = mk & 32u ? hkp : 0.f;
+        }
         float sum = 0.f, comp = 0.f;
         ff_acc(awh[io], awl[io], him, sum, comp);
         ff_acc(aeh[io], ael[io], hip, sum, comp);
@@ -911,7 +925,8 @@ __global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const i
                              const double* __restrict__ U, const double* __restrict__ V,
                              const double* __restrict__ W, const double* __restrict__ RDDX,
                              const double* __restrict__ RDDY, const double* __restrict__ RDDZ,
-                             const double* __restrict__ pfak) {
+                             const double* __restrict__ pfak, const double* __restrict__ SDIV,
+                             const double* __restrict__ BP) {
     const int g = blockIdx.y;
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= npp) return;
@@ -927,12 +942,42 @@ __global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const i
     const int k = id % kk + 1, j = (id / kk) % jj + 1, i = id / (kk * jj) + 1;
     const double *u = U + G.ip3, *v = V + G.ip3, *w = W + G.ip3;
     const double fak = *pfak;
-    const double d = fak * ((u[id] - u[id - kk * jj]) * RDDX[G.ipx + i - 1] +
-                            (v[id] - v[id - kk]) * RDDY[G.ipy + j - 1] +
-                            (w[id] - w[id - 1]) * RDDZ[G.ipz + k - 1]);
+    double d = fak * ((u[id] - u[id - kk * jj]) * RDDX[G.ipx + i - 1] +
+                      (v[id] - v[id - kk]) * RDDY[G.ipy + j - 1] +
+                      (w[id] - w[id - 1]) * RDDZ[G.ipz + k - 1]);
+    if (SDIV) {   // ghost-cell IB (gc_mod.F90:278-347): the flux correction, masked by BP
+        d = d + fak * SDIV[G.ip3 + id];
+        d = BP[G.ip3 + id] * d;
+    }
     const float dh = (float)d;   // float-float: leading float and the rounding of the rest
     RHS[o] = dh;
     RHSL[o] = (float)(d - (double)dh);
+}
+
+// The open couplings of every padded position (ghost-cell IB): bit f (faces
+// i-1, i+1, j-1, j+1, k-1, k+1) is set where bp(neighbour) * bp(point) is
+// 1, the factor laplacephi puts on that neighbour (BP is 0 or 1).
+__global__ void k_sip_bpmask(const DevGrid* __restrict__ grids, int npp, const int* __restrict__ idxp,
+                             const double* __restrict__ BP, unsigned char* BM) {
+    const int g = blockIdx.y;
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= npp) return;
+    const int id = idxp[q];
+    const long long o = (long long)g * npp + q;
+    if (id < 0) {
+        BM[o] = 0;
+        return;
+    }
+    const DevGrid G = grids[g];
+    const int kk = G.kk, jj = G.jj;
+    const double* bp = BP + G.ip3;
+    const long long st[3] = {(long long)kk * jj, kk, 1};
+    unsigned mk = 0;
+    for (int d = 0; d < 3; ++d) {
+        if (bp[id - st[d]] * bp[id] == 1.0) mk |= 1u << (2 * d);       // st[0] is i, st[2] k
+        if (bp[id] * bp[id + st[d]] == 1.0) mk |= 1u << (2 * d + 1);
+    }
+    BM[o] = (unsigned char)mk;
 }
 
 // dp (plane order, float-float) -> DP field (natural layout, interior, FP64)
@@ -1469,6 +1514,13 @@ int sip_init(Ctx* c, SipState& st) {
 int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* d_idx,
                 bool planeorder, float** cf, float** cb, float** apx) {
     const size_t n = (size_t)nclass * st.npp;
+    // a second extraction (new classes after the ghost-cell set-up) replaces
+    // the records of the first
+    for (void** p : {(void**)&st.swf, (void**)&st.swb, (void**)&st.spr, (void**)&st.uni}) {
+        cudaFree(*p);
+        *p = nullptr;
+    }
+    st.unicls = false;
     MG_CUDA(cudaMalloc(cf, 5 * n * sizeof(float)));
     MG_CUDA(cudaMalloc(cb, 3 * n * sizeof(float)));
     MG_CUDA(cudaMalloc(apx, 2 * n * sizeof(float)));
@@ -1489,7 +1541,7 @@ int sip_extract(Ctx* c, SipState& st, int nclass, const int* d_reps, const int* 
         MG_CUDA(cudaMalloc(&st.spr, 3 * n * sizeof(float4)));
         k_sip_pre_records<<<grid, 256, 0, c->stream>>>(
             c->d_grids, d_reps, st.d_pst, st.nm, st.npp, st.d_pq, st.d_pcode, *cf, st.a1[0], st.a1[1],
-            st.a1[2], st.a1[3], st.a1[4], st.a1[5], st.spr);
+            st.a1[2], st.a1[3], st.a1[4], st.a1[5], st.bm, st.spr);
         MG_LAUNCHED(c);
         // classes whose seven Laplacian coefficients are the same at every point
         std::vector<float4> rec(3 * n);
@@ -1534,7 +1586,7 @@ void sip_release(SipState& st) {
                     (void*)st.d_pcode, (void*)st.spr, (void*)st.uni, (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
-                    (void*)st.a1lo[4], (void*)st.a1lo[5], (void*)st.pg})
+                    (void*)st.a1lo[4], (void*)st.a1lo[5], (void*)st.pg, (void*)st.bm})
         cudaFree(p);
 }
 
@@ -1543,7 +1595,9 @@ int sip_divcal(Ctx* c, SipState& st, const double* fak) {
     dim3 grid((st.npp + 255) / 256, c->ngrid);
     k_sip_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.rhs32, st.rhsl,
                                               c->F("U"), c->F("V"), c->F("W"), c->L("RDDX"),
-                                              c->L("RDDY"), c->L("RDDZ"), fak);
+                                              c->L("RDDY"), c->L("RDDZ"), fak,
+                                              c->ibtype == 1 ? c->F("SDIV") : nullptr,
+                                              c->ibtype == 1 ? c->F("BP") : nullptr);
     MG_LAUNCHED(c);
     return 0;
 }
@@ -1633,6 +1687,7 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     OuterArgs a{};
     a.s = shape(st);
     a.PG = st.pg;
+    a.BM = st.bm;
     a.fnbr = st.d_fnbr; a.gcls = gcls;
     a.H = st.h32;
     a.RHS = st.rhs32; a.RHSL = st.rhsl; a.DPH = st.dph; a.DPL = st.dpl; a.APX = apx;
@@ -1646,6 +1701,14 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     a.ctl_err = const_cast<int*>(ctl) + 2;
     a.rev = next_order(st);
     k_sip_outer<<<c->ngrid, 512, stencil_smem(st), c->stream>>>(a);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int sip_bpmask(Ctx* c, SipState& st) {
+    if (!st.bm) MG_CUDA(cudaMalloc(&st.bm, (size_t)c->ngrid * st.npp));
+    dim3 grid((st.npp + 255) / 256, c->ngrid);
+    k_sip_bpmask<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, c->F("BP"), st.bm);
     MG_LAUNCHED(c);
     return 0;
 }

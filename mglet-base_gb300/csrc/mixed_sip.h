@@ -57,6 +57,9 @@ struct SipState {
     // hierarchies: the hilf ghost planes of PAR faces [ngrid][6][fs], set by
     // the mixed bound_pressure before every inner iteration of a level
     float* pg = nullptr;
+    // ghost-cell IB: per grid and padded position the open couplings (bit f
+    // for faces i-1, i+1, j-1, j+1, k-1, k+1), null without the IB
+    unsigned char* bm = nullptr;
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
@@ -77,6 +80,8 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
                  bool hzero, const int* glist = nullptr, int nlist = 0);
 int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl);
 int sip_scatter_dp(Ctx* c, SipState& st);
+// The open-coupling masks of every grid from BP (ghost-cell IB)
+int sip_bpmask(Ctx* c, SipState& st);
 // Times every valid pre-pass variant on the current buffers and keeps the
 // fastest (cached per grid shape and class layout for the process).
 int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl);

@@ -266,8 +266,11 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
                                                 const double* __restrict__ P, const double* __restrict__ Gf,
                                                 Wall wl, double iles, double gx, double gy, double gz,
                                                 const double* __restrict__ FX, const double* __restrict__ FY,
-                                                const double* __restrict__ FZ, const double* __restrict__ GU) {
-    const DevGrid G = grids[blockIdx.y];
+                                                const double* __restrict__ FZ, const double* __restrict__ GU,
+                                                const int* __restrict__ list) {
+    // list: the grids of this launch (null: grid = blockIdx.y)
+    const int gi = list ? list[blockIdx.y] : blockIdx.y;
+    const DevGrid G = grids[gi];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int npts = kk * jj * ii;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -276,8 +279,8 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
     const int j = (t / kk) % jj + 1;
     const int i = t / (kk * jj) + 1;
     if (GU) {
-        wl.guni = GU[2 * blockIdx.y] != 0.0;
-        wl.h2 = GU[2 * blockIdx.y + 1];
+        wl.guni = GU[2 * gi] != 0.0;
+        wl.h2 = GU[2 * gi + 1];
     }
     GridPtrs s;
     s.kk = kk; s.jj = jj; s.ii = ii;
@@ -402,10 +405,37 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
                                           c->prm.gradp[2],
                                           c->bodyforce ? c->F("FBX") : nullptr,
                                           c->bodyforce ? c->F("FBY") : nullptr,
-                                          c->bodyforce ? c->F("FBZ") : nullptr, c->d_guni);
+                                          c->bodyforce ? c->F("FBZ") : nullptr, c->d_guni, nullptr);
     MG_LAUNCHED(c);
     // tstle4_mod.F90:114: tstle4_par after kon, diff and gradp (PAR faces)
     return launch_tstle4_par(c, uo, vo, wo, u, v, w, ut, vt, wt);
+}
+
+// kon, diff and gradp of tstle4 (no tstle4_par) on the n grids of a device
+// list only: the mixed form's grids next to an immersed boundary, whose
+// transported velocities (PWU, PWV, PWW) differ from the transporting ones.
+int launch_tstle4_grids(Ctx* c, const int* list, int n, double* uo, double* vo, double* wo,
+                        const double* u, const double* v, const double* w, const double* ut,
+                        const double* vt, const double* wt, const double* p, const double* g) {
+    if (n <= 0) return 0;
+    ProfScope ps_(c, "tstle4_grids");
+    k_g_uniform<<<c->ngrid, 256, 0, c->stream>>>(c->d_grids, g, c->prm.gmol, c->d_guni);
+    MG_LAUNCHED(c);
+    Wall wl = {};
+    const double gmol = c->prm.gmol, rho = c->prm.rho, cwa = 8.3, cwb = 1.0 / 7.0;
+    const double cpo1 = 1.0 - cwb, cpo2 = 1.0 + cwb;
+    wl.rho = rho;
+    wl.gmol = gmol;
+    wl.cpo4 = cpo2 / cwa * std::pow(gmol / rho, cwb);
+    wl.cpo5 = 0.5 * cpo1 * std::pow(cwa, cpo2 / cpo1) * std::pow(gmol / rho, cpo2);
+    wl.cpo6 = 0.5 * gmol / rho * std::pow(cwa, 2.0 / cpo1);
+    wl.cpo8 = 2.0 / cpo2;
+    dim3 grid((max_points(c) + 255) / 256, n);
+    k_tstle4<<<grid, 256, 0, c->stream>>>(c->d_grids, spacing(c), uo, vo, wo, u, v, w, ut, vt, wt, p, g,
+                                          wl, 0.0, c->prm.gradp[0], c->prm.gradp[1], c->prm.gradp[2],
+                                          nullptr, nullptr, nullptr, c->d_guni, list);
+    MG_LAUNCHED(c);
+    return 0;
 }
 
 int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu) {
