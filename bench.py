@@ -647,6 +647,8 @@ def run_precision(args, rank, local):
             row["divmax_mixed"] = mix.itinfo(dtp).divmax
             row["divmax_plain"] = ref.itinfo(dtp).divmax
             rows.append(row)
+            # progress on stderr: a run cut short still leaves its rows
+            print(json.dumps(row), file=sys.stderr, flush=True)
     field = ("Taylor-Green + splitmix64 noise 1e-2 (seed 42), nu=1/1600, RK3 dt=5e-4" if tg else
              "solenoidal random field (k ~ 4, rms 1), nu=1e-3, RK3 dt=2e-4")
     line = {"precision": "mixed vs plain FP64", "workload":
@@ -774,6 +776,30 @@ def run_adjoint(args, rank, local):
     return 0
 
 
+def perturb_fp32(s, case, seed=5):
+    """Multiplies the interior of U, V, W by 1 +- 2^-24 (one FP32 unit
+    roundoff, random signs): the start of the FP64 form's sensitivity run,
+    which measures how far rounding at FP32 level alone carries the flow."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    for nm in "UVW":
+        a = s.get(nm)
+        it = case.interior(a)
+        it *= 1.0 + 2.0 ** -24 * rng.choice((-1.0, 1.0), size=it.shape)
+        s.set(nm, a)
+
+
+def field_diff(fa, fb):
+    """Relative L2 of the velocity vector and of the pressure (mean removed)
+    between two sets of interior fields."""
+    import numpy as np
+    num = sum(np.sum((fa[n] - fb[n]) ** 2) for n in "UVW")
+    den = sum(np.sum(fb[n] ** 2) for n in "UVW")
+    pa, pb = fa["P"] - fa["P"].mean(), fb["P"] - fb["P"].mean()
+    return {"velocity_rel_l2": float(np.sqrt(num / den)),
+            "pressure_rel_l2": float(np.linalg.norm(pa - pb) / np.linalg.norm(pb))}
+
+
 def run_sphere(args, rank, local):
     """The sphere in a channel, 8D x 4D x 4D: level 1 = 16 x 8 x 8 grids of
     24^3, levels 2 and 3 refined around the sphere (1024 + 704 + 2112
@@ -784,7 +810,9 @@ def run_sphere(args, rank, local):
     run the warm-up and the timed steps from the same start (CUDA events on
     each solver's stream); the line reports the form --form names (mixed by
     default) with the other beside it and the relative L2 difference of the
-    fields after the run."""
+    fields after the run, and beside that the same difference for the FP64
+    form started from a state perturbed by one FP32 unit roundoff (how far
+    rounding alone carries this flow)."""
     import numpy as np
     import torch
     from mglet_gb300 import abi, channel, gpu
@@ -800,11 +828,13 @@ def run_sphere(args, rank, local):
     dt = sc.dt(0.5)
     rk = gpu.rk_scheme("williamson")
     res, fields = {}, {}
-    for form in ("mixed", "plain"):
+    for form in ("mixed", "plain", "perturbed"):
         prm = sc.flow_params(abi.FORM_MIXED if form == "mixed" else abi.FORM_PLAIN, epcorr=1e-10,
                              nouter=9, ninner=5)
         s = gpu.Solver(case, prm, device=local)
         sc.setup(s)
+        if form == "perturbed":
+            perturb_fp32(s, case)
         stream = torch.cuda.ExternalStream(s.stream, device=local)
         state = {"it": 0}
 
@@ -839,10 +869,6 @@ def run_sphere(args, rank, local):
                      "tuning": s.tuning() if form == "mixed" else ""}
         fields[form] = {nm: case.interior(s.get(nm)) for nm in "UVWP"}
         s.close()
-    fm, fp = fields["mixed"], fields["plain"]
-    num = sum(np.sum((fm[n] - fp[n]) ** 2) for n in "UVW")
-    den = sum(np.sum(fp[n] ** 2) for n in "UVW")
-    pm, pp = fm["P"] - fm["P"].mean(), fp["P"] - fp["P"].mean()
     check = None
     if args.sphere_check:
         from oracle import binding
@@ -882,8 +908,9 @@ def run_sphere(args, rank, local):
         "tuning": res["mixed"]["tuning"],
         other + "_form": {k: side[k] for k in ("value", "ms_per_step", "launches", "itinfo")},
         "mixed_vs_plain": {"steps": args.warmup + args.steps,
-                           "velocity_rel_l2": float(np.sqrt(num / den)),
-                           "pressure_rel_l2": float(np.linalg.norm(pm - pp) / np.linalg.norm(pp))},
+                           **field_diff(fields["mixed"], fields["plain"])},
+        "fp64_sensitivity": {"what": "plain form from a start perturbed by 2^-24 vs plain form",
+                             **field_diff(fields["perturbed"], fields["plain"])},
         "oracle_check": check,
     }
     print(json.dumps(line), flush=True)
@@ -899,7 +926,10 @@ def run_channel(args, rank, local):
     epcorr = 1e-10.  The mixed form and the plain FP64 form each run the
     warm-up and the timed steps from the same start (CUDA events on each
     solver's stream); the line reports the mixed form and, beside it, the
-    plain one and the relative L2 difference of the fields after the run."""
+    plain one and the relative L2 difference of the fields after the run,
+    and the same difference for the FP64 form started from a state
+    perturbed by one FP32 unit roundoff (how far rounding alone carries this
+    flow)."""
     import numpy as np
     import torch
     from mglet_gb300 import abi, cases, gpu
@@ -917,7 +947,8 @@ def run_channel(args, rank, local):
     rk = gpu.rk_scheme("williamson")
     out = {}
     fields = {}
-    for form in (abi.FORM_MIXED, abi.FORM_PLAIN):
+    for name in ("mixed", "plain", "perturbed"):
+        form = abi.FORM_MIXED if name == "mixed" else abi.FORM_PLAIN
         prm = abi.make_flow_params(gmol=1.0 / 300.0, epcorr=1e-10, nouter=9, ninner=5, nouter_min=0,
                                    form=form)
         s = gpu.Solver(case, prm, device=local)
@@ -935,6 +966,8 @@ def run_channel(args, rank, local):
             s.connect(lvl, 1, v1="U", v2="V", v3="W", normal=True, forward=1)
             s.parent(lvl, v=("U", "V", "W"), s=("P",))
             s.bound_flow(lvl)
+        if name == "perturbed":
+            perturb_fp32(s, case)
         stream = torch.cuda.ExternalStream(s.stream, device=local)
         it = [0]
 
@@ -961,17 +994,13 @@ def run_channel(args, rank, local):
         e1.synchronize()
         clk = clocks.stop()
         ms = e0.elapsed_time(e1)
-        out[form] = {"value": case.ncells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+        out[name] = {"value": case.ncells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
                      "launches": s.launches - l0, "clocks": clk,
                      "nouter_last": last.nouter_done if last else None,
-                     "tuning": s.tuning() if form == abi.FORM_MIXED else ""}
-        fields[form] = {nm: case.interior(s.get(nm)) for nm in "UVWP"}
+                     "tuning": s.tuning() if name == "mixed" else ""}
+        fields[name] = {nm: case.interior(s.get(nm)) for nm in "UVWP"}
         s.close()
-    fm, fp = fields[abi.FORM_MIXED], fields[abi.FORM_PLAIN]
-    num = sum(np.sum((fm[n] - fp[n]) ** 2) for n in "UVW")
-    den = sum(np.sum(fp[n] ** 2) for n in "UVW")
-    pm, pp = fm["P"] - fm["P"].mean(), fp["P"] - fp["P"].mean()
-    mixed, plain = out[abi.FORM_MIXED], out[abi.FORM_PLAIN]
+    mixed, plain = out["mixed"], out["plain"]
     line = {
         "metric": METRIC, "value": mixed["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": mixed["ms_per_step"], "higher_is_better": True,
@@ -986,8 +1015,9 @@ def run_channel(args, rank, local):
         "nouter_last": mixed["nouter_last"], "tuning": mixed["tuning"],
         "plain_fp64": {k: plain[k] for k in ("value", "ms_per_step", "launches", "nouter_last")},
         "mixed_vs_plain": {"steps": args.warmup + args.steps,
-                           "velocity_rel_l2": float(np.sqrt(num / den)),
-                           "pressure_rel_l2": float(np.linalg.norm(pm - pp) / np.linalg.norm(pp))},
+                           **field_diff(fields["mixed"], fields["plain"])},
+        "fp64_sensitivity": {"what": "plain form from a start perturbed by 2^-24 vs plain form",
+                             **field_diff(fields["perturbed"], fields["plain"])},
     }
     print(json.dumps(line), flush=True)
     return 0

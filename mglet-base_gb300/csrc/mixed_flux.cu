@@ -93,6 +93,9 @@ struct FluxArgs {
     // per grid: 1 where another kernel computes the fluxes (grids next to an
     // immersed boundary, whose transported velocities are PWU, PWV, PWW)
     const unsigned char* skip;
+    // per grid {1, h2} where G is one value on the box 2..n-1: the uniform
+    // face viscosities hold there too
+    const double* guni;
     int* err;                          // set when a bulk-copy wait gives up
     int skip_plane;                    // test switch: this plane's copy is not issued (0: none)
     int nslab;                         // j-slabs (CTAs) per grid
@@ -260,9 +263,10 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
 }
 
 // ---- grids with faces that have no neighbour --------------------------------
-// harmonic face mean of tstle4_diff: g*g'/MAX(g+g', gmol)
-__device__ __forceinline__ double fhm(double x, double y, double gmol) {
-    const double s = x + y;
+// harmonic face mean of tstle4_diff: g*g'/MAX(g+g', gmol), in FP32 like
+// the rest of the fluxes
+__device__ __forceinline__ float fhm(float x, float y, float gmol) {
+    const float s = x + y;
     return x * y / (s < gmol ? gmol : s);
 }
 
@@ -275,29 +279,29 @@ __device__ __forceinline__ Visc3 visc_uniform(const FluxArgs& a) {
 // the point (k, j, i) of one grid, from its viscosity field gg: next to a face
 // without a neighbour the ghost values of G enter the means (zero on the
 // walls of the coarsest level, so no viscous flux crosses them).
-__device__ Visc3 visc_field(const double* gg, int kk, int jj, int k, int j, int i, double gm) {
-    auto G = [&](int kq, int jq, int iq) {
-        return gg[(long long)(iq - 1) * kk * jj + (long long)(jq - 1) * kk + (kq - 1)];
+__device__ Visc3 visc_field(const double* gg, int kk, int jj, int k, int j, int i, float gm) {
+    auto G = [&](int kq, int jq, int iq) -> float {
+        return (float)gg[(long long)(iq - 1) * kk * jj + (long long)(jq - 1) * kk + (kq - 1)];
     };
     Visc3 v;
-    v.u.e = (float)G(k, j, i + 1);
-    v.u.w = (float)G(k, j, i);
-    v.u.n = (float)(fhm(G(k, j, i), G(k, j + 1, i), gm) + fhm(G(k, j, i + 1), G(k, j + 1, i + 1), gm));
-    v.u.s = (float)(fhm(G(k, j - 1, i), G(k, j, i), gm) + fhm(G(k, j - 1, i + 1), G(k, j, i + 1), gm));
-    v.u.t = (float)(fhm(G(k, j, i), G(k + 1, j, i), gm) + fhm(G(k, j, i + 1), G(k + 1, j, i + 1), gm));
-    v.u.b = (float)(fhm(G(k - 1, j, i), G(k, j, i), gm) + fhm(G(k - 1, j, i + 1), G(k, j, i + 1), gm));
-    v.v.e = (float)(fhm(G(k, j, i), G(k, j, i + 1), gm) + fhm(G(k, j + 1, i), G(k, j + 1, i + 1), gm));
-    v.v.w = (float)(fhm(G(k, j, i - 1), G(k, j, i), gm) + fhm(G(k, j + 1, i - 1), G(k, j + 1, i), gm));
-    v.v.n = (float)G(k, j + 1, i);
-    v.v.s = (float)G(k, j, i);
-    v.v.t = (float)(fhm(G(k, j, i), G(k + 1, j, i), gm) + fhm(G(k, j + 1, i), G(k + 1, j + 1, i), gm));
-    v.v.b = (float)(fhm(G(k - 1, j, i), G(k, j, i), gm) + fhm(G(k - 1, j + 1, i), G(k, j + 1, i), gm));
-    v.w.e = (float)(fhm(G(k, j, i), G(k, j, i + 1), gm) + fhm(G(k + 1, j, i), G(k + 1, j, i + 1), gm));
-    v.w.w = (float)(fhm(G(k, j, i - 1), G(k, j, i), gm) + fhm(G(k + 1, j, i - 1), G(k + 1, j, i), gm));
-    v.w.n = (float)(fhm(G(k, j, i), G(k, j + 1, i), gm) + fhm(G(k + 1, j, i), G(k + 1, j + 1, i), gm));
-    v.w.s = (float)(fhm(G(k, j - 1, i), G(k, j, i), gm) + fhm(G(k + 1, j - 1, i), G(k + 1, j, i), gm));
-    v.w.t = (float)G(k + 1, j, i);
-    v.w.b = (float)G(k, j, i);
+    v.u.e = G(k, j, i + 1);
+    v.u.w = G(k, j, i);
+    v.u.n = fhm(G(k, j, i), G(k, j + 1, i), gm) + fhm(G(k, j, i + 1), G(k, j + 1, i + 1), gm);
+    v.u.s = fhm(G(k, j - 1, i), G(k, j, i), gm) + fhm(G(k, j - 1, i + 1), G(k, j, i + 1), gm);
+    v.u.t = fhm(G(k, j, i), G(k + 1, j, i), gm) + fhm(G(k, j, i + 1), G(k + 1, j, i + 1), gm);
+    v.u.b = fhm(G(k - 1, j, i), G(k, j, i), gm) + fhm(G(k - 1, j, i + 1), G(k, j, i + 1), gm);
+    v.v.e = fhm(G(k, j, i), G(k, j, i + 1), gm) + fhm(G(k, j + 1, i), G(k, j + 1, i + 1), gm);
+    v.v.w = fhm(G(k, j, i - 1), G(k, j, i), gm) + fhm(G(k, j + 1, i - 1), G(k, j + 1, i), gm);
+    v.v.n = G(k, j + 1, i);
+    v.v.s = G(k, j, i);
+    v.v.t = fhm(G(k, j, i), G(k + 1, j, i), gm) + fhm(G(k, j + 1, i), G(k + 1, j + 1, i), gm);
+    v.v.b = fhm(G(k - 1, j, i), G(k, j, i), gm) + fhm(G(k - 1, j + 1, i), G(k, j + 1, i), gm);
+    v.w.e = fhm(G(k, j, i), G(k, j, i + 1), gm) + fhm(G(k + 1, j, i), G(k + 1, j, i + 1), gm);
+    v.w.w = fhm(G(k, j, i - 1), G(k, j, i), gm) + fhm(G(k + 1, j, i - 1), G(k + 1, j, i), gm);
+    v.w.n = fhm(G(k, j, i), G(k, j + 1, i), gm) + fhm(G(k + 1, j, i), G(k + 1, j + 1, i), gm);
+    v.w.s = fhm(G(k, j - 1, i), G(k, j, i), gm) + fhm(G(k + 1, j - 1, i), G(k + 1, j, i), gm);
+    v.w.t = G(k + 1, j, i);
+    v.w.b = G(k, j, i);
     return v;
 }
 
@@ -314,11 +318,12 @@ __device__ __forceinline__ bool has_par_face(const DevGrid& G) {
 }
 
 // The face viscosities of the point: from G on the outermost interior layer
-// of a grid with a face without a neighbour, else the uniform ones.
-__device__ __forceinline__ Visc3 visc_at(const FluxArgs& a, const DevGrid& G, bool wg, int k, int j,
+// of a grid whose G is not one value (wv: a wall's zero ghosts), else the
+// uniform ones.
+__device__ __forceinline__ Visc3 visc_at(const FluxArgs& a, const DevGrid& G, bool wv, int k, int j,
                                          int i) {
     const bool shell = i == 3 || i == G.ii - 2 || j == 3 || j == G.jj - 2 || k == 3 || k == G.kk - 2;
-    if (wg && shell) return visc_field(a.G + G.ip3, G.kk, G.jj, k, j, i, a.wgmol);
+    if (wv && shell) return visc_field(a.G + G.ip3, G.kk, G.jj, k, j, i, (float)a.wgmol);
     return visc_uniform(a);
 }
 
@@ -455,11 +460,12 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     const float gfl = (float)G.gradpflag;
     const bool wg = kW && has_open_face(G);
     const bool pgrid = kW && has_par_face(G);
+    const bool wv = wg && !(a.guni && a.guni[2 * (blockIdx.x / a.nslab)] != 0.0);
     for (int i = 3; i <= ii - 2; ++i) {
         float uo = 0.f, vo = 0.f, wo = 0.f;
         if (on) {
             if constexpr (kW) {
-                const Visc3 vs = visc_at(a, G, wg, k, j, i);
+                const Visc3 vs = visc_at(a, G, wv, k, j, i);
                 flux_point<true>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo, wo);
                 if (wg) boundary_terms(a, G, k, j, i, ucur, vcur, wcur, uo, vo, wo);
             } else {
@@ -665,11 +671,12 @@ __global__ void __launch_bounds__(576, 2)
     const float gfl = (float)G.gradpflag;
     const bool wg = kW && has_open_face(G);
     const bool pgrid = kW && has_par_face(G);
+    const bool wv = wg && !(a.guni && a.guni[2 * gid] != 0.0);
     for (int i = 3; i <= ii - 2; ++i) {
         float uo = 0.f, vo = 0.f, wo = 0.f;
         if (on) {
             if constexpr (kW) {
-                const Visc3 vs = visc_at(a, G, wg, k, j, i);
+                const Visc3 vs = visc_at(a, G, wv, k, j, i);
                 flux_point<true>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo, wo);
                 if (wg) boundary_terms(a, G, k, j, i, ucur, vcur, wcur, uo, vo, wo);
             } else {
@@ -858,6 +865,7 @@ static FluxArgs flux_args(Ctx* c, float* du, float* dv, float* dw, const float* 
     a.G = c->F("G");
     a.UO = c->F("UO"); a.VO = c->F("VO"); a.WO = c->F("WO");
     a.skip = g_flux[c].d_skip;
+    a.guni = c->d_guni;
     a.ddx = c->L("DDX"); a.ddy = c->L("DDY"); a.ddz = c->L("DDZ");
     a.wwx = c->L("WWX"); a.wwy = c->L("WWY"); a.wwz = c->L("WWZ");
     const double rho = c->prm.rho, cwa = 8.3, cwb = 1.0 / 7.0;
@@ -930,6 +938,9 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
     int threads;
     FluxArgs a = flux_args(c, du, dv, dw, sx, sy, sz, sprm, err, &threads);
     const FluxState& fs = g_flux[c];
+    // the boundary instantiation reads G only on grids where it is not one value
+    if (fs.walls)
+        if (int rc = launch_g_uniform(c)) return rc;
     if (skip && fs.tma) {
         a.skip_plane = 4;
         return launch_variant(c, 1, a, threads);

@@ -377,6 +377,14 @@ __global__ void k_g_uniform(const DevGrid* __restrict__ grids, const double* __r
     }
 }
 
+// Per grid {1, h2} where G is one value on the box 2..n-1 (see k_g_uniform)
+// into the context's d_guni.
+int launch_g_uniform(Ctx* c) {
+    k_g_uniform<<<c->ngrid, 256, 0, c->stream>>>(c->d_grids, c->F("G"), c->prm.gmol, c->d_guni);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
 static int max_points(Ctx* c) {
     int m = 0;
     for (const DevGrid& g : c->grids) m = std::max(m, g.kk * g.jj * g.ii);
