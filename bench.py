@@ -805,7 +805,10 @@ def run_sphere(args, rank, local):
     24^3, levels 2 and 3 refined around the sphere (1024 + 704 + 2112
     grids, 53.1 M cells), the ghost-cell IB built from the sphere's signed
     distance, FIX inflow u = 1, OP1 outflow, periodic in y and z, Re_D = 300,
-    dt of CFL 0.5 on the finest level, Williamson RK3, SIP ninner = 5,
+    dt = 0.25 h / U on the finest level, which holds the measured CFL number
+    (itinfo's cflmax: the flow speeds up around the body) at about 0.5 -- at
+    0.5 h / U the impulsive start drives it above 1 and the run diverges
+    within seven steps in both forms; Williamson RK3, SIP ninner = 5,
     nouter = 9, epcorr = 1e-10.  The mixed form and the plain FP64 form each
     run the warm-up and the timed steps from the same start (CUDA events on
     each solver's stream); the line reports the form --form names (mixed by
@@ -825,7 +828,7 @@ def run_sphere(args, rank, local):
     case = sc.case
     lists = sc.lists
     t_setup = time.perf_counter() - t0
-    dt = sc.dt(0.5)
+    dt = sc.dt(0.25)
     rk = gpu.rk_scheme("williamson")
     res, fields = {}, {}
     for form in ("mixed", "plain", "perturbed"):
@@ -897,7 +900,7 @@ def run_sphere(args, rank, local):
         "data": "synthetic: uniform inflow past a sphere given by its signed distance",
         "config": {"workload": f"sphere channel 8D x 4D x 4D, {levels[0]}+{levels[1]}+{levels[2]} "
                                f"grids of 24^3 on 3 levels ({case.ncells} cells), ghost-cell IB, "
-                               "FIX inflow, OP1 outflow, Re_D=300, CFL 0.5, RK3, SIP ninner=5 "
+                               "FIX inflow, OP1 outflow, Re_D=300, measured CFL ~0.5 (dt = 0.25 h/U), RK3, SIP ninner=5 "
                                "nouter=9 epcorr=1e-10",
                    "form": form, "cells": case.ncells, "grids_per_level": levels,
                    "ghost_cell_entries": int(sum(gl[1][0] + gl[2][0] + gl[3][0] for gl in lists)),
@@ -921,8 +924,9 @@ def run_channel(args, rank, local):
     """The sphere channel's hierarchy without the sphere: 16 x 8 x 8 level-1
     grids of 24^3 refined twice around the quarter point (1024 + 704 + 2112
     grids, 53.1 M cells), FIX inflow u = 1, OP1 outflow, periodic in y and z,
-    nu = 1/300, a Taylor-Green perturbation of 10 % on the mean flow, dt of
-    CFL 0.5 on the finest level, Williamson RK3, SIP ninner = 5, nouter = 9,
+    nu = 1/300, a Taylor-Green perturbation of 10 % on the mean flow, dt =
+    0.25 h / U on the finest level (measured CFL about 0.5), Williamson RK3,
+    SIP ninner = 5, nouter = 9,
     epcorr = 1e-10.  The mixed form and the plain FP64 form each run the
     warm-up and the timed steps from the same start (CUDA events on each
     solver's stream); the line reports the mixed form and, beside it, the
@@ -943,7 +947,7 @@ def run_channel(args, rank, local):
     u, v, w, p = cases.taylor_green(case)
     init = dict(zip("UVWP", (1.0 + 0.1 * u, 0.1 * v, 0.1 * w, 0.01 * p)))
     one = np.ones(case.kk * case.jj)
-    dt = 0.5 * float(case.ddx.min())
+    dt = 0.25 * float(case.ddx.min())
     rk = gpu.rk_scheme("williamson")
     out = {}
     fields = {}
@@ -994,7 +998,9 @@ def run_channel(args, rank, local):
         e1.synchronize()
         clk = clocks.stop()
         ms = e0.elapsed_time(e1)
-        out[name] = {"value": case.ncells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+        info = s.itinfo(dt)
+        out[name] = {"itinfo": {"cflmax": info.cflmax, "divmax": info.divmax, "energy": info.energy},
+                     "value": case.ncells * args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
                      "launches": s.launches - l0, "clocks": clk,
                      "nouter_last": last.nouter_done if last else None,
                      "tuning": s.tuning() if name == "mixed" else ""}
@@ -1008,12 +1014,12 @@ def run_channel(args, rank, local):
         "data": "synthetic: uniform inflow with a Taylor-Green perturbation",
         "config": {"workload": f"channel 8 x 4 x 4, {levels[0]}+{levels[1]}+{levels[2]} grids of 24^3 "
                                f"on 3 levels ({case.ncells} cells), FIX inflow, OP1 outflow, nu=1/300, "
-                               "CFL 0.5, RK3, SIP ninner=5 nouter=9 epcorr=1e-10",
+                               "measured CFL ~0.5 (dt = 0.25 h/U), RK3, SIP ninner=5 nouter=9 epcorr=1e-10",
                    "form": "mixed", "cells": case.ncells, "grids_per_level": levels, "dt": dt,
                    "l2": "working set > L2 (no flush needed)"},
         "clocks": mixed["clocks"], "gpu_launches": mixed["launches"],
-        "nouter_last": mixed["nouter_last"], "tuning": mixed["tuning"],
-        "plain_fp64": {k: plain[k] for k in ("value", "ms_per_step", "launches", "nouter_last")},
+        "nouter_last": mixed["nouter_last"], "tuning": mixed["tuning"], "itinfo": mixed["itinfo"],
+        "plain_fp64": {k: plain[k] for k in ("value", "ms_per_step", "launches", "nouter_last", "itinfo")},
         "mixed_vs_plain": {"steps": args.warmup + args.steps,
                            **field_diff(fields["mixed"], fields["plain"])},
         "fp64_sensitivity": {"what": "plain form from a start perturbed by 2^-24 vs plain form",
