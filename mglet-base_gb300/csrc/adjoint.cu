@@ -9,7 +9,9 @@
 // velocity and is linearised about the stored stage input.  The adjoint of
 // each operator is written out as its transpose:
 //
-//   connect           dst <- src copies  -> lambda(src) += lambda(dst), lambda(dst) = 0
+//   connect           dst <- src copies  -> lambda(src) += lambda(dst), lambda(dst) = 0,
+//                     the copies grouped by the grid they read, one CTA per
+//                     group walking its copies in order
 //   mgpcorr           gather of lambda(dp) from the velocity faces and p
 //   pressure solve    dp = L^-1 rhs with the symmetric periodic Laplacian of
 //                     uniform grids: lambda(rhs) = L^-1 lambda(dp), solved by
@@ -18,8 +20,13 @@
 //   divcal            gather of lambda(u) from the two cells of each face
 //   rkstep            dU = frhs dU + UO, U = U + dtfu dU
 //   tstle4            per output point, the derivatives of its flux formula
-//                     scattered (atomicAdd) into lambda(u, v, w, p); the body
-//                     force takes lambda(uo) directly
+//                     added into lambda(u, v, w, p) of its 3x3x3 neighbourhood;
+//                     the points run in 27 colour classes (i, j, k mod 3), so
+//                     no two points of a launch touch the same value and the
+//                     sums are formed in a fixed order; the body force takes
+//                     lambda(uo) directly
+//
+// No atomics anywhere: the gradient is the same bits on every run.
 //
 // The objective is the kinetic energy of enerfg (timeintegration_mod.F90:
 // 417-452): sum vol 0.5 (up^2 + vp^2 + wp^2) / sum vol over the interior.
@@ -45,19 +52,27 @@ struct AdjSlots {
     double* f[6];
 };
 
-// transpose of k_connect: the ghost's adjoint goes to its source
-__global__ void k_adj_connect(const BoxCopy* __restrict__ tasks, AdjSlots fs) {
-    const BoxCopy t = tasks[blockIdx.x];
-    double* a = fs.f[t.slot];
-    if (!a) return;
-    const int nkj = t.nk * t.nj;
-    for (int q = threadIdx.x; q < t.npts; q += blockDim.x) {
-        const int k = q % t.nk, j = (q / t.nk) % t.nj, i = q / nkj;
-        const long long d = t.dst + (long long)i * t.djj + (long long)j * t.dkk + k;
-        const long long s = t.src + (long long)i * t.sjj + (long long)j * t.skk + k;
-        const double v = a[d];
-        a[d] = 0.0;
-        atomicAdd(&a[s], v);
+// transpose of k_connect: the ghost's adjoint goes to its source.  One CTA
+// per group of copies that read the same grid, the copies of a group in
+// their order: within one copy every source point is distinct, and the
+// groups add into disjoint grids.
+__global__ void k_adj_connect(const BoxCopy* __restrict__ tasks, const int* __restrict__ start,
+                              AdjSlots fs) {
+    for (int ti = start[blockIdx.x]; ti < start[blockIdx.x + 1]; ++ti) {
+        const BoxCopy t = tasks[ti];
+        double* a = fs.f[t.slot];
+        if (a) {
+            const int nkj = t.nk * t.nj;
+            for (int q = threadIdx.x; q < t.npts; q += blockDim.x) {
+                const int k = q % t.nk, j = (q / t.nk) % t.nj, i = q / nkj;
+                const long long d = t.dst + (long long)i * t.djj + (long long)j * t.dkk + k;
+                const long long s = t.src + (long long)i * t.sjj + (long long)j * t.skk + k;
+                const double v = a[d];
+                a[d] = 0.0;
+                a[s] += v;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -180,21 +195,23 @@ struct AdjGrid {
 // one convective face flux q = 0.5 F (xa + xb) with F = A (c1 t1 + c2 t2):
 // gq = dJ/dq scattered into the transported (la, lb) and transporting
 // (lt1, lt2) adjoints
+__device__ __forceinline__ void acc(double* p, double v) { *p += v; }
+
 __device__ __forceinline__ void adj_face(double gq, double F, double xa, double xb, double* la,
                                          double* lb, double A, double c1, double* lt1, double c2,
                                          double* lt2) {
     const double gx = gq * 0.5 * F;
-    atomicAdd(la, gx);
-    atomicAdd(lb, gx);
+    acc(la, gx);
+    acc(lb, gx);
     const double gF = gq * 0.5 * (xa + xb) * A;
-    atomicAdd(lt1, gF * c1);
-    atomicAdd(lt2, gF * c2);
+    acc(lt1, gF * c1);
+    acc(lt2, gF * c2);
 }
 
 // one viscous face flux: the output carries +cf (x1 - x0)
 __device__ __forceinline__ void adj_diff(double l, double cf, double* l1, double* l0) {
-    atomicAdd(l1, l * cf);
-    atomicAdd(l0, -l * cf);
+    acc(l1, l * cf);
+    acc(l0, -l * cf);
 }
 
 // transpose of the linearised tstle4 (kon about U, V, W; diff; gradp; body force)
@@ -209,12 +226,13 @@ __global__ void __launch_bounds__(256) k_adj_tstle4(const DevGrid* __restrict__ 
                                                     const double* __restrict__ LWO,
                                                     double* LU, double* LV, double* LW, double* LP,
                                                     double* GFX, double* GFY, double* GFZ,
-                                                    double gmol, double rho) {
+                                                    double gmol, double rho, int color) {
     const DevGrid Gd = grids[blockIdx.y];
     const int kk = Gd.kk, jj = Gd.jj, ii = Gd.ii;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= kk * jj * ii) return;
     const int k = t % kk + 1, j = (t / kk) % jj + 1, i = t / (kk * jj) + 1;
+    if (i % 3 + 3 * (j % 3) + 9 * (k % 3) != color) return;
     const long long o = Gd.ip3;
     // every face is CON: the ranges of tstle4 are 3..n-2 for every component
     if (i < 3 || i > ii - 2 || j < 3 || j > jj - 2 || k < 3 || k > kk - 2) return;
@@ -231,8 +249,8 @@ __global__ void __launch_bounds__(256) k_adj_tstle4(const DevGrid* __restrict__ 
         const double l = LUO[o + t];
         GFX[o + t] += l;
         const double cp = 1.0 / (rho * dx[i]);
-        atomicAdd(P(lp, k, j, i + 1), -cp * l);
-        atomicAdd(P(lp, k, j, i), cp * l);
+        acc(P(lp, k, j, i + 1), -cp * l);
+        acc(P(lp, k, j, i), cp * l);
         // diff
         const double ax = ddy[j] * ddz[k], ay = dx[i] * ddz[k], az = dx[i] * ddy[j];
         const double fak = 1.0 / rho * rddy[j] * rdx[i] * rddz[k];
@@ -274,8 +292,8 @@ __global__ void __launch_bounds__(256) k_adj_tstle4(const DevGrid* __restrict__ 
         const double l = LVO[o + t];
         GFY[o + t] += l;
         const double cp = 1.0 / (rho * dy[j]);
-        atomicAdd(P(lp, k, j + 1, i), -cp * l);
-        atomicAdd(P(lp, k, j, i), cp * l);
+        acc(P(lp, k, j + 1, i), -cp * l);
+        acc(P(lp, k, j, i), cp * l);
         const double ax = dy[j] * ddz[k], ay = ddx[i] * ddz[k], az = ddx[i] * dy[j];
         const double fak = 1.0 / rho * rddx[i] * rdy[j] * rddz[k];
         const double ge = hmean(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hmean(A(gg, k, j + 1, i), A(gg, k, j + 1, i + 1), gmol);
@@ -315,8 +333,8 @@ __global__ void __launch_bounds__(256) k_adj_tstle4(const DevGrid* __restrict__ 
         const double l = LWO[o + t];
         GFZ[o + t] += l;
         const double cp = 1.0 / (rho * dz[k]);
-        atomicAdd(P(lp, k + 1, j, i), -cp * l);
-        atomicAdd(P(lp, k, j, i), cp * l);
+        acc(P(lp, k + 1, j, i), -cp * l);
+        acc(P(lp, k, j, i), cp * l);
         const double ax = ddy[j] * dz[k], ay = ddx[i] * dz[k], az = ddx[i] * ddy[j];
         const double fak = 1.0 / rho * rddx[i] * rddy[j] * rdz[k];
         const double ge = hmean(A(gg, k, j, i), A(gg, k, j, i + 1), gmol) + hmean(A(gg, k + 1, j, i), A(gg, k + 1, j, i + 1), gmol);
@@ -427,12 +445,43 @@ dim3 box_grid(Ctx* c) {
 
 int adj_connect(Ctx* c, int ilevel, int layers, int slots, bool corners, bool normal, int fwd,
                 double* const f[6]) {
-    const ConnectPlan* plan = nullptr;
-    if (int rc = get_plan(c, ilevel, layers, slots, corners, normal, fwd, &plan)) return rc;
-    if (plan->ntasks == 0) return 0;
+    const ConnectPlan* cplan = nullptr;
+    if (int rc = get_plan(c, ilevel, layers, slots, corners, normal, fwd, &cplan)) return rc;
+    if (cplan->ntasks == 0) return 0;
+    ConnectPlan* plan = const_cast<ConnectPlan*>(cplan);
+    if (!plan->d_bysrc) {
+        // group the copies by the grid holding their source (stable: the
+        // copies of a group keep the plan's order)
+        std::vector<BoxCopy> tasks(plan->ntasks);
+        MG_CUDA(copy_on(c->stream, tasks.data(), plan->d_tasks, tasks.size() * sizeof(BoxCopy),
+                        cudaMemcpyDeviceToHost));
+        auto src_grid = [&](long long src) {
+            int g = 0;
+            for (int q = 0; q < c->ngrid; ++q)
+                if (c->grids[q].ip3 <= src) g = q;
+            return g;
+        };
+        std::vector<std::pair<int, int>> key(tasks.size());
+        for (size_t q = 0; q < tasks.size(); ++q) key[q] = {src_grid(tasks[q].src), (int)q};
+        std::stable_sort(key.begin(), key.end());
+        std::vector<BoxCopy> sorted;
+        std::vector<int> start;
+        for (size_t q = 0; q < key.size(); ++q) {
+            if (q == 0 || key[q].first != key[q - 1].first) start.push_back((int)q);
+            sorted.push_back(tasks[key[q].second]);
+        }
+        start.push_back((int)key.size());
+        MG_CUDA(cudaMalloc(&plan->d_bysrc, sorted.size() * sizeof(BoxCopy)));
+        MG_CUDA(copy_on(c->stream, plan->d_bysrc, sorted.data(), sorted.size() * sizeof(BoxCopy),
+                        cudaMemcpyHostToDevice));
+        MG_CUDA(cudaMalloc(&plan->d_srcstart, start.size() * sizeof(int)));
+        MG_CUDA(copy_on(c->stream, plan->d_srcstart, start.data(), start.size() * sizeof(int),
+                        cudaMemcpyHostToDevice));
+        plan->nsrc = (int)start.size() - 1;
+    }
     AdjSlots fs;
     for (int q = 0; q < 6; ++q) fs.f[q] = f[q];
-    k_adj_connect<<<plan->ntasks, 128, 0, c->stream>>>(plan->d_tasks, fs);
+    k_adj_connect<<<plan->nsrc, 128, 0, c->stream>>>(plan->d_bysrc, plan->d_srcstart, fs);
     MG_LAUNCHED(c);
     return 0;
 }
@@ -530,11 +579,13 @@ int adjoint_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) {
     MG_LAUNCHED(c);
     const double* const* sp = spacing_table(c);
     if (!sp) return fail(MGLET_ERR_CUDA, "adjoint: spacing table");
-    k_adj_tstle4<<<bg, 256, 0, c->stream>>>(c->d_grids, sp, c->F("U"), c->F("V"), c->F("W"), c->F("G"),
-                                            c->F("UO"), c->F("VO"), c->F("WO"), LU, LV, LW, LP,
-                                            c->F("GFX"), c->F("GFY"), c->F("GFZ"), c->prm.gmol,
-                                            c->prm.rho);
-    MG_LAUNCHED(c);
+    for (int color = 0; color < 27; ++color) {
+        k_adj_tstle4<<<bg, 256, 0, c->stream>>>(c->d_grids, sp, c->F("U"), c->F("V"), c->F("W"),
+                                                c->F("G"), c->F("UO"), c->F("VO"), c->F("WO"), LU, LV,
+                                                LW, LP, c->F("GFX"), c->F("GFY"), c->F("GFZ"),
+                                                c->prm.gmol, c->prm.rho, color);
+        MG_LAUNCHED(c);
+    }
     return 0;
 }
 

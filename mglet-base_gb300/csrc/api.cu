@@ -782,7 +782,11 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     release_tables(c);
     for (auto& kv : c->f3) cudaFree(kv.second);
     for (auto& kv : c->f1) cudaFree(kv.second);
-    for (auto& kv : c->plans) cudaFree(kv.second.d_tasks);
+    for (auto& kv : c->plans) {
+        cudaFree(kv.second.d_tasks);
+        cudaFree(kv.second.d_bysrc);
+        cudaFree(kv.second.d_srcstart);
+    }
     for (HpTable& t : c->hp) { cudaFree(t.d_mip); cudaFree(t.d_idx); }
     cudaFree(c->d_grids);
     for (double* b : c->d_buf) cudaFree(b);

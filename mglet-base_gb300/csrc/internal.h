@@ -84,6 +84,12 @@ struct ConnectPlan {
     BoxCopy* d_tasks = nullptr;
     int ntasks = 0;
     long long npts = 0;
+    // the same tasks grouped by the grid they read (the adjoint's transposed
+    // copies add into the sources: one group per CTA, in a fixed order),
+    // built on first use; group s is d_bysrc[d_srcstart[s] .. d_srcstart[s+1])
+    BoxCopy* d_bysrc = nullptr;
+    int* d_srcstart = nullptr;
+    int nsrc = 0;
 };
 
 // Hyperplane traversal table of one grid shape (sip_hyperplane_mod.F90:269-334):

@@ -9,6 +9,7 @@
   that the linearised convection, diffusion, pressure solve and projection
   all carry weight.  The pressure solve runs a fixed number of outer
   iterations, so that J is a smooth function of f.
+* Two runs give the same gradient bit for bit (no atomics).
 * The same gradient through a thin torch.autograd.Function, as a gradient
   check harness would use it.
 """
@@ -94,6 +95,27 @@ def test_energy_gradient_matches_finite_differences(gpu_lib, oracle_lib, nsteps,
               - _oracle_energy(oracle_lib, case, prm, fields, fm, nsteps, dt)) / (2 * h)
         ad = sum(float(np.dot(g, b)) for g, b in zip(grad, d))
         assert abs(ad - fd) <= 1e-6 * abs(fd), (ad, fd)
+
+
+def test_energy_gradient_is_reproducible(gpu_lib, oracle_lib):
+    """The adjoint adds its scattered derivatives without atomics (the flux
+    transpose in 27 colour classes, the connect transpose grouped by source
+    grid), so two runs from the same state give the same gradient bit for
+    bit, on a tiling where every grid both sends and receives copies."""
+    case = cases.periodic_box(2, 2, 1, n=8, length=(2.0, 2.0, 1.0))
+    prm = _prm()
+    fields, f = _fields(case), _force(case)
+    out = []
+    for _ in range(2):
+        gs = gpu_lib.Solver(case, prm)
+        _load(gs, fields, f)
+        J, grad = gs.energy_gradient(3, 1, 2e-2, oracle_lib.rk_scheme("williamson"))
+        out.append((J, [g.copy() for g in grad], gs.get("LU")))
+        gs.close()
+    assert out[0][0] == out[1][0]
+    for a, b in zip(out[0][1], out[1][1]):
+        assert np.array_equal(a, b)
+    assert np.array_equal(out[0][2], out[1][2])
 
 
 def test_adjoint_stage_refuses_walls(gpu_lib, oracle_lib):
