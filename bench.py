@@ -871,6 +871,13 @@ def run_sphere(args, rank, local):
                      "itinfo": {"cflmax": info.cflmax, "divmax": info.divmax, "energy": info.energy},
                      "tuning": s.tuning() if form == "mixed" else ""}
         fields[form] = {nm: case.interior(s.get(nm)) for nm in "UVWP"}
+        if form == "mixed" and not args.no_profile:
+            # per-kernel times of one more step, issued eagerly with events
+            s.profile(True)
+            step()
+            s.synchronize()
+            res[form]["kernels_ms"] = {n: s.profile_get(n)[0] for n in s.profile_names()}
+            s.profile(False)
         s.close()
     check = None
     if args.sphere_check:
@@ -909,6 +916,7 @@ def run_sphere(args, rank, local):
                    "l2": "working set > L2 (no flush needed)"},
         "clocks": main["clocks"], "gpu_launches": main["launches"], "itinfo": main["itinfo"],
         "tuning": res["mixed"]["tuning"],
+        "kernels_ms_mixed_step": res["mixed"].get("kernels_ms"),
         other + "_form": {k: side[k] for k in ("value", "ms_per_step", "launches", "itinfo")},
         "mixed_vs_plain": {"steps": args.warmup + args.steps,
                            **field_diff(fields["mixed"], fields["plain"])},
