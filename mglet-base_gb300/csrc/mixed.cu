@@ -678,12 +678,55 @@ int mixed_ghostcell(Ctx* c) {
             }
             if (v != 1.0) own[g] = 1;
         }
+        // the points the lists write (ghost-cell values: comps 1-3; the flux
+        // correction: a cell and its lower neighbours); a neighbour whose
+        // ghost layer copies one of them sees point values PWU.. that differ
+        // from U..: it too takes the FP64 fluxes
         const GcHostList& L = c->gch[g];
-        if (L.n[0] + L.n[1] + L.n[2] + L.n[3] > 0) {
-            ib[g] = 1;
+        if (L.n[0] + L.n[1] + L.n[2] + L.n[3] == 0) continue;
+        ib[g] = 1;
+        const long long kj = (long long)G.kk * G.jj;
+        unsigned sides_seen[64] = {0};
+        auto touch = [&](long long idx1) {   // 1-based position in the grid
+            const long long c0 = idx1 - 1;
+            const int k = (int)(c0 % G.kk) + 1, j = (int)((c0 / G.kk) % G.jj) + 1;
+            const int i = (int)(c0 / kj) + 1;
+            unsigned sd = 0;
+            if (i == 3) sd |= 1u << 1;
+            if (i == G.ii - 2) sd |= 1u << 2;
+            if (j == 3) sd |= 1u << 3;
+            if (j == G.jj - 2) sd |= 1u << 4;
+            if (k == 3) sd |= 1u << 5;
+            if (k == G.kk - 2) sd |= 1u << 6;
+            sides_seen[sd >> 1] = 1;
+        };
+        for (int q = 0; q < 3; ++q) {
+            const std::vector<long long>& xi = L.xi[q];
+            size_t pi = 0;
+            for (int cell = 0; cell < L.n[q] && pi + 1 < xi.size(); ++cell) {
+                touch(xi[pi]);
+                pi += 2 + (size_t)xi[pi + 1];
+            }
+        }
+        {
+            const std::vector<long long>& xi = L.xi[3];
+            for (int cell = 0; cell < L.n[3] && 2 * (size_t)cell + 1 < xi.size(); ++cell) {
+                const long long c1 = xi[2 * (size_t)cell + 1];
+                touch(c1);
+                touch(c1 - kj);
+                touch(c1 - G.kk);
+                touch(c1 - 1);
+            }
+        }
+        for (unsigned sd = 1; sd < 64; ++sd) {
+            if (!sides_seen[sd]) continue;
+            const unsigned mask = sd << 1;
             for (int sl = 1; sl <= 26; ++sl) {
+                const int* fc = slot_faces(sl);
+                bool all = true;
+                for (int q = 1; q <= fc[0]; ++q) all &= ((mask >> fc[q]) & 1u) != 0;
                 const int nb = c->nbr[g + 1][sl];
-                if (nb > 0) ib[nb - 1] = 1;
+                if (all && nb > 0) ib[nb - 1] = 1;
             }
         }
     }
