@@ -78,13 +78,7 @@ const int kRescueNbr[27][7] = {
 
 bool coupled(int t) { return t == MGLET_BC_CON || t == MGLET_BC_CO1; }
 
-}  // namespace
 
-// {count, faces...} of neighbour slot s (1..26): the faces the direction
-// crosses (1 -x, 2 +x, 3 -y, 4 +y, 5 -z, 6 +z)
-const int* slot_faces(int s) { return kFaces[s]; }
-
-namespace {
 
 struct Box {
     int lo[3], hi[3];   // k, j, i ranges (1-based, inclusive)

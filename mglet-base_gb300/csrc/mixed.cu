@@ -315,18 +315,21 @@ int enqueue_stage(Ctx* c) {
     }
     const bool skip = m->skip_once;
     m->skip_once = false;
+    // ghost-cell IB: which grids' point values differ from U, V, W now (the
+    // fused flux kernel leaves those to the FP64 tstle4 below)
+    if (c->ibtype == 1)
+        if (int rc = mx_pw_flags(c, m->lv)) return rc;
     if (int rc = launch_mx_flux(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, m->d_sprm,
                                 m->d_ctl + 2, skip))
         return rc;
     double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P");
     const bool gc = c->ibtype == 1;
     if (gc) {
-        // grids next to the immersed boundary: tstle4 of the transported
-        // point values PWU, PWV, PWW by the transporting U, V, W
+        // grids whose point values differ from U, V, W: tstle4 of the
+        // transported PWU, PWV, PWW by the transporting U, V, W
         // (timeintegration_mod.F90:100-101), in FP64
-        const LevelState& lv = m->lv;
-        if (int rc = launch_tstle4_grids(c, lv.d_ib, (int)lv.ib.size(), c->F("UO"), c->F("VO"), c->F("WO"),
-                                         c->F("PWU"), c->F("PWV"), c->F("PWW"), U, V, W, P, c->F("G")))
+        if (int rc = launch_tstle4_grids(c, m->lv.d_skip, c->F("UO"), c->F("VO"), c->F("WO"), c->F("PWU"),
+                                         c->F("PWV"), c->F("PWW"), U, V, W, P, c->F("G")))
             return rc;
     }
     if (c->minlevel != c->maxlevel)
@@ -654,9 +657,10 @@ static int levels_ready(Ctx* c) {
 //  * BP must be 0 or 1 (the couplings laplacephi's bp products close become
 //    per-point masks); grids where it is not 1 everywhere get classes of their
 //    own, whose Laplacian records carry the masks;
-//  * grids with ghost-cell lists and their neighbours on the same level
-//    (whose ghost layers hold the lists' point values) take the FP64 tstle4
-//    of PWU, PWV, PWW by U, V, W and the separate RK update.
+//  * at every stage the grids whose point values PWU, PWV, PWW differ from
+//    U, V, W anywhere the flux kernel reads (those with lists, and the
+//    neighbours and parents whose copies of them differ) take the FP64
+//    tstle4 of the point values by U, V, W and the separate RK update.
 int mixed_ghostcell(Ctx* c) {
     MixedState* m = c->mx;
     SipState& st = m->sip;
@@ -666,7 +670,7 @@ int mixed_ghostcell(Ctx* c) {
     }
     std::vector<double> bp((size_t)c->idim3d);
     MG_CUDA(copy_on(c->stream, bp.data(), c->F("BP"), bp.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    std::vector<unsigned char> own(c->ngrid, 0), ib(c->ngrid, 0);
+    std::vector<unsigned char> own(c->ngrid, 0);
     for (int g = 0; g < c->ngrid; ++g) {
         const DevGrid& G = c->grids[g];
         const long long n = (long long)G.kk * G.jj * G.ii;
@@ -677,57 +681,6 @@ int mixed_ghostcell(Ctx* c) {
                 return MGLET_ERR_UNSUPPORTED;
             }
             if (v != 1.0) own[g] = 1;
-        }
-        // the points the lists write (ghost-cell values: comps 1-3; the flux
-        // correction: a cell and its lower neighbours); a neighbour whose
-        // ghost layer copies one of them sees point values PWU.. that differ
-        // from U..: it too takes the FP64 fluxes
-        const GcHostList& L = c->gch[g];
-        if (L.n[0] + L.n[1] + L.n[2] + L.n[3] == 0) continue;
-        ib[g] = 1;
-        const long long kj = (long long)G.kk * G.jj;
-        unsigned sides_seen[64] = {0};
-        auto touch = [&](long long idx1) {   // 1-based position in the grid
-            const long long c0 = idx1 - 1;
-            const int k = (int)(c0 % G.kk) + 1, j = (int)((c0 / G.kk) % G.jj) + 1;
-            const int i = (int)(c0 / kj) + 1;
-            unsigned sd = 0;
-            if (i == 3) sd |= 1u << 1;
-            if (i == G.ii - 2) sd |= 1u << 2;
-            if (j == 3) sd |= 1u << 3;
-            if (j == G.jj - 2) sd |= 1u << 4;
-            if (k == 3) sd |= 1u << 5;
-            if (k == G.kk - 2) sd |= 1u << 6;
-            sides_seen[sd >> 1] = 1;
-        };
-        for (int q = 0; q < 3; ++q) {
-            const std::vector<long long>& xi = L.xi[q];
-            size_t pi = 0;
-            for (int cell = 0; cell < L.n[q] && pi + 1 < xi.size(); ++cell) {
-                touch(xi[pi]);
-                pi += 2 + (size_t)xi[pi + 1];
-            }
-        }
-        {
-            const std::vector<long long>& xi = L.xi[3];
-            for (int cell = 0; cell < L.n[3] && 2 * (size_t)cell + 1 < xi.size(); ++cell) {
-                const long long c1 = xi[2 * (size_t)cell + 1];
-                touch(c1);
-                touch(c1 - kj);
-                touch(c1 - G.kk);
-                touch(c1 - 1);
-            }
-        }
-        for (unsigned sd = 1; sd < 64; ++sd) {
-            if (!sides_seen[sd]) continue;
-            const unsigned mask = sd << 1;
-            for (int sl = 1; sl <= 26; ++sl) {
-                const int* fc = slot_faces(sl);
-                bool all = true;
-                for (int q = 1; q <= fc[0]; ++q) all &= ((mask >> fc[q]) & 1u) != 0;
-                const int nb = c->nbr[g + 1][sl];
-                if (all && nb > 0) ib[nb - 1] = 1;
-            }
         }
     }
     // classes with the BP masks
@@ -746,9 +699,9 @@ int mixed_ghostcell(Ctx* c) {
     // a uniform-coefficient pre-pass no longer applies: the same launch shape
     // with per-point records
     if (!st.unicls && sip_pre_variant_uniform(st.pre_variant)) st.pre_variant -= 5;
-    // the grids next to the body
+    // per-stage flags of the grids whose point values differ from U, V, W
     mx_level_release(m->lv);
-    m->lv.ibflag = ib;
+    m->lv.ibflag.assign(c->ngrid, 1);
     if (int rc = mx_level_prepare(c, st, m->lv)) return rc;
     mx_flux_set_skip(c, m->lv.d_skip);
     if (m->graph) {

@@ -254,6 +254,31 @@ __global__ void k_mx_ftoc(const DevGrid* __restrict__ grids, const int4* __restr
         return LO ? (double)H[o] + (double)LO[o] : (double)H[o];
     };
     double val;
+    if (!LO) {
+        // the FP32 correction: its mean in FP32 (the FP64 units of this part
+        // issue at a small fraction of the FP32 rate)
+        auto Ff = [&](int kx, int jx, int ix) -> float { return H[base + m.pos(ix - 3, jx - 3, kx - 3)]; };
+        const float zx[2] = {(float)ddx[i], (float)ddx[i + 1]}, zy[2] = {(float)ddy[j], (float)ddy[j + 1]};
+        const float zz[2] = {(float)ddz[k], (float)ddz[k + 1]};
+        const double* bp = BP ? BP + G.ip3 : nullptr;
+        const int kk = G.kk, jj = G.jj;
+        float spv = 0.f, sv = 0.f;
+        for (int l = 0; l < 2; ++l)
+            for (int mq = 0; mq < 2; ++mq)
+                for (int n = 0; n < 2; ++n) {
+                    float vol = zz[l] * zy[mq] * zx[n];
+                    if (bp)
+                        vol *= (float)bp[(long long)(i + n - 1) * kk * jj + (long long)(j + mq - 1) * kk + (k + l - 1)];
+                    spv += Ff(k + l, j + mq, i + n) * vol;
+                    sv += vol;
+                }
+        const float hv = sv > 0.f ? spv / sv : 0.f;
+        const int4 h = hier[g];
+        const int ioc = h.y + (i - 3) / 2 - 3, joc = h.z + (j - 3) / 2 - 3, koc = h.w + (k - 3) / 2 - 3;
+        if (ioc < 0 || ioc >= m.ni || joc < 0 || joc >= m.nj || koc < 0 || koc >= m.nk) return;
+        H[(long long)h.x * m.npp + m.pos(ioc, joc, koc)] = hv;
+        return;
+    }
     if (!BP) {
         const double s = F(k, j, i) * ddz[k] * ddy[j] * ddx[i] + F(k, j, i + 1) * ddz[k] * ddy[j] * ddx[i + 1] +
                          F(k, j + 1, i) * ddz[k] * ddy[j + 1] * ddx[i] +
@@ -292,34 +317,56 @@ __global__ void k_mx_ftoc(const DevGrid* __restrict__ grids, const int4* __restr
     if (LO) LO[o] = (float)(val - (double)hv);
 }
 
-// max |rhs| per grid of the float-float residual (maxabscal_grid after the
-// restriction of the residual into the coarse grids)
-__global__ void k_mx_gridmax(int npp, const float* __restrict__ H, const float* __restrict__ LO,
-                             double* gridmax, const int* ctl) {
+// max |rhs| per grid (maxabscal_grid after the restriction of the residual
+// into the coarse grids), of its leading float as the outer step forms it
+__global__ void k_mx_gridmax(int npp, const float* __restrict__ H, double* gridmax, const int* ctl) {
     if (ctl[0]) return;
-    __shared__ double sh[32];
+    __shared__ float sh[32];
     const long long base = (long long)blockIdx.x * npp;
-    double v = 0.0;
-    for (int q = threadIdx.x; q < npp; q += blockDim.x)
-        v = fmax(fabs((double)H[base + q] + (double)LO[base + q]), v);
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+    float v = 0.f;
+    for (int q = threadIdx.x; q < npp; q += blockDim.x) v = fmaxf(fabsf(H[base + q]), v);
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
     __syncthreads();
     if (threadIdx.x < 32) {
-        v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-        if (threadIdx.x == 0) gridmax[blockIdx.x] = v;
+        v = threadIdx.x < (blockDim.x >> 5) ? sh[threadIdx.x] : 0.f;
+        for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (threadIdx.x == 0) gridmax[blockIdx.x] = (double)v;
     }
 }
 
-// rkstep (rungekutta_mod.F90:315-333) over the whole box of the grids with
-// a PAR face, in the mixed form's arithmetic (FP32 register, FP64 field):
-// their fluxes were written to UO, VO, WO and corrected by tstle4_par; UO..
-// are cleared for the next stage, as tstle4 starts from zero fluxes.
-__global__ void k_mx_rk_par(const DevGrid* __restrict__ grids, const int* __restrict__ list,
+// Per grid: do the transported point values PWU, PWV, PWW differ from U, V,
+// W anywhere on the box 2..n-1 the flux kernel reads (ghost-cell IB)?  Such
+// grids take the FP64 tstle4 of the point values and the separate RK update.
+__global__ void k_mx_pwflag(const DevGrid* __restrict__ grids, const double* __restrict__ U,
+                            const double* __restrict__ V, const double* __restrict__ W,
+                            const double* __restrict__ PU, const double* __restrict__ PV,
+                            const double* __restrict__ PW, unsigned char* flag) {
+    const DevGrid G = grids[blockIdx.x];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const int nk = kk - 2, nj = jj - 2, ni = ii - 2;
+    int d = 0;
+    for (int t = threadIdx.x; t < nk * nj * ni; t += blockDim.x) {
+        const int k = t % nk + 2, j = (t / nk) % nj + 2, i = t / (nk * nj) + 2;
+        const long long c = G.ip3 + (long long)(i - 1) * kk * jj + (long long)(j - 1) * kk + (k - 1);
+        d |= (U[c] != PU[c]) | (V[c] != PV[c]) | (W[c] != PW[c]);
+    }
+    d = __syncthreads_or(d);
+    if (threadIdx.x == 0) flag[blockIdx.x] = d ? 1 : 0;
+}
+
+// rkstep (rungekutta_mod.F90:315-333) over the whole box of the grids whose
+// fluxes came from UO, VO, WO -- a PAR face (tstle4_par corrected them) or a
+// flag in sel (FP64 fluxes of the point values) -- in the mixed form's
+// arithmetic (FP32 register, FP64 field); UO.. are cleared for the next
+// stage, as tstle4 starts from zero fluxes.
+__global__ void k_mx_rk_par(const DevGrid* __restrict__ grids, const unsigned char* __restrict__ sel,
                             double* U, double* V, double* W, float* DU, float* DV, float* DW,
                             double* UO, double* VO, double* WO, const double* __restrict__ sprm) {
-    const DevGrid G = grids[list[blockIdx.y]];
+    const DevGrid G = grids[blockIdx.y];
+    bool par = false;
+    for (int f = 0; f < 6; ++f) par |= G.bc[f] == MGLET_BC_PAR;
+    if (!par && !(sel && sel[blockIdx.y])) return;
     const long long n = (long long)G.kk * G.jj * G.ii;
     const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
@@ -362,7 +409,6 @@ int mx_level_prepare(Ctx* c, SipState& st, LevelState& lv) {
         lv.grids[l].push_back(g);
         bool par = false;
         for (int f = 0; f < 6; ++f) par |= G.bc[f] == MGLET_BC_PAR;
-        const bool ib = !lv.ibflag.empty() && lv.ibflag[g];
         if (par) {
             lv.pars[l].push_back(g);
             anypar = true;
@@ -371,8 +417,7 @@ int mx_level_prepare(Ctx* c, SipState& st, LevelState& lv) {
                 return MGLET_ERR_ARG;
             }
         }
-        if (par || ib) lv.parall.push_back(g);
-        if (ib) lv.ib.push_back(g);
+        if (par) lv.parall.push_back(g);
         if (l > 0 && (c->hier.empty() || c->hier[g].x < 0)) {
             set_error("mixed form: a fine grid without parent (mglet_gpu_set_hierarchy first)");
             return MGLET_ERR_ARG;
@@ -383,10 +428,10 @@ int mx_level_prepare(Ctx* c, SipState& st, LevelState& lv) {
         if (int rc = upload(c, lv.pars[l], &lv.d_pars[l])) return rc;
     }
     if (int rc = upload(c, lv.parall, &lv.d_parall)) return rc;
-    if (int rc = upload(c, lv.ib, &lv.d_ib)) return rc;
-    if (!lv.ib.empty()) {
+    if (!lv.ibflag.empty()) {
+        // ghost-cell IB: per-grid flags, set at every stage by k_mx_pwflag
         MG_CUDA(cudaMalloc(&lv.d_skip, (size_t)c->ngrid));
-        MG_CUDA(copy_on(c->stream, lv.d_skip, lv.ibflag.data(), (size_t)c->ngrid, cudaMemcpyHostToDevice));
+        MG_CUDA(zero_on(c->stream, lv.d_skip, (size_t)c->ngrid));
     }
     if (anypar && !st.pg) {
         const size_t n = (size_t)c->ngrid * 6 * st.fs * sizeof(float);
@@ -414,7 +459,6 @@ void mx_level_release(LevelState& lv) {
     for (int* p : lv.d_grids) cudaFree(p);
     for (int* p : lv.d_pars) cudaFree(p);
     cudaFree(lv.d_parall);
-    cudaFree(lv.d_ib);
     cudaFree(lv.d_skip);
     lv = LevelState();
 }
@@ -470,22 +514,28 @@ int mx_ftoc(Ctx* c, SipState& st, const LevelState& lv, int ilevel, bool rhs, co
 
 int mx_gridmax(Ctx* c, SipState& st, const int* ctl) {
     ProfScope ps_(c, "mx_gridmax");
-    k_mx_gridmax<<<c->ngrid, 256, 0, c->stream>>>(st.npp, st.rhs32, st.rhsl, c->d_gridred, ctl);
+    k_mx_gridmax<<<c->ngrid, 256, 0, c->stream>>>(st.npp, st.rhs32, c->d_gridred, ctl);
     MG_LAUNCHED(c);
     return 0;
 }
 
 int mx_rk_par(Ctx* c, const LevelState& lv, float* du, float* dv, float* dw, const double* sprm) {
-    if (lv.parall.empty()) return 0;
+    if (lv.parall.empty() && !lv.d_skip) return 0;
     ProfScope ps_(c, "mx_rk_par");
     long long npts = 0;
-    for (int g : lv.parall) {
-        const DevGrid& G = c->grids[g];
-        npts = std::max(npts, (long long)G.kk * G.jj * G.ii);
-    }
-    const dim3 grid((unsigned)((npts + 255) / 256), (unsigned)lv.parall.size());
-    k_mx_rk_par<<<grid, 256, 0, c->stream>>>(c->d_grids, lv.d_parall, c->F("U"), c->F("V"), c->F("W"),
+    for (const DevGrid& G : c->grids) npts = std::max(npts, (long long)G.kk * G.jj * G.ii);
+    const dim3 grid((unsigned)((npts + 255) / 256), (unsigned)c->ngrid);
+    k_mx_rk_par<<<grid, 256, 0, c->stream>>>(c->d_grids, lv.d_skip, c->F("U"), c->F("V"), c->F("W"),
                                              du, dv, dw, c->F("UO"), c->F("VO"), c->F("WO"), sprm);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int mx_pw_flags(Ctx* c, const LevelState& lv) {
+    if (!lv.d_skip) return 0;
+    ProfScope ps_(c, "mx_pwflag");
+    k_mx_pwflag<<<c->ngrid, 256, 0, c->stream>>>(c->d_grids, c->F("U"), c->F("V"), c->F("W"), c->F("PWU"),
+                                                  c->F("PWV"), c->F("PWW"), lv.d_skip);
     MG_LAUNCHED(c);
     return 0;
 }

@@ -8,11 +8,11 @@
 namespace mg {
 
 // Per level (index ilevel - minlevel): its grids and those with a PAR face,
-// host and device lists; every grid whose fluxes and RK update run apart
-// from the fused flux kernel (a PAR face, or next to an immersed boundary);
-// the grids next to an immersed boundary (ibflag, set before the set-up:
-// their transported velocities PWU, PWV, PWW differ from U, V, W) as a list
-// and as per-grid skip flags of the flux kernel.
+// host and device lists; every grid with a PAR face.  With the ghost-cell IB
+// (ibflag set before the set-up: the grids with lists) d_skip holds per grid,
+// at every stage, whether its transported point values PWU, PWV, PWW differ
+// from U, V, W: those grids take the FP64 tstle4 and the separate RK update,
+// and the fused flux kernel skips them.
 struct LevelState {
     bool ready = false;
     std::vector<std::vector<int>> grids, pars;
@@ -20,8 +20,6 @@ struct LevelState {
     std::vector<int> parall;
     int* d_parall = nullptr;
     std::vector<unsigned char> ibflag;
-    std::vector<int> ib;
-    int* d_ib = nullptr;
     unsigned char* d_skip = nullptr;
 };
 
@@ -38,7 +36,9 @@ int mx_bound_pressure(Ctx* c, SipState& st, const LevelState& lv, int ilevel, co
 int mx_ftoc(Ctx* c, SipState& st, const LevelState& lv, int ilevel, bool rhs, const int* ctl);
 // per-grid max |rhs| into the context's grid reduction array
 int mx_gridmax(Ctx* c, SipState& st, const int* ctl);
-// the RK update of the grids with a PAR face from UO, VO, WO
+// the RK update from UO, VO, WO of the grids with a PAR face or a d_skip flag
 int mx_rk_par(Ctx* c, const LevelState& lv, float* du, float* dv, float* dw, const double* sprm);
+// ghost-cell IB: d_skip = the grids whose PWU, PWV, PWW differ from U, V, W
+int mx_pw_flags(Ctx* c, const LevelState& lv);
 
 }  // namespace mg
