@@ -366,11 +366,11 @@ int mglet_gpu_set_stencils(mglet_ctx* ctx, int32_t igrid, int32_t comp, int32_t 
  * and every grid's lists are set: Poisson coefficients and SIP factors are
  * rebuilt with the blocked cells (giteig, src/ib/noib_mod.F90:81-250), the
  * lists go to the device and SDIV is built (setsdivfield,
- * gc_flowstencils_mod.F90:1488-1535).  In the mixed form the grids whose
- * point values PWU, PWV, PWW differ from U, V, W take FP64 fluxes of the
- * point values (found at every stage) and grids with blocked cells their
- * own SIP classes with the blocked couplings masked; BP must be 0 or 1
- * there (else MGLET_ERR_UNSUPPORTED). */
+ * gc_flowstencils_mod.F90:1488-1535).  In the mixed form the flux kernel
+ * transports the point values PWU, PWV, PWW on the grids where they differ
+ * from U, V, W (found at every stage), and grids with blocked cells get
+ * SIP classes of their own with the blocked couplings masked; BP must be 0
+ * or 1 there (else MGLET_ERR_UNSUPPORTED). */
 int mglet_gpu_set_ghostcell(mglet_ctx* ctx);
 /* ---- Ghost-cell stencil construction (host only, no device needed) -------
  * Replaces create_flowstencils (src/flow/gc_flowstencils_mod.F90:37-100):

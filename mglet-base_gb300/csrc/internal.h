@@ -267,9 +267,6 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
                   const double* p, const double* g);
 int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu);
 int launch_g_uniform(Ctx* c);   // d_guni: per grid, is G one value on the box 2..n-1
-int launch_tstle4_grids(Ctx* c, const unsigned char* only, double* uo, double* vo, double* wo,
-                        const double* u, const double* v, const double* w, const double* ut,
-                        const double* vt, const double* wt, const double* p, const double* g);
 int launch_divcal(Ctx* c, double* div, const double* u, const double* v, const double* w,
                   double fak);
 int launch_bp_ones(Ctx* c);

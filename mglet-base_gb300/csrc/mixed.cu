@@ -36,7 +36,7 @@ namespace mg {
 int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
                    const float* sz, const double* sprm, int* err, bool skip);
 bool mx_flux_has_tma(Ctx* c);
-void mx_flux_set_skip(Ctx* c, const unsigned char* d_skip);
+int mx_flux_set_pw(Ctx* c, const unsigned char* d_pw);
 int mx_flux_prepare(Ctx* c);
 void mx_flux_release(Ctx* c);
 int mx_flux_tune(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
@@ -316,7 +316,8 @@ int enqueue_stage(Ctx* c) {
     const bool skip = m->skip_once;
     m->skip_once = false;
     // ghost-cell IB: which grids' point values differ from U, V, W now (the
-    // fused flux kernel leaves those to the FP64 tstle4 below)
+    // flux kernel transports their point values PWU, PWV, PWW by U, V, W,
+    // timeintegration_mod.F90:100-101)
     if (c->ibtype == 1)
         if (int rc = mx_pw_flags(c, m->lv)) return rc;
     if (int rc = launch_mx_flux(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, m->d_sprm,
@@ -324,21 +325,13 @@ int enqueue_stage(Ctx* c) {
         return rc;
     double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P");
     const bool gc = c->ibtype == 1;
-    if (gc) {
-        // grids whose point values differ from U, V, W: tstle4 of the
-        // transported PWU, PWV, PWW by the transporting U, V, W
-        // (timeintegration_mod.F90:100-101), in FP64
-        if (int rc = launch_tstle4_grids(c, m->lv.d_skip, c->F("UO"), c->F("VO"), c->F("WO"), c->F("PWU"),
-                                         c->F("PWV"), c->F("PWW"), U, V, W, P, c->F("G")))
-            return rc;
-    }
     if (c->minlevel != c->maxlevel)
         // grids with a PAR face: tstle4_par (tstle4_mod.F90:114) on the fluxes
         // left in UO, VO, WO
         if (int rc = launch_tstle4_par(c, c->F("UO"), c->F("VO"), c->F("WO"), gc ? c->F("PWU") : U,
                                        gc ? c->F("PWV") : V, gc ? c->F("PWW") : W, U, V, W))
             return rc;
-    // the RK update of the grids whose fluxes came from UO, VO, WO
+    // the RK update of the grids with a PAR face (their fluxes in UO, VO, WO)
     if (int rc = mx_rk_par(c, m->lv, m->du32, m->dv32, m->dw32, m->d_sprm)) return rc;
     if (gc) {   // timeintegration_mod.F90:110-116: maskbp, getibvalues
         if (int rc = launch_maskbp(c, U, V, W, P)) return rc;
@@ -659,8 +652,8 @@ static int levels_ready(Ctx* c) {
 //    own, whose Laplacian records carry the masks;
 //  * at every stage the grids whose point values PWU, PWV, PWW differ from
 //    U, V, W anywhere the flux kernel reads (those with lists, and the
-//    neighbours and parents whose copies of them differ) take the FP64
-//    tstle4 of the point values by U, V, W and the separate RK update.
+//    neighbours and parents whose copies of them differ) are flagged, and
+//    the flux kernel transports their point values by U, V, W.
 int mixed_ghostcell(Ctx* c) {
     MixedState* m = c->mx;
     SipState& st = m->sip;
@@ -703,7 +696,7 @@ int mixed_ghostcell(Ctx* c) {
     mx_level_release(m->lv);
     m->lv.ibflag.assign(c->ngrid, 1);
     if (int rc = mx_level_prepare(c, st, m->lv)) return rc;
-    mx_flux_set_skip(c, m->lv.d_skip);
+    if (int rc = mx_flux_set_pw(c, m->lv.d_skip)) return rc;
     if (m->graph) {
         cudaGraphExecDestroy(m->graph);
         m->graph = nullptr;

@@ -90,9 +90,12 @@ struct FluxArgs {
     // the RK update follow in separate kernels)
     double *UO, *VO, *WO;
     double wrho, wgmol, cpo4, cpo5, cpo6, cpo8;
-    // per grid: 1 where another kernel computes the fluxes (grids next to an
-    // immersed boundary, whose transported velocities are PWU, PWV, PWW)
-    const unsigned char* skip;
+    // ghost-cell IB: per grid 1 where the transported velocities are the
+    // point values PWU, PWV, PWW (PU0, PV0, PW0), loaded into windows of
+    // their own (pw: the launch has those windows)
+    const unsigned char* pwflag;
+    const double *PU0, *PV0, *PW0;
+    int pw;
     // per grid {1, h2} where G is one value on the box 2..n-1: the uniform
     // face viscosities hold there too
     const double* guni;
@@ -139,12 +142,16 @@ struct Visc3 {
 // (i+1)%3; p: slots i%2, (i+1)%2)
 // kW: the face viscosities come from vs (grids with boundary faces); else
 // every face has the uniform a.g / a.gh.  gfl is the grid's gradpflag.
-template <bool kW>
+// kPW: the transported velocities are the point values in the windows xu,
+// xv, xw (ghost-cell IB), the transporting ones U, V, W in su, sv, sw; else
+// both are su, sv, sw and xu.. are not read.
+template <bool kW, bool kPW = false>
 __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, long long nx,
                                            const Col& cl, const float2* su, const float2* sv,
                                            const float2* sw, const float2* sp, int plane, int pk,
                                            int q, int i, float gfl, const Visc3& vs, float& uo,
-                                           float& vo, float& wo) {
+                                           float& vo, float& wo, const float2* xu = nullptr,
+                                           const float2* xv = nullptr, const float2* xw = nullptr) {
     const float g = a.g, gh = a.gh;
     const float dy_j = cl.dy_j, ddy_j = cl.ddy_j, rdy_j = cl.rdy_j, rdy_jm = cl.rdy_jm;
     const float rddy_j = cl.rddy_j, rddy_jp = cl.rddy_jp, ry1 = cl.ry1, ry0 = cl.ry0;
@@ -169,19 +176,30 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
         const float fdy_j = dy_j, fddy = ddy_j, fdz_k = dz_k, fddz = ddz_k;
         // ---------------- U at (k, j, i+1/2)
         {
-            const float2 c = u_0[q];
+            // transporting U along x (mass fluxes fe, fw), transported u
+            const float2 ct = u_0[q];
+            const float tE = dif(u_p[q], ct), tW = dif(u_m[q], ct);
+            float2 c = ct;
+            float dE = tE, dW = tW, dN, dS, dT, dB;
+            if constexpr (kPW) {
+                const float2 *x_m = xu + sm1 * plane, *x_0 = xu + s0 * plane, *x_p = xu + sp1 * plane;
+                c = x_0[q];
+                dE = dif(x_p[q], c); dW = dif(x_m[q], c);
+                dN = dif(x_0[qn], c); dS = dif(x_0[qs], c);
+                dT = dif(x_0[qt], c); dB = dif(x_0[qb], c);
+            } else {
+                dN = dif(u_0[qn], c); dS = dif(u_0[qs], c);
+                dT = dif(u_0[qt], c); dB = dif(u_0[qb], c);
+            }
             const float cf = val(c);
-            const float dE = dif(u_p[q], c), dW = dif(u_m[q], c);
-            const float dN = dif(u_0[qn], c), dS = dif(u_0[qs], c);
-            const float dT = dif(u_0[qt], c), dB = dif(u_0[qb], c);
             const float ax = fddy * fddz, ay = fdx_i * fddz, az = fdx_i * fddy;
-            const float fe = ax * (cf + 0.5f * dE * rx1);
-            const float fw = ax * (val(u_m[q]) - 0.5f * dW * rx0);
+            const float fe = ax * (val(ct) + 0.5f * tE * rx1);
+            const float fw = ax * (val(u_m[q]) - 0.5f * tW * rx0);
             const float fn = 0.5f * ay * (val(v_0[q]) + val(v_p[q]));
             const float fs = 0.5f * ay * (val(v_0[qs]) + val(v_p[qs]));
             const float ft = 0.5f * az * (val(w_0[q]) + val(w_p[q]));
             const float fb = 0.5f * az * (val(w_0[qb]) + val(w_p[qb]));
-            const float divf = ax * (-dW + 0.5f * dE * rx1 + 0.5f * dW * rx0) +
+            const float divf = ax * (-tW + 0.5f * tE * rx1 + 0.5f * tW * rx0) +
                                0.5f * ay * (dif(v_0[q], v_0[qs]) + dif(v_p[q], v_p[qs])) +
                                0.5f * az * (dif(w_0[q], w_0[qb]) + dif(w_p[q], w_p[qb]));
             const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
@@ -200,20 +218,31 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
         }
         // ---------------- V at (k, j+1/2, i)
         {
-            const float2 c = v_0[q];
+            // transporting V along y (mass fluxes fn, fs), transported v
+            const float2 ct = v_0[q];
+            const float tN = dif(v_0[qn], ct), tS = dif(v_0[qs], ct);
+            float2 c = ct;
+            float dE, dW, dN = tN, dS = tS, dT, dB;
+            if constexpr (kPW) {
+                const float2 *x_m = xv + sm1 * plane, *x_0 = xv + s0 * plane, *x_p = xv + sp1 * plane;
+                c = x_0[q];
+                dE = dif(x_p[q], c); dW = dif(x_m[q], c);
+                dN = dif(x_0[qn], c); dS = dif(x_0[qs], c);
+                dT = dif(x_0[qt], c); dB = dif(x_0[qb], c);
+            } else {
+                dE = dif(v_p[q], c); dW = dif(v_m[q], c);
+                dT = dif(v_0[qt], c); dB = dif(v_0[qb], c);
+            }
             const float cf = val(c);
-            const float dE = dif(v_p[q], c), dW = dif(v_m[q], c);
-            const float dN = dif(v_0[qn], c), dS = dif(v_0[qs], c);
-            const float dT = dif(v_0[qt], c), dB = dif(v_0[qb], c);
             const float ax = fdy_j * fddz, ay = fddx * fddz, az = fddx * fdy_j;
             const float fe = 0.5f * ax * (val(u_0[q]) + val(u_0[qn]));
             const float fw = 0.5f * ax * (val(u_m[q]) + val(u_m[qn]));
-            const float fn = ay * (cf + 0.5f * dN * ry1);
-            const float fs = ay * (val(v_0[qs]) - 0.5f * dS * ry0);
+            const float fn = ay * (val(ct) + 0.5f * tN * ry1);
+            const float fs = ay * (val(v_0[qs]) - 0.5f * tS * ry0);
             const float ft = 0.5f * az * (val(w_0[q]) + val(w_0[qn]));
             const float fb = 0.5f * az * (val(w_0[qb]) + val(w_0[qb + pk]));
             const float divf = 0.5f * ax * (dif(u_0[q], u_m[q]) + dif(u_0[qn], u_m[qn])) +
-                               ay * (-dS + 0.5f * dN * ry1 + 0.5f * dS * ry0) +
+                               ay * (-tS + 0.5f * tN * ry1 + 0.5f * tS * ry0) +
                                0.5f * az * (dif(w_0[q], w_0[qb]) + dif(w_0[qn], w_0[qb + pk]));
             const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
                                                   ft * dT - fb * dB);
@@ -231,21 +260,32 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
         }
         // ---------------- W at (k+1/2, j, i)
         {
-            const float2 c = w_0[q];
+            // transporting W along z (mass fluxes ft, fb), transported w
+            const float2 ct = w_0[q];
+            const float tT = dif(w_0[qt], ct), tB = dif(w_0[qb], ct);
+            float2 c = ct;
+            float dE, dW, dN, dS, dT = tT, dB = tB;
+            if constexpr (kPW) {
+                const float2 *x_m = xw + sm1 * plane, *x_0 = xw + s0 * plane, *x_p = xw + sp1 * plane;
+                c = x_0[q];
+                dE = dif(x_p[q], c); dW = dif(x_m[q], c);
+                dN = dif(x_0[qn], c); dS = dif(x_0[qs], c);
+                dT = dif(x_0[qt], c); dB = dif(x_0[qb], c);
+            } else {
+                dE = dif(w_p[q], c); dW = dif(w_m[q], c);
+                dN = dif(w_0[qn], c); dS = dif(w_0[qs], c);
+            }
             const float cf = val(c);
-            const float dE = dif(w_p[q], c), dW = dif(w_m[q], c);
-            const float dN = dif(w_0[qn], c), dS = dif(w_0[qs], c);
-            const float dT = dif(w_0[qt], c), dB = dif(w_0[qb], c);
             const float ax = fddy * fdz_k, ay = fddx * fdz_k, az = fddx * fddy;
             const float fe = 0.5f * ax * (val(u_0[q]) + val(u_0[qt]));
             const float fw = 0.5f * ax * (val(u_m[q]) + val(u_m[qt]));
             const float fn = 0.5f * ay * (val(v_0[q]) + val(v_0[qt]));
             const float fs = 0.5f * ay * (val(v_0[qs]) + val(v_0[qs + 1]));
-            const float ft = az * (cf + 0.5f * dT * rz1);
-            const float fb = az * (val(w_0[qb]) - 0.5f * dB * rz0);
+            const float ft = az * (val(ct) + 0.5f * tT * rz1);
+            const float fb = az * (val(w_0[qb]) - 0.5f * tB * rz0);
             const float divf = 0.5f * ax * (dif(u_0[q], u_m[q]) + dif(u_0[qt], u_m[qt])) +
                                0.5f * ay * (dif(v_0[q], v_0[qs]) + dif(v_0[qt], v_0[qs + 1])) +
-                               az * (-dB + 0.5f * dT * rz1 + 0.5f * dB * rz0);
+                               az * (-tB + 0.5f * tT * rz1 + 0.5f * tB * rz0);
             const float sig = cf * divf + 0.5f * (fe * dE - fw * dW + fn * dN - fs * dS +
                                                   ft * dT - fb * dB);
             const float vol = rddx_i * rddy_j * rdz_k;
@@ -382,7 +422,6 @@ __device__ void boundary_terms(const FluxArgs& a, const DevGrid& G, int k, int j
 template <bool kW>
 __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     extern __shared__ float2 sm[];
-    if (kW && a.skip && a.skip[blockIdx.x / a.nslab]) return;
     const DevGrid G = a.grids[blockIdx.x / a.nslab];
     const int slab = blockIdx.x % a.nslab;
     const int kk = G.kk, jj = G.jj, ii = G.ii;
@@ -395,6 +434,11 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     float2* sv = su + 3 * plane;
     float2* sw = sv + 3 * plane;
     float2* sp = sw + 3 * plane;      // [2][plane]
+    // point-value windows (ghost-cell IB), [3][plane] each, when the launch has them
+    float2* xu = sp + 2 * plane;
+    float2* xv = xu + 3 * plane;
+    float2* xw = xv + 3 * plane;
+    const bool pwg = kW && a.pw && a.pwflag && a.pwflag[blockIdx.x / a.nslab];
     const long long o = G.ip3;
     const int kj = kk * jj;
     const int nk = kk - 4;
@@ -437,6 +481,11 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
             sv[slot3 * plane + q] = split64(v);
             sw[slot3 * plane + q] = split64(w);
             if (with_p) sp[slot2 * plane + q] = split64(P0[c]);
+            if (pwg) {
+                xu[slot3 * plane + q] = split64(a.PU0[o + c]);
+                xv[slot3 * plane + q] = split64(a.PV0[o + c]);
+                xw[slot3 * plane + q] = split64(a.PW0[o + c]);
+            }
         }
         for (int r = t; r < nring; r += blockDim.x) {
             int kq, jq;
@@ -447,6 +496,11 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
             sv[slot3 * plane + q] = split64(V0[c]);
             sw[slot3 * plane + q] = split64(W0[c]);
             if (with_p) sp[slot2 * plane + q] = split64(P0[c]);
+            if (pwg) {
+                xu[slot3 * plane + q] = split64(a.PU0[o + c]);
+                xv[slot3 * plane + q] = split64(a.PV0[o + c]);
+                xw[slot3 * plane + q] = split64(a.PW0[o + c]);
+            }
         }
     };
 
@@ -466,7 +520,11 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
         if (on) {
             if constexpr (kW) {
                 const Visc3 vs = visc_at(a, G, wv, k, j, i);
-                flux_point<true>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo, wo);
+                if (pwg)
+                    flux_point<true, true>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo,
+                                           wo, xu, xv, xw);
+                else
+                    flux_point<true>(a, X, nx, cl, su, sv, sw, sp, plane, pk, q, i, gfl, vs, uo, vo, wo);
                 if (wg) boundary_terms(a, G, k, j, i, ucur, vcur, wcur, uo, vo, wo);
             } else {
                 const Visc3 vs{};
@@ -559,7 +617,6 @@ __global__ void __launch_bounds__(576, 2)
     unsigned char* fsm = reinterpret_cast<unsigned char*>(
         (reinterpret_cast<unsigned long long>(fraw) + 127) & ~127ULL);
     const int gid = blockIdx.x;
-    if (kW && a.skip && a.skip[gid]) return;
     const DevGrid G = a.grids[gid];
     const int kk = G.kk, jj = G.jj, ii = G.ii, kj = kk * jj;
     const int nk = kk - 4, nj = jj - 4, j0 = 3;
@@ -723,10 +780,12 @@ static int flux_slabs(const DevGrid& G0) {
     return 0;
 }
 
-static size_t flux_smem(const DevGrid& G0) {
+// 11 planes of (hi, lo) windows (U, V, W: 3 each; P: 2), 20 with the point
+// values' windows of the ghost-cell IB
+static size_t flux_smem(const DevGrid& G0, bool pw = false) {
     const int nslab = flux_slabs(G0);
     const int js = (G0.jj - 4 + nslab - 1) / nslab;
-    return (size_t)11 * (G0.kk - 2) * (js + 2) * sizeof(float2);
+    return (size_t)(pw ? 20 : 11) * (G0.kk - 2) * (js + 2) * sizeof(float2);
 }
 
 // Per context: the tensor maps of U, V, W, P for the TMA variant and the
@@ -735,7 +794,9 @@ struct FluxState {
     CUtensorMap map[4];
     bool tma = false;
     bool walls = false;     // some grid has a face that is not CON: the boundary path
-    const unsigned char* d_skip = nullptr;   // grids whose fluxes another kernel computes
+    // ghost-cell IB: per-grid flags of the grids whose transported velocities
+    // are the point values (the plane-load kernel then carries their windows)
+    const unsigned char* d_pw = nullptr;
     int variant = -1;
     double ms[2] = {0.0, 0.0};
 };
@@ -819,9 +880,9 @@ void mx_flux_release(Ctx* c) { g_flux.erase(c); }
 static int launch_variant(Ctx* c, int v, const FluxArgs& a, int threads) {
     const DevGrid& G0 = c->grids[0];
     FluxState& fs = g_flux[c];
-    const size_t tsm = flux_tma_smem(G0), psm = flux_smem(G0);
+    const size_t tsm = flux_tma_smem(G0), psm = flux_smem(G0, fs.d_pw != nullptr);
     const unsigned nb = (unsigned)(c->ngrid * a.nslab);
-    if (v == 1 && fs.tma) {
+    if (v == 1 && fs.tma && !fs.d_pw) {
         if (fs.walls)
             k_mx_flux_tma<true><<<c->ngrid, threads, tsm, c->stream>>>(a, fs.map[0], fs.map[1],
                                                                       fs.map[2], fs.map[3]);
@@ -864,7 +925,11 @@ static FluxArgs flux_args(Ctx* c, float* du, float* dv, float* dw, const float* 
     // (wernerwengle_mod.F90:13-28 init_wernerwengle)
     a.G = c->F("G");
     a.UO = c->F("UO"); a.VO = c->F("VO"); a.WO = c->F("WO");
-    a.skip = g_flux[c].d_skip;
+    a.pwflag = g_flux[c].d_pw;
+    a.pw = a.pwflag ? 1 : 0;
+    a.PU0 = c->f3.count("PWU") ? c->F("PWU") : nullptr;
+    a.PV0 = c->f3.count("PWV") ? c->F("PWV") : nullptr;
+    a.PW0 = c->f3.count("PWW") ? c->F("PWW") : nullptr;
     a.guni = c->d_guni;
     a.ddx = c->L("DDX"); a.ddy = c->L("DDY"); a.ddz = c->L("DDZ");
     a.wwx = c->L("WWX"); a.wwy = c->L("WWY"); a.wwz = c->L("WWZ");
@@ -950,13 +1015,22 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
 
 bool mx_flux_has_tma(Ctx* c) { return g_flux[c].tma; }
 
-// Grids (device flags, 1 = skip) whose fluxes the caller computes with
-// another kernel; the boundary instantiation, which honours the flags, is
-// used from then on.
-void mx_flux_set_skip(Ctx* c, const unsigned char* d_skip) {
+// Ghost-cell IB: device flags (per grid, 1 = the transported velocities are
+// the point values PWU, PWV, PWW); the boundary instantiation of the
+// plane-load kernel, which carries the point values' windows, is used from
+// then on.
+int mx_flux_set_pw(Ctx* c, const unsigned char* d_pw) {
     FluxState& fs = g_flux[c];
-    fs.d_skip = d_skip;
-    if (d_skip) fs.walls = true;
+    fs.d_pw = d_pw;
+    if (!d_pw) return 0;
+    fs.walls = true;
+    const size_t smem = flux_smem(c->grids[0], true);
+    if (smem > 227 * 1024) {
+        set_error("mixed form: grid planes too large for the ghost-cell flux windows");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    MG_CUDA(cudaFuncSetAttribute(k_mx_flux<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return 0;
 }
 
 }  // namespace mg

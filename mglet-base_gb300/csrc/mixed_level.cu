@@ -520,12 +520,12 @@ int mx_gridmax(Ctx* c, SipState& st, const int* ctl) {
 }
 
 int mx_rk_par(Ctx* c, const LevelState& lv, float* du, float* dv, float* dw, const double* sprm) {
-    if (lv.parall.empty() && !lv.d_skip) return 0;
+    if (lv.parall.empty()) return 0;
     ProfScope ps_(c, "mx_rk_par");
     long long npts = 0;
     for (const DevGrid& G : c->grids) npts = std::max(npts, (long long)G.kk * G.jj * G.ii);
     const dim3 grid((unsigned)((npts + 255) / 256), (unsigned)c->ngrid);
-    k_mx_rk_par<<<grid, 256, 0, c->stream>>>(c->d_grids, lv.d_skip, c->F("U"), c->F("V"), c->F("W"),
+    k_mx_rk_par<<<grid, 256, 0, c->stream>>>(c->d_grids, nullptr, c->F("U"), c->F("V"), c->F("W"),
                                              du, dv, dw, c->F("UO"), c->F("VO"), c->F("WO"), sprm);
     MG_LAUNCHED(c);
     return 0;

@@ -9,10 +9,9 @@ namespace mg {
 
 // Per level (index ilevel - minlevel): its grids and those with a PAR face,
 // host and device lists; every grid with a PAR face.  With the ghost-cell IB
-// (ibflag set before the set-up: the grids with lists) d_skip holds per grid,
-// at every stage, whether its transported point values PWU, PWV, PWW differ
-// from U, V, W: those grids take the FP64 tstle4 and the separate RK update,
-// and the fused flux kernel skips them.
+// (ibflag set before the set-up) d_skip holds per grid, at every stage,
+// whether its transported point values PWU, PWV, PWW differ from U, V, W:
+// the flux kernel then transports those point values.
 struct LevelState {
     bool ready = false;
     std::vector<std::vector<int>> grids, pars;
@@ -36,7 +35,7 @@ int mx_bound_pressure(Ctx* c, SipState& st, const LevelState& lv, int ilevel, co
 int mx_ftoc(Ctx* c, SipState& st, const LevelState& lv, int ilevel, bool rhs, const int* ctl);
 // per-grid max |rhs| into the context's grid reduction array
 int mx_gridmax(Ctx* c, SipState& st, const int* ctl);
-// the RK update from UO, VO, WO of the grids with a PAR face or a d_skip flag
+// the RK update from UO, VO, WO of the grids with a PAR face
 int mx_rk_par(Ctx* c, const LevelState& lv, float* du, float* dv, float* dw, const double* sprm);
 // ghost-cell IB: d_skip = the grids whose PWU, PWV, PWW differ from U, V, W
 int mx_pw_flags(Ctx* c, const LevelState& lv);

@@ -266,11 +266,8 @@ __global__ void __launch_bounds__(256) k_tstle4(const DevGrid* __restrict__ grid
                                                 const double* __restrict__ P, const double* __restrict__ Gf,
                                                 Wall wl, double iles, double gx, double gy, double gz,
                                                 const double* __restrict__ FX, const double* __restrict__ FY,
-                                                const double* __restrict__ FZ, const double* __restrict__ GU,
-                                                const unsigned char* __restrict__ only) {
-    // only: per grid, 1 where this launch computes (null: every grid)
+                                                const double* __restrict__ FZ, const double* __restrict__ GU) {
     const int gi = blockIdx.y;
-    if (only && !only[gi]) return;
     const DevGrid G = grids[gi];
     const int kk = G.kk, jj = G.jj, ii = G.ii;
     const int npts = kk * jj * ii;
@@ -414,36 +411,10 @@ int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, c
                                           c->prm.gradp[2],
                                           c->bodyforce ? c->F("FBX") : nullptr,
                                           c->bodyforce ? c->F("FBY") : nullptr,
-                                          c->bodyforce ? c->F("FBZ") : nullptr, c->d_guni, nullptr);
+                                          c->bodyforce ? c->F("FBZ") : nullptr, c->d_guni);
     MG_LAUNCHED(c);
     // tstle4_mod.F90:114: tstle4_par after kon, diff and gradp (PAR faces)
     return launch_tstle4_par(c, uo, vo, wo, u, v, w, ut, vt, wt);
-}
-
-// kon, diff and gradp of tstle4 (no tstle4_par) on the grids flagged in
-// only (device, per grid): the mixed form's grids whose transported point
-// values (PWU, PWV, PWW) differ from the transporting velocities.
-int launch_tstle4_grids(Ctx* c, const unsigned char* only, double* uo, double* vo, double* wo,
-                        const double* u, const double* v, const double* w, const double* ut,
-                        const double* vt, const double* wt, const double* p, const double* g) {
-    ProfScope ps_(c, "tstle4_grids");
-    k_g_uniform<<<c->ngrid, 256, 0, c->stream>>>(c->d_grids, g, c->prm.gmol, c->d_guni);
-    MG_LAUNCHED(c);
-    Wall wl = {};
-    const double gmol = c->prm.gmol, rho = c->prm.rho, cwa = 8.3, cwb = 1.0 / 7.0;
-    const double cpo1 = 1.0 - cwb, cpo2 = 1.0 + cwb;
-    wl.rho = rho;
-    wl.gmol = gmol;
-    wl.cpo4 = cpo2 / cwa * std::pow(gmol / rho, cwb);
-    wl.cpo5 = 0.5 * cpo1 * std::pow(cwa, cpo2 / cpo1) * std::pow(gmol / rho, cpo2);
-    wl.cpo6 = 0.5 * gmol / rho * std::pow(cwa, 2.0 / cpo1);
-    wl.cpo8 = 2.0 / cpo2;
-    dim3 grid((max_points(c) + 255) / 256, c->ngrid);
-    k_tstle4<<<grid, 256, 0, c->stream>>>(c->d_grids, spacing(c), uo, vo, wo, u, v, w, ut, vt, wt, p, g,
-                                          wl, 0.0, c->prm.gradp[0], c->prm.gradp[1], c->prm.gradp[2],
-                                          nullptr, nullptr, nullptr, c->d_guni, only);
-    MG_LAUNCHED(c);
-    return 0;
 }
 
 int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu) {
