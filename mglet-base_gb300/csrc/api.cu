@@ -795,7 +795,8 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     cudaFree(c->d_bface);
     for (void* p : {(void*)c->gcd.seg, (void*)c->gcd.xpoli, (void*)c->gcd.xpolr,
                     (void*)c->gcd.xpolrvel, (void*)c->gcd.oldsol, (void*)c->gcd.oldsolvel,
-                    (void*)c->gcd.poldsol, (void*)c->gcd.poldsolvel})
+                    (void*)c->gcd.poldsol, (void*)c->gcd.poldsolvel, (void*)c->gcd.cell,
+                    (void*)c->gcd.lvstart})
         cudaFree(p);
     for (int* b : c->d_bgrids) cudaFree(b);
     for (int* b : c->d_pgrids) cudaFree(b);

@@ -50,6 +50,10 @@ struct GcHostList {
 struct GcSeg {
     long long xi, xr, sv;   // offsets into xpoli, xpolr (= xpolrvel), save buffers
     int n;
+    // the list's cells in dependency levels: cells cell0 + lvstart[lv0 + L]
+    // .. cell0 + lvstart[lv0 + L + 1] of the cell table form level L (nlv
+    // levels); within a level no cell writes what another reads or writes
+    int cell0, lv0, nlv;
 };
 struct GcDev {
     GcSeg* seg = nullptr;           // [ngrid][4]
@@ -57,6 +61,10 @@ struct GcDev {
     double *xpolr = nullptr, *xpolrvel = nullptr;
     double *oldsol = nullptr, *oldsolvel = nullptr;
     long long *poldsol = nullptr, *poldsolvel = nullptr;
+    // per cell {offset of its record in the segment's xpoli, in its xpolr,
+    // its position in the list, 0}, ordered by segment and level
+    int4* cell = nullptr;
+    int* lvstart = nullptr;
 };
 
 // One box copy of connect_self_single (connect2_mod.F90:947-995): the

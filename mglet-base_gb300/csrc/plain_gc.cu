@@ -1,13 +1,18 @@
 // plain_gc.cu -- ghost-cell immersed boundary runtime, FP64.
 //
 // The stencil lists come from the caller in the formats the reference reads
-// (gc_flowstencils_mod.F90:37-100).  Every list is walked in its own order by
-// one thread -- a ghost value may feed a later stencil of the same list
+// (gc_flowstencils_mod.F90:37-100).  The reference walks each list in order,
+// updating in place: a ghost value may feed a later stencil of the same list
 // (wmxpolsol, :963-1005) and the flux correction updates faces shared by
-// neighbouring cut cells (wmxpolsolcorr, :1113-1183) -- and the grids and
-// velocity components run in parallel.  maskbp (timeintegration_mod.F90
-// :255-303) is elementwise.  Compiled without FMA contraction.
+// neighbouring cut cells (wmxpolsolcorr, :1113-1183).  At upload every list
+// is cut into dependency levels (a cell goes after every earlier cell that
+// writes a value it reads or writes, or reads a value it writes); one CTA
+// per list runs the levels in order, the cells of a level in parallel, so
+// every cell sees exactly the values of the ordered walk.  maskbp
+// (timeintegration_mod.F90:255-303) is elementwise.  Compiled without FMA
+// contraction.
 #include <algorithm>
+#include <unordered_map>
 #include <vector>
 
 #include "internal.h"
@@ -17,72 +22,89 @@ namespace mg {
 namespace {
 
 // modes F / X: var(intcell) = sum var(stcell) coeff + const
+// One CTA per (grid, component) list.
 __global__ void k_gc_sol(const DevGrid* __restrict__ grids, GcDev d, double* U, double* V,
                          double* W, int ngrid, int vel, int ilevel) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 3 * ngrid) return;
-    const int g = t / 3, cmp = t % 3;
+    const int g = blockIdx.x / 3, cmp = blockIdx.x % 3;
     if (ilevel && grids[g].level != ilevel) return;
     const GcSeg s = d.seg[4 * g + cmp];
+    if (s.n == 0) return;
     double* var = (cmp == 0 ? U : (cmp == 1 ? V : W)) + grids[g].ip3;
     const long long* xi = d.xpoli + s.xi;
     const double* xr = (vel ? d.xpolrvel : d.xpolr) + s.xr;
-    long long pi = 0, pr = 0;
-    for (int cell = 0; cell < s.n; ++cell) {
-        const long long intcell = xi[pi++];
-        const long long n = xi[pi++];
-        double flux = 0.0;
-        for (long long q = 0; q < n; ++q) {
-            const long long st = xi[pi++];
-            flux = flux + var[st - 1] * xr[pr++];
+    for (int L = 0; L < s.nlv; ++L) {
+        const int a = d.lvstart[s.lv0 + L], b = d.lvstart[s.lv0 + L + 1];
+        for (int e = a + threadIdx.x; e < b; e += blockDim.x) {
+            const int4 cr = d.cell[s.cell0 + e];
+            long long pi = cr.x, pr = cr.y;
+            const long long intcell = xi[pi++];
+            const long long n = xi[pi++];
+            double flux = 0.0;
+            for (long long q = 0; q < n; ++q) {
+                const long long st = xi[pi++];
+                flux = flux + var[st - 1] * xr[pr++];
+            }
+            flux = flux + xr[pr++];
+            var[intcell - 1] = flux;
         }
-        flux = flux + xr[pr++];
-        var[intcell - 1] = flux;
+        __syncthreads();
     }
 }
 
 // modes S / Z (save) and R / Y (restore)
+// One CTA per (grid, component) list; a restore writes in the levels of the
+// list (a position written twice keeps the later cell's value).
 __global__ void k_gc_savrst(const DevGrid* __restrict__ grids, GcDev d, double* U, double* V,
                             double* W, int ngrid, int vel, int save, int ilevel) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= 3 * ngrid) return;
-    const int g = t / 3, cmp = t % 3;
+    const int g = blockIdx.x / 3, cmp = blockIdx.x % 3;
     if (ilevel && grids[g].level != ilevel) return;
     const GcSeg s = d.seg[4 * g + cmp];
+    if (s.n == 0) return;
     double* var = (cmp == 0 ? U : (cmp == 1 ? V : W)) + grids[g].ip3;
     double* old = (vel ? d.oldsolvel : d.oldsol) + s.sv;
     long long* pold = (vel ? d.poldsolvel : d.poldsol) + s.sv;
-    if (save) {
-        const long long* xi = d.xpoli + s.xi;
-        long long pi = 0;
-        for (int q = 0; q < s.n; ++q) {
-            const long long idx = xi[pi++];
-            const long long n = xi[pi++];
-            pi += n;
-            pold[q] = idx;
-            old[q] = var[idx - 1];
+    const long long* xi = d.xpoli + s.xi;
+    for (int L = 0; L < s.nlv; ++L) {
+        const int a = d.lvstart[s.lv0 + L], b = d.lvstart[s.lv0 + L + 1];
+        for (int e = a + threadIdx.x; e < b; e += blockDim.x) {
+            const int4 cr = d.cell[s.cell0 + e];
+            const int q = cr.z;
+            if (save) {
+                const long long idx = xi[cr.x];
+                pold[q] = idx;
+                old[q] = var[idx - 1];
+            } else {
+                var[pold[q] - 1] = old[q];
+            }
         }
-    } else {
-        for (int q = 0; q < s.n; ++q) var[pold[q] - 1] = old[q];
+        __syncthreads();
     }
 }
 
-// mode C: wmxpolsolcorr, one thread per grid
+// mode C: wmxpolsolcorr, one CTA per grid
 __global__ void k_gc_corr(const DevGrid* __restrict__ grids, GcDev d, double* U, double* V,
                           double* W, const double* __restrict__ DDX, const double* __restrict__ DDY,
                           const double* __restrict__ DDZ, int ngrid, int* err, int ilevel) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= ngrid) return;
+    const int g = blockIdx.x;
     const DevGrid G = grids[g];
     if (ilevel && G.level != ilevel) return;
     const GcSeg s = d.seg[4 * g + 3];
+    if (s.n == 0) return;
     double *u = U + G.ip3, *v = V + G.ip3, *w = W + G.ip3;
     const double *ddx = DDX + G.ipx - 1, *ddy = DDY + G.ipy - 1, *ddz = DDZ + G.ipz - 1;
     const long long ishift = (long long)G.jj * G.kk, jshift = G.kk, kshift = 1;
     const long long* fi = d.xpoli + s.xi;
     const double* fr = d.xpolr + s.xr;
-    long long pi = 0, pr = 0;
-    for (int cell = 0; cell < s.n; ++cell) {
+    // a cut cell without open area stops the reference's walk: the cells of
+    // later levels are skipped too
+    __shared__ int bad;
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    for (int L = 0; L < s.nlv && !bad; ++L) {
+      const int a = d.lvstart[s.lv0 + L], b = d.lvstart[s.lv0 + L + 1];
+      for (int e = a + threadIdx.x; e < b; e += blockDim.x) {
+        const int4 cr = d.cell[s.cell0 + e];
+        long long pi = cr.x, pr = cr.y;
         pi++;   // foundnr
         const long long c0 = fi[pi++] - 1;
         const double ax1 = fr[pr++], ax2 = fr[pr++], ay1 = fr[pr++];
@@ -96,7 +118,8 @@ __global__ void k_gc_corr(const DevGrid* __restrict__ grids, GcDev d, double* U,
         const double sarea = ax1 + ax2 + ay1 + ay2 + az1 + az2;
         if (sarea < 2.2250738585072014e-308) {   // TINY(1.0_realk): errr in the reference
             atomicExch(err, 1);
-            return;
+            bad = 1;
+            continue;
         }
         div = div / sarea;
         u[c0] = u[c0] - ax1 * div / (ddy[j] * ddz[k]);
@@ -105,6 +128,8 @@ __global__ void k_gc_corr(const DevGrid* __restrict__ grids, GcDev d, double* U,
         v[c0 - jshift] = v[c0 - jshift] + ay2 * div / (ddx[i] * ddz[k]);
         w[c0] = w[c0] - az1 * div / (ddx[i] * ddy[j]);
         w[c0 - kshift] = w[c0 - kshift] + az2 * div / (ddx[i] * ddy[j]);
+      }
+      __syncthreads();
     }
 }
 
@@ -177,9 +202,77 @@ int gc_upload(Ctx* c) {
             }
         }
     }
+    // dependency levels of every list (see the file comment): a cell goes one
+    // level after the last earlier cell that wrote a value it reads or
+    // writes, or read a value it writes; within a level the list's order
+    std::vector<int4> cells;
+    std::vector<int> lvstart;
+    for (int g = 0; g < c->ngrid; ++g) {
+        const GcHostList& L = c->gch[g];
+        const DevGrid& G = c->grids[g];
+        const long long box = (long long)G.kk * G.jj * G.ii;
+        for (int q = 0; q < 4; ++q) {
+            GcSeg& sg = seg[4 * g + q];
+            const int n = L.n[q];
+            std::vector<int> lev(n, 0);
+            std::vector<int4> rec(n);
+            std::unordered_map<long long, int> lastw, maxr;
+            const std::vector<long long>& x = L.xi[q];
+            long long pi = 0, pr = 0;
+            int nlv = 0;
+            for (int cell = 0; cell < n; ++cell) {
+                rec[cell] = make_int4((int)pi, (int)pr, cell, 0);
+                int lv = 0;
+                auto after_write = [&](long long loc) {
+                    auto it = lastw.find(loc);
+                    if (it != lastw.end()) lv = std::max(lv, it->second + 1);
+                };
+                auto after_read = [&](long long loc) {
+                    auto it = maxr.find(loc);
+                    if (it != maxr.end()) lv = std::max(lv, it->second + 1);
+                };
+                if (q < 3) {
+                    const long long w = x[pi], m = x[pi + 1];
+                    for (long long t = 0; t < m; ++t) after_write(x[pi + 2 + t]);
+                    after_read(w);
+                    after_write(w);
+                    lastw[w] = lv;
+                    for (long long t = 0; t < m; ++t) {
+                        int& r = maxr[x[pi + 2 + t]];
+                        r = std::max(r, lv);
+                    }
+                    pi += 2 + m;
+                    pr += m + 1;
+                } else {
+                    // the six faces of wmxpolsolcorr, read and written
+                    const long long c0 = x[pi + 1] - 1;
+                    const long long loc[6] = {c0, c0 - (long long)G.kk * G.jj, box + c0, box + c0 - G.kk,
+                                              2 * box + c0, 2 * box + c0 - 1};
+                    for (long long l : loc) after_write(l);
+                    for (long long l : loc) lastw[l] = lv;
+                    pi += 2;
+                    pr += 7;
+                }
+                lev[cell] = lv;
+                nlv = std::max(nlv, lv + 1);
+            }
+            sg.cell0 = (int)cells.size();
+            sg.lv0 = (int)lvstart.size();
+            sg.nlv = n ? nlv : 0;
+            std::vector<int> count(nlv + 1, 0);
+            for (int cell = 0; cell < n; ++cell) count[lev[cell] + 1]++;
+            for (int l = 0; l < nlv; ++l) count[l + 1] += count[l];
+            lvstart.insert(lvstart.end(), count.begin(), count.end());
+            std::vector<int4> ord(n);
+            std::vector<int> fillp(count.begin(), count.end() - 1);
+            for (int cell = 0; cell < n; ++cell) ord[fillp[lev[cell]]++] = rec[cell];
+            cells.insert(cells.end(), ord.begin(), ord.end());
+        }
+    }
     GcDev& d = c->gcd;
     for (void* p : {(void*)d.seg, (void*)d.xpoli, (void*)d.xpolr, (void*)d.xpolrvel, (void*)d.oldsol,
-                    (void*)d.oldsolvel, (void*)d.poldsol, (void*)d.poldsolvel})
+                    (void*)d.oldsolvel, (void*)d.poldsol, (void*)d.poldsolvel, (void*)d.cell,
+                    (void*)d.lvstart})
         cudaFree(p);
     d = GcDev();
     auto up = [&](auto** dst, const auto& v) -> int {
@@ -191,6 +284,8 @@ int gc_upload(Ctx* c) {
         return 0;
     };
     if (int rc = up(&d.seg, seg)) return rc;
+    if (int rc = up(&d.cell, cells)) return rc;
+    if (int rc = up(&d.lvstart, lvstart)) return rc;
     if (int rc = up(&d.xpoli, xi)) return rc;
     if (int rc = up(&d.xpolr, xr)) return rc;
     if (int rc = up(&d.xpolrvel, xv)) return rc;
@@ -228,8 +323,7 @@ int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w, int ileve
     switch (mode) {
     case 'F':
     case 'X':
-        k_gc_sol<<<(nt + 127) / 128, 128, 0, c->stream>>>(c->d_grids, d, u, v, w, c->ngrid,
-                                                           mode == 'X', ilevel);
+        k_gc_sol<<<nt, 128, 0, c->stream>>>(c->d_grids, d, u, v, w, c->ngrid, mode == 'X', ilevel);
         break;
     case 'S':
     case 'Z':
@@ -243,15 +337,14 @@ int launch_gc_mode(Ctx* c, char mode, double* u, double* v, double* w, int ileve
                           : "gc: restore R before any save S (setibvalues first, as flow_mod.F90:84 does)");
             return MGLET_ERR_ARG;
         }
-        k_gc_savrst<<<(nt + 127) / 128, 128, 0, c->stream>>>(c->d_grids, d, u, v, w, c->ngrid, vel, save,
-                                                              ilevel);
+        k_gc_savrst<<<nt, 128, 0, c->stream>>>(c->d_grids, d, u, v, w, c->ngrid, vel, save, ilevel);
         if (save) c->gc_saved[vel] = true;
         break;
     }
     case 'C': {
         int* err = reinterpret_cast<int*>(c->d_scalar + 7);
         MG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-        k_gc_corr<<<(c->ngrid + 127) / 128, 128, 0, c->stream>>>(
+        k_gc_corr<<<c->ngrid, 128, 0, c->stream>>>(
             c->d_grids, d, u, v, w, c->L("DDX"), c->L("DDY"), c->L("DDZ"), c->ngrid, err, ilevel);
         MG_LAUNCHED(c);
         int herr = 0;

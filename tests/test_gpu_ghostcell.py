@@ -50,6 +50,45 @@ def test_ghostcell_ops(gpu_lib, oracle_lib, op):
         assert np.array_equal(gs.get(nm), o.get(nm)), nm
 
 
+def _chained(case, lists):
+    """The synthetic lists with three cells appended to the first grid's u
+    list that depend on each other and on the list: cell A writes a, reading
+    b and the first cell's ghost value; cell B writes c, reading a (after A);
+    cell C writes b (after A read it).  The level-parallel walk must give the
+    values of the ordered walk."""
+    kk, jj = case.kk, case.jj
+    flat = lambda i, j, k: (k - 1) + (j - 1) * kk + (i - 1) * kk * jj + 1
+    n, xi, xr, xv = lists[0][1]
+    first = int(xi[0])
+    a, b, cc = flat(4, 4, 4), flat(4, 5, 4), flat(5, 4, 4)
+    xi2 = list(xi) + [a, 2, b, first] + [cc, 1, a] + [b, 1, flat(5, 5, 5)]
+    xr2 = list(xr) + [0.5, 0.25, 0.1] + [0.7, -0.2] + [0.3, 0.05]
+    xv2 = list(xv) + [0.4, 0.3, 0.0] + [0.6, 0.0] + [0.2, 0.0]
+    out = [dict(gl) for gl in lists]
+    out[0][1] = (n + 3, np.array(xi2, dtype=np.int64), np.array(xr2), np.array(xv2))
+    return out
+
+
+@pytest.mark.parametrize("op", ["I", "X"])
+def test_ghostcell_dependent_cells_bit_exact(gpu_lib, oracle_lib, op):
+    """Cells of one list that read values earlier cells write (and write
+    values earlier cells read) come out as the reference's ordered walk
+    gives them, bit for bit, in setibvalues and setpointvalues."""
+    case, bp, lists = gc_case(seed=7)
+    lists = _chained(case, lists)
+    fields = random_fields(case, 5)
+    gs, o = gpu_lib.Solver(case, _prm()), oracle_lib.Oracle(case, _prm())
+    for s in (gs, o):
+        load(s, case, bp, lists, fields)
+        if op == "I":
+            s.gc_mode("I")
+        else:
+            s.setpointvalues(True)
+    names = ("U", "V", "W") if op == "I" else ("PWU", "PWV", "PWW")
+    for nm in names:
+        assert np.array_equal(gs.get(nm), o.get(nm)), nm
+
+
 def test_ghostcell_stages_bit_exact(gpu_lib, oracle_lib):
     """Two time steps (six stages): setibvalues on the first stage of each
     step, maskbp + getibvalues after the RK update, the ghost-cell divcal
