@@ -500,10 +500,15 @@ int mglet_gpu_set_partition(mglet_ctx* ctx, const int32_t* halo, int32_t nsend,
  * (points loaded ahead, CTAs per SM, and the uniform-coefficient variant
  * where every coefficient class allows it) on the case itself and keeps the
  * fastest, cached per grid shape for the process; the environment variable
- * MGLET_TUNE=0 keeps the defaults.  mglet_gpu_tuning describes the choice
- * ("" for the plain form); mglet_gpu_force_variant overrides it (kernel
- * "mx_sip_pre", variant 0..9, -1 = default).  All variants compute the same
- * bits. */
+ * MGLET_TUNE=0 keeps the defaults.  The same holds for the packed sweeps
+ * (ranks per thread, CTAs per SM), the flux kernel (plane loads or TMA) and
+ * the persistent solve of single-level cases (the whole outer loop of
+ * mgpoisl as one cooperative launch with grid-wide barriers; kept only when
+ * it is faster than the per-phase kernels).  mglet_gpu_tuning describes the
+ * choices ("" for the plain form); mglet_gpu_force_variant overrides one
+ * (kernel "mx_sip_pre" 0..9, "mx_sip_sweep" 0..4, "mx_flux" 0..1,
+ * "mx_sip_solve" 0..5; -1 = default, for "mx_sip_solve" the per-phase
+ * kernels).  All variants compute the same bits. */
 int mglet_gpu_tuning(mglet_ctx* ctx, char* buf, int64_t buflen);
 int mglet_gpu_force_variant(mglet_ctx* ctx, const char* kernel, int32_t variant);
 /* Test switch for the failure path of the bounded waits: the next mixed
@@ -513,6 +518,13 @@ int mglet_gpu_force_variant(mglet_ctx* ctx, const char* kernel, int32_t variant)
  * out waiting for its bulk copies"); the context stays usable and the next
  * stage runs normally.  No fault, trap or hang is involved. */
 int mglet_gpu_test_wait_timeout(mglet_ctx* ctx);
+/* Test switch for the grid-wide barriers of the persistent solve: in the next
+ * mixed stage (issued without its graph) one CTA of the persistent solve
+ * leaves before its first arrival, so the other CTAs' barrier wait gives up
+ * after about a second; they raise the error flag and return, and the stage
+ * returns MGLET_ERR_CUDA ("timed out").  Needs the persistent solve in use
+ * (mglet_gpu_force_variant "mx_sip_solve").  The context stays usable. */
+int mglet_gpu_test_barrier_timeout(mglet_ctx* ctx);
 
 /* ---- Misc ----------------------------------------------------------------- */
 int mglet_gpu_synchronize(mglet_ctx* ctx);

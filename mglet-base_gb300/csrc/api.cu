@@ -1336,6 +1336,11 @@ int mglet_gpu_test_wait_timeout(mglet_ctx* c) {
     return mixed_test_wait_timeout(c);
 }
 
+int mglet_gpu_test_barrier_timeout(mglet_ctx* c) {
+    if (!c) return fail(MGLET_ERR_ARG, "test_barrier_timeout: null context");
+    return mixed_test_barrier_timeout(c);
+}
+
 int mglet_gpu_force_variant(mglet_ctx* c, const char* kernel, int32_t variant) {
     if (!c || !kernel) return fail(MGLET_ERR_ARG, "force_variant: null argument");
     return mixed_force_variant(c, kernel, variant);

@@ -81,39 +81,6 @@ struct MixedState {
 
 namespace {
 
-__device__ __forceinline__ double block_max_d(double v, double* sh) {
-    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) sh[w] = v;
-    __syncthreads();
-    if (w == 0) {
-        v = (l < (int)(blockDim.x >> 5)) ? sh[l] : 0.0;
-        for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
-    }
-    __syncthreads();
-    return v;
-}
-
-// maxabscal over grids + the outer-loop stopping test of mgpoisl
-// (pressuresolver_mod.F90:275,294-301), on the device.
-__global__ void k_mx_conv(const DevGrid* __restrict__ grids, int ngrid, int maxlevel,
-                          const double* __restrict__ gridmax, int* ctl, double* maxrhs,
-                          const double* __restrict__ sprm, double epcorr, int nouter_min) {
-    if (ctl[0]) return;
-    const double prefak = sprm[2];
-    __shared__ double sh[32];
-    double m = 0.0;
-    for (int g = threadIdx.x; g < ngrid; g += blockDim.x)
-        m = fmax(fabs(gridmax[g] * ldexp(1.0, maxlevel - grids[g].level)), m);
-    m = block_max_d(m, sh);
-    if (threadIdx.x == 0) {
-        const int done = ctl[1] + 1;
-        ctl[1] = done;
-        maxrhs[0] = m;
-        if (done >= nouter_min && m / prefak < epcorr) ctl[0] = 1;
-    }
-}
-
 #define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
 
 // mgpcorr (pressuresolver_mod.F90:808-844; BPF non-null: the bp form of the
@@ -204,7 +171,12 @@ int enqueue_mgpoisl(Ctx* c) {
     // covered every face (the rotating res slots of each level's grids)
     const int nl = c->maxlevel - c->minlevel + 1;
     std::vector<int> gi(nl, 0), lastfull(nl, 0);
-    for (int ipcount = 1; ipcount <= c->prm.nouter; ++ipcount) {
+    // one level: the whole outer loop as one persistent launch when the
+    // tuner (or the caller) chose it
+    const bool persistent = !multi && s.solve_variant >= 0;
+    if (persistent)
+        if (int rc = sip_solve(c, s, m->cf, m->apx, m->d_gcls, ctl, m->d_maxrhs, m->d_sprm)) return rc;
+    for (int ipcount = 1; ipcount <= (persistent ? 0 : c->prm.nouter); ++ipcount) {
         // pressuresolver_mod.F90:218-302: level by level, coarse to fine
         for (int l = c->minlevel; l <= c->maxlevel; ++l) {
             const int li = l - c->minlevel;
@@ -240,13 +212,7 @@ int enqueue_mgpoisl(Ctx* c) {
                 if (int rc = mx_ftoc(c, s, lv, l, true, ctl)) return rc;
             if (int rc = mx_gridmax(c, s, ctl)) return rc;
         }
-        {
-            ProfScope ps_(c, "mx_conv");
-            k_mx_conv<<<1, 1024, 0, c->stream>>>(c->d_grids, c->ngrid, c->maxlevel, c->d_gridred,
-                                                 m->d_ctl, m->d_maxrhs, m->d_sprm, c->prm.epcorr,
-                                                 c->prm.nouter_min);
-            MG_LAUNCHED(c);
-        }
+        if (int rc = sip_conv(c, m->d_ctl, m->d_maxrhs, m->d_sprm)) return rc;
     }
     if (int rc = sip_scatter_dp(c, s)) return rc;
     // dp ghosts (the reference accumulates the connected hilf ghosts into dp)
@@ -355,12 +321,14 @@ int enqueue_stage(Ctx* c) {
     return enqueue_mgpoisl(c);
 }
 
-// 0, or MGLET_ERR_CUDA when a wavefront kernel gave up waiting for its
-// bulk copies (the device error flag of the control block).
+// 0, or MGLET_ERR_CUDA when a kernel gave up waiting for its bulk copies or
+// at a grid-wide barrier of the persistent solve (the device error flag of
+// the control block).
 int check_device_flag(Ctx* c) {
     MixedState* m = c->mx;
     if (m->h_ctl[2] != 0) {
-        set_error("mixed form: a kernel timed out waiting for its bulk copies");
+        set_error("mixed form: a kernel timed out waiting for its bulk copies or at a grid-wide "
+                  "barrier");
         return MGLET_ERR_CUDA;
     }
     return 0;
@@ -529,6 +497,9 @@ int mixed_init(Ctx* c) {
     const char* tune = std::getenv("MGLET_TUNE");
     if (!(tune && tune[0] == '0')) {
         if (int rc2 = sip_tune(c, m->sip, m->cf, m->d_gcls, m->d_ctl)) return rc2;
+        if (int rc2 = sip_tune_solve(c, m->sip, m->cf, m->apx, m->d_gcls, m->d_ctl, m->d_maxrhs,
+                                     m->d_sprm))
+            return rc2;
         if (int rc2 = mx_flux_tune(c, m->du32, m->dv32, m->dw32, m->sx, m->sy, m->sz, m->d_sprm,
                                    m->d_ctl + 2))
             return rc2;
@@ -550,7 +521,15 @@ std::string mixed_tuning(Ctx* c) {
                   s.pre_variant >= 0 ? "" : " [default]", s.pre_ms, s.unicls ? "yes" : "no",
                   sip_sweep_variant_name(s.sweep_variant >= 0 ? s.sweep_variant : 0),
                   s.sweep_variant >= 0 ? "" : " [default]", s.sweep_ms);
-    return buf + mx_flux_tuning(c);
+    char sbuf[512];
+    int n = std::snprintf(sbuf, sizeof sbuf,
+                          "mx_sip_solve: %s (persistent %.4f ms, per-phase kernels %.4f ms per "
+                          "outer iteration; variants",
+                          sip_solve_variant_name(s.solve_variant), s.solve_ms, s.phases_ms);
+    for (int v = 0; v < sip_solve_variants() && n > 0 && n < (int)sizeof sbuf; ++v)
+        n += std::snprintf(sbuf + n, sizeof sbuf - n, " %d: %.4f", v, s.solve_var_ms[v]);
+    if (n > 0 && n < (int)sizeof sbuf) std::snprintf(sbuf + n, sizeof sbuf - n, "); ");
+    return std::string(buf) + sbuf + mx_flux_tuning(c);
 }
 
 int mixed_test_wait_timeout(Ctx* c) {
@@ -563,8 +542,36 @@ int mixed_test_wait_timeout(Ctx* c) {
     return 0;
 }
 
+int mixed_test_barrier_timeout(Ctx* c) {
+    MixedState* m = c->mx;
+    if (!m || m->sip.solve_variant < 0) {
+        set_error("test_barrier_timeout: needs the mixed form with the persistent solve");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    m->sip.solve_skip = true;
+    return 0;
+}
+
 int mixed_force_variant(Ctx* c, const char* kernel, int v) {
     MixedState* m = c->mx;
+    if (m && std::strcmp(kernel, "mx_sip_solve") == 0) {
+        if (v < -1 || v >= sip_solve_variants()) {
+            set_error("force_variant: mx_sip_solve variants are 0..5 (-1: the per-phase kernels)");
+            return MGLET_ERR_ARG;
+        }
+        if (v >= 0 && !sip_solve_fits(c, m->sip, v)) {
+            set_error("force_variant: this persistent solve variant does not apply to this case");
+            return MGLET_ERR_UNSUPPORTED;
+        }
+        if (v >= 0)
+            if (int rc = sip_solve_alloc(m->sip)) return rc;
+        m->sip.solve_variant = v;
+        if (m->graph) {
+            cudaGraphExecDestroy(m->graph);
+            m->graph = nullptr;
+        }
+        return 0;
+    }
     if (m && std::strcmp(kernel, "mx_sip_sweep") == 0) {
         if (v < -1 || v >= sip_sweep_variants()) {
             set_error("force_variant: mx_sip_sweep variants are 0..4 (-1 default)");
@@ -692,6 +699,11 @@ int mixed_ghostcell(Ctx* c) {
     // a uniform-coefficient pre-pass no longer applies: the same launch shape
     // with per-point records
     if (!st.unicls && sip_pre_variant_uniform(st.pre_variant)) st.pre_variant -= 5;
+    // the same for the persistent solve (variants 3..5 are the uniform ones)
+    if (st.solve_variant >= 0 && !sip_solve_fits(c, st, st.solve_variant))
+        st.solve_variant = st.solve_variant >= 3 && sip_solve_fits(c, st, st.solve_variant - 3)
+                               ? st.solve_variant - 3
+                               : -1;
     // per-stage flags of the grids whose point values differ from U, V, W
     mx_level_release(m->lv);
     m->lv.ibflag.assign(c->ngrid, 1);
@@ -734,7 +746,7 @@ int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_sta
     if (gc && irk == 1)
         if (int rc = gc_setibvalues(c, c->F("U"), c->F("V"), c->F("W"))) return rc;
     if (int rc = set_stage_scalars(c, frhs, dt * fu, dtrk * dt)) return rc;
-    if (c->prof || m->skip_once) {
+    if (c->prof || m->skip_once || m->sip.solve_skip) {
         if (int rc = enqueue_stage(c)) return rc;
     } else {
         if (!m->graph) {

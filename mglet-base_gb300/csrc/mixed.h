@@ -16,6 +16,7 @@ int mixed_mgpoisl(Ctx* c, double dt, mglet_stage_stats* st);
 std::string mixed_tuning(Ctx* c);
 int mixed_force_variant(Ctx* c, const char* kernel, int v);
 int mixed_test_wait_timeout(Ctx* c);
+int mixed_test_barrier_timeout(Ctx* c);
 // the ghost-cell IB (after mglet_gpu_set_ghostcell's plain set-up)
 int mixed_ghostcell(Ctx* c);
 

@@ -40,6 +40,7 @@
 #include <algorithm>
 #include <cstring>
 #include <map>
+#include <tuple>
 #include <vector>
 
 #include "internal.h"
@@ -129,12 +130,35 @@ __device__ __forceinline__ bool stage_wait(unsigned long long* bar) {
     return false;
 }
 
+// A load of a value that another CTA of the same launch may have written:
+// through L2 (ld.global.cg, coherent across SMs) in the persistent solve,
+// through the read-only path in the per-phase kernels, whose launch
+// boundaries order every write before the read.  ldxs: the same for a stream
+// read once (evict-first on the per-phase path).
+template <bool kCoh>
+__device__ __forceinline__ float ldx(const float* p) {
+    if constexpr (kCoh) return __ldcg(p);
+    else return __ldg(p);
+}
+template <bool kCoh>
+__device__ __forceinline__ float ldxs(const float* p) {
+    if constexpr (kCoh) return __ldcg(p);
+    else return __ldcs(p);
+}
+// ldxp: the same for a value the per-phase kernel itself rewrites (a plain load there)
+template <bool kCoh>
+__device__ __forceinline__ float ldxp(const float* p) {
+    if constexpr (kCoh) return __ldcg(p);
+    else return *p;
+}
+
 // All threads: the hilf ghosts of grid g into gh[6][fs] -- ghost face f is
 // the facing boundary plane of the neighbour across face f (its face f ^ 1),
 // gathered from that neighbour's plane-ordered hilf at the facepos positions;
 // across a face without a neighbour (fn < 0) the grid's own ghost plane in
 // pg ([6][fs], what bound_pressure set on a PAR face) or zero (no pg: walls,
 // inflow and outflow faces).
+template <bool kCoh = false>
 __device__ __forceinline__ void gather_hilf_ghosts(float* gh, const Shape& s, const float* H,
                                                    const int* fn, const float* pg) {
     const int fs = s.fs;
@@ -144,7 +168,7 @@ __device__ __forceinline__ void gather_hilf_ghosts(float* gh, const Shape& s, co
         const int nb = fn[f];
         float v = 0.f;
         if (nb >= 0) {
-            if (pos >= 0) v = __ldg(H + (long long)nb * s.npp + pos);
+            if (pos >= 0) v = ldx<kCoh>(H + (long long)nb * s.npp + pos);
         } else if (pg) {
             v = pg[q];
         }
@@ -286,21 +310,21 @@ __global__ void __launch_bounds__(512) k_sip_pre(PreArgs a) {
 // coefficients at all its points (a uniform tiling without walls), so only
 // the first record {codes, lpr} is read per point and the coefficients come
 // from UNI; the arithmetic is the same, so the result is bit-identical.
-template <int kAhead, int kMinBlocks, bool kUni>
-__global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
-    if (a.ctl[0]) return;
-    extern __shared__ __align__(16) float gh[];   // [6][fs]
-    const Shape s = a.s;
-    const int g = cta_grid(a.glist, a.rev);
-    const bool hz = a.hzero != 0;
+//
+// pre_grid: one grid into PRE (hz: hilf is zero); gh is shared memory for
+// the ghost faces [6][fs].
+template <int kAhead, bool kUni, bool kCoh>
+__device__ __forceinline__ void pre_grid(const PreArgs& a, int g, float* gh, float* PREALL, bool hz) {
+    const Shape& s = a.s;
     const int npp = s.npp;
     if (!hz)
-        gather_hilf_ghosts(gh, s, a.H, a.fnbr + 6 * g, a.PG ? a.PG + (long long)g * 6 * s.fs : nullptr);
+        gather_hilf_ghosts<kCoh>(gh, s, a.H, a.fnbr + 6 * g,
+                                 a.PG ? a.PG + (long long)g * 6 * s.fs : nullptr);
     __syncthreads();
     const long long base = (long long)g * npp;
     const float* __restrict__ H = a.H + base;
     const float* __restrict__ RHS = a.RHS + base;
-    float* __restrict__ PRE = a.PRE + base;
+    float* __restrict__ PRE = PREALL + base;
     const float4* __restrict__ P1 = a.PR + (long long)a.gcls[g] * 3 * npp;
     const float* ghb = gh - npp;
     const int nt = blockDim.x;
@@ -308,8 +332,8 @@ __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
 #pragma unroll
     for (int j = 0; j < kAhead; ++j) {
         const int q = threadIdx.x + j * nt;
-        hq[j] = (!hz && q < npp) ? __ldcs(H + q) : 0.f;
-        rq[j] = q < npp ? __ldcs(RHS + q) : 0.f;
+        hq[j] = (!hz && q < npp) ? ldxs<kCoh>(H + q) : 0.f;
+        rq[j] = q < npp ? ldxs<kCoh>(RHS + q) : 0.f;
     }
     for (int q = threadIdx.x; q < npp; q += nt) {
         const float hc = hq[0], rh = rq[0];
@@ -319,8 +343,8 @@ __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
             rq[j] = rq[j + 1];
         }
         const int qn = q + kAhead * nt;
-        hq[kAhead - 1] = (!hz && qn < npp) ? __ldcs(H + qn) : 0.f;
-        rq[kAhead - 1] = qn < npp ? __ldcs(RHS + qn) : 0.f;
+        hq[kAhead - 1] = (!hz && qn < npp) ? ldxs<kCoh>(H + qn) : 0.f;
+        rq[kAhead - 1] = qn < npp ? ldxs<kCoh>(RHS + qn) : 0.f;
         const float4 r1 = __ldg(P1 + q);
         const int w0 = __float_as_int(r1.x);
         float v = 0.f;
@@ -337,7 +361,7 @@ __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
                     r3 = __ldg(P1 + 2 * npp + q);
                 }
                 const int w1 = __float_as_int(r1.y), w2 = __float_as_int(r1.z);
-                auto nbv = [&](int code) -> float { return code < npp ? __ldg(H + code) : ghb[code]; };
+                auto nbv = [&](int code) -> float { return code < npp ? ldx<kCoh>(H + code) : ghb[code]; };
                 lap = -r2.x * nbv(w0 & 0xffff) - r2.y * nbv(w0 >> 16) - r2.z * nbv(w1 & 0xffff) -
                       r2.w * nbv(w1 >> 16) - r3.x * nbv(w2 & 0xffff) - r3.y * nbv(w2 >> 16) - r3.z * hc;
             }
@@ -345,6 +369,13 @@ __global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
         }
         PRE[q] = v;
     }
+}
+
+template <int kAhead, int kMinBlocks, bool kUni>
+__global__ void __launch_bounds__(512, kMinBlocks) k_sip_pre_pf(PreArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(16) float gh[];   // [6][fs]
+    pre_grid<kAhead, kUni, false>(a, cta_grid(a.glist, a.rev), gh, a.PRE, a.hzero != 0);
 }
 
 // class pre-pass records (see k_sip_pre_pf) from the shape's codes, the
@@ -598,21 +629,22 @@ struct PRec {
     float v;     // pre (forward) / res (backward)
 };
 
-template <int kThreads, int kMinBlocks, int kPts>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd_packed(FwdArgs a) {
-    if (a.ctl[0]) return;
-    extern __shared__ __align__(16) unsigned char rsm[];
-    const Shape s = a.s;
+// One grid of the packed forward sweep: R (the slot the pre-pass filled)
+// holds (rhs + lap) * lpr on entry and res on exit; RLOW is the slot of the
+// last fully exchanged iteration (null: zero low ghosts).
+template <int kPts, bool kCoh>
+__device__ __forceinline__ void fwd_grid(const FwdArgs& a, int g, unsigned char* rsm, float* RALL,
+                                         const float* RLOW) {
+    const Shape& s = a.s;
     const int fs = s.fs, nm = s.nm, mlp = s.maxlp;
     const int rs = (int)packed_region(mlp, fs);
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // two regions
-    const int g = cta_grid(a.glist, a.rev);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float4* SW = a.SW + (long long)a.gcls[g] * s.npp;
     const int* fn = a.fnbr + 6 * g;
-    float* R = a.R + base;
+    float* R = RALL + base;
     for (int q = tid; q <= nm; q += nt) pst[q] = s.pst[q];
     // low res ghosts: the facing boundary planes of the -x, -y, -z neighbours
     // (their high faces 2, 4, 6), gathered from the res of the iteration whose
@@ -621,7 +653,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd_packed(FwdArgs
         const int d = q / fs, fi = q - d * fs;
         const int pos = s.facepos[(2 * d + 1) * fs + fi];
         put_ghost(nb, rs, mlp, fs, d, fi,
-                  (a.RLOW && pos >= 0 && fn[2 * d] >= 0) ? a.RLOW[(long long)fn[2 * d] * s.npp + pos] : 0.f);
+                  (RLOW && pos >= 0 && fn[2 * d] >= 0) ? ldx<kCoh>(RLOW + (long long)fn[2 * d] * s.npp + pos)
+                                                       : 0.f);
     }
     __syncthreads();
     auto fetch = [&](int t, PRec* r) {
@@ -671,21 +704,27 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd_packed(FwdArgs
 }
 
 template <int kThreads, int kMinBlocks, int kPts>
-__global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs a) {
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_fwd_packed(FwdArgs a) {
     if (a.ctl[0]) return;
     extern __shared__ __align__(16) unsigned char rsm[];
-    const Shape s = a.s;
+    fwd_grid<kPts, false>(a, cta_grid(a.glist, a.rev), rsm, a.R, a.RLOW);
+}
+
+// One grid of the packed backward sweep: R is this iteration's res slot,
+// hilf += res (hz: hilf = res).
+template <int kPts, bool kCoh>
+__device__ __forceinline__ void bwd_grid(const BwdArgs& a, int g, unsigned char* rsm, const float* RALL,
+                                         bool hz) {
+    const Shape& s = a.s;
     const int fs = s.fs, nm = s.nm, mlp = s.maxlp;
     const int rs = (int)packed_region(mlp, fs);
     int* pst = reinterpret_cast<int*>(rsm);
     float* nb = reinterpret_cast<float*>(rsm + rp_nb_offset(nm));   // two regions
-    const int g = cta_grid(a.glist, a.rev);
     const int tid = threadIdx.x, nt = blockDim.x;
     const long long base = (long long)g * s.npp;
     const float4* SW = a.SW + (long long)a.gcls[g] * s.npp;
     const int* fn = a.fnbr + 6 * g;
-    const bool hz = a.hzero != 0;
-    const float* R = a.R + base;
+    const float* R = RALL + base;
     float* H = a.H + base;
     for (int q = tid; q <= nm; q += nt) pst[q] = s.pst[q];
     // high res ghosts: the facing boundary planes of the +x, +y, +z
@@ -694,7 +733,8 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs
         const int d = q / fs, fi = q - d * fs;
         const int pos = s.facepos[(2 * d) * fs + fi];
         put_ghost(nb, rs, mlp, fs, d, fi,
-                  (pos >= 0 && fn[2 * d + 1] >= 0) ? a.R[(long long)fn[2 * d + 1] * s.npp + pos] : 0.f);
+                  (pos >= 0 && fn[2 * d + 1] >= 0) ? ldx<kCoh>(RALL + (long long)fn[2 * d + 1] * s.npp + pos)
+                                                   : 0.f);
     }
     __syncthreads();
     // step t is plane nm-1-t
@@ -706,7 +746,7 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs
             const int k = tid + i * nt;
             if (k < lp) {
                 r[i].w = __ldg(SW + p0 + k);
-                r[i].v = __ldg(R + p0 + k);
+                r[i].v = ldx<kCoh>(R + p0 + k);
             } else {
                 r[i].w.x = __int_as_float(-1);
             }
@@ -747,6 +787,13 @@ __global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs
         step(t + 1, qb);
         __syncthreads();
     }
+}
+
+template <int kThreads, int kMinBlocks, int kPts>
+__global__ void __launch_bounds__(kThreads, kMinBlocks) k_sip_bwd_packed(BwdArgs a) {
+    if (a.ctl[0]) return;
+    extern __shared__ __align__(16) unsigned char rsm[];
+    bwd_grid<kPts, false>(a, cta_grid(a.glist, a.rev), rsm, a.R, a.hzero != 0);
 }
 
 // packed records of a class: {position word, the three coefficients of the
@@ -817,6 +864,85 @@ __device__ __forceinline__ void ff_acc(float ch, float cl, float h, float& sum, 
     comp += t + fmaf(cl, h, e);
 }
 
+// The points of grid g: H is its hilf (shared memory in k_sip_outer; global,
+// read through L2, in the persistent solve), gh its ghost faces, spst / ro
+// the plane tables in shared memory.  Writes gridmax[g].
+template <bool kCoh>
+__device__ __forceinline__ void outer_grid(const OuterArgs& a, int g, const float* H, const float* gh,
+                                           const int* spst, const short* ro, double* sh) {
+    const Shape& s = a.s;
+    const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs;
+    const long long base = (long long)g * s.npp;
+    auto hv = [&](int q) -> float {
+        if constexpr (kCoh) return __ldcg(H + q);
+        else return H[q];
+    };
+    const DevGrid G = a.grids[g];
+    const float* APH = a.APX + (long long)a.gcls[g] * 2 * s.npp;
+    const float* APL = APH + s.npp;
+    // 1-D coefficients indexed by io, jo, ko (interior index 3 is io = 0)
+    const float *awh = a.A1[0] + G.ipx + 2, *awl = a.A1L[0] + G.ipx + 2;
+    const float *aeh = a.A1[1] + G.ipx + 2, *ael = a.A1L[1] + G.ipx + 2;
+    const float *ash = a.A1[2] + G.ipy + 2, *asl = a.A1L[2] + G.ipy + 2;
+    const float *anh = a.A1[3] + G.ipy + 2, *anl = a.A1L[3] + G.ipy + 2;
+    const float *abh = a.A1[4] + G.ipz + 2, *abl = a.A1L[4] + G.ipz + 2;
+    const float *ath = a.A1[5] + G.ipz + 2, *atl = a.A1L[5] + G.ipz + 2;
+    float mx = 0.f;      // max |rhs| (its leading float)
+    for (int q = threadIdx.x; q < s.npp; q += blockDim.x) {
+        const int v = s.pq[q];
+        if (v < 0) continue;
+        const int io = v & 1023, jo = (v >> 10) & 1023, ko = v >> 20;
+        const int t = io + jo + ko;
+        // positions of (io, jo, ko-1) on plane t-1 and (io, jo, ko+1) on plane
+        // t+1; the j neighbours sit next to them, the i neighbours one row over
+        const int bm = (ko > 0 || jo > 0) ? spst[t - 1] + ro[(t - 1) * ni + io] + jo : 0;
+        const int bp = (ko < nk - 1 || jo < nj - 1) ? spst[t + 1] + ro[(t + 1) * ni + io] + jo : 0;
+        const float hc = hv(q);
+        float him = io > 0 ? hv(spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo) : gh[0 * fs + fidx_x(s, ko, jo)];
+        float hip = io < ni - 1 ? hv(spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo) : gh[1 * fs + fidx_x(s, ko, jo)];
+        float hjm = jo > 0 ? hv(bm - 1) : gh[2 * fs + fidx_y(s, ko, io)];
+        float hjp = jo < nj - 1 ? hv(bp + 1) : gh[3 * fs + fidx_y(s, ko, io)];
+        float hkm = ko > 0 ? hv(bm) : gh[4 * fs + fidx_z(s, jo, io)];
+        float hkp = ko < nk - 1 ? hv(bp) : gh[5 * fs + fidx_z(s, jo, io)];
+        if (a.BM) {   // couplings BP closes contribute nothing (laplacephi's bp products)
+            const unsigned mk = a.BM[base + q];
+            him = mk & 1u ? him : 0.f;
+            hip = mk & 2u ? hip : 0.f;
+            hjm = mk & 4u ? hjm : 0.f;
+            hjp = mk & 8u ? hjp : 0.f;
+            hkm = mk & 16u ? hkm : 0.f;
+            hkp = mk & 32u ? hkp : 0.f;
+        }
+        float sum = 0.f, comp = 0.f;
+        ff_acc(awh[io], awl[io], him, sum, comp);
+        ff_acc(aeh[io], ael[io], hip, sum, comp);
+        ff_acc(ash[jo], asl[jo], hjm, sum, comp);
+        ff_acc(anh[jo], anl[jo], hjp, sum, comp);
+        ff_acc(abh[ko], abl[ko], hkm, sum, comp);
+        ff_acc(ath[ko], atl[ko], hkp, sum, comp);
+        ff_acc(APH[q], APL[q], hc, sum, comp);
+        // (rh + rl) - (sum + comp)
+        float rh, e;
+        two_sum(ldxp<kCoh>(a.RHS + base + q), -sum, rh, e);
+        e = e + (ldxp<kCoh>(a.RHSL + base + q) - comp);
+        float rl;
+        two_sum(rh, e, rh, rl);
+        a.RHS[base + q] = rh;
+        a.RHSL[base + q] = rl;
+        // (dh + dl) + hc
+        float dh, de;
+        two_sum(ldxp<kCoh>(a.DPH + base + q), hc, dh, de);
+        de = de + ldxp<kCoh>(a.DPL + base + q);
+        float dl;
+        two_sum(dh, de, dh, dl);
+        a.DPH[base + q] = dh;
+        a.DPL[base + q] = dl;
+        mx = fmaxf(mx, fabsf(rh));
+    }
+    const double mxd = block_max2((double)mx, sh);
+    if (threadIdx.x == 0) a.gridmax[g] = mxd;
+}
+
 // Outer step (laplacephi + rescal + maxabscal_grid + accumulate_pcorr):
 // rhs <- rhs - A hilf, dp <- dp + hilf, per-grid max|rhs|.  The residual and
 // the accumulated correction are float-float pairs (about 48 significant
@@ -828,7 +954,7 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
     __shared__ double sh[32];
     extern __shared__ __align__(16) unsigned char osm[];
     const Shape s = a.s;
-    const int nj = s.nj, ni = s.ni, nk = s.nk, fs = s.fs, nm = s.nm;
+    const int ni = s.ni, fs = s.fs, nm = s.nm;
     int* spst = reinterpret_cast<int*>(osm);
     short* ro = reinterpret_cast<short*>(spst + nm + 1);
     float* H = reinterpret_cast<float*>(osm + stencil_tables_bytes(nm, ni));   // the grid's hilf
@@ -853,70 +979,189 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
         if (threadIdx.x == 0) atomicExch(a.ctl_err, 1);
         return;
     }
-    const DevGrid G = a.grids[g];
-    const float* APH = a.APX + (long long)a.gcls[g] * 2 * s.npp;
-    const float* APL = APH + s.npp;
-    // 1-D coefficients indexed by io, jo, ko (interior index 3 is io = 0)
-    const float *awh = a.A1[0] + G.ipx + 2, *awl = a.A1L[0] + G.ipx + 2;
-    const float *aeh = a.A1[1] + G.ipx + 2, *ael = a.A1L[1] + G.ipx + 2;
-    const float *ash = a.A1[2] + G.ipy + 2, *asl = a.A1L[2] + G.ipy + 2;
-    const float *anh = a.A1[3] + G.ipy + 2, *anl = a.A1L[3] + G.ipy + 2;
-    const float *abh = a.A1[4] + G.ipz + 2, *abl = a.A1L[4] + G.ipz + 2;
-    const float *ath = a.A1[5] + G.ipz + 2, *atl = a.A1L[5] + G.ipz + 2;
-    float mx = 0.f;      // max |rhs| (its leading float)
-    for (int q = threadIdx.x; q < s.npp; q += blockDim.x) {
-        const int v = s.pq[q];
-        if (v < 0) continue;
-        const int io = v & 1023, jo = (v >> 10) & 1023, ko = v >> 20;
-        const int t = io + jo + ko;
-        // positions of (io, jo, ko-1) on plane t-1 and (io, jo, ko+1) on plane
-        // t+1; the j neighbours sit next to them, the i neighbours one row over
-        const int bm = (ko > 0 || jo > 0) ? spst[t - 1] + ro[(t - 1) * ni + io] + jo : 0;
-        const int bp = (ko < nk - 1 || jo < nj - 1) ? spst[t + 1] + ro[(t + 1) * ni + io] + jo : 0;
-        const float hc = H[q];
-        float him = io > 0 ? H[spst[t - 1] + ro[(t - 1) * ni + io - 1] + jo] : gh[0 * fs + fidx_x(s, ko, jo)];
-        float hip = io < ni - 1 ? H[spst[t + 1] + ro[(t + 1) * ni + io + 1] + jo] : gh[1 * fs + fidx_x(s, ko, jo)];
-        float hjm = jo > 0 ? H[bm - 1] : gh[2 * fs + fidx_y(s, ko, io)];
-        float hjp = jo < nj - 1 ? H[bp + 1] : gh[3 * fs + fidx_y(s, ko, io)];
-        float hkm = ko > 0 ? H[bm] : gh[4 * fs + fidx_z(s, jo, io)];
-        float hkp = ko < nk - 1 ? H[bp] : gh[5 * fs + fidx_z(s, jo, io)];
-        if (a.BM) {   // couplings BP closes contribute nothing (laplacephi's bp products)
-            const unsigned mk = a.BM[base + q];
-            him = mk & 1u ? him : 0.f;
-            hip = mk & 2u ? hip : 0.f;
-            hjm = mk & 4u ? hjm : 0.f;
-            hjp = mk & 8u ? hjp : 0.f;
-            hkm = mk & 16u ? hkm : 0.f;
-            hkp = mk & 32u ? hkp : 0.f;
-        }
-        float sum = 0.f, comp = 0.f;
-        ff_acc(awh[io], awl[io], him, sum, comp);
-        ff_acc(aeh[io], ael[io], hip, sum, comp);
-        ff_acc(ash[jo], asl[jo], hjm, sum, comp);
-        ff_acc(anh[jo], anl[jo], hjp, sum, comp);
-        ff_acc(abh[ko], abl[ko], hkm, sum, comp);
-        ff_acc(ath[ko], atl[ko], hkp, sum, comp);
-        ff_acc(APH[q], APL[q], hc, sum, comp);
-        // (rh + rl) - (sum + comp)
-        float rh, e;
-        two_sum(a.RHS[base + q], -sum, rh, e);
-        e = e + (a.RHSL[base + q] - comp);
-        float rl;
-        two_sum(rh, e, rh, rl);
-        a.RHS[base + q] = rh;
-        a.RHSL[base + q] = rl;
-        // (dh + dl) + hc
-        float dh, de;
-        two_sum(a.DPH[base + q], hc, dh, de);
-        de = de + a.DPL[base + q];
-        float dl;
-        two_sum(dh, de, dh, dl);
-        a.DPH[base + q] = dh;
-        a.DPL[base + q] = dl;
-        mx = fmaxf(mx, fabsf(rh));
+    outer_grid<false>(a, g, H, gh, spst, ro, sh);
+}
+
+// maxabscal over grids + the outer-loop stopping test of mgpoisl
+// (pressuresolver_mod.F90:275,294-301), by one CTA: the largest |rhs| of
+// the grids (scaled to the finest level), the outer count, the converged
+// flag.  The maximum is exact, so the result does not depend on the CTA size.
+template <bool kCoh>
+__device__ __forceinline__ void conv_step(const DevGrid* grids, int ngrid, int maxlevel,
+                                          const double* gridmax, int* ctl, double* maxrhs,
+                                          const double* sprm, double epcorr, int nouter_min,
+                                          double* sh) {
+    const double prefak = sprm[2];
+    double m = 0.0;
+    for (int g = threadIdx.x; g < ngrid; g += blockDim.x) {
+        double gm;
+        if constexpr (kCoh) gm = __ldcg(gridmax + g);
+        else gm = gridmax[g];
+        m = fmax(fabs(gm * ldexp(1.0, maxlevel - grids[g].level)), m);
     }
-    const double mxd = block_max2((double)mx, sh);
-    if (threadIdx.x == 0) a.gridmax[g] = mxd;
+    m = block_max2(m, sh);
+    if (threadIdx.x == 0) {
+        const int done = ctl[1] + 1;
+        ctl[1] = done;
+        maxrhs[0] = m;
+        if (done >= nouter_min && m / prefak < epcorr) ctl[0] = 1;
+    }
+}
+
+__global__ void k_mx_conv(const DevGrid* __restrict__ grids, int ngrid, int maxlevel,
+                          const double* __restrict__ gridmax, int* ctl, double* maxrhs,
+                          const double* __restrict__ sprm, double epcorr, int nouter_min) {
+    if (ctl[0]) return;
+    __shared__ double sh[32];
+    conv_step<false>(grids, ngrid, maxlevel, gridmax, ctl, maxrhs, sprm, epcorr, nouter_min, sh);
+}
+
+// ---- Persistent solve -------------------------------------------------------
+// Every inner iteration, outer step and stopping test of one single-level
+// mgpoisl in one cooperative launch (all CTAs resident).  Each CTA walks its
+// share of the grids phase by phase -- the pre-pass and forward sweep of a
+// grid back to back (the forward sweep reads only its own grid's pre-pass
+// values and older res slots), then the backward sweeps, then the outer
+// step -- with a grid-wide barrier between phases and one more after the
+// stopping test.  The arithmetic per point is that of the per-phase
+// kernels, so the results are the same bits.  Values written inside the
+// launch are read through L2 (ldx<true>).
+
+// A barrier wait gives up after this many nanoseconds (a phase takes well
+// under a millisecond on the largest cases).
+constexpr unsigned long long kBarrierNs = 1000000000ULL;
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Grid-wide barrier number k (1, 2, ...): each CTA adds one arrival to
+// bar[0] and waits until k arrivals per CTA are counted.  Bounded: a CTA
+// that waits longer than kBarrierNs sets bar[1] (abort) and the error flag;
+// a CTA that sees bar[1] stops waiting.  Both return false, and the caller
+// leaves the kernel.
+__device__ __forceinline__ bool grid_sync(unsigned* bar, int* err, unsigned k) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(bar, 1u);
+        const unsigned target = k * gridDim.x;
+        int ok = 1;
+        const unsigned long long t0 = global_ns();
+        while (ld_acquire_u32(bar) < target) {
+            if (ld_acquire_u32(bar + 1) != 0u) {
+                ok = 0;
+                break;
+            }
+            if (global_ns() - t0 > kBarrierNs) {
+                atomicExch(bar + 1, 1u);
+                atomicExch(err, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(64);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+struct SolveArgs {
+    PreArgs pre;
+    FwdArgs fwd;
+    BwdArgs bwd;
+    OuterArgs out;
+    float* rs[3];               // the rotating res slots
+    int ngrid, maxlevel, ninner, nouter, nouter_min;
+    int noconv;                 // run all nouter outer iterations (timing)
+    double epcorr;
+    double* maxrhs;
+    const double* sprm;
+    int* ctl;                   // [0] converged, [1] outer count, [2] error flag
+    unsigned* bar;              // [0] arrivals, [1] abort: zero at launch
+    int skip_cta;               // test switch: this CTA leaves before its first arrival (-1: none)
+};
+
+constexpr int kSolveThreads = 256;
+
+// res slot r (0..2) of the rotation
+__device__ __forceinline__ float* res_slot(const SolveArgs& a, int r) {
+    return r == 0 ? a.rs[0] : (r == 1 ? a.rs[1] : a.rs[2]);
+}
+
+// The solve is one loop over phases, 2 ninner + 2 per outer iteration: the
+// pre-pass and forward sweep of inner iteration il, its backward sweep, ...,
+// the outer step, the stopping test; a grid-wide barrier closes every
+// phase.  Everything a phase needs (inner iteration count, res slots, the
+// last fully exchanged iteration, barrier number) follows from the phase
+// number, so no state is carried across phases in registers.
+template <int kMinBlocks, bool kUni>
+__global__ void __launch_bounds__(kSolveThreads, kMinBlocks) k_sip_solve(const __grid_constant__ SolveArgs a) {
+    extern __shared__ __align__(16) unsigned char ssm[];
+    __shared__ double sh[32];
+    if ((int)blockIdx.x == a.skip_cta) return;
+    const Shape& s = a.out.s;
+    // the outer step's plane tables stay at the front; the phases share the rest
+    int* spst = reinterpret_cast<int*>(ssm);
+    short* ro = reinterpret_cast<short*>(spst + s.nm + 1);
+    unsigned char* work = ssm + stencil_tables_bytes(s.nm, s.ni);
+    for (int q = threadIdx.x; q <= s.nm; q += blockDim.x) spst[q] = s.pst[q];
+    for (int q = threadIdx.x; q < s.nm * s.ni; q += blockDim.x) ro[q] = s.rowoff[q];
+    __syncthreads();
+    const int per = 2 * a.ninner + 2;
+    const int total = a.nouter * per;
+    for (int ph = 0; ph < total; ++ph) {
+        const int io = ph / per, r = ph - io * per;   // outer iteration (0-based), phase in it
+        const int ng = a.ngrid;
+        const bool rev = ph & 1;                       // alternate the walk for L2 reuse
+        if (r < 2 * a.ninner) {
+            const int il = r >> 1;                     // inner iteration (0-based)
+            const int gi = io * a.ninner + il + 1;     // inner iterations since the solve began
+            // the first inner iteration starts from hilf = 0 (accumulate_pcorr
+            // cleared it); iteration gi writes res slot gi % 3
+            const bool hz = il == 0;
+            float* R = res_slot(a, gi % 3);
+            if ((r & 1) == 0) {
+                // low ghosts from the last iteration whose exchange covered every
+                // face: every inner iteration but the last of an outer one
+                const int lastfull = a.ninner < 2 ? 0 : (il > 0 ? gi - 1 : (io > 0 ? gi - 2 : 0));
+                const float* RLOW = lastfull > 0 ? res_slot(a, lastfull % 3) : nullptr;
+                for (int w = blockIdx.x; w < ng; w += gridDim.x) {
+                    const int g = rev ? ng - 1 - w : w;
+                    pre_grid<2, kUni, true>(a.pre, g, reinterpret_cast<float*>(work), R, hz);
+                    __syncthreads();
+                    fwd_grid<2, true>(a.fwd, g, work, R, RLOW);
+                }
+            } else {
+                for (int w = blockIdx.x; w < ng; w += gridDim.x)
+                    bwd_grid<2, true>(a.bwd, rev ? ng - 1 - w : w, work, R, hz);
+            }
+        } else if (r == 2 * a.ninner) {
+            float* gh = reinterpret_cast<float*>(work);
+            for (int w = blockIdx.x; w < ng; w += gridDim.x) {
+                const int g = rev ? ng - 1 - w : w;
+                gather_hilf_ghosts<true>(gh, s, a.out.H, a.out.fnbr + 6 * g, nullptr);
+                __syncthreads();
+                outer_grid<true>(a.out, g, a.out.H + (long long)g * s.npp, gh, spst, ro, sh);
+            }
+        } else if (!a.noconv && blockIdx.x == 0) {
+            conv_step<true>(a.out.grids, ng, a.maxlevel, a.out.gridmax, a.ctl, a.maxrhs, a.sprm,
+                            a.epcorr, a.nouter_min, sh);
+        }
+        if (!grid_sync(a.bar, a.ctl + 2, (unsigned)ph + 1)) return;
+        if (r == per - 1 && !a.noconv && __ldcg(a.ctl) != 0) break;
+    }
 }
 
 // divcal into the plane-ordered FP64/FP32 residual (noib_mod.F90:304-354)
@@ -1166,6 +1411,137 @@ PreArgs pre_args(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ct
     p.UNI = st.uni;
     p.rev = 0;
     return p;
+}
+
+FwdArgs fwd_args(SipState& st, const float* cf, const int* gcls, int* ctl) {
+    FwdArgs a{};
+    a.s = shape(st);
+    a.fnbr = st.d_fnbr; a.gcls = gcls;
+    a.CF = cf;
+    a.ctl = ctl;
+    a.SW = st.swf;
+    return a;
+}
+
+BwdArgs bwd_args(SipState& st, const float* cb, const int* gcls, int* ctl) {
+    BwdArgs a{};
+    a.s = shape(st);
+    a.fnbr = st.d_fnbr; a.gcls = gcls;
+    a.H = st.h32;
+    a.CB = cb;
+    a.ctl = ctl;
+    a.SW = st.swb;
+    return a;
+}
+
+OuterArgs outer_args(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl) {
+    OuterArgs a{};
+    a.s = shape(st);
+    a.PG = st.pg;
+    a.BM = st.bm;
+    a.fnbr = st.d_fnbr; a.gcls = gcls;
+    a.H = st.h32;
+    a.RHS = st.rhs32; a.RHSL = st.rhsl; a.DPH = st.dph; a.DPL = st.dpl; a.APX = apx;
+    for (int q = 0; q < 6; ++q) {
+        a.A1[q] = st.a1[q];
+        a.A1L[q] = st.a1lo[q];
+    }
+    a.grids = c->d_grids;
+    a.gridmax = c->d_gridred;
+    a.ctl = ctl;
+    a.ctl_err = const_cast<int*>(ctl) + 2;
+    return a;
+}
+
+// Persistent-solve variants: minimum CTAs per SM (the register bound) and
+// the uniform-class pre-pass.
+struct SolveVariant {
+    int minblocks;
+    bool uni;
+    const char* name;
+};
+const SolveVariant kSolveVariants[] = {
+    {8, false, "256 threads, 8 CTAs/SM"},         {6, false, "256 threads, 6 CTAs/SM"},
+    {4, false, "256 threads, 4 CTAs/SM"},         {8, true, "256 threads, 8 CTAs/SM, uniform"},
+    {6, true, "256 threads, 6 CTAs/SM, uniform"}, {4, true, "256 threads, 4 CTAs/SM, uniform"},
+};
+constexpr int kNumSolve = (int)(sizeof(kSolveVariants) / sizeof(kSolveVariants[0]));
+
+const void* solve_kernel(int v) {
+    switch (v) {
+        case 0: return (const void*)k_sip_solve<8, false>;
+        case 1: return (const void*)k_sip_solve<6, false>;
+        case 2: return (const void*)k_sip_solve<4, false>;
+        case 3: return (const void*)k_sip_solve<8, true>;
+        case 4: return (const void*)k_sip_solve<6, true>;
+        default: return (const void*)k_sip_solve<4, true>;
+    }
+}
+
+size_t solve_smem(const SipState& st) {
+    return stencil_tables_bytes(st.nm, st.ni) +
+           std::max((size_t)6 * st.fs * 4, rp_nb_offset(st.nm) + 2 * packed_region(st.maxlp, st.fs) * 4);
+}
+
+// CTAs of a cooperative launch of variant v (all resident), at most one per grid
+int solve_ctas(Ctx* c, const SipState& st, int v) {
+    int nb = 0, dev = 0, nsm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, solve_kernel(v), kSolveThreads,
+                                                      solve_smem(st)) != cudaSuccess)
+        return 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    return std::min(nb * nsm, c->ngrid);
+}
+
+// One persistent solve of nouter outer iterations (noconv: no stopping test)
+// on the stream: the barrier counter is cleared first.
+int launch_solve(Ctx* c, SipState& st, int v, const float* cf, const float* apx, const int* gcls,
+                 int* ctl, double* maxrhs, const double* sprm, int nouter, bool noconv, int skip_cta) {
+    const int ctas = solve_ctas(c, st, v);
+    if (ctas <= 0) {
+        set_error("mixed form: the persistent solve does not fit on an SM");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    // barrier counts stay below 2^31
+    const long long nbar = (long long)nouter * (2LL * c->prm.ninner + 2);
+    if (nbar * ctas >= (1LL << 31)) {
+        set_error("mixed form: too many outer iterations for the persistent solve");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    SolveArgs a{};
+    a.pre = pre_args(c, st, cf, gcls, ctl, 0, false);
+    a.fwd = fwd_args(st, cf, gcls, ctl);
+    a.bwd = bwd_args(st, nullptr, gcls, ctl);
+    a.out = outer_args(c, st, apx, gcls, ctl);
+    for (int r = 0; r < 3; ++r) a.rs[r] = st.rs[r];
+    a.ngrid = c->ngrid;
+    a.maxlevel = c->maxlevel;
+    a.ninner = c->prm.ninner;
+    a.nouter = nouter;
+    a.nouter_min = c->prm.nouter_min;
+    a.noconv = noconv ? 1 : 0;
+    a.epcorr = c->prm.epcorr;
+    a.maxrhs = maxrhs;
+    a.sprm = sprm;
+    a.ctl = ctl;
+    a.bar = st.d_bar;
+    a.skip_cta = skip_cta;
+    MG_CUDA(cudaMemsetAsync(st.d_bar, 0, 2 * sizeof(unsigned), c->stream));
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(kSolveThreads);
+    cfg.dynamicSmemBytes = solve_smem(st);
+    cfg.stream = c->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    void* args[] = {&a};
+    MG_CUDA(cudaLaunchKernelExC(&cfg, solve_kernel(v), args));
+    MG_LAUNCHED(c);
+    return 0;
 }
 
 }  // namespace
@@ -1586,7 +1962,7 @@ void sip_release(SipState& st) {
                     (void*)st.d_pcode, (void*)st.spr, (void*)st.uni, (void*)st.a1[0], (void*)st.a1[1],
                     (void*)st.a1[2], (void*)st.a1[3], (void*)st.a1[4], (void*)st.a1[5],
                     (void*)st.a1lo[0], (void*)st.a1lo[1], (void*)st.a1lo[2], (void*)st.a1lo[3],
-                    (void*)st.a1lo[4], (void*)st.a1lo[5], (void*)st.pg, (void*)st.bm})
+                    (void*)st.a1lo[4], (void*)st.a1lo[5], (void*)st.pg, (void*)st.bm, (void*)st.d_bar})
         cudaFree(p);
 }
 
@@ -1720,6 +2096,155 @@ int sip_scatter_dp(Ctx* c, SipState& st) {
                                                c->F("DP"));
     MG_LAUNCHED(c);
     return 0;
+}
+
+int sip_conv(Ctx* c, int* ctl, double* maxrhs, const double* sprm) {
+    ProfScope ps_(c, "mx_conv");
+    k_mx_conv<<<1, 1024, 0, c->stream>>>(c->d_grids, c->ngrid, c->maxlevel, c->d_gridred, ctl,
+                                         maxrhs, sprm, c->prm.epcorr, c->prm.nouter_min);
+    MG_LAUNCHED(c);
+    return 0;
+}
+
+int sip_solve_variants() { return kNumSolve; }
+const char* sip_solve_variant_name(int v) {
+    return v >= 0 && v < kNumSolve ? kSolveVariants[v].name : "per-phase kernels";
+}
+
+bool sip_solve_fits(Ctx* c, const SipState& st, int v) {
+    if (v < 0 || v >= kNumSolve) return false;
+    if (kSolveVariants[v].uni && !st.unicls) return false;
+    return c->minlevel == c->maxlevel && st.prepk && st.packed && !st.pg &&
+           (st.maxlp + 1) / 2 <= kSolveThreads && solve_ctas(c, st, v) > 0;
+}
+
+int sip_solve_alloc(SipState& st) {
+    if (!st.d_bar) MG_CUDA(cudaMalloc(&st.d_bar, 2 * sizeof(unsigned)));
+    return 0;
+}
+
+int sip_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int* gcls, int* ctl,
+              double* maxrhs, const double* sprm) {
+    ProfScope ps_(c, "mx_sip_solve");
+    if (!st.d_bar || !sip_solve_fits(c, st, st.solve_variant)) {
+        set_error("mixed form: the persistent solve is not set up for this case");
+        return MGLET_ERR_UNSUPPORTED;
+    }
+    const int skip = st.solve_skip ? 0 : -1;
+    st.solve_skip = false;
+    return launch_solve(c, st, st.solve_variant, cf, apx, gcls, ctl, maxrhs, sprm, c->prm.nouter,
+                        false, skip);
+}
+
+// Times two outer iterations of the per-phase kernels (the variants the
+// tuner kept) against each persistent variant, without stopping tests, and
+// keeps the persistent solve only if it is faster.
+int sip_tune_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int* gcls,
+                   int* ctl, double* maxrhs, const double* sprm) {
+    st.solve_variant = -1;
+    for (int v = 0; v < kNumSolve; ++v) st.solve_var_ms[v] = 0.0;
+    bool any = false;
+    for (int v = 0; v < kNumSolve; ++v) any = any || sip_solve_fits(c, st, v);
+    if (!any) return 0;
+    static std::map<std::vector<long long>, std::tuple<int, double, double, std::vector<double>>> cache;
+    const std::vector<long long> key = {st.kk, st.jj, st.ii, c->ngrid, st.unicls ? 1 : 0,
+                                        c->prm.ninner, st.bm ? 1 : 0};
+    auto it = cache.find(key);
+    if (it != cache.end()) {
+        st.solve_variant = std::get<0>(it->second);
+        st.solve_ms = std::get<1>(it->second);
+        st.phases_ms = std::get<2>(it->second);
+        for (int v = 0; v < kNumSolve; ++v) st.solve_var_ms[v] = std::get<3>(it->second)[v];
+        if (st.solve_variant >= 0) return sip_solve_alloc(st);
+        return 0;
+    }
+    if (int rc = sip_solve_alloc(st)) return rc;
+    const int nouter = 2;
+    cudaEvent_t e0, e1;
+    MG_CUDA(cudaEventCreate(&e0));
+    MG_CUDA(cudaEventCreate(&e1));
+    auto elapsed = [&](float* ms) -> cudaError_t {
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+        return e;
+    };
+    auto done = [&](cudaError_t e, const char* what) -> int {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return e == cudaSuccess ? 0 : cuda_fail(e, what);
+    };
+    auto quit = [&](int rc) -> int {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        return rc;
+    };
+    MG_CUDA(cudaMemsetAsync(ctl, 0, 3 * sizeof(int), c->stream));
+    // the per-phase form: nouter x (ninner x (pre, forward, backward), outer)
+    auto phases = [&]() -> int {
+        int gi = 0, lastfull = 0;
+        for (int o = 0; o < nouter; ++o) {
+            for (int il = 1; il <= c->prm.ninner; ++il) {
+                ++gi;
+                const int rlow = lastfull > 0 ? lastfull % 3 : -1;
+                if (int rc = sip_forward(c, st, cf, gcls, ctl, rlow, gi % 3, il == 1)) return rc;
+                if (int rc = sip_backward(c, st, nullptr, gcls, ctl, gi % 3, il == 1)) return rc;
+                if (il < c->prm.ninner) lastfull = gi;
+            }
+            if (int rc = sip_outer(c, st, apx, gcls, ctl)) return rc;
+        }
+        return 0;
+    };
+    if (int rc = phases()) return quit(rc);
+    MG_CUDA(cudaEventRecord(e0, c->stream));
+    if (int rc = phases()) return quit(rc);
+    MG_CUDA(cudaEventRecord(e1, c->stream));
+    float pms = 0.f;
+    if (cudaError_t e = elapsed(&pms)) return done(e, "sip_tune_solve");
+    st.phases_ms = pms / nouter;
+    int best = -1;
+    double best_ms = st.phases_ms;
+    double best_solve = 1e30;
+    for (int v = 0; v < kNumSolve; ++v) {
+        if (!sip_solve_fits(c, st, v)) continue;
+        // a refused launch (not all CTAs resident) leaves this variant out
+        if (launch_solve(c, st, v, cf, apx, gcls, ctl, maxrhs, sprm, nouter, true, -1)) {
+            cudaGetLastError();
+            MG_CUDA(cudaStreamSynchronize(c->stream));
+            continue;
+        }
+        MG_CUDA(cudaEventRecord(e0, c->stream));
+        if (launch_solve(c, st, v, cf, apx, gcls, ctl, maxrhs, sprm, nouter, true, -1)) {
+            cudaGetLastError();
+            MG_CUDA(cudaStreamSynchronize(c->stream));
+            continue;
+        }
+        MG_CUDA(cudaEventRecord(e1, c->stream));
+        float ms = 0.f;
+        if (cudaError_t e = elapsed(&ms)) return done(e, "sip_tune_solve: persistent");
+        int flag = 0;
+        MG_CUDA(cudaMemcpy(&flag, ctl + 2, sizeof(int), cudaMemcpyDeviceToHost));
+        if (flag) {   // a barrier wait ran out: keep the per-phase kernels
+            MG_CUDA(cudaMemset(ctl, 0, 3 * sizeof(int)));
+            continue;
+        }
+        const double per = ms / nouter;
+        st.solve_var_ms[v] = per;
+        best_solve = std::min(best_solve, per);
+        if (per < best_ms) {
+            best_ms = per;
+            best = v;
+        }
+    }
+    st.solve_variant = best;
+    st.solve_ms = best_solve < 1e30 ? best_solve : 0.0;
+    cache[key] = {best, st.solve_ms, st.phases_ms,
+                  std::vector<double>(st.solve_var_ms, st.solve_var_ms + kNumSolve)};
+    // the timing runs wrote the solver's arrays; leave them zeroed
+    for (float* p : {st.rs[0], st.rs[1], st.rs[2], st.h32, st.rhs32, st.rhsl, st.dph, st.dpl})
+        MG_CUDA(cudaMemsetAsync(p, 0, (size_t)c->ngrid * st.npp * sizeof(float), c->stream));
+    MG_CUDA(cudaMemsetAsync(ctl, 0, 3 * sizeof(int), c->stream));
+    return done(cudaSuccess, "");
 }
 
 }  // namespace mg

@@ -60,6 +60,15 @@ struct SipState {
     // ghost-cell IB: per grid and padded position the open couplings (bit f
     // for faces i-1, i+1, j-1, j+1, k-1, k+1), null without the IB
     unsigned char* bm = nullptr;
+    // persistent solve (one cooperative launch per mgpoisl): its variant
+    // (-1: the per-phase kernels), the tuner's times of one outer iteration
+    // in it and in the per-phase kernels, the barrier words [arrivals,
+    // abort], and the test switch that makes its first barrier wait run out
+    int solve_variant = -1;
+    double solve_ms = 0.0, phases_ms = 0.0;
+    double solve_var_ms[6] = {0, 0, 0, 0, 0, 0};   // each variant's time (0: not run)
+    unsigned* d_bar = nullptr;
+    bool solve_skip = false;
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
@@ -91,5 +100,21 @@ const char* sip_pre_variant_name(int v);
 bool sip_pre_variant_uniform(int v);
 int sip_sweep_variants();
 const char* sip_sweep_variant_name(int v);
+// maxabscal over the grids and the outer-loop stopping test (one CTA)
+int sip_conv(Ctx* c, int* ctl, double* maxrhs, const double* sprm);
+// The persistent solve: every inner iteration, outer step and stopping test
+// of one single-level mgpoisl in one cooperative launch, the same bits as the
+// per-phase kernels.  fits: variant v can run on this case (one level, the
+// packed pre-pass and sweeps, planes of at most 512 points).
+int sip_solve_variants();
+const char* sip_solve_variant_name(int v);
+bool sip_solve_fits(Ctx* c, const SipState& st, int v);
+int sip_solve_alloc(SipState& st);
+int sip_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int* gcls, int* ctl,
+              double* maxrhs, const double* sprm);
+// Times the persistent variants against the per-phase kernels (which the
+// tuner must have picked already) and keeps the faster form.
+int sip_tune_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int* gcls,
+                   int* ctl, double* maxrhs, const double* sprm);
 
 }  // namespace mg

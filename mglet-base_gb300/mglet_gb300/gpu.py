@@ -36,7 +36,8 @@ EXPORTS = [
     "mglet_gpu_add_scalar_source", "mglet_gpu_fp64_roof", "mglet_gpu_tuning",
     "mglet_gpu_force_variant", "mglet_create_flowstencils", "mglet_flowstencils_size",
     "mglet_flowstencils_copy", "mglet_flowstencils_free", "mglet_gpu_set_partition",
-    "mglet_gpu_test_wait_timeout", "mglet_mesh_create", "mglet_mesh_distance", "mglet_mesh_free",
+    "mglet_gpu_test_wait_timeout", "mglet_gpu_test_barrier_timeout", "mglet_mesh_create",
+    "mglet_mesh_distance", "mglet_mesh_free",
 ]
 
 
@@ -119,6 +120,7 @@ def load(path=None):
     L.mglet_gpu_tuning.argtypes = [vp, cp, C.c_int64]
     L.mglet_gpu_force_variant.argtypes = [vp, cp, C.c_int32]
     L.mglet_gpu_test_wait_timeout.argtypes = [vp]
+    L.mglet_gpu_test_barrier_timeout.argtypes = [vp]
     L.mglet_mesh_create.argtypes = [vp, C.c_int64, C.POINTER(vp)]
     L.mglet_mesh_distance.argtypes = [vp, vp, C.c_int64, vp, vp]
     L.mglet_mesh_free.argtypes = [vp]
@@ -390,12 +392,15 @@ class Solver:
                                               len(recv), recv.ctypes.data, fnp, None))
 
     def tuning(self):
-        buf = C.create_string_buffer(512)
+        buf = C.create_string_buffer(2048)
         _check(load().mglet_gpu_tuning(self.h, buf, len(buf)))
         return buf.value.decode()
 
     def test_wait_timeout(self):
         _check(load().mglet_gpu_test_wait_timeout(self.h))
+
+    def test_barrier_timeout(self):
+        _check(load().mglet_gpu_test_barrier_timeout(self.h))
 
     def force_variant(self, kernel, variant):
         _check(load().mglet_gpu_force_variant(self.h, kernel.encode(), variant))
