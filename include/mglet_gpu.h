@@ -72,8 +72,9 @@ enum {
      * CUDA graph with a device-side convergence flag.  Runs grids of equal
      * dimensions with CON, CO1, FIX, NOS, SLI, PAR (hierarchies, SIP on
      * every level) and OP1 faces (OP1 on the high faces 2, 4, 6), with or
-     * without the ghost-cell IB (BP of 0 or 1); LES models stay with the
-     * plain form. */
+     * without the ghost-cell IB (BP of 0 or 1), and with an LES model or a
+     * caller-set viscosity field G (the fluxes then read G at every point;
+     * the LES model itself runs in FP64). */
     MGLET_FORM_MIXED = 1
 };
 
@@ -289,7 +290,7 @@ int mglet_gpu_ctof(mglet_ctx* ctx, int32_t ilevel, const char* ff, const char* f
  * the fine mean next to the face; with_bp selects the BP-weighted form
  * (the reference passes bp for the ghost-cell IB only). */
 int mglet_gpu_bound_pressure(mglet_ctx* ctx, int32_t ilevel, const char* dp, int32_t with_bp);
-/* The LES model of the stage (lesmodel_mod.F90:34-84, plain form): 0 none,
+/* The LES model of the stage (lesmodel_mod.F90:34-84, both forms): 0 none,
  * 1 smagorinsky, 2 wale, 5 sigma; cm < 0 takes the model's default
  * constant.  Computes G of the current velocity at once, as
  * init_lesmodel does; the stage then updates G after the pressure solve and

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "internal.h"
+#include "mixed.h"
 
 namespace mg {
 namespace {
@@ -238,11 +239,10 @@ int set_lesmodel(Ctx* c, int model, double cm) {
         set_error("set_lesmodel: model 0 (none), 1 (smagorinsky), 2 (wale) or 5 (sigma)");
         return MGLET_ERR_ARG;
     }
-    if (model != 0 && c->prm.form != MGLET_FORM_PLAIN) {
-        set_error("set_lesmodel: the LES models run in the plain form");
-        return MGLET_ERR_UNSUPPORTED;
-    }
     c->ilesmodel = model;
+    // the mixed form's fluxes read G at every point from now on, and the
+    // captured stage is rebuilt with (or without) the LES model's steps
+    if (c->prm.form == MGLET_FORM_MIXED) mixed_g_field(c);
     c->cm = cm < 0.0 ? (model == 1 ? (double)0.1f : (model == 2 ? 0.5 : (double)1.35f)) : cm;
     if (model == 0) return init_viscosity(c);
     if (!c->f3.count("LESD")) {

@@ -37,6 +37,7 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
                    const float* sz, const double* sprm, int* err, bool skip);
 bool mx_flux_has_tma(Ctx* c);
 int mx_flux_set_pw(Ctx* c, const unsigned char* d_pw);
+void mx_flux_set_gfield(Ctx* c);
 int mx_flux_prepare(Ctx* c);
 void mx_flux_release(Ctx* c);
 int mx_flux_tune(Ctx* c, float* du, float* dv, float* dw, const float* sx, const float* sy,
@@ -58,7 +59,6 @@ struct MixedState {
     float *du32 = nullptr, *dv32 = nullptr, *dw32 = nullptr;
     // FP32 spacing tables per axis: d, dd, rd, rdd, d(i)/dd(i+1), d(i-1)/dd(i)
     float *sx = nullptr, *sy = nullptr, *sz = nullptr;
-    bool g_uniform = true;
     bool walls = false;             // some grid has a FIX, OP1, NOS or SLI face
     LevelState lv;                  // hierarchies: per-level lists (set up at the first stage)
     // device control block: [0] converged flag, [1] outer iterations done
@@ -273,12 +273,13 @@ int set_stage_scalars(Ctx* c, double frhs, double dtfu, double dtsolve) {
     return 0;
 }
 
+// The stage after the fluxes and the RK update: the connects, parent and
+// bound_flow of each level, the pressure solve, and the LES model's G for
+// the next stage (timeintegration_mod.F90:117-125).
+static int enqueue_after_rk(Ctx* c);
+
 int enqueue_stage(Ctx* c) {
     MixedState* m = c->mx;
-    if (!m->g_uniform) {
-        set_error("mixed form: needs a uniform viscosity field G = gmol (no LES model)");
-        return MGLET_ERR_UNSUPPORTED;
-    }
     const bool skip = m->skip_once;
     m->skip_once = false;
     // ghost-cell IB: which grids' point values differ from U, V, W now (the
@@ -303,22 +304,31 @@ int enqueue_stage(Ctx* c) {
         if (int rc = launch_maskbp(c, U, V, W, P)) return rc;
         if (int rc = launch_gc_mode(c, 'R', U, V, W)) return rc;
     }
+    return enqueue_after_rk(c);
+}
+
+static int enqueue_after_rk(Ctx* c) {
+    MixedState* m = c->mx;
+    double *U = c->F("U"), *V = c->F("V"), *W = c->F("W"), *P = c->F("P");
     if (c->minlevel == c->maxlevel) {
         if (int rc = connect(c, 0, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
         // timeintegration_mod.F90:117-122: bound_flow after the connect
         if (m->walls)
             if (int rc = launch_bound_flow(c, U, V, W, P, 0)) return rc;
-        return enqueue_mgpoisl(c);
+    } else {
+        // timeintegration_mod.F90:117-122: per level connect, parent, bound_flow
+        static const char* const vn[3] = {"U", "V", "W"};
+        static const char* const sn[3] = {"P", nullptr, nullptr};
+        for (int l = c->minlevel; l <= c->maxlevel; ++l) {
+            if (int rc = connect(c, l, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
+            if (int rc = launch_parent(c, l, vn, sn, false)) return rc;
+            if (int rc = launch_bound_flow(c, U, V, W, P, l)) return rc;
+        }
     }
-    // timeintegration_mod.F90:117-122: per level connect, parent, bound_flow
-    static const char* const vn[3] = {"U", "V", "W"};
-    static const char* const sn[3] = {"P", nullptr, nullptr};
-    for (int l = c->minlevel; l <= c->maxlevel; ++l) {
-        if (int rc = connect(c, l, 1, U, V, W, nullptr, nullptr, nullptr, false, true, 1)) return rc;
-        if (int rc = launch_parent(c, l, vn, sn, false)) return rc;
-        if (int rc = launch_bound_flow(c, U, V, W, P, l)) return rc;
-    }
-    return enqueue_mgpoisl(c);
+    if (int rc = enqueue_mgpoisl(c)) return rc;
+    // timeintegration_mod.F90:125: the LES model's G from the new velocity
+    // (FP64, the plain kernels), read by the next stage's fluxes
+    return lesmodel(c);
 }
 
 // 0, or MGLET_ERR_CUDA when a kernel gave up waiting for its bulk copies or
@@ -628,10 +638,22 @@ void mixed_release(Ctx* c) {
 // A field was uploaded: the FP32 RK registers follow DU/DV/DW, and a
 // viscosity field that is not the uniform gmol takes the stage off the
 // mixed path (LES models are outside this form).
+// G becomes a field the fluxes read (an LES model, or a G the caller set):
+// the stage graph holds the uniform-viscosity flux launch, so it is dropped.
+void mixed_g_field(Ctx* c) {
+    MixedState* m = c->mx;
+    if (!m) return;
+    mx_flux_set_gfield(c);
+    if (m->graph) {
+        cudaGraphExecDestroy(m->graph);
+        m->graph = nullptr;
+    }
+}
+
 void mixed_field_changed(Ctx* c, const char* name) {
     MixedState* m = c->mx;
     if (!m) return;
-    if (!std::strcmp(name, "G")) m->g_uniform = false;
+    if (!std::strcmp(name, "G")) mixed_g_field(c);
     if (float* f = du_buffer(c, name)) {
         k_cvt_64_32<<<(unsigned)((c->idim3d + 255) / 256), 256, 0, c->stream>>>(f, c->F(name), c->idim3d);
         cudaStreamSynchronize(c->stream);
@@ -735,10 +757,6 @@ int mixed_stage(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk, mglet_sta
     MixedState* m = c->mx;
     double frhs, fu, dtrk, dtrki;
     if (int rc = rk_coeffs(rk, irk, &frhs, &fu, &dtrk, &dtrki)) return rc;
-    if (!m->g_uniform) {
-        set_error("mixed form: needs a uniform viscosity field G = gmol (no LES model)");
-        return MGLET_ERR_UNSUPPORTED;
-    }
     if (int rc = levels_ready(c)) return rc;
     const bool gc = c->ibtype == 1;
     // timeintegration_mod.F90:96-99: the ghost-cell values of the step, issued

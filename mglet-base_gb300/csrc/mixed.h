@@ -17,6 +17,8 @@ std::string mixed_tuning(Ctx* c);
 int mixed_force_variant(Ctx* c, const char* kernel, int v);
 int mixed_test_wait_timeout(Ctx* c);
 int mixed_test_barrier_timeout(Ctx* c);
+// G is a field from now on (LES model or a caller-set G)
+void mixed_g_field(Ctx* c);
 // the ghost-cell IB (after mglet_gpu_set_ghostcell's plain set-up)
 int mixed_ghostcell(Ctx* c);
 

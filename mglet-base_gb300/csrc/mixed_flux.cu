@@ -99,6 +99,9 @@ struct FluxArgs {
     // per grid {1, h2} where G is one value on the box 2..n-1: the uniform
     // face viscosities hold there too
     const double* guni;
+    int gall;                          // G is a field (LES or uploaded): every point of a grid
+                                       // whose G is not one value reads it
+    int iles;                          // an LES model is on: tstle4_diff's cross term
     int* err;                          // set when a bulk-copy wait gives up
     int skip_plane;                    // test switch: this plane's copy is not issued (0: none)
     int nslab;                         // j-slabs (CTAs) per grid
@@ -174,6 +177,15 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
         const float fdx_i = DX(i), fddx = DDX(i), rdx_i = RDX(i), rdx_im = RDX(i - 1);
         const float rddx_i = RDDX(i), rddx_ip = RDDX(i + 1), rx1 = RX1(i), rx0 = RX0(i);
         const float fdy_j = dy_j, fddy = ddy_j, fdz_k = dz_k, fddz = ddz_k;
+        // the transported velocities (the point values under the ghost-cell
+        // IB), which the LES cross term differentiates
+        const float2* tu_m = kPW ? xu + sm1 * plane : u_m;
+        const float2* tu_0 = kPW ? xu + s0 * plane : u_0;
+        const float2* tv_0 = kPW ? xv + s0 * plane : v_0;
+        const float2* tv_p = kPW ? xv + sp1 * plane : v_p;
+        const float2* tw_0 = kPW ? xw + s0 * plane : w_0;
+        const float2* tw_p = kPW ? xw + sp1 * plane : w_p;
+        const bool cross = kW && a.iles;
         // ---------------- U at (k, j, i+1/2)
         {
             // transporting U along x (mass fluxes fe, fw), transported u
@@ -212,9 +224,15 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                                 : -g * ax * (rddx_ip * dE + rddx_i * dW) -
                                       gh * ay * (rdy_j * dN + rdy_jm * dS) -
                                       gh * az * (rdz_k * dT + rdz_km * dB);
+            // the LES cross term of tstle4_diff (src/flow/tstle4_mod.F90:268-458)
+            float qc = 0.f;
+            if (cross)
+                qc = (vs.u.e * dE * rddx_ip + vs.u.w * dW * rddx_i) * ax +
+                     (vs.u.n * dif(tv_p[q], tv_0[q]) - vs.u.s * dif(tv_p[qs], tv_0[qs])) * fddz +
+                     (vs.u.t * dif(tw_p[q], tw_0[q]) - vs.u.b * dif(tw_p[qb], tw_0[qb])) * fddy;
             const float fak = a.rrho * vol;
             const float gp = (dif(p_p[q], p_0[q]) + a.gpx * gfl * fdx_i) * (a.rrho / fdx_i);
-            uo = conv - fak * qd - gp;
+            uo = conv - fak * (qd - qc) - gp;
         }
         // ---------------- V at (k, j+1/2, i)
         {
@@ -254,9 +272,14 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                                 : -gh * ax * (rdx_i * dE + rdx_im * dW) -
                                       g * ay * (rddy_jp * dN + rddy_j * dS) -
                                       gh * az * (rdz_k * dT + rdz_km * dB);
+            float qc = 0.f;
+            if (cross)
+                qc = (vs.v.e * dif(tu_0[qn], tu_0[q]) - vs.v.w * dif(tu_m[qn], tu_m[q])) * fddz +
+                     (vs.v.n * dN * rddy_jp + vs.v.s * dS * rddy_j) * ay +
+                     (vs.v.t * dif(tw_0[qn], tw_0[q]) - vs.v.b * dif(tw_0[qb + pk], tw_0[qb])) * fddx;
             const float fak = a.rrho * vol;
             const float gp = (dif(p_0[qn], p_0[q]) + a.gpy * gfl * fdy_j) * (a.rrho / fdy_j);
-            vo = conv - fak * qd - gp;
+            vo = conv - fak * (qd - qc) - gp;
         }
         // ---------------- W at (k+1/2, j, i)
         {
@@ -296,9 +319,14 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                                 : -gh * ax * (rdx_i * dE + rdx_im * dW) -
                                       gh * ay * (rdy_j * dN + rdy_jm * dS) -
                                       g * az * (rddz_kp * dT + rddz_k * dB);
+            float qc = 0.f;
+            if (cross)
+                qc = (vs.w.e * dif(tu_0[qt], tu_0[q]) - vs.w.w * dif(tu_m[qt], tu_m[q])) * fddy +
+                     (vs.w.n * dif(tv_0[qt], tv_0[q]) - vs.w.s * dif(tv_0[qs + 1], tv_0[qs])) * fddx +
+                     (vs.w.t * dT * rddz_kp + vs.w.b * dB * rddz_k) * az;
             const float fak = a.rrho * vol;
             const float gp = (dif(p_0[qt], p_0[q]) + a.gpz * gfl * fdz_k) * (a.rrho / fdz_k);
-            wo = conv - fak * qd - gp;
+            wo = conv - fak * (qd - qc) - gp;
         }
 }
 
@@ -357,13 +385,14 @@ __device__ __forceinline__ bool has_par_face(const DevGrid& G) {
     return w;
 }
 
-// The face viscosities of the point: from G on the outermost interior layer
-// of a grid whose G is not one value (wv: a wall's zero ghosts), else the
-// uniform ones.
+// The face viscosities of the point on a grid whose G is not one value (wv):
+// from G at every point when G is a field (LES, or a G the caller set), else
+// on the outermost interior layer only (a wall's zero ghosts); the uniform
+// ones otherwise.
 __device__ __forceinline__ Visc3 visc_at(const FluxArgs& a, const DevGrid& G, bool wv, int k, int j,
                                          int i) {
     const bool shell = i == 3 || i == G.ii - 2 || j == 3 || j == G.jj - 2 || k == 3 || k == G.kk - 2;
-    if (wv && shell) return visc_field(a.G + G.ip3, G.kk, G.jj, k, j, i, (float)a.wgmol);
+    if (wv && (a.gall || shell)) return visc_field(a.G + G.ip3, G.kk, G.jj, k, j, i, (float)a.wgmol);
     return visc_uniform(a);
 }
 
@@ -514,7 +543,7 @@ __global__ void __launch_bounds__(576, 2) k_mx_flux(FluxArgs a) {
     const float gfl = (float)G.gradpflag;
     const bool wg = kW && has_open_face(G);
     const bool pgrid = kW && has_par_face(G);
-    const bool wv = wg && !(a.guni && a.guni[2 * (blockIdx.x / a.nslab)] != 0.0);
+    const bool wv = (wg || (kW && a.gall)) && !(a.guni && a.guni[2 * (blockIdx.x / a.nslab)] != 0.0);
     for (int i = 3; i <= ii - 2; ++i) {
         float uo = 0.f, vo = 0.f, wo = 0.f;
         if (on) {
@@ -728,7 +757,7 @@ __global__ void __launch_bounds__(576, 2)
     const float gfl = (float)G.gradpflag;
     const bool wg = kW && has_open_face(G);
     const bool pgrid = kW && has_par_face(G);
-    const bool wv = wg && !(a.guni && a.guni[2 * gid] != 0.0);
+    const bool wv = (wg || (kW && a.gall)) && !(a.guni && a.guni[2 * gid] != 0.0);
     for (int i = 3; i <= ii - 2; ++i) {
         float uo = 0.f, vo = 0.f, wo = 0.f;
         if (on) {
@@ -794,6 +823,7 @@ struct FluxState {
     CUtensorMap map[4];
     bool tma = false;
     bool walls = false;     // some grid has a face that is not CON: the boundary path
+    bool gfield = false;    // G is a field: the boundary instantiation, G at every point
     // ghost-cell IB: per-grid flags of the grids whose transported velocities
     // are the point values (the plane-load kernel then carries their windows)
     const unsigned char* d_pw = nullptr;
@@ -877,19 +907,22 @@ int mx_flux_prepare(Ctx* c) {
 
 void mx_flux_release(Ctx* c) { g_flux.erase(c); }
 
+void mx_flux_set_gfield(Ctx* c) { g_flux[c].gfield = true; }
+
 static int launch_variant(Ctx* c, int v, const FluxArgs& a, int threads) {
     const DevGrid& G0 = c->grids[0];
     FluxState& fs = g_flux[c];
     const size_t tsm = flux_tma_smem(G0), psm = flux_smem(G0, fs.d_pw != nullptr);
     const unsigned nb = (unsigned)(c->ngrid * a.nslab);
+    const bool kw = fs.walls || fs.gfield;
     if (v == 1 && fs.tma && !fs.d_pw) {
-        if (fs.walls)
+        if (kw)
             k_mx_flux_tma<true><<<c->ngrid, threads, tsm, c->stream>>>(a, fs.map[0], fs.map[1],
                                                                       fs.map[2], fs.map[3]);
         else
             k_mx_flux_tma<false><<<c->ngrid, threads, tsm, c->stream>>>(a, fs.map[0], fs.map[1],
                                                                        fs.map[2], fs.map[3]);
-    } else if (fs.walls) {
+    } else if (kw) {
         k_mx_flux<true><<<nb, threads, psm, c->stream>>>(a);
     } else {
         k_mx_flux<false><<<nb, threads, psm, c->stream>>>(a);
@@ -931,6 +964,8 @@ static FluxArgs flux_args(Ctx* c, float* du, float* dv, float* dw, const float* 
     a.PV0 = c->f3.count("PWV") ? c->F("PWV") : nullptr;
     a.PW0 = c->f3.count("PWW") ? c->F("PWW") : nullptr;
     a.guni = c->d_guni;
+    a.gall = g_flux[c].gfield ? 1 : 0;
+    a.iles = c->ilesmodel != 0 ? 1 : 0;
     a.ddx = c->L("DDX"); a.ddy = c->L("DDY"); a.ddz = c->L("DDZ");
     a.wwx = c->L("WWX"); a.wwy = c->L("WWY"); a.wwz = c->L("WWZ");
     const double rho = c->prm.rho, cwa = 8.3, cwb = 1.0 / 7.0;
@@ -1004,7 +1039,7 @@ int launch_mx_flux(Ctx* c, float* du, float* dv, float* dw, const float* sx, con
     FluxArgs a = flux_args(c, du, dv, dw, sx, sy, sz, sprm, err, &threads);
     const FluxState& fs = g_flux[c];
     // the boundary instantiation reads G only on grids where it is not one value
-    if (fs.walls)
+    if (fs.walls || fs.gfield)
         if (int rc = launch_g_uniform(c)) return rc;
     if (skip && fs.tma) {
         a.skip_plane = 4;

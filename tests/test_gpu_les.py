@@ -99,13 +99,6 @@ def test_les_turbulent_walls(gpu_lib, oracle_lib, model):
         assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max(), n
 
 
-def test_mixed_form_refuses_les(gpu_lib):
-    case = cases.periodic_box(2, 2, 2, n=8)
-    s = gpu_lib.Solver(case, _prm(form=abi.FORM_MIXED, nouter_min=0))
-    with pytest.raises(gpu_lib.MgletError):
-        s.set_lesmodel(1)
-
-
 def test_sigma_model(gpu_lib, oracle_lib):
     """The sigma model takes pow, acos and cos, CUDA's on the GPU and the C
     library's in the oracle: G and three stages agree to a relative 1e-10."""
@@ -126,3 +119,76 @@ def test_sigma_model(gpu_lib, oracle_lib):
     for n in ("U", "V", "W", "P"):
         a, b = gs.get(n), o.get(n)
         assert np.abs(a - b).max() <= 1e-10 * np.abs(b).max(), n
+
+
+def _converged(a, b):
+    """Relative L2 of a - b over the interior (pressure: mean removed)."""
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("model", [1, 2, 5])
+@pytest.mark.parametrize("name", list(CASES))
+def test_mixed_form_with_les(gpu_lib, oracle_lib, model, name):
+    """The batched mixed form with an LES model against the FP64 oracle: the
+    LES kernel (FP64) sets G after every pressure solve, and the FP32 fluxes
+    read the face viscosities of tstle4_diff from G at every point.  Two RK3
+    steps with the outer loop converged on both sides: velocity to relative
+    L2 <= 1e-7, pressure (mean removed) and G to 1e-5."""
+    case = CASES[name]()
+    fields = _fields(case)
+    kw = dict(gmol=GMOL[name], epcorr=1e-11, nouter=40, nouter_min=0)
+    gs = gpu_lib.Solver(case, _prm(form=abi.FORM_MIXED, **kw))
+    o = oracle_lib.Oracle(case, _prm(**kw))
+    for s in (gs, o):
+        for n, a in fields.items():
+            s.set(n, a)
+        s.connect(0, 2, "U", "V", "W", "P", corners=True)
+        s.set_lesmodel(model)
+    # sigma takes pow, acos and cos: CUDA's against the C library's
+    eg0 = _converged(gs.get("G"), o.get("G"))
+    print(f"G of set_lesmodel({model}) {name}: {eg0:.3e}")
+    assert eg0 <= 1e-9, eg0
+    rkg, rko = gpu_lib.rk_scheme("williamson"), oracle_lib.rk_scheme("williamson")
+    for it in (1, 2):
+        for irk in (1, 2, 3):
+            sg = gs.timeintegrate_flow(it, it, 0.0, 5e-3, irk, rkg)
+            o.timeintegrate_flow(it, it, 0.0, 5e-3, irk, rko)
+            assert np.isfinite(sg.maxrhs)
+    iv = [case.interior(gs.get(n)) for n in "UVW"]
+    ov = [case.interior(o.get(n)) for n in "UVW"]
+    ev = float(np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(iv, ov)) / sum(np.sum(b ** 2) for b in ov)))
+    pg, po = case.interior(gs.get("P")), case.interior(o.get("P"))
+    ep = _converged(pg - pg.mean(), po - po.mean())
+    eg = _converged(case.interior(gs.get("G")), case.interior(o.get("G")))
+    print(f"mixed LES model {model} {name}: velocity {ev:.3e}, pressure {ep:.3e}, G {eg:.3e}")
+    assert ev <= 1e-7, ev
+    assert ep <= 1e-5, ep
+    assert eg <= 1e-5, eg
+    gs.close()
+
+
+def test_mixed_form_with_a_viscosity_field(gpu_lib, oracle_lib):
+    """A G field set by the caller (no LES model) in the mixed form: the
+    fluxes read it at every point; against the FP64 oracle as above."""
+    case = CASES["periodic"]()
+    fields = _fields(case)
+    rng = np.random.default_rng(5)
+    fields["G"] = 1e-3 * (1.0 + 0.5 * rng.random(case.idim3d))
+    kw = dict(gmol=1e-3, epcorr=1e-11, nouter=40, nouter_min=0)
+    gs = gpu_lib.Solver(case, _prm(form=abi.FORM_MIXED, **kw))
+    o = oracle_lib.Oracle(case, _prm(**kw))
+    for s in (gs, o):
+        for n, a in fields.items():
+            s.set(n, a)
+        s.connect(0, 2, "U", "V", "W", "P", corners=True)
+        s.connect(0, 2, s1="G", corners=True)
+    rkg, rko = gpu_lib.rk_scheme("williamson"), oracle_lib.rk_scheme("williamson")
+    for irk in (1, 2, 3):
+        gs.timeintegrate_flow(1, 1, 0.0, 5e-3, irk, rkg)
+        o.timeintegrate_flow(1, 1, 0.0, 5e-3, irk, rko)
+    iv = [case.interior(gs.get(n)) for n in "UVW"]
+    ov = [case.interior(o.get(n)) for n in "UVW"]
+    ev = float(np.sqrt(sum(np.sum((a - b) ** 2) for a, b in zip(iv, ov)) / sum(np.sum(b ** 2) for b in ov)))
+    print(f"mixed, caller-set G: velocity {ev:.3e}")
+    assert ev <= 1e-7, ev
+    gs.close()
