@@ -185,9 +185,9 @@ DT = 5e-4
 
 def flow_params(form):
     from mglet_gb300 import abi
+    forms = {"mixed": abi.FORM_MIXED, "plain": abi.FORM_PLAIN, "plain_fma": abi.FORM_PLAIN_FMA}
     return abi.make_flow_params(gmol=1.0 / 1600, rho=1.0, epcorr=1e-10, nouter=9, ninner=5,
-                                nouter_min=0,
-                                form=abi.FORM_MIXED if form == "mixed" else abi.FORM_PLAIN)
+                                nouter_min=0, form=forms[form])
 
 
 class Clocks:
@@ -477,6 +477,7 @@ def kernel_roofs(kern, case, ninner, fp64=None):
 
 
 def run_ours(args, rank, world, local):
+    import numpy as np
     import torch
 
     torch.cuda.set_device(local)
@@ -522,6 +523,7 @@ def run_ours(args, rank, world, local):
     plain = None
     if args.form == "mixed" and not args.no_plain:
         q = time_form(args, "plain", case, fields, local, dist, profile=prof)
+        parity = [q["solver"].get(nm) for nm in "UVWP"]
         q["solver"].close()
         pv = case.ncells * args.steps * world / (q["ms"] / 1e3)
         plain = {"value": pv, "unit": UNIT, "ms_per_step": q["ms"] / args.steps,
@@ -531,6 +533,26 @@ def run_ours(args, rank, world, local):
                  "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]}
                                 for k, v in q["kern"].items()},
                  "mixed_over_plain": value / pv}
+        # the same steps with the contracted build of the plain kernels
+        f = time_form(args, "plain_fma", case, fields, local, dist, profile=prof)
+        fv = case.ncells * args.steps * world / (f["ms"] / 1e3)
+        diff = {}
+        for nm, a in zip("UVWP", parity):
+            b = f["solver"].get(nm)
+            if nm == "P":
+                a, b = a - a.mean(), b - b.mean()
+            diff[nm] = float(np.linalg.norm(b - a) / np.linalg.norm(a))
+        f["solver"].close()
+        del parity
+        plain["fma_build"] = {
+            "value": fv, "unit": UNIT, "ms_per_step": f["ms"] / args.steps,
+            "over_parity_build": fv / pv, "mixed_over_plain_fma": value / fv,
+            "rel_l2_vs_parity_build": diff,
+            "what": "MGLET_FORM_PLAIN_FMA: the plain flux and Poisson kernels compiled with "
+                    "multiply-add contraction; relative L2 against the bit-exact build after "
+                    "the same steps (pressure with its mean removed)",
+            "kernels_ms": {k: {"total_ms": v[0], "launches": v[1]} for k, v in f["kern"].items()},
+        }
 
     cpu = None
     if rank == 0 and not args.no_cpu:

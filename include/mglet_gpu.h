@@ -75,7 +75,13 @@ enum {
      * without the ghost-cell IB (BP of 0 or 1), and with an LES model or a
      * caller-set viscosity field G (the fluxes then read G at every point;
      * the LES model itself runs in FP64). */
-    MGLET_FORM_MIXED = 1
+    MGLET_FORM_MIXED = 1,
+    /* The plain FP64 form with multiply-add contraction in its flux and
+     * Poisson kernels (the performance build the parity bar allows): the
+     * same operations in the same order, each a*b+c rounded once, so the
+     * fields stay within a relative 1e-12 of the reference instead of
+     * matching it bit for bit. */
+    MGLET_FORM_PLAIN_FMA = 2
 };
 
 /* Grid hierarchy description: what grids.h5 (GRIDINFO + BC tables,

@@ -36,7 +36,6 @@ static int fail(int code, const std::string& msg) {
     return code;
 }
 
-void release_tables(Ctx* c);
 
 namespace {
 
@@ -340,14 +339,14 @@ static int mgpoisit_plain(Ctx* c, int ilevel, double* dp, double* rhs, double* r
     for (int iloop = 1; iloop <= ninner; ++iloop) {
         if (int rc = launch_bound_pressure(c, ilevel, dp, hbuf, withbp)) return rc;
         if (c->prm.psolver == MGLET_PSOLVER_SOR && ilevel > c->minlevel) {
-            if (int rc = launch_sor(c, ilevel, dp, rhs)) return rc;
+            if (int rc = MG_PLAIN_FN(c, launch_sor)(c, ilevel, dp, rhs)) return rc;
         } else {
-            if (int rc = launch_laplacephi(c, ilevel, res, dp)) return rc;
-            if (int rc = launch_sipiter1(c, ilevel, rhs, res)) return rc;
+            if (int rc = MG_PLAIN_FN(c, launch_laplacephi)(c, ilevel, res, dp)) return rc;
+            if (int rc = MG_PLAIN_FN(c, launch_sipiter1)(c, ilevel, rhs, res)) return rc;
             if (int rc = connect(c, ilevel, 1, nullptr, nullptr, nullptr, res, nullptr, nullptr,
                                  false, false, iloop < ninner ? 0 : -1))
                 return rc;
-            if (int rc = launch_sipiter2(c, ilevel, dp, res)) return rc;
+            if (int rc = MG_PLAIN_FN(c, launch_sipiter2)(c, ilevel, dp, res)) return rc;
         }
         if (int rc = connect(c, ilevel, 1, nullptr, nullptr, nullptr, dp, nullptr, nullptr, false,
                              false, 0))
@@ -368,7 +367,7 @@ int solve_pressure_system(Ctx* c, double prefak, mglet_stage_stats* st, bool zer
         for (double* a : {dp, hilf, res}) MG_CUDA(cudaMemsetAsync(a, 0, bytes, c->stream));
     if (int rc = launch_bp_ones(c)) return rc;
     if (prefak <= 0.0) {
-        if (int rc = launch_rescal_maxabs(c, rhs, nullptr)) return rc;
+        if (int rc = MG_PLAIN_FN(c, launch_rescal_maxabs)(c, rhs, nullptr)) return rc;
         MG_CUDA(cudaMemcpyAsync(c->h_scalar, c->d_scalar, sizeof(double), cudaMemcpyDeviceToHost,
                                 c->stream));
         MG_CUDA(cudaStreamSynchronize(c->stream));
@@ -395,15 +394,15 @@ int solve_pressure_system(Ctx* c, double prefak, mglet_stage_stats* st, bool zer
         if (int rc = connect(c, 0, 1, nullptr, nullptr, nullptr, hilf, nullptr, nullptr, false,
                              false, 0))
             return rc;
-        if (int rc = launch_laplacephi(c, 0, res, hilf)) return rc;
-        if (int rc = launch_rescal_maxabs(c, rhs, res)) return rc;
+        if (int rc = MG_PLAIN_FN(c, launch_laplacephi)(c, 0, res, hilf)) return rc;
+        if (int rc = MG_PLAIN_FN(c, launch_rescal_maxabs)(c, rhs, res)) return rc;
         if (multi) {
             // rhs restricted into the coarse grids, then its maximum again
             for (int l = c->maxlevel; l >= c->minlevel + 1; --l)
                 if (int rc = launch_ftoc(c, l, rhs, rhs, 'R')) return rc;
-            if (int rc = launch_rescal_maxabs(c, rhs, nullptr)) return rc;
+            if (int rc = MG_PLAIN_FN(c, launch_rescal_maxabs)(c, rhs, nullptr)) return rc;
         }
-        if (int rc = launch_accumulate(c, dp, hilf)) return rc;
+        if (int rc = MG_PLAIN_FN(c, launch_accumulate)(c, dp, hilf)) return rc;
         ipc += c->prm.ninner;
         done = ipcount;
         if (ipcount >= c->prm.nouter_min) {
@@ -441,7 +440,7 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
     for (double* a : {dp, hilf, rhs, res}) MG_CUDA(cudaMemsetAsync(a, 0, bytes, c->stream));
     const double prefak = c->prm.rho / dt;
     const char* const none[3] = {nullptr, nullptr, nullptr};
-    if (int rc = launch_divcal(c, rhs, U, V, W, prefak)) return rc;
+    if (int rc = MG_PLAIN_FN(c, launch_divcal)(c, rhs, U, V, W, prefak)) return rc;
     for (int l = c->maxlevel; l >= c->minlevel; --l)
         if (int rc = launch_ftoc(c, l, rhs, rhs, 'R')) return rc;
     if (int rc = solve_pressure_system(c, prefak, st, false)) return rc;
@@ -452,7 +451,7 @@ static int mgpoisl_plain(Ctx* c, double dt, mglet_stage_stats* st) {
         if (int rc = launch_parent(c, l, none, sdp, false)) return rc;
         if (int rc = launch_bound_pressure(c, l, dp, dbuf, c->ibtype == 1)) return rc;
     }
-    if (int rc = launch_mgpcorr(c, U, V, W, P, dp, dt / c->prm.rho)) return rc;
+    if (int rc = MG_PLAIN_FN(c, launch_mgpcorr)(c, U, V, W, P, dp, dt / c->prm.rho)) return rc;
     // pressuresolver_mod.F90:334-348: ftoc fine to coarse, then per level
     // parent, bound and the corner connect
     for (int l = c->maxlevel; l >= c->minlevel; --l) {
@@ -506,13 +505,14 @@ static int stage_plain(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk,
     // timeintegration_mod.F90:96-99: the ghost-cell fluxes of the step
     if (irk == 1 && gc)
         if (int rc = gc_setibvalues(c, U, V, W)) return rc;
-    if (int rc = launch_tstle4(c, UO, VO, WO, gc ? c->F("PWU") : U, gc ? c->F("PWV") : V,
-                               gc ? c->F("PWW") : W, U, V, W, P, G))
+    if (int rc = MG_PLAIN_FN(c, launch_tstle4)(c, UO, VO, WO, gc ? c->F("PWU") : U,
+                                               gc ? c->F("PWV") : V, gc ? c->F("PWW") : W, U, V, W,
+                                               P, G))
         return rc;
     if (int rc = launch_momentum_sources(c)) return rc;     // :102-103 boussinesq, coriolis
-    if (int rc = launch_rkstep(c, U, c->F("DU"), UO, frhs, dt * fu)) return rc;
-    if (int rc = launch_rkstep(c, V, c->F("DV"), VO, frhs, dt * fu)) return rc;
-    if (int rc = launch_rkstep(c, W, c->F("DW"), WO, frhs, dt * fu)) return rc;
+    if (int rc = MG_PLAIN_FN(c, launch_rkstep)(c, U, c->F("DU"), UO, frhs, dt * fu)) return rc;
+    if (int rc = MG_PLAIN_FN(c, launch_rkstep)(c, V, c->F("DV"), VO, frhs, dt * fu)) return rc;
+    if (int rc = MG_PLAIN_FN(c, launch_rkstep)(c, W, c->F("DW"), WO, frhs, dt * fu)) return rc;
     if (gc) {   // timeintegration_mod.F90:110-116: maskbp, getibvalues
         if (int rc = launch_maskbp(c, U, V, W, P)) return rc;
         if (int rc = launch_gc_mode(c, 'R', U, V, W)) return rc;
@@ -636,7 +636,8 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     if (prm->psolver < 0 || prm->psolver > 2) return fail(MGLET_ERR_ARG, "create: bad psolver");
     if (prm->psolver == MGLET_PSOLVER_SOR && (prm->omega <= 0.0 || prm->omega >= 2.0))
         return fail(MGLET_ERR_ARG, "create: invalid omega");
-    if (prm->form != MGLET_FORM_PLAIN && prm->form != MGLET_FORM_MIXED)
+    if (prm->form != MGLET_FORM_PLAIN && prm->form != MGLET_FORM_MIXED &&
+        prm->form != MGLET_FORM_PLAIN_FMA)
         return fail(MGLET_ERR_ARG, "create: bad form");
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
@@ -646,6 +647,9 @@ int mglet_gpu_create(const mglet_grid_desc* d, const mglet_flow_params* prm, int
     mglet_ctx* c = new mglet_ctx();
     c->device = device;
     c->prm = *prm;
+    // the contracted build runs the plain form's code path with its own kernels
+    c->fma = prm->form == MGLET_FORM_PLAIN_FMA;
+    if (c->fma) c->prm.form = MGLET_FORM_PLAIN;
     c->ngrid = d->ngrid;
     auto bail = [&](int rc) {
         mglet_gpu_destroy(c);
@@ -782,6 +786,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
         }
     mixed_release(c);
     release_tables(c);
+    contract::release_tables(c);
     for (auto& kv : c->f3) cudaFree(kv.second);
     for (auto& kv : c->f1) cudaFree(kv.second);
     for (auto& kv : c->plans) {
@@ -872,9 +877,10 @@ int mglet_gpu_tstle4(mglet_ctx* c) {
     if (!c) return fail(MGLET_ERR_ARG, "tstle4: null context");
     cudaSetDevice(c->device);
     const bool gc = c->ibtype == 1;
-    return launch_tstle4(c, c->F("UO"), c->F("VO"), c->F("WO"), c->F(gc ? "PWU" : "U"),
-                         c->F(gc ? "PWV" : "V"), c->F(gc ? "PWW" : "W"), c->F("U"), c->F("V"), c->F("W"),
-                         c->F("P"), c->F("G"));
+    return MG_PLAIN_FN(c, launch_tstle4)(c, c->F("UO"), c->F("VO"), c->F("WO"),
+                                         c->F(gc ? "PWU" : "U"), c->F(gc ? "PWV" : "V"),
+                                         c->F(gc ? "PWW" : "W"), c->F("U"), c->F("V"), c->F("W"),
+                                         c->F("P"), c->F("G"));
 }
 
 int mglet_gpu_rkstep(mglet_ctx* c, const char* p, const char* dp, const char* rhsp, double frhs,
@@ -883,7 +889,7 @@ int mglet_gpu_rkstep(mglet_ctx* c, const char* p, const char* dp, const char* rh
     double *a = field_ptr(c, p), *b = field_ptr(c, dp), *r = field_ptr(c, rhsp);
     if (!a || !b || !r) return fail(MGLET_ERR_NAME, "rkstep: unknown field");
     cudaSetDevice(c->device);
-    return launch_rkstep(c, a, b, r, frhs, dtfu);
+    return MG_PLAIN_FN(c, launch_rkstep)(c, a, b, r, frhs, dtfu);
 }
 
 int mglet_gpu_connect(mglet_ctx* c, int32_t ilevel, int32_t layers, const char* v1,
@@ -906,7 +912,7 @@ int mglet_gpu_divcal(mglet_ctx* c, const char* div, double fak) {
     double* d = field_ptr(c, div);
     if (!d) return fail(MGLET_ERR_NAME, "divcal: unknown field");
     cudaSetDevice(c->device);
-    return launch_divcal(c, d, c->F("U"), c->F("V"), c->F("W"), fak);
+    return MG_PLAIN_FN(c, launch_divcal)(c, d, c->F("U"), c->F("V"), c->F("W"), fak);
 }
 
 int mglet_gpu_laplacephi(mglet_ctx* c, const char* res, const char* phi) {
@@ -915,7 +921,7 @@ int mglet_gpu_laplacephi(mglet_ctx* c, const char* res, const char* phi) {
     if (!r || !p) return fail(MGLET_ERR_NAME, "laplacephi: unknown field");
     cudaSetDevice(c->device);
     if (int rc = launch_bp_ones(c)) return rc;
-    return launch_laplacephi(c, 0, r, p);
+    return MG_PLAIN_FN(c, launch_laplacephi)(c, 0, r, p);
 }
 
 int mglet_gpu_mgpoisl(mglet_ctx* c, double dt, int32_t ittot, int32_t irk, mglet_stage_stats* st) {

@@ -188,6 +188,7 @@ struct Ctx {
     double gravity[3] = {0.0, 0.0, 0.0}, beta = 0.0, omega[3] = {0.0, 0.0, 0.0};
     int buoyancy_scalar = 1;
     int ilesmodel = 0;           // 0 none, 1 smagorinsky, 2 wale, 5 sigma
+    bool fma = false;            // MGLET_FORM_PLAIN_FMA: the plain kernels' contracted build
     double cm = 0.0;             // the LES model constant
     void* d_sptab = nullptr;     // device table of the 12 spacing arrays (adjoint)
     std::vector<GcHostList> gch;
@@ -268,27 +269,22 @@ struct ProfScope {
 };
 
 // ---- kernels: FP64 parity form (plain_*.cu, compiled with -fmad=false) ---
-// u, v, w: the transported velocities (point values PWU.. with the ghost-cell
-// IB), ut, vt, wt: the transporting ones (tstle4_mod.F90:13, 139)
-int launch_tstle4(Ctx* c, double* uo, double* vo, double* wo, const double* u, const double* v,
-                  const double* w, const double* ut, const double* vt, const double* wt,
-                  const double* p, const double* g);
-int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs, double dtfu);
-int launch_g_uniform(Ctx* c);   // d_guni: per grid, is G one value on the box 2..n-1
-int launch_divcal(Ctx* c, double* div, const double* u, const double* v, const double* w,
-                  double fak);
-int launch_bp_ones(Ctx* c);
-int launch_laplacephi(Ctx* c, int ilevel, double* res, const double* phi);
-int launch_sip_lu_hp(Ctx* c);
-int launch_sip_lu_classic(Ctx* c);
-int launch_sipiter1(Ctx* c, int ilevel, const double* rhs, double* res);
-int launch_sipiter2(Ctx* c, int ilevel, double* phi, double* res);
-int launch_sor(Ctx* c, int ilevel, double* dp, const double* rhs);
-int launch_giteig(Ctx* c);
-int launch_rescal_maxabs(Ctx* c, double* rhs, const double* res);
-int launch_accumulate(Ctx* c, double* dp, double* hilf);
-int launch_mgpcorr(Ctx* c, double* u, double* v, double* w, double* p, const double* dp,
-                   double rfak);
+// The flux and Poisson kernels (plain_flux.cu, plain_poisson.cu) are also
+// compiled a second time with multiply-add contraction, into mg::contract: the
+// plain form's performance build (MGLET_FORM_PLAIN_FMA).  MG_PLAIN_FN picks
+// the build the context runs.
+#include "plain_decl.h"
+namespace contract {
+#include "plain_decl.h"
+}
+#define MG_PLAIN_FN(c, fn) ((c)->fma ? ::mg::contract::fn : ::mg::fn)
+#ifdef MG_FMA_BUILD
+#define MG_PLAIN_BEGIN namespace contract {
+#define MG_PLAIN_END }
+#else
+#define MG_PLAIN_BEGIN
+#define MG_PLAIN_END
+#endif
 int launch_itinfo(Ctx* c, double dt);
 // bound_flow%bound on U, V, W and (unless null) P: faces 1..6 in order, the
 // grids of ilevel (0: all levels)

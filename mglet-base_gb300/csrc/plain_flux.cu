@@ -14,6 +14,7 @@
 #include "internal.h"
 
 namespace mg {
+MG_PLAIN_BEGIN
 namespace {
 
 struct GridPtrs {
@@ -426,4 +427,5 @@ int launch_rkstep(Ctx* c, double* p, double* dp, const double* rhs, double frhs,
     return 0;
 }
 
+MG_PLAIN_END
 }  // namespace mg

@@ -23,6 +23,7 @@
 #include "internal.h"
 
 namespace mg {
+MG_PLAIN_BEGIN
 namespace {
 
 #define IX(k, j, i) ((long long)((i) - 1) * kk * jj + (long long)((j) - 1) * kk + ((k) - 1))
@@ -729,4 +730,5 @@ int launch_mgpcorr(Ctx* c, double* u, double* v, double* w, double* p, const dou
     return 0;
 }
 
+MG_PLAIN_END
 }  // namespace mg

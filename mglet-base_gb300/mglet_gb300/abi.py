@@ -17,7 +17,7 @@ MGLET_ERR_NOMEM = 7
 BC_FIX, BC_OP1, BC_NOS, BC_SLI, BC_CON, BC_PAR, BC_CO1 = 2, 3, 5, 6, 7, 8, 19
 
 PSOLVER_SIP, PSOLVER_SOR, PSOLVER_CLASSIC = 0, 1, 2
-FORM_PLAIN, FORM_MIXED = 0, 1
+FORM_PLAIN, FORM_MIXED, FORM_PLAIN_FMA = 0, 1, 2
 
 _i32p = C.POINTER(C.c_int32)
 _f64p = C.POINTER(C.c_double)

@@ -2,7 +2,9 @@
 
 Each translation unit is compiled in parallel with nvcc; the FP64 parity
 kernels (plain_*.cu) get -fmad=false so no multiply-add is contracted, the
-mixed-precision kernels keep FMA.  Output goes next to the sources, into
+mixed-precision kernels keep FMA.  The plain flux and Poisson units are
+compiled a second time with contraction (-DMG_FMA_BUILD, namespace mg::contract),
+the plain form's performance build.  Output goes next to the sources, into
 mglet-base_gb300/_build/ (git-ignored), so the library stays in-tree.
 """
 import concurrent.futures as cf
@@ -26,6 +28,9 @@ SOURCES = ["api.cu", "plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "plai
 # translation units whose FP64 arithmetic must not be contracted into FMAs
 NO_FMA = {"plain_flux.cu", "plain_poisson.cu", "plain_misc.cu", "plain_bound.cu", "plain_gc.cu",
           "plain_level.cu", "noalloc.cu", "les.cu", "scalar.cu"}
+# compiled a second time with contraction, into namespace mg::contract (the plain
+# form's performance build, MGLET_FORM_PLAIN_FMA)
+FMA_TWINS = ["plain_flux.cu", "plain_poisson.cu"]
 
 
 def nvcc():
@@ -40,9 +45,11 @@ def nvcc():
 HOST_NO_FMA = {"gc_create.cu"}
 
 
-def _flags(src):
+def _flags(src, twin=False):
     f = list(BASE) + ARCH
-    if src in NO_FMA:
+    if twin:
+        f.append("-DMG_FMA_BUILD")
+    elif src in NO_FMA:
         f.append("-fmad=false")
     if src in HOST_NO_FMA:
         f += ["-Xcompiler", "-ffp-contract=off"]
@@ -62,12 +69,13 @@ def build(verbose=False, force=False, extra=None):
     headers.append(os.path.join(os.path.dirname(ROOT), "include", "mglet_gpu.h"))
     jobs = []
     objs = []
-    for s in SOURCES:
+    units = [(s, False) for s in SOURCES] + [(s, True) for s in FMA_TWINS]
+    for s, twin in units:
         src = os.path.join(CSRC, s)
-        obj = os.path.join(OUT, s.replace(".cu", ".o"))
+        obj = os.path.join(OUT, s.replace(".cu", "_fma.o" if twin else ".o"))
         objs.append(obj)
         if force or _needs(obj, [src] + headers):
-            cmd = [nvcc()] + _flags(s) + (extra or []) + ["-c", src, "-o", obj]
+            cmd = [nvcc()] + _flags(s, twin) + (extra or []) + ["-c", src, "-o", obj]
             jobs.append(cmd)
 
     def run(cmd):
