@@ -514,8 +514,10 @@ int mglet_gpu_set_partition(mglet_ctx* ctx, const int32_t* halo, int32_t nsend,
  * it is faster than the per-phase kernels).  mglet_gpu_tuning describes the
  * choices ("" for the plain form); mglet_gpu_force_variant overrides one
  * (kernel "mx_sip_pre" 0..9, "mx_sip_sweep" 0..4, "mx_flux" 0..1,
- * "mx_sip_solve" 0..5; -1 = default, for "mx_sip_solve" the per-phase
- * kernels).  All variants compute the same bits. */
+ * "mx_sip_solve" 0..5, "mx_outer_pre" 0..1 -- 1: on one level the outer step
+ * writes the next hilf-zero pre-pass itself; -1 = default, for
+ * "mx_sip_solve" the per-phase kernels).  All variants compute the same
+ * bits. */
 int mglet_gpu_tuning(mglet_ctx* ctx, char* buf, int64_t buflen);
 int mglet_gpu_force_variant(mglet_ctx* ctx, const char* kernel, int32_t variant);
 /* Test switch for the failure path of the bounded waits: the next mixed

@@ -174,6 +174,9 @@ int enqueue_mgpoisl(Ctx* c) {
     // one level: the whole outer loop as one persistent launch when the
     // tuner (or the caller) chose it
     const bool persistent = !multi && s.solve_variant >= 0;
+    // one level with the packed pre-pass: the outer step writes the pre-pass
+    // of the next outer iteration's first inner iteration (hilf = 0)
+    const bool fuse = !multi && s.prepk && s.fuse_pre;
     if (persistent)
         if (int rc = sip_solve(c, s, m->cf, m->apx, m->d_gcls, ctl, m->d_maxrhs, m->d_sprm)) return rc;
     for (int ipcount = 1; ipcount <= (persistent ? 0 : c->prm.nouter); ++ipcount) {
@@ -193,8 +196,10 @@ int enqueue_mgpoisl(Ctx* c) {
                 // cleared it); the finer levels start from the ctof values
                 const bool hz = iloop == 1 && l == c->minlevel;
                 const int rlow = lastfull[li] > 0 ? lastfull[li] % 3 : -1;
+                // the outer step before wrote this iteration's pre-pass
+                const bool prewritten = fuse && hz && ipcount > 1;
                 if (int rc = sip_forward(c, s, m->cf, m->d_gcls, ctl, rlow, gi[li] % 3, hz, glist,
-                                         nlist))
+                                         nlist, prewritten))
                     return rc;
                 if (int rc = sip_backward(c, s, m->cb, m->d_gcls, ctl, gi[li] % 3, hz, glist, nlist))
                     return rc;
@@ -205,7 +210,9 @@ int enqueue_mgpoisl(Ctx* c) {
         }
         for (int l = c->maxlevel; l > c->minlevel; --l)
             if (int rc = mx_ftoc(c, s, lv, l, false, ctl)) return rc;
-        if (int rc = sip_outer(c, s, m->apx, m->d_gcls, ctl)) return rc;
+        if (int rc = sip_outer(c, s, m->apx, m->d_gcls, ctl,
+                               fuse && ipcount < c->prm.nouter ? s.rs[(gi[0] + 1) % 3] : nullptr))
+            return rc;
         if (multi) {
             // the residual restricted into the coarse grids, then its maxima again
             for (int l = c->maxlevel; l > c->minlevel; --l)
@@ -539,7 +546,11 @@ std::string mixed_tuning(Ctx* c) {
     for (int v = 0; v < sip_solve_variants() && n > 0 && n < (int)sizeof sbuf; ++v)
         n += std::snprintf(sbuf + n, sizeof sbuf - n, " %d: %.4f", v, s.solve_var_ms[v]);
     if (n > 0 && n < (int)sizeof sbuf) std::snprintf(sbuf + n, sizeof sbuf - n, "); ");
-    return std::string(buf) + sbuf + mx_flux_tuning(c);
+    return std::string(buf) + sbuf +
+           (s.fuse_pre && s.prepk && c->minlevel == c->maxlevel
+                ? "mx_outer: writes the next pre-pass from hilf = 0; "
+                : "mx_outer: plain; ") +
+           mx_flux_tuning(c);
 }
 
 int mixed_test_wait_timeout(Ctx* c) {
@@ -564,6 +575,19 @@ int mixed_test_barrier_timeout(Ctx* c) {
 
 int mixed_force_variant(Ctx* c, const char* kernel, int v) {
     MixedState* m = c->mx;
+    if (m && std::strcmp(kernel, "mx_outer_pre") == 0) {
+        if (v < -1 || v > 1) {
+            set_error("force_variant: mx_outer_pre is 1 (the outer step writes the next pre-pass), "
+                      "0 (the pre-pass kernel does) or -1 (default 0)");
+            return MGLET_ERR_ARG;
+        }
+        m->sip.fuse_pre = v == 1;
+        if (m->graph) {
+            cudaGraphExecDestroy(m->graph);
+            m->graph = nullptr;
+        }
+        return 0;
+    }
     if (m && std::strcmp(kernel, "mx_sip_solve") == 0) {
         if (v < -1 || v >= sip_solve_variants()) {
             set_error("force_variant: mx_sip_solve variants are 0..5 (-1: the per-phase kernels)");

@@ -845,6 +845,11 @@ struct OuterArgs {
     const int* ctl;
     int* ctl_err;               // ctl[2]
     int rev;                    // walk the grids in reverse block order
+    // one level: the next inner iteration starts from hilf = 0, so its
+    // pre-pass is rhs * lpr; the outer step writes it into PRE (the res slot
+    // of that iteration) from the packed pre-pass records PR (null: not)
+    float* PRE;
+    const float4* PR;
 };
 
 // a + b = s + e exactly (Knuth's TwoSum, no order of magnitudes assumed)
@@ -929,6 +934,8 @@ __device__ __forceinline__ void outer_grid(const OuterArgs& a, int g, const floa
         two_sum(rh, e, rh, rl);
         a.RHS[base + q] = rh;
         a.RHSL[base + q] = rl;
+        // the pre-pass of an iteration from hilf = 0, (rhs + 0) * lpr
+        if (a.PRE) a.PRE[base + q] = (rh + 0.f) * __ldg(a.PR + (long long)a.gcls[g] * 3 * s.npp + q).w;
         // (dh + dl) + hc
         float dh, de;
         two_sum(ldxp<kCoh>(a.DPH + base + q), hc, dh, de);
@@ -1979,9 +1986,9 @@ int sip_divcal(Ctx* c, SipState& st, const double* fak) {
 }
 
 int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
-                int rwrite, bool hzero, const int* glist, int nlist) {
+                int rwrite, bool hzero, const int* glist, int nlist, bool skip_pre) {
     const int ng = glist ? nlist : c->ngrid;
-    {
+    if (!skip_pre) {
         ProfScope ps_(c, "mx_sip_pre");
         PreArgs p = pre_args(c, st, cf, gcls, ctl, rwrite, hzero);
         p.glist = glist;
@@ -2058,7 +2065,8 @@ int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ct
     return 0;
 }
 
-int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl) {
+int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl,
+              float* pre_next) {
     ProfScope ps_(c, "mx_outer");
     OuterArgs a{};
     a.s = shape(st);
@@ -2076,6 +2084,8 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     a.ctl = ctl;
     a.ctl_err = const_cast<int*>(ctl) + 2;
     a.rev = next_order(st);
+    a.PRE = st.prepk ? pre_next : nullptr;
+    a.PR = st.spr;
     k_sip_outer<<<c->ngrid, 512, stencil_smem(st), c->stream>>>(a);
     MG_LAUNCHED(c);
     return 0;

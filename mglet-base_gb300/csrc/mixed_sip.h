@@ -69,6 +69,11 @@ struct SipState {
     double solve_var_ms[6] = {0, 0, 0, 0, 0, 0};   // each variant's time (0: not run)
     unsigned* d_bar = nullptr;
     bool solve_skip = false;
+    // one level: the outer step writes the next iteration's pre-pass (its
+    // hilf is zero), which then is not launched.  Off by default: on 4096
+    // grids of 24^3 it saves 3.2 ms of pre-pass per step and costs the outer
+    // step 3.5 ms (the records' lpr and one more array written)
+    bool fuse_pre = false;
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
@@ -83,11 +88,17 @@ void sip_release(SipState& st);
 // fak (the solve's prefak) is read from device memory
 int sip_divcal(Ctx* c, SipState& st, const double* fak);
 // glist / nlist: the grids of one level (null: every grid)
+// skip_pre: the pre-pass values are in slot rwrite already (the outer step
+// wrote them, pre_next of sip_outer)
 int sip_forward(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl, int rlow,
-                int rwrite, bool hzero, const int* glist = nullptr, int nlist = 0);
+                int rwrite, bool hzero, const int* glist = nullptr, int nlist = 0,
+                bool skip_pre = false);
 int sip_backward(Ctx* c, SipState& st, const float* cb, const int* gcls, int* ctl, int rhi,
                  bool hzero, const int* glist = nullptr, int nlist = 0);
-int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl);
+// pre_next: where the next inner iteration's pre-pass goes when it starts from
+// hilf = 0 on a single level (null: the pre-pass kernel computes it)
+int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int* ctl,
+              float* pre_next = nullptr);
 int sip_scatter_dp(Ctx* c, SipState& st);
 // The open-coupling masks of every grid from BP (ghost-cell IB)
 int sip_bpmask(Ctx* c, SipState& st);

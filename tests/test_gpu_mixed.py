@@ -264,3 +264,31 @@ def test_bounded_wait_runs_out_and_recovers(gpu_lib):
     assert np.isfinite(st.maxrhs)
     assert np.all(np.isfinite(g.get("U")))
     g.close()
+
+
+@pytest.mark.parametrize("walls", [False, True])
+def test_outer_step_writes_the_next_pre_pass(gpu_lib, walls):
+    """On one level the outer step writes the pre-pass of the next outer
+    iteration's first inner iteration (hilf = 0: rhs * lpr), which is then
+    not launched: the same bits as launching it, with and without walls
+    (per-point records), at the outer cap and with an early stop."""
+    kw = {"walls": {1: abi.BC_NOS, 2: abi.BC_SLI}} if walls else {}
+    case = cases.periodic_box(2, 2, 1, n=24, **kw)
+    for eps, nouter in ((1e-10, 4), (1e-5, 30)):
+        out = []
+        for v in (0, 1):
+            g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=eps, nouter=nouter))
+            g.force_variant("mx_outer_pre", v)
+            assert ("writes the next pre-pass" in g.tuning()) == (v == 1)
+            _init(g, case)
+            rk = gpu_lib.rk_scheme("williamson")
+            stats = []
+            for it in (1, 2):
+                for irk in range(1, 4):
+                    st = g.timeintegrate_flow(it, it, 0.0, 5e-4, irk, rk)
+                    stats.append((st.nouter_done, st.maxrhs))
+            out.append((stats, [g.get(nm) for nm in "UVWP"]))
+            g.close()
+        assert out[0][0] == out[1][0]
+        for a, b in zip(out[0][1], out[1][1]):
+            assert np.array_equal(a, b)
