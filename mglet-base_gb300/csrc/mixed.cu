@@ -575,6 +575,19 @@ int mixed_test_barrier_timeout(Ctx* c) {
 
 int mixed_force_variant(Ctx* c, const char* kernel, int v) {
     MixedState* m = c->mx;
+    if (m && std::strcmp(kernel, "mx_order") == 0) {
+        if (v < -1 || v > 1) {
+            set_error("force_variant: mx_order is 1 (divcal and scatter in natural order), 0 (plane "
+                      "order) or -1 (default 1)");
+            return MGLET_ERR_ARG;
+        }
+        m->sip.natural = v != 0;
+        if (m->graph) {
+            cudaGraphExecDestroy(m->graph);
+            m->graph = nullptr;
+        }
+        return 0;
+    }
     if (m && std::strcmp(kernel, "mx_outer_pre") == 0) {
         if (v < -1 || v > 1) {
             set_error("force_variant: mx_outer_pre is 1 (the outer step writes the next pre-pass), "

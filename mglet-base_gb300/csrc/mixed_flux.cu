@@ -232,7 +232,8 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                      (vs.u.t * dif(tw_p[q], tw_0[q]) - vs.u.b * dif(tw_p[qb], tw_0[qb])) * fddy;
             const float fak = a.rrho * vol;
             const float gp = (dif(p_p[q], p_0[q]) + a.gpx * gfl * fdx_i) * (a.rrho / fdx_i);
-            uo = conv - fak * (qd - qc) - gp;
+            uo = conv - fak * qd - gp;
+            if (cross) uo += fak * qc;
         }
         // ---------------- V at (k, j+1/2, i)
         {
@@ -279,7 +280,8 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                      (vs.v.t * dif(tw_0[qn], tw_0[q]) - vs.v.b * dif(tw_0[qb + pk], tw_0[qb])) * fddx;
             const float fak = a.rrho * vol;
             const float gp = (dif(p_0[qn], p_0[q]) + a.gpy * gfl * fdy_j) * (a.rrho / fdy_j);
-            vo = conv - fak * (qd - qc) - gp;
+            vo = conv - fak * qd - gp;
+            if (cross) vo += fak * qc;
         }
         // ---------------- W at (k+1/2, j, i)
         {
@@ -326,7 +328,8 @@ __device__ __forceinline__ void flux_point(const FluxArgs& a, const float* X, lo
                      (vs.w.t * dT * rddz_kp + vs.w.b * dB * rddz_k) * az;
             const float fak = a.rrho * vol;
             const float gp = (dif(p_0[qt], p_0[q]) + a.gpz * gfl * fdz_k) * (a.rrho / fdz_k);
-            wo = conv - fak * (qd - qc) - gp;
+            wo = conv - fak * qd - gp;
+            if (cross) wo += fak * qc;
         }
 }
 

@@ -1206,6 +1206,62 @@ __global__ void k_sip_divcal(const DevGrid* __restrict__ grids, int npp, const i
     RHSL[o] = (float)(d - (double)dh);
 }
 
+// Natural-order forms of divcal and the scatter: one thread per interior
+// point with k fastest, so the FP64 fields are read or written in
+// contiguous runs; the point's padded plane position (tpos[(io+jo+ko) * ni +
+// io] + jo) takes the scattered 4-byte side, whose partial sectors L2
+// merges.  The arithmetic per point is that of the plane-order kernels.
+__device__ __forceinline__ void nat_point(int t, int ni, int nj, int nk, int& io, int& jo, int& ko) {
+    ko = t % nk;
+    jo = (t / nk) % nj;
+    io = t / (nk * nj);
+}
+
+__global__ void k_sip_divcal_nat(const DevGrid* __restrict__ grids, int ni, int nj, int nk,
+                                 const int* __restrict__ tpos, int npp, float* __restrict__ RHS,
+                                 float* __restrict__ RHSL, const double* __restrict__ U,
+                                 const double* __restrict__ V, const double* __restrict__ W,
+                                 const double* __restrict__ RDDX, const double* __restrict__ RDDY,
+                                 const double* __restrict__ RDDZ, const double* __restrict__ pfak,
+                                 const double* __restrict__ SDIV, const double* __restrict__ BP) {
+    const int g = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ni * nj * nk) return;
+    int io, jo, ko;
+    nat_point(t, ni, nj, nk, io, jo, ko);
+    const DevGrid G = grids[g];
+    const int kk = G.kk, jj = G.jj;
+    const int k = ko + 3, j = jo + 3, i = io + 3;
+    const int id = (i - 1) * kk * jj + (j - 1) * kk + (k - 1);
+    const double *u = U + G.ip3, *v = V + G.ip3, *w = W + G.ip3;
+    const double fak = *pfak;
+    double d = fak * ((u[id] - u[id - kk * jj]) * RDDX[G.ipx + i - 1] +
+                      (v[id] - v[id - kk]) * RDDY[G.ipy + j - 1] +
+                      (w[id] - w[id - 1]) * RDDZ[G.ipz + k - 1]);
+    if (SDIV) {
+        d = d + fak * SDIV[G.ip3 + id];
+        d = BP[G.ip3 + id] * d;
+    }
+    const float dh = (float)d;
+    const long long o = (long long)g * npp + tpos[(io + jo + ko) * ni + io] + jo;
+    RHS[o] = dh;
+    RHSL[o] = (float)(d - (double)dh);
+}
+
+__global__ void k_sip_scatter_nat(const DevGrid* __restrict__ grids, int ni, int nj, int nk,
+                                  const int* __restrict__ tpos, int npp, const float* __restrict__ DPH,
+                                  const float* __restrict__ DPL, double* __restrict__ DP) {
+    const int g = blockIdx.y;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= ni * nj * nk) return;
+    int io, jo, ko;
+    nat_point(t, ni, nj, nk, io, jo, ko);
+    const DevGrid G = grids[g];
+    const int id = (io + 2) * G.kk * G.jj + (jo + 2) * G.kk + (ko + 2);
+    const long long o = (long long)g * npp + tpos[(io + jo + ko) * ni + io] + jo;
+    DP[G.ip3 + id] = (double)DPH[o] + (double)DPL[o];
+}
+
 // The open couplings of every padded position (ghost-cell IB): bit f (faces
 // i-1, i+1, j-1, j+1, k-1, k+1) is set where bp(neighbour) * bp(point) is
 // 1, the factor laplacephi puts on that neighbour (BP is 0 or 1).
@@ -1975,6 +2031,15 @@ void sip_release(SipState& st) {
 
 int sip_divcal(Ctx* c, SipState& st, const double* fak) {
     ProfScope ps_(c, "mx_divcal");
+    if (st.natural) {
+        dim3 grid((st.npts + 255) / 256, c->ngrid);
+        k_sip_divcal_nat<<<grid, 256, 0, c->stream>>>(
+            c->d_grids, st.ni, st.nj, st.nk, st.d_tpos, st.npp, st.rhs32, st.rhsl, c->F("U"),
+            c->F("V"), c->F("W"), c->L("RDDX"), c->L("RDDY"), c->L("RDDZ"), fak,
+            c->ibtype == 1 ? c->F("SDIV") : nullptr, c->ibtype == 1 ? c->F("BP") : nullptr);
+        MG_LAUNCHED(c);
+        return 0;
+    }
     dim3 grid((st.npp + 255) / 256, c->ngrid);
     k_sip_divcal<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.rhs32, st.rhsl,
                                               c->F("U"), c->F("V"), c->F("W"), c->L("RDDX"),
@@ -2101,6 +2166,13 @@ int sip_bpmask(Ctx* c, SipState& st) {
 
 int sip_scatter_dp(Ctx* c, SipState& st) {
     ProfScope ps_(c, "mx_scatter");
+    if (st.natural) {
+        dim3 grid((st.npts + 255) / 256, c->ngrid);
+        k_sip_scatter_nat<<<grid, 256, 0, c->stream>>>(c->d_grids, st.ni, st.nj, st.nk, st.d_tpos,
+                                                       st.npp, st.dph, st.dpl, c->F("DP"));
+        MG_LAUNCHED(c);
+        return 0;
+    }
     dim3 grid((st.npp + 255) / 256, c->ngrid);
     k_sip_scatter<<<grid, 256, 0, c->stream>>>(c->d_grids, st.npp, st.d_idxp, st.dph, st.dpl,
                                                c->F("DP"));

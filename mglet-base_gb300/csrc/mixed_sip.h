@@ -74,6 +74,9 @@ struct SipState {
     // grids of 24^3 it saves 3.2 ms of pre-pass per step and costs the outer
     // step 3.5 ms (the records' lpr and one more array written)
     bool fuse_pre = false;
+    // divcal and the scatter of dp in natural order (coalesced FP64 side);
+    // false: in plane order
+    bool natural = true;
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };

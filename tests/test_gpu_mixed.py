@@ -292,3 +292,21 @@ def test_outer_step_writes_the_next_pre_pass(gpu_lib, walls):
         assert out[0][0] == out[1][0]
         for a, b in zip(out[0][1], out[1][1]):
             assert np.array_equal(a, b)
+
+
+def test_natural_order_divcal_and_scatter_same_bits(gpu_lib):
+    """divcal and the scatter of dp in natural order (the default) and in
+    plane order give the same bits: one level, and a two-level hierarchy."""
+    for case in (cases.periodic_box(2, 2, 1, n=24), cases.refined_box(2, 2, 2, n=8, refine=(1,))):
+        out = []
+        for v in (0, 1):
+            g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=4))
+            g.force_variant("mx_order", v)
+            _init(g, case)
+            rk = gpu_lib.rk_scheme("williamson")
+            for irk in range(1, 4):
+                g.timeintegrate_flow(1, 1, 0.0, 5e-4, irk, rk)
+            out.append([g.get(nm) for nm in ("U", "V", "W", "P", "DP")])
+            g.close()
+        for a, b in zip(*out):
+            assert np.array_equal(a, b)
