@@ -368,7 +368,74 @@ MODULE mglet_gpu_mod
             REAL(c_double), VALUE :: dt
             TYPE(mglet_itinfo), INTENT(out) :: out
         END FUNCTION mglet_gpu_itinfo
+
+        INTEGER(c_int) FUNCTION mglet_gpu_ftoc_multiple(ctx, ilevel, v1, v2, v3, s1, s2, s3) &
+                BIND(C, name="mglet_gpu_ftoc_multiple")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: ilevel
+            TYPE(c_ptr), VALUE :: v1, v2, v3, s1, s2, s3
+        END FUNCTION mglet_gpu_ftoc_multiple
+
+        INTEGER(c_int) FUNCTION mglet_gpu_get_buffer(ctx, name, igrid, iface, host, n) &
+                BIND(C, name="mglet_gpu_get_buffer")
+            IMPORT :: c_int, c_int32_t, c_int64_t, c_ptr, c_char, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(in) :: name(*)
+            INTEGER(c_int32_t), VALUE :: igrid, iface
+            REAL(c_double), INTENT(out) :: host(*)
+            INTEGER(c_int64_t), VALUE :: n
+        END FUNCTION mglet_gpu_get_buffer
+
+        INTEGER(c_int) FUNCTION mglet_gpu_divmax_noalloc(u, v, w, ngrid, kk, jj, ii, rddx, rddy, &
+                rddz, divmax, stream) BIND(C, name="mglet_gpu_divmax_noalloc")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: u, v, w, rddx, rddy, rddz, divmax, stream
+            INTEGER(c_int32_t), VALUE :: ngrid, kk, jj, ii
+        END FUNCTION mglet_gpu_divmax_noalloc
+
+        INTEGER(c_int) FUNCTION mglet_gpu_synchronize(ctx) BIND(C, name="mglet_gpu_synchronize")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+        END FUNCTION mglet_gpu_synchronize
+
+        INTEGER(c_int64_t) FUNCTION mglet_gpu_idim3d(ctx) BIND(C, name="mglet_gpu_idim3d")
+            IMPORT :: c_int64_t, c_ptr
+            TYPE(c_ptr), VALUE :: ctx
+        END FUNCTION mglet_gpu_idim3d
+
+        TYPE(c_ptr) FUNCTION mglet_gpu_last_error() BIND(C, name="mglet_gpu_last_error")
+            IMPORT :: c_ptr
+        END FUNCTION mglet_gpu_last_error
+
+        INTEGER(c_int) FUNCTION mglet_rk_get_coeffs(rk, irk, frhs, fu, dtrk, dtrki) &
+                BIND(C, name="mglet_rk_get_coeffs")
+            IMPORT :: c_int, c_int32_t, c_double, mglet_rk_scheme
+            TYPE(mglet_rk_scheme), INTENT(in) :: rk
+            INTEGER(c_int32_t), VALUE :: irk
+            REAL(c_double), INTENT(out) :: frhs, fu, dtrk, dtrki
+        END FUNCTION mglet_rk_get_coeffs
+
+        INTEGER(c_int) FUNCTION mglet_gpu_tuning(ctx, buf, buflen) BIND(C, name="mglet_gpu_tuning")
+            IMPORT :: c_int, c_int64_t, c_ptr, c_char
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(out) :: buf(*)
+            INTEGER(c_int64_t), VALUE :: buflen
+        END FUNCTION mglet_gpu_tuning
+
+        INTEGER(c_int) FUNCTION mglet_gpu_force_variant(ctx, kernel, variant) &
+                BIND(C, name="mglet_gpu_force_variant")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_char
+            TYPE(c_ptr), VALUE :: ctx
+            CHARACTER(kind=c_char), INTENT(in) :: kernel(*)
+            INTEGER(c_int32_t), VALUE :: variant
+        END FUNCTION mglet_gpu_force_variant
     END INTERFACE
+
+    ! mglet_flow_params%form: the FP64 form bit for bit with the reference, the
+    ! batched mixed-precision form, the FP64 form with multiply-add contraction
+    INTEGER(c_int32_t), PARAMETER :: MGLET_FORM_PLAIN = 0, MGLET_FORM_MIXED = 1, &
+        MGLET_FORM_PLAIN_FMA = 2
 
     TYPE(c_ptr), SAVE :: gctx = C_NULL_PTR
     TYPE(mglet_rk_scheme), SAVE :: grk
@@ -381,7 +448,8 @@ MODULE mglet_gpu_mod
         gpu_energy_gradient, gpu_set_scalars, gpu_timeintegrate_scalar, gpu_set_scalar_bc, &
         gpu_add_scalar_source, gpu_tstle4, gpu_rkstep, gpu_divcal, gpu_laplacephi, gpu_mgpoisl, &
         gpu_maskbp, gpu_getibvalues, gpu_adjoint_rk_stage, mglet_ib_geometry, &
-        gpu_create_flowstencils
+        gpu_create_flowstencils, gpu_ftoc_multiple, gpu_download_buffer, gpu_synchronize, &
+        gpu_tuning, gpu_force_variant, MGLET_FORM_PLAIN, MGLET_FORM_MIXED, MGLET_FORM_PLAIN_FMA
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -669,6 +737,71 @@ CONTAINS
         END DO
         IF (mglet_flowstencils_free(s) /= 0) CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_create_flowstencils
+
+    ! Drop-in for ftoc_multiple(ilevel, v1, v2, v3, s1, s2, s3): blank names
+    ! leave a slot out
+    SUBROUTINE gpu_ftoc_multiple(ilevel, v1, v2, v3, s1, s2, s3)
+        INTEGER, INTENT(in) :: ilevel
+        CHARACTER(len=*), INTENT(in) :: v1, v2, v3, s1, s2, s3
+        ! one NUL-terminated name per column (field names are short)
+        CHARACTER(kind=c_char), TARGET :: n(64, 6)
+        TYPE(c_ptr) :: p(6)
+        INTEGER :: q
+        CALL put(1, v1); CALL put(2, v2); CALL put(3, v3)
+        CALL put(4, s1); CALL put(5, s2); CALL put(6, s3)
+        DO q = 1, 6
+            p(q) = C_NULL_PTR
+            IF (n(1, q) /= C_NULL_CHAR) p(q) = C_LOC(n(1, q))
+        END DO
+        IF (mglet_gpu_ftoc_multiple(gctx, INT(ilevel, c_int32_t), p(1), p(2), p(3), p(4), p(5), &
+            p(6)) /= 0) CALL errr(__FILE__, __LINE__)
+    CONTAINS
+        SUBROUTINE put(col, name)
+            INTEGER, INTENT(in) :: col
+            CHARACTER(len=*), INTENT(in) :: name
+            INTEGER :: c, l
+            l = MIN(LEN_TRIM(name), 63)
+            DO c = 1, l
+                n(c, col) = name(c:c)
+            END DO
+            n(l + 1, col) = C_NULL_CHAR
+        END SUBROUTINE put
+    END SUBROUTINE gpu_ftoc_multiple
+
+    ! field_t%get_buffer(buf, igrid, iface) of the device copy
+    SUBROUTINE gpu_download_buffer(name, igrid, iface, buf)
+        CHARACTER(len=*), INTENT(in) :: name
+        INTEGER, INTENT(in) :: igrid, iface
+        REAL(c_double), INTENT(out) :: buf(:)
+        IF (mglet_gpu_get_buffer(gctx, TRIM(name)//C_NULL_CHAR, INT(igrid, c_int32_t), &
+            INT(iface, c_int32_t), buf, INT(SIZE(buf), c_int64_t)) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_download_buffer
+
+    SUBROUTINE gpu_synchronize()
+        IF (mglet_gpu_synchronize(gctx) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_synchronize
+
+    ! The launch variants the mixed form's tuner chose, as text
+    SUBROUTINE gpu_tuning(text)
+        CHARACTER(len=*), INTENT(out) :: text
+        CHARACTER(kind=c_char) :: buf(4096)
+        INTEGER :: q
+        IF (mglet_gpu_tuning(gctx, buf, INT(SIZE(buf), c_int64_t)) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+        text = ''
+        DO q = 1, MIN(LEN(text), SIZE(buf))
+            IF (buf(q) == C_NULL_CHAR) EXIT
+            text(q:q) = buf(q)
+        END DO
+    END SUBROUTINE gpu_tuning
+
+    SUBROUTINE gpu_force_variant(kernel, variant)
+        CHARACTER(len=*), INTENT(in) :: kernel
+        INTEGER, INTENT(in) :: variant
+        IF (mglet_gpu_force_variant(gctx, TRIM(kernel)//C_NULL_CHAR, INT(variant, c_int32_t)) /= 0) &
+            CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_force_variant
 
     SUBROUTINE gpu_itinfo(dt, cflmax, divmax, energy, exploded)
         REAL(c_double), INTENT(in) :: dt
