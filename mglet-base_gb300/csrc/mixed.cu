@@ -514,6 +514,7 @@ int mixed_init(Ctx* c) {
     const char* tune = std::getenv("MGLET_TUNE");
     if (!(tune && tune[0] == '0')) {
         if (int rc2 = sip_tune(c, m->sip, m->cf, m->d_gcls, m->d_ctl)) return rc2;
+        if (int rc2 = sip_tune_outer(c, m->sip, m->apx, m->d_gcls, m->d_ctl)) return rc2;
         if (int rc2 = sip_tune_solve(c, m->sip, m->cf, m->apx, m->d_gcls, m->d_ctl, m->d_maxrhs,
                                      m->d_sprm))
             return rc2;
@@ -546,11 +547,16 @@ std::string mixed_tuning(Ctx* c) {
     for (int v = 0; v < sip_solve_variants() && n > 0 && n < (int)sizeof sbuf; ++v)
         n += std::snprintf(sbuf + n, sizeof sbuf - n, " %d: %.4f", v, s.solve_var_ms[v]);
     if (n > 0 && n < (int)sizeof sbuf) std::snprintf(sbuf + n, sizeof sbuf - n, "); ");
-    return std::string(buf) + sbuf +
-           (s.fuse_pre && s.prepk && c->minlevel == c->maxlevel
-                ? "mx_outer: writes the next pre-pass from hilf = 0; "
-                : "mx_outer: plain; ") +
-           mx_flux_tuning(c);
+    char obuf[256];
+    std::snprintf(obuf, sizeof obuf,
+                  "mx_outer: %s%s (staged %.4f ms, direct 3 CTAs/SM %.4f ms, 4 CTAs/SM %.4f ms)%s; ",
+                  sip_outer_variant_name(s.outer_variant >= 0 ? s.outer_variant : 0),
+                  s.outer_variant >= 0 ? "" : " [default]", s.outer_ms[0], s.outer_ms[1],
+                  s.outer_ms[2],
+                  s.fuse_pre && s.prepk && c->minlevel == c->maxlevel
+                      ? ", writes the next pre-pass from hilf = 0"
+                      : "");
+    return std::string(buf) + sbuf + obuf + mx_flux_tuning(c);
 }
 
 int mixed_test_wait_timeout(Ctx* c) {
@@ -575,6 +581,18 @@ int mixed_test_barrier_timeout(Ctx* c) {
 
 int mixed_force_variant(Ctx* c, const char* kernel, int v) {
     MixedState* m = c->mx;
+    if (m && std::strcmp(kernel, "mx_outer") == 0) {
+        if (v < -1 || v >= sip_outer_variants()) {
+            set_error("force_variant: mx_outer variants are 0 (staged), 1, 2 (direct) or -1");
+            return MGLET_ERR_ARG;
+        }
+        m->sip.outer_variant = v;
+        if (m->graph) {
+            cudaGraphExecDestroy(m->graph);
+            m->graph = nullptr;
+        }
+        return 0;
+    }
     if (m && std::strcmp(kernel, "mx_order") == 0) {
         if (v < -1 || v > 1) {
             set_error("force_variant: mx_order is 1 (divcal and scatter in natural order), 0 (plane "

@@ -989,6 +989,27 @@ __global__ void __launch_bounds__(512, 3) k_sip_outer(OuterArgs a) {
     outer_grid<false>(a, g, H, gh, spst, ro, sh);
 }
 
+// The outer step without staging: hilf is read from global memory through
+// L1 (the tables and ghost faces alone in shared memory, so more CTAs fit
+// and each starts computing at once); the same points and arithmetic.
+template <int kMinBlocks>
+__global__ void __launch_bounds__(512, kMinBlocks) k_sip_outer_direct(OuterArgs a) {
+    if (a.ctl[0]) return;
+    __shared__ double sh[32];
+    extern __shared__ __align__(16) unsigned char osm[];
+    const Shape s = a.s;
+    const int ni = s.ni, nm = s.nm;
+    int* spst = reinterpret_cast<int*>(osm);
+    short* ro = reinterpret_cast<short*>(spst + nm + 1);
+    float* gh = reinterpret_cast<float*>(osm + stencil_tables_bytes(nm, ni));   // [6][fs]
+    const int g = a.rev ? gridDim.x - 1 - blockIdx.x : blockIdx.x;
+    for (int q = threadIdx.x; q <= nm; q += blockDim.x) spst[q] = s.pst[q];
+    for (int q = threadIdx.x; q < nm * ni; q += blockDim.x) ro[q] = s.rowoff[q];
+    gather_hilf_ghosts(gh, s, a.H, a.fnbr + 6 * g, a.PG ? a.PG + (long long)g * 6 * s.fs : nullptr);
+    __syncthreads();
+    outer_grid<false>(a, g, a.H + (long long)g * s.npp, gh, spst, ro, sh);
+}
+
 // maxabscal over grids + the outer-loop stopping test of mgpoisl
 // (pressuresolver_mod.F90:275,294-301), by one CTA: the largest |rhs| of
 // the grids (scaled to the finest level), the outer count, the converged
@@ -1380,6 +1401,24 @@ size_t sweep_smem(const SipState& st) {
     return rp_nb_offset(st.nm) + ((size_t)2 * st.maxlp + 3 * st.fs) * 4;
 }
 
+size_t outer_direct_smem(const SipState& st) {
+    return stencil_tables_bytes(st.nm, st.ni) + (size_t)6 * st.fs * 4;
+}
+
+// Outer-step variants: 0 staged (one bulk copy of hilf), 1 and 2 direct at
+// three and four CTAs per SM.
+const char* const kOuterNames[3] = {"hilf staged by a bulk copy", "direct loads, 3 CTAs/SM",
+                                    "direct loads, 4 CTAs/SM"};
+
+void launch_outer_variant(int v, int ngrid, const SipState& st, cudaStream_t s, const OuterArgs& a) {
+    if (v == 1)
+        k_sip_outer_direct<3><<<ngrid, 512, outer_direct_smem(st), s>>>(a);
+    else if (v == 2)
+        k_sip_outer_direct<4><<<ngrid, 512, outer_direct_smem(st), s>>>(a);
+    else
+        k_sip_outer<<<ngrid, 512, stencil_smem(st), s>>>(a);
+}
+
 size_t pre_smem(const SipState& st) {
     return stencil_tables_bytes(st.nm, st.ni) + (size_t)6 * st.fs * 4;
 }
@@ -1721,6 +1760,51 @@ int sip_tune(Ctx* c, SipState& st, const float* cf, const int* gcls, int* ctl) {
     for (int r = 0; r < 3; ++r)
         MG_CUDA(cudaMemsetAsync(st.rs[r], 0, (size_t)c->ngrid * st.npp * sizeof(float), c->stream));
     MG_CUDA(cudaMemsetAsync(st.h32, 0, (size_t)c->ngrid * st.npp * sizeof(float), c->stream));
+    return 0;
+}
+
+int sip_tune_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, int* ctl) {
+    static std::map<std::vector<long long>, std::vector<double>> cache;
+    const std::vector<long long> key = {st.kk, st.jj, st.ii, c->ngrid, st.bm ? 1 : 0,
+                                        st.pg ? 1 : 0};
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+        OuterArgs a = outer_args(c, st, apx, gcls, ctl);
+        cudaEvent_t e0, e1;
+        MG_CUDA(cudaEventCreate(&e0));
+        MG_CUDA(cudaEventCreate(&e1));
+        std::vector<double> ms(3, 0.0);
+        for (int v = 0; v < 3; ++v) {
+            for (int w = 0; w < 2; ++w) launch_outer_variant(v, c->ngrid, st, c->stream, a);
+            cudaEventRecord(e0, c->stream);
+            const int reps = 5;
+            for (int r = 0; r < reps; ++r) {
+                a.rev = r & 1;
+                launch_outer_variant(v, c->ngrid, st, c->stream, a);
+            }
+            cudaEventRecord(e1, c->stream);
+            cudaError_t e = cudaEventSynchronize(e1);
+            if (e == cudaSuccess) e = cudaGetLastError();
+            if (e != cudaSuccess) {
+                cudaEventDestroy(e0);
+                cudaEventDestroy(e1);
+                return cuda_fail(e, "sip_tune_outer");
+            }
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            ms[v] = t / reps;
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        it = cache.emplace(key, ms).first;
+        // the timing launches ran on zero hilf: rhs and dp are unchanged
+    }
+    int best = 0;
+    for (int v = 0; v < 3; ++v) {
+        st.outer_ms[v] = it->second[v];
+        if (it->second[v] < it->second[best]) best = v;
+    }
+    st.outer_variant = best;
     return 0;
 }
 
@@ -2151,7 +2235,7 @@ int sip_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, const int
     a.rev = next_order(st);
     a.PRE = st.prepk ? pre_next : nullptr;
     a.PR = st.spr;
-    k_sip_outer<<<c->ngrid, 512, stencil_smem(st), c->stream>>>(a);
+    launch_outer_variant(st.outer_variant < 0 ? 0 : st.outer_variant, c->ngrid, st, c->stream, a);
     MG_LAUNCHED(c);
     return 0;
 }
@@ -2187,6 +2271,9 @@ int sip_conv(Ctx* c, int* ctl, double* maxrhs, const double* sprm) {
     MG_LAUNCHED(c);
     return 0;
 }
+
+int sip_outer_variants() { return 3; }
+const char* sip_outer_variant_name(int v) { return v >= 0 && v < 3 ? kOuterNames[v] : ""; }
 
 int sip_solve_variants() { return kNumSolve; }
 const char* sip_solve_variant_name(int v) {

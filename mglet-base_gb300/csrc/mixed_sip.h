@@ -77,6 +77,10 @@ struct SipState {
     // divcal and the scatter of dp in natural order (coalesced FP64 side);
     // false: in plane order
     bool natural = true;
+    // outer-step variant (0 staged, 1 / 2 direct at 3 / 4 CTAs per SM; -1
+    // default 0) and the tuner's times per launch
+    int outer_variant = -1;
+    double outer_ms[3] = {0, 0, 0};
     float* a1[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};   // FP32 GSAW..GSAT
     float* a1lo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}; // FP32 of the remainders
 };
@@ -114,6 +118,8 @@ const char* sip_pre_variant_name(int v);
 bool sip_pre_variant_uniform(int v);
 int sip_sweep_variants();
 const char* sip_sweep_variant_name(int v);
+int sip_outer_variants();
+const char* sip_outer_variant_name(int v);
 // maxabscal over the grids and the outer-loop stopping test (one CTA)
 int sip_conv(Ctx* c, int* ctl, double* maxrhs, const double* sprm);
 // The persistent solve: every inner iteration, outer step and stopping test
@@ -126,6 +132,8 @@ bool sip_solve_fits(Ctx* c, const SipState& st, int v);
 int sip_solve_alloc(SipState& st);
 int sip_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int* gcls, int* ctl,
               double* maxrhs, const double* sprm);
+// Times the outer-step variants on the case and keeps the fastest.
+int sip_tune_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, int* ctl);
 // Times the persistent variants against the per-phase kernels (which the
 // tuner must have picked already) and keeps the faster form.
 int sip_tune_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int* gcls,

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 from mglet_gb300 import abi, cases
+from test_oracle_levels import prepare_levels
 
 pytestmark = pytest.mark.gpu
 
@@ -294,6 +295,21 @@ def test_outer_step_writes_the_next_pre_pass(gpu_lib, walls):
             assert np.array_equal(a, b)
 
 
+def _init_any(g, case):
+    """Taylor-Green with noise on a single level or a hierarchy."""
+    if case.iparent is None or all(p == 0 for p in case.iparent):
+        _init(g, case)
+        return
+    u, v, w, p = cases.taylor_green(case)
+    u, v, w = cases.add_noise(case, (u, v, w), amplitude=1e-2, seed=42)
+    for nm, a in zip("UVWP", (u, v, w, p)):
+        g.set(nm, a)
+    g.set_hierarchy(case.iparent, case.position)
+    for lvl in (1, 2):
+        g.connect(lvl, 2, v1="U", v2="V", v3="W", s1="P", corners=True)
+    prepare_levels(g, case)
+
+
 def test_natural_order_divcal_and_scatter_same_bits(gpu_lib):
     """divcal and the scatter of dp in natural order (the default) and in
     plane order give the same bits: one level, and a two-level hierarchy."""
@@ -302,7 +318,7 @@ def test_natural_order_divcal_and_scatter_same_bits(gpu_lib):
         for v in (0, 1):
             g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=4))
             g.force_variant("mx_order", v)
-            _init(g, case)
+            _init_any(g, case)
             rk = gpu_lib.rk_scheme("williamson")
             for irk in range(1, 4):
                 g.timeintegrate_flow(1, 1, 0.0, 5e-4, irk, rk)
@@ -310,3 +326,26 @@ def test_natural_order_divcal_and_scatter_same_bits(gpu_lib):
             g.close()
         for a, b in zip(*out):
             assert np.array_equal(a, b)
+
+
+def test_outer_step_variants_same_bits(gpu_lib):
+    """The outer step with hilf staged by a bulk copy and the two direct-load
+    variants give the same bits: one level, walls, and a hierarchy (PAR
+    ghost planes)."""
+    for case in (cases.periodic_box(2, 2, 1, n=24),
+                 cases.periodic_box(2, 2, 1, n=8, walls={1: abi.BC_NOS, 2: abi.BC_SLI}),
+                 cases.refined_box(2, 2, 2, n=8, refine=(1,))):
+        out = []
+        for v in range(3):
+            g = gpu_lib.Solver(case, _prm(abi.FORM_MIXED, epcorr=1e-10, nouter=4))
+            assert "mx_outer:" in g.tuning()
+            g.force_variant("mx_outer", v)
+            _init_any(g, case)
+            rk = gpu_lib.rk_scheme("williamson")
+            for irk in range(1, 4):
+                g.timeintegrate_flow(1, 1, 0.0, 5e-4, irk, rk)
+            out.append([g.get(nm) for nm in "UVWP"])
+            g.close()
+        for o in out[1:]:
+            for a, b in zip(out[0], o):
+                assert np.array_equal(a, b)
