@@ -510,8 +510,9 @@ int mglet_gpu_set_partition(mglet_ctx* ctx, const int32_t* halo, int32_t nsend,
  * MGLET_TUNE=0 keeps the defaults.  The same holds for the packed sweeps
  * (ranks per thread, CTAs per SM), the flux kernel (plane loads or TMA) and
  * the persistent solve of single-level cases (the whole outer loop of
- * mgpoisl as one cooperative launch with grid-wide barriers; kept only when
- * it is faster than the per-phase kernels).  mglet_gpu_tuning describes the
+ * mgpoisl as one cooperative launch with grid-wide barriers; timed and
+ * reported, run only when forced: the per-phase kernels are faster in the
+ * stage graph).  mglet_gpu_tuning describes the
  * choices ("" for the plain form); mglet_gpu_force_variant overrides one
  * (kernel "mx_sip_pre" 0..9, "mx_sip_sweep" 0..4, "mx_flux" 0..1,
  * "mx_sip_solve" 0..5, "mx_outer_pre" 0..1 -- 1: on one level the outer step

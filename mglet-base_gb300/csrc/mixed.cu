@@ -541,9 +541,11 @@ std::string mixed_tuning(Ctx* c) {
                   s.sweep_variant >= 0 ? "" : " [default]", s.sweep_ms);
     char sbuf[512];
     int n = std::snprintf(sbuf, sizeof sbuf,
-                          "mx_sip_solve: %s (persistent %.4f ms, per-phase kernels %.4f ms per "
-                          "outer iteration; variants",
-                          sip_solve_variant_name(s.solve_variant), s.solve_ms, s.phases_ms);
+                          "mx_sip_solve: %s (fastest persistent: %s, %.4f ms; per-phase kernels "
+                          "%.4f ms per outer iteration; variants",
+                          sip_solve_variant_name(s.solve_variant),
+                          s.solve_best >= 0 ? sip_solve_variant_name(s.solve_best) : "none",
+                          s.solve_ms, s.phases_ms);
     for (int v = 0; v < sip_solve_variants() && n > 0 && n < (int)sizeof sbuf; ++v)
         n += std::snprintf(sbuf + n, sizeof sbuf - n, " %d: %.4f", v, s.solve_var_ms[v]);
     if (n > 0 && n < (int)sizeof sbuf) std::snprintf(sbuf + n, sizeof sbuf - n, "); ");

@@ -2307,7 +2307,10 @@ int sip_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int
 
 // Times two outer iterations of the per-phase kernels (the variants the
 // tuner kept) against each persistent variant, without stopping tests, and
-// keeps the persistent solve only if it is faster.
+// records the times.  The per-phase kernels stay in use: their eager
+// timing here carries launch costs that the stage graph does not pay, and
+// under a profiler's serialised launches it is skewed further, so the
+// persistent solve runs only when the caller forces it.
 int sip_tune_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int* gcls,
                    int* ctl, double* maxrhs, const double* sprm) {
     st.solve_variant = -1;
@@ -2320,11 +2323,10 @@ int sip_tune_solve(Ctx* c, SipState& st, const float* cf, const float* apx, cons
                                         c->prm.ninner, st.bm ? 1 : 0};
     auto it = cache.find(key);
     if (it != cache.end()) {
-        st.solve_variant = std::get<0>(it->second);
+        st.solve_best = std::get<0>(it->second);
         st.solve_ms = std::get<1>(it->second);
         st.phases_ms = std::get<2>(it->second);
         for (int v = 0; v < kNumSolve; ++v) st.solve_var_ms[v] = std::get<3>(it->second)[v];
-        if (st.solve_variant >= 0) return sip_solve_alloc(st);
         return 0;
     }
     if (int rc = sip_solve_alloc(st)) return rc;
@@ -2372,7 +2374,6 @@ int sip_tune_solve(Ctx* c, SipState& st, const float* cf, const float* apx, cons
     if (cudaError_t e = elapsed(&pms)) return done(e, "sip_tune_solve");
     st.phases_ms = pms / nouter;
     int best = -1;
-    double best_ms = st.phases_ms;
     double best_solve = 1e30;
     for (int v = 0; v < kNumSolve; ++v) {
         if (!sip_solve_fits(c, st, v)) continue;
@@ -2399,13 +2400,12 @@ int sip_tune_solve(Ctx* c, SipState& st, const float* cf, const float* apx, cons
         }
         const double per = ms / nouter;
         st.solve_var_ms[v] = per;
-        best_solve = std::min(best_solve, per);
-        if (per < best_ms) {
-            best_ms = per;
+        if (per < best_solve) {
+            best_solve = per;
             best = v;
         }
     }
-    st.solve_variant = best;
+    st.solve_best = best;
     st.solve_ms = best_solve < 1e30 ? best_solve : 0.0;
     cache[key] = {best, st.solve_ms, st.phases_ms,
                   std::vector<double>(st.solve_var_ms, st.solve_var_ms + kNumSolve)};

@@ -65,6 +65,7 @@ struct SipState {
     // in it and in the per-phase kernels, the barrier words [arrivals,
     // abort], and the test switch that makes its first barrier wait run out
     int solve_variant = -1;
+    int solve_best = -1;        // the fastest persistent variant the tuner timed
     double solve_ms = 0.0, phases_ms = 0.0;
     double solve_var_ms[6] = {0, 0, 0, 0, 0, 0};   // each variant's time (0: not run)
     unsigned* d_bar = nullptr;
@@ -135,7 +136,8 @@ int sip_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int
 // Times the outer-step variants on the case and keeps the fastest.
 int sip_tune_outer(Ctx* c, SipState& st, const float* apx, const int* gcls, int* ctl);
 // Times the persistent variants against the per-phase kernels (which the
-// tuner must have picked already) and keeps the faster form.
+// tuner must have picked already) and records the times; the persistent
+// solve runs only when forced.
 int sip_tune_solve(Ctx* c, SipState& st, const float* cf, const float* apx, const int* gcls,
                    int* ctl, double* maxrhs, const double* sprm);
 
