@@ -133,6 +133,9 @@ def parse():
                     help="skip the plain FP64 form timed beside the mixed headline")
     ap.add_argument("--no-profile", action="store_true",
                     help="skip the profiled pass (per-kernel times, roofline)")
+    ap.add_argument("--persistent", action="store_true",
+                    help="mixed form: run each pressure solve as the persistent cooperative "
+                         "launch (the fastest variant that applies) instead of the per-phase graph")
     ap.add_argument("--precision", action="store_true",
                     help="error of the mixed form against the plain FP64 form")
     ap.add_argument("--precision-field", choices=["solenoidal", "taylor-green"],
@@ -364,6 +367,14 @@ def time_form(args, form, case, fields, local, dist, profile=True):
 
     prm = flow_params(form)
     s = gpu.Solver(case, prm, device=local)
+    if form == "mixed" and getattr(args, "persistent", False):
+        # 256-thread variants, fastest first as measured on 24^3 grids
+        for v in (5, 2, 4, 1, 3, 0):
+            try:
+                s.force_variant("mx_sip_solve", v)
+                break
+            except gpu.MgletError:
+                continue
     for nm, a in zip("UVWP", fields):
         s.set(nm, a)
     s.connect(0, 2, "U", "V", "W", "P", corners=True)
