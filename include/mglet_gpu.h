@@ -326,6 +326,24 @@ int mglet_gpu_set_scalar_bc(mglet_ctx* ctx, int32_t igrid, int32_t iface, int32_
  * apply in the order added, after a constant source from
  * mglet_gpu_set_scalars; at most 8 per scalar. */
 int mglet_gpu_add_scalar_source(mglet_ctx* ctx, int32_t isca, const char* field, double value);
+/* Ghost-cell IB of the scalars (plain form).  With the ghost-cell IB
+ * (mglet_gpu_set_ghostcell) the scalars' blocking BT comes from BP as
+ * blockbt does (blockbt_mod.F90:11-208, also opening the cells behind PAR
+ * faces from the coarse BT), and each stage applies maskbt and
+ * set_scastencils("P") to QTT (the fixed-flux bodies) and to T (the
+ * fixed-value bodies), timeintegrate_scalar_mod.F90:71-90; the ftoc of T
+ * weighs by BT.  mglet_gpu_set_scastencils uploads grid igrid's list
+ * (gc_scastencils_mod.F90:10-16): per cell 9 integers {intcell, body,
+ * nstencils <= 6, six stencil cells; 1-based positions in the grid's flat
+ * array} and 8 reals {areabyvol, six coefficients, acoeffvel}, for the 'C'
+ * (xpolr) and 'P' (xpolrvel) forms.  mglet_gpu_set_scalar_geometry sets a
+ * scalar's condition per body (sca%geometries): flag 0 fixed value, 1 fixed
+ * flux, and the value; at most 16 bodies.  A cell without a body counts as
+ * fixed flux 0, as in the reference. */
+int mglet_gpu_set_scastencils(mglet_ctx* ctx, int32_t igrid, int32_t ncells, const int64_t* xpoli,
+                              const double* xpolr, const double* xpolrvel);
+int mglet_gpu_set_scalar_geometry(mglet_ctx* ctx, int32_t isca, int32_t nbody, const int32_t* flag,
+                                  const double* value);
 /* timeintegrate_scalar (src/scalar/timeintegrate_scalar_mod.F90:17-108): one
  * RK stage of every scalar on the current velocity; the reference calls it
  * before timeintegrate_flow in each stage (timeloop_mod.F90:233-235). */

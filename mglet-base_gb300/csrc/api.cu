@@ -814,6 +814,7 @@ int mglet_gpu_destroy(mglet_ctx* c) {
     cudaFree(c->d_pargrids);
     cudaFree(c->d_sptab);
     cudaFree(c->d_scabc_kind);
+    for (void* p : {(void*)c->d_sxi, (void*)c->d_sxr, (void*)c->d_sxrv, (void*)c->d_scell0}) cudaFree(p);
     cudaFree(c->d_scabc_type);
     for (auto& kv : c->d_pftasks) cudaFree(kv.second);
     cudaFree(c->d_gridred);
@@ -1200,7 +1201,21 @@ int mglet_gpu_set_ghostcell(mglet_ctx* c) {
     c->gc_saved[0] = c->gc_saved[1] = false;
     MG_CUDA(cudaStreamSynchronize(c->stream));
     if (c->prm.form == MGLET_FORM_MIXED) return mixed_ghostcell(c);
-    return 0;
+    // scalars set before the blocking: their BT from BP now
+    return scalar_blockbt(c);
+}
+
+int mglet_gpu_set_scastencils(mglet_ctx* c, int32_t igrid, int32_t ncells, const int64_t* xpoli,
+                              const double* xpolr, const double* xpolrvel) {
+    if (!c) return fail(MGLET_ERR_ARG, "set_scastencils: null context");
+    cudaSetDevice(c->device);
+    return set_scastencils(c, igrid, ncells, xpoli, xpolr, xpolrvel);
+}
+
+int mglet_gpu_set_scalar_geometry(mglet_ctx* c, int32_t isca, int32_t nbody, const int32_t* flag,
+                                  const double* value) {
+    if (!c) return fail(MGLET_ERR_ARG, "set_scalar_geometry: null context");
+    return set_scalar_geometry(c, isca, nbody, flag, value);
 }
 
 static int gc_ready(Ctx* c) {

@@ -176,6 +176,10 @@ struct Ctx {
         // sources in order: empty field name = constant (sourceterm_const),
         // else value * field (sourceterm_field)
         std::vector<std::pair<std::string, double>> sources;
+        // per body of the ghost-cell IB (sca%geometries): flag 0 fixed
+        // value, 1 fixed flux, and the value
+        std::vector<int> geo_flag;
+        std::vector<double> geo_value;
     };
     std::vector<ScalarDef> sca;
     double prturb = 1.0;
@@ -193,6 +197,20 @@ struct Ctx {
     void* d_sptab = nullptr;     // device table of the 12 spacing arrays (adjoint)
     std::vector<GcHostList> gch;
     GcDev gcd;
+    // scalar ghost-cell lists (gc_scastencils_mod.F90:10-16) per grid: per
+    // cell 9 integers {intcell, body, nstencils, six stencil cells} and 8
+    // reals {areabyvol, six coefficients, acoeffvel}; on the device all
+    // grids' records back to back with the first cell of each grid
+    struct ScaList {
+        int ncells = 0;
+        std::vector<int64_t> xpoli;
+        std::vector<double> xpolr, xpolrvel;
+    };
+    std::vector<ScaList> scal;
+    long long* d_sxi = nullptr;
+    double *d_sxr = nullptr, *d_sxrv = nullptr;
+    long long* d_scell0 = nullptr;   // [ngrid + 1]
+    int scal_maxbody = 0;            // the largest body number in the lists
     // grid hierarchy (gridinfo%iparent, i/j/kposition): per grid {parent
     // 0-based or -1, iposition, jposition, kposition}; per level the grids
     // with a parent (ftoc / ctof) and per level and face the grids with a
@@ -295,6 +313,11 @@ int init_viscosity(Ctx* c);                  // G of init_lesmodel, model "none"
 int launch_bound_g(Ctx* c, int ilevel);      // the bound of G (lesmodel_mod.F90:573-764)
 int lesmodel(Ctx* c);                        // G from the LES model (les.cu)
 int set_lesmodel(Ctx* c, int model, double cm);
+// scalar ghost-cell IB (scalar.cu): BT from BP, the lists, the conditions
+int scalar_blockbt(Ctx* c);
+int set_scastencils(Ctx* c, int igrid, int ncells, const int64_t* xpoli, const double* xpolr,
+                    const double* xpolrvel);
+int set_scalar_geometry(Ctx* c, int isca, int nbody, const int32_t* flag, const double* value);
 int fill_field(Ctx* c, double* a, double v);   // a[0..idim3d) = v (api.cu)
 // scalar transport (scalar.cu)
 int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawford, const double* source,

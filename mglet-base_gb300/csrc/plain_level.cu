@@ -1265,8 +1265,13 @@ int launch_ftoc(Ctx* c, int ilevel, const double* ff, double* fc, char flag) {
     if (c->ibtype == 1 && flag == 'P') A.flag = 'G';       // gc_restrict_t
     if (c->ibtype == 1 && flag == 'R') A.flag = 'H';
     if (c->ibtype == 1 && flag == 'T') {
-        set_error("ftoc: the ghost-cell T restriction weighs by BT, which is not kept");
-        return MGLET_ERR_UNSUPPORTED;
+        // restrict_p weighted by BT instead of BP (gc_restrict_mod.F90:85-89)
+        if (!c->f3.count("BT")) {
+            set_error("ftoc: the ghost-cell T restriction weighs by BT (set_scalars first)");
+            return MGLET_ERR_UNSUPPORTED;
+        }
+        A.flag = 'G';
+        A.bp = c->F("BT");
     }
     int maxq = 0;
     for (int g : list) {

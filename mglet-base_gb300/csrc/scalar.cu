@@ -318,6 +318,114 @@ __global__ void k_momentum_sources(const DevGrid* __restrict__ grids, double* UO
     }
 }
 
+// ---- ghost-cell IB of the scalars -------------------------------------------
+// blockbt (blockbt_mod.F90:11-208), maskbt (scacore_mod.F90:265-306) and
+// set_scastencils (gc_scastencils_mod.F90:949-1125).
+constexpr int kScaIsize = 9, kScaRsize = 8, kScaNperi = 6, kScaMaxBody = 16;
+
+__device__ __forceinline__ double mxd(double a, double b) { return a < b ? b : a; }
+
+// blockbt_grid (:73-91): bt = the largest bp of the cell and its six face
+// neighbours, on 2..n-1
+__global__ void k_blockbt(const DevGrid* __restrict__ grids, const double* __restrict__ BP, double* BT) {
+    const DevGrid G = grids[blockIdx.y];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)kk * jj * ii) return;
+    const int k = (int)(q % kk) + 1, j = (int)((q / kk) % jj) + 1, i = (int)(q / ((long long)kk * jj)) + 1;
+    if (i < 2 || i > ii - 1 || j < 2 || j > jj - 1 || k < 2 || k > kk - 1) return;
+    const double* bp = BP + G.ip3;
+    BT[G.ip3 + IX(k, j, i)] = mxd(mxd(mxd(mxd(mxd(mxd(bp[IX(k, j, i)], bp[IX(k, j, i + 1)]), bp[IX(k, j, i - 1)]),
+                                                 bp[IX(k, j + 1, i)]),
+                                             bp[IX(k, j - 1, i)]),
+                                         bp[IX(k + 1, j, i)]),
+                                     bp[IX(k - 1, j, i)]);
+}
+
+// open_scalarflux_boundary (:93-208): one CTA per grid of the level, its PAR
+// faces in order; the receiver layer opens where the coarse cell lets a
+// scalar flux through (hilf from ctof of BT, -1 where ctof wrote nothing)
+__global__ void k_open_scaflux(const DevGrid* __restrict__ grids, const int* __restrict__ list,
+                               const double* __restrict__ HILF, double* BT, int* err) {
+    const DevGrid G = grids[list[blockIdx.x]];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const double* hf = HILF + G.ip3;
+    double* bt = BT + G.ip3;
+    for (int f = 1; f <= 6; ++f) {
+        if (G.bc[f - 1] != MGLET_BC_PAR) continue;
+        const int ax = (f - 1) / 2, hi = (f - 1) % 2;
+        const int n = ax == 0 ? ii : (ax == 1 ? jj : kk);
+        const int p2 = hi ? n - 1 : 2, p3 = hi ? n - 2 : 3;
+        const int na = ax == 0 ? jj : ii, nb = ax == 2 ? jj : kk;
+        for (int t = threadIdx.x; t < (na - 2) * (nb - 2); t += blockDim.x) {
+            const int a = 2 + t / (nb - 2), b = 2 + t % (nb - 2);
+            int k2, j2, i2, k3, j3, i3;
+            if (ax == 0) { i2 = p2; i3 = p3; j2 = j3 = a; k2 = k3 = b; }
+            else if (ax == 1) { j2 = p2; j3 = p3; i2 = i3 = a; k2 = k3 = b; }
+            else { k2 = p2; k3 = p3; i2 = i3 = a; j2 = j3 = b; }
+            const double c2 = hf[IX(k2, j2, i2)], c3 = hf[IX(k3, j3, i3)];
+            if (c2 < -0.5 || c3 < -0.5) {
+                atomicExch(err, 1);
+                continue;
+            }
+            bt[IX(k3, j3, i3)] = mxd(c2 * c3, bt[IX(k3, j3, i3)]);
+        }
+        __syncthreads();
+    }
+}
+
+// maskbt_grid (scacore_mod.F90:289-306): t *= bt on 3..n-2
+__global__ void k_maskbt(const DevGrid* __restrict__ grids, double* T, const double* __restrict__ BT) {
+    const DevGrid G = grids[blockIdx.y];
+    const int kk = G.kk, jj = G.jj, ii = G.ii;
+    const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= (long long)kk * jj * ii) return;
+    const int k = (int)(q % kk) + 1, j = (int)((q / kk) % jj) + 1, i = (int)(q / ((long long)kk * jj)) + 1;
+    if (i < 3 || i > ii - 2 || j < 3 || j > jj - 2 || k < 3 || k > kk - 2) return;
+    T[G.ip3 + q] = T[G.ip3 + q] * BT[G.ip3 + q];
+}
+
+// the conditions of the bodies for one scalar (sca%geometries)
+struct ScaGeo {
+    int n;
+    int flag[kScaMaxBody];
+    double value[kScaMaxBody];
+};
+
+// set_scastencils (:1005-1125): one thread per grid walks its cells in list
+// order (a value set for one cell may feed a later cell's stencil).  tmode:
+// a fixed-value body sets var(intcell) from its stencil cells and acoeffvel
+// * value; else a fixed-flux body (or no body) adds areabyvol * value.
+__global__ void k_scastencils(const DevGrid* __restrict__ grids, int ngrid, const long long* __restrict__ xi,
+                              const double* __restrict__ xr, const long long* __restrict__ cell0, ScaGeo geo,
+                              double* var, int tmode) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= ngrid) return;
+    double* v = var + grids[g].ip3;
+    for (long long cell = cell0[g]; cell < cell0[g + 1]; ++cell) {
+        const long long* I = xi + cell * kScaIsize;
+        const double* r = xr + cell * kScaRsize;
+        const long long intcell = I[0], body = I[1];
+        int bctype = 1;
+        double bcval = 0.0;
+        if (body > 0) {
+            bctype = geo.flag[body - 1];
+            bcval = geo.value[body - 1];
+        }
+        if (tmode) {
+            double val = 0.0;
+            for (long long n = 1; n <= I[2]; ++n) val = val + v[I[2 + n] - 1] * r[n];
+            const double coeff = r[1 + kScaNperi];
+            if (bctype == 0) {
+                val = val + coeff * bcval;
+                v[intcell - 1] = val;
+            }
+        } else if (bctype == 1) {
+            v[intcell - 1] = v[intcell - 1] + r[0] * bcval;
+        }
+    }
+}
+
 #undef IX
 
 }  // namespace
@@ -343,8 +451,8 @@ int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawfo
         set_error("set_scalars: 0..9 scalars with prmol and kayscrawford");
         return MGLET_ERR_ARG;
     }
-    if (nsca && (c->prm.form != MGLET_FORM_PLAIN || c->ibtype == 1)) {
-        set_error("set_scalars: the plain form without the ghost-cell IB");
+    if (nsca && c->prm.form != MGLET_FORM_PLAIN) {
+        set_error("set_scalars: the plain form");
         return MGLET_ERR_UNSUPPORTED;
     }
     c->sca.clear();
@@ -366,7 +474,138 @@ int set_scalars(Ctx* c, int nsca, const double* prmol, const int32_t* kayscrawfo
         if (!c->f3.count(n))
             if (int rc = alloc_field3(c, n)) return rc;
     // blockbt: every cell open without the ghost-cell IB
-    return fill_field(c, c->F("BT"), 1.0);
+    if (int rc = fill_field(c, c->F("BT"), 1.0)) return rc;
+    return c->ibtype == 1 ? scalar_blockbt(c) : 0;
+}
+
+// blockbt (blockbt_mod.F90:11-70) with the ghost-cell IB: BT from BP,
+// connected per level, then per level the cells behind PAR faces opened
+// from ctof of BT into a scratch field preset to -1
+int scalar_blockbt(Ctx* c) {
+    if (!c->f3.count("BT")) return 0;
+    int m = 0;
+    for (const DevGrid& g : c->grids) m = std::max(m, g.kk * g.jj * g.ii);
+    double* BT = c->F("BT");
+    k_blockbt<<<dim3((m + 255) / 256, c->ngrid), 256, 0, c->stream>>>(c->d_grids, c->F("BP"), BT);
+    MG_LAUNCHED(c);
+    for (int l = c->minlevel; l <= c->maxlevel; ++l)
+        if (int rc = connect(c, l, 2, nullptr, nullptr, nullptr, BT, nullptr, nullptr, true, false, 0)) return rc;
+    if (!c->f3.count("BTH"))
+        if (int rc = alloc_field3(c, "BTH")) return rc;
+    int* d_err = nullptr;
+    MG_CUDA(cudaMalloc(&d_err, sizeof(int)));
+    MG_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), c->stream));
+    int rc = 0;
+    for (int l = c->minlevel; l <= c->maxlevel && !rc; ++l) {
+        if ((rc = fill_field(c, c->F("BTH"), -1.0))) break;
+        if (c->minlevel != c->maxlevel) {
+            if ((rc = launch_ctof(c, l, c->F("BTH"), BT))) break;
+            auto it = c->d_children.find(l);
+            if (l != c->minlevel && it != c->d_children.end()) {
+                k_open_scaflux<<<(unsigned)c->children[l].size(), 128, 0, c->stream>>>(
+                    c->d_grids, it->second, c->F("BTH"), BT, d_err);
+                if (cudaGetLastError() != cudaSuccess) rc = MGLET_ERR_CUDA;
+                c->launches++;
+            }
+        }
+        if (!rc) rc = connect(c, l, 2, nullptr, nullptr, nullptr, BT, nullptr, nullptr, true, false, 0);
+    }
+    int herr = 0;
+    cudaMemcpyAsync(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_err);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "blockbt");
+    if (herr) {
+        set_error("blockbt: a fine cell behind a PAR face has no coarse value");
+        return MGLET_ERR_ARG;
+    }
+    return 0;
+}
+
+// The scalar ghost-cell list of grid igrid (1-based), kept on the host and
+// uploaded with every grid's list back to back.
+int set_scastencils(Ctx* c, int igrid, int ncells, const int64_t* xpoli, const double* xpolr,
+                    const double* xpolrvel) {
+    if (igrid < 1 || igrid > c->ngrid || ncells < 0 || (ncells && (!xpoli || !xpolr || !xpolrvel))) {
+        set_error("set_scastencils: bad grid or lists");
+        return MGLET_ERR_ARG;
+    }
+    const DevGrid& G = c->grids[igrid - 1];
+    const int64_t npts = (int64_t)G.kk * G.jj * G.ii;
+    for (int cell = 0; cell < ncells; ++cell) {
+        const int64_t* xi = xpoli + (size_t)cell * kScaIsize;
+        bool bad = xi[0] < 1 || xi[0] > npts || xi[2] < 0 || xi[2] > kScaNperi || xi[1] > kScaMaxBody;
+        for (int64_t n = 1; n <= xi[2] && !bad; ++n) bad = xi[2 + n] < 1 || xi[2 + n] > npts;
+        if (bad) {
+            set_error("set_scastencils: cell, body or stencil out of range");
+            return MGLET_ERR_ARG;
+        }
+    }
+    if ((int)c->scal.size() < c->ngrid) c->scal.resize(c->ngrid);
+    Ctx::ScaList& L = c->scal[igrid - 1];
+    L.ncells = ncells;
+    L.xpoli.assign(xpoli, xpoli + (size_t)ncells * kScaIsize);
+    L.xpolr.assign(xpolr, xpolr + (size_t)ncells * kScaRsize);
+    L.xpolrvel.assign(xpolrvel, xpolrvel + (size_t)ncells * kScaRsize);
+    std::vector<long long> xi, cell0(c->ngrid + 1, 0);
+    std::vector<double> xr, xv;
+    c->scal_maxbody = 0;
+    for (int g = 0; g < c->ngrid; ++g) {
+        const Ctx::ScaList& S = c->scal[g];
+        cell0[g + 1] = cell0[g] + S.ncells;
+        xi.insert(xi.end(), S.xpoli.begin(), S.xpoli.end());
+        xr.insert(xr.end(), S.xpolr.begin(), S.xpolr.end());
+        xv.insert(xv.end(), S.xpolrvel.begin(), S.xpolrvel.end());
+        for (int cell = 0; cell < S.ncells; ++cell)
+            c->scal_maxbody = std::max(c->scal_maxbody, (int)S.xpoli[(size_t)cell * kScaIsize + 1]);
+    }
+    for (void* p : {(void*)c->d_sxi, (void*)c->d_sxr, (void*)c->d_sxrv, (void*)c->d_scell0}) cudaFree(p);
+    c->d_sxi = nullptr; c->d_sxr = nullptr; c->d_sxrv = nullptr; c->d_scell0 = nullptr;
+    auto up = [&](void** d, const void* h, size_t n) -> int {
+        MG_CUDA(cudaMalloc(d, std::max<size_t>(n, 8)));
+        if (n) MG_CUDA(copy_on(c->stream, *d, h, n, cudaMemcpyHostToDevice));
+        return 0;
+    };
+    if (int rc = up((void**)&c->d_sxi, xi.data(), xi.size() * sizeof(long long))) return rc;
+    if (int rc = up((void**)&c->d_sxr, xr.data(), xr.size() * sizeof(double))) return rc;
+    if (int rc = up((void**)&c->d_sxrv, xv.data(), xv.size() * sizeof(double))) return rc;
+    return up((void**)&c->d_scell0, cell0.data(), cell0.size() * sizeof(long long));
+}
+
+int set_scalar_geometry(Ctx* c, int isca, int nbody, const int32_t* flag, const double* value) {
+    if (isca < 1 || isca > (int)c->sca.size() || nbody < 0 || nbody > kScaMaxBody ||
+        (nbody && (!flag || !value))) {
+        set_error("set_scalar_geometry: bad scalar or bodies (at most 16)");
+        return MGLET_ERR_ARG;
+    }
+    for (int b = 0; b < nbody; ++b)
+        if (flag[b] != 0 && flag[b] != 1) {
+            set_error("set_scalar_geometry: flag 0 (fixed value) or 1 (fixed flux)");
+            return MGLET_ERR_ARG;
+        }
+    c->sca[isca - 1].geo_flag.assign(flag, flag + nbody);
+    c->sca[isca - 1].geo_value.assign(value, value + nbody);
+    return 0;
+}
+
+// set_scastencils("P", sca, t= or qtt=) on every grid
+static int launch_scastencils(Ctx* c, const Ctx::ScalarDef& sd, double* var, bool tmode) {
+    if (!c->d_scell0) return 0;
+    if (c->scal_maxbody > (int)sd.geo_flag.size()) {
+        set_error("timeintegrate_scalar: a body of the lists has no condition for " + sd.name);
+        return MGLET_ERR_ARG;
+    }
+    ScaGeo geo{};
+    geo.n = (int)sd.geo_flag.size();
+    for (int b = 0; b < geo.n; ++b) {
+        geo.flag[b] = sd.geo_flag[b];
+        geo.value[b] = sd.geo_value[b];
+    }
+    k_scastencils<<<(c->ngrid + 63) / 64, 64, 0, c->stream>>>(c->d_grids, c->ngrid, c->d_sxi, c->d_sxrv,
+                                                             c->d_scell0, geo, var, tmode ? 1 : 0);
+    MG_LAUNCHED(c);
+    return 0;
 }
 
 int add_scalar_source(Ctx* c, int isca, const char* field, double value) {
@@ -503,7 +742,20 @@ int timeintegrate_scalar(Ctx* c, double dt, int irk, const mglet_rk_scheme* rk) 
         k_fluxbalance<<<bg, 256, 0, c->stream>>>(c->d_grids, c->F("QTU"), c->F("QTV"), c->F("QTW"), c->F("QTT"),
                                                  c->L("RDDX"), c->L("RDDY"), c->L("RDDZ"), src);
         MG_LAUNCHED(c);
+        const bool gc = c->ibtype == 1;
+        // timeintegrate_scalar_mod.F90:71-73: the flux condition of the bodies
+        if (gc)
+            if (int rc = launch_scastencils(c, sd, c->F("QTT"), false)) return rc;
         if (int rc = launch_rkstep(c, T, DT, c->F("QTT"), frhs, dt * fu)) return rc;
+        if (gc) {
+            // :84 maskbt (a no-op with BT = 1 without the IB), :87-90 the value
+            // condition of the bodies after the connect
+            k_maskbt<<<bg, 256, 0, c->stream>>>(c->d_grids, T, c->F("BT"));
+            MG_LAUNCHED(c);
+            if (int rc = connect(c, 0, 2, nullptr, nullptr, nullptr, T, nullptr, nullptr, true, false, 0))
+                return rc;
+            if (int rc = launch_scastencils(c, sd, T, true)) return rc;
+        }
         for (int l = c->maxlevel; l > c->minlevel; --l)
             if (int rc = launch_ftoc(c, l, T, T, 'T')) return rc;
         if (int rc = connect(c, 0, 2, nullptr, nullptr, nullptr, T, nullptr, nullptr, true, false, 0)) return rc;

@@ -36,7 +36,8 @@ EXPORTS = [
     "mglet_gpu_add_scalar_source", "mglet_gpu_fp64_roof", "mglet_gpu_tuning",
     "mglet_gpu_force_variant", "mglet_create_flowstencils", "mglet_flowstencils_size",
     "mglet_flowstencils_copy", "mglet_flowstencils_free", "mglet_gpu_set_partition",
-    "mglet_gpu_test_wait_timeout", "mglet_gpu_test_barrier_timeout", "mglet_mesh_create",
+    "mglet_gpu_test_wait_timeout", "mglet_gpu_test_barrier_timeout", "mglet_gpu_set_scastencils",
+    "mglet_gpu_set_scalar_geometry", "mglet_mesh_create",
     "mglet_mesh_distance", "mglet_mesh_free",
 ]
 
@@ -121,6 +122,8 @@ def load(path=None):
     L.mglet_gpu_force_variant.argtypes = [vp, cp, C.c_int32]
     L.mglet_gpu_test_wait_timeout.argtypes = [vp]
     L.mglet_gpu_test_barrier_timeout.argtypes = [vp]
+    L.mglet_gpu_set_scastencils.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp]
+    L.mglet_gpu_set_scalar_geometry.argtypes = [vp, C.c_int32, C.c_int32, vp, vp]
     L.mglet_mesh_create.argtypes = [vp, C.c_int64, C.POINTER(vp)]
     L.mglet_mesh_distance.argtypes = [vp, vp, C.c_int64, vp, vp]
     L.mglet_mesh_free.argtypes = [vp]
@@ -398,6 +401,22 @@ class Solver:
 
     def test_wait_timeout(self):
         _check(load().mglet_gpu_test_wait_timeout(self.h))
+
+    def set_scastencils(self, igrid, xpoli, xpolr, xpolrvel):
+        """Scalar ghost-cell list of grid igrid (1-based): per cell 9 integers
+        and 8 reals (see mglet_gpu_set_scastencils)."""
+        xi = np.ascontiguousarray(xpoli, dtype=np.int64)
+        xr = np.ascontiguousarray(xpolr, dtype=np.float64)
+        xv = np.ascontiguousarray(xpolrvel, dtype=np.float64)
+        _check(load().mglet_gpu_set_scastencils(self.h, igrid, len(xi) // 9, xi.ctypes.data_as(C.c_void_p),
+                                                xr.ctypes.data_as(C.c_void_p), xv.ctypes.data_as(C.c_void_p)))
+
+    def set_scalar_geometry(self, isca, flags, values):
+        """Per body the scalar's condition: flag 0 fixed value, 1 fixed flux."""
+        fl = np.ascontiguousarray(flags, dtype=np.int32)
+        va = np.ascontiguousarray(values, dtype=np.float64)
+        _check(load().mglet_gpu_set_scalar_geometry(self.h, isca, len(fl), fl.ctypes.data_as(C.c_void_p),
+                                                    va.ctypes.data_as(C.c_void_p)))
 
     def test_barrier_timeout(self):
         _check(load().mglet_gpu_test_barrier_timeout(self.h))

@@ -71,6 +71,8 @@ def lib():
         _lib.oracle_set_coriolis.argtypes = [vp, vp]
         _lib.oracle_set_scalar_bc.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp]
         _lib.oracle_add_scalar_source.argtypes = [vp, C.c_int, C.c_char_p, C.c_double]
+        _lib.oracle_set_scastencils.argtypes = [vp, C.c_int, C.c_int, vp, vp, vp]
+        _lib.oracle_set_scalar_geometry.argtypes = [vp, C.c_int, C.c_int, vp, vp]
         _lib.oracle_par_ftoc_norm.argtypes = [vp, C.c_int] + [C.c_char_p] * 3 + [C.c_int]
         _lib.oracle_ctof.argtypes = [vp, C.c_int, C.c_char_p, C.c_char_p]
         _lib.oracle_bound_pressure.argtypes = [vp, C.c_int, C.c_char_p, C.c_int]
@@ -260,6 +262,25 @@ class Oracle:
 
     def add_scalar_source(self, isca, value, field=None):
         _check(lib().oracle_add_scalar_source(self.h, isca, field.encode() if field else None, value))
+
+    def set_scastencils(self, igrid, xpoli, xpolr, xpolrvel):
+        """Scalar ghost-cell list of grid igrid (1-based): per cell 9 integers
+        {intcell, body, nstencils, six stencil cells} and 8 reals {areabyvol,
+        six coefficients, acoeffvel}, for the 'C' (xpolr) and 'P' (xpolrvel)
+        forms."""
+        xi = np.ascontiguousarray(xpoli, dtype=np.int64)
+        xr = np.ascontiguousarray(xpolr, dtype=np.float64)
+        xv = np.ascontiguousarray(xpolrvel, dtype=np.float64)
+        _check(lib().oracle_set_scastencils(self.h, igrid, len(xi) // 9, xi.ctypes.data_as(C.c_void_p),
+                                            xr.ctypes.data_as(C.c_void_p), xv.ctypes.data_as(C.c_void_p)))
+
+    def set_scalar_geometry(self, isca, flags, values):
+        """Per body of the ghost-cell IB the scalar's condition: flag 0 fixed
+        value, 1 fixed flux, and its value."""
+        fl = np.ascontiguousarray(flags, dtype=np.int32)
+        va = np.ascontiguousarray(values, dtype=np.float64)
+        _check(lib().oracle_set_scalar_geometry(self.h, isca, len(fl), fl.ctypes.data_as(C.c_void_p),
+                                                va.ctypes.data_as(C.c_void_p)))
 
     def set_scalar_bc(self, igrid, iface, kind, types=()):
         ty = np.ascontiguousarray(list(types) + [0] * 9, dtype=np.int32)

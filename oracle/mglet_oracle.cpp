@@ -159,6 +159,10 @@ struct Ctx {
         // the scalar's sources in order (sca%sources): an empty field name
         // is sourceterm_const, else sourceterm_field of that field
         std::vector<std::pair<std::string, double>> sources;
+        // per body of the ghost-cell IB (sca%geometries): flag 0 fixed
+        // value, 1 fixed flux, and the value
+        std::vector<int> geo_flag;
+        std::vector<double> geo_value;
     };
     std::vector<ScalarDef> sca;
     double prturb = 1.0;
@@ -171,6 +175,15 @@ struct Ctx {
     int buoyancy_scalar = 1;
     double cm = 0.0;             // LES model constant
     std::vector<std::array<GcList, 3>> gcl;   // [grid][component], 1-based grids
+    // scalar ghost-cell lists (gc_scastencils_mod.F90:10-16), 1-based grids:
+    // per cell 9 integers {intcell, body, nstencils, six stencil cells} and
+    // 8 reals {areabyvol, six coefficients, acoeffvel}
+    struct ScaList {
+        int ncells = 0;
+        std::vector<int64_t> xpoli;
+        std::vector<double> xpolr, xpolrvel;
+    };
+    std::vector<ScaList> scal;
     std::vector<GcFlux> gcf;
     // grid hierarchy (gridinfo%iparent and i/j/kposition, grids_mod.F90):
     // iparent[g] 1-based (0 = none), pos[g] = (iposition, jposition,
@@ -1539,13 +1552,14 @@ void restrict_range(const Grid& G, char flag, int r[6]) {
 // take the BP-weighted forms; U, V, W and S stay the no-IB means.
 void ftoc_one(Ctx& c, int ilevel, const std::string& ff, const std::string& fc, char flag) {
     const char f = (flag == 'P' || flag == 'R' || flag == 'S' || flag == 'T') ? 'P' : flag;
-    const bool gcp = c.ibtype == 1 && flag == 'P', gcr = c.ibtype == 1 && flag == 'R';
+    // restrict_p weighs P by BP and T by BT (gc_restrict_mod.F90:85-89)
+    const bool gcp = c.ibtype == 1 && (flag == 'P' || flag == 'T'), gcr = c.ibtype == 1 && flag == 'R';
     for (int g = 1; g <= c.ngrid; ++g) {
         const Grid& G = c.g[g];
         if (G.level != ilevel || !c.iparent[g]) continue;
         const Grid& P = c.g[c.iparent[g]];
         const int kk = G.kk, jj = G.jj;
-        const double* bp = c.F("BP") + G.ip3;
+        const double* bp = c.F(flag == 'T' && c.ibtype == 1 ? "BT" : "BP") + G.ip3;
         const double* fv = c.F(ff.c_str()) + G.ip3;
         double* cv = c.F(fc.c_str()) + P.ip3;
         const double* ddx = c.L("DDX") + G.ipx - 1;
@@ -2398,6 +2412,126 @@ void bound_scaflux_walls(Ctx& c, int ilevel, int l, const double* T) {
 // timeintegrate_scalar (timeintegrate_scalar_mod.F90:17-108) for every
 // scalar: fluxes, PAR fluxes from the parent, flux balance, source, RK
 // update, restriction and the corner connect
+// ---------------------------------------------------------------------------
+// Ghost-cell IB of the scalars: blockbt (blockbt_mod.F90:11-208), maskbt
+// (scacore_mod.F90:265-306) and set_scastencils (gc_scastencils_mod.F90:
+// 949-1125).
+constexpr int kScaIsize = 9, kScaRsize = 8, kScaNperi = 6;
+
+// BT from BP: a cell is open where it or a face neighbour is fluid
+// (blockbt_grid, :73-91, on 2..n-1), connected per level; on the finer levels
+// the cells behind a PAR face open where the coarse cell lets a scalar flux
+// through (open_scalarflux_boundary, :93-208, from ctof of BT).
+int blockbt(Ctx& c) {
+    double* BT = c.F("BT");
+    const double* BP = c.F("BP");
+    auto mx = [](double a, double b) { return a < b ? b : a; };
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        const double* bp = BP + G.ip3;
+        double* bt = BT + G.ip3;
+        for (int i = 2; i <= ii - 1; ++i)
+            for (int j = 2; j <= jj - 1; ++j)
+                for (int k = 2; k <= kk - 1; ++k)
+                    bt[IX(k, j, i)] = mx(mx(mx(mx(mx(mx(bp[IX(k, j, i)], bp[IX(k, j, i + 1)]), bp[IX(k, j, i - 1)]),
+                                                  bp[IX(k, j + 1, i)]),
+                                               bp[IX(k, j - 1, i)]),
+                                            bp[IX(k + 1, j, i)]),
+                                         bp[IX(k - 1, j, i)]);
+    }
+    for (int l = c.minlevel; l <= c.maxlevel; ++l)
+        connect(c, l, 2, nullptr, nullptr, nullptr, BT, nullptr, nullptr, true, false, 0);
+    c.f3["BTH"].assign(c.idim3d, 0.0);
+    for (int l = c.minlevel; l <= c.maxlevel; ++l) {
+        std::fill(c.f3["BTH"].begin(), c.f3["BTH"].end(), -1.0);
+        if (c.minlevel != c.maxlevel) ctof(c, l, "BTH", "BT");
+        const double* H = c.F("BTH");
+        BT = c.F("BT");
+        for (int g = 1; g <= c.ngrid; ++g) {
+            const Grid& G = c.g[g];
+            if (G.level != l) continue;
+            const int kk = G.kk, jj = G.jj, ii = G.ii;
+            const double* hf = H + G.ip3;
+            double* bt = BT + G.ip3;
+            // faces front, back, right, left, bottom, top: the receiver
+            // layer (3 or n-2) from the ghost (2 or n-1) and itself
+            for (int f = 1; f <= 6; ++f) {
+                if (G.bc[f] != MGLET_BC_PAR) continue;
+                const int ax = (f - 1) / 2, hi = (f - 1) % 2;
+                const int n = ax == 0 ? ii : (ax == 1 ? jj : kk);
+                const int p2 = hi ? n - 1 : 2, p3 = hi ? n - 2 : 3;
+                const int na = ax == 0 ? jj : ii, nb = ax == 2 ? jj : kk;   // the two other axes
+                for (int a = 2; a <= na - 1; ++a)
+                    for (int b = 2; b <= nb - 1; ++b) {
+                        int k2, j2, i2, k3, j3, i3;
+                        if (ax == 0) { i2 = p2; i3 = p3; j2 = j3 = a; k2 = k3 = b; }
+                        else if (ax == 1) { j2 = p2; j3 = p3; i2 = i3 = a; k2 = k3 = b; }
+                        else { k2 = p2; k3 = p3; i2 = i3 = a; j2 = j3 = b; }
+                        const double c2 = hf[IX(k2, j2, i2)], c3 = hf[IX(k3, j3, i3)];
+                        if (c2 < -0.5 || c3 < -0.5)
+                            return fail(MGLET_ERR_ARG, "blockbt: a fine cell behind a PAR face has no coarse value");
+                        bt[IX(k3, j3, i3)] = mx(c2 * c3, bt[IX(k3, j3, i3)]);
+                    }
+            }
+        }
+        connect(c, l, 2, nullptr, nullptr, nullptr, BT, nullptr, nullptr, true, false, 0);
+    }
+    return 0;
+}
+
+// maskbt_grid (scacore_mod.F90:289-306): t *= bt on 3..n-2
+void maskbt(Ctx& c, double* T) {
+    const double* BT = c.F("BT");
+    for (int g = 1; g <= c.ngrid; ++g) {
+        const Grid& G = c.g[g];
+        const int kk = G.kk, jj = G.jj, ii = G.ii;
+        double* t = T + G.ip3;
+        const double* bt = BT + G.ip3;
+        for (int i = 3; i <= ii - 2; ++i)
+            for (int j = 3; j <= jj - 2; ++j)
+                for (int k = 3; k <= kk - 2; ++k) t[IX(k, j, i)] = t[IX(k, j, i)] * bt[IX(k, j, i)];
+    }
+}
+
+// set_scastencils(ctyp, sca, t= or qtt=) (:949-1125): per grid the cells in
+// list order; t: a fixed-value body sets var(intcell) from its stencil
+// cells and acoeffvel * value; qtt: a fixed-flux body adds areabyvol *
+// value.  A cell without a body (body <= 0) counts as fixed flux 0.
+int sca_stencils(Ctx& c, char ctyp, const Ctx::ScalarDef& sd, double* T, double* QTT) {
+    for (int g = 1; g <= c.ngrid; ++g) {
+        if ((int)c.scal.size() <= g) break;
+        const Ctx::ScaList& L = c.scal[g];
+        const std::vector<double>& xr = ctyp == 'C' ? L.xpolr : L.xpolrvel;
+        double* var = (T ? T : QTT) + c.g[g].ip3;
+        for (int cell = 0; cell < L.ncells; ++cell) {
+            const int64_t* xi = L.xpoli.data() + (size_t)cell * kScaIsize;
+            const double* r = xr.data() + (size_t)cell * kScaRsize;
+            const int64_t intcell = xi[0], body = xi[1];
+            int bctype = 1;
+            double bcval = 0.0;
+            if (body > 0) {
+                if (body > (int64_t)sd.geo_flag.size())
+                    return fail(MGLET_ERR_ARG, "set_scastencils: a body without a scalar condition");
+                bctype = sd.geo_flag[body - 1];
+                bcval = sd.geo_value[body - 1];
+            }
+            if (T) {
+                double val = 0.0;
+                for (int64_t n = 1; n <= xi[2]; ++n) val = val + var[xi[2 + n] - 1] * r[n];
+                const double coeff = r[1 + kScaNperi];
+                if (bctype == 0) {
+                    val = val + coeff * bcval;
+                    var[intcell - 1] = val;
+                }
+            } else if (bctype == 1) {
+                var[intcell - 1] = var[intcell - 1] + r[0] * bcval;
+            }
+        }
+    }
+    return 0;
+}
+
 int timeintegrate_scalar(Ctx& c, double dt, int irk, const mglet_rk_scheme* rk) {
     double frhs, fu, dtrk, dtrki;
     if (irk > rk->nrk || irk < 1) return fail(MGLET_ERR_ARG, "timeintegrate_scalar: irk out of range");
@@ -2446,7 +2580,15 @@ int timeintegrate_scalar(Ctx& c, double dt, int irk, const mglet_rk_scheme* rk) 
                         qtt[o + IX(k, j, i)] = q;
                     }
         }
+        // timeintegrate_scalar_mod.F90:71-73: the flux condition of the bodies
+        if (c.ibtype == 1)
+            if (int rc = sca_stencils(c, 'P', sd, nullptr, qtt)) return rc;
         rkstep(T, DT, qtt, c.idim3d, frhs, dt * fu);
+        maskbt(c, T);   // :84 (BT = 1 without the ghost-cell IB)
+        if (c.ibtype == 1) {   // :87-90: the value condition of the bodies
+            connect(c, 0, 2, nullptr, nullptr, nullptr, T, nullptr, nullptr, true, false, 0);
+            if (int rc = sca_stencils(c, 'P', sd, T, nullptr)) return rc;
+        }
         for (int l = c.maxlevel; l > c.minlevel; --l) ftoc_one(c, l, sd.name, sd.name, 'T');
         connect(c, 0, 2, nullptr, nullptr, nullptr, T, nullptr, nullptr, true, false, 0);
     }
@@ -4045,6 +4187,7 @@ int oracle_set_ghostcell(oracle_ctx* c) {
     giteig(*c);                       // Poisson coefficients with the blocked cells
     if (int rc = init_pressuresolver(*c)) return rc;
     setsdivfield(*c);
+    if (c->f3.count("BT")) return blockbt(*c);   // scalars set before the blocking
     return 0;
 }
 
@@ -4111,8 +4254,8 @@ int oracle_parent(oracle_ctx* c, int ilevel, const char* v1, const char* v2, con
 int oracle_ftoc(oracle_ctx* c, int ilevel, const char* ff, const char* fc, char flag) {
     if (!c->f3.count(ff) || !c->f3.count(fc)) return fail(MGLET_ERR_NAME, "ftoc: unknown field");
     if (!std::strchr("UVWPRST", flag)) return fail(MGLET_ERR_ARG, "ftoc: flag is one of U V W P R S T");
-    if (c->ibtype == 1 && flag == 'T')
-        return fail(MGLET_ERR_UNSUPPORTED, "ftoc: the ghost-cell T restriction weighs by BT, which is not kept");
+    if (c->ibtype == 1 && flag == 'T' && !c->f3.count("BT"))
+        return fail(MGLET_ERR_UNSUPPORTED, "ftoc: the ghost-cell T restriction weighs by BT (set_scalars first)");
     ftoc_one(*c, ilevel, ff, fc, flag);
     return 0;
 }
@@ -4132,8 +4275,6 @@ int oracle_set_scalars(oracle_ctx* c, int nsca, const double* prmol, const int32
                        const double* source, double prturb) {
     if (!c || nsca < 0 || nsca > 9 || (nsca && (!prmol || !kayscrawford)))
         return fail(MGLET_ERR_ARG, "set_scalars: 0..9 scalars with prmol and kayscrawford");
-    if (nsca && c->ibtype == 1)
-        return fail(MGLET_ERR_UNSUPPORTED, "set_scalars: the ghost-cell scalar stencils are not restated");
     c->sca.clear();
     for (int l = 0; l < nsca; ++l) {
         Ctx::ScalarDef sd;
@@ -4149,6 +4290,39 @@ int oracle_set_scalars(oracle_ctx* c, int nsca, const double* prmol, const int32
     c->prturb = prturb;
     for (const char* n : {"QTU", "QTV", "QTW", "QTT", "BT"}) c->f3[n].assign(c->idim3d, 0.0);
     std::fill(c->f3["BT"].begin(), c->f3["BT"].end(), 1.0);   // blockbt: open everywhere (noib)
+    if (c->ibtype == 1) return blockbt(*c);
+    return 0;
+}
+
+int oracle_set_scastencils(oracle_ctx* c, int igrid, int ncells, const int64_t* xpoli, const double* xpolr,
+                           const double* xpolrvel) {
+    if (!c || igrid < 1 || igrid > c->ngrid || ncells < 0 || (ncells && (!xpoli || !xpolr || !xpolrvel)))
+        return fail(MGLET_ERR_ARG, "set_scastencils: bad grid or lists");
+    const Grid& G = c->g[igrid];
+    const int64_t npts = (int64_t)G.kk * G.jj * G.ii;
+    for (int cell = 0; cell < ncells; ++cell) {
+        const int64_t* xi = xpoli + (size_t)cell * kScaIsize;
+        if (xi[0] < 1 || xi[0] > npts || xi[2] < 0 || xi[2] > kScaNperi)
+            return fail(MGLET_ERR_ARG, "set_scastencils: cell or stencil count out of range");
+        for (int64_t n = 1; n <= xi[2]; ++n)
+            if (xi[2 + n] < 1 || xi[2 + n] > npts) return fail(MGLET_ERR_ARG, "set_scastencils: stencil cell out of range");
+    }
+    if ((int)c->scal.size() < c->ngrid + 1) c->scal.resize(c->ngrid + 1);
+    Ctx::ScaList& L = c->scal[igrid];
+    L.ncells = ncells;
+    L.xpoli.assign(xpoli, xpoli + (size_t)ncells * kScaIsize);
+    L.xpolr.assign(xpolr, xpolr + (size_t)ncells * kScaRsize);
+    L.xpolrvel.assign(xpolrvel, xpolrvel + (size_t)ncells * kScaRsize);
+    return 0;
+}
+
+int oracle_set_scalar_geometry(oracle_ctx* c, int isca, int nbody, const int32_t* flag, const double* value) {
+    if (!c || isca < 1 || isca > (int)c->sca.size() || nbody < 0 || (nbody && (!flag || !value)))
+        return fail(MGLET_ERR_ARG, "set_scalar_geometry: bad scalar or bodies");
+    for (int b = 0; b < nbody; ++b)
+        if (flag[b] != 0 && flag[b] != 1) return fail(MGLET_ERR_ARG, "set_scalar_geometry: flag 0 or 1");
+    c->sca[isca - 1].geo_flag.assign(flag, flag + nbody);
+    c->sca[isca - 1].geo_value.assign(value, value + nbody);
     return 0;
 }
 
