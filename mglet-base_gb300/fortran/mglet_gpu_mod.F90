@@ -423,6 +423,24 @@ MODULE mglet_gpu_mod
             INTEGER(c_int64_t), VALUE :: buflen
         END FUNCTION mglet_gpu_tuning
 
+        INTEGER(c_int) FUNCTION mglet_gpu_set_scastencils(ctx, igrid, ncells, xpoli, xpolr, &
+                xpolrvel) BIND(C, name="mglet_gpu_set_scastencils")
+            IMPORT :: c_int, c_int32_t, c_int64_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: igrid, ncells
+            INTEGER(c_int64_t), INTENT(in) :: xpoli(*)
+            REAL(c_double), INTENT(in) :: xpolr(*), xpolrvel(*)
+        END FUNCTION mglet_gpu_set_scastencils
+
+        INTEGER(c_int) FUNCTION mglet_gpu_set_scalar_geometry(ctx, isca, nbody, flag, value) &
+                BIND(C, name="mglet_gpu_set_scalar_geometry")
+            IMPORT :: c_int, c_int32_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: ctx
+            INTEGER(c_int32_t), VALUE :: isca, nbody
+            INTEGER(c_int32_t), INTENT(in) :: flag(*)
+            REAL(c_double), INTENT(in) :: value(*)
+        END FUNCTION mglet_gpu_set_scalar_geometry
+
         INTEGER(c_int) FUNCTION mglet_gpu_force_variant(ctx, kernel, variant) &
                 BIND(C, name="mglet_gpu_force_variant")
             IMPORT :: c_int, c_int32_t, c_ptr, c_char
@@ -449,7 +467,8 @@ MODULE mglet_gpu_mod
         gpu_add_scalar_source, gpu_tstle4, gpu_rkstep, gpu_divcal, gpu_laplacephi, gpu_mgpoisl, &
         gpu_maskbp, gpu_getibvalues, gpu_adjoint_rk_stage, mglet_ib_geometry, &
         gpu_create_flowstencils, gpu_ftoc_multiple, gpu_download_buffer, gpu_synchronize, &
-        gpu_tuning, gpu_force_variant, MGLET_FORM_PLAIN, MGLET_FORM_MIXED, MGLET_FORM_PLAIN_FMA
+        gpu_tuning, gpu_force_variant, MGLET_FORM_PLAIN, MGLET_FORM_MIXED, MGLET_FORM_PLAIN_FMA, &
+        gpu_set_scastencils, gpu_set_scalar_geometry
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -777,6 +796,27 @@ CONTAINS
             INT(iface, c_int32_t), buf, INT(SIZE(buf), c_int64_t)) /= 0) &
             CALL errr(__FILE__, __LINE__)
     END SUBROUTINE gpu_download_buffer
+
+    ! The scalar ghost-cell list of grid igrid as create_scastencils leaves
+    ! it: ncells cells of 9 integers (scaxpoli) and 8 reals (scaxpolr,
+    ! scaxpolrvel)
+    SUBROUTINE gpu_set_scastencils(igrid, ncells, xpoli, xpolr, xpolrvel)
+        INTEGER, INTENT(in) :: igrid, ncells
+        INTEGER(c_int64_t), INTENT(in) :: xpoli(:)
+        REAL(c_double), INTENT(in) :: xpolr(:), xpolrvel(:)
+        IF (mglet_gpu_set_scastencils(gctx, INT(igrid, c_int32_t), INT(ncells, c_int32_t), xpoli, &
+            xpolr, xpolrvel) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_set_scastencils
+
+    ! sca%geometries of scalar isca: per body flag (0 fixed value, 1 fixed
+    ! flux) and value
+    SUBROUTINE gpu_set_scalar_geometry(isca, flag, value)
+        INTEGER, INTENT(in) :: isca
+        INTEGER(c_int32_t), INTENT(in) :: flag(:)
+        REAL(c_double), INTENT(in) :: value(:)
+        IF (mglet_gpu_set_scalar_geometry(gctx, INT(isca, c_int32_t), INT(SIZE(flag), c_int32_t), &
+            flag, value) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_set_scalar_geometry
 
     SUBROUTINE gpu_synchronize()
         IF (mglet_gpu_synchronize(gctx) /= 0) CALL errr(__FILE__, __LINE__)
