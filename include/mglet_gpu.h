@@ -440,6 +440,26 @@ int mglet_flowstencils_size(const mglet_flowstencils* s, int32_t igrid, int32_t 
 int mglet_flowstencils_copy(const mglet_flowstencils* s, int32_t igrid, int32_t comp,
                             int64_t* xpoli, double* xpolr, double* xpolrvel);
 int mglet_flowstencils_free(mglet_flowstencils* s);
+/* The scalar ghost-cell lists, create_scastencils (src/scalar/
+ * gc_scastencils_mod.F90:21-946), host code: from BP, BZELLTYP and per cut
+ * cell (gc_t) its plane, interface area and body id; per grid the records
+ * mglet_gpu_set_scastencils takes (9 integers, 8 reals per cell; unused
+ * stencil slots -1 and -HUGE as in the reference). */
+typedef struct mglet_sca_geometry {
+    const double* bp;
+    const int32_t* bzelltyp;  /* negative: 1-based index into the grid's cut cells */
+    const int32_t* icells;    /* [ngrid] */
+    const double* nvecs;      /* [sum icells][4]: a, b, c, dpl */
+    const double* arealist;   /* [sum icells] */
+    const int32_t* bodyid;    /* [sum icells] */
+} mglet_sca_geometry;
+typedef struct mglet_scastencils mglet_scastencils;
+int mglet_create_scastencils(const mglet_grid_desc* desc, const mglet_sca_geometry* geo,
+                             mglet_scastencils** out);
+int mglet_scastencils_size(const mglet_scastencils* s, int32_t igrid, int32_t* ncells);
+int mglet_scastencils_copy(const mglet_scastencils* s, int32_t igrid, int64_t* xpoli, double* xpolr,
+                           double* xpolrvel);
+int mglet_scastencils_free(mglet_scastencils* s);
 /* setibvalues(u, v, w), getibvalues(u, v, w) and setpointvalues(pwu, pwv,
  * pww, u, v, w, comp_new) (gc_flowstencils_mod.F90:1323-1453), maskbp(u, v,
  * w, p) (src/flow/timeintegration_mod.F90:255-303) on the device fields. */

@@ -18,6 +18,7 @@
 // widened to double), so the lists do not depend on how they are produced.
 // This file is compiled with -ffp-contract=off for the host.
 #include <array>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -32,6 +33,16 @@ struct mglet_flowstencils {
         std::vector<double> xr, xv;
     };
     std::vector<std::array<List, 4>> g;
+};
+
+// per grid the scalar list: 9 integers and 8 reals per cell
+struct mglet_scastencils {
+    struct List {
+        int ncells = 0;
+        std::vector<int64_t> xi;
+        std::vector<double> xr, xv;
+    };
+    std::vector<List> g;
 };
 
 namespace mg {
@@ -438,8 +449,288 @@ void fluxcorrection(const GridView& G, Lists& L) {
             }
 }
 
+// ---- scalar stencils (src/scalar/gc_scastencils_mod.F90:127-946) ---------
+// Per treated cell one standard-sized record: 9 integers {cell, body, N, N
+// stencil cells, -1 for the unused of the six} and 8 reals {areabyvol, N
+// coefficients, -HUGE for the unused, the additive constant}, for the
+// cell-value ('C', xpolr) and the point-value ('P', xpolrvel) forms.
+constexpr int kScaNperi = 6;
+
+struct ScaLists {
+    int n = 0;
+    std::vector<int64_t> xi;
+    std::vector<double> xr, xv;
+    void record(int64_t cell, int body, int nst, const int64_t* st, double areabyvol, const double* c,
+                const double* cv, double ac, double acv) {
+        xi.push_back(cell);
+        xi.push_back(body);
+        xi.push_back(nst);
+        xr.push_back(areabyvol);
+        xv.push_back(areabyvol);
+        for (int q = 0; q < kScaNperi; ++q) {
+            const bool used = q < nst;
+            xi.push_back(used ? st[q] : -1);
+            xr.push_back(used ? c[q] : -DBL_MAX);
+            xv.push_back(used ? cv[q] : -DBL_MAX);
+        }
+        xr.push_back(ac);
+        xv.push_back(acv);
+        ++n;
+    }
+};
+
+// the cut cell idx (1-based within the grid) of a negative bzelltyp
+struct ScaCut {
+    const double* nvecs;     // [icells][4]
+    const double* area;      // [icells]
+    const int32_t* body;     // [icells]
+};
+
+// calcfluxtsca (:525-782): from the cut cell's plane a x + b y + c z = dpl,
+// the cell-value stencil (the mean over the fluid part of the cell, by a
+// 20^3 midpoint integration) and the point-value stencil (linear in the
+// distance to the plane); 1 on success, -11 without a usable distance,
+// -12 when the cell-value weights exceed 0.61, -99 on a non-finite
+// coefficient (an error in the reference).
+int calcfluxtsca(const GridView& G, const ScaCut& cut, int k, int j, int i, int kt, int jt, int it,
+                 const std::vector<int>& is, const std::vector<int>& js, const std::vector<int>& ks,
+                 int velpts, double* co, double& ac, double* cv, double& acv) {
+    const double* nv = cut.nvecs + 4 * (long long)(-G.bz[G.at(kt, jt, it)] - 1);
+    const double a = nv[0], b = nv[1], c = nv[2], dpl = nv[3];
+    for (int n = 0; n < kScaNperi; ++n) co[n] = cv[n] = 0.0;
+    ac = acv = 0.0;
+    double dpoint = a * G.x[i] + b * G.y[j] + c * G.z[k] - dpl;
+    double dall = 0.0, dist[kScaNperi] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int n = 0; n < velpts; ++n) {
+        dist[n] = a * G.x[is[n]] + b * G.y[js[n]] + c * G.z[ks[n]] - dpl;
+        if (dist[n] < std::fabs(dpoint) * (double)0.2f) dist[n] = 0.0;
+        dall = dall + dist[n] * dist[n];
+    }
+    if (std::fabs(dall) < DBL_MIN) return -11;
+    double ce[kScaNperi], cesum = 0.0;
+    for (int n = 0; n < velpts; ++n) {
+        ce[n] = dist[n] / dall;
+        cesum = cesum + ce[n];
+    }
+    const int parts = 20;
+    const double ddi = G.ddx[i] / parts, ddj = G.ddy[j] / parts, ddk = G.ddz[k] / parts;
+    const double xs = G.xs[i - 1] - ddi / 2.0, ys = G.ys[j - 1] - ddj / 2.0, zs = G.zs[k - 1] - ddk / 2.0;
+    int cvol1 = 0;
+    const double dvol = ddi * ddj * ddk;
+    for (int i2 = 1; i2 <= parts; ++i2) {
+        const double xm = xs + ddi * (double)i2;
+        for (int j2 = 1; j2 <= parts; ++j2) {
+            const double ym = ys + ddj * (double)j2;
+            for (int k2 = 1; k2 <= parts; ++k2) {
+                const double zm = zs + ddk * (double)k2;
+                const double dir = (a * xm + b * ym + c * zm) - dpl;
+                if (dir > 0.0) {
+                    for (int n = 0; n < velpts; ++n) co[n] = co[n] + dir * ce[n];
+                    ac = ac + (1.0 - dir * cesum);
+                    ++cvol1;
+                }
+            }
+        }
+    }
+    if (cvol1 > 0) {
+        for (int n = 0; n < velpts; ++n) co[n] = co[n] * dvol / ((double)cvol1 * dvol);
+        ac = ac * dvol / ((double)cvol1 * dvol);
+    } else {
+        for (int n = 0; n < velpts; ++n) co[n] = 0.0;
+        ac = 0.0;
+    }
+    dpoint = a * G.x[i] + b * G.y[j] + c * G.z[k] - dpl;
+    for (int n = 0; n < velpts; ++n) cv[n] = dpoint * ce[n];
+    acv = 1.0 - dpoint * cesum;
+    int found = 1;
+    double sum = 0.0;
+    for (int n = 0; n < velpts; ++n) sum = sum + co[n];
+    if (sum > (double)0.61f) found = -12;
+    bool bad = !std::isfinite(acv) || !std::isfinite(ac);
+    for (int n = 0; n < velpts; ++n) bad = bad || !std::isfinite(cv[n]) || !std::isfinite(co[n]);
+    return bad ? -99 : found;
+}
+
+// tscastencilcoeff (:447-522): the open neighbours, the chosen stencil and
+// its coefficients; the full record on success.  Returns the reference's
+// found (<= 0: the caller writes the rescue record), -99 on an error.
+int tscastencilcoeff(const GridView& G, const ScaCut& cut, const Ball& ball, int k, int j, int i, int kt,
+                     int jt, int it, double areabyvol, int body, ScaLists& L) {
+    std::vector<int> is, js, ks;
+    checkneighbor(G, G.bp, k, j, i, ball, is, js, ks);
+    const int velpts = choosestencil(k, j, i, is, js, ks);
+    if (velpts > kScaNperi) return -2;
+    if (velpts == 0) return -3;
+    double co[kScaNperi], cv[kScaNperi], ac, acv;
+    const int found = calcfluxtsca(G, cut, k, j, i, kt, jt, it, is, js, ks, velpts, co, ac, cv, acv);
+    if (found == -99) return -99;
+    for (int n = 0; n < velpts; ++n)
+        if (std::fabs(cv[n]) > 12.0) return -4;
+    if (found == 1) {
+        int64_t st[kScaNperi];
+        for (int n = 0; n < velpts; ++n) st[n] = G.flat1(ks[n], js[n], is[n]);
+        L.record(G.flat1(k, j, i), body, velpts, st, areabyvol, co, cv, ac, acv);
+    }
+    return found;
+}
+
+// tscastencil (:127-363): every blocked interior cell with an open face
+// neighbour (findinterface2) gets a stencil from the cut cell with the
+// boundary information -- itself, else the face neighbour with the largest
+// body id -- or the rescue record (no stencil points, constant 1: the
+// cell takes the body's value); an open cut cell gets the area record (its
+// interface area per volume only, for the flux condition).
+int tscastencil(const GridView& G, const ScaCut& cut, const Ball& ball, ScaLists& L) {
+    const int64_t none[1] = {0};
+    const double zero[1] = {0.0};
+    for (int i = 3; i <= G.ii - 2; ++i)
+        for (int j = 3; j <= G.jj - 2; ++j)
+            for (int k = 3; k <= G.kk - 2; ++k) {
+                const Found f = findinterface2(G, G.bp, k, j, i);
+                const int32_t bz = G.bz[G.at(k, j, i)];
+                const double vol = G.ddx[i] * G.ddy[j] * G.ddz[k];
+                if (!f.found) {
+                    if (bz < 0 && G.bp[G.at(k, j, i)] > 0.5) {
+                        // tscastencilcoeffarea (:366-444): the cell itself, weight 1
+                        const double areabyvol = cut.area[-bz - 1] / vol;
+                        const int64_t self[1] = {G.flat1(k, j, i)};
+                        const double one[1] = {1.0};
+                        L.record(G.flat1(k, j, i), cut.body[-bz - 1], 1, self, areabyvol, one, one, 0.0, 0.0);
+                    }
+                    continue;
+                }
+                int found2 = 0, kt = 0, jt = 0, it = 0, body = 0;
+                if (bz < 0) {
+                    it = i; jt = j; kt = k;
+                    found2 = 1;
+                } else {
+                    const int flag[6] = {f.x1, f.x2, f.y1, f.y2, f.z1, f.z2};
+                    const int off[6][3] = {{0, 0, 1}, {0, 0, -1}, {0, 1, 0}, {0, -1, 0}, {1, 0, 0}, {-1, 0, 0}};
+                    for (int q = 0; q < 6; ++q) {
+                        const int kq = k + off[q][0], jq = j + off[q][1], iq = i + off[q][2];
+                        const int32_t bq = G.bz[G.at(kq, jq, iq)];
+                        if (flag[q] == 1 && bq < 0 && cut.body[-bq - 1] > body) {
+                            body = cut.body[-bq - 1];
+                            it = iq; jt = jq; kt = kq;
+                        }
+                    }
+                    if (body > 0) found2 = 1;
+                }
+                if (found2 == 1) {
+                    const int32_t bt = G.bz[G.at(kt, jt, it)];
+                    const double areabyvol = (k == kt && j == jt && i == it) ? cut.area[-bt - 1] / vol : 0.0;
+                    body = cut.body[-bt - 1];
+                    const int found3 = tscastencilcoeff(G, cut, ball, k, j, i, kt, jt, it, areabyvol, body, L);
+                    if (found3 == -99) return MGLET_ERR_ARG;
+                    // tscastencilcoeffrescue (:872-946): no points, constant 1
+                    if (found3 <= 0) L.record(G.flat1(k, j, i), body, 0, none, areabyvol, zero, zero, 1.0, 1.0);
+                } else {
+                    L.record(G.flat1(k, j, i), 0, 0, none, 0.0, zero, zero, 1.0, 1.0);
+                }
+            }
+    return 0;
+}
+
 }  // namespace
 }  // namespace mg
+
+extern "C" int mglet_create_scastencils(const mglet_grid_desc* d, const mglet_sca_geometry* geo,
+                                        mglet_scastencils** out) {
+    using namespace mg;
+    if (!d || !geo || !out || d->ngrid <= 0 || !d->mgdims || !d->bctype || !d->x || !d->dx || !d->ddx ||
+        !geo->bp || !geo->bzelltyp || !geo->icells) {
+        set_error("create_scastencils: null argument");
+        return MGLET_ERR_ARG;
+    }
+    long long ncut = 0;
+    for (int g = 0; g < d->ngrid; ++g) {
+        if (geo->icells[g] < 0) {
+            set_error("create_scastencils: negative icells");
+            return MGLET_ERR_ARG;
+        }
+        ncut += geo->icells[g];
+    }
+    if (ncut > 0 && (!geo->nvecs || !geo->arealist || !geo->bodyid)) {
+        set_error("create_scastencils: nvecs, arealist and bodyid are needed for intersected cells");
+        return MGLET_ERR_ARG;
+    }
+    static const Ball ball;
+    auto* S = new mglet_scastencils();
+    S->g.resize(d->ngrid);
+    long long ip3 = 0, ipx = 0, ipy = 0, ipz = 0, ipc = 0;
+    std::vector<double> xs, ys, zs;
+    for (int g = 0; g < d->ngrid; ++g) {
+        GridView G{};
+        G.kk = d->mgdims[3 * g];
+        G.jj = d->mgdims[3 * g + 1];
+        G.ii = d->mgdims[3 * g + 2];
+        for (int f = 0; f < 6; ++f) G.bc[f] = d->bctype[6 * g + f];
+        xs.assign(G.ii + 1, 0.0);
+        ys.assign(G.jj + 1, 0.0);
+        zs.assign(G.kk + 1, 0.0);
+        for (int i = 1; i <= G.ii; ++i) xs[i] = d->x[ipx + i - 1] + 0.5 * d->dx[ipx + i - 1];
+        for (int j = 1; j <= G.jj; ++j) ys[j] = d->y[ipy + j - 1] + 0.5 * d->dy[ipy + j - 1];
+        for (int k = 1; k <= G.kk; ++k) zs[k] = d->z[ipz + k - 1] + 0.5 * d->dz[ipz + k - 1];
+        G.x = d->x + ipx - 1; G.y = d->y + ipy - 1; G.z = d->z + ipz - 1;
+        G.xs = xs.data(); G.ys = ys.data(); G.zs = zs.data();
+        G.ddx = d->ddx + ipx - 1; G.ddy = d->ddy + ipy - 1; G.ddz = d->ddz + ipz - 1;
+        G.bp = geo->bp + ip3;
+        G.bz = geo->bzelltyp + ip3;
+        G.icells = geo->icells[g];
+        const long long npts = (long long)G.kk * G.jj * G.ii;
+        for (long long q = 0; q < npts; ++q)
+            if (G.bz[q] < -G.icells) {
+                delete S;
+                set_error("create_scastencils: bzelltyp refers past the grid's intersected cells");
+                return MGLET_ERR_ARG;
+            }
+        ScaCut cut{geo->nvecs ? geo->nvecs + 4 * ipc : nullptr, geo->arealist ? geo->arealist + ipc : nullptr,
+                   geo->bodyid ? geo->bodyid + ipc : nullptr};
+        ScaLists L;
+        if (int rc = tscastencil(G, cut, ball, L)) {
+            delete S;
+            set_error("create_scastencils: a non-finite stencil coefficient");
+            return rc;
+        }
+        auto& o = S->g[g];
+        o.ncells = L.n;
+        o.xi = std::move(L.xi);
+        o.xr = std::move(L.xr);
+        o.xv = std::move(L.xv);
+        ip3 += npts;
+        ipx += G.ii; ipy += G.jj; ipz += G.kk;
+        ipc += G.icells;
+    }
+    *out = S;
+    return 0;
+}
+
+extern "C" int mglet_scastencils_size(const mglet_scastencils* s, int32_t igrid, int32_t* ncells) {
+    if (!s || igrid < 1 || igrid > (int)s->g.size()) {
+        mg::set_error("scastencils_size: bad handle or grid");
+        return MGLET_ERR_ARG;
+    }
+    if (ncells) *ncells = s->g[igrid - 1].ncells;
+    return 0;
+}
+
+extern "C" int mglet_scastencils_copy(const mglet_scastencils* s, int32_t igrid, int64_t* xpoli,
+                                      double* xpolr, double* xpolrvel) {
+    if (!s || igrid < 1 || igrid > (int)s->g.size()) {
+        mg::set_error("scastencils_copy: bad handle or grid");
+        return MGLET_ERR_ARG;
+    }
+    const auto& L = s->g[igrid - 1];
+    if (xpoli && !L.xi.empty()) std::memcpy(xpoli, L.xi.data(), L.xi.size() * sizeof(int64_t));
+    if (xpolr && !L.xr.empty()) std::memcpy(xpolr, L.xr.data(), L.xr.size() * sizeof(double));
+    if (xpolrvel && !L.xv.empty()) std::memcpy(xpolrvel, L.xv.data(), L.xv.size() * sizeof(double));
+    return 0;
+}
+
+extern "C" int mglet_scastencils_free(mglet_scastencils* s) {
+    delete s;
+    return 0;
+}
 
 extern "C" int mglet_create_flowstencils(const mglet_grid_desc* d, const mglet_ib_geometry* geo,
                                          mglet_flowstencils** out) {

@@ -50,6 +50,12 @@ MODULE mglet_gpu_mod
         TYPE(c_ptr) :: bp, bu, bv, bw, areau, areav, areaw, bzelltyp, icells, nvecs, ucell
     END TYPE mglet_ib_geometry
 
+    ! create_scastencils' inputs: BP, BZELLTYP, per grid the cut-cell count,
+    ! per cut cell its plane, interface area and body id (gc_t)
+    TYPE, BIND(C) :: mglet_sca_geometry
+        TYPE(c_ptr) :: bp, bzelltyp, icells, nvecs, arealist, bodyid
+    END TYPE mglet_sca_geometry
+
     INTERFACE
         INTEGER(c_int) FUNCTION mglet_rk_init(name, rk) BIND(C, name="mglet_rk_init")
             IMPORT :: c_int, c_char, mglet_rk_scheme
@@ -321,6 +327,36 @@ MODULE mglet_gpu_mod
             TYPE(mglet_rk_scheme), INTENT(in) :: rk
         END FUNCTION mglet_gpu_adjoint_rk_stage
 
+        INTEGER(c_int) FUNCTION mglet_create_scastencils(desc, geo, out) &
+                BIND(C, name="mglet_create_scastencils")
+            IMPORT :: c_int, c_ptr, mglet_grid_desc, mglet_sca_geometry
+            TYPE(mglet_grid_desc), INTENT(in) :: desc
+            TYPE(mglet_sca_geometry), INTENT(in) :: geo
+            TYPE(c_ptr), INTENT(out) :: out
+        END FUNCTION mglet_create_scastencils
+
+        INTEGER(c_int) FUNCTION mglet_scastencils_size(s, igrid, ncells) &
+                BIND(C, name="mglet_scastencils_size")
+            IMPORT :: c_int, c_int32_t, c_ptr
+            TYPE(c_ptr), VALUE :: s
+            INTEGER(c_int32_t), VALUE :: igrid
+            INTEGER(c_int32_t), INTENT(out) :: ncells
+        END FUNCTION mglet_scastencils_size
+
+        INTEGER(c_int) FUNCTION mglet_scastencils_copy(s, igrid, xpoli, xpolr, xpolrvel) &
+                BIND(C, name="mglet_scastencils_copy")
+            IMPORT :: c_int, c_int32_t, c_int64_t, c_ptr, c_double
+            TYPE(c_ptr), VALUE :: s
+            INTEGER(c_int32_t), VALUE :: igrid
+            INTEGER(c_int64_t), INTENT(out) :: xpoli(*)
+            REAL(c_double), INTENT(out) :: xpolr(*), xpolrvel(*)
+        END FUNCTION mglet_scastencils_copy
+
+        INTEGER(c_int) FUNCTION mglet_scastencils_free(s) BIND(C, name="mglet_scastencils_free")
+            IMPORT :: c_int, c_ptr
+            TYPE(c_ptr), VALUE :: s
+        END FUNCTION mglet_scastencils_free
+
         INTEGER(c_int) FUNCTION mglet_create_flowstencils(desc, geo, out) &
                 BIND(C, name="mglet_create_flowstencils")
             IMPORT :: c_int, c_ptr, mglet_grid_desc, mglet_ib_geometry
@@ -468,7 +504,7 @@ MODULE mglet_gpu_mod
         gpu_maskbp, gpu_getibvalues, gpu_adjoint_rk_stage, mglet_ib_geometry, &
         gpu_create_flowstencils, gpu_ftoc_multiple, gpu_download_buffer, gpu_synchronize, &
         gpu_tuning, gpu_force_variant, MGLET_FORM_PLAIN, MGLET_FORM_MIXED, MGLET_FORM_PLAIN_FMA, &
-        gpu_set_scastencils, gpu_set_scalar_geometry
+        gpu_set_scastencils, gpu_set_scalar_geometry, mglet_sca_geometry, gpu_create_scastencils
 
 CONTAINS
     ! Called once after init_flow: builds the device state from the same
@@ -732,6 +768,28 @@ CONTAINS
     ! Replaces create_flowstencils (gc_flowstencils_mod.F90:37): builds every
     ! grid's lists from the blocking fields and uploads them; call
     ! gpu_start_ghostcell afterwards.
+    ! Drop-in for create_scastencils(gc): builds every grid's scalar list
+    ! from the cut cells and uploads it
+    SUBROUTINE gpu_create_scastencils(desc, geo)
+        TYPE(mglet_grid_desc), INTENT(in) :: desc
+        TYPE(mglet_sca_geometry), INTENT(in) :: geo
+        TYPE(c_ptr) :: s
+        INTEGER :: ig
+        INTEGER(c_int32_t) :: nc
+        INTEGER(c_int64_t), ALLOCATABLE :: xi(:)
+        REAL(c_double), ALLOCATABLE :: xr(:), xv(:)
+        IF (mglet_create_scastencils(desc, geo, s) /= 0) CALL errr(__FILE__, __LINE__)
+        DO ig = 1, desc%ngrid
+            IF (mglet_scastencils_size(s, INT(ig, c_int32_t), nc) /= 0) CALL errr(__FILE__, __LINE__)
+            ALLOCATE(xi(MAX(9 * nc, 1)), xr(MAX(8 * nc, 1)), xv(MAX(8 * nc, 1)))
+            IF (mglet_scastencils_copy(s, INT(ig, c_int32_t), xi, xr, xv) /= 0) &
+                CALL errr(__FILE__, __LINE__)
+            CALL gpu_set_scastencils(ig, INT(nc), xi(1:9 * nc), xr(1:8 * nc), xv(1:8 * nc))
+            DEALLOCATE(xi, xr, xv)
+        END DO
+        IF (mglet_scastencils_free(s) /= 0) CALL errr(__FILE__, __LINE__)
+    END SUBROUTINE gpu_create_scastencils
+
     SUBROUTINE gpu_create_flowstencils(desc, geo)
         TYPE(mglet_grid_desc), INTENT(in) :: desc
         TYPE(mglet_ib_geometry), INTENT(in) :: geo

@@ -88,6 +88,11 @@ class IbGeometry(C.Structure):
                                           "bzelltyp", "icells", "nvecs", "ucell")]
 
 
+class ScaGeometry(C.Structure):
+    """mglet_sca_geometry: the inputs of create_scastencils."""
+    _fields_ = [(n, C.c_void_p) for n in ("bp", "bzelltyp", "icells", "nvecs", "arealist", "bodyid")]
+
+
 def make_flow_params(gmol, rho=1.0, gradp=(0.0, 0.0, 0.0), psolver=PSOLVER_SIP, ninner=5,
                      nouter=9, nouter_min=0, epcorr=1e-10, omega=1.1, form=FORM_PLAIN):
     p = FlowParams()

@@ -37,7 +37,8 @@ EXPORTS = [
     "mglet_gpu_force_variant", "mglet_create_flowstencils", "mglet_flowstencils_size",
     "mglet_flowstencils_copy", "mglet_flowstencils_free", "mglet_gpu_set_partition",
     "mglet_gpu_test_wait_timeout", "mglet_gpu_test_barrier_timeout", "mglet_gpu_set_scastencils",
-    "mglet_gpu_set_scalar_geometry", "mglet_mesh_create",
+    "mglet_gpu_set_scalar_geometry", "mglet_create_scastencils", "mglet_scastencils_size",
+    "mglet_scastencils_copy", "mglet_scastencils_free", "mglet_mesh_create",
     "mglet_mesh_distance", "mglet_mesh_free",
 ]
 
@@ -124,6 +125,10 @@ def load(path=None):
     L.mglet_gpu_test_barrier_timeout.argtypes = [vp]
     L.mglet_gpu_set_scastencils.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp]
     L.mglet_gpu_set_scalar_geometry.argtypes = [vp, C.c_int32, C.c_int32, vp, vp]
+    L.mglet_create_scastencils.argtypes = [vp, vp, C.POINTER(vp)]
+    L.mglet_scastencils_size.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32)]
+    L.mglet_scastencils_copy.argtypes = [vp, C.c_int32, vp, vp, vp]
+    L.mglet_scastencils_free.argtypes = [vp]
     L.mglet_mesh_create.argtypes = [vp, C.c_int64, C.POINTER(vp)]
     L.mglet_mesh_distance.argtypes = [vp, vp, C.c_int64, vp, vp]
     L.mglet_mesh_free.argtypes = [vp]
@@ -427,6 +432,39 @@ class Solver:
     @property
     def launches(self):
         return load().mglet_gpu_kernel_launches(self.h)
+
+
+def create_scastencils(case, geo, arealist, bodyid):
+    """The scalar ghost-cell lists of every grid (mglet_create_scastencils,
+    host code, no device needed) from the blocking fields (geometry.block)
+    and, per cut cell, its interface area and body id.  Returns per grid
+    (xpoli, xpolr, xpolrvel), the layout mglet_gpu_set_scastencils takes."""
+    L = load()
+    keep = {"bp": np.ascontiguousarray(geo["bp"], dtype=np.float64),
+            "bzelltyp": np.ascontiguousarray(geo["bzelltyp"], dtype=np.int32),
+            "icells": np.ascontiguousarray(geo["icells"], dtype=np.int32),
+            "nvecs": np.ascontiguousarray(geo["nvecs"], dtype=np.float64).reshape(-1),
+            "arealist": np.ascontiguousarray(arealist, dtype=np.float64),
+            "bodyid": np.ascontiguousarray(bodyid, dtype=np.int32)}
+    g = abi.ScaGeometry()
+    for n, a in keep.items():
+        setattr(g, n, a.ctypes.data_as(C.c_void_p))
+    desc = case.desc()
+    h = C.c_void_p()
+    _check(L.mglet_create_scastencils(C.byref(desc), C.byref(g), C.byref(h)))
+    out = []
+    try:
+        for ig in range(1, case.ngrid + 1):
+            n = C.c_int32()
+            _check(L.mglet_scastencils_size(h, ig, C.byref(n)))
+            xi = np.zeros(9 * n.value, dtype=np.int64)
+            xr, xv = np.zeros(8 * n.value), np.zeros(8 * n.value)
+            _check(L.mglet_scastencils_copy(h, ig, xi.ctypes.data_as(C.c_void_p), xr.ctypes.data_as(C.c_void_p),
+                                            xv.ctypes.data_as(C.c_void_p)))
+            out.append((xi, xr, xv))
+    finally:
+        L.mglet_scastencils_free(h)
+    return out
 
 
 def create_flowstencils(case, geo):

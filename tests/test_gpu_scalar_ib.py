@@ -86,3 +86,34 @@ def test_scalar_body_without_condition_is_refused(gpu_lib):
     with pytest.raises(gpu_lib.MgletError):
         g.timeintegrate_scalar(5e-3, 1, gpu_lib.rk_scheme("williamson"))
     g.close()
+
+
+def test_constructed_scalar_lists_on_the_sphere_bit_exact(gpu_lib, oracle_lib):
+    """The lists of mglet_create_scastencils on the two-level sphere case
+    (synthetic cut-cell areas and body ids): one scalar stage and one flow
+    stage on the GPU and on the oracle, bit for bit."""
+    from mglet_gb300 import channel
+    sc = channel.SphereChannel(tiles=(4, 2, 2), n=8, grid_size=0.5, diameter=0.4, refine_radii=(0.35,))
+    ncut = int(sc.geo["icells"].sum())
+    area = 0.05 + np.random.default_rng(4).random(ncut)
+    body = (1 + np.arange(ncut) % 2).astype(np.int32)
+    scal = gpu_lib.create_scastencils(sc.case, sc.geo, area, body)
+    prm = sc.flow_params(nouter=6, ninner=5, nouter_min=6)
+    gs, o = gpu_lib.Solver(sc.case, prm), oracle_lib.Oracle(sc.case, prm)
+    t1 = 1.0 + 0.1 * np.random.default_rng(6).standard_normal(sc.case.idim3d)
+    for s in (gs, o):
+        sc.setup(s)
+        s.set_scalars([0.71])
+        s.set("T1", t1)
+        for lvl in (1, 2):
+            s.connect(lvl, 2, s1="T1", corners=True)
+        for g, (xi, xr, xv) in enumerate(scal):
+            s.set_scastencils(g + 1, xi, xr, xv)
+        s.set_scalar_geometry(1, [0, 1], [2.0, 0.5])
+    rk = oracle_lib.rk_scheme("williamson")
+    for s in (gs, o):
+        s.timeintegrate_scalar(sc.dt(), 1, rk)
+        s.timeintegrate_flow(1, 1, 0.0, sc.dt(), 1, rk)
+    for n in ("BT", "T1", "DT1", "U", "P"):
+        assert np.array_equal(gs.get(n), o.get(n)), n
+    gs.close()
