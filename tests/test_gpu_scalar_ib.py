@@ -6,7 +6,7 @@ hierarchy), and scalar stages with the bodies' flux and value conditions
 import numpy as np
 import pytest
 
-from mglet_gb300 import abi, cases
+from mglet_gb300 import cases
 from test_oracle_ghostcell import gc_case
 from test_oracle_levels import prepare_levels
 from test_oracle_scalar_ib import GEO, _prm, sca_lists, scalar_ib_setup
