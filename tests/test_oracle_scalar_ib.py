@@ -1,9 +1,10 @@
 """The oracle's ghost-cell IB of the scalars against direct numpy
 restatements of the reference's loops: blockbt (blockbt_mod.F90:73-91,
 bt = the largest bp of a cell and its six face neighbours) and the
-set_scastencils walk (gc_scastencils_mod.F90:1036-1125: a fixed-value body
-sets the interface cell from its stencil cells and acoeffvel * value).  The
-GPU path is compared with the oracle bit for bit in test_gpu_scalar_ib.py."""
+set_scastencils walks (gc_scastencils_mod.F90:1036-1125: a fixed-value body
+sets the interface cell from its stencil cells and acoeffvel * value, a
+fixed-flux body adds areabyvol * value to its QTT).  The GPU path is
+compared with the oracle bit for bit in test_gpu_scalar_ib.py."""
 import numpy as np
 
 from mglet_gb300 import abi, cases
@@ -132,3 +133,36 @@ def test_value_condition_of_the_bodies(oracle_lib):
                 assert t[base + rec[0] - 1] == val
                 n_checked += 1
     assert n_checked > 10
+
+
+def test_flux_condition_of_the_bodies(oracle_lib):
+    """With every body a fixed-flux body, the first RK stage (frhs = 0, so
+    T += dt b1 QTT) moves each interface cell by dt b1 areabyvol value
+    against the same stage without lists; every other interior cell is
+    unchanged (set_scastencils "P" on QTT, :71-73; maskbt keeps interface
+    cells, whose BT is 1)."""
+    case, bp, lists = gc_case(seed=7)
+    u, v, w, p = cases.taylor_green(case)
+    fields = dict(zip("UVWP", (u + 0.2, v, w, p)))
+    t1 = 1.0 + 0.1 * np.random.default_rng(5).standard_normal(case.idim3d)
+    scal, _ = sca_lists(case, bp)
+    geo = [([1, 1], [0.8, -0.4]), ([1, 1], [0.0, 0.0])]
+    dt, rk = 5e-3, oracle_lib.rk_scheme("williamson")
+    out = []
+    for with_lists in (False, True):
+        o = oracle_lib.Oracle(case, _prm())
+        scalar_ib_setup(o, case, bp, lists, fields, scal if with_lists else [], geo, t1)
+        o.timeintegrate_scalar(dt, 1, rk)
+        out.append(o.get("T1"))
+    dtfu = dt * rk.b[0]
+    expect = np.zeros(case.idim3d)
+    flags, values = geo[0]
+    for g, (xi, xr, xv) in enumerate(scal):
+        base = g * case.ii * case.jj * case.kk
+        for cell in range(len(xi) // ISIZE):
+            body = xi[cell * ISIZE + 1]
+            if body > 0:
+                expect[base + xi[cell * ISIZE] - 1] += dtfu * xv[cell * RSIZE] * values[body - 1]
+    diff = case.interior(out[1] - out[0])
+    assert np.count_nonzero(case.interior(expect)) > 10
+    assert np.allclose(diff, case.interior(expect), rtol=1e-9, atol=1e-14)
