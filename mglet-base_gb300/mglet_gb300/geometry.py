@@ -23,11 +23,15 @@ included:
   nvecs   per intersected cell the tangent plane of the body at the surface
           point nearest the cell centre, a x + b y + c z = dpl, with the unit
           normal pointing into the fluid;
-  ucell   the body velocity there (a stationary body: 0).
+  ucell   the body velocity there (a stationary body: 0);
+  arealist per intersected cell the area of its tangent plane inside the
+          cell box (the interface area the scalar flux condition weighs);
+  bodyid  per intersected cell the body's id (`body.body_id`, 1 by default).
 
 These are the inputs of the stencil construction (create_flowstencils,
-gc_flowstencils_mod.F90:37-100), built by the library's
-mglet_create_flowstencils.
+gc_flowstencils_mod.F90:37-100, and create_scastencils,
+gc_scastencils_mod.F90:21-946), built by the library's
+mglet_create_flowstencils and mglet_create_scastencils.
 """
 import numpy as np
 
@@ -180,11 +184,56 @@ def _open(levels, body, P, L):
     return out
 
 
+# the 12 edges of a box as pairs of corner numbers (bit 0: x, 1: y, 2: z)
+_EDGES = [(q, q | b) for b in (1, 2, 4) for q in range(8) if not q & b]
+
+
+def plane_box_area(nv, lo, hi):
+    """Area of the plane a x + b y + c z = dpl (rows of nv, unit normal)
+    inside each box [lo, hi] (rows of 3): the polygon through the points
+    where the plane crosses the box edges, ordered by angle about their
+    mean in the plane, summed as triangles (0 where fewer than three)."""
+    nv, lo, hi = (np.atleast_2d(np.asarray(a, dtype=np.float64)) for a in (nv, lo, hi))
+    nrm, dpl = nv[:, :3], nv[:, 3]
+    m = len(nv)
+    corners = np.empty((m, 8, 3))
+    for q in range(8):
+        for ax in range(3):
+            corners[:, q, ax] = np.where((q >> ax) & 1, hi[:, ax], lo[:, ax])
+    f = np.einsum("nqa,na->nq", corners, nrm) - dpl[:, None]
+    pts = np.zeros((m, 12, 3))
+    ok = np.zeros((m, 12), dtype=bool)
+    for e, (q0, q1) in enumerate(_EDGES):
+        f0, f1 = f[:, q0], f[:, q1]
+        hit = ((f0 <= 0) & (f1 > 0)) | ((f1 <= 0) & (f0 > 0))
+        t = np.where(hit, f0 / np.where(hit, f0 - f1, 1.0), 0.0)
+        pts[:, e] = corners[:, q0] + t[:, None] * (corners[:, q1] - corners[:, q0])
+        ok[:, e] = hit
+    cnt = ok.sum(1)
+    cen = (pts * ok[..., None]).sum(1) / np.maximum(cnt, 1)[:, None]
+    # an in-plane basis: u orthogonal to the normal, w = n x u
+    ref = np.eye(3)[np.argmin(np.abs(nrm), axis=1)]
+    u = np.cross(nrm, ref)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    w = np.cross(nrm, u)
+    rel = pts - cen[:, None, :]
+    ang = np.arctan2(np.einsum("nea,na->ne", rel, w), np.einsum("nea,na->ne", rel, u))
+    order = np.argsort(np.where(ok, ang, np.inf), axis=1)
+    rel = np.take_along_axis(rel, order[..., None], axis=1)
+    nxt = (np.arange(12)[None, :] + 1) % np.maximum(cnt, 1)[:, None]
+    rel2 = np.take_along_axis(rel, nxt[..., None], axis=1)
+    tri = np.einsum("nea,na->ne", np.cross(rel, rel2), nrm)
+    use = np.arange(12)[None, :] < cnt[:, None]
+    area = 0.5 * np.abs((tri * use).sum(1))
+    return np.where(cnt >= 3, area, 0.0)
+
+
 def block(case, body, samples=8):
     """Blocking fields of every grid of `case` for `body`.  Returns a dict
     with flat field_t-layout arrays bp, bu, bv, bw, areau, areav, areaw
     (float64) and bzelltyp (int32), plus icells (int32 [ngrid]), nvecs
-    (float64 [sum icells, 4]) and ucell (float64 [sum icells, 3])."""
+    (float64 [sum icells, 4]), ucell (float64 [sum icells, 3]), arealist
+    (float64 [sum icells]) and bodyid (int32 [sum icells])."""
     ng, ii, jj, kk = case.ngrid, case.ii, case.jj, case.kk
     npg = ii * jj * kk
     out = {n: np.ones(case.idim3d) for n in ("bp", "bu", "bv", "bw")}
@@ -192,7 +241,7 @@ def block(case, body, samples=8):
         out[n] = np.empty(case.idim3d)
     out["bzelltyp"] = np.ones(case.idim3d, dtype=np.int32)
     icells = np.zeros(ng, dtype=np.int32)
-    nvecs, ucell = [], []
+    nvecs, ucell, areas = [], [], []
     levels = _Levels(case)
     X, Y, Z = case.coords()
     DX, DY, DZ = (a.reshape(ng, -1) for a in (case.dx, case.dy, case.dz))
@@ -242,11 +291,15 @@ def block(case, body, samples=8):
             bz = np.ones(npg, dtype=np.int32)
             bz[cut] = -np.arange(1, n + 1, dtype=np.int32)
             out["bzelltyp"][sl] = bz
-            nvecs.append(body.plane(XC.ravel()[cut], YC.ravel()[cut], ZC.ravel()[cut]))
+            pl = body.plane(XC.ravel()[cut], YC.ravel()[cut], ZC.ravel()[cut])
+            nvecs.append(pl)
             ucell.append(np.zeros((n, 3)))
+            areas.append(plane_box_area(pl, lo3.reshape(-1, 3)[cut], hi3.reshape(-1, 3)[cut]))
     out["icells"] = icells
     out["nvecs"] = np.concatenate(nvecs) if nvecs else np.zeros((0, 4))
     out["ucell"] = np.concatenate(ucell) if ucell else np.zeros((0, 3))
+    out["arealist"] = np.concatenate(areas) if areas else np.zeros(0)
+    out["bodyid"] = np.full(int(icells.sum()), int(getattr(body, "body_id", 1)), dtype=np.int32)
     return out
 
 

@@ -190,3 +190,39 @@ def test_scalar_stencils_drive_the_oracle(small, oracle_lib):
     o.set_scalar_geometry(1, [0, 1], [2.0, 0.5])
     o.timeintegrate_scalar(5e-3, 1, oracle_lib.rk_scheme("williamson"))
     assert np.all(np.isfinite(o.get("T1")))
+
+
+def test_plane_box_areas():
+    """Sections of the unit cube with known areas: a mid plane (1), the
+    hexagon normal to a diagonal (3 sqrt(3) / 4), the diagonal rectangle
+    (sqrt 2), a corner triangle (sqrt(3) / 8), and a plane that misses."""
+    from mglet_gb300.geometry import plane_box_area
+    s2, s3 = np.sqrt(2.0), np.sqrt(3.0)
+    nv = np.array([[1, 0, 0, 0.5], [1 / s3, 1 / s3, 1 / s3, 1.5 / s3], [1 / s2, 1 / s2, 0, 1 / s2],
+                   [1 / s3, 1 / s3, 1 / s3, 0.5 / s3], [0, 0, 1, 2.0]])
+    lo, hi = np.zeros((5, 3)), np.ones((5, 3))
+    assert np.allclose(plane_box_area(nv, lo, hi), [1.0, 3 * s3 / 4, s2, s3 / 8, 0.0], rtol=1e-12, atol=0)
+
+
+def test_sphere_interface_area_and_scalar_lists(small):
+    """The blocking's interface areas of the finer level (which covers the
+    sphere) add up to the sphere's surface within 15 %, and the scalar lists
+    built from them carry areabyvol = area / cell volume on the cut cells."""
+    case, geo = small.case, small.geo
+    r = 0.2
+    fine = [g for g in range(case.ngrid) if case.level[g] == case.level.max()]
+    off = np.concatenate([[0], np.cumsum(geo["icells"])])
+    total = 0.0
+    for g in fine:   # interior cells only: ghost layers repeat the neighbours' cells
+        bz = geo["bzelltyp"].reshape(case.ngrid, case.ii, case.jj, case.kk)[g, 2:-2, 2:-2, 2:-2]
+        total += geo["arealist"][off[g] - bz[bz < 0] - 1].sum()
+    assert abs(total / (4 * np.pi * r * r) - 1.0) < 0.15, total
+    assert np.all(geo["bodyid"] == 1)
+    scal = gpu.create_scastencils(case, geo, geo["arealist"], geo["bodyid"])
+    n_area = 0
+    for g in fine:
+        xi, xr, _ = scal[g]
+        rec_i, rec_r = xi.reshape(-1, 9), xr.reshape(-1, 8)
+        assert np.all(rec_r[:, 0] >= 0.0)
+        n_area += int(np.count_nonzero(rec_r[:, 0] > 0.0))
+    assert n_area > 0
